@@ -1,0 +1,172 @@
+"""ctypes mirror of ``include/shdom_problem.h`` and the numpy-side problem builder.
+
+The problem struct carries plain pointers into numpy arrays; :class:`Problem`
+keeps those arrays alive for as long as the struct is in use.  Field meanings
+and layouts follow the arguments ``at3d.solver.RTE`` hands to the Fortran core
+(at3d/solver.py:2324-2478 for the property arrays, at3d/solver.py:1960-2034
+for the numerical parameters).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_f = C.POINTER(C.c_float)
+_i = C.POINTER(C.c_int)
+
+
+class ShdomProblem(C.Structure):
+    _fields_ = [
+        ("npx", C.c_int), ("npy", C.c_int), ("npz", C.c_int),
+        ("delx", C.c_float), ("dely", C.c_float),
+        ("zlevels", _f),
+        ("npart", C.c_int), ("maxnmicro", C.c_int),
+        ("extinctp", _f), ("albedop", _f), ("iphasep", _i), ("phasewtp", _f),
+        ("numphase", C.c_int), ("nlegp", C.c_int), ("legenp", _f),
+        ("bc_x_open", C.c_int), ("bc_y_open", C.c_int), ("ipflag", C.c_int),
+        ("solarflux", C.c_float), ("solarmu", C.c_float), ("solaraz", C.c_float), ("skyrad", C.c_float),
+        ("sfc_variable", C.c_int), ("gndalbedo", C.c_float), ("gndtemp", C.c_float),
+        ("nxsfc", C.c_int), ("nysfc", C.c_int), ("delxsfc", C.c_float), ("delysfc", C.c_float),
+        ("sfc_albedo", _f),
+        ("nmu", C.c_int), ("nphi", C.c_int), ("angle_set", C.c_int),
+        ("deltam", C.c_int), ("accelflag", C.c_int), ("highorderrad", C.c_int), ("iterfixsh", C.c_int),
+        ("solacc", C.c_float), ("shacc", C.c_float), ("splitacc", C.c_float),
+        ("tautol", C.c_double), ("transcut", C.c_double),
+        ("transmin", C.c_float),
+        ("nstokes", C.c_int),
+    ]
+
+
+def _fp(a):
+    return a.ctypes.data_as(_f)
+
+
+def _ip(a):
+    return a.ctypes.data_as(_i)
+
+
+@dataclass
+class NumericalParams:
+    """Numerical parameters with the reference defaults (default_config.json)."""
+    num_mu_bins: int = 16
+    num_phi_bins: int = 32
+    deltam: bool = True
+    acceleration_flag: bool = True
+    solution_accuracy: float = 1e-4
+    spherical_harmonics_accuracy: float = 0.0
+    split_accuracy: float = 0.0
+    high_order_radiance: bool = False
+    iterfixsh: int = 30
+    tautol: float = 0.1
+    transcut: float = 1e-5
+    transmin: float = 1.0
+    angle_set: int = 2
+    ip_flag: int = 0
+    x_boundary_condition: str = "open"
+    y_boundary_condition: str = "open"
+
+
+@dataclass
+class Species:
+    """One scattering species on the property grid (a member of RTE.medium)."""
+    extinction: np.ndarray            # [npx, npy, npz] 1/km
+    ssalb: np.ndarray                 # [npx, npy, npz]
+    legcoef: np.ndarray               # [nleg+1] or [ntable, nleg+1]; a_l with the 2l+1 factor
+    table_index: np.ndarray | None = None   # [nmicro, npx, npy, npz], 1-based into legcoef rows
+    phase_weights: np.ndarray | None = None  # [nmicro, npx, npy, npz]
+
+
+@dataclass
+class Problem:
+    """All inputs of one RTE solve, held as numpy arrays."""
+    delx: float
+    dely: float
+    zlevels: np.ndarray
+    species: list
+    solarmu: float                    # SHDOM convention: negative, radiance propagation direction
+    solaraz: float                    # radians
+    solarflux: float = 1.0
+    skyrad: float = 0.0
+    surface_albedo: float | np.ndarray = 0.0
+    surface_delx: float = 0.0
+    surface_dely: float = 0.0
+    params: NumericalParams = field(default_factory=NumericalParams)
+    _keep: list = field(default_factory=list, repr=False)
+
+    @property
+    def shape(self):
+        return self.species[0].extinction.shape
+
+    def to_struct(self) -> ShdomProblem:
+        npx, npy, npz = self.shape
+        ng = npx * npy * npz
+        nspec = len(self.species)
+        maxnmicro = max((s.table_index.shape[0] if s.table_index is not None else 1) for s in self.species)
+        # Concatenate every species' Legendre table into one table
+        # (at3d/solver.py:2376-2411): each species' indices are offset by the
+        # number of rows already in the table.
+        rows, offsets = [], []
+        for s in self.species:
+            lc = np.atleast_2d(np.asarray(s.legcoef, dtype=np.float64))
+            offsets.append(len(rows))
+            rows.extend(list(lc))
+        nl = self.params.num_mu_bins
+        nmu = max(2, 2 * int((nl + 1) / 2))
+        ml = nmu - 1
+        nleg = ml + 1 if self.params.deltam else ml
+        nlegp = max(max(len(r) for r in rows) - 1, nleg)
+        legenp = np.zeros((len(rows), nlegp + 1), np.float32)
+        for k, r in enumerate(rows):
+            legenp[k, :len(r)] = r
+        ext = np.zeros((nspec, ng), np.float32)
+        alb = np.zeros((nspec, ng), np.float32)
+        iph = np.ones((nspec, ng, maxnmicro), np.int32)
+        pwt = np.zeros((nspec, ng, maxnmicro), np.float32)
+        for k, s in enumerate(self.species):
+            ext[k] = np.asarray(s.extinction, np.float32).reshape(-1)
+            alb[k] = np.asarray(s.ssalb, np.float32).reshape(-1)
+            if s.table_index is None:
+                iph[k, :, 0] = 1 + offsets[k]
+                pwt[k, :, 0] = 1.0
+            else:
+                nm = s.table_index.shape[0]
+                iph[k, :, :nm] = (np.asarray(s.table_index).reshape(nm, -1).T + offsets[k]).astype(np.int32)
+                pwt[k, :, :nm] = np.asarray(s.phase_weights, np.float32).reshape(nm, -1).T
+        zl = np.ascontiguousarray(self.zlevels, np.float32)
+        p = self.params
+        st = ShdomProblem()
+        st.npx, st.npy, st.npz = npx, npy, npz
+        st.delx, st.dely = self.delx, self.dely
+        st.zlevels = _fp(zl)
+        st.npart, st.maxnmicro = nspec, maxnmicro
+        st.extinctp, st.albedop, st.iphasep, st.phasewtp = _fp(ext), _fp(alb), _ip(iph), _fp(pwt)
+        st.numphase, st.nlegp, st.legenp = legenp.shape[0], nlegp, _fp(legenp)
+        st.bc_x_open = int(p.x_boundary_condition == "open")
+        st.bc_y_open = int(p.y_boundary_condition == "open")
+        st.ipflag = p.ip_flag
+        st.solarflux, st.solarmu, st.solaraz, st.skyrad = self.solarflux, self.solarmu, self.solaraz, self.skyrad
+        sa = np.asarray(self.surface_albedo, np.float32)
+        keep = [zl, ext, alb, iph, pwt, legenp]
+        if sa.size == 1:
+            st.sfc_variable, st.gndalbedo = 0, float(sa.reshape(-1)[0])
+            st.nxsfc = st.nysfc = 0
+        else:
+            sa2 = np.atleast_2d(sa)                   # [nxsfc, nysfc]
+            buf = np.ascontiguousarray(sa2.T, np.float32)  # [nysfc][nxsfc]
+            keep.append(buf)
+            st.sfc_variable = 1
+            st.nxsfc, st.nysfc = sa2.shape
+            st.delxsfc, st.delysfc = self.surface_delx, self.surface_dely
+            st.sfc_albedo = _fp(buf)
+            st.gndalbedo = float(sa2.mean())
+        st.gndtemp = 288.0
+        st.nmu, st.nphi, st.angle_set = p.num_mu_bins, p.num_phi_bins, p.angle_set
+        st.deltam, st.accelflag = int(p.deltam), int(p.acceleration_flag)
+        st.highorderrad, st.iterfixsh = int(p.high_order_radiance), p.iterfixsh
+        st.solacc, st.shacc, st.splitacc = p.solution_accuracy, p.spherical_harmonics_accuracy, p.split_accuracy
+        st.tautol, st.transcut, st.transmin = p.tautol, p.transcut, p.transmin
+        st.nstokes = 1
+        self._keep = keep
+        return st

@@ -1,0 +1,57 @@
+"""Optical-property producers the benchmark scenes need.
+
+* :func:`rayleigh_legcoef` -- Rayleigh phase-function Legendre coefficients
+  with the King depolarisation factor (RAYLEIGH_PHASE_FUNCTION,
+  src/polarized/shdomsub4.f:2350-2386, scalar P11 row).
+* :func:`rayleigh_extinction_profile` -- molecular extinction from a
+  temperature profile (at3d.rayleigh.compute_extinction,
+  at3d/rayleigh.py:139-185, and RAYLEIGH_EXTINCT, src/shdomsub5.f:1457-1490),
+  evaluated in single precision like the reference.
+* :func:`henyey_greenstein_legcoef` -- a_l = (2l+1) g^l.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def rayleigh_legcoef(wavelength: float) -> np.ndarray:
+    """Scalar Rayleigh Legendre series [a_0, a_1, a_2] at ``wavelength`` (um)."""
+    a_k, b_k, c_k = 1.0469541, 3.2503153e-04, 3.8622851e-05
+    w = np.float32(wavelength)
+    fking = np.float32(a_k + b_k / np.float64(w) ** 2 + c_k / np.float64(w) ** 4)
+    depol = np.float32(6.0 * (np.float64(fking) - 1.0) / (3.0 + 7.0 * np.float64(fking)))
+    delta = np.float32((np.float32(1.0) - depol) / (np.float32(1.0) + np.float32(0.5) * depol))
+    return np.array([1.0, 0.0, np.float32(0.5) * delta], np.float32)
+
+
+def rayleigh_extinction_profile(wavelength: float, zlevels, temperature, surface_pressure: float = 1013.25):
+    """Rayleigh extinction [1/km] at each level of a temperature profile."""
+    lam = float(wavelength)
+    raylcoef = 0.03370 * (surface_pressure / 1013.25) * 0.0021520 * (
+        1.0455996 - 341.29061 / lam ** 2 - 0.90230850 * lam ** 2) / \
+        (1 + 0.0027059889 / lam ** 2 - 85.968563 * lam ** 2)
+    f32 = np.float32
+    z = np.asarray(zlevels, f32)
+    t = np.asarray(temperature, f32)
+    rc = f32(raylcoef)
+    pres = f32(surface_pressure)
+    ts = t[0]
+    lapse = f32(6.5) * f32(0.001)
+    pres = f32(pres * (ts / (ts + lapse * z[0] * f32(1000.0))) ** (f32(9.8) / (f32(287.0) * lapse)))
+    out = np.zeros(len(z), f32)
+    for i in range(len(z) - 1):
+        out[i] = rc * pres / t[i]
+        dz = f32(1000.0) * (z[i + 1] - z[i])
+        lapse = (t[i] - t[i + 1]) / dz
+        if abs(lapse) > 0.00001:
+            pres = f32(pres * (t[i + 1] / t[i]) ** (f32(9.8) / (f32(287.0) * lapse)))
+        else:
+            pres = f32(pres * np.exp(f32(-9.8) * dz / (f32(287.0) * t[i])))
+    out[-1] = rc * pres / t[-1]
+    return out
+
+
+def henyey_greenstein_legcoef(g: float, nterms: int) -> np.ndarray:
+    """Henyey-Greenstein Legendre series a_l = (2l+1) g^l, l = 0..nterms-1."""
+    l = np.arange(nterms, dtype=np.float64)
+    return ((2 * l + 1) * g ** l).astype(np.float32)

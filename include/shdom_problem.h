@@ -1,0 +1,69 @@
+/*
+ * shdom_problem.h -- plain-C description of one SHDOM radiative-transfer
+ * problem (medium on a property grid, boundary conditions, solar source,
+ * Lambertian surface, numerical parameters).
+ *
+ * This is the input format of the drop-in C-ABI (shdom_gb300.h).  Every
+ * field mirrors an argument that at3d.solver.RTE passes to the Fortran
+ * core through f2py:
+ *   property grid / species  : at3d/solver.py:2336-2411 (extinctp, albedop,
+ *                              iphasep, phasewtp, legenp) and
+ *                              at3d/solver.py:2057-2064 (npx, npy, npz,
+ *                              delx, dely, zlevels)
+ *   boundary conditions      : at3d/solver.py:2110-2127 (bcflag, ipflag)
+ *   source                   : at3d/source.py:14-80 (solar)
+ *   surface                  : at3d/surface.py:28-105 (lambertian)
+ *   numerical parameters     : at3d/solver.py:1960-2034, default_config.json
+ *
+ * Array layouts are the Fortran (column-major) layouts of the reference,
+ * written here as C row-major with the slowest index first:
+ *   extinctp[npart][npx][npy][npz]
+ *   iphasep [npart][npx][npy][npz][maxnmicro]   (1-based table index)
+ *   legenp  [numphase][nlegp+1]                 (scalar legcoef a_l, which
+ *                                                carry the 2l+1 factor)
+ *   sfc_albedo[nysfc][nxsfc]                    (x fastest)
+ */
+#ifndef SHDOM_PROBLEM_H
+#define SHDOM_PROBLEM_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct shdom_problem {
+    /* ---- property grid ---- */
+    int npx, npy, npz;
+    float delx, dely;
+    const float *zlevels;          /* [npz] km, increasing, zlevels[0] is the ground */
+    /* ---- scattering species ---- */
+    int npart, maxnmicro;
+    const float *extinctp;         /* [npart][npx*npy*npz] 1/km */
+    const float *albedop;          /* [npart][npx*npy*npz] */
+    const int   *iphasep;          /* [npart][npx*npy*npz][maxnmicro], 1..numphase */
+    const float *phasewtp;         /* [npart][npx*npy*npz][maxnmicro] */
+    int numphase, nlegp;
+    const float *legenp;           /* [numphase][nlegp+1] */
+    /* ---- boundary conditions ---- */
+    int bc_x_open, bc_y_open;      /* 0 periodic, 1 open */
+    int ipflag;                    /* independent-pixel bit flags, 0..7 */
+    /* ---- solar source (SHDOM convention: solarmu < 0, radians) ---- */
+    float solarflux, solarmu, solaraz, skyrad;
+    /* ---- Lambertian surface ---- */
+    int sfc_variable;              /* 0: fixed 'FL', 1: variable 'VL' */
+    float gndalbedo, gndtemp;
+    int nxsfc, nysfc;
+    float delxsfc, delysfc;
+    const float *sfc_albedo;       /* [nysfc][nxsfc] when sfc_variable */
+    /* ---- numerical parameters ---- */
+    int nmu, nphi, angle_set;
+    int deltam, accelflag, highorderrad, iterfixsh;
+    float solacc, shacc, splitacc; /* splitacc must be <= 0 (no adaptive splitting) */
+    double tautol, transcut;
+    float transmin;
+    int nstokes;                   /* 1 (scalar) */
+} shdom_problem;
+
+#ifdef __cplusplus
+}
+#endif
+#endif

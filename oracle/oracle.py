@@ -1,0 +1,110 @@
+"""TEST INFRASTRUCTURE: ctypes binding of the CPU oracle (oracle/shdom_oracle.cpp).
+
+The oracle is a restatement of the reference Fortran path (see the header of
+shdom_oracle.cpp for the citations).  Only tests/, __graft_entry__.smoke()
+and bench.py's cpu_baseline leg use it; the at3d_gb300 package never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "_build", "liboracle.so")
+        src = os.path.join(_HERE, "shdom_oracle.cpp")
+        if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+            build()
+        L = C.CDLL(path)
+        L.oracle_create.restype = C.c_void_p
+        L.oracle_create.argtypes = [C.c_void_p, C.c_int]
+        L.oracle_error.restype = C.c_char_p
+        L.oracle_error.argtypes = [C.c_void_p]
+        for n in ("oracle_sizes", "oracle_solve", "oracle_init_solution", "oracle_export",
+                  "oracle_render", "oracle_grid", "oracle_angles"):
+            getattr(L, n).restype = C.c_int
+        L.oracle_destroy.argtypes = [C.c_void_p]
+        _LIB = L
+    return _LIB
+
+
+def _p(a, t=C.c_float):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class Oracle:
+    """One RTE problem solved on the CPU by the oracle (fp64=False mirrors
+    the reference's REAL arithmetic, fp64=True is the FP64 oracle)."""
+
+    def __init__(self, problem, fp64: bool = False):
+        self._lib = lib()
+        self._problem = problem
+        st = problem.to_struct()
+        self._h = self._lib.oracle_create(C.byref(st), int(fp64))
+        err = self._lib.oracle_error(self._h)
+        if err:
+            raise RuntimeError(err.decode())
+        self.sizes = self._sizes()
+
+    def _sizes(self):
+        out = np.zeros(16, np.int32)
+        self._lib.oracle_sizes(C.c_void_p(self._h), _p(out, C.c_int))
+        keys = ["npts", "nlm", "nmu", "nang", "ncells", "nx1", "ny1", "nz", "bcflag", "ipflag", "iters", "ml", "mm"]
+        return dict(zip(keys, [int(v) for v in out[:len(keys)]]))
+
+    def solve(self, maxiter: int, verbose: bool = False):
+        sc = C.c_float(0)
+        rc = self._lib.oracle_solve(C.c_void_p(self._h), int(maxiter), int(verbose), C.byref(sc))
+        if rc:
+            raise RuntimeError(self._lib.oracle_error(C.c_void_p(self._h)).decode())
+        self.sizes = self._sizes()
+        return self.sizes["iters"], float(sc.value)
+
+    def init_solution(self):
+        if self._lib.oracle_init_solution(C.c_void_p(self._h)):
+            raise RuntimeError(self._lib.oracle_error(C.c_void_p(self._h)).decode())
+
+    def export(self):
+        n, nlm = self.sizes["npts"], self.sizes["nlm"]
+        src = np.zeros((n, nlm), np.float32); rad = np.zeros((n, nlm), np.float32)
+        ns = np.zeros(n, np.int32); nr = np.zeros(n, np.int32)
+        flx = np.zeros((n, 2), np.float32); dfl = np.zeros(n, np.float32)
+        self._lib.oracle_export(C.c_void_p(self._h), _p(src), _p(ns, C.c_int), _p(rad), _p(nr, C.c_int),
+                                _p(flx), _p(dfl))
+        return dict(source=src, ns=ns, radiance=rad, nr=nr, fluxes=flx, dirflux=dfl)
+
+    def render(self, x, y, z, mu, phi, nthreads: int = 1):
+        x = np.ascontiguousarray(x, np.float32); y = np.ascontiguousarray(y, np.float32)
+        z = np.ascontiguousarray(z, np.float32)
+        mu = np.ascontiguousarray(mu, np.float64); phi = np.ascontiguousarray(phi, np.float64)
+        out = np.zeros(len(x), np.float32)
+        rc = self._lib.oracle_render(C.c_void_p(self._h), len(x), _p(x), _p(y), _p(z), _p(mu, C.c_double),
+                                     _p(phi, C.c_double), _p(out), int(nthreads))
+        if rc:
+            raise RuntimeError(self._lib.oracle_error(C.c_void_p(self._h)).decode())
+        return out
+
+    def grid(self):
+        n, nc = self.sizes["npts"], self.sizes["ncells"]
+        gp = np.zeros((n, 3), np.float32); gptr = np.zeros((nc, 8), np.int32)
+        nb = np.zeros((nc, 6), np.int32); cf = np.zeros(nc, np.int16)
+        self._lib.oracle_grid(C.c_void_p(self._h), _p(gp), _p(gptr, C.c_int), _p(nb, C.c_int), _p(cf, C.c_short))
+        return gp, gptr, nb, cf
+
+    def __del__(self):
+        try:
+            self._lib.oracle_destroy(C.c_void_p(self._h))
+        except Exception:
+            pass

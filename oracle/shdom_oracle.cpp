@@ -1,0 +1,1683 @@
+// shdom_oracle.cpp -- TEST INFRASTRUCTURE ONLY.
+//
+// CPU restatement of the reference SHDOM solve / render path (AT3D 4.1.3,
+// Fortran in src/polarized/*.f, src/shdom_nompi.f, src/surface.f).  It is
+// the checker that the GPU path is compared against; nothing in the
+// at3d_gb300 package may include, link or call it.  Only tests/,
+// __graft_entry__.smoke() and bench.py's cpu_baseline leg use it.
+//
+// Parity pinning: the restatement is checked against the reference's own
+// golden files tests/data/brdf_L1{f,r}.out (original SHDOM fluxes and
+// radiances, tests/test_shdom.py:597-632) through tests/golden/.
+//
+// The numeric type of the reference's REAL arrays is the template parameter
+// R (float reproduces the reference, double gives the FP64 oracle).  Local
+// variables the reference declares DOUBLE PRECISION are double in both.
+// Each routine cites the reference routine it restates.  Indices are 0-based
+// here; "no neighbour" is -1 (the reference uses 0 with 1-based cells).
+//
+// Differences from the reference, all documented in the design doc:
+//  * the azimuthal transform always uses the DFT (the reference switches to
+//    FFTPACK RFFTB/RFFTF when NPHI0>14, src/polarized/shdomsub2.f:1137); the
+//    two are the same linear map (src/polarized/shdomsub1.f:3008-3030,
+//    :3222-3237), only rounding differs;
+//  * adaptive cell splitting is not implemented (splitacc must be <= 0);
+//  * the 2D independent-pixel sweep (ipflag 1 or 2) is not implemented.
+
+#include "../include/shdom_problem.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace orc {
+
+static const int kGoodNFFT[256] = {
+    1,   2,   3,   4,   5,   6,   7,   8,   9,   10,  11,  12,  13,  14,  16,  16,  18,  18,  20,
+    20,  24,  24,  24,  24,  25,  27,  27,  30,  30,  30,  32,  32,  36,  36,  36,  36,  40,  40,
+    40,  40,  45,  45,  45,  45,  45,  48,  48,  48,  50,  50,  54,  54,  54,  54,  60,  60,  60,
+    60,  60,  60,  64,  64,  64,  64,  72,  72,  72,  72,  72,  72,  72,  72,  80,  80,  80,  80,
+    80,  80,  80,  80,  81,  90,  90,  90,  90,  90,  90,  90,  90,  90,  96,  96,  96,  96,  96,
+    96,  100, 100, 100, 100, 108, 108, 108, 108, 108, 108, 108, 108, 120, 120, 120, 120, 120, 120,
+    120, 120, 120, 120, 120, 120, 128, 128, 128, 128, 128, 128, 128, 128, 144, 144, 144, 144, 144,
+    144, 144, 144, 144, 144, 144, 144, 144, 144, 144, 144, 160, 160, 160, 160, 160, 160, 160, 160,
+    160, 160, 160, 160, 160, 160, 160, 160, 180, 180, 180, 180, 180, 180, 180, 180, 180, 180, 180,
+    180, 180, 180, 180, 180, 180, 180, 180, 180, 192, 192, 192, 192, 192, 192, 192, 192, 192, 192,
+    192, 192, 200, 200, 200, 200, 200, 200, 200, 200, 216, 216, 216, 216, 216, 216, 216, 216, 216,
+    216, 216, 216, 216, 216, 216, 216, 240, 240, 240, 240, 240, 240, 240, 240, 240, 240, 240, 240,
+    240, 240, 240, 240, 240, 240, 240, 240, 240, 240, 240, 240, 256, 256, 256, 256, 256, 256, 256,
+    256, 256, 256, 256, 256, 256, 256, 256, 256};
+
+// Face corner table (GRIDFACE in src/polarized/shdomsub1.f:3726), 0-based.
+static const int kGridFace[6][4] = {{0, 2, 4, 6}, {1, 3, 5, 7}, {0, 1, 4, 5},
+                                    {2, 3, 6, 7}, {0, 1, 2, 3}, {4, 5, 6, 7}};
+static const int kOppFace[6] = {1, 0, 3, 2, 5, 4};
+
+// Normalized Wigner d^l_{m0}(x)*sqrt(l+1/2) for l = 0..lmax at fixed m >= 0
+// (WIGNERFCT02P2M_NORMALIZED dm0 output, src/polarized/shdomsub2.f:4357-4395).
+static void wigner_dm0(double x, int lmax, int m, std::vector<double> &d) {
+  d.assign(lmax + 1, 0.0);
+  if (m > lmax) return;
+  if (m == 0) {
+    d[0] = 1.0;
+    if (lmax >= 1) d[1] = x;
+    for (int n = 1; n < lmax; ++n) d[n + 1] = ((2 * n + 1) * x * d[n] - n * d[n - 1]) / (n + 1);
+  } else {
+    // d^m_{m0} = (-1)^m sqrt((2m)!)/(2^m m!) (1-x^2)^{m/2}  (DMM1_N0 with m1=0)
+    double prod = 1.0;
+    for (int p = 1; p <= m; ++p) prod *= std::sqrt((double)(m + p) / (double)p);
+    double s = std::sqrt((1.0 - x) * (1.0 + x)) * 0.5;
+    d[m] = ((m & 1) ? -1.0 : 1.0) * prod * std::pow(s, m);
+    for (int n = m; n < lmax; ++n) {
+      double a = std::sqrt((double)((n + 1) * (n + 1) - m * m));
+      double b = (n > m) ? std::sqrt((double)(n * n - m * m)) : 0.0;
+      d[n + 1] = ((2 * n + 1) * x * d[n] - b * (n > m ? d[n - 1] : 0.0)) / a;
+    }
+  }
+  for (int n = 0; n <= lmax; ++n) d[n] *= std::sqrt(n + 0.5);
+}
+
+static inline int sh_index(int l, int m, int mm) {
+  // J = L(L+1)+M (L<=MM) or (2MM+1)L-MM^2+M, 0-based (YLMALL header,
+  // src/polarized/shdomsub2.f:4252-4253).
+  return (l <= mm) ? l * (l + 1) + m : (2 * mm + 1) * l - mm * mm + m;
+}
+
+template <typename R>
+struct Solver {
+  shdom_problem p{};
+  std::vector<float> zlev, extp, albp, phwtp, legp, sfcalb;
+  std::vector<int> iphp;
+  std::string err;
+
+  // grid
+  int nx = 0, ny = 0, nz = 0, nx1 = 0, ny1 = 0, npts = 0, ncells = 0, bcflag = 0, ipflag = 0;
+  std::vector<float> xgrid, ygrid, zgrid, gridpos;  // gridpos[npts][3]
+  std::vector<int> gridptr, neighptr;              // [ncells][8], [ncells][6]
+  std::vector<short> cellflags;
+  int noct = 8;
+  std::vector<int> sweep_cell, sweep_corner;  // [noct][npts]
+
+  // angles
+  int nmu = 0, nphi = 0, ml = 0, mm = 0, nlm = 0, nphi0max = 0, nang = 0, nleg = 0;
+  std::vector<int> nphi0, lofj, mofj;
+  std::vector<float> mu, wtmu, phi, wtdo;  // phi/wtdo [nmu][nphi0max]
+  std::vector<R> cmu1, cmu2;               // [nmu][nlm]
+  std::vector<R> cphi1, cphi2;             // [nmu][nphi0max][2mm+1] (m index offset +mm)
+  std::vector<R> ylmsun;                   // [nlm]
+
+  // medium on the grid
+  int npart = 0, maxnmicro = 0, numphase = 0, nq = 0;
+  std::vector<R> extinct, albedo, total_ext;  // [npart][npts], [npts]
+  std::vector<int> iphase;                    // [npart][npts][8*maxnmicro]
+  std::vector<R> phaseinterpwt;
+  std::vector<R> legen;  // [numphase][nleg+1]
+  double extmin = 0, scatmin = 0;
+  R albmax = 0;
+  const float phasemax = 0.999f;
+
+  // direct beam
+  std::vector<R> dirflux;
+  // solution
+  std::vector<R> source, delsource, radiance, fluxes;  // fluxes [npts][2]
+  std::vector<int> shptr, rshptr, oshptr;
+  R deljdot = 0, deljold = 0, deljnew = 0, jnorm = 0;
+  R solcrit = 1, accel_a = 0;
+  int iter = 0;
+  // boundaries
+  std::vector<int> topp, botp;
+  std::vector<R> sfcgridalb;  // per bottom point
+  std::vector<R> bcrad_top, bcrad_bot;
+  bool sweep_ready = false;
+
+  // ------------------------------------------------------------ setup
+  bool init(const shdom_problem *in) {
+    p = *in;
+    int ng = p.npx * p.npy * p.npz;
+    zlev.assign(p.zlevels, p.zlevels + p.npz);
+    extp.assign(p.extinctp, p.extinctp + (size_t)p.npart * ng);
+    albp.assign(p.albedop, p.albedop + (size_t)p.npart * ng);
+    iphp.assign(p.iphasep, p.iphasep + (size_t)p.npart * ng * p.maxnmicro);
+    phwtp.assign(p.phasewtp, p.phasewtp + (size_t)p.npart * ng * p.maxnmicro);
+    legp.assign(p.legenp, p.legenp + (size_t)p.numphase * (p.nlegp + 1));
+    if (p.sfc_variable) sfcalb.assign(p.sfc_albedo, p.sfc_albedo + (size_t)p.nxsfc * p.nysfc);
+    p.zlevels = nullptr; p.extinctp = p.albedop = p.phasewtp = p.legenp = p.sfc_albedo = nullptr;
+    p.iphasep = nullptr;
+    if (p.splitacc > 0) { err = "adaptive splitting is not supported"; return false; }
+    if (p.nstokes != 1) { err = "only nstokes=1 is supported"; return false; }
+    if (!setup_grid()) return false;
+    setup_angles();
+    if (!transfer_properties()) return false;
+    return true;
+  }
+
+  // _setup_grid (at3d/solver.py:2036-2168), NEW_GRIDS and INIT_CELL_STRUCTURE
+  // (src/polarized/shdomsub2.f:16-310).
+  bool setup_grid() {
+    nx = std::max(1, p.npx); ny = std::max(1, p.npy); nz = std::max(2, p.npz);
+    ipflag = p.ipflag;
+    if (nx == 1) ipflag |= 1;
+    if (ny == 1) ipflag |= 2;
+    bcflag = 0;
+    if (p.bc_x_open && (ipflag == 0 || ipflag == 2 || ipflag == 4 || ipflag == 6)) bcflag += 1;
+    if (p.bc_y_open && (ipflag == 0 || ipflag == 1 || ipflag == 4 || ipflag == 5)) bcflag += 2;
+    if (bcflag == 1) { err = "open x with periodic y boundaries is not supported"; return false; }
+    if ((ipflag & 3) == 1 || (ipflag & 3) == 2) { err = "2D independent pixel mode is not supported"; return false; }
+    nx1 = nx + 1; ny1 = ny + 1;
+    if ((bcflag & 5) || (ipflag & 1)) nx1 -= 1;
+    if ((bcflag & 7) || (ipflag & 2)) ny1 -= 1;
+    xgrid.resize(nx + 1); ygrid.resize(ny + 1);
+    float dxp = p.delx > 0 ? p.delx : 1.0f, dyp = p.dely > 0 ? p.dely : 1.0f;
+    for (int i = 0; i <= nx; ++i) xgrid[i] = ((float)i * (dxp * (float)p.npx)) / (float)nx;
+    for (int i = 0; i <= ny; ++i) ygrid[i] = ((float)i * (dyp * (float)p.npy)) / (float)ny;
+    zgrid = zlev;
+    npts = nx1 * ny1 * nz;
+    gridpos.resize((size_t)npts * 3);
+    int ip = 0;
+    for (int ix = 0; ix < nx1; ++ix)
+      for (int iy = 0; iy < ny1; ++iy)
+        for (int iz = 0; iz < nz; ++iz, ++ip) {
+          gridpos[3 * ip] = xgrid[ix]; gridpos[3 * ip + 1] = ygrid[iy]; gridpos[3 * ip + 2] = zgrid[iz];
+        }
+    int nxc = nx, nyc = ny;
+    if (bcflag & 1) nxc = nx + 1;
+    if (bcflag & 2) nyc = ny + 1;
+    ncells = nxc * nyc * (nz - 1);
+    gridptr.assign((size_t)ncells * 8, 0); neighptr.assign((size_t)ncells * 6, -1);
+    cellflags.assign(ncells, 0);
+    int ic = 0;
+    for (int ix = 1; ix <= nxc; ++ix) {
+      int ix0, ix1;
+      if (ipflag & 1) { ix0 = ix; ix1 = ix; }
+      else if (bcflag & 1) { ix0 = std::max(1, ix - 1); ix1 = std::min(nx, ix); }
+      else { ix0 = ix; ix1 = ix + 1; }
+      for (int iy = 1; iy <= nyc; ++iy) {
+        int iy0, iy1;
+        if (ipflag & 2) { iy0 = iy; iy1 = iy; }
+        else if (bcflag & 2) { iy0 = std::max(1, iy - 1); iy1 = std::min(ny, iy); }
+        else { iy0 = iy; iy1 = iy + 1; }
+        for (int iz = 1; iz <= nz - 1; ++iz, ++ic) {
+          int *g = &gridptr[8 * ic];
+          auto P = [&](int z, int y, int x) { return (z - 1) + nz * (y - 1) + nz * ny1 * (x - 1); };
+          g[0] = P(iz, iy0, ix0); g[1] = P(iz, iy0, ix1); g[2] = P(iz, iy1, ix0); g[3] = P(iz, iy1, ix1);
+          g[4] = P(iz + 1, iy0, ix0); g[5] = P(iz + 1, iy0, ix1); g[6] = P(iz + 1, iy1, ix0);
+          g[7] = P(iz + 1, iy1, ix1);
+          int *nb = &neighptr[6 * ic];
+          int sx = (nz - 1) * nyc;
+          if (ipflag & 1) { nb[0] = ic; nb[1] = ic; cellflags[ic] |= 1; }
+          else if (bcflag & 1) {
+            if (ix == 1) { nb[0] = ic; nb[1] = ic + sx; cellflags[ic] |= 1; }
+            else if (ix == nxc) { nb[0] = ic - sx; nb[1] = ic; cellflags[ic] |= 1; }
+            else { nb[0] = ic - sx; nb[1] = ic + sx; }
+          } else {
+            nb[0] = (ix == 1) ? ic + (nxc - 1) * sx : ic - sx;
+            nb[1] = (ix == nx) ? ic - (nxc - 1) * sx : ic + sx;
+          }
+          int sy = nz - 1;
+          if (ipflag & 2) { nb[2] = ic; nb[3] = ic; cellflags[ic] |= 2; }
+          else if (bcflag & 2) {
+            if (iy == 1) { nb[2] = ic; nb[3] = ic + sy; cellflags[ic] |= 2; }
+            else if (iy == nyc) { nb[2] = ic - sy; nb[3] = ic; cellflags[ic] |= 2; }
+            else { nb[2] = ic - sy; nb[3] = ic + sy; }
+          } else {
+            nb[2] = (iy == 1) ? ic + (nyc - 1) * sy : ic - sy;
+            nb[3] = (iy == ny) ? ic - (nyc - 1) * sy : ic + sy;
+          }
+          nb[4] = (iz == 1) ? -1 : ic - 1;
+          nb[5] = (iz == nz - 1) ? -1 : ic + 1;
+        }
+      }
+    }
+    return true;
+  }
+
+  // SWEEPING_ORDER / SWEEP_BASE_CELL (src/polarized/shdomsub1.f:3261-3351,
+  // :4529-4622), base grid only.
+  void sweeping_order() {
+    static const int ioctorder[8] = {1, 5, 2, 6, 3, 7, 4, 8};
+    if ((ipflag & 2) && (ipflag & 1)) noct = 2;
+    else if (ipflag & 2) noct = 4;
+    else noct = 8;
+    int nxc = nx, nyc = ny;
+    if (bcflag & 1) nxc = nx + 1;
+    if (bcflag & 2) nyc = ny + 1;
+    sweep_cell.assign((size_t)noct * npts, 0); sweep_corner.assign((size_t)noct * npts, 0);
+    std::vector<char> done(npts);
+    for (int joct = 0; joct < noct; ++joct) {
+      int ioct = ioctorder[joct];
+      int b = ioct - 1;
+      int dix, six, eix, diy, siy, eiy, diz, siz, eiz;
+      if (b & 1) { dix = 1; if (bcflag & 1) { six = nxc; eix = std::max(nxc - 1, 1); } else { six = 1; eix = nxc; } }
+      else { dix = -1; if (bcflag & 1) { six = 1; eix = std::min(2, nxc); } else { six = nxc; eix = 1; } }
+      if (b & 2) { diy = 1; if (bcflag & 2) { siy = nyc; eiy = std::max(nyc - 1, 1); } else { siy = 1; eiy = nyc; } }
+      else { diy = -1; if (bcflag & 2) { siy = 1; eiy = std::min(2, nyc); } else { siy = nyc; eiy = 1; } }
+      if (b & 4) { diz = 1; siz = 1; eiz = nz - 1; } else { diz = -1; siz = nz - 1; eiz = 1; }
+      std::fill(done.begin(), done.end(), 0);
+      int iorder = 0;
+      int ix = six, iy = siy, iz = siz;
+      while (true) {
+        int icell = (iz - 1) + (nz - 1) * (iy - 1) + (nz - 1) * nyc * (ix - 1);
+        for (int k = 0; k < 8; ++k) {
+          int corner = (k ^ b) ^ 7;
+          int ipt = gridptr[8 * icell + corner];
+          if (done[ipt]) continue;
+          done[ipt] = 1;
+          sweep_cell[(size_t)joct * npts + iorder] = icell;
+          sweep_corner[(size_t)joct * npts + iorder] = corner;
+          ++iorder;
+        }
+        if (ix == eix) {
+          if (iy == eiy) {
+            if (iz == eiz) break;
+            iz += diz;
+            iy = siy;
+          } else {
+            iy = (iy + diy + nyc - 1) % nyc + 1;
+          }
+          ix = six;
+        } else {
+          ix = (ix + dix + nxc - 1) % nxc + 1;
+        }
+      }
+    }
+    sweep_ready = true;
+  }
+
+  // MAKE_ANGLE_SET / GAUSQUADS / MAKE_SH_DO_COEF / PLMALL / YLMALL_UNPOL
+  // (src/polarized/shdomsub2.f:1061-1220, :4874-4912, :4650-4755, :4497-4535).
+  void setup_angles() {
+    nmu = std::max(2, 2 * ((p.nmu + 1) / 2));
+    nphi = std::max(1, p.nphi);
+    ml = nmu - 1;
+    mm = std::max(0, nphi / 2 - 1);
+    nlm = (2 * mm + 1) * (ml + 1) - mm * (mm + 1);
+    nleg = p.deltam ? ml + 1 : ml;
+    nphi0max = nphi;
+    lofj.resize(nlm); mofj.resize(nlm);
+    for (int l = 0, j = 0; l <= ml; ++l)
+      for (int m = -std::min(l, mm); m <= std::min(l, mm); ++m, ++j) { lofj[j] = l; mofj[j] = m; }
+    mu.resize(nmu); wtmu.resize(nmu);
+    int k = nmu / 2;
+    for (int j = 1; j <= k; ++j) {
+      double x = std::cos(3.141592654 * (j - .25) / (nmu + .5)), xp, pl, pl1, pl2, dpl;
+      int it = 0;
+      do {
+        pl1 = 1; pl = x;
+        for (int l = 2; l <= nmu; ++l) { pl2 = pl1; pl1 = pl; pl = ((2 * l - 1) * x * pl1 - (l - 1) * pl2) / l; }
+        dpl = nmu * (x * pl - pl1) / (x * x - 1);
+        xp = x; x = xp - pl / dpl; ++it;
+      } while (std::fabs(x - xp) > 3.0e-7 && it < 10);
+      mu[j - 1] = (float)(-x); mu[j - 1 + k] = (float)x;
+      wtmu[j - 1] = (float)(2.0 / ((1.0 - x * x) * dpl * dpl)); wtmu[j - 1 + k] = wtmu[j - 1];
+    }
+    nphi0.resize(nmu);
+    phi.assign((size_t)nmu * nphi0max, 0.f); wtdo.assign((size_t)nmu * nphi0max, 0.f);
+    nang = 0;
+    const float pif = (float)std::acos(-1.0f);
+    for (int j = 0; j < nmu; ++j) {
+      if (p.angle_set == 1) nphi0[j] = nphi0max;
+      else {
+        int n = (int)(0.9f + (float)nphi0max * std::sqrt(1.0f - mu[j] * mu[j]));
+        nphi0[j] = std::min(nphi0max, kGoodNFFT[std::max(1, n) - 1]);
+      }
+      float delphi = 2.0f * pif / (float)nphi0[j];
+      for (int kk = 0; kk < nphi0[j]; ++kk) {
+        phi[(size_t)j * nphi0max + kk] = (float)kk * delphi;
+        wtdo[(size_t)j * nphi0max + kk] = delphi * wtmu[j];
+      }
+      nang += nphi0[j];
+    }
+    cmu1.assign((size_t)nmu * nlm, 0); cmu2.assign((size_t)nmu * nlm, 0);
+    std::vector<double> d;
+    const double fct = 1.0 / std::sqrt(2.0 * std::acos(-1.0));
+    for (int i = 0; i < nmu; ++i) {
+      for (int m = 0; m <= mm; ++m) {
+        wigner_dm0((double)mu[i], ml, m, d);
+        for (int l = m; l <= ml; ++l) {
+          R v = (R)(fct * d[l]);
+          int jp = sh_index(l, m, mm), jn = sh_index(l, -m, mm);
+          cmu1[(size_t)i * nlm + jp] = v; cmu1[(size_t)i * nlm + jn] = v;
+          cmu2[(size_t)i * nlm + jp] = v * (R)wtmu[i]; cmu2[(size_t)i * nlm + jn] = v * (R)wtmu[i];
+        }
+      }
+    }
+    int nm = 2 * mm + 1;
+    cphi1.assign((size_t)nmu * nphi0max * nm, 0); cphi2.assign((size_t)nmu * nphi0max * nm, 0);
+    for (int i = 0; i < nmu; ++i) {
+      R w = (R)1 / (R)wtmu[i];
+      for (int kk = 0; kk < nphi0[i]; ++kk) {
+        R *c1 = &cphi1[((size_t)i * nphi0max + kk) * nm + mm];
+        R *c2 = &cphi2[((size_t)i * nphi0max + kk) * nm + mm];
+        R wd = (R)wtdo[(size_t)i * nphi0max + kk];
+        c1[0] = 1; c2[0] = wd * w;
+        for (int m = 1; m <= mm; ++m) {
+          R ph = (R)phi[(size_t)i * nphi0max + kk];
+          c1[m] = std::cos((R)m * ph); c1[-m] = std::sin((R)m * ph);
+          c2[m] = c1[m] * wd * w; c2[-m] = c1[-m] * wd * w;
+        }
+      }
+    }
+    // YLMSUN (YLMALL_UNPOL at the solar direction)
+    ylmsun = ylmall((double)p.solarmu, p.solaraz);
+  }
+
+  std::vector<R> ylmall(double muv, float phiv) const {
+    std::vector<R> y(nlm, 0);
+    std::vector<double> d;
+    const double fct = 1.0 / std::sqrt(2.0 * std::acos(-1.0));
+    double x = (double)(float)muv;
+    for (int m = 0; m <= mm; ++m) {
+      wigner_dm0(x, ml, m, d);
+      double cosm = 1, sinm = 0;
+      if (m > 0) { cosm = std::cos(m * (double)phiv); sinm = std::sin(m * (double)phiv); }
+      for (int l = m; l <= ml; ++l) {
+        double v = fct * d[l];
+        int j = sh_index(l, m, mm);
+        y[j] = (R)((cosm - sinm) * v);
+        y[j - 2 * m] = (R)((cosm + sinm) * v);
+      }
+    }
+    return y;
+  }
+
+  // TRANSFER_PA_TO_GRID -> INTERP_GRID -> TRILIN_INTERP_PROP -> PREPARE_PROP
+  // (src/polarized/shdomsub1.f:19-110, src/polarized/shdomsub2.f:313-390,
+  // src/polarized/shdom90.f90:17-350, src/polarized/shdomsub2.f:479-611).
+  bool transfer_properties() {
+    npart = p.npart; maxnmicro = p.maxnmicro; numphase = p.numphase;
+    nq = 8 * maxnmicro;
+    int npx = p.npx, npy = p.npy, npz = p.npz, ng = npx * npy * npz;
+    legen.assign((size_t)numphase * (nleg + 1), 0);
+    for (int i = 0; i < numphase; ++i)
+      for (int l = 0; l <= nleg; ++l)
+        legen[(size_t)i * (nleg + 1) + l] =
+            (l <= p.nlegp) ? (R)(legp[(size_t)i * (p.nlegp + 1) + l] / (float)(2 * l + 1)) : (R)0;
+    extmin = (double)(1.0e-5f / ((zlev[npz - 1] - zlev[0]) / (float)npz));
+    scatmin = 0.1 * extmin;
+    extinct.assign((size_t)npart * npts, 0); albedo.assign((size_t)npart * npts, 0);
+    total_ext.assign(npts, 0);
+    iphase.assign((size_t)npart * npts * nq, 1); phaseinterpwt.assign((size_t)npart * npts * nq, 0);
+    for (int ipa = 0; ipa < npart; ++ipa) {
+      for (int ipt = 0; ipt < npts; ++ipt) {
+        float x = gridpos[3 * ipt], y = gridpos[3 * ipt + 1], z = gridpos[3 * ipt + 2];
+        int il = 0, iu = npz;
+        while (iu - il > 1) { int im = (iu + il) / 2; if (z >= zlev[im - 1]) il = im; else iu = im; }
+        int iz = std::max(il, 1);
+        double w = (double)(z - zlev[iz - 1]) / (zlev[iz] - zlev[iz - 1]);
+        w = std::max(std::min(w, 1.0), 0.0);
+        int ix = (int)(x / p.delx) + 1;
+        if (std::fabs(x - npx * p.delx) < 0.01f * p.delx) ix = npx;
+        if (ix < 1 || ix > npx) { err = "TRILIN: Beyond X domain"; return false; }
+        int ixp = ix % npx + 1;
+        double u = (double)(x - p.delx * (ix - 1)) / p.delx;
+        u = std::max(std::min(u, 1.0), 0.0);
+        if (u < 1e-5) u = 0; if (u > 1 - 1e-5) u = 1;
+        int iy = (int)(y / p.dely) + 1;
+        if (std::fabs(y - npy * p.dely) < 0.01f * p.dely) iy = npy;
+        if (iy < 1 || iy > npy) { err = "TRILIN: Beyond Y domain"; return false; }
+        int iyp = iy % npy + 1;
+        double v = (double)(y - p.dely * (iy - 1)) / p.dely;
+        v = std::max(std::min(v, 1.0), 0.0);
+        if (v < 1e-5) v = 0; if (v > 1 - 1e-5) v = 1;
+        double f[8] = {(1 - u) * (1 - v) * (1 - w), u * (1 - v) * (1 - w), (1 - u) * v * (1 - w),
+                       u * v * (1 - w),             (1 - u) * (1 - v) * w, u * (1 - v) * w,
+                       (1 - u) * v * w,             u * v * w};
+        int i1 = (iz - 1) + npz * (iy - 1) + npz * npy * (ix - 1);
+        int i2 = (iz - 1) + npz * (iy - 1) + npz * npy * (ixp - 1);
+        int i3 = (iz - 1) + npz * (iyp - 1) + npz * npy * (ix - 1);
+        int i4 = (iz - 1) + npz * (iyp - 1) + npz * npy * (ixp - 1);
+        int ii[8] = {i1, i2, i3, i4, i1 + 1, i2 + 1, i3 + 1, i4 + 1};
+        const float *E = &extp[(size_t)ipa * ng];
+        const float *A = &albp[(size_t)ipa * ng];
+        double ext = 0, scat[8], scatter = 0;
+        for (int c = 0; c < 8; ++c) { ext += f[c] * E[ii[c]]; scat[c] = f[c] * E[ii[c]] * A[ii[c]]; scatter += scat[c]; }
+        R extr = (R)ext;
+        R alb = (ext > extmin) ? (R)(scatter / ext) : (R)(scatter / extmin);
+        extinct[(size_t)ipa * npts + ipt] = extr;
+        albedo[(size_t)ipa * npts + ipt] = alb;
+        int *IPH = &iphase[((size_t)ipa * npts + ipt) * nq];
+        R *PW = &phaseinterpwt[((size_t)ipa * npts + ipt) * nq];
+        for (int c = 0; c < 8; ++c)
+          for (int q = 0; q < maxnmicro; ++q) {
+            IPH[c * maxnmicro + q] = iphp[((size_t)ipa * ng + ii[c]) * maxnmicro + q];
+            double pw = phwtp[((size_t)ipa * ng + ii[c]) * maxnmicro + q];
+            PW[c * maxnmicro + q] = (R)(scatter >= scatmin ? pw * scat[c] / scatter : pw * scat[c] / scatmin);
+          }
+        for (int q = 0; q < nq; ++q)
+          for (int q2 = q + 1; q2 < nq; ++q2)
+            if (IPH[q] == IPH[q2]) { PW[q] += PW[q2]; PW[q2] = 0; }
+        std::vector<std::pair<R, int>> srt(nq);
+        for (int q = 0; q < nq; ++q) srt[q] = {PW[q], IPH[q]};
+        std::stable_sort(srt.begin(), srt.end(), [](const std::pair<R, int> &a, const std::pair<R, int> &b) { return a.first > b.first; });
+        for (int q = 0; q < nq; ++q) { PW[q] = srt[q].first; IPH[q] = srt[q].second; }
+        total_ext[ipt] += extr;
+      }
+    }
+    // PREPARE_PROP, 'N' interpolation method
+    if (p.deltam) {
+      for (int i = 0; i < numphase; ++i) {
+        R *L = &legen[(size_t)i * (nleg + 1)];
+        R f = L[ml + 1];
+        for (int l = 0; l <= ml; ++l) L[l] = L[l] - f;
+      }
+      for (int ipt = 0; ipt < npts; ++ipt) {
+        R s = 0;
+        for (int ipa = 0; ipa < npart; ++ipa) s += extinct[(size_t)ipa * npts + ipt];
+        total_ext[ipt] = total_ext[ipt] - s;
+        if (total_ext[ipt] < 0) total_ext[ipt] = 0;
+      }
+      for (int ipa = 0; ipa < npart; ++ipa)
+        for (int ipt = 0; ipt < npts; ++ipt) {
+          const int *IPH = &iphase[((size_t)ipa * npts + ipt) * nq];
+          const R *PW = &phaseinterpwt[((size_t)ipa * npts + ipt) * nq];
+          R f;
+          if (PW[0] >= phasemax) f = legen[(size_t)(IPH[0] - 1) * (nleg + 1) + ml + 1];
+          else { f = 0; for (int q = 0; q < nq; ++q) f += legen[(size_t)(IPH[q] - 1) * (nleg + 1) + ml + 1] * PW[q]; }
+          R &e = extinct[(size_t)ipa * npts + ipt];
+          R &a = albedo[(size_t)ipa * npts + ipt];
+          R anew = ((R)1 - f) * a / ((R)1 - a * f);
+          e = ((R)1 - a * f) * e;
+          a = anew;
+          total_ext[ipt] += e;
+        }
+    }
+    albmax = 0;
+    for (auto a : albedo) albmax = std::max(albmax, a);
+    return true;
+  }
+
+  // Per-point mixed, delta-M rescaled Legendre series (the LEGENT1 block of
+  // COMPUTE_SOURCE, src/polarized/shdomsub1.f:1432-1450).
+  void point_legen(int ipt, int ipa, std::vector<R> &lt, R &fout) const {
+    const int *IPH = &iphase[((size_t)ipa * npts + ipt) * nq];
+    const R *PW = &phaseinterpwt[((size_t)ipa * npts + ipt) * nq];
+    lt.assign(nleg + 1, 0);
+    if (PW[0] >= phasemax) {
+      for (int l = 0; l <= nleg; ++l) lt[l] = legen[(size_t)(IPH[0] - 1) * (nleg + 1) + l];
+    } else {
+      for (int q = 0; q < nq; ++q) {
+        if (PW[q] <= (R)1e-5) continue;
+        for (int l = 0; l <= nleg; ++l) lt[l] += legen[(size_t)(IPH[q] - 1) * (nleg + 1) + l] * PW[q];
+      }
+    }
+    fout = 0;
+    if (p.deltam) {
+      R f = lt[ml + 1];
+      fout = f;
+      for (int l = 0; l <= ml; ++l) lt[l] = lt[l] / ((R)1 - f);
+    }
+  }
+
+  // DIRECT_BEAM_PROP (src/polarized/shdom90.f90:352-867) via MAKE_DIRECT
+  // (src/polarized/shdomsub2.f:393-476); regular property grid, no gas.
+  void make_direct() {
+    int npx = p.npx, npy = p.npy, npz = p.npz, ng = npx * npy * npz;
+    std::vector<double> extdirp(ng, 0.0);
+    for (int ip = 0; ip < ng; ++ip) {
+      float acc = 0.f;
+      for (int ipa = 0; ipa < npart; ++ipa) {
+        double e = extp[(size_t)ipa * ng + ip], a = albp[(size_t)ipa * ng + ip];
+        if (p.deltam) {
+          int L = ml + 1;
+          double f = 0;
+          for (int q = 0; q < maxnmicro; ++q) {
+            int iph = iphp[((size_t)ipa * ng + ip) * maxnmicro + q];
+            f += phwtp[((size_t)ipa * ng + ip) * maxnmicro + q] *
+                 (double)(legp[(size_t)(iph - 1) * (p.nlegp + 1) + L] / (float)(2 * L + 1));
+          }
+          e = (1.0 - a * f) * e;
+        }
+        acc = (float)(acc + e);
+      }
+      extdirp[ip] = acc;
+    }
+    int ipdirect = ipflag;
+    if (ipflag & 4) ipdirect = 0;
+    double sunmu = -(double)p.solarmu;
+    double sunaz = (double)(float)(p.solaraz + (float)std::acos(-1.0f));
+    double cx = std::sqrt(1.0 - sunmu * sunmu) * std::cos(sunaz);
+    double cy = std::sqrt(1.0 - sunmu * sunmu) * std::sin(sunaz);
+    double cz = std::fabs(sunmu), cxinv, cyinv, czinv;
+    if (std::fabs(cx) > 1e-6) cxinv = 1.0 / cx; else { cx = 0; cxinv = 1e20; }
+    if (std::fabs(cy) > 1e-6) cyinv = 1.0 / cy; else { cy = 0; cyinv = 1e20; }
+    if (std::fabs(cz) > 1e-6) czinv = 1.0 / cz; else { cz = 0; czinv = 1e20; }
+    int di = cx >= 0 ? 1 : -1, dj = cy >= 0 ? 1 : -1, dk = cz >= 0 ? 1 : -1;
+    double epsz = 1.0e-6 * (zlev[npz - 1] - zlev[0]);
+    double epss = 1.0e-3 * (zlev[npz - 1] - zlev[0]) / npz;
+    if (!(ipdirect & 1)) epss = std::max(epss, 1.0e-4 * p.delx);
+    if (!(ipdirect & 2)) epss = std::max(epss, 1.0e-4 * p.dely);
+    double delxd = p.delx, delyd = p.dely;
+    epss = std::max(std::max(0.001 * delxd, 0.001 * delyd), epss);
+    double xdomain = delxd * npx, ydomain = delyd * npy;
+    dirflux.assign(npts, 0);
+    for (int ipt = 0; ipt < npts; ++ipt) {
+      double z = gridpos[3 * ipt + 2], x = gridpos[3 * ipt], y = gridpos[3 * ipt + 1];
+      int il = 0, iu = npz;
+      while (iu - il > 1) { int im = (iu + il) / 2; if (z >= zlev[im - 1]) il = im; else iu = im; }
+      int k = std::max(il, 1);
+      int i = (int)(x / delxd) + 1;
+      if (i > npx && std::fabs(x - xdomain) < 0.001 * delxd) i = npx;
+      int j = (int)(y / delyd) + 1;
+      if (j > npy && std::fabs(y - ydomain) < 0.001 * delyd) j = npy;
+      double xe = x, ye = y, ze = z, xp = xe, yp = ye, zp = ze;
+      bool constx = ipdirect & 1, consty = ipdirect & 2;
+      if (cx == 0.0) constx = true;
+      if (cy == 0.0) consty = true;
+      if ((bcflag & 1) && (std::fabs(x) < 0.01 * delxd || std::fabs(x - (npx - 1) * delxd) < 0.01 * delxd)) constx = true;
+      if ((bcflag & 2) && (std::fabs(y) < 0.01 * delyd || std::fabs(y - (npy - 1) * delyd) < 0.01 * delyd)) consty = true;
+      double path = 0.0;
+      int guard = 0;
+      while (std::fabs(ze - zlev[npz - 1]) > epsz && guard++ < 10000000) {
+        int ipn = i + 1;
+        if (i == npx) ipn = (bcflag & 1) ? npx : 1;
+        int jpn = j + 1;
+        if (j == npy) jpn = (bcflag & 2) ? npy : 1;
+        double x0 = delxd * (i - 1), x1 = x0 + delxd, y0 = delyd * (j - 1), y1 = y0 + delyd;
+        double z0 = zlev[k - 1], z1 = zlev[k];
+        int I1 = (k - 1) + npz * (j - 1) + npz * npy * (i - 1);
+        int I2 = (k - 1) + npz * (j - 1) + npz * npy * (ipn - 1);
+        int I3 = (k - 1) + npz * (jpn - 1) + npz * npy * (i - 1);
+        int I4 = (k - 1) + npz * (jpn - 1) + npz * npy * (ipn - 1);
+        double e1 = extdirp[I1], e2 = extdirp[I2], e3 = extdirp[I3], e4 = extdirp[I4];
+        double e5 = extdirp[I1 + 1], e6 = extdirp[I2 + 1], e7 = extdirp[I3 + 1], e8 = extdirp[I4 + 1];
+        double sox, soy, soz;
+        if (constx) sox = 1e30; else if (cx > 0) { sox = (x1 - xe) * cxinv; xp = x1; } else { sox = (x0 - xe) * cxinv; xp = x0; }
+        if (consty) soy = 1e30; else if (cy > 0) { soy = (y1 - ye) * cyinv; yp = y1; } else { soy = (y0 - ye) * cyinv; yp = y0; }
+        if (cz > 0) { soz = (z1 - ze) * czinv; zp = z1; } else if (cz < 0) { soz = (z0 - ze) * czinv; zp = z0; } else soz = 1e30;
+        double xoffs = 0, yoffs = 0, so;
+        if (soz <= sox && soz <= soy) {
+          so = soz;
+          if (!constx) xp = xe + so * cx;
+          if (!consty) yp = ye + so * cy;
+          k += dk;
+        } else if (sox <= soy) {
+          so = sox;
+          if (!consty) yp = ye + so * cy;
+          zp = ze + so * cz;
+          i += di;
+          if (i == 0) { if (bcflag & 1) { i = 1; constx = true; } else { i = npx; xoffs = xdomain; } }
+          else if (i == npx + 1) { if (bcflag & 1) { i = npx; constx = true; } else { i = 1; xoffs = -xdomain; } }
+        } else {
+          so = soy;
+          if (!constx) xp = xe + so * cx;
+          zp = ze + so * cz;
+          j += dj;
+          if (j == 0) { if (bcflag & 2) { j = 1; consty = true; } else { j = npy; yoffs = ydomain; } }
+          else if (j == npy + 1) { if (bcflag & 2) { j = npy; consty = true; } else { j = 1; yoffs = -ydomain; } }
+        }
+        so = std::max(so, 0.0);
+        double ax = 1.0 / (x1 - x0), ay = 1.0 / (y1 - y0), az = 1.0 / (z1 - z0);
+        double u0 = (xe - x0) * ax, v0 = (ye - y0) * ay, w0 = (ze - z0) * az;
+        double u1 = (xp - x0) * ax, v1 = (yp - y0) * ay, w1 = (zp - z0) * az;
+        double u0m = 1 - u0, v0m = 1 - v0, w0m = 1 - w0;
+        double du = u1 - u0, dv = v1 - v0, dw = w1 - w0;
+        double uv = u0 * v0, umv = u0m * v0, uvm = u0 * v0m, umvm = u0m * v0m;
+        double uw = u0 * w0, umw = u0m * w0, uwm = u0 * w0m, umwm = u0m * w0m;
+        double vw = v0 * w0, vmw = v0m * w0, vwm = v0 * w0m, vmwm = v0m * w0m;
+        double A = (e1 * u0m + e2 * u0) * vmwm + (e3 * u0m + e4 * u0) * vwm + (e5 * u0m + e6 * u0) * vmw +
+                   (e7 * u0m + e8 * u0) * vw;
+        double b1 = -du * vmwm - dv * umwm - dw * umvm, b2 = du * vmwm - dv * uwm - dw * uvm;
+        double b3 = -du * vwm + dv * umwm - dw * umv, b4 = du * vwm + dv * uwm - dw * uv;
+        double b5 = -du * vmw - dv * umw + dw * umvm, b6 = du * vmw - dv * uw + dw * uvm;
+        double b7 = -du * vw + dv * umw + dw * umv, b8 = du * vw + dv * uw + dw * uv;
+        double B = b1 * e1 + b2 * e2 + b3 * e3 + b4 * e4 + b5 * e5 + b6 * e6 + b7 * e7 + b8 * e8;
+        double VW = dv * dw, vwu = VW * u0, vwum = VW * u0m, UW = du * dw, uwv = UW * v0, uwvm = UW * v0m;
+        double UV = du * dv, uvw = UV * w0, uvwm = UV * w0m;
+        double c1 = vwum + uwvm + uvwm, c2 = vwu - uwvm - uvwm, c3 = -vwum + uwv - uvwm, c4 = -vwu - uwv + uvwm;
+        double c5 = -vwum - uwvm + uvw, c6 = -vwu + uwvm - uvw, c7 = vwum - uwv - uvw, c8 = vwu + uwv + uvw;
+        double C = c1 * e1 + c2 * e2 + c3 * e3 + c4 * e4 + c5 * e5 + c6 * e6 + c7 * e7 + c8 * e8;
+        double D = du * dv * dw * (e2 + e3 + e5 + e8 - e1 - e4 - e6 - e7);
+        path += so * (A + 0.5 * B + 0.3333333333333333 * C + 0.25 * D);
+        xe = xp + xoffs; ye = yp + yoffs; ze = zp;
+      }
+      dirflux[ipt] = (R)(p.solarflux * std::exp(-path));
+    }
+  }
+
+  // INIT_RADIANCE / EDDRTF / TRIDIAG (src/polarized/shdomsub2.f:614-1058),
+  // solar source, base grid columns.
+  void init_radiance() {
+    radiance.assign((size_t)npts * nlm, 0);
+    rshptr.assign(npts + 2, 0);
+    const float pi = (float)std::acos(-1.0f);
+    const float c0 = std::sqrt(1.0f / pi), c1 = std::sqrt(3.0f / (4 * pi));
+    int nlayer = nz - 1, nxy = nx1 * ny1;
+    std::vector<float> od(nlayer + 1), al(nlayer + 1), as(nlayer + 1);
+    std::vector<double> fl(2 * (nlayer + 1));
+    int ir = 0;
+    std::vector<R> lt; R fdum;
+    for (int col = 0; col < nxy; ++col) {
+      for (int iz = 0; iz < nlayer; ++iz) {
+        int L = nz - 1 - iz - 1;  // 0-based layer from the top
+        int i0 = iz + nz * col, i1 = iz + 1 + nz * col;
+        float ext0 = (float)total_ext[i0], ext1 = (float)total_ext[i1];
+        float scat0 = 0, scat1 = 0, g0 = 0, g1 = 0;
+        for (int ipa = 0; ipa < npart; ++ipa) {
+          scat0 += (float)(albedo[(size_t)ipa * npts + i0] * extinct[(size_t)ipa * npts + i0]);
+          scat1 += (float)(albedo[(size_t)ipa * npts + i1] * extinct[(size_t)ipa * npts + i1]);
+        }
+        od[L] = (zgrid[iz + 1] - zgrid[iz]) * (ext0 + ext1) / 2;
+        al[L] = (ext0 + ext1 > 0) ? (scat0 + scat1) / (ext0 + ext1) : 0.f;
+        for (int ipa = 0; ipa < npart; ++ipa) {
+          point_legen(i0, ipa, lt, fdum);
+          g0 += (float)(albedo[(size_t)ipa * npts + i0] * extinct[(size_t)ipa * npts + i0] * lt[1]);
+          point_legen(i1, ipa, lt, fdum);
+          g1 += (float)(albedo[(size_t)ipa * npts + i1] * extinct[(size_t)ipa * npts + i1] * lt[1]);
+        }
+        as[L] = (scat0 + scat1 > 0) ? (g0 + g1) / (scat0 + scat1) : 0.f;
+      }
+      eddrtf(nlayer, od, al, as, fl);
+      for (int iz = 0; iz < nz; ++iz) {
+        int L = nz - 1 - iz;
+        R *rad = &radiance[(size_t)ir];
+        rad[0] = (R)(c0 * (float)(fl[2 * L] + fl[2 * L + 1]));
+        rad[1] = 0;
+        rad[2] = (R)(c1 * (float)(fl[2 * L] - fl[2 * L + 1]));
+        rad[3] = 0;
+        ir += 4;
+        rshptr[iz + nz * col + 1] = ir;
+      }
+    }
+    rshptr[npts + 1] = ir;
+  }
+
+  void eddrtf(int nlayer, const std::vector<float> &od, const std::vector<float> &al,
+              const std::vector<float> &as, std::vector<double> &fluxout) {
+    int n = 2 * nlayer + 2;
+    std::vector<double> lower(n + 1), upper(n + 1), diag(n + 1), rhs(n + 1);
+    const double pi = 3.1415926535;
+    double mu0 = std::fabs((double)p.solarmu), tau = 0.0, sf = p.solarflux;
+    int i = 2;
+    for (int l = 0; l < nlayer; ++l) {
+      double deltau = od[l], trans, reflect, sourcep, sourcem;
+      if (deltau == 0.0) { trans = 1; reflect = 0; sourcep = 0; sourcem = 0; }
+      else {
+        double omega = al[l], g = as[l];
+        double r = (1.0 - omega * (4.0 - 3.0 * g)) / 4.0, t = (7.0 - omega * (4.0 + 3.0 * g)) / 4.0;
+        double lambda = std::sqrt(3.0 * (1.0 - omega) * (1.0 - omega * g));
+        double d, x1 = 0, x2 = 0, exlp = 0, exlm = 0;
+        if (lambda == 0.0) { d = 1.0 / (1.0 + t * deltau); trans = d; reflect = -r * deltau * d; }
+        else {
+          x1 = -r; x2 = lambda + t;
+          exlp = std::exp(std::min(lambda * deltau, 75.0)); exlm = 1.0 / exlp;
+          trans = 2. * lambda / (x2 * exlp + (lambda - t) * exlm);
+          reflect = x1 * (exlp - exlm) * trans / (2. * lambda);
+          d = 1.0 / (x2 * x2 * exlp - x1 * x1 * exlm);
+        }
+        double ds = 1.0 / (lambda * lambda - 1.0 / (mu0 * mu0));
+        double b1 = 0.5 * omega * (sf / mu0) * std::exp(-tau / mu0) * ds;
+        double b2 = 0.5 * omega * (sf / mu0) * std::exp(-(tau + deltau) / mu0) * ds;
+        double solpp = 1.0 + 1.5 * g * mu0, solpm = -1.0 + 1.5 * g * mu0;
+        double radp1p = ((t + 1.0 / mu0) * solpp + r * solpm) * b1;
+        double radp2m = ((-t + 1.0 / mu0) * solpm - r * solpp) * b2;
+        double radp2p = ((t + 1.0 / mu0) * solpp + r * solpm) * b2;
+        double radp1m = ((-t + 1.0 / mu0) * solpm - r * solpp) * b1;
+        if (lambda == 0.0) {
+          double A = (r * deltau * radp1p - radp2m) * d, B = -(r * radp1p + t * radp2m) * d;
+          sourcep = (B - t * (A + B * deltau)) / r + radp2p;
+          sourcem = A + radp1m;
+        } else {
+          double cp = (x1 * exlm * radp1p - x2 * radp2m) * d, cm = (-x2 * exlp * radp1p + x1 * radp2m) * d;
+          sourcep = x1 * cp * exlp + x2 * cm * exlm + radp2p;
+          sourcem = x2 * cp + x1 * cm + radp1m;
+        }
+        tau += deltau;
+      }
+      diag[i] = -reflect; diag[i + 1] = -reflect;
+      lower[i] = 1.0; lower[i + 1] = -trans;
+      upper[i] = -trans; upper[i + 1] = 1.0;
+      rhs[i] = sourcem; rhs[i + 1] = sourcep;
+      i += 2;
+    }
+    double gndemis = 1.0 - (double)p.gndalbedo;
+    double gndflux = (1.0 - gndemis) * sf * std::exp(-tau / mu0);
+    double skyflux = pi * p.skyrad;
+    rhs[1] = skyflux; diag[1] = 0.0; upper[1] = 1.0;
+    diag[n] = -(1.0 - gndemis); lower[n] = 1.0; rhs[n] = gndflux;
+    // TRIDIAG (Linpack DGTSL style with pivoting), 1-based arrays
+    lower[1] = diag[1]; diag[1] = upper[1]; upper[1] = 0.0; upper[n] = 0.0;
+    for (int k = 1; k <= n - 1; ++k) {
+      if (std::fabs(lower[k + 1]) >= std::fabs(lower[k])) {
+        std::swap(lower[k + 1], lower[k]); std::swap(diag[k + 1], diag[k]);
+        std::swap(upper[k + 1], upper[k]); std::swap(rhs[k + 1], rhs[k]);
+      }
+      double t = -lower[k + 1] / lower[k];
+      lower[k + 1] = diag[k + 1] + t * diag[k];
+      diag[k + 1] = upper[k + 1] + t * upper[k];
+      upper[k + 1] = 0.0;
+      rhs[k + 1] = rhs[k + 1] + t * rhs[k];
+    }
+    rhs[n] = rhs[n] / lower[n];
+    rhs[n - 1] = (rhs[n - 1] - diag[n - 1] * rhs[n]) / lower[n - 1];
+    for (int kb = 1; kb <= n - 2; ++kb) {
+      int k = n - 2 - kb + 1;
+      rhs[k] = (rhs[k] - diag[k] * rhs[k + 1] - upper[k] * rhs[k + 2]) / lower[k];
+    }
+    fluxout.assign(2 * (nlayer + 1), 0.0);
+    for (int l = 0, ii = 1; l <= nlayer; ++l, ii += 2) {
+      fluxout[2 * l] = (float)rhs[ii];
+      fluxout[2 * l + 1] = (float)rhs[ii + 1];
+    }
+  }
+
+  // Per-point source function SH vector (CALC_SOURCE_PNT_UNPOL with the
+  // NEWMETHOD species mixing, src/polarized/shdomsub1.f:913-962, :1413-1485).
+  void point_source(int i, std::vector<R> &sourcet, const std::vector<R> &rad, int ir, int nr,
+                    std::vector<R> &lt, std::vector<R> &lt1) const {
+    double alb = 0.0;
+    lt.assign(nleg + 1, 0);
+    R fdum;
+    for (int ipa = 0; ipa < npart; ++ipa) {
+      double scat = (double)(R)(extinct[(size_t)ipa * npts + i] * albedo[(size_t)ipa * npts + i]);
+      alb += scat;
+      point_legen(i, ipa, lt1, fdum);
+      for (int l = 0; l <= nleg; ++l) lt[l] = (R)(lt[l] + scat * lt1[l]);
+    }
+    if (alb > 1e-10) { for (int l = 0; l <= nleg; ++l) lt[l] = (R)(lt[l] / alb); }
+    else { for (int l = 0; l <= nleg; ++l) lt[l] = lt[l] / (R)npart; }
+    R ext = total_ext[i];
+    if (ext > (R)1e-10) alb = alb / ext; else alb = 0.0;
+    lt[0] = 1;
+    R albr = (R)alb;
+    R flux0 = dirflux[i] * ((R)1 / std::fabs((R)p.solarmu));
+    sourcet.assign(nlm, 0);
+    for (int j = 0; j < nlm; ++j) sourcet[j] = flux0 * albr * lt[lofj[j]] * ylmsun[j];
+    for (int j = 0; j < nr; ++j) sourcet[j] = sourcet[j] + albr * lt[lofj[j]] * rad[(size_t)ir + j];
+  }
+
+  // COMPUTE_SOURCE (src/polarized/shdomsub1.f:967-1611), NEWMETHOD, 'N'.
+  void compute_source(bool fixsh, bool first) {
+    std::vector<R> sourcet, lt, lt1;
+    R srcmin = (R)p.shacc;
+    if (!first) {
+      R djdot = 0, djold = 0, djnew = 0, jn = 0;
+      for (int i = 0; i < npts; ++i) {
+        int ir = rshptr[i], nr = rshptr[i + 1] - ir;
+        point_source(i, sourcet, radiance, ir, nr, lt, lt1);
+        int is = shptr[i];
+        if (p.accelflag) {
+          int iso = oshptr[i];
+          int ns = std::min(shptr[i + 1] - is, oshptr[i + 1] - iso);
+          for (int j = 0; j < ns; ++j) {
+            R dn = sourcet[j] - source[(size_t)is + j];
+            djdot += dn * delsource[(size_t)iso + j];
+            djold += delsource[(size_t)iso + j] * delsource[(size_t)iso + j];
+            djnew += dn * dn;
+            jn += source[(size_t)is + j] * source[(size_t)is + j];
+          }
+        } else {
+          int ns = shptr[i + 1] - is;
+          for (int j = 0; j < ns; ++j) {
+            R dn = sourcet[j] - source[(size_t)is + j];
+            djnew += dn * dn;
+            jn += source[(size_t)is + j] * source[(size_t)is + j];
+          }
+        }
+      }
+      deljdot = djdot; deljold = djold; deljnew = djnew; jnorm = jn;
+      if (p.accelflag) {
+        for (int i = 0; i < npts; ++i) {
+          int ir = rshptr[i], nr = rshptr[i + 1] - ir;
+          point_source(i, sourcet, radiance, ir, nr, lt, lt1);
+          int is = shptr[i], ns = shptr[i + 1] - is;
+          oshptr[i] = is;
+          for (int j = 0; j < ns; ++j) delsource[(size_t)is + j] = sourcet[j] - source[(size_t)is + j];
+        }
+        oshptr[npts] = shptr[npts];
+      }
+    }
+    int is = 0;
+    for (int i = 0; i < npts; ++i) {
+      int ir = rshptr[i], nr = rshptr[i + 1] - ir;
+      point_source(i, sourcet, radiance, ir, nr, lt, lt1);
+      int ns;
+      if (fixsh) ns = shptr[i + 1] - is;
+      else {
+        int js = 0;  // solar source
+        for (int j = 1; j <= nlm; ++j)
+          if (std::fabs(sourcet[j - 1]) > srcmin) js = j;
+        if (js == 0) ns = 0;
+        else {
+          int ls = lofj[js - 1];
+          ns = (ls <= mm) ? ls * (ls + 1) + ls + 1 : (2 * mm + 1) * ls - mm * (mm - 1 + 1) + mm + 1;
+        }
+        shptr[i] = is;
+      }
+      for (int j = 0; j < ns; ++j) source[(size_t)is + j] = sourcet[j];
+      is += ns;
+    }
+    shptr[npts] = is;
+  }
+
+  // RADIANCE_TRUNCATION (src/polarized/shdomsub1.f:1615-1803), 'N', no new points.
+  void radiance_truncation(bool fixsh) {
+    std::vector<int> newr(npts + 2, 0);
+    if (!fixsh) {
+      R radmin = (R)p.shacc;
+      bool notend = true;
+      int iro = 0, ir = 0;
+      newr[0] = 0;
+      for (int i = 0; i < npts; ++i) {
+        int nro = rshptr[i + 1] - iro;
+        if (nro == 0) notend = false;
+        R ext = total_ext[i];
+        int lr;
+        if (notend) {
+          std::vector<R> f(npart, 0);
+          if (p.deltam) {
+            for (int ipa = 0; ipa < npart; ++ipa) {
+              std::vector<R> lt; R ff;
+              const int *IPH = &iphase[((size_t)ipa * npts + i) * nq];
+              const R *PW = &phaseinterpwt[((size_t)ipa * npts + i) * nq];
+              if (PW[0] >= phasemax) f[ipa] = legen[(size_t)(IPH[0] - 1) * (nleg + 1) + ml + 1];
+              else {
+                // The reference indexes LEGEN(Q,ML+1,...) with the Stokes slot
+                // (src/polarized/shdomsub1.f:1688); for scalar tables this
+                // reads the series at L=ML+Q.  Restated as such.
+                for (int q = 0; q < nq; ++q) {
+                  if (PW[q] <= (R)1e-5) continue;
+                  int L = ml + 1 + q;
+                  R v = (L <= nleg) ? legen[(size_t)(IPH[q] - 1) * (nleg + 1) + L]
+                                    : legen[(size_t)(IPH[q] - 1) * (nleg + 1) + std::min(L, nleg)];
+                  f[ipa] += v * PW[q];
+                }
+              }
+              (void)lt; (void)ff;
+            }
+            for (int ipa = 0; ipa < npart; ++ipa) f[ipa] = (R)1 / ((R)1 - f[ipa]);
+          }
+          lr = 1;
+          for (int l = 1; l <= ml; ++l) {
+            R rad = 0;
+            for (int ipa = 0; ipa < npart; ++ipa) {
+              R w = (ext == 0) ? (R)1 : extinct[(size_t)ipa * npts + i] / ext;
+              if (w == 0) continue;
+              const int *IPH = &iphase[((size_t)ipa * npts + i) * nq];
+              const R *PW = &phaseinterpwt[((size_t)ipa * npts + i) * nq];
+              R legt;
+              if (PW[0] >= phasemax) legt = legen[(size_t)(IPH[0] - 1) * (nleg + 1) + l];
+              else {
+                legt = 0;
+                for (int q = 0; q < nq; ++q) {
+                  if (PW[q] <= (R)1e-5) continue;
+                  legt += legen[(size_t)(IPH[q] - 1) * (nleg + 1) + l] * PW[q];
+                }
+              }
+              if (p.deltam) legt = legt * f[ipa];
+              rad += w * albedo[(size_t)ipa * npts + i] * legt * radiance[(size_t)iro];
+            }
+            if (rad > radmin) lr = l;
+          }
+        } else {
+          lr = ml;
+        }
+        iro += nro;
+        int ns = std::max(1, shptr[i + 1] - shptr[i]);
+        int ls = lofj[ns - 1];
+        lr = std::min(lr, ls + ml / 8 + 2);
+        if (p.highorderrad) lr = ml;
+        int nr = (lr <= mm) ? lr * (lr + 1) + lr + 1 : (2 * mm + 1) * lr - mm * (mm - 1 + 1) + mm + 1;
+        ir += nr;
+        newr[i + 1] = ir;
+      }
+      newr[npts + 1] = ir;
+    } else {
+      int ir = 0;
+      newr[0] = 0;
+      for (int i = 0; i < npts; ++i) {
+        int nr = std::max(4, shptr[i + 1] - shptr[i]);
+        if (p.highorderrad) nr = nlm;
+        ir += nr;
+        newr[i + 1] = ir;
+      }
+      newr[npts + 1] = ir;
+    }
+    // RSHPTR only changes the view onto RADIANCE (which PATH_INTEGRATION zeroes
+    // and rebuilds); COMPUTE_SOURCE reads the radiance with the old pointer
+    // before this routine runs, so the array content is left in place.
+    rshptr = newr;
+  }
+
+  void boundary_points() {
+    topp.clear(); botp.clear();
+    for (int i = 0; i < npts; ++i) {
+      if (gridpos[3 * i + 2] >= zgrid[nz - 1]) topp.push_back(i);
+      if (gridpos[3 * i + 2] <= zgrid[0]) botp.push_back(i);
+    }
+    sfcgridalb.assign(botp.size(), (R)p.gndalbedo);
+    if (p.sfc_variable) {
+      // PREP_SURFACE periodic surface grid + SURFACE_PARM_INTERP
+      // (src/surface.f:2-270, src/polarized/shdomsub1.f:2218-2268).
+      int nxs = p.nxsfc, nys = p.nysfc;
+      std::vector<float> g((size_t)(nxs + 1) * (nys + 1));
+      for (int iy = 0; iy <= nys; ++iy)
+        for (int ix = 0; ix <= nxs; ++ix)
+          g[(size_t)iy * (nxs + 1) + ix] = sfcalb[(size_t)(iy % nys) * nxs + (ix % nxs)];
+      for (size_t b = 0; b < botp.size(); ++b) {
+        int i = botp[b];
+        float rx = gridpos[3 * i] / p.delxsfc, ry = gridpos[3 * i + 1] / p.delysfc;
+        int ix = std::max(1, std::min(nxs, (int)rx + 1)), iy = std::max(1, std::min(nys, (int)ry + 1));
+        float u = std::max(0.0f, std::min(1.0f, rx - (ix - 1))), v = std::max(0.0f, std::min(1.0f, ry - (iy - 1)));
+        auto G = [&](int x, int y) { return g[(size_t)(y - 1) * (nxs + 1) + (x - 1)]; };
+        sfcgridalb[b] = (R)((1 - u) * (1 - v) * G(ix, iy) + (1 - u) * v * G(ix, iy + 1) +
+                            u * (1 - v) * G(ix + 1, iy) + u * v * G(ix + 1, iy + 1));
+      }
+    }
+  }
+
+  // FIXED/VARIABLE_LAMBERTIAN_BOUNDARY (src/polarized/shdomsub1.f:2438-2529).
+  void lambertian_boundary() {
+    bcrad_bot.assign(botp.size(), 0);
+    const R opi = (R)1 / (R)std::acos(-1.0f);
+    for (size_t b = 0; b < botp.size(); ++b) {
+      int i = botp[b];
+      bcrad_bot[b] = opi * sfcgridalb[b] * (dirflux[i] + fluxes[2 * (size_t)i]);
+    }
+  }
+
+  bool init_solution() {
+    make_direct();
+    init_radiance();
+    source.assign((size_t)npts * nlm, 0);
+    delsource.assign(p.accelflag ? (size_t)npts * nlm : 1, 0);
+    shptr.assign(npts + 1, 0); oshptr.assign(npts + 1, 0);
+    fluxes.assign((size_t)2 * npts, 0);
+    compute_source(false, true);
+    if (p.accelflag) {
+      oshptr = shptr;
+      std::fill(delsource.begin(), delsource.end(), (R)0);
+    }
+    boundary_points();
+    iter = 0; solcrit = 1; accel_a = 0;
+    return true;
+  }
+
+  // SH_TO_DO_UNPOL (src/polarized/shdomsub1.f:2928-3036) with the DFT branch.
+  void sh_to_do(int imu, std::vector<R> &work) const {
+    int n0 = nphi0[imu], nm = 2 * mm + 1;
+    std::vector<R> sumuv(nm), sumcs(nm);
+    for (int i = 0; i < npts; ++i) {
+      int is = shptr[i], nsh = shptr[i + 1] - is;
+      R *out = &work[(size_t)i * nphi0max];
+      if (nsh == 0) { for (int k = 0; k < n0; ++k) out[k] = 0; continue; }
+      int me = std::max(0, std::min(n0 / 2 - 1, mofj[nsh - 1]));
+      std::fill(sumuv.begin(), sumuv.end(), (R)0);
+      for (int j = 0; j < nsh; ++j) sumuv[mofj[j] + mm] += cmu1[(size_t)imu * nlm + j] * source[(size_t)is + j];
+      sumcs[mm] = sumuv[mm];
+      for (int m = 1; m <= me; ++m) {
+        sumcs[mm + m] = sumuv[mm + m] + sumuv[mm - m];
+        sumcs[mm - m] = sumuv[mm - m] - sumuv[mm + m];
+      }
+      for (int k = 0; k < n0; ++k) {
+        const R *c = &cphi1[((size_t)imu * nphi0max + k) * nm + mm];
+        R s = 0;
+        for (int m = -me; m <= me; ++m) s += c[m] * sumcs[mm + m];
+        out[k] = s;
+      }
+    }
+  }
+
+  // DO_TO_SH_UNPOL (src/polarized/shdomsub1.f:3164-3254) with the DFT branch.
+  void do_to_sh(int imu, const std::vector<R> &work) {
+    int n0 = nphi0[imu], nm = 2 * mm + 1;
+    std::vector<R> sumuv(nm), sumcs(nm);
+    int is = 0;
+    for (int i = 0; i < npts; ++i) {
+      int nsh = rshptr[i + 1] - rshptr[i];
+      std::fill(sumcs.begin(), sumcs.end(), (R)0);
+      int me = std::max(0, std::min(n0 / 2 - 1, mofj[std::max(nsh, 1) - 1]));
+      const R *in = &work[(size_t)i * nphi0max];
+      for (int m = -me; m <= me; ++m) {
+        R s = 0;
+        for (int k = 0; k < n0; ++k) s += cphi2[((size_t)imu * nphi0max + k) * nm + mm + m] * in[k];
+        sumcs[mm + m] = s;
+      }
+      sumuv[mm] = sumcs[mm];
+      for (int m = 1; m <= mm; ++m) {
+        sumuv[mm + m] = sumcs[mm + m] - sumcs[mm - m];
+        sumuv[mm - m] = sumcs[mm + m] + sumcs[mm - m];
+      }
+      for (int j = 0; j < nsh; ++j) radiance[(size_t)is + j] += cmu2[(size_t)imu * nlm + j] * sumuv[mofj[j] + mm];
+      is += nsh;
+    }
+  }
+
+  // BACK_INT_GRID3D_UNPOL (src/polarized/shdomsub1.f:3695-4038).
+  bool back_int_grid3d(float muv, float phiv, int kang, const std::vector<R> &work,
+                       std::vector<R> &gridrad) {
+    double eps = 1.0e-3 * (gridpos[3 * gridptr[7] + 2] - gridpos[3 * gridptr[0] + 2]);
+    const double pi = (double)(float)std::acos(-1.0f);
+    double smu = (double)std::sqrt(1.0f - muv * muv);
+    double cx = smu * std::cos((double)phiv + pi);
+    double cy = smu * std::sin((double)phiv + pi);
+    double cz = -(double)muv, cxinv, cyinv, czinv;
+    if (std::fabs(cx) > 1.0e-5) cxinv = 1.0 / cx; else { cx = 0; cxinv = 1.0e6; }
+    if (std::fabs(cy) > 1.0e-5) cyinv = 1.0 / cy; else { cy = 0; cyinv = 1.0e6; }
+    czinv = 1.0 / cz;
+    int bitx = cx < 0 ? 1 : 0, bity = cy < 0 ? 1 : 0, bitz;
+    if (cz < -1.0e-3) bitz = 1; else if (cz > 1.0e-3) bitz = 0; else { err = "BACK_INT_GRID: Bad MU"; return false; }
+    int ioct = 1 + bitx + 2 * bity + 4 * bitz;
+    static const int joctorder3[8] = {1, 3, 5, 7, 2, 4, 6, 8};
+    int joct = joctorder3[ioct - 1] - 1;
+    double transmin = p.transmin;
+    for (int iorder = 0; iorder < npts; ++iorder) {
+      int ipcell = sweep_cell[(size_t)joct * npts + iorder];
+      int ipt = gridptr[8 * ipcell + sweep_corner[(size_t)joct * npts + iorder]];
+      if (gridrad[ipt] >= 0) continue;
+      int icell = ipcell;
+      double rad = 0.0, transmit = 1.0;
+      double ext1 = total_ext[ipt], srcext1 = ext1 * work[(size_t)ipt * nphi0max + kang];
+      double xe = gridpos[3 * ipt], ye = gridpos[3 * ipt + 1], ze = gridpos[3 * ipt + 2];
+      bool validrad = false;
+      int guard = 0;
+      while (!validrad) {
+        if (icell < 0 || ++guard > 100000) { err = "BACK_INT_GRID: ICELL=0"; return false; }
+        bool ipinx = cellflags[icell] & 1, ipiny = cellflags[icell] & 2;
+        int iopp = gridptr[8 * icell + (8 - ioct)];
+        double sox = ipinx ? 1.0e20 : (gridpos[3 * iopp] - xe) * cxinv;
+        double soy = ipiny ? 1.0e20 : (gridpos[3 * iopp + 1] - ye) * cyinv;
+        double soz = (gridpos[3 * iopp + 2] - ze) * czinv;
+        double so = std::min(sox, std::min(soy, soz));
+        if (so < -eps) { err = "BACK_INT_GRID: SO<0"; return false; }
+        xe += so * cx; ye += so * cy; ze += so * cz;
+        int iface, jface;
+        if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; }
+        else if (soy <= soz) { iface = 3 - bity; jface = 1; }
+        else { iface = 5 - bitz; jface = 2; }
+        int inext = neighptr[6 * icell + iface];
+        const int *g = &gridptr[8 * icell];
+        int i1 = g[kGridFace[iface][0]], i2 = g[kGridFace[iface][1]], i3 = g[kGridFace[iface][2]],
+            i4 = g[kGridFace[iface][3]];
+        double u, v;
+        if (jface == 0) {
+          u = (ze - gridpos[3 * i1 + 2]) / (gridpos[3 * i3 + 2] - gridpos[3 * i1 + 2]);
+          v = ipiny ? 0.5 : (ye - gridpos[3 * i1 + 1]) / (gridpos[3 * i2 + 1] - gridpos[3 * i1 + 1]);
+        } else if (jface == 1) {
+          u = (ze - gridpos[3 * i1 + 2]) / (gridpos[3 * i3 + 2] - gridpos[3 * i1 + 2]);
+          v = ipinx ? 0.5 : (xe - gridpos[3 * i1]) / (gridpos[3 * i2] - gridpos[3 * i1]);
+        } else {
+          u = ipiny ? 0.5 : (ye - gridpos[3 * i1 + 1]) / (gridpos[3 * i3 + 1] - gridpos[3 * i1 + 1]);
+          v = ipinx ? 0.5 : (xe - gridpos[3 * i1]) / (gridpos[3 * i2] - gridpos[3 * i1]);
+        }
+        if (inext >= 0) {
+          if (jface == 0) xe = gridpos[3 * gridptr[8 * inext + ioct - 1]];
+          else if (jface == 1) ye = gridpos[3 * gridptr[8 * inext + ioct - 1] + 1];
+          else ze = gridpos[3 * gridptr[8 * inext + ioct - 1] + 2];
+        }
+        double f1 = (1 - u) * (1 - v), f2 = (1 - u) * v, f3 = u * (1 - v), f4 = u * v;
+        const R *W = work.data();
+        double ext0 = f1 * total_ext[i1] + f2 * total_ext[i2] + f3 * total_ext[i3] + f4 * total_ext[i4];
+        double srcext0 = f1 * W[(size_t)i1 * nphi0max + kang] * total_ext[i1] +
+                         f2 * W[(size_t)i2 * nphi0max + kang] * total_ext[i2] +
+                         f3 * W[(size_t)i3 * nphi0max + kang] * total_ext[i3] +
+                         f4 * W[(size_t)i4 * nphi0max + kang] * total_ext[i4];
+        double ext = 0.5 * (ext0 + ext1), tau = ext * so, transcell, abscell, src;
+        if (tau >= 0.5) { transcell = std::exp(-tau); abscell = 1.0 - transcell; }
+        else { abscell = tau * (1.0 - 0.5 * tau * (1.0 - 0.33333333333 * tau * (1 - 0.25 * tau))); transcell = 1.0 - abscell; }
+        if (tau <= 2.0) {
+          if (ext == 0.0) src = 0.0;
+          else src = (0.5 * (srcext0 + srcext1) + 0.08333333333 * (ext0 * srcext1 - ext1 * srcext0) * so) / ext;
+        } else {
+          double ext0p = ext0, srcext0p = srcext0;
+          if (tau > 4.0) { ext0p = ext1 + (ext0 - ext1) * 4.0 / tau; if (ext0 > 0.0) srcext0p = srcext0 * ext0p / ext0; }
+          src = 1.0 / (ext0p + ext1) * (srcext0p + srcext1 + (ext0p * srcext1 - ext1 * srcext0p) * 2.0 / (ext0p + ext1) * (1 - 2 / tau + 2 * transcell / abscell));
+        }
+        src = std::max(src, 0.0);
+        rad += transmit * src * abscell;
+        transmit *= transcell;
+        bool validface = gridrad[i1] >= -0.1 && gridrad[i2] >= -0.1 && gridrad[i3] >= -0.1 && gridrad[i4] >= -0.1;
+        if (inext < 0 || (transmit <= transmin && validface)) {
+          if (validface) {
+            validrad = true;
+            rad += transmit * (f1 * gridrad[i1] + f2 * gridrad[i2] + f3 * gridrad[i3] + f4 * gridrad[i4]);
+          } else { err = "BACK_INT_GRID3D: INEXTCELL=0"; return false; }
+        } else {
+          ext1 = ext0; srcext1 = srcext0; icell = inext;
+        }
+      }
+      gridrad[ipt] = (R)rad;
+    }
+    return true;
+  }
+
+  // BACK_INT_GRID1D (src/polarized/shdomsub1.f:4295-4465).
+  bool back_int_grid1d(float muv, int kang, const std::vector<R> &work, std::vector<R> &gridrad) {
+    double eps = 1.0e-3 * (gridpos[3 * gridptr[7] + 2] - gridpos[3 * gridptr[0] + 2]);
+    (void)eps;
+    double cz = -(double)muv, czinv = 1.0 / cz;
+    int bitz;
+    if (cz < -1.0e-3) bitz = 1; else if (cz > 1.0e-3) bitz = 0; else { err = "BACK_INT_GRID1D: Bad MU"; return false; }
+    int ioct = 1 + 4 * bitz;
+    int joct = bitz;  // JOCTORDER(1..4)=1, (5..8)=2
+    for (int iorder = 0; iorder < npts; ++iorder) {
+      int ipcell = sweep_cell[(size_t)joct * npts + iorder];
+      int ipt = gridptr[8 * ipcell + sweep_corner[(size_t)joct * npts + iorder]];
+      if (gridrad[ipt] >= 0) continue;
+      int icell = ipcell;
+      double transmit = 1.0, ext1 = total_ext[ipt], rad = 0.0;
+      double srcext1 = ext1 * work[(size_t)ipt * nphi0max + kang];
+      double ze = gridpos[3 * ipt + 2];
+      bool validrad = false;
+      int guard = 0;
+      while (!validrad) {
+        if (icell < 0 || ++guard > 100000) { err = "BACK_INT_GRID1D: ICELL=0"; return false; }
+        int iopp = gridptr[8 * icell + (8 - ioct)];
+        double so = (gridpos[3 * iopp + 2] - ze) * czinv;
+        ze += so * cz;
+        int iface = 5 - bitz;
+        int inext = neighptr[6 * icell + iface];
+        int i1 = gridptr[8 * icell + (iface == 4 ? 0 : 4)];
+        if (inext >= 0) ze = gridpos[3 * gridptr[8 * inext + ioct - 1] + 2];
+        double ext0 = total_ext[i1], srcext0 = total_ext[i1] * work[(size_t)i1 * nphi0max + kang];
+        double ext = 0.5 * (ext0 + ext1), tau = ext * so, transcell, abscell, src;
+        if (tau >= 0.5) { transcell = std::exp(-tau); abscell = 1.0 - transcell; }
+        else { abscell = tau * (1.0 - 0.5 * tau * (1.0 - 0.33333333333 * tau * (1 - 0.25 * tau))); transcell = 1.0 - abscell; }
+        if (tau <= 2.0) {
+          if (ext == 0.0) src = 0.0;
+          else src = (0.5 * (srcext0 + srcext1) + 0.08333333333 * (ext0 * srcext1 - ext1 * srcext0) * so) / ext;
+        } else {
+          double ext0p = ext0, srcext0p = srcext0;
+          if (tau > 4.0) { ext0p = ext1 + (ext0 - ext1) * 4.0 / tau; if (ext0 > 0.0) srcext0p = srcext0 * ext0p / ext0; }
+          src = 1.0 / (ext0p + ext1) * (srcext0p + srcext1 + (ext0p * srcext1 - ext1 * srcext0p) * 2.0 / (ext0p + ext1) * (1 - 2 / tau + 2 * transcell / abscell));
+        }
+        src = std::max(src, 0.0);
+        if (gridrad[i1] >= -0.1) {
+          validrad = true;
+          rad += transmit * (gridrad[i1] * transcell + src * abscell);
+        } else {
+          rad += transmit * src * abscell;
+          srcext1 = srcext0; transmit *= transcell; ext1 = ext0; icell = inext;
+        }
+      }
+      gridrad[ipt] = (R)rad;
+    }
+    return true;
+  }
+
+  // PATH_INTEGRATION (src/polarized/shdomsub1.f:1836-2167), Lambertian.
+  bool path_integration() {
+    if (!sweep_ready) sweeping_order();
+    std::fill(fluxes.begin(), fluxes.end(), (R)0);
+    std::vector<R> gridrad(npts, (R)-1);
+    radiance.assign((size_t)npts * nlm, 0);
+    std::vector<R> work((size_t)npts * nphi0max, 0);
+    for (int imu = 0; imu < nmu; ++imu) {
+      if (imu == nmu / 2) lambertian_boundary();
+      sh_to_do(imu, work);
+      for (int i = 0; i < npts; ++i)
+        for (int k = 0; k < nphi0[imu]; ++k) work[(size_t)i * nphi0max + k] = std::max((R)0, work[(size_t)i * nphi0max + k]);
+      for (int iphi = 0; iphi < nphi0[imu]; ++iphi) {
+        int iupdown;
+        if (mu[imu] < 0) {
+          iupdown = 0;
+          for (int t : topp) gridrad[t] = (R)p.skyrad;
+        } else {
+          iupdown = 1;
+          for (size_t b = 0; b < botp.size(); ++b) gridrad[botp[b]] = bcrad_bot[b];
+        }
+        bool ok;
+        if ((ipflag & 2) && (ipflag & 1)) ok = back_int_grid1d(mu[imu], iphi, work, gridrad);
+        else ok = back_int_grid3d(mu[imu], phi[(size_t)imu * nphi0max + iphi], iphi, work, gridrad);
+        if (!ok) return false;
+        for (int i = 0; i < npts; ++i) {
+          if (gridrad[i] < (R)-0.0001) { err = "PATH_INTEGRATION: Grid point has no value"; return false; }
+          work[(size_t)i * nphi0max + iphi] = gridrad[i];
+          gridrad[i] = -1;
+        }
+        R a = std::fabs((R)mu[imu]) * (R)wtdo[(size_t)imu * nphi0max + iphi];
+        for (int i = 0; i < npts; ++i) fluxes[2 * (size_t)i + iupdown] += a * work[(size_t)i * nphi0max + iphi];
+      }
+      do_to_sh(imu, work);
+    }
+    return true;
+  }
+
+  // CALC_ACCEL_SOLCRIT (src/shdom_nompi.f:317-348) and ACCELERATE_SOLUTION
+  // (src/polarized/shdomsub1.f:1807-1831).
+  void accel_solcrit() {
+    R accelpar;
+    if (p.accelflag && accel_a == 0 && deljnew < deljold) {
+      R r = std::sqrt(deljnew / deljold);
+      R theta = std::acos(deljdot / std::sqrt(deljold * deljnew));
+      R a = ((R)1 - r * std::cos(theta) + std::pow(r, (R)1 + (R)0.5 * (R)3.14159 / theta)) /
+                ((R)1 + r * r - (R)2 * r * std::cos(theta)) - (R)1;
+      accel_a = std::min((R)10, std::max((R)0, a));
+    } else {
+      accel_a = 0;
+    }
+    accelpar = accel_a;
+    if (jnorm > 0) solcrit = std::sqrt(deljnew / jnorm);
+    else if (deljnew == 0) solcrit = 0;
+    if (accelpar > 0) {
+      for (int i = 0; i < npts; ++i) {
+        int is = shptr[i], ns = shptr[i + 1] - is, isd = oshptr[i], nsd = oshptr[i + 1] - isd;
+        int nsc = std::min(ns, nsd);
+        for (int j = 0; j < nsc; ++j) source[(size_t)is + j] += accelpar * delsource[(size_t)isd + j];
+      }
+    }
+  }
+
+  // SOLUTION_ITERATIONS (src/polarized/shdomsub1.f:445-818), no splitting.
+  bool solution_iterations(int maxiter, int verbose) {
+    bool fixsh = false;
+    const R endadaptsol = (R)0.001;
+    while (iter < maxiter && solcrit > (R)p.solacc) {
+      ++iter;
+      radiance_truncation(fixsh);
+      if (!path_integration()) return false;
+      if (solcrit < endadaptsol || iter > p.iterfixsh) fixsh = true;
+      compute_source(fixsh, false);
+      accel_solcrit();
+      if (albmax < (R)p.solacc) solcrit = (R)p.solacc;
+      if (verbose)
+        std::printf("  %4d %8.3f %10.3e %8d %8.2f\n", iter, std::log10(std::max((double)solcrit, 1e-20)), 0.0,
+                    npts, (double)shptr[npts] / npts);
+    }
+    return true;
+  }
+
+  // ---------------------------------------------------------- rendering
+  // PRECOMPUTE_PHASE_CHECK (src/polarized/shdomsub4.f:2388-2491) on the
+  // unscaled table (at3d/solver.py:2800-2825).
+  int nscatangle = 0;
+  std::vector<R> phasetab;  // [nscatangle][numphase]
+  bool precompute_phase() {
+    int nlegp = std::max(p.nlegp, nleg);
+    nscatangle = std::max(36, std::min(721, 2 * nlegp));
+    phasetab.assign((size_t)nscatangle * numphase, 0);
+    const double pi = std::acos(-1.0), ofourpi = 1.0 / (4.0 * pi);
+    std::vector<double> d;
+    for (int j = 0; j < nscatangle; ++j) {
+      double x = std::cos(pi * (double)j / (nscatangle - 1));
+      // Legendre polynomials P_l(x) = d^l_{00}(x)
+      d.assign(nlegp + 1, 0.0);
+      d[0] = 1.0;
+      if (nlegp >= 1) d[1] = x;
+      for (int n = 1; n < nlegp; ++n) d[n + 1] = ((2 * n + 1) * x * d[n] - n * d[n - 1]) / (n + 1);
+      for (int iph = 0; iph < numphase; ++iph) {
+        double a1 = 0.0;
+        for (int l = 0; l <= nlegp; ++l) {
+          float lg = (l <= p.nlegp) ? legp[(size_t)iph * (p.nlegp + 1) + l] : 0.f;
+          double unsc = (double)(float)(lg / (float)(2 * l + 1));
+          a1 += (2.0 * l + 1.0) * unsc * d[l];
+        }
+        if (a1 <= 0.0) { err = "PRECOMPUTE_PHASE_CHECK: negative phase function"; return false; }
+        phasetab[(size_t)j * numphase + iph] = (R)(a1 * ofourpi);
+      }
+    }
+    return true;
+  }
+
+  // LOCATE_GRID_CELL (src/polarized/shdomsub2.f:4043-4211), base grid.
+  int locate_grid_cell(double &x0, double &y0, double z0) const {
+    if (!(bcflag & 1)) {
+      double xd = xgrid[nx] - xgrid[0];
+      if (x0 < xgrid[0]) x0 = x0 - xd * ((int)((x0 - xgrid[0]) / xd) - 1);
+      else if (x0 > xgrid[nx]) x0 = x0 - xd * (int)((x0 - xgrid[0]) / xd);
+    }
+    if (!(bcflag & 2)) {
+      double yd = ygrid[ny] - ygrid[0];
+      if (y0 < ygrid[0]) y0 = y0 - yd * ((int)((y0 - ygrid[0]) / yd) - 1);
+      else if (y0 > ygrid[ny]) y0 = y0 - yd * (int)((y0 - ygrid[0]) / yd);
+    }
+    int il = 0, iu, ix, iy, iz;
+    if (ipflag & 1) {
+      iu = nx;
+      while (iu - il > 1) { int im = (iu + il) / 2; if (x0 >= 0.5 * (xgrid[im - 1] + xgrid[im])) il = im; else iu = im; }
+      il += 1;
+    } else {
+      iu = nx + 1;
+      while (iu - il > 1) { int im = (iu + il) / 2; if (x0 >= xgrid[im - 1]) il = im; else iu = im; }
+    }
+    ix = std::max(il, 1);
+    il = 0;
+    if (ipflag & 2) {
+      iu = ny;
+      while (iu - il > 1) { int im = (iu + il) / 2; if (y0 >= 0.5 * (ygrid[im - 1] + ygrid[im])) il = im; else iu = im; }
+      il += 1;
+    } else {
+      iu = ny + 1;
+      while (iu - il > 1) { int im = (iu + il) / 2; if (y0 >= ygrid[im - 1]) il = im; else iu = im; }
+    }
+    iy = std::max(il, 1);
+    il = 0; iu = nz;
+    while (iu - il > 1) { int im = (iu + il) / 2; if (z0 >= zgrid[im - 1]) il = im; else iu = im; }
+    iz = std::max(il, 1);
+    int nxc = nx, nyc = ny;
+    if (bcflag & 1) {
+      nxc = nx + 1;
+      if (x0 < xgrid[0]) ix = 1; else if (x0 > xgrid[nx - 1]) ix = nx + 1; else ix = ix + 1;
+    }
+    if (bcflag & 2) {
+      nyc = ny + 1;
+      if (y0 < ygrid[0]) iy = 1; else if (y0 > ygrid[ny - 1]) iy = ny + 1; else iy = iy + 1;
+    }
+    return (iz - 1) + (nz - 1) * (iy - 1) + (nz - 1) * nyc * (ix - 1);
+  }
+
+  // INTEGRATE_1RAY + COMPUTE_SOURCE_1CELL_UNPOL + FIND_BOUNDARY_RADIANCE
+  // (src/polarized/shdomsub2.f:2311-2863, :3046-3192).
+  bool integrate_1ray(double mu2, double phi2, double x0, double y0, double z0, double &radout,
+                      std::string &err) const {
+    const double pi = std::acos(-1.0);
+    double eps = 1.0e-5 * (gridpos[3 * gridptr[7] + 2] - gridpos[3 * gridptr[0] + 2]);
+    int maxcellscross = 500 * std::max(nx, std::max(ny, nz));
+    std::vector<R> ylmdir = ylmall((double)(float)mu2, (float)phi2);
+    std::vector<R> singscat(numphase, 0);
+    bool tms = p.deltam;
+    if (tms) {
+      double cosscat = (double)p.solarmu * mu2 +
+                       std::sqrt((1.0 - (double)p.solarmu * p.solarmu) * (1.0 - mu2 * mu2)) * std::cos((double)p.solaraz - phi2);
+      cosscat = std::max(std::min(1.0, cosscat), -1.0);
+      float F = (float)((nscatangle - 1) * (std::acos(cosscat) / pi) + 1);
+      int J = std::min(nscatangle - 1, (int)F);
+      F = F - J;
+      for (int i = 0; i < numphase; ++i)
+        singscat[i] = (R)((1 - F) * phasetab[(size_t)(J - 1) * numphase + i] + F * phasetab[(size_t)J * numphase + i]);
+    }
+    double cx = std::sqrt(1.0 - mu2 * mu2) * std::cos(phi2 - pi), cy = std::sqrt(1.0 - mu2 * mu2) * std::sin(phi2 - pi);
+    double cz = -mu2, cxinv, cyinv, czinv;
+    if (std::fabs(cx) > 1e-6) cxinv = 1.0 / cx; else { cx = 0; cxinv = 1e6; }
+    if (std::fabs(cy) > 1e-6) cyinv = 1.0 / cy; else { cy = 0; cyinv = 1e6; }
+    if (std::fabs(cz) > 1e-6) czinv = 1.0 / cz; else { cz = 0; czinv = 1e6; }
+    int bitx = cx < 0, bity = cy < 0, bitz = cz < 0;
+    int ioct = 1 + bitx + 2 * bity + 4 * bitz;
+    float xm = 0.5f * (xgrid[0] + xgrid[nx - 1]), ym = 0.5f * (ygrid[0] + ygrid[ny - 1]);
+    double xe = x0, ye = y0, ze = z0;
+    int icell = locate_grid_cell(xe, ye, ze);
+    int iface = -1, ngrid = 0;
+    double transmit = 1.0, radiance_acc = 0.0;
+    R extinct8[8] = {0, 0, 0, 0, 0, 0, 0, 0}, srcext8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int oldipts[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+    bool validrad = false;
+    double ext1 = 0, srcext1 = 0;
+    const R secmu0 = (R)1 / std::fabs((R)p.solarmu);
+    std::vector<R> lt; R fdum;
+    // DONEFACE(8,7): which corner of the previous cell is reused (1-based, 0 none)
+    static const int doneface[7][8] = {{0, 0, 0, 0, 0, 0, 0, 0}, {0, 1, 0, 3, 0, 5, 0, 7}, {2, 0, 4, 0, 6, 0, 8, 0},
+                                       {0, 0, 1, 2, 0, 0, 5, 6}, {3, 4, 0, 0, 7, 8, 0, 0}, {0, 0, 0, 0, 1, 2, 3, 4},
+                                       {5, 6, 7, 8, 0, 0, 0, 0}};
+    while (!validrad && icell >= 0) {
+      ++ngrid;
+      R oext8[8], osrc8[8];
+      for (int i = 0; i < 8; ++i) { oext8[i] = extinct8[i]; osrc8[i] = srcext8[i]; }
+      for (int n = 0; n < 8; ++n) {
+        int ip = gridptr[8 * icell + n];
+        int I = doneface[iface + 1][n];
+        if (I > 0 && ip == oldipts[n]) { extinct8[n] = oext8[I - 1]; srcext8[n] = osrc8[I - 1]; continue; }
+        R ext = total_ext[ip];
+        oldipts[n] = ip;
+        int is = shptr[ip], ns = shptr[ip + 1] - is;
+        R s = 0;
+        for (int j = 0; j < ns; ++j) s += source[(size_t)is + j] * ylmdir[j];
+        if (tms) {
+          for (int ipa = 0; ipa < npart; ++ipa) {
+            R w = (ext == 0) ? (R)1 : extinct[(size_t)ipa * npts + ip] / ext;
+            if (w == 0) continue;
+            point_legen(ip, ipa, lt, fdum);
+            R f = fdum;
+            R da = albedo[(size_t)ipa * npts + ip] * dirflux[ip] * secmu0 * w;
+            int J = 0;
+            for (int l = 0; l <= ml; ++l) {
+              int me = std::min(l, mm);
+              R a1 = da * lt[l];
+              if (J < ns) {
+                for (int m = -me; m <= me; ++m) { s = s - a1 * ylmdir[J] * ylmsun[J]; ++J; }
+              }
+            }
+            const int *IPH = &iphase[((size_t)ipa * npts + ip) * nq];
+            const R *PW = &phaseinterpwt[((size_t)ipa * npts + ip) * nq];
+            if (PW[0] >= phasemax) s = s + da * singscat[IPH[0] - 1] / ((R)1 - f);
+            else
+              for (int q = 0; q < nq; ++q) {
+                if (PW[q] <= (R)1e-5) continue;
+                s = s + da * singscat[IPH[q] - 1] * PW[q] / ((R)1 - f);
+              }
+          }
+        }
+        srcext8[n] = s * ext;
+        extinct8[n] = ext;
+      }
+      int ipt1 = gridptr[8 * icell], ipt2 = gridptr[8 * icell + 7];
+      double delx = gridpos[3 * ipt2] - gridpos[3 * ipt1], dely = gridpos[3 * ipt2 + 1] - gridpos[3 * ipt1 + 1];
+      double delz = gridpos[3 * ipt2 + 2] - gridpos[3 * ipt1 + 2];
+      double invdelx = delx <= 0 ? 1.0 : 1.0 / delx, invdely = dely <= 0 ? 1.0 : 1.0 / dely, invdelz = 1.0 / delz;
+      auto interp = [&](const R *a, double u, double v, double w) {
+        return (R)((1 - w) * ((1 - v) * ((1 - u) * a[0] + u * a[1]) + v * ((1 - u) * a[2] + u * a[3])) +
+                   w * ((1 - v) * ((1 - u) * a[4] + u * a[5]) + v * ((1 - u) * a[6] + u * a[7])));
+      };
+      double u = (xe - gridpos[3 * ipt1]) * invdelx, v = (ye - gridpos[3 * ipt1 + 1]) * invdely,
+             w = (ze - gridpos[3 * ipt1 + 2]) * invdelz;
+      srcext1 = std::max((R)0, interp(srcext8, u, v, w));
+      ext1 = interp(extinct8, u, v, w);
+      bool ipinx = (cellflags[icell] & 1) && !((bcflag & 1) && ((cx > 0 && xe < xm) || (cx < 0 && xe > xm)));
+      bool ipiny = (cellflags[icell] & 2) && !((bcflag & 2) && ((cy > 0 && ye < ym) || (cy < 0 && ye > ym)));
+      int iopp = gridptr[8 * icell + (8 - ioct)];
+      double sox = ipinx ? 1e20 : (gridpos[3 * iopp] - xe) * cxinv;
+      double soy = ipiny ? 1e20 : (gridpos[3 * iopp + 1] - ye) * cyinv;
+      double soz = (gridpos[3 * iopp + 2] - ze) * czinv;
+      double so = std::min(sox, std::min(soy, soz));
+      if (so < -eps) { err = "INTEGRATE_1RAY: SO<0"; return false; }
+      double xn = xe + so * cx, yn = ye + so * cy, zn = ze + so * cz;
+      u = (xn - gridpos[3 * ipt1]) * invdelx; v = (yn - gridpos[3 * ipt1 + 1]) * invdely; w = (zn - gridpos[3 * ipt1 + 2]) * invdelz;
+      R extn = interp(extinct8, u, v, w);
+      double taugrid = so * 0.5 * (ext1 + extn);
+      int ntau = std::max(1, 1 + (int)(taugrid / p.tautol));
+      double dels = so / ntau;
+      for (int it = 1; it <= ntau; ++it) {
+        double s = it * dels;
+        double xi = xe + s * cx, yi = ye + s * cy, zi = ze + s * cz;
+        u = (xi - gridpos[3 * ipt1]) * invdelx; v = (yi - gridpos[3 * ipt1 + 1]) * invdely; w = (zi - gridpos[3 * ipt1 + 2]) * invdelz;
+        R ext0 = interp(extinct8, u, v, w);
+        R srcext0 = std::max((R)0, interp(srcext8, u, v, w));
+        double ext = 0.5 * (ext0 + ext1), tau, abscell, transcell, src;
+        if (ext != 0.0) {
+          tau = ext * dels;
+          abscell = tau * (1.0 - 0.5 * tau * (1.0 - 0.33333333333 * tau));
+          transcell = 1.0 - abscell;
+          src = (0.5 * (srcext0 + srcext1) + 0.08333333333 * (ext0 * srcext1 - ext1 * srcext0) * dels * (1.0 - 0.05 * (ext1 - ext0) * dels)) / ext;
+        } else { abscell = 0; transcell = 1; src = 0; }
+        radiance_acc += transmit * src * abscell;
+        transmit *= transcell;
+        ext1 = ext0; srcext1 = srcext0;
+      }
+      int jface; bool openbcface;
+      if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; openbcface = (cellflags[icell] & 1) && (bcflag & 1); }
+      else if (soy <= soz) { iface = 3 - bity; jface = 1; openbcface = (cellflags[icell] & 2) && (bcflag & 2); }
+      else { iface = 5 - bitz; jface = 2; openbcface = false; }
+      int inext = neighptr[6 * icell + iface];
+      int kface, ic;
+      if (!openbcface) { kface = iface; ic = icell; }
+      else { kface = kOppFace[iface]; ic = inext; iface = -1; }
+      if (inext >= 0) {
+        if (jface == 0) xn = gridpos[3 * gridptr[8 * inext + ioct - 1]];
+        else if (jface == 1) yn = gridpos[3 * gridptr[8 * inext + ioct - 1] + 1];
+        else zn = gridpos[3 * gridptr[8 * inext + ioct - 1] + 2];
+      }
+      if (transmit < p.transcut || ngrid > maxcellscross) validrad = true;
+      else if (inext < 0 && iface >= 4) {
+        validrad = true;
+        // FIND_BOUNDARY_RADIANCE, Lambertian, zero surface emission source
+        double xs[4], ys[4], rb[4];
+        for (int jj = 0; jj < 4; ++jj) {
+          int ipb = gridptr[8 * ic + kGridFace[kface][jj]];
+          xs[jj] = gridpos[3 * ipb]; ys[jj] = gridpos[3 * ipb + 1];
+          if ((float)mu2 < 0.0f) {
+            rb[jj] = p.skyrad;  // isotropic sky radiance at the top boundary
+            if (std::find(topp.begin(), topp.end(), ipb) == topp.end()) { err = "FIND_BOUNDARY_RADIANCE: Not at boundary"; return false; }
+          } else {
+            auto itb = std::lower_bound(botp.begin(), botp.end(), ipb);
+            if (itb == botp.end() || *itb != ipb) { err = "FIND_BOUNDARY_RADIANCE: Not at boundary"; return false; }
+            rb[jj] = bcrad_bot[itb - botp.begin()];
+          }
+        }
+        float uu = (xs[1] - xs[0] > 0) ? (float)((xn - xs[0]) / (xs[1] - xs[0])) : 0.f;
+        float vv = (ys[2] - ys[0] > 0) ? (float)((yn - ys[0]) / (ys[2] - ys[0])) : 0.f;
+        float radbnd = (1 - uu) * (1 - vv) * (float)rb[0] + uu * (1 - vv) * (float)rb[1] + (1 - uu) * vv * (float)rb[2] + uu * vv * (float)rb[3];
+        radiance_acc += transmit * radbnd;
+      } else {
+        icell = inext;
+      }
+      xe = xn; ye = yn; ze = zn;
+    }
+    radout = radiance_acc;
+    return true;
+  }
+
+  // RENDER (src/polarized/shdomsub4.f:93-286), scalar, solar.
+  bool render(int n, const float *camx, const float *camy, const float *camz, const double *cammu,
+              const double *camphi, float *out, int nthreads) {
+    if (!precompute_phase()) return false;
+    lambertian_boundary();
+    const double pi = std::acos(-1.0);
+    std::vector<int> bad(std::max(1, nthreads), 0);
+    std::vector<std::string> errs(std::max(1, nthreads));
+    auto work = [&](int t, int b, int e) {
+      Solver<R> &S = *this;
+      for (int iv = b; iv < e; ++iv) {
+        double x0 = camx[iv], y0 = camy[iv], z0 = camz[iv], mu2 = cammu[iv], phi2 = camphi[iv];
+        double muray = -mu2, phiray = phi2 - pi;
+        if (z0 > S.zgrid[nz - 1]) {
+          if (muray >= 0.0) { out[iv] = 0.f; continue; }
+          double r = (S.zgrid[nz - 1] - z0) / muray;
+          x0 = x0 + r * std::sqrt(1 - muray * muray) * std::cos(phiray);
+          y0 = y0 + r * std::sqrt(1 - muray * muray) * std::sin(phiray);
+          z0 = S.zgrid[nz - 1];
+        } else if (z0 < S.zgrid[0]) { bad[t] = 1; errs[t] = "RENDER: Level below domain"; return; }
+        double rad;
+        if (!S.integrate_1ray(mu2, phi2, x0, y0, z0, rad, errs[t])) { bad[t] = 1; return; }
+        out[iv] = (float)rad;
+      }
+    };
+    if (nthreads <= 1) work(0, 0, n);
+    else {
+      std::vector<std::thread> th;
+      int chunk = (n + nthreads - 1) / nthreads;
+      for (int t = 0; t < nthreads; ++t) th.emplace_back(work, t, std::min(n, t * chunk), std::min(n, (t + 1) * chunk));
+      for (auto &x : th) x.join();
+    }
+    for (int t = 0; t < (int)bad.size(); ++t) if (bad[t]) { err = errs[t]; return false; }
+    return true;
+  }
+
+};
+
+struct Handle {
+  int fp64 = 0;
+  Solver<float> *s32 = nullptr;
+  Solver<double> *s64 = nullptr;
+  std::string err;
+};
+
+}  // namespace orc
+
+using orc::Handle;
+
+extern "C" {
+
+void *oracle_create(const shdom_problem *p, int fp64) {
+  Handle *h = new Handle();
+  h->fp64 = fp64;
+  bool ok;
+  if (fp64) { h->s64 = new orc::Solver<double>(); ok = h->s64->init(p); if (!ok) h->err = h->s64->err; }
+  else { h->s32 = new orc::Solver<float>(); ok = h->s32->init(p); if (!ok) h->err = h->s32->err; }
+  return h;
+}
+
+const char *oracle_error(void *hv) {
+  Handle *h = (Handle *)hv;
+  if (!h->err.empty()) return h->err.c_str();
+  if (h->fp64) return h->s64->err.c_str();
+  return h->s32->err.c_str();
+}
+
+int oracle_sizes(void *hv, int *out) {
+  Handle *h = (Handle *)hv;
+  auto fill = [&](auto *s) {
+    out[0] = s->npts; out[1] = s->nlm; out[2] = s->nmu; out[3] = s->nang; out[4] = s->ncells;
+    out[5] = s->nx1; out[6] = s->ny1; out[7] = s->nz; out[8] = s->bcflag; out[9] = s->ipflag;
+    out[10] = s->iter; out[11] = s->ml; out[12] = s->mm;
+  };
+  if (h->fp64) fill(h->s64); else fill(h->s32);
+  return 0;
+}
+
+int oracle_solve(void *hv, int maxiter, int verbose, float *solcrit_out) {
+  Handle *h = (Handle *)hv;
+  auto run = [&](auto *s) -> int {
+    if (s->source.empty()) { if (!s->init_solution()) return 1; }
+    if (!s->solution_iterations(maxiter, verbose)) return 1;
+    if (solcrit_out) *solcrit_out = (float)s->solcrit;
+    return 0;
+  };
+  return h->fp64 ? run(h->s64) : run(h->s32);
+}
+
+int oracle_init_solution(void *hv) {
+  Handle *h = (Handle *)hv;
+  return h->fp64 ? !h->s64->init_solution() : !h->s32->init_solution();
+}
+
+// Exports the solution densely: source/radiance [npts][nlm] (zero beyond
+// the per-point truncation), ns/nr per point, fluxes [npts][2], dirflux.
+int oracle_export(void *hv, float *source, int *ns, float *radiance, int *nr, float *fluxes, float *dirflux) {
+  Handle *h = (Handle *)hv;
+  auto ex = [&](auto *s) {
+    int n = s->npts, L = s->nlm;
+    for (int i = 0; i < n; ++i) {
+      int is = s->shptr[i], k = s->shptr[i + 1] - is;
+      if (ns) ns[i] = k;
+      if (source) for (int j = 0; j < L; ++j) source[(size_t)i * L + j] = j < k ? (float)s->source[(size_t)is + j] : 0.f;
+      int ir = s->rshptr[i], kr = s->rshptr[i + 1] - ir;
+      if (nr) nr[i] = kr;
+      if (radiance) for (int j = 0; j < L; ++j) radiance[(size_t)i * L + j] = j < kr ? (float)s->radiance[(size_t)ir + j] : 0.f;
+      if (fluxes) { fluxes[2 * i] = (float)s->fluxes[2 * (size_t)i]; fluxes[2 * i + 1] = (float)s->fluxes[2 * (size_t)i + 1]; }
+      if (dirflux) dirflux[i] = (float)s->dirflux[i];
+    }
+  };
+  if (h->fp64) ex(h->s64); else ex(h->s32);
+  return 0;
+}
+
+int oracle_render(void *hv, int n, const float *camx, const float *camy, const float *camz, const double *cammu,
+                  const double *camphi, float *out, int nthreads) {
+  Handle *h = (Handle *)hv;
+  bool ok = h->fp64 ? h->s64->render(n, camx, camy, camz, cammu, camphi, out, nthreads)
+                    : h->s32->render(n, camx, camy, camz, cammu, camphi, out, nthreads);
+  return ok ? 0 : 1;
+}
+
+int oracle_grid(void *hv, float *gridpos, int *gridptr, int *neighptr, short *cellflags) {
+  Handle *h = (Handle *)hv;
+  auto g = [&](auto *s) {
+    if (gridpos) std::memcpy(gridpos, s->gridpos.data(), s->gridpos.size() * sizeof(float));
+    if (gridptr) std::memcpy(gridptr, s->gridptr.data(), s->gridptr.size() * sizeof(int));
+    if (neighptr) std::memcpy(neighptr, s->neighptr.data(), s->neighptr.size() * sizeof(int));
+    if (cellflags) std::memcpy(cellflags, s->cellflags.data(), s->cellflags.size() * sizeof(short));
+  };
+  if (h->fp64) g(h->s64); else g(h->s32);
+  return 0;
+}
+
+int oracle_angles(void *hv, float *mu, float *phi, float *wtdo, int *nphi0) {
+  Handle *h = (Handle *)hv;
+  auto g = [&](auto *s) {
+    if (mu) std::memcpy(mu, s->mu.data(), s->mu.size() * sizeof(float));
+    if (phi) std::memcpy(phi, s->phi.data(), s->phi.size() * sizeof(float));
+    if (wtdo) std::memcpy(wtdo, s->wtdo.data(), s->wtdo.size() * sizeof(float));
+    if (nphi0) std::memcpy(nphi0, s->nphi0.data(), s->nphi0.size() * sizeof(int));
+  };
+  if (h->fp64) g(h->s64); else g(h->s32);
+  return 0;
+}
+
+void oracle_destroy(void *hv) {
+  Handle *h = (Handle *)hv;
+  delete h->s32; delete h->s64; delete h;
+}
+
+}  // extern "C"

@@ -1,0 +1,35 @@
+"""Generates tests/golden/brdf_L1.npz from the reference's golden files.
+
+Reads the original-SHDOM outputs tests/data/brdf_L1f.out (fluxes) and
+tests/data/brdf_L1r.out (radiances) of the reference repository, parsed the
+way tests/test_shdom.py:17-27 parses them, and stores the numeric columns.
+Run once in a checkout that has the reference mounted:
+
+    python tests/golden/make_brdf_l1_fixture.py /path/to/reference
+"""
+import os
+import sys
+
+import numpy as np
+
+
+def parse(path, comment="!"):
+    rows = []
+    with open(path) as f:
+        for line in f:
+            if comment not in line:
+                rows.append(np.array(line.split(), dtype=np.float64))
+    return np.array(rows)
+
+
+def main(ref):
+    d = os.path.join(ref, "tests", "data")
+    fl = parse(os.path.join(d, "brdf_L1f.out"))
+    ra = parse(os.path.join(d, "brdf_L1r.out"))
+    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "brdf_L1.npz")
+    np.savez(out, fluxes=fl, radiances=ra)
+    print(out, fl.shape, ra.shape)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
