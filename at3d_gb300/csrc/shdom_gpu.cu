@@ -1,0 +1,1213 @@
+// shdom_gpu.cu -- device kernels and the C-ABI (include/shdom_gb300.h) of
+// the GB300 SHDOM solve / render path.
+//
+// One iteration (SOLUTION_ITERATIONS, src/polarized/shdomsub1.f:674-797):
+//   1. SH -> DO   : SRCDO[p][c] = max(0, sum_j SOURCE[p][j] A[j][c])   (k_gemm, mode 0)
+//   2. sweeps     : downward ordinates, Lambertian bottom, upward ordinates;
+//                   every wavefront level is one k_sweep launch over all
+//                   (octant, point, ordinate) tasks of that level
+//   3. DO -> SH   : RADIANCE[p][j] = sum_c RADDO[p][c] B[c][j] (masked to
+//                   the point's radiance truncation) + hemispheric fluxes
+//   4. source     : k_source (COMPUTE_SOURCE fused: dot products in FP64,
+//                   delta-source, new truncation, next radiance truncation)
+//   5. k_accel_param, k_accelerate (CALC_ACCEL_SOLCRIT, ACCELERATE_SOLUTION)
+// Layouts are dense: [point][term] for the spherical-harmonic fields (terms
+// beyond a point's truncation are zero) and [point][column] for the
+// ordinate fields, columns grouped by hemisphere and trace octant.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/shdom_gb300.h"
+#include "shdom_plan.h"
+
+namespace shdom {
+
+#define CK(x)                                                                        \
+  do {                                                                               \
+    cudaError_t e_ = (x);                                                            \
+    if (e_ != cudaSuccess) {                                                         \
+      throw std::runtime_error(std::string("CUDA error: ") + cudaGetErrorString(e_) + \
+                               " at " #x);                                           \
+    }                                                                                \
+  } while (0)
+
+// Device error codes written to Dev::err (first error wins).
+enum { ERR_NONE = 0, ERR_SWEEP_NOFACE = 1, ERR_SWEEP_STEPS = 2, ERR_RAY_STEPS = 3, ERR_RAY_SO = 4, ERR_RAY_BELOW = 5 };
+
+__constant__ int c_face[6][4] = {{0, 2, 4, 6}, {1, 3, 5, 7}, {0, 1, 4, 5}, {2, 3, 6, 7}, {0, 1, 2, 3}, {4, 5, 6, 7}};
+
+// ------------------------------------------------------------------ GEMM
+// C[M x N] = A[M x K] * B[K x N], all row-major FP32, with an epilogue.
+// mode 0: C = max(0, acc) (source to discrete ordinates)
+// mode 1: columns < nlm -> radiance masked by nr[row]; nlm, nlm+1 -> fluxes
+constexpr int GBM = 128, GBN = 64, GBK = 16;
+
+__global__ void __launch_bounds__(256) k_gemm(const float *__restrict__ A, const float *__restrict__ B, int M, int N,
+                                              int K, int lda, int ldb, int mode, float *__restrict__ C, int ldc,
+                                              const int *__restrict__ nr, int nlm, float *__restrict__ fluxes) {
+  __shared__ float As[GBK][GBM + 4];
+  __shared__ float Bs[GBK][GBN];
+  const int tid = threadIdx.x;
+  const int m0 = blockIdx.y * GBM, n0 = blockIdx.x * GBN;
+  const int tr = tid / 16, tc = tid % 16;  // 16 x 16 threads, 8 x 4 outputs each
+  float acc[8][4];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+  for (int k0 = 0; k0 < K; k0 += GBK) {
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {  // A tile 128 x 16
+      int idx = tid + r * 256;
+      int am = idx / GBK, ak = idx % GBK;
+      int gm = m0 + am, gk = k0 + ak;
+      As[ak][am] = (gm < M && gk < K) ? A[(size_t)gm * lda + gk] : 0.f;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {  // B tile 16 x 64
+      int idx = tid + r * 256;
+      int bk = idx / GBN, bn = idx % GBN;
+      int gk = k0 + bk, gn = n0 + bn;
+      Bs[bk][bn] = (gk < K && gn < N) ? B[(size_t)gk * ldb + gn] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < GBK; ++kk) {
+      float a[8], b[4];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) a[i] = As[kk][tr * 8 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tc + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    int gm = m0 + tr * 8 + i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int gn = n0 + tc + 16 * j;
+      if (gn >= N) continue;
+      float v = acc[i][j];
+      if (mode == 0) {
+        C[(size_t)gm * ldc + gn] = fmaxf(v, 0.f);
+      } else {
+        if (gn < nlm) C[(size_t)gm * ldc + gn] = (gn < nr[gm]) ? v : 0.f;
+        else fluxes[(size_t)gm * 2 + (gn - nlm)] = v;
+      }
+    }
+  }
+}
+
+// ----------------------------------------------------------------- sweep
+struct SweepArgs {
+  const float *gridpos;
+  const int *gridptr, *neighptr, *cellflags;
+  const uint8_t *bnd;
+  const int *rank, *start, *level;
+  const float *text, *srcdo;
+  float *raddo;
+  const float *col_cx, *col_cy, *col_cz;
+  const uint32_t *tasks;
+  int *err;
+  int npts, nang, is1d;
+  float transmin;
+  int oct_col0[8], oct_ncol[8];
+};
+
+// One backward short-characteristic trace (BACK_INT_GRID3D_UNPOL,
+// src/polarized/shdomsub1.f:3695-4038, and BACK_INT_GRID1D :4295-4465 for the
+// 1D independent-pixel case) up to the face it stops at.  The result does
+// not depend on radiance values: rad(P) = radsrc + tr * sum_k f[k] rad(q[k]).
+// A face is usable when each corner is a preset boundary point or precedes P
+// in the reference sweep order (and, with use_level, sits at a lower
+// wavefront level, so level-synchronous execution never reads a value that
+// is not yet computed).
+struct Trace {
+  float radsrc, tr, f[4];
+  int q[4];
+  int status;  // 0 ok, ERR_* otherwise
+};
+
+__device__ __forceinline__ Trace trace_point(const SweepArgs &a, int b, int pt, int col, bool use_level) {
+  Trace t;
+  t.radsrc = 0.f; t.tr = 1.f; t.status = ERR_SWEEP_STEPS;
+  t.q[0] = t.q[1] = t.q[2] = t.q[3] = pt; t.f[0] = t.f[1] = t.f[2] = t.f[3] = 0.f;
+  const int nang = a.nang, n = a.npts;
+  const float cx = a.col_cx[col], cy = a.col_cy[col], cz = a.col_cz[col];
+  const float cxinv = cx != 0.f ? 1.f / cx : 1.0e6f, cyinv = cy != 0.f ? 1.f / cy : 1.0e6f, czinv = 1.f / cz;
+  const int bitx = cx < 0.f, bity = cy < 0.f, bitz = cz < 0.f;
+  const int hb = bitz ? 2 : 1;
+  const int *rk = a.rank + (size_t)b * n, *lv = a.level + (size_t)b * n;
+  const int rP = rk[pt], lP = use_level ? lv[pt] : 0;
+  int cell = a.start[(size_t)b * n + pt];
+  float xe = a.gridpos[3 * pt], ye = a.gridpos[3 * pt + 1], ze = a.gridpos[3 * pt + 2];
+  float ext1 = a.text[pt];
+  float srcext1 = ext1 * a.srcdo[(size_t)pt * nang + col];
+  float rad = 0.f, tr = 1.f;
+  for (int guard = 0; guard < 65536; ++guard) {
+    if (cell < 0) break;
+    const int *g = a.gridptr + 8 * (size_t)cell;
+    int i1, i2, i3, i4, nxt;
+    float so, f1, f2, f3, f4;
+    if (a.is1d) {
+      int iopp = g[7 - b];
+      so = (a.gridpos[3 * iopp + 2] - ze) * czinv;
+      ze += so * cz;
+      int iface = 5 - bitz;
+      nxt = a.neighptr[6 * (size_t)cell + iface];
+      i1 = i2 = i3 = i4 = g[iface == 4 ? 0 : 4];
+      if (nxt >= 0) ze = a.gridpos[3 * a.gridptr[8 * (size_t)nxt + b] + 2];
+      f1 = 1.f; f2 = f3 = f4 = 0.f;
+    } else {
+      const int cf = a.cellflags[cell];
+      const bool ipx = cf & 1, ipy = cf & 2;
+      const int iopp = g[7 - b];
+      float sox = ipx ? 1.0e20f : (a.gridpos[3 * iopp] - xe) * cxinv;
+      float soy = ipy ? 1.0e20f : (a.gridpos[3 * iopp + 1] - ye) * cyinv;
+      float soz = (a.gridpos[3 * iopp + 2] - ze) * czinv;
+      so = fminf(sox, fminf(soy, soz));
+      xe += so * cx; ye += so * cy; ze += so * cz;
+      int iface, jface;
+      if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; }
+      else if (soy <= soz) { iface = 3 - bity; jface = 1; }
+      else { iface = 5 - bitz; jface = 2; }
+      nxt = a.neighptr[6 * (size_t)cell + iface];
+      i1 = g[c_face[iface][0]]; i2 = g[c_face[iface][1]]; i3 = g[c_face[iface][2]]; i4 = g[c_face[iface][3]];
+      const float *p1 = a.gridpos + 3 * i1, *p2 = a.gridpos + 3 * i2, *p3 = a.gridpos + 3 * i3;
+      float u, v;
+      if (jface == 0) {
+        u = (ze - p1[2]) / (p3[2] - p1[2]);
+        v = ipy ? 0.5f : (ye - p1[1]) / (p2[1] - p1[1]);
+      } else if (jface == 1) {
+        u = (ze - p1[2]) / (p3[2] - p1[2]);
+        v = ipx ? 0.5f : (xe - p1[0]) / (p2[0] - p1[0]);
+      } else {
+        u = ipy ? 0.5f : (ye - p1[1]) / (p3[1] - p1[1]);
+        v = ipx ? 0.5f : (xe - p1[0]) / (p2[0] - p1[0]);
+      }
+      if (nxt >= 0) {
+        const float *q = a.gridpos + 3 * a.gridptr[8 * (size_t)nxt + b];
+        if (jface == 0) xe = q[0]; else if (jface == 1) ye = q[1]; else ze = q[2];
+      }
+      f1 = (1.f - u) * (1.f - v); f2 = (1.f - u) * v; f3 = u * (1.f - v); f4 = u * v;
+    }
+    const float e1 = a.text[i1], e2 = a.text[i2], e3 = a.text[i3], e4 = a.text[i4];
+    const float ext0 = f1 * e1 + f2 * e2 + f3 * e3 + f4 * e4;
+    const float srcext0 = f1 * a.srcdo[(size_t)i1 * nang + col] * e1 + f2 * a.srcdo[(size_t)i2 * nang + col] * e2 +
+                          f3 * a.srcdo[(size_t)i3 * nang + col] * e3 + f4 * a.srcdo[(size_t)i4 * nang + col] * e4;
+    const float ext = 0.5f * (ext0 + ext1), tau = ext * so;
+    float transcell, abscell, src;
+    if (tau >= 0.5f) { transcell = __expf(-tau); abscell = 1.f - transcell; }
+    else {
+      abscell = tau * (1.f - 0.5f * tau * (1.f - 0.33333333333f * tau * (1.f - 0.25f * tau)));
+      transcell = 1.f - abscell;
+    }
+    if (tau <= 2.f) {
+      src = (ext == 0.f) ? 0.f : (0.5f * (srcext0 + srcext1) + 0.08333333333f * (ext0 * srcext1 - ext1 * srcext0) * so) / ext;
+    } else {
+      float ext0p = ext0, srcext0p = srcext0;
+      if (tau > 4.f) { ext0p = ext1 + (ext0 - ext1) * 4.f / tau; if (ext0 > 0.f) srcext0p = srcext0 * ext0p / ext0; }
+      src = 1.f / (ext0p + ext1) *
+            (srcext0p + srcext1 + (ext0p * srcext1 - ext1 * srcext0p) * 2.f / (ext0p + ext1) * (1.f - 2.f / tau + 2.f * transcell / abscell));
+    }
+    src = fmaxf(src, 0.f);
+    rad += tr * src * abscell;
+    tr *= transcell;
+    auto ok = [&](int q) { return (a.bnd[q] & hb) || (rk[q] < rP && (!use_level || lv[q] < lP)); };
+    const bool valid = ok(i1) && ok(i2) && ok(i3) && ok(i4);
+    if (nxt < 0 || (tr <= a.transmin && valid)) {
+      t.radsrc = rad; t.tr = tr;
+      t.q[0] = i1; t.q[1] = i2; t.q[2] = i3; t.q[3] = i4;
+      t.f[0] = f1; t.f[1] = f2; t.f[2] = f3; t.f[3] = f4;
+      t.status = valid ? ERR_NONE : ERR_SWEEP_NOFACE;
+      if (!valid) t.tr = 0.f;
+      return t;
+    }
+    ext1 = ext0; srcext1 = srcext0; cell = nxt;
+  }
+  t.radsrc = 0.f; t.tr = 0.f;
+  return t;
+}
+
+// Level-synchronous sweep: one launch per wavefront level, one thread per
+// (octant, point, ordinate-of-the-octant) task of that level.
+__global__ void __launch_bounds__(256) k_sweep(SweepArgs a, int t0, int ntask, int omax) {
+  int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  int task = tid / omax, slot = tid - task * omax;
+  if (task >= ntask) return;
+  uint32_t tk = a.tasks[t0 + task];
+  int b = (int)(tk >> 28), pt = (int)(tk & 0x0FFFFFFFu);
+  if (slot >= a.oct_ncol[b]) return;
+  const int col = a.oct_col0[b] + slot, nang = a.nang;
+  Trace t = trace_point(a, b, pt, col, true);
+  if (t.status != ERR_NONE) atomicCAS(a.err, ERR_NONE, t.status);
+  float rad = t.radsrc;
+  if (t.tr != 0.f)
+    rad += t.tr * (t.f[0] * a.raddo[(size_t)t.q[0] * nang + col] + t.f[1] * a.raddo[(size_t)t.q[1] * nang + col] +
+                   t.f[2] * a.raddo[(size_t)t.q[2] * nang + col] + t.f[3] * a.raddo[(size_t)t.q[3] * nang + col]);
+  a.raddo[(size_t)pt * nang + col] = rad;
+}
+
+// Sequential-order sweep for grids whose wavefront is too deep (periodic
+// wrap-around long characteristics chain points of one ordinate through the
+// whole grid): one block per ordinate walks the reference sweep order in
+// windows of SEQW points.  The traces of a window run in parallel; the
+// final combination is resolved warp by warp in rank order, in-window
+// dependencies through shared memory.
+constexpr int SEQW = 256;
+
+__global__ void __launch_bounds__(SEQW) k_sweep_seq(SweepArgs a, const int *order, int col_begin) {
+  __shared__ float sval[SEQW];
+  __shared__ int sdone[SEQW];
+  const int col = col_begin + blockIdx.x, nang = a.nang, n = a.npts;
+  int b = 0;
+  for (int k = 0; k < 8; ++k)
+    if (a.oct_ncol[k] > 0 && col >= a.oct_col0[k] && col < a.oct_col0[k] + a.oct_ncol[k]) b = k;
+  const int hb = (b & 4) ? 2 : 1;
+  const int *ord = order + (size_t)b * n, *rk = a.rank + (size_t)b * n;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int r0 = 0; r0 < n; r0 += SEQW) {
+    const int r = r0 + tid;
+    const int pt = r < n ? ord[r] : 0;
+    bool pending = r < n && !(a.bnd[pt] & hb);
+    Trace t;
+    if (pending) {
+      t = trace_point(a, b, pt, col, false);
+      if (t.status != ERR_NONE) atomicCAS(a.err, ERR_NONE, t.status);
+    }
+    int wl[4];
+    float wv = 0.f;  // contribution of the dependencies already final
+    if (pending) {
+      wv = t.radsrc;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        int q = t.q[k];
+        if (t.f[k] == 0.f || t.tr == 0.f) { wl[k] = -1; continue; }
+        int rq = (a.bnd[q] & hb) ? -1 : rk[q];
+        if (rq >= r0 && t.f[k] != 0.f) wl[k] = rq - r0;
+        else { wl[k] = -1; wv += t.tr * t.f[k] * a.raddo[(size_t)q * nang + col]; }
+      }
+    }
+    sdone[tid] = pending ? 0 : 1;
+    __syncthreads();
+    for (int w = 0; w < SEQW / 32; ++w) {
+      if (warp == w) {
+        bool todo = pending;
+        for (int round = 0; round < 33 && __any_sync(0xffffffffu, todo); ++round) {
+          if (todo) {
+            bool ready = true;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) if (wl[k] >= 0 && !sdone[wl[k]]) ready = false;
+            if (ready) {
+              float v = wv;
+#pragma unroll
+              for (int k = 0; k < 4; ++k) if (wl[k] >= 0) v += t.tr * t.f[k] * sval[wl[k]];
+              sval[tid] = v;
+              a.raddo[(size_t)pt * nang + col] = v;
+              todo = false;
+            }
+          }
+          __syncwarp();
+          if (!todo && pending) sdone[tid] = 1;
+          __syncwarp();
+        }
+        if (todo) atomicCAS(a.err, ERR_NONE, ERR_SWEEP_STEPS);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// Preset boundary radiances for one hemisphere: top points get the sky
+// radiance for downward columns; bottom points get the Lambertian surface
+// radiance computed from the downwelling flux (FIXED/VARIABLE_LAMBERTIAN_
+// BOUNDARY, src/polarized/shdomsub1.f:2438-2529).
+__global__ void k_preset_top(const int *topp, int ntop, float *raddo, int nang, int ncol_down, float skyrad) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntop * ncol_down) return;
+  int k = t / ncol_down, c = t - k * ncol_down;
+  raddo[(size_t)topp[k] * nang + c] = skyrad;
+}
+
+__global__ void k_lambertian(const int *botp, int nbot, const float *botalb, const float *dirflux, const float *fluxw,
+                             float *raddo, int nang, int ncol_down, float *bcrad) {
+  int k = blockIdx.x;
+  if (k >= nbot) return;
+  int p = botp[k];
+  __shared__ float red[256];
+  float s = 0.f;
+  for (int c = threadIdx.x; c < ncol_down; c += blockDim.x) s += fluxw[c] * raddo[(size_t)p * nang + c];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  const float opi = 0.318309886f;
+  float b = opi * botalb[k] * (dirflux[p] + red[0]);
+  if (threadIdx.x == 0) bcrad[k] = b;
+  for (int c = ncol_down + threadIdx.x; c < nang; c += blockDim.x) raddo[(size_t)p * nang + c] = b;
+}
+
+// ---------------------------------------------------------------- source
+struct SourceArgs {
+  const float *coef;      // [npts][nl]
+  const float *dirflux, *radiance, *ylmsun;
+  const int *lofj;
+  float *source, *delsource;
+  int *ns, *nso, *nr;     // nr is read (current) and rewritten (next)
+  double *red;            // [4] deljdot, deljold, deljnew, jnorm
+  int npts, nlm, nl, ml, mm;
+  float secmu0, shacc;
+  int first, fixsh, accel, highorder;
+};
+
+// COMPUTE_SOURCE (src/polarized/shdomsub1.f:967-1611) for all three passes
+// at once, one warp per point, plus the next RADIANCE_TRUNCATION
+// (src/polarized/shdomsub1.f:1615-1803) for the same point.
+__global__ void __launch_bounds__(256) k_source(SourceArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  double djdot = 0, djold = 0, djnew = 0, jn = 0;
+  for (int p = warp; p < a.npts; p += nwarps) {
+    const float *cf = a.coef + (size_t)p * a.nl;
+    const float f0 = a.dirflux[p] * a.secmu0;
+    const int nrp = a.nr[p];
+    const int nsold = a.ns[p], nsoold = a.nso[p];
+    const int nsmin = min(nsold, nsoold);
+    float *S = a.source + (size_t)p * a.nlm;
+    float *D = a.delsource + (size_t)p * a.nlm;
+    const float *R = a.radiance + (size_t)p * a.nlm;
+    int jlast = 0;  // 1-based index of the last term above shacc
+    for (int j0 = 0; j0 < a.nlm; j0 += 32) {
+      int j = j0 + lane;
+      float jt = 0.f;
+      if (j < a.nlm) {
+        float c = cf[a.lofj[j]];
+        jt = f0 * c * a.ylmsun[j];
+        if (j < nrp) jt += c * R[j];
+        if (!a.first) {
+          float sold = S[j];
+          if (a.accel) {
+            if (j < nsmin) {
+              float dn = jt - sold, dd = D[j];
+              djdot += (double)dn * dd; djold += (double)dd * dd; djnew += (double)dn * dn; jn += (double)sold * sold;
+            }
+            if (j < nsold) D[j] = jt - sold; else D[j] = 0.f;
+          } else if (j < nsold) {
+            float dn = jt - sold;
+            djnew += (double)dn * dn; jn += (double)sold * sold;
+          }
+        }
+      }
+      unsigned m = __ballot_sync(0xffffffffu, j < a.nlm && fabsf(jt) > a.shacc);
+      if (m) jlast = j0 + 32 - __clz(m);
+      // stash the new term in the output row; truncated below once jlast is known
+      if (j < a.nlm) S[j] = jt;
+    }
+    int nsnew;
+    if (a.fixsh && !a.first) nsnew = nsold;
+    else if (jlast == 0) nsnew = 0;
+    else {
+      int ls = a.lofj[jlast - 1];
+      nsnew = (ls <= a.mm) ? ls * (ls + 1) + ls + 1 : (2 * a.mm + 1) * ls - a.mm * a.mm + a.mm + 1;
+    }
+    for (int j = nsnew + lane; j < a.nlm; j += 32) S[j] = 0.f;
+    // next radiance truncation
+    int nrnext;
+    if (a.fixsh && !a.first) nrnext = max(4, nsnew);
+    else {
+      float r0 = a.radiance[(size_t)p * a.nlm];
+      int lr = 1;
+      for (int l = 1; l <= a.ml; ++l)
+        if (cf[l] * r0 > a.shacc) lr = l;
+      int ls = a.lofj[max(1, nsnew) - 1];
+      lr = min(lr, ls + a.ml / 8 + 2);
+      if (a.highorder) lr = a.ml;
+      nrnext = (lr <= a.mm) ? lr * (lr + 1) + lr + 1 : (2 * a.mm + 1) * lr - a.mm * a.mm + a.mm + 1;
+    }
+    if (a.highorder && a.fixsh && !a.first) nrnext = a.nlm;
+    __syncwarp();
+    if (lane == 0) {
+      a.ns[p] = nsnew;
+      if (!a.first && a.accel) a.nso[p] = nsold;
+      if (a.first) a.nso[p] = nsnew;
+      a.nr[p] = nrnext;
+    }
+  }
+  if (!a.first) {
+    for (int o = 16; o > 0; o >>= 1) {
+      djdot += __shfl_xor_sync(0xffffffffu, djdot, o);
+      djold += __shfl_xor_sync(0xffffffffu, djold, o);
+      djnew += __shfl_xor_sync(0xffffffffu, djnew, o);
+      jn += __shfl_xor_sync(0xffffffffu, jn, o);
+    }
+    __shared__ double sred[4][8];
+    int w = threadIdx.x >> 5;
+    if (lane == 0) { sred[0][w] = djdot; sred[1][w] = djold; sred[2][w] = djnew; sred[3][w] = jn; }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+      double s = 0;
+      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sred[threadIdx.x][k];
+      atomicAdd(&a.red[threadIdx.x], s);
+    }
+  }
+}
+
+struct AccelState {
+  double a;        // acceleration parameter of the last iteration
+  float solcrit;
+  float accelpar;
+};
+
+// CALC_ACCEL_SOLCRIT (src/shdom_nompi.f:317-348).
+__global__ void k_accel_param(const double *red, AccelState *st, int doaccel) {
+  double djdot = red[0], djold = red[1], djnew = red[2], jn = red[3];
+  double a;
+  if (doaccel && st->a == 0.0 && djnew < djold) {
+    double r = sqrt(djnew / djold);
+    double theta = acos(djdot / sqrt(djold * djnew));
+    a = (1 - r * cos(theta) + pow(r, 1 + 0.5 * 3.14159 / theta)) / (1 + r * r - 2 * r * cos(theta)) - 1.0;
+    a = fmin(10.0, fmax(0.0, a));
+    if (!(a == a)) a = 0.0;
+  } else {
+    a = 0.0;
+  }
+  st->a = a;
+  st->accelpar = (float)a;
+  if (jn > 0) st->solcrit = (float)sqrt(djnew / jn);
+  else if (djnew == 0) st->solcrit = 0.f;
+}
+
+// ACCELERATE_SOLUTION (src/polarized/shdomsub1.f:1807-1831).
+__global__ void k_accelerate(float *source, const float *delsource, const int *ns, const int *nso, int npts, int nlm,
+                             const AccelState *st) {
+  float a = st->accelpar;
+  if (!(a > 0.f)) return;
+  size_t total = (size_t)npts * nlm;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+    int p = (int)(t / nlm), j = (int)(t - (size_t)p * nlm);
+    if (j < min(ns[p], nso[p])) source[t] += a * delsource[t];
+  }
+}
+
+__global__ void k_init_radiance(const float *rad0, float *radiance, int *nr, int npts, int nlm) {
+  size_t total = (size_t)npts * nlm;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+    int p = (int)(t / nlm), j = (int)(t - (size_t)p * nlm);
+    radiance[t] = j < 4 ? rad0[(size_t)p * 4 + j] : 0.f;
+    if (j == 0) nr[p] = 4;
+  }
+}
+
+// ---------------------------------------------------------------- render
+struct RenderArgs {
+  const float *gridpos, *xgrid, *ygrid, *zgrid;
+  const int *gridptr, *neighptr, *cellflags;
+  const float *text, *source, *coef, *dirflux;
+  const int *ns, *lofj;
+  const int *tms_ptr, *tms_iph;
+  const float *tms_w, *phasetab, *ylmsun;
+  const int *botp;
+  const float *bcrad_bot;
+  const int *bot_index;  // point -> bottom list index or -1
+  const float *camx, *camy, *camz;
+  const double *cammu, *camphi;
+  float *out;
+  int *err;
+  int nrays, nx, ny, nz, nlm, nl, ml, mm, bcflag, ipflag, numphase, nscatangle, deltam;
+  float solarmu, solaraz, secmu0, skyrad;
+  double tautol, transcut;
+};
+
+__device__ int locate_cell(const RenderArgs &a, double &x0, double &y0, double z0) {
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  if (!(a.bcflag & 1)) {
+    double xd = a.xgrid[nx] - a.xgrid[0];
+    if (x0 < a.xgrid[0]) x0 = x0 - xd * ((int)((x0 - a.xgrid[0]) / xd) - 1);
+    else if (x0 > a.xgrid[nx]) x0 = x0 - xd * (int)((x0 - a.xgrid[0]) / xd);
+  }
+  if (!(a.bcflag & 2)) {
+    double yd = a.ygrid[ny] - a.ygrid[0];
+    if (y0 < a.ygrid[0]) y0 = y0 - yd * ((int)((y0 - a.ygrid[0]) / yd) - 1);
+    else if (y0 > a.ygrid[ny]) y0 = y0 - yd * (int)((y0 - a.ygrid[0]) / yd);
+  }
+  int il = 0, iu, ix, iy, iz;
+  if (a.ipflag & 1) {
+    iu = nx;
+    while (iu - il > 1) { int im = (iu + il) / 2; if (x0 >= 0.5 * (a.xgrid[im - 1] + a.xgrid[im])) il = im; else iu = im; }
+    il += 1;
+  } else {
+    iu = nx + 1;
+    while (iu - il > 1) { int im = (iu + il) / 2; if (x0 >= a.xgrid[im - 1]) il = im; else iu = im; }
+  }
+  ix = max(il, 1);
+  il = 0;
+  if (a.ipflag & 2) {
+    iu = ny;
+    while (iu - il > 1) { int im = (iu + il) / 2; if (y0 >= 0.5 * (a.ygrid[im - 1] + a.ygrid[im])) il = im; else iu = im; }
+    il += 1;
+  } else {
+    iu = ny + 1;
+    while (iu - il > 1) { int im = (iu + il) / 2; if (y0 >= a.ygrid[im - 1]) il = im; else iu = im; }
+  }
+  iy = max(il, 1);
+  il = 0; iu = nz;
+  while (iu - il > 1) { int im = (iu + il) / 2; if (z0 >= a.zgrid[im - 1]) il = im; else iu = im; }
+  iz = max(il, 1);
+  int nyc = ny;
+  if (a.bcflag & 1) { if (x0 < a.xgrid[0]) ix = 1; else if (x0 > a.xgrid[nx - 1]) ix = nx + 1; else ix = ix + 1; }
+  if (a.bcflag & 2) { nyc = ny + 1; if (y0 < a.ygrid[0]) iy = 1; else if (y0 > a.ygrid[ny - 1]) iy = ny + 1; else iy = iy + 1; }
+  return (iz - 1) + (nz - 1) * (iy - 1) + (nz - 1) * nyc * (ix - 1);
+}
+
+constexpr int RWARPS = 4;     // rays (warps) per block
+constexpr int RNLM = 1024;    // max spherical-harmonic terms for the per-ray tables
+
+// One warp per ray (RENDER / INTEGRATE_1RAY / COMPUTE_SOURCE_1CELL_UNPOL /
+// FIND_BOUNDARY_RADIANCE, src/polarized/shdomsub4.f:93-286,
+// src/polarized/shdomsub2.f:2311-2863, :3046-3192).  The spherical-harmonic
+// dot products of the new cell corners are split over groups of four lanes;
+// the path integration is evaluated uniformly by all lanes.
+__global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
+  __shared__ float ydir[RWARPS][RNLM];
+  __shared__ float tl[RWARPS][64];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int ray = blockIdx.x * RWARPS + w;
+  if (ray >= a.nrays) return;
+  const double pi = 3.141592653589793;
+  double x0 = a.camx[ray], y0 = a.camy[ray], z0 = a.camz[ray], mu2 = a.cammu[ray], phi2 = a.camphi[ray];
+  const double muray = -mu2, phiray = phi2 - pi;
+  const float ztop = a.zgrid[a.nz - 1];
+  if (z0 > ztop) {
+    if (muray >= 0.0) { if (lane == 0) a.out[ray] = 0.f; return; }
+    double r = (ztop - z0) / muray;
+    x0 += r * sqrt(1 - muray * muray) * cos(phiray);
+    y0 += r * sqrt(1 - muray * muray) * sin(phiray);
+    z0 = ztop;
+  } else if (z0 < a.zgrid[0]) {
+    if (lane == 0) { atomicCAS(a.err, ERR_NONE, ERR_RAY_BELOW); a.out[ray] = 0.f; }
+    return;
+  }
+  // Y_lm in the ray direction: lane m runs the l recurrence of its m
+  {
+    const double x = (double)(float)mu2;
+    const float phf = (float)phi2;
+    const double fct = 0.3989422804014327;  // 1/sqrt(2 pi)
+    for (int m = lane; m <= a.mm; m += 32) {
+      double c = 1.0, s = 0.0;
+      if (m > 0) { c = cos(m * (double)phf); s = sin(m * (double)phf); }
+      double dprev = 0.0, dcur;
+      if (m == 0) dcur = 1.0;
+      else {
+        double cc = 1.0;
+        for (int k = 1; k <= m; ++k) cc *= sqrt((double)(m + k) / (double)k);
+        dcur = ((m & 1) ? -cc : cc) * pow(0.5 * sqrt((1.0 - x) * (1.0 + x)), m);
+      }
+      for (int l = m; l <= a.ml; ++l) {
+        double v = fct * dcur * sqrt(l + 0.5);
+        int j = (l <= a.mm) ? l * (l + 1) + m : (2 * a.mm + 1) * l - a.mm * a.mm + m;
+        ydir[w][j] = (float)((c - s) * v);
+        ydir[w][j - 2 * m] = (float)((c + s) * v);
+        double dn;
+        if (m == 0) dn = ((2 * l + 1) * x * dcur - l * dprev) / (l + 1);
+        else dn = ((2 * l + 1) * x * dcur - (l > m ? sqrt((double)(l * l - m * m)) * dprev : 0.0)) / sqrt((double)((l + 1) * (l + 1) - m * m));
+        dprev = dcur; dcur = dn;
+      }
+    }
+  }
+  __syncwarp();
+  // t_l = sum_m Ydir(l,m) Ysun(l,m)
+  for (int l = lane; l <= a.ml; l += 32) {
+    int me = min(l, a.mm), j0 = (l <= a.mm) ? l * l : (2 * a.mm + 1) * l - a.mm * a.mm - a.mm;
+    float s = 0.f;
+    for (int k = 0; k < 2 * me + 1; ++k) s += ydir[w][j0 + k] * a.ylmsun[j0 + k];
+    tl[w][l] = s;
+  }
+  __syncwarp();
+  // single-scatter phase table interpolation parameters
+  int sj = 0;
+  float sf = 0.f;
+  if (a.deltam) {
+    double cosscat = (double)a.solarmu * mu2 + sqrt((1.0 - (double)a.solarmu * a.solarmu) * (1.0 - mu2 * mu2)) * cos((double)a.solaraz - phi2);
+    cosscat = fmax(fmin(1.0, cosscat), -1.0);
+    float F = (float)((a.nscatangle - 1) * (acos(cosscat) / pi) + 1);
+    int J = min(a.nscatangle - 1, (int)F);
+    sf = F - J; sj = J - 1;
+  }
+  double cx = sqrt(1.0 - mu2 * mu2) * cos(phi2 - pi), cy = sqrt(1.0 - mu2 * mu2) * sin(phi2 - pi), cz = -mu2;
+  double cxinv, cyinv, czinv;
+  if (fabs(cx) > 1e-6) cxinv = 1.0 / cx; else { cx = 0; cxinv = 1e6; }
+  if (fabs(cy) > 1e-6) cyinv = 1.0 / cy; else { cy = 0; cyinv = 1e6; }
+  if (fabs(cz) > 1e-6) czinv = 1.0 / cz; else { cz = 0; czinv = 1e6; }
+  const int bitx = cx < 0, bity = cy < 0, bitz = cz < 0, ioct0 = bitx + 2 * bity + 4 * bitz;
+  const float xm = 0.5f * (a.xgrid[0] + a.xgrid[a.nx - 1]), ym = 0.5f * (a.ygrid[0] + a.ygrid[a.ny - 1]);
+  double xe = x0, ye = y0, ze = z0;
+  int cell = locate_cell(a, xe, ye, ze);
+  const double eps = 1.0e-5 * (a.gridpos[3 * a.gridptr[7] + 2] - a.gridpos[3 * a.gridptr[0] + 2]);
+  const int maxcross = 500 * max(a.nx, max(a.ny, a.nz));
+  int oldp[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+  float osrc[8] = {0};
+  float ext8[8], src8[8];
+  double radacc = 0.0, transmit = 1.0;
+  int ngrid = 0;
+  bool validrad = false;
+  const int grp = lane >> 2, gl = lane & 3;  // 8 groups of 4 lanes, one corner per group
+  while (!validrad && cell >= 0) {
+    ++ngrid;
+    const int *g = a.gridptr + 8 * (size_t)cell;
+    int mypt = g[grp];
+    // reuse corners already evaluated for the previous cell
+    int reuse = -1;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) if (oldp[k] == mypt) reuse = k;
+    float cval = 0.f, cext = a.text[mypt];
+    const bool need = reuse < 0;
+    const int ns = need ? a.ns[mypt] : 0;
+    float s = 0.f;
+    {
+      const float *S = a.source + (size_t)mypt * a.nlm;
+      for (int j = gl; j < ns; j += 4) s += S[j] * ydir[w][j];
+    }
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    if (!need) {
+      cval = osrc[reuse];
+    } else {
+      if (a.deltam) {
+        const float da = a.dirflux[mypt] * a.secmu0;
+        const float *cf = a.coef + (size_t)mypt * a.nl;
+        if (ns > 0) {
+          int ls = a.lofj[ns - 1];
+          float sub = 0.f;
+          for (int l = 0; l <= ls; ++l) sub += cf[l] * tl[w][l];
+          s -= da * sub;
+        }
+        float add = 0.f;
+        for (int q = a.tms_ptr[mypt]; q < a.tms_ptr[mypt + 1]; ++q) {
+          int iph = a.tms_iph[q];
+          float ss = (1.f - sf) * a.phasetab[(size_t)sj * a.numphase + iph] + sf * a.phasetab[(size_t)(sj + 1) * a.numphase + iph];
+          add += a.tms_w[q] * ss;
+        }
+        s += da * add;
+      }
+      cval = s * cext;
+    }
+    // gather the 8 corners from the groups
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      src8[k] = __shfl_sync(0xffffffffu, cval, 4 * k);
+      ext8[k] = __shfl_sync(0xffffffffu, cext, 4 * k);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) { oldp[k] = g[k]; osrc[k] = src8[k]; }
+    const int ip1 = g[0], ip2 = g[7];
+    const float *P1 = a.gridpos + 3 * ip1, *P2 = a.gridpos + 3 * ip2;
+    double delx = P2[0] - P1[0], dely = P2[1] - P1[1], delz = P2[2] - P1[2];
+    double idx = delx <= 0 ? 1.0 : 1.0 / delx, idy = dely <= 0 ? 1.0 : 1.0 / dely, idz = 1.0 / delz;
+    auto tri = [&](const float *v, double u, double vv, double ww) {
+      return (float)((1 - ww) * ((1 - vv) * ((1 - u) * v[0] + u * v[1]) + vv * ((1 - u) * v[2] + u * v[3])) +
+                     ww * ((1 - vv) * ((1 - u) * v[4] + u * v[5]) + vv * ((1 - u) * v[6] + u * v[7])));
+    };
+    double u = (xe - P1[0]) * idx, v = (ye - P1[1]) * idy, ww = (ze - P1[2]) * idz;
+    float srcext1 = fmaxf(0.f, tri(src8, u, v, ww));
+    float ext1 = tri(ext8, u, v, ww);
+    const int cf = a.cellflags[cell];
+    bool ipinx = (cf & 1) && !((a.bcflag & 1) && ((cx > 0 && xe < xm) || (cx < 0 && xe > xm)));
+    bool ipiny = (cf & 2) && !((a.bcflag & 2) && ((cy > 0 && ye < ym) || (cy < 0 && ye > ym)));
+    const int iopp = g[7 - ioct0];
+    double sox = ipinx ? 1e20 : (a.gridpos[3 * iopp] - xe) * cxinv;
+    double soy = ipiny ? 1e20 : (a.gridpos[3 * iopp + 1] - ye) * cyinv;
+    double soz = (a.gridpos[3 * iopp + 2] - ze) * czinv;
+    double so = fmin(sox, fmin(soy, soz));
+    if (so < -eps) { if (lane == 0) atomicCAS(a.err, ERR_NONE, ERR_RAY_SO); break; }
+    double xn = xe + so * cx, yn = ye + so * cy, zn = ze + so * cz;
+    u = (xn - P1[0]) * idx; v = (yn - P1[1]) * idy; ww = (zn - P1[2]) * idz;
+    float extn = tri(ext8, u, v, ww);
+    double taugrid = so * 0.5 * (ext1 + extn);
+    int ntau = max(1, 1 + (int)(taugrid / a.tautol));
+    double dels = so / ntau;
+    for (int it = 1; it <= ntau; ++it) {
+      double s = it * dels;
+      u = (xe + s * cx - P1[0]) * idx; v = (ye + s * cy - P1[1]) * idy; ww = (ze + s * cz - P1[2]) * idz;
+      float ext0 = tri(ext8, u, v, ww);
+      float srcext0 = fmaxf(0.f, tri(src8, u, v, ww));
+      float ext = 0.5f * (ext0 + ext1);
+      float absc, trc, src;
+      if (ext != 0.f) {
+        float tau = ext * (float)dels;
+        absc = tau * (1.f - 0.5f * tau * (1.f - 0.33333333333f * tau));
+        trc = 1.f - absc;
+        src = (0.5f * (srcext0 + srcext1) + 0.08333333333f * (ext0 * srcext1 - ext1 * srcext0) * (float)dels *
+                                                (1.f - 0.05f * (ext1 - ext0) * (float)dels)) / ext;
+      } else { absc = 0.f; trc = 1.f; src = 0.f; }
+      radacc += transmit * src * absc;
+      transmit *= trc;
+      ext1 = ext0; srcext1 = srcext0;
+    }
+    int iface, jface;
+    bool openbc;
+    if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; openbc = (cf & 1) && (a.bcflag & 1); }
+    else if (soy <= soz) { iface = 3 - bity; jface = 1; openbc = (cf & 2) && (a.bcflag & 2); }
+    else { iface = 5 - bitz; jface = 2; openbc = false; }
+    int nxt = a.neighptr[6 * (size_t)cell + iface];
+    int kface = iface, kc = cell;
+    if (openbc) { kface = iface ^ 1; kc = nxt; iface = -1; }
+    if (nxt >= 0) {
+      const float *q = a.gridpos + 3 * a.gridptr[8 * (size_t)nxt + ioct0];
+      if (jface == 0) xn = q[0]; else if (jface == 1) yn = q[1]; else zn = q[2];
+    }
+    if (transmit < a.transcut || ngrid > maxcross) {
+      validrad = true;
+    } else if (nxt < 0 && iface >= 4) {
+      validrad = true;
+      const int *gk = a.gridptr + 8 * (size_t)kc;
+      float xs[4], ys[4], rb[4];
+      for (int k = 0; k < 4; ++k) {
+        int q = gk[c_face[kface][k]];
+        xs[k] = a.gridpos[3 * q]; ys[k] = a.gridpos[3 * q + 1];
+        if ((float)mu2 < 0.f) rb[k] = a.skyrad;
+        else { int bi = a.bot_index[q]; rb[k] = bi >= 0 ? a.bcrad_bot[bi] : 0.f; }
+      }
+      float uu = (xs[1] - xs[0] > 0) ? (float)((xn - xs[0]) / (xs[1] - xs[0])) : 0.f;
+      float vv = (ys[2] - ys[0] > 0) ? (float)((yn - ys[0]) / (ys[2] - ys[0])) : 0.f;
+      radacc += transmit * ((1 - uu) * (1 - vv) * rb[0] + uu * (1 - vv) * rb[1] + (1 - uu) * vv * rb[2] + uu * vv * rb[3]);
+    } else {
+      cell = nxt;
+    }
+    xe = xn; ye = yn; ze = zn;
+  }
+  if (lane == 0) a.out[ray] = (float)radacc;
+}
+
+__global__ void k_bcrad_bottom(const int *botp, int nbot, const float *botalb, const float *dirflux,
+                               const float *fluxes, float *bcrad) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nbot) return;
+  int p = botp[k];
+  bcrad[k] = 0.318309886f * botalb[k] * (dirflux[p] + fluxes[2 * (size_t)p]);
+}
+
+// ----------------------------------------------------------------- handle
+template <class T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  void alloc(size_t k) {
+    free();
+    n = k;
+    if (k) CK(cudaMalloc(&p, k * sizeof(T)));
+  }
+  void upload(const std::vector<T> &v) {
+    alloc(v.size());
+    if (n) CK(cudaMemcpy(p, v.data(), n * sizeof(T), cudaMemcpyHostToDevice));
+  }
+  void zero() { if (n) CK(cudaMemset(p, 0, n * sizeof(T))); }
+  void free() { if (p) cudaFree(p); p = nullptr; n = 0; }
+  ~DBuf() { free(); }
+};
+
+struct Handle {
+  Plan P;
+  std::string err;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  // geometry
+  DBuf<float> gridpos, xgrid, ygrid, zgrid;
+  DBuf<int> gridptr, neighptr, cellflags, rank, start, level, order, topp, botp, bot_index, lofj;
+  DBuf<uint8_t> bnd;
+  DBuf<uint32_t> tasks[2];
+  DBuf<float> col_cx, col_cy, col_cz, col_fluxw, amat, bmat, ylmsun;
+  // medium
+  DBuf<float> text, dirflux, coef, tms_w, phasetab, botalb, rad0;
+  DBuf<int> tms_ptr, tms_iph;
+  // state
+  DBuf<float> source, delsource, radiance, srcdo, raddo, fluxes, bcrad;
+  DBuf<int> ns, nso, nr, errflag;
+  DBuf<double> red;
+  DBuf<AccelState> accel;
+  int omax[2] = {0, 0};
+  bool seq[2] = {false, false};  // sequential-order sweep engine per hemisphere
+  bool initialized = false;
+  int iters = 0;
+  float solcrit = 1.f;
+  float timings[5] = {0, 0, 0, 0, 0};
+};
+
+static void upload_plan(Handle &H) {
+  Plan &P = H.P;
+  H.gridpos.upload(P.gridpos); H.xgrid.upload(P.xgrid); H.ygrid.upload(P.ygrid); H.zgrid.upload(P.zgrid);
+  H.gridptr.upload(P.gridptr); H.neighptr.upload(P.neighptr); H.cellflags.upload(P.cellflags);
+  H.rank.upload(P.rank); H.start.upload(P.startcell); H.level.upload(P.level);
+  {
+    std::vector<int> ord((size_t)8 * P.npts, 0);
+    for (int b = 0; b < 8; ++b)
+      for (int i = 0; i < P.npts; ++i) {
+        int r = P.rank[(size_t)b * P.npts + i];
+        if (r >= 0) ord[(size_t)b * P.npts + r] = i;
+      }
+    H.order.upload(ord);
+  }
+  for (int h = 0; h < 2; ++h) {
+    int nlev = (int)P.level_off[h].size() - 1;
+    H.seq[h] = nlev > 4 * (P.nx1 + P.ny1 + P.nz) + 64;
+  }
+  H.bnd.upload(P.bnd); H.topp.upload(P.topp); H.botp.upload(P.botp); H.lofj.upload(P.lofj);
+  std::vector<int> bi(P.npts, -1);
+  for (size_t k = 0; k < P.botp.size(); ++k) bi[P.botp[k]] = (int)k;
+  H.bot_index.upload(bi);
+  for (int h = 0; h < 2; ++h) H.tasks[h].upload(P.tasks[h]);
+  H.col_cx.upload(P.col_cx); H.col_cy.upload(P.col_cy); H.col_cz.upload(P.col_cz); H.col_fluxw.upload(P.col_fluxw);
+  H.ylmsun.upload(P.ylmsun);
+  // dense masked transform matrices in column order
+  const int nlm = P.nlm, nang = P.nang, mm = P.mm, nm = 2 * mm + 1;
+  std::vector<float> A((size_t)nlm * nang, 0.f), B((size_t)nang * (nlm + 2), 0.f);
+  for (int c = 0; c < nang; ++c) {
+    int i = P.col_imu[c], k = P.col_iphi[c];
+    int me = std::max(0, P.nphi0[i] / 2 - 1);
+    const float *c1 = &P.cphi1[((size_t)i * P.nphi0max + k) * nm + mm];
+    const float *c2 = &P.cphi2[((size_t)i * P.nphi0max + k) * nm + mm];
+    for (int j = 0; j < nlm; ++j) {
+      int m = P.mofj[j], ma = std::abs(m);
+      if (ma > me) continue;
+      float fa, fb;
+      if (m == 0) { fa = 1.f; fb = c2[0]; }
+      else if (m > 0) { fa = c1[ma] - c1[-ma]; fb = c2[ma] - c2[-ma]; }
+      else { fa = c1[ma] + c1[-ma]; fb = c2[ma] + c2[-ma]; }
+      A[(size_t)j * nang + c] = P.cmu1[(size_t)i * nlm + j] * fa;
+      B[(size_t)c * (nlm + 2) + j] = P.cmu2[(size_t)i * nlm + j] * fb;
+    }
+    B[(size_t)c * (nlm + 2) + nlm + (c < P.ncol_down ? 0 : 1)] = P.col_fluxw[c];
+  }
+  H.amat.upload(A); H.bmat.upload(B);
+  H.text.upload(P.total_ext); H.dirflux.upload(P.dirflux); H.coef.upload(P.coef);
+  H.tms_ptr.upload(P.tms_ptr); H.tms_iph.upload(P.tms_iph); H.tms_w.upload(P.tms_w);
+  H.phasetab.upload(P.phasetab); H.botalb.upload(P.botalb); H.rad0.upload(P.rad0);
+  for (int h = 0; h < 2; ++h) {
+    int m = 0;
+    for (int b = 0; b < 8; ++b) if (((b >> 2) & 1) == h) m = std::max(m, P.oct_ncol[b]);
+    H.omax[h] = m;
+  }
+  const size_t nf = (size_t)P.npts * nlm, nd = (size_t)P.npts * nang;
+  H.source.alloc(nf); H.delsource.alloc(nf); H.radiance.alloc(nf);
+  H.srcdo.alloc(nd); H.raddo.alloc(nd);
+  H.fluxes.alloc((size_t)P.npts * 2); H.bcrad.alloc(std::max<size_t>(1, P.botp.size()));
+  H.ns.alloc(P.npts); H.nso.alloc(P.npts); H.nr.alloc(P.npts); H.errflag.alloc(1);
+  H.red.alloc(4); H.accel.alloc(1);
+}
+
+static void launch_source(Handle &H, int first, int fixsh) {
+  Plan &P = H.P;
+  SourceArgs a;
+  a.coef = H.coef.p; a.dirflux = H.dirflux.p; a.radiance = H.radiance.p; a.ylmsun = H.ylmsun.p; a.lofj = H.lofj.p;
+  a.source = H.source.p; a.delsource = H.delsource.p; a.ns = H.ns.p; a.nso = H.nso.p; a.nr = H.nr.p; a.red = H.red.p;
+  a.npts = P.npts; a.nlm = P.nlm; a.nl = P.ml + 1; a.ml = P.ml; a.mm = P.mm;
+  a.secmu0 = 1.0f / std::fabs(P.prob.solarmu); a.shacc = P.prob.shacc;
+  a.first = first; a.fixsh = fixsh; a.accel = P.prob.accelflag; a.highorder = P.prob.highorderrad;
+  CK(cudaMemsetAsync(H.red.p, 0, 4 * sizeof(double), H.stream));
+  int blocks = std::min((P.npts + 7) / 8, 152 * 16);
+  k_source<<<blocks, 256, 0, H.stream>>>(a);
+  CK(cudaGetLastError());
+}
+
+static void gemm(Handle &H, const float *A, const float *B, int M, int N, int K, int lda, int ldb, int mode, float *C,
+                 int ldc) {
+  dim3 grid((N + GBN - 1) / GBN, (M + GBM - 1) / GBM);
+  k_gemm<<<grid, 256, 0, H.stream>>>(A, B, M, N, K, lda, ldb, mode, C, ldc, H.nr.p, H.P.nlm, H.fluxes.p);
+  CK(cudaGetLastError());
+}
+
+static void sweep_hemisphere(Handle &H, int hemi) {
+  Plan &P = H.P;
+  SweepArgs a;
+  a.gridpos = H.gridpos.p; a.gridptr = H.gridptr.p; a.neighptr = H.neighptr.p; a.cellflags = H.cellflags.p;
+  a.bnd = H.bnd.p; a.rank = H.rank.p; a.start = H.start.p; a.level = H.level.p; a.text = H.text.p;
+  a.srcdo = H.srcdo.p; a.raddo = H.raddo.p; a.col_cx = H.col_cx.p; a.col_cy = H.col_cy.p; a.col_cz = H.col_cz.p;
+  a.tasks = H.tasks[hemi].p; a.err = H.errflag.p; a.npts = P.npts; a.nang = P.nang; a.is1d = P.is1d;
+  a.transmin = P.prob.transmin;
+  for (int b = 0; b < 8; ++b) { a.oct_col0[b] = P.oct_col0[b]; a.oct_ncol[b] = P.oct_ncol[b]; }
+  if (H.seq[hemi]) {
+    int c0 = hemi ? P.ncol_down : 0, nc = hemi ? P.nang - P.ncol_down : P.ncol_down;
+    if (nc > 0) k_sweep_seq<<<nc, SEQW, 0, H.stream>>>(a, H.order.p, c0);
+    CK(cudaGetLastError());
+    return;
+  }
+  const std::vector<int> &off = P.level_off[hemi];
+  const int omax = std::max(1, H.omax[hemi]);
+  for (size_t l = 0; l + 1 < off.size(); ++l) {
+    int t0 = off[l], nt = off[l + 1] - off[l];
+    if (nt <= 0) continue;
+    long long threads = (long long)nt * omax;
+    int blocks = (int)((threads + 255) / 256);
+    k_sweep<<<blocks, 256, 0, H.stream>>>(a, t0, nt, omax);
+  }
+  CK(cudaGetLastError());
+}
+
+static int check_device_error(Handle &H) {
+  int e = 0;
+  CK(cudaMemcpy(&e, H.errflag.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e == ERR_NONE) return 0;
+  const char *m = "device error";
+  if (e == ERR_SWEEP_NOFACE) m = "BACK_INT_GRID3D: INEXTCELL=0 (no valid face for a boundary trace)";
+  if (e == ERR_SWEEP_STEPS) m = "BACK_INT_GRID: trace exceeded the step limit";
+  if (e == ERR_RAY_SO) m = "INTEGRATE_1RAY: SO<0";
+  if (e == ERR_RAY_BELOW) m = "RENDER: Level below domain";
+  H.err = m;
+  CK(cudaMemset(H.errflag.p, 0, sizeof(int)));
+  return 1;
+}
+
+}  // namespace shdom
+
+using shdom::Handle;
+
+struct shdom_handle {
+  Handle h;
+};
+
+static thread_local std::string g_static_err;
+
+static int fail(shdom_handle *h, const std::string &m) {
+  if (h) h->h.err = m; else g_static_err = m;
+  return 1;
+}
+
+extern "C" {
+
+int shdom_create(const shdom_problem *problem, int device, shdom_handle **out) {
+  if (!problem || !out) return fail(nullptr, "shdom_create: null argument");
+  *out = nullptr;
+  std::unique_ptr<shdom_handle> H(new shdom_handle());
+  try {
+    if (!shdom::build_plan(*problem, H->h.P)) return fail(nullptr, H->h.P.err);
+    if (device >= 0) CK(cudaSetDevice(device));
+    CK(cudaGetDevice(&H->h.device));
+    CK(cudaStreamCreateWithFlags(&H->h.stream, cudaStreamNonBlocking));
+    shdom::upload_plan(H->h);
+    CK(cudaMemset(H->h.errflag.p, 0, sizeof(int)));
+  } catch (const std::exception &e) {
+    return fail(nullptr, e.what());
+  }
+  *out = H.release();
+  return 0;
+}
+
+int shdom_init_solution(shdom_handle *hh) {
+  if (!hh) return fail(nullptr, "null handle");
+  Handle &H = hh->h;
+  try {
+    shdom::Plan &P = H.P;
+    size_t tot = (size_t)P.npts * P.nlm;
+    int blocks = (int)std::min<size_t>((tot + 255) / 256, 152 * 64);
+    shdom::k_init_radiance<<<blocks, 256, 0, H.stream>>>(H.rad0.p, H.radiance.p, H.nr.p, P.npts, P.nlm);
+    CK(cudaMemsetAsync(H.source.p, 0, tot * sizeof(float), H.stream));
+    CK(cudaMemsetAsync(H.delsource.p, 0, tot * sizeof(float), H.stream));
+    CK(cudaMemsetAsync(H.ns.p, 0, P.npts * sizeof(int), H.stream));
+    CK(cudaMemsetAsync(H.nso.p, 0, P.npts * sizeof(int), H.stream));
+    CK(cudaMemsetAsync(H.fluxes.p, 0, (size_t)P.npts * 2 * sizeof(float), H.stream));
+    shdom::AccelState st{0.0, 1.0f, 0.0f};
+    CK(cudaMemcpyAsync(H.accel.p, &st, sizeof(st), cudaMemcpyHostToDevice, H.stream));
+    shdom::launch_source(H, 1, 0);
+    CK(cudaStreamSynchronize(H.stream));
+    H.initialized = true;
+    H.iters = 0;
+    H.solcrit = 1.f;
+  } catch (const std::exception &e) {
+    return fail(hh, e.what());
+  }
+  return 0;
+}
+
+int shdom_solution_iterations(shdom_handle *hh, int maxiter, int *iters, float *solcrit) {
+  if (!hh) return fail(nullptr, "null handle");
+  Handle &H = hh->h;
+  if (!H.initialized) {
+    int rc = shdom_init_solution(hh);
+    if (rc) return rc;
+  }
+  try {
+    shdom::Plan &P = H.P;
+    cudaEvent_t ev[6];
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    for (float &t : H.timings) t = 0.f;
+    bool fixsh = false;
+    const int nlm = P.nlm, nang = P.nang;
+    {  // SOLUTION_ITERATIONS starts every call with no acceleration pending
+      double zero = 0.0;
+      CK(cudaMemcpyAsync(&H.accel.p->a, &zero, sizeof(double), cudaMemcpyHostToDevice, H.stream));
+    }
+    while (H.iters < maxiter && H.solcrit > P.prob.solacc) {
+      ++H.iters;
+      CK(cudaEventRecord(ev[0], H.stream));
+      shdom::gemm(H, H.source.p, H.amat.p, P.npts, nang, nlm, nlm, nang, 0, H.srcdo.p, nang);
+      CK(cudaEventRecord(ev[1], H.stream));
+      int ntop = (int)P.topp.size(), nbot = (int)P.botp.size();
+      if (ntop && P.ncol_down) {
+        int t = ntop * P.ncol_down;
+        shdom::k_preset_top<<<(t + 255) / 256, 256, 0, H.stream>>>(H.topp.p, ntop, H.raddo.p, nang, P.ncol_down, P.prob.skyrad);
+      }
+      shdom::sweep_hemisphere(H, 0);
+      if (nbot)
+        shdom::k_lambertian<<<nbot, 256, 0, H.stream>>>(H.botp.p, nbot, H.botalb.p, H.dirflux.p, H.col_fluxw.p, H.raddo.p,
+                                                         nang, P.ncol_down, H.bcrad.p);
+      shdom::sweep_hemisphere(H, 1);
+      CK(cudaEventRecord(ev[2], H.stream));
+      shdom::gemm(H, H.raddo.p, H.bmat.p, P.npts, nlm + 2, nang, nang, nlm + 2, 1, H.radiance.p, nlm);
+      CK(cudaEventRecord(ev[3], H.stream));
+      if (H.solcrit < 0.001f || H.iters > P.prob.iterfixsh) fixsh = true;
+      shdom::launch_source(H, 0, fixsh ? 1 : 0);
+      shdom::k_accel_param<<<1, 1, 0, H.stream>>>(H.red.p, H.accel.p, P.prob.accelflag);
+      int blocks = (int)std::min<size_t>(((size_t)P.npts * nlm + 255) / 256, 152 * 64);
+      shdom::k_accelerate<<<blocks, 256, 0, H.stream>>>(H.source.p, H.delsource.p, H.ns.p, H.nso.p, P.npts, nlm, H.accel.p);
+      CK(cudaEventRecord(ev[4], H.stream));
+      shdom::AccelState st;
+      CK(cudaMemcpyAsync(&st, H.accel.p, sizeof(st), cudaMemcpyDeviceToHost, H.stream));
+      CK(cudaStreamSynchronize(H.stream));
+      if (shdom::check_device_error(H)) { for (auto &e : ev) cudaEventDestroy(e); return 1; }
+      H.solcrit = st.solcrit;
+      if (P.albmax < P.prob.solacc) H.solcrit = P.prob.solacc;
+      float t01, t12, t23, t34;
+      CK(cudaEventElapsedTime(&t01, ev[0], ev[1])); CK(cudaEventElapsedTime(&t12, ev[1], ev[2]));
+      CK(cudaEventElapsedTime(&t23, ev[2], ev[3])); CK(cudaEventElapsedTime(&t34, ev[3], ev[4]));
+      H.timings[0] += t01; H.timings[1] += t12; H.timings[2] += t23; H.timings[3] += t34;
+      H.timings[4] += t01 + t12 + t23 + t34;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+  } catch (const std::exception &e) {
+    return fail(hh, e.what());
+  }
+  if (iters) *iters = H.iters;
+  if (solcrit) *solcrit = H.solcrit;
+  return 0;
+}
+
+static int render_impl(shdom_handle *hh, int nrays, const float *camx, const float *camy, const float *camz,
+                       const double *cammu, const double *camphi, float *out, cudaStream_t stream) {
+  Handle &H = hh->h;
+  shdom::Plan &P = H.P;
+  int nbot = (int)P.botp.size();
+  if (nbot)
+    shdom::k_bcrad_bottom<<<(nbot + 127) / 128, 128, 0, stream>>>(H.botp.p, nbot, H.botalb.p, H.dirflux.p, H.fluxes.p,
+                                                                  H.bcrad.p);
+  shdom::RenderArgs a;
+  a.gridpos = H.gridpos.p; a.xgrid = H.xgrid.p; a.ygrid = H.ygrid.p; a.zgrid = H.zgrid.p;
+  a.gridptr = H.gridptr.p; a.neighptr = H.neighptr.p; a.cellflags = H.cellflags.p;
+  a.text = H.text.p; a.source = H.source.p; a.coef = H.coef.p; a.dirflux = H.dirflux.p;
+  a.ns = H.ns.p; a.lofj = H.lofj.p; a.tms_ptr = H.tms_ptr.p; a.tms_iph = H.tms_iph.p; a.tms_w = H.tms_w.p;
+  a.phasetab = H.phasetab.p; a.ylmsun = H.ylmsun.p; a.botp = H.botp.p; a.bcrad_bot = H.bcrad.p;
+  a.bot_index = H.bot_index.p; a.camx = camx; a.camy = camy; a.camz = camz; a.cammu = cammu; a.camphi = camphi;
+  a.out = out; a.err = H.errflag.p; a.nrays = nrays; a.nx = P.nx; a.ny = P.ny; a.nz = P.nz; a.nlm = P.nlm;
+  a.nl = P.ml + 1; a.ml = P.ml; a.mm = P.mm; a.bcflag = P.bcflag; a.ipflag = P.ipflag; a.numphase = P.numphase;
+  a.nscatangle = P.nscatangle; a.deltam = P.prob.deltam; a.solarmu = P.prob.solarmu; a.solaraz = P.prob.solaraz;
+  a.secmu0 = 1.0f / std::fabs(P.prob.solarmu); a.skyrad = P.prob.skyrad; a.tautol = P.prob.tautol;
+  a.transcut = P.prob.transcut;
+  if (P.nlm > shdom::RNLM || P.ml + 1 > 64) return fail(hh, "render: too many spherical-harmonic terms");
+  int blocks = (nrays + shdom::RWARPS - 1) / shdom::RWARPS;
+  if (blocks > 0) shdom::k_render<<<blocks, shdom::RWARPS * 32, 0, stream>>>(a);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int shdom_render_device(shdom_handle *hh, int nrays, const float *camx, const float *camy, const float *camz,
+                        const double *cammu, const double *camphi, float *stokes_out, void *stream) {
+  if (!hh) return fail(nullptr, "null handle");
+  try {
+    return render_impl(hh, nrays, camx, camy, camz, cammu, camphi, stokes_out, (cudaStream_t)stream);
+  } catch (const std::exception &e) {
+    return fail(hh, e.what());
+  }
+}
+
+int shdom_render(shdom_handle *hh, int nrays, const float *camx, const float *camy, const float *camz,
+                 const double *cammu, const double *camphi, float *stokes_out) {
+  if (!hh) return fail(nullptr, "null handle");
+  Handle &H = hh->h;
+  if (nrays <= 0) return 0;
+  try {
+    float *d;
+    size_t fb = (size_t)nrays * sizeof(float), db = (size_t)nrays * sizeof(double);
+    CK(cudaMalloc(&d, 3 * fb + 2 * db + fb));
+    float *dx = d, *dy = d + nrays, *dz = d + 2 * (size_t)nrays;
+    double *dmu = (double *)(d + 3 * (size_t)nrays), *dphi = dmu + nrays;
+    float *dout = (float *)(dphi + nrays);
+    CK(cudaMemcpyAsync(dx, camx, fb, cudaMemcpyHostToDevice, H.stream));
+    CK(cudaMemcpyAsync(dy, camy, fb, cudaMemcpyHostToDevice, H.stream));
+    CK(cudaMemcpyAsync(dz, camz, fb, cudaMemcpyHostToDevice, H.stream));
+    CK(cudaMemcpyAsync(dmu, cammu, db, cudaMemcpyHostToDevice, H.stream));
+    CK(cudaMemcpyAsync(dphi, camphi, db, cudaMemcpyHostToDevice, H.stream));
+    int rc = render_impl(hh, nrays, dx, dy, dz, dmu, dphi, dout, H.stream);
+    if (!rc) CK(cudaMemcpyAsync(stokes_out, dout, fb, cudaMemcpyDeviceToHost, H.stream));
+    CK(cudaStreamSynchronize(H.stream));
+    cudaFree(d);
+    if (rc) return rc;
+    if (shdom::check_device_error(H)) return 1;
+  } catch (const std::exception &e) {
+    return fail(hh, e.what());
+  }
+  return 0;
+}
+
+int shdom_export_state(shdom_handle *hh, float *source, int *ns, float *radiance, int *nr, float *fluxes,
+                       float *dirflux) {
+  if (!hh) return fail(nullptr, "null handle");
+  Handle &H = hh->h;
+  shdom::Plan &P = H.P;
+  try {
+    CK(cudaStreamSynchronize(H.stream));
+    size_t nf = (size_t)P.npts * P.nlm;
+    if (source) CK(cudaMemcpy(source, H.source.p, nf * sizeof(float), cudaMemcpyDeviceToHost));
+    if (radiance) CK(cudaMemcpy(radiance, H.radiance.p, nf * sizeof(float), cudaMemcpyDeviceToHost));
+    if (ns) CK(cudaMemcpy(ns, H.ns.p, P.npts * sizeof(int), cudaMemcpyDeviceToHost));
+    if (nr) CK(cudaMemcpy(nr, H.nr.p, P.npts * sizeof(int), cudaMemcpyDeviceToHost));
+    if (fluxes) CK(cudaMemcpy(fluxes, H.fluxes.p, (size_t)P.npts * 2 * sizeof(float), cudaMemcpyDeviceToHost));
+    if (dirflux) CK(cudaMemcpy(dirflux, H.dirflux.p, (size_t)P.npts * sizeof(float), cudaMemcpyDeviceToHost));
+  } catch (const std::exception &e) {
+    return fail(hh, e.what());
+  }
+  return 0;
+}
+
+int shdom_get_sizes(shdom_handle *hh, shdom_sizes *o) {
+  if (!hh || !o) return fail(hh, "null argument");
+  shdom::Plan &P = hh->h.P;
+  o->npts = P.npts; o->ncells = P.ncells; o->nx1 = P.nx1; o->ny1 = P.ny1; o->nz = P.nz; o->nlm = P.nlm;
+  o->nmu = P.nmu; o->nang = P.nang; o->ml = P.ml; o->mm = P.mm; o->bcflag = P.bcflag; o->ipflag = P.ipflag;
+  o->iters = hh->h.iters; o->solcrit = hh->h.solcrit; o->albmax = P.albmax;
+  o->nlevels_down = (int)P.level_off[0].size() - 1;
+  o->nlevels_up = (int)P.level_off[1].size() - 1;
+  return 0;
+}
+
+int shdom_last_timings(shdom_handle *hh, float *ms5) {
+  if (!hh || !ms5) return fail(hh, "null argument");
+  for (int i = 0; i < 5; ++i) ms5[i] = hh->h.timings[i];
+  return 0;
+}
+
+const char *shdom_last_error(shdom_handle *hh) { return hh ? hh->h.err.c_str() : g_static_err.c_str(); }
+
+void shdom_destroy(shdom_handle *hh) {
+  if (!hh) return;
+  if (hh->h.stream) cudaStreamDestroy(hh->h.stream);
+  delete hh;
+}
+
+}  // extern "C"

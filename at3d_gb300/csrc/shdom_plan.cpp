@@ -1,0 +1,891 @@
+// shdom_plan.cpp -- host-side planning for the GPU solve (see shdom_plan.h).
+//
+// Reference routines restated here (AT3D 4.1.3):
+//   grid and cells        _setup_grid at3d/solver.py:2036-2168, NEW_GRIDS and
+//                         INIT_CELL_STRUCTURE src/polarized/shdomsub2.f:16-310
+//   sweep order           SWEEPING_ORDER / SWEEP_BASE_CELL
+//                         src/polarized/shdomsub1.f:3261-3351, :4529-4622
+//   ordinates, SH tables  MAKE_ANGLE_SET, GAUSQUADS, MAKE_SH_DO_COEF, PLMALL,
+//                         YLMALL_UNPOL src/polarized/shdomsub2.f:1061-1220,
+//                         :4874-4912, :4650-4755, :4497-4535
+//   medium                TRILIN_INTERP_PROP src/polarized/shdom90.f90:17-350,
+//                         PREPARE_PROP src/polarized/shdomsub2.f:479-611
+//   direct beam           DIRECT_BEAM_PROP src/polarized/shdom90.f90:352-867
+//   initial radiance      INIT_RADIANCE / EDDRTF / TRIDIAG
+//                         src/polarized/shdomsub2.f:614-1058
+//   single-scatter table  PRECOMPUTE_PHASE_CHECK src/polarized/shdomsub4.f:2388-2491
+//
+// The wavefront level schedule has no counterpart in the reference: the
+// reference sweeps the points of one ordinate one at a time in SWEEPORD
+// order, a point's trace stopping at the first face whose corners come
+// earlier in that order.  Here level(P) = 1 + max level over every corner a
+// trace from P can read for any ordinate of the octant, so all points of one
+// level (and all ordinates) can run at once while every face a trace stops
+// at is still "earlier" in the reference's sense.
+#include "shdom_plan.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <thread>
+
+namespace shdom {
+
+namespace {
+
+const int kGoodNFFT[256] = {
+    1,   2,   3,   4,   5,   6,   7,   8,   9,   10,  11,  12,  13,  14,  16,  16,  18,  18,  20,
+    20,  24,  24,  24,  24,  25,  27,  27,  30,  30,  30,  32,  32,  36,  36,  36,  36,  40,  40,
+    40,  40,  45,  45,  45,  45,  45,  48,  48,  48,  50,  50,  54,  54,  54,  54,  60,  60,  60,
+    60,  60,  60,  64,  64,  64,  64,  72,  72,  72,  72,  72,  72,  72,  72,  80,  80,  80,  80,
+    80,  80,  80,  80,  81,  90,  90,  90,  90,  90,  90,  90,  90,  90,  96,  96,  96,  96,  96,
+    96,  100, 100, 100, 100, 108, 108, 108, 108, 108, 108, 108, 108, 120, 120, 120, 120, 120, 120,
+    120, 120, 120, 120, 120, 120, 128, 128, 128, 128, 128, 128, 128, 128, 144, 144, 144, 144, 144,
+    144, 144, 144, 144, 144, 144, 144, 144, 144, 144, 144, 160, 160, 160, 160, 160, 160, 160, 160,
+    160, 160, 160, 160, 160, 160, 160, 160, 180, 180, 180, 180, 180, 180, 180, 180, 180, 180, 180,
+    180, 180, 180, 180, 180, 180, 180, 180, 180, 192, 192, 192, 192, 192, 192, 192, 192, 192, 192,
+    192, 192, 200, 200, 200, 200, 200, 200, 200, 200, 216, 216, 216, 216, 216, 216, 216, 216, 216,
+    216, 216, 216, 216, 216, 216, 216, 240, 240, 240, 240, 240, 240, 240, 240, 240, 240, 240, 240,
+    240, 240, 240, 240, 240, 240, 240, 240, 240, 240, 240, 240, 256, 256, 256, 256, 256, 256, 256,
+    256, 256, 256, 256, 256, 256, 256, 256, 256};
+
+const int kFace[6][4] = {{0, 2, 4, 6}, {1, 3, 5, 7}, {0, 1, 4, 5}, {2, 3, 6, 7}, {0, 1, 2, 3}, {4, 5, 6, 7}};
+
+template <class F>
+void parallel_for(int n, F f) {
+  int nt = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  if (n < 4096 || nt == 1) { f(0, n); return; }
+  std::vector<std::thread> th;
+  int chunk = (n + nt - 1) / nt;
+  for (int t = 0; t < nt; ++t) {
+    int b = t * chunk, e = std::min(n, b + chunk);
+    if (b < e) th.emplace_back(f, b, e);
+  }
+  for (auto &x : th) x.join();
+}
+
+// d^l_{m0}(x) * sqrt(l + 1/2), l = 0..lmax, by the standard upward recurrence
+// in l started from the closed form at l = m.
+void dm0(double x, int lmax, int m, std::vector<double> &d) {
+  d.assign(lmax + 1, 0.0);
+  if (m > lmax) return;
+  if (m == 0) {
+    d[0] = 1.0;
+    if (lmax >= 1) d[1] = x;
+    for (int n = 1; n < lmax; ++n) d[n + 1] = ((2 * n + 1) * x * d[n] - n * d[n - 1]) / (n + 1);
+  } else {
+    double c = 1.0;
+    for (int k = 1; k <= m; ++k) c *= std::sqrt((double)(m + k) / (double)k);
+    d[m] = ((m & 1) ? -c : c) * std::pow(0.5 * std::sqrt((1.0 - x) * (1.0 + x)), m);
+    for (int n = m; n < lmax; ++n) {
+      double prev = (n > m) ? std::sqrt((double)(n * n - m * m)) * d[n - 1] : 0.0;
+      d[n + 1] = ((2 * n + 1) * x * d[n] - prev) / std::sqrt((double)((n + 1) * (n + 1) - m * m));
+    }
+  }
+  for (int n = 0; n <= lmax; ++n) d[n] *= std::sqrt(n + 0.5);
+}
+
+inline int jidx(int l, int m, int mm) { return (l <= mm) ? l * (l + 1) + m : (2 * mm + 1) * l - mm * mm + m; }
+
+}  // namespace
+
+void ylm_unpol(int ml, int mm, double mu, float phi, float *y) {
+  std::vector<double> d;
+  const double fct = 1.0 / std::sqrt(2.0 * std::acos(-1.0));
+  double x = (double)(float)mu;
+  for (int m = 0; m <= mm; ++m) {
+    dm0(x, ml, m, d);
+    double c = 1, s = 0;
+    if (m > 0) { c = std::cos(m * (double)phi); s = std::sin(m * (double)phi); }
+    for (int l = m; l <= ml; ++l) {
+      double v = fct * d[l];
+      int j = jidx(l, m, mm);
+      y[j] = (float)((c - s) * v);
+      y[j - 2 * m] = (float)((c + s) * v);
+    }
+  }
+}
+
+namespace {
+
+bool build_grid(const shdom_problem &p, Plan &P) {
+  P.nx = std::max(1, p.npx); P.ny = std::max(1, p.npy); P.nz = std::max(2, p.npz);
+  int ip = p.ipflag;
+  if (P.nx == 1) ip |= 1;
+  if (P.ny == 1) ip |= 2;
+  P.ipflag = ip;
+  int bc = 0;
+  if (p.bc_x_open && (ip == 0 || ip == 2 || ip == 4 || ip == 6)) bc += 1;
+  if (p.bc_y_open && (ip == 0 || ip == 1 || ip == 4 || ip == 5)) bc += 2;
+  P.bcflag = bc;
+  if (bc == 1) { P.err = "open x with periodic y boundary conditions is not supported"; return false; }
+  if ((ip & 3) == 1 || (ip & 3) == 2) { P.err = "2D independent pixel mode (ip_flag 1 or 2) is not supported"; return false; }
+  P.is1d = (ip & 3) == 3;
+  P.noct = P.is1d ? 2 : 8;
+  int nx = P.nx, ny = P.ny, nz = P.nz;
+  P.nx1 = nx + 1; P.ny1 = ny + 1;
+  if ((bc & 5) || (ip & 1)) P.nx1 -= 1;
+  if ((bc & 7) || (ip & 2)) P.ny1 -= 1;
+  float dxp = p.delx > 0 ? p.delx : 1.f, dyp = p.dely > 0 ? p.dely : 1.f;
+  P.xgrid.resize(nx + 1); P.ygrid.resize(ny + 1);
+  for (int i = 0; i <= nx; ++i) P.xgrid[i] = ((float)i * (dxp * (float)p.npx)) / (float)nx;
+  for (int i = 0; i <= ny; ++i) P.ygrid[i] = ((float)i * (dyp * (float)p.npy)) / (float)ny;
+  P.zgrid.assign(p.zlevels, p.zlevels + p.npz);
+  P.npts = P.nx1 * P.ny1 * nz;
+  P.gridpos.resize((size_t)P.npts * 3);
+  for (int ix = 0, i = 0; ix < P.nx1; ++ix)
+    for (int iy = 0; iy < P.ny1; ++iy)
+      for (int iz = 0; iz < nz; ++iz, ++i) {
+        P.gridpos[3 * i] = P.xgrid[ix]; P.gridpos[3 * i + 1] = P.ygrid[iy]; P.gridpos[3 * i + 2] = P.zgrid[iz];
+      }
+  int nxc = (bc & 1) ? nx + 1 : nx, nyc = (bc & 2) ? ny + 1 : ny;
+  P.ncells = nxc * nyc * (nz - 1);
+  P.gridptr.assign((size_t)P.ncells * 8, 0);
+  P.neighptr.assign((size_t)P.ncells * 6, -1);
+  P.cellflags.assign(P.ncells, 0);
+  int ic = 0;
+  for (int ix = 1; ix <= nxc; ++ix) {
+    int x0, x1;
+    if (ip & 1) { x0 = x1 = ix; } else if (bc & 1) { x0 = std::max(1, ix - 1); x1 = std::min(nx, ix); } else { x0 = ix; x1 = ix + 1; }
+    for (int iy = 1; iy <= nyc; ++iy) {
+      int y0, y1;
+      if (ip & 2) { y0 = y1 = iy; } else if (bc & 2) { y0 = std::max(1, iy - 1); y1 = std::min(ny, iy); } else { y0 = iy; y1 = iy + 1; }
+      for (int iz = 1; iz < nz; ++iz, ++ic) {
+        auto pt = [&](int z, int y, int x) { return (z - 1) + nz * (y - 1) + nz * P.ny1 * (x - 1); };
+        int *g = &P.gridptr[8 * (size_t)ic];
+        g[0] = pt(iz, y0, x0); g[1] = pt(iz, y0, x1); g[2] = pt(iz, y1, x0); g[3] = pt(iz, y1, x1);
+        g[4] = pt(iz + 1, y0, x0); g[5] = pt(iz + 1, y0, x1); g[6] = pt(iz + 1, y1, x0); g[7] = pt(iz + 1, y1, x1);
+        int *nb = &P.neighptr[6 * (size_t)ic];
+        int sx = (nz - 1) * nyc, sy = nz - 1;
+        if (ip & 1) { nb[0] = nb[1] = ic; P.cellflags[ic] |= 1; }
+        else if (bc & 1) {
+          nb[0] = (ix == 1) ? ic : ic - sx;
+          nb[1] = (ix == nxc) ? ic : ic + sx;
+          if (ix == 1 || ix == nxc) P.cellflags[ic] |= 1;
+        } else {
+          nb[0] = (ix == 1) ? ic + (nxc - 1) * sx : ic - sx;
+          nb[1] = (ix == nx) ? ic - (nxc - 1) * sx : ic + sx;
+        }
+        if (ip & 2) { nb[2] = nb[3] = ic; P.cellflags[ic] |= 2; }
+        else if (bc & 2) {
+          nb[2] = (iy == 1) ? ic : ic - sy;
+          nb[3] = (iy == nyc) ? ic : ic + sy;
+          if (iy == 1 || iy == nyc) P.cellflags[ic] |= 2;
+        } else {
+          nb[2] = (iy == 1) ? ic + (nyc - 1) * sy : ic - sy;
+          nb[3] = (iy == ny) ? ic - (nyc - 1) * sy : ic + sy;
+        }
+        nb[4] = (iz == 1) ? -1 : ic - 1;
+        nb[5] = (iz == nz - 1) ? -1 : ic + 1;
+      }
+    }
+  }
+  P.bnd.assign(P.npts, 0);
+  for (int i = 0; i < P.npts; ++i) {
+    if (P.gridpos[3 * i + 2] >= P.zgrid[nz - 1]) { P.bnd[i] |= 1; P.topp.push_back(i); }
+    if (P.gridpos[3 * i + 2] <= P.zgrid[0]) { P.bnd[i] |= 2; P.botp.push_back(i); }
+  }
+  return true;
+}
+
+// The reference's visiting order of grid points for one trace octant, as a
+// rank per point and the cell through which the point was first reached.
+void sweep_order(Plan &P, int ioct) {
+  int nx = P.nx, ny = P.ny, nz = P.nz, bc = P.bcflag;
+  int nxc = (bc & 1) ? nx + 1 : nx, nyc = (bc & 2) ? ny + 1 : ny;
+  int b = ioct - 1;
+  int six, eix, dix, siy, eiy, diy, siz, eiz, diz;
+  if (b & 1) { dix = 1; if (bc & 1) { six = nxc; eix = std::max(nxc - 1, 1); } else { six = 1; eix = nxc; } }
+  else { dix = -1; if (bc & 1) { six = 1; eix = std::min(2, nxc); } else { six = nxc; eix = 1; } }
+  if (b & 2) { diy = 1; if (bc & 2) { siy = nyc; eiy = std::max(nyc - 1, 1); } else { siy = 1; eiy = nyc; } }
+  else { diy = -1; if (bc & 2) { siy = 1; eiy = std::min(2, nyc); } else { siy = nyc; eiy = 1; } }
+  if (b & 4) { diz = 1; siz = 1; eiz = nz - 1; } else { diz = -1; siz = nz - 1; eiz = 1; }
+  int *rk = &P.rank[(size_t)b * P.npts];
+  int *sc = &P.startcell[(size_t)b * P.npts];
+  std::fill(rk, rk + P.npts, -1);
+  int order = 0, ix = six, iy = siy, iz = siz;
+  while (true) {
+    int cell = (iz - 1) + (nz - 1) * (iy - 1) + (nz - 1) * nyc * (ix - 1);
+    for (int k = 0; k < 8; ++k) {
+      int corner = (k ^ b) ^ 7;  // furthest upstream corner first
+      int pt = P.gridptr[8 * (size_t)cell + corner];
+      if (rk[pt] >= 0) continue;
+      rk[pt] = order++;
+      sc[pt] = cell;
+    }
+    if (ix == eix) {
+      if (iy == eiy) {
+        if (iz == eiz) break;
+        iz += diz;
+        iy = siy;
+      } else {
+        iy = (iy + diy + nyc - 1) % nyc + 1;
+      }
+      ix = six;
+    } else {
+      ix = (ix + dix + nxc - 1) % nxc + 1;
+    }
+  }
+}
+
+// Trace back from point pt along one ordinate with the reference's validity
+// rule (a face is usable when all four corners precede pt in the sweep order
+// or are preset boundary points); returns the corners of the stopping face.
+bool trace_final_face(const Plan &P, int ioct, int pt, double cx, double cy, double cz, int hemi_bnd,
+                      double transmin, int face_out[4]) {
+  const int b = ioct - 1;
+  const int *rk = &P.rank[(size_t)b * P.npts];
+  double cxinv = cx != 0 ? 1.0 / cx : 1e6, cyinv = cy != 0 ? 1.0 / cy : 1e6, czinv = 1.0 / cz;
+  int bitx = cx < 0, bity = cy < 0, bitz = cz < 0;
+  int cell = P.startcell[(size_t)b * P.npts + pt];
+  double xe = P.gridpos[3 * pt], ye = P.gridpos[3 * pt + 1], ze = P.gridpos[3 * pt + 2];
+  double transmit = 1.0;
+  const float *gp = P.gridpos.data();
+  for (int guard = 0; guard < 1000000; ++guard) {
+    if (cell < 0) return false;
+    if (P.is1d) {
+      int iface = 5 - bitz;
+      int i1 = P.gridptr[8 * (size_t)cell + (iface == 4 ? 0 : 4)];
+      int nxt = P.neighptr[6 * (size_t)cell + iface];
+      if ((P.bnd[i1] & hemi_bnd) || rk[i1] < rk[pt]) { face_out[0] = face_out[1] = face_out[2] = face_out[3] = i1; return true; }
+      cell = nxt;
+      continue;
+    }
+    bool ipinx = P.cellflags[cell] & 1, ipiny = P.cellflags[cell] & 2;
+    int iopp = P.gridptr[8 * (size_t)cell + (8 - ioct)];
+    double sox = ipinx ? 1e20 : (gp[3 * iopp] - xe) * cxinv;
+    double soy = ipiny ? 1e20 : (gp[3 * iopp + 1] - ye) * cyinv;
+    double soz = (gp[3 * iopp + 2] - ze) * czinv;
+    double so = std::min(sox, std::min(soy, soz));
+    xe += so * cx; ye += so * cy; ze += so * cz;
+    int iface, jface;
+    if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; }
+    else if (soy <= soz) { iface = 3 - bity; jface = 1; }
+    else { iface = 5 - bitz; jface = 2; }
+    int nxt = P.neighptr[6 * (size_t)cell + iface];
+    int f[4];
+    for (int k = 0; k < 4; ++k) f[k] = P.gridptr[8 * (size_t)cell + kFace[iface][k]];
+    if (nxt >= 0) {
+      int q = P.gridptr[8 * (size_t)nxt + ioct - 1];
+      if (jface == 0) xe = gp[3 * q]; else if (jface == 1) ye = gp[3 * q + 1]; else ze = gp[3 * q + 2];
+    }
+    bool valid = true;
+    for (int k = 0; k < 4; ++k) valid = valid && ((P.bnd[f[k]] & hemi_bnd) || rk[f[k]] < rk[pt]);
+    if (nxt < 0 || (transmit <= transmin && valid)) {
+      if (!valid) return false;
+      for (int k = 0; k < 4; ++k) face_out[k] = f[k];
+      return true;
+    }
+    cell = nxt;
+  }
+  return false;
+}
+
+void trace_dir(float mu, float phi, double &cx, double &cy, double &cz) {
+  const double pi = (double)(float)std::acos(-1.0f);
+  double s = (double)std::sqrt(1.0f - mu * mu);
+  cx = s * std::cos((double)phi + pi);
+  cy = s * std::sin((double)phi + pi);
+  cz = -(double)mu;
+  if (std::fabs(cx) <= 1.0e-5) cx = 0;
+  if (std::fabs(cy) <= 1.0e-5) cy = 0;
+}
+
+int trace_octant(float mu, float phi, int is1d) {
+  double cx, cy, cz;
+  trace_dir(mu, phi, cx, cy, cz);
+  int bz = cz < 0;
+  if (is1d) return 1 + 4 * bz;
+  return 1 + (cx < 0) + 2 * (cy < 0) + 4 * bz;
+}
+
+void build_angles(const shdom_problem &p, Plan &P) {
+  P.nmu = std::max(2, 2 * ((p.nmu + 1) / 2));
+  P.nphi = std::max(1, p.nphi);
+  P.ml = P.nmu - 1;
+  P.mm = std::max(0, P.nphi / 2 - 1);
+  P.nlm = (2 * P.mm + 1) * (P.ml + 1) - P.mm * (P.mm + 1);
+  P.nleg = p.deltam ? P.ml + 1 : P.ml;
+  P.nphi0max = P.nphi;
+  P.lofj.resize(P.nlm); P.mofj.resize(P.nlm);
+  for (int l = 0, j = 0; l <= P.ml; ++l)
+    for (int m = -std::min(l, P.mm); m <= std::min(l, P.mm); ++m, ++j) { P.lofj[j] = l; P.mofj[j] = m; }
+  int nmu = P.nmu, k = nmu / 2;
+  P.mu.resize(nmu); P.wtmu.resize(nmu);
+  for (int j = 1; j <= k; ++j) {  // Gauss-Legendre nodes by Newton iteration
+    double x = std::cos(3.141592654 * (j - .25) / (nmu + .5)), xp, pl, pl1, pl2, dpl;
+    int it = 0;
+    do {
+      pl1 = 1; pl = x;
+      for (int l = 2; l <= nmu; ++l) { pl2 = pl1; pl1 = pl; pl = ((2 * l - 1) * x * pl1 - (l - 1) * pl2) / l; }
+      dpl = nmu * (x * pl - pl1) / (x * x - 1);
+      xp = x; x = xp - pl / dpl; ++it;
+    } while (std::fabs(x - xp) > 3.0e-7 && it < 10);
+    P.mu[j - 1] = (float)-x; P.mu[j - 1 + k] = (float)x;
+    P.wtmu[j - 1] = P.wtmu[j - 1 + k] = (float)(2.0 / ((1.0 - x * x) * dpl * dpl));
+  }
+  P.nphi0.resize(nmu);
+  P.phi.assign((size_t)nmu * P.nphi0max, 0.f); P.wtdo.assign((size_t)nmu * P.nphi0max, 0.f);
+  const float pif = (float)std::acos(-1.0f);
+  P.nang = 0;
+  for (int j = 0; j < nmu; ++j) {
+    if (p.angle_set == 1) P.nphi0[j] = P.nphi0max;
+    else {
+      int n = (int)(0.9f + (float)P.nphi0max * std::sqrt(1.0f - P.mu[j] * P.mu[j]));
+      P.nphi0[j] = std::min(P.nphi0max, kGoodNFFT[std::max(1, std::min(256, n)) - 1]);
+    }
+    float dphi = 2.0f * pif / (float)P.nphi0[j];
+    for (int q = 0; q < P.nphi0[j]; ++q) {
+      P.phi[(size_t)j * P.nphi0max + q] = (float)q * dphi;
+      P.wtdo[(size_t)j * P.nphi0max + q] = dphi * P.wtmu[j];
+    }
+    P.nang += P.nphi0[j];
+  }
+  // column order: hemisphere, trace octant, (imu, iphi)
+  P.col_of.assign((size_t)nmu * P.nphi0max, -1);
+  int col = 0;
+  for (int hemi = 0; hemi < 2; ++hemi) {
+    if (hemi == 1) P.ncol_down = col;
+    for (int ioct = 1; ioct <= 8; ++ioct) {
+      if (((ioct - 1) >> 2 & 1) != hemi) continue;  // bitz=1 traces down: upward ordinates
+      P.oct_col0[ioct - 1] = col;
+      for (int j = (hemi ? k : 0); j < (hemi ? nmu : k); ++j)
+        for (int q = 0; q < P.nphi0[j]; ++q) {
+          if (trace_octant(P.mu[j], P.phi[(size_t)j * P.nphi0max + q], P.is1d) != ioct) continue;
+          P.col_of[(size_t)j * P.nphi0max + q] = col++;
+          P.col_imu.push_back(j); P.col_iphi.push_back(q); P.col_oct.push_back(ioct);
+        }
+      P.oct_ncol[ioct - 1] = col - P.oct_col0[ioct - 1];
+    }
+  }
+  P.col_cx.resize(P.nang); P.col_cy.resize(P.nang); P.col_cz.resize(P.nang); P.col_fluxw.resize(P.nang);
+  for (int c = 0; c < P.nang; ++c) {
+    int j = P.col_imu[c], q = P.col_iphi[c];
+    double cx, cy, cz;
+    trace_dir(P.mu[j], P.phi[(size_t)j * P.nphi0max + q], cx, cy, cz);
+    P.col_cx[c] = (float)cx; P.col_cy[c] = (float)cy; P.col_cz[c] = (float)cz;
+    P.col_fluxw[c] = std::fabs(P.mu[j]) * P.wtdo[(size_t)j * P.nphi0max + q];
+  }
+  // transform coefficients
+  int nlm = P.nlm, mm = P.mm, nm = 2 * mm + 1;
+  P.cmu1.assign((size_t)nmu * nlm, 0.f); P.cmu2.assign((size_t)nmu * nlm, 0.f);
+  std::vector<double> d;
+  const double fct = 1.0 / std::sqrt(2.0 * std::acos(-1.0));
+  for (int i = 0; i < nmu; ++i)
+    for (int m = 0; m <= mm; ++m) {
+      dm0((double)P.mu[i], P.ml, m, d);
+      for (int l = m; l <= P.ml; ++l) {
+        float v = (float)(fct * d[l]);
+        for (int s : {m, -m}) {
+          int j = jidx(l, s, mm);
+          P.cmu1[(size_t)i * nlm + j] = v;
+          P.cmu2[(size_t)i * nlm + j] = v * P.wtmu[i];
+        }
+      }
+    }
+  P.cphi1.assign((size_t)nmu * P.nphi0max * nm, 0.f); P.cphi2.assign((size_t)nmu * P.nphi0max * nm, 0.f);
+  for (int i = 0; i < nmu; ++i) {
+    float w = 1.0f / P.wtmu[i];
+    for (int q = 0; q < P.nphi0[i]; ++q) {
+      float *c1 = &P.cphi1[((size_t)i * P.nphi0max + q) * nm + mm];
+      float *c2 = &P.cphi2[((size_t)i * P.nphi0max + q) * nm + mm];
+      float wd = P.wtdo[(size_t)i * P.nphi0max + q], ph = P.phi[(size_t)i * P.nphi0max + q];
+      c1[0] = 1.f; c2[0] = wd * w;
+      for (int m = 1; m <= mm; ++m) {
+        c1[m] = std::cos((float)m * ph); c1[-m] = std::sin((float)m * ph);
+        c2[m] = c1[m] * wd * w; c2[-m] = c1[-m] * wd * w;
+      }
+    }
+  }
+  P.ylmsun.resize(nlm);
+  ylm_unpol(P.ml, P.mm, (double)p.solarmu, p.solaraz, P.ylmsun.data());
+}
+
+bool build_medium(const shdom_problem &p, Plan &P) {
+  const int npx = p.npx, npy = p.npy, npz = p.npz, ng = npx * npy * npz;
+  const int npart = p.npart, nmic = p.maxnmicro, nq = 8 * nmic, npts = P.npts, nleg = P.nleg, ml = P.ml;
+  P.npart = npart; P.numphase = p.numphase;
+  // Legendre table divided by 2l+1; with delta-M the 0..ML terms hold
+  // chi_l - f (the 'N' interpolation method keeps f in term ML+1).
+  std::vector<float> leg((size_t)p.numphase * (nleg + 1), 0.f);
+  for (int i = 0; i < p.numphase; ++i) {
+    for (int l = 0; l <= nleg && l <= p.nlegp; ++l)
+      leg[(size_t)i * (nleg + 1) + l] = p.legenp[(size_t)i * (p.nlegp + 1) + l] / (float)(2 * l + 1);
+    if (p.deltam) {
+      float f = leg[(size_t)i * (nleg + 1) + ml + 1];
+      for (int l = 0; l <= ml; ++l) leg[(size_t)i * (nleg + 1) + l] -= f;
+    }
+  }
+  for (int k = 0; k < ng * npart * nmic; ++k)
+    if (p.iphasep[k] < 1 || p.iphasep[k] > p.numphase) { P.err = "Phase function indices are out of bounds."; return false; }
+  const float zspan = p.zlevels[npz - 1] - p.zlevels[0];
+  const double extmin = (double)(1.0e-5f / (zspan / (float)npz)), scatmin = 0.1 * extmin;
+  std::vector<float> ext((size_t)npart * npts), alb((size_t)npart * npts);
+  std::vector<int> iph((size_t)npart * npts * nq);
+  std::vector<float> pw((size_t)npart * npts * nq);
+  P.total_ext.assign(npts, 0.f);
+  bool bad = false;
+  for (int ipa = 0; ipa < npart; ++ipa) {
+    parallel_for(npts, [&](int b, int e) {
+      std::vector<std::pair<float, int>> srt(nq);
+      for (int ipt = b; ipt < e; ++ipt) {
+        float x = P.gridpos[3 * ipt], y = P.gridpos[3 * ipt + 1], z = P.gridpos[3 * ipt + 2];
+        int il = 0, iu = npz;
+        while (iu - il > 1) { int im = (iu + il) / 2; if (z >= p.zlevels[im - 1]) il = im; else iu = im; }
+        int iz = std::max(il, 1);
+        double w = std::max(0.0, std::min(1.0, (double)(z - p.zlevels[iz - 1]) / (p.zlevels[iz] - p.zlevels[iz - 1])));
+        int ix = (int)(x / p.delx) + 1;
+        if (std::fabs(x - npx * p.delx) < 0.01f * p.delx) ix = npx;
+        int iy = (int)(y / p.dely) + 1;
+        if (std::fabs(y - npy * p.dely) < 0.01f * p.dely) iy = npy;
+        if (ix < 1 || ix > npx || iy < 1 || iy > npy) { bad = true; continue; }
+        int ixp = ix % npx + 1, iyp = iy % npy + 1;
+        double u = std::max(0.0, std::min(1.0, (double)(x - p.delx * (ix - 1)) / p.delx));
+        if (u < 1e-5) u = 0;
+        if (u > 1 - 1e-5) u = 1;
+        double v = std::max(0.0, std::min(1.0, (double)(y - p.dely * (iy - 1)) / p.dely));
+        if (v < 1e-5) v = 0;
+        if (v > 1 - 1e-5) v = 1;
+        double f[8] = {(1 - u) * (1 - v) * (1 - w), u * (1 - v) * (1 - w), (1 - u) * v * (1 - w), u * v * (1 - w),
+                       (1 - u) * (1 - v) * w,       u * (1 - v) * w,       (1 - u) * v * w,       u * v * w};
+        int i1 = (iz - 1) + npz * (iy - 1) + npz * npy * (ix - 1), i2 = (iz - 1) + npz * (iy - 1) + npz * npy * (ixp - 1);
+        int i3 = (iz - 1) + npz * (iyp - 1) + npz * npy * (ix - 1), i4 = (iz - 1) + npz * (iyp - 1) + npz * npy * (ixp - 1);
+        int ii[8] = {i1, i2, i3, i4, i1 + 1, i2 + 1, i3 + 1, i4 + 1};
+        const float *E = p.extinctp + (size_t)ipa * ng, *A = p.albedop + (size_t)ipa * ng;
+        double e = 0, sc[8], scat = 0;
+        for (int c = 0; c < 8; ++c) { e += f[c] * E[ii[c]]; sc[c] = f[c] * E[ii[c]] * A[ii[c]]; scat += sc[c]; }
+        size_t o = (size_t)ipa * npts + ipt;
+        ext[o] = (float)e;
+        alb[o] = (float)(e > extmin ? scat / e : scat / extmin);
+        int *IP = &iph[o * nq];
+        float *PW = &pw[o * nq];
+        for (int c = 0; c < 8; ++c)
+          for (int q = 0; q < nmic; ++q) {
+            size_t src = ((size_t)ipa * ng + ii[c]) * nmic + q;
+            IP[c * nmic + q] = p.iphasep[src];
+            PW[c * nmic + q] = (float)(scat >= scatmin ? p.phasewtp[src] * sc[c] / scat : p.phasewtp[src] * sc[c] / scatmin);
+          }
+        for (int q = 0; q < nq; ++q)
+          for (int q2 = q + 1; q2 < nq; ++q2)
+            if (IP[q] == IP[q2]) { PW[q] += PW[q2]; PW[q2] = 0.f; }
+        for (int q = 0; q < nq; ++q) srt[q] = {PW[q], IP[q]};
+        std::stable_sort(srt.begin(), srt.end(), [](const std::pair<float, int> &a, const std::pair<float, int> &b2) { return a.first > b2.first; });
+        for (int q = 0; q < nq; ++q) { PW[q] = srt[q].first; IP[q] = srt[q].second; }
+      }
+    });
+    for (int ipt = 0; ipt < npts; ++ipt) P.total_ext[ipt] += ext[(size_t)ipa * npts + ipt];
+  }
+  if (bad) { P.err = "TRILIN: grid point beyond the property grid"; return false; }
+  const float phasemax = 0.999f;
+  auto fterm = [&](size_t o) {  // f = mixed Legendre term ML+1 of one species at one point
+    const int *IP = &iph[o * nq];
+    const float *PW = &pw[o * nq];
+    if (PW[0] >= phasemax) return leg[(size_t)(IP[0] - 1) * (nleg + 1) + ml + 1];
+    float f = 0.f;
+    for (int q = 0; q < nq; ++q) f += leg[(size_t)(IP[q] - 1) * (nleg + 1) + ml + 1] * PW[q];
+    return f;
+  };
+  if (p.deltam) {
+    for (int ipt = 0; ipt < npts; ++ipt) {
+      float s = 0.f;
+      for (int ipa = 0; ipa < npart; ++ipa) s += ext[(size_t)ipa * npts + ipt];
+      P.total_ext[ipt] = std::max(0.f, P.total_ext[ipt] - s);
+    }
+    for (int ipa = 0; ipa < npart; ++ipa)
+      for (int ipt = 0; ipt < npts; ++ipt) {
+        size_t o = (size_t)ipa * npts + ipt;
+        float f = fterm(o);
+        float a = alb[o];
+        alb[o] = (1.f - f) * a / (1.f - a * f);
+        ext[o] = (1.f - a * f) * ext[o];
+        P.total_ext[ipt] += ext[o];
+      }
+  }
+  P.albmax = 0.f;
+  for (float a : alb) P.albmax = std::max(P.albmax, a);
+  // Per-point source coefficients c_l = albedo_mix * chi_mix(l) (the
+  // NEWMETHOD mixing of COMPUTE_SOURCE, src/polarized/shdomsub1.f:1413-1485)
+  // and the exact single-scatter mixture of COMPUTE_SOURCE_1CELL_UNPOL
+  // (src/polarized/shdomsub2.f:3113-3170).
+  const int nl = ml + 1;
+  P.coef.assign((size_t)npts * nl, 0.f);
+  P.tms_ptr.assign(npts + 1, 0);
+  P.tms_iph.clear(); P.tms_w.clear();
+  std::vector<float> lt1(nleg + 1);
+  std::vector<double> lt(nleg + 1);
+  for (int ipt = 0; ipt < npts; ++ipt) {
+    double sumscat = 0.0;
+    std::fill(lt.begin(), lt.end(), 0.0);
+    float etot = P.total_ext[ipt];
+    for (int ipa = 0; ipa < npart; ++ipa) {
+      size_t o = (size_t)ipa * npts + ipt;
+      const int *IP = &iph[o * nq];
+      const float *PW = &pw[o * nq];
+      std::fill(lt1.begin(), lt1.end(), 0.f);
+      bool single = PW[0] >= phasemax;
+      if (single) for (int l = 0; l <= nleg; ++l) lt1[l] = leg[(size_t)(IP[0] - 1) * (nleg + 1) + l];
+      else
+        for (int q = 0; q < nq; ++q) {
+          if (PW[q] <= 1e-5f) continue;
+          for (int l = 0; l <= nleg; ++l) lt1[l] += leg[(size_t)(IP[q] - 1) * (nleg + 1) + l] * PW[q];
+        }
+      float f = 0.f;
+      if (p.deltam) { f = lt1[ml + 1]; for (int l = 0; l <= ml; ++l) lt1[l] /= (1.f - f); }
+      double scat = (double)(ext[o] * alb[o]);
+      sumscat += scat;
+      for (int l = 0; l <= nleg; ++l) lt[l] += scat * lt1[l];
+      // exact single scatter: weight (albedo * ext_ipa / ext) / (1 - f) per phase function
+      float wgt = (etot == 0.f) ? 1.f : ext[o] / etot;
+      if (wgt != 0.f && p.deltam) {
+        float base = alb[o] * wgt / (1.f - f);
+        if (single) { P.tms_iph.push_back(IP[0] - 1); P.tms_w.push_back(base); }
+        else
+          for (int q = 0; q < nq; ++q) {
+            if (PW[q] <= 1e-5f) continue;
+            P.tms_iph.push_back(IP[q] - 1); P.tms_w.push_back(base * PW[q]);
+          }
+      }
+    }
+    double albp = (etot > 1e-10f) ? sumscat / etot : 0.0;
+    for (int l = 0; l <= ml; ++l) {
+      double chi = (sumscat > 1e-10) ? lt[l] / sumscat : lt[l] / npart;
+      if (l == 0) chi = 1.0;
+      P.coef[(size_t)ipt * nl + l] = (float)(albp * chi);
+    }
+    P.tms_ptr[ipt + 1] = (int)P.tms_iph.size();
+  }
+  // Eddington initial radiance per column (INIT_RADIANCE).
+  P.rad0.assign((size_t)npts * 4, 0.f);
+  const int nz = P.nz, nlay = nz - 1;
+  const float pif = (float)std::acos(-1.0f);
+  const float c0 = std::sqrt(1.0f / pif), c1 = std::sqrt(3.0f / (4 * pif));
+  const int ncol = P.nx1 * P.ny1;
+  parallel_for(ncol, [&](int cb, int ce) {
+    std::vector<double> lo(2 * nlay + 3), up(2 * nlay + 3), dg(2 * nlay + 3), rhs(2 * nlay + 3);
+    std::vector<float> od(nlay), al(nlay), as(nlay);
+    for (int col = cb; col < ce; ++col) {
+      for (int iz = 0; iz < nlay; ++iz) {
+        int L = nz - iz - 2, i0 = iz + nz * col, i1 = i0 + 1;
+        float e0 = P.total_ext[i0], e1 = P.total_ext[i1], s0 = 0, s1 = 0, g0 = 0, g1 = 0;
+        for (int ipa = 0; ipa < npart; ++ipa) {
+          size_t o0 = (size_t)ipa * npts + i0, o1 = (size_t)ipa * npts + i1;
+          s0 += alb[o0] * ext[o0]; s1 += alb[o1] * ext[o1];
+          for (int side = 0; side < 2; ++side) {
+            size_t o = side ? o1 : o0;
+            const int *IP = &iph[o * nq];
+            const float *PW = &pw[o * nq];
+            float l1 = 0.f, fm = 0.f;
+            if (PW[0] >= phasemax) { l1 = leg[(size_t)(IP[0] - 1) * (nleg + 1) + 1]; fm = p.deltam ? leg[(size_t)(IP[0] - 1) * (nleg + 1) + ml + 1] : 0.f; }
+            else
+              for (int q = 0; q < nq; ++q) {
+                l1 += leg[(size_t)(IP[q] - 1) * (nleg + 1) + 1] * PW[q];
+                if (p.deltam) fm += leg[(size_t)(IP[q] - 1) * (nleg + 1) + ml + 1] * PW[q];
+              }
+            if (p.deltam) l1 /= (1.f - fm);
+            (side ? g1 : g0) += alb[o] * ext[o] * l1;
+          }
+        }
+        od[L] = (P.zgrid[iz + 1] - P.zgrid[iz]) * (e0 + e1) / 2;
+        al[L] = (e0 + e1 > 0) ? (s0 + s1) / (e0 + e1) : 0.f;
+        as[L] = (s0 + s1 > 0) ? (g0 + g1) / (s0 + s1) : 0.f;
+      }
+      // Eddington two-stream layer coefficients and the pentadiagonal system
+      // reduced to tridiagonal form; solved with partial pivoting.
+      const int n = 2 * nlay + 2;
+      const double mu0 = std::fabs((double)p.solarmu), sf = p.solarflux;
+      double tau = 0.0;
+      for (int l = 0, i = 2; l < nlay; ++l, i += 2) {
+        double dt = od[l], tr, rf, sp, sm;
+        if (dt == 0.0) { tr = 1; rf = 0; sp = 0; sm = 0; }
+        else {
+          double om = al[l], g = as[l];
+          double r = (1.0 - om * (4.0 - 3.0 * g)) / 4.0, t = (7.0 - om * (4.0 + 3.0 * g)) / 4.0;
+          double lam = std::sqrt(3.0 * (1.0 - om) * (1.0 - om * g)), dd, x1 = 0, x2 = 0, ep = 0, em = 0;
+          if (lam == 0.0) { dd = 1.0 / (1.0 + t * dt); tr = dd; rf = -r * dt * dd; }
+          else {
+            x1 = -r; x2 = lam + t;
+            ep = std::exp(std::min(lam * dt, 75.0)); em = 1.0 / ep;
+            tr = 2. * lam / (x2 * ep + (lam - t) * em);
+            rf = x1 * (ep - em) * tr / (2. * lam);
+            dd = 1.0 / (x2 * x2 * ep - x1 * x1 * em);
+          }
+          double ds = 1.0 / (lam * lam - 1.0 / (mu0 * mu0));
+          double b1 = 0.5 * om * (sf / mu0) * std::exp(-tau / mu0) * ds;
+          double b2 = 0.5 * om * (sf / mu0) * std::exp(-(tau + dt) / mu0) * ds;
+          double spp = 1.0 + 1.5 * g * mu0, spm = -1.0 + 1.5 * g * mu0;
+          double r1p = ((t + 1.0 / mu0) * spp + r * spm) * b1, r2m = ((-t + 1.0 / mu0) * spm - r * spp) * b2;
+          double r2p = ((t + 1.0 / mu0) * spp + r * spm) * b2, r1m = ((-t + 1.0 / mu0) * spm - r * spp) * b1;
+          if (lam == 0.0) {
+            double A = (r * dt * r1p - r2m) * dd, B = -(r * r1p + t * r2m) * dd;
+            sp = (B - t * (A + B * dt)) / r + r2p; sm = A + r1m;
+          } else {
+            double cp = (x1 * em * r1p - x2 * r2m) * dd, cm = (-x2 * ep * r1p + x1 * r2m) * dd;
+            sp = x1 * cp * ep + x2 * cm * em + r2p; sm = x2 * cp + x1 * cm + r1m;
+          }
+          tau += dt;
+        }
+        dg[i] = -rf; dg[i + 1] = -rf; lo[i] = 1.0; lo[i + 1] = -tr; up[i] = -tr; up[i + 1] = 1.0;
+        rhs[i] = sm; rhs[i + 1] = sp;
+      }
+      double gem = 1.0 - (double)p.gndalbedo;
+      rhs[1] = 3.1415926535 * p.skyrad; dg[1] = 0.0; up[1] = 1.0;
+      dg[n] = -(1.0 - gem); lo[n] = 1.0; rhs[n] = (1.0 - gem) * sf * std::exp(-tau / mu0);
+      lo[1] = dg[1]; dg[1] = up[1]; up[1] = 0.0; up[n] = 0.0;
+      for (int k = 1; k <= n - 1; ++k) {
+        if (std::fabs(lo[k + 1]) >= std::fabs(lo[k])) {
+          std::swap(lo[k + 1], lo[k]); std::swap(dg[k + 1], dg[k]); std::swap(up[k + 1], up[k]); std::swap(rhs[k + 1], rhs[k]);
+        }
+        double t = -lo[k + 1] / lo[k];
+        lo[k + 1] = dg[k + 1] + t * dg[k];
+        dg[k + 1] = up[k + 1] + t * up[k];
+        up[k + 1] = 0.0;
+        rhs[k + 1] += t * rhs[k];
+      }
+      rhs[n] /= lo[n];
+      rhs[n - 1] = (rhs[n - 1] - dg[n - 1] * rhs[n]) / lo[n - 1];
+      for (int k = n - 2; k >= 1; --k) rhs[k] = (rhs[k] - dg[k] * rhs[k + 1] - up[k] * rhs[k + 2]) / lo[k];
+      for (int iz = 0; iz < nz; ++iz) {
+        int L = nz - 1 - iz;
+        float fu = (float)rhs[2 * L + 1], fd = (float)rhs[2 * L + 2];
+        float *r = &P.rad0[(size_t)(iz + nz * col) * 4];
+        r[0] = c0 * (fu + fd); r[1] = 0.f; r[2] = c1 * (fu - fd); r[3] = 0.f;
+      }
+    }
+  });
+  // Unscaled single-scatter phase table (PRECOMPUTE_PHASE_CHECK).
+  int nlegp = std::max(p.nlegp, nleg);
+  P.nscatangle = std::max(36, std::min(721, 2 * nlegp));
+  P.phasetab.assign((size_t)P.nscatangle * p.numphase, 0.f);
+  const double pi = std::acos(-1.0);
+  std::vector<double> pl(nlegp + 1);
+  for (int j = 0; j < P.nscatangle; ++j) {
+    double x = std::cos(pi * (double)j / (P.nscatangle - 1));
+    pl[0] = 1.0;
+    if (nlegp >= 1) pl[1] = x;
+    for (int n2 = 1; n2 < nlegp; ++n2) pl[n2 + 1] = ((2 * n2 + 1) * x * pl[n2] - n2 * pl[n2 - 1]) / (n2 + 1);
+    for (int i = 0; i < p.numphase; ++i) {
+      double a1 = 0.0;
+      for (int l = 0; l <= nlegp; ++l) {
+        float lg = (l <= p.nlegp) ? p.legenp[(size_t)i * (p.nlegp + 1) + l] : 0.f;
+        a1 += (2.0 * l + 1.0) * (double)(lg / (float)(2 * l + 1)) * pl[l];
+      }
+      if (a1 <= 0.0) { P.err = "PRECOMPUTE_PHASE_CHECK: negative phase function"; return false; }
+      P.phasetab[(size_t)j * p.numphase + i] = (float)(a1 / (4.0 * pi));
+    }
+  }
+  return true;
+}
+
+// DIRECT_BEAM_PROP: per grid point, integrate the delta-M scaled extinction
+// of the property grid along the ray to the sun (trilinear extinction
+// integrated exactly within each property cell).
+void build_direct(const shdom_problem &p, Plan &P) {
+  const int npx = p.npx, npy = p.npy, npz = p.npz, ng = npx * npy * npz, ml = P.ml, nmic = p.maxnmicro;
+  std::vector<double> edp(ng, 0.0);
+  for (int ip = 0; ip < ng; ++ip) {
+    float acc = 0.f;
+    for (int ipa = 0; ipa < p.npart; ++ipa) {
+      double e = p.extinctp[(size_t)ipa * ng + ip], a = p.albedop[(size_t)ipa * ng + ip];
+      if (p.deltam) {
+        int L = ml + 1;
+        double f = 0;
+        for (int q = 0; q < nmic; ++q) {
+          int iph = p.iphasep[((size_t)ipa * ng + ip) * nmic + q];
+          float a_l = (L <= p.nlegp) ? p.legenp[(size_t)(iph - 1) * (p.nlegp + 1) + L] : 0.f;
+          f += (double)(p.phasewtp[((size_t)ipa * ng + ip) * nmic + q] * a_l) / (2 * L + 1);
+        }
+        e = (1.0 - a * f) * e;
+      }
+      acc = (float)(acc + e);
+    }
+    edp[ip] = acc;
+  }
+  const int ipd = (P.ipflag & 4) ? 0 : P.ipflag, bc = P.bcflag;
+  const double sunmu = -(double)p.solarmu, sunaz = (double)(float)(p.solaraz + (float)std::acos(-1.0f));
+  double cx = std::sqrt(1.0 - sunmu * sunmu) * std::cos(sunaz), cy = std::sqrt(1.0 - sunmu * sunmu) * std::sin(sunaz);
+  double cz = std::fabs(sunmu), cxi, cyi, czi;
+  if (std::fabs(cx) > 1e-6) cxi = 1.0 / cx; else { cx = 0; cxi = 1e20; }
+  if (std::fabs(cy) > 1e-6) cyi = 1.0 / cy; else { cy = 0; cyi = 1e20; }
+  if (std::fabs(cz) > 1e-6) czi = 1.0 / cz; else { cz = 0; czi = 1e20; }
+  const int di = cx >= 0 ? 1 : -1, dj = cy >= 0 ? 1 : -1, dk = cz >= 0 ? 1 : -1;
+  const double epsz = 1.0e-6 * (p.zlevels[npz - 1] - p.zlevels[0]);
+  const double dxd = p.delx, dyd = p.dely, xdom = dxd * npx, ydom = dyd * npy;
+  P.dirflux.assign(P.npts, 0.f);
+  parallel_for(P.npts, [&](int b, int e) {
+    for (int ipt = b; ipt < e; ++ipt) {
+      double z = P.gridpos[3 * ipt + 2], x = P.gridpos[3 * ipt], y = P.gridpos[3 * ipt + 1];
+      int il = 0, iu = npz;
+      while (iu - il > 1) { int im = (iu + il) / 2; if (z >= p.zlevels[im - 1]) il = im; else iu = im; }
+      int k = std::max(il, 1), i = (int)(x / dxd) + 1, j = (int)(y / dyd) + 1;
+      if (i > npx && std::fabs(x - xdom) < 0.001 * dxd) i = npx;
+      if (j > npy && std::fabs(y - ydom) < 0.001 * dyd) j = npy;
+      double xe = x, ye = y, ze = z, xp = xe, yp = ye, zp = ze;
+      bool cxf = (ipd & 1) || cx == 0.0, cyf = (ipd & 2) || cy == 0.0;
+      if ((bc & 1) && (std::fabs(x) < 0.01 * dxd || std::fabs(x - (npx - 1) * dxd) < 0.01 * dxd)) cxf = true;
+      if ((bc & 2) && (std::fabs(y) < 0.01 * dyd || std::fabs(y - (npy - 1) * dyd) < 0.01 * dyd)) cyf = true;
+      double path = 0.0;
+      for (int guard = 0; std::fabs(ze - p.zlevels[npz - 1]) > epsz && guard < 4 * (npx + npy + npz) * 64; ++guard) {
+        int ipn = (i == npx) ? ((bc & 1) ? npx : 1) : i + 1, jpn = (j == npy) ? ((bc & 2) ? npy : 1) : j + 1;
+        double x0 = dxd * (i - 1), x1 = x0 + dxd, y0 = dyd * (j - 1), y1 = y0 + dyd, z0 = p.zlevels[k - 1], z1 = p.zlevels[k];
+        int I1 = (k - 1) + npz * (j - 1) + npz * npy * (i - 1), I2 = (k - 1) + npz * (j - 1) + npz * npy * (ipn - 1);
+        int I3 = (k - 1) + npz * (jpn - 1) + npz * npy * (i - 1), I4 = (k - 1) + npz * (jpn - 1) + npz * npy * (ipn - 1);
+        double e1 = edp[I1], e2 = edp[I2], e3 = edp[I3], e4 = edp[I4], e5 = edp[I1 + 1], e6 = edp[I2 + 1], e7 = edp[I3 + 1], e8 = edp[I4 + 1];
+        double sox, soy, soz;
+        if (cxf) sox = 1e30; else if (cx > 0) { sox = (x1 - xe) * cxi; xp = x1; } else { sox = (x0 - xe) * cxi; xp = x0; }
+        if (cyf) soy = 1e30; else if (cy > 0) { soy = (y1 - ye) * cyi; yp = y1; } else { soy = (y0 - ye) * cyi; yp = y0; }
+        if (cz > 0) { soz = (z1 - ze) * czi; zp = z1; } else if (cz < 0) { soz = (z0 - ze) * czi; zp = z0; } else soz = 1e30;
+        double xo = 0, yo = 0, so;
+        if (soz <= sox && soz <= soy) {
+          so = soz; if (!cxf) xp = xe + so * cx; if (!cyf) yp = ye + so * cy; k += dk;
+        } else if (sox <= soy) {
+          so = sox; if (!cyf) yp = ye + so * cy; zp = ze + so * cz; i += di;
+          if (i == 0) { if (bc & 1) { i = 1; cxf = true; } else { i = npx; xo = xdom; } }
+          else if (i == npx + 1) { if (bc & 1) { i = npx; cxf = true; } else { i = 1; xo = -xdom; } }
+        } else {
+          so = soy; if (!cxf) xp = xe + so * cx; zp = ze + so * cz; j += dj;
+          if (j == 0) { if (bc & 2) { j = 1; cyf = true; } else { j = npy; yo = ydom; } }
+          else if (j == npy + 1) { if (bc & 2) { j = npy; cyf = true; } else { j = 1; yo = -ydom; } }
+        }
+        so = std::max(so, 0.0);
+        double ax = 1.0 / (x1 - x0), ay = 1.0 / (y1 - y0), az = 1.0 / (z1 - z0);
+        double u0 = (xe - x0) * ax, v0 = (ye - y0) * ay, w0 = (ze - z0) * az;
+        double du = (xp - x0) * ax - u0, dv = (yp - y0) * ay - v0, dw = (zp - z0) * az - w0;
+        double u0m = 1 - u0, v0m = 1 - v0, w0m = 1 - w0;
+        // trilinear extinction integrated along the segment: a + b/2 + c/3 + d/4
+        double A = (e1 * u0m + e2 * u0) * v0m * w0m + (e3 * u0m + e4 * u0) * v0 * w0m +
+                   (e5 * u0m + e6 * u0) * v0m * w0 + (e7 * u0m + e8 * u0) * v0 * w0;
+        double B = (-du * v0m * w0m - dv * u0m * w0m - dw * u0m * v0m) * e1 + (du * v0m * w0m - dv * u0 * w0m - dw * u0 * v0m) * e2 +
+                   (-du * v0 * w0m + dv * u0m * w0m - dw * u0m * v0) * e3 + (du * v0 * w0m + dv * u0 * w0m - dw * u0 * v0) * e4 +
+                   (-du * v0m * w0 - dv * u0m * w0 + dw * u0m * v0m) * e5 + (du * v0m * w0 - dv * u0 * w0 + dw * u0 * v0m) * e6 +
+                   (-du * v0 * w0 + dv * u0m * w0 + dw * u0m * v0) * e7 + (du * v0 * w0 + dv * u0 * w0 + dw * u0 * v0) * e8;
+        double vw = dv * dw, uw = du * dw, uv = du * dv;
+        double Cc = (vw * u0m + uw * v0m + uv * w0m) * e1 + (vw * u0 - uw * v0m - uv * w0m) * e2 +
+                    (-vw * u0m + uw * v0 - uv * w0m) * e3 + (-vw * u0 - uw * v0 + uv * w0m) * e4 +
+                    (-vw * u0m - uw * v0m + uv * w0) * e5 + (-vw * u0 + uw * v0m - uv * w0) * e6 +
+                    (vw * u0m - uw * v0 - uv * w0) * e7 + (vw * u0 + uw * v0 + uv * w0) * e8;
+        double D = du * dv * dw * (e2 + e3 + e5 + e8 - e1 - e4 - e6 - e7);
+        path += so * (A + 0.5 * B + 0.3333333333333333 * Cc + 0.25 * D);
+        xe = xp + xo; ye = yp + yo; ze = zp;
+      }
+      P.dirflux[ipt] = (float)(p.solarflux * std::exp(-path));
+    }
+  });
+}
+
+bool build_schedule(const shdom_problem &p, Plan &P) {
+  P.rank.assign((size_t)8 * P.npts, -1);
+  P.startcell.assign((size_t)8 * P.npts, -1);
+  P.level.assign((size_t)8 * P.npts, 0);
+  std::vector<int> octs = P.is1d ? std::vector<int>{1, 5} : std::vector<int>{1, 2, 3, 4, 5, 6, 7, 8};
+  const double transmin = p.transmin;
+  bool ok = true;
+  std::vector<std::thread> th;
+  std::vector<std::string> errs(8);
+  for (int ioct : octs) {
+    th.emplace_back([&, ioct]() {
+      sweep_order(P, ioct);
+      const int b = ioct - 1, n = P.npts;
+      const int hemi_bnd = (b & 4) ? 2 : 1;  // trace down: bottom points preset
+      const int *rk = &P.rank[(size_t)b * n];
+      const int *sc = &P.startcell[(size_t)b * n];
+      int *lv = &P.level[(size_t)b * n];
+      std::vector<int> order(n);
+      for (int i = 0; i < n; ++i) order[rk[i]] = i;
+      const int c0 = P.oct_col0[b], nc = P.oct_ncol[b];
+      for (int r = 0; r < n; ++r) {
+        int pt = order[r];
+        if (P.bnd[pt] & hemi_bnd) { lv[pt] = 0; continue; }
+        int cell = sc[pt];
+        const int *g = &P.gridptr[8 * (size_t)cell];
+        bool fast = transmin >= 1.0 && !P.is1d && g[b] == pt;
+        int lvl = 0;
+        if (fast) {
+          for (int k = 0; k < 8 && fast; ++k) {
+            if (k == b) continue;
+            int q = g[k];
+            if (q == pt || !((P.bnd[q] & hemi_bnd) || rk[q] < r)) fast = false;
+            else lvl = std::max(lvl, lv[q]);
+          }
+        }
+        if (!fast) {
+          lvl = 0;
+          for (int c = c0; c < c0 + nc; ++c) {
+            int f[4];
+            double tcx, tcy, tcz;
+            trace_dir(P.mu[P.col_imu[c]], P.phi[(size_t)P.col_imu[c] * P.nphi0max + P.col_iphi[c]], tcx, tcy, tcz);
+            if (!trace_final_face(P, ioct, pt, tcx, tcy, tcz, hemi_bnd, transmin, f)) {
+              errs[b] = "sweep planning: trace found no valid face (BACK_INT_GRID: INEXTCELL=0)";
+              return;
+            }
+            for (int k = 0; k < 4; ++k) lvl = std::max(lvl, lv[f[k]]);
+          }
+        }
+        lv[pt] = lvl + 1;
+      }
+    });
+  }
+  for (auto &t : th) t.join();
+  for (auto &e : errs) if (!e.empty()) { P.err = e; ok = false; }
+  if (!ok) return false;
+  // bucket (octant, point) tasks by level for each hemisphere
+  for (int hemi = 0; hemi < 2; ++hemi) {
+    int maxl = 0;
+    for (int ioct : octs) {
+      int b = ioct - 1;
+      if (((b >> 2) & 1) != hemi || P.oct_ncol[b] == 0) continue;
+      for (int i = 0; i < P.npts; ++i) maxl = std::max(maxl, P.level[(size_t)b * P.npts + i]);
+    }
+    std::vector<int> cnt(maxl + 2, 0);
+    for (int ioct : octs) {
+      int b = ioct - 1;
+      if (((b >> 2) & 1) != hemi || P.oct_ncol[b] == 0) continue;
+      for (int i = 0; i < P.npts; ++i) { int l = P.level[(size_t)b * P.npts + i]; if (l > 0) cnt[l]++; }
+    }
+    P.level_off[hemi].assign(maxl + 1, 0);  // level l (1..maxl) -> offset at index l-1; last = total
+    int acc = 0;
+    for (int l = 1; l <= maxl; ++l) { P.level_off[hemi][l - 1] = acc; acc += cnt[l]; }
+    P.level_off[hemi][maxl] = acc;
+    P.tasks[hemi].assign(acc, 0);
+    std::vector<int> fill(P.level_off[hemi].begin(), P.level_off[hemi].end());
+    for (int ioct : octs) {
+      int b = ioct - 1;
+      if (((b >> 2) & 1) != hemi || P.oct_ncol[b] == 0) continue;
+      for (int i = 0; i < P.npts; ++i) {
+        int l = P.level[(size_t)b * P.npts + i];
+        if (l > 0) P.tasks[hemi][fill[l - 1]++] = ((uint32_t)b << 28) | (uint32_t)i;
+      }
+    }
+  }
+  return true;
+}
+
+}  // namespace
+
+bool build_plan(const shdom_problem &p, Plan &P) {
+  P.prob = p;
+  if (p.nstokes != 1) { P.err = "only nstokes=1 is supported"; return false; }
+  if (p.splitacc > 0) { P.err = "adaptive cell splitting is not supported (split_accuracy must be <= 0)"; return false; }
+  if (p.npart < 1 || p.numphase < 1 || p.maxnmicro < 1) { P.err = "empty medium"; return false; }
+  if (!build_grid(p, P)) return false;
+  build_angles(p, P);
+  if (P.npts >= (1 << 28)) { P.err = "grid too large for the sweep task encoding"; return false; }
+  if (!build_medium(p, P)) return false;
+  build_direct(p, P);
+  // bottom surface albedo (PREP_SURFACE periodic grid + SURFACE_PARM_INTERP)
+  P.botalb.assign(P.botp.size(), p.gndalbedo);
+  if (p.sfc_variable) {
+    int nxs = p.nxsfc, nys = p.nysfc;
+    auto G = [&](int x, int y) { return p.sfc_albedo[(size_t)((y - 1) % nys) * nxs + ((x - 1) % nxs)]; };
+    for (size_t k = 0; k < P.botp.size(); ++k) {
+      int i = P.botp[k];
+      float rx = P.gridpos[3 * i] / p.delxsfc, ry = P.gridpos[3 * i + 1] / p.delysfc;
+      int ix = std::max(1, std::min(nxs, (int)rx + 1)), iy = std::max(1, std::min(nys, (int)ry + 1));
+      float u = std::max(0.f, std::min(1.f, rx - (ix - 1))), v = std::max(0.f, std::min(1.f, ry - (iy - 1)));
+      P.botalb[k] = (1 - u) * (1 - v) * G(ix, iy) + (1 - u) * v * G(ix, iy + 1) + u * (1 - v) * G(ix + 1, iy) + u * v * G(ix + 1, iy + 1);
+    }
+  }
+  if (!build_schedule(p, P)) return false;
+  return true;
+}
+
+}  // namespace shdom

@@ -1,0 +1,75 @@
+// shdom_plan.h -- host-side planning for one SHDOM solve on the GPU.
+//
+// The planner turns a shdom_problem into the flat tables the device kernels
+// read: the base grid and its cells, the reference's sweep order expressed
+// as per-octant ranks and start cells, the wavefront level schedule that
+// lets all ordinates of a hemisphere sweep concurrently, the discrete
+// ordinates with their transform coefficients, and the delta-M scaled
+// medium, direct beam and Eddington initial radiance.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/shdom_problem.h"
+
+namespace shdom {
+
+struct Plan {
+  // ---- base grid (INIT_CELL_STRUCTURE layout, 0-based, -1 = no neighbour)
+  int nx = 0, ny = 0, nz = 0, nx1 = 0, ny1 = 0, npts = 0, ncells = 0;
+  int bcflag = 0, ipflag = 0, is1d = 0, noct = 8;
+  std::vector<float> xgrid, ygrid, zgrid;
+  std::vector<float> gridpos;      // [npts][3]
+  std::vector<int> gridptr;        // [ncells][8]
+  std::vector<int> neighptr;       // [ncells][6]
+  std::vector<int> cellflags;      // [ncells]
+  std::vector<uint8_t> bnd;        // [npts] bit0 top boundary point, bit1 bottom
+  std::vector<int> topp, botp;     // boundary point lists in point order
+  // ---- sweep order per trace octant (index ioct-1): rank and start cell
+  std::vector<int> rank;           // [8][npts], -1 when the octant is unused
+  std::vector<int> startcell;      // [8][npts]
+  std::vector<int> level;          // [8][npts] wavefront level (0 for boundary points)
+  // ---- discrete ordinates
+  int nmu = 0, nphi = 0, ml = 0, mm = 0, nlm = 0, nleg = 0, nang = 0, nphi0max = 0;
+  std::vector<int> nphi0, lofj, mofj;
+  std::vector<float> mu, wtmu, phi, wtdo;        // phi/wtdo [nmu][nphi0max]
+  // Column order of the ordinate-space arrays: hemisphere (down, up), then
+  // trace octant, then (mu, phi) in the reference order.
+  std::vector<int> col_imu, col_iphi, col_oct;   // [nang]
+  std::vector<int> col_of;                       // [nmu][nphi0max] -> column
+  int ncol_down = 0;                             // columns [0, ncol_down) are mu < 0
+  int oct_col0[8] = {0}, oct_ncol[8] = {0};      // column range of each trace octant
+  std::vector<float> col_cx, col_cy, col_cz;     // trace (back) direction per column
+  std::vector<float> col_fluxw;                  // |mu| * wtdo per column
+  std::vector<float> cmu1, cmu2;                 // [nmu][nlm]
+  std::vector<float> cphi1, cphi2;               // [nmu][nphi0max][2mm+1]
+  std::vector<float> ylmsun;                     // [nlm]
+  // ---- medium on the grid
+  int npart = 0, numphase = 0;
+  std::vector<float> total_ext, dirflux;
+  std::vector<float> coef;                       // [npts][ml+1]: albedo * delta-M scaled Legendre term
+  std::vector<int> tms_ptr, tms_iph;             // CSR per point: exact single-scatter mixture
+  std::vector<float> tms_w;
+  std::vector<float> phasetab;                   // [nscatangle][numphase]
+  int nscatangle = 0;
+  float albmax = 0.f;
+  std::vector<float> rad0;                       // [npts][4] Eddington initial radiance
+  std::vector<float> botalb;                     // surface albedo at the bottom points
+  // ---- numerical parameters
+  shdom_problem prob{};
+  // ---- wavefront task lists, per hemisphere (0 down, 1 up)
+  std::vector<uint32_t> tasks[2];                // (ioct-1) << 28 | point
+  std::vector<int> level_off[2];                 // level -> first task
+  std::string err;
+};
+
+// Fills every table of the plan; returns false with plan.err set on error.
+bool build_plan(const shdom_problem &p, Plan &plan);
+
+// Real generalized spherical harmonics (unpolarized element) at one
+// direction, NLM values in the SHDOM term order.
+void ylm_unpol(int ml, int mm, double mu, float phi, float *y);
+
+}  // namespace shdom

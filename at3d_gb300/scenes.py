@@ -1,0 +1,105 @@
+"""Seeded synthetic scenes for the benchmark configurations.
+
+There is no public dataset behind the hot path's benchmark: every field is
+drawn from ``numpy.random.default_rng(seed)`` with the shapes and value
+distributions of the workload descriptions:
+
+* ``cloud_blob``: scalar solar scene on a 32x32x24 periodic grid
+  (dx=dy=0.02 km, dz=0.04 km), NMU=8/NPHI=16; a 3D Gaussian cloud blob
+  (peak 20/km, sigma 0.15 km) times lognormal noise (sigma 0.3), ssa
+  0.999999, Henyey-Greenstein g=0.85 as 64 Legendre terms, plus a Rayleigh
+  layer (0.01/km, ssa 1); Lambertian albedo 0.05, sun zenith 30 deg.
+* ``cloud_field``: 128x128x64 grid (dz=0.025 km), NMU=16/NPHI=32, a k^-5/3
+  Gaussian random field thresholded to 30% cloud fraction, in-cloud
+  lognormal extinction (mean 30/km, log-sigma 0.5), per-wavelength ssa and
+  HG g from the four-wavelength set, 128 Legendre terms.
+* ``orthographic_views``: parallel rays on a regular pixel grid at the domain
+  top for a list of view zenith angles in the azimuth-0 plane; mu and phi
+  point towards the sensor (at3d/sensor.py:44-47 convention).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from ._abi import NumericalParams, Problem, Species
+from .medium import henyey_greenstein_legcoef, rayleigh_legcoef
+
+VIEW_ZENITHS = (0.0, 26.1, -26.1, 45.6, -45.6, 60.0, -60.0, 70.5, -70.5)
+FIELD_SSA = (0.99999, 0.9999, 0.999, 0.99)
+FIELD_G = (0.85, 0.84, 0.82, 0.80)
+
+
+def cloud_blob(seed: int = 1, nx: int = 32, ny: int = 32, nz: int = 24, dx: float = 0.02,
+               dz: float = 0.04, boundary: str = "periodic", nmu: int = 8, nphi: int = 16,
+               solacc: float = 1e-5) -> Problem:
+    rng = np.random.default_rng(seed)
+    x = np.arange(nx) * dx
+    y = np.arange(ny) * dx
+    z = (np.arange(nz) * dz).astype(np.float32)
+    cx, cy, cz = nx * dx / 2, ny * dx / 2, z[-1] / 2
+    X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
+    r2 = (X - cx) ** 2 + (Y - cy) ** 2 + (Z - cz) ** 2
+    ln = rng.lognormal(mean=0.0, sigma=0.3, size=(nx, ny, nz))
+    ext = (20.0 * np.exp(-r2 / (2 * 0.15 ** 2)) * ln).astype(np.float32)
+    cloud = Species(extinction=ext, ssalb=np.full_like(ext, 0.999999),
+                    legcoef=henyey_greenstein_legcoef(0.85, 64))
+    ray_ext = np.full_like(ext, 0.01)
+    rayleigh = Species(extinction=ray_ext, ssalb=np.ones_like(ext), legcoef=rayleigh_legcoef(0.86))
+    params = NumericalParams(num_mu_bins=nmu, num_phi_bins=nphi, solution_accuracy=solacc,
+                             split_accuracy=0.0, x_boundary_condition=boundary,
+                             y_boundary_condition=boundary)
+    return Problem(delx=dx, dely=dx, zlevels=z, species=[cloud, rayleigh],
+                   solarmu=-float(np.cos(np.deg2rad(30.0))), solaraz=0.0, solarflux=1.0,
+                   surface_albedo=0.05, params=params)
+
+
+def powerlaw_field(rng, shape, fraction: float):
+    """Boolean cloud mask from a k^-5/3 Gaussian random field thresholded at
+    the (1-fraction) quantile, plus the field itself."""
+    noise = rng.standard_normal(shape)
+    k = [np.fft.fftfreq(n) for n in shape]
+    K = np.sqrt(sum(np.meshgrid(*[kk ** 2 for kk in k], indexing="ij")))
+    K[0, 0, 0] = np.inf
+    amp = K ** (-5.0 / 6.0)  # power spectrum k^-5/3 -> amplitude k^-5/6
+    f = np.real(np.fft.ifftn(np.fft.fftn(noise) * amp))
+    thr = np.quantile(f, 1.0 - fraction)
+    return f > thr, f
+
+
+def cloud_field(seed: int = 2, wavelength_index: int = 0, nx: int = 128, ny: int = 128, nz: int = 64,
+                dx: float = 0.02, dz: float = 0.025, fraction: float = 0.3, mean_ext: float = 30.0,
+                boundary: str = "open", nmu: int = 16, nphi: int = 32, nleg: int = 128,
+                solacc: float = 1e-4, ssa=None, g=None) -> Problem:
+    rng = np.random.default_rng(seed)
+    mask, _ = powerlaw_field(rng, (nx, ny, nz), fraction)
+    sig = 0.5
+    ln = rng.lognormal(mean=np.log(mean_ext) - 0.5 * sig ** 2, sigma=sig, size=(nx, ny, nz))
+    ext = np.where(mask, ln, 0.0).astype(np.float32)
+    ssa = FIELD_SSA[wavelength_index] if ssa is None else ssa
+    g = FIELD_G[wavelength_index] if g is None else g
+    cloud = Species(extinction=ext, ssalb=np.full_like(ext, ssa), legcoef=henyey_greenstein_legcoef(g, nleg))
+    z = (np.arange(nz) * dz).astype(np.float32)
+    params = NumericalParams(num_mu_bins=nmu, num_phi_bins=nphi, solution_accuracy=solacc,
+                             split_accuracy=0.0, x_boundary_condition=boundary,
+                             y_boundary_condition=boundary)
+    return Problem(delx=dx, dely=dx, zlevels=z, species=[cloud],
+                   solarmu=-float(np.cos(np.deg2rad(30.0))), solaraz=0.0, solarflux=1.0,
+                   surface_albedo=0.05, params=params)
+
+
+def orthographic_views(problem: Problem, npix_x: int, npix_y: int, zeniths=VIEW_ZENITHS):
+    """Ray arrays (x, y, z, mu, phi) for parallel views covering the domain."""
+    npx, npy, npz = problem.shape
+    lx, ly = npx * problem.delx, npy * problem.dely
+    xs = (np.arange(npix_x) + 0.5) * lx / npix_x
+    ys = (np.arange(npix_y) + 0.5) * ly / npix_y
+    X, Y = np.meshgrid(xs, ys, indexing="ij")
+    ztop = float(problem.zlevels[-1])
+    out = [[], [], [], [], []]
+    for zen in zeniths:
+        mu = np.cos(np.deg2rad(abs(zen)))
+        phi = 0.0 if zen >= 0 else np.pi
+        out[0].append(X.ravel()); out[1].append(Y.ravel())
+        out[2].append(np.full(X.size, ztop)); out[3].append(np.full(X.size, mu))
+        out[4].append(np.full(X.size, phi))
+    return tuple(np.concatenate(a) for a in out)

@@ -1,0 +1,168 @@
+"""``RTE``: the SHDOM solver object, GB300 edition.
+
+Mirrors the surface of ``at3d.solver.RTE`` (at3d/solver.py:143-791) for the
+solve / render path: construction from numerical parameters, medium, source
+and surface; ``solve(maxiter)``; ``integrate_to_sensor(sensor)``; ``fluxes``;
+``save_solution``-style state export.  All numerical work happens in the
+CUDA library behind include/shdom_gb300.h; the solution stays resident in
+HBM between calls.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import warnings
+
+import numpy as np
+
+from . import _lib
+from ._abi import NumericalParams, Problem, Species
+
+
+class SHDOMError(RuntimeError):
+    """Raised for a non-zero SHDOM error code (at3d/checks.py:300-311)."""
+
+
+def _check(h, rc):
+    if rc != 0:
+        msg = _lib.lib().shdom_last_error(h)
+        raise SHDOMError(msg.decode() if msg else f"SHDOM error code {rc}")
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class RTE:
+    """Radiative-transfer solve of one medium at one wavelength.
+
+    Parameters follow the reference: ``numerical_params`` (a NumericalParams),
+    ``medium`` (dict name -> Species on a common property grid, given by
+    ``grid``), ``source`` (source.solar), ``surface`` (surface.lambertian).
+    """
+
+    def __init__(self, numerical_params: NumericalParams, medium: dict, source, surface, grid,
+                 num_stokes: int = 1, name: str | None = None, device: int = 0):
+        if num_stokes != 1:
+            raise ValueError("num_stokes must be 1 (scalar radiance)")
+        species = list(medium.values())
+        sa = surface.albedo
+        self.problem = Problem(delx=grid.delx, dely=grid.dely, zlevels=np.asarray(grid.z, np.float32),
+                               species=species, solarmu=source.solarmu, solaraz=source.solaraz,
+                               solarflux=source.solarflux, skyrad=source.skyrad, surface_albedo=sa,
+                               surface_delx=surface.delx, surface_dely=surface.dely, params=numerical_params)
+        self.name = name or f"Radiance {source.wavelength:1.3f} micron"
+        self._create(device)
+
+    @classmethod
+    def from_problem(cls, problem: Problem, device: int = 0, name: str | None = None):
+        self = cls.__new__(cls)
+        self.problem = problem
+        self.name = name or "RTE"
+        self._create(device)
+        return self
+
+    def _create(self, device):
+        L = _lib.lib()
+        self._struct = self.problem.to_struct()
+        h = C.c_void_p()
+        rc = L.shdom_create(C.byref(self._struct), int(device), C.byref(h))
+        if rc:
+            raise SHDOMError(L.shdom_last_error(None).decode())
+        self._h = h
+        self._initialized = False
+
+    # ------------------------------------------------------------------
+    @property
+    def sizes(self) -> dict:
+        s = _lib.ShdomSizes()
+        _check(self._h, _lib.lib().shdom_get_sizes(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def solve(self, maxiter: int, init_solution: bool = True, setup_grid: bool = True, verbose: bool = True,
+              solve: bool = True):
+        """Initialise (direct beam, Eddington radiance, first source) and
+        iterate until the solution criterion reaches solution_accuracy or the
+        iteration count reaches maxiter (at3d/solver.py:279-631)."""
+        L = _lib.lib()
+        if init_solution or not self._initialized:
+            _check(self._h, L.shdom_init_solution(self._h))
+            self._initialized = True
+        it, sc = C.c_int(0), C.c_float(0)
+        _check(self._h, L.shdom_solution_iterations(self._h, int(maxiter), C.byref(it), C.byref(sc)))
+        if verbose:
+            print(f"! Iterations: {it.value:6d}     Final Criterion: {sc.value:9.6f}   [{self.name}]")
+        if sc.value > self.problem.params.solution_accuracy:
+            warnings.warn(f"solver did not converge to solution_accuracy in {it.value} iterations")
+        return it.value, sc.value
+
+    def check_solved(self, verbose: bool = True) -> bool:
+        s = self.sizes
+        ok = self._initialized and s["solcrit"] <= self.problem.params.solution_accuracy
+        if not ok and verbose:
+            warnings.warn("RTE is not converged to the specified solution_accuracy")
+        return ok
+
+    def integrate_to_sensor(self, sensor: dict, single_scatter: bool = False, nosurface: bool = False) -> dict:
+        """Radiance along the sensor's rays (at3d/solver.py:633-791); writes
+        sensor['I'] and returns the sensor."""
+        if single_scatter or nosurface:
+            raise NotImplementedError("single_scatter / nosurface rendering is not supported")
+        self.check_solved(verbose=False)
+        out = self.render(sensor["ray_x"], sensor["ray_y"], sensor["ray_z"], sensor["ray_mu"], sensor["ray_phi"])
+        sensor["I"] = out
+        return sensor
+
+    def render(self, x, y, z, mu, phi) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.float32); y = np.ascontiguousarray(y, np.float32)
+        z = np.ascontiguousarray(z, np.float32)
+        mu = np.ascontiguousarray(mu, np.float64); phi = np.ascontiguousarray(phi, np.float64)
+        out = np.zeros(len(x), np.float32)
+        dp = C.POINTER(C.c_double)
+        _check(self._h, _lib.lib().shdom_render(self._h, len(x), _fp(x), _fp(y), _fp(z), mu.ctypes.data_as(dp),
+                                                 phi.ctypes.data_as(dp), _fp(out)))
+        return out
+
+    def render_device(self, x_ptr: int, y_ptr: int, z_ptr: int, mu_ptr: int, phi_ptr: int, out_ptr: int,
+                      nrays: int, stream: int = 0):
+        """Device-resident variant: CUDA device pointers (e.g. torch
+        ``data_ptr()``) to float32 x/y/z/out and float64 mu/phi; launched
+        asynchronously on ``stream``."""
+        ptrs = [C.c_void_p(v) for v in (x_ptr, y_ptr, z_ptr, mu_ptr, phi_ptr, out_ptr, stream)]
+        _check(self._h, _lib.lib().shdom_render_device(self._h, int(nrays), *ptrs))
+
+    def export_state(self) -> dict:
+        s = self.sizes
+        n, nlm = s["npts"], s["nlm"]
+        src = np.zeros((n, nlm), np.float32); rad = np.zeros((n, nlm), np.float32)
+        ns = np.zeros(n, np.int32); nr = np.zeros(n, np.int32)
+        flx = np.zeros((n, 2), np.float32); dfl = np.zeros(n, np.float32)
+        ip = C.POINTER(C.c_int)
+        _check(self._h, _lib.lib().shdom_export_state(self._h, _fp(src), ns.ctypes.data_as(ip), _fp(rad),
+                                                       nr.ctypes.data_as(ip), _fp(flx), _fp(dfl)))
+        return dict(source=src, ns=ns, radiance=rad, nr=nr, fluxes=flx, dirflux=dfl)
+
+    @property
+    def fluxes(self) -> dict:
+        """Hemispheric fluxes on the base grid: flux_down, flux_up,
+        flux_direct shaped [nx1, ny1, nz] (at3d/solver.py:1148-1200)."""
+        s = self.sizes
+        st = self.export_state()
+        shp = (s["nx1"], s["ny1"], s["nz"])
+        return {"flux_down": st["fluxes"][:, 0].reshape(shp), "flux_up": st["fluxes"][:, 1].reshape(shp),
+                "flux_direct": st["dirflux"].reshape(shp)}
+
+    def timings(self) -> np.ndarray:
+        t = np.zeros(5, np.float32)
+        _check(self._h, _lib.lib().shdom_last_timings(self._h, _fp(t)))
+        return t
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().shdom_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,103 @@
+/*
+ * shdom_gb300.h -- C-ABI of the GB300-native SHDOM solve / render path.
+ *
+ * The reference reaches its Fortran core through f2py (module at3d.core,
+ * exported list tools/generate_pyf.py:51-139).  A drop-in replacement binds
+ * these entry points instead; each one names the at3d.core routine (and the
+ * Python call site) it replaces.  All buffers are plain host pointers unless
+ * the name says _device; sizes are explicit; no library types cross the
+ * boundary.  Every call returns an SHDOM error code with the meaning of
+ * at3d/checks.py:300-311: 0 ok, 1 error (message from shdom_last_error),
+ * 2 out of memory for spherical-harmonic terms.  No call aborts the process.
+ *
+ * A handle owns one solve's state in HBM (medium, source function, radiance,
+ * fluxes, sweep schedule) between calls, the way RTE keeps its numpy arrays
+ * between solve() and integrate_to_sensor() (at3d/solver.py:2635-2652).
+ * Calls on one handle must not overlap; different handles are independent.
+ */
+#ifndef SHDOM_GB300_H
+#define SHDOM_GB300_H
+
+#include <stdint.h>
+
+#include "shdom_problem.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct shdom_handle shdom_handle;
+
+typedef struct shdom_sizes {
+    int npts;      /* grid points (NPTS) */
+    int ncells;    /* grid cells (NCELLS) */
+    int nx1, ny1, nz;
+    int nlm;       /* spherical-harmonic terms (NLM) */
+    int nmu, nang; /* zenith angles, discrete ordinates (NANG) */
+    int ml, mm;
+    int bcflag, ipflag;
+    int iters;     /* iterations done so far (RTE._iters) */
+    int nlevels_down, nlevels_up; /* sweep wavefront levels per hemisphere */
+    float solcrit; /* current solution criterion (RTE._solcrit) */
+    float albmax;
+} shdom_sizes;
+
+/* Builds the grid, the cell structure, the sweep schedule and the medium on
+ * the device for one problem.  Replaces RTE.__init__'s _setup_grid
+ * (core.new_grids, core.init_cell_structure; at3d/solver.py:2036-2168) and
+ * _prepare_optical_properties (core.transfer_pa_to_grid;
+ * at3d/solver.py:2324-2519).  device < 0 keeps the current CUDA device. */
+int shdom_create(const shdom_problem *problem, int device, shdom_handle **out);
+
+/* Direct beam, Eddington initial radiance and the first source function.
+ * Replaces core.make_angle_set, core.make_sh_do_coef and core.init_solution
+ * (at3d/solver.py:2539-2798). */
+int shdom_init_solution(shdom_handle *h);
+
+/* Runs iterations until the solution criterion reaches solacc or the
+ * iteration count reaches maxiter (the count persists across calls, as
+ * RTE._iters does).  Replaces core.solution_iterations
+ * (at3d/solver.py:447-618, SOLUTION_ITERATIONS
+ * src/polarized/shdomsub1.f:445-818).  iters/solcrit may be NULL. */
+int shdom_solution_iterations(shdom_handle *h, int maxiter, int *iters, float *solcrit);
+
+/* Radiance along nrays rays through the solved field.  Host buffers; ray
+ * positions are single precision and directions double precision as in the
+ * reference's RENDER interface (src/polarized/shdomsub4.f:164-165); mu/phi
+ * point towards the sensor.  Replaces core.render (at3d/solver.py:681-759).
+ * stokes_out: [nrays] (Stokes I). */
+int shdom_render(shdom_handle *h, int nrays, const float *camx, const float *camy, const float *camz,
+                 const double *cammu, const double *camphi, float *stokes_out);
+
+/* Same as shdom_render with device-resident ray and output buffers, launched
+ * on the given CUDA stream (cudaStream_t passed as void*, NULL = legacy
+ * default stream).  Asynchronous: returns after the launch. */
+int shdom_render_device(shdom_handle *h, int nrays, const float *camx, const float *camy,
+                        const float *camz, const double *cammu, const double *camphi,
+                        float *stokes_out, void *stream);
+
+/* Solution state export (RTE.save_solution fields, at3d/solver.py:1621-1686)
+ * in a dense layout: source/radiance [npts][nlm] with the terms beyond each
+ * point's truncation set to zero, ns/nr the truncations (SHPTR/RSHPTR
+ * differences), fluxes [npts][2] (down, up) and dirflux [npts].  Any output
+ * pointer may be NULL. */
+int shdom_export_state(shdom_handle *h, float *source, int *ns, float *radiance, int *nr,
+                       float *fluxes, float *dirflux);
+
+int shdom_get_sizes(shdom_handle *h, shdom_sizes *out);
+
+/* Device time (ms, CUDA events) of the last shdom_solution_iterations call
+ * split by phase: [0] source->ordinate transform, [1] sweeps, [2]
+ * ordinate->harmonic transform, [3] source + acceleration, [4] total. */
+int shdom_last_timings(shdom_handle *h, float *ms5);
+
+/* Message of the last non-zero return on this handle (CHARACTER*600 errmsg
+ * of the reference); a static message when h is NULL. */
+const char *shdom_last_error(shdom_handle *h);
+
+void shdom_destroy(shdom_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
