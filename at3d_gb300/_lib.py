@@ -18,7 +18,8 @@ class ShdomSizes(C.Structure):
     _fields_ = [("npts", C.c_int), ("ncells", C.c_int), ("nx1", C.c_int), ("ny1", C.c_int), ("nz", C.c_int),
                 ("nlm", C.c_int), ("nmu", C.c_int), ("nang", C.c_int), ("ml", C.c_int), ("mm", C.c_int),
                 ("bcflag", C.c_int), ("ipflag", C.c_int), ("iters", C.c_int), ("nlevels_down", C.c_int),
-                ("nlevels_up", C.c_int), ("solcrit", C.c_float), ("albmax", C.c_float)]
+                ("nlevels_up", C.c_int), ("solcrit", C.c_float), ("albmax", C.c_float),
+                ("launches", C.c_longlong)]
 
 
 # name -> (restype, argtypes): the exported surface of include/shdom_gb300.h

@@ -849,6 +849,7 @@ struct Handle {
   int iters = 0;
   float solcrit = 1.f;
   float timings[5] = {0, 0, 0, 0, 0};
+  long long launches = 0;
 };
 
 static void upload_plan(Handle &H) {
@@ -924,6 +925,7 @@ static void launch_source(Handle &H, int first, int fixsh) {
   CK(cudaMemsetAsync(H.red.p, 0, 4 * sizeof(double), H.stream));
   int blocks = std::min((P.npts + 7) / 8, 152 * 16);
   k_source<<<blocks, 256, 0, H.stream>>>(a);
+  H.launches += 1;
   CK(cudaGetLastError());
 }
 
@@ -931,6 +933,7 @@ static void gemm(Handle &H, const float *A, const float *B, int M, int N, int K,
                  int ldc) {
   dim3 grid((N + GBN - 1) / GBN, (M + GBM - 1) / GBM);
   k_gemm<<<grid, 256, 0, H.stream>>>(A, B, M, N, K, lda, ldb, mode, C, ldc, H.nr.p, H.P.nlm, H.fluxes.p);
+  H.launches += 1;
   CK(cudaGetLastError());
 }
 
@@ -957,6 +960,7 @@ static void sweep_hemisphere(Handle &H, int hemi) {
     long long threads = (long long)nt * omax;
     int blocks = (int)((threads + 255) / 256);
     k_sweep<<<blocks, 256, 0, H.stream>>>(a, t0, nt, omax);
+    H.launches += 1;
   }
   CK(cudaGetLastError());
 }
@@ -1018,6 +1022,7 @@ int shdom_init_solution(shdom_handle *hh) {
     size_t tot = (size_t)P.npts * P.nlm;
     int blocks = (int)std::min<size_t>((tot + 255) / 256, 152 * 64);
     shdom::k_init_radiance<<<blocks, 256, 0, H.stream>>>(H.rad0.p, H.radiance.p, H.nr.p, P.npts, P.nlm);
+    H.launches += 1;
     CK(cudaMemsetAsync(H.source.p, 0, tot * sizeof(float), H.stream));
     CK(cudaMemsetAsync(H.delsource.p, 0, tot * sizeof(float), H.stream));
     CK(cudaMemsetAsync(H.ns.p, 0, P.npts * sizeof(int), H.stream));
@@ -1063,11 +1068,14 @@ int shdom_solution_iterations(shdom_handle *hh, int maxiter, int *iters, float *
       if (ntop && P.ncol_down) {
         int t = ntop * P.ncol_down;
         shdom::k_preset_top<<<(t + 255) / 256, 256, 0, H.stream>>>(H.topp.p, ntop, H.raddo.p, nang, P.ncol_down, P.prob.skyrad);
+        H.launches += 1;
       }
       shdom::sweep_hemisphere(H, 0);
-      if (nbot)
+      if (nbot) {
         shdom::k_lambertian<<<nbot, 256, 0, H.stream>>>(H.botp.p, nbot, H.botalb.p, H.dirflux.p, H.col_fluxw.p, H.raddo.p,
                                                          nang, P.ncol_down, H.bcrad.p);
+        H.launches += 1;
+      }
       shdom::sweep_hemisphere(H, 1);
       CK(cudaEventRecord(ev[2], H.stream));
       shdom::gemm(H, H.raddo.p, H.bmat.p, P.npts, nlm + 2, nang, nang, nlm + 2, 1, H.radiance.p, nlm);
@@ -1075,6 +1083,7 @@ int shdom_solution_iterations(shdom_handle *hh, int maxiter, int *iters, float *
       if (H.solcrit < 0.001f || H.iters > P.prob.iterfixsh) fixsh = true;
       shdom::launch_source(H, 0, fixsh ? 1 : 0);
       shdom::k_accel_param<<<1, 1, 0, H.stream>>>(H.red.p, H.accel.p, P.prob.accelflag);
+      H.launches += 2;
       int blocks = (int)std::min<size_t>(((size_t)P.npts * nlm + 255) / 256, 152 * 64);
       shdom::k_accelerate<<<blocks, 256, 0, H.stream>>>(H.source.p, H.delsource.p, H.ns.p, H.nso.p, P.npts, nlm, H.accel.p);
       CK(cudaEventRecord(ev[4], H.stream));
@@ -1104,9 +1113,11 @@ static int render_impl(shdom_handle *hh, int nrays, const float *camx, const flo
   Handle &H = hh->h;
   shdom::Plan &P = H.P;
   int nbot = (int)P.botp.size();
-  if (nbot)
+  if (nbot) {
     shdom::k_bcrad_bottom<<<(nbot + 127) / 128, 128, 0, stream>>>(H.botp.p, nbot, H.botalb.p, H.dirflux.p, H.fluxes.p,
                                                                   H.bcrad.p);
+    H.launches += 1;
+  }
   shdom::RenderArgs a;
   a.gridpos = H.gridpos.p; a.xgrid = H.xgrid.p; a.ygrid = H.ygrid.p; a.zgrid = H.zgrid.p;
   a.gridptr = H.gridptr.p; a.neighptr = H.neighptr.p; a.cellflags = H.cellflags.p;
@@ -1121,7 +1132,10 @@ static int render_impl(shdom_handle *hh, int nrays, const float *camx, const flo
   a.transcut = P.prob.transcut;
   if (P.nlm > shdom::RNLM || P.ml + 1 > 64) return fail(hh, "render: too many spherical-harmonic terms");
   int blocks = (nrays + shdom::RWARPS - 1) / shdom::RWARPS;
-  if (blocks > 0) shdom::k_render<<<blocks, shdom::RWARPS * 32, 0, stream>>>(a);
+  if (blocks > 0) {
+    shdom::k_render<<<blocks, shdom::RWARPS * 32, 0, stream>>>(a);
+    H.launches += 1;
+  }
   CK(cudaGetLastError());
   return 0;
 }
@@ -1193,6 +1207,7 @@ int shdom_get_sizes(shdom_handle *hh, shdom_sizes *o) {
   o->iters = hh->h.iters; o->solcrit = hh->h.solcrit; o->albmax = P.albmax;
   o->nlevels_down = (int)P.level_off[0].size() - 1;
   o->nlevels_up = (int)P.level_off[1].size() - 1;
+  o->launches = hh->h.launches;
   return 0;
 }
 

@@ -1,0 +1,300 @@
+"""Benchmark of the SHDOM solve + render path on GB300.
+
+Workload (one step): the four-wavelength scalar scene -- a 128x128x64 grid
+(dx=dy=0.02 km, dz=0.025 km), NMU=16 / NPHI=32 (NLM=256, 354 ordinates), a
+seeded k^-5/3 power-law cloud field at 30% cloud fraction with lognormal
+in-cloud extinction (mean 30/km), per-wavelength ssa 0.99999/0.9999/0.999/0.99
+and Henyey-Greenstein g 0.85/0.84/0.82/0.80 (128 Legendre terms), open
+boundaries (the workload does not state them), solar zenith 30 deg,
+Lambertian albedo 0.05 -- solved to solution accuracy 1e-4 and rendered on
+64x64 pixels x 9 view zeniths per wavelength.  All data synthetic (seeded).
+
+value: solves/s with the medium resident in HBM (init + iterations + render
+from device-resident rays); e2e: the same through the public host-buffer API
+(problem arrays and rays from host memory, radiances back to host).
+
+--impl reference times the CPU restatement of the reference Fortran
+(oracle/, the reference's Fortran core cannot be compiled: no Fortran
+compiler) on the same scenes.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NWAVE = 4
+# Iterations per solve of the four benchmark scenes (GB300 FP32 path; the
+# oracle converges in the same count to +-1, see tests/test_gpu_parity.py).
+# Used by the CPU arms to scale a one-iteration sample to a full solve.
+SOLVE_ITERS = None
+
+
+def scenes(args):
+    from at3d_gb300.scenes import cloud_field, orthographic_views
+    pbs = [cloud_field(seed=2, wavelength_index=w, nx=args.nx, ny=args.nx, nz=args.nz,
+                       boundary=args.boundary, solacc=args.solacc) for w in range(args.nwave)]
+    rays = orthographic_views(pbs[0], args.npix, args.npix)
+    return pbs, rays
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    return rank, ws
+
+
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons while running."""
+
+    def __init__(self, gpu: int):
+        self.gpu, self.samples, self.proc = gpu, [], None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 6:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[2 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons}
+
+
+def gb300_arm(args, rank, ws):
+    import torch
+    from at3d_gb300.solver import RTE
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    pbs, rays = scenes(args)
+    nr = len(rays[0])
+    rtes = [RTE.from_problem(pb, device=dev, name=f"wavelength {w}") for w, pb in enumerate(pbs)]
+    d = [torch.tensor(np.asarray(r), dtype=torch.float32 if i < 3 else torch.float64, device="cuda")
+         for i, r in enumerate(rays)]
+    outs = [torch.empty(nr, dtype=torch.float32, device="cuda") for _ in range(args.nwave)]
+    iters = [0] * args.nwave
+
+    def step():
+        for w, r in enumerate(rtes):
+            it, _ = r.solve(args.maxiter, verbose=False)
+            iters[w] = it
+            r.render_device(d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), d[3].data_ptr(), d[4].data_ptr(),
+                            outs[w].data_ptr(), nr, 0)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    launches0 = sum(r.sizes["launches"] for r in rtes)
+    phase = np.zeros(5)
+    t_ev0, t_ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        barrier()
+        t_ev0.record()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step()
+            phase += sum(np.asarray(r.timings(), np.float64) for r in rtes)
+        t_ev1.record()
+        barrier()
+        wall = time.perf_counter() - t0
+    launches = sum(r.sizes["launches"] for r in rtes) - launches0
+    ms_dev = t_ev0.elapsed_time(t_ev1)
+    ms_step = max(ms_dev, wall * 1e3) / args.steps
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms_step], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    solves_per_s = ws * args.nwave / (ms_step / 1e3)
+    rays_per_s = ws * args.nwave * nr / (ms_step / 1e3)
+
+    # ---- end to end through the host-buffer API (create + solve + render)
+    def e2e_step():
+        res = []
+        for w, pb in enumerate(pbs):
+            r = RTE.from_problem(pb, device=dev)
+            r.solve(args.maxiter, verbose=False)
+            res.append(r.render(*rays))
+            r.close()
+        return res
+
+    e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    ne = max(1, args.steps // 2)
+    for _ in range(ne):
+        res = e2e_step()
+    barrier()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / ne
+    h2d = 0
+    for pb in pbs:
+        for s in pb.species:
+            h2d += s.extinction.nbytes + s.ssalb.nbytes + np.asarray(s.legcoef).nbytes
+        h2d += pb.zlevels.nbytes
+    h2d += args.nwave * sum(np.asarray(r, np.float32 if i < 3 else np.float64).nbytes for i, r in enumerate(rays))
+    d2h = args.nwave * nr * 4
+    e2e = {"value": ws * args.nwave / (e2e_ms / 1e3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms}
+
+    # ---- roofline of the dominant phase
+    s0 = rtes[0].sizes
+    npts, nlm, nang = s0["npts"], s0["nlm"], s0["nang"]
+    total_iters = args.steps * sum(iters)
+    names = ["transform_sh_to_do", "sweep", "transform_do_to_sh", "source"]
+    dom = int(np.argmax(phase[:4]))
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    per_iter_ms = phase[dom] / max(1, total_iters)
+    if dom == 0:
+        alg = 4.0 * npts * (nlm + nang)          # read SOURCE, write the ordinate-space source
+    elif dom == 2:
+        alg = 4.0 * npts * (nang + nlm + 2)      # read ordinate radiance, write RADIANCE + fluxes
+    elif dom == 1:
+        alg = 4.0 * npts * nang * 2 + 4.0 * npts  # ordinate source in, ordinate radiance out, extinction
+    else:
+        alg = 4.0 * npts * (nlm * 5 + 8)          # radiance, source, delsource r/w, coefficients
+    achieved = alg / (per_iter_ms / 1e3) / 1e9
+    roofline = {"kernel": names[dom], "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": None, "peak_source": "measured" if peaks else "fallback",
+                "phase_ms_per_iter": {n: float(phase[i] / max(1, total_iters)) for i, n in enumerate(names)}}
+    return dict(solves_per_s=solves_per_s, rays_per_s=rays_per_s, ms_step=ms_step, launches=launches,
+                iters=list(iters), e2e=e2e, roofline=roofline, clocks=clk.summary(), npts=npts)
+
+
+def cpu_sample(args, wavelength: int, iters: int):
+    """One oracle iteration of one wavelength, scaled to a full solve."""
+    from oracle.oracle import Oracle
+    pbs, _ = scenes(args)
+    o = Oracle(pbs[wavelength], fp64=False)
+    t0 = time.perf_counter()
+    o.init_solution()
+    t_init = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    o.solve(1)
+    t_it = time.perf_counter() - t0
+    return t_init + iters * t_it, t_init, t_it
+
+
+def reference_arm(args, rank, ws):
+    if rank != 0:
+        return None
+    iters = args.ref_iters
+    per_step = []
+    for s in range(args.warmup + args.steps):
+        w = s % args.nwave
+        t_solve, t_init, t_it = cpu_sample(args, w, iters[w])
+        if s >= args.warmup:
+            per_step.append(t_solve)
+    sec_per_solve = float(np.mean(per_step))
+    v = 1.0 / sec_per_solve
+    return {"metric": "SHDOM solves/s", "value": v, "unit": "solves/s", "impl": "reference", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec_per_solve * 1e3,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": config_dict(args),
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": 1, "kind": "port",
+                             "sample": f"one SHDOM iteration of one wavelength per step on the full grid, "
+                                       f"scaled by the iterations per solve {iters} plus the measured "
+                                       f"initialisation; single thread (one solve per thread, as the reference)"},
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def config_dict(args):
+    return {"workload": f"4-wavelength scalar SHDOM {args.nx}x{args.nx}x{args.nz}, NMU=16 NPHI=32, "
+                        f"{args.npix}x{args.npix}x9 renders per wavelength",
+            "grid": [args.nx, args.nx, args.nz], "wavelengths": NWAVE, "nmu": 16, "nphi": 32,
+            "boundary": args.boundary, "solution_accuracy": args.solacc,
+            "rays_per_wavelength": args.npix * args.npix * 9,
+            "l2": "inputs larger than L2 (about 6 GB of state per wavelength)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nx", type=int, default=128)
+    ap.add_argument("--nz", type=int, default=64)
+    ap.add_argument("--npix", type=int, default=64)
+    ap.add_argument("--boundary", default="open")
+    ap.add_argument("--solacc", type=float, default=1e-4)
+    ap.add_argument("--maxiter", type=int, default=100)
+    ap.add_argument("--nwave", type=int, default=NWAVE, help="wavelengths per step (profiling runs use 1)")
+    ap.add_argument("--ref-iters", type=str, default="")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.ref_iters = [int(x) for x in args.ref_iters.split(",")] if args.ref_iters else \
+        (SOLVE_ITERS or [12, 12, 12, 12])
+    rank, ws = dist_init()
+    if args.impl == "reference":
+        out = reference_arm(args, rank, ws)
+        if out:
+            print(json.dumps(out))
+        return
+    r = gb300_arm(args, rank, ws)
+    if rank != 0:
+        return
+    cpu = None
+    if ws == 1 and not args.no_cpu_baseline:
+        t_solve, t_init, t_it = cpu_sample(args, 0, r["iters"][0])
+        cpu = {"value": 1.0 / t_solve, "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": f"oracle (CPU restatement of the reference Fortran): initialisation ({t_init:.1f} s) "
+                         f"plus one iteration ({t_it:.1f} s) of wavelength 0 on the full grid, scaled to the "
+                         f"{r['iters'][0]} iterations of its solve; single thread"}
+    out = {"metric": "SHDOM solves/s", "value": r["solves_per_s"], "unit": "solves/s", "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_step"], "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": config_dict(args), "rays_per_s": r["rays_per_s"], "iterations_per_solve": r["iters"],
+           "e2e": r["e2e"], "gpu_launches": r["launches"], "roofline": r["roofline"], "cpu_baseline": cpu,
+           "clocks": r["clocks"]}
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

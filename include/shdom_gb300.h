@@ -40,6 +40,7 @@ typedef struct shdom_sizes {
     int nlevels_down, nlevels_up; /* sweep wavefront levels per hemisphere */
     float solcrit; /* current solution criterion (RTE._solcrit) */
     float albmax;
+    long long launches; /* kernels launched on this handle since creation */
 } shdom_sizes;
 
 /* Builds the grid, the cell structure, the sweep schedule and the medium on

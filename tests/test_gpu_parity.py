@@ -80,3 +80,23 @@ def test_cloud_blob_converged_render(rte_cls):
     rg = r.render(*rays)
     ro = o.render(*rays, nthreads=8)
     assert relrms(rg, ro) < 1e-4
+
+
+def test_cloud_field_nmu16_open(rte_cls):
+    """The multi-wavelength scene's regime (NMU=16, NPHI=32, 256 SH terms,
+    open boundaries, zero extinction outside the cloud) at reduced size."""
+    from at3d_gb300.scenes import cloud_field
+    pb = cloud_field(seed=7, wavelength_index=3, nx=20, ny=20, nz=12, nleg=128)
+    r = rte_cls.from_problem(pb)
+    r.solve(3, verbose=False)
+    o = Oracle(pb, fp64=False)
+    o.solve(3)
+    a, b = r.export_state(), o.export()
+    assert np.array_equal(a["ns"], b["ns"]) and np.array_equal(a["nr"], b["nr"])
+    assert relrms(a["source"], b["source"]) < 1e-4
+    assert relrms(a["radiance"], b["radiance"]) < 1e-4
+    it_g, _ = r.solve(100, init_solution=False, verbose=False)
+    it_o, _ = o.solve(100)
+    assert abs(it_g - it_o) <= 1
+    rays = orthographic_views(pb, 12, 12)
+    assert relrms(r.render(*rays), o.render(*rays, nthreads=8)) < 1e-4
