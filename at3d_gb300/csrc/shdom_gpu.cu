@@ -2,12 +2,14 @@
 // the GB300 SHDOM solve / render path.
 //
 // One iteration (SOLUTION_ITERATIONS, src/polarized/shdomsub1.f:674-797):
-//   1. SH -> DO   : SRCDO[p][c] = max(0, sum_j SOURCE[p][j] A[j][c])   (k_gemm, mode 0)
+//   1. SH -> DO   : SRCDO[p][c] = max(0, source in ordinate c)  (k_sh_to_do)
 //   2. sweeps     : downward ordinates, Lambertian bottom, upward ordinates;
 //                   every wavefront level is one k_sweep launch over all
-//                   (octant, point, ordinate) tasks of that level
-//   3. DO -> SH   : RADIANCE[p][j] = sum_c RADDO[p][c] B[c][j] (masked to
+//                   (octant, point, ordinate) tasks of that level, or one
+//                   k_sweep_seq launch for grids whose wavefront is too deep
+//   3. DO -> SH   : RADIANCE[p][j] from the ordinate radiances (masked to
 //                   the point's radiance truncation) + hemispheric fluxes
+//                   (k_do_to_sh)
 //   4. source     : k_source (COMPUTE_SOURCE fused: dot products in FP64,
 //                   delta-source, new truncation, next radiance truncation)
 //   5. k_accel_param, k_accelerate (CALC_ACCEL_SOLCRIT, ACCELERATE_SOLUTION)
@@ -15,6 +17,8 @@
 // beyond a point's truncation are zero) and [point][column] for the
 // ordinate fields, columns grouped by hemisphere and trace octant.
 
+#include <cooperative_groups.h>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,6 +33,7 @@
 
 #include "../../include/shdom_gb300.h"
 #include "shdom_plan.h"
+#include "shdom_tc.cuh"
 
 namespace shdom {
 
@@ -42,75 +47,151 @@ namespace shdom {
   } while (0)
 
 // Device error codes written to Dev::err (first error wins).
-enum { ERR_NONE = 0, ERR_SWEEP_NOFACE = 1, ERR_SWEEP_STEPS = 2, ERR_RAY_STEPS = 3, ERR_RAY_SO = 4, ERR_RAY_BELOW = 5 };
+enum {
+  ERR_NONE = 0, ERR_SWEEP_NOFACE = 1, ERR_SWEEP_STEPS = 2, ERR_RAY_STEPS = 3, ERR_RAY_SO = 4, ERR_RAY_BELOW = 5,
+  ERR_TC_WAIT = 6  // a tensor-core transform gave up waiting on its pipeline
+};
 
 __constant__ int c_face[6][4] = {{0, 2, 4, 6}, {1, 3, 5, 7}, {0, 1, 4, 5}, {2, 3, 6, 7}, {0, 1, 2, 3}, {4, 5, 6, 7}};
 
-// ------------------------------------------------------------------ GEMM
-// C[M x N] = A[M x K] * B[K x N], all row-major FP32, with an epilogue.
-// mode 0: C = max(0, acc) (source to discrete ordinates)
-// mode 1: columns < nlm -> radiance masked by nr[row]; nlm, nlm+1 -> fluxes
-constexpr int GBM = 128, GBN = 64, GBK = 16;
+// ------------------------------------------------------------ transforms
+// Spherical harmonics <-> discrete ordinates, factorized as in SH_TO_DO_UNPOL
+// and DO_TO_SH_UNPOL (src/polarized/shdomsub1.f:2928-3036, :3164-3254): a
+// Legendre contraction over l for each azimuthal mode m (CMU1/CMU2) and an
+// azimuthal Fourier synthesis/analysis per zenith angle (CPHI1/CPHI2; the
+// reference's FFT branch is the same linear map).  One warp per point; for
+// the Legendre step lane t handles mode m = t - mm, for the Fourier step the
+// lanes run over azimuths (synthesis) or modes (analysis).
+struct XfArgs {
+  const float *cmu;      // [nlm][nmu] (CMU1 for sh_to_do, CMU2 for do_to_sh)
+  const float *cphi;     // sh_to_do: [nmu][nm][nphi0max] (CPHI1 transposed); do_to_sh: [nmu][nphi0max][nm]
+  const int *nphi0, *col_of;
+  const float *fluxw;
+  const int *nr;
+  float *fluxes;
+  int npts, nlm, ml, mm, nmu, nang, nphi0max, ncol_down;
+  int ldo;               // row stride of the ordinate arrays (nang rounded up to 4)
+};
 
-__global__ void __launch_bounds__(256) k_gemm(const float *__restrict__ A, const float *__restrict__ B, int M, int N,
-                                              int K, int lda, int ldb, int mode, float *__restrict__ C, int ldc,
-                                              const int *__restrict__ nr, int nlm, float *__restrict__ fluxes) {
-  __shared__ float As[GBK][GBM + 4];
-  __shared__ float Bs[GBK][GBN];
-  const int tid = threadIdx.x;
-  const int m0 = blockIdx.y * GBM, n0 = blockIdx.x * GBN;
-  const int tr = tid / 16, tc = tid % 16;  // 16 x 16 threads, 8 x 4 outputs each
-  float acc[8][4];
-#pragma unroll
-  for (int i = 0; i < 8; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
-  for (int k0 = 0; k0 < K; k0 += GBK) {
-#pragma unroll
-    for (int r = 0; r < 8; ++r) {  // A tile 128 x 16
-      int idx = tid + r * 256;
-      int am = idx / GBK, ak = idx % GBK;
-      int gm = m0 + am, gk = k0 + ak;
-      As[ak][am] = (gm < M && gk < K) ? A[(size_t)gm * lda + gk] : 0.f;
-    }
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {  // B tile 16 x 64
-      int idx = tid + r * 256;
-      int bk = idx / GBN, bn = idx % GBN;
-      int gk = k0 + bk, gn = n0 + bn;
-      Bs[bk][bn] = (gk < K && gn < N) ? B[(size_t)gk * ldb + gn] : 0.f;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < GBK; ++kk) {
-      float a[8], b[4];
-#pragma unroll
-      for (int i = 0; i < 8; ++i) a[i] = As[kk][tr * 8 + i];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tc + 16 * j];
-#pragma unroll
-      for (int i = 0; i < 8; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
-    }
-    __syncthreads();
+__device__ __forceinline__ int jindex(int l, int m, int mm) {
+  return (l <= mm) ? l * (l + 1) + m : (2 * mm + 1) * l - mm * mm + m;
+}
+
+template <int NMU>
+__global__ void __launch_bounds__(256) k_sh_to_do(XfArgs x, const float *__restrict__ S, float *__restrict__ srcdo) {
+  extern __shared__ float sm[];
+  const int nm = 2 * x.mm + 1;
+  float *scmu = sm;                                   // [nlm][NMU+1]
+  float *sw = sm + x.nlm * (NMU + 1) + (threadIdx.x >> 5) * NMU * nm;
+  for (int t = threadIdx.x; t < x.nlm * NMU; t += blockDim.x) {
+    int j = t / NMU, i = t - j * NMU;
+    scmu[j * (NMU + 1) + i] = (i < x.nmu) ? x.cmu[(size_t)j * x.nmu + i] : 0.f;
   }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+  const bool active = lane < nm;
+  const int m = lane - x.mm, ma = m < 0 ? -m : m;
+  const int partner = active ? 2 * x.mm - lane : lane;
+  for (int p = warp; p < x.npts; p += nwarps) {
+    const float *Sp = S + (size_t)p * x.nlm;
+    float U[NMU];
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    int gm = m0 + tr * 8 + i;
-    if (gm >= M) continue;
+    for (int i = 0; i < NMU; ++i) U[i] = 0.f;
+    if (active)
+      for (int l = ma; l <= x.ml; ++l) {
+        const int j = jindex(l, m, x.mm);
+        const float sv = Sp[j];
+        const float *c = scmu + j * (NMU + 1);
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      int gn = n0 + tc + 16 * j;
-      if (gn >= N) continue;
-      float v = acc[i][j];
-      if (mode == 0) {
-        C[(size_t)gm * ldc + gn] = fmaxf(v, 0.f);
-      } else {
-        if (gn < nlm) C[(size_t)gm * ldc + gn] = (gn < nr[gm]) ? v : 0.f;
-        else fluxes[(size_t)gm * 2 + (gn - nlm)] = v;
+        for (int i = 0; i < NMU; ++i) U[i] = fmaf(c[i], sv, U[i]);
+      }
+#pragma unroll
+    for (int i = 0; i < NMU; ++i) {
+      const float up = __shfl_sync(0xffffffffu, U[i], partner);
+      if (active && i < x.nmu) {
+        const int me = max(0, x.nphi0[i] / 2 - 1);
+        float cs = (m == 0) ? U[i] : (m > 0 ? U[i] + up : U[i] - up);
+        sw[i * nm + lane] = (ma <= me) ? cs : 0.f;
       }
     }
+    __syncwarp();
+    for (int i = 0; i < x.nmu; ++i) {
+      const int n0 = x.nphi0[i], me = max(0, n0 / 2 - 1);
+      const float *cs = sw + i * nm + x.mm;
+      for (int k = lane; k < n0; k += 32) {
+        const float *c = x.cphi + ((size_t)i * nm + x.mm) * x.nphi0max + k;
+        float o = 0.f;
+        for (int mm2 = -me; mm2 <= me; ++mm2) o = fmaf(c[mm2 * x.nphi0max], cs[mm2], o);
+        srcdo[(size_t)p * x.ldo + x.col_of[i * x.nphi0max + k]] = fmaxf(o, 0.f);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+template <int NMU>
+__global__ void __launch_bounds__(256) k_do_to_sh(XfArgs x, const float *__restrict__ raddo, float *__restrict__ R) {
+  extern __shared__ float sm[];
+  const int nm = 2 * x.mm + 1;
+  float *scmu = sm;                                               // [nlm][NMU+1]
+  float *sr = sm + x.nlm * (NMU + 1) + (threadIdx.x >> 5) * x.nang;  // this warp's ordinate radiances
+  for (int t = threadIdx.x; t < x.nlm * NMU; t += blockDim.x) {
+    int j = t / NMU, i = t - j * NMU;
+    scmu[j * (NMU + 1) + i] = (i < x.nmu) ? x.cmu[(size_t)j * x.nmu + i] : 0.f;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+  const bool active = lane < nm;
+  const int m = lane - x.mm, ma = m < 0 ? -m : m;
+  const int partner = active ? 2 * x.mm - lane : lane;
+  for (int p = warp; p < x.npts; p += nwarps) {
+    float fd = 0.f, fu = 0.f;
+    for (int c = lane; c < x.nang; c += 32) {
+      const float r = raddo[(size_t)p * x.ldo + c];
+      sr[c] = r;
+      const float w = x.fluxw[c] * r;
+      if (c < x.ncol_down) fd += w; else fu += w;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      fd += __shfl_xor_sync(0xffffffffu, fd, o);
+      fu += __shfl_xor_sync(0xffffffffu, fu, o);
+    }
+    if (lane == 0) { x.fluxes[2 * (size_t)p] = fd; x.fluxes[2 * (size_t)p + 1] = fu; }
+    __syncwarp();
+    float CS[NMU];
+#pragma unroll
+    for (int i = 0; i < NMU; ++i) {
+      CS[i] = 0.f;
+      if (active && i < x.nmu) {
+        const int n0 = x.nphi0[i], me = max(0, n0 / 2 - 1);
+        if (ma <= me) {
+          const float *c = x.cphi + (size_t)i * x.nphi0max * nm + lane;
+          const int *co = x.col_of + i * x.nphi0max;
+          float s = 0.f;
+          for (int k = 0; k < n0; ++k) s = fmaf(c[k * nm], sr[co[k]], s);
+          CS[i] = s;
+        }
+      }
+    }
+    const int nrp = x.nr[p];
+    float *Rp = R + (size_t)p * x.nlm;
+#pragma unroll
+    for (int i = 0; i < NMU; ++i) {
+      const float cp = __shfl_sync(0xffffffffu, CS[i], partner);
+      CS[i] = (m == 0) ? CS[i] : (m > 0 ? CS[i] - cp : cp + CS[i]);  // SUMUV(m)
+    }
+    if (active)
+      for (int l = ma; l <= x.ml; ++l) {
+        const int j = jindex(l, m, x.mm);
+        const float *c = scmu + j * (NMU + 1);
+        float v = 0.f;
+#pragma unroll
+        for (int i = 0; i < NMU; ++i) v = fmaf(c[i], CS[i], v);
+        Rp[j] = (j < nrp) ? v : 0.f;
+      }
+    __syncwarp();
   }
 }
 
@@ -124,8 +205,10 @@ struct SweepArgs {
   float *raddo;
   const float *col_cx, *col_cy, *col_cz;
   const uint32_t *tasks;
+  const uint8_t *regular;
+  const float *geo;
   int *err;
-  int npts, nang, is1d;
+  int npts, nang, ldo, is1d, nz, ny1;
   float transmin;
   int oct_col0[8], oct_ncol[8];
 };
@@ -144,11 +227,60 @@ struct Trace {
   int status;  // 0 ok, ERR_* otherwise
 };
 
+// Trace of a regular point: one interior cell, exit geometry from the
+// per-(layer, ordinate) table, corner indices by arithmetic on the
+// (x, y, z) point numbering of the base grid.
+__device__ __forceinline__ Trace trace_regular(const SweepArgs &a, int b, int pt, int col) {
+  Trace t;
+  const int nz = a.nz, nang = a.nang, ldo = a.ldo;
+  const int iz = pt % nz;
+  const int layer = (b & 4) ? iz - 1 : iz;
+  const float4 *g = reinterpret_cast<const float4 *>(a.geo) + ((size_t)layer * nang + col) * 2;
+  const float4 g0 = g[0], g1 = g[1];
+  const float so = g0.x;
+  t.f[0] = g0.y; t.f[1] = g0.z; t.f[2] = g0.w; t.f[3] = g1.x;
+  const int iface = (int)g1.y;
+  const int ox = (b & 1) ? -nz * a.ny1 : nz * a.ny1, oy = (b & 2) ? -nz : nz, oz = (b & 4) ? -1 : 1;
+  float ext0 = 0.f, srcext0 = 0.f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int d = c_face[iface][k] ^ b;
+    const int q = pt + ((d & 1) ? ox : 0) + ((d & 2) ? oy : 0) + ((d & 4) ? oz : 0);
+    t.q[k] = q;
+    const float e = a.text[q];
+    ext0 += t.f[k] * e;
+    srcext0 += t.f[k] * a.srcdo[(size_t)q * ldo + col] * e;
+  }
+  const float ext1 = a.text[pt];
+  const float srcext1 = ext1 * a.srcdo[(size_t)pt * ldo + col];
+  const float ext = 0.5f * (ext0 + ext1), tau = ext * so;
+  float transcell, abscell, src;
+  if (tau >= 0.5f) { transcell = __expf(-tau); abscell = 1.f - transcell; }
+  else {
+    abscell = tau * (1.f - 0.5f * tau * (1.f - 0.33333333333f * tau * (1.f - 0.25f * tau)));
+    transcell = 1.f - abscell;
+  }
+  if (tau <= 2.f) {
+    src = (ext == 0.f) ? 0.f : (0.5f * (srcext0 + srcext1) + 0.08333333333f * (ext0 * srcext1 - ext1 * srcext0) * so) / ext;
+  } else {
+    float ext0p = ext0, srcext0p = srcext0;
+    if (tau > 4.f) { ext0p = ext1 + (ext0 - ext1) * 4.f / tau; if (ext0 > 0.f) srcext0p = srcext0 * ext0p / ext0; }
+    src = 1.f / (ext0p + ext1) *
+          (srcext0p + srcext1 + (ext0p * srcext1 - ext1 * srcext0p) * 2.f / (ext0p + ext1) * (1.f - 2.f / tau + 2.f * transcell / abscell));
+  }
+  src = fmaxf(src, 0.f);
+  t.radsrc = src * abscell;
+  t.tr = transcell;
+  t.status = ERR_NONE;
+  return t;
+}
+
 __device__ __forceinline__ Trace trace_point(const SweepArgs &a, int b, int pt, int col, bool use_level) {
+  if (a.regular[(size_t)b * a.npts + pt]) return trace_regular(a, b, pt, col);
   Trace t;
   t.radsrc = 0.f; t.tr = 1.f; t.status = ERR_SWEEP_STEPS;
   t.q[0] = t.q[1] = t.q[2] = t.q[3] = pt; t.f[0] = t.f[1] = t.f[2] = t.f[3] = 0.f;
-  const int nang = a.nang, n = a.npts;
+  const int ldo = a.ldo, n = a.npts;
   const float cx = a.col_cx[col], cy = a.col_cy[col], cz = a.col_cz[col];
   const float cxinv = cx != 0.f ? 1.f / cx : 1.0e6f, cyinv = cy != 0.f ? 1.f / cy : 1.0e6f, czinv = 1.f / cz;
   const int bitx = cx < 0.f, bity = cy < 0.f, bitz = cz < 0.f;
@@ -158,7 +290,7 @@ __device__ __forceinline__ Trace trace_point(const SweepArgs &a, int b, int pt, 
   int cell = a.start[(size_t)b * n + pt];
   float xe = a.gridpos[3 * pt], ye = a.gridpos[3 * pt + 1], ze = a.gridpos[3 * pt + 2];
   float ext1 = a.text[pt];
-  float srcext1 = ext1 * a.srcdo[(size_t)pt * nang + col];
+  float srcext1 = ext1 * a.srcdo[(size_t)pt * ldo + col];
   float rad = 0.f, tr = 1.f;
   for (int guard = 0; guard < 65536; ++guard) {
     if (cell < 0) break;
@@ -209,8 +341,8 @@ __device__ __forceinline__ Trace trace_point(const SweepArgs &a, int b, int pt, 
     }
     const float e1 = a.text[i1], e2 = a.text[i2], e3 = a.text[i3], e4 = a.text[i4];
     const float ext0 = f1 * e1 + f2 * e2 + f3 * e3 + f4 * e4;
-    const float srcext0 = f1 * a.srcdo[(size_t)i1 * nang + col] * e1 + f2 * a.srcdo[(size_t)i2 * nang + col] * e2 +
-                          f3 * a.srcdo[(size_t)i3 * nang + col] * e3 + f4 * a.srcdo[(size_t)i4 * nang + col] * e4;
+    const float srcext0 = f1 * a.srcdo[(size_t)i1 * ldo + col] * e1 + f2 * a.srcdo[(size_t)i2 * ldo + col] * e2 +
+                          f3 * a.srcdo[(size_t)i3 * ldo + col] * e3 + f4 * a.srcdo[(size_t)i4 * ldo + col] * e4;
     const float ext = 0.5f * (ext0 + ext1), tau = ext * so;
     float transcell, abscell, src;
     if (tau >= 0.5f) { transcell = __expf(-tau); abscell = 1.f - transcell; }
@@ -254,14 +386,41 @@ __global__ void __launch_bounds__(256) k_sweep(SweepArgs a, int t0, int ntask, i
   uint32_t tk = a.tasks[t0 + task];
   int b = (int)(tk >> 28), pt = (int)(tk & 0x0FFFFFFFu);
   if (slot >= a.oct_ncol[b]) return;
-  const int col = a.oct_col0[b] + slot, nang = a.nang;
+  const int col = a.oct_col0[b] + slot, ldo = a.ldo;
   Trace t = trace_point(a, b, pt, col, true);
   if (t.status != ERR_NONE) atomicCAS(a.err, ERR_NONE, t.status);
   float rad = t.radsrc;
   if (t.tr != 0.f)
-    rad += t.tr * (t.f[0] * a.raddo[(size_t)t.q[0] * nang + col] + t.f[1] * a.raddo[(size_t)t.q[1] * nang + col] +
-                   t.f[2] * a.raddo[(size_t)t.q[2] * nang + col] + t.f[3] * a.raddo[(size_t)t.q[3] * nang + col]);
-  a.raddo[(size_t)pt * nang + col] = rad;
+    rad += t.tr * (t.f[0] * a.raddo[(size_t)t.q[0] * ldo + col] + t.f[1] * a.raddo[(size_t)t.q[1] * ldo + col] +
+                   t.f[2] * a.raddo[(size_t)t.q[2] * ldo + col] + t.f[3] * a.raddo[(size_t)t.q[3] * ldo + col]);
+  a.raddo[(size_t)pt * ldo + col] = rad;
+}
+
+// All wavefront levels of one hemisphere in one cooperative launch: the
+// blocks stride over the tasks of a level, then meet at a grid barrier.
+__global__ void __launch_bounds__(256) k_sweep_levels(SweepArgs a, const int *__restrict__ level_off, int nlev,
+                                                      int omax) {
+  cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (int l = 0; l < nlev; ++l) {
+    const int t0 = level_off[l], nt = level_off[l + 1] - t0;
+    const long long total = (long long)nt * omax;
+    for (long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x; tid < total; tid += stride) {
+      const int task = (int)(tid / omax), slot = (int)(tid - (long long)task * omax);
+      const uint32_t tk = a.tasks[t0 + task];
+      const int b = (int)(tk >> 28), pt = (int)(tk & 0x0FFFFFFFu);
+      if (slot >= a.oct_ncol[b]) continue;
+      const int col = a.oct_col0[b] + slot, ldo = a.ldo;
+      Trace t = trace_point(a, b, pt, col, true);
+      if (t.status != ERR_NONE) atomicCAS(a.err, ERR_NONE, t.status);
+      float rad = t.radsrc;
+      if (t.tr != 0.f)
+        rad += t.tr * (t.f[0] * a.raddo[(size_t)t.q[0] * ldo + col] + t.f[1] * a.raddo[(size_t)t.q[1] * ldo + col] +
+                       t.f[2] * a.raddo[(size_t)t.q[2] * ldo + col] + t.f[3] * a.raddo[(size_t)t.q[3] * ldo + col]);
+      a.raddo[(size_t)pt * ldo + col] = rad;
+    }
+    grid.sync();
+  }
 }
 
 // Sequential-order sweep for grids whose wavefront is too deep (periodic
@@ -275,7 +434,7 @@ constexpr int SEQW = 256;
 __global__ void __launch_bounds__(SEQW) k_sweep_seq(SweepArgs a, const int *order, int col_begin) {
   __shared__ float sval[SEQW];
   __shared__ int sdone[SEQW];
-  const int col = col_begin + blockIdx.x, nang = a.nang, n = a.npts;
+  const int col = col_begin + blockIdx.x, ldo = a.ldo, n = a.npts;
   int b = 0;
   for (int k = 0; k < 8; ++k)
     if (a.oct_ncol[k] > 0 && col >= a.oct_col0[k] && col < a.oct_col0[k] + a.oct_ncol[k]) b = k;
@@ -301,7 +460,7 @@ __global__ void __launch_bounds__(SEQW) k_sweep_seq(SweepArgs a, const int *orde
         if (t.f[k] == 0.f || t.tr == 0.f) { wl[k] = -1; continue; }
         int rq = (a.bnd[q] & hb) ? -1 : rk[q];
         if (rq >= r0 && t.f[k] != 0.f) wl[k] = rq - r0;
-        else { wl[k] = -1; wv += t.tr * t.f[k] * a.raddo[(size_t)q * nang + col]; }
+        else { wl[k] = -1; wv += t.tr * t.f[k] * a.raddo[(size_t)q * ldo + col]; }
       }
     }
     sdone[tid] = pending ? 0 : 1;
@@ -319,7 +478,7 @@ __global__ void __launch_bounds__(SEQW) k_sweep_seq(SweepArgs a, const int *orde
 #pragma unroll
               for (int k = 0; k < 4; ++k) if (wl[k] >= 0) v += t.tr * t.f[k] * sval[wl[k]];
               sval[tid] = v;
-              a.raddo[(size_t)pt * nang + col] = v;
+              a.raddo[(size_t)pt * ldo + col] = v;
               todo = false;
             }
           }
@@ -338,21 +497,21 @@ __global__ void __launch_bounds__(SEQW) k_sweep_seq(SweepArgs a, const int *orde
 // radiance for downward columns; bottom points get the Lambertian surface
 // radiance computed from the downwelling flux (FIXED/VARIABLE_LAMBERTIAN_
 // BOUNDARY, src/polarized/shdomsub1.f:2438-2529).
-__global__ void k_preset_top(const int *topp, int ntop, float *raddo, int nang, int ncol_down, float skyrad) {
+__global__ void k_preset_top(const int *topp, int ntop, float *raddo, int ldo, int ncol_down, float skyrad) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntop * ncol_down) return;
   int k = t / ncol_down, c = t - k * ncol_down;
-  raddo[(size_t)topp[k] * nang + c] = skyrad;
+  raddo[(size_t)topp[k] * ldo + c] = skyrad;
 }
 
 __global__ void k_lambertian(const int *botp, int nbot, const float *botalb, const float *dirflux, const float *fluxw,
-                             float *raddo, int nang, int ncol_down, float *bcrad) {
+                             float *raddo, int nang, int ldo, int ncol_down, float *bcrad) {
   int k = blockIdx.x;
   if (k >= nbot) return;
   int p = botp[k];
   __shared__ float red[256];
   float s = 0.f;
-  for (int c = threadIdx.x; c < ncol_down; c += blockDim.x) s += fluxw[c] * raddo[(size_t)p * nang + c];
+  for (int c = threadIdx.x; c < ncol_down; c += blockDim.x) s += fluxw[c] * raddo[(size_t)p * ldo + c];
   red[threadIdx.x] = s;
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
@@ -362,7 +521,7 @@ __global__ void k_lambertian(const int *botp, int nbot, const float *botalb, con
   const float opi = 0.318309886f;
   float b = opi * botalb[k] * (dirflux[p] + red[0]);
   if (threadIdx.x == 0) bcrad[k] = b;
-  for (int c = ncol_down + threadIdx.x; c < nang; c += blockDim.x) raddo[(size_t)p * nang + c] = b;
+  for (int c = ncol_down + threadIdx.x; c < nang; c += blockDim.x) raddo[(size_t)p * ldo + c] = b;
 }
 
 // ---------------------------------------------------------------- source
@@ -396,6 +555,7 @@ __global__ void __launch_bounds__(256) k_source(SourceArgs a) {
     float *D = a.delsource + (size_t)p * a.nlm;
     const float *R = a.radiance + (size_t)p * a.nlm;
     int jlast = 0;  // 1-based index of the last term above shacc
+    float pdot = 0.f, pold = 0.f, pnew = 0.f, pn = 0.f;  // this point's partial sums
     for (int j0 = 0; j0 < a.nlm; j0 += 32) {
       int j = j0 + lane;
       float jt = 0.f;
@@ -408,12 +568,12 @@ __global__ void __launch_bounds__(256) k_source(SourceArgs a) {
           if (a.accel) {
             if (j < nsmin) {
               float dn = jt - sold, dd = D[j];
-              djdot += (double)dn * dd; djold += (double)dd * dd; djnew += (double)dn * dn; jn += (double)sold * sold;
+              pdot += dn * dd; pold += dd * dd; pnew += dn * dn; pn += sold * sold;
             }
             if (j < nsold) D[j] = jt - sold; else D[j] = 0.f;
           } else if (j < nsold) {
             float dn = jt - sold;
-            djnew += (double)dn * dn; jn += (double)sold * sold;
+            pnew += dn * dn; pn += sold * sold;
           }
         }
       }
@@ -422,6 +582,7 @@ __global__ void __launch_bounds__(256) k_source(SourceArgs a) {
       // stash the new term in the output row; truncated below once jlast is known
       if (j < a.nlm) S[j] = jt;
     }
+    djdot += (double)pdot; djold += (double)pold; djnew += (double)pnew; jn += (double)pn;
     int nsnew;
     if (a.fixsh && !a.first) nsnew = nsold;
     else if (jlast == 0) nsnew = 0;
@@ -832,9 +993,13 @@ struct Handle {
   // geometry
   DBuf<float> gridpos, xgrid, ygrid, zgrid;
   DBuf<int> gridptr, neighptr, cellflags, rank, start, level, order, topp, botp, bot_index, lofj;
-  DBuf<uint8_t> bnd;
+  DBuf<uint8_t> bnd, regular;
+  DBuf<float> geo;
   DBuf<uint32_t> tasks[2];
-  DBuf<float> col_cx, col_cy, col_cz, col_fluxw, amat, bmat, ylmsun;
+  DBuf<int> level_off[2];
+  int coop_blocks = 0;
+  DBuf<float> col_cx, col_cy, col_cz, col_fluxw, cmu1t, cmu2t, cphi1t, cphi2, ylmsun;
+  DBuf<int> nphi0, col_of;
   // medium
   DBuf<float> text, dirflux, coef, tms_w, phasetab, botalb, rad0;
   DBuf<int> tms_ptr, tms_iph;
@@ -843,6 +1008,13 @@ struct Handle {
   DBuf<int> ns, nso, nr, errflag;
   DBuf<double> red;
   DBuf<AccelState> accel;
+  int ldo = 0;  // row stride of srcdo/raddo: nang rounded up to 4 (16-byte rows for TMA)
+  // tensor-core transforms, per direction (0: SH -> DO, 1: DO -> SH)
+  int xf_mode = 0;  // 0: 3xTF32 tensor cores, 1: single TF32 product, 2: CUDA-core factorized
+  bool tc_ok[2] = {false, false};
+  int tc_bn[2] = {0, 0}, tc_ntiles[2] = {0, 0}, tc_kpad[2] = {0, 0};
+  DBuf<float> tc_bh[2], tc_bl[2];
+  CUtensorMap tm_a[2], tm_bh[2], tm_bl[2];
   int omax[2] = {0, 0};
   bool seq[2] = {false, false};  // sequential-order sweep engine per hemisphere
   bool initialized = false;
@@ -851,6 +1023,132 @@ struct Handle {
   float timings[5] = {0, 0, 0, 0, 0};
   long long launches = 0;
 };
+
+// ---------------------------------------------- dense transform matrices
+// The factorized transforms above are linear maps; their matrices are formed
+// here once per plan from the same coefficients (CMU1/CPHI1, CMU2/CPHI2 with
+// the per-zenith azimuthal cut ME = NPHI0/2 - 1), in double precision.
+// T1[c][j]: ordinate column c from harmonic term j (SH_TO_DO_UNPOL,
+// src/polarized/shdomsub1.f:2928-3036).
+static void dense_sh_to_do(const Plan &P, std::vector<double> &T) {
+  const int nlm = P.nlm, nm = 2 * P.mm + 1, np0 = P.nphi0max;
+  T.assign((size_t)P.nang * nlm, 0.0);
+  for (int j = 0; j < nlm; ++j) {
+    const int m = P.mofj[j], ma = std::abs(m);
+    for (int i = 0; i < P.nmu; ++i) {
+      const int n0 = P.nphi0[i], me = std::max(0, n0 / 2 - 1);
+      if (ma > me) continue;
+      const double u = P.cmu1[(size_t)i * nlm + j];
+      for (int k = 0; k < n0; ++k) {
+        const float *cp = &P.cphi1[((size_t)i * np0 + k) * nm + P.mm];
+        double w = (m == 0) ? cp[0] : (m > 0 ? (double)cp[m] - cp[-m] : (double)cp[m] + cp[-m]);
+        T[(size_t)P.col_of[i * np0 + k] * nlm + j] += u * w;
+      }
+    }
+  }
+}
+
+// T2[j][c]: harmonic term j from ordinate column c (DO_TO_SH_UNPOL,
+// src/polarized/shdomsub1.f:3164-3254); rows nlm and nlm+1 are the downward
+// and upward hemispheric flux weights.
+static void dense_do_to_sh(const Plan &P, std::vector<double> &T) {
+  const int nlm = P.nlm, nm = 2 * P.mm + 1, np0 = P.nphi0max, nang = P.nang;
+  T.assign((size_t)(nlm + 2) * nang, 0.0);
+  for (int j = 0; j < nlm; ++j) {
+    const int m = P.mofj[j], ma = std::abs(m);
+    for (int i = 0; i < P.nmu; ++i) {
+      const int n0 = P.nphi0[i], me = std::max(0, n0 / 2 - 1);
+      if (ma > me) continue;
+      const double u = P.cmu2[(size_t)i * nlm + j];
+      for (int k = 0; k < n0; ++k) {
+        const float *cp = &P.cphi2[((size_t)i * np0 + k) * nm + P.mm];
+        double w = (m == 0) ? cp[0] : (m > 0 ? (double)cp[m] - cp[-m] : (double)cp[-m] + cp[m]);
+        T[(size_t)j * nang + P.col_of[i * np0 + k]] += u * w;
+      }
+    }
+  }
+  for (int c = 0; c < nang; ++c) T[(size_t)(c < P.ncol_down ? nlm : nlm + 1) * nang + c] = P.col_fluxw[c];
+}
+
+// Round to TF32 (10 explicit mantissa bits), nearest with ties away from
+// zero, as cvt.rna.tf32.f32 does on the device.
+static float tf32_rna(float x) {
+  uint32_t b;
+  std::memcpy(&b, &x, 4);
+  if ((b & 0x7f800000u) != 0x7f800000u) b = (b + 0x1000u) & 0xffffe000u;
+  float y;
+  std::memcpy(&y, &b, 4);
+  return y;
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    CK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !p) throw std::runtime_error("cuTensorMapEncodeTiled not available");
+    fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+// 2-D fp32 tensor map: rows x inner elements, row stride ld elements, box of
+// box_rows x 32 elements (one 128-byte swizzle row), zero fill outside.
+static void make_map(CUtensorMap *m, const float *base, uint64_t inner, uint64_t rows, uint64_t ld, uint32_t box_rows) {
+  cuuint64_t dims[2] = {inner, rows};
+  cuuint64_t strides[1] = {ld * sizeof(float)};
+  cuuint32_t box[2] = {(cuuint32_t)tc::BK, box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = encode_tiled()(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)base, dims, strides, box, es,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+}
+
+// Forms the dense matrices, splits them into TF32 high and low parts
+// ([Npad][Kpad], zero padded) and encodes the tensor maps.  A direction whose
+// operand rows are not 16-byte multiples, or too small for one tile, keeps
+// the factorized CUDA-core transform.
+static void setup_tc(Handle &H) {
+  Plan &P = H.P;
+  int dev = 0, major = 0, minor = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+  CK(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+  if (major != 10) return;
+  for (int dir = 0; dir < 2; ++dir) {
+    const int K = dir == 0 ? P.nlm : P.nang, N = dir == 0 ? P.nang : P.nlm + 2;
+    const int lda = dir == 0 ? P.nlm : H.ldo;
+    if (lda % 4 != 0 || K < tc::BK || P.npts < tc::BM) continue;
+    const int ntiles = (N + 255) / 256;
+    const int bn = ((N + ntiles - 1) / ntiles + 15) / 16 * 16;
+    const int npad = ntiles * bn, kpad = (K + tc::BK - 1) / tc::BK * tc::BK;
+    std::vector<double> T;
+    if (dir == 0) dense_sh_to_do(P, T); else dense_do_to_sh(P, T);
+    std::vector<float> bh((size_t)npad * kpad, 0.f), bl((size_t)npad * kpad, 0.f);
+    for (int n = 0; n < N; ++n)
+      for (int k = 0; k < K; ++k) {
+        const double t = T[(size_t)n * K + k];
+        const float h = tf32_rna((float)t);
+        bh[(size_t)n * kpad + k] = h;
+        bl[(size_t)n * kpad + k] = tf32_rna((float)(t - (double)h));
+      }
+    H.tc_bh[dir].upload(bh);
+    H.tc_bl[dir].upload(bl);
+    const float *a = dir == 0 ? H.source.p : H.raddo.p;
+    make_map(&H.tm_a[dir], a, (uint64_t)K, (uint64_t)P.npts, (uint64_t)lda, tc::BM);
+    make_map(&H.tm_bh[dir], H.tc_bh[dir].p, (uint64_t)kpad, (uint64_t)npad, (uint64_t)kpad, (uint32_t)bn);
+    make_map(&H.tm_bl[dir], H.tc_bl[dir].p, (uint64_t)kpad, (uint64_t)npad, (uint64_t)kpad, (uint32_t)bn);
+    H.tc_bn[dir] = bn; H.tc_ntiles[dir] = ntiles; H.tc_kpad[dir] = kpad;
+    CK(cudaFuncSetAttribute(tc::k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::smem_bytes(256)));
+    H.tc_ok[dir] = true;
+  }
+}
 
 static void upload_plan(Handle &H) {
   Plan &P = H.P;
@@ -870,34 +1168,34 @@ static void upload_plan(Handle &H) {
     int nlev = (int)P.level_off[h].size() - 1;
     H.seq[h] = nlev > 4 * (P.nx1 + P.ny1 + P.nz) + 64;
   }
+  H.regular.upload(P.regular); H.geo.upload(P.geo);
   H.bnd.upload(P.bnd); H.topp.upload(P.topp); H.botp.upload(P.botp); H.lofj.upload(P.lofj);
   std::vector<int> bi(P.npts, -1);
   for (size_t k = 0; k < P.botp.size(); ++k) bi[P.botp[k]] = (int)k;
   H.bot_index.upload(bi);
-  for (int h = 0; h < 2; ++h) H.tasks[h].upload(P.tasks[h]);
+  for (int h = 0; h < 2; ++h) { H.tasks[h].upload(P.tasks[h]); H.level_off[h].upload(P.level_off[h]); }
+  {
+    int dev = 0, nsm = 0, per = 0, coop = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep_levels, 256, 0));
+    H.coop_blocks = coop ? nsm * per : 0;
+  }
   H.col_cx.upload(P.col_cx); H.col_cy.upload(P.col_cy); H.col_cz.upload(P.col_cz); H.col_fluxw.upload(P.col_fluxw);
   H.ylmsun.upload(P.ylmsun);
-  // dense masked transform matrices in column order
-  const int nlm = P.nlm, nang = P.nang, mm = P.mm, nm = 2 * mm + 1;
-  std::vector<float> A((size_t)nlm * nang, 0.f), B((size_t)nang * (nlm + 2), 0.f);
-  for (int c = 0; c < nang; ++c) {
-    int i = P.col_imu[c], k = P.col_iphi[c];
-    int me = std::max(0, P.nphi0[i] / 2 - 1);
-    const float *c1 = &P.cphi1[((size_t)i * P.nphi0max + k) * nm + mm];
-    const float *c2 = &P.cphi2[((size_t)i * P.nphi0max + k) * nm + mm];
-    for (int j = 0; j < nlm; ++j) {
-      int m = P.mofj[j], ma = std::abs(m);
-      if (ma > me) continue;
-      float fa, fb;
-      if (m == 0) { fa = 1.f; fb = c2[0]; }
-      else if (m > 0) { fa = c1[ma] - c1[-ma]; fb = c2[ma] - c2[-ma]; }
-      else { fa = c1[ma] + c1[-ma]; fb = c2[ma] + c2[-ma]; }
-      A[(size_t)j * nang + c] = P.cmu1[(size_t)i * nlm + j] * fa;
-      B[(size_t)c * (nlm + 2) + j] = P.cmu2[(size_t)i * nlm + j] * fb;
-    }
-    B[(size_t)c * (nlm + 2) + nlm + (c < P.ncol_down ? 0 : 1)] = P.col_fluxw[c];
+  // transform tables: CMU1/CMU2 as [j][mu], CPHI1 as [mu][m][phi], CPHI2 as [mu][phi][m]
+  {
+    const int nlm = P.nlm, nmu = P.nmu, nm = 2 * P.mm + 1, np0 = P.nphi0max;
+    std::vector<float> c1t((size_t)nlm * nmu), c2t((size_t)nlm * nmu), p1t((size_t)nmu * nm * np0, 0.f);
+    for (int i = 0; i < nmu; ++i)
+      for (int j = 0; j < nlm; ++j) { c1t[(size_t)j * nmu + i] = P.cmu1[(size_t)i * nlm + j]; c2t[(size_t)j * nmu + i] = P.cmu2[(size_t)i * nlm + j]; }
+    for (int i = 0; i < nmu; ++i)
+      for (int k = 0; k < np0; ++k)
+        for (int m = 0; m < nm; ++m) p1t[((size_t)i * nm + m) * np0 + k] = P.cphi1[((size_t)i * np0 + k) * nm + m];
+    H.cmu1t.upload(c1t); H.cmu2t.upload(c2t); H.cphi1t.upload(p1t); H.cphi2.upload(P.cphi2);
+    H.nphi0.upload(P.nphi0); H.col_of.upload(P.col_of);
   }
-  H.amat.upload(A); H.bmat.upload(B);
   H.text.upload(P.total_ext); H.dirflux.upload(P.dirflux); H.coef.upload(P.coef);
   H.tms_ptr.upload(P.tms_ptr); H.tms_iph.upload(P.tms_iph); H.tms_w.upload(P.tms_w);
   H.phasetab.upload(P.phasetab); H.botalb.upload(P.botalb); H.rad0.upload(P.rad0);
@@ -906,12 +1204,15 @@ static void upload_plan(Handle &H) {
     for (int b = 0; b < 8; ++b) if (((b >> 2) & 1) == h) m = std::max(m, P.oct_ncol[b]);
     H.omax[h] = m;
   }
-  const size_t nf = (size_t)P.npts * nlm, nd = (size_t)P.npts * nang;
+  H.ldo = (P.nang + 3) & ~3;
+  const size_t nf = (size_t)P.npts * P.nlm, nd = (size_t)P.npts * H.ldo;
   H.source.alloc(nf); H.delsource.alloc(nf); H.radiance.alloc(nf);
   H.srcdo.alloc(nd); H.raddo.alloc(nd);
+  H.srcdo.zero(); H.raddo.zero();
   H.fluxes.alloc((size_t)P.npts * 2); H.bcrad.alloc(std::max<size_t>(1, P.botp.size()));
   H.ns.alloc(P.npts); H.nso.alloc(P.npts); H.nr.alloc(P.npts); H.errflag.alloc(1);
   H.red.alloc(4); H.accel.alloc(1);
+  setup_tc(H);
 }
 
 static void launch_source(Handle &H, int first, int fixsh) {
@@ -929,12 +1230,52 @@ static void launch_source(Handle &H, int first, int fixsh) {
   CK(cudaGetLastError());
 }
 
-static void gemm(Handle &H, const float *A, const float *B, int M, int N, int K, int lda, int ldb, int mode, float *C,
-                 int ldc) {
-  dim3 grid((N + GBN - 1) / GBN, (M + GBM - 1) / GBM);
-  k_gemm<<<grid, 256, 0, H.stream>>>(A, B, M, N, K, lda, ldb, mode, C, ldc, H.nr.p, H.P.nlm, H.fluxes.p);
-  H.launches += 1;
+template <int NMU>
+static void transforms_launch(Handle &H, int dir) {
+  Plan &P = H.P;
+  XfArgs x;
+  x.cmu = dir == 0 ? H.cmu1t.p : H.cmu2t.p;
+  x.cphi = dir == 0 ? H.cphi1t.p : H.cphi2.p;
+  x.nphi0 = H.nphi0.p; x.col_of = H.col_of.p; x.fluxw = H.col_fluxw.p; x.nr = H.nr.p; x.fluxes = H.fluxes.p;
+  x.npts = P.npts; x.nlm = P.nlm; x.ml = P.ml; x.mm = P.mm; x.nmu = P.nmu; x.nang = P.nang; x.nphi0max = P.nphi0max;
+  x.ncol_down = P.ncol_down; x.ldo = H.ldo;
+  const int nm = 2 * P.mm + 1;
+  size_t smem = (size_t)P.nlm * (NMU + 1) * sizeof(float) + 8 * sizeof(float) * (dir == 0 ? (size_t)NMU * nm : (size_t)P.nang);
+  int blocks = std::min((P.npts + 7) / 8, 152 * 8);
+  if (dir == 0) {
+    CK(cudaFuncSetAttribute(k_sh_to_do<NMU>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_sh_to_do<NMU><<<blocks, 256, smem, H.stream>>>(x, H.source.p, H.srcdo.p);
+  } else {
+    CK(cudaFuncSetAttribute(k_do_to_sh<NMU>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_do_to_sh<NMU><<<blocks, 256, smem, H.stream>>>(x, H.raddo.p, H.radiance.p);
+  }
   CK(cudaGetLastError());
+  H.launches += 1;
+}
+
+// dir 0: SOURCE -> SRCDO (with the non-negativity clamp); dir 1: RADDO ->
+// RADIANCE (masked to the radiance truncation) and the hemispheric fluxes.
+static void transform(Handle &H, int dir) {
+  if (H.xf_mode != 2 && H.tc_ok[dir]) {
+    Plan &P = H.P;
+    tc::Epilogue g{};
+    g.M = P.npts; g.err = H.errflag.p; g.split = H.xf_mode == 0 ? 1 : 0;
+    if (dir == 0) {
+      g.N = P.nang; g.mode = 0; g.C = H.srcdo.p; g.ldc = H.ldo;
+    } else {
+      g.N = P.nlm + 2; g.mode = 1; g.R = H.radiance.p; g.nlm = P.nlm; g.nr = H.nr.p; g.fluxes = H.fluxes.p;
+    }
+    dim3 grid((P.npts + tc::BM - 1) / tc::BM, H.tc_ntiles[dir]);
+    tc::k_tc_gemm<<<grid, 128, tc::smem_bytes(H.tc_bn[dir]), H.stream>>>(H.tm_a[dir], H.tm_bh[dir], H.tm_bl[dir],
+                                                                         H.tc_kpad[dir], H.tc_bn[dir], g);
+    CK(cudaGetLastError());
+    H.launches += 1;
+    return;
+  }
+  const int nmu = H.P.nmu;
+  if (nmu <= 8) transforms_launch<8>(H, dir);
+  else if (nmu <= 16) transforms_launch<16>(H, dir);
+  else transforms_launch<32>(H, dir);
 }
 
 static void sweep_hemisphere(Handle &H, int hemi) {
@@ -943,7 +1284,8 @@ static void sweep_hemisphere(Handle &H, int hemi) {
   a.gridpos = H.gridpos.p; a.gridptr = H.gridptr.p; a.neighptr = H.neighptr.p; a.cellflags = H.cellflags.p;
   a.bnd = H.bnd.p; a.rank = H.rank.p; a.start = H.start.p; a.level = H.level.p; a.text = H.text.p;
   a.srcdo = H.srcdo.p; a.raddo = H.raddo.p; a.col_cx = H.col_cx.p; a.col_cy = H.col_cy.p; a.col_cz = H.col_cz.p;
-  a.tasks = H.tasks[hemi].p; a.err = H.errflag.p; a.npts = P.npts; a.nang = P.nang; a.is1d = P.is1d;
+  a.tasks = H.tasks[hemi].p; a.err = H.errflag.p; a.npts = P.npts; a.nang = P.nang; a.ldo = H.ldo; a.is1d = P.is1d;
+  a.regular = H.regular.p; a.geo = H.geo.p; a.nz = P.nz; a.ny1 = P.ny1;
   a.transmin = P.prob.transmin;
   for (int b = 0; b < 8; ++b) { a.oct_col0[b] = P.oct_col0[b]; a.oct_ncol[b] = P.oct_ncol[b]; }
   if (H.seq[hemi]) {
@@ -954,6 +1296,15 @@ static void sweep_hemisphere(Handle &H, int hemi) {
   }
   const std::vector<int> &off = P.level_off[hemi];
   const int omax = std::max(1, H.omax[hemi]);
+  if (H.coop_blocks > 0 && off.size() > 1) {
+    int nlev = (int)off.size() - 1;
+    const int *lo = H.level_off[hemi].p;
+    int om = omax;
+    void *args[] = {&a, (void *)&lo, &nlev, &om};
+    CK(cudaLaunchCooperativeKernel((const void *)k_sweep_levels, dim3(H.coop_blocks), dim3(256), args, 0, H.stream));
+    H.launches += 1;
+    return;
+  }
   for (size_t l = 0; l + 1 < off.size(); ++l) {
     int t0 = off[l], nt = off[l + 1] - off[l];
     if (nt <= 0) continue;
@@ -974,6 +1325,7 @@ static int check_device_error(Handle &H) {
   if (e == ERR_SWEEP_STEPS) m = "BACK_INT_GRID: trace exceeded the step limit";
   if (e == ERR_RAY_SO) m = "INTEGRATE_1RAY: SO<0";
   if (e == ERR_RAY_BELOW) m = "RENDER: Level below domain";
+  if (e == ERR_TC_WAIT) m = "tensor-core transform: pipeline wait expired";
   H.err = m;
   CK(cudaMemset(H.errflag.p, 0, sizeof(int)));
   return 1;
@@ -1062,23 +1414,23 @@ int shdom_solution_iterations(shdom_handle *hh, int maxiter, int *iters, float *
     while (H.iters < maxiter && H.solcrit > P.prob.solacc) {
       ++H.iters;
       CK(cudaEventRecord(ev[0], H.stream));
-      shdom::gemm(H, H.source.p, H.amat.p, P.npts, nang, nlm, nlm, nang, 0, H.srcdo.p, nang);
+      shdom::transform(H, 0);
       CK(cudaEventRecord(ev[1], H.stream));
       int ntop = (int)P.topp.size(), nbot = (int)P.botp.size();
       if (ntop && P.ncol_down) {
         int t = ntop * P.ncol_down;
-        shdom::k_preset_top<<<(t + 255) / 256, 256, 0, H.stream>>>(H.topp.p, ntop, H.raddo.p, nang, P.ncol_down, P.prob.skyrad);
+        shdom::k_preset_top<<<(t + 255) / 256, 256, 0, H.stream>>>(H.topp.p, ntop, H.raddo.p, H.ldo, P.ncol_down, P.prob.skyrad);
         H.launches += 1;
       }
       shdom::sweep_hemisphere(H, 0);
       if (nbot) {
         shdom::k_lambertian<<<nbot, 256, 0, H.stream>>>(H.botp.p, nbot, H.botalb.p, H.dirflux.p, H.col_fluxw.p, H.raddo.p,
-                                                         nang, P.ncol_down, H.bcrad.p);
+                                                         nang, H.ldo, P.ncol_down, H.bcrad.p);
         H.launches += 1;
       }
       shdom::sweep_hemisphere(H, 1);
       CK(cudaEventRecord(ev[2], H.stream));
-      shdom::gemm(H, H.raddo.p, H.bmat.p, P.npts, nlm + 2, nang, nang, nlm + 2, 1, H.radiance.p, nlm);
+      shdom::transform(H, 1);
       CK(cudaEventRecord(ev[3], H.stream));
       if (H.solcrit < 0.001f || H.iters > P.prob.iterfixsh) fixsh = true;
       shdom::launch_source(H, 0, fixsh ? 1 : 0);
@@ -1196,6 +1548,13 @@ int shdom_export_state(shdom_handle *hh, float *source, int *ns, float *radiance
   } catch (const std::exception &e) {
     return fail(hh, e.what());
   }
+  return 0;
+}
+
+int shdom_set_transform_mode(shdom_handle *hh, int mode) {
+  if (!hh) return fail(nullptr, "null handle");
+  if (mode < 0 || mode > 2) return fail(hh, "shdom_set_transform_mode: mode must be 0, 1 or 2");
+  hh->h.xf_mode = mode;
   return 0;
 }
 

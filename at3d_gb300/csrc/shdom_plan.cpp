@@ -776,6 +776,7 @@ bool build_schedule(const shdom_problem &p, Plan &P) {
   P.rank.assign((size_t)8 * P.npts, -1);
   P.startcell.assign((size_t)8 * P.npts, -1);
   P.level.assign((size_t)8 * P.npts, 0);
+  P.regular.assign((size_t)8 * P.npts, 0);
   std::vector<int> octs = P.is1d ? std::vector<int>{1, 5} : std::vector<int>{1, 2, 3, 4, 5, 6, 7, 8};
   const double transmin = p.transmin;
   bool ok = true;
@@ -807,6 +808,7 @@ bool build_schedule(const shdom_problem &p, Plan &P) {
             else lvl = std::max(lvl, lv[q]);
           }
         }
+        if (fast && P.cellflags[cell] == 0) P.regular[(size_t)b * n + pt] = 1;
         if (!fast) {
           lvl = 0;
           for (int c = c0; c < c0 + nc; ++c) {
@@ -859,6 +861,45 @@ bool build_schedule(const shdom_problem &p, Plan &P) {
   return true;
 }
 
+// Exit geometry of a trace that starts at corner b of a full interior cell
+// (dx, dy, dz) and leaves through the far side, computed with the same
+// single-precision steps as the device trace.
+void build_geo(Plan &P) {
+  const int nl = P.nz - 1, nang = P.nang;
+  P.geo.assign((size_t)std::max(nl, 1) * nang * 8, 0.f);
+  if (P.is1d || P.nx1 < 2 || P.ny1 < 2) return;
+  const float dx = P.xgrid[1] - P.xgrid[0], dy = P.ygrid[1] - P.ygrid[0];
+  for (int L = 0; L < nl; ++L) {
+    const float dz = P.zgrid[L + 1] - P.zgrid[L];
+    for (int c = 0; c < nang; ++c) {
+      const float cx = P.col_cx[c], cy = P.col_cy[c], cz = P.col_cz[c];
+      const int b = P.col_oct[c] - 1;
+      const float cxinv = cx != 0.f ? 1.f / cx : 1.0e6f, cyinv = cy != 0.f ? 1.f / cy : 1.0e6f, czinv = 1.f / cz;
+      const int bitx = cx < 0.f, bity = cy < 0.f, bitz = cz < 0.f;
+      auto pos = [&](int k, float &x, float &y, float &z) { x = (k & 1) * dx; y = ((k >> 1) & 1) * dy; z = ((k >> 2) & 1) * dz; };
+      float xe, ye, ze, xo, yo, zo;
+      pos(b, xe, ye, ze);
+      pos(7 - b, xo, yo, zo);
+      float sox = (xo - xe) * cxinv, soy = (yo - ye) * cyinv, soz = (zo - ze) * czinv;
+      float so = std::min(sox, std::min(soy, soz));
+      xe += so * cx; ye += so * cy; ze += so * cz;
+      int iface, jface;
+      if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; }
+      else if (soy <= soz) { iface = 3 - bity; jface = 1; }
+      else { iface = 5 - bitz; jface = 2; }
+      float x1, y1, z1, x2, y2, z2, x3, y3, z3;
+      pos(kFace[iface][0], x1, y1, z1); pos(kFace[iface][1], x2, y2, z2); pos(kFace[iface][2], x3, y3, z3);
+      float u, v;
+      if (jface == 0) { u = (ze - z1) / (z3 - z1); v = (ye - y1) / (y2 - y1); }
+      else if (jface == 1) { u = (ze - z1) / (z3 - z1); v = (xe - x1) / (x2 - x1); }
+      else { u = (ye - y1) / (y3 - y1); v = (xe - x1) / (x2 - x1); }
+      float *g = &P.geo[((size_t)L * nang + c) * 8];
+      g[0] = so; g[1] = (1.f - u) * (1.f - v); g[2] = (1.f - u) * v; g[3] = u * (1.f - v); g[4] = u * v;
+      g[5] = (float)iface;
+    }
+  }
+}
+
 }  // namespace
 
 bool build_plan(const shdom_problem &p, Plan &P) {
@@ -885,6 +926,7 @@ bool build_plan(const shdom_problem &p, Plan &P) {
     }
   }
   if (!build_schedule(p, P)) return false;
+  build_geo(P);
   return true;
 }
 

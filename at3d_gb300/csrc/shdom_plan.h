@@ -31,6 +31,11 @@ struct Plan {
   std::vector<int> rank;           // [8][npts], -1 when the octant is unused
   std::vector<int> startcell;      // [8][npts]
   std::vector<int> level;          // [8][npts] wavefront level (0 for boundary points)
+  // regular[b][p] = 1 when point p's trace for trace octant b crosses one
+  // full interior cell whose seven other corners all precede p; such traces
+  // depend only on the ordinate and the z layer, tabulated in geo.
+  std::vector<uint8_t> regular;    // [8][npts]
+  std::vector<float> geo;          // [nz-1][nang][8]: so, f1..f4, face, 0, 0
   // ---- discrete ordinates
   int nmu = 0, nphi = 0, ml = 0, mm = 0, nlm = 0, nleg = 0, nang = 0, nphi0max = 0;
   std::vector<int> nphi0, lofj, mofj;

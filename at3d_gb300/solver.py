@@ -151,6 +151,16 @@ class RTE:
         return {"flux_down": st["fluxes"][:, 0].reshape(shp), "flux_up": st["fluxes"][:, 1].reshape(shp),
                 "flux_direct": st["dirflux"].reshape(shp)}
 
+    TRANSFORM_MODES = {"tf32x3": 0, "tf32": 1, "fp32": 2}
+
+    def set_transform_mode(self, mode: str):
+        """Arithmetic of the SH <-> DO transforms: 'tf32x3' (tensor cores,
+        FP32-level accuracy; default), 'tf32' (tensor cores, one TF32
+        product) or 'fp32' (CUDA-core factorized transforms)."""
+        if mode not in self.TRANSFORM_MODES:
+            raise ValueError(f"transform mode must be one of {sorted(self.TRANSFORM_MODES)}")
+        _check(self._h, _lib.lib().shdom_set_transform_mode(self._h, self.TRANSFORM_MODES[mode]))
+
     def timings(self) -> np.ndarray:
         t = np.zeros(5, np.float32)
         _check(self._h, _lib.lib().shdom_last_timings(self._h, _fp(t)))

@@ -92,6 +92,17 @@ int shdom_get_sizes(shdom_handle *h, shdom_sizes *out);
  * ordinate->harmonic transform, [3] source + acceleration, [4] total. */
 int shdom_last_timings(shdom_handle *h, float *ms5);
 
+/* Arithmetic of the two spherical-harmonic <-> discrete-ordinate transforms
+ * of each iteration (SH_TO_DO / DO_TO_SH, src/polarized/shdomsub1.f:2928-3254,
+ * which the reference runs in FP32 on the CPU):
+ *   0 (default) tensor cores, TF32 operands split into high and low parts,
+ *     three products accumulated in FP32 (FP32-level accuracy);
+ *   1 tensor cores, one TF32 product (about 1e-3 relative; reduced precision);
+ *   2 CUDA-core FP32 factorized transforms.
+ * Problems whose operand rows are not multiples of 16 bytes use 2 in every
+ * mode.  No reference counterpart: the reference has a single FP32 path. */
+int shdom_set_transform_mode(shdom_handle *h, int mode);
+
 /* Message of the last non-zero return on this handle (CHARACTER*600 errmsg
  * of the reference); a static message when h is NULL. */
 const char *shdom_last_error(shdom_handle *h);

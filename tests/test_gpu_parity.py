@@ -100,3 +100,20 @@ def test_cloud_field_nmu16_open(rte_cls):
     assert abs(it_g - it_o) <= 1
     rays = orthographic_views(pb, 12, 12)
     assert relrms(r.render(*rays), o.render(*rays, nthreads=8)) < 1e-4
+
+
+@pytest.mark.parametrize("mode,tol", [("tf32x3", 1e-4), ("fp32", 1e-4), ("tf32", 5e-3)])
+def test_transform_modes(rte_cls, mode, tol):
+    """Each transform arithmetic against the oracle after 3 iterations; the
+    single-product TF32 mode is the reduced-precision variant (about 1e-3)."""
+    from at3d_gb300.scenes import cloud_field
+    pb = cloud_field(seed=11, wavelength_index=1, nx=18, ny=18, nz=12, nleg=64)
+    r = rte_cls.from_problem(pb)
+    r.set_transform_mode(mode)
+    r.solve(3, verbose=False)
+    o = Oracle(pb, fp64=False)
+    o.solve(3)
+    a, b = r.export_state(), o.export()
+    assert relrms(a["source"], b["source"]) < tol
+    assert relrms(a["radiance"], b["radiance"]) < tol
+    assert relrms(a["fluxes"], b["fluxes"]) < tol
