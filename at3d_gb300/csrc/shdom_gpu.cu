@@ -200,11 +200,11 @@ struct SweepArgs {
   const float *gridpos;
   const int *gridptr, *neighptr, *cellflags;
   const uint8_t *bnd;
-  const int *rank, *start, *level;
+  const int *rank, *start, *level;  // level: [8 octants][4 face classes][npts]
   const float *text, *srcdo;
   float *raddo;
   const float *col_cx, *col_cy, *col_cz;
-  const uint32_t *tasks;
+  const uint32_t *tasks;          // point indices of the level schedule
   const uint8_t *regular;
   const float *geo;
   int *err;
@@ -227,34 +227,43 @@ struct Trace {
   int status;  // 0 ok, ERR_* otherwise
 };
 
-// Trace of a regular point: one interior cell, exit geometry from the
-// per-(layer, ordinate) table, corner indices by arithmetic on the
-// (x, y, z) point numbering of the base grid.
-__device__ __forceinline__ Trace trace_regular(const SweepArgs &a, int b, int pt, int col) {
-  Trace t;
-  const int nz = a.nz, nang = a.nang, ldo = a.ldo;
-  const int iz = pt % nz;
+// Regular-point traces: one interior cell, exit geometry (so, u, v, face)
+// from the per-(layer, ordinate) table, corner indices by arithmetic on the
+// (x, y, z) point numbering of the base grid.  Split in a load step (all
+// memory reads, no use of their values) and a combine step so that a thread
+// can keep the reads of several traces in flight.
+struct RegLoad {
+  float4 g;
+  float e1, s1, e[4], s[4], r[4];
+  int pt, col;
+};
+
+__device__ __forceinline__ void reg_load(const SweepArgs &a, int b, int pt, int col, RegLoad &x, bool upstream) {
+  const int ldo = a.ldo;
+  const int iz = pt % a.nz;
   const int layer = (b & 4) ? iz - 1 : iz;
-  const float4 *g = reinterpret_cast<const float4 *>(a.geo) + ((size_t)layer * nang + col) * 2;
-  const float4 g0 = g[0], g1 = g[1];
-  const float so = g0.x;
-  t.f[0] = g0.y; t.f[1] = g0.z; t.f[2] = g0.w; t.f[3] = g1.x;
-  const int iface = (int)g1.y;
-  const int ox = (b & 1) ? -nz * a.ny1 : nz * a.ny1, oy = (b & 2) ? -nz : nz, oz = (b & 4) ? -1 : 1;
-  float ext0 = 0.f, srcext0 = 0.f;
+  x.pt = pt; x.col = col;
+  x.g = __ldg(reinterpret_cast<const float4 *>(a.geo) + (size_t)layer * a.nang + col);
+  const int iface = (int)x.g.w;
+  const int ox = (b & 1) ? -a.nz * a.ny1 : a.nz * a.ny1, oy = (b & 2) ? -a.nz : a.nz, oz = (b & 4) ? -1 : 1;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int d = c_face[iface][k] ^ b;
     const int q = pt + ((d & 1) ? ox : 0) + ((d & 2) ? oy : 0) + ((d & 4) ? oz : 0);
-    t.q[k] = q;
-    const float e = a.text[q];
-    ext0 += t.f[k] * e;
-    srcext0 += t.f[k] * a.srcdo[(size_t)q * ldo + col] * e;
+    x.e[k] = __ldg(a.text + q);
+    x.s[k] = __ldg(a.srcdo + (size_t)q * ldo + col);
+    x.r[k] = upstream ? a.raddo[(size_t)q * ldo + col] : 0.f;
   }
-  const float ext1 = a.text[pt];
-  const float srcext1 = ext1 * a.srcdo[(size_t)pt * ldo + col];
+  x.e1 = __ldg(a.text + pt);
+  x.s1 = __ldg(a.srcdo + (size_t)pt * ldo + col);
+}
+
+// Source integral over one cell (the reference's linear-in-tau source
+// approximation, with the large-tau limiting form).
+__device__ __forceinline__ void cell_source(float ext0, float srcext0, float ext1, float srcext1, float so,
+                                            float &radsrc, float &transcell) {
   const float ext = 0.5f * (ext0 + ext1), tau = ext * so;
-  float transcell, abscell, src;
+  float abscell, src;
   if (tau >= 0.5f) { transcell = __expf(-tau); abscell = 1.f - transcell; }
   else {
     abscell = tau * (1.f - 0.5f * tau * (1.f - 0.33333333333f * tau * (1.f - 0.25f * tau)));
@@ -269,14 +278,49 @@ __device__ __forceinline__ Trace trace_regular(const SweepArgs &a, int b, int pt
           (srcext0p + srcext1 + (ext0p * srcext1 - ext1 * srcext0p) * 2.f / (ext0p + ext1) * (1.f - 2.f / tau + 2.f * transcell / abscell));
   }
   src = fmaxf(src, 0.f);
-  t.radsrc = src * abscell;
-  t.tr = transcell;
+  radsrc = src * abscell;
+}
+
+__device__ __forceinline__ Trace reg_trace(const RegLoad &x, int b, int pt_unused) {
+  Trace t;
+  const float u = x.g.y, v = x.g.z;
+  t.f[0] = (1.f - u) * (1.f - v); t.f[1] = (1.f - u) * v; t.f[2] = u * (1.f - v); t.f[3] = u * v;
+  float ext0 = 0.f, srcext0 = 0.f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    ext0 += t.f[k] * x.e[k];
+    srcext0 += t.f[k] * x.s[k] * x.e[k];
+  }
+  cell_source(ext0, srcext0, x.e1, x.e1 * x.s1, x.g.x, t.radsrc, t.tr);
   t.status = ERR_NONE;
   return t;
 }
 
-__device__ __forceinline__ Trace trace_point(const SweepArgs &a, int b, int pt, int col, bool use_level) {
-  if (a.regular[(size_t)b * a.npts + pt]) return trace_regular(a, b, pt, col);
+__device__ __forceinline__ Trace trace_regular(const SweepArgs &a, int b, int pt, int col) {
+  RegLoad x;
+  reg_load(a, b, pt, col, x, false);
+  Trace t = reg_trace(x, b, pt);
+  const int iface = (int)x.g.w;
+  const int ox = (b & 1) ? -a.nz * a.ny1 : a.nz * a.ny1, oy = (b & 2) ? -a.nz : a.nz, oz = (b & 4) ? -1 : 1;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int d = c_face[iface][k] ^ b;
+    t.q[k] = pt + ((d & 1) ? ox : 0) + ((d & 2) ? oy : 0) + ((d & 4) ? oz : 0);
+  }
+  return t;
+}
+
+// Radiance of a regular point from its loaded trace inputs.
+__device__ __forceinline__ void reg_finish(const SweepArgs &a, const RegLoad &x, int b) {
+  Trace t = reg_trace(x, b, x.pt);
+  float rad = t.radsrc;
+  if (t.tr != 0.f) rad += t.tr * (t.f[0] * x.r[0] + t.f[1] * x.r[1] + t.f[2] * x.r[2] + t.f[3] * x.r[3]);
+  a.raddo[(size_t)x.pt * a.ldo + x.col] = rad;
+}
+
+// General trace (any point); with use_level the level of the ordinate's
+// face class must also precede the point's (level-synchronous execution).
+__device__ __forceinline__ Trace trace_general(const SweepArgs &a, int b, int cls, int pt, int col, bool use_level) {
   Trace t;
   t.radsrc = 0.f; t.tr = 1.f; t.status = ERR_SWEEP_STEPS;
   t.q[0] = t.q[1] = t.q[2] = t.q[3] = pt; t.f[0] = t.f[1] = t.f[2] = t.f[3] = 0.f;
@@ -285,7 +329,7 @@ __device__ __forceinline__ Trace trace_point(const SweepArgs &a, int b, int pt, 
   const float cxinv = cx != 0.f ? 1.f / cx : 1.0e6f, cyinv = cy != 0.f ? 1.f / cy : 1.0e6f, czinv = 1.f / cz;
   const int bitx = cx < 0.f, bity = cy < 0.f, bitz = cz < 0.f;
   const int hb = bitz ? 2 : 1;
-  const int *rk = a.rank + (size_t)b * n, *lv = a.level + (size_t)b * n;
+  const int *rk = a.rank + (size_t)b * n, *lv = a.level + ((size_t)b * 4 + cls) * n;
   const int rP = rk[pt], lP = use_level ? lv[pt] : 0;
   int cell = a.start[(size_t)b * n + pt];
   float xe = a.gridpos[3 * pt], ye = a.gridpos[3 * pt + 1], ze = a.gridpos[3 * pt + 2];
@@ -343,23 +387,9 @@ __device__ __forceinline__ Trace trace_point(const SweepArgs &a, int b, int pt, 
     const float ext0 = f1 * e1 + f2 * e2 + f3 * e3 + f4 * e4;
     const float srcext0 = f1 * a.srcdo[(size_t)i1 * ldo + col] * e1 + f2 * a.srcdo[(size_t)i2 * ldo + col] * e2 +
                           f3 * a.srcdo[(size_t)i3 * ldo + col] * e3 + f4 * a.srcdo[(size_t)i4 * ldo + col] * e4;
-    const float ext = 0.5f * (ext0 + ext1), tau = ext * so;
-    float transcell, abscell, src;
-    if (tau >= 0.5f) { transcell = __expf(-tau); abscell = 1.f - transcell; }
-    else {
-      abscell = tau * (1.f - 0.5f * tau * (1.f - 0.33333333333f * tau * (1.f - 0.25f * tau)));
-      transcell = 1.f - abscell;
-    }
-    if (tau <= 2.f) {
-      src = (ext == 0.f) ? 0.f : (0.5f * (srcext0 + srcext1) + 0.08333333333f * (ext0 * srcext1 - ext1 * srcext0) * so) / ext;
-    } else {
-      float ext0p = ext0, srcext0p = srcext0;
-      if (tau > 4.f) { ext0p = ext1 + (ext0 - ext1) * 4.f / tau; if (ext0 > 0.f) srcext0p = srcext0 * ext0p / ext0; }
-      src = 1.f / (ext0p + ext1) *
-            (srcext0p + srcext1 + (ext0p * srcext1 - ext1 * srcext0p) * 2.f / (ext0p + ext1) * (1.f - 2.f / tau + 2.f * transcell / abscell));
-    }
-    src = fmaxf(src, 0.f);
-    rad += tr * src * abscell;
+    float radsrc, transcell;
+    cell_source(ext0, srcext0, ext1, srcext1, so, radsrc, transcell);
+    rad += tr * radsrc;
     tr *= transcell;
     auto ok = [&](int q) { return (a.bnd[q] & hb) || (rk[q] < rP && (!use_level || lv[q] < lP)); };
     const bool valid = ok(i1) && ok(i2) && ok(i3) && ok(i4);
@@ -377,48 +407,88 @@ __device__ __forceinline__ Trace trace_point(const SweepArgs &a, int b, int pt, 
   return t;
 }
 
-// Level-synchronous sweep: one launch per wavefront level, one thread per
-// (octant, point, ordinate-of-the-octant) task of that level.
-__global__ void __launch_bounds__(256) k_sweep(SweepArgs a, int t0, int ntask, int omax) {
-  int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  int task = tid / omax, slot = tid - task * omax;
-  if (task >= ntask) return;
-  uint32_t tk = a.tasks[t0 + task];
-  int b = (int)(tk >> 28), pt = (int)(tk & 0x0FFFFFFFu);
-  if (slot >= a.oct_ncol[b]) return;
-  const int col = a.oct_col0[b] + slot, ldo = a.ldo;
-  Trace t = trace_point(a, b, pt, col, true);
+__device__ __forceinline__ Trace trace_point(const SweepArgs &a, int b, int pt, int col) {
+  if (a.regular[(size_t)b * a.npts + pt]) return trace_regular(a, b, pt, col);
+  return trace_general(a, b, 3, pt, col, false);
+}
+
+__device__ __forceinline__ void general_item(const SweepArgs &a, int b, int cls, int pt, int col) {
+  Trace t = trace_general(a, b, cls, pt, col, true);
   if (t.status != ERR_NONE) atomicCAS(a.err, ERR_NONE, t.status);
   float rad = t.radsrc;
+  const int ldo = a.ldo;
   if (t.tr != 0.f)
     rad += t.tr * (t.f[0] * a.raddo[(size_t)t.q[0] * ldo + col] + t.f[1] * a.raddo[(size_t)t.q[1] * ldo + col] +
                    t.f[2] * a.raddo[(size_t)t.q[2] * ldo + col] + t.f[3] * a.raddo[(size_t)t.q[3] * ldo + col]);
   a.raddo[(size_t)pt * ldo + col] = rad;
 }
 
-// All wavefront levels of one hemisphere in one cooperative launch: the
-// blocks stride over the tasks of a level, then meet at a grid barrier.
-__global__ void __launch_bounds__(256) k_sweep_levels(SweepArgs a, const int *__restrict__ level_off, int nlev,
-                                                      int omax) {
-  cooperative_groups::grid_group grid = cooperative_groups::this_grid();
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (int l = 0; l < nlev; ++l) {
-    const int t0 = level_off[l], nt = level_off[l + 1] - t0;
-    const long long total = (long long)nt * omax;
-    for (long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x; tid < total; tid += stride) {
-      const int task = (int)(tid / omax), slot = (int)(tid - (long long)task * omax);
-      const uint32_t tk = a.tasks[t0 + task];
-      const int b = (int)(tk >> 28), pt = (int)(tk & 0x0FFFFFFFu);
-      if (slot >= a.oct_ncol[b]) continue;
-      const int col = a.oct_col0[b] + slot, ldo = a.ldo;
-      Trace t = trace_point(a, b, pt, col, true);
-      if (t.status != ERR_NONE) atomicCAS(a.err, ERR_NONE, t.status);
-      float rad = t.radsrc;
-      if (t.tr != 0.f)
-        rad += t.tr * (t.f[0] * a.raddo[(size_t)t.q[0] * ldo + col] + t.f[1] * a.raddo[(size_t)t.q[1] * ldo + col] +
-                       t.f[2] * a.raddo[(size_t)t.q[2] * ldo + col] + t.f[3] * a.raddo[(size_t)t.q[3] * ldo + col]);
-      a.raddo[(size_t)pt * ldo + col] = rad;
+// Level-synchronous sweep.  A level's work is a list of segments (octant,
+// face class, regular or not); its items (task x column of the class) are
+// numbered consecutively and strided over the threads; consecutive threads
+// take consecutive columns of one point.  Regular items are taken two at a
+// time with all reads of both issued before either is combined.
+constexpr int MAXSEG = 32;
+
+__device__ __forceinline__ int seg_item(const Seg *sg, int nseg, int i, int &si, const SweepArgs &a, int &pt,
+                                        int &col) {
+  while (si + 1 < nseg && i >= sg[si + 1].start) ++si;
+  const Seg &s = sg[si];
+  const int li = i - s.start, task = li / s.ncol, slot = li - task * s.ncol;
+  pt = (int)__ldg(a.tasks + s.t0 + task);
+  col = s.col0 + slot;
+  return si;
+}
+
+__device__ __forceinline__ void sweep_level(const SweepArgs &a, const Seg *sg, int nseg, int items, int gtid,
+                                            int gstride) {
+  int si = 0;
+  for (int i = gtid; i < items; i += 2 * gstride) {
+    int pt1, col1, pt2 = 0, col2 = 0;
+    const int s1 = seg_item(sg, nseg, i, si, a, pt1, col1);
+    const bool two = i + gstride < items;
+    int sj = si;
+    const int s2 = two ? seg_item(sg, nseg, i + gstride, sj, a, pt2, col2) : s1;
+    const Seg &g1 = sg[s1], &g2 = sg[s2];
+    if (g1.regular && two && g2.regular) {
+      RegLoad x1, x2;
+      reg_load(a, g1.b, pt1, col1, x1, true);
+      reg_load(a, g2.b, pt2, col2, x2, true);
+      reg_finish(a, x1, g1.b);
+      reg_finish(a, x2, g2.b);
+    } else {
+      if (g1.regular) { RegLoad x1; reg_load(a, g1.b, pt1, col1, x1, true); reg_finish(a, x1, g1.b); }
+      else general_item(a, g1.b, g1.cls, pt1, col1);
+      if (two) {
+        if (g2.regular) { RegLoad x2; reg_load(a, g2.b, pt2, col2, x2, true); reg_finish(a, x2, g2.b); }
+        else general_item(a, g2.b, g2.cls, pt2, col2);
+      }
     }
+    si = sj;
+  }
+}
+
+// One launch per level (used when a cooperative launch is not available).
+__global__ void __launch_bounds__(256) k_sweep(SweepArgs a, const Seg *__restrict__ segs, int nseg, int items) {
+  __shared__ Seg sg[MAXSEG];
+  for (int t = threadIdx.x; t < nseg; t += blockDim.x) sg[t] = segs[t];
+  __syncthreads();
+  sweep_level(a, sg, nseg, items, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
+// All levels of one hemisphere in one cooperative launch: the blocks share
+// out the items of a level, then meet at a grid barrier.
+__global__ void __launch_bounds__(256) k_sweep_levels(SweepArgs a, const Seg *__restrict__ segs,
+                                                      const int *__restrict__ seg_off,
+                                                      const int *__restrict__ level_items, int nlev) {
+  cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+  __shared__ Seg sg[MAXSEG];
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
+  for (int l = 0; l < nlev; ++l) {
+    const int s0 = seg_off[l], ns = seg_off[l + 1] - s0;
+    for (int t = threadIdx.x; t < ns; t += blockDim.x) sg[t] = segs[s0 + t];
+    __syncthreads();
+    sweep_level(a, sg, ns, level_items[l], gtid, gstride);
     grid.sync();
   }
 }
@@ -447,7 +517,7 @@ __global__ void __launch_bounds__(SEQW) k_sweep_seq(SweepArgs a, const int *orde
     bool pending = r < n && !(a.bnd[pt] & hb);
     Trace t;
     if (pending) {
-      t = trace_point(a, b, pt, col, false);
+      t = trace_point(a, b, pt, col);
       if (t.status != ERR_NONE) atomicCAS(a.err, ERR_NONE, t.status);
     }
     int wl[4];
@@ -996,7 +1066,8 @@ struct Handle {
   DBuf<uint8_t> bnd, regular;
   DBuf<float> geo;
   DBuf<uint32_t> tasks[2];
-  DBuf<int> level_off[2];
+  DBuf<Seg> segs[2];
+  DBuf<int> seg_off[2], level_items[2];
   int coop_blocks = 0;
   DBuf<float> col_cx, col_cy, col_cz, col_fluxw, cmu1t, cmu2t, cphi1t, cphi2, ylmsun;
   DBuf<int> nphi0, col_of;
@@ -1015,7 +1086,6 @@ struct Handle {
   int tc_bn[2] = {0, 0}, tc_ntiles[2] = {0, 0}, tc_kpad[2] = {0, 0};
   DBuf<float> tc_bh[2], tc_bl[2];
   CUtensorMap tm_a[2], tm_bh[2], tm_bl[2];
-  int omax[2] = {0, 0};
   bool seq[2] = {false, false};  // sequential-order sweep engine per hemisphere
   bool initialized = false;
   int iters = 0;
@@ -1165,15 +1235,20 @@ static void upload_plan(Handle &H) {
     H.order.upload(ord);
   }
   for (int h = 0; h < 2; ++h) {
-    int nlev = (int)P.level_off[h].size() - 1;
+    int nlev = (int)P.seg_off[h].size() - 1;
     H.seq[h] = nlev > 4 * (P.nx1 + P.ny1 + P.nz) + 64;
+    for (int l = 0; l < nlev; ++l)
+      if (P.seg_off[h][l + 1] - P.seg_off[h][l] > MAXSEG) throw std::runtime_error("sweep schedule: too many segments in a level");
   }
   H.regular.upload(P.regular); H.geo.upload(P.geo);
   H.bnd.upload(P.bnd); H.topp.upload(P.topp); H.botp.upload(P.botp); H.lofj.upload(P.lofj);
   std::vector<int> bi(P.npts, -1);
   for (size_t k = 0; k < P.botp.size(); ++k) bi[P.botp[k]] = (int)k;
   H.bot_index.upload(bi);
-  for (int h = 0; h < 2; ++h) { H.tasks[h].upload(P.tasks[h]); H.level_off[h].upload(P.level_off[h]); }
+  for (int h = 0; h < 2; ++h) {
+    H.tasks[h].upload(P.tasks[h]); H.segs[h].upload(P.segs[h]);
+    H.seg_off[h].upload(P.seg_off[h]); H.level_items[h].upload(P.level_items[h]);
+  }
   {
     int dev = 0, nsm = 0, per = 0, coop = 0;
     CK(cudaGetDevice(&dev));
@@ -1199,11 +1274,6 @@ static void upload_plan(Handle &H) {
   H.text.upload(P.total_ext); H.dirflux.upload(P.dirflux); H.coef.upload(P.coef);
   H.tms_ptr.upload(P.tms_ptr); H.tms_iph.upload(P.tms_iph); H.tms_w.upload(P.tms_w);
   H.phasetab.upload(P.phasetab); H.botalb.upload(P.botalb); H.rad0.upload(P.rad0);
-  for (int h = 0; h < 2; ++h) {
-    int m = 0;
-    for (int b = 0; b < 8; ++b) if (((b >> 2) & 1) == h) m = std::max(m, P.oct_ncol[b]);
-    H.omax[h] = m;
-  }
   H.ldo = (P.nang + 3) & ~3;
   const size_t nf = (size_t)P.npts * P.nlm, nd = (size_t)P.npts * H.ldo;
   H.source.alloc(nf); H.delsource.alloc(nf); H.radiance.alloc(nf);
@@ -1294,23 +1364,23 @@ static void sweep_hemisphere(Handle &H, int hemi) {
     CK(cudaGetLastError());
     return;
   }
-  const std::vector<int> &off = P.level_off[hemi];
-  const int omax = std::max(1, H.omax[hemi]);
-  if (H.coop_blocks > 0 && off.size() > 1) {
-    int nlev = (int)off.size() - 1;
-    const int *lo = H.level_off[hemi].p;
-    int om = omax;
-    void *args[] = {&a, (void *)&lo, &nlev, &om};
+  const std::vector<int> &off = P.seg_off[hemi];
+  const int nlev = (int)off.size() - 1;
+  if (nlev <= 0) return;
+  if (H.coop_blocks > 0) {
+    const Seg *sp = H.segs[hemi].p;
+    const int *so = H.seg_off[hemi].p, *li = H.level_items[hemi].p;
+    int nl = nlev;
+    void *args[] = {&a, (void *)&sp, (void *)&so, (void *)&li, &nl};
     CK(cudaLaunchCooperativeKernel((const void *)k_sweep_levels, dim3(H.coop_blocks), dim3(256), args, 0, H.stream));
     H.launches += 1;
     return;
   }
-  for (size_t l = 0; l + 1 < off.size(); ++l) {
-    int t0 = off[l], nt = off[l + 1] - off[l];
-    if (nt <= 0) continue;
-    long long threads = (long long)nt * omax;
-    int blocks = (int)((threads + 255) / 256);
-    k_sweep<<<blocks, 256, 0, H.stream>>>(a, t0, nt, omax);
+  for (int l = 0; l < nlev; ++l) {
+    const int items = P.level_items[hemi][l];
+    if (items <= 0) continue;
+    int blocks = std::min((items + 511) / 512, 152 * 8);
+    k_sweep<<<blocks, 256, 0, H.stream>>>(a, H.segs[hemi].p + off[l], off[l + 1] - off[l], items);
     H.launches += 1;
   }
   CK(cudaGetLastError());
@@ -1564,8 +1634,8 @@ int shdom_get_sizes(shdom_handle *hh, shdom_sizes *o) {
   o->npts = P.npts; o->ncells = P.ncells; o->nx1 = P.nx1; o->ny1 = P.ny1; o->nz = P.nz; o->nlm = P.nlm;
   o->nmu = P.nmu; o->nang = P.nang; o->ml = P.ml; o->mm = P.mm; o->bcflag = P.bcflag; o->ipflag = P.ipflag;
   o->iters = hh->h.iters; o->solcrit = hh->h.solcrit; o->albmax = P.albmax;
-  o->nlevels_down = (int)P.level_off[0].size() - 1;
-  o->nlevels_up = (int)P.level_off[1].size() - 1;
+  o->nlevels_down = (int)P.seg_off[0].size() - 1;
+  o->nlevels_up = (int)P.seg_off[1].size() - 1;
   o->launches = hh->h.launches;
   return 0;
 }

@@ -299,6 +299,32 @@ int trace_octant(float mu, float phi, int is1d) {
   return 1 + (cx < 0) + 2 * (cy < 0) + 4 * bz;
 }
 
+// Exit of a trace that starts at corner b of a full interior cell of size
+// (dx, dy, dz) and leaves through the far side, with the same
+// single-precision steps as the device trace: path length so, bilinear face
+// coordinates (u, v) and the face index (0/1 x, 2/3 y, 4/5 z).
+int regular_exit(float cx, float cy, float cz, int b, float dx, float dy, float dz, float &so, float &u, float &v) {
+  const float cxinv = cx != 0.f ? 1.f / cx : 1.0e6f, cyinv = cy != 0.f ? 1.f / cy : 1.0e6f, czinv = 1.f / cz;
+  const int bitx = cx < 0.f, bity = cy < 0.f, bitz = cz < 0.f;
+  auto pos = [&](int k, float &x, float &y, float &z) { x = (k & 1) * dx; y = ((k >> 1) & 1) * dy; z = ((k >> 2) & 1) * dz; };
+  float xe, ye, ze, xo, yo, zo;
+  pos(b, xe, ye, ze);
+  pos(7 - b, xo, yo, zo);
+  float sox = (xo - xe) * cxinv, soy = (yo - ye) * cyinv, soz = (zo - ze) * czinv;
+  so = std::min(sox, std::min(soy, soz));
+  xe += so * cx; ye += so * cy; ze += so * cz;
+  int iface, jface;
+  if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; }
+  else if (soy <= soz) { iface = 3 - bity; jface = 1; }
+  else { iface = 5 - bitz; jface = 2; }
+  float x1, y1, z1, x2, y2, z2, x3, y3, z3;
+  pos(kFace[iface][0], x1, y1, z1); pos(kFace[iface][1], x2, y2, z2); pos(kFace[iface][2], x3, y3, z3);
+  if (jface == 0) { u = (ze - z1) / (z3 - z1); v = (ye - y1) / (y2 - y1); }
+  else if (jface == 1) { u = (ze - z1) / (z3 - z1); v = (xe - x1) / (x2 - x1); }
+  else { u = (ye - y1) / (y3 - y1); v = (xe - x1) / (x2 - x1); }
+  return iface;
+}
+
 void build_angles(const shdom_problem &p, Plan &P) {
   P.nmu = std::max(2, 2 * ((p.nmu + 1) / 2));
   P.nphi = std::max(1, p.nphi);
@@ -341,7 +367,24 @@ void build_angles(const shdom_problem &p, Plan &P) {
     }
     P.nang += P.nphi0[j];
   }
-  // column order: hemisphere, trace octant, (imu, iphi)
+  // Face class of each ordinate: the face through which a trace from a
+  // regular point leaves its cell, when it is the same kind (x, y or z) in
+  // every layer; class 3 otherwise (and for 1D and single-column grids).
+  auto face_class = [&](int j, int q) {
+    if (P.is1d || P.nx1 < 2 || P.ny1 < 2 || P.nz < 2) return 3;
+    double dcx, dcy, dcz;
+    trace_dir(P.mu[j], P.phi[(size_t)j * P.nphi0max + q], dcx, dcy, dcz);
+    const float cx = (float)dcx, cy = (float)dcy, cz = (float)dcz;
+    const int b = (cx < 0.f) + 2 * (cy < 0.f) + 4 * (cz < 0.f);
+    const float dx = P.xgrid[1] - P.xgrid[0], dy = P.ygrid[1] - P.ygrid[0];
+    int mask = 0;
+    for (int L = 0; L + 1 < P.nz; ++L) {
+      float so, u, v;
+      mask |= 1 << (regular_exit(cx, cy, cz, b, dx, dy, P.zgrid[L + 1] - P.zgrid[L], so, u, v) / 2);
+    }
+    return mask == 1 ? 0 : mask == 2 ? 1 : mask == 4 ? 2 : 3;
+  };
+  // column order: hemisphere, trace octant, face class, (imu, iphi)
   P.col_of.assign((size_t)nmu * P.nphi0max, -1);
   int col = 0;
   for (int hemi = 0; hemi < 2; ++hemi) {
@@ -349,12 +392,17 @@ void build_angles(const shdom_problem &p, Plan &P) {
     for (int ioct = 1; ioct <= 8; ++ioct) {
       if (((ioct - 1) >> 2 & 1) != hemi) continue;  // bitz=1 traces down: upward ordinates
       P.oct_col0[ioct - 1] = col;
-      for (int j = (hemi ? k : 0); j < (hemi ? nmu : k); ++j)
-        for (int q = 0; q < P.nphi0[j]; ++q) {
-          if (trace_octant(P.mu[j], P.phi[(size_t)j * P.nphi0max + q], P.is1d) != ioct) continue;
-          P.col_of[(size_t)j * P.nphi0max + q] = col++;
-          P.col_imu.push_back(j); P.col_iphi.push_back(q); P.col_oct.push_back(ioct);
-        }
+      for (int cls = 0; cls < 4; ++cls) {
+        P.cls_col0[ioct - 1][cls] = col;
+        for (int j = (hemi ? k : 0); j < (hemi ? nmu : k); ++j)
+          for (int q = 0; q < P.nphi0[j]; ++q) {
+            if (trace_octant(P.mu[j], P.phi[(size_t)j * P.nphi0max + q], P.is1d) != ioct) continue;
+            if (face_class(j, q) != cls) continue;
+            P.col_of[(size_t)j * P.nphi0max + q] = col++;
+            P.col_imu.push_back(j); P.col_iphi.push_back(q); P.col_oct.push_back(ioct); P.col_cls.push_back(cls);
+          }
+        P.cls_ncol[ioct - 1][cls] = col - P.cls_col0[ioct - 1][cls];
+      }
       P.oct_ncol[ioct - 1] = col - P.oct_col0[ioct - 1];
     }
   }
@@ -773,10 +821,11 @@ void build_direct(const shdom_problem &p, Plan &P) {
 }
 
 bool build_schedule(const shdom_problem &p, Plan &P) {
-  P.rank.assign((size_t)8 * P.npts, -1);
-  P.startcell.assign((size_t)8 * P.npts, -1);
-  P.level.assign((size_t)8 * P.npts, 0);
-  P.regular.assign((size_t)8 * P.npts, 0);
+  const int n = P.npts;
+  P.rank.assign((size_t)8 * n, -1);
+  P.startcell.assign((size_t)8 * n, -1);
+  P.level.assign((size_t)32 * n, 0);
+  P.regular.assign((size_t)8 * n, 0);
   std::vector<int> octs = P.is1d ? std::vector<int>{1, 5} : std::vector<int>{1, 2, 3, 4, 5, 6, 7, 8};
   const double transmin = p.transmin;
   bool ok = true;
@@ -785,119 +834,131 @@ bool build_schedule(const shdom_problem &p, Plan &P) {
   for (int ioct : octs) {
     th.emplace_back([&, ioct]() {
       sweep_order(P, ioct);
-      const int b = ioct - 1, n = P.npts;
+      const int b = ioct - 1;
       const int hemi_bnd = (b & 4) ? 2 : 1;  // trace down: bottom points preset
       const int *rk = &P.rank[(size_t)b * n];
       const int *sc = &P.startcell[(size_t)b * n];
-      int *lv = &P.level[(size_t)b * n];
       std::vector<int> order(n);
       for (int i = 0; i < n; ++i) order[rk[i]] = i;
-      const int c0 = P.oct_col0[b], nc = P.oct_ncol[b];
       for (int r = 0; r < n; ++r) {
         int pt = order[r];
-        if (P.bnd[pt] & hemi_bnd) { lv[pt] = 0; continue; }
+        if (P.bnd[pt] & hemi_bnd) continue;
         int cell = sc[pt];
         const int *g = &P.gridptr[8 * (size_t)cell];
-        bool fast = transmin >= 1.0 && !P.is1d && g[b] == pt;
-        int lvl = 0;
-        if (fast) {
-          for (int k = 0; k < 8 && fast; ++k) {
-            if (k == b) continue;
-            int q = g[k];
-            if (q == pt || !((P.bnd[q] & hemi_bnd) || rk[q] < r)) fast = false;
-            else lvl = std::max(lvl, lv[q]);
-          }
+        bool fast = transmin >= 1.0 && !P.is1d && g[b] == pt && P.cellflags[cell] == 0;
+        for (int k = 0; k < 8 && fast; ++k) {
+          if (k == b) continue;
+          int q = g[k];
+          if (q == pt || !((P.bnd[q] & hemi_bnd) || rk[q] < r)) fast = false;
         }
-        if (fast && P.cellflags[cell] == 0) P.regular[(size_t)b * n + pt] = 1;
-        if (!fast) {
-          lvl = 0;
-          for (int c = c0; c < c0 + nc; ++c) {
-            int f[4];
-            double tcx, tcy, tcz;
-            trace_dir(P.mu[P.col_imu[c]], P.phi[(size_t)P.col_imu[c] * P.nphi0max + P.col_iphi[c]], tcx, tcy, tcz);
-            if (!trace_final_face(P, ioct, pt, tcx, tcy, tcz, hemi_bnd, transmin, f)) {
-              errs[b] = "sweep planning: trace found no valid face (BACK_INT_GRID: INEXTCELL=0)";
-              return;
+        if (fast) P.regular[(size_t)b * n + pt] = 1;
+        for (int cls = 0; cls < 4; ++cls) {
+          const int nc = P.cls_ncol[b][cls], c0 = P.cls_col0[b][cls];
+          if (nc == 0) continue;
+          int *lv = &P.level[((size_t)b * 4 + cls) * n];
+          int lvl = 0;
+          if (fast) {
+            // corners of the class's exit face (all seven for class 3)
+            if (cls < 3) {
+              const int bit = (cls == 0) ? (b & 1) : (cls == 1) ? ((b >> 1) & 1) : ((b >> 2) & 1);
+              const int iface = 2 * cls + 1 - bit;
+              for (int k = 0; k < 4; ++k) lvl = std::max(lvl, lv[g[kFace[iface][k]]]);
+            } else {
+              for (int k = 0; k < 8; ++k) if (k != b) lvl = std::max(lvl, lv[g[k]]);
             }
-            for (int k = 0; k < 4; ++k) lvl = std::max(lvl, lv[f[k]]);
+          } else {
+            for (int c = c0; c < c0 + nc; ++c) {
+              int f[4];
+              double tcx, tcy, tcz;
+              trace_dir(P.mu[P.col_imu[c]], P.phi[(size_t)P.col_imu[c] * P.nphi0max + P.col_iphi[c]], tcx, tcy, tcz);
+              if (!trace_final_face(P, ioct, pt, tcx, tcy, tcz, hemi_bnd, transmin, f)) {
+                errs[b] = "sweep planning: trace found no valid face (BACK_INT_GRID: INEXTCELL=0)";
+                return;
+              }
+              for (int k = 0; k < 4; ++k) lvl = std::max(lvl, lv[f[k]]);
+            }
           }
+          lv[pt] = lvl + 1;
         }
-        lv[pt] = lvl + 1;
       }
     });
   }
   for (auto &t : th) t.join();
   for (auto &e : errs) if (!e.empty()) { P.err = e; ok = false; }
   if (!ok) return false;
-  // bucket (octant, point) tasks by level for each hemisphere
+  // Segments: per hemisphere and level, the (octant, class, regular) groups
+  // of points at that level, each with the class's column range.
   for (int hemi = 0; hemi < 2; ++hemi) {
     int maxl = 0;
+    std::vector<std::pair<int, int>> groups;  // (octant, class) pairs of this hemisphere
     for (int ioct : octs) {
       int b = ioct - 1;
-      if (((b >> 2) & 1) != hemi || P.oct_ncol[b] == 0) continue;
-      for (int i = 0; i < P.npts; ++i) maxl = std::max(maxl, P.level[(size_t)b * P.npts + i]);
-    }
-    std::vector<int> cnt(maxl + 2, 0);
-    for (int ioct : octs) {
-      int b = ioct - 1;
-      if (((b >> 2) & 1) != hemi || P.oct_ncol[b] == 0) continue;
-      for (int i = 0; i < P.npts; ++i) { int l = P.level[(size_t)b * P.npts + i]; if (l > 0) cnt[l]++; }
-    }
-    P.level_off[hemi].assign(maxl + 1, 0);  // level l (1..maxl) -> offset at index l-1; last = total
-    int acc = 0;
-    for (int l = 1; l <= maxl; ++l) { P.level_off[hemi][l - 1] = acc; acc += cnt[l]; }
-    P.level_off[hemi][maxl] = acc;
-    P.tasks[hemi].assign(acc, 0);
-    std::vector<int> fill(P.level_off[hemi].begin(), P.level_off[hemi].end());
-    for (int ioct : octs) {
-      int b = ioct - 1;
-      if (((b >> 2) & 1) != hemi || P.oct_ncol[b] == 0) continue;
-      for (int i = 0; i < P.npts; ++i) {
-        int l = P.level[(size_t)b * P.npts + i];
-        if (l > 0) P.tasks[hemi][fill[l - 1]++] = ((uint32_t)b << 28) | (uint32_t)i;
+      if (((b >> 2) & 1) != hemi) continue;
+      for (int cls = 0; cls < 4; ++cls) {
+        if (P.cls_ncol[b][cls] == 0) continue;
+        groups.push_back({b, cls});
+        const int *lv = &P.level[((size_t)b * 4 + cls) * n];
+        for (int i = 0; i < n; ++i) maxl = std::max(maxl, lv[i]);
       }
+    }
+    // counts per (level, group, regular)
+    const int ng = (int)groups.size();
+    std::vector<int> cnt((size_t)(maxl + 1) * ng * 2, 0);
+    for (int gi = 0; gi < ng; ++gi) {
+      const int b = groups[gi].first;
+      const int *lv = &P.level[((size_t)b * 4 + groups[gi].second) * n];
+      const uint8_t *rg = &P.regular[(size_t)b * n];
+      for (int i = 0; i < n; ++i)
+        if (lv[i] > 0) cnt[((size_t)lv[i] * ng + gi) * 2 + (rg[i] ? 0 : 1)]++;
+    }
+    P.segs[hemi].clear();
+    P.seg_off[hemi].assign(1, 0);
+    P.level_items[hemi].clear();
+    std::vector<int> fill((size_t)(maxl + 1) * ng * 2, 0);
+    int t = 0;
+    for (int l = 1; l <= maxl; ++l) {
+      long long items = 0;
+      for (int gi = 0; gi < ng; ++gi)
+        for (int irr = 0; irr < 2; ++irr) {
+          const int c = cnt[((size_t)l * ng + gi) * 2 + irr];
+          if (c == 0) continue;
+          const int b = groups[gi].first, cls = groups[gi].second;
+          Seg sg;
+          sg.t0 = t; sg.ntask = c; sg.start = (int)items; sg.b = b; sg.cls = cls;
+          sg.col0 = P.cls_col0[b][cls]; sg.ncol = P.cls_ncol[b][cls]; sg.regular = irr ? 0 : 1;
+          fill[((size_t)l * ng + gi) * 2 + irr] = t;
+          P.segs[hemi].push_back(sg);
+          t += c;
+          items += (long long)c * sg.ncol;
+        }
+      if (items >= (1LL << 31)) { P.err = "sweep level too large"; return false; }
+      P.seg_off[hemi].push_back((int)P.segs[hemi].size());
+      P.level_items[hemi].push_back((int)items);
+    }
+    P.tasks[hemi].assign(t, 0);
+    for (int gi = 0; gi < ng; ++gi) {
+      const int b = groups[gi].first;
+      const int *lv = &P.level[((size_t)b * 4 + groups[gi].second) * n];
+      const uint8_t *rg = &P.regular[(size_t)b * n];
+      for (int i = 0; i < n; ++i)
+        if (lv[i] > 0) P.tasks[hemi][fill[((size_t)lv[i] * ng + gi) * 2 + (rg[i] ? 0 : 1)]++] = (uint32_t)i;
     }
   }
   return true;
 }
 
-// Exit geometry of a trace that starts at corner b of a full interior cell
-// (dx, dy, dz) and leaves through the far side, computed with the same
-// single-precision steps as the device trace.
+// Exit geometry of regular-point traces per (layer, ordinate): so, u, v, face.
 void build_geo(Plan &P) {
   const int nl = P.nz - 1, nang = P.nang;
-  P.geo.assign((size_t)std::max(nl, 1) * nang * 8, 0.f);
+  P.geo.assign((size_t)std::max(nl, 1) * nang * 4, 0.f);
   if (P.is1d || P.nx1 < 2 || P.ny1 < 2) return;
   const float dx = P.xgrid[1] - P.xgrid[0], dy = P.ygrid[1] - P.ygrid[0];
-  for (int L = 0; L < nl; ++L) {
-    const float dz = P.zgrid[L + 1] - P.zgrid[L];
+  for (int L = 0; L < nl; ++L)
     for (int c = 0; c < nang; ++c) {
-      const float cx = P.col_cx[c], cy = P.col_cy[c], cz = P.col_cz[c];
+      float *g = &P.geo[((size_t)L * nang + c) * 4];
       const int b = P.col_oct[c] - 1;
-      const float cxinv = cx != 0.f ? 1.f / cx : 1.0e6f, cyinv = cy != 0.f ? 1.f / cy : 1.0e6f, czinv = 1.f / cz;
-      const int bitx = cx < 0.f, bity = cy < 0.f, bitz = cz < 0.f;
-      auto pos = [&](int k, float &x, float &y, float &z) { x = (k & 1) * dx; y = ((k >> 1) & 1) * dy; z = ((k >> 2) & 1) * dz; };
-      float xe, ye, ze, xo, yo, zo;
-      pos(b, xe, ye, ze);
-      pos(7 - b, xo, yo, zo);
-      float sox = (xo - xe) * cxinv, soy = (yo - ye) * cyinv, soz = (zo - ze) * czinv;
-      float so = std::min(sox, std::min(soy, soz));
-      xe += so * cx; ye += so * cy; ze += so * cz;
-      int iface, jface;
-      if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; }
-      else if (soy <= soz) { iface = 3 - bity; jface = 1; }
-      else { iface = 5 - bitz; jface = 2; }
-      float x1, y1, z1, x2, y2, z2, x3, y3, z3;
-      pos(kFace[iface][0], x1, y1, z1); pos(kFace[iface][1], x2, y2, z2); pos(kFace[iface][2], x3, y3, z3);
-      float u, v;
-      if (jface == 0) { u = (ze - z1) / (z3 - z1); v = (ye - y1) / (y2 - y1); }
-      else if (jface == 1) { u = (ze - z1) / (z3 - z1); v = (xe - x1) / (x2 - x1); }
-      else { u = (ye - y1) / (y3 - y1); v = (xe - x1) / (x2 - x1); }
-      float *g = &P.geo[((size_t)L * nang + c) * 8];
-      g[0] = so; g[1] = (1.f - u) * (1.f - v); g[2] = (1.f - u) * v; g[3] = u * (1.f - v); g[4] = u * v;
-      g[5] = (float)iface;
+      g[3] = (float)regular_exit(P.col_cx[c], P.col_cy[c], P.col_cz[c], b, dx, dy, P.zgrid[L + 1] - P.zgrid[L], g[0], g[1], g[2]);
     }
-  }
 }
 
 }  // namespace

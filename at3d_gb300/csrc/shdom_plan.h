@@ -16,6 +16,14 @@
 
 namespace shdom {
 
+// One group of sweep tasks at one wavefront level: the points (tasks[t0,
+// t0+ntask)) of trace octant b whose traces for the ordinates of face class
+// cls (columns [col0, col0+ncol)) are all regular or all not.  start is the
+// group's first item (task x column) within its level.
+struct Seg {
+  int t0, ntask, start, b, cls, col0, ncol, regular;
+};
+
 struct Plan {
   // ---- base grid (INIT_CELL_STRUCTURE layout, 0-based, -1 = no neighbour)
   int nx = 0, ny = 0, nz = 0, nx1 = 0, ny1 = 0, npts = 0, ncells = 0;
@@ -30,12 +38,12 @@ struct Plan {
   // ---- sweep order per trace octant (index ioct-1): rank and start cell
   std::vector<int> rank;           // [8][npts], -1 when the octant is unused
   std::vector<int> startcell;      // [8][npts]
-  std::vector<int> level;          // [8][npts] wavefront level (0 for boundary points)
+  std::vector<int> level;          // [8][4][npts] wavefront level per octant and face class (0: preset)
   // regular[b][p] = 1 when point p's trace for trace octant b crosses one
   // full interior cell whose seven other corners all precede p; such traces
   // depend only on the ordinate and the z layer, tabulated in geo.
   std::vector<uint8_t> regular;    // [8][npts]
-  std::vector<float> geo;          // [nz-1][nang][8]: so, f1..f4, face, 0, 0
+  std::vector<float> geo;          // [nz-1][nang][4]: so, u, v, face
   // ---- discrete ordinates
   int nmu = 0, nphi = 0, ml = 0, mm = 0, nlm = 0, nleg = 0, nang = 0, nphi0max = 0;
   std::vector<int> nphi0, lofj, mofj;
@@ -43,6 +51,8 @@ struct Plan {
   // Column order of the ordinate-space arrays: hemisphere (down, up), then
   // trace octant, then (mu, phi) in the reference order.
   std::vector<int> col_imu, col_iphi, col_oct;   // [nang]
+  std::vector<int> col_cls;                      // [nang] face class: 0 x, 1 y, 2 z, 3 mixed
+  int cls_col0[8][4] = {{0}}, cls_ncol[8][4] = {{0}};  // column range per octant and class
   std::vector<int> col_of;                       // [nmu][nphi0max] -> column
   int ncol_down = 0;                             // columns [0, ncol_down) are mu < 0
   int oct_col0[8] = {0}, oct_ncol[8] = {0};      // column range of each trace octant
@@ -64,9 +74,11 @@ struct Plan {
   std::vector<float> botalb;                     // surface albedo at the bottom points
   // ---- numerical parameters
   shdom_problem prob{};
-  // ---- wavefront task lists, per hemisphere (0 down, 1 up)
-  std::vector<uint32_t> tasks[2];                // (ioct-1) << 28 | point
-  std::vector<int> level_off[2];                 // level -> first task
+  // ---- wavefront schedule, per hemisphere (0 down, 1 up)
+  std::vector<uint32_t> tasks[2];                // point indices grouped by level and segment
+  std::vector<Seg> segs[2];
+  std::vector<int> seg_off[2];                   // level -> first segment (nlevels + 1 entries)
+  std::vector<int> level_items[2];               // level -> task x column items
   std::string err;
 };
 
