@@ -1220,6 +1220,37 @@ static void setup_tc(Handle &H) {
   }
 }
 
+// Device memory a handle for this plan holds: the uploaded tables, the
+// solution state and the tensor-core transform matrices.
+template <typename T>
+static long long vbytes(const std::vector<T> &v) { return (long long)v.size() * (long long)sizeof(T); }
+
+static long long plan_device_bytes(const Plan &P) {
+  long long b = 0;
+  b += vbytes(P.gridpos) + vbytes(P.xgrid) + vbytes(P.ygrid) + vbytes(P.zgrid) + vbytes(P.gridptr) + vbytes(P.neighptr);
+  b += vbytes(P.cellflags) + vbytes(P.rank) + vbytes(P.startcell) + vbytes(P.level) + vbytes(P.rank);  // + order
+  b += vbytes(P.topp) + vbytes(P.botp) + 4LL * P.npts + vbytes(P.lofj) + vbytes(P.bnd) + vbytes(P.regular) + vbytes(P.geo);
+  for (int h = 0; h < 2; ++h) b += vbytes(P.tasks[h]) + vbytes(P.segs[h]) + vbytes(P.seg_off[h]) + vbytes(P.level_items[h]);
+  b += 4LL * 5 * P.nang + vbytes(P.cmu1) + vbytes(P.cmu2) + vbytes(P.cphi1) + vbytes(P.cphi2) + vbytes(P.ylmsun);
+  b += vbytes(P.nphi0) + vbytes(P.col_of) + vbytes(P.total_ext) + vbytes(P.dirflux) + vbytes(P.coef) + vbytes(P.tms_ptr);
+  b += vbytes(P.tms_iph) + vbytes(P.tms_w) + vbytes(P.phasetab) + vbytes(P.botalb) + vbytes(P.rad0);
+  const long long ldo = (P.nang + 3) & ~3;
+  b += 4LL * P.npts * (3LL * P.nlm + 2 * ldo + 2 + 3) + 4LL * (long long)P.botp.size() + 64;
+  const long long kp0 = (P.nlm + 31) / 32 * 32, kp1 = (P.nang + 31) / 32 * 32;
+  const long long np0 = ((P.nang + 255) / 256) * 256 + 256, np1 = ((P.nlm + 2 + 255) / 256) * 256 + 256;
+  b += 8LL * (np0 * kp0 + np1 * kp1);  // upper bound of the padded hi/lo matrices
+  return b;
+}
+
+static void fill_sizes(const Plan &P, shdom_sizes *o) {
+  o->npts = P.npts; o->ncells = P.ncells; o->nx1 = P.nx1; o->ny1 = P.ny1; o->nz = P.nz; o->nlm = P.nlm;
+  o->nmu = P.nmu; o->nang = P.nang; o->ml = P.ml; o->mm = P.mm; o->bcflag = P.bcflag; o->ipflag = P.ipflag;
+  o->albmax = P.albmax;
+  o->nlevels_down = (int)P.seg_off[0].size() - 1;
+  o->nlevels_up = (int)P.seg_off[1].size() - 1;
+  o->device_bytes = plan_device_bytes(P);
+}
+
 static void upload_plan(Handle &H) {
   Plan &P = H.P;
   H.gridpos.upload(P.gridpos); H.xgrid.upload(P.xgrid); H.ygrid.upload(P.ygrid); H.zgrid.upload(P.zgrid);
@@ -1630,13 +1661,23 @@ int shdom_set_transform_mode(shdom_handle *hh, int mode) {
 
 int shdom_get_sizes(shdom_handle *hh, shdom_sizes *o) {
   if (!hh || !o) return fail(hh, "null argument");
-  shdom::Plan &P = hh->h.P;
-  o->npts = P.npts; o->ncells = P.ncells; o->nx1 = P.nx1; o->ny1 = P.ny1; o->nz = P.nz; o->nlm = P.nlm;
-  o->nmu = P.nmu; o->nang = P.nang; o->ml = P.ml; o->mm = P.mm; o->bcflag = P.bcflag; o->ipflag = P.ipflag;
-  o->iters = hh->h.iters; o->solcrit = hh->h.solcrit; o->albmax = P.albmax;
-  o->nlevels_down = (int)P.seg_off[0].size() - 1;
-  o->nlevels_up = (int)P.seg_off[1].size() - 1;
+  shdom::fill_sizes(hh->h.P, o);
+  o->iters = hh->h.iters; o->solcrit = hh->h.solcrit;
   o->launches = hh->h.launches;
+  return 0;
+}
+
+int shdom_plan_summary(const shdom_problem *problem, shdom_sizes *o) {
+  if (!problem || !o) return fail(nullptr, "shdom_plan_summary: null argument");
+  std::memset(o, 0, sizeof(*o));
+  try {
+    std::unique_ptr<shdom::Plan> P(new shdom::Plan());
+    if (!shdom::build_plan(*problem, *P)) return fail(nullptr, P->err);
+    shdom::fill_sizes(*P, o);
+    o->solcrit = 1.f;
+  } catch (const std::exception &e) {
+    return fail(nullptr, e.what());
+  }
   return 0;
 }
 

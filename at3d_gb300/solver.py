@@ -32,6 +32,22 @@ def _fp(a):
     return a.ctypes.data_as(C.POINTER(C.c_float))
 
 
+def _sizes_dict(s) -> dict:
+    return {name: getattr(s, name) for name, _ in s._fields_}
+
+
+def plan_summary(problem: Problem) -> dict:
+    """Sizes, sweep depths and the device memory of a problem, planned on the
+    host only (no GPU is touched): for admission by memory budget."""
+    L = _lib.lib()
+    st = problem.to_struct()
+    out = _lib.ShdomSizes()
+    rc = L.shdom_plan_summary(C.byref(st), C.byref(out))
+    if rc:
+        raise SHDOMError(L.shdom_last_error(None).decode())
+    return _sizes_dict(out)
+
+
 class RTE:
     """Radiative-transfer solve of one medium at one wavelength.
 

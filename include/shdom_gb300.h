@@ -41,6 +41,7 @@ typedef struct shdom_sizes {
     float solcrit; /* current solution criterion (RTE._solcrit) */
     float albmax;
     long long launches; /* kernels launched on this handle since creation */
+    long long device_bytes; /* device memory the handle holds (estimate before creation) */
 } shdom_sizes;
 
 /* Builds the grid, the cell structure, the sweep schedule and the medium on
@@ -49,6 +50,13 @@ typedef struct shdom_sizes {
  * _prepare_optical_properties (core.transfer_pa_to_grid;
  * at3d/solver.py:2324-2519).  device < 0 keeps the current CUDA device. */
 int shdom_create(const shdom_problem *problem, int device, shdom_handle **out);
+
+/* Plans a problem on the host only (grid, sweep schedule, ordinates, medium)
+ * and reports its sizes, wavefront depths and the device memory a handle for
+ * it would hold; touches no GPU.  For admission by memory budget before
+ * shdom_create.  No direct reference counterpart (the reference sizes its
+ * arrays in RTE._setup_grid, at3d/solver.py:2122-2191). */
+int shdom_plan_summary(const shdom_problem *problem, shdom_sizes *out);
 
 /* Direct beam, Eddington initial radiance and the first source function.
  * Replaces core.make_angle_set, core.make_sh_do_coef and core.init_solution

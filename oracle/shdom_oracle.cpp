@@ -16,7 +16,7 @@
 // Each routine cites the reference routine it restates.  Indices are 0-based
 // here; "no neighbour" is -1 (the reference uses 0 with 1-based cells).
 //
-// Differences from the reference, all documented in the design doc:
+// Differences from the reference:
 //  * the azimuthal transform always uses the DFT (the reference switches to
 //    FFTPACK RFFTB/RFFTF when NPHI0>14, src/polarized/shdomsub2.f:1137); the
 //    two are the same linear map (src/polarized/shdomsub1.f:3008-3030,

@@ -1,0 +1,97 @@
+"""Host-side tests of the C-ABI library (no GPU needed): the library loads
+and exports every entry point include/shdom_gb300.h declares, the host
+planner sizes problems as the reference does (at3d/solver.py:2122-2191,
+src/polarized/shdomsub2.f:1104-1146), and unsupported problems are refused
+with an error code and message, never an abort (at3d/checks.py:300-311)."""
+import ctypes as C
+import dataclasses
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from at3d_gb300 import _lib
+    from at3d_gb300.build import build
+    if not os.path.exists(_lib.LIB):
+        build()
+    return _lib.lib()
+
+
+def declared_functions():
+    txt = open(os.path.join(ROOT, "include", "shdom_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(shdom_[a-z_]+)\s*\(", txt)))
+
+
+def test_exports_every_declared_symbol(lib):
+    from at3d_gb300 import _lib
+    names = declared_functions()
+    assert len(names) >= 12
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, f"symbols declared but not exported: {missing}"
+    # the Python binding types every declared entry point
+    assert sorted(_lib.SIGNATURES) == names
+
+
+def test_plan_sizes_periodic_8_16():
+    """32x32x24 periodic, NMU 8 / NPHI 16: NPTS 33*33*24, NLM 64, NANG 90."""
+    from at3d_gb300.scenes import cloud_blob
+    from at3d_gb300.solver import plan_summary
+    s = plan_summary(cloud_blob())
+    assert (s["npts"], s["nlm"], s["nang"], s["ml"], s["mm"]) == (26136, 64, 90, 7, 7)
+    assert (s["nx1"], s["ny1"], s["nz"], s["ncells"]) == (33, 33, 24, 32 * 32 * 23)
+    assert s["nlevels_down"] > 0 and s["nlevels_up"] > 0
+    assert s["device_bytes"] > 4 * 26136 * (3 * 64 + 2 * 92)
+
+
+def test_plan_sizes_open_16_32():
+    """Open boundaries, NMU 16 / NPHI 32: NPTS nx*ny*nz, NLM 256, NANG 354;
+    the sweep depth is about nx+ny+nz wavefront levels."""
+    from at3d_gb300.scenes import cloud_field
+    from at3d_gb300.solver import plan_summary
+    pb = cloud_field(seed=2, wavelength_index=0, nx=24, ny=24, nz=16)
+    s = plan_summary(pb)
+    assert (s["npts"], s["nlm"], s["nang"]) == (24 * 24 * 16, 256, 354)
+    assert s["bcflag"] == 3
+    assert 24 + 24 + 16 - 6 <= s["nlevels_down"] <= 2 * (24 + 24 + 16)
+
+
+def _with_params(pb, **kw):
+    return dataclasses.replace(pb, params=dataclasses.replace(pb.params, **kw))
+
+
+@pytest.mark.parametrize("kw,msg", [
+    ({"split_accuracy": 0.03}, "splitting"),
+    ({"x_boundary_condition": "open", "y_boundary_condition": "periodic"}, "open x with periodic y"),
+])
+def test_unsupported_problems_are_refused(kw, msg):
+    from at3d_gb300.scenes import cloud_blob
+    from at3d_gb300.solver import SHDOMError, plan_summary
+    pb = _with_params(cloud_blob(nx=8, ny=8, nz=6), **kw)
+    with pytest.raises(SHDOMError, match=msg):
+        plan_summary(pb)
+
+
+def test_vector_radiance_is_refused(lib):
+    from at3d_gb300._lib import ShdomSizes
+    from at3d_gb300.scenes import cloud_blob
+    st = cloud_blob(nx=8, ny=8, nz=6).to_struct()
+    st.nstokes = 3
+    out = ShdomSizes()
+    assert lib.shdom_plan_summary(C.byref(st), C.byref(out)) == 1
+    assert b"nstokes" in lib.shdom_last_error(None)
+
+
+def test_null_arguments(lib):
+    h = C.c_void_p()
+    assert lib.shdom_create(None, 0, C.byref(h)) == 1
+    assert lib.shdom_last_error(None)
+    assert lib.shdom_init_solution(None) == 1
+    assert lib.shdom_set_transform_mode(None, 0) == 1
+    lib.shdom_destroy(None)
