@@ -196,6 +196,17 @@ __global__ void __launch_bounds__(256) k_do_to_sh(XfArgs x, const float *__restr
 }
 
 // ----------------------------------------------------------------- sweep
+// Final face of a general (not regular) trace: corner indices q and the
+// bilinear face coordinates.  g = (so, u, v, 1) for a trace that stops on
+// the first face it meets (the open-boundary edge cells, points off their
+// start cell's corner), built once per handle; g.w = 0 for a trace that
+// needs the run-time cell walk, whose face the source pass writes each
+// iteration (q, and g = (0, u, v, 0)).
+struct IrrRec {
+  int4 q;
+  float4 g;
+};
+
 struct SweepArgs {
   const float *gridpos;
   const int *gridptr, *neighptr, *cellflags;
@@ -207,6 +218,7 @@ struct SweepArgs {
   const uint32_t *tasks;          // point indices of the level schedule
   const uint8_t *regular;
   const float *geo;
+  const IrrRec *irr;               // stored single-cell general traces of this hemisphere
   int *err;
   int npts, nang, ldo, is1d, nz, ny1;
   float transmin;
@@ -222,7 +234,7 @@ struct SweepArgs {
 // wavefront level, so level-synchronous execution never reads a value that
 // is not yet computed).
 struct Trace {
-  float radsrc, tr, f[4];
+  float radsrc, tr, f[4], u, v;  // u, v: bilinear coordinates of the final face
   int q[4];
   int status;  // 0 ok, ERR_* otherwise
 };
@@ -253,6 +265,23 @@ __device__ __forceinline__ void reg_load(const SweepArgs &a, int b, int pt, int 
     x.e[k] = __ldg(a.text + q);
     x.s[k] = __ldg(a.srcdo + (size_t)q * ldo + col);
     x.r[k] = upstream ? a.raddo[(size_t)q * ldo + col] : 0.f;
+  }
+  x.e1 = __ldg(a.text + pt);
+  x.s1 = __ldg(a.srcdo + (size_t)pt * ldo + col);
+}
+
+// Same inputs for a stored single-cell general trace.
+__device__ __forceinline__ void rec_load(const SweepArgs &a, const IrrRec &rec, int pt, int col, RegLoad &x,
+                                         bool upstream) {
+  const int ldo = a.ldo;
+  x.pt = pt; x.col = col;
+  x.g = rec.g;
+  const int q[4] = {rec.q.x, rec.q.y, rec.q.z, rec.q.w};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    x.e[k] = __ldg(a.text + q[k]);
+    x.s[k] = __ldg(a.srcdo + (size_t)q[k] * ldo + col);
+    x.r[k] = upstream ? a.raddo[(size_t)q[k] * ldo + col] : 0.f;
   }
   x.e1 = __ldg(a.text + pt);
   x.s1 = __ldg(a.srcdo + (size_t)pt * ldo + col);
@@ -310,24 +339,91 @@ __device__ __forceinline__ Trace trace_regular(const SweepArgs &a, int b, int pt
   return t;
 }
 
-// Radiance of a regular point from its loaded trace inputs.
-__device__ __forceinline__ void reg_finish(const SweepArgs &a, const RegLoad &x, int b) {
-  Trace t = reg_trace(x, b, x.pt);
-  float rad = t.radsrc;
-  if (t.tr != 0.f) rad += t.tr * (t.f[0] * x.r[0] + t.f[1] * x.r[1] + t.f[2] * x.r[2] + t.f[3] * x.r[3]);
-  a.raddo[(size_t)x.pt * a.ldo + x.col] = rad;
+// Exit of a backward trace from (xe, ye, ze) through one cell of a 3D grid
+// (the geometry step of BACK_INT_GRID3D): the face's four corners, the next
+// cell, the path length and the bilinear face coordinates; the position is
+// advanced to the exit point.
+struct CellExit {
+  int i[4];
+  int nxt;
+  float so, u, v;
+};
+
+__device__ __forceinline__ CellExit cell_exit3d(const SweepArgs &a, int b, int cell, float &xe, float &ye, float &ze,
+                                                float cx, float cy, float cz, float cxinv, float cyinv, float czinv) {
+  CellExit c;
+  const int bitx = cx < 0.f, bity = cy < 0.f, bitz = cz < 0.f;
+  const int *g = a.gridptr + 8 * (size_t)cell;
+  const int cf = a.cellflags[cell];
+  const bool ipx = cf & 1, ipy = cf & 2;
+  const int iopp = g[7 - b];
+  float sox = ipx ? 1.0e20f : (a.gridpos[3 * iopp] - xe) * cxinv;
+  float soy = ipy ? 1.0e20f : (a.gridpos[3 * iopp + 1] - ye) * cyinv;
+  float soz = (a.gridpos[3 * iopp + 2] - ze) * czinv;
+  c.so = fminf(sox, fminf(soy, soz));
+  xe += c.so * cx; ye += c.so * cy; ze += c.so * cz;
+  int iface, jface;
+  if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; }
+  else if (soy <= soz) { iface = 3 - bity; jface = 1; }
+  else { iface = 5 - bitz; jface = 2; }
+  c.nxt = a.neighptr[6 * (size_t)cell + iface];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) c.i[k] = g[c_face[iface][k]];
+  const float *p1 = a.gridpos + 3 * c.i[0], *p2 = a.gridpos + 3 * c.i[1], *p3 = a.gridpos + 3 * c.i[2];
+  if (jface == 0) {
+    c.u = (ze - p1[2]) / (p3[2] - p1[2]);
+    c.v = ipy ? 0.5f : (ye - p1[1]) / (p2[1] - p1[1]);
+  } else if (jface == 1) {
+    c.u = (ze - p1[2]) / (p3[2] - p1[2]);
+    c.v = ipx ? 0.5f : (xe - p1[0]) / (p2[0] - p1[0]);
+  } else {
+    c.u = ipy ? 0.5f : (ye - p1[1]) / (p3[1] - p1[1]);
+    c.v = ipx ? 0.5f : (xe - p1[0]) / (p2[0] - p1[0]);
+  }
+  if (c.nxt >= 0) {
+    const float *q = a.gridpos + 3 * a.gridptr[8 * (size_t)c.nxt + b];
+    if (jface == 0) xe = q[0]; else if (jface == 1) ye = q[1]; else ze = q[2];
+  }
+  return c;
+}
+
+__device__ __forceinline__ IrrRec trace_geom1(const SweepArgs &a, int b, int cls, int pt, int col) {
+  IrrRec r;
+  r.q = make_int4(pt, pt, pt, pt);
+  r.g = make_float4(0.f, 0.f, 0.f, 0.f);
+  const int n = a.npts;
+  const int cell = a.start[(size_t)b * n + pt];
+  if (a.is1d || cell < 0 || a.transmin < 1.f) return r;
+  const float cx = a.col_cx[col], cy = a.col_cy[col], cz = a.col_cz[col];
+  const float cxinv = cx != 0.f ? 1.f / cx : 1.0e6f, cyinv = cy != 0.f ? 1.f / cy : 1.0e6f, czinv = 1.f / cz;
+  const int hb = (cz < 0.f) ? 2 : 1;
+  const int *rk = a.rank + (size_t)b * n, *lv = a.level + ((size_t)b * 4 + cls) * n;
+  const int rP = rk[pt], lP = lv[pt];
+  float xe = a.gridpos[3 * pt], ye = a.gridpos[3 * pt + 1], ze = a.gridpos[3 * pt + 2];
+  const CellExit c = cell_exit3d(a, b, cell, xe, ye, ze, cx, cy, cz, cxinv, cyinv, czinv);
+  bool valid = true;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int q = c.i[k];
+    valid = valid && ((a.bnd[q] & hb) || (rk[q] < rP && lv[q] < lP));
+  }
+  if (valid) {
+    r.q = make_int4(c.i[0], c.i[1], c.i[2], c.i[3]);
+    r.g = make_float4(c.so, c.u, c.v, 1.f);
+  }
+  return r;
 }
 
 // General trace (any point); with use_level the level of the ordinate's
 // face class must also precede the point's (level-synchronous execution).
 __device__ __forceinline__ Trace trace_general(const SweepArgs &a, int b, int cls, int pt, int col, bool use_level) {
   Trace t;
-  t.radsrc = 0.f; t.tr = 1.f; t.status = ERR_SWEEP_STEPS;
+  t.radsrc = 0.f; t.tr = 1.f; t.status = ERR_SWEEP_STEPS; t.u = 0.f; t.v = 0.f;
   t.q[0] = t.q[1] = t.q[2] = t.q[3] = pt; t.f[0] = t.f[1] = t.f[2] = t.f[3] = 0.f;
   const int ldo = a.ldo, n = a.npts;
   const float cx = a.col_cx[col], cy = a.col_cy[col], cz = a.col_cz[col];
   const float cxinv = cx != 0.f ? 1.f / cx : 1.0e6f, cyinv = cy != 0.f ? 1.f / cy : 1.0e6f, czinv = 1.f / cz;
-  const int bitx = cx < 0.f, bity = cy < 0.f, bitz = cz < 0.f;
+  const int bitz = cz < 0.f;
   const int hb = bitz ? 2 : 1;
   const int *rk = a.rank + (size_t)b * n, *lv = a.level + ((size_t)b * 4 + cls) * n;
   const int rP = rk[pt], lP = use_level ? lv[pt] : 0;
@@ -340,7 +436,7 @@ __device__ __forceinline__ Trace trace_general(const SweepArgs &a, int b, int cl
     if (cell < 0) break;
     const int *g = a.gridptr + 8 * (size_t)cell;
     int i1, i2, i3, i4, nxt;
-    float so, f1, f2, f3, f4;
+    float so, f1, f2, f3, f4, fu = 0.f, fv = 0.f;
     if (a.is1d) {
       int iopp = g[7 - b];
       so = (a.gridpos[3 * iopp + 2] - ze) * czinv;
@@ -351,36 +447,10 @@ __device__ __forceinline__ Trace trace_general(const SweepArgs &a, int b, int cl
       if (nxt >= 0) ze = a.gridpos[3 * a.gridptr[8 * (size_t)nxt + b] + 2];
       f1 = 1.f; f2 = f3 = f4 = 0.f;
     } else {
-      const int cf = a.cellflags[cell];
-      const bool ipx = cf & 1, ipy = cf & 2;
-      const int iopp = g[7 - b];
-      float sox = ipx ? 1.0e20f : (a.gridpos[3 * iopp] - xe) * cxinv;
-      float soy = ipy ? 1.0e20f : (a.gridpos[3 * iopp + 1] - ye) * cyinv;
-      float soz = (a.gridpos[3 * iopp + 2] - ze) * czinv;
-      so = fminf(sox, fminf(soy, soz));
-      xe += so * cx; ye += so * cy; ze += so * cz;
-      int iface, jface;
-      if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; }
-      else if (soy <= soz) { iface = 3 - bity; jface = 1; }
-      else { iface = 5 - bitz; jface = 2; }
-      nxt = a.neighptr[6 * (size_t)cell + iface];
-      i1 = g[c_face[iface][0]]; i2 = g[c_face[iface][1]]; i3 = g[c_face[iface][2]]; i4 = g[c_face[iface][3]];
-      const float *p1 = a.gridpos + 3 * i1, *p2 = a.gridpos + 3 * i2, *p3 = a.gridpos + 3 * i3;
-      float u, v;
-      if (jface == 0) {
-        u = (ze - p1[2]) / (p3[2] - p1[2]);
-        v = ipy ? 0.5f : (ye - p1[1]) / (p2[1] - p1[1]);
-      } else if (jface == 1) {
-        u = (ze - p1[2]) / (p3[2] - p1[2]);
-        v = ipx ? 0.5f : (xe - p1[0]) / (p2[0] - p1[0]);
-      } else {
-        u = ipy ? 0.5f : (ye - p1[1]) / (p3[1] - p1[1]);
-        v = ipx ? 0.5f : (xe - p1[0]) / (p2[0] - p1[0]);
-      }
-      if (nxt >= 0) {
-        const float *q = a.gridpos + 3 * a.gridptr[8 * (size_t)nxt + b];
-        if (jface == 0) xe = q[0]; else if (jface == 1) ye = q[1]; else ze = q[2];
-      }
+      const CellExit c = cell_exit3d(a, b, cell, xe, ye, ze, cx, cy, cz, cxinv, cyinv, czinv);
+      i1 = c.i[0]; i2 = c.i[1]; i3 = c.i[2]; i4 = c.i[3]; nxt = c.nxt; so = c.so;
+      const float u = c.u, v = c.v;
+      fu = u; fv = v;
       f1 = (1.f - u) * (1.f - v); f2 = (1.f - u) * v; f3 = u * (1.f - v); f4 = u * v;
     }
     const float e1 = a.text[i1], e2 = a.text[i2], e3 = a.text[i3], e4 = a.text[i4];
@@ -397,6 +467,7 @@ __device__ __forceinline__ Trace trace_general(const SweepArgs &a, int b, int cl
       t.radsrc = rad; t.tr = tr;
       t.q[0] = i1; t.q[1] = i2; t.q[2] = i3; t.q[3] = i4;
       t.f[0] = f1; t.f[1] = f2; t.f[2] = f3; t.f[3] = f4;
+      t.u = fu; t.v = fv;
       t.status = valid ? ERR_NONE : ERR_SWEEP_NOFACE;
       if (!valid) t.tr = 0.f;
       return t;
@@ -412,75 +483,207 @@ __device__ __forceinline__ Trace trace_point(const SweepArgs &a, int b, int pt, 
   return trace_general(a, b, 3, pt, col, false);
 }
 
-__device__ __forceinline__ void general_item(const SweepArgs &a, int b, int cls, int pt, int col) {
-  Trace t = trace_general(a, b, cls, pt, col, true);
-  if (t.status != ERR_NONE) atomicCAS(a.err, ERR_NONE, t.status);
-  float rad = t.radsrc;
-  const int ldo = a.ldo;
-  if (t.tr != 0.f)
-    rad += t.tr * (t.f[0] * a.raddo[(size_t)t.q[0] * ldo + col] + t.f[1] * a.raddo[(size_t)t.q[1] * ldo + col] +
-                   t.f[2] * a.raddo[(size_t)t.q[2] * ldo + col] + t.f[3] * a.raddo[(size_t)t.q[3] * ldo + col]);
-  a.raddo[(size_t)pt * ldo + col] = rad;
-}
-
-// Level-synchronous sweep.  A level's work is a list of segments (octant,
-// face class, regular or not); its items (task x column of the class) are
-// numbered consecutively and strided over the threads; consecutive threads
-// take consecutive columns of one point.  Regular items are taken two at a
-// time with all reads of both issued before either is combined.
+// Level-synchronous sweep of one hemisphere in three parts.
+//
+// Every trace gives rad(P) = radsrc + tr * sum_k f_k rad(q_k), and radsrc, tr
+// depend on the source function only.
+//  * Phase 1 (k_sweep_p1, one block per (octant, face class) group, on a
+//    second stream): the general-trace points whose dependencies are all
+//    preset or phase-1 points -- on open boundaries the edge-cell planes,
+//    whose traces stay in the plane.  Levels are separated by block
+//    barriers.
+//  * Source pass (k_sweep_prep, point-major, concurrent with phase 1):
+//    (radsrc, tr) of every phase-2 item into w[point][column].
+//  * Phase 2 (k_sweep_levels, cooperative): the remaining levels; per item
+//    one read of the point index, then (radsrc, tr) and the four upstream
+//    radiances, then the combine.  Phase-1 values count as level 0 here.
+// A level's items (task x column of a face class) are numbered
+// consecutively (Seg::start); consecutive threads take consecutive columns
+// of one point.
 constexpr int MAXSEG = 32;
 
-__device__ __forceinline__ int seg_item(const Seg *sg, int nseg, int i, int &si, const SweepArgs &a, int &pt,
-                                        int &col) {
+// Locates item j of a table of general-trace items: segs sorted by irr0,
+// the segment with the largest irr0 <= j.
+__device__ __forceinline__ int irr_seg_find(const Seg *__restrict__ segs, int nseg, int j) {
+  int lo = 0, hi = nseg - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (segs[mid].irr0 <= j) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Source pass, regular phase-2 items, one thread per (point, column).
+__global__ void __launch_bounds__(256) k_sweep_prep(SweepArgs a, const uint8_t *__restrict__ kind,
+                                                    const int *__restrict__ col_oct, const int *__restrict__ col_cls,
+                                                    int c0, int nc, float2 *__restrict__ w) {
+  const int total = a.npts * nc;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+    const int pt = idx / nc, col = c0 + (idx - pt * nc);
+    if (__ldg(a.col_cz + col) == 0.f) continue;  // padding ordinate
+    const int b = __ldg(col_oct + col) - 1, cls = __ldg(col_cls + col);
+    if (__ldg(kind + ((size_t)b * 4 + cls) * a.npts + pt) != 1) continue;
+    RegLoad x;
+    reg_load(a, b, pt, col, x, false);
+    const Trace t = reg_trace(x, b, pt);
+    w[(size_t)pt * a.ldo + col] = make_float2(t.radsrc, t.tr);
+  }
+}
+
+// Source pass, general phase-2 items (irr table entries [j0, j0 + n)); a
+// trace that needs the cell walk also stores its final face.
+__global__ void __launch_bounds__(256) k_sweep_prep_irr(SweepArgs a, const Seg *__restrict__ segs, int nseg, int j0,
+                                                        int n, float2 *__restrict__ w, IrrRec *__restrict__ irr) {
+  for (int jj = blockIdx.x * blockDim.x + threadIdx.x; jj < n; jj += gridDim.x * blockDim.x) {
+    const int j = j0 + jj;
+    const Seg g = segs[irr_seg_find(segs, nseg, j)];
+    const int li = j - g.irr0, task = li / g.ncol, slot = li - task * g.ncol;
+    const int pt = (int)__ldg(a.tasks + g.t0 + task), col = g.col0 + slot;
+    const IrrRec rec = irr[j];
+    float2 out;
+    if (rec.g.w > 0.5f) {
+      RegLoad x;
+      rec_load(a, rec, pt, col, x, false);
+      const Trace t = reg_trace(x, g.b, pt);
+      out = make_float2(t.radsrc, t.tr);
+    } else {
+      const Trace t = trace_general(a, g.b, g.cls, pt, col, true);
+      if (t.status != ERR_NONE) atomicCAS(a.err, ERR_NONE, t.status);
+      out = make_float2(t.radsrc, t.tr);
+      IrrRec r;
+      r.q = make_int4(t.q[0], t.q[1], t.q[2], t.q[3]);
+      r.g = make_float4(0.f, t.u, t.v, 0.f);
+      irr[j] = r;
+    }
+    w[(size_t)pt * a.ldo + col] = out;
+  }
+}
+
+// Stored first-face records of all general-trace items of a hemisphere.
+__global__ void __launch_bounds__(256) k_irr_build(SweepArgs a, const Seg *__restrict__ segs, int nseg, int nirr,
+                                                   IrrRec *__restrict__ out) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nirr; j += gridDim.x * blockDim.x) {
+    const Seg g = segs[irr_seg_find(segs, nseg, j)];
+    const int li = j - g.irr0, task = li / g.ncol, slot = li - task * g.ncol;
+    const int pt = (int)a.tasks[g.t0 + task];
+    out[j] = trace_geom1(a, g.b, g.cls, pt, g.col0 + slot);
+  }
+}
+
+// Phase 1: block g sweeps the levels of its group with block barriers.
+constexpr int P1_THREADS = 1024;
+
+__global__ void __launch_bounds__(P1_THREADS) k_sweep_p1(SweepArgs a, const Seg *__restrict__ p1segs,
+                                                         const int *__restrict__ p1off) {
+  const int s0 = p1off[blockIdx.x], s1 = p1off[blockIdx.x + 1];
+  for (int si = s0; si < s1; ++si) {
+    const Seg g = p1segs[si];
+    const int items = g.ntask * g.ncol;
+    for (int i = threadIdx.x; i < items; i += blockDim.x) {
+      const int task = i / g.ncol, slot = i - task * g.ncol;
+      const int pt = (int)__ldg(a.tasks + g.t0 + task), col = g.col0 + slot;
+      const IrrRec rec = a.irr[g.irr0 + i];
+      float rad;
+      if (rec.g.w > 0.5f) {
+        RegLoad x;
+        rec_load(a, rec, pt, col, x, true);
+        const Trace t = reg_trace(x, g.b, pt);
+        rad = t.radsrc;
+        if (t.tr != 0.f) rad += t.tr * (t.f[0] * x.r[0] + t.f[1] * x.r[1] + t.f[2] * x.r[2] + t.f[3] * x.r[3]);
+      } else {
+        const Trace t = trace_general(a, g.b, g.cls, pt, col, true);
+        if (t.status != ERR_NONE) atomicCAS(a.err, ERR_NONE, t.status);
+        const int ldo = a.ldo;
+        rad = t.radsrc;
+        if (t.tr != 0.f)
+          rad += t.tr * (t.f[0] * a.raddo[(size_t)t.q[0] * ldo + col] + t.f[1] * a.raddo[(size_t)t.q[1] * ldo + col] +
+                         t.f[2] * a.raddo[(size_t)t.q[2] * ldo + col] + t.f[3] * a.raddo[(size_t)t.q[3] * ldo + col]);
+      }
+      a.raddo[(size_t)pt * a.ldo + col] = rad;
+    }
+    __syncthreads();
+  }
+}
+
+// Phase 2, one item: point, (radsrc, tr), face corners and weights, then the
+// four upstream radiances.
+struct LevelItem {
+  float2 w;
+  float u, v;
+  int pt, col, q[4];
+};
+
+__device__ __forceinline__ void level_load(const SweepArgs &a, const Seg &g, int li, const float2 *__restrict__ w,
+                                           LevelItem &x, float r[4]) {
+  const int task = li / g.ncol, slot = li - task * g.ncol;
+  x.col = g.col0 + slot;
+  x.pt = (int)__ldg(a.tasks + g.t0 + task);
+  x.w = w[(size_t)x.pt * a.ldo + x.col];
+  if (g.regular) {
+    const int b = g.b, iz = x.pt % a.nz, layer = (b & 4) ? iz - 1 : iz;
+    const float4 geo = __ldg(reinterpret_cast<const float4 *>(a.geo) + (size_t)layer * a.nang + x.col);
+    x.u = geo.y; x.v = geo.z;
+    const int iface = (g.cls < 3) ? 2 * g.cls + 1 - ((b >> g.cls) & 1) : (int)geo.w;
+    const int ox = (b & 1) ? -a.nz * a.ny1 : a.nz * a.ny1, oy = (b & 2) ? -a.nz : a.nz, oz = (b & 4) ? -1 : 1;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int d = c_face[iface][k] ^ b;
+      x.q[k] = x.pt + ((d & 1) ? ox : 0) + ((d & 2) ? oy : 0) + ((d & 4) ? oz : 0);
+    }
+  } else {
+    const IrrRec rec = a.irr[g.irr0 + li];
+    x.q[0] = rec.q.x; x.q[1] = rec.q.y; x.q[2] = rec.q.z; x.q[3] = rec.q.w;
+    x.u = rec.g.y; x.v = rec.g.z;
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) r[k] = a.raddo[(size_t)x.q[k] * a.ldo + x.col];
+}
+
+__device__ __forceinline__ void level_finish(const SweepArgs &a, const LevelItem &x, const float r[4]) {
+  const float u = x.u, v = x.v;
+  const float f0 = (1.f - u) * (1.f - v), f1 = (1.f - u) * v, f2 = u * (1.f - v), f3 = u * v;
+  float rad = x.w.x;
+  if (x.w.y != 0.f) rad += x.w.y * (f0 * r[0] + f1 * r[1] + f2 * r[2] + f3 * r[3]);
+  a.raddo[(size_t)x.pt * a.ldo + x.col] = rad;
+}
+
+__device__ __forceinline__ int seg_find(const Seg *sg, int nseg, int i, int si) {
   while (si + 1 < nseg && i >= sg[si + 1].start) ++si;
-  const Seg &s = sg[si];
-  const int li = i - s.start, task = li / s.ncol, slot = li - task * s.ncol;
-  pt = (int)__ldg(a.tasks + s.t0 + task);
-  col = s.col0 + slot;
   return si;
 }
 
-__device__ __forceinline__ void sweep_level(const SweepArgs &a, const Seg *sg, int nseg, int items, int gtid,
-                                            int gstride) {
+__device__ __forceinline__ void sweep_level(const SweepArgs &a, const Seg *sg, int nseg, int items,
+                                            const float2 *__restrict__ w, int gtid, int gstride) {
   int si = 0;
   for (int i = gtid; i < items; i += 2 * gstride) {
-    int pt1, col1, pt2 = 0, col2 = 0;
-    const int s1 = seg_item(sg, nseg, i, si, a, pt1, col1);
-    const bool two = i + gstride < items;
-    int sj = si;
-    const int s2 = two ? seg_item(sg, nseg, i + gstride, sj, a, pt2, col2) : s1;
-    const Seg &g1 = sg[s1], &g2 = sg[s2];
-    if (g1.regular && two && g2.regular) {
-      RegLoad x1, x2;
-      reg_load(a, g1.b, pt1, col1, x1, true);
-      reg_load(a, g2.b, pt2, col2, x2, true);
-      reg_finish(a, x1, g1.b);
-      reg_finish(a, x2, g2.b);
-    } else {
-      if (g1.regular) { RegLoad x1; reg_load(a, g1.b, pt1, col1, x1, true); reg_finish(a, x1, g1.b); }
-      else general_item(a, g1.b, g1.cls, pt1, col1);
-      if (two) {
-        if (g2.regular) { RegLoad x2; reg_load(a, g2.b, pt2, col2, x2, true); reg_finish(a, x2, g2.b); }
-        else general_item(a, g2.b, g2.cls, pt2, col2);
-      }
-    }
+    const int i2 = i + gstride;
+    si = seg_find(sg, nseg, i, si);
+    const int sj = i2 < items ? seg_find(sg, nseg, i2, si) : si;
+    LevelItem x1, x2;
+    float r1[4], r2[4];
+    level_load(a, sg[si], i - sg[si].start, w, x1, r1);
+    if (i2 < items) level_load(a, sg[sj], i2 - sg[sj].start, w, x2, r2);
+    level_finish(a, x1, r1);
+    if (i2 < items) level_finish(a, x2, r2);
     si = sj;
   }
 }
 
-// One launch per level (used when a cooperative launch is not available).
-__global__ void __launch_bounds__(256) k_sweep(SweepArgs a, const Seg *__restrict__ segs, int nseg, int items) {
+// One launch per phase-2 level (used when a cooperative launch is not available).
+__global__ void __launch_bounds__(256) k_sweep(SweepArgs a, const Seg *__restrict__ segs, int nseg, int items,
+                                               const float2 *__restrict__ w) {
   __shared__ Seg sg[MAXSEG];
   for (int t = threadIdx.x; t < nseg; t += blockDim.x) sg[t] = segs[t];
   __syncthreads();
-  sweep_level(a, sg, nseg, items, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+  sweep_level(a, sg, nseg, items, w, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
-// All levels of one hemisphere in one cooperative launch: the blocks share
-// out the items of a level, then meet at a grid barrier.
+// All phase-2 levels of one hemisphere in one cooperative launch: the blocks
+// share out the items of a level, then meet at a grid barrier.
 __global__ void __launch_bounds__(256) k_sweep_levels(SweepArgs a, const Seg *__restrict__ segs,
                                                       const int *__restrict__ seg_off,
-                                                      const int *__restrict__ level_items, int nlev) {
+                                                      const int *__restrict__ level_items,
+                                                      const float2 *__restrict__ w, int nlev) {
   cooperative_groups::grid_group grid = cooperative_groups::this_grid();
   __shared__ Seg sg[MAXSEG];
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
@@ -488,7 +691,7 @@ __global__ void __launch_bounds__(256) k_sweep_levels(SweepArgs a, const Seg *__
     const int s0 = seg_off[l], ns = seg_off[l + 1] - s0;
     for (int t = threadIdx.x; t < ns; t += blockDim.x) sg[t] = segs[s0 + t];
     __syncthreads();
-    sweep_level(a, sg, ns, level_items[l], gtid, gstride);
+    sweep_level(a, sg, ns, level_items[l], w, gtid, gstride);
     grid.sync();
   }
 }
@@ -505,6 +708,7 @@ __global__ void __launch_bounds__(SEQW) k_sweep_seq(SweepArgs a, const int *orde
   __shared__ float sval[SEQW];
   __shared__ int sdone[SEQW];
   const int col = col_begin + blockIdx.x, ldo = a.ldo, n = a.npts;
+  if (a.col_cz[col] == 0.f) return;  // padding ordinate
   int b = 0;
   for (int k = 0; k < 8; ++k)
     if (a.oct_ncol[k] > 0 && col >= a.oct_col0[k] && col < a.oct_col0[k] + a.oct_ncol[k]) b = k;
@@ -1066,8 +1270,14 @@ struct Handle {
   DBuf<uint8_t> bnd, regular;
   DBuf<float> geo;
   DBuf<uint32_t> tasks[2];
-  DBuf<Seg> segs[2];
-  DBuf<int> seg_off[2], level_items[2];
+  DBuf<Seg> segs[2], p1segs[2], irrsegs[2];
+  DBuf<int> seg_off[2], level_items[2], p1off[2], col_oct, col_cls;
+  DBuf<uint8_t> kind;
+  DBuf<IrrRec> irr[2];
+  DBuf<float2> sweepw;  // (radsrc, tr) of the phase-2 items, [npts][ldo]
+  int n_irrseg[2] = {0, 0}, p2_irrseg0[2] = {0, 0}, p2_irr_j0[2] = {0, 0};
+  cudaStream_t stream2 = nullptr;  // phase-1 sweeps, concurrent with the source pass
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int coop_blocks = 0;
   DBuf<float> col_cx, col_cy, col_cz, col_fluxw, cmu1t, cmu2t, cphi1t, cphi2, ylmsun;
   DBuf<int> nphi0, col_of;
@@ -1230,7 +1440,9 @@ static long long plan_device_bytes(const Plan &P) {
   b += vbytes(P.gridpos) + vbytes(P.xgrid) + vbytes(P.ygrid) + vbytes(P.zgrid) + vbytes(P.gridptr) + vbytes(P.neighptr);
   b += vbytes(P.cellflags) + vbytes(P.rank) + vbytes(P.startcell) + vbytes(P.level) + vbytes(P.rank);  // + order
   b += vbytes(P.topp) + vbytes(P.botp) + 4LL * P.npts + vbytes(P.lofj) + vbytes(P.bnd) + vbytes(P.regular) + vbytes(P.geo);
-  for (int h = 0; h < 2; ++h) b += vbytes(P.tasks[h]) + vbytes(P.segs[h]) + vbytes(P.seg_off[h]) + vbytes(P.level_items[h]);
+  for (int h = 0; h < 2; ++h)
+    b += vbytes(P.tasks[h]) + vbytes(P.segs[h]) + vbytes(P.seg_off[h]) + vbytes(P.level_items[h]) + 32LL * P.nirr[h];
+  b += 8LL * P.npts * ((P.nang + 3) & ~3) + vbytes(P.kind);  // (radsrc, tr) per point and ordinate
   b += 4LL * 5 * P.nang + vbytes(P.cmu1) + vbytes(P.cmu2) + vbytes(P.cphi1) + vbytes(P.cphi2) + vbytes(P.ylmsun);
   b += vbytes(P.nphi0) + vbytes(P.col_of) + vbytes(P.total_ext) + vbytes(P.dirflux) + vbytes(P.coef) + vbytes(P.tms_ptr);
   b += vbytes(P.tms_iph) + vbytes(P.tms_w) + vbytes(P.phasetab) + vbytes(P.botalb) + vbytes(P.rad0);
@@ -1244,7 +1456,7 @@ static long long plan_device_bytes(const Plan &P) {
 
 static void fill_sizes(const Plan &P, shdom_sizes *o) {
   o->npts = P.npts; o->ncells = P.ncells; o->nx1 = P.nx1; o->ny1 = P.ny1; o->nz = P.nz; o->nlm = P.nlm;
-  o->nmu = P.nmu; o->nang = P.nang; o->ml = P.ml; o->mm = P.mm; o->bcflag = P.bcflag; o->ipflag = P.ipflag;
+  o->nmu = P.nmu; o->nang = P.nang_real; o->ml = P.ml; o->mm = P.mm; o->bcflag = P.bcflag; o->ipflag = P.ipflag;
   o->albmax = P.albmax;
   o->nlevels_down = (int)P.seg_off[0].size() - 1;
   o->nlevels_up = (int)P.seg_off[1].size() - 1;
@@ -1267,7 +1479,7 @@ static void upload_plan(Handle &H) {
   }
   for (int h = 0; h < 2; ++h) {
     int nlev = (int)P.seg_off[h].size() - 1;
-    H.seq[h] = nlev > 4 * (P.nx1 + P.ny1 + P.nz) + 64;
+    H.seq[h] = std::max(nlev, P.p1depth[h]) > 4 * (P.nx1 + P.ny1 + P.nz) + 64;
     for (int l = 0; l < nlev; ++l)
       if (P.seg_off[h][l + 1] - P.seg_off[h][l] > MAXSEG) throw std::runtime_error("sweep schedule: too many segments in a level");
   }
@@ -1279,6 +1491,20 @@ static void upload_plan(Handle &H) {
   for (int h = 0; h < 2; ++h) {
     H.tasks[h].upload(P.tasks[h]); H.segs[h].upload(P.segs[h]);
     H.seg_off[h].upload(P.seg_off[h]); H.level_items[h].upload(P.level_items[h]);
+    H.p1segs[h].upload(P.p1segs[h]); H.p1off[h].upload(P.p1off[h]);
+    // general-trace segments of both phases in irr0 order
+    std::vector<Seg> is(P.p1segs[h]);
+    H.p2_irrseg0[h] = (int)is.size();
+    H.p2_irr_j0[h] = 0;
+    for (const Seg &g : P.p1segs[h]) H.p2_irr_j0[h] = std::max(H.p2_irr_j0[h], g.irr0 + g.ntask * g.ncol);
+    for (const Seg &g : P.segs[h]) if (!g.regular) is.push_back(g);
+    H.n_irrseg[h] = (int)is.size();
+    H.irrsegs[h].upload(is);
+  }
+  H.kind.upload(P.kind);
+  {
+    std::vector<int> cls(P.col_cls.begin(), P.col_cls.end());
+    H.col_oct.upload(P.col_oct); H.col_cls.upload(cls);
   }
   {
     int dev = 0, nsm = 0, per = 0, coop = 0;
@@ -1379,7 +1605,7 @@ static void transform(Handle &H, int dir) {
   else transforms_launch<32>(H, dir);
 }
 
-static void sweep_hemisphere(Handle &H, int hemi) {
+static SweepArgs sweep_args(Handle &H, int hemi) {
   Plan &P = H.P;
   SweepArgs a;
   a.gridpos = H.gridpos.p; a.gridptr = H.gridptr.p; a.neighptr = H.neighptr.p; a.cellflags = H.cellflags.p;
@@ -1388,7 +1614,39 @@ static void sweep_hemisphere(Handle &H, int hemi) {
   a.tasks = H.tasks[hemi].p; a.err = H.errflag.p; a.npts = P.npts; a.nang = P.nang; a.ldo = H.ldo; a.is1d = P.is1d;
   a.regular = H.regular.p; a.geo = H.geo.p; a.nz = P.nz; a.ny1 = P.ny1;
   a.transmin = P.prob.transmin;
+  a.irr = H.irr[hemi].p;
   for (int b = 0; b < 8; ++b) { a.oct_col0[b] = P.oct_col0[b]; a.oct_ncol[b] = P.oct_ncol[b]; }
+  return a;
+}
+
+// Stored single-cell general traces of both hemispheres (once per handle;
+// they depend on the geometry and the sweep schedule only).
+static void build_irr(Handle &H) {
+  Plan &P = H.P;
+  for (int h = 0; h < 2; ++h) {
+    H.irr[h].alloc((size_t)std::max<long long>(P.nirr[h], 1));
+    if (P.nirr[h] == 0 || H.n_irrseg[h] == 0 || H.seq[h]) continue;
+    SweepArgs a = sweep_args(H, h);
+    const int nirr = (int)P.nirr[h];
+    const int blocks = std::min((nirr + 255) / 256, 152 * 16);
+    k_irr_build<<<blocks, 256, 0, H.stream>>>(a, H.irrsegs[h].p, H.n_irrseg[h], nirr, H.irr[h].p);
+    CK(cudaGetLastError());
+    H.launches += 1;
+  }
+  CK(cudaStreamSynchronize(H.stream));
+  H.sweepw.alloc((size_t)P.npts * H.ldo);
+  {  // phase 1 runs on a high-priority stream so its blocks start before the source pass fills the SMs
+    int lo = 0, hi = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    CK(cudaStreamCreateWithPriority(&H.stream2, cudaStreamNonBlocking, hi));
+  }
+  CK(cudaEventCreateWithFlags(&H.ev_fork, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&H.ev_join, cudaEventDisableTiming));
+}
+
+static void sweep_hemisphere(Handle &H, int hemi) {
+  Plan &P = H.P;
+  SweepArgs a = sweep_args(H, hemi);
   if (H.seq[hemi]) {
     int c0 = hemi ? P.ncol_down : 0, nc = hemi ? P.nang - P.ncol_down : P.ncol_down;
     if (nc > 0) k_sweep_seq<<<nc, SEQW, 0, H.stream>>>(a, H.order.p, c0);
@@ -1397,12 +1655,41 @@ static void sweep_hemisphere(Handle &H, int hemi) {
   }
   const std::vector<int> &off = P.seg_off[hemi];
   const int nlev = (int)off.size() - 1;
+  // phase 1 on the second stream, after everything queued so far
+  const int ng1 = (int)P.p1off[hemi].size() - 1;
+  if (ng1 > 0) {
+    CK(cudaEventRecord(H.ev_fork, H.stream));
+    CK(cudaStreamWaitEvent(H.stream2, H.ev_fork, 0));
+    k_sweep_p1<<<ng1, P1_THREADS, 0, H.stream2>>>(a, H.p1segs[hemi].p, H.p1off[hemi].p);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(H.ev_join, H.stream2));
+    H.launches += 1;
+  }
+  // source pass of the phase-2 items
+  if (nlev > 0) {
+    const int c0 = hemi ? P.ncol_down : 0, nc = hemi ? P.nang - P.ncol_down : P.ncol_down;
+    const long long total = (long long)P.npts * nc;
+    const int blocks = (int)std::min<long long>((total + 255) / 256, 152 * 16);
+    k_sweep_prep<<<blocks, 256, 0, H.stream>>>(a, H.kind.p, H.col_oct.p, H.col_cls.p, c0, nc, H.sweepw.p);
+    CK(cudaGetLastError());
+    H.launches += 1;
+    const int n2 = (int)P.nirr[hemi] - H.p2_irr_j0[hemi];
+    if (n2 > 0) {
+      const int b2 = std::min((n2 + 255) / 256, 152 * 16);
+      k_sweep_prep_irr<<<b2, 256, 0, H.stream>>>(a, H.irrsegs[hemi].p, H.n_irrseg[hemi], H.p2_irr_j0[hemi], n2,
+                                                   H.sweepw.p, H.irr[hemi].p);
+      CK(cudaGetLastError());
+      H.launches += 1;
+    }
+  }
+  if (ng1 > 0) CK(cudaStreamWaitEvent(H.stream, H.ev_join, 0));
   if (nlev <= 0) return;
   if (H.coop_blocks > 0) {
     const Seg *sp = H.segs[hemi].p;
     const int *so = H.seg_off[hemi].p, *li = H.level_items[hemi].p;
+    const float2 *wp = H.sweepw.p;
     int nl = nlev;
-    void *args[] = {&a, (void *)&sp, (void *)&so, (void *)&li, &nl};
+    void *args[] = {&a, (void *)&sp, (void *)&so, (void *)&li, (void *)&wp, &nl};
     CK(cudaLaunchCooperativeKernel((const void *)k_sweep_levels, dim3(H.coop_blocks), dim3(256), args, 0, H.stream));
     H.launches += 1;
     return;
@@ -1411,7 +1698,7 @@ static void sweep_hemisphere(Handle &H, int hemi) {
     const int items = P.level_items[hemi][l];
     if (items <= 0) continue;
     int blocks = std::min((items + 511) / 512, 152 * 8);
-    k_sweep<<<blocks, 256, 0, H.stream>>>(a, H.segs[hemi].p + off[l], off[l + 1] - off[l], items);
+    k_sweep<<<blocks, 256, 0, H.stream>>>(a, H.segs[hemi].p + off[l], off[l + 1] - off[l], items, H.sweepw.p);
     H.launches += 1;
   }
   CK(cudaGetLastError());
@@ -1460,6 +1747,7 @@ int shdom_create(const shdom_problem *problem, int device, shdom_handle **out) {
     CK(cudaStreamCreateWithFlags(&H->h.stream, cudaStreamNonBlocking));
     shdom::upload_plan(H->h);
     CK(cudaMemset(H->h.errflag.p, 0, sizeof(int)));
+    shdom::build_irr(H->h);
   } catch (const std::exception &e) {
     return fail(nullptr, e.what());
   }
@@ -1692,6 +1980,9 @@ const char *shdom_last_error(shdom_handle *hh) { return hh ? hh->h.err.c_str() :
 void shdom_destroy(shdom_handle *hh) {
   if (!hh) return;
   if (hh->h.stream) cudaStreamDestroy(hh->h.stream);
+  if (hh->h.stream2) cudaStreamDestroy(hh->h.stream2);
+  if (hh->h.ev_fork) cudaEventDestroy(hh->h.ev_fork);
+  if (hh->h.ev_join) cudaEventDestroy(hh->h.ev_join);
   delete hh;
 }
 

@@ -325,6 +325,11 @@ int regular_exit(float cx, float cy, float cz, int b, float dx, float dy, float 
   return iface;
 }
 
+// Padding ordinates per (octant, class) group (0: groups packed).  The
+// device code handles padding ordinates (zero direction and weight) in
+// every kernel, so the layout can be changed here alone.
+constexpr int kColumnPad = 0;
+
 void build_angles(const shdom_problem &p, Plan &P) {
   P.nmu = std::max(2, 2 * ((p.nmu + 1) / 2));
   P.nphi = std::max(1, p.nphi);
@@ -402,13 +407,24 @@ void build_angles(const shdom_problem &p, Plan &P) {
             P.col_imu.push_back(j); P.col_iphi.push_back(q); P.col_oct.push_back(ioct); P.col_cls.push_back(cls);
           }
         P.cls_ncol[ioct - 1][cls] = col - P.cls_col0[ioct - 1][cls];
+        // (Padding each group to whole 32-byte sectors was measured: fewer
+        // partly written sectors in the sweep, but 24% wider transforms; a
+        // net loss at NMU=16, so the groups are packed.)
+        for (int pad = 0; pad < kColumnPad && P.cls_ncol[ioct - 1][cls] > 0 && (col - P.cls_col0[ioct - 1][cls]) % 8 != 0; ++pad) {
+          ++col;
+          P.col_imu.push_back(-1); P.col_iphi.push_back(-1); P.col_oct.push_back(ioct); P.col_cls.push_back(cls);
+        }
       }
       P.oct_ncol[ioct - 1] = col - P.oct_col0[ioct - 1];
     }
   }
-  P.col_cx.resize(P.nang); P.col_cy.resize(P.nang); P.col_cz.resize(P.nang); P.col_fluxw.resize(P.nang);
+  P.nang_real = P.nang;
+  P.nang = col;  // columns including the padding ordinates
+  P.col_cx.assign(P.nang, 0.f); P.col_cy.assign(P.nang, 0.f); P.col_cz.assign(P.nang, 0.f);
+  P.col_fluxw.assign(P.nang, 0.f);
   for (int c = 0; c < P.nang; ++c) {
     int j = P.col_imu[c], q = P.col_iphi[c];
+    if (j < 0) continue;  // padding: zero direction and weight
     double cx, cy, cz;
     trace_dir(P.mu[j], P.phi[(size_t)j * P.nphi0max + q], cx, cy, cz);
     P.col_cx[c] = (float)cx; P.col_cy[c] = (float)cy; P.col_cz[c] = (float)cz;
@@ -825,6 +841,7 @@ bool build_schedule(const shdom_problem &p, Plan &P) {
   P.rank.assign((size_t)8 * n, -1);
   P.startcell.assign((size_t)8 * n, -1);
   P.level.assign((size_t)32 * n, 0);
+  P.kind.assign((size_t)32 * n, 0);
   P.regular.assign((size_t)8 * n, 0);
   std::vector<int> octs = P.is1d ? std::vector<int>{1, 5} : std::vector<int>{1, 2, 3, 4, 5, 6, 7, 8};
   const double transmin = p.transmin;
@@ -838,7 +855,7 @@ bool build_schedule(const shdom_problem &p, Plan &P) {
       const int hemi_bnd = (b & 4) ? 2 : 1;  // trace down: bottom points preset
       const int *rk = &P.rank[(size_t)b * n];
       const int *sc = &P.startcell[(size_t)b * n];
-      std::vector<int> order(n);
+      std::vector<int> order(n), corners;
       for (int i = 0; i < n; ++i) order[rk[i]] = i;
       for (int r = 0; r < n; ++r) {
         int pt = order[r];
@@ -856,15 +873,16 @@ bool build_schedule(const shdom_problem &p, Plan &P) {
           const int nc = P.cls_ncol[b][cls], c0 = P.cls_col0[b][cls];
           if (nc == 0) continue;
           int *lv = &P.level[((size_t)b * 4 + cls) * n];
-          int lvl = 0;
+          uint8_t *kd = &P.kind[((size_t)b * 4 + cls) * n];
+          // the corners the point's traces for this class end on
+          corners.clear();
           if (fast) {
-            // corners of the class's exit face (all seven for class 3)
             if (cls < 3) {
-              const int bit = (cls == 0) ? (b & 1) : (cls == 1) ? ((b >> 1) & 1) : ((b >> 2) & 1);
+              const int bit = (b >> cls) & 1;
               const int iface = 2 * cls + 1 - bit;
-              for (int k = 0; k < 4; ++k) lvl = std::max(lvl, lv[g[kFace[iface][k]]]);
+              for (int k = 0; k < 4; ++k) corners.push_back(g[kFace[iface][k]]);
             } else {
-              for (int k = 0; k < 8; ++k) if (k != b) lvl = std::max(lvl, lv[g[k]]);
+              for (int k = 0; k < 8; ++k) if (k != b) corners.push_back(g[k]);
             }
           } else {
             for (int c = c0; c < c0 + nc; ++c) {
@@ -875,10 +893,25 @@ bool build_schedule(const shdom_problem &p, Plan &P) {
                 errs[b] = "sweep planning: trace found no valid face (BACK_INT_GRID: INEXTCELL=0)";
                 return;
               }
-              for (int k = 0; k < 4; ++k) lvl = std::max(lvl, lv[f[k]]);
+              for (int k = 0; k < 4; ++k) corners.push_back(f[k]);
             }
           }
-          lv[pt] = lvl + 1;
+          // A general-trace point whose corners are all preset or phase-1
+          // points is a phase-1 point (boundary-plane chains); any other
+          // point is phase 2, where phase-1 corners count as level 0.
+          bool one = !fast;
+          int m1 = 0, m2 = 0;
+          for (int q : corners) {
+            if (P.bnd[q] & hemi_bnd) continue;
+            if (kd[q] == 3) m1 = std::max(m1, lv[q]);
+            else { one = false; m2 = std::max(m2, lv[q] - Plan::kPhase2); }
+          }
+          if (one) { kd[pt] = 3; lv[pt] = m1 + 1; }
+          else { kd[pt] = fast ? 1 : 2; lv[pt] = Plan::kPhase2 + m2 + 1; }
+          if (lv[pt] >= 2 * Plan::kPhase2 - 1 || (one && lv[pt] >= Plan::kPhase2)) {
+            errs[b] = "sweep planning: wavefront too deep";
+            return;
+          }
         }
       }
     });
@@ -886,62 +919,96 @@ bool build_schedule(const shdom_problem &p, Plan &P) {
   for (auto &t : th) t.join();
   for (auto &e : errs) if (!e.empty()) { P.err = e; ok = false; }
   if (!ok) return false;
-  // Segments: per hemisphere and level, the (octant, class, regular) groups
-  // of points at that level, each with the class's column range.
   for (int hemi = 0; hemi < 2; ++hemi) {
-    int maxl = 0;
     std::vector<std::pair<int, int>> groups;  // (octant, class) pairs of this hemisphere
     for (int ioct : octs) {
       int b = ioct - 1;
       if (((b >> 2) & 1) != hemi) continue;
-      for (int cls = 0; cls < 4; ++cls) {
-        if (P.cls_ncol[b][cls] == 0) continue;
-        groups.push_back({b, cls});
-        const int *lv = &P.level[((size_t)b * 4 + cls) * n];
-        for (int i = 0; i < n; ++i) maxl = std::max(maxl, lv[i]);
-      }
+      for (int cls = 0; cls < 4; ++cls)
+        if (P.cls_ncol[b][cls] > 0) groups.push_back({b, cls});
     }
-    // counts per (level, group, regular)
     const int ng = (int)groups.size();
+    std::vector<uint32_t> &tasks = P.tasks[hemi];
+    tasks.clear();
+    long long irr = 0;
+    // Phase 1: per (octant, class) group, one segment per level.
+    P.p1segs[hemi].clear();
+    P.p1off[hemi].assign(1, 0);
+    P.p1depth[hemi] = 0;
+    for (int gi = 0; gi < ng; ++gi) {
+      const int b = groups[gi].first, cls = groups[gi].second;
+      const int *lv = &P.level[((size_t)b * 4 + cls) * n];
+      const uint8_t *kd = &P.kind[((size_t)b * 4 + cls) * n];
+      int depth = 0;
+      for (int i = 0; i < n; ++i) if (kd[i] == 3) depth = std::max(depth, lv[i]);
+      if (depth == 0) continue;
+      std::vector<std::vector<int>> by(depth + 1);
+      for (int i = 0; i < n; ++i) if (kd[i] == 3) by[lv[i]].push_back(i);
+      for (int l = 1; l <= depth; ++l) {
+        Seg sg;
+        sg.t0 = (int)tasks.size(); sg.ntask = (int)by[l].size(); sg.start = 0; sg.b = b; sg.cls = cls;
+        sg.col0 = P.cls_col0[b][cls]; sg.ncol = P.cls_ncol[b][cls]; sg.regular = 0; sg.irr0 = (int)irr;
+        irr += (long long)sg.ntask * sg.ncol;
+        for (int i : by[l]) tasks.push_back((uint32_t)i);
+        P.p1segs[hemi].push_back(sg);
+      }
+      P.p1off[hemi].push_back((int)P.p1segs[hemi].size());
+      P.p1depth[hemi] = std::max(P.p1depth[hemi], depth);
+    }
+    // Phase 2: per level, the (group, regular or not) segments.
+    int maxl = 0;
+    for (int gi = 0; gi < ng; ++gi) {
+      const int b = groups[gi].first, cls = groups[gi].second;
+      const int *lv = &P.level[((size_t)b * 4 + cls) * n];
+      const uint8_t *kd = &P.kind[((size_t)b * 4 + cls) * n];
+      for (int i = 0; i < n; ++i) if (kd[i] == 1 || kd[i] == 2) maxl = std::max(maxl, lv[i] - Plan::kPhase2);
+    }
     std::vector<int> cnt((size_t)(maxl + 1) * ng * 2, 0);
     for (int gi = 0; gi < ng; ++gi) {
-      const int b = groups[gi].first;
-      const int *lv = &P.level[((size_t)b * 4 + groups[gi].second) * n];
-      const uint8_t *rg = &P.regular[(size_t)b * n];
+      const int b = groups[gi].first, cls = groups[gi].second;
+      const int *lv = &P.level[((size_t)b * 4 + cls) * n];
+      const uint8_t *kd = &P.kind[((size_t)b * 4 + cls) * n];
       for (int i = 0; i < n; ++i)
-        if (lv[i] > 0) cnt[((size_t)lv[i] * ng + gi) * 2 + (rg[i] ? 0 : 1)]++;
+        if (kd[i] == 1 || kd[i] == 2) cnt[((size_t)(lv[i] - Plan::kPhase2) * ng + gi) * 2 + (kd[i] == 1 ? 0 : 1)]++;
     }
     P.segs[hemi].clear();
     P.seg_off[hemi].assign(1, 0);
     P.level_items[hemi].clear();
     std::vector<int> fill((size_t)(maxl + 1) * ng * 2, 0);
-    int t = 0;
+    long long gitems = 0;
+    int t = (int)tasks.size();
     for (int l = 1; l <= maxl; ++l) {
       long long items = 0;
       for (int gi = 0; gi < ng; ++gi)
-        for (int irr = 0; irr < 2; ++irr) {
-          const int c = cnt[((size_t)l * ng + gi) * 2 + irr];
+        for (int isirr = 0; isirr < 2; ++isirr) {
+          const int c = cnt[((size_t)l * ng + gi) * 2 + isirr];
           if (c == 0) continue;
           const int b = groups[gi].first, cls = groups[gi].second;
           Seg sg;
           sg.t0 = t; sg.ntask = c; sg.start = (int)items; sg.b = b; sg.cls = cls;
-          sg.col0 = P.cls_col0[b][cls]; sg.ncol = P.cls_ncol[b][cls]; sg.regular = irr ? 0 : 1;
-          fill[((size_t)l * ng + gi) * 2 + irr] = t;
+          sg.col0 = P.cls_col0[b][cls]; sg.ncol = P.cls_ncol[b][cls]; sg.regular = isirr ? 0 : 1;
+          sg.irr0 = (int)irr;
+          if (isirr) irr += (long long)c * sg.ncol;
+          fill[((size_t)l * ng + gi) * 2 + isirr] = t;
           P.segs[hemi].push_back(sg);
           t += c;
           items += (long long)c * sg.ncol;
         }
-      if (items >= (1LL << 31)) { P.err = "sweep level too large"; return false; }
+      if (items >= (1LL << 31) || irr >= (1LL << 31)) { P.err = "sweep level too large"; return false; }
       P.seg_off[hemi].push_back((int)P.segs[hemi].size());
       P.level_items[hemi].push_back((int)items);
+      gitems += items;
     }
-    P.tasks[hemi].assign(t, 0);
+    P.nirr[hemi] = irr;
+    P.nitems[hemi] = gitems;
+    tasks.resize(t);
     for (int gi = 0; gi < ng; ++gi) {
-      const int b = groups[gi].first;
-      const int *lv = &P.level[((size_t)b * 4 + groups[gi].second) * n];
-      const uint8_t *rg = &P.regular[(size_t)b * n];
+      const int b = groups[gi].first, cls = groups[gi].second;
+      const int *lv = &P.level[((size_t)b * 4 + cls) * n];
+      const uint8_t *kd = &P.kind[((size_t)b * 4 + cls) * n];
       for (int i = 0; i < n; ++i)
-        if (lv[i] > 0) P.tasks[hemi][fill[((size_t)lv[i] * ng + gi) * 2 + (rg[i] ? 0 : 1)]++] = (uint32_t)i;
+        if (kd[i] == 1 || kd[i] == 2)
+          tasks[fill[((size_t)(lv[i] - Plan::kPhase2) * ng + gi) * 2 + (kd[i] == 1 ? 0 : 1)]++] = (uint32_t)i;
     }
   }
   return true;
@@ -955,6 +1022,7 @@ void build_geo(Plan &P) {
   const float dx = P.xgrid[1] - P.xgrid[0], dy = P.ygrid[1] - P.ygrid[0];
   for (int L = 0; L < nl; ++L)
     for (int c = 0; c < nang; ++c) {
+      if (P.col_imu[c] < 0) continue;
       float *g = &P.geo[((size_t)L * nang + c) * 4];
       const int b = P.col_oct[c] - 1;
       g[3] = (float)regular_exit(P.col_cx[c], P.col_cy[c], P.col_cz[c], b, dx, dy, P.zgrid[L + 1] - P.zgrid[L], g[0], g[1], g[2]);

@@ -19,12 +19,16 @@ namespace shdom {
 // One group of sweep tasks at one wavefront level: the points (tasks[t0,
 // t0+ntask)) of trace octant b whose traces for the ordinates of face class
 // cls (columns [col0, col0+ncol)) are all regular or all not.  start is the
-// group's first item (task x column) within its level.
+// group's first item (task x column) within its level; for a group that is
+// not regular, irr0 is its first item in the hemisphere's table of general
+// traces.
 struct Seg {
-  int t0, ntask, start, b, cls, col0, ncol, regular;
+  int t0, ntask, start, b, cls, col0, ncol, regular, irr0;
 };
 
 struct Plan {
+  // Level numbers of phase-2 points start at kPhase2 (phase 1 < kPhase2).
+  static constexpr int kPhase2 = 1 << 16;
   // ---- base grid (INIT_CELL_STRUCTURE layout, 0-based, -1 = no neighbour)
   int nx = 0, ny = 0, nz = 0, nx1 = 0, ny1 = 0, npts = 0, ncells = 0;
   int bcflag = 0, ipflag = 0, is1d = 0, noct = 8;
@@ -39,20 +43,26 @@ struct Plan {
   std::vector<int> rank;           // [8][npts], -1 when the octant is unused
   std::vector<int> startcell;      // [8][npts]
   std::vector<int> level;          // [8][4][npts] wavefront level per octant and face class (0: preset)
+  // kind[8][4][npts]: 0 preset or unused, 1 phase-2 regular trace, 2 phase-2
+  // general trace, 3 phase 1 (a general-trace point whose dependencies are
+  // all preset or phase-1 points: the open-boundary planes' own chains).
+  std::vector<uint8_t> kind;
   // regular[b][p] = 1 when point p's trace for trace octant b crosses one
   // full interior cell whose seven other corners all precede p; such traces
   // depend only on the ordinate and the z layer, tabulated in geo.
   std::vector<uint8_t> regular;    // [8][npts]
   std::vector<float> geo;          // [nz-1][nang][4]: so, u, v, face
   // ---- discrete ordinates
-  int nmu = 0, nphi = 0, ml = 0, mm = 0, nlm = 0, nleg = 0, nang = 0, nphi0max = 0;
+  // nang counts the ordinate columns including the padding ordinates that
+  // align each (octant, face class) group to 8 columns; nang_real = NANG.
+  int nmu = 0, nphi = 0, ml = 0, mm = 0, nlm = 0, nleg = 0, nang = 0, nang_real = 0, nphi0max = 0;
   std::vector<int> nphi0, lofj, mofj;
   std::vector<float> mu, wtmu, phi, wtdo;        // phi/wtdo [nmu][nphi0max]
   // Column order of the ordinate-space arrays: hemisphere (down, up), then
   // trace octant, then (mu, phi) in the reference order.
-  std::vector<int> col_imu, col_iphi, col_oct;   // [nang]
+  std::vector<int> col_imu, col_iphi, col_oct;   // [nang]; col_imu < 0 for a padding ordinate
   std::vector<int> col_cls;                      // [nang] face class: 0 x, 1 y, 2 z, 3 mixed
-  int cls_col0[8][4] = {{0}}, cls_ncol[8][4] = {{0}};  // column range per octant and class
+  int cls_col0[8][4] = {{0}}, cls_ncol[8][4] = {{0}};  // first column and real ordinates per octant and class
   std::vector<int> col_of;                       // [nmu][nphi0max] -> column
   int ncol_down = 0;                             // columns [0, ncol_down) are mu < 0
   int oct_col0[8] = {0}, oct_ncol[8] = {0};      // column range of each trace octant
@@ -75,10 +85,15 @@ struct Plan {
   // ---- numerical parameters
   shdom_problem prob{};
   // ---- wavefront schedule, per hemisphere (0 down, 1 up)
-  std::vector<uint32_t> tasks[2];                // point indices grouped by level and segment
+  std::vector<uint32_t> tasks[2];                // point indices: phase-1 segments, then phase-2 levels
+  std::vector<Seg> p1segs[2];                    // phase 1: one segment per level per (octant, class) group
+  std::vector<int> p1off[2];                     // group -> first segment (ngroups + 1 entries)
+  int p1depth[2] = {0, 0};
   std::vector<Seg> segs[2];
   std::vector<int> seg_off[2];                   // level -> first segment (nlevels + 1 entries)
   std::vector<int> level_items[2];               // level -> task x column items
+  long long nirr[2] = {0, 0};                    // general-trace items per hemisphere
+  long long nitems[2] = {0, 0};                  // phase-2 task x column items per hemisphere
   std::string err;
 };
 
