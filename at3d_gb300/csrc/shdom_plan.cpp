@@ -27,6 +27,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <list>
+#include <memory>
+#include <mutex>
 #include <thread>
 
 namespace shdom {
@@ -461,11 +464,11 @@ void build_angles(const shdom_problem &p, Plan &P) {
       }
     }
   }
-  P.ylmsun.resize(nlm);
-  ylm_unpol(P.ml, P.mm, (double)p.solarmu, p.solaraz, P.ylmsun.data());
 }
 
 bool build_medium(const shdom_problem &p, Plan &P) {
+  P.ylmsun.resize(P.nlm);
+  ylm_unpol(P.ml, P.mm, (double)p.solarmu, p.solaraz, P.ylmsun.data());
   const int npx = p.npx, npy = p.npy, npz = p.npz, ng = npx * npy * npz;
   const int npart = p.npart, nmic = p.maxnmicro, nq = 8 * nmic, npts = P.npts, nleg = P.nleg, ml = P.ml;
   P.npart = npart; P.numphase = p.numphase;
@@ -1031,14 +1034,54 @@ void build_geo(Plan &P) {
 
 }  // namespace
 
+// The geometric part of a plan (grid, cells, ordinates, transform
+// coefficients, sweep order and schedule) depends only on the grid, the
+// boundary flags, the angular resolution and TRANSMIN.  Several solves on
+// one grid (wavelengths, inversion iterates) share it: the last few are kept.
+namespace {
+std::string geometry_key(const shdom_problem &p) {
+  std::string k;
+  auto put = [&](const void *d, size_t n) { k.append(static_cast<const char *>(d), n); };
+  put(&p.npx, sizeof(int)); put(&p.npy, sizeof(int)); put(&p.npz, sizeof(int));
+  put(&p.delx, sizeof(float)); put(&p.dely, sizeof(float)); put(p.zlevels, sizeof(float) * (size_t)p.npz);
+  put(&p.bc_x_open, sizeof(int)); put(&p.bc_y_open, sizeof(int)); put(&p.ipflag, sizeof(int));
+  put(&p.nmu, sizeof(int)); put(&p.nphi, sizeof(int)); put(&p.angle_set, sizeof(int));
+  put(&p.deltam, sizeof(int)); put(&p.transmin, sizeof(float));
+  return k;
+}
+
+std::mutex g_geom_mu;
+std::list<std::pair<std::string, std::shared_ptr<const Plan>>> g_geom;  // most recent first
+constexpr size_t kGeomCache = 2;
+}  // namespace
+
 bool build_plan(const shdom_problem &p, Plan &P) {
-  P.prob = p;
   if (p.nstokes != 1) { P.err = "only nstokes=1 is supported"; return false; }
   if (p.splitacc > 0) { P.err = "adaptive cell splitting is not supported (split_accuracy must be <= 0)"; return false; }
   if (p.npart < 1 || p.numphase < 1 || p.maxnmicro < 1) { P.err = "empty medium"; return false; }
-  if (!build_grid(p, P)) return false;
-  build_angles(p, P);
-  if (P.npts >= (1 << 28)) { P.err = "grid too large for the sweep task encoding"; return false; }
+  const std::string key = geometry_key(p);
+  std::shared_ptr<const Plan> hit;
+  {
+    std::lock_guard<std::mutex> lk(g_geom_mu);
+    for (auto it = g_geom.begin(); it != g_geom.end(); ++it)
+      if (it->first == key) { hit = it->second; g_geom.splice(g_geom.begin(), g_geom, it); break; }
+  }
+  if (hit) {
+    P = *hit;
+  } else {
+    P.prob = p;
+    if (!build_grid(p, P)) return false;
+    build_angles(p, P);
+    if (P.npts >= (1 << 28)) { P.err = "grid too large for the sweep task encoding"; return false; }
+    if (!build_schedule(p, P)) return false;
+    build_geo(P);
+    auto keep = std::make_shared<const Plan>(P);
+    std::lock_guard<std::mutex> lk(g_geom_mu);
+    g_geom.emplace_front(key, std::move(keep));
+    while (g_geom.size() > kGeomCache) g_geom.pop_back();
+  }
+  P.prob = p;
+  P.err.clear();
   if (!build_medium(p, P)) return false;
   build_direct(p, P);
   // bottom surface albedo (PREP_SURFACE periodic grid + SURFACE_PARM_INTERP)
@@ -1054,8 +1097,6 @@ bool build_plan(const shdom_problem &p, Plan &P) {
       P.botalb[k] = (1 - u) * (1 - v) * G(ix, iy) + (1 - u) * v * G(ix, iy + 1) + u * (1 - v) * G(ix + 1, iy) + u * v * G(ix + 1, iy + 1);
     }
   }
-  if (!build_schedule(p, P)) return false;
-  build_geo(P);
   return true;
 }
 
