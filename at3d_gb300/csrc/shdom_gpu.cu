@@ -1240,6 +1240,12 @@ __global__ void k_bcrad_bottom(const int *botp, int nbot, const float *botalb, c
   bcrad[k] = 0.318309886f * botalb[k] * (dirflux[p] + fluxes[2 * (size_t)p]);
 }
 
+}  // namespace shdom
+
+#include "shdom_grad.cuh"
+
+namespace shdom {
+
 // ----------------------------------------------------------------- handle
 template <class T>
 struct DBuf {
@@ -1277,6 +1283,12 @@ struct Handle {
   DBuf<float2> sweepw;  // (radsrc, tr) of the phase-2 items, [npts][ldo]
   int n_irrseg[2] = {0, 0}, p2_irrseg0[2] = {0, 0}, p2_irr_j0[2] = {0, 0};
   cudaStream_t stream2 = nullptr;  // phase-1 sweeps, concurrent with the source pass
+  // Levis gradient tables for one species (built on the first gradient call)
+  int grad_ipa = -1;
+  DBuf<int> g_interpptr, g_sjptr, g_sjiph, g_piph;
+  DBuf<float> g_optwt, g_dextm, g_dalbm, g_dfj, g_albsp, g_sjw, g_legu, g_legs, g_fmix, g_scatj, g_legp, g_extp,
+      g_albp, g_pphw;
+  DBuf<double> g_grad, g_beam, g_adj;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int coop_blocks = 0;
   DBuf<float> col_cx, col_cy, col_cz, col_fluxw, cmu1t, cmu2t, cphi1t, cphi2, ylmsun;
@@ -1849,16 +1861,9 @@ int shdom_solution_iterations(shdom_handle *hh, int maxiter, int *iters, float *
   return 0;
 }
 
-static int render_impl(shdom_handle *hh, int nrays, const float *camx, const float *camy, const float *camz,
-                       const double *cammu, const double *camphi, float *out, cudaStream_t stream) {
-  Handle &H = hh->h;
+static shdom::RenderArgs render_args(Handle &H, int nrays, const float *camx, const float *camy, const float *camz,
+                                     const double *cammu, const double *camphi, float *out) {
   shdom::Plan &P = H.P;
-  int nbot = (int)P.botp.size();
-  if (nbot) {
-    shdom::k_bcrad_bottom<<<(nbot + 127) / 128, 128, 0, stream>>>(H.botp.p, nbot, H.botalb.p, H.dirflux.p, H.fluxes.p,
-                                                                  H.bcrad.p);
-    H.launches += 1;
-  }
   shdom::RenderArgs a;
   a.gridpos = H.gridpos.p; a.xgrid = H.xgrid.p; a.ygrid = H.ygrid.p; a.zgrid = H.zgrid.p;
   a.gridptr = H.gridptr.p; a.neighptr = H.neighptr.p; a.cellflags = H.cellflags.p;
@@ -1871,6 +1876,20 @@ static int render_impl(shdom_handle *hh, int nrays, const float *camx, const flo
   a.nscatangle = P.nscatangle; a.deltam = P.prob.deltam; a.solarmu = P.prob.solarmu; a.solaraz = P.prob.solaraz;
   a.secmu0 = 1.0f / std::fabs(P.prob.solarmu); a.skyrad = P.prob.skyrad; a.tautol = P.prob.tautol;
   a.transcut = P.prob.transcut;
+  return a;
+}
+
+static int render_impl(shdom_handle *hh, int nrays, const float *camx, const float *camy, const float *camz,
+                       const double *cammu, const double *camphi, float *out, cudaStream_t stream) {
+  Handle &H = hh->h;
+  shdom::Plan &P = H.P;
+  int nbot = (int)P.botp.size();
+  if (nbot) {
+    shdom::k_bcrad_bottom<<<(nbot + 127) / 128, 128, 0, stream>>>(H.botp.p, nbot, H.botalb.p, H.dirflux.p, H.fluxes.p,
+                                                                  H.bcrad.p);
+    H.launches += 1;
+  }
+  shdom::RenderArgs a = render_args(H, nrays, camx, camy, camz, cammu, camphi, out);
   if (P.nlm > shdom::RNLM || P.ml + 1 > 64) return fail(hh, "render: too many spherical-harmonic terms");
   int blocks = (nrays + shdom::RWARPS - 1) / shdom::RWARPS;
   if (blocks > 0) {
@@ -1878,6 +1897,213 @@ static int render_impl(shdom_handle *hh, int nrays, const float *camx, const flo
     H.launches += 1;
   }
   CK(cudaGetLastError());
+  return 0;
+}
+
+// Derivative tables of PREPARE_DERIV_INTERPS (src/polarized/shdomsub4.f:
+// 2917-3080) and the direction-independent parts of
+// COMPUTE_SOURCE_GRAD_1CELL (:1546-2042) for the extinction and albedo of
+// species ipa, with the 'table' derivative method (no phase derivative).
+static void prepare_grad(Handle &H, int ipa) {
+  shdom::Plan &P = H.P;
+  const int npx = P.npx, npy = P.npy, npz = P.npz, ng = npx * npy * npz, npts = P.npts;
+  const int ml = P.ml, nl = ml + 1, nl1 = P.nleg + 1, nmic = P.maxnmicro;
+  const bool deltam = P.prob.deltam != 0;
+  const float *E = &P.prop_ext[(size_t)ipa * ng], *A = &P.prop_alb[(size_t)ipa * ng];
+  const int *IPH = &P.prop_iph[(size_t)ipa * ng * nmic];
+  const float *PHW = &P.prop_phw[(size_t)ipa * ng * nmic];
+  auto L = [&](int iph1, int l) { return P.leg[(size_t)(iph1 - 1) * nl1 + l]; };
+  std::vector<int> iptr((size_t)npts * 8);
+  std::vector<float> owt((size_t)npts * 8);
+  for (int ip = 0; ip < npts; ++ip) {  // COMPUTE_INTERP_WEIGHTS
+    float x = P.gridpos[3 * ip], y = P.gridpos[3 * ip + 1], z = P.gridpos[3 * ip + 2];
+    int il = 0, iu = npz;
+    while (iu - il > 1) { int im = (iu + il) / 2; if (z >= P.zgrid[im - 1]) il = im; else iu = im; }
+    int iz = std::max(il, 1);
+    double w = std::max(0.0, std::min(1.0, (double)(z - P.zgrid[iz - 1]) / (P.zgrid[iz] - P.zgrid[iz - 1])));
+    int ix = (int)(x / P.delx) + 1;
+    if (std::fabs(x - npx * P.delx) < 0.01f * P.delx) ix = npx;
+    int iy = (int)(y / P.dely) + 1;
+    if (std::fabs(y - npy * P.dely) < 0.01f * P.dely) iy = npy;
+    ix = std::max(1, std::min(npx, ix)); iy = std::max(1, std::min(npy, iy));
+    int ixp = ix % npx + 1, iyp = iy % npy + 1;
+    double u = std::max(0.0, std::min(1.0, (double)(x - P.delx * (ix - 1)) / P.delx));
+    if (u < 1e-5) u = 0;
+    if (u > 1 - 1e-5) u = 1;
+    double v = std::max(0.0, std::min(1.0, (double)(y - P.dely * (iy - 1)) / P.dely));
+    if (v < 1e-5) v = 0;
+    if (v > 1 - 1e-5) v = 1;
+    const double f[8] = {(1 - u) * (1 - v) * (1 - w), u * (1 - v) * (1 - w), (1 - u) * v * (1 - w), u * v * (1 - w),
+                         (1 - u) * (1 - v) * w,       u * (1 - v) * w,       (1 - u) * v * w,       u * v * w};
+    int i1 = (iz - 1) + npz * (iy - 1) + npz * npy * (ix - 1), i2 = (iz - 1) + npz * (iy - 1) + npz * npy * (ixp - 1);
+    int i3 = (iz - 1) + npz * (iyp - 1) + npz * npy * (ix - 1), i4 = (iz - 1) + npz * (iyp - 1) + npz * npy * (ixp - 1);
+    const int ii[8] = {i1, i2, i3, i4, i1 + 1, i2 + 1, i3 + 1, i4 + 1};
+    for (int k = 0; k < 8; ++k) { iptr[(size_t)ip * 8 + k] = ii[k]; owt[(size_t)ip * 8 + k] = (float)f[k]; }
+  }
+  std::vector<float> fp(ng, 0.f), dextm((size_t)ng * 2), legp((size_t)ng * nl, 0.f);
+  for (int ib = 0; ib < ng; ++ib) {
+    float fv = 0.f;
+    if (deltam) for (int q = 0; q < nmic; ++q) fv += PHW[(size_t)ib * nmic + q] * L(IPH[(size_t)ib * nmic + q], ml + 1);
+    fp[ib] = fv;
+    dextm[(size_t)ib * 2 + 0] = 1.f - fv * A[ib];  // d/d(extinction)
+    dextm[(size_t)ib * 2 + 1] = -fv * E[ib];       // d/d(albedo)
+    for (int q = 0; q < nmic; ++q) {
+      const int i1 = IPH[(size_t)ib * nmic + q];
+      const float w = PHW[(size_t)ib * nmic + q], ft = deltam ? L(i1, ml + 1) : 0.f;
+      for (int l = 0; l < nl; ++l) legp[(size_t)ib * nl + l] += w * (L(i1, l) + ft);
+    }
+  }
+  std::vector<float> dalbm((size_t)npts * 16), dfj((size_t)npts * 16), scatj(npts, 0.f), legu((size_t)npts * nl),
+      legs((size_t)npts * nl, 0.f), fmix(npts, 0.f), sjw;
+  std::vector<int> sjptr(npts + 1, 0), sjiph;
+  const float scatmin = (float)P.scatmin;
+  std::vector<float> lt(nl + 1);
+  for (int ip = 0; ip < npts; ++ip) {
+    const size_t o = (size_t)ipa * npts + ip;
+    const float F = P.sp_f[o], alb = P.sp_alb[o];
+    const float albj = deltam ? alb / (F * (alb - 1.f) + 1.f) : alb;
+    const float divide = 1.f / (1.f - albj * F);
+    float sc = 0.f;
+    for (int nb = 0; nb < 8; ++nb) {
+      const int ib = iptr[(size_t)ip * 8 + nb];
+      const float FP = fp[ib];
+      // d = 0: extinction (DEXT 1, DALB 0); d = 1: albedo (DEXT 0, DALB 1)
+      dalbm[((size_t)ip * 8 + nb) * 2 + 0] = divide * (((1.f - F) * (A[ib] - albj) + (albj - 1.f) * A[ib] * (FP - F)));
+      dalbm[((size_t)ip * 8 + nb) * 2 + 1] = divide * (((1.f - F) * E[ib] + (albj - 1.f) * E[ib] * (FP - F)));
+      dfj[((size_t)ip * 8 + nb) * 2 + 0] = ((FP - F) * A[ib]) / (1.f - F);
+      dfj[((size_t)ip * 8 + nb) * 2 + 1] = ((FP - F) * E[ib]) / (1.f - F);
+      if (deltam) sc += owt[(size_t)ip * 8 + nb] * A[ib] * E[ib];
+    }
+    scatj[ip] = sc;
+    const float div = sc > scatmin ? sc : scatmin;
+    if (deltam) {
+      for (int nb = 0; nb < 8; ++nb) {
+        const int ib = iptr[(size_t)ip * 8 + nb];
+        const float sw = owt[(size_t)ip * 8 + nb] * A[ib] * E[ib];
+        if (sw <= 1e-6f) continue;
+        for (int q = 0; q < nmic; ++q) {
+          const float w = PHW[(size_t)ib * nmic + q];
+          if (w <= 1e-6f) continue;
+          sjiph.push_back(IPH[(size_t)ib * nmic + q] - 1);
+          sjw.push_back(sw * w / div);
+        }
+      }
+    }
+    sjptr[ip + 1] = (int)sjiph.size();
+    if (P.npart == 1) {
+      for (int l = 0; l < nl; ++l) legu[(size_t)ip * nl + l] = P.sp_legu[o * nl + l];
+    } else {
+      std::fill(lt.begin(), lt.end(), 0.f);
+      for (int nb = 0; nb < 8; ++nb) {
+        const int ib = iptr[(size_t)ip * 8 + nb];
+        const float sw = owt[(size_t)ip * 8 + nb] * A[ib] * E[ib];
+        if (sw <= 1e-6f) continue;
+        for (int q = 0; q < nmic; ++q) {
+          const float w = PHW[(size_t)ib * nmic + q];
+          if (w <= 1e-6f) continue;
+          for (int l = 0; l <= nl; ++l) lt[l] += sw * w * L(IPH[(size_t)ib * nmic + q], l);
+        }
+      }
+      for (int l = 0; l <= nl; ++l) lt[l] /= div;
+      float Fm = 0.f;
+      if (deltam) { Fm = lt[ml + 1]; for (int l = 0; l < nl; ++l) lt[l] /= (1.f - Fm); }
+      fmix[ip] = Fm;
+      for (int l = 0; l < nl; ++l) {
+        legs[(size_t)ip * nl + l] = lt[l];
+        legu[(size_t)ip * nl + l] = deltam ? lt[l] * (1.f - Fm) + Fm : lt[l];
+      }
+    }
+  }
+  if (sjiph.empty()) { sjiph.push_back(0); sjw.push_back(0.f); }
+  std::vector<float> albsp(P.sp_alb.begin() + (size_t)ipa * npts, P.sp_alb.begin() + (size_t)(ipa + 1) * npts);
+  std::vector<float> ep(E, E + ng), ap(A, A + ng), phw(PHW, PHW + (size_t)ng * nmic);
+  std::vector<int> piph(IPH, IPH + (size_t)ng * nmic);
+  H.g_interpptr.upload(iptr); H.g_optwt.upload(owt); H.g_dextm.upload(dextm); H.g_dalbm.upload(dalbm);
+  H.g_dfj.upload(dfj); H.g_albsp.upload(albsp); H.g_sjptr.upload(sjptr); H.g_sjiph.upload(sjiph); H.g_sjw.upload(sjw);
+  H.g_legu.upload(legu); H.g_legs.upload(legs); H.g_fmix.upload(fmix); H.g_scatj.upload(scatj); H.g_legp.upload(legp);
+  H.g_extp.upload(ep); H.g_albp.upload(ap); H.g_piph.upload(piph); H.g_pphw.upload(phw);
+  H.g_grad.alloc((size_t)ng * 2); H.g_beam.alloc(npts);
+  H.grad_ipa = ipa;
+}
+
+// Phases 3 and 4 of the adjoint branch on device-resident rays and weights;
+// the gradient is left in H.g_grad.
+static void levis_adjoint_device(Handle &H, int nrays, const float *dx, const float *dy, const float *dz,
+                                 const double *dmu, const double *dphi, const double *dadj) {
+  shdom::Plan &P = H.P;
+  shdom::GradArgs G;
+  G.r = render_args(H, nrays, dx, dy, dz, dmu, dphi, nullptr);
+  G.radiance = H.radiance.p; G.nr = H.nr.p; G.interpptr = H.g_interpptr.p; G.optinterpwt = H.g_optwt.p;
+  G.dextm = H.g_dextm.p; G.dalbm = H.g_dalbm.p; G.dfj = H.g_dfj.p; G.alb_sp = H.g_albsp.p;
+  G.sj_ptr = H.g_sjptr.p; G.sj_iph = H.g_sjiph.p; G.sj_w = H.g_sjw.p; G.legent_u = H.g_legu.p; G.legent_s = H.g_legs.p;
+  G.fmix = H.g_fmix.p; G.scatterj = H.g_scatj.p; G.legenp_u = H.g_legp.p; G.extp = H.g_extp.p; G.albp = H.g_albp.p;
+  G.piph = H.g_piph.p; G.pphw = H.g_pphw.p; G.adj = dadj; G.gradout = H.g_grad.p; G.beam = H.g_beam.p;
+  G.botalb = H.botalb.p; G.npart = P.npart; G.maxnmicro = P.maxnmicro; G.ng = P.npx * P.npy * P.npz;
+  G.scatmin = (float)P.scatmin;
+  CK(cudaMemsetAsync(H.g_grad.p, 0, H.g_grad.n * sizeof(double), H.stream));
+  CK(cudaMemsetAsync(H.g_beam.p, 0, H.g_beam.n * sizeof(double), H.stream));
+  const int blocks = (nrays + shdom::GWARPS - 1) / shdom::GWARPS;
+  shdom::k_levis_adjoint<<<blocks, shdom::GWARPS * 32, 0, H.stream>>>(G);
+  CK(cudaGetLastError());
+  shdom::BeamArgs b;
+  b.gridpos = H.gridpos.p; b.zlev = H.zgrid.p; b.beam = H.g_beam.p; b.dextm = H.g_dextm.p; b.gradout = H.g_grad.p;
+  b.npts = P.npts; b.npx = P.npx; b.npy = P.npy; b.npz = P.npz; b.bcflag = P.bcflag; b.ipflag = P.ipflag;
+  b.delx = P.delx; b.dely = P.dely; b.solarmu = P.prob.solarmu; b.solaraz = P.prob.solaraz;
+  shdom::k_levis_beam<<<(P.npts + 255) / 256, 256, 0, H.stream>>>(b);
+  CK(cudaGetLastError());
+  H.launches += 2;
+}
+
+// Host-buffer form of the gradient: measurements given -> L2 cost and its
+// adjoint weights (COMPUTE_ADJOINT_WEIGHTS, unit uncertainty); otherwise
+// the caller's weights.
+static int levis_host(shdom_handle *hh, int species, int nrays, const float *camx, const float *camy,
+                      const float *camz, const double *cammu, const double *camphi, const float *meas,
+                      const double *weights, double *gradient, double *cost, float *stokes_out) {
+  Handle &H = hh->h;
+  shdom::Plan &P = H.P;
+  if (species < 0 || species >= P.npart) return fail(hh, "levis gradient: species index out of range");
+  if (P.ml + 1 > 32 || P.nlm > shdom::RNLM) return fail(hh, "levis gradient: at most 32 Legendre terms are supported");
+  if (!H.initialized) return fail(hh, "levis gradient: the solution has not been initialized");
+  if (H.grad_ipa != species) prepare_grad(H, species);
+  const int ng = P.npx * P.npy * P.npz;
+  float *d;
+  const size_t fb = (size_t)nrays * sizeof(float), db = (size_t)nrays * sizeof(double);
+  CK(cudaMalloc(&d, 4 * fb + 3 * db));
+  float *dx = d, *dy = d + nrays, *dz = d + 2 * (size_t)nrays, *dout = d + 3 * (size_t)nrays;
+  double *dmu = (double *)(d + 4 * (size_t)nrays), *dphi = dmu + nrays, *dadj = dphi + nrays;
+  int rc = 0;
+  CK(cudaMemcpyAsync(dx, camx, fb, cudaMemcpyHostToDevice, H.stream));
+  CK(cudaMemcpyAsync(dy, camy, fb, cudaMemcpyHostToDevice, H.stream));
+  CK(cudaMemcpyAsync(dz, camz, fb, cudaMemcpyHostToDevice, H.stream));
+  CK(cudaMemcpyAsync(dmu, cammu, db, cudaMemcpyHostToDevice, H.stream));
+  CK(cudaMemcpyAsync(dphi, camphi, db, cudaMemcpyHostToDevice, H.stream));
+  rc = render_impl(hh, nrays, dx, dy, dz, dmu, dphi, dout, H.stream);  // forward radiances, surface radiance
+  std::vector<double> adj(nrays, 0.0);
+  std::vector<float> st(nrays, 0.f);
+  if (!rc) {
+    CK(cudaMemcpyAsync(st.data(), dout, fb, cudaMemcpyDeviceToHost, H.stream));
+    CK(cudaStreamSynchronize(H.stream));
+    if (meas) {
+      double c = 0.0;
+      for (int i = 0; i < nrays; ++i) {
+        const double e = (double)st[i] - (double)meas[i];
+        c += 0.5 * e * e;
+        adj[i] = e;
+      }
+      if (cost) *cost = c;
+    } else {
+      for (int i = 0; i < nrays; ++i) adj[i] = weights[i];
+    }
+    if (stokes_out) std::memcpy(stokes_out, st.data(), fb);
+    CK(cudaMemcpyAsync(dadj, adj.data(), db, cudaMemcpyHostToDevice, H.stream));
+    levis_adjoint_device(H, nrays, dx, dy, dz, dmu, dphi, dadj);
+    CK(cudaMemcpyAsync(gradient, H.g_grad.p, (size_t)ng * 2 * sizeof(double), cudaMemcpyDeviceToHost, H.stream));
+  }
+  CK(cudaStreamSynchronize(H.stream));
+  cudaFree(d);
+  if (rc) return rc;
+  if (shdom::check_device_error(H)) return 1;
   return 0;
 }
 
@@ -1918,6 +2144,32 @@ int shdom_render(shdom_handle *hh, int nrays, const float *camx, const float *ca
     return fail(hh, e.what());
   }
   return 0;
+}
+
+int shdom_levis_gradient(shdom_handle *hh, int species, int nrays, const float *camx, const float *camy,
+                         const float *camz, const double *cammu, const double *camphi, const float *measurements,
+                         double *gradient, double *cost, float *stokes_out) {
+  if (!hh) return fail(nullptr, "null handle");
+  if (nrays <= 0 || !measurements || !gradient) return fail(hh, "shdom_levis_gradient: bad arguments");
+  try {
+    return levis_host(hh, species, nrays, camx, camy, camz, cammu, camphi, measurements, nullptr, gradient, cost,
+                      stokes_out);
+  } catch (const std::exception &e) {
+    return fail(hh, e.what());
+  }
+}
+
+int shdom_levis_adjoint(shdom_handle *hh, int species, int nrays, const float *camx, const float *camy,
+                        const float *camz, const double *cammu, const double *camphi, const double *weights,
+                        double *gradient) {
+  if (!hh) return fail(nullptr, "null handle");
+  if (nrays <= 0 || !weights || !gradient) return fail(hh, "shdom_levis_adjoint: bad arguments");
+  try {
+    return levis_host(hh, species, nrays, camx, camy, camz, cammu, camphi, nullptr, weights, gradient, nullptr,
+                      nullptr);
+  } catch (const std::exception &e) {
+    return fail(hh, e.what());
+  }
 }
 
 int shdom_export_state(shdom_handle *hh, float *source, int *ns, float *radiance, int *nr, float *fluxes,

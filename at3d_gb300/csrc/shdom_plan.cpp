@@ -570,6 +570,18 @@ bool build_medium(const shdom_problem &p, Plan &P) {
   }
   P.albmax = 0.f;
   for (float a : alb) P.albmax = std::max(P.albmax, a);
+  // kept for the gradient: the property grid of every species, the stored
+  // Legendre table and the scaled species properties on the grid points
+  P.npx = npx; P.npy = npy; P.npz = npz; P.maxnmicro = nmic; P.delx = p.delx; P.dely = p.dely;
+  P.scatmin = scatmin;
+  P.prop_ext.assign(p.extinctp, p.extinctp + (size_t)npart * ng);
+  P.prop_alb.assign(p.albedop, p.albedop + (size_t)npart * ng);
+  P.prop_iph.assign(p.iphasep, p.iphasep + (size_t)npart * ng * nmic);
+  P.prop_phw.assign(p.phasewtp, p.phasewtp + (size_t)npart * ng * nmic);
+  P.leg = leg;
+  P.sp_ext = ext; P.sp_alb = alb;
+  P.sp_f.assign((size_t)npart * npts, 0.f);
+  P.sp_legu.assign((size_t)npart * npts * (ml + 1), 0.f);
   // Per-point source coefficients c_l = albedo_mix * chi_mix(l) (the
   // NEWMETHOD mixing of COMPUTE_SOURCE, src/polarized/shdomsub1.f:1413-1485)
   // and the exact single-scatter mixture of COMPUTE_SOURCE_1CELL_UNPOL
@@ -598,6 +610,11 @@ bool build_medium(const shdom_problem &p, Plan &P) {
         }
       float f = 0.f;
       if (p.deltam) { f = lt1[ml + 1]; for (int l = 0; l <= ml; ++l) lt1[l] /= (1.f - f); }
+      {  // the species' own series, delta-M scaling undone (COMPUTE_SOURCE_GRAD_1CELL)
+        P.sp_f[o] = f;
+        float *u = &P.sp_legu[o * (ml + 1)];
+        for (int l = 0; l <= ml; ++l) u[l] = p.deltam ? lt1[l] * (1.f - f) + f : lt1[l];
+      }
       double scat = (double)(ext[o] * alb[o]);
       sumscat += scat;
       for (int l = 0; l <= nleg; ++l) lt[l] += scat * lt1[l];

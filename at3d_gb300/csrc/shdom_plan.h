@@ -82,6 +82,15 @@ struct Plan {
   float albmax = 0.f;
   std::vector<float> rad0;                       // [npts][4] Eddington initial radiance
   std::vector<float> botalb;                     // surface albedo at the bottom points
+  // ---- species data kept for the gradient (property grid and grid points)
+  int npx = 0, npy = 0, npz = 0, maxnmicro = 0;
+  float delx = 0.f, dely = 0.f;
+  double scatmin = 0.0;
+  std::vector<float> prop_ext, prop_alb, prop_phw;  // [npart][ng], [npart][ng][maxnmicro]
+  std::vector<int> prop_iph;                        // [npart][ng][maxnmicro], 1-based table rows
+  std::vector<float> leg;                           // [numphase][nleg+1] l/(2l+1) scaled, minus f for l <= ML with delta-M
+  std::vector<float> sp_ext, sp_alb, sp_f;          // [npart][npts] delta-M scaled extinction, albedo, f
+  std::vector<float> sp_legu;                       // [npart][npts][ml+1] species phase series, unscaled
   // ---- numerical parameters
   shdom_problem prob{};
   // ---- wavefront schedule, per hemisphere (0 down, 1 up)

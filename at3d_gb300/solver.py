@@ -167,6 +167,46 @@ class RTE:
         return {"flux_down": st["fluxes"][:, 0].reshape(shp), "flux_up": st["fluxes"][:, 1].reshape(shp),
                 "flux_direct": st["dirflux"].reshape(shp)}
 
+    def _property_shape(self):
+        sp = self.problem.species[0]
+        return tuple(np.asarray(sp.extinction).shape)
+
+    @staticmethod
+    def _ray_arrays(x, y, z, mu, phi):
+        return (np.ascontiguousarray(x, np.float32), np.ascontiguousarray(y, np.float32),
+                np.ascontiguousarray(z, np.float32), np.ascontiguousarray(mu, np.float64),
+                np.ascontiguousarray(phi, np.float64))
+
+    def levis_gradient(self, rays, measurements, species: int = 0):
+        """Levis approximate gradient of the L2 cost 0.5*sum (I - m)^2 of
+        one-ray pixels with respect to the extinction and albedo of
+        `species` on the property grid (LEVISAPPROX_GRADIENT, adjoint
+        branch).  Returns (gradient [npx, npy, npz, 2], cost, radiances)."""
+        x, y, z, mu, phi = self._ray_arrays(*rays)
+        meas = np.ascontiguousarray(measurements, np.float32)
+        shp = self._property_shape()
+        grad = np.zeros(int(np.prod(shp)) * 2, np.float64)
+        out = np.zeros(len(x), np.float32)
+        cost = C.c_double(0)
+        dp = C.POINTER(C.c_double)
+        _check(self._h, _lib.lib().shdom_levis_gradient(
+            self._h, int(species), len(x), _fp(x), _fp(y), _fp(z), mu.ctypes.data_as(dp), phi.ctypes.data_as(dp),
+            _fp(meas), grad.ctypes.data_as(dp), C.byref(cost), _fp(out)))
+        return grad.reshape(shp + (2,)), float(cost.value), out
+
+    def levis_adjoint(self, rays, weights, species: int = 0) -> np.ndarray:
+        """Levis gradient of sum_r w_r I_r for given ray weights (the
+        vector-Jacobian product of the rendered radiances): [npx, npy, npz, 2]."""
+        x, y, z, mu, phi = self._ray_arrays(*rays)
+        w = np.ascontiguousarray(weights, np.float64)
+        shp = self._property_shape()
+        grad = np.zeros(int(np.prod(shp)) * 2, np.float64)
+        dp = C.POINTER(C.c_double)
+        _check(self._h, _lib.lib().shdom_levis_adjoint(
+            self._h, int(species), len(x), _fp(x), _fp(y), _fp(z), mu.ctypes.data_as(dp), phi.ctypes.data_as(dp),
+            w.ctypes.data_as(dp), grad.ctypes.data_as(dp)))
+        return grad.reshape(shp + (2,))
+
     TRANSFORM_MODES = {"tf32x3": 0, "tf32": 1, "fp32": 2}
 
     def set_transform_mode(self, mode: str):

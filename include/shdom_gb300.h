@@ -85,6 +85,30 @@ int shdom_render_device(shdom_handle *h, int nrays, const float *camx, const flo
                         const float *camz, const double *cammu, const double *camphi,
                         float *stokes_out, void *stream);
 
+/* Levis approximate gradient of the L2 cost 0.5 * sum_r (I_r - m_r)^2 of
+ * nrays one-ray pixels (unit uncertainty, ray and Stokes weights) with
+ * respect to the extinction and single-scattering albedo of species
+ * `species` (0-based, the order of the problem's species) on the property
+ * grid.  Replaces core.levisapprox_gradient in its adjoint branch
+ * (at3d/gradient.py:262-398, LEVISAPPROX_GRADIENT src/polarized/shdomsub4.f:
+ * 288-809) for a scalar solar problem with a Lambertian surface and the
+ * 'table' derivative method.  gradient: [npx*npy*npz][2] (d/d extinction,
+ * d/d albedo) in the property-grid order (z fastest); cost and stokes_out
+ * (the rendered radiances, [nrays]) may be NULL.  The solution is frozen:
+ * call after shdom_solution_iterations. */
+int shdom_levis_gradient(shdom_handle *h, int species, int nrays, const float *camx, const float *camy,
+                         const float *camz, const double *cammu, const double *camphi,
+                         const float *measurements, double *gradient, double *cost, float *stokes_out);
+
+/* The same adjoint for caller-supplied ray weights w_r: the Levis gradient
+ * of sum_r w_r I_r (the vector-Jacobian product of the rendered radiances).
+ * No reference counterpart as a separate call: it is the adjoint pass of
+ * LEVISAPPROX_GRADIENT with ADJ_WEIGHTS given, used for automatic
+ * differentiation. */
+int shdom_levis_adjoint(shdom_handle *h, int species, int nrays, const float *camx, const float *camy,
+                        const float *camz, const double *cammu, const double *camphi, const double *weights,
+                        double *gradient);
+
 /* Solution state export (RTE.save_solution fields, at3d/solver.py:1621-1686)
  * in a dense layout: source/radiance [npts][nlm] with the terms beyond each
  * point's truncation set to zero, ns/nr the truncations (SHPTR/RSHPTR

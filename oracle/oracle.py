@@ -33,7 +33,8 @@ def lib():
         L.oracle_error.restype = C.c_char_p
         L.oracle_error.argtypes = [C.c_void_p]
         for n in ("oracle_sizes", "oracle_solve", "oracle_init_solution", "oracle_export",
-                  "oracle_render", "oracle_grid", "oracle_angles"):
+                  "oracle_render", "oracle_grid", "oracle_angles", "oracle_levis_gradient",
+                  "oracle_frozen_render"):
             getattr(L, n).restype = C.c_int
         L.oracle_destroy.argtypes = [C.c_void_p]
         _LIB = L
@@ -92,6 +93,43 @@ class Oracle:
         out = np.zeros(len(x), np.float32)
         rc = self._lib.oracle_render(C.c_void_p(self._h), len(x), _p(x), _p(y), _p(z), _p(mu, C.c_double),
                                      _p(phi, C.c_double), _p(out), int(nthreads))
+        if rc:
+            raise RuntimeError(self._lib.oracle_error(C.c_void_p(self._h)).decode())
+        return out
+
+    @staticmethod
+    def _rays(x, y, z, mu, phi):
+        return (np.ascontiguousarray(x, np.float32), np.ascontiguousarray(y, np.float32),
+                np.ascontiguousarray(z, np.float32), np.ascontiguousarray(mu, np.float64),
+                np.ascontiguousarray(phi, np.float64))
+
+    def levis_gradient(self, species: int, rays, measurements, nthreads: int = 1):
+        """Levis approximate gradient of the L2 cost (one ray per pixel) with
+        respect to the extinction and albedo of `species` on the property
+        grid: (gradient [npx*npy*npz, 2], cost, radiances)."""
+        x, y, z, mu, phi = self._rays(*rays)
+        meas = np.ascontiguousarray(measurements, np.float32)
+        pb = self._problem
+        ng = pb.species[0].extinction.size
+        grad = np.zeros((ng, 2), np.float64)
+        cost = C.c_double(0)
+        out = np.zeros(len(x), np.float32)
+        rc = self._lib.oracle_levis_gradient(C.c_void_p(self._h), int(species), len(x), _p(x), _p(y), _p(z),
+                                             _p(mu, C.c_double), _p(phi, C.c_double), _p(meas),
+                                             _p(grad, C.c_double), C.byref(cost), _p(out), int(nthreads))
+        if rc:
+            raise RuntimeError(self._lib.oracle_error(C.c_void_p(self._h)).decode())
+        return grad, float(cost.value), out
+
+    def frozen_render(self, species: int, voxel: int, dext: float, dalb: float, rays, nthreads: int = 1):
+        """Render with one voxel's extinction / albedo perturbed and the source
+        recomputed from the frozen radiance field (the forward model the
+        Levis approximation differentiates)."""
+        x, y, z, mu, phi = self._rays(*rays)
+        out = np.zeros(len(x), np.float32)
+        rc = self._lib.oracle_frozen_render(C.c_void_p(self._h), int(species), int(voxel), C.c_float(dext),
+                                            C.c_float(dalb), len(x), _p(x), _p(y), _p(z), _p(mu, C.c_double),
+                                            _p(phi, C.c_double), _p(out), int(nthreads))
         if rc:
             raise RuntimeError(self._lib.oracle_error(C.c_void_p(self._h)).decode())
         return out

@@ -1566,6 +1566,660 @@ struct Solver {
 
 };
 
+// ------------------------------------------------- Levis approximate gradient
+// The adjoint branch of LEVISAPPROX_GRADIENT (src/polarized/shdomsub4.f:
+// 288-809) for a scalar solar problem with a Lambertian surface: the
+// unknowns are the extinction (IDR 0) and single-scattering albedo (IDR 1)
+// of one species on the property grid, with the 'table' derivative method
+// (DOEXACT = 0, no phase-function derivative), and the L2 cost with unit
+// uncertainty, one ray per pixel, unit ray and Stokes weights.
+template <typename R>
+struct Levis {
+  const Solver<R> &S;
+  int ipa = 0, ng = 0;
+  std::vector<int> interpptr;     // [npts][8] property point per trilinear corner (0-based)
+  std::vector<R> optinterpwt;     // [npts][8]
+  std::vector<R> fp, dextm;       // [ng], [ng][2]
+  std::vector<R> dalbm, dfj;      // [npts][8][2]
+  static constexpr int NUMDER = 2;
+  explicit Levis(const Solver<R> &s) : S(s) {}
+
+  R dext(int, int idr) const { return idr == 0 ? (R)1 : (R)0; }
+  R dalb(int, int idr) const { return idr == 1 ? (R)1 : (R)0; }
+  R extp(int ib) const { return (R)S.extp[(size_t)ipa * ng + ib]; }
+  R albp(int ib) const { return (R)S.albp[(size_t)ipa * ng + ib]; }
+  int iphp(int q, int ib) const { return S.iphp[((size_t)ipa * ng + ib) * S.maxnmicro + q]; }
+  R phwtp(int q, int ib) const { return (R)S.phwtp[((size_t)ipa * ng + ib) * S.maxnmicro + q]; }
+
+  // COMPUTE_INTERP_WEIGHTS (src/polarized/shdomsub4.f:3083-3160) and
+  // PREPARE_DERIV_INTERPS (src/polarized/shdomsub4.f:2917-3080).
+  bool prepare(int ipa_der, std::string &err) {
+    ipa = ipa_der;
+    const auto &p = S.p;
+    const int npx = p.npx, npy = p.npy, npz = p.npz, npts = S.npts, ml = S.ml, nl1 = S.nleg + 1;
+    ng = npx * npy * npz;
+    interpptr.assign((size_t)npts * 8, 0); optinterpwt.assign((size_t)npts * 8, 0);
+    for (int ip = 0; ip < npts; ++ip) {
+      float x = S.gridpos[3 * ip], y = S.gridpos[3 * ip + 1], z = S.gridpos[3 * ip + 2];
+      int il = 0, iu = npz;
+      while (iu - il > 1) { int im = (iu + il) / 2; if (z >= S.zlev[im - 1]) il = im; else iu = im; }
+      int iz = std::max(il, 1);
+      double w = (double)(z - S.zlev[iz - 1]) / (S.zlev[iz] - S.zlev[iz - 1]);
+      w = std::max(std::min(w, 1.0), 0.0);
+      int ix = (int)(x / p.delx) + 1;
+      if (std::fabs(x - npx * p.delx) < 0.01f * p.delx) ix = npx;
+      if (ix < 1 || ix > npx) { err = "TRILIN: Beyond X domain"; return false; }
+      int ixp = ix % npx + 1;
+      double u = (double)(x - p.delx * (ix - 1)) / p.delx;
+      u = std::max(std::min(u, 1.0), 0.0);
+      if (u < 1e-5) u = 0; if (u > 1 - 1e-5) u = 1;
+      int iy = (int)(y / p.dely) + 1;
+      if (std::fabs(y - npy * p.dely) < 0.01f * p.dely) iy = npy;
+      if (iy < 1 || iy > npy) { err = "TRILIN: Beyond Y domain"; return false; }
+      int iyp = iy % npy + 1;
+      double v = (double)(y - p.dely * (iy - 1)) / p.dely;
+      v = std::max(std::min(v, 1.0), 0.0);
+      if (v < 1e-5) v = 0; if (v > 1 - 1e-5) v = 1;
+      const double f[8] = {(1 - u) * (1 - v) * (1 - w), u * (1 - v) * (1 - w), (1 - u) * v * (1 - w), u * v * (1 - w),
+                           (1 - u) * (1 - v) * w,       u * (1 - v) * w,       (1 - u) * v * w,       u * v * w};
+      int i1 = (iz - 1) + npz * (iy - 1) + npz * npy * (ix - 1), i2 = (iz - 1) + npz * (iy - 1) + npz * npy * (ixp - 1);
+      int i3 = (iz - 1) + npz * (iyp - 1) + npz * npy * (ix - 1), i4 = (iz - 1) + npz * (iyp - 1) + npz * npy * (ixp - 1);
+      const int ii[8] = {i1, i2, i3, i4, i1 + 1, i2 + 1, i3 + 1, i4 + 1};
+      for (int k = 0; k < 8; ++k) { interpptr[(size_t)ip * 8 + k] = ii[k]; optinterpwt[(size_t)ip * 8 + k] = (R)f[k]; }
+    }
+    fp.assign(ng, 0); dextm.assign((size_t)ng * NUMDER, 0);
+    for (int ib = 0; ib < ng; ++ib) {
+      R fv = 0;
+      if (p.deltam)
+        for (int q = 0; q < S.maxnmicro; ++q) fv += phwtp(q, ib) * S.legen[(size_t)(iphp(q, ib) - 1) * nl1 + ml + 1];
+      fp[ib] = fv;
+      for (int idr = 0; idr < NUMDER; ++idr)
+        dextm[(size_t)ib * NUMDER + idr] = dext(ib, idr) * ((R)1 - fv * albp(ib)) - dalb(ib, idr) * fv * extp(ib);
+    }
+    dalbm.assign((size_t)npts * 8 * NUMDER, 0); dfj.assign((size_t)npts * 8 * NUMDER, 0);
+    for (int ip = 0; ip < npts; ++ip) {
+      R F = 0, albj;
+      const R alb = S.albedo[(size_t)ipa * npts + ip];
+      if (p.deltam) {
+        const int *IPH = &S.iphase[((size_t)ipa * npts + ip) * S.nq];
+        const R *PW = &S.phaseinterpwt[((size_t)ipa * npts + ip) * S.nq];
+        if (PW[0] >= S.phasemax) F = S.legen[(size_t)(IPH[0] - 1) * nl1 + ml + 1];
+        else
+          for (int q = 0; q < S.nq; ++q) {
+            if (PW[q] < (R)1e-7) continue;
+            F += PW[q] * S.legen[(size_t)(IPH[q] - 1) * nl1 + ml + 1];
+          }
+        albj = alb / (F * (alb - 1) + 1);
+      } else {
+        albj = alb;
+      }
+      const R divide = (R)1 / ((R)1 - albj * F);
+      for (int nb = 0; nb < 8; ++nb) {
+        const int ib = interpptr[(size_t)ip * 8 + nb];
+        for (int idr = 0; idr < NUMDER; ++idr) {
+          const R DE = dext(ib, idr), DA = dalb(ib, idr), FP = fp[ib];
+          dalbm[((size_t)ip * 8 + nb) * NUMDER + idr] =
+              divide * (DE * (((R)1 - F) * (albp(ib) - albj) + (albj - 1) * albp(ib) * (FP - F)) +
+                        DA * (((R)1 - F) * extp(ib) + (albj - 1) * extp(ib) * (FP - F)));
+          dfj[((size_t)ip * 8 + nb) * NUMDER + idr] = (DE * (FP - F) * albp(ib) + DA * (FP - F) * extp(ib)) / ((R)1 - F);
+        }
+      }
+    }
+    return true;
+  }
+
+  // COMPUTE_SOURCE_DIRECTION (src/polarized/shdomsub4.f:2836-2915), scalar.
+  R source_direction(const R *L, int ip, const std::vector<R> &ylmdir, R secmu0) const {
+    R s = 0;
+    const int ris = S.rshptr[ip], rns = S.rshptr[ip + 1] - ris;
+    for (int j = 0; j < rns; ++j) s += L[S.lofj[j]] * S.radiance[(size_t)ris + j] * ylmdir[j];
+    if (!S.p.deltam)
+      for (int j = 0; j < S.nlm; ++j) s += S.dirflux[ip] * secmu0 * L[S.lofj[j]] * S.ylmsun[j] * ylmdir[j];
+    return s;
+  }
+
+  // COMPUTE_SOURCE_GRAD_1CELL (src/polarized/shdomsub4.f:1546-2042) for one
+  // new grid point: extinction, source x extinction, single scatter x
+  // extinction and GRAD8(NB, IDR).
+  void point_grad(int ip, const std::vector<R> &ylmdir, const std::vector<R> &singscat, R &ext8, R &srcext8,
+                  R &singscat8, R grad8[8][NUMDER]) const {
+    const auto &p = S.p;
+    const int npts = S.npts, ml = S.ml, mm = S.mm, nl1 = S.nleg + 1;
+    const R secmu0 = (R)1 / std::fabs((R)p.solarmu);
+    const R ext = S.total_ext[ip];
+    const int is = S.shptr[ip], ns = S.shptr[ip + 1] - is;
+    for (int nb = 0; nb < 8; ++nb) for (int idr = 0; idr < NUMDER; ++idr) grad8[nb][idr] = 0;
+    R src = 0, ss = 0;
+    for (int j = 0; j < ns; ++j) src += S.source[(size_t)is + j] * ylmdir[j];
+    std::vector<R> legent(nl1, 0);
+    R F = 0;
+    for (int ipa2 = 0; ipa2 < S.npart; ++ipa2) {
+      const R w = (ext == 0) ? (R)1 : S.extinct[(size_t)ipa2 * npts + ip] / ext;
+      if (w == 0) continue;
+      S.point_legen(ip, ipa2, legent, F);  // delta-M divided when deltam
+      const R da = S.albedo[(size_t)ipa2 * npts + ip] * S.dirflux[ip] * secmu0 * w;
+      R trunc = 0;
+      int J = 0;
+      for (int l = 0; l <= ml; ++l) {
+        const int me = std::min(l, mm);
+        const R a1 = da * legent[l];
+        if (J < ns)
+          for (int m = -me; m <= me; ++m) { trunc += a1 * ylmdir[J] * S.ylmsun[J]; ++J; }
+      }
+      if (p.deltam) {
+        const int *IPH = &S.iphase[((size_t)ipa2 * npts + ip) * S.nq];
+        const R *PW = &S.phaseinterpwt[((size_t)ipa2 * npts + ip) * S.nq];
+        if (PW[0] >= S.phasemax) ss += da * singscat[IPH[0] - 1] / ((R)1 - F);
+        else
+          for (int q = 0; q < S.nq; ++q) {
+            if (PW[q] <= (R)1e-5) continue;
+            ss += da * singscat[IPH[q] - 1] * PW[q] / ((R)1 - F);
+          }
+        src -= trunc;
+      } else {
+        ss += trunc;
+      }
+    }
+    if (p.deltam) src += ss;
+    // gradient: species ipa (the same for both derivatives)
+    R scatterj = 0, singscatj = 0, sourcet;
+    if (p.deltam) {
+      for (int nb = 0; nb < 8; ++nb) {
+        const int ib = interpptr[(size_t)ip * 8 + nb];
+        const R xi = optinterpwt[(size_t)ip * 8 + nb];
+        const R sw = xi * albp(ib) * extp(ib);
+        scatterj += sw;
+        if (sw <= (R)1e-6) continue;
+        for (int q = 0; q < S.maxnmicro; ++q) {
+          if (phwtp(q, ib) <= (R)1e-6) continue;
+          singscatj += sw * phwtp(q, ib) * singscat[iphp(q, ib) - 1];
+        }
+      }
+      singscatj = (scatterj > (R)S.scatmin) ? singscatj / scatterj : singscatj / (R)S.scatmin;
+    }
+    if (S.npart == 1) {
+      const R a = S.albedo[(size_t)ipa * npts + ip];
+      sourcet = (a > (R)1e-8) ? src / a : (R)0;
+    } else {
+      std::fill(legent.begin(), legent.end(), (R)0);
+      F = 0;
+      for (int nb = 0; nb < 8; ++nb) {
+        const int ib = interpptr[(size_t)ip * 8 + nb];
+        const R sw = optinterpwt[(size_t)ip * 8 + nb] * albp(ib) * extp(ib);
+        if (sw <= (R)1e-6) continue;
+        for (int q = 0; q < S.maxnmicro; ++q) {
+          if (phwtp(q, ib) <= (R)1e-6) continue;
+          const R *L = &S.legen[(size_t)(iphp(q, ib) - 1) * nl1];
+          for (int l = 0; l < nl1; ++l) legent[l] += sw * phwtp(q, ib) * L[l];
+        }
+      }
+      const R div = (scatterj > (R)S.scatmin) ? scatterj : (R)S.scatmin;
+      for (int l = 0; l < nl1; ++l) legent[l] /= div;
+      if (p.deltam) {
+        F = legent[ml + 1];
+        for (int l = 0; l <= ml; ++l) legent[l] /= ((R)1 - F);
+      }
+      sourcet = 0;
+      if (scatterj > (R)S.scatmin) {
+        sourcet = source_direction(legent.data(), ip, ylmdir, secmu0);
+        if (p.deltam) sourcet += S.dirflux[ip] * singscatj * secmu0 / ((R)1 - F);
+      }
+    }
+    sourcet = std::max((R)0, sourcet);
+    if (p.deltam)
+      for (int l = 0; l <= ml; ++l) legent[l] = legent[l] * ((R)1 - F) + F;
+    std::vector<R> legenp(nl1), dlegt(nl1);
+    const R albip = S.albedo[(size_t)ipa * npts + ip];
+    for (int nb = 0; nb < 8; ++nb) {
+      const int ib = interpptr[(size_t)ip * 8 + nb];
+      const R xi = optinterpwt[(size_t)ip * 8 + nb];
+      if (xi < (R)1e-7) continue;
+      std::fill(legenp.begin(), legenp.end(), (R)0);
+      for (int q = 0; q < S.maxnmicro; ++q) {
+        const R *L = &S.legen[(size_t)(iphp(q, ib) - 1) * nl1];
+        const R ft = p.deltam ? L[ml + 1] : (R)0;
+        for (int l = 0; l < nl1; ++l) legenp[l] += phwtp(q, ib) * ((p.deltam && l <= ml) ? L[l] + ft : L[l]);
+      }
+      R singscatp = 0;
+      if (p.deltam)
+        for (int q = 0; q < S.maxnmicro; ++q) singscatp += phwtp(q, ib) * singscat[iphp(q, ib) - 1];
+      for (int idr = 0; idr < NUMDER; ++idr) {
+        const R DE = dext(ib, idr), DA = dalb(ib, idr);
+        const R DFJ = dfj[((size_t)ip * 8 + nb) * NUMDER + idr];
+        for (int l = 0; l < nl1; ++l) {
+          const R diff = legenp[l] - legent[l];
+          dlegt[l] = DE * diff * albp(ib) + DA * diff * extp(ib) + (legent[l] - 1) * DFJ;
+        }
+        const R dsource = source_direction(dlegt.data(), ip, ylmdir, secmu0);
+        R g = xi * (sourcet * (albip * dextm[(size_t)ib * NUMDER + idr] + dalbm[((size_t)ip * 8 + nb) * NUMDER + idr]) + dsource);
+        if (p.deltam)
+          g += S.dirflux[ip] * secmu0 * xi *
+               (singscatj * DFJ + DA * (singscatp - singscatj) * extp(ib) + DE * (singscatp - singscatj) * albp(ib));
+        grad8[nb][idr] += g;
+      }
+    }
+    singscat8 = ss * ext;
+    srcext8 = src * ext;
+    ext8 = ext;
+  }
+
+  // ADJOINT_INTEGRATE_1RAY (src/polarized/shdomsub4.f:3223-3967) with
+  // COMPUTE_RADIANCE_DERIVATIVE_ADJOINT (:4037-4114); accumulates into
+  // gradout [ng][2] and beam_weight [npts].
+  bool adjoint_ray(double mu2, double phi2, double x0, double y0, double z0, double adj, std::vector<double> &gradout,
+                   std::vector<double> &beam, std::string &err) const {
+    const auto &p = S.p;
+    const double pi = std::acos(-1.0);
+    const int nx = S.nx, ny = S.ny;
+    const double eps = 1.0e-5 * (S.gridpos[3 * S.gridptr[7] + 2] - S.gridpos[3 * S.gridptr[0] + 2]);
+    std::vector<R> ylmdir = S.ylmall((double)(float)mu2, (float)phi2);
+    std::vector<R> singscat(S.numphase, 0);
+    if (p.deltam) {
+      double cosscat = (double)p.solarmu * mu2 +
+                       std::sqrt((1.0 - (double)p.solarmu * p.solarmu) * (1.0 - mu2 * mu2)) * std::cos((double)p.solaraz - phi2);
+      cosscat = std::max(std::min(1.0, cosscat), -1.0);
+      float F = (float)((S.nscatangle - 1) * (std::acos(cosscat) / pi) + 1);
+      int J = std::min(S.nscatangle - 1, (int)F);
+      F = F - J;
+      for (int i = 0; i < S.numphase; ++i)
+        singscat[i] = (R)((1 - F) * S.phasetab[(size_t)(J - 1) * S.numphase + i] + F * S.phasetab[(size_t)J * S.numphase + i]);
+    }
+    double cx = std::sqrt(1.0 - mu2 * mu2) * std::cos(phi2 - pi), cy = std::sqrt(1.0 - mu2 * mu2) * std::sin(phi2 - pi);
+    double cz = -mu2, cxinv, cyinv, czinv;
+    if (std::fabs(cx) > 1e-6) cxinv = 1.0 / cx; else { cx = 0; cxinv = 1e6; }
+    if (std::fabs(cy) > 1e-6) cyinv = 1.0 / cy; else { cy = 0; cyinv = 1e6; }
+    if (std::fabs(cz) > 1e-6) czinv = 1.0 / cz; else { cz = 0; czinv = 1e6; }
+    const int bitx = cx < 0, bity = cy < 0, bitz = cz < 0, ioct = 1 + bitx + 2 * bity + 4 * bitz;
+    const float xm = 0.5f * (S.xgrid[0] + S.xgrid[nx - 1]), ym = 0.5f * (S.ygrid[0] + S.ygrid[ny - 1]);
+    double xe = x0, ye = y0, ze = z0;
+    int icell = S.locate_grid_cell(xe, ye, ze);
+    int iface = -1;
+    double transmit = 1.0;
+    R extinct8[8] = {0}, srcext8[8] = {0}, singscat8[8] = {0}, grad8[8][8][NUMDER];
+    for (auto &a : grad8) for (auto &b : a) for (auto &c : b) c = 0;
+    int oldipts[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+    static const int doneface[7][8] = {{0, 0, 0, 0, 0, 0, 0, 0}, {0, 1, 0, 3, 0, 5, 0, 7}, {2, 0, 4, 0, 6, 0, 8, 0},
+                                       {0, 0, 1, 2, 0, 0, 5, 6}, {3, 4, 0, 0, 7, 8, 0, 0}, {0, 0, 0, 0, 1, 2, 3, 4},
+                                       {5, 6, 7, 8, 0, 0, 0, 0}};
+    // per subgrid interval (PASSED* arrays)
+    std::vector<int> ppts;
+    std::vector<double> pint0, pint1, pdels, prad, pabs, ptr;
+    auto push = [&]() {
+      ppts.resize(ppts.size() + 8, 0); pint0.resize(pint0.size() + 8, 0.0); pint1.resize(pint1.size() + 8, 0.0);
+      pdels.push_back(0); prad.push_back(0); pabs.push_back(0); ptr.push_back(1);
+    };
+    push();
+    int np = 0;  // current interval index (NPASSED - 1)
+    bool validrad = false;
+    const double c12 = (double)0.08333333333f;
+    while (!validrad && icell >= 0) {
+      R oext8[8], osrc8[8], oss8[8], ogr8[8][8][NUMDER];
+      for (int i = 0; i < 8; ++i) {
+        oext8[i] = extinct8[i]; osrc8[i] = srcext8[i]; oss8[i] = singscat8[i];
+        for (int nb = 0; nb < 8; ++nb) for (int d = 0; d < NUMDER; ++d) ogr8[i][nb][d] = grad8[i][nb][d];
+      }
+      for (int n = 0; n < 8; ++n) {
+        const int ip = S.gridptr[8 * icell + n];
+        const int I = doneface[iface + 1][n];
+        if (I > 0 && ip == oldipts[n]) {
+          extinct8[n] = oext8[I - 1]; srcext8[n] = osrc8[I - 1]; singscat8[n] = oss8[I - 1];
+          for (int nb = 0; nb < 8; ++nb) for (int d = 0; d < NUMDER; ++d) grad8[n][nb][d] = ogr8[I - 1][nb][d];
+          continue;
+        }
+        oldipts[n] = ip;
+        point_grad(ip, ylmdir, singscat, extinct8[n], srcext8[n], singscat8[n], grad8[n]);
+      }
+      const int ipt1 = S.gridptr[8 * icell], ipt2 = S.gridptr[8 * icell + 7];
+      const double delx = S.gridpos[3 * ipt2] - S.gridpos[3 * ipt1], dely = S.gridpos[3 * ipt2 + 1] - S.gridpos[3 * ipt1 + 1];
+      const double delz = S.gridpos[3 * ipt2 + 2] - S.gridpos[3 * ipt1 + 2];
+      const double ivx = delx <= 0 ? 1.0 : 1.0 / delx, ivy = dely <= 0 ? 1.0 : 1.0 / dely, ivz = 1.0 / delz;
+      auto kernel = [&](double x, double y, double z, double fc[8]) {
+        const double u = (x - S.gridpos[3 * ipt1]) * ivx, v = (y - S.gridpos[3 * ipt1 + 1]) * ivy,
+                     w = (z - S.gridpos[3 * ipt1 + 2]) * ivz;
+        fc[0] = (1 - w) * (1 - v) * (1 - u); fc[1] = (1 - w) * (1 - v) * u; fc[2] = (1 - w) * v * (1 - u); fc[3] = (1 - w) * v * u;
+        fc[4] = w * (1 - v) * (1 - u); fc[5] = w * (1 - v) * u; fc[6] = w * v * (1 - u); fc[7] = w * v * u;
+      };
+      double fc[8];
+      kernel(xe, ye, ze, fc);
+      R srcext1 = 0, ext1 = 0;
+      for (int k = 0; k < 8; ++k) { srcext1 = (R)(srcext1 + fc[k] * srcext8[k]); }
+      srcext1 = std::max((R)0, srcext1);
+      for (int k = 0; k < 8; ++k) ext1 = (R)(ext1 + fc[k] * extinct8[k]);
+      for (int k = 0; k < 8; ++k) pint1[8 * np + k] = fc[k];
+      R ss1[8], gr1[8][8][NUMDER];
+      for (int n = 0; n < 8; ++n) {
+        ss1[n] = std::max((R)0, (R)(fc[n] * singscat8[n]));
+        for (int nb = 0; nb < 8; ++nb) for (int d = 0; d < NUMDER; ++d) gr1[n][nb][d] = (R)(fc[n] * grad8[n][nb][d]);
+      }
+      const bool ipinx = (S.cellflags[icell] & 1) && !((S.bcflag & 1) && ((cx > 0 && xe < xm) || (cx < 0 && xe > xm)));
+      const bool ipiny = (S.cellflags[icell] & 2) && !((S.bcflag & 2) && ((cy > 0 && ye < ym) || (cy < 0 && ye > ym)));
+      const int iopp = S.gridptr[8 * icell + (8 - ioct)];
+      const double sox = ipinx ? 1e20 : (S.gridpos[3 * iopp] - xe) * cxinv;
+      const double soy = ipiny ? 1e20 : (S.gridpos[3 * iopp + 1] - ye) * cyinv;
+      const double soz = (S.gridpos[3 * iopp + 2] - ze) * czinv;
+      const double so = std::min(sox, std::min(soy, soz));
+      if (so < -eps) { err = "ADJOINT_INTEGRATE_1RAY: SO<0"; return false; }
+      double xn = xe + so * cx, yn = ye + so * cy, zn = ze + so * cz;
+      double fcn[8];
+      kernel(xn, yn, zn, fcn);
+      R extn = 0;
+      for (int k = 0; k < 8; ++k) extn = (R)(extn + fcn[k] * extinct8[k]);
+      const double taugrid = so * 0.5 * (ext1 + extn);
+      const int ntau = std::max(1, 1 + (int)(taugrid / p.tautol));
+      const double dels = so / ntau;
+      double srcss[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      for (int it = 1; it <= ntau; ++it) {
+        pdels[np] = dels;
+        for (int k = 0; k < 8; ++k) { pint1[8 * np + k] = fc[k]; ppts[8 * np + k] = S.gridptr[8 * icell + k]; }
+        const double s = it * dels;
+        kernel(xe + s * cx, ye + s * cy, ze + s * cz, fc);
+        R srcext0 = 0, ext0 = 0;
+        for (int k = 0; k < 8; ++k) srcext0 = (R)(srcext0 + fc[k] * srcext8[k]);
+        if (it != ntau) { for (int k = 0; k < 8; ++k) ext0 = (R)(ext0 + fc[k] * extinct8[k]); }
+        else ext0 = extn;
+        srcext0 = std::max((R)0, srcext0);
+        for (int k = 0; k < 8; ++k) pint0[8 * np + k] = fc[k];
+        R ss0[8], gr0[8][8][NUMDER];
+        for (int n = 0; n < 8; ++n) {
+          ss0[n] = std::max((R)0, (R)(fc[n] * singscat8[n]));
+          for (int nb = 0; nb < 8; ++nb) for (int d = 0; d < NUMDER; ++d) gr0[n][nb][d] = (R)(fc[n] * grad8[n][nb][d]);
+        }
+        const double ext = 0.5 * (ext0 + ext1);
+        double transcell;
+        if (ext != 0.0) {
+          const double tau = ext * dels;
+          const double abscell = tau * (1.0 - 0.5 * tau * (1.0 - 0.33333333333 * tau));
+          transcell = 1.0 - abscell;
+          const double corr = dels * (1.0 - 0.05 * (ext1 - ext0) * dels);
+          const double src = (0.5 * (srcext0 + srcext1) + c12 * (ext0 * srcext1 - ext1 * srcext0) * corr) / ext;
+          for (int n = 0; n < 8; ++n) {
+            srcss[n] += transmit * abscell * (0.5 * (ss0[n] + ss1[n]) + c12 * (ext0 * ss1[n] - ext1 * ss0[n]) * corr) / ext;
+          }
+          pabs[np] = abscell; ptr[np] = transmit; prad[np] = transmit * src * abscell;
+          for (int kk = 0; kk < 8; ++kk) {
+            const int ip = S.gridptr[8 * icell + kk];
+            for (int k = 0; k < 8; ++k) {
+              const int ib = interpptr[(size_t)ip * 8 + k];
+              for (int d = 0; d < NUMDER; ++d) {
+                const R sg = (R)((0.5 * (gr0[kk][k][d] + gr1[kk][k][d]) + c12 * (ext0 * gr1[kk][k][d] - ext1 * gr0[kk][k][d]) * corr) / ext);
+                gradout[(size_t)ib * NUMDER + d] += transmit * (adj * sg) * abscell;
+              }
+            }
+          }
+          ++np;
+          push();
+        } else {
+          transcell = 1.0;
+          for (int n = 0; n < 8; ++n) srcss[n] = 0;
+        }
+        transmit *= transcell;
+        ext1 = ext0; srcext1 = srcext0;
+        for (int n = 0; n < 8; ++n) {
+          ss1[n] = ss0[n];
+          for (int nb = 0; nb < 8; ++nb) for (int d = 0; d < NUMDER; ++d) gr1[n][nb][d] = gr0[n][nb][d];
+        }
+      }
+      for (int kk = 0; kk < 8; ++kk) beam[S.gridptr[8 * icell + kk]] += adj * srcss[kk];
+      int jface;
+      bool openbcface;
+      if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; openbcface = (S.cellflags[icell] & 1) && (S.bcflag & 1); }
+      else if (soy <= soz) { iface = 3 - bity; jface = 1; openbcface = (S.cellflags[icell] & 2) && (S.bcflag & 2); }
+      else { iface = 5 - bitz; jface = 2; openbcface = false; }
+      const int inext = S.neighptr[6 * icell + iface];
+      int kface, ic;
+      if (!openbcface) { kface = iface; ic = icell; }
+      else { kface = kOppFace[iface]; ic = inext; iface = -1; }
+      if (inext >= 0) {
+        if (jface == 0) xn = S.gridpos[3 * S.gridptr[8 * inext + ioct - 1]];
+        else if (jface == 1) yn = S.gridpos[3 * S.gridptr[8 * inext + ioct - 1] + 1];
+        else zn = S.gridpos[3 * S.gridptr[8 * inext + ioct - 1] + 2];
+      }
+      if (transmit < p.transcut) {
+        validrad = true;
+        prad[np] = 0.0; ptr[np] = 1.0;
+      } else if (inext < 0 && iface >= 4) {
+        validrad = true;
+        double xs[4], ys[4], rb[4], dr[4];
+        int bp[4];
+        for (int jj = 0; jj < 4; ++jj) {
+          const int ipb = S.gridptr[8 * ic + kGridFace[kface][jj]];
+          bp[jj] = ipb; xs[jj] = S.gridpos[3 * ipb]; ys[jj] = S.gridpos[3 * ipb + 1]; dr[jj] = 0;
+          if ((float)mu2 < 0.0f) {
+            rb[jj] = p.skyrad;
+          } else {
+            auto itb = std::lower_bound(S.botp.begin(), S.botp.end(), ipb);
+            if (itb == S.botp.end() || *itb != ipb) { err = "FIND_BOUNDARY_RADIANCE: Not at boundary"; return false; }
+            const size_t b = itb - S.botp.begin();
+            rb[jj] = S.bcrad_bot[b];
+            dr[jj] = (double)((float)(1.0 / std::acos(-1.0)) * S.sfcgridalb[b] * S.dirflux[ipb]);
+          }
+        }
+        const double uu = (xs[1] - xs[0] > 0) ? (xn - xs[0]) / (xs[1] - xs[0]) : 0.0;
+        const double vv = (ys[2] - ys[0] > 0) ? (yn - ys[0]) / (ys[2] - ys[0]) : 0.0;
+        const double bi[4] = {(1 - uu) * (1 - vv), uu * (1 - vv), (1 - uu) * vv, uu * vv};
+        const float radbnd = (float)(bi[0] * rb[0] + bi[1] * rb[1] + bi[2] * rb[2] + bi[3] * rb[3]);
+        ptr[np] = transmit; pabs[np] = -1.0; prad[np] = transmit * radbnd;
+        for (int kk = 0; kk < 4; ++kk) beam[bp[kk]] += adj * transmit * bi[kk] * dr[kk];
+      } else {
+        icell = inext;
+      }
+      xe = xn; ye = yn; ze = zn;
+    }
+    // future radiance: backward sum, divided by the transmission
+    const int npassed = np + 1;
+    for (int kk = npassed - 2; kk >= 0; --kk) prad[kk] += prad[kk + 1];
+    for (int kk = 0; kk < npassed; ++kk) prad[kk] /= ptr[kk];
+    for (int kk = 0; kk < npassed - 1; ++kk) {
+      double ext0 = 0, ext1 = 0;
+      for (int k = 0; k < 8; ++k) {
+        ext0 += S.total_ext[ppts[8 * kk + k]] * pint0[8 * kk + k];
+        ext1 += S.total_ext[ppts[8 * kk + k]] * pint1[8 * kk + k];
+      }
+      const double ext = 0.5 * (ext0 + ext1), dl = pdels[kk];
+      if (ext == 0.0) continue;
+      for (int k = 0; k < 8; ++k) {
+        const int ip = ppts[8 * kk + k];
+        const double g0 = -adj * prad[kk + 1] * pint0[8 * kk + k];
+        const double g1 = -adj * prad[kk] * pint1[8 * kk + k];
+        double ag = (0.5 * (g0 + g1) + c12 * (ext0 * g1 - ext1 * g0) * dl * (1.0 - 0.05 * (ext1 - ext0) * dl)) / ext;
+        ag *= ptr[kk] * pabs[kk];
+        for (int d = 0; d < NUMDER; ++d)
+          for (int nb = 0; nb < 8; ++nb) {
+            const int ib = interpptr[(size_t)ip * 8 + nb];
+            const float eg = (float)(dextm[(size_t)ib * NUMDER + d] * optinterpwt[(size_t)ip * 8 + nb]);
+            gradout[(size_t)ib * NUMDER + d] += eg * ag;
+          }
+      }
+    }
+    return true;
+  }
+
+  // COMPUTE_DIRECT_BEAM_DERIV_ADJOINT (src/polarized/shdomsub4.f:4117-4143)
+  // with the sun-path derivatives of DIRECT_BEAM_AND_PATHS_PROP
+  // (src/shdomsub5.f:1608-2345): d(optical path)/d(extinction at each
+  // property corner) of the trilinear path integral, cell by cell.
+  void direct_beam_deriv(int ipt, double weight, std::vector<double> &gradout) const {
+    const auto &p = S.p;
+    const int npx = p.npx, npy = p.npy, npz = p.npz, bcflag = S.bcflag;
+    int ipdirect = S.ipflag;
+    if (S.ipflag & 4) ipdirect = 0;
+    const double sunmu = -(double)p.solarmu, sunaz = (double)(float)(p.solaraz + (float)std::acos(-1.0f));
+    double cx = std::sqrt(1.0 - sunmu * sunmu) * std::cos(sunaz), cy = std::sqrt(1.0 - sunmu * sunmu) * std::sin(sunaz);
+    double cz = std::fabs(sunmu), cxinv, cyinv, czinv;
+    if (std::fabs(cx) > 1e-6) cxinv = 1.0 / cx; else { cx = 0; cxinv = 1e20; }
+    if (std::fabs(cy) > 1e-6) cyinv = 1.0 / cy; else { cy = 0; cyinv = 1e20; }
+    if (std::fabs(cz) > 1e-6) czinv = 1.0 / cz; else { cz = 0; czinv = 1e20; }
+    const int di = cx >= 0 ? 1 : -1, dj = cy >= 0 ? 1 : -1, dk = cz >= 0 ? 1 : -1;
+    const double epsz = 1.0e-6 * (S.zlev[npz - 1] - S.zlev[0]);
+    const double delxd = p.delx, delyd = p.dely, xdomain = delxd * npx, ydomain = delyd * npy;
+    const double z = S.gridpos[3 * ipt + 2], x = S.gridpos[3 * ipt], y = S.gridpos[3 * ipt + 1];
+    int il = 0, iu = npz;
+    while (iu - il > 1) { int im = (iu + il) / 2; if (z >= S.zlev[im - 1]) il = im; else iu = im; }
+    int k = std::max(il, 1);
+    int i = (int)(x / delxd) + 1;
+    if (i > npx && std::fabs(x - xdomain) < 0.001 * delxd) i = npx;
+    int j = (int)(y / delyd) + 1;
+    if (j > npy && std::fabs(y - ydomain) < 0.001 * delyd) j = npy;
+    double xe = x, ye = y, ze = z, xp = xe, yp = ye, zp = ze;
+    bool constx = ipdirect & 1, consty = ipdirect & 2;
+    if (cx == 0.0) constx = true;
+    if (cy == 0.0) consty = true;
+    if ((bcflag & 1) && (std::fabs(x) < 0.01 * delxd || std::fabs(x - (npx - 1) * delxd) < 0.01 * delxd)) constx = true;
+    if ((bcflag & 2) && (std::fabs(y) < 0.01 * delyd || std::fabs(y - (npy - 1) * delyd) < 0.01 * delyd)) consty = true;
+    int guard = 0;
+    while (std::fabs(ze - S.zlev[npz - 1]) > epsz && guard++ < 10000000) {
+      int ipn = i + 1;
+      if (i == npx) ipn = (bcflag & 1) ? npx : 1;
+      int jpn = j + 1;
+      if (j == npy) jpn = (bcflag & 2) ? npy : 1;
+      const double x0 = delxd * (i - 1), x1 = x0 + delxd, y0 = delyd * (j - 1), y1 = y0 + delyd;
+      const double z0 = S.zlev[k - 1], z1 = S.zlev[k];
+      const int I1 = (k - 1) + npz * (j - 1) + npz * npy * (i - 1), I2 = (k - 1) + npz * (j - 1) + npz * npy * (ipn - 1);
+      const int I3 = (k - 1) + npz * (jpn - 1) + npz * npy * (i - 1), I4 = (k - 1) + npz * (jpn - 1) + npz * npy * (ipn - 1);
+      double sox, soy, soz;
+      if (constx) sox = 1e30; else if (cx > 0) { sox = (x1 - xe) * cxinv; xp = x1; } else { sox = (x0 - xe) * cxinv; xp = x0; }
+      if (consty) soy = 1e30; else if (cy > 0) { soy = (y1 - ye) * cyinv; yp = y1; } else { soy = (y0 - ye) * cyinv; yp = y0; }
+      if (cz > 0) { soz = (z1 - ze) * czinv; zp = z1; } else if (cz < 0) { soz = (z0 - ze) * czinv; zp = z0; } else soz = 1e30;
+      double xoffs = 0, yoffs = 0, so;
+      if (soz <= sox && soz <= soy) {
+        so = soz;
+        if (!constx) xp = xe + so * cx;
+        if (!consty) yp = ye + so * cy;
+        k += dk;
+      } else if (sox <= soy) {
+        so = sox;
+        if (!consty) yp = ye + so * cy;
+        zp = ze + so * cz;
+        i += di;
+        if (i == 0) { if (bcflag & 1) { i = 1; constx = true; } else { i = npx; xoffs = xdomain; } }
+        else if (i == npx + 1) { if (bcflag & 1) { i = npx; constx = true; } else { i = 1; xoffs = -xdomain; } }
+      } else {
+        so = soy;
+        if (!constx) xp = xe + so * cx;
+        zp = ze + so * cz;
+        j += dj;
+        if (j == 0) { if (bcflag & 2) { j = 1; consty = true; } else { j = npy; yoffs = ydomain; } }
+        else if (j == npy + 1) { if (bcflag & 2) { j = npy; consty = true; } else { j = 1; yoffs = -ydomain; } }
+      }
+      so = std::max(so, 0.0);
+      const double ax = 1.0 / (x1 - x0), ay = 1.0 / (y1 - y0), az = 1.0 / (z1 - z0);
+      const double u0 = (xe - x0) * ax, v0 = (ye - y0) * ay, w0 = (ze - z0) * az;
+      const double du = (xp - x0) * ax - u0, dv = (yp - y0) * ay - v0, dw = (zp - z0) * az - w0;
+      const double u0m = 1 - u0, v0m = 1 - v0, w0m = 1 - w0;
+      const double uv = u0 * v0, umv = u0m * v0, uvm = u0 * v0m, umvm = u0m * v0m;
+      const double uw = u0 * w0, umw = u0m * w0, uwm = u0 * w0m, umwm = u0m * w0m;
+      const double vw = v0 * w0, vmw = v0m * w0, vwm = v0 * w0m, vmwm = v0m * w0m;
+      const double A[8] = {u0m * vmwm, u0 * vmwm, u0m * vwm, u0 * vwm, u0m * vmw, u0 * vmw, u0m * vw, u0 * vw};
+      const double B[8] = {-du * vmwm - dv * umwm - dw * umvm, du * vmwm - dv * uwm - dw * uvm,
+                           -du * vwm + dv * umwm - dw * umv,   du * vwm + dv * uwm - dw * uv,
+                           -du * vmw - dv * umw + dw * umvm,   du * vmw - dv * uw + dw * uvm,
+                           -du * vw + dv * umw + dw * umv,     du * vw + dv * uw + dw * uv};
+      const double VW = dv * dw, vwu = VW * u0, vwum = VW * u0m, UW = du * dw, uwv = UW * v0, uwvm = UW * v0m;
+      const double UV = du * dv, uvw = UV * w0, uvwm = UV * w0m;
+      const double C[8] = {vwum + uwvm + uvwm, vwu - uwvm - uvwm, -vwum + uwv - uvwm, -vwu - uwv + uvwm,
+                           -vwum - uwvm + uvw, -vwu + uwvm - uvw, vwum - uwv - uvw,   vwu + uwv + uvw};
+      const double sgn[8] = {-1, 1, 1, -1, 1, -1, -1, 1}, ddd = du * dv * dw;
+      const int ptrs[8] = {I1, I2, I3, I4, I1 + 1, I2 + 1, I3 + 1, I4 + 1};
+      for (int c = 0; c < 8; ++c) {
+        const float dpath = (float)(so * (A[c] + 0.5 * B[c] + 0.3333333333333333 * C[c] + sgn[c] * 0.25 * ddd));
+        for (int d = 0; d < NUMDER; ++d)
+          gradout[(size_t)ptrs[c] * NUMDER + d] -= dextm[(size_t)ptrs[c] * NUMDER + d] * dpath * weight;
+      }
+      xe = xp + xoffs; ye = yp + yoffs; ze = zp;
+    }
+  }
+};
+
+// Render with the properties of one property-grid voxel of species ipa
+// perturbed and the source function recomputed from the frozen RADIANCE
+// (new delta-M medium and direct beam, same truncations): the forward model
+// whose derivative the Levis approximation is.  The solver state is
+// restored afterwards.
+template <typename R>
+bool frozen_render(Solver<R> &S, int ipa, int voxel, float dext, float dalb, int n, const float *camx,
+                   const float *camy, const float *camz, const double *cammu, const double *camphi, float *out,
+                   int nthreads) {
+  const int ng = S.p.npx * S.p.npy * S.p.npz;
+  if (ipa < 0 || ipa >= S.npart || voxel < 0 || voxel >= ng) { S.err = "frozen_render: bad index"; return false; }
+  auto extp = S.extp, albp = S.albp;
+  auto source = S.source;
+  auto shptr = S.shptr;
+  auto extinct = S.extinct, albedo = S.albedo, total_ext = S.total_ext, phaseinterpwt = S.phaseinterpwt;
+  auto iphase = S.iphase;
+  auto dirflux = S.dirflux;
+  auto legen = S.legen;
+  const R albmax = S.albmax;
+  S.extp[(size_t)ipa * ng + voxel] += dext;
+  S.albp[(size_t)ipa * ng + voxel] += dalb;
+  bool ok = S.transfer_properties();
+  if (ok) {
+    S.make_direct();
+    S.compute_source(true, true);
+    ok = S.render(n, camx, camy, camz, cammu, camphi, out, nthreads);
+  }
+  S.extp = extp; S.albp = albp; S.source = source; S.shptr = shptr; S.extinct = extinct; S.albedo = albedo;
+  S.total_ext = total_ext; S.phaseinterpwt = phaseinterpwt; S.iphase = iphase; S.dirflux = dirflux; S.legen = legen;
+  S.albmax = albmax;
+  return ok;
+}
+
+template <typename R>
+bool levis_gradient(Solver<R> &S, int ipa, int n, const float *camx, const float *camy, const float *camz,
+                    const double *cammu, const double *camphi, const float *meas, double *gradout, double *cost,
+                    float *stokesout, int nthreads) {
+  if (ipa < 0 || ipa >= S.npart) { S.err = "levis_gradient: bad species index"; return false; }
+  if (!S.render(n, camx, camy, camz, cammu, camphi, stokesout, nthreads)) return false;  // phase 1 (with phasetab, bcrad)
+  Levis<R> L(S);
+  if (!L.prepare(ipa, S.err)) return false;
+  // phase 2: L2 adjoint weights and cost
+  std::vector<double> adj(n);
+  double c = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const double e = (double)stokesout[i] - (double)meas[i];
+    c += 0.5 * e * e;
+    adj[i] = e;
+  }
+  *cost = c;
+  // phase 3: adjoint rays (per-thread accumulators)
+  const int nt = std::max(1, nthreads);
+  std::vector<std::vector<double>> g(nt, std::vector<double>((size_t)L.ng * 2, 0.0)), bw(nt, std::vector<double>(S.npts, 0.0));
+  std::vector<std::string> errs(nt);
+  std::vector<int> bad(nt, 0);
+  const double pi = std::acos(-1.0);
+  auto work = [&](int t, int b, int e) {
+    for (int iv = b; iv < e; ++iv) {
+      double x0 = camx[iv], y0 = camy[iv], z0 = camz[iv], mu2 = cammu[iv], phi2 = camphi[iv];
+      double muray = -mu2, phiray = phi2 - pi;
+      if (z0 > S.zgrid[S.nz - 1]) {
+        if (muray >= 0.0) continue;
+        double r = (S.zgrid[S.nz - 1] - z0) / muray;
+        x0 = x0 + r * std::sqrt(1 - muray * muray) * std::cos(phiray);
+        y0 = y0 + r * std::sqrt(1 - muray * muray) * std::sin(phiray);
+        z0 = S.zgrid[S.nz - 1];
+      } else if (z0 < S.zgrid[0]) { bad[t] = 1; errs[t] = "LEVISAPPROX_GRADIENT: Level below domain"; return; }
+      if (!L.adjoint_ray(mu2, phi2, x0, y0, z0, adj[iv], g[t], bw[t], errs[t])) { bad[t] = 1; return; }
+    }
+  };
+  if (nt <= 1) work(0, 0, n);
+  else {
+    std::vector<std::thread> th;
+    int chunk = (n + nt - 1) / nt;
+    for (int t = 0; t < nt; ++t) th.emplace_back(work, t, std::min(n, t * chunk), std::min(n, (t + 1) * chunk));
+    for (auto &x : th) x.join();
+  }
+  for (int t = 0; t < nt; ++t) if (bad[t]) { S.err = errs[t]; return false; }
+  std::vector<double> G((size_t)L.ng * 2, 0.0), beam(S.npts, 0.0);
+  for (int t = 0; t < nt; ++t) {
+    for (size_t k = 0; k < G.size(); ++k) G[k] += g[t][k];
+    for (int k = 0; k < S.npts; ++k) beam[k] += bw[t][k];
+  }
+  // phase 4: direct-beam derivative per grid point
+  for (int ip = 0; ip < S.npts; ++ip)
+    if (beam[ip] != 0.0) L.direct_beam_deriv(ip, beam[ip], G);
+  for (size_t k = 0; k < G.size(); ++k) gradout[k] = G[k];
+  return true;
+}
+
 struct Handle {
   int fp64 = 0;
   Solver<float> *s32 = nullptr;
@@ -1648,6 +2302,30 @@ int oracle_render(void *hv, int n, const float *camx, const float *camy, const f
   Handle *h = (Handle *)hv;
   bool ok = h->fp64 ? h->s64->render(n, camx, camy, camz, cammu, camphi, out, nthreads)
                     : h->s32->render(n, camx, camy, camz, cammu, camphi, out, nthreads);
+  return ok ? 0 : 1;
+}
+
+// Levis approximate gradient (adjoint branch) of the L2 cost of n one-ray
+// pixels with respect to the extinction and single-scattering albedo of
+// species ipa (0-based) on the property grid: gradout [npx*npy*npz][2]
+// (extinction, albedo), cost, and the rendered radiances.
+int oracle_levis_gradient(void *hv, int ipa, int n, const float *camx, const float *camy, const float *camz,
+                          const double *cammu, const double *camphi, const float *meas, double *gradout,
+                          double *cost, float *stokesout, int nthreads) {
+  Handle *h = (Handle *)hv;
+  bool ok = h->fp64 ? orc::levis_gradient(*h->s64, ipa, n, camx, camy, camz, cammu, camphi, meas, gradout, cost,
+                                          stokesout, nthreads)
+                    : orc::levis_gradient(*h->s32, ipa, n, camx, camy, camz, cammu, camphi, meas, gradout, cost,
+                                          stokesout, nthreads);
+  return ok ? 0 : 1;
+}
+
+int oracle_frozen_render(void *hv, int ipa, int voxel, float dext, float dalb, int n, const float *camx,
+                         const float *camy, const float *camz, const double *cammu, const double *camphi, float *out,
+                         int nthreads) {
+  Handle *h = (Handle *)hv;
+  bool ok = h->fp64 ? orc::frozen_render(*h->s64, ipa, voxel, dext, dalb, n, camx, camy, camz, cammu, camphi, out, nthreads)
+                    : orc::frozen_render(*h->s32, ipa, voxel, dext, dalb, n, camx, camy, camz, cammu, camphi, out, nthreads);
   return ok ? 0 : 1;
 }
 
