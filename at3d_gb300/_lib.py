@@ -30,6 +30,7 @@ SIGNATURES = {
     "shdom_render": (C.c_int, [C.c_void_p, C.c_int, _f, _f, _f, _d, _d, _f]),
     "shdom_render_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.c_void_p, C.c_void_p]),
+    "shdom_render_noalloc": (C.c_int, [C.c_void_p, C.c_int, _f, _f, _f, _d, _d, _f]),
     "shdom_export_state": (C.c_int, [C.c_void_p, _f, _i, _f, _i, _f, _f]),
     "shdom_get_sizes": (C.c_int, [C.c_void_p, C.POINTER(ShdomSizes)]),
     "shdom_last_timings": (C.c_int, [C.c_void_p, _f]),

@@ -27,6 +27,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -2170,6 +2171,77 @@ int shdom_levis_adjoint(shdom_handle *hh, int species, int nrays, const float *c
   } catch (const std::exception &e) {
     return fail(hh, e.what());
   }
+}
+
+}  // extern "C"
+
+// ------------------------------------------------ render without allocation
+// Staging for shdom_render_noalloc: the rays and the radiances of one call
+// in a fixed device array (x, y, z, out as float, mu, phi as double), so
+// the call needs no device allocation.  Its address is looked up once per
+// device.
+namespace shdom {
+constexpr int kNoAllocMaxRays = 1 << 16;
+constexpr size_t kNoAllocBytes = (size_t)kNoAllocMaxRays * (4 * sizeof(float) + 2 * sizeof(double));
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+}  // namespace shdom
+
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_ptr[64] = {nullptr};
+
+// Address of the scratch array on the current device (set up on first use).
+static void *noalloc_scratch(std::string &err) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) { err = std::string("cudaGetDevice: ") + cudaGetErrorString(e); return nullptr; }
+  if (dev < 0 || dev >= 64) { err = "shdom_render_noalloc: device index out of range"; return nullptr; }
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, shdom::g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+      return nullptr;
+    }
+    g_noalloc_ptr[dev] = p;
+  }
+  return g_noalloc_ptr[dev];
+}
+
+extern "C" {
+
+int shdom_render_noalloc(shdom_handle *hh, int nrays, const float *camx, const float *camy, const float *camz,
+                         const double *cammu, const double *camphi, float *stokes_out) {
+  if (!hh) return fail(nullptr, "null handle");
+  Handle &H = hh->h;
+  if (nrays <= 0) return 0;
+  if (nrays > shdom::kNoAllocMaxRays)
+    return fail(hh, "shdom_render_noalloc: at most " + std::to_string(shdom::kNoAllocMaxRays) +
+                        " rays per call (got " + std::to_string(nrays) + ")");
+  if (!camx || !camy || !camz || !cammu || !camphi || !stokes_out) return fail(hh, "shdom_render_noalloc: null argument");
+  try {
+    std::string err;
+    void *base = noalloc_scratch(err);
+    if (!base) return fail(hh, err);
+    const size_t n = (size_t)nrays, cap = (size_t)shdom::kNoAllocMaxRays;
+    double *dmu = (double *)base, *dphi = dmu + cap;
+    float *dx = (float *)(dphi + cap), *dy = dx + cap, *dz = dy + cap, *dout = dz + cap;
+    const size_t fb = n * sizeof(float), db = n * sizeof(double);
+    CK(cudaMemcpyAsync(dx, camx, fb, cudaMemcpyHostToDevice, H.stream));
+    CK(cudaMemcpyAsync(dy, camy, fb, cudaMemcpyHostToDevice, H.stream));
+    CK(cudaMemcpyAsync(dz, camz, fb, cudaMemcpyHostToDevice, H.stream));
+    CK(cudaMemcpyAsync(dmu, cammu, db, cudaMemcpyHostToDevice, H.stream));
+    CK(cudaMemcpyAsync(dphi, camphi, db, cudaMemcpyHostToDevice, H.stream));
+    CK(cudaMemsetAsync(dout, 0, fb, H.stream));
+    int rc = render_impl(hh, nrays, dx, dy, dz, dmu, dphi, dout, H.stream);
+    if (!rc) CK(cudaMemcpyAsync(stokes_out, dout, fb, cudaMemcpyDeviceToHost, H.stream));
+    CK(cudaStreamSynchronize(H.stream));
+    if (rc) return rc;
+    if (shdom::check_device_error(H)) return 1;
+  } catch (const std::exception &e) {
+    return fail(hh, e.what());
+  }
+  return 0;
 }
 
 int shdom_export_state(shdom_handle *hh, float *source, int *ns, float *radiance, int *nr, float *fluxes,

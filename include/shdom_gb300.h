@@ -109,6 +109,19 @@ int shdom_levis_adjoint(shdom_handle *h, int species, int nrays, const float *ca
                         const float *camz, const double *cammu, const double *camphi, const double *weights,
                         double *gradient);
 
+/* shdom_render for callers that cannot allocate device memory during the
+ * call.  It has no counterpart in the reference.  The rays and radiances of
+ * the call are staged in one fixed device array inside the library (2 MiB)
+ * instead of memory allocated per call, so at most 65536 rays per call are
+ * accepted; more is refused with an error.  The array is shared by every
+ * handle on a device: calls that overlap in time (any thread or stream)
+ * overwrite each other's rays and must be serialized by the caller.  The
+ * first call on a device looks the array's address up; make that first
+ * call before any stream capture.  Same arguments and results as
+ * shdom_render. */
+int shdom_render_noalloc(shdom_handle *h, int nrays, const float *camx, const float *camy,
+                         const float *camz, const double *cammu, const double *camphi, float *stokes_out);
+
 /* Solution state export (RTE.save_solution fields, at3d/solver.py:1621-1686)
  * in a dense layout: source/radiance [npts][nlm] with the terms beyond each
  * point's truncation set to zero, ns/nr the truncations (SHPTR/RSHPTR
