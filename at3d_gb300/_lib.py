@@ -35,12 +35,16 @@ SIGNATURES = {
     "shdom_get_sizes": (C.c_int, [C.c_void_p, C.POINTER(ShdomSizes)]),
     "shdom_last_timings": (C.c_int, [C.c_void_p, _f]),
     "shdom_set_transform_mode": (C.c_int, [C.c_void_p, C.c_int]),
+    "shdom_set_sweep_mode": (C.c_int, [C.c_void_p, C.c_int]),
     "shdom_plan_summary": (C.c_int, [C.c_void_p, C.POINTER(ShdomSizes)]),
     "shdom_levis_gradient": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _f, _f, _f, _d, _d, _f, _d,
                                        C.POINTER(C.c_double), _f]),
     "shdom_levis_adjoint": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _f, _f, _f, _d, _d, _d, _d]),
     "shdom_last_error": (C.c_char_p, [C.c_void_p]),
     "shdom_destroy": (None, [C.c_void_p]),
+    "shdom_plan_create": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(ShdomSizes)]),
+    "shdom_create_planned": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
+    "shdom_plan_destroy": (None, [C.c_void_p]),
 }
 
 _LIB = None

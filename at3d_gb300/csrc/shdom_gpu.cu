@@ -1261,7 +1261,8 @@ struct DBuf {
     alloc(v.size());
     if (n) CK(cudaMemcpy(p, v.data(), n * sizeof(T), cudaMemcpyHostToDevice));
   }
-  void zero() { if (n) CK(cudaMemset(p, 0, n * sizeof(T))); }
+  // on the handle's (non-blocking) stream, so that later kernels on it are ordered after the fill
+  void zero(cudaStream_t st) { if (n) CK(cudaMemsetAsync(p, 0, n * sizeof(T), st)); }
   void free() { if (p) cudaFree(p); p = nullptr; n = 0; }
   ~DBuf() { free(); }
 };
@@ -1292,6 +1293,7 @@ struct Handle {
   DBuf<double> g_grad, g_beam, g_adj;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int coop_blocks = 0;
+  int sweep_mode = 0;  // 0: cooperative persistent kernel when available, 1: one launch per level
   DBuf<float> col_cx, col_cy, col_cz, col_fluxw, cmu1t, cmu2t, cphi1t, cphi2, ylmsun;
   DBuf<int> nphi0, col_of;
   // medium
@@ -1548,11 +1550,15 @@ static void upload_plan(Handle &H) {
   const size_t nf = (size_t)P.npts * P.nlm, nd = (size_t)P.npts * H.ldo;
   H.source.alloc(nf); H.delsource.alloc(nf); H.radiance.alloc(nf);
   H.srcdo.alloc(nd); H.raddo.alloc(nd);
-  H.srcdo.zero(); H.raddo.zero();
+  H.srcdo.zero(H.stream); H.raddo.zero(H.stream);
   H.fluxes.alloc((size_t)P.npts * 2); H.bcrad.alloc(std::max<size_t>(1, P.botp.size()));
   H.ns.alloc(P.npts); H.nso.alloc(P.npts); H.nr.alloc(P.npts); H.errflag.alloc(1);
   H.red.alloc(4); H.accel.alloc(1);
   setup_tc(H);
+  // the uploads are legacy-stream copies from pageable memory, which may
+  // return before their DMA lands; the handle's non-blocking stream is not
+  // ordered after them
+  CK(cudaStreamSynchronize(cudaStreamLegacy));
 }
 
 static void launch_source(Handle &H, int first, int fixsh) {
@@ -1697,7 +1703,7 @@ static void sweep_hemisphere(Handle &H, int hemi) {
   }
   if (ng1 > 0) CK(cudaStreamWaitEvent(H.stream, H.ev_join, 0));
   if (nlev <= 0) return;
-  if (H.coop_blocks > 0) {
+  if (H.coop_blocks > 0 && H.sweep_mode == 0) {
     const Seg *sp = H.segs[hemi].p;
     const int *so = H.seg_off[hemi].p, *li = H.level_items[hemi].p;
     const float2 *wp = H.sweepw.p;
@@ -1728,7 +1734,8 @@ static int check_device_error(Handle &H) {
   if (e == ERR_RAY_BELOW) m = "RENDER: Level below domain";
   if (e == ERR_TC_WAIT) m = "tensor-core transform: pipeline wait expired";
   H.err = m;
-  CK(cudaMemset(H.errflag.p, 0, sizeof(int)));
+  CK(cudaMemsetAsync(H.errflag.p, 0, sizeof(int), H.stream));
+  CK(cudaStreamSynchronize(H.stream));
   return 1;
 }
 
@@ -1738,6 +1745,16 @@ using shdom::Handle;
 
 struct shdom_handle {
   Handle h;
+  ~shdom_handle() {
+    if (h.stream) cudaStreamDestroy(h.stream);
+    if (h.stream2) cudaStreamDestroy(h.stream2);
+    if (h.ev_fork) cudaEventDestroy(h.ev_fork);
+    if (h.ev_join) cudaEventDestroy(h.ev_join);
+  }
+};
+
+struct shdom_plan {
+  shdom::Plan P;
 };
 
 static thread_local std::string g_static_err;
@@ -1749,17 +1766,14 @@ static int fail(shdom_handle *h, const std::string &m) {
 
 extern "C" {
 
-int shdom_create(const shdom_problem *problem, int device, shdom_handle **out) {
-  if (!problem || !out) return fail(nullptr, "shdom_create: null argument");
-  *out = nullptr;
-  std::unique_ptr<shdom_handle> H(new shdom_handle());
+// Device part of shdom_create: H->h.P holds a finished host plan.
+static int create_on_device(std::unique_ptr<shdom_handle> &H, int device, shdom_handle **out) {
   try {
-    if (!shdom::build_plan(*problem, H->h.P)) return fail(nullptr, H->h.P.err);
     if (device >= 0) CK(cudaSetDevice(device));
     CK(cudaGetDevice(&H->h.device));
     CK(cudaStreamCreateWithFlags(&H->h.stream, cudaStreamNonBlocking));
     shdom::upload_plan(H->h);
-    CK(cudaMemset(H->h.errflag.p, 0, sizeof(int)));
+    CK(cudaMemsetAsync(H->h.errflag.p, 0, sizeof(int), H->h.stream));
     shdom::build_irr(H->h);
   } catch (const std::exception &e) {
     return fail(nullptr, e.what());
@@ -1767,6 +1781,52 @@ int shdom_create(const shdom_problem *problem, int device, shdom_handle **out) {
   *out = H.release();
   return 0;
 }
+
+int shdom_create(const shdom_problem *problem, int device, shdom_handle **out) {
+  if (!problem || !out) return fail(nullptr, "shdom_create: null argument");
+  *out = nullptr;
+  std::unique_ptr<shdom_handle> H(new shdom_handle());
+  try {
+    if (!shdom::build_plan(*problem, H->h.P)) return fail(nullptr, H->h.P.err);
+  } catch (const std::exception &e) {
+    return fail(nullptr, e.what());
+  }
+  return create_on_device(H, device, out);
+}
+
+int shdom_plan_create(const shdom_problem *problem, shdom_plan **out, shdom_sizes *sizes) {
+  if (!problem || !out) return fail(nullptr, "shdom_plan_create: null argument");
+  *out = nullptr;
+  if (sizes) std::memset(sizes, 0, sizeof(*sizes));
+  std::unique_ptr<shdom_plan> p(new shdom_plan());
+  try {
+    if (!shdom::build_plan(*problem, p->P)) return fail(nullptr, p->P.err);
+    // the plan keeps copies of everything it uses; drop the caller's array pointers
+    shdom_problem &pr = p->P.prob;
+    pr.zlevels = nullptr; pr.extinctp = nullptr; pr.albedop = nullptr; pr.iphasep = nullptr;
+    pr.phasewtp = nullptr; pr.legenp = nullptr; pr.sfc_albedo = nullptr;
+    if (sizes) {
+      shdom::fill_sizes(p->P, sizes);
+      sizes->solcrit = 1.f;
+    }
+  } catch (const std::exception &e) {
+    return fail(nullptr, e.what());
+  }
+  *out = p.release();
+  return 0;
+}
+
+int shdom_create_planned(shdom_plan *plan, int device, shdom_handle **out) {
+  std::unique_ptr<shdom_plan> p(plan);  // released by this call in every case
+  if (!plan || !out) return fail(nullptr, "shdom_create_planned: null argument");
+  *out = nullptr;
+  std::unique_ptr<shdom_handle> H(new shdom_handle());
+  H->h.P = std::move(p->P);
+  p.reset();
+  return create_on_device(H, device, out);
+}
+
+void shdom_plan_destroy(shdom_plan *plan) { delete plan; }
 
 int shdom_init_solution(shdom_handle *hh) {
   if (!hh) return fail(nullptr, "null handle");
@@ -2024,6 +2084,7 @@ static void prepare_grad(Handle &H, int ipa) {
   H.g_legu.upload(legu); H.g_legs.upload(legs); H.g_fmix.upload(fmix); H.g_scatj.upload(scatj); H.g_legp.upload(legp);
   H.g_extp.upload(ep); H.g_albp.upload(ap); H.g_piph.upload(piph); H.g_pphw.upload(phw);
   H.g_grad.alloc((size_t)ng * 2); H.g_beam.alloc(npts);
+  CK(cudaStreamSynchronize(cudaStreamLegacy));  // uploads land before the stream's kernels read them
   H.grad_ipa = ipa;
 }
 
@@ -2264,6 +2325,13 @@ int shdom_export_state(shdom_handle *hh, float *source, int *ns, float *radiance
   return 0;
 }
 
+int shdom_set_sweep_mode(shdom_handle *hh, int mode) {
+  if (!hh) return fail(nullptr, "null handle");
+  if (mode < 0 || mode > 1) return fail(hh, "shdom_set_sweep_mode: mode must be 0 or 1");
+  hh->h.sweep_mode = mode;
+  return 0;
+}
+
 int shdom_set_transform_mode(shdom_handle *hh, int mode) {
   if (!hh) return fail(nullptr, "null handle");
   if (mode < 0 || mode > 2) return fail(hh, "shdom_set_transform_mode: mode must be 0, 1 or 2");
@@ -2301,13 +2369,6 @@ int shdom_last_timings(shdom_handle *hh, float *ms5) {
 
 const char *shdom_last_error(shdom_handle *hh) { return hh ? hh->h.err.c_str() : g_static_err.c_str(); }
 
-void shdom_destroy(shdom_handle *hh) {
-  if (!hh) return;
-  if (hh->h.stream) cudaStreamDestroy(hh->h.stream);
-  if (hh->h.stream2) cudaStreamDestroy(hh->h.stream2);
-  if (hh->h.ev_fork) cudaEventDestroy(hh->h.ev_fork);
-  if (hh->h.ev_join) cudaEventDestroy(hh->h.ev_join);
-  delete hh;
-}
+void shdom_destroy(shdom_handle *hh) { delete hh; }
 
 }  // extern "C"

@@ -103,3 +103,40 @@ def orthographic_views(problem: Problem, npix_x: int, npix_y: int, zeniths=VIEW_
         out[2].append(np.full(X.size, ztop)); out[3].append(np.full(X.size, mu))
         out[4].append(np.full(X.size, phi))
     return tuple(np.concatenate(a) for a in out)
+
+
+SERVING_GRIDS = ((32, 32, 24), (64, 64, 32), (96, 96, 48), (128, 128, 64))
+SERVING_VIEWS = (0.0, 26.1, -26.1, 45.6, -45.6)
+
+
+def request_mix(seed: int, n: int, grids=SERVING_GRIDS, max_wavelengths: int = 8, solacc: float = 1e-4):
+    """A seeded stream of serving requests: each one a power-law cloud field on
+    a grid drawn uniformly from ``grids``, NMU/NPHI 8/16 or 16/32, 1 to
+    ``max_wavelengths`` wavelengths (one problem each, sharing the field),
+    cloud fraction 10-50%, mean in-cloud extinction 10-40/km, HG g 0.75-0.88,
+    and a 32x32 to 64x64-pixel render at 5 view zeniths.  Returns a list of
+    (problems, rays) pairs."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        nx, ny, nz = grids[rng.integers(len(grids))]
+        nmu, nphi = (8, 16) if rng.integers(2) == 0 else (16, 32)
+        nw = int(rng.integers(1, max_wavelengths + 1))
+        frac = float(rng.uniform(0.1, 0.5))
+        mext = float(rng.uniform(10.0, 40.0))
+        g0 = float(rng.uniform(0.75, 0.88))
+        fseed = int(rng.integers(1 << 30))
+        base = cloud_field(seed=fseed, nx=nx, ny=ny, nz=nz, fraction=frac, mean_ext=mext, nmu=nmu, nphi=nphi,
+                           nleg=64, solacc=solacc, ssa=FIELD_SSA[0], g=g0)
+        ext = base.species[0].extinction
+        pbs = []
+        for w in range(nw):
+            ssa = FIELD_SSA[w % len(FIELD_SSA)]
+            g = max(0.70, g0 - 0.01 * w)
+            sp = Species(extinction=ext, ssalb=np.full_like(ext, ssa), legcoef=henyey_greenstein_legcoef(g, 64))
+            pbs.append(Problem(delx=base.delx, dely=base.dely, zlevels=base.zlevels, species=[sp],
+                               solarmu=base.solarmu, solaraz=base.solaraz, solarflux=base.solarflux,
+                               surface_albedo=base.surface_albedo, params=base.params))
+        npix = int(rng.choice([32, 48, 64]))
+        out.append((pbs, orthographic_views(pbs[0], npix, npix, zeniths=SERVING_VIEWS)))
+    return out

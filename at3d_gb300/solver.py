@@ -48,6 +48,35 @@ def plan_summary(problem: Problem) -> dict:
     return _sizes_dict(out)
 
 
+class HostPlan:
+    """A problem planned on the host (grid, sweep schedule, ordinates,
+    medium, direct beam), not yet on a GPU; ``sizes["device_bytes"]`` is the
+    memory a handle for it will hold.  ``RTE.from_plan`` consumes it."""
+
+    def __init__(self, problem: Problem):
+        L = _lib.lib()
+        st = problem.to_struct()
+        out = _lib.ShdomSizes()
+        p = C.c_void_p()
+        rc = L.shdom_plan_create(C.byref(st), C.byref(p), C.byref(out))
+        if rc:
+            raise SHDOMError(L.shdom_last_error(None).decode())
+        self.problem = problem
+        self.sizes = _sizes_dict(out)
+        self._p = p
+
+    def release(self):
+        if self._p:
+            _lib.lib().shdom_plan_destroy(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
 class RTE:
     """Radiative-transfer solve of one medium at one wavelength.
 
@@ -75,6 +104,25 @@ class RTE:
         self.problem = problem
         self.name = name or "RTE"
         self._create(device)
+        return self
+
+    @classmethod
+    def from_plan(cls, plan: HostPlan, device: int = 0, name: str | None = None):
+        """Put a host plan on the device (the plan is consumed)."""
+        if not plan._p:
+            raise ValueError("plan already used or released")
+        self = cls.__new__(cls)
+        self.problem = plan.problem
+        self.name = name or "RTE"
+        L = _lib.lib()
+        self._struct = None
+        p, plan._p = plan._p, None
+        h = C.c_void_p()
+        rc = L.shdom_create_planned(p, int(device), C.byref(h))
+        if rc:
+            raise SHDOMError(L.shdom_last_error(None).decode())
+        self._h = h
+        self._initialized = False
         return self
 
     def _create(self, device):
@@ -206,6 +254,15 @@ class RTE:
             self._h, int(species), len(x), _fp(x), _fp(y), _fp(z), mu.ctypes.data_as(dp), phi.ctypes.data_as(dp),
             w.ctypes.data_as(dp), grad.ctypes.data_as(dp)))
         return grad.reshape(shp + (2,))
+
+    def set_sweep_mode(self, mode: str):
+        """'persistent' (one cooperative kernel per hemisphere; default) or
+        'per_level' (one launch per wavefront level; for solves that run
+        concurrently on one device)."""
+        modes = {"persistent": 0, "per_level": 1}
+        if mode not in modes:
+            raise ValueError(f"sweep mode must be one of {sorted(modes)}")
+        _check(self._h, _lib.lib().shdom_set_sweep_mode(self._h, modes[mode]))
 
     TRANSFORM_MODES = {"tf32x3": 0, "tf32": 1, "fp32": 2}
 

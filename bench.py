@@ -208,6 +208,125 @@ def gb300_arm(args, rank, ws):
                 iters=list(iters), e2e=e2e, roofline=roofline, clocks=clk.summary(), npts=npts)
 
 
+def relrms(a, b) -> float:
+    a = np.asarray(a, np.float64); b = np.asarray(b, np.float64)
+    return float(np.sqrt(np.mean((a - b) ** 2)) / max(np.sqrt(np.mean(b ** 2)), 1e-300))
+
+
+PRECISION_FIXTURE = os.path.join(ROOT, "tests", "golden", "fp64_cloud_field_128x128x64.npz")
+
+
+def precision_block(args, dev):
+    """The transform arithmetics on the benchmark scenes at a fixed iteration
+    count: solves/s and rays/s of each mode (one step of all wavelengths,
+    timed with CUDA events, inputs resident), and the relative RMS of its
+    radiances against the plain FP32 GPU mode and against an FP64 run of the
+    plain algorithm (committed fixture, made by
+    tests/golden/make_fp64_fixture.py with the same scenes, rays and
+    iteration count)."""
+    import torch
+    from at3d_gb300.scenes import cloud_field, orthographic_views
+    fx = np.load(PRECISION_FIXTURE) if os.path.exists(PRECISION_FIXTURE) else None
+    niter = int(fx["iterations"]) if fx is not None else 30
+    pbs = [cloud_field(seed=2, wavelength_index=w, nx=args.nx, ny=args.nx, nz=args.nz, boundary=args.boundary,
+                       solacc=0.0) for w in range(args.nwave)]
+    rays = orthographic_views(pbs[0], args.npix, args.npix)
+    nr = len(rays[0])
+    from at3d_gb300.solver import RTE
+    rtes = [RTE.from_problem(pb, device=dev) for pb in pbs]
+    d = [torch.tensor(np.asarray(r), dtype=torch.float32 if i < 3 else torch.float64, device="cuda")
+         for i, r in enumerate(rays)]
+    outs = [torch.empty(nr, dtype=torch.float32, device="cuda") for _ in pbs]
+    res = {}
+    for mode in ("fp32", "tf32x3", "tf32"):
+        for r in rtes:
+            r.set_transform_mode(mode)
+        ms = []
+        for rep in range(2):  # the second pass is timed (the first warms the mode's code path)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for w, r in enumerate(rtes):
+                r.solve(niter, verbose=False)
+                r.render_device(d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), d[3].data_ptr(),
+                                d[4].data_ptr(), outs[w].data_ptr(), nr, 0)
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        rad = [o.cpu().numpy() for o in outs]
+        res[mode] = {"solves_per_s": len(rtes) / (ms[-1] / 1e3), "rays_per_s": len(rtes) * nr / (ms[-1] / 1e3),
+                     "ms_per_step": ms[-1], "rad": rad}
+    for r in rtes:
+        r.close()
+    out = {"iterations": niter, "modes": {}}
+    for mode, v in res.items():
+        e = {"solves_per_s": v["solves_per_s"], "rays_per_s": v["rays_per_s"], "ms_per_step": v["ms_per_step"],
+             "relrms_vs_fp32": max(relrms(a, b) for a, b in zip(v["rad"], res["fp32"]["rad"]))}
+        if fx is not None:
+            e["relrms_vs_fp64"] = [relrms(a, fx[f"radiance_{w}"]) for w, a in enumerate(v["rad"])]
+            e["max_relrms_vs_fp64"] = max(e["relrms_vs_fp64"])
+        out["modes"][mode] = e
+    out["fp64_reference"] = ("oracle FP64 (CPU restatement of the reference algorithm), same scenes, rays and "
+                             f"{niter} iterations" if fx is not None else "fixture absent")
+    return out
+
+
+def gradient_block(args, dev):
+    """Levis approximate gradient on the differentiation workload: 64x64x32
+    cloud field at 20% cloud fraction, NMU=8/NPHI=16; L2 cost of 64x64-pixel
+    radiances at 9 views against a target rendered from a second seeded
+    field.  Times the gradient call (forward render with the adjoint
+    weights + adjoint ray pass + direct-beam term, FP64 reductions) with
+    the solved field resident."""
+    import torch
+    from at3d_gb300.scenes import cloud_field, orthographic_views
+    from at3d_gb300.solver import RTE
+    mk = lambda seed: cloud_field(seed=seed, nx=64, ny=64, nz=32, fraction=0.2, nmu=8, nphi=16, nleg=64,
+                                  solacc=1e-4)
+    pb, pt = mk(4), mk(5)
+    rays = orthographic_views(pb, 64, 64)
+    tgt = RTE.from_problem(pt, device=dev)
+    tgt.solve(args.maxiter, verbose=False)
+    meas = tgt.render(*rays)
+    tgt.close()
+    r = RTE.from_problem(pb, device=dev)
+    t0 = time.perf_counter()
+    it, _ = r.solve(args.maxiter, verbose=False)
+    torch.cuda.synchronize()
+    t_solve = time.perf_counter() - t0
+    ms = []
+    for rep in range(4):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g, cost, _ = r.levis_gradient(rays, meas, species=0)
+        ms.append((time.perf_counter() - t0) * 1e3)
+    r.close()
+    nr = len(rays[0])
+    return {"workload": "64x64x32 cloud field, 20% cloud fraction, NMU=8 NPHI=16, 64x64 px x 9 views",
+            "ms_per_gradient": float(np.median(ms[1:])), "rays_per_s": nr / (np.median(ms[1:]) / 1e3),
+            "solve_s": t_solve, "iterations": it, "cost": float(cost),
+            "note": "host buffers in and out (rays, measurements, gradient), wall clock"}
+
+
+def serving_block(args, dev):
+    """A Poisson stream of mixed requests through the continuous-admission
+    loop (at3d_gb300.serving): grids 32x32x24 to 128x128x64, NMU/NPHI 8/16
+    or 16/32, 1-8 wavelengths each, 32-64 px renders at 5 views."""
+    from at3d_gb300.scenes import request_mix
+    from at3d_gb300.serving import SolveServer, poisson_arrivals, run_stream
+    out = []
+    for k, rate in enumerate(args.serve_rates):
+        reqs = request_mix(100 + k, args.serve_requests)
+        arr = poisson_arrivals(rate, len(reqs), seed=7 + k)
+        with SolveServer(device=dev, slots=args.serve_slots) as srv:
+            run_stream(srv, reqs, arr, maxiter=args.maxiter)
+            st = srv.stats()
+        st.update({"rate_per_s": rate, "requests": len(reqs), "slots": args.serve_slots,
+                   "wavelength_solves": int(sum(len(p) for p, _ in reqs))})
+        out.append(st)
+    return out
+
+
 def cpu_sample(args, wavelength: int, iters: int):
     """One oracle iteration of one wavelength, scaled to a full solve."""
     from oracle.oracle import Oracle
@@ -269,7 +388,12 @@ def main():
     ap.add_argument("--nwave", type=int, default=NWAVE, help="wavelengths per step (profiling runs use 1)")
     ap.add_argument("--ref-iters", type=str, default="")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the precision, gradient and serving blocks")
+    ap.add_argument("--serve-rates", type=str, default="2", help="Poisson arrival rates (requests/s) to run")
+    ap.add_argument("--serve-requests", type=int, default=16)
+    ap.add_argument("--serve-slots", type=int, default=4)
     args = ap.parse_args()
+    args.serve_rates = [float(x) for x in args.serve_rates.split(",") if x]
     args.ref_iters = [int(x) for x in args.ref_iters.split(",")] if args.ref_iters else \
         SOLVE_ITERS[:args.nwave]
     rank, ws = dist_init()
@@ -281,6 +405,12 @@ def main():
     r = gb300_arm(args, rank, ws)
     if rank != 0:
         return
+    extras = {}
+    if ws == 1 and not args.no_extras:
+        dev = int(os.environ.get("LOCAL_RANK", "0"))
+        extras["precision"] = precision_block(args, dev)
+        extras["gradient"] = gradient_block(args, dev)
+        extras["serving"] = serving_block(args, dev)
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
         t_solve, t_init, t_it = cpu_sample(args, 0, r["iters"][0])
@@ -294,6 +424,7 @@ def main():
            "config": config_dict(args), "rays_per_s": r["rays_per_s"], "iterations_per_solve": r["iters"],
            "e2e": r["e2e"], "gpu_launches": r["launches"], "roofline": r["roofline"], "cpu_baseline": cpu,
            "clocks": r["clocks"]}
+    out.update(extras)
     print(json.dumps(out))
 
 

@@ -58,6 +58,20 @@ int shdom_create(const shdom_problem *problem, int device, shdom_handle **out);
  * arrays in RTE._setup_grid, at3d/solver.py:2122-2191). */
 int shdom_plan_summary(const shdom_problem *problem, shdom_sizes *out);
 
+/* Two-stage form of shdom_create for callers that admit work by device
+ * memory: shdom_plan_create does the host part (grid, cell structure, sweep
+ * schedule, ordinates, medium, direct beam) without touching a GPU and
+ * reports the sizes (device_bytes: the memory the handle will hold; sizes
+ * may be NULL); the plan keeps copies of the problem's arrays.
+ * shdom_create_planned puts a plan on the device and takes ownership of it:
+ * the plan is released by that call whether it succeeds or not.
+ * shdom_plan_destroy releases a plan that is not used.  The pair does what
+ * shdom_create does. */
+typedef struct shdom_plan shdom_plan;
+int shdom_plan_create(const shdom_problem *problem, shdom_plan **out, shdom_sizes *sizes);
+int shdom_create_planned(shdom_plan *plan, int device, shdom_handle **out);
+void shdom_plan_destroy(shdom_plan *plan);
+
 /* Direct beam, Eddington initial radiance and the first source function.
  * Replaces core.make_angle_set, core.make_sh_do_coef and core.init_solution
  * (at3d/solver.py:2539-2798). */
@@ -147,6 +161,13 @@ int shdom_last_timings(shdom_handle *h, float *ms5);
  * Problems whose operand rows are not multiples of 16 bytes use 2 in every
  * mode.  No reference counterpart: the reference has a single FP32 path. */
 int shdom_set_transform_mode(shdom_handle *h, int mode);
+
+/* How the interior sweep levels are launched: 0 (default) one persistent
+ * cooperative kernel per hemisphere with a grid barrier between levels
+ * (when the device supports cooperative launch), 1 one kernel launch per
+ * level.  Use 1 when several handles solve concurrently on one device: it
+ * has no waits between thread blocks.  No reference counterpart. */
+int shdom_set_sweep_mode(shdom_handle *h, int mode);
 
 /* Message of the last non-zero return on this handle (CHARACTER*600 errmsg
  * of the reference); a static message when h is NULL. */

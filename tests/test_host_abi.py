@@ -96,3 +96,25 @@ def test_null_arguments(lib):
     assert lib.shdom_init_solution(None) == 1
     assert lib.shdom_set_transform_mode(None, 0) == 1
     lib.shdom_destroy(None)
+
+
+def test_host_plan_matches_summary():
+    """The two-stage create: a host plan reports the same sizes as the
+    summary and can be released without ever touching a device."""
+    from at3d_gb300.scenes import cloud_field
+    from at3d_gb300.solver import HostPlan, plan_summary
+    pb = cloud_field(seed=3, wavelength_index=2, nx=20, ny=16, nz=10, nmu=8, nphi=16, nleg=64)
+    hp = HostPlan(pb)
+    s = plan_summary(pb)
+    for k in ("npts", "nlm", "nang", "nlevels_down", "nlevels_up", "device_bytes"):
+        assert hp.sizes[k] == s[k]
+    hp.release()
+    hp.release()  # idempotent
+
+
+def test_planned_create_null_arguments(lib):
+    h = C.c_void_p()
+    assert lib.shdom_create_planned(None, 0, C.byref(h)) == 1
+    assert lib.shdom_plan_create(None, C.byref(h), None) == 1
+    assert lib.shdom_set_sweep_mode(None, 0) == 1
+    lib.shdom_plan_destroy(None)
