@@ -1405,6 +1405,40 @@ static void make_map(CUtensorMap *m, const float *base, uint64_t inner, uint64_t
   if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
 }
 
+// The tensor-core GEMM is instantiated for N tiles of 32..256 columns.
+template <int BN>
+static void tc_attr1() {
+  CK(cudaFuncSetAttribute(tc::k_tc_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::smem_bytes<BN>()));
+}
+static void tc_attr(int bn) {
+  switch (bn) {
+    case 32: tc_attr1<32>(); break;   case 64: tc_attr1<64>(); break;
+    case 96: tc_attr1<96>(); break;   case 128: tc_attr1<128>(); break;
+    case 160: tc_attr1<160>(); break; case 192: tc_attr1<192>(); break;
+    case 224: tc_attr1<224>(); break; case 256: tc_attr1<256>(); break;
+    default: throw std::runtime_error("tensor-core transform: unsupported tile width");
+  }
+}
+template <int BN>
+static void tc_launch1(dim3 grid, cudaStream_t st, const CUtensorMap &a, const CUtensorMap &bh, const CUtensorMap &bl,
+                       int K, const tc::Epilogue &g) {
+  tc::k_tc_gemm<BN><<<grid, tc::kThreads, tc::smem_bytes<BN>(), st>>>(a, bh, bl, K, g);
+}
+static void tc_launch(int bn, dim3 grid, cudaStream_t st, const CUtensorMap &a, const CUtensorMap &bh,
+                      const CUtensorMap &bl, int K, const tc::Epilogue &g) {
+  switch (bn) {
+    case 32: tc_launch1<32>(grid, st, a, bh, bl, K, g); break;
+    case 64: tc_launch1<64>(grid, st, a, bh, bl, K, g); break;
+    case 96: tc_launch1<96>(grid, st, a, bh, bl, K, g); break;
+    case 128: tc_launch1<128>(grid, st, a, bh, bl, K, g); break;
+    case 160: tc_launch1<160>(grid, st, a, bh, bl, K, g); break;
+    case 192: tc_launch1<192>(grid, st, a, bh, bl, K, g); break;
+    case 224: tc_launch1<224>(grid, st, a, bh, bl, K, g); break;
+    case 256: tc_launch1<256>(grid, st, a, bh, bl, K, g); break;
+    default: throw std::runtime_error("tensor-core transform: unsupported tile width");
+  }
+}
+
 // Forms the dense matrices, splits them into TF32 high and low parts
 // ([Npad][Kpad], zero padded) and encodes the tensor maps.  A direction whose
 // operand rows are not 16-byte multiples, or too small for one tile, keeps
@@ -1417,14 +1451,15 @@ static void setup_tc(Handle &H) {
   CK(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
   if (major != 10) return;
   for (int dir = 0; dir < 2; ++dir) {
-    const int K = dir == 0 ? P.nlm : P.nang, N = dir == 0 ? P.nang : P.nlm + 2;
+    // the ordinate-to-harmonic direction forms the fluxes from A on the CUDA cores
+    const int K = dir == 0 ? P.nlm : P.nang, N = dir == 0 ? P.nang : P.nlm;
     const int lda = dir == 0 ? P.nlm : H.ldo;
     if (lda % 4 != 0 || K < tc::BK || P.npts < tc::BM) continue;
     const int ntiles = (N + 255) / 256;
-    const int bn = ((N + ntiles - 1) / ntiles + 15) / 16 * 16;
+    const int bn = ((N + ntiles - 1) / ntiles + 31) / 32 * 32;
     const int npad = ntiles * bn, kpad = (K + tc::BK - 1) / tc::BK * tc::BK;
     std::vector<double> T;
-    if (dir == 0) dense_sh_to_do(P, T); else dense_do_to_sh(P, T);
+    if (dir == 0) dense_sh_to_do(P, T); else dense_do_to_sh(P, T);  // rows [0, N) are used
     std::vector<float> bh((size_t)npad * kpad, 0.f), bl((size_t)npad * kpad, 0.f);
     for (int n = 0; n < N; ++n)
       for (int k = 0; k < K; ++k) {
@@ -1440,7 +1475,7 @@ static void setup_tc(Handle &H) {
     make_map(&H.tm_bh[dir], H.tc_bh[dir].p, (uint64_t)kpad, (uint64_t)npad, (uint64_t)kpad, (uint32_t)bn);
     make_map(&H.tm_bl[dir], H.tc_bl[dir].p, (uint64_t)kpad, (uint64_t)npad, (uint64_t)kpad, (uint32_t)bn);
     H.tc_bn[dir] = bn; H.tc_ntiles[dir] = ntiles; H.tc_kpad[dir] = kpad;
-    CK(cudaFuncSetAttribute(tc::k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::smem_bytes(256)));
+    tc_attr(bn);
     H.tc_ok[dir] = true;
   }
 }
@@ -1609,11 +1644,12 @@ static void transform(Handle &H, int dir) {
     if (dir == 0) {
       g.N = P.nang; g.mode = 0; g.C = H.srcdo.p; g.ldc = H.ldo;
     } else {
-      g.N = P.nlm + 2; g.mode = 1; g.R = H.radiance.p; g.nlm = P.nlm; g.nr = H.nr.p; g.fluxes = H.fluxes.p;
+      g.N = P.nlm; g.mode = 1; g.R = H.radiance.p; g.nlm = P.nlm; g.nr = H.nr.p; g.fluxes = H.fluxes.p;
+      g.fluxw = H.col_fluxw.p; g.ncol_down = P.ncol_down;
     }
-    dim3 grid((P.npts + tc::BM - 1) / tc::BM, H.tc_ntiles[dir]);
-    tc::k_tc_gemm<<<grid, 128, tc::smem_bytes(H.tc_bn[dir]), H.stream>>>(H.tm_a[dir], H.tm_bh[dir], H.tm_bl[dir],
-                                                                         H.tc_kpad[dir], H.tc_bn[dir], g);
+    // the N tiles of a row tile are adjacent in launch order: A is read from DRAM once
+    dim3 grid(H.tc_ntiles[dir], (P.npts + tc::BM - 1) / tc::BM);
+    tc_launch(H.tc_bn[dir], grid, H.stream, H.tm_a[dir], H.tm_bh[dir], H.tm_bl[dir], dir == 0 ? P.nlm : P.nang, g);
     CK(cudaGetLastError());
     H.launches += 1;
     return;
