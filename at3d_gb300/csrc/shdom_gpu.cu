@@ -1293,7 +1293,8 @@ struct Handle {
   DBuf<double> g_grad, g_beam, g_adj;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int coop_blocks = 0;
-  int sweep_mode = 0;  // 0: cooperative persistent kernel when available, 1: one launch per level
+  int sweep_mode = 0;
+  int nsm = 152;  // streaming multiprocessors of the handle's device  // 0: cooperative persistent kernel when available, 1: one launch per level
   DBuf<float> col_cx, col_cy, col_cz, col_fluxw, cmu1t, cmu2t, cphi1t, cphi2, ylmsun;
   DBuf<int> nphi0, col_of;
   // medium
@@ -1405,7 +1406,7 @@ static void make_map(CUtensorMap *m, const float *base, uint64_t inner, uint64_t
   if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
 }
 
-// The tensor-core GEMM is instantiated for N tiles of 32..256 columns.
+// The tensor-core GEMM is instantiated for N tiles of 32..128 columns.
 template <int BN>
 static void tc_attr1() {
   CK(cudaFuncSetAttribute(tc::k_tc_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::smem_bytes<BN>()));
@@ -1414,27 +1415,24 @@ static void tc_attr(int bn) {
   switch (bn) {
     case 32: tc_attr1<32>(); break;   case 64: tc_attr1<64>(); break;
     case 96: tc_attr1<96>(); break;   case 128: tc_attr1<128>(); break;
-    case 160: tc_attr1<160>(); break; case 192: tc_attr1<192>(); break;
-    case 224: tc_attr1<224>(); break; case 256: tc_attr1<256>(); break;
     default: throw std::runtime_error("tensor-core transform: unsupported tile width");
   }
 }
 template <int BN>
-static void tc_launch1(dim3 grid, cudaStream_t st, const CUtensorMap &a, const CUtensorMap &bh, const CUtensorMap &bl,
-                       int K, const tc::Epilogue &g) {
-  tc::k_tc_gemm<BN><<<grid, tc::kThreads, tc::smem_bytes<BN>(), st>>>(a, bh, bl, K, g);
+static void tc_launch1(int nblocks, cudaStream_t st, const CUtensorMap &a, const CUtensorMap &bh,
+                       const CUtensorMap &bl, int K, int ntn, int ntiles, const tc::Epilogue &g) {
+  tc::k_tc_gemm<BN><<<nblocks, tc::kThreads, tc::smem_bytes<BN>(), st>>>(a, bh, bl, K, ntn, ntiles, g);
 }
-static void tc_launch(int bn, dim3 grid, cudaStream_t st, const CUtensorMap &a, const CUtensorMap &bh,
-                      const CUtensorMap &bl, int K, const tc::Epilogue &g) {
+// Persistent launch: one CTA per SM (the pipeline fills the shared memory),
+// each walking its share of the ntiles = ntn x row-tile tiles.
+static void tc_launch(int bn, int nsm, cudaStream_t st, const CUtensorMap &a, const CUtensorMap &bh,
+                      const CUtensorMap &bl, int K, int ntn, int ntiles, const tc::Epilogue &g) {
+  const int nb = std::max(1, std::min(ntiles, nsm));
   switch (bn) {
-    case 32: tc_launch1<32>(grid, st, a, bh, bl, K, g); break;
-    case 64: tc_launch1<64>(grid, st, a, bh, bl, K, g); break;
-    case 96: tc_launch1<96>(grid, st, a, bh, bl, K, g); break;
-    case 128: tc_launch1<128>(grid, st, a, bh, bl, K, g); break;
-    case 160: tc_launch1<160>(grid, st, a, bh, bl, K, g); break;
-    case 192: tc_launch1<192>(grid, st, a, bh, bl, K, g); break;
-    case 224: tc_launch1<224>(grid, st, a, bh, bl, K, g); break;
-    case 256: tc_launch1<256>(grid, st, a, bh, bl, K, g); break;
+    case 32: tc_launch1<32>(nb, st, a, bh, bl, K, ntn, ntiles, g); break;
+    case 64: tc_launch1<64>(nb, st, a, bh, bl, K, ntn, ntiles, g); break;
+    case 96: tc_launch1<96>(nb, st, a, bh, bl, K, ntn, ntiles, g); break;
+    case 128: tc_launch1<128>(nb, st, a, bh, bl, K, ntn, ntiles, g); break;
     default: throw std::runtime_error("tensor-core transform: unsupported tile width");
   }
 }
@@ -1449,13 +1447,15 @@ static void setup_tc(Handle &H) {
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
   CK(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+  CK(cudaDeviceGetAttribute(&H.nsm, cudaDevAttrMultiProcessorCount, dev));
   if (major != 10) return;
   for (int dir = 0; dir < 2; ++dir) {
     // the ordinate-to-harmonic direction forms the fluxes from A on the CUDA cores
     const int K = dir == 0 ? P.nlm : P.nang, N = dir == 0 ? P.nang : P.nlm;
     const int lda = dir == 0 ? P.nlm : H.ldo;
     if (lda % 4 != 0 || K < tc::BK || P.npts < tc::BM) continue;
-    const int ntiles = (N + 255) / 256;
+    if (dir == 1 && (K + tc::BK - 1) / tc::BK * tc::BK * 8 > 16 * 1024) continue;  // flux weight table
+    const int ntiles = (N + 127) / 128;  // tiles of at most 128 columns keep the FP32 sums in registers
     const int bn = ((N + ntiles - 1) / ntiles + 31) / 32 * 32;
     const int npad = ntiles * bn, kpad = (K + tc::BK - 1) / tc::BK * tc::BK;
     std::vector<double> T;
@@ -1647,9 +1647,9 @@ static void transform(Handle &H, int dir) {
       g.N = P.nlm; g.mode = 1; g.R = H.radiance.p; g.nlm = P.nlm; g.nr = H.nr.p; g.fluxes = H.fluxes.p;
       g.fluxw = H.col_fluxw.p; g.ncol_down = P.ncol_down;
     }
-    // the N tiles of a row tile are adjacent in launch order: A is read from DRAM once
-    dim3 grid(H.tc_ntiles[dir], (P.npts + tc::BM - 1) / tc::BM);
-    tc_launch(H.tc_bn[dir], grid, H.stream, H.tm_a[dir], H.tm_bh[dir], H.tm_bl[dir], dir == 0 ? P.nlm : P.nang, g);
+    const int ntn = H.tc_ntiles[dir], ntiles = ntn * ((P.npts + tc::BM - 1) / tc::BM);
+    tc_launch(H.tc_bn[dir], H.nsm, H.stream, H.tm_a[dir], H.tm_bh[dir], H.tm_bl[dir], dir == 0 ? P.nlm : P.nang, ntn,
+              ntiles, g);
     CK(cudaGetLastError());
     H.launches += 1;
     return;

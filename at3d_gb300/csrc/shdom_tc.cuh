@@ -95,22 +95,46 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-// One CTA: a 128-row tile of A against a BN-column tile of B (BN a multiple
-// of 32, at most 256).  The N tiles of one row tile are adjacent in launch
-// order (blockIdx.x), so they run together and A comes from DRAM once.
+// 16 columns of this warp's 32 tensor-memory lanes into registers (async;
+// complete after tcgen05.wait::ld).
+__device__ __forceinline__ void tmem_ld16(uint32_t ta, uint32_t *r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(ta));
+}
+// Orders later uses of 16 registers after the preceding volatile asm (the wait).
+__device__ __forceinline__ void reg_fence16(uint32_t *r) {
+  asm volatile(""
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]));
+}
+
+// Persistent kernel: CTA i takes the tiles i, i + gridDim.x, ... of the
+// (row tile, N tile) grid, N tile fastest, so the N tiles of one row tile
+// run at the same time on neighbouring CTAs and A comes from DRAM once.  A
+// tile is a 128-row block of A against a BN-column block of B (BN a
+// multiple of 32, at most 128 so that the FP32 sums stay in registers).
+// The chunks of all the CTA's tiles form one pipeline, so loads for the
+// next tile start while the current one is in the tensor cores and its
+// results are stored.
 //
-// Warp roles (320 threads):
+// Warp roles (448 threads):
 //   warp 0 lane 0  TMA producer: A chunk (128 x 32 fp32) and the B hi / lo
-//                  chunks (BN x 32) into stage c % S;
+//                  chunks (BN x 32) into stage g % S;
 //   warp 1 lane 0  MMA issuer: the chunk's 3 (or 1) x BK/8 tcgen05.mma into a
-//                  FRESH accumulator (TMEM buffer c % 2, BN columns each);
+//                  FRESH accumulator (tensor-memory buffer g % 2, BN columns);
 //                  warp 1 also owns the tensor-memory allocation;
-//   warps 2..9     split and accumulate: split chunk c of A into TF32 high
-//                  (in place) and low parts (and, for the ordinate-to-
-//                  harmonic direction, add its ordinates into the two
-//                  hemispheric flux sums in FP32), then read chunk c-1's
-//                  partial product from tensor memory and add it into FP32
-//                  registers (each thread: one row, half of the BN columns).
+//   warps 2..5     split: one row of the chunk per thread, into TF32 high (in
+//                  place) and low parts (and, for the ordinate-to-harmonic
+//                  direction, the row's ordinates into the two hemispheric
+//                  flux sums in FP32);
+//   warps 6..13    accumulate: read chunk g's partial product from tensor
+//                  memory and add it into FP32 registers (each thread: one
+//                  row, half of the BN columns); after a tile's last chunk,
+//                  store its results (while the tensor cores work on the
+//                  next tile).
 // Summing the per-chunk partial products on the CUDA cores (round to
 // nearest) keeps the tensor-core accumulation chains 32 K-elements long.
 template <int BN>
@@ -118,17 +142,25 @@ struct Cfg {
   static constexpr int HALF = BN / 2;
   static constexpr int A_BYTES = BM * BK * 4, B_BYTES = BN * BK * 4;
   static constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;
-  static constexpr int S = (227 * 1024 - 2048) / STAGE > 4 ? 4 : (227 * 1024 - 2048) / STAGE;
+  static constexpr int kFluxTab = 16 * 1024;  // down and up flux weights, K padded to 32 (K <= 2048)
+  static constexpr int S = (227 * 1024 - 2048 - kFluxTab) / STAGE > 4 ? 4 : (227 * 1024 - 2048 - kFluxTab) / STAGE;
   static constexpr uint32_t TCOLS = 2 * BN <= 256 ? 256u : 512u;
-  static constexpr size_t smem() { return (size_t)S * STAGE + 256 + 1024; }
+  static constexpr size_t smem() { return (size_t)S * STAGE + 256 + kFluxTab + 1024; }
 };
-constexpr int kThreads = 320;
+constexpr int kThreads = 448;
+
+// Round to TF32, nearest with ties away from zero (the rounding of
+// cvt.rna.tf32.f32), on the integer pipe: add half of the dropped range to
+// the magnitude bits and clear the 13 low bits.  Finite inputs.
+__device__ __forceinline__ float tf32_rna_bits(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xffffe000u);
+}
 
 template <int BN>
 __global__ void __launch_bounds__(kThreads, 1) k_tc_gemm(const __grid_constant__ CUtensorMap tmA,
                                                          const __grid_constant__ CUtensorMap tmBh,
-                                                         const __grid_constant__ CUtensorMap tmBl, int K,
-                                                         Epilogue g) {
+                                                         const __grid_constant__ CUtensorMap tmBl, int K, int ntn,
+                                                         int ntiles, Epilogue g) {
   using C = Cfg<BN>;
   constexpr int S = C::S, HALF = C::HALF, A_BYTES = C::A_BYTES, B_BYTES = C::B_BYTES, STAGE = C::STAGE;
   extern __shared__ uint8_t smem_raw[];
@@ -143,13 +175,26 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_gemm(const __grid_constant__
   uint32_t *tslot = reinterpret_cast<uint32_t *>(&bars[3 * S + 5]);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(&bars[3 * S + 6]);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;
-  const int KB = (K + BK - 1) / BK;
+  const int KB = (K + BK - 1) / BK, kpad = KB * BK;
+  float *fw = reinterpret_cast<float *>(smem + S * STAGE + 256);  // [2][kpad]: down, up weights
+  if (g.mode == 1)
+    for (int i = tid; i < kpad; i += blockDim.x) {
+      const float w = i < K ? g.fluxw[i] : 0.f;
+      fw[i] = i < g.ncol_down ? w : 0.f;
+      fw[kpad + i] = i < g.ncol_down ? 0.f : w;
+    }
+  const int mine = blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  const int G = mine * KB;  // chunks of all this CTA's tiles
+  auto tile_origin = [&](int gc, int &m0, int &n0) {
+    const int t = (int)blockIdx.x + (gc / KB) * (int)gridDim.x;
+    n0 = (t % ntn) * BN;
+    m0 = (t / ntn) * BM;
+  };
 
   if (tid == 0) {
     for (int i = 0; i < S; ++i) {
       mbar_init(full0 + 8 * i, 1);
-      mbar_init(split0 + 8 * i, 8);
+      mbar_init(split0 + 8 * i, 4);
       mbar_init(empty0 + 8 * i, 1);
     }
     mbar_init(accf0, 1); mbar_init(accf0 + 8, 1);
@@ -171,19 +216,22 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_gemm(const __grid_constant__
     // ---------------------------------------------------------- producer
     if (lane == 0) {
       int issued = 0;
-      for (int c = 0; c < KB && !*abort_flag; ++c) {
-        const int s = c % S;
-        if (c >= S && !mbar_wait(empty0 + 8 * s, ((c / S) - 1) & 1)) { *abort_flag = 1; break; }
+      for (int gc = 0; gc < G && !*abort_flag; ++gc) {
+        const int s = gc % S;
+        if (gc >= S && !mbar_wait(empty0 + 8 * s, ((gc / S) - 1) & 1)) { *abort_flag = 1; break; }
+        int m0, n0;
+        tile_origin(gc, m0, n0);
+        const int kx = (gc % KB) * BK;
         const uint32_t st = sbase + s * STAGE;
         mbar_expect_tx(full0 + 8 * s, A_BYTES + 2 * B_BYTES);
-        tma_load(st, &tmA, full0 + 8 * s, c * BK, m0);
-        tma_load(st + 2 * A_BYTES, &tmBh, full0 + 8 * s, c * BK, n0);
-        tma_load(st + 2 * A_BYTES + B_BYTES, &tmBl, full0 + 8 * s, c * BK, n0);
-        issued = c + 1;
+        tma_load(st, &tmA, full0 + 8 * s, kx, m0);
+        tma_load(st + 2 * A_BYTES, &tmBh, full0 + 8 * s, kx, n0);
+        tma_load(st + 2 * A_BYTES + B_BYTES, &tmBl, full0 + 8 * s, kx, n0);
+        issued = gc + 1;
       }
       if (*abort_flag) {
         // let the loads still in flight land before the shared memory is released
-        for (int c = issued > S ? issued - S : 0; c < issued; ++c) mbar_wait(full0 + 8 * (c % S), (c / S) & 1);
+        for (int gc = issued > S ? issued - S : 0; gc < issued; ++gc) mbar_wait(full0 + 8 * (gc % S), (gc / S) & 1);
       }
     }
   } else if (warp == 1) {
@@ -191,11 +239,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_gemm(const __grid_constant__
     if (lane == 0) {
       const uint32_t idesc =
           (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
-      for (int c = 0; c < KB; ++c) {
-        const int s = c % S, b = c & 1;
+      for (int gc = 0; gc < G; ++gc) {
+        const int s = gc % S, b = gc & 1;
         if (*abort_flag) break;
-        if (!mbar_wait(split0 + 8 * s, (c / S) & 1)) { *abort_flag = 1; break; }
-        if (c >= 2 && !mbar_wait(acce0 + 8 * b, ((c >> 1) - 1) & 1)) { *abort_flag = 1; break; }
+        if (!mbar_wait(split0 + 8 * s, (gc / S) & 1)) { *abort_flag = 1; break; }
+        if (gc >= 2 && !mbar_wait(acce0 + 8 * b, ((gc >> 1) - 1) & 1)) { *abort_flag = 1; break; }
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t st = sbase + s * STAGE, dt = tmem + (uint32_t)(b * BN);
 #pragma unroll
@@ -219,117 +267,128 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_gemm(const __grid_constant__
       mma_commit(fin);
       mbar_wait(fin, 0);
     }
-  } else {
-    // ---------------------------------------------------------- split + accumulate
-    const int e = tid - 64;                 // 0..255
-    const int srow = e >> 1, sh = e & 1;    // split: row of the tile, half of its 32 elements
-    const int lg = warp & 3, half = (warp - 2) >> 2;
-    const int row = m0 + lg * 32 + lane;    // accumulate: this thread's TMEM lane
-    float acc[HALF];
-#pragma unroll
-    for (int j = 0; j < HALF; ++j) acc[j] = 0.f;
+  } else if (warp < 6) {
+    // ---------------------------------------------------------- split
+    const int srow = tid - 64;  // 0..127
+    const int swz = srow & 7;
     float fd = 0.f, fu = 0.f;
-    auto consume = [&](int c) -> bool {
-      const int b = c & 1;
-      if (!__all_sync(0xffffffffu, mbar_wait(accf0 + 8 * b, (c >> 1) & 1))) return false;
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t ta = tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)(b * BN + half * HALF);
+    bool flux = false;
+    if (G > 0) {
+      int m0, n0;
+      tile_origin(0, m0, n0);
+      flux = g.mode == 1 && n0 == 0;
+    }
+    for (int gc = 0; gc < G; ++gc) {
+      const int s = gc % S, c = gc % KB;
+      const bool go = !*abort_flag && mbar_wait(full0 + 8 * s, (gc / S) & 1);
+      if (!__all_sync(0xffffffffu, go)) { *abort_flag = 1; break; }
+      uint8_t *arow = smem + s * STAGE + (srow >> 3) * 1024 + swz * 128;
+      float4 v[8];
 #pragma unroll
-      for (int c0 = 0; c0 < HALF; c0 += 16) {
-        uint32_t r[16];
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-            : "r"(ta + (uint32_t)c0));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      for (int u = 0; u < 8; ++u) v[u] = *reinterpret_cast<const float4 *>(arow + ((u ^ swz) << 4));
 #pragma unroll
-        for (int j = 0; j < 16; ++j) acc[c0 + j] += __uint_as_float(r[j]);
+      for (int u = 0; u < 8; ++u) {
+        // u is the logical 16-byte unit of the row; (u ^ swz) its place in the 128-byte swizzle row
+        float4 h, l;
+        h.x = tf32_rna_bits(v[u].x); l.x = tf32_rna_bits(v[u].x - h.x);
+        h.y = tf32_rna_bits(v[u].y); l.y = tf32_rna_bits(v[u].y - h.y);
+        h.z = tf32_rna_bits(v[u].z); l.z = tf32_rna_bits(v[u].z - h.z);
+        h.w = tf32_rna_bits(v[u].w); l.w = tf32_rna_bits(v[u].w - h.w);
+        *reinterpret_cast<float4 *>(arow + ((u ^ swz) << 4)) = h;
+        *reinterpret_cast<float4 *>(arow + A_BYTES + ((u ^ swz) << 4)) = l;
       }
-      asm volatile("tcgen05.fence::before_thread_sync;");
-      __syncwarp();
-      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(acce0 + 8 * b) : "memory");
-      return true;
-    };
-    bool ok = true;
-    for (int c = 0; c < KB; ++c) {
-      const int s = c % S;
-      const bool go = !*abort_flag && mbar_wait(full0 + 8 * s, (c / S) & 1);
-      if (!__all_sync(0xffffffffu, go)) { ok = false; break; }
-      uint8_t *arow = smem + s * STAGE + (srow >> 3) * 1024 + (srow & 7) * 128;
+      if (flux) {
+        // down / up weights of the chunk's 32 ordinates (zero past K): broadcast reads
+        const float4 *wd = reinterpret_cast<const float4 *>(fw + c * BK);
+        const float4 *wu = reinterpret_cast<const float4 *>(fw + kpad + c * BK);
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int j = sh * 4 + u;                       // logical 16-byte unit of the row
-        const int off = ((j ^ (srow & 7)) << 4);        // its place in the 128-byte swizzle row
-        float4 v = *reinterpret_cast<float4 *>(arow + off), h, l;
-        uint32_t t;
-        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v.x)); h.x = __uint_as_float(t);
-        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v.y)); h.y = __uint_as_float(t);
-        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v.z)); h.z = __uint_as_float(t);
-        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v.w)); h.w = __uint_as_float(t);
-        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v.x - h.x)); l.x = __uint_as_float(t);
-        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v.y - h.y)); l.y = __uint_as_float(t);
-        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v.z - h.z)); l.z = __uint_as_float(t);
-        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v.w - h.w)); l.w = __uint_as_float(t);
-        *reinterpret_cast<float4 *>(arow + off) = h;
-        *reinterpret_cast<float4 *>(arow + A_BYTES + off) = l;
-        if (g.mode == 1) {
-          const int col = c * BK + j * 4;
-          const float vv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const int cc = col + q;
-            if (cc < K) {
-              const float w = __ldg(&g.fluxw[cc]) * vv[q];
-              if (cc < g.ncol_down) fd += w; else fu += w;
-            }
-          }
+        for (int u = 0; u < 8; ++u) {
+          const float4 a = wd[u], b = wu[u];
+          fd = fmaf(a.x, v[u].x, fd); fd = fmaf(a.y, v[u].y, fd); fd = fmaf(a.z, v[u].z, fd); fd = fmaf(a.w, v[u].w, fd);
+          fu = fmaf(b.x, v[u].x, fu); fu = fmaf(b.y, v[u].y, fu); fu = fmaf(b.z, v[u].z, fu); fu = fmaf(b.w, v[u].w, fu);
         }
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncwarp();
       if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(split0 + 8 * s) : "memory");
-      if (c >= 1 && !consume(c - 1)) { ok = false; break; }
-    }
-    if (ok && KB > 0) ok = consume(KB - 1);
-    if (!ok) {
-      *abort_flag = 1;
-    } else {
-      if (g.mode == 1) {
-        fd += __shfl_xor_sync(0xffffffffu, fd, 1);
-        fu += __shfl_xor_sync(0xffffffffu, fu, 1);
+      if (flux && c == KB - 1) {
+        // the tile's fluxes are complete once its last chunk is split
+        int m0, n0;
+        tile_origin(gc, m0, n0);
         const int frow = m0 + srow;
-        if (sh == 0 && n0 == 0 && frow < g.M) {
+        if (frow < g.M) {
           g.fluxes[2 * (size_t)frow] = fd;
           g.fluxes[2 * (size_t)frow + 1] = fu;
         }
+        fd = 0.f; fu = 0.f;
       }
-      if (row < g.M) {
-        const int cb = n0 + half * HALF;
-        if (g.mode == 0) {
-          float *out = g.C + (size_t)row * g.ldc;
+      if (c == KB - 1 && gc + 1 < G) {
+        int m0, n0;
+        tile_origin(gc + 1, m0, n0);
+        flux = g.mode == 1 && n0 == 0;  // one N tile of a row tile forms its fluxes
+      }
+    }
+  } else {
+    // ---------------------------------------------------------- accumulate
+    const int lg = warp & 3, half = (warp - 6) >> 2;
+    float acc[HALF];
 #pragma unroll
-          for (int j = 0; j < HALF; j += 4) {
-            const int col = cb + j;
-            const float4 v = make_float4(fmaxf(acc[j], 0.f), fmaxf(acc[j + 1], 0.f), fmaxf(acc[j + 2], 0.f),
-                                         fmaxf(acc[j + 3], 0.f));
-            if (col + 3 < g.N) {
-              *reinterpret_cast<float4 *>(out + col) = v;  // col and ldc are multiples of 4
-            } else {
-              if (col < g.N) out[col] = v.x;
-              if (col + 1 < g.N) out[col + 1] = v.y;
-              if (col + 2 < g.N) out[col + 2] = v.z;
+    for (int j = 0; j < HALF; ++j) acc[j] = 0.f;
+    for (int gc = 0; gc < G; ++gc) {
+      const int b = gc & 1;
+      const bool go = !*abort_flag && mbar_wait(accf0 + 8 * b, (gc >> 1) & 1);
+      if (!__all_sync(0xffffffffu, go)) { *abort_flag = 1; break; }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t ta = tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)(b * BN + half * HALF);
+      // two loads in flight per wait
+#pragma unroll
+      for (int c0 = 0; c0 < HALF; c0 += 32) {
+        uint32_t r[32];
+        tmem_ld16(ta + (uint32_t)c0, r);
+        if (c0 + 16 < HALF) tmem_ld16(ta + (uint32_t)(c0 + 16), r + 16);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        reg_fence16(r);
+        if (c0 + 16 < HALF) reg_fence16(r + 16);
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          if (c0 + j < HALF) acc[c0 + j] += __uint_as_float(r[j]);
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(acce0 + 8 * b) : "memory");
+      if (gc % KB == KB - 1) {
+        int m0, n0;
+        tile_origin(gc, m0, n0);
+        const int row = m0 + lg * 32 + lane;
+        if (row < g.M) {
+          const int cb = n0 + half * HALF;
+          if (g.mode == 0) {
+            float *out = g.C + (size_t)row * g.ldc;
+#pragma unroll
+            for (int j = 0; j < HALF; j += 4) {
+              const int col = cb + j;
+              const float4 v = make_float4(fmaxf(acc[j], 0.f), fmaxf(acc[j + 1], 0.f), fmaxf(acc[j + 2], 0.f),
+                                           fmaxf(acc[j + 3], 0.f));
+              if (col + 3 < g.N) {
+                *reinterpret_cast<float4 *>(out + col) = v;  // col and ldc are multiples of 4
+              } else {
+                if (col < g.N) out[col] = v.x;
+                if (col + 1 < g.N) out[col + 1] = v.y;
+                if (col + 2 < g.N) out[col + 2] = v.z;
+              }
+            }
+          } else {
+            const int nrp = g.nr[row];
+            float *out = g.R + (size_t)row * g.nlm;
+#pragma unroll
+            for (int j = 0; j < HALF; ++j) {
+              const int col = cb + j;
+              if (col < g.nlm) out[col] = (col < nrp) ? acc[j] : 0.f;
             }
           }
-        } else {
-          const int nrp = g.nr[row];
-          float *out = g.R + (size_t)row * g.nlm;
-#pragma unroll
-          for (int j = 0; j < HALF; ++j) {
-            const int col = cb + j;
-            if (col < g.nlm) out[col] = (col < nrp) ? acc[j] : 0.f;
-          }
         }
+#pragma unroll
+        for (int j = 0; j < HALF; ++j) acc[j] = 0.f;
       }
     }
   }
