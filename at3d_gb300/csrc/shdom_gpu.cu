@@ -2,14 +2,17 @@
 // the GB300 SHDOM solve / render path.
 //
 // One iteration (SOLUTION_ITERATIONS, src/polarized/shdomsub1.f:674-797):
-//   1. SH -> DO   : SRCDO[p][c] = max(0, source in ordinate c)  (k_sh_to_do)
+//   1. SH -> DO   : SRCDO[p][c] = max(0, source in ordinate c)  (tensor-core
+//                   k_tc_gemm, or the factorized k_sh_to_do)
 //   2. sweeps     : downward ordinates, Lambertian bottom, upward ordinates;
-//                   every wavefront level is one k_sweep launch over all
-//                   (octant, point, ordinate) tasks of that level, or one
-//                   k_sweep_seq launch for grids whose wavefront is too deep
+//                   boundary-plane chains (k_sweep_p1) beside the source
+//                   pass (k_sweep_prep), then the wavefront levels
+//                   (k_sweep_levels, or one k_sweep per level); grids whose
+//                   wavefront is too deep are walked in the reference order
+//                   (k_sweep_seq)
 //   3. DO -> SH   : RADIANCE[p][j] from the ordinate radiances (masked to
 //                   the point's radiance truncation) + hemispheric fluxes
-//                   (k_do_to_sh)
+//                   (k_tc_gemm, or k_do_to_sh)
 //   4. source     : k_source (COMPUTE_SOURCE fused: dot products in FP64,
 //                   delta-source, new truncation, next radiance truncation)
 //   5. k_accel_param, k_accelerate (CALC_ACCEL_SOLCRIT, ACCELERATE_SOLUTION)
@@ -314,6 +317,7 @@ __device__ __forceinline__ void cell_source(float ext0, float srcext0, float ext
 __device__ __forceinline__ Trace reg_trace(const RegLoad &x, int b, int pt_unused) {
   Trace t;
   const float u = x.g.y, v = x.g.z;
+  t.u = u; t.v = v;
   t.f[0] = (1.f - u) * (1.f - v); t.f[1] = (1.f - u) * v; t.f[2] = u * (1.f - v); t.f[3] = u * v;
   float ext0 = 0.f, srcext0 = 0.f;
 #pragma unroll
@@ -1293,8 +1297,12 @@ struct Handle {
   DBuf<double> g_grad, g_beam, g_adj;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int coop_blocks = 0;
+  int nsm = 152;  // streaming multiprocessors of the handle's device
+  // 0: cooperative persistent kernel when available; 1: one launch per level;
+  // 2: as 1, with each iteration's launches replayed from a CUDA graph
   int sweep_mode = 0;
-  int nsm = 152;  // streaming multiprocessors of the handle's device  // 0: cooperative persistent kernel when available, 1: one launch per level
+  cudaGraphExec_t iter_graph[2] = {nullptr, nullptr};  // one iteration, without / with the fixed truncation
+  long long iter_graph_launches[2] = {0, 0};
   DBuf<float> col_cx, col_cy, col_cz, col_fluxw, cmu1t, cmu2t, cphi1t, cphi2, ylmsun;
   DBuf<int> nphi0, col_of;
   // medium
@@ -1312,7 +1320,8 @@ struct Handle {
   int tc_bn[2] = {0, 0}, tc_ntiles[2] = {0, 0}, tc_kpad[2] = {0, 0};
   DBuf<float> tc_bh[2], tc_bl[2];
   CUtensorMap tm_a[2], tm_bh[2], tm_bl[2];
-  bool seq[2] = {false, false};  // sequential-order sweep engine per hemisphere
+  bool seq[2] = {false, false};  // reference-order sweep engine per hemisphere
+
   bool initialized = false;
   int iters = 0;
   float solcrit = 1.f;
@@ -1485,6 +1494,13 @@ static void setup_tc(Handle &H) {
 template <typename T>
 static long long vbytes(const std::vector<T> &v) { return (long long)v.size() * (long long)sizeof(T); }
 
+// A hemisphere is swept in the reference order when its wavefront is too
+// deep for level scheduling.
+static bool reference_order(const Plan &P, int h) {
+  const int nlev = (int)P.seg_off[h].size() - 1;
+  return P.deep[h] || std::max(nlev, P.p1depth[h]) > 4 * (P.nx1 + P.ny1 + P.nz) + 64;
+}
+
 static long long plan_device_bytes(const Plan &P) {
   long long b = 0;
   b += vbytes(P.gridpos) + vbytes(P.xgrid) + vbytes(P.ygrid) + vbytes(P.zgrid) + vbytes(P.gridptr) + vbytes(P.neighptr);
@@ -1529,10 +1545,11 @@ static void upload_plan(Handle &H) {
   }
   for (int h = 0; h < 2; ++h) {
     int nlev = (int)P.seg_off[h].size() - 1;
-    H.seq[h] = std::max(nlev, P.p1depth[h]) > 4 * (P.nx1 + P.ny1 + P.nz) + 64;
+    H.seq[h] = reference_order(P, h);
     for (int l = 0; l < nlev; ++l)
       if (P.seg_off[h][l + 1] - P.seg_off[h][l] > MAXSEG) throw std::runtime_error("sweep schedule: too many segments in a level");
   }
+
   H.regular.upload(P.regular); H.geo.upload(P.geo);
   H.bnd.upload(P.bnd); H.topp.upload(P.topp); H.botp.upload(P.botp); H.lofj.upload(P.lofj);
   std::vector<int> bi(P.npts, -1);
@@ -1703,9 +1720,10 @@ static void sweep_hemisphere(Handle &H, int hemi) {
   Plan &P = H.P;
   SweepArgs a = sweep_args(H, hemi);
   if (H.seq[hemi]) {
-    int c0 = hemi ? P.ncol_down : 0, nc = hemi ? P.nang - P.ncol_down : P.ncol_down;
+    const int c0 = hemi ? P.ncol_down : 0, nc = hemi ? P.nang - P.ncol_down : P.ncol_down;
     if (nc > 0) k_sweep_seq<<<nc, SEQW, 0, H.stream>>>(a, H.order.p, c0);
     CK(cudaGetLastError());
+    H.launches += 1;
     return;
   }
   const std::vector<int> &off = P.seg_off[hemi];
@@ -1739,7 +1757,7 @@ static void sweep_hemisphere(Handle &H, int hemi) {
   }
   if (ng1 > 0) CK(cudaStreamWaitEvent(H.stream, H.ev_join, 0));
   if (nlev <= 0) return;
-  if (H.coop_blocks > 0 && H.sweep_mode == 0) {
+  if (H.coop_blocks > 0 && H.sweep_mode == 0) {  // (graph mode never takes the cooperative path)
     const Seg *sp = H.segs[hemi].p;
     const int *so = H.seg_off[hemi].p, *li = H.level_items[hemi].p;
     const float2 *wp = H.sweepw.p;
@@ -1782,6 +1800,8 @@ using shdom::Handle;
 struct shdom_handle {
   Handle h;
   ~shdom_handle() {
+    for (auto &g : h.iter_graph)
+      if (g) cudaGraphExecDestroy(g);
     if (h.stream) cudaStreamDestroy(h.stream);
     if (h.stream2) cudaStreamDestroy(h.stream2);
     if (h.ev_fork) cudaEventDestroy(h.ev_fork);
@@ -1909,11 +1929,11 @@ int shdom_solution_iterations(shdom_handle *hh, int maxiter, int *iters, float *
       double zero = 0.0;
       CK(cudaMemcpyAsync(&H.accel.p->a, &zero, sizeof(double), cudaMemcpyHostToDevice, H.stream));
     }
-    while (H.iters < maxiter && H.solcrit > P.prob.solacc) {
-      ++H.iters;
-      CK(cudaEventRecord(ev[0], H.stream));
+    // one iteration's launches; with timing, events between the phases
+    auto body = [&](bool fix, bool timed) {
+      if (timed) CK(cudaEventRecord(ev[0], H.stream));
       shdom::transform(H, 0);
-      CK(cudaEventRecord(ev[1], H.stream));
+      if (timed) CK(cudaEventRecord(ev[1], H.stream));
       int ntop = (int)P.topp.size(), nbot = (int)P.botp.size();
       if (ntop && P.ncol_down) {
         int t = ntop * P.ncol_down;
@@ -1927,15 +1947,44 @@ int shdom_solution_iterations(shdom_handle *hh, int maxiter, int *iters, float *
         H.launches += 1;
       }
       shdom::sweep_hemisphere(H, 1);
-      CK(cudaEventRecord(ev[2], H.stream));
+      if (timed) CK(cudaEventRecord(ev[2], H.stream));
       shdom::transform(H, 1);
-      CK(cudaEventRecord(ev[3], H.stream));
-      if (H.solcrit < 0.001f || H.iters > P.prob.iterfixsh) fixsh = true;
-      shdom::launch_source(H, 0, fixsh ? 1 : 0);
+      if (timed) CK(cudaEventRecord(ev[3], H.stream));
+      shdom::launch_source(H, 0, fix ? 1 : 0);
       shdom::k_accel_param<<<1, 1, 0, H.stream>>>(H.red.p, H.accel.p, P.prob.accelflag);
       H.launches += 2;
       int blocks = (int)std::min<size_t>(((size_t)P.npts * nlm + 255) / 256, 152 * 64);
       shdom::k_accelerate<<<blocks, 256, 0, H.stream>>>(H.source.p, H.delsource.p, H.ns.p, H.nso.p, P.npts, nlm, H.accel.p);
+    };
+    const bool graphed = H.sweep_mode == 2;
+    while (H.iters < maxiter && H.solcrit > P.prob.solacc) {
+      ++H.iters;
+      if (H.solcrit < 0.001f || H.iters > P.prob.iterfixsh) fixsh = true;
+      if (graphed) {
+        const int gi = fixsh ? 1 : 0;
+        if (!H.iter_graph[gi]) {
+          // capture only this thread's launches, so that other threads' handles keep working
+          const long long l0 = H.launches;
+          cudaGraph_t g = nullptr;
+          CK(cudaStreamBeginCapture(H.stream, cudaStreamCaptureModeThreadLocal));
+          body(fixsh, false);
+          CK(cudaStreamEndCapture(H.stream, &g));
+          const cudaError_t ie = cudaGraphInstantiate(&H.iter_graph[gi], g, 0);
+          cudaGraphDestroy(g);
+          CK(ie);
+          H.iter_graph_launches[gi] = H.launches - l0;
+          H.launches = l0;
+        }
+        CK(cudaEventRecord(ev[0], H.stream));
+        CK(cudaGraphLaunch(H.iter_graph[gi], H.stream));
+        H.launches += H.iter_graph_launches[gi];
+        // graph mode: the whole iteration counts as the first phase
+        CK(cudaEventRecord(ev[1], H.stream));
+        CK(cudaEventRecord(ev[2], H.stream));
+        CK(cudaEventRecord(ev[3], H.stream));
+      } else {
+        body(fixsh, true);
+      }
       CK(cudaEventRecord(ev[4], H.stream));
       shdom::AccelState st;
       CK(cudaMemcpyAsync(&st, H.accel.p, sizeof(st), cudaMemcpyDeviceToHost, H.stream));
@@ -2363,7 +2412,7 @@ int shdom_export_state(shdom_handle *hh, float *source, int *ns, float *radiance
 
 int shdom_set_sweep_mode(shdom_handle *hh, int mode) {
   if (!hh) return fail(nullptr, "null handle");
-  if (mode < 0 || mode > 1) return fail(hh, "shdom_set_sweep_mode: mode must be 0 or 1");
+  if (mode < 0 || mode > 2) return fail(hh, "shdom_set_sweep_mode: mode must be 0, 1 or 2");
   hh->h.sweep_mode = mode;
   return 0;
 }

@@ -868,6 +868,7 @@ bool build_schedule(const shdom_problem &p, Plan &P) {
   bool ok = true;
   std::vector<std::thread> th;
   std::vector<std::string> errs(8);
+  std::vector<int> deep(8, 0);  // octants whose wavefront is too deep for level scheduling
   for (int ioct : octs) {
     th.emplace_back([&, ioct]() {
       sweep_order(P, ioct);
@@ -929,7 +930,9 @@ bool build_schedule(const shdom_problem &p, Plan &P) {
           if (one) { kd[pt] = 3; lv[pt] = m1 + 1; }
           else { kd[pt] = fast ? 1 : 2; lv[pt] = Plan::kPhase2 + m2 + 1; }
           if (lv[pt] >= 2 * Plan::kPhase2 - 1 || (one && lv[pt] >= Plan::kPhase2)) {
-            errs[b] = "sweep planning: wavefront too deep";
+            // (periodic grids chain whole rows through the wrap-around) the
+            // hemisphere is swept in the reference order instead
+            deep[b] = 1;
             return;
           }
         }
@@ -940,6 +943,15 @@ bool build_schedule(const shdom_problem &p, Plan &P) {
   for (auto &e : errs) if (!e.empty()) { P.err = e; ok = false; }
   if (!ok) return false;
   for (int hemi = 0; hemi < 2; ++hemi) {
+    P.deep[hemi] = 0;
+    for (int ioct : octs)
+      if (((((ioct - 1) >> 2) & 1) == hemi) && deep[ioct - 1]) P.deep[hemi] = 1;
+    if (P.deep[hemi]) {
+      P.tasks[hemi].clear(); P.p1segs[hemi].clear(); P.p1off[hemi].assign(1, 0); P.p1depth[hemi] = 0;
+      P.segs[hemi].clear(); P.seg_off[hemi].assign(1, 0); P.level_items[hemi].clear();
+      P.nirr[hemi] = 0; P.nitems[hemi] = 0;
+      continue;
+    }
     std::vector<std::pair<int, int>> groups;  // (octant, class) pairs of this hemisphere
     for (int ioct : octs) {
       int b = ioct - 1;

@@ -98,6 +98,7 @@ struct Plan {
   std::vector<Seg> p1segs[2];                    // phase 1: one segment per level per (octant, class) group
   std::vector<int> p1off[2];                     // group -> first segment (ngroups + 1 entries)
   int p1depth[2] = {0, 0};
+  int deep[2] = {0, 0};  // hemisphere swept in the reference order (no level schedule)
   std::vector<Seg> segs[2];
   std::vector<int> seg_off[2];                   // level -> first segment (nlevels + 1 entries)
   std::vector<int> level_items[2];               // level -> task x column items

@@ -14,7 +14,8 @@ through two stages:
    handle and CUDA stream, so the kernels of all admitted units interleave
    on the GPU (each handle launches its sweep level by level, so no kernel
    waits on thread blocks that another unit's kernels could keep from
-   running).  Its state stays in HBM from upload to render and is freed
+   running, and replays each solution iteration from a captured CUDA
+   graph).  Its state stays in HBM from upload to render and is freed
    when the unit completes, which frees its slot and memory for the next.
 
 Units of a request that arrives while others are on the GPU start as soon
@@ -272,7 +273,7 @@ class SolveServer:
                     raise RuntimeError("request already failed")
                 rte = RTE.from_plan(u.plan, device=self.device)
                 u.plan = None
-                rte.set_sweep_mode("per_level")
+                rte.set_sweep_mode("graph")
                 if u.req.transform_mode:
                     rte.set_transform_mode(u.req.transform_mode)
                 it, sc = rte.solve(u.req.maxiter, verbose=False)

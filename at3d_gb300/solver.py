@@ -256,10 +256,11 @@ class RTE:
         return grad.reshape(shp + (2,))
 
     def set_sweep_mode(self, mode: str):
-        """'persistent' (one cooperative kernel per hemisphere; default) or
+        """'persistent' (one cooperative kernel per hemisphere; default),
         'per_level' (one launch per wavefront level; for solves that run
-        concurrently on one device)."""
-        modes = {"persistent": 0, "per_level": 1}
+        concurrently on one device) or 'graph' (per-level launches, each
+        iteration replayed from a captured CUDA graph)."""
+        modes = {"persistent": 0, "per_level": 1, "graph": 2}
         if mode not in modes:
             raise ValueError(f"sweep mode must be one of {sorted(modes)}")
         _check(self._h, _lib.lib().shdom_set_sweep_mode(self._h, modes[mode]))

@@ -37,7 +37,7 @@ typedef struct shdom_sizes {
     int ml, mm;
     int bcflag, ipflag;
     int iters;     /* iterations done so far (RTE._iters) */
-    int nlevels_down, nlevels_up; /* sweep wavefront levels per hemisphere */
+    int nlevels_down, nlevels_up; /* sweep wavefront levels per hemisphere (0: swept in the reference order) */
     float solcrit; /* current solution criterion (RTE._solcrit) */
     float albmax;
     long long launches; /* kernels launched on this handle since creation */
@@ -165,8 +165,11 @@ int shdom_set_transform_mode(shdom_handle *h, int mode);
 /* How the interior sweep levels are launched: 0 (default) one persistent
  * cooperative kernel per hemisphere with a grid barrier between levels
  * (when the device supports cooperative launch), 1 one kernel launch per
- * level.  Use 1 when several handles solve concurrently on one device: it
- * has no waits between thread blocks.  No reference counterpart. */
+ * level, 2 as 1 with each solution iteration's launches captured once in
+ * a CUDA graph (one per source-truncation state) and replayed.  Use 1 or 2
+ * when several handles solve concurrently on one device: they have no
+ * waits between thread blocks.  In mode 2 shdom_last_timings reports the
+ * whole iteration in its first entry.  No reference counterpart. */
 int shdom_set_sweep_mode(shdom_handle *h, int mode);
 
 /* Message of the last non-zero return on this handle (CHARACTER*600 errmsg

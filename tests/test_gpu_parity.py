@@ -68,6 +68,25 @@ def test_state_fixed_iterations(rte_cls, boundary):
     assert relrms(a["fluxes"], b["fluxes"]) < 1e-4
 
 
+def test_deep_periodic_grid(rte_cls):
+    """A periodic grid whose wrap-around chains are too deep for a level
+    schedule (planned as reference-order sweeps) against the oracle after 2
+    iterations."""
+    from at3d_gb300.scenes import cloud_field
+    from at3d_gb300.solver import plan_summary
+    pb = cloud_field(seed=4, nx=56, ny=56, nz=24, nmu=8, nphi=16, nleg=64, boundary="periodic")
+    s = plan_summary(pb)
+    assert s["nlevels_down"] == 0 and s["nlevels_up"] == 0
+    r = rte_cls.from_problem(pb)
+    r.solve(2, verbose=False)
+    o = Oracle(pb, fp64=False)
+    o.solve(2)
+    a, b = r.export_state(), o.export()
+    assert relrms(a["source"], b["source"]) < 1e-4
+    assert relrms(a["radiance"], b["radiance"]) < 1e-4
+    assert relrms(a["fluxes"], b["fluxes"]) < 1e-4
+
+
 def test_cloud_blob_converged_render(rte_cls):
     """The cloud-blob benchmark scene: converged solve and 9-view render."""
     pb = cloud_blob()

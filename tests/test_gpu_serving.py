@@ -35,15 +35,19 @@ def test_mix_equals_alone(requests):
     alone = []
     for k, (pb, rays) in enumerate(requests):
         r = RTE.from_problem(pb)
-        r.set_sweep_mode("per_level")
+        r.set_sweep_mode("graph")
         r.solve(100, verbose=False)
         alone.append(r.render(*rays))
+        it_graph = r.sizes["iters"]
         r.close()
-        if k < 2:  # the two sweep launch modes give the same field
-            r = RTE.from_problem(pb)
-            r.solve(100, verbose=False)
-            assert relrms(r.render(*rays), alone[-1]) < 1e-6
-            r.close()
+        if k < 2:  # the three sweep launch modes give the same field
+            for mode in ("persistent", "per_level"):
+                r = RTE.from_problem(pb)
+                r.set_sweep_mode(mode)
+                r.solve(100, verbose=False)
+                assert r.sizes["iters"] == it_graph
+                assert relrms(r.render(*rays), alone[-1]) < 1e-6
+                r.close()
     with SolveServer(slots=3) as srv:
         res = run_stream(srv, requests, poisson_arrivals(200.0, len(requests), seed=3))
         st = srv.stats()

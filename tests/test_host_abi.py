@@ -118,3 +118,12 @@ def test_planned_create_null_arguments(lib):
     assert lib.shdom_plan_create(None, C.byref(h), None) == 1
     assert lib.shdom_set_sweep_mode(None, 0) == 1
     lib.shdom_plan_destroy(None)
+
+
+def test_deep_periodic_plans():
+    """Periodic grids chain whole rows through the wrap-around; past the
+    level-schedule depth they plan as reference-order sweeps (no error)."""
+    from at3d_gb300.scenes import cloud_field
+    from at3d_gb300.solver import plan_summary
+    s = plan_summary(cloud_field(seed=4, nx=64, ny=64, nz=32, nmu=8, nphi=16, nleg=64, boundary="periodic"))
+    assert s["npts"] == 65 * 65 * 32 and s["nlevels_down"] == 0 and s["nlevels_up"] == 0

@@ -38,7 +38,7 @@ class FakeRTE:
         return r
 
     def set_sweep_mode(self, m):
-        assert m == "per_level"
+        assert m == "graph"
 
     def set_transform_mode(self, m):
         pass
