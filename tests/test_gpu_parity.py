@@ -136,3 +136,20 @@ def test_transform_modes(rte_cls, mode, tol):
     assert relrms(a["source"], b["source"]) < tol
     assert relrms(a["radiance"], b["radiance"]) < tol
     assert relrms(a["fluxes"], b["fluxes"]) < tol
+
+
+@pytest.mark.parametrize("mode", ["tf32x3", "fp32"])
+def test_precision_vs_fp64_fixture(rte_cls, mode):
+    """The 128x128x64 benchmark field (wavelength 3, ssa 0.99) after 30
+    iterations against the oracle run in FP64 (committed fixture): the
+    tensor-core 3xTF32 and the CUDA-core FP32 transforms both within 1e-4
+    relative RMS of the FP64 radiances."""
+    import os
+    from at3d_gb300.scenes import cloud_field
+    fx = np.load(os.path.join(os.path.dirname(__file__), "golden", "fp64_cloud_field_128x128x64.npz"))
+    pb = cloud_field(seed=2, wavelength_index=3, solacc=0.0)
+    r = rte_cls.from_problem(pb)
+    r.set_transform_mode(mode)
+    r.solve(int(fx["iterations"]), verbose=False)
+    rad = r.render(*orthographic_views(pb, 64, 64))
+    assert relrms(rad, fx["radiance_3"]) < 1e-4
