@@ -34,6 +34,7 @@ SIGNATURES = {
     "shdom_export_state": (C.c_int, [C.c_void_p, _f, _i, _f, _i, _f, _f]),
     "shdom_get_sizes": (C.c_int, [C.c_void_p, C.POINTER(ShdomSizes)]),
     "shdom_last_timings": (C.c_int, [C.c_void_p, _f]),
+    "shdom_sweep_timings": (C.c_int, [C.c_void_p, _f, _i]),
     "shdom_set_transform_mode": (C.c_int, [C.c_void_p, C.c_int]),
     "shdom_set_sweep_mode": (C.c_int, [C.c_void_p, C.c_int]),
     "shdom_plan_summary": (C.c_int, [C.c_void_p, C.POINTER(ShdomSizes)]),

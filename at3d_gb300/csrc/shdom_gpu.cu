@@ -1162,13 +1162,18 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
     const float *P1 = a.gridpos + 3 * ip1, *P2 = a.gridpos + 3 * ip2;
     double delx = P2[0] - P1[0], dely = P2[1] - P1[1], delz = P2[2] - P1[2];
     double idx = delx <= 0 ? 1.0 : 1.0 / delx, idy = dely <= 0 ? 1.0 : 1.0 / dely, idz = 1.0 / delz;
-    auto tri = [&](const float *v, double u, double vv, double ww) {
-      return (float)((1 - ww) * ((1 - vv) * ((1 - u) * v[0] + u * v[1]) + vv * ((1 - u) * v[2] + u * v[3])) +
-                     ww * ((1 - vv) * ((1 - u) * v[4] + u * v[5]) + vv * ((1 - u) * v[6] + u * v[7])));
+    // Positions and path lengths stay in FP64 (as the reference's); the
+    // trilinear weights are cell-relative coordinates in [0, 1] and the
+    // blend runs in FP32 (GB300's FP64 rate is a small fraction of FP32's).
+    auto tri = [&](const float *v, float u, float vv, float ww) {
+      const float a0 = fmaf(u, v[1] - v[0], v[0]), a1 = fmaf(u, v[3] - v[2], v[2]);
+      const float a2 = fmaf(u, v[5] - v[4], v[4]), a3 = fmaf(u, v[7] - v[6], v[6]);
+      const float b0 = fmaf(vv, a1 - a0, a0), b1 = fmaf(vv, a3 - a2, a2);
+      return fmaf(ww, b1 - b0, b0);
     };
-    double u = (xe - P1[0]) * idx, v = (ye - P1[1]) * idy, ww = (ze - P1[2]) * idz;
-    float srcext1 = fmaxf(0.f, tri(src8, u, v, ww));
-    float ext1 = tri(ext8, u, v, ww);
+    const float u0 = (float)((xe - P1[0]) * idx), v0 = (float)((ye - P1[1]) * idy), w0 = (float)((ze - P1[2]) * idz);
+    float srcext1 = fmaxf(0.f, tri(src8, u0, v0, w0));
+    float ext1 = tri(ext8, u0, v0, w0);
     const int cf = a.cellflags[cell];
     bool ipinx = (cf & 1) && !((a.bcflag & 1) && ((cx > 0 && xe < xm) || (cx < 0 && xe > xm)));
     bool ipiny = (cf & 2) && !((a.bcflag & 2) && ((cy > 0 && ye < ym) || (cy < 0 && ye > ym)));
@@ -1179,16 +1184,19 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
     double so = fmin(sox, fmin(soy, soz));
     if (so < -eps) { if (lane == 0) atomicCAS(a.err, ERR_NONE, ERR_RAY_SO); break; }
     double xn = xe + so * cx, yn = ye + so * cy, zn = ze + so * cz;
-    u = (xn - P1[0]) * idx; v = (yn - P1[1]) * idy; ww = (zn - P1[2]) * idz;
-    float extn = tri(ext8, u, v, ww);
+    // per unit path length, the cell-relative coordinates move by (du, dv, dw)
+    const float du = (float)(cx * idx), dv = (float)(cy * idy), dw = (float)(cz * idz);
+    const float sof = (float)so;
+    float extn = tri(ext8, fmaf(sof, du, u0), fmaf(sof, dv, v0), fmaf(sof, dw, w0));
     double taugrid = so * 0.5 * (ext1 + extn);
     int ntau = max(1, 1 + (int)(taugrid / a.tautol));
     double dels = so / ntau;
+    const float delsf = (float)dels;
     for (int it = 1; it <= ntau; ++it) {
-      double s = it * dels;
-      u = (xe + s * cx - P1[0]) * idx; v = (ye + s * cy - P1[1]) * idy; ww = (ze + s * cz - P1[2]) * idz;
-      float ext0 = tri(ext8, u, v, ww);
-      float srcext0 = fmaxf(0.f, tri(src8, u, v, ww));
+      const float sf_ = it * delsf;
+      const float uu_ = fmaf(sf_, du, u0), vv_ = fmaf(sf_, dv, v0), ww_ = fmaf(sf_, dw, w0);
+      float ext0 = tri(ext8, uu_, vv_, ww_);
+      float srcext0 = fmaxf(0.f, tri(src8, uu_, vv_, ww_));
       float ext = 0.5f * (ext0 + ext1);
       float absc, trc, src;
       if (ext != 0.f) {
@@ -1326,6 +1334,13 @@ struct Handle {
   int iters = 0;
   float solcrit = 1.f;
   float timings[5] = {0, 0, 0, 0, 0};
+  // sweep kernels of the last solve: [0] phase 1 beside the source pass (or
+  // the whole reference-order sweep), [1] the level pass; launches counted
+  float ktimes[2] = {0, 0};
+  int klaunches[2] = {0, 0};
+  bool ktime_on = false;             // record the sweep events in this iteration
+  bool ktime_rec[2] = {false, false};
+  cudaEvent_t ev_k[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
   long long launches = 0;
 };
 
@@ -1714,16 +1729,24 @@ static void build_irr(Handle &H) {
   }
   CK(cudaEventCreateWithFlags(&H.ev_fork, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&H.ev_join, cudaEventDisableTiming));
+  for (auto &hs : H.ev_k)
+    for (auto &e : hs) CK(cudaEventCreate(&e));
 }
 
 static void sweep_hemisphere(Handle &H, int hemi) {
   Plan &P = H.P;
   SweepArgs a = sweep_args(H, hemi);
+  H.ktime_rec[hemi] = H.ktime_on;
+  if (H.ktime_on) CK(cudaEventRecord(H.ev_k[hemi][0], H.stream));
   if (H.seq[hemi]) {
     const int c0 = hemi ? P.ncol_down : 0, nc = hemi ? P.nang - P.ncol_down : P.ncol_down;
     if (nc > 0) k_sweep_seq<<<nc, SEQW, 0, H.stream>>>(a, H.order.p, c0);
     CK(cudaGetLastError());
     H.launches += 1;
+    if (H.ktime_on) {
+      CK(cudaEventRecord(H.ev_k[hemi][1], H.stream));
+      CK(cudaEventRecord(H.ev_k[hemi][2], H.stream));
+    }
     return;
   }
   const std::vector<int> &off = P.seg_off[hemi];
@@ -1756,7 +1779,11 @@ static void sweep_hemisphere(Handle &H, int hemi) {
     }
   }
   if (ng1 > 0) CK(cudaStreamWaitEvent(H.stream, H.ev_join, 0));
-  if (nlev <= 0) return;
+  if (H.ktime_on) CK(cudaEventRecord(H.ev_k[hemi][1], H.stream));
+  if (nlev <= 0) {
+    if (H.ktime_on) CK(cudaEventRecord(H.ev_k[hemi][2], H.stream));
+    return;
+  }
   if (H.coop_blocks > 0 && H.sweep_mode == 0) {  // (graph mode never takes the cooperative path)
     const Seg *sp = H.segs[hemi].p;
     const int *so = H.seg_off[hemi].p, *li = H.level_items[hemi].p;
@@ -1765,6 +1792,7 @@ static void sweep_hemisphere(Handle &H, int hemi) {
     void *args[] = {&a, (void *)&sp, (void *)&so, (void *)&li, (void *)&wp, &nl};
     CK(cudaLaunchCooperativeKernel((const void *)k_sweep_levels, dim3(H.coop_blocks), dim3(256), args, 0, H.stream));
     H.launches += 1;
+    if (H.ktime_on) CK(cudaEventRecord(H.ev_k[hemi][2], H.stream));
     return;
   }
   for (int l = 0; l < nlev; ++l) {
@@ -1775,6 +1803,7 @@ static void sweep_hemisphere(Handle &H, int hemi) {
     H.launches += 1;
   }
   CK(cudaGetLastError());
+  if (H.ktime_on) CK(cudaEventRecord(H.ev_k[hemi][2], H.stream));
 }
 
 static int check_device_error(Handle &H) {
@@ -1806,6 +1835,9 @@ struct shdom_handle {
     if (h.stream2) cudaStreamDestroy(h.stream2);
     if (h.ev_fork) cudaEventDestroy(h.ev_fork);
     if (h.ev_join) cudaEventDestroy(h.ev_join);
+    for (auto &hs : h.ev_k)
+      for (auto &e : hs)
+        if (e) cudaEventDestroy(e);
   }
 };
 
@@ -1923,6 +1955,8 @@ int shdom_solution_iterations(shdom_handle *hh, int maxiter, int *iters, float *
     cudaEvent_t ev[6];
     for (auto &e : ev) CK(cudaEventCreate(&e));
     for (float &t : H.timings) t = 0.f;
+    H.ktimes[0] = H.ktimes[1] = 0.f;
+    H.klaunches[0] = H.klaunches[1] = 0;
     bool fixsh = false;
     const int nlm = P.nlm, nang = P.nang;
     {  // SOLUTION_ITERATIONS starts every call with no acceleration pending
@@ -1983,7 +2017,9 @@ int shdom_solution_iterations(shdom_handle *hh, int maxiter, int *iters, float *
         CK(cudaEventRecord(ev[2], H.stream));
         CK(cudaEventRecord(ev[3], H.stream));
       } else {
+        H.ktime_on = true;
         body(fixsh, true);
+        H.ktime_on = false;
       }
       CK(cudaEventRecord(ev[4], H.stream));
       shdom::AccelState st;
@@ -1996,7 +2032,16 @@ int shdom_solution_iterations(shdom_handle *hh, int maxiter, int *iters, float *
       CK(cudaEventElapsedTime(&t01, ev[0], ev[1])); CK(cudaEventElapsedTime(&t12, ev[1], ev[2]));
       CK(cudaEventElapsedTime(&t23, ev[2], ev[3])); CK(cudaEventElapsedTime(&t34, ev[3], ev[4]));
       H.timings[0] += t01; H.timings[1] += t12; H.timings[2] += t23; H.timings[3] += t34;
-      H.timings[4] += t01 + t12 + t23 + t34;
+      H.timings[4] += t01 + t12 + t23 + t34;  // (graph mode: the whole iteration is in the first entry)
+      for (int h = 0; h < 2; ++h) {
+        if (!H.ktime_rec[h]) continue;
+        float a0, a1;
+        CK(cudaEventElapsedTime(&a0, H.ev_k[h][0], H.ev_k[h][1]));
+        CK(cudaEventElapsedTime(&a1, H.ev_k[h][1], H.ev_k[h][2]));
+        H.ktimes[0] += a0; H.ktimes[1] += a1;
+        H.klaunches[0] += 1; H.klaunches[1] += 1;
+        H.ktime_rec[h] = false;
+      }
     }
     for (auto &e : ev) cudaEventDestroy(e);
   } catch (const std::exception &e) {
@@ -2449,6 +2494,15 @@ int shdom_plan_summary(const shdom_problem *problem, shdom_sizes *o) {
 int shdom_last_timings(shdom_handle *hh, float *ms5) {
   if (!hh || !ms5) return fail(hh, "null argument");
   for (int i = 0; i < 5; ++i) ms5[i] = hh->h.timings[i];
+  return 0;
+}
+
+int shdom_sweep_timings(shdom_handle *hh, float *ms2, int *launches2) {
+  if (!hh || !ms2) return fail(hh, "null argument");
+  for (int i = 0; i < 2; ++i) {
+    ms2[i] = hh->h.ktimes[i];
+    if (launches2) launches2[i] = hh->h.klaunches[i];
+  }
   return 0;
 }
 

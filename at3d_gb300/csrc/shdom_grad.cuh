@@ -263,19 +263,26 @@ __device__ void levis_traverse(const GradArgs &G, int ray, const float *ydir, co
     const float *P1 = a.gridpos + 3 * ip1, *P2 = a.gridpos + 3 * ip2;
     const double delx = P2[0] - P1[0], dely = P2[1] - P1[1], delz = P2[2] - P1[2];
     const double idx = delx <= 0 ? 1.0 : 1.0 / delx, idy = dely <= 0 ? 1.0 : 1.0 / dely, idz = 1.0 / delz;
-    auto kernel8 = [&](double x, double y, double z, double fc[8]) {
-      const double u = (x - P1[0]) * idx, v = (y - P1[1]) * idy, w = (z - P1[2]) * idz;
+    // Positions and path lengths stay in FP64 (as the reference's); the
+    // trilinear weights come from cell-relative coordinates in [0, 1] in
+    // FP32, and so do the interpolated extinction and source (GB300's FP64
+    // rate is a small fraction of FP32's).  The integrals, the future
+    // radiance and the gradient accumulations stay in FP64.
+    const float u0 = (float)((xe - P1[0]) * idx), v0 = (float)((ye - P1[1]) * idy), w0c = (float)((ze - P1[2]) * idz);
+    const float du = (float)(cx * idx), dv = (float)(cy * idy), dw = (float)(cz * idz);
+    auto kernel8 = [&](float s, float fc[8]) {
+      const float u = fmaf(s, du, u0), v = fmaf(s, dv, v0), w = fmaf(s, dw, w0c);
       fc[0] = (1 - w) * (1 - v) * (1 - u); fc[1] = (1 - w) * (1 - v) * u; fc[2] = (1 - w) * v * (1 - u); fc[3] = (1 - w) * v * u;
       fc[4] = w * (1 - v) * (1 - u); fc[5] = w * (1 - v) * u; fc[6] = w * v * (1 - u); fc[7] = w * v * u;
     };
-    double fc1[8], fc0[8];
-    kernel8(xe, ye, ze, fc1);
+    float fc1[8], fc0[8];
+    kernel8(0.f, fc1);
     float srcext1 = 0.f, ext1 = 0.f;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) srcext1 = (float)(srcext1 + fc1[k] * src8[k]);
+    for (int k = 0; k < 8; ++k) srcext1 = fmaf(fc1[k], src8[k], srcext1);
     srcext1 = fmaxf(0.f, srcext1);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) ext1 = (float)(ext1 + fc1[k] * ext8[k]);
+    for (int k = 0; k < 8; ++k) ext1 = fmaf(fc1[k], ext8[k], ext1);
     const int cf = a.cellflags[cell];
     const bool ipinx = (cf & 1) && !((a.bcflag & 1) && ((cx > 0 && xe < xm) || (cx < 0 && xe > xm)));
     const bool ipiny = (cf & 2) && !((a.bcflag & 2) && ((cy > 0 && ye < ym) || (cy < 0 && ye > ym)));
@@ -286,25 +293,24 @@ __device__ void levis_traverse(const GradArgs &G, int ray, const float *ydir, co
     const double so = fmin(sox, fmin(soy, soz));
     if (so < -eps) { if (lane == 0) atomicCAS(a.err, ERR_NONE, ERR_RAY_SO); break; }
     double xn = xe + so * cx, yn = ye + so * cy, zn = ze + so * cz;
-    double fcn[8];
-    kernel8(xn, yn, zn, fcn);
+    float fcn[8];
+    kernel8((float)so, fcn);
     float extn = 0.f;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) extn = (float)(extn + fcn[k] * ext8[k]);
+    for (int k = 0; k < 8; ++k) extn = fmaf(fcn[k], ext8[k], extn);
     const double taugrid = so * 0.5 * (ext1 + extn);
     const int ntau = max(1, 1 + (int)(taugrid / a.tautol));
     const double dels = so / ntau;
     double accG = 0.0, accS = 0.0, accR = 0.0;  // per-cell weights of this lane's corner
     const float ss8 = myss * myext;                // this corner's single scatter x extinction
     for (int it = 1; it <= ntau; ++it) {
-      const double sd = it * dels;
-      kernel8(xe + sd * cx, ye + sd * cy, ze + sd * cz, fc0);
+      kernel8((float)(it * dels), fc0);
       float srcext0 = 0.f, ext0 = 0.f;
 #pragma unroll
-      for (int k = 0; k < 8; ++k) srcext0 = (float)(srcext0 + fc0[k] * src8[k]);
+      for (int k = 0; k < 8; ++k) srcext0 = fmaf(fc0[k], src8[k], srcext0);
       if (it != ntau) {
 #pragma unroll
-        for (int k = 0; k < 8; ++k) ext0 = (float)(ext0 + fc0[k] * ext8[k]);
+        for (int k = 0; k < 8; ++k) ext0 = fmaf(fc0[k], ext8[k], ext0);
       } else {
         ext0 = extn;
       }
@@ -332,9 +338,10 @@ __device__ void levis_traverse(const GradArgs &G, int ray, const float *ydir, co
           const double pr1 = (rtot - cumf) / transmit;
           const double tnext = transmit * transcell;
           const double pr0 = (rtot - cumf - fn) / tnext;
-          double e0 = 0.0, e1 = 0.0;
+          float e0f = 0.f, e1f = 0.f;
 #pragma unroll
-          for (int k = 0; k < 8; ++k) { e0 += (double)ext8[k] * fc0[k]; e1 += (double)ext8[k] * fc1[k]; }
+          for (int k = 0; k < 8; ++k) { e0f = fmaf(ext8[k], fc0[k], e0f); e1f = fmaf(ext8[k], fc1[k], e1f); }
+          const double e0 = e0f, e1 = e1f;
           const double eavg = 0.5 * (e0 + e1);
           if (eavg != 0.0) {
             const double gb0 = -adj * pr0 * w0, gb1 = -adj * pr1 * w1;

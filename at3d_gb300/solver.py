@@ -280,6 +280,15 @@ class RTE:
         _check(self._h, _lib.lib().shdom_last_timings(self._h, _fp(t)))
         return t
 
+    def sweep_timings(self) -> dict:
+        """Device ms of the sweep's parts over the last solve: 'prep' (phase 1
+        beside the source pass), 'levels' (the level pass), and the number of
+        hemisphere sweeps timed."""
+        t = np.zeros(2, np.float32)
+        n = np.zeros(2, np.int32)
+        _check(self._h, _lib.lib().shdom_sweep_timings(self._h, _fp(t), n.ctypes.data_as(C.POINTER(C.c_int))))
+        return {"prep": float(t[0]), "levels": float(t[1]), "sweeps": int(n[1])}
+
     def close(self):
         if getattr(self, "_h", None):
             _lib.lib().shdom_destroy(self._h)

@@ -38,6 +38,10 @@ NWAVE = 4
 # tests/test_gpu_parity.py).  Used by the CPU arms to scale a one-iteration
 # sample to a full solve.
 SOLVE_ITERS = [30, 30, 30, 23]
+# DRAM bytes (read + write) per point-ordinate of one k_sweep_levels launch,
+# from ncu on the 96x96x48 field (2.195 GB for 73.5M point-ordinates);
+# profiles/k_sweep_levels_cloud_field_96x96x48.md.
+LEVELS_DRAM_BYTES_PER_ITEM = 29.9
 
 
 def scenes(args):
@@ -132,6 +136,7 @@ def gb300_arm(args, rank, ws):
     barrier()
     launches0 = sum(r.sizes["launches"] for r in rtes)
     phase = np.zeros(5)
+    sweep_parts = np.zeros(3)  # prep-side ms, level-pass ms, hemisphere sweeps timed
     t_ev0, t_ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev) as clk:
         barrier()
@@ -140,6 +145,9 @@ def gb300_arm(args, rank, ws):
         for _ in range(args.steps):
             step()
             phase += sum(np.asarray(r.timings(), np.float64) for r in rtes)
+            for r in rtes:
+                st = r.sweep_timings()
+                sweep_parts += (st["prep"], st["levels"], st["sweeps"])
         t_ev1.record()
         barrier()
         wall = time.perf_counter() - t0
@@ -182,28 +190,33 @@ def gb300_arm(args, rank, ws):
     e2e = {"value": ws * args.nwave / (e2e_ms / 1e3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms}
 
-    # ---- roofline of the dominant phase
+    # ---- roofline of the dominant kernel: the sweep's level pass (k_sweep_levels)
     s0 = rtes[0].sizes
     npts, nlm, nang = s0["npts"], s0["nlm"], s0["nang"]
     total_iters = args.steps * sum(iters)
     names = ["transform_sh_to_do", "sweep", "transform_do_to_sh", "source"]
-    dom = int(np.argmax(phase[:4]))
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    per_iter_ms = phase[dom] / max(1, total_iters)
-    if dom == 0:
-        alg = 4.0 * npts * (nlm + nang)          # read SOURCE, write the ordinate-space source
-    elif dom == 2:
-        alg = 4.0 * npts * (nang + nlm + 2)      # read ordinate radiance, write RADIANCE + fluxes
-    elif dom == 1:
-        alg = 4.0 * npts * nang * 2 + 4.0 * npts  # ordinate source in, ordinate radiance out, extinction
-    else:
-        alg = 4.0 * npts * (nlm * 5 + 8)          # radiance, source, delsource r/w, coefficients
-    achieved = alg / (per_iter_ms / 1e3) / 1e9
-    roofline = {"kernel": names[dom], "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "traffic": None, "peak_source": "measured" if peaks else "fallback",
-                "phase_ms_per_iter": {n: float(phase[i] / max(1, total_iters)) for i, n in enumerate(names)}}
+    nsweeps = max(1.0, sweep_parts[2])
+    items = npts * (nang / 2.0)                # point-ordinates of one hemisphere
+    alg = 12.0 * items                         # (radsrc, tr) read + radiance write per point-ordinate
+    levels_ms = sweep_parts[1] / nsweeps       # mean CUDA-event time of one level-pass launch
+    achieved = alg / (levels_ms / 1e3) / 1e9
+    # DRAM bytes per launch from ncu (96x96x48 capture, 29.9 bytes per point-ordinate), scaled
+    traffic = LEVELS_DRAM_BYTES_PER_ITEM * items
+    roofline = {"kernel": "k_sweep_levels", "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": traffic, "alg_bytes_per_launch": alg,
+                "ms_per_launch": levels_ms, "peak_source": "measured" if peaks else "fallback",
+                "phase_ms_per_iter": {n: float(phase[i] / max(1, total_iters)) for i, n in enumerate(names)},
+                "sweep_ms_per_hemisphere": {"phase1_and_source_pass": float(sweep_parts[0] / nsweeps),
+                                            "level_pass": float(levels_ms)}}
+    # the whole iteration against the per-iteration algorithmic bytes of the scope table:
+    # 4 NPTS (NLM (4 + 2 accel) + 8)
+    it_ms = phase[4] / max(1, total_iters)
+    b_it = 4.0 * npts * (nlm * 6 + 8)
+    roofline["iteration"] = {"alg_bytes": b_it, "ms": float(it_ms), "achieved": b_it / (it_ms / 1e3) / 1e9,
+                             "frac": b_it / (it_ms / 1e3) / 1e9 / hbm_peak}
     return dict(solves_per_s=solves_per_s, rays_per_s=rays_per_s, ms_step=ms_step, launches=launches,
                 iters=list(iters), e2e=e2e, roofline=roofline, clocks=clk.summary(), npts=npts)
 
@@ -227,6 +240,8 @@ def precision_block(args, dev):
     import torch
     from at3d_gb300.scenes import cloud_field, orthographic_views
     fx = np.load(PRECISION_FIXTURE) if os.path.exists(PRECISION_FIXTURE) else None
+    if fx is not None and (args.nx, args.nz, args.npix, args.boundary) != (128, 64, 64, "open"):
+        fx = None  # the fixture holds the 128x128x64 open-boundary field at 64x64 pixels
     niter = int(fx["iterations"]) if fx is not None else 30
     pbs = [cloud_field(seed=2, wavelength_index=w, nx=args.nx, ny=args.nx, nz=args.nz, boundary=args.boundary,
                        solacc=0.0) for w in range(args.nwave)]

@@ -151,6 +151,15 @@ int shdom_get_sizes(shdom_handle *h, shdom_sizes *out);
  * ordinate->harmonic transform, [3] source + acceleration, [4] total. */
 int shdom_last_timings(shdom_handle *h, float *ms5);
 
+/* Device time (ms, CUDA events on the handle's stream) of the sweep's two
+ * parts over the last shdom_solution_iterations call, summed over both
+ * hemispheres and all iterations: ms2[0] from the start of a hemisphere's
+ * sweep to the start of its level pass (phase 1 beside the source pass, or
+ * the whole reference-order sweep), ms2[1] the level pass.  launches2
+ * (may be NULL) counts the hemisphere sweeps timed; sweep mode 2 records
+ * none.  No reference counterpart (diagnostics). */
+int shdom_sweep_timings(shdom_handle *h, float *ms2, int *launches2);
+
 /* Arithmetic of the two spherical-harmonic <-> discrete-ordinate transforms
  * of each iteration (SH_TO_DO / DO_TO_SH, src/polarized/shdomsub1.f:2928-3254,
  * which the reference runs in FP32 on the CPU):
