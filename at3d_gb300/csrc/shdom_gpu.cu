@@ -1026,6 +1026,37 @@ constexpr int RNLM = 1024;    // max spherical-harmonic terms for the per-ray ta
 // src/polarized/shdomsub2.f:2311-2863, :3046-3192).  The spherical-harmonic
 // dot products of the new cell corners are split over groups of four lanes;
 // the path integration is evaluated uniformly by all lanes.
+// Real spherical harmonics Y_lm of one direction (mu, phi) into y[NLM] (the
+// j(l, m) term order of the solver), lane m of the warp running the upward
+// l recurrence of the normalised Wigner d^l_{m0}(mu) for its m.  FP32: the
+// values are stored as FP32 and dotted with FP32 coefficients.
+__device__ __forceinline__ void ylm_dir_warp(float *y, float x, float phf, int ml, int mm, int lane) {
+  const float fct = 0.3989422804014327f;  // 1/sqrt(2 pi)
+  for (int m = lane; m <= mm; m += 32) {
+    float c = 1.f, s = 0.f;
+    if (m > 0) sincosf(m * phf, &s, &c);
+    float dprev = 0.f, dcur;
+    if (m == 0) dcur = 1.f;
+    else {
+      float cc = 1.f;
+      for (int k = 1; k <= m; ++k) cc *= sqrtf((float)(m + k) / (float)k);
+      dcur = ((m & 1) ? -cc : cc) * powf(0.5f * sqrtf((1.f - x) * (1.f + x)), (float)m);
+    }
+    for (int l = m; l <= ml; ++l) {
+      const float v = fct * dcur * sqrtf(l + 0.5f);
+      const int j = (l <= mm) ? l * (l + 1) + m : (2 * mm + 1) * l - mm * mm + m;
+      y[j] = (c - s) * v;
+      y[j - 2 * m] = (c + s) * v;
+      float dn;
+      if (m == 0) dn = ((2 * l + 1) * x * dcur - l * dprev) / (l + 1);
+      else dn = ((2 * l + 1) * x * dcur - (l > m ? sqrtf((float)(l * l - m * m)) * dprev : 0.f)) /
+                sqrtf((float)((l + 1) * (l + 1) - m * m));
+      dprev = dcur;
+      dcur = dn;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
   __shared__ float ydir[RWARPS][RNLM];
   __shared__ float tl[RWARPS][64];
@@ -1047,32 +1078,7 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
     return;
   }
   // Y_lm in the ray direction: lane m runs the l recurrence of its m
-  {
-    const double x = (double)(float)mu2;
-    const float phf = (float)phi2;
-    const double fct = 0.3989422804014327;  // 1/sqrt(2 pi)
-    for (int m = lane; m <= a.mm; m += 32) {
-      double c = 1.0, s = 0.0;
-      if (m > 0) { c = cos(m * (double)phf); s = sin(m * (double)phf); }
-      double dprev = 0.0, dcur;
-      if (m == 0) dcur = 1.0;
-      else {
-        double cc = 1.0;
-        for (int k = 1; k <= m; ++k) cc *= sqrt((double)(m + k) / (double)k);
-        dcur = ((m & 1) ? -cc : cc) * pow(0.5 * sqrt((1.0 - x) * (1.0 + x)), m);
-      }
-      for (int l = m; l <= a.ml; ++l) {
-        double v = fct * dcur * sqrt(l + 0.5);
-        int j = (l <= a.mm) ? l * (l + 1) + m : (2 * a.mm + 1) * l - a.mm * a.mm + m;
-        ydir[w][j] = (float)((c - s) * v);
-        ydir[w][j - 2 * m] = (float)((c + s) * v);
-        double dn;
-        if (m == 0) dn = ((2 * l + 1) * x * dcur - l * dprev) / (l + 1);
-        else dn = ((2 * l + 1) * x * dcur - (l > m ? sqrt((double)(l * l - m * m)) * dprev : 0.0)) / sqrt((double)((l + 1) * (l + 1) - m * m));
-        dprev = dcur; dcur = dn;
-      }
-    }
-  }
+  ylm_dir_warp(ydir[w], (float)mu2, (float)phi2, a.ml, a.mm, lane);
   __syncwarp();
   // t_l = sum_m Ydir(l,m) Ysun(l,m)
   for (int l = lane; l <= a.ml; l += 32) {
@@ -1107,6 +1113,7 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
   float osrc[8] = {0};
   float ext8[8], src8[8];
   double radacc = 0.0, transmit = 1.0;
+  const double inv_tautol = 1.0 / (double)a.tautol;
   int ngrid = 0;
   bool validrad = false;
   const int grp = lane >> 2, gl = lane & 3;  // 8 groups of 4 lanes, one corner per group
@@ -1160,8 +1167,8 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
     for (int k = 0; k < 8; ++k) { oldp[k] = g[k]; osrc[k] = src8[k]; }
     const int ip1 = g[0], ip2 = g[7];
     const float *P1 = a.gridpos + 3 * ip1, *P2 = a.gridpos + 3 * ip2;
-    double delx = P2[0] - P1[0], dely = P2[1] - P1[1], delz = P2[2] - P1[2];
-    double idx = delx <= 0 ? 1.0 : 1.0 / delx, idy = dely <= 0 ? 1.0 : 1.0 / dely, idz = 1.0 / delz;
+    const float delx = P2[0] - P1[0], dely = P2[1] - P1[1], delz = P2[2] - P1[2];
+    const float idx = delx <= 0.f ? 1.f : 1.f / delx, idy = dely <= 0.f ? 1.f : 1.f / dely, idz = 1.f / delz;
     // Positions and path lengths stay in FP64 (as the reference's); the
     // trilinear weights are cell-relative coordinates in [0, 1] and the
     // blend runs in FP32 (GB300's FP64 rate is a small fraction of FP32's).
@@ -1171,7 +1178,7 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
       const float b0 = fmaf(vv, a1 - a0, a0), b1 = fmaf(vv, a3 - a2, a2);
       return fmaf(ww, b1 - b0, b0);
     };
-    const float u0 = (float)((xe - P1[0]) * idx), v0 = (float)((ye - P1[1]) * idy), w0 = (float)((ze - P1[2]) * idz);
+    const float u0 = (float)(xe - P1[0]) * idx, v0 = (float)(ye - P1[1]) * idy, w0 = (float)(ze - P1[2]) * idz;
     float srcext1 = fmaxf(0.f, tri(src8, u0, v0, w0));
     float ext1 = tri(ext8, u0, v0, w0);
     const int cf = a.cellflags[cell];
@@ -1185,13 +1192,12 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
     if (so < -eps) { if (lane == 0) atomicCAS(a.err, ERR_NONE, ERR_RAY_SO); break; }
     double xn = xe + so * cx, yn = ye + so * cy, zn = ze + so * cz;
     // per unit path length, the cell-relative coordinates move by (du, dv, dw)
-    const float du = (float)(cx * idx), dv = (float)(cy * idy), dw = (float)(cz * idz);
+    const float du = (float)cx * idx, dv = (float)cy * idy, dw = (float)cz * idz;
     const float sof = (float)so;
     float extn = tri(ext8, fmaf(sof, du, u0), fmaf(sof, dv, v0), fmaf(sof, dw, w0));
     double taugrid = so * 0.5 * (ext1 + extn);
-    int ntau = max(1, 1 + (int)(taugrid / a.tautol));
-    double dels = so / ntau;
-    const float delsf = (float)dels;
+    int ntau = max(1, 1 + (int)(taugrid * inv_tautol));
+    const float delsf = sof / (float)ntau;
     for (int it = 1; it <= ntau; ++it) {
       const float sf_ = it * delsf;
       const float uu_ = fmaf(sf_, du, u0), vv_ = fmaf(sf_, dv, v0), ww_ = fmaf(sf_, dw, w0);
@@ -1200,11 +1206,11 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
       float ext = 0.5f * (ext0 + ext1);
       float absc, trc, src;
       if (ext != 0.f) {
-        float tau = ext * (float)dels;
+        float tau = ext * delsf;
         absc = tau * (1.f - 0.5f * tau * (1.f - 0.33333333333f * tau));
         trc = 1.f - absc;
-        src = (0.5f * (srcext0 + srcext1) + 0.08333333333f * (ext0 * srcext1 - ext1 * srcext0) * (float)dels *
-                                                (1.f - 0.05f * (ext1 - ext0) * (float)dels)) / ext;
+        src = (0.5f * (srcext0 + srcext1) + 0.08333333333f * (ext0 * srcext1 - ext1 * srcext0) * delsf *
+                                                (1.f - 0.05f * (ext1 - ext0) * delsf)) / ext;
       } else { absc = 0.f; trc = 1.f; src = 0.f; }
       radacc += transmit * src * absc;
       transmit *= trc;

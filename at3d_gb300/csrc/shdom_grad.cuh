@@ -261,15 +261,15 @@ __device__ void levis_traverse(const GradArgs &G, int ray, const float *ydir, co
     for (int k = 0; k < 8; ++k) oldp[k] = g[k];
     const int ip1 = g[0], ip2 = g[7];
     const float *P1 = a.gridpos + 3 * ip1, *P2 = a.gridpos + 3 * ip2;
-    const double delx = P2[0] - P1[0], dely = P2[1] - P1[1], delz = P2[2] - P1[2];
-    const double idx = delx <= 0 ? 1.0 : 1.0 / delx, idy = dely <= 0 ? 1.0 : 1.0 / dely, idz = 1.0 / delz;
+    const float delx = P2[0] - P1[0], dely = P2[1] - P1[1], delz = P2[2] - P1[2];
+    const float idx = delx <= 0.f ? 1.f : 1.f / delx, idy = dely <= 0.f ? 1.f : 1.f / dely, idz = 1.f / delz;
     // Positions and path lengths stay in FP64 (as the reference's); the
     // trilinear weights come from cell-relative coordinates in [0, 1] in
     // FP32, and so do the interpolated extinction and source (GB300's FP64
     // rate is a small fraction of FP32's).  The integrals, the future
     // radiance and the gradient accumulations stay in FP64.
-    const float u0 = (float)((xe - P1[0]) * idx), v0 = (float)((ye - P1[1]) * idy), w0c = (float)((ze - P1[2]) * idz);
-    const float du = (float)(cx * idx), dv = (float)(cy * idy), dw = (float)(cz * idz);
+    const float u0 = (float)(xe - P1[0]) * idx, v0 = (float)(ye - P1[1]) * idy, w0c = (float)(ze - P1[2]) * idz;
+    const float du = (float)cx * idx, dv = (float)cy * idy, dw = (float)cz * idz;
     auto kernel8 = [&](float s, float fc[8]) {
       const float u = fmaf(s, du, u0), v = fmaf(s, dv, v0), w = fmaf(s, dw, w0c);
       fc[0] = (1 - w) * (1 - v) * (1 - u); fc[1] = (1 - w) * (1 - v) * u; fc[2] = (1 - w) * v * (1 - u); fc[3] = (1 - w) * v * u;
@@ -439,32 +439,7 @@ __global__ void __launch_bounds__(GWARPS * 32) k_levis_adjoint(GradArgs G) {
   if (ray >= a.nrays) return;
   if (G.adj[ray] == 0.0) return;
   float *ydir = ydir_s[w], *tl = tl_s[w];
-  {
-    const double x = (double)(float)a.cammu[ray];
-    const float phf = (float)a.camphi[ray];
-    const double fct = 0.3989422804014327;
-    for (int m = lane; m <= a.mm; m += 32) {
-      double c = 1.0, s = 0.0;
-      if (m > 0) { c = cos(m * (double)phf); s = sin(m * (double)phf); }
-      double dprev = 0.0, dcur;
-      if (m == 0) dcur = 1.0;
-      else {
-        double cc = 1.0;
-        for (int k = 1; k <= m; ++k) cc *= sqrt((double)(m + k) / (double)k);
-        dcur = ((m & 1) ? -cc : cc) * pow(0.5 * sqrt((1.0 - x) * (1.0 + x)), m);
-      }
-      for (int l = m; l <= a.ml; ++l) {
-        double v = fct * dcur * sqrt(l + 0.5);
-        int j = (l <= a.mm) ? l * (l + 1) + m : (2 * a.mm + 1) * l - a.mm * a.mm + m;
-        ydir[j] = (float)((c - s) * v);
-        ydir[j - 2 * m] = (float)((c + s) * v);
-        double dn;
-        if (m == 0) dn = ((2 * l + 1) * x * dcur - l * dprev) / (l + 1);
-        else dn = ((2 * l + 1) * x * dcur - (l > m ? sqrt((double)(l * l - m * m)) * dprev : 0.0)) / sqrt((double)((l + 1) * (l + 1) - m * m));
-        dprev = dcur; dcur = dn;
-      }
-    }
-  }
+  ylm_dir_warp(ydir, (float)a.cammu[ray], (float)a.camphi[ray], a.ml, a.mm, lane);
   __syncwarp();
   for (int l = lane; l <= a.ml; l += 32) {
     int me = min(l, a.mm), j0 = (l <= a.mm) ? l * l : (2 * a.mm + 1) * l - a.mm * a.mm - a.mm;
