@@ -264,6 +264,11 @@ class RTE:
         if mode not in modes:
             raise ValueError(f"sweep mode must be one of {sorted(modes)}")
         _check(self._h, _lib.lib().shdom_set_sweep_mode(self._h, modes[mode]))
+        self._sweep_mode = mode
+
+    @property
+    def sweep_mode(self) -> str:
+        return getattr(self, "_sweep_mode", "persistent")
 
     TRANSFORM_MODES = {"tf32x3": 0, "tf32": 1, "fp32": 2}
 

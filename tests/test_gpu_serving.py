@@ -74,3 +74,28 @@ def test_budget_admission(requests):
     with pytest.raises(MemoryError):
         too_big.submit(*requests[0]).result()
     too_big.close()
+
+
+def test_solvers_dict_concurrent_equals_sequential(requests):
+    """SolversDict.solve(n_jobs) (at3d/containers.py:699-742) solving several
+    wavelengths at once gives each solver the result it has alone."""
+    from at3d_gb300.containers import SolversDict
+    from at3d_gb300.solver import RTE
+    sub = requests[:4]
+    alone = []
+    for pb, rays in sub:
+        r = RTE.from_problem(pb)
+        r.solve(100, verbose=False)
+        alone.append((r.sizes["iters"], r.render(*rays)))
+        r.close()
+    sd = SolversDict()
+    for k, (pb, _) in enumerate(sub):
+        sd.add_solver(k, RTE.from_problem(pb))
+    sd.solve(n_jobs=4, maxiter=100, verbose=False)
+    for k, (pb, rays) in enumerate(sub):
+        r = sd[k]
+        assert r.sweep_mode == "persistent"          # restored after the threaded solve
+        assert r.sizes["iters"] == alone[k][0]
+        assert relrms(r.render(*rays), alone[k][1]) < 1e-6
+        assert r.check_solved(verbose=False)
+        r.close()
