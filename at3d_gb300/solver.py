@@ -10,6 +10,7 @@ HBM between calls.
 from __future__ import annotations
 
 import ctypes as C
+import threading
 import warnings
 
 import numpy as np
@@ -99,11 +100,16 @@ class RTE:
         self._create(device)
 
     @classmethod
-    def from_problem(cls, problem: Problem, device: int = 0, name: str | None = None):
+    def from_problem(cls, problem: Problem, device: int = 0, name: str | None = None, defer: bool = False):
+        """An RTE for a ready Problem.  With defer=True the host planning and
+        the upload run on a background thread: the call returns at once, the
+        first method that needs the device state waits for them, and a
+        planning error is raised there (so several solvers can be planned
+        while others already solve)."""
         self = cls.__new__(cls)
         self.problem = problem
         self.name = name or "RTE"
-        self._create(device)
+        self._create(device, defer)
         return self
 
     @classmethod
@@ -125,15 +131,46 @@ class RTE:
         self._initialized = False
         return self
 
-    def _create(self, device):
+    def _create(self, device, defer: bool = False):
         L = _lib.lib()
         self._struct = self.problem.to_struct()
-        h = C.c_void_p()
-        rc = L.shdom_create(C.byref(self._struct), int(device), C.byref(h))
-        if rc:
-            raise SHDOMError(L.shdom_last_error(None).decode())
-        self._h = h
         self._initialized = False
+
+        def make():
+            h = C.c_void_p()
+            rc = L.shdom_create(C.byref(self._struct), int(device), C.byref(h))
+            if rc:
+                raise SHDOMError(L.shdom_last_error(None).decode())
+            return h
+
+        if not defer:
+            self._h = make()
+            return
+        box = {}
+
+        def job():
+            try:
+                box["h"] = make()
+            except BaseException as e:  # raised at the first use of the handle
+                box["err"] = e
+
+        self.__dict__["_pending"] = (threading.Thread(target=job, daemon=True), box)
+        self.__dict__["_pending"][0].start()
+
+    @property
+    def _h(self):
+        pend = self.__dict__.pop("_pending", None)
+        if pend is not None:
+            pend[0].join()
+            if "err" in pend[1]:
+                self.__dict__["_hv"] = None
+                raise pend[1]["err"]
+            self.__dict__["_hv"] = pend[1]["h"]
+        return self.__dict__.get("_hv")
+
+    @_h.setter
+    def _h(self, value):
+        self.__dict__["_hv"] = value
 
     # ------------------------------------------------------------------
     @property

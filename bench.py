@@ -176,7 +176,8 @@ def gb300_arm(args, rank, ws):
     def e2e_step():
         sd = SolversDict()
         for w, pb in enumerate(pbs):
-            sd.add_solver(w, RTE.from_problem(pb, device=dev))
+            # host planning on background threads, overlapping the solves already running
+            sd.add_solver(w, RTE.from_problem(pb, device=dev, defer=True))
         sd.solve(n_jobs=args.jobs, maxiter=args.maxiter, verbose=False)
         res = [r.render(*rays) for r in sd.values()]
         for r in sd.values():

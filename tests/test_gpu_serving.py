@@ -90,7 +90,7 @@ def test_solvers_dict_concurrent_equals_sequential(requests):
         r.close()
     sd = SolversDict()
     for k, (pb, _) in enumerate(sub):
-        sd.add_solver(k, RTE.from_problem(pb))
+        sd.add_solver(k, RTE.from_problem(pb, defer=True))  # planned in the background
     sd.solve(n_jobs=4, maxiter=100, verbose=False)
     for k, (pb, rays) in enumerate(sub):
         r = sd[k]
