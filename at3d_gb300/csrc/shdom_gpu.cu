@@ -835,7 +835,54 @@ __global__ void __launch_bounds__(256) k_source(SourceArgs a) {
     const float *R = a.radiance + (size_t)p * a.nlm;
     int jlast = 0;  // 1-based index of the last term above shacc
     float pdot = 0.f, pold = 0.f, pnew = 0.f, pn = 0.f;  // this point's partial sums
-    for (int j0 = 0; j0 < a.nlm; j0 += 32) {
+    int jstart = 0;
+    if ((a.nlm & 3) == 0) {
+      // four consecutive terms per lane: 16-byte loads and stores, 128 terms per warp pass
+      for (int j0 = 0; j0 < a.nlm; j0 += 128) {
+        const int j = j0 + 4 * lane;
+        float jt[4] = {0.f, 0.f, 0.f, 0.f};
+        if (j < a.nlm) {
+          // rows are read only as far as the truncations use them (clear points keep few terms)
+          const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+          const float4 y4 = *reinterpret_cast<const float4 *>(a.ylmsun + j);
+          const float4 r4 = j < nrp ? *reinterpret_cast<const float4 *>(R + j) : z4;
+          const float yv[4] = {y4.x, y4.y, y4.z, y4.w}, rv[4] = {r4.x, r4.y, r4.z, r4.w};
+          float4 s4 = z4, d4 = z4;
+          if (!a.first) {
+            if (j < nsold) s4 = *reinterpret_cast<const float4 *>(S + j);
+            if (a.accel && j < nsmin) d4 = *reinterpret_cast<const float4 *>(D + j);
+          }
+          const float sv[4] = {s4.x, s4.y, s4.z, s4.w}, dv[4] = {d4.x, d4.y, d4.z, d4.w};
+          float dnew[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float c = cf[a.lofj[j + q]];
+            jt[q] = f0 * c * yv[q];
+            if (j + q < nrp) jt[q] += c * rv[q];
+            dnew[q] = 0.f;
+            if (!a.first) {
+              const float dn = jt[q] - sv[q];
+              if (a.accel) {
+                if (j + q < nsmin) { pdot += dn * dv[q]; pold += dv[q] * dv[q]; pnew += dn * dn; pn += sv[q] * sv[q]; }
+                if (j + q < nsold) dnew[q] = dn;
+              } else if (j + q < nsold) {
+                pnew += dn * dn; pn += sv[q] * sv[q];
+              }
+            }
+          }
+          if (!a.first && a.accel) *reinterpret_cast<float4 *>(D + j) = make_float4(dnew[0], dnew[1], dnew[2], dnew[3]);
+          // stash the new terms in the output row; truncated below once jlast is known
+          *reinterpret_cast<float4 *>(S + j) = make_float4(jt[0], jt[1], jt[2], jt[3]);
+        }
+        int lastq = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (j + q < a.nlm && fabsf(jt[q]) > a.shacc) lastq = j + q + 1;
+        jlast = max(jlast, __reduce_max_sync(0xffffffffu, lastq));
+      }
+      jstart = a.nlm;
+    }
+    for (int j0 = jstart; j0 < a.nlm; j0 += 32) {
       int j = j0 + lane;
       float jt = 0.f;
       if (j < a.nlm) {
