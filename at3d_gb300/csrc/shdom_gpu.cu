@@ -518,13 +518,20 @@ __device__ __forceinline__ int irr_seg_find(const Seg *__restrict__ segs, int ns
   return lo;
 }
 
-// Source pass, regular phase-2 items, one thread per (point, column).
+// Source pass, regular phase-2 items, one thread per (point, column).  A
+// regular trace stays in the point's start cell; where no point of the
+// cells around the point scatters (nbscat = 0) the source function is zero
+// in every iteration, so radsrc = 0 and tr depends on the extinction only:
+// once w holds those items (*ready != 0) they are skipped.
 __global__ void __launch_bounds__(256) k_sweep_prep(SweepArgs a, const uint8_t *__restrict__ kind,
                                                     const int *__restrict__ col_oct, const int *__restrict__ col_cls,
-                                                    int c0, int nc, float2 *__restrict__ w) {
+                                                    int c0, int nc, float2 *__restrict__ w,
+                                                    const uint8_t *__restrict__ nbscat, const int *__restrict__ ready) {
   const int total = a.npts * nc;
+  const bool skip_static = *ready != 0;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
     const int pt = idx / nc, col = c0 + (idx - pt * nc);
+    if (skip_static && !__ldg(nbscat + pt)) continue;
     if (__ldg(a.col_cz + col) == 0.f) continue;  // padding ordinate
     const int b = __ldg(col_oct + col) - 1, cls = __ldg(col_cls + col);
     if (__ldg(kind + ((size_t)b * 4 + cls) * a.npts + pt) != 1) continue;
@@ -575,17 +582,24 @@ __global__ void __launch_bounds__(256) k_irr_build(SweepArgs a, const Seg *__res
   }
 }
 
-// Phase 1: block g sweeps the levels of its group with block barriers.
-constexpr int P1_THREADS = 1024;
+// Phase 1: the levels of each group with block barriers.  The ordinates
+// of a group are independent of one another, so a group's columns are
+// split into P1_SPLIT contiguous ranges, one block each (block b: group
+// b / P1_SPLIT, range b % P1_SPLIT): shorter levels per block, more SMs.
+constexpr int P1_THREADS = 512;
+constexpr int P1_SPLIT = 4;
 
 __global__ void __launch_bounds__(P1_THREADS) k_sweep_p1(SweepArgs a, const Seg *__restrict__ p1segs,
                                                          const int *__restrict__ p1off) {
-  const int s0 = p1off[blockIdx.x], s1 = p1off[blockIdx.x + 1];
+  const int grp = blockIdx.x / P1_SPLIT, sid = blockIdx.x % P1_SPLIT;
+  const int s0 = p1off[grp], s1 = p1off[grp + 1];
   for (int si = s0; si < s1; ++si) {
     const Seg g = p1segs[si];
-    const int items = g.ntask * g.ncol;
-    for (int i = threadIdx.x; i < items; i += blockDim.x) {
-      const int task = i / g.ncol, slot = i - task * g.ncol;
+    const int cw = (g.ncol + P1_SPLIT - 1) / P1_SPLIT, cbeg = sid * cw, ncs = max(0, min(g.ncol, cbeg + cw) - cbeg);
+    const int items = g.ntask * ncs;
+    for (int ii = threadIdx.x; ii < items; ii += blockDim.x) {
+      const int task = ii / ncs, slot = cbeg + (ii - task * ncs);
+      const int i = task * g.ncol + slot;  // item of the segment
       const int pt = (int)__ldg(a.tasks + g.t0 + task), col = g.col0 + slot;
       const IrrRec rec = a.irr[g.irr0 + i];
       float rad;
@@ -776,6 +790,61 @@ __global__ void __launch_bounds__(SEQW) k_sweep_seq(SweepArgs a, const int *orde
 // radiance for downward columns; bottom points get the Lambertian surface
 // radiance computed from the downwelling flux (FIXED/VARIABLE_LAMBERTIAN_
 // BOUNDARY, src/polarized/shdomsub1.f:2438-2529).
+// Rows of the scattering points gathered into a dense block (the A operand
+// of the compacted tensor-core transforms); rowlen a multiple of 4.
+__global__ void k_gather_rows(const float *__restrict__ src, const int *__restrict__ rows, int nrows, int rowlen,
+                              float *__restrict__ dst) {
+  const int q = rowlen >> 2;
+  const long long total = (long long)nrows * q;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t / q), k = (int)(t - (long long)i * q);
+    reinterpret_cast<float4 *>(dst + (size_t)i * rowlen)[k] =
+        __ldg(reinterpret_cast<const float4 *>(src + (size_t)__ldg(rows + i) * rowlen) + k);
+  }
+}
+
+// Ordinate-to-harmonic transform of the points that do not scatter (a zero
+// coefficient row): their source is zero in every iteration and their
+// radiance is truncated to its first 4 terms, so only those 4 and the two
+// hemispheric fluxes are formed (FP32 sums over the ordinates, one warp
+// per point).  t4: the first 4 rows of the transform matrix [4][nang].
+__global__ void __launch_bounds__(256) k_do_to_sh_light(const float *__restrict__ raddo, int ldo, int nang, int ncol_down,
+                                                         const int *__restrict__ pts, int npts_light,
+                                                         const float *__restrict__ t4, const float *__restrict__ fluxw,
+                                                         float *__restrict__ radiance, int nlm, float *__restrict__ fluxes) {
+  const int lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < npts_light; w += nw) {
+    const int p = __ldg(pts + w);
+    const float *row = raddo + (size_t)p * ldo;
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f, fd = 0.f, fu = 0.f;
+    for (int c = lane; c < nang; c += 32) {
+      const float v = row[c];
+      a0 = fmaf(__ldg(t4 + c), v, a0);
+      a1 = fmaf(__ldg(t4 + nang + c), v, a1);
+      a2 = fmaf(__ldg(t4 + 2 * nang + c), v, a2);
+      a3 = fmaf(__ldg(t4 + 3 * nang + c), v, a3);
+      const float fv = __ldg(fluxw + c) * v;
+      if (c < ncol_down) fd += fv; else fu += fv;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+      a3 += __shfl_xor_sync(0xffffffffu, a3, o);
+      fd += __shfl_xor_sync(0xffffffffu, fd, o);
+      fu += __shfl_xor_sync(0xffffffffu, fu, o);
+    }
+    if (lane == 0) {
+      float *r = radiance + (size_t)p * nlm;
+      r[0] = a0; r[1] = a1; r[2] = a2; r[3] = a3;
+      fluxes[2 * (size_t)p] = fd;
+      fluxes[2 * (size_t)p + 1] = fu;
+    }
+  }
+}
+
 __global__ void k_preset_top(const int *topp, int ntop, float *raddo, int ldo, int ncol_down, float skyrad) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntop * ncol_down) return;
@@ -1368,6 +1437,8 @@ struct Handle {
   DBuf<int> nphi0, col_of;
   // medium
   DBuf<float> text, dirflux, coef, tms_w, phasetab, botalb, rad0;
+  DBuf<uint8_t> nbscat;  // 1 where a cell containing the point has a scattering corner
+  DBuf<int> wready;      // per hemisphere: the source pass has filled every item once
   DBuf<int> tms_ptr, tms_iph;
   // state
   DBuf<float> source, delsource, radiance, srcdo, raddo, fluxes, bcrad;
@@ -1379,6 +1450,13 @@ struct Handle {
   int xf_mode = 0;  // 0: 3xTF32 tensor cores, 1: single TF32 product, 2: CUDA-core factorized
   bool tc_ok[2] = {false, false};
   int tc_bn[2] = {0, 0}, tc_ntiles[2] = {0, 0}, tc_kpad[2] = {0, 0};
+  // compacted transforms: the scattering points' rows only (non-scattering
+  // points have a zero source and a 4-term radiance)
+  bool compact = false;
+  int nheavy = 0, nlight = 0;
+  DBuf<int> heavy, light;
+  DBuf<float> src_c, rad_c, t4;
+  CUtensorMap tm_ac[2];
   DBuf<float> tc_bh[2], tc_bl[2];
   CUtensorMap tm_a[2], tm_bh[2], tm_bl[2];
   bool seq[2] = {false, false};  // reference-order sweep engine per hemisphere
@@ -1554,6 +1632,38 @@ static void setup_tc(Handle &H) {
     H.tc_bn[dir] = bn; H.tc_ntiles[dir] = ntiles; H.tc_kpad[dir] = kpad;
     tc_attr(bn);
     H.tc_ok[dir] = true;
+    if (dir == 1) {  // first 4 rows of the ordinate-to-harmonic matrix, for the non-scattering points
+      std::vector<float> t4((size_t)4 * P.nang, 0.f);
+      for (int n = 0; n < std::min(4, N); ++n)
+        for (int k = 0; k < K; ++k) t4[(size_t)n * P.nang + k] = (float)T[(size_t)n * K + k];
+      H.t4.upload(t4);
+    }
+  }
+  // Non-scattering points (zero coefficient row) have a zero source in every
+  // iteration and a 4-term radiance (the radiance truncation of a point
+  // without scattering stays at 4), so the transforms need only the
+  // scattering points' rows: gathered into dense blocks for the tensor
+  // cores; the others get their 4 radiance terms and fluxes on the CUDA
+  // cores.  (Not with HIGHORDERRAD, which keeps every radiance term.)
+  if (H.tc_ok[0] && H.tc_ok[1] && !P.prob.highorderrad && P.nlm >= 4) {
+    const int nl = P.ml + 1;
+    std::vector<int> hv, lt;
+    for (int p = 0; p < P.npts; ++p) {
+      bool sc = false;
+      for (int l = 0; l < nl && !sc; ++l) sc = P.coef[(size_t)p * nl + l] != 0.f;
+      (sc ? hv : lt).push_back(p);
+    }
+    if (!lt.empty() && (long long)hv.size() * 10 < (long long)P.npts * 9) {
+      H.compact = true;
+      H.nheavy = (int)hv.size(); H.nlight = (int)lt.size();
+      H.heavy.upload(hv); H.light.upload(lt);
+      if (H.nheavy > 0) {
+        H.src_c.alloc((size_t)H.nheavy * P.nlm);
+        H.rad_c.alloc((size_t)H.nheavy * H.ldo);
+        make_map(&H.tm_ac[0], H.src_c.p, (uint64_t)P.nlm, (uint64_t)H.nheavy, (uint64_t)P.nlm, tc::BM);
+        make_map(&H.tm_ac[1], H.rad_c.p, (uint64_t)P.nang, (uint64_t)H.nheavy, (uint64_t)H.ldo, tc::BM);
+      }
+    }
   }
 }
 
@@ -1582,6 +1692,14 @@ static long long plan_device_bytes(const Plan &P) {
   b += vbytes(P.tms_iph) + vbytes(P.tms_w) + vbytes(P.phasetab) + vbytes(P.botalb) + vbytes(P.rad0);
   const long long ldo = (P.nang + 3) & ~3;
   b += 4LL * P.npts * (3LL * P.nlm + 2 * ldo + 2 + 3) + 4LL * (long long)P.botp.size() + 64;
+  {  // gathered rows of the scattering points for the compacted transforms
+    const int nl = P.ml + 1;
+    long long nh = 0;
+    for (int p = 0; p < P.npts; ++p)
+      for (int l = 0; l < nl; ++l)
+        if (P.coef[(size_t)p * nl + l] != 0.f) { ++nh; break; }
+    if (nh * 10 < (long long)P.npts * 9) b += 4LL * nh * (P.nlm + ldo) + 4LL * P.npts + 16LL * P.nang;
+  }
   const long long kp0 = (P.nlm + 31) / 32 * 32, kp1 = (P.nang + 31) / 32 * 32;
   const long long np0 = ((P.nang + 255) / 256) * 256 + 256, np1 = ((P.nlm + 2 + 255) / 256) * 256 + 256;
   b += 8LL * (np0 * kp0 + np1 * kp1);  // upper bound of the padded hi/lo matrices
@@ -1664,6 +1782,24 @@ static void upload_plan(Handle &H) {
     H.nphi0.upload(P.nphi0); H.col_of.upload(P.col_of);
   }
   H.text.upload(P.total_ext); H.dirflux.upload(P.dirflux); H.coef.upload(P.coef);
+  {
+    // scattering points (a non-zero coefficient row makes a non-zero source), spread to their cells' corners
+    const int nl = P.ml + 1;
+    std::vector<uint8_t> sc(P.npts, 0), nb(P.npts, 0);
+    for (int p = 0; p < P.npts; ++p)
+      for (int l = 0; l < nl; ++l)
+        if (P.coef[(size_t)p * nl + l] != 0.f) { sc[p] = 1; break; }
+    for (int c = 0; c < P.ncells; ++c) {
+      const int *g = &P.gridptr[8 * (size_t)c];
+      bool any = false;
+      for (int k = 0; k < 8; ++k) any = any || sc[g[k]];
+      if (any)
+        for (int k = 0; k < 8; ++k) nb[g[k]] = 1;
+    }
+    H.nbscat.upload(nb);
+    H.wready.alloc(2);
+    H.wready.zero(H.stream);
+  }
   H.tms_ptr.upload(P.tms_ptr); H.tms_iph.upload(P.tms_iph); H.tms_w.upload(P.tms_w);
   H.phasetab.upload(P.phasetab); H.botalb.upload(P.botalb); H.rad0.upload(P.rad0);
   H.ldo = (P.nang + 3) & ~3;
@@ -1732,7 +1868,35 @@ static void transform(Handle &H, int dir) {
       g.N = P.nlm; g.mode = 1; g.R = H.radiance.p; g.nlm = P.nlm; g.nr = H.nr.p; g.fluxes = H.fluxes.p;
       g.fluxw = H.col_fluxw.p; g.ncol_down = P.ncol_down;
     }
-    const int ntn = H.tc_ntiles[dir], ntiles = ntn * ((P.npts + tc::BM - 1) / tc::BM);
+    const int ntn = H.tc_ntiles[dir];
+    if (H.compact) {
+      // the scattering points' rows, gathered; the rest on the CUDA cores (ordinate-to-harmonic) or zero (source)
+      g.rowmap = H.heavy.p;
+      g.M = H.nheavy;
+      const int rowlen = dir == 0 ? P.nlm : H.ldo;
+      if (H.nheavy > 0) {
+        const long long q = (long long)H.nheavy * (rowlen / 4);
+        const int gb = (int)std::min<long long>((q + 255) / 256, 152 * 16);
+        k_gather_rows<<<gb, 256, 0, H.stream>>>(dir == 0 ? H.source.p : H.raddo.p, H.heavy.p, H.nheavy, rowlen,
+                                                 dir == 0 ? H.src_c.p : H.rad_c.p);
+        CK(cudaGetLastError());
+        const int ntiles = ntn * ((H.nheavy + tc::BM - 1) / tc::BM);
+        tc_launch(H.tc_bn[dir], H.nsm, H.stream, H.tm_ac[dir], H.tm_bh[dir], H.tm_bl[dir], dir == 0 ? P.nlm : P.nang,
+                  ntn, ntiles, g);
+        CK(cudaGetLastError());
+        H.launches += 1;
+      }
+      if (dir == 1 && H.nlight > 0) {
+        const int lb = std::min((H.nlight + 7) / 8, 152 * 16);
+        k_do_to_sh_light<<<lb, 256, 0, H.stream>>>(H.raddo.p, H.ldo, P.nang, P.ncol_down, H.light.p, H.nlight, H.t4.p,
+                                                    H.col_fluxw.p, H.radiance.p, P.nlm, H.fluxes.p);
+        CK(cudaGetLastError());
+        H.launches += 1;
+      }
+      H.launches += 1;
+      return;
+    }
+    const int ntiles = ntn * ((P.npts + tc::BM - 1) / tc::BM);
     tc_launch(H.tc_bn[dir], H.nsm, H.stream, H.tm_a[dir], H.tm_bh[dir], H.tm_bl[dir], dir == 0 ? P.nlm : P.nang, ntn,
               ntiles, g);
     CK(cudaGetLastError());
@@ -1809,7 +1973,7 @@ static void sweep_hemisphere(Handle &H, int hemi) {
   if (ng1 > 0) {
     CK(cudaEventRecord(H.ev_fork, H.stream));
     CK(cudaStreamWaitEvent(H.stream2, H.ev_fork, 0));
-    k_sweep_p1<<<ng1, P1_THREADS, 0, H.stream2>>>(a, H.p1segs[hemi].p, H.p1off[hemi].p);
+    k_sweep_p1<<<ng1 * P1_SPLIT, P1_THREADS, 0, H.stream2>>>(a, H.p1segs[hemi].p, H.p1off[hemi].p);
     CK(cudaGetLastError());
     CK(cudaEventRecord(H.ev_join, H.stream2));
     H.launches += 1;
@@ -1819,7 +1983,9 @@ static void sweep_hemisphere(Handle &H, int hemi) {
     const int c0 = hemi ? P.ncol_down : 0, nc = hemi ? P.nang - P.ncol_down : P.ncol_down;
     const long long total = (long long)P.npts * nc;
     const int blocks = (int)std::min<long long>((total + 255) / 256, 152 * 16);
-    k_sweep_prep<<<blocks, 256, 0, H.stream>>>(a, H.kind.p, H.col_oct.p, H.col_cls.p, c0, nc, H.sweepw.p);
+    k_sweep_prep<<<blocks, 256, 0, H.stream>>>(a, H.kind.p, H.col_oct.p, H.col_cls.p, c0, nc, H.sweepw.p, H.nbscat.p,
+                                                H.wready.p + hemi);
+    CK(cudaMemsetAsync(H.wready.p + hemi, 0xff, sizeof(int), H.stream));
     CK(cudaGetLastError());
     H.launches += 1;
     const int n2 = (int)P.nirr[hemi] - H.p2_irr_j0[hemi];

@@ -48,6 +48,7 @@ struct Epilogue {
   int ncol_down;     // columns below this are downward ordinates
   int *err;
   int split;
+  const int *rowmap;  // output point of each A row (A holds a compacted subset of the points), or null
 };
 
 __device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -317,8 +318,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_gemm(const __grid_constant__
         tile_origin(gc, m0, n0);
         const int frow = m0 + srow;
         if (frow < g.M) {
-          g.fluxes[2 * (size_t)frow] = fd;
-          g.fluxes[2 * (size_t)frow + 1] = fu;
+          const size_t fp = g.rowmap ? (size_t)g.rowmap[frow] : (size_t)frow;
+          g.fluxes[2 * fp] = fd;
+          g.fluxes[2 * fp + 1] = fu;
         }
         fd = 0.f; fu = 0.f;
       }
@@ -359,8 +361,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_gemm(const __grid_constant__
       if (gc % KB == KB - 1) {
         int m0, n0;
         tile_origin(gc, m0, n0);
-        const int row = m0 + lg * 32 + lane;
-        if (row < g.M) {
+        const int arow = m0 + lg * 32 + lane;
+        if (arow < g.M) {
+          const int row = g.rowmap ? g.rowmap[arow] : arow;
           const int cb = n0 + half * HALF;
           if (g.mode == 0) {
             float *out = g.C + (size_t)row * g.ldc;
