@@ -342,8 +342,8 @@ def serving_block(args, dev):
     from at3d_gb300.scenes import request_mix
     from at3d_gb300.serving import SolveServer, poisson_arrivals, run_stream
     out = []
+    reqs = request_mix(100, args.serve_requests)  # the same requests at every rate
     for k, rate in enumerate(args.serve_rates):
-        reqs = request_mix(100 + k, args.serve_requests)
         arr = poisson_arrivals(rate, len(reqs), seed=7 + k)
         with SolveServer(device=dev, slots=args.serve_slots) as srv:
             run_stream(srv, reqs, arr, maxiter=args.maxiter)
