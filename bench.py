@@ -55,14 +55,9 @@ def scenes(args):
 
 
 def dist_init():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    if ws > 1:
-        import torch.distributed as dist
-        import torch
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        dist.init_process_group("nccl")
-    return rank, ws
+    """One process per GPU under torchrun; replicas only (at3d_gb300.replicas)."""
+    from at3d_gb300 import replicas
+    return replicas.init()
 
 
 class ClockSampler:
@@ -133,10 +128,9 @@ def gb300_arm(args, rank, ws):
                             outs[w].data_ptr(), nr, 0)
 
     def barrier():
+        from at3d_gb300 import replicas
         torch.cuda.synchronize()
-        if ws > 1:
-            import torch.distributed as dist
-            dist.barrier()
+        replicas.barrier()
 
     for _ in range(args.warmup):
         step()
@@ -164,11 +158,8 @@ def gb300_arm(args, rank, ws):
         sweep_parts += (st["prep"], st["levels"], st["sweeps"])
     ms_dev = t_ev0.elapsed_time(t_ev1)
     ms_step = max(ms_dev, wall * 1e3) / args.steps
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
+    from at3d_gb300 import replicas
+    ms_step = replicas.max_over_ranks(ms_step)  # the slowest rank's step
     solves_per_s = ws * args.nwave / (ms_step / 1e3)
     rays_per_s = ws * args.nwave * nr / (ms_step / 1e3)
 
