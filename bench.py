@@ -356,7 +356,22 @@ def cpu_sample(args, wavelength: int, iters: int):
     t0 = time.perf_counter()
     o.solve(1)
     t_it = time.perf_counter() - t0
+    cpu_sample.oracle = o
     return t_init + iters * t_it, t_init, t_it
+
+
+def cpu_render_sample(args, nrays: int = 4096):
+    """The oracle's render of the first nrays rays of the benchmark views on
+    every host core (one ray slice per thread, as the reference's joblib
+    ray slicing), from the state of the last cpu_sample: rays/s and cores."""
+    _, rays = scenes(args)
+    sub = tuple(np.ascontiguousarray(np.asarray(a)[:nrays]) for a in rays)
+    cores = os.cpu_count() or 1
+    o = cpu_sample.oracle
+    t0 = time.perf_counter()
+    o.render(*sub, nthreads=cores)
+    dt = time.perf_counter() - t0
+    return nrays / dt, cores
 
 
 def reference_arm(args, rank, ws):
@@ -434,10 +449,13 @@ def main():
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
         t_solve, t_init, t_it = cpu_sample(args, 0, r["iters"][0])
+        rr, cores = cpu_render_sample(args)
         cpu = {"value": 1.0 / t_solve, "unit": "solves/s", "cores": 1, "kind": "port",
                "sample": f"oracle (CPU restatement of the reference Fortran): initialisation ({t_init:.1f} s) "
                          f"plus one iteration ({t_it:.1f} s) of wavelength 0 on the full grid, scaled to the "
-                         f"{r['iters'][0]} iterations of its solve; single thread"}
+                         f"{r['iters'][0]} iterations of its solve; single thread",
+               "render_rays_per_s": rr, "render_cores": cores,
+               "render_sample": "4096 rays of the benchmark views, one ray slice per host core"}
     out = {"metric": "SHDOM solves/s", "value": r["solves_per_s"], "unit": "solves/s", "n_gpus": ws,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_step"], "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",

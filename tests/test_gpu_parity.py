@@ -153,3 +153,21 @@ def test_precision_vs_fp64_fixture(rte_cls, mode):
     r.solve(int(fx["iterations"]), verbose=False)
     rad = r.render(*orthographic_views(pb, 64, 64))
     assert relrms(rad, fx["radiance_3"]) < 1e-4
+
+
+def test_device_error_is_reported_and_handle_stays_usable(rte_cls):
+    """A ray that starts below the domain makes the render kernel record an
+    error (RENDER: Level below domain, src/polarized/shdomsub4.f:223-236);
+    the host raises SHDOMError with the message and the handle renders on."""
+    from at3d_gb300.solver import SHDOMError
+    pb = cloud_blob(seed=7, nx=8, ny=8, nz=6, dx=0.04, dz=0.08)
+    r = rte_cls.from_problem(pb)
+    r.solve(3, verbose=False)
+    rays = orthographic_views(pb, 4, 4, zeniths=(0.0,))
+    good = r.render(*rays)
+    x, y, z, mu, phi = (np.array(a, copy=True) for a in rays)
+    z[0] = -1.0
+    with pytest.raises(SHDOMError, match="below domain"):
+        r.render(x, y, z, mu, phi)
+    again = r.render(*rays)
+    assert np.array_equal(again, good)
