@@ -73,7 +73,9 @@ class Species:
     """One scattering species on the property grid (a member of RTE.medium)."""
     extinction: np.ndarray            # [npx, npy, npz] 1/km
     ssalb: np.ndarray                 # [npx, npy, npz]
-    legcoef: np.ndarray               # [nleg+1] or [ntable, nleg+1]; a_l with the 2l+1 factor
+    legcoef: np.ndarray               # [nleg+1] or [ntable, nleg+1]; a_l with the 2l+1 factor.
+                                      # Polarized problems: [6, nleg+1] or [ntable, 6, nleg+1], the
+                                      # elements a1, a2, a3, a4, b1, b2 (at3d legcoef 'stokes_index')
     table_index: np.ndarray | None = None   # [nmicro, npx, npy, npz], 1-based into legcoef rows
     phase_weights: np.ndarray | None = None  # [nmicro, npx, npy, npz]
 
@@ -93,6 +95,7 @@ class Problem:
     surface_delx: float = 0.0
     surface_dely: float = 0.0
     params: NumericalParams = field(default_factory=NumericalParams)
+    num_stokes: int = 1               # 1 (scalar) or 3 (I, Q, U)
     _keep: list = field(default_factory=list, repr=False)
 
     @property
@@ -107,19 +110,36 @@ class Problem:
         # Concatenate every species' Legendre table into one table
         # (at3d/solver.py:2376-2411): each species' indices are offset by the
         # number of rows already in the table.
+        if self.num_stokes not in (1, 3):
+            raise ValueError("num_stokes must be 1 or 3")
+        pol = self.num_stokes == 3
         rows, offsets = [], []
         for s in self.species:
-            lc = np.atleast_2d(np.asarray(s.legcoef, dtype=np.float64))
+            lc = np.asarray(s.legcoef, dtype=np.float64)
+            if pol:
+                if lc.ndim == 2 and lc.shape[0] != 6:
+                    raise ValueError("a polarized legcoef has the 6 elements a1 a2 a3 a4 b1 b2 as rows")
+                lc = lc.reshape(-1, 6, lc.shape[-1])
+            else:
+                lc = np.atleast_2d(lc)
+                if lc.ndim != 2:
+                    raise ValueError("a scalar problem takes [nleg+1] or [ntable, nleg+1] legcoef")
             offsets.append(len(rows))
             rows.extend(list(lc))
         nl = self.params.num_mu_bins
         nmu = max(2, 2 * int((nl + 1) / 2))
         ml = nmu - 1
         nleg = ml + 1 if self.params.deltam else ml
-        nlegp = max(max(len(r) for r in rows) - 1, nleg)
-        legenp = np.zeros((len(rows), nlegp + 1), np.float32)
-        for k, r in enumerate(rows):
-            legenp[k, :len(r)] = r
+        nlegp = max(max(r.shape[-1] for r in rows) - 1, nleg)
+        if pol:
+            # LEGENP(NSTLEG, 0:NLEGP, NUMPHASE): [numphase][nlegp+1][6]
+            legenp = np.zeros((len(rows), nlegp + 1, 6), np.float32)
+            for k, r in enumerate(rows):
+                legenp[k, :r.shape[-1], :] = r.T
+        else:
+            legenp = np.zeros((len(rows), nlegp + 1), np.float32)
+            for k, r in enumerate(rows):
+                legenp[k, :len(r)] = r
         ext = np.zeros((nspec, ng), np.float32)
         alb = np.zeros((nspec, ng), np.float32)
         iph = np.ones((nspec, ng, maxnmicro), np.int32)
@@ -167,6 +187,6 @@ class Problem:
         st.highorderrad, st.iterfixsh = int(p.high_order_radiance), p.iterfixsh
         st.solacc, st.shacc, st.splitacc = p.solution_accuracy, p.spherical_harmonics_accuracy, p.split_accuracy
         st.tautol, st.transcut, st.transmin = p.tautol, p.transcut, p.transmin
-        st.nstokes = 1
+        st.nstokes = self.num_stokes
         self._keep = keep
         return st

@@ -8,6 +8,12 @@
   at3d/rayleigh.py:139-185, and RAYLEIGH_EXTINCT, src/shdomsub5.f:1457-1490),
   evaluated in single precision like the reference.
 * :func:`henyey_greenstein_legcoef` -- a_l = (2l+1) g^l.
+* :func:`rayleigh_legcoef6` -- the six Wigner-function expansion elements
+  (a1, a2, a3, a4, b1, b2) of the Rayleigh phase matrix with depolarisation
+  (RAYLEIGH_PHASE_FUNCTION, src/polarized/shdomsub4.f:2350-2386).
+* :func:`hg_matrix_legcoef6` -- a phase matrix whose I-I element is
+  Henyey-Greenstein and whose polarization elements follow the same series
+  scaled by a linear depolarisation factor (synthetic polarized medium).
 """
 from __future__ import annotations
 
@@ -55,3 +61,31 @@ def henyey_greenstein_legcoef(g: float, nterms: int) -> np.ndarray:
     """Henyey-Greenstein Legendre series a_l = (2l+1) g^l, l = 0..nterms-1."""
     l = np.arange(nterms, dtype=np.float64)
     return ((2 * l + 1) * g ** l).astype(np.float32)
+
+
+def rayleigh_legcoef6(depol: float) -> np.ndarray:
+    """Rayleigh phase matrix [6, 3] for linear depolarisation ratio ``depol``:
+    a1 = (1, 0, D/2), a2 = (0, 0, 3D), a4 = (0, 3DD'/2, 0), b1 = (0, 0, sqrt(3/2) D),
+    with D = (1-depol)/(1+depol/2), D' = (1-2 depol)/(1-depol)."""
+    d = (1.0 - depol) / (1.0 + 0.5 * depol)
+    dp = (1.0 - 2.0 * depol) / (1.0 - depol)
+    c = np.zeros((6, 3), np.float64)
+    c[0, 0] = 1.0
+    c[0, 2] = 0.5 * d
+    c[1, 2] = 3.0 * d
+    c[3, 1] = 1.5 * dp * d
+    c[4, 2] = np.sqrt(1.5) * d
+    return c.astype(np.float32)
+
+
+def hg_matrix_legcoef6(g: float, depol: float, nterms: int) -> np.ndarray:
+    """[6, nterms] phase matrix: a1 = (2l+1) g^l; a2 = a3 = (1-depol) a1 for
+    l >= 2 (the generalized functions of a2, a3 start at l = 2); a4 =
+    (1-2 depol) a1; b1 = b2 = 0 (no polarization created by single scattering)."""
+    a1 = henyey_greenstein_legcoef(g, nterms).astype(np.float64)
+    c = np.zeros((6, nterms), np.float64)
+    c[0] = a1
+    c[1, 2:] = (1.0 - depol) * a1[2:]
+    c[2, 2:] = (1.0 - depol) * a1[2:]
+    c[3] = (1.0 - 2.0 * depol) * a1
+    return c.astype(np.float32)

@@ -62,7 +62,8 @@ class Oracle:
     def _sizes(self):
         out = np.zeros(16, np.int32)
         self._lib.oracle_sizes(C.c_void_p(self._h), _p(out, C.c_int))
-        keys = ["npts", "nlm", "nmu", "nang", "ncells", "nx1", "ny1", "nz", "bcflag", "ipflag", "iters", "ml", "mm"]
+        keys = ["npts", "nlm", "nmu", "nang", "ncells", "nx1", "ny1", "nz", "bcflag", "ipflag", "iters", "ml", "mm",
+                "nstokes"]
         return dict(zip(keys, [int(v) for v in out[:len(keys)]]))
 
     def solve(self, maxiter: int, verbose: bool = False):
@@ -78,8 +79,9 @@ class Oracle:
             raise RuntimeError(self._lib.oracle_error(C.c_void_p(self._h)).decode())
 
     def export(self):
-        n, nlm = self.sizes["npts"], self.sizes["nlm"]
-        src = np.zeros((n, nlm), np.float32); rad = np.zeros((n, nlm), np.float32)
+        n, nlm, nst = self.sizes["npts"], self.sizes["nlm"], self.sizes["nstokes"]
+        shape = (n, nlm) if nst == 1 else (n, nst, nlm)
+        src = np.zeros(shape, np.float32); rad = np.zeros(shape, np.float32)
         ns = np.zeros(n, np.int32); nr = np.zeros(n, np.int32)
         flx = np.zeros((n, 2), np.float32); dfl = np.zeros(n, np.float32)
         self._lib.oracle_export(C.c_void_p(self._h), _p(src), _p(ns, C.c_int), _p(rad), _p(nr, C.c_int),
@@ -90,7 +92,8 @@ class Oracle:
         x = np.ascontiguousarray(x, np.float32); y = np.ascontiguousarray(y, np.float32)
         z = np.ascontiguousarray(z, np.float32)
         mu = np.ascontiguousarray(mu, np.float64); phi = np.ascontiguousarray(phi, np.float64)
-        out = np.zeros(len(x), np.float32)
+        nst = self.sizes["nstokes"]
+        out = np.zeros(len(x) if nst == 1 else (len(x), nst), np.float32)
         rc = self._lib.oracle_render(C.c_void_p(self._h), len(x), _p(x), _p(y), _p(z), _p(mu, C.c_double),
                                      _p(phi, C.c_double), _p(out), int(nthreads))
         if rc:

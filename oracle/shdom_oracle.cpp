@@ -22,7 +22,8 @@
 //    two are the same linear map (src/polarized/shdomsub1.f:3008-3030,
 //    :3222-3237), only rounding differs;
 //  * adaptive cell splitting is not implemented (splitacc must be <= 0);
-//  * the 2D independent-pixel sweep (ipflag 1 or 2) is not implemented.
+//  * the 2D independent-pixel sweep (ipflag 1 or 2) is not implemented;
+//  * NSTOKES is 1 or 3 (the V component, NSTOKES = 4, is not restated).
 
 #include "../include/shdom_problem.h"
 
@@ -81,16 +82,112 @@ static void wigner_dm0(double x, int lmax, int m, std::vector<double> &d) {
   for (int n = 0; n <= lmax; ++n) d[n] *= std::sqrt(n + 0.5);
 }
 
+// Wigner d^n_{m m1}(x) at n = max(m, m1) for m, m1 >= 0 (DMM1_N0,
+// src/polarized/shdomsub2.f:4431-4461): the closed form
+// c sqrt(prod_{p=1}^{|m-m1|} (m+m1+p)/p) ((1-x)/2)^{|m-m1|/2} ((1+x)/2)^{(m+m1)/2}.
+static double wigner_start(double x, int m, int m1) {
+  if (m == m1) return std::pow((1.0 + x) / 2.0, m);
+  const double c = (m1 > m) ? 1.0 : (((m - m1) & 1) ? -1.0 : 1.0);
+  const int hi = std::max(m, m1), lo = std::min(m, m1);
+  double prod = 1.0;
+  for (int q = 1; q <= hi - lo; ++q) prod *= std::sqrt((double)(m + m1 + q) / (double)q);
+  return c * prod * std::pow(std::sqrt((1.0 - x) / 2.0), hi - lo) * std::pow(std::sqrt((1.0 + x) / 2.0), hi + lo);
+}
+
+// Wigner d^n_{m m1}(x), n = 0..lmax, by the three-term upward recurrence in n
+// (WIGNERFCT, src/polarized/shdomsub2.f:4604-4646), not normalised.
+static void wigner_d(double x, int lmax, int m, int m1, std::vector<double> &d) {
+  d.assign(lmax + 1, 0.0);
+  const int n0 = std::max(m, m1);
+  if (n0 == 0) {
+    d[0] = 1.0;
+    if (lmax >= 1) d[1] = x;
+    for (int n = 1; n < lmax; ++n) d[n + 1] = (double)(2 * n + 1) * x / (n + 1) * d[n] - (double)n / (n + 1) * d[n - 1];
+    return;
+  }
+  if (n0 > lmax) return;
+  d[n0] = wigner_start(x, m, m1);
+  for (int n = n0; n < lmax; ++n) {
+    const double a = std::sqrt((double)((n + 1) * (n + 1) - m * m)), b = std::sqrt((double)((n + 1) * (n + 1) - m1 * m1));
+    const double f1 = ((double)(n * (n + 1)) * x - (double)(m * m1)) / a / b * (double)(2 * n + 1) / n;
+    const double f2 = std::sqrt((double)(n * n - m * m)) * std::sqrt((double)(n * n - m1 * m1)) / a / b * (double)(n + 1) / n;
+    d[n + 1] = f1 * d[n] - f2 * (n > n0 ? d[n - 1] : 0.0);
+  }
+}
+
+// The m1 = +2 and m1 = -2 functions of WIGNERFCT02P2M_NORMALIZED
+// (src/polarized/shdomsub2.f:4363-4428): d^n_{m,2}(x) and
+// d^n_{m,-2}(x) = (-1)^{n+m} d^n_{m,2}(-x), both times sqrt(n + 1/2).
+static void wigner_d2pm(double x, int lmax, int m, std::vector<double> &dp, std::vector<double> &dm) {
+  dp.assign(lmax + 1, 0.0); dm.assign(lmax + 1, 0.0);
+  if (m > lmax || lmax < 2) return;
+  const int n0 = std::max(m, 2);
+  dp[n0] = wigner_start(x, m, 2);
+  dm[n0] = wigner_start(-x, m, 2);
+  for (int n = n0; n < lmax; ++n) {
+    const double a = std::sqrt((double)((n + 1) * (n + 1) - m * m)), b = std::sqrt((double)((n + 1) * (n + 1) - 4));
+    const double f1 = 1.0 / a / b * (double)(2 * n + 1) / n;
+    const double f2 = std::sqrt((double)(n * n - m * m)) * std::sqrt((double)(n * n - 4)) / a / b * (double)(n + 1) / n;
+    const double fp = (double)(n * (n + 1)) * x - 2.0 * m, fm = -(double)(n * (n + 1)) * x - 2.0 * m;
+    dp[n + 1] = fp * f1 * dp[n] - f2 * (n > n0 ? dp[n - 1] : 0.0);
+    dm[n + 1] = fm * f1 * dm[n] - f2 * (n > n0 ? dm[n - 1] : 0.0);
+  }
+  for (int n = 0; n <= lmax; ++n) {
+    dm[n] *= ((n + m) & 1) ? -1.0 : 1.0;
+    dp[n] *= std::sqrt(n + 0.5);
+    dm[n] *= std::sqrt(n + 0.5);
+  }
+}
+
 static inline int sh_index(int l, int m, int mm) {
   // J = L(L+1)+M (L<=MM) or (2MM+1)L-MM^2+M, 0-based (YLMALL header,
   // src/polarized/shdomsub2.f:4252-4253).
   return (l <= mm) ? l * (l + 1) + m : (2 * mm + 1) * l - mm * mm + m;
 }
 
+// The six elements of the real generalized spherical functions, in the
+// reference's element order (1 I-I, 2 Q-Q, 3 U-U, 4 V-V, 5 I-Q, 6 Q-U):
+// PLMALL (src/polarized/shdomsub2.f:4650-4755) for the mu part alone
+// (phi < 0: out[j][6] is P), YLMALL (src/polarized/shdomsub2.f:4244-4354)
+// with the azimuth factors.  transpose flips the sign of the 5/6 parts that
+// the transposed matrices carry.
+static void genylm6(bool transpose, double x, double phi, bool with_phi, int ml, int mm, std::vector<double> &out) {
+  const int nlm = (2 * mm + 1) * (ml + 1) - mm * (mm + 1);
+  out.assign((size_t)nlm * 6, 0.0);
+  const double fct = 1.0 / std::sqrt(2.0 * std::acos(-1.0)), sg = transpose ? -1.0 : 1.0;
+  std::vector<double> d0, dp, dm;
+  for (int ma = 0; ma <= mm; ++ma) {
+    wigner_dm0(x, ml, ma, d0);
+    wigner_d2pm(x, ml, ma, dp, dm);
+    const double c = (with_phi && ma > 0) ? std::cos(ma * phi) : 1.0, s = (with_phi && ma > 0) ? std::sin(ma * phi) : 0.0;
+    for (int l = ma; l <= ml; ++l) {
+      const double p1 = fct * d0[l], p2 = -0.5 * fct * (dp[l] + dm[l]), p3 = -0.5 * fct * (dp[l] - dm[l]);
+      double *o = &out[(size_t)sh_index(l, ma, mm) * 6];
+      if (ma == 0 || !with_phi) {
+        o[0] = p1; o[1] = p2; o[2] = p2; o[3] = p1; o[4] = p3; o[5] = p3;
+      } else {
+        o[0] = p1 * c - p1 * s; o[1] = p2 * c - p2 * s; o[2] = p2 * c + p2 * s;
+        o[3] = p1 * c + p1 * s; o[4] = p3 * c - sg * p3 * s; o[5] = p3 * c + sg * p3 * s;
+      }
+      if (ma == 0) continue;
+      double *n = &out[(size_t)sh_index(l, -ma, mm) * 6];
+      if (!with_phi) {
+        n[0] = p1; n[1] = p2; n[2] = -p2; n[3] = -p1; n[4] = sg * p3; n[5] = -sg * p3;
+      } else {
+        n[0] = p1 * s + p1 * c; n[1] = p2 * s + p2 * c; n[2] = p2 * s - p2 * c;
+        n[3] = p1 * s - p1 * c; n[4] = p3 * s + sg * p3 * c; n[5] = p3 * s - sg * p3 * c;
+      }
+    }
+  }
+}
+
 template <typename R>
 struct Solver {
   shdom_problem p{};
   std::vector<float> zlev, extp, albp, phwtp, legp, sfcalb;
+  // input Legendre table: legenp [numphase][nlegp+1] or, polarized,
+  // [numphase][nlegp+1][6] (LEGENP(NSTLEG,0:NLEGP,NUMPHASE))
+  float leg_in(int i, int l, int k) const { return legp[((size_t)i * (p.nlegp + 1) + l) * nstleg + k]; }
   std::vector<int> iphp;
   std::string err;
 
@@ -109,13 +206,17 @@ struct Solver {
   std::vector<R> cmu1, cmu2;               // [nmu][nlm]
   std::vector<R> cphi1, cphi2;             // [nmu][nphi0max][2mm+1] (m index offset +mm)
   std::vector<R> ylmsun;                   // [nlm]
+  // polarized (nst = 3): Stokes components per SH term / ordinate value
+  int nst = 1, nstleg = 1;
+  std::vector<R> cmu1p, cmu2p;             // [nmu][nlm][6] generalized functions (CMU1 / CMU2)
 
   // medium on the grid
   int npart = 0, maxnmicro = 0, numphase = 0, nq = 0;
   std::vector<R> extinct, albedo, total_ext;  // [npart][npts], [npts]
   std::vector<int> iphase;                    // [npart][npts][8*maxnmicro]
   std::vector<R> phaseinterpwt;
-  std::vector<R> legen;  // [numphase][nleg+1]
+  std::vector<R> legen;  // [numphase][nleg+1] (the I-I element)
+  std::vector<R> legen6;  // [numphase][6][nleg+1] all six elements when nst = 3
   double extmin = 0, scatmin = 0;
   R albmax = 0;
   const float phasemax = 0.999f;
@@ -143,12 +244,14 @@ struct Solver {
     albp.assign(p.albedop, p.albedop + (size_t)p.npart * ng);
     iphp.assign(p.iphasep, p.iphasep + (size_t)p.npart * ng * p.maxnmicro);
     phwtp.assign(p.phasewtp, p.phasewtp + (size_t)p.npart * ng * p.maxnmicro);
-    legp.assign(p.legenp, p.legenp + (size_t)p.numphase * (p.nlegp + 1));
+    nst = p.nstokes;
+    if (nst != 1 && nst != 3) { err = "nstokes must be 1 or 3"; return false; }
+    nstleg = nst == 1 ? 1 : 6;
+    legp.assign(p.legenp, p.legenp + (size_t)p.numphase * (p.nlegp + 1) * nstleg);
     if (p.sfc_variable) sfcalb.assign(p.sfc_albedo, p.sfc_albedo + (size_t)p.nxsfc * p.nysfc);
     p.zlevels = nullptr; p.extinctp = p.albedop = p.phasewtp = p.legenp = p.sfc_albedo = nullptr;
     p.iphasep = nullptr;
     if (p.splitacc > 0) { err = "adaptive splitting is not supported"; return false; }
-    if (p.nstokes != 1) { err = "only nstokes=1 is supported"; return false; }
     if (!setup_grid()) return false;
     setup_angles();
     if (!transfer_properties()) return false;
@@ -345,6 +448,17 @@ struct Solver {
         }
       }
     }
+    if (nst == 3) {
+      // MAKE_SH_DO_COEF: CMU1 = PLMALL(.FALSE.), CMU2 = PLMALL(.TRUE.) * WTMU
+      cmu1p.assign((size_t)nmu * nlm * 6, 0); cmu2p.assign((size_t)nmu * nlm * 6, 0);
+      std::vector<double> prc;
+      for (int i = 0; i < nmu; ++i) {
+        genylm6(false, (double)mu[i], 0.0, false, ml, mm, prc);
+        for (int q = 0; q < nlm * 6; ++q) cmu1p[(size_t)i * nlm * 6 + q] = (R)prc[q];
+        genylm6(true, (double)mu[i], 0.0, false, ml, mm, prc);
+        for (int q = 0; q < nlm * 6; ++q) cmu2p[(size_t)i * nlm * 6 + q] = (R)prc[q] * (R)wtmu[i];
+      }
+    }
     int nm = 2 * mm + 1;
     cphi1.assign((size_t)nmu * nphi0max * nm, 0); cphi2.assign((size_t)nmu * nphi0max * nm, 0);
     for (int i = 0; i < nmu; ++i) {
@@ -395,7 +509,14 @@ struct Solver {
     for (int i = 0; i < numphase; ++i)
       for (int l = 0; l <= nleg; ++l)
         legen[(size_t)i * (nleg + 1) + l] =
-            (l <= p.nlegp) ? (R)(legp[(size_t)i * (p.nlegp + 1) + l] / (float)(2 * l + 1)) : (R)0;
+            (l <= p.nlegp) ? (R)(leg_in(i, l, 0) / (float)(2 * l + 1)) : (R)0;
+    if (nst == 3) {
+      legen6.assign((size_t)numphase * 6 * (nleg + 1), 0);
+      for (int i = 0; i < numphase; ++i)
+        for (int k = 0; k < 6; ++k)
+          for (int l = 0; l <= nleg && l <= p.nlegp; ++l)
+            legen6[((size_t)i * 6 + k) * (nleg + 1) + l] = (R)(leg_in(i, l, k) / (float)(2 * l + 1));
+    }
     extmin = (double)(1.0e-5f / ((zlev[npz - 1] - zlev[0]) / (float)npz));
     scatmin = 0.1 * extmin;
     extinct.assign((size_t)npart * npts, 0); albedo.assign((size_t)npart * npts, 0);
@@ -463,6 +584,13 @@ struct Solver {
         R *L = &legen[(size_t)i * (nleg + 1)];
         R f = L[ml + 1];
         for (int l = 0; l <= ml; ++l) L[l] = L[l] - f;
+        if (nst == 3) {
+          // diagonal elements lose f, the off-diagonal ones are kept (PREPARE_PROP 'N')
+          for (int k = 0; k < 4; ++k) {
+            R *L6 = &legen6[((size_t)i * 6 + k) * (nleg + 1)];
+            for (int l = 0; l <= ml; ++l) L6[l] = L6[l] - f;
+          }
+        }
       }
       for (int ipt = 0; ipt < npts; ++ipt) {
         R s = 0;
@@ -512,6 +640,30 @@ struct Solver {
     }
   }
 
+  // point_legen for all six elements (lt [6][nleg+1]); the delta-M division
+  // applies to every element's 0..ML terms (src/polarized/shdomsub1.f:1432-1450).
+  void point_legen6(int ipt, int ipa, std::vector<R> &lt, R &fout) const {
+    const int *IPH = &iphase[((size_t)ipa * npts + ipt) * nq];
+    const R *PW = &phaseinterpwt[((size_t)ipa * npts + ipt) * nq];
+    const int n1 = nleg + 1;
+    lt.assign((size_t)6 * n1, 0);
+    if (PW[0] >= phasemax) {
+      for (int q = 0; q < 6 * n1; ++q) lt[q] = legen6[(size_t)(IPH[0] - 1) * 6 * n1 + q];
+    } else {
+      for (int q = 0; q < nq; ++q) {
+        if (PW[q] <= (R)1e-5) continue;
+        for (int t = 0; t < 6 * n1; ++t) lt[t] += legen6[(size_t)(IPH[q] - 1) * 6 * n1 + t] * PW[q];
+      }
+    }
+    fout = 0;
+    if (p.deltam) {
+      R f = lt[ml + 1];
+      fout = f;
+      for (int k = 0; k < 6; ++k)
+        for (int l = 0; l <= ml; ++l) lt[(size_t)k * n1 + l] = lt[(size_t)k * n1 + l] / ((R)1 - f);
+    }
+  }
+
   // DIRECT_BEAM_PROP (src/polarized/shdom90.f90:352-867) via MAKE_DIRECT
   // (src/polarized/shdomsub2.f:393-476); regular property grid, no gas.
   void make_direct() {
@@ -527,7 +679,7 @@ struct Solver {
           for (int q = 0; q < maxnmicro; ++q) {
             int iph = iphp[((size_t)ipa * ng + ip) * maxnmicro + q];
             f += phwtp[((size_t)ipa * ng + ip) * maxnmicro + q] *
-                 (double)(legp[(size_t)(iph - 1) * (p.nlegp + 1) + L] / (float)(2 * L + 1));
+                 (double)(leg_in(iph - 1, L, 0) / (float)(2 * L + 1));
           }
           e = (1.0 - a * f) * e;
         }
@@ -641,7 +793,7 @@ struct Solver {
   // INIT_RADIANCE / EDDRTF / TRIDIAG (src/polarized/shdomsub2.f:614-1058),
   // solar source, base grid columns.
   void init_radiance() {
-    radiance.assign((size_t)npts * nlm, 0);
+    radiance.assign((size_t)npts * nlm * nst, 0);
     rshptr.assign(npts + 2, 0);
     const float pi = (float)std::acos(-1.0f);
     const float c0 = std::sqrt(1.0f / pi), c1 = std::sqrt(3.0f / (4 * pi));
@@ -673,11 +825,11 @@ struct Solver {
       eddrtf(nlayer, od, al, as, fl);
       for (int iz = 0; iz < nz; ++iz) {
         int L = nz - 1 - iz;
-        R *rad = &radiance[(size_t)ir];
+        // Only the I Stokes parameter is initialised (Q, U stay zero)
+        R *rad = &radiance[(size_t)ir * nst];
+        for (int q = 0; q < 4 * nst; ++q) rad[q] = 0;
         rad[0] = (R)(c0 * (float)(fl[2 * L] + fl[2 * L + 1]));
-        rad[1] = 0;
-        rad[2] = (R)(c1 * (float)(fl[2 * L] - fl[2 * L + 1]));
-        rad[3] = 0;
+        rad[2 * nst] = (R)(c1 * (float)(fl[2 * L] - fl[2 * L + 1]));
         ir += 4;
         rshptr[iz + nz * col + 1] = ir;
       }
@@ -768,6 +920,7 @@ struct Solver {
   // NEWMETHOD species mixing, src/polarized/shdomsub1.f:913-962, :1413-1485).
   void point_source(int i, std::vector<R> &sourcet, const std::vector<R> &rad, int ir, int nr,
                     std::vector<R> &lt, std::vector<R> &lt1) const {
+    if (nst == 3) { point_source_pol(i, sourcet, rad, ir, nr, lt, lt1); return; }
     double alb = 0.0;
     lt.assign(nleg + 1, 0);
     R fdum;
@@ -789,6 +942,42 @@ struct Solver {
     for (int j = 0; j < nr; ++j) sourcet[j] = sourcet[j] + albr * lt[lofj[j]] * rad[(size_t)ir + j];
   }
 
+  // Polarized form: CALC_SOURCE_PNT (src/polarized/shdomsub1.f:823-909) with
+  // the same species mixing applied to all six elements; sourcet [nlm][3]
+  // (Stokes fastest), rad in the same layout from term ir.
+  void point_source_pol(int i, std::vector<R> &sourcet, const std::vector<R> &rad, int ir, int nr,
+                        std::vector<R> &lt, std::vector<R> &lt1) const {
+    const int n1 = nleg + 1;
+    double alb = 0.0;
+    lt.assign((size_t)6 * n1, 0);
+    R fdum;
+    for (int ipa = 0; ipa < npart; ++ipa) {
+      double scat = (double)(R)(extinct[(size_t)ipa * npts + i] * albedo[(size_t)ipa * npts + i]);
+      alb += scat;
+      point_legen6(i, ipa, lt1, fdum);
+      for (int t = 0; t < 6 * n1; ++t) lt[t] = (R)(lt[t] + scat * lt1[t]);
+    }
+    if (alb > 1e-10) { for (int t = 0; t < 6 * n1; ++t) lt[t] = (R)(lt[t] / alb); }
+    else { for (int t = 0; t < 6 * n1; ++t) lt[t] = lt[t] / (R)npart; }
+    R ext = total_ext[i];
+    if (ext > (R)1e-10) alb = alb / ext; else alb = 0.0;
+    lt[0] = 1;
+    const R albr = (R)alb;
+    const R *a1 = &lt[0], *a2 = &lt[n1], *a3 = &lt[2 * n1], *b1 = &lt[4 * n1];
+    const R *Rd = &rad[(size_t)ir * 3];
+    sourcet.assign((size_t)nlm * 3, 0);
+    for (int j = 0; j < nr; ++j) sourcet[3 * j] += a1[lofj[j]] * Rd[3 * j];
+    for (int j = 0; j < nr; ++j) sourcet[3 * j] += b1[lofj[j]] * Rd[3 * j + 1];
+    for (int j = 4; j < nr; ++j) {
+      sourcet[3 * j + 1] += b1[lofj[j]] * Rd[3 * j] + a2[lofj[j]] * Rd[3 * j + 1];
+      sourcet[3 * j + 2] += a3[lofj[j]] * Rd[3 * j + 2];
+    }
+    for (int t = 0; t < 3 * nlm; ++t) sourcet[t] = albr * sourcet[t];
+    const R flux0 = dirflux[i] * ((R)1 / std::fabs((R)p.solarmu));
+    for (int j = 0; j < nlm; ++j) sourcet[3 * j] += flux0 * albr * a1[lofj[j]] * ylmsun[j];
+    for (int j = 4; j < nlm; ++j) sourcet[3 * j + 1] += flux0 * albr * b1[lofj[j]] * ylmsun[j];
+  }
+
   // COMPUTE_SOURCE (src/polarized/shdomsub1.f:967-1611), NEWMETHOD, 'N'.
   void compute_source(bool fixsh, bool first) {
     std::vector<R> sourcet, lt, lt1;
@@ -802,19 +991,21 @@ struct Solver {
         if (p.accelflag) {
           int iso = oshptr[i];
           int ns = std::min(shptr[i + 1] - is, oshptr[i + 1] - iso);
-          for (int j = 0; j < ns; ++j) {
-            R dn = sourcet[j] - source[(size_t)is + j];
-            djdot += dn * delsource[(size_t)iso + j];
-            djold += delsource[(size_t)iso + j] * delsource[(size_t)iso + j];
+          for (int t = 0; t < ns * nst; ++t) {
+            const size_t js = (size_t)is * nst + t, jo = (size_t)iso * nst + t;
+            R dn = sourcet[t] - source[js];
+            djdot += dn * delsource[jo];
+            djold += delsource[jo] * delsource[jo];
             djnew += dn * dn;
-            jn += source[(size_t)is + j] * source[(size_t)is + j];
+            jn += source[js] * source[js];
           }
         } else {
           int ns = shptr[i + 1] - is;
-          for (int j = 0; j < ns; ++j) {
-            R dn = sourcet[j] - source[(size_t)is + j];
+          for (int t = 0; t < ns * nst; ++t) {
+            const size_t js = (size_t)is * nst + t;
+            R dn = sourcet[t] - source[js];
             djnew += dn * dn;
-            jn += source[(size_t)is + j] * source[(size_t)is + j];
+            jn += source[js] * source[js];
           }
         }
       }
@@ -825,7 +1016,8 @@ struct Solver {
           point_source(i, sourcet, radiance, ir, nr, lt, lt1);
           int is = shptr[i], ns = shptr[i + 1] - is;
           oshptr[i] = is;
-          for (int j = 0; j < ns; ++j) delsource[(size_t)is + j] = sourcet[j] - source[(size_t)is + j];
+          for (int t = 0; t < ns * nst; ++t)
+            delsource[(size_t)is * nst + t] = sourcet[t] - source[(size_t)is * nst + t];
         }
         oshptr[npts] = shptr[npts];
       }
@@ -839,7 +1031,8 @@ struct Solver {
       else {
         int js = 0;  // solar source
         for (int j = 1; j <= nlm; ++j)
-          if (std::fabs(sourcet[j - 1]) > srcmin) js = j;
+          for (int k = 0; k < nst; ++k)
+            if (std::fabs(sourcet[(size_t)(j - 1) * nst + k]) > srcmin) js = j;
         if (js == 0) ns = 0;
         else {
           int ls = lofj[js - 1];
@@ -847,7 +1040,7 @@ struct Solver {
         }
         shptr[i] = is;
       }
-      for (int j = 0; j < ns; ++j) source[(size_t)is + j] = sourcet[j];
+      for (int t = 0; t < ns * nst; ++t) source[(size_t)is * nst + t] = sourcet[t];
       is += ns;
     }
     shptr[npts] = is;
@@ -908,7 +1101,7 @@ struct Solver {
                 }
               }
               if (p.deltam) legt = legt * f[ipa];
-              rad += w * albedo[(size_t)ipa * npts + i] * legt * radiance[(size_t)iro];
+              rad += w * albedo[(size_t)ipa * npts + i] * legt * radiance[(size_t)iro * nst];
             }
             if (rad > radmin) lr = l;
           }
@@ -982,8 +1175,8 @@ struct Solver {
   bool init_solution() {
     make_direct();
     init_radiance();
-    source.assign((size_t)npts * nlm, 0);
-    delsource.assign(p.accelflag ? (size_t)npts * nlm : 1, 0);
+    source.assign((size_t)npts * nlm * nst, 0);
+    delsource.assign(p.accelflag ? (size_t)npts * nlm * nst : 1, 0);
     shptr.assign(npts + 1, 0); oshptr.assign(npts + 1, 0);
     fluxes.assign((size_t)2 * npts, 0);
     compute_source(false, true);
@@ -1046,10 +1239,92 @@ struct Solver {
     }
   }
 
+  // SH_TO_DO (src/polarized/shdomsub1.f:2789-2926), DFT branch, NSTOKES = 3:
+  // work [npts][nphi0max][3].
+  void sh_to_do_pol(int imu, std::vector<R> &work) const {
+    const int n0 = nphi0[imu], nm = 2 * mm + 1;
+    std::vector<R> uv((size_t)3 * nm), cs((size_t)3 * nm);
+    const R *C1 = &cmu1p[(size_t)imu * nlm * 6];
+    for (int i = 0; i < npts; ++i) {
+      const int is = shptr[i], nsh = shptr[i + 1] - is;
+      R *out = &work[(size_t)i * nphi0max * 3];
+      if (nsh == 0) { for (int k = 0; k < 3 * n0; ++k) out[k] = 0; continue; }
+      const int me = std::max(0, std::min(n0 / 2 - 1, mofj[nsh - 1]));
+      std::fill(uv.begin(), uv.end(), (R)0);
+      const R *in = &source[(size_t)is * 3];
+      for (int j = 0; j < nsh; ++j) {
+        const int m = mofj[j] + mm;
+        const R *c = &C1[(size_t)j * 6];
+        uv[m] += c[0] * in[3 * j];
+        uv[nm + m] += c[1] * in[3 * j + 1] + c[4] * in[3 * j + 2];
+        uv[2 * nm + m] += c[5] * in[3 * j + 1] + c[2] * in[3 * j + 2];
+      }
+      std::fill(cs.begin(), cs.end(), (R)0);
+      for (int n = 0; n < 3; ++n) cs[n * nm + mm] = uv[n * nm + mm];
+      for (int m = 1; m <= me; ++m)
+        for (int n = 0; n < 2; ++n) {
+          cs[n * nm + mm + m] = uv[n * nm + mm + m] + uv[n * nm + mm - m];
+          cs[n * nm + mm - m] = uv[n * nm + mm - m] - uv[n * nm + mm + m];
+        }
+      for (int m = 1; m <= me; ++m) {
+        cs[2 * nm + mm - m] = uv[2 * nm + mm + m] - uv[2 * nm + mm - m];
+        cs[2 * nm + mm + m] = uv[2 * nm + mm + m] + uv[2 * nm + mm - m];
+      }
+      for (int k = 0; k < n0; ++k) {
+        const R *c = &cphi1[((size_t)imu * nphi0max + k) * nm + mm];
+        for (int n = 0; n < 3; ++n) {
+          R sum = 0;
+          for (int m = -me; m <= me; ++m) sum += c[m] * cs[n * nm + mm + m];
+          out[3 * k + n] = sum;
+        }
+      }
+    }
+  }
+
+  // DO_TO_SH (src/polarized/shdomsub1.f:3041-3160), DFT branch, NSTOKES = 3.
+  void do_to_sh_pol(int imu, const std::vector<R> &work) {
+    const int n0 = nphi0[imu], nm = 2 * mm + 1;
+    std::vector<R> uv((size_t)3 * nm), cs((size_t)3 * nm);
+    const R *C2 = &cmu2p[(size_t)imu * nlm * 6];
+    int is = 0;
+    for (int i = 0; i < npts; ++i) {
+      const int nsh = rshptr[i + 1] - rshptr[i];
+      const int me = std::max(0, std::min(n0 / 2 - 1, mofj[std::max(nsh, 1) - 1]));
+      const R *in = &work[(size_t)i * nphi0max * 3];
+      std::fill(cs.begin(), cs.end(), (R)0);
+      for (int m = -me; m <= me; ++m)
+        for (int n = 0; n < 3; ++n) {
+          R sum = 0;
+          for (int k = 0; k < n0; ++k) sum += cphi2[((size_t)imu * nphi0max + k) * nm + mm + m] * in[3 * k + n];
+          cs[n * nm + mm + m] = sum;
+        }
+      std::fill(uv.begin(), uv.end(), (R)0);
+      for (int n = 0; n < 3; ++n) uv[n * nm + mm] = cs[n * nm + mm];
+      for (int m = 1; m <= me; ++m) {
+        for (int n = 0; n < 2; ++n) {
+          uv[n * nm + mm + m] = cs[n * nm + mm + m] - cs[n * nm + mm - m];
+          uv[n * nm + mm - m] = cs[n * nm + mm + m] + cs[n * nm + mm - m];
+        }
+        uv[2 * nm + mm + m] = cs[2 * nm + mm + m] + cs[2 * nm + mm - m];
+        uv[2 * nm + mm - m] = cs[2 * nm + mm + m] - cs[2 * nm + mm - m];
+      }
+      R *out = &radiance[(size_t)is * 3];
+      for (int j = 0; j < nsh; ++j) {
+        const int m = mofj[j] + mm;
+        const R *c = &C2[(size_t)j * 6];
+        out[3 * j] += c[0] * uv[m];
+        out[3 * j + 1] += c[1] * uv[nm + m] + c[4] * uv[2 * nm + m];
+        out[3 * j + 2] += c[5] * uv[nm + m] + c[2] * uv[2 * nm + m];
+      }
+      is += nsh;
+    }
+  }
+
   // BACK_INT_GRID3D_UNPOL (src/polarized/shdomsub1.f:3695-4038).
   bool back_int_grid3d(float muv, float phiv, int kang, const std::vector<R> &work,
                        std::vector<R> &gridrad) {
     double eps = 1.0e-3 * (gridpos[3 * gridptr[7] + 2] - gridpos[3 * gridptr[0] + 2]);
+    auto Wv = [&](int q, int k) { return (double)work[((size_t)q * nphi0max + kang) * nst + k]; };
     const double pi = (double)(float)std::acos(-1.0f);
     double smu = (double)std::sqrt(1.0f - muv * muv);
     double cx = smu * std::cos((double)phiv + pi);
@@ -1067,10 +1342,11 @@ struct Solver {
     for (int iorder = 0; iorder < npts; ++iorder) {
       int ipcell = sweep_cell[(size_t)joct * npts + iorder];
       int ipt = gridptr[8 * ipcell + sweep_corner[(size_t)joct * npts + iorder]];
-      if (gridrad[ipt] >= 0) continue;
+      if (gridrad[(size_t)ipt * nst] >= 0) continue;
       int icell = ipcell;
-      double rad = 0.0, transmit = 1.0;
-      double ext1 = total_ext[ipt], srcext1 = ext1 * work[(size_t)ipt * nphi0max + kang];
+      double rad[3] = {0.0, 0.0, 0.0}, transmit = 1.0, srcext1[3], srcext0[3];
+      double ext1 = total_ext[ipt];
+      for (int k = 0; k < nst; ++k) srcext1[k] = ext1 * Wv(ipt, k);
       double xe = gridpos[3 * ipt], ye = gridpos[3 * ipt + 1], ze = gridpos[3 * ipt + 2];
       bool validrad = false;
       int guard = 0;
@@ -1109,37 +1385,39 @@ struct Solver {
           else ze = gridpos[3 * gridptr[8 * inext + ioct - 1] + 2];
         }
         double f1 = (1 - u) * (1 - v), f2 = (1 - u) * v, f3 = u * (1 - v), f4 = u * v;
-        const R *W = work.data();
         double ext0 = f1 * total_ext[i1] + f2 * total_ext[i2] + f3 * total_ext[i3] + f4 * total_ext[i4];
-        double srcext0 = f1 * W[(size_t)i1 * nphi0max + kang] * total_ext[i1] +
-                         f2 * W[(size_t)i2 * nphi0max + kang] * total_ext[i2] +
-                         f3 * W[(size_t)i3 * nphi0max + kang] * total_ext[i3] +
-                         f4 * W[(size_t)i4 * nphi0max + kang] * total_ext[i4];
-        double ext = 0.5 * (ext0 + ext1), tau = ext * so, transcell, abscell, src;
+        for (int k = 0; k < nst; ++k)
+          srcext0[k] = f1 * Wv(i1, k) * total_ext[i1] + f2 * Wv(i2, k) * total_ext[i2] + f3 * Wv(i3, k) * total_ext[i3] +
+                       f4 * Wv(i4, k) * total_ext[i4];
+        double ext = 0.5 * (ext0 + ext1), tau = ext * so, transcell, abscell;
         if (tau >= 0.5) { transcell = std::exp(-tau); abscell = 1.0 - transcell; }
         else { abscell = tau * (1.0 - 0.5 * tau * (1.0 - 0.33333333333 * tau * (1 - 0.25 * tau))); transcell = 1.0 - abscell; }
-        if (tau <= 2.0) {
-          if (ext == 0.0) src = 0.0;
-          else src = (0.5 * (srcext0 + srcext1) + 0.08333333333 * (ext0 * srcext1 - ext1 * srcext0) * so) / ext;
-        } else {
-          double ext0p = ext0, srcext0p = srcext0;
-          if (tau > 4.0) { ext0p = ext1 + (ext0 - ext1) * 4.0 / tau; if (ext0 > 0.0) srcext0p = srcext0 * ext0p / ext0; }
-          src = 1.0 / (ext0p + ext1) * (srcext0p + srcext1 + (ext0p * srcext1 - ext1 * srcext0p) * 2.0 / (ext0p + ext1) * (1 - 2 / tau + 2 * transcell / abscell));
+        for (int k = 0; k < nst; ++k) {
+          double src;
+          if (tau <= 2.0) {
+            if (ext == 0.0) src = 0.0;
+            else src = (0.5 * (srcext0[k] + srcext1[k]) + 0.08333333333 * (ext0 * srcext1[k] - ext1 * srcext0[k]) * so) / ext;
+          } else {
+            double ext0p = ext0, srcext0p = srcext0[k];
+            if (tau > 4.0) { ext0p = ext1 + (ext0 - ext1) * 4.0 / tau; if (ext0 > 0.0) srcext0p = srcext0[k] * ext0p / ext0; }
+            src = 1.0 / (ext0p + ext1) * (srcext0p + srcext1[k] + (ext0p * srcext1[k] - ext1 * srcext0p) * 2.0 / (ext0p + ext1) * (1 - 2 / tau + 2 * transcell / abscell));
+          }
+          if (k == 0) src = std::max(src, 0.0);  // only the I source is clipped
+          rad[k] += transmit * src * abscell;
         }
-        src = std::max(src, 0.0);
-        rad += transmit * src * abscell;
         transmit *= transcell;
-        bool validface = gridrad[i1] >= -0.1 && gridrad[i2] >= -0.1 && gridrad[i3] >= -0.1 && gridrad[i4] >= -0.1;
+        auto G = [&](int q, int k) { return (double)gridrad[(size_t)q * nst + k]; };
+        bool validface = G(i1, 0) >= -0.1 && G(i2, 0) >= -0.1 && G(i3, 0) >= -0.1 && G(i4, 0) >= -0.1;
         if (inext < 0 || (transmit <= transmin && validface)) {
           if (validface) {
             validrad = true;
-            rad += transmit * (f1 * gridrad[i1] + f2 * gridrad[i2] + f3 * gridrad[i3] + f4 * gridrad[i4]);
+            for (int k = 0; k < nst; ++k) rad[k] += transmit * (f1 * G(i1, k) + f2 * G(i2, k) + f3 * G(i3, k) + f4 * G(i4, k));
           } else { err = "BACK_INT_GRID3D: INEXTCELL=0"; return false; }
         } else {
-          ext1 = ext0; srcext1 = srcext0; icell = inext;
+          ext1 = ext0; for (int k = 0; k < nst; ++k) srcext1[k] = srcext0[k]; icell = inext;
         }
       }
-      gridrad[ipt] = (R)rad;
+      for (int k = 0; k < nst; ++k) gridrad[(size_t)ipt * nst + k] = (R)rad[k];
     }
     return true;
   }
@@ -1148,6 +1426,7 @@ struct Solver {
   bool back_int_grid1d(float muv, int kang, const std::vector<R> &work, std::vector<R> &gridrad) {
     double eps = 1.0e-3 * (gridpos[3 * gridptr[7] + 2] - gridpos[3 * gridptr[0] + 2]);
     (void)eps;
+    auto Wv = [&](int q, int k) { return (double)work[((size_t)q * nphi0max + kang) * nst + k]; };
     double cz = -(double)muv, czinv = 1.0 / cz;
     int bitz;
     if (cz < -1.0e-3) bitz = 1; else if (cz > 1.0e-3) bitz = 0; else { err = "BACK_INT_GRID1D: Bad MU"; return false; }
@@ -1156,10 +1435,10 @@ struct Solver {
     for (int iorder = 0; iorder < npts; ++iorder) {
       int ipcell = sweep_cell[(size_t)joct * npts + iorder];
       int ipt = gridptr[8 * ipcell + sweep_corner[(size_t)joct * npts + iorder]];
-      if (gridrad[ipt] >= 0) continue;
+      if (gridrad[(size_t)ipt * nst] >= 0) continue;
       int icell = ipcell;
-      double transmit = 1.0, ext1 = total_ext[ipt], rad = 0.0;
-      double srcext1 = ext1 * work[(size_t)ipt * nphi0max + kang];
+      double transmit = 1.0, ext1 = total_ext[ipt], rad[3] = {0.0, 0.0, 0.0}, srcext1[3], srcext0[3], src[3];
+      for (int k = 0; k < nst; ++k) srcext1[k] = ext1 * Wv(ipt, k);
       double ze = gridpos[3 * ipt + 2];
       bool validrad = false;
       int guard = 0;
@@ -1172,28 +1451,31 @@ struct Solver {
         int inext = neighptr[6 * icell + iface];
         int i1 = gridptr[8 * icell + (iface == 4 ? 0 : 4)];
         if (inext >= 0) ze = gridpos[3 * gridptr[8 * inext + ioct - 1] + 2];
-        double ext0 = total_ext[i1], srcext0 = total_ext[i1] * work[(size_t)i1 * nphi0max + kang];
-        double ext = 0.5 * (ext0 + ext1), tau = ext * so, transcell, abscell, src;
+        double ext0 = total_ext[i1];
+        for (int k = 0; k < nst; ++k) srcext0[k] = total_ext[i1] * Wv(i1, k);
+        double ext = 0.5 * (ext0 + ext1), tau = ext * so, transcell, abscell;
         if (tau >= 0.5) { transcell = std::exp(-tau); abscell = 1.0 - transcell; }
         else { abscell = tau * (1.0 - 0.5 * tau * (1.0 - 0.33333333333 * tau * (1 - 0.25 * tau))); transcell = 1.0 - abscell; }
-        if (tau <= 2.0) {
-          if (ext == 0.0) src = 0.0;
-          else src = (0.5 * (srcext0 + srcext1) + 0.08333333333 * (ext0 * srcext1 - ext1 * srcext0) * so) / ext;
-        } else {
-          double ext0p = ext0, srcext0p = srcext0;
-          if (tau > 4.0) { ext0p = ext1 + (ext0 - ext1) * 4.0 / tau; if (ext0 > 0.0) srcext0p = srcext0 * ext0p / ext0; }
-          src = 1.0 / (ext0p + ext1) * (srcext0p + srcext1 + (ext0p * srcext1 - ext1 * srcext0p) * 2.0 / (ext0p + ext1) * (1 - 2 / tau + 2 * transcell / abscell));
+        for (int k = 0; k < nst; ++k) {
+          if (tau <= 2.0) {
+            if (ext == 0.0) src[k] = 0.0;
+            else src[k] = (0.5 * (srcext0[k] + srcext1[k]) + 0.08333333333 * (ext0 * srcext1[k] - ext1 * srcext0[k]) * so) / ext;
+          } else {
+            double ext0p = ext0, srcext0p = srcext0[k];
+            if (tau > 4.0) { ext0p = ext1 + (ext0 - ext1) * 4.0 / tau; if (ext0 > 0.0) srcext0p = srcext0[k] * ext0p / ext0; }
+            src[k] = 1.0 / (ext0p + ext1) * (srcext0p + srcext1[k] + (ext0p * srcext1[k] - ext1 * srcext0p) * 2.0 / (ext0p + ext1) * (1 - 2 / tau + 2 * transcell / abscell));
+          }
         }
-        src = std::max(src, 0.0);
-        if (gridrad[i1] >= -0.1) {
+        src[0] = std::max(src[0], 0.0);
+        if (gridrad[(size_t)i1 * nst] >= -0.1) {
           validrad = true;
-          rad += transmit * (gridrad[i1] * transcell + src * abscell);
+          for (int k = 0; k < nst; ++k) rad[k] += transmit * (gridrad[(size_t)i1 * nst + k] * transcell + src[k] * abscell);
         } else {
-          rad += transmit * src * abscell;
-          srcext1 = srcext0; transmit *= transcell; ext1 = ext0; icell = inext;
+          for (int k = 0; k < nst; ++k) { rad[k] += transmit * src[k] * abscell; srcext1[k] = srcext0[k]; }
+          transmit *= transcell; ext1 = ext0; icell = inext;
         }
       }
-      gridrad[ipt] = (R)rad;
+      for (int k = 0; k < nst; ++k) gridrad[(size_t)ipt * nst + k] = (R)rad[k];
     }
     return true;
   }
@@ -1202,36 +1484,43 @@ struct Solver {
   bool path_integration() {
     if (!sweep_ready) sweeping_order();
     std::fill(fluxes.begin(), fluxes.end(), (R)0);
-    std::vector<R> gridrad(npts, (R)-1);
-    radiance.assign((size_t)npts * nlm, 0);
-    std::vector<R> work((size_t)npts * nphi0max, 0);
+    std::vector<R> gridrad((size_t)npts * nst, (R)0);
+    for (int i = 0; i < npts; ++i) gridrad[(size_t)i * nst] = -1;
+    radiance.assign((size_t)npts * nlm * nst, 0);
+    std::vector<R> work((size_t)npts * nphi0max * nst, 0);
+    auto W = [&](int i, int k, int s) -> R & { return work[((size_t)i * nphi0max + k) * nst + s]; };
     for (int imu = 0; imu < nmu; ++imu) {
       if (imu == nmu / 2) lambertian_boundary();
-      sh_to_do(imu, work);
+      if (nst == 3) sh_to_do_pol(imu, work); else sh_to_do(imu, work);
+      // the discrete-ordinate I source is made non-negative
       for (int i = 0; i < npts; ++i)
-        for (int k = 0; k < nphi0[imu]; ++k) work[(size_t)i * nphi0max + k] = std::max((R)0, work[(size_t)i * nphi0max + k]);
+        for (int k = 0; k < nphi0[imu]; ++k) W(i, k, 0) = std::max((R)0, W(i, k, 0));
       for (int iphi = 0; iphi < nphi0[imu]; ++iphi) {
         int iupdown;
+        // boundary radiances: unpolarized (Q = U = 0) sky and Lambertian surface
         if (mu[imu] < 0) {
           iupdown = 0;
-          for (int t : topp) gridrad[t] = (R)p.skyrad;
+          for (int t : topp) { gridrad[(size_t)t * nst] = (R)p.skyrad; for (int s = 1; s < nst; ++s) gridrad[(size_t)t * nst + s] = 0; }
         } else {
           iupdown = 1;
-          for (size_t b = 0; b < botp.size(); ++b) gridrad[botp[b]] = bcrad_bot[b];
+          for (size_t b = 0; b < botp.size(); ++b) {
+            gridrad[(size_t)botp[b] * nst] = bcrad_bot[b];
+            for (int s = 1; s < nst; ++s) gridrad[(size_t)botp[b] * nst + s] = 0;
+          }
         }
         bool ok;
         if ((ipflag & 2) && (ipflag & 1)) ok = back_int_grid1d(mu[imu], iphi, work, gridrad);
         else ok = back_int_grid3d(mu[imu], phi[(size_t)imu * nphi0max + iphi], iphi, work, gridrad);
         if (!ok) return false;
         for (int i = 0; i < npts; ++i) {
-          if (gridrad[i] < (R)-0.0001) { err = "PATH_INTEGRATION: Grid point has no value"; return false; }
-          work[(size_t)i * nphi0max + iphi] = gridrad[i];
-          gridrad[i] = -1;
+          if (gridrad[(size_t)i * nst] < (R)-0.0001) { err = "PATH_INTEGRATION: Grid point has no value"; return false; }
+          for (int s = 0; s < nst; ++s) W(i, iphi, s) = gridrad[(size_t)i * nst + s];
+          gridrad[(size_t)i * nst] = -1;
         }
         R a = std::fabs((R)mu[imu]) * (R)wtdo[(size_t)imu * nphi0max + iphi];
-        for (int i = 0; i < npts; ++i) fluxes[2 * (size_t)i + iupdown] += a * work[(size_t)i * nphi0max + iphi];
+        for (int i = 0; i < npts; ++i) fluxes[2 * (size_t)i + iupdown] += a * W(i, iphi, 0);
       }
-      do_to_sh(imu, work);
+      if (nst == 3) do_to_sh_pol(imu, work); else do_to_sh(imu, work);
     }
     return true;
   }
@@ -1256,7 +1545,7 @@ struct Solver {
       for (int i = 0; i < npts; ++i) {
         int is = shptr[i], ns = shptr[i + 1] - is, isd = oshptr[i], nsd = oshptr[i + 1] - isd;
         int nsc = std::min(ns, nsd);
-        for (int j = 0; j < nsc; ++j) source[(size_t)is + j] += accelpar * delsource[(size_t)isd + j];
+        for (int t = 0; t < nsc * nst; ++t) source[(size_t)is * nst + t] += accelpar * delsource[(size_t)isd * nst + t];
       }
     }
   }
@@ -1284,11 +1573,14 @@ struct Solver {
   // PRECOMPUTE_PHASE_CHECK (src/polarized/shdomsub4.f:2388-2491) on the
   // unscaled table (at3d/solver.py:2800-2825).
   int nscatangle = 0;
-  std::vector<R> phasetab;  // [nscatangle][numphase]
+  std::vector<R> phasetab;   // [nscatangle][numphase]
+  std::vector<R> phasetab2;  // [nscatangle][numphase] I-Q element (nst = 3)
   bool precompute_phase() {
     int nlegp = std::max(p.nlegp, nleg);
     nscatangle = std::max(36, std::min(721, 2 * nlegp));
     phasetab.assign((size_t)nscatangle * numphase, 0);
+    if (nst == 3) phasetab2.assign((size_t)nscatangle * numphase, 0);
+    std::vector<double> d2;
     const double pi = std::acos(-1.0), ofourpi = 1.0 / (4.0 * pi);
     std::vector<double> d;
     for (int j = 0; j < nscatangle; ++j) {
@@ -1301,12 +1593,23 @@ struct Solver {
       for (int iph = 0; iph < numphase; ++iph) {
         double a1 = 0.0;
         for (int l = 0; l <= nlegp; ++l) {
-          float lg = (l <= p.nlegp) ? legp[(size_t)iph * (p.nlegp + 1) + l] : 0.f;
+          float lg = (l <= p.nlegp) ? leg_in(iph, l, 0) : 0.f;
           double unsc = (double)(float)(lg / (float)(2 * l + 1));
           a1 += (2.0 * l + 1.0) * unsc * d[l];
         }
         if (a1 <= 0.0) { err = "PRECOMPUTE_PHASE_CHECK: negative phase function"; return false; }
         phasetab[(size_t)j * numphase + iph] = (R)(a1 * ofourpi);
+        if (nst == 3) {
+          // B1 = -sum (2l+1) b1_l d^l_{20}(cos theta)
+          if (iph == 0) wigner_d(x, nlegp, 2, 0, d2);
+          double b1 = 0.0;
+          for (int l = 0; l <= nlegp; ++l) {
+            float lg = (l <= p.nlegp) ? leg_in(iph, l, 4) : 0.f;
+            double unsc = (double)(float)(lg / (float)(2 * l + 1));
+            b1 -= (2.0 * l + 1.0) * unsc * d2[l];
+          }
+          phasetab2[(size_t)j * numphase + iph] = (R)(b1 * ofourpi);
+        }
       }
     }
     return true;
@@ -1360,14 +1663,26 @@ struct Solver {
   }
 
   // INTEGRATE_1RAY + COMPUTE_SOURCE_1CELL_UNPOL + FIND_BOUNDARY_RADIANCE
-  // (src/polarized/shdomsub2.f:2311-2863, :3046-3192).
-  bool integrate_1ray(double mu2, double phi2, double x0, double y0, double z0, double &radout,
+  // (src/polarized/shdomsub2.f:2311-2863, :3046-3192); with nst = 3 the
+  // polarized COMPUTE_SOURCE_1CELL (src/polarized/shdomsub2.f:2868-3042) and
+  // ROTATE_POL_PLANE (src/polarized/shdomsub2.f:3277-3316).  radout[nst].
+  bool integrate_1ray(double mu2, double phi2, double x0, double y0, double z0, double *radout,
                       std::string &err) const {
     const double pi = std::acos(-1.0);
     double eps = 1.0e-5 * (gridpos[3 * gridptr[7] + 2] - gridpos[3 * gridptr[0] + 2]);
     int maxcellscross = 500 * std::max(nx, std::max(ny, nz));
-    std::vector<R> ylmdir = ylmall((double)(float)mu2, (float)phi2);
-    std::vector<R> singscat(numphase, 0);
+    std::vector<R> ylmdir, y6;  // y6 [nlm][6] generalized functions when nst = 3
+    if (nst == 3) {
+      std::vector<double> yd;
+      genylm6(false, (double)(float)mu2, (double)(float)phi2, true, ml, mm, yd);
+      y6.assign(yd.size(), 0);
+      for (size_t q = 0; q < yd.size(); ++q) y6[q] = (R)yd[q];
+      ylmdir.resize(nlm);
+      for (int j = 0; j < nlm; ++j) ylmdir[j] = y6[(size_t)j * 6];
+    } else {
+      ylmdir = ylmall((double)(float)mu2, (float)phi2);
+    }
+    std::vector<R> singscat((size_t)numphase * nst, 0);  // [numphase][nst]
     bool tms = p.deltam;
     if (tms) {
       double cosscat = (double)p.solarmu * mu2 +
@@ -1376,8 +1691,24 @@ struct Solver {
       float F = (float)((nscatangle - 1) * (std::acos(cosscat) / pi) + 1);
       int J = std::min(nscatangle - 1, (int)F);
       F = F - J;
-      for (int i = 0; i < numphase; ++i)
-        singscat[i] = (R)((1 - F) * phasetab[(size_t)(J - 1) * numphase + i] + F * phasetab[(size_t)J * numphase + i]);
+      for (int i = 0; i < numphase; ++i) {
+        singscat[(size_t)i * nst] = (R)((1 - F) * phasetab[(size_t)(J - 1) * numphase + i] + F * phasetab[(size_t)J * numphase + i]);
+        if (nst == 3) {
+          // I-Q element, then the polarization plane turned from the
+          // scattering plane to the outgoing meridional plane
+          const float b1 = (float)((1 - F) * phasetab2[(size_t)(J - 1) * numphase + i] + F * phasetab2[(size_t)J * numphase + i]);
+          const float smu = p.solarmu, mu2f = (float)mu2, dphi = p.solaraz - (float)phi2;
+          const double sin_scat = std::sqrt(std::max(0.0, 1.0 - cosscat * cosscat));
+          const double st1 = std::sqrt(1.0 - (double)(smu * smu)), st2 = std::sqrt(1.0 - (double)(mu2f * mu2f));
+          const double sp = std::sin((double)dphi), cp = std::cos((double)dphi);
+          double sin2, cos2;
+          if (sin_scat == 0.0) { sin2 = 0.0; cos2 = -1.0; }
+          else { sin2 = st1 * sp / sin_scat; cos2 = (st2 * smu - st1 * mu2f * cp) / sin_scat; }
+          const double sin22 = 2.0 * sin2 * cos2, cos22 = 1.0 - 2.0 * sin2 * sin2;
+          singscat[(size_t)i * 3 + 1] = (R)(float)(b1 * cos22);
+          singscat[(size_t)i * 3 + 2] = (R)(float)(b1 * sin22);
+        }
+      }
     }
     double cx = std::sqrt(1.0 - mu2 * mu2) * std::cos(phi2 - pi), cy = std::sqrt(1.0 - mu2 * mu2) * std::sin(phi2 - pi);
     double cz = -mu2, cxinv, cyinv, czinv;
@@ -1390,11 +1721,11 @@ struct Solver {
     double xe = x0, ye = y0, ze = z0;
     int icell = locate_grid_cell(xe, ye, ze);
     int iface = -1, ngrid = 0;
-    double transmit = 1.0, radiance_acc = 0.0;
-    R extinct8[8] = {0, 0, 0, 0, 0, 0, 0, 0}, srcext8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    double transmit = 1.0, radiance_acc[3] = {0.0, 0.0, 0.0};
+    R extinct8[8] = {0, 0, 0, 0, 0, 0, 0, 0}, srcext8[3][8] = {{0}};
     int oldipts[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
     bool validrad = false;
-    double ext1 = 0, srcext1 = 0;
+    double ext1 = 0, srcext1[3] = {0, 0, 0};
     const R secmu0 = (R)1 / std::fabs((R)p.solarmu);
     std::vector<R> lt; R fdum;
     // DONEFACE(8,7): which corner of the previous cell is reused (1-based, 0 none)
@@ -1403,15 +1734,26 @@ struct Solver {
                                        {5, 6, 7, 8, 0, 0, 0, 0}};
     while (!validrad && icell >= 0) {
       ++ngrid;
-      R oext8[8], osrc8[8];
-      for (int i = 0; i < 8; ++i) { oext8[i] = extinct8[i]; osrc8[i] = srcext8[i]; }
+      R oext8[8], osrc8[3][8];
+      for (int i = 0; i < 8; ++i) { oext8[i] = extinct8[i]; for (int k = 0; k < 3; ++k) osrc8[k][i] = srcext8[k][i]; }
       for (int n = 0; n < 8; ++n) {
         int ip = gridptr[8 * icell + n];
         int I = doneface[iface + 1][n];
-        if (I > 0 && ip == oldipts[n]) { extinct8[n] = oext8[I - 1]; srcext8[n] = osrc8[I - 1]; continue; }
+        if (I > 0 && ip == oldipts[n]) {
+          extinct8[n] = oext8[I - 1];
+          for (int k = 0; k < nst; ++k) srcext8[k][n] = osrc8[k][I - 1];
+          continue;
+        }
         R ext = total_ext[ip];
         oldipts[n] = ip;
         int is = shptr[ip], ns = shptr[ip + 1] - is;
+        if (nst == 3) {
+          R sv[3];
+          source_1cell_pol(ip, ns, is, ext, y6, singscat, secmu0, sv);
+          for (int k = 0; k < 3; ++k) srcext8[k][n] = sv[k] * ext;
+          extinct8[n] = ext;
+          continue;
+        }
         R s = 0;
         for (int j = 0; j < ns; ++j) s += source[(size_t)is + j] * ylmdir[j];
         if (tms) {
@@ -1439,7 +1781,7 @@ struct Solver {
               }
           }
         }
-        srcext8[n] = s * ext;
+        srcext8[0][n] = s * ext;
         extinct8[n] = ext;
       }
       int ipt1 = gridptr[8 * icell], ipt2 = gridptr[8 * icell + 7];
@@ -1452,7 +1794,8 @@ struct Solver {
       };
       double u = (xe - gridpos[3 * ipt1]) * invdelx, v = (ye - gridpos[3 * ipt1 + 1]) * invdely,
              w = (ze - gridpos[3 * ipt1 + 2]) * invdelz;
-      srcext1 = std::max((R)0, interp(srcext8, u, v, w));
+      for (int k = 0; k < nst; ++k) srcext1[k] = interp(srcext8[k], u, v, w);
+      srcext1[0] = std::max(0.0, srcext1[0]);
       ext1 = interp(extinct8, u, v, w);
       bool ipinx = (cellflags[icell] & 1) && !((bcflag & 1) && ((cx > 0 && xe < xm) || (cx < 0 && xe > xm)));
       bool ipiny = (cellflags[icell] & 2) && !((bcflag & 2) && ((cy > 0 && ye < ym) || (cy < 0 && ye > ym)));
@@ -1473,17 +1816,24 @@ struct Solver {
         double xi = xe + s * cx, yi = ye + s * cy, zi = ze + s * cz;
         u = (xi - gridpos[3 * ipt1]) * invdelx; v = (yi - gridpos[3 * ipt1 + 1]) * invdely; w = (zi - gridpos[3 * ipt1 + 2]) * invdelz;
         R ext0 = interp(extinct8, u, v, w);
-        R srcext0 = std::max((R)0, interp(srcext8, u, v, w));
-        double ext = 0.5 * (ext0 + ext1), tau, abscell, transcell, src;
+        R srcext0[3];
+        for (int k = 0; k < nst; ++k) srcext0[k] = interp(srcext8[k], u, v, w);
+        srcext0[0] = std::max((R)0, srcext0[0]);
+        double ext = 0.5 * (ext0 + ext1), tau, abscell, transcell;
         if (ext != 0.0) {
           tau = ext * dels;
           abscell = tau * (1.0 - 0.5 * tau * (1.0 - 0.33333333333 * tau));
           transcell = 1.0 - abscell;
-          src = (0.5 * (srcext0 + srcext1) + 0.08333333333 * (ext0 * srcext1 - ext1 * srcext0) * dels * (1.0 - 0.05 * (ext1 - ext0) * dels)) / ext;
-        } else { abscell = 0; transcell = 1; src = 0; }
-        radiance_acc += transmit * src * abscell;
+        } else { abscell = 0; transcell = 1; }
+        for (int k = 0; k < nst; ++k) {
+          double src = 0.0;
+          if (ext != 0.0)
+            src = (0.5 * (srcext0[k] + srcext1[k]) + 0.08333333333 * (ext0 * srcext1[k] - ext1 * srcext0[k]) * dels * (1.0 - 0.05 * (ext1 - ext0) * dels)) / ext;
+          radiance_acc[k] += transmit * src * abscell;
+          srcext1[k] = srcext0[k];
+        }
         transmit *= transcell;
-        ext1 = ext0; srcext1 = srcext0;
+        ext1 = ext0;
       }
       int jface; bool openbcface;
       if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; openbcface = (cellflags[icell] & 1) && (bcflag & 1); }
@@ -1518,14 +1868,62 @@ struct Solver {
         float uu = (xs[1] - xs[0] > 0) ? (float)((xn - xs[0]) / (xs[1] - xs[0])) : 0.f;
         float vv = (ys[2] - ys[0] > 0) ? (float)((yn - ys[0]) / (ys[2] - ys[0])) : 0.f;
         float radbnd = (1 - uu) * (1 - vv) * (float)rb[0] + uu * (1 - vv) * (float)rb[1] + (1 - uu) * vv * (float)rb[2] + uu * vv * (float)rb[3];
-        radiance_acc += transmit * radbnd;
+        radiance_acc[0] += transmit * radbnd;  // the boundaries emit unpolarized radiance
       } else {
         icell = inext;
       }
       xe = xn; ye = yn; ze = zn;
     }
-    radout = radiance_acc;
+    for (int k = 0; k < nst; ++k) radout[k] = radiance_acc[k];
     return true;
+  }
+
+  // Polarized COMPUTE_SOURCE_1CELL at one grid point (src/polarized/
+  // shdomsub2.f:2868-3042): the Stokes source in the ray direction from the
+  // generalized SH series, with the TMS single-scatter correction.
+  void source_1cell_pol(int ip, int ns, int is, R ext, const std::vector<R> &y6, const std::vector<R> &singscat,
+                        R secmu0, R *sv) const {
+    sv[0] = sv[1] = sv[2] = 0;
+    const R *S = &source[(size_t)is * 3];
+    for (int j = 0; j < ns; ++j) sv[0] += S[3 * j] * y6[(size_t)j * 6];
+    for (int j = 0; j < ns; ++j) {
+      sv[1] += S[3 * j + 1] * y6[(size_t)j * 6 + 1] + S[3 * j + 2] * y6[(size_t)j * 6 + 4];
+      sv[2] += S[3 * j + 1] * y6[(size_t)j * 6 + 5] + S[3 * j + 2] * y6[(size_t)j * 6 + 2];
+    }
+    if (!p.deltam) return;
+    const int n1 = nleg + 1;
+    std::vector<R> lt;
+    for (int ipa = 0; ipa < npart; ++ipa) {
+      R w = (ext == 0) ? (R)1 : extinct[(size_t)ipa * npts + ip] / ext;
+      if (w == 0) continue;
+      R f;
+      point_legen6(ip, ipa, lt, f);
+      const R da = albedo[(size_t)ipa * npts + ip] * dirflux[ip] * secmu0 * w;
+      int J = 0;
+      for (int l = 0; l <= ml; ++l) {
+        const int me = std::min(l, mm);
+        const R a1 = da * lt[l], b1 = da * lt[(size_t)4 * n1 + l];
+        if (J < ns) {
+          const int jt = J;
+          for (int m = -me; m <= me; ++m, ++J) sv[0] = sv[0] - a1 * y6[(size_t)J * 6] * ylmsun[J];
+          J = jt;
+          for (int m = -me; m <= me; ++m, ++J) {
+            sv[1] = sv[1] - b1 * y6[(size_t)J * 6 + 1] * ylmsun[J];
+            sv[2] = sv[2] - b1 * y6[(size_t)J * 6 + 5] * ylmsun[J];
+          }
+        }
+      }
+      const int *IPH = &iphase[((size_t)ipa * npts + ip) * nq];
+      const R *PW = &phaseinterpwt[((size_t)ipa * npts + ip) * nq];
+      if (PW[0] >= phasemax) {
+        for (int k = 0; k < 3; ++k) sv[k] = sv[k] + da * singscat[(size_t)(IPH[0] - 1) * 3 + k] / ((R)1 - f);
+      } else {
+        for (int q = 0; q < nq; ++q) {
+          if (PW[q] <= (R)1e-5) continue;
+          for (int k = 0; k < 3; ++k) sv[k] = sv[k] + da * singscat[(size_t)(IPH[q] - 1) * 3 + k] * PW[q] / ((R)1 - f);
+        }
+      }
+    }
   }
 
   // RENDER (src/polarized/shdomsub4.f:93-286), scalar, solar.
@@ -1542,15 +1940,15 @@ struct Solver {
         double x0 = camx[iv], y0 = camy[iv], z0 = camz[iv], mu2 = cammu[iv], phi2 = camphi[iv];
         double muray = -mu2, phiray = phi2 - pi;
         if (z0 > S.zgrid[nz - 1]) {
-          if (muray >= 0.0) { out[iv] = 0.f; continue; }
+          if (muray >= 0.0) { for (int k = 0; k < S.nst; ++k) out[(size_t)iv * S.nst + k] = 0.f; continue; }
           double r = (S.zgrid[nz - 1] - z0) / muray;
           x0 = x0 + r * std::sqrt(1 - muray * muray) * std::cos(phiray);
           y0 = y0 + r * std::sqrt(1 - muray * muray) * std::sin(phiray);
           z0 = S.zgrid[nz - 1];
         } else if (z0 < S.zgrid[0]) { bad[t] = 1; errs[t] = "RENDER: Level below domain"; return; }
-        double rad;
+        double rad[3];
         if (!S.integrate_1ray(mu2, phi2, x0, y0, z0, rad, errs[t])) { bad[t] = 1; return; }
-        out[iv] = (float)rad;
+        for (int k = 0; k < S.nst; ++k) out[(size_t)iv * S.nst + k] = (float)rad[k];
       }
     };
     if (nthreads <= 1) work(0, 0, n);
@@ -2141,6 +2539,7 @@ bool frozen_render(Solver<R> &S, int ipa, int voxel, float dext, float dalb, int
                    int nthreads) {
   const int ng = S.p.npx * S.p.npy * S.p.npz;
   if (ipa < 0 || ipa >= S.npart || voxel < 0 || voxel >= ng) { S.err = "frozen_render: bad index"; return false; }
+  if (S.nst != 1) { S.err = "frozen_render: scalar problems only"; return false; }
   auto extp = S.extp, albp = S.albp;
   auto source = S.source;
   auto shptr = S.shptr;
@@ -2168,6 +2567,7 @@ bool levis_gradient(Solver<R> &S, int ipa, int n, const float *camx, const float
                     const double *cammu, const double *camphi, const float *meas, double *gradout, double *cost,
                     float *stokesout, int nthreads) {
   if (ipa < 0 || ipa >= S.npart) { S.err = "levis_gradient: bad species index"; return false; }
+  if (S.nst != 1) { S.err = "levis_gradient: scalar problems only"; return false; }
   if (!S.render(n, camx, camy, camz, cammu, camphi, stokesout, nthreads)) return false;  // phase 1 (with phasetab, bcrad)
   Levis<R> L(S);
   if (!L.prepare(ipa, S.err)) return false;
@@ -2254,7 +2654,7 @@ int oracle_sizes(void *hv, int *out) {
   auto fill = [&](auto *s) {
     out[0] = s->npts; out[1] = s->nlm; out[2] = s->nmu; out[3] = s->nang; out[4] = s->ncells;
     out[5] = s->nx1; out[6] = s->ny1; out[7] = s->nz; out[8] = s->bcflag; out[9] = s->ipflag;
-    out[10] = s->iter; out[11] = s->ml; out[12] = s->mm;
+    out[10] = s->iter; out[11] = s->ml; out[12] = s->mm; out[13] = s->nst;
   };
   if (h->fp64) fill(h->s64); else fill(h->s32);
   return 0;
@@ -2276,7 +2676,7 @@ int oracle_init_solution(void *hv) {
   return h->fp64 ? !h->s64->init_solution() : !h->s32->init_solution();
 }
 
-// Exports the solution densely: source/radiance [npts][nlm] (zero beyond
+// Exports the solution densely: source/radiance [npts][nstokes][nlm] (zero beyond
 // the per-point truncation), ns/nr per point, fluxes [npts][2], dirflux.
 int oracle_export(void *hv, float *source, int *ns, float *radiance, int *nr, float *fluxes, float *dirflux) {
   Handle *h = (Handle *)hv;
@@ -2285,10 +2685,17 @@ int oracle_export(void *hv, float *source, int *ns, float *radiance, int *nr, fl
     for (int i = 0; i < n; ++i) {
       int is = s->shptr[i], k = s->shptr[i + 1] - is;
       if (ns) ns[i] = k;
-      if (source) for (int j = 0; j < L; ++j) source[(size_t)i * L + j] = j < k ? (float)s->source[(size_t)is + j] : 0.f;
+      const int ns_ = s->nst;
+      if (source)
+        for (int q = 0; q < ns_; ++q)
+          for (int j = 0; j < L; ++j)
+            source[((size_t)i * ns_ + q) * L + j] = j < k ? (float)s->source[((size_t)is + j) * ns_ + q] : 0.f;
       int ir = s->rshptr[i], kr = s->rshptr[i + 1] - ir;
       if (nr) nr[i] = kr;
-      if (radiance) for (int j = 0; j < L; ++j) radiance[(size_t)i * L + j] = j < kr ? (float)s->radiance[(size_t)ir + j] : 0.f;
+      if (radiance)
+        for (int q = 0; q < ns_; ++q)
+          for (int j = 0; j < L; ++j)
+            radiance[((size_t)i * ns_ + q) * L + j] = j < kr ? (float)s->radiance[((size_t)ir + j) * ns_ + q] : 0.f;
       if (fluxes) { fluxes[2 * i] = (float)s->fluxes[2 * (size_t)i]; fluxes[2 * i + 1] = (float)s->fluxes[2 * (size_t)i + 1]; }
       if (dirflux) dirflux[i] = (float)s->dirflux[i];
     }
