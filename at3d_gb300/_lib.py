@@ -19,7 +19,7 @@ class ShdomSizes(C.Structure):
                 ("nlm", C.c_int), ("nmu", C.c_int), ("nang", C.c_int), ("ml", C.c_int), ("mm", C.c_int),
                 ("bcflag", C.c_int), ("ipflag", C.c_int), ("iters", C.c_int), ("nlevels_down", C.c_int),
                 ("nlevels_up", C.c_int), ("solcrit", C.c_float), ("albmax", C.c_float),
-                ("launches", C.c_longlong), ("device_bytes", C.c_longlong)]
+                ("launches", C.c_longlong), ("device_bytes", C.c_longlong), ("nstokes", C.c_int)]
 
 
 # name -> (restype, argtypes): the exported surface of include/shdom_gb300.h

@@ -223,6 +223,7 @@ struct SweepArgs {
   const uint8_t *regular;
   const float *geo;
   const IrrRec *irr;               // stored single-cell general traces of this hemisphere
+  const uint8_t *stk;              // polarized: Stokes component per column (null: all I)
   int *err;
   int npts, nang, ldo, is1d, nz, ny1;
   float transmin;
@@ -252,6 +253,7 @@ struct RegLoad {
   float4 g;
   float e1, s1, e[4], s[4], r[4];
   int pt, col;
+  bool clamp;  // the column holds I (its cell source is kept non-negative)
 };
 
 __device__ __forceinline__ void reg_load(const SweepArgs &a, int b, int pt, int col, RegLoad &x, bool upstream) {
@@ -259,6 +261,7 @@ __device__ __forceinline__ void reg_load(const SweepArgs &a, int b, int pt, int 
   const int iz = pt % a.nz;
   const int layer = (b & 4) ? iz - 1 : iz;
   x.pt = pt; x.col = col;
+  x.clamp = !a.stk || !a.stk[col];
   x.g = __ldg(reinterpret_cast<const float4 *>(a.geo) + (size_t)layer * a.nang + col);
   const int iface = (int)x.g.w;
   const int ox = (b & 1) ? -a.nz * a.ny1 : a.nz * a.ny1, oy = (b & 2) ? -a.nz : a.nz, oz = (b & 4) ? -1 : 1;
@@ -279,6 +282,7 @@ __device__ __forceinline__ void rec_load(const SweepArgs &a, const IrrRec &rec, 
                                          bool upstream) {
   const int ldo = a.ldo;
   x.pt = pt; x.col = col;
+  x.clamp = !a.stk || !a.stk[col];
   x.g = rec.g;
   const int q[4] = {rec.q.x, rec.q.y, rec.q.z, rec.q.w};
 #pragma unroll
@@ -294,7 +298,7 @@ __device__ __forceinline__ void rec_load(const SweepArgs &a, const IrrRec &rec, 
 // Source integral over one cell (the reference's linear-in-tau source
 // approximation, with the large-tau limiting form).
 __device__ __forceinline__ void cell_source(float ext0, float srcext0, float ext1, float srcext1, float so,
-                                            float &radsrc, float &transcell) {
+                                            float &radsrc, float &transcell, bool clamp = true) {
   const float ext = 0.5f * (ext0 + ext1), tau = ext * so;
   float abscell, src;
   if (tau >= 0.5f) { transcell = __expf(-tau); abscell = 1.f - transcell; }
@@ -310,7 +314,7 @@ __device__ __forceinline__ void cell_source(float ext0, float srcext0, float ext
     src = 1.f / (ext0p + ext1) *
           (srcext0p + srcext1 + (ext0p * srcext1 - ext1 * srcext0p) * 2.f / (ext0p + ext1) * (1.f - 2.f / tau + 2.f * transcell / abscell));
   }
-  src = fmaxf(src, 0.f);
+  if (clamp) src = fmaxf(src, 0.f);  // the I source only; Q and U keep their sign
   radsrc = src * abscell;
 }
 
@@ -325,7 +329,7 @@ __device__ __forceinline__ Trace reg_trace(const RegLoad &x, int b, int pt_unuse
     ext0 += t.f[k] * x.e[k];
     srcext0 += t.f[k] * x.s[k] * x.e[k];
   }
-  cell_source(ext0, srcext0, x.e1, x.e1 * x.s1, x.g.x, t.radsrc, t.tr);
+  cell_source(ext0, srcext0, x.e1, x.e1 * x.s1, x.g.x, t.radsrc, t.tr, x.clamp);
   t.status = ERR_NONE;
   return t;
 }
@@ -437,6 +441,7 @@ __device__ __forceinline__ Trace trace_general(const SweepArgs &a, int b, int cl
   float ext1 = a.text[pt];
   float srcext1 = ext1 * a.srcdo[(size_t)pt * ldo + col];
   float rad = 0.f, tr = 1.f;
+  const bool clamp = !a.stk || !a.stk[col];
   for (int guard = 0; guard < 65536; ++guard) {
     if (cell < 0) break;
     const int *g = a.gridptr + 8 * (size_t)cell;
@@ -463,7 +468,7 @@ __device__ __forceinline__ Trace trace_general(const SweepArgs &a, int b, int cl
     const float srcext0 = f1 * a.srcdo[(size_t)i1 * ldo + col] * e1 + f2 * a.srcdo[(size_t)i2 * ldo + col] * e2 +
                           f3 * a.srcdo[(size_t)i3 * ldo + col] * e3 + f4 * a.srcdo[(size_t)i4 * ldo + col] * e4;
     float radsrc, transcell;
-    cell_source(ext0, srcext0, ext1, srcext1, so, radsrc, transcell);
+    cell_source(ext0, srcext0, ext1, srcext1, so, radsrc, transcell, clamp);
     rad += tr * radsrc;
     tr *= transcell;
     auto ok = [&](int q) { return (a.bnd[q] & hb) || (rk[q] < rP && (!use_level || lv[q] < lP)); };
@@ -845,15 +850,18 @@ __global__ void __launch_bounds__(256) k_do_to_sh_light(const float *__restrict_
   }
 }
 
-__global__ void k_preset_top(const int *topp, int ntop, float *raddo, int ldo, int ncol_down, float skyrad) {
+// stk (polarized): Stokes component per column; the sky and the surface
+// emit unpolarized radiance, so the Q and U columns are preset to zero.
+__global__ void k_preset_top(const int *topp, int ntop, float *raddo, int ldo, int ncol_down, float skyrad,
+                             const uint8_t *stk) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntop * ncol_down) return;
   int k = t / ncol_down, c = t - k * ncol_down;
-  raddo[(size_t)topp[k] * ldo + c] = skyrad;
+  raddo[(size_t)topp[k] * ldo + c] = (stk && stk[c]) ? 0.f : skyrad;
 }
 
 __global__ void k_lambertian(const int *botp, int nbot, const float *botalb, const float *dirflux, const float *fluxw,
-                             float *raddo, int nang, int ldo, int ncol_down, float *bcrad) {
+                             float *raddo, int nang, int ldo, int ncol_down, float *bcrad, const uint8_t *stk) {
   int k = blockIdx.x;
   if (k >= nbot) return;
   int p = botp[k];
@@ -869,12 +877,84 @@ __global__ void k_lambertian(const int *botp, int nbot, const float *botalb, con
   const float opi = 0.318309886f;
   float b = opi * botalb[k] * (dirflux[p] + red[0]);
   if (threadIdx.x == 0) bcrad[k] = b;
-  for (int c = ncol_down + threadIdx.x; c < nang; c += blockDim.x) raddo[(size_t)p * ldo + c] = b;
+  for (int c = ncol_down + threadIdx.x; c < nang; c += blockDim.x) raddo[(size_t)p * ldo + c] = (stk && stk[c]) ? 0.f : b;
+}
+
+// Polarized transforms on the CUDA cores (the FP32 path): C[M][N] = A[M][K]
+// (row stride lda) x B[K][N], 64 x 64 tiles, 4 x 4 outputs per thread, K in
+// steps of 16 through shared memory.  mode 0 writes the ordinate sources
+// (I clamped at zero, Q and U kept); mode 1 writes the harmonic radiance
+// rows masked to the radiance truncation ((col mod nlm) < nr).
+__global__ void __launch_bounds__(256) k_dense_xf(const float *__restrict__ A, int lda, const float *__restrict__ B,
+                                                  int K, int N, int M, int mode, float *__restrict__ C, int ldc,
+                                                  const uint8_t *__restrict__ stk, const int *__restrict__ nr, int nlm) {
+  __shared__ float As[16][65];
+  __shared__ float Bs[16][64];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int row0 = blockIdx.y * 64, col0 = blockIdx.x * 64;
+  float acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    for (int t = threadIdx.x; t < 64 * 16; t += 256) {
+      const int r = t >> 4, kk = t & 15, gr = row0 + r, gk = k0 + kk;
+      As[kk][r] = (gr < M && gk < K) ? A[(size_t)gr * lda + gk] : 0.f;
+    }
+    for (int t = threadIdx.x; t < 16 * 64; t += 256) {
+      const int kk = t >> 6, c = t & 63, gk = k0 + kk, gc = col0 + c;
+      Bs[kk][c] = (gk < K && gc < N) ? B[(size_t)gk * N + gc] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      float a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) { a[i] = As[kk][ty * 4 + i]; b[i] = Bs[kk][tx * 4 + i]; }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int row = row0 + ty * 4 + i;
+    if (row >= M) continue;
+    const int nrp = mode == 1 ? nr[row] : 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int col = col0 + tx * 4 + j;
+      if (col >= N) continue;
+      float v = acc[i][j];
+      if (mode == 0) { if (!stk[col]) v = fmaxf(v, 0.f); }
+      else if (col % nlm >= nrp) v = 0.f;
+      C[(size_t)row * ldc + col] = v;
+    }
+  }
+}
+
+// Hemispheric fluxes of every point from its ordinate radiances (one warp per point).
+__global__ void __launch_bounds__(256) k_do_fluxes(const float *__restrict__ raddo, int ldo, int nang, int ncol_down,
+                                                   const float *__restrict__ fluxw, int npts, float *__restrict__ fluxes) {
+  const int lane = threadIdx.x & 31;
+  for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < npts; p += (gridDim.x * blockDim.x) >> 5) {
+    float fd = 0.f, fu = 0.f;
+    for (int c = lane; c < nang; c += 32) {
+      const float v = fluxw[c] * raddo[(size_t)p * ldo + c];
+      if (c < ncol_down) fd += v; else fu += v;
+    }
+    for (int o = 16; o > 0; o >>= 1) { fd += __shfl_xor_sync(0xffffffffu, fd, o); fu += __shfl_xor_sync(0xffffffffu, fu, o); }
+    if (lane == 0) { fluxes[2 * (size_t)p] = fd; fluxes[2 * (size_t)p + 1] = fu; }
+  }
 }
 
 // ---------------------------------------------------------------- source
 struct SourceArgs {
   const float *coef;      // [npts][nl]
+  const float *coefp;     // polarized: [npts][3][nl] a2, a3, b1 times the albedo
   const float *dirflux, *radiance, *ylmsun;
   const int *lofj;
   float *source, *delsource;
@@ -1027,6 +1107,109 @@ __global__ void __launch_bounds__(256) k_source(SourceArgs a) {
   }
 }
 
+// Polarized COMPUTE_SOURCE: CALC_SOURCE_PNT (src/polarized/shdomsub1.f:
+// 823-909) per point, one warp per point, rows [I][Q][U] of nlm terms:
+//   S_I = c1 (f0 Ysun + R_I) + cb1 R_Q,  S_Q = cb1 (R_I + f0 Ysun) + ca2 R_Q,
+//   S_U = ca3 R_U  (Q and U from the term j = 4 on, that is l >= 2),
+// the series-acceleration sums over all three Stokes rows, the truncation
+// at the last term where any Stokes component exceeds SHACC, and the next
+// radiance truncation from the I row as in the scalar kernel.
+__global__ void __launch_bounds__(256) k_source_pol(SourceArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int nlm = a.nlm, nl = a.nl;
+  double djdot = 0, djold = 0, djnew = 0, jn = 0;
+  for (int p = warp; p < a.npts; p += nwarps) {
+    const float *c1 = a.coef + (size_t)p * nl, *cp = a.coefp + (size_t)p * 3 * nl;
+    const float f0 = a.dirflux[p] * a.secmu0;
+    const int nrp = a.nr[p], nsold = a.ns[p], nsoold = a.nso[p], nsmin = min(nsold, nsoold);
+    float *S = a.source + (size_t)p * 3 * nlm;
+    float *D = a.delsource + (size_t)p * 3 * nlm;
+    const float *R = a.radiance + (size_t)p * 3 * nlm;
+    int jlast = 0;
+    float pdot = 0.f, pold = 0.f, pnew = 0.f, pn = 0.f;
+    for (int j0 = 0; j0 < nlm; j0 += 32) {
+      const int j = j0 + lane;
+      float jt[3] = {0.f, 0.f, 0.f};
+      if (j < nlm) {
+        const int l = a.lofj[j];
+        const float ri = j < nrp ? R[j] : 0.f, rq = j < nrp ? R[nlm + j] : 0.f, ru = j < nrp ? R[2 * nlm + j] : 0.f;
+        const float ys = f0 * a.ylmsun[j], ca = c1[l], ca2 = cp[l], ca3 = cp[nl + l], cb1 = cp[2 * nl + l];
+        jt[0] = ca * ys + ca * ri + cb1 * rq;
+        if (j >= 4) { jt[1] = cb1 * ri + ca2 * rq + cb1 * ys; jt[2] = ca3 * ru; }
+        if (!a.first) {
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            const float sold = S[k * nlm + j];
+            if (a.accel) {
+              if (j < nsmin) {
+                const float dn = jt[k] - sold, dd = D[k * nlm + j];
+                pdot += dn * dd; pold += dd * dd; pnew += dn * dn; pn += sold * sold;
+              }
+              D[k * nlm + j] = j < nsold ? jt[k] - sold : 0.f;
+            } else if (j < nsold) {
+              const float dn = jt[k] - sold;
+              pnew += dn * dn; pn += sold * sold;
+            }
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) S[k * nlm + j] = jt[k];  // truncated below once jlast is known
+      }
+      const bool big = j < nlm && (fabsf(jt[0]) > a.shacc || fabsf(jt[1]) > a.shacc || fabsf(jt[2]) > a.shacc);
+      const unsigned m = __ballot_sync(0xffffffffu, big);
+      if (m) jlast = j0 + 32 - __clz(m);
+    }
+    djdot += (double)pdot; djold += (double)pold; djnew += (double)pnew; jn += (double)pn;
+    int nsnew;
+    if (a.fixsh && !a.first) nsnew = nsold;
+    else if (jlast == 0) nsnew = 0;
+    else {
+      const int ls = a.lofj[jlast - 1];
+      nsnew = (ls <= a.mm) ? ls * (ls + 1) + ls + 1 : (2 * a.mm + 1) * ls - a.mm * a.mm + a.mm + 1;
+    }
+    for (int j = nsnew + lane; j < nlm; j += 32) { S[j] = 0.f; S[nlm + j] = 0.f; S[2 * nlm + j] = 0.f; }
+    int nrnext;
+    if (a.fixsh && !a.first) nrnext = max(4, nsnew);
+    else {
+      const float r0 = R[0];
+      int lr = 1;
+      for (int l = 1; l <= a.ml; ++l)
+        if (c1[l] * r0 > a.shacc) lr = l;
+      const int ls = a.lofj[max(1, nsnew) - 1];
+      lr = min(lr, ls + a.ml / 8 + 2);
+      if (a.highorder) lr = a.ml;
+      nrnext = (lr <= a.mm) ? lr * (lr + 1) + lr + 1 : (2 * a.mm + 1) * lr - a.mm * a.mm + a.mm + 1;
+    }
+    if (a.highorder && a.fixsh && !a.first) nrnext = nlm;
+    __syncwarp();
+    if (lane == 0) {
+      a.ns[p] = nsnew;
+      if (!a.first && a.accel) a.nso[p] = nsold;
+      if (a.first) a.nso[p] = nsnew;
+      a.nr[p] = nrnext;
+    }
+  }
+  if (!a.first) {
+    for (int o = 16; o > 0; o >>= 1) {
+      djdot += __shfl_xor_sync(0xffffffffu, djdot, o);
+      djold += __shfl_xor_sync(0xffffffffu, djold, o);
+      djnew += __shfl_xor_sync(0xffffffffu, djnew, o);
+      jn += __shfl_xor_sync(0xffffffffu, jn, o);
+    }
+    __shared__ double sred[4][8];
+    const int w = threadIdx.x >> 5;
+    if (lane == 0) { sred[0][w] = djdot; sred[1][w] = djold; sred[2][w] = djnew; sred[3][w] = jn; }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+      double t = 0;
+      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sred[threadIdx.x][k];
+      atomicAdd(&a.red[threadIdx.x], t);
+    }
+  }
+}
+
 struct AccelState {
   double a;        // acceleration parameter of the last iteration
   float solcrit;
@@ -1053,21 +1236,25 @@ __global__ void k_accel_param(const double *red, AccelState *st, int doaccel) {
 }
 
 // ACCELERATE_SOLUTION (src/polarized/shdomsub1.f:1807-1831).
+// rows of nst * nlm values per point (Stokes rows of nlm terms)
 __global__ void k_accelerate(float *source, const float *delsource, const int *ns, const int *nso, int npts, int nlm,
-                             const AccelState *st) {
+                             const AccelState *st, int nst) {
   float a = st->accelpar;
   if (!(a > 0.f)) return;
-  size_t total = (size_t)npts * nlm;
+  const int row = nst * nlm;
+  size_t total = (size_t)npts * row;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
-    int p = (int)(t / nlm), j = (int)(t - (size_t)p * nlm);
+    int p = (int)(t / row), j = (int)(t - (size_t)p * row) % nlm;
     if (j < min(ns[p], nso[p])) source[t] += a * delsource[t];
   }
 }
 
-__global__ void k_init_radiance(const float *rad0, float *radiance, int *nr, int npts, int nlm) {
-  size_t total = (size_t)npts * nlm;
+// Eddington initial radiance: 4 I terms per point, Q and U zero (INIT_RADIANCE).
+__global__ void k_init_radiance(const float *rad0, float *radiance, int *nr, int npts, int nlm, int nst) {
+  const int row = nst * nlm;
+  size_t total = (size_t)npts * row;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
-    int p = (int)(t / nlm), j = (int)(t - (size_t)p * nlm);
+    int p = (int)(t / row), j = (int)(t - (size_t)p * row);
     radiance[t] = j < 4 ? rad0[(size_t)p * 4 + j] : 0.f;
     if (j == 0) nr[p] = 4;
   }
@@ -1084,6 +1271,7 @@ struct RenderArgs {
   const int *botp;
   const float *bcrad_bot;
   const int *bot_index;  // point -> bottom list index or -1
+  const float *coefp, *phasetab2;  // polarized: a2/a3/b1 coefficients, I-Q single-scatter table
   const float *camx, *camy, *camz;
   const double *cammu, *camphi;
   float *out;
@@ -1367,6 +1555,303 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
   if (lane == 0) a.out[ray] = (float)radacc;
 }
 
+// Wigner d^n_{m m1}(x) at n = max(m, m1), m, m1 >= 0 (double precision).
+__device__ __forceinline__ double wig_start_d(double x, int m, int m1) {
+  if (m == m1) return pow(0.5 * (1.0 + x), (double)m);
+  const int hi = max(m, m1), lo = min(m, m1);
+  double c = (m1 > m || ((m - m1) % 2 == 0)) ? 1.0 : -1.0;
+  for (int q = 1; q <= hi - lo; ++q) c *= sqrt((double)(m + m1 + q) / q);
+  return c * pow(sqrt(0.5 * (1.0 - x)), (double)(hi - lo)) * pow(sqrt(0.5 * (1.0 + x)), (double)(hi + lo));
+}
+
+// The five generalized spherical functions a polarized ray needs (YLMALL,
+// src/polarized/shdomsub2.f:4244-4354, elements 1 I-I, 2 Q-Q, 3 U-U, 5 I-Q,
+// 6 Q-U) at one direction: y[e * nlm + j], e = 0..4.  Lane m runs the upward
+// recurrences in l of d^l_{m0}(x), d^l_{m2}(x) and d^l_{m2}(-x) in double
+// precision.
+__device__ void ylm6_dir_warp(float *y, int nlm, double x, double phi, int ml, int mm, int lane) {
+  const double fct = 0.3989422804014327;  // 1/sqrt(2 pi)
+  for (int m = lane; m <= mm; m += 32) {
+    double c = 1.0, sn = 0.0;
+    if (m > 0) sincos(m * phi, &sn, &c);
+    // d^l_{m0}
+    double a0p = 0.0, a0 = (m == 0) ? 1.0 : 0.0;
+    if (m > 0) {
+      double cc = 1.0;
+      for (int k = 1; k <= m; ++k) cc *= sqrt((double)(m + k) / (double)k);
+      a0 = ((m & 1) ? -cc : cc) * pow(0.5 * sqrt((1.0 - x) * (1.0 + x)), (double)m);
+    }
+    // d^l_{m2}(x) and d^l_{m2}(-x), from l = max(m, 2)
+    const int n2 = max(m, 2);
+    double bp = 0.0, bpp = 0.0, bm = 0.0, bmp = 0.0;
+    for (int l = m; l <= ml; ++l) {
+      if (l == n2) { bp = wig_start_d(x, m, 2); bm = wig_start_d(-x, m, 2); bpp = 0.0; bmp = 0.0; }
+      const double nrm = sqrt(l + 0.5);
+      const double dp = (l >= n2) ? bp * nrm : 0.0, dm = (l >= n2) ? (((l + m) & 1) ? -bm : bm) * nrm : 0.0;
+      const double p1 = fct * a0 * nrm, p2 = -0.5 * fct * (dp + dm), p3 = -0.5 * fct * (dp - dm);
+      const int j = (l <= mm) ? l * (l + 1) + m : (2 * mm + 1) * l - mm * mm + m;
+      y[j] = (float)(p1 * (c - sn));
+      y[nlm + j] = (float)(p2 * (c - sn));
+      y[2 * nlm + j] = (float)(p2 * (c + sn));
+      y[3 * nlm + j] = (float)(p3 * (c - sn));
+      y[4 * nlm + j] = (float)(p3 * (c + sn));
+      if (m > 0) {
+        const int jn = j - 2 * m;
+        y[jn] = (float)(p1 * (sn + c));
+        y[nlm + jn] = (float)(p2 * (sn + c));
+        y[2 * nlm + jn] = (float)(p2 * (sn - c));
+        y[3 * nlm + jn] = (float)(p3 * (sn + c));
+        y[4 * nlm + jn] = (float)(p3 * (sn - c));
+      }
+      // next degree
+      double an;
+      if (m == 0) an = ((2 * l + 1) * x * a0 - l * a0p) / (l + 1);
+      else an = ((2 * l + 1) * x * a0 - (l > m ? sqrt((double)(l * l - m * m)) * a0p : 0.0)) / sqrt((double)((l + 1) * (l + 1) - m * m));
+      a0p = a0; a0 = an;
+      if (l >= n2) {
+        const double q = sqrt((double)((l + 1) * (l + 1) - m * m)) * sqrt((double)((l + 1) * (l + 1) - 4));
+        const double r = sqrt((double)(l * l - m * m)) * sqrt((double)(l * l - 4));
+        const double f1 = (2.0 * l + 1.0) / l / q, f2 = r * (l + 1.0) / l / q;
+        const double np_ = (l * (l + 1.0) * x - 2.0 * m) * f1 * bp - f2 * (l > n2 ? bpp : 0.0);
+        const double nm_ = (-l * (l + 1.0) * x - 2.0 * m) * f1 * bm - f2 * (l > n2 ? bmp : 0.0);
+        bpp = bp; bp = np_; bmp = bm; bm = nm_;
+      }
+    }
+  }
+}
+
+// Polarized ray integration (INTEGRATE_1RAY with the polarized
+// COMPUTE_SOURCE_1CELL, src/polarized/shdomsub2.f:2311-2863, :2868-3042,
+// and ROTATE_POL_PLANE :3277-3316): as k_render, with the I, Q, U sources
+// of each corner and a Stokes vector along the ray.  Dynamic shared memory:
+// the five generalized functions (5 nlm floats) per warp.  out[ray][3].
+__global__ void __launch_bounds__(RWARPS * 32) k_render_pol(RenderArgs a) {
+  extern __shared__ float rsm[];
+  __shared__ float tl[RWARPS][3][64];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int ray = blockIdx.x * RWARPS + w;
+  if (ray >= a.nrays) return;
+  const int nlm = a.nlm;
+  float *Y = rsm + (size_t)w * 5 * nlm;
+  const double pi = 3.141592653589793;
+  double x0 = a.camx[ray], y0 = a.camy[ray], z0 = a.camz[ray], mu2 = a.cammu[ray], phi2 = a.camphi[ray];
+  const double muray = -mu2, phiray = phi2 - pi;
+  const float ztop = a.zgrid[a.nz - 1];
+  if (z0 > ztop) {
+    if (muray >= 0.0) { if (lane < 3) a.out[(size_t)ray * 3 + lane] = 0.f; return; }
+    double r = (ztop - z0) / muray;
+    x0 += r * sqrt(1 - muray * muray) * cos(phiray);
+    y0 += r * sqrt(1 - muray * muray) * sin(phiray);
+    z0 = ztop;
+  } else if (z0 < a.zgrid[0]) {
+    if (lane == 0) atomicCAS(a.err, ERR_NONE, ERR_RAY_BELOW);
+    if (lane < 3) a.out[(size_t)ray * 3 + lane] = 0.f;
+    return;
+  }
+  ylm6_dir_warp(Y, nlm, (double)(float)mu2, (double)(float)phi2, a.ml, a.mm, lane);
+  __syncwarp();
+  // TMS subtraction series: t_k(l) = sum_m Y_k(l, m) Ysun(l, m) for k = I-I, Q-Q, Q-U
+  for (int l = lane; l <= a.ml; l += 32) {
+    const int me = min(l, a.mm), j0 = (l <= a.mm) ? l * l : (2 * a.mm + 1) * l - a.mm * a.mm - a.mm;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+    for (int k = 0; k < 2 * me + 1; ++k) {
+      const float ys = a.ylmsun[j0 + k];
+      s0 += Y[j0 + k] * ys; s1 += Y[nlm + j0 + k] * ys; s2 += Y[4 * nlm + j0 + k] * ys;
+    }
+    tl[w][0][l] = s0; tl[w][1][l] = s1; tl[w][2][l] = s2;
+  }
+  __syncwarp();
+  int sj = 0;
+  float sf = 0.f, cos22 = 1.f, sin22 = 0.f;
+  if (a.deltam) {
+    double cosscat = (double)a.solarmu * mu2 + sqrt((1.0 - (double)a.solarmu * a.solarmu) * (1.0 - mu2 * mu2)) * cos((double)a.solaraz - phi2);
+    cosscat = fmax(fmin(1.0, cosscat), -1.0);
+    float F = (float)((a.nscatangle - 1) * (acos(cosscat) / pi) + 1);
+    int J = min(a.nscatangle - 1, (int)F);
+    sf = F - J; sj = J - 1;
+    // rotation of the single-scatter polarization to the outgoing meridional plane
+    const float smu = a.solarmu, mu2f = (float)mu2, dphi = a.solaraz - (float)phi2;
+    const double sin_scat = sqrt(fmax(0.0, 1.0 - cosscat * cosscat));
+    const double st1 = sqrt(1.0 - (double)(smu * smu)), st2 = sqrt(1.0 - (double)(mu2f * mu2f));
+    double sp, cp;
+    sincos((double)dphi, &sp, &cp);
+    double sin2, cos2;
+    if (sin_scat == 0.0) { sin2 = 0.0; cos2 = -1.0; }
+    else { sin2 = st1 * sp / sin_scat; cos2 = (st2 * smu - st1 * mu2f * cp) / sin_scat; }
+    cos22 = (float)(1.0 - 2.0 * sin2 * sin2);
+    sin22 = (float)(2.0 * sin2 * cos2);
+  }
+  double cx = sqrt(1.0 - mu2 * mu2) * cos(phi2 - pi), cy = sqrt(1.0 - mu2 * mu2) * sin(phi2 - pi), cz = -mu2;
+  double cxinv, cyinv, czinv;
+  if (fabs(cx) > 1e-6) cxinv = 1.0 / cx; else { cx = 0; cxinv = 1e6; }
+  if (fabs(cy) > 1e-6) cyinv = 1.0 / cy; else { cy = 0; cyinv = 1e6; }
+  if (fabs(cz) > 1e-6) czinv = 1.0 / cz; else { cz = 0; czinv = 1e6; }
+  const int bitx = cx < 0, bity = cy < 0, bitz = cz < 0, ioct0 = bitx + 2 * bity + 4 * bitz;
+  const float xm = 0.5f * (a.xgrid[0] + a.xgrid[a.nx - 1]), ym = 0.5f * (a.ygrid[0] + a.ygrid[a.ny - 1]);
+  double xe = x0, ye = y0, ze = z0;
+  int cell = locate_cell(a, xe, ye, ze);
+  const double eps = 1.0e-5 * (a.gridpos[3 * a.gridptr[7] + 2] - a.gridpos[3 * a.gridptr[0] + 2]);
+  const int maxcross = 500 * max(a.nx, max(a.ny, a.nz));
+  int oldp[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+  float osrc[3][8] = {{0}};
+  float ext8[8], src8[3][8];
+  double radacc[3] = {0.0, 0.0, 0.0}, transmit = 1.0;
+  const double inv_tautol = 1.0 / (double)a.tautol;
+  const int nl = a.nl;
+  int ngrid = 0;
+  bool validrad = false;
+  const int grp = lane >> 2, gl = lane & 3;
+  while (!validrad && cell >= 0) {
+    ++ngrid;
+    const int *g = a.gridptr + 8 * (size_t)cell;
+    const int mypt = g[grp];
+    int reuse = -1;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) if (oldp[k] == mypt) reuse = k;
+    const float cext = a.text[mypt];
+    const bool need = reuse < 0;
+    const int ns = need ? a.ns[mypt] : 0;
+    float sI = 0.f, sQ = 0.f, sU = 0.f;
+    {
+      const float *S = a.source + (size_t)mypt * 3 * nlm;
+      for (int j = gl; j < ns; j += 4) {
+        const float si = S[j], sq = S[nlm + j], su = S[2 * nlm + j];
+        sI += si * Y[j];
+        sQ += sq * Y[nlm + j] + su * Y[3 * nlm + j];
+        sU += sq * Y[4 * nlm + j] + su * Y[2 * nlm + j];
+      }
+    }
+#pragma unroll
+    for (int o = 1; o <= 2; o <<= 1) {
+      sI += __shfl_xor_sync(0xffffffffu, sI, o);
+      sQ += __shfl_xor_sync(0xffffffffu, sQ, o);
+      sU += __shfl_xor_sync(0xffffffffu, sU, o);
+    }
+    float cv[3];
+    if (!need) {
+      cv[0] = osrc[0][reuse]; cv[1] = osrc[1][reuse]; cv[2] = osrc[2][reuse];
+    } else {
+      if (a.deltam) {
+        const float da = a.dirflux[mypt] * a.secmu0;
+        const float *c1 = a.coef + (size_t)mypt * nl, *cb1 = a.coefp + ((size_t)mypt * 3 + 2) * nl;
+        if (ns > 0) {
+          const int ls = a.lofj[ns - 1];
+          float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+          for (int l = 0; l <= ls; ++l) { s0 += c1[l] * tl[w][0][l]; s1 += cb1[l] * tl[w][1][l]; s2 += cb1[l] * tl[w][2][l]; }
+          sI -= da * s0; sQ -= da * s1; sU -= da * s2;
+        }
+        float add0 = 0.f, add1 = 0.f;
+        for (int q = a.tms_ptr[mypt]; q < a.tms_ptr[mypt + 1]; ++q) {
+          const int iph = a.tms_iph[q];
+          const size_t o0 = (size_t)sj * a.numphase + iph, o1 = (size_t)(sj + 1) * a.numphase + iph;
+          add0 += a.tms_w[q] * ((1.f - sf) * a.phasetab[o0] + sf * a.phasetab[o1]);
+          add1 += a.tms_w[q] * ((1.f - sf) * a.phasetab2[o0] + sf * a.phasetab2[o1]);
+        }
+        sI += da * add0; sQ += da * add1 * cos22; sU += da * add1 * sin22;
+      }
+      cv[0] = sI * cext; cv[1] = sQ * cext; cv[2] = sU * cext;
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      ext8[k] = __shfl_sync(0xffffffffu, cext, 4 * k);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) src8[c][k] = __shfl_sync(0xffffffffu, cv[c], 4 * k);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) { oldp[k] = g[k]; osrc[0][k] = src8[0][k]; osrc[1][k] = src8[1][k]; osrc[2][k] = src8[2][k]; }
+    const int ip1 = g[0], ip2 = g[7];
+    const float *P1 = a.gridpos + 3 * ip1, *P2 = a.gridpos + 3 * ip2;
+    const float delx = P2[0] - P1[0], dely = P2[1] - P1[1], delz = P2[2] - P1[2];
+    const float idx = delx <= 0.f ? 1.f : 1.f / delx, idy = dely <= 0.f ? 1.f : 1.f / dely, idz = 1.f / delz;
+    auto tri = [&](const float *v, float u, float vv, float ww) {
+      const float a0 = fmaf(u, v[1] - v[0], v[0]), a1 = fmaf(u, v[3] - v[2], v[2]);
+      const float a2 = fmaf(u, v[5] - v[4], v[4]), a3 = fmaf(u, v[7] - v[6], v[6]);
+      const float b0 = fmaf(vv, a1 - a0, a0), b1 = fmaf(vv, a3 - a2, a2);
+      return fmaf(ww, b1 - b0, b0);
+    };
+    const float u0 = (float)(xe - P1[0]) * idx, v0 = (float)(ye - P1[1]) * idy, w0 = (float)(ze - P1[2]) * idz;
+    float srcext1[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) srcext1[c] = tri(src8[c], u0, v0, w0);
+    srcext1[0] = fmaxf(0.f, srcext1[0]);
+    float ext1 = tri(ext8, u0, v0, w0);
+    const int cf = a.cellflags[cell];
+    bool ipinx = (cf & 1) && !((a.bcflag & 1) && ((cx > 0 && xe < xm) || (cx < 0 && xe > xm)));
+    bool ipiny = (cf & 2) && !((a.bcflag & 2) && ((cy > 0 && ye < ym) || (cy < 0 && ye > ym)));
+    const int iopp = g[7 - ioct0];
+    double sox = ipinx ? 1e20 : (a.gridpos[3 * iopp] - xe) * cxinv;
+    double soy = ipiny ? 1e20 : (a.gridpos[3 * iopp + 1] - ye) * cyinv;
+    double soz = (a.gridpos[3 * iopp + 2] - ze) * czinv;
+    double so = fmin(sox, fmin(soy, soz));
+    if (so < -eps) { if (lane == 0) atomicCAS(a.err, ERR_NONE, ERR_RAY_SO); break; }
+    double xn = xe + so * cx, yn = ye + so * cy, zn = ze + so * cz;
+    const float du = (float)cx * idx, dv = (float)cy * idy, dw = (float)cz * idz;
+    const float sof = (float)so;
+    float extn = tri(ext8, fmaf(sof, du, u0), fmaf(sof, dv, v0), fmaf(sof, dw, w0));
+    double taugrid = so * 0.5 * (ext1 + extn);
+    int ntau = max(1, 1 + (int)(taugrid * inv_tautol));
+    const float delsf = sof / (float)ntau;
+    for (int it = 1; it <= ntau; ++it) {
+      const float sf_ = it * delsf;
+      const float uu_ = fmaf(sf_, du, u0), vv_ = fmaf(sf_, dv, v0), ww_ = fmaf(sf_, dw, w0);
+      const float ext0 = tri(ext8, uu_, vv_, ww_);
+      float srcext0[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) srcext0[c] = tri(src8[c], uu_, vv_, ww_);
+      srcext0[0] = fmaxf(0.f, srcext0[0]);
+      const float ext = 0.5f * (ext0 + ext1);
+      float absc, trc;
+      if (ext != 0.f) {
+        const float tau = ext * delsf;
+        absc = tau * (1.f - 0.5f * tau * (1.f - 0.33333333333f * tau));
+        trc = 1.f - absc;
+        const float iext = 1.f / ext, corr = delsf * (1.f - 0.05f * (ext1 - ext0) * delsf);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float src = (0.5f * (srcext0[c] + srcext1[c]) + 0.08333333333f * (ext0 * srcext1[c] - ext1 * srcext0[c]) * corr) * iext;
+          radacc[c] += transmit * src * absc;
+        }
+      } else { trc = 1.f; }
+      transmit *= trc;
+      ext1 = ext0;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) srcext1[c] = srcext0[c];
+    }
+    int iface, jface;
+    bool openbc;
+    if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; openbc = (cf & 1) && (a.bcflag & 1); }
+    else if (soy <= soz) { iface = 3 - bity; jface = 1; openbc = (cf & 2) && (a.bcflag & 2); }
+    else { iface = 5 - bitz; jface = 2; openbc = false; }
+    int nxt = a.neighptr[6 * (size_t)cell + iface];
+    int kface = iface, kc = cell;
+    if (openbc) { kface = iface ^ 1; kc = nxt; iface = -1; }
+    if (nxt >= 0) {
+      const float *q = a.gridpos + 3 * a.gridptr[8 * (size_t)nxt + ioct0];
+      if (jface == 0) xn = q[0]; else if (jface == 1) yn = q[1]; else zn = q[2];
+    }
+    if (transmit < a.transcut || ngrid > maxcross) {
+      validrad = true;
+    } else if (nxt < 0 && iface >= 4) {
+      validrad = true;  // unpolarized boundary radiance (I only)
+      const int *gk = a.gridptr + 8 * (size_t)kc;
+      float xs[4], ys[4], rb[4];
+      for (int k = 0; k < 4; ++k) {
+        int q = gk[c_face[kface][k]];
+        xs[k] = a.gridpos[3 * q]; ys[k] = a.gridpos[3 * q + 1];
+        if ((float)mu2 < 0.f) rb[k] = a.skyrad;
+        else { int bi = a.bot_index[q]; rb[k] = bi >= 0 ? a.bcrad_bot[bi] : 0.f; }
+      }
+      float uu = (xs[1] - xs[0] > 0) ? (float)((xn - xs[0]) / (xs[1] - xs[0])) : 0.f;
+      float vv = (ys[2] - ys[0] > 0) ? (float)((yn - ys[0]) / (ys[2] - ys[0])) : 0.f;
+      radacc[0] += transmit * ((1 - uu) * (1 - vv) * rb[0] + uu * (1 - vv) * rb[1] + (1 - uu) * vv * rb[2] + uu * vv * rb[3]);
+    } else {
+      cell = nxt;
+    }
+    xe = xn; ye = yn; ze = zn;
+  }
+  if (lane < 3) a.out[(size_t)ray * 3 + lane] = (float)radacc[lane];
+}
+
 __global__ void k_bcrad_bottom(const int *botp, int nbot, const float *botalb, const float *dirflux,
                                const float *fluxes, float *bcrad) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1434,6 +1919,12 @@ struct Handle {
   cudaGraphExec_t iter_graph[2] = {nullptr, nullptr};  // one iteration, without / with the fixed truncation
   long long iter_graph_launches[2] = {0, 0};
   DBuf<float> col_cx, col_cy, col_cz, col_fluxw, cmu1t, cmu2t, cphi1t, cphi2, ylmsun;
+  // polarized (nst = 3): Stokes component per ordinate column, the a2/a3/b1
+  // source coefficients and the I-Q single-scatter table
+  int nst = 1;
+  DBuf<uint8_t> col_stk;
+  DBuf<float> coefp, phasetab2;
+  DBuf<float> pol_t[2];  // FP32 dense transform matrices for the CUDA-core path, [K][N]
   DBuf<int> nphi0, col_of;
   // medium
   DBuf<float> text, dirflux, coef, tms_w, phasetab, botalb, rad0;
@@ -1521,6 +2012,76 @@ static void dense_do_to_sh(const Plan &P, std::vector<double> &T) {
   for (int c = 0; c < nang; ++c) T[(size_t)(c < P.ncol_down ? nlm : nlm + 1) * nang + c] = P.col_fluxw[c];
 }
 
+// Polarized matrices (SH_TO_DO / DO_TO_SH, src/polarized/shdomsub1.f:
+// 2789-2926, :3041-3160).  Harmonic rows are [Stokes][nlm] (I, Q, U), ordinate
+// columns are the plan's Stokes columns.  The mu part mixes Q and U with the
+// generalized functions (elements 2, 3, 5, 6); in azimuth the I and Q
+// harmonics use cos/sin like the scalar transform and U the swapped pair
+// (the reference's SUMCS(3, +-m) rules).
+// T1[c][s * nlm + j]: column c from Stokes harmonic (s, j).
+static void dense_sh_to_do_pol(const Plan &P, std::vector<double> &T) {
+  const int nlm = P.nlm, nm = 2 * P.mm + 1, np0 = P.nphi0max, K = 3 * nlm;
+  T.assign((size_t)P.nang * K, 0.0);
+  // mu coefficient of input Stokes si in output Stokes so, element index into the 6 generalized functions
+  const int el[3][3] = {{0, -1, -1}, {-1, 1, 4}, {-1, 5, 2}};
+  for (int j = 0; j < nlm; ++j) {
+    const int m = P.mofj[j], ma = std::abs(m);
+    for (int i = 0; i < P.nmu; ++i) {
+      const int n0 = P.nphi0[i], me = std::max(0, n0 / 2 - 1);
+      if (ma > me) continue;
+      const float *c6 = &P.cmu1p[((size_t)i * nlm + j) * 6];
+      for (int k = 0; k < n0; ++k) {
+        const float *cp = &P.cphi1[((size_t)i * np0 + k) * nm + P.mm];
+        const int c0 = P.col_of[i * np0 + k];  // the I column; Q and U follow at the group's stride
+        for (int so = 0; so < 3; ++so) {
+          double w;
+          if (m == 0) w = cp[0];
+          else if (so < 2) w = m > 0 ? (double)cp[ma] - cp[-ma] : (double)cp[ma] + cp[-ma];
+          else w = m > 0 ? (double)cp[ma] + cp[-ma] : (double)cp[ma] - cp[-ma];
+          const int col = c0 + so * (P.cls_ncol[P.col_oct[c0] - 1][P.col_cls[c0]] / 3);
+          for (int si = 0; si < 3; ++si) {
+            const int e = el[so][si];
+            if (e < 0) continue;
+            T[(size_t)col * K + si * nlm + j] += (double)c6[e] * w;
+          }
+        }
+      }
+    }
+  }
+}
+
+// T2[s * nlm + j][c]: Stokes harmonic (s, j) from column c.
+static void dense_do_to_sh_pol(const Plan &P, std::vector<double> &T) {
+  const int nlm = P.nlm, nm = 2 * P.mm + 1, np0 = P.nphi0max, nang = P.nang;
+  T.assign((size_t)(3 * nlm) * nang, 0.0);
+  // mu coefficient of ordinate Stokes si in harmonic Stokes so
+  const int el[3][3] = {{0, -1, -1}, {-1, 1, 4}, {-1, 5, 2}};
+  for (int j = 0; j < nlm; ++j) {
+    const int m = P.mofj[j], ma = std::abs(m);
+    for (int i = 0; i < P.nmu; ++i) {
+      const int n0 = P.nphi0[i], me = std::max(0, n0 / 2 - 1);
+      if (ma > me) continue;
+      const float *c6 = &P.cmu2p[((size_t)i * nlm + j) * 6];
+      for (int k = 0; k < n0; ++k) {
+        const float *cp = &P.cphi2[((size_t)i * np0 + k) * nm + P.mm];
+        const int c0 = P.col_of[i * np0 + k];
+        for (int si = 0; si < 3; ++si) {
+          double w;
+          if (m == 0) w = cp[0];
+          else if (si < 2) w = m > 0 ? (double)cp[ma] - cp[-ma] : (double)cp[ma] + cp[-ma];
+          else w = m > 0 ? (double)cp[ma] + cp[-ma] : (double)cp[ma] - cp[-ma];
+          const int col = c0 + si * (P.cls_ncol[P.col_oct[c0] - 1][P.col_cls[c0]] / 3);
+          for (int so = 0; so < 3; ++so) {
+            const int e = el[so][si];
+            if (e < 0) continue;
+            T[(size_t)(so * nlm + j) * nang + col] += (double)c6[e] * w;
+          }
+        }
+      }
+    }
+  }
+}
+
 // Round to TF32 (10 explicit mantissa bits), nearest with ties away from
 // zero, as cvt.rna.tf32.f32 does on the device.
 static float tf32_rna(float x) {
@@ -1603,18 +2164,35 @@ static void setup_tc(Handle &H) {
   CK(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
   CK(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
   CK(cudaDeviceGetAttribute(&H.nsm, cudaDevAttrMultiProcessorCount, dev));
+  if (H.nst == 3) {  // [K][N] FP32 matrices of the CUDA-core transforms
+    std::vector<double> T;
+    const int nsh3 = 3 * P.nlm;
+    dense_sh_to_do_pol(P, T);  // [nang][3 nlm]
+    std::vector<float> t((size_t)nsh3 * P.nang);
+    for (int c = 0; c < P.nang; ++c)
+      for (int k = 0; k < nsh3; ++k) t[(size_t)k * P.nang + c] = (float)T[(size_t)c * nsh3 + k];
+    H.pol_t[0].upload(t);
+    dense_do_to_sh_pol(P, T);  // [3 nlm][nang]
+    t.assign((size_t)P.nang * nsh3, 0.f);
+    for (int j = 0; j < nsh3; ++j)
+      for (int c = 0; c < P.nang; ++c) t[(size_t)c * nsh3 + j] = (float)T[(size_t)j * P.nang + c];
+    H.pol_t[1].upload(t);
+  }
   if (major != 10) return;
+  const int nsh = H.nst * P.nlm;  // harmonic row length (I, Q, U rows when polarized)
   for (int dir = 0; dir < 2; ++dir) {
     // the ordinate-to-harmonic direction forms the fluxes from A on the CUDA cores
-    const int K = dir == 0 ? P.nlm : P.nang, N = dir == 0 ? P.nang : P.nlm;
-    const int lda = dir == 0 ? P.nlm : H.ldo;
+    const int K = dir == 0 ? nsh : P.nang, N = dir == 0 ? P.nang : nsh;
+    const int lda = dir == 0 ? nsh : H.ldo;
     if (lda % 4 != 0 || K < tc::BK || P.npts < tc::BM) continue;
     if (dir == 1 && (K + tc::BK - 1) / tc::BK * tc::BK * 8 > 16 * 1024) continue;  // flux weight table
     const int ntiles = (N + 127) / 128;  // tiles of at most 128 columns keep the FP32 sums in registers
     const int bn = ((N + ntiles - 1) / ntiles + 31) / 32 * 32;
     const int npad = ntiles * bn, kpad = (K + tc::BK - 1) / tc::BK * tc::BK;
     std::vector<double> T;
-    if (dir == 0) dense_sh_to_do(P, T); else dense_do_to_sh(P, T);  // rows [0, N) are used
+    if (H.nst == 3) { if (dir == 0) dense_sh_to_do_pol(P, T); else dense_do_to_sh_pol(P, T); }
+    else if (dir == 0) dense_sh_to_do(P, T);
+    else dense_do_to_sh(P, T);  // rows [0, N) are used
     std::vector<float> bh((size_t)npad * kpad, 0.f), bl((size_t)npad * kpad, 0.f);
     for (int n = 0; n < N; ++n)
       for (int k = 0; k < K; ++k) {
@@ -1645,7 +2223,7 @@ static void setup_tc(Handle &H) {
   // scattering points' rows: gathered into dense blocks for the tensor
   // cores; the others get their 4 radiance terms and fluxes on the CUDA
   // cores.  (Not with HIGHORDERRAD, which keeps every radiance term.)
-  if (H.tc_ok[0] && H.tc_ok[1] && !P.prob.highorderrad && P.nlm >= 4) {
+  if (H.tc_ok[0] && H.tc_ok[1] && !P.prob.highorderrad && P.nlm >= 4 && H.nst == 1) {
     const int nl = P.ml + 1;
     std::vector<int> hv, lt;
     for (int p = 0; p < P.npts; ++p) {
@@ -1691,7 +2269,8 @@ static long long plan_device_bytes(const Plan &P) {
   b += vbytes(P.nphi0) + vbytes(P.col_of) + vbytes(P.total_ext) + vbytes(P.dirflux) + vbytes(P.coef) + vbytes(P.tms_ptr);
   b += vbytes(P.tms_iph) + vbytes(P.tms_w) + vbytes(P.phasetab) + vbytes(P.botalb) + vbytes(P.rad0);
   const long long ldo = (P.nang + 3) & ~3;
-  b += 4LL * P.npts * (3LL * P.nlm + 2 * ldo + 2 + 3) + 4LL * (long long)P.botp.size() + 64;
+  b += 4LL * P.npts * (3LL * P.nst * P.nlm + 2 * ldo + 2 + 3) + 4LL * (long long)P.botp.size() + 64;
+  if (P.nst == 3) b += vbytes(P.col_stk) + vbytes(P.coefp) + vbytes(P.phasetab2) + 8LL * P.nlm * 3 * P.nang;
   {  // gathered rows of the scattering points for the compacted transforms
     const int nl = P.ml + 1;
     long long nh = 0;
@@ -1700,8 +2279,9 @@ static long long plan_device_bytes(const Plan &P) {
         if (P.coef[(size_t)p * nl + l] != 0.f) { ++nh; break; }
     if (nh * 10 < (long long)P.npts * 9) b += 4LL * nh * (P.nlm + ldo) + 4LL * P.npts + 16LL * P.nang;
   }
-  const long long kp0 = (P.nlm + 31) / 32 * 32, kp1 = (P.nang + 31) / 32 * 32;
-  const long long np0 = ((P.nang + 255) / 256) * 256 + 256, np1 = ((P.nlm + 2 + 255) / 256) * 256 + 256;
+  const long long nsh = (long long)P.nst * P.nlm;
+  const long long kp0 = (nsh + 31) / 32 * 32, kp1 = (P.nang + 31) / 32 * 32;
+  const long long np0 = ((P.nang + 255) / 256) * 256 + 256, np1 = ((nsh + 2 + 255) / 256) * 256 + 256;
   b += 8LL * (np0 * kp0 + np1 * kp1);  // upper bound of the padded hi/lo matrices
   return b;
 }
@@ -1713,10 +2293,12 @@ static void fill_sizes(const Plan &P, shdom_sizes *o) {
   o->nlevels_down = (int)P.seg_off[0].size() - 1;
   o->nlevels_up = (int)P.seg_off[1].size() - 1;
   o->device_bytes = plan_device_bytes(P);
+  o->nstokes = P.nst;
 }
 
 static void upload_plan(Handle &H) {
   Plan &P = H.P;
+  H.nst = P.nst;
   H.gridpos.upload(P.gridpos); H.xgrid.upload(P.xgrid); H.ygrid.upload(P.ygrid); H.zgrid.upload(P.zgrid);
   H.gridptr.upload(P.gridptr); H.neighptr.upload(P.neighptr); H.cellflags.upload(P.cellflags);
   H.rank.upload(P.rank); H.start.upload(P.startcell); H.level.upload(P.level);
@@ -1802,8 +2384,9 @@ static void upload_plan(Handle &H) {
   }
   H.tms_ptr.upload(P.tms_ptr); H.tms_iph.upload(P.tms_iph); H.tms_w.upload(P.tms_w);
   H.phasetab.upload(P.phasetab); H.botalb.upload(P.botalb); H.rad0.upload(P.rad0);
+  if (H.nst == 3) { H.col_stk.upload(P.col_stk); H.coefp.upload(P.coefp); H.phasetab2.upload(P.phasetab2); }
   H.ldo = (P.nang + 3) & ~3;
-  const size_t nf = (size_t)P.npts * P.nlm, nd = (size_t)P.npts * H.ldo;
+  const size_t nf = (size_t)P.npts * H.nst * P.nlm, nd = (size_t)P.npts * H.ldo;
   H.source.alloc(nf); H.delsource.alloc(nf); H.radiance.alloc(nf);
   H.srcdo.alloc(nd); H.raddo.alloc(nd);
   H.srcdo.zero(H.stream); H.raddo.zero(H.stream);
@@ -1825,9 +2408,11 @@ static void launch_source(Handle &H, int first, int fixsh) {
   a.npts = P.npts; a.nlm = P.nlm; a.nl = P.ml + 1; a.ml = P.ml; a.mm = P.mm;
   a.secmu0 = 1.0f / std::fabs(P.prob.solarmu); a.shacc = P.prob.shacc;
   a.first = first; a.fixsh = fixsh; a.accel = P.prob.accelflag; a.highorder = P.prob.highorderrad;
+  a.coefp = H.nst == 3 ? H.coefp.p : nullptr;
   CK(cudaMemsetAsync(H.red.p, 0, 4 * sizeof(double), H.stream));
   int blocks = std::min((P.npts + 7) / 8, 152 * 16);
-  k_source<<<blocks, 256, 0, H.stream>>>(a);
+  if (H.nst == 3) k_source_pol<<<blocks, 256, 0, H.stream>>>(a);
+  else k_source<<<blocks, 256, 0, H.stream>>>(a);
   H.launches += 1;
   CK(cudaGetLastError());
 }
@@ -1858,14 +2443,16 @@ static void transforms_launch(Handle &H, int dir) {
 // dir 0: SOURCE -> SRCDO (with the non-negativity clamp); dir 1: RADDO ->
 // RADIANCE (masked to the radiance truncation) and the hemispheric fluxes.
 static void transform(Handle &H, int dir) {
+  const int nsh = H.nst * H.P.nlm;
   if (H.xf_mode != 2 && H.tc_ok[dir]) {
     Plan &P = H.P;
     tc::Epilogue g{};
     g.M = P.npts; g.err = H.errflag.p; g.split = H.xf_mode == 0 ? 1 : 0;
     if (dir == 0) {
       g.N = P.nang; g.mode = 0; g.C = H.srcdo.p; g.ldc = H.ldo;
+      g.stk = H.nst == 3 ? H.col_stk.p : nullptr;
     } else {
-      g.N = P.nlm; g.mode = 1; g.R = H.radiance.p; g.nlm = P.nlm; g.nr = H.nr.p; g.fluxes = H.fluxes.p;
+      g.N = nsh; g.mode = 1; g.R = H.radiance.p; g.nlm = P.nlm; g.ldr = nsh; g.nr = H.nr.p; g.fluxes = H.fluxes.p;
       g.fluxw = H.col_fluxw.p; g.ncol_down = P.ncol_down;
     }
     const int ntn = H.tc_ntiles[dir];
@@ -1897,10 +2484,30 @@ static void transform(Handle &H, int dir) {
       return;
     }
     const int ntiles = ntn * ((P.npts + tc::BM - 1) / tc::BM);
-    tc_launch(H.tc_bn[dir], H.nsm, H.stream, H.tm_a[dir], H.tm_bh[dir], H.tm_bl[dir], dir == 0 ? P.nlm : P.nang, ntn,
+    tc_launch(H.tc_bn[dir], H.nsm, H.stream, H.tm_a[dir], H.tm_bh[dir], H.tm_bl[dir], dir == 0 ? nsh : P.nang, ntn,
               ntiles, g);
     CK(cudaGetLastError());
     H.launches += 1;
+    return;
+  }
+  if (H.nst == 3) {  // FP32 dense transforms on the CUDA cores
+    Plan &P = H.P;
+    const int K = dir == 0 ? nsh : P.nang, N = dir == 0 ? P.nang : nsh;
+    const dim3 grid((N + 63) / 64, (P.npts + 63) / 64);
+    if (dir == 0)
+      k_dense_xf<<<grid, 256, 0, H.stream>>>(H.source.p, nsh, H.pol_t[0].p, K, N, P.npts, 0, H.srcdo.p, H.ldo,
+                                              H.col_stk.p, nullptr, P.nlm);
+    else
+      k_dense_xf<<<grid, 256, 0, H.stream>>>(H.raddo.p, H.ldo, H.pol_t[1].p, K, N, P.npts, 1, H.radiance.p, nsh,
+                                              nullptr, H.nr.p, P.nlm);
+    CK(cudaGetLastError());
+    H.launches += 1;
+    if (dir == 1) {
+      const int fb = std::min((P.npts + 7) / 8, 152 * 16);
+      k_do_fluxes<<<fb, 256, 0, H.stream>>>(H.raddo.p, H.ldo, P.nang, P.ncol_down, H.col_fluxw.p, P.npts, H.fluxes.p);
+      CK(cudaGetLastError());
+      H.launches += 1;
+    }
     return;
   }
   const int nmu = H.P.nmu;
@@ -1919,6 +2526,7 @@ static SweepArgs sweep_args(Handle &H, int hemi) {
   a.regular = H.regular.p; a.geo = H.geo.p; a.nz = P.nz; a.ny1 = P.ny1;
   a.transmin = P.prob.transmin;
   a.irr = H.irr[hemi].p;
+  a.stk = H.nst == 3 ? H.col_stk.p : nullptr;
   for (int b = 0; b < 8; ++b) { a.oct_col0[b] = P.oct_col0[b]; a.oct_ncol[b] = P.oct_ncol[b]; }
   return a;
 }
@@ -2140,9 +2748,9 @@ int shdom_init_solution(shdom_handle *hh) {
   Handle &H = hh->h;
   try {
     shdom::Plan &P = H.P;
-    size_t tot = (size_t)P.npts * P.nlm;
+    size_t tot = (size_t)P.npts * H.nst * P.nlm;
     int blocks = (int)std::min<size_t>((tot + 255) / 256, 152 * 64);
-    shdom::k_init_radiance<<<blocks, 256, 0, H.stream>>>(H.rad0.p, H.radiance.p, H.nr.p, P.npts, P.nlm);
+    shdom::k_init_radiance<<<blocks, 256, 0, H.stream>>>(H.rad0.p, H.radiance.p, H.nr.p, P.npts, P.nlm, H.nst);
     H.launches += 1;
     CK(cudaMemsetAsync(H.source.p, 0, tot * sizeof(float), H.stream));
     CK(cudaMemsetAsync(H.delsource.p, 0, tot * sizeof(float), H.stream));
@@ -2190,13 +2798,14 @@ int shdom_solution_iterations(shdom_handle *hh, int maxiter, int *iters, float *
       int ntop = (int)P.topp.size(), nbot = (int)P.botp.size();
       if (ntop && P.ncol_down) {
         int t = ntop * P.ncol_down;
-        shdom::k_preset_top<<<(t + 255) / 256, 256, 0, H.stream>>>(H.topp.p, ntop, H.raddo.p, H.ldo, P.ncol_down, P.prob.skyrad);
+        shdom::k_preset_top<<<(t + 255) / 256, 256, 0, H.stream>>>(H.topp.p, ntop, H.raddo.p, H.ldo, P.ncol_down, P.prob.skyrad,
+                                                                   H.nst == 3 ? H.col_stk.p : nullptr);
         H.launches += 1;
       }
       shdom::sweep_hemisphere(H, 0);
       if (nbot) {
         shdom::k_lambertian<<<nbot, 256, 0, H.stream>>>(H.botp.p, nbot, H.botalb.p, H.dirflux.p, H.col_fluxw.p, H.raddo.p,
-                                                         nang, H.ldo, P.ncol_down, H.bcrad.p);
+                                                         nang, H.ldo, P.ncol_down, H.bcrad.p, H.nst == 3 ? H.col_stk.p : nullptr);
         H.launches += 1;
       }
       shdom::sweep_hemisphere(H, 1);
@@ -2206,8 +2815,9 @@ int shdom_solution_iterations(shdom_handle *hh, int maxiter, int *iters, float *
       shdom::launch_source(H, 0, fix ? 1 : 0);
       shdom::k_accel_param<<<1, 1, 0, H.stream>>>(H.red.p, H.accel.p, P.prob.accelflag);
       H.launches += 2;
-      int blocks = (int)std::min<size_t>(((size_t)P.npts * nlm + 255) / 256, 152 * 64);
-      shdom::k_accelerate<<<blocks, 256, 0, H.stream>>>(H.source.p, H.delsource.p, H.ns.p, H.nso.p, P.npts, nlm, H.accel.p);
+      int blocks = (int)std::min<size_t>(((size_t)P.npts * H.nst * nlm + 255) / 256, 152 * 64);
+      shdom::k_accelerate<<<blocks, 256, 0, H.stream>>>(H.source.p, H.delsource.p, H.ns.p, H.nso.p, P.npts, nlm, H.accel.p,
+                                                        H.nst);
     };
     const bool graphed = H.sweep_mode == 2;
     while (H.iters < maxiter && H.solcrit > P.prob.solacc) {
@@ -2286,6 +2896,8 @@ static shdom::RenderArgs render_args(Handle &H, int nrays, const float *camx, co
   a.nscatangle = P.nscatangle; a.deltam = P.prob.deltam; a.solarmu = P.prob.solarmu; a.solaraz = P.prob.solaraz;
   a.secmu0 = 1.0f / std::fabs(P.prob.solarmu); a.skyrad = P.prob.skyrad; a.tautol = P.prob.tautol;
   a.transcut = P.prob.transcut;
+  a.coefp = H.nst == 3 ? H.coefp.p : nullptr;
+  a.phasetab2 = H.nst == 3 ? H.phasetab2.p : nullptr;
   return a;
 }
 
@@ -2303,7 +2915,13 @@ static int render_impl(shdom_handle *hh, int nrays, const float *camx, const flo
   if (P.nlm > shdom::RNLM || P.ml + 1 > 64) return fail(hh, "render: too many spherical-harmonic terms");
   int blocks = (nrays + shdom::RWARPS - 1) / shdom::RWARPS;
   if (blocks > 0) {
-    shdom::k_render<<<blocks, shdom::RWARPS * 32, 0, stream>>>(a);
+    if (H.nst == 3) {
+      const size_t smem = (size_t)shdom::RWARPS * 5 * P.nlm * sizeof(float);
+      CK(cudaFuncSetAttribute(shdom::k_render_pol, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      shdom::k_render_pol<<<blocks, shdom::RWARPS * 32, smem, stream>>>(a);
+    } else {
+      shdom::k_render<<<blocks, shdom::RWARPS * 32, 0, stream>>>(a);
+    }
     H.launches += 1;
   }
   CK(cudaGetLastError());
@@ -2474,6 +3092,7 @@ static int levis_host(shdom_handle *hh, int species, int nrays, const float *cam
   Handle &H = hh->h;
   shdom::Plan &P = H.P;
   if (species < 0 || species >= P.npart) return fail(hh, "levis gradient: species index out of range");
+  if (H.nst != 1) return fail(hh, "levis gradient: scalar (nstokes = 1) problems only");
   if (P.ml + 1 > 32 || P.nlm > shdom::RNLM) return fail(hh, "levis gradient: at most 32 Legendre terms are supported");
   if (!H.initialized) return fail(hh, "levis gradient: the solution has not been initialized");
   if (H.grad_ipa != species) prepare_grad(H, species);
@@ -2536,7 +3155,7 @@ int shdom_render(shdom_handle *hh, int nrays, const float *camx, const float *ca
   try {
     float *d;
     size_t fb = (size_t)nrays * sizeof(float), db = (size_t)nrays * sizeof(double);
-    CK(cudaMalloc(&d, 3 * fb + 2 * db + fb));
+    CK(cudaMalloc(&d, 3 * fb + 2 * db + fb * H.nst));
     float *dx = d, *dy = d + nrays, *dz = d + 2 * (size_t)nrays;
     double *dmu = (double *)(d + 3 * (size_t)nrays), *dphi = dmu + nrays;
     float *dout = (float *)(dphi + nrays);
@@ -2546,7 +3165,7 @@ int shdom_render(shdom_handle *hh, int nrays, const float *camx, const float *ca
     CK(cudaMemcpyAsync(dmu, cammu, db, cudaMemcpyHostToDevice, H.stream));
     CK(cudaMemcpyAsync(dphi, camphi, db, cudaMemcpyHostToDevice, H.stream));
     int rc = render_impl(hh, nrays, dx, dy, dz, dmu, dphi, dout, H.stream);
-    if (!rc) CK(cudaMemcpyAsync(stokes_out, dout, fb, cudaMemcpyDeviceToHost, H.stream));
+    if (!rc) CK(cudaMemcpyAsync(stokes_out, dout, fb * H.nst, cudaMemcpyDeviceToHost, H.stream));
     CK(cudaStreamSynchronize(H.stream));
     cudaFree(d);
     if (rc) return rc;
@@ -2629,6 +3248,7 @@ int shdom_render_noalloc(shdom_handle *hh, int nrays, const float *camx, const f
     return fail(hh, "shdom_render_noalloc: at most " + std::to_string(shdom::kNoAllocMaxRays) +
                         " rays per call (got " + std::to_string(nrays) + ")");
   if (!camx || !camy || !camz || !cammu || !camphi || !stokes_out) return fail(hh, "shdom_render_noalloc: null argument");
+  if (H.nst != 1) return fail(hh, "shdom_render_noalloc: scalar (nstokes = 1) problems only");
   try {
     std::string err;
     void *base = noalloc_scratch(err);
@@ -2661,7 +3281,7 @@ int shdom_export_state(shdom_handle *hh, float *source, int *ns, float *radiance
   shdom::Plan &P = H.P;
   try {
     CK(cudaStreamSynchronize(H.stream));
-    size_t nf = (size_t)P.npts * P.nlm;
+    size_t nf = (size_t)P.npts * H.nst * P.nlm;
     if (source) CK(cudaMemcpy(source, H.source.p, nf * sizeof(float), cudaMemcpyDeviceToHost));
     if (radiance) CK(cudaMemcpy(radiance, H.radiance.p, nf * sizeof(float), cudaMemcpyDeviceToHost));
     if (ns) CK(cudaMemcpy(ns, H.ns.p, P.npts * sizeof(int), cudaMemcpyDeviceToHost));

@@ -90,6 +90,62 @@ void dm0(double x, int lmax, int m, std::vector<double> &d) {
 
 inline int jidx(int l, int m, int mm) { return (l <= mm) ? l * (l + 1) + m : (2 * mm + 1) * l - mm * mm + m; }
 
+// Wigner d^n_{m m1}(x) at its first degree n = max(m, m1) (m, m1 >= 0).
+double wig_start(double x, int m, int m1) {
+  if (m == m1) return std::pow(0.5 * (1.0 + x), m);
+  const int hi = std::max(m, m1), lo = std::min(m, m1);
+  double c = (m1 > m || ((m - m1) % 2 == 0)) ? 1.0 : -1.0;
+  for (int q = 1; q <= hi - lo; ++q) c *= std::sqrt((double)(m + m1 + q) / q);
+  return c * std::pow(std::sqrt(0.5 * (1.0 - x)), hi - lo) * std::pow(std::sqrt(0.5 * (1.0 + x)), hi + lo);
+}
+
+// d^n_{m m1}(x) for n = 0..lmax by the upward three-term recurrence in n.
+void wig(double x, int lmax, int m, int m1, std::vector<double> &d) {
+  d.assign(lmax + 1, 0.0);
+  const int n0 = std::max(m, m1);
+  if (n0 > lmax) return;
+  if (n0 == 0) {
+    d[0] = 1.0;
+    if (lmax >= 1) d[1] = x;
+    for (int n = 1; n < lmax; ++n) d[n + 1] = ((2 * n + 1) * x * d[n] - n * d[n - 1]) / (n + 1);
+    return;
+  }
+  d[n0] = wig_start(x, m, m1);
+  for (int n = n0; n < lmax; ++n) {
+    const double a = std::sqrt((double)((n + 1) * (n + 1) - m * m)) * std::sqrt((double)((n + 1) * (n + 1) - m1 * m1));
+    const double b = std::sqrt((double)(n * n - m * m)) * std::sqrt((double)(n * n - m1 * m1));
+    d[n + 1] = ((n * (n + 1.0) * x - (double)m * m1) * (2 * n + 1) / n * d[n] - b * (n + 1.0) / n * (n > n0 ? d[n - 1] : 0.0)) / a;
+  }
+}
+
+// The six generalized spherical functions of the mu part (PLMALL,
+// src/polarized/shdomsub2.f:4650-4755) in the element order I-I, Q-Q, U-U,
+// V-V, I-Q, Q-U: out [nlm][6].  With P1 = d^l_{m0}, P2 = -(d^l_{m2} +
+// d^l_{m,-2})/2, P3 = -(d^l_{m2} - d^l_{m,-2})/2 (each times
+// sqrt((2l+1)/(4 pi))), the m >= 0 terms hold (P1, P2, P2, P1, P3, P3) and
+// the m < 0 terms (P1, P2, -P2, -P1, s P3, -s P3), s = -1 for the
+// transposed (ordinate-to-harmonic) set.
+void gen6_mu(bool transpose, double x, int ml, int mm, std::vector<double> &out) {
+  const int nlm = (2 * mm + 1) * (ml + 1) - mm * (mm + 1);
+  out.assign((size_t)nlm * 6, 0.0);
+  const double fct = 1.0 / std::sqrt(2.0 * std::acos(-1.0)), sg = transpose ? -1.0 : 1.0;
+  std::vector<double> d0, dp, dm;
+  for (int m = 0; m <= mm; ++m) {
+    dm0(x, ml, m, d0);
+    wig(x, ml, m, 2, dp);
+    wig(-x, ml, m, 2, dm);
+    for (int l = m; l <= ml; ++l) {
+      const double nrm = std::sqrt(l + 0.5), dpl = dp[l] * nrm, dml = (((l + m) & 1) ? -1.0 : 1.0) * dm[l] * nrm;
+      const double p1 = fct * d0[l], p2 = -0.5 * fct * (dpl + dml), p3 = -0.5 * fct * (dpl - dml);
+      double *o = &out[(size_t)jidx(l, m, mm) * 6];
+      o[0] = p1; o[1] = p2; o[2] = p2; o[3] = p1; o[4] = p3; o[5] = p3;
+      if (m == 0) continue;
+      double *n = &out[(size_t)jidx(l, -m, mm) * 6];
+      n[0] = p1; n[1] = p2; n[2] = -p2; n[3] = -p1; n[4] = sg * p3; n[5] = -sg * p3;
+    }
+  }
+}
+
 }  // namespace
 
 void ylm_unpol(int ml, int mm, double mu, float phi, float *y) {
@@ -450,6 +506,16 @@ void build_angles(const shdom_problem &p, Plan &P) {
         }
       }
     }
+  if (p.nstokes == 3) {  // MAKE_SH_DO_COEF: CMU1 = PLMALL(.FALSE.), CMU2 = PLMALL(.TRUE.) * WTMU
+    P.cmu1p.assign((size_t)nmu * nlm * 6, 0.f); P.cmu2p.assign((size_t)nmu * nlm * 6, 0.f);
+    std::vector<double> g;
+    for (int i = 0; i < nmu; ++i) {
+      gen6_mu(false, (double)P.mu[i], P.ml, mm, g);
+      for (int q = 0; q < nlm * 6; ++q) P.cmu1p[(size_t)i * nlm * 6 + q] = (float)g[q];
+      gen6_mu(true, (double)P.mu[i], P.ml, mm, g);
+      for (int q = 0; q < nlm * 6; ++q) P.cmu2p[(size_t)i * nlm * 6 + q] = (float)g[q] * P.wtmu[i];
+    }
+  }
   P.cphi1.assign((size_t)nmu * P.nphi0max * nm, 0.f); P.cphi2.assign((size_t)nmu * P.nphi0max * nm, 0.f);
   for (int i = 0; i < nmu; ++i) {
     float w = 1.0f / P.wtmu[i];
@@ -472,16 +538,35 @@ bool build_medium(const shdom_problem &p, Plan &P) {
   const int npx = p.npx, npy = p.npy, npz = p.npz, ng = npx * npy * npz;
   const int npart = p.npart, nmic = p.maxnmicro, nq = 8 * nmic, npts = P.npts, nleg = P.nleg, ml = P.ml;
   P.npart = npart; P.numphase = p.numphase;
+  // input table: [numphase][nlegp+1], or [numphase][nlegp+1][6] (a1 a2 a3 a4 b1 b2) when polarized
+  const int nstleg = p.nstokes == 3 ? 6 : 1;
+  auto legin = [&](int i, int l, int k) { return p.legenp[((size_t)i * (p.nlegp + 1) + l) * nstleg + k]; };
   // Legendre table divided by 2l+1; with delta-M the 0..ML terms hold
   // chi_l - f (the 'N' interpolation method keeps f in term ML+1).
   std::vector<float> leg((size_t)p.numphase * (nleg + 1), 0.f);
   for (int i = 0; i < p.numphase; ++i) {
     for (int l = 0; l <= nleg && l <= p.nlegp; ++l)
-      leg[(size_t)i * (nleg + 1) + l] = p.legenp[(size_t)i * (p.nlegp + 1) + l] / (float)(2 * l + 1);
+      leg[(size_t)i * (nleg + 1) + l] = legin(i, l, 0) / (float)(2 * l + 1);
     if (p.deltam) {
       float f = leg[(size_t)i * (nleg + 1) + ml + 1];
       for (int l = 0; l <= ml; ++l) leg[(size_t)i * (nleg + 1) + l] -= f;
     }
+  }
+  // polarized elements a2, a3, b1 (PREPARE_PROP 'N': the diagonal elements
+  // lose f, the off-diagonal b1 is kept), [numphase][3][nleg+1]
+  std::vector<float> legp3;
+  if (nstleg == 6) {
+    legp3.assign((size_t)p.numphase * 3 * (nleg + 1), 0.f);
+    const int kel[3] = {1, 2, 4};
+    for (int i = 0; i < p.numphase; ++i)
+      for (int e = 0; e < 3; ++e) {
+        float *L = &legp3[((size_t)i * 3 + e) * (nleg + 1)];
+        for (int l = 0; l <= nleg && l <= p.nlegp; ++l) L[l] = legin(i, l, kel[e]) / (float)(2 * l + 1);
+        if (p.deltam && e < 2) {
+          const float f = leg[(size_t)i * (nleg + 1) + ml + 1];
+          for (int l = 0; l <= ml; ++l) L[l] -= f;
+        }
+      }
   }
   for (int k = 0; k < ng * npart * nmic; ++k)
     if (p.iphasep[k] < 1 || p.iphasep[k] > p.numphase) { P.err = "Phase function indices are out of bounds."; return false; }
@@ -588,6 +673,10 @@ bool build_medium(const shdom_problem &p, Plan &P) {
   // (src/polarized/shdomsub2.f:3113-3170).
   const int nl = ml + 1;
   P.coef.assign((size_t)npts * nl, 0.f);
+  if (nstleg == 6) P.coefp.assign((size_t)npts * 3 * nl, 0.f);
+  else P.coefp.clear();
+  std::vector<double> ltp(nstleg == 6 ? 3 * nl : 0);
+  std::vector<float> ltp1(nstleg == 6 ? 3 * nl : 0);
   P.tms_ptr.assign(npts + 1, 0);
   P.tms_iph.clear(); P.tms_w.clear();
   std::vector<float> lt1(nleg + 1);
@@ -595,6 +684,7 @@ bool build_medium(const shdom_problem &p, Plan &P) {
   for (int ipt = 0; ipt < npts; ++ipt) {
     double sumscat = 0.0;
     std::fill(lt.begin(), lt.end(), 0.0);
+    std::fill(ltp.begin(), ltp.end(), 0.0);
     float etot = P.total_ext[ipt];
     for (int ipa = 0; ipa < npart; ++ipa) {
       size_t o = (size_t)ipa * npts + ipt;
@@ -618,6 +708,20 @@ bool build_medium(const shdom_problem &p, Plan &P) {
       double scat = (double)(ext[o] * alb[o]);
       sumscat += scat;
       for (int l = 0; l <= nleg; ++l) lt[l] += scat * lt1[l];
+      if (nstleg == 6) {  // a2, a3, b1 mixed the same way (all six elements are divided by 1 - f)
+        std::fill(ltp1.begin(), ltp1.end(), 0.f);
+        for (int e = 0; e < 3; ++e) {
+          float *L1 = &ltp1[(size_t)e * nl];
+          if (single) for (int l = 0; l < nl; ++l) L1[l] = legp3[((size_t)(IP[0] - 1) * 3 + e) * (nleg + 1) + l];
+          else
+            for (int q = 0; q < nq; ++q) {
+              if (PW[q] <= 1e-5f) continue;
+              for (int l = 0; l < nl; ++l) L1[l] += legp3[((size_t)(IP[q] - 1) * 3 + e) * (nleg + 1) + l] * PW[q];
+            }
+          if (p.deltam) for (int l = 0; l < nl; ++l) L1[l] /= (1.f - f);
+          for (int l = 0; l < nl; ++l) ltp[(size_t)e * nl + l] += scat * L1[l];
+        }
+      }
       // exact single scatter: weight (albedo * ext_ipa / ext) / (1 - f) per phase function
       float wgt = (etot == 0.f) ? 1.f : ext[o] / etot;
       if (wgt != 0.f && p.deltam) {
@@ -636,6 +740,12 @@ bool build_medium(const shdom_problem &p, Plan &P) {
       if (l == 0) chi = 1.0;
       P.coef[(size_t)ipt * nl + l] = (float)(albp * chi);
     }
+    if (nstleg == 6)
+      for (int e = 0; e < 3; ++e)
+        for (int l = 0; l < nl; ++l) {
+          const double chi = (sumscat > 1e-10) ? ltp[(size_t)e * nl + l] / sumscat : ltp[(size_t)e * nl + l] / npart;
+          P.coefp[((size_t)ipt * 3 + e) * nl + l] = (float)(albp * chi);
+        }
     P.tms_ptr[ipt + 1] = (int)P.tms_iph.size();
   }
   // Eddington initial radiance per column (INIT_RADIANCE).
@@ -750,11 +860,29 @@ bool build_medium(const shdom_problem &p, Plan &P) {
     for (int i = 0; i < p.numphase; ++i) {
       double a1 = 0.0;
       for (int l = 0; l <= nlegp; ++l) {
-        float lg = (l <= p.nlegp) ? p.legenp[(size_t)i * (p.nlegp + 1) + l] : 0.f;
+        float lg = (l <= p.nlegp) ? legin(i, l, 0) : 0.f;
         a1 += (2.0 * l + 1.0) * (double)(lg / (float)(2 * l + 1)) * pl[l];
       }
       if (a1 <= 0.0) { P.err = "PRECOMPUTE_PHASE_CHECK: negative phase function"; return false; }
       P.phasetab[(size_t)j * p.numphase + i] = (float)(a1 / (4.0 * pi));
+    }
+  }
+  // polarized: the I-Q element -sum_l b1_l d^l_{20}(cos theta) / (4 pi)
+  P.phasetab2.clear();
+  if (nstleg == 6) {
+    P.phasetab2.assign((size_t)P.nscatangle * p.numphase, 0.f);
+    std::vector<double> d2;
+    for (int j = 0; j < P.nscatangle; ++j) {
+      const double x = std::cos(pi * (double)j / (P.nscatangle - 1));
+      wig(x, nlegp, 2, 0, d2);
+      for (int i = 0; i < p.numphase; ++i) {
+        double b1 = 0.0;
+        for (int l = 0; l <= nlegp; ++l) {
+          float lg = (l <= p.nlegp) ? legin(i, l, 4) : 0.f;
+          b1 -= (2.0 * l + 1.0) * (double)(lg / (float)(2 * l + 1)) * d2[l];
+        }
+        P.phasetab2[(size_t)j * p.numphase + i] = (float)(b1 / (4.0 * pi));
+      }
     }
   }
   return true;
@@ -775,7 +903,7 @@ void build_direct(const shdom_problem &p, Plan &P) {
         double f = 0;
         for (int q = 0; q < nmic; ++q) {
           int iph = p.iphasep[((size_t)ipa * ng + ip) * nmic + q];
-          float a_l = (L <= p.nlegp) ? p.legenp[(size_t)(iph - 1) * (p.nlegp + 1) + L] : 0.f;
+          float a_l = (L <= p.nlegp) ? p.legenp[((size_t)(iph - 1) * (p.nlegp + 1) + L) * (p.nstokes == 3 ? 6 : 1)] : 0.f;
           f += (double)(p.phasewtp[((size_t)ipa * ng + ip) * nmic + q] * a_l) / (2 * L + 1);
         }
         e = (1.0 - a * f) * e;
@@ -1046,6 +1174,46 @@ bool build_schedule(const shdom_problem &p, Plan &P) {
   return true;
 }
 
+// Polarized column layout: every (octant, face class) group [c0, c0+n) of
+// the scalar layout becomes [3 c0, 3 c0 + 3n) holding the group's ordinates
+// for I, then Q, then U.  A sweep segment always spans a whole group, so its
+// columns, item offsets and general-trace table offsets scale by three.
+void expand_stokes(Plan &P) {
+  const int n = P.nang;
+  std::vector<int> g0(n, -1), gn(n, 0);
+  for (int b = 0; b < 8; ++b)
+    for (int cls = 0; cls < 4; ++cls)
+      for (int c = P.cls_col0[b][cls]; c < P.cls_col0[b][cls] + P.cls_ncol[b][cls]; ++c) { g0[c] = P.cls_col0[b][cls]; gn[c] = P.cls_ncol[b][cls]; }
+  auto nc = [&](int c, int st) { return 3 * g0[c] + st * gn[c] + (c - g0[c]); };
+  std::vector<int> imu(3 * n), iphi(3 * n), oct(3 * n), cls(3 * n);
+  std::vector<float> cx(3 * n), cy(3 * n), cz(3 * n), fw(3 * n, 0.f);
+  P.col_stk.assign(3 * n, 0);
+  for (int c = 0; c < n; ++c)
+    for (int st = 0; st < 3; ++st) {
+      const int d = nc(c, st);
+      imu[d] = P.col_imu[c]; iphi[d] = P.col_iphi[c]; oct[d] = P.col_oct[c]; cls[d] = P.col_cls[c];
+      cx[d] = P.col_cx[c]; cy[d] = P.col_cy[c]; cz[d] = P.col_cz[c];
+      if (st == 0) fw[d] = P.col_fluxw[c];  // the hemispheric fluxes are fluxes of I
+      P.col_stk[d] = (uint8_t)st;
+    }
+  for (int &c : P.col_of)
+    if (c >= 0) c = nc(c, 0);
+  P.col_imu.swap(imu); P.col_iphi.swap(iphi); P.col_oct.swap(oct); P.col_cls.swap(cls);
+  P.col_cx.swap(cx); P.col_cy.swap(cy); P.col_cz.swap(cz); P.col_fluxw.swap(fw);
+  for (int b = 0; b < 8; ++b) {
+    P.oct_col0[b] *= 3; P.oct_ncol[b] *= 3;
+    for (int k = 0; k < 4; ++k) { P.cls_col0[b][k] *= 3; P.cls_ncol[b][k] *= 3; }
+  }
+  P.ncol_down *= 3;
+  P.nang = 3 * n;
+  for (int h = 0; h < 2; ++h) {
+    for (auto *v : {&P.segs[h], &P.p1segs[h]})
+      for (Seg &g : *v) { g.col0 *= 3; g.ncol *= 3; g.start *= 3; g.irr0 *= 3; }
+    for (int &x : P.level_items[h]) x *= 3;
+    P.nirr[h] *= 3; P.nitems[h] *= 3;
+  }
+}
+
 // Exit geometry of regular-point traces per (layer, ordinate): so, u, v, face.
 void build_geo(Plan &P) {
   const int nl = P.nz - 1, nang = P.nang;
@@ -1075,7 +1243,7 @@ std::string geometry_key(const shdom_problem &p) {
   put(&p.delx, sizeof(float)); put(&p.dely, sizeof(float)); put(p.zlevels, sizeof(float) * (size_t)p.npz);
   put(&p.bc_x_open, sizeof(int)); put(&p.bc_y_open, sizeof(int)); put(&p.ipflag, sizeof(int));
   put(&p.nmu, sizeof(int)); put(&p.nphi, sizeof(int)); put(&p.angle_set, sizeof(int));
-  put(&p.deltam, sizeof(int)); put(&p.transmin, sizeof(float));
+  put(&p.deltam, sizeof(int)); put(&p.transmin, sizeof(float)); put(&p.nstokes, sizeof(int));
   return k;
 }
 
@@ -1085,7 +1253,7 @@ constexpr size_t kGeomCache = 2;
 }  // namespace
 
 bool build_plan(const shdom_problem &p, Plan &P) {
-  if (p.nstokes != 1) { P.err = "only nstokes=1 is supported"; return false; }
+  if (p.nstokes != 1 && p.nstokes != 3) { P.err = "nstokes must be 1 or 3"; return false; }
   if (p.splitacc > 0) { P.err = "adaptive cell splitting is not supported (split_accuracy must be <= 0)"; return false; }
   if (p.npart < 1 || p.numphase < 1 || p.maxnmicro < 1) { P.err = "empty medium"; return false; }
   const std::string key = geometry_key(p);
@@ -1103,6 +1271,9 @@ bool build_plan(const shdom_problem &p, Plan &P) {
     build_angles(p, P);
     if (P.npts >= (1 << 28)) { P.err = "grid too large for the sweep task encoding"; return false; }
     if (!build_schedule(p, P)) return false;
+    P.nst = p.nstokes;
+    P.col_stk.assign(P.nang, 0);
+    if (P.nst == 3) expand_stokes(P);
     build_geo(P);
     auto keep = std::make_shared<const Plan>(P);
     std::lock_guard<std::mutex> lk(g_geom_mu);

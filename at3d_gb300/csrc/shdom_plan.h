@@ -67,17 +67,26 @@ struct Plan {
   int ncol_down = 0;                             // columns [0, ncol_down) are mu < 0
   int oct_col0[8] = {0}, oct_ncol[8] = {0};      // column range of each trace octant
   std::vector<float> col_cx, col_cy, col_cz;     // trace (back) direction per column
-  std::vector<float> col_fluxw;                  // |mu| * wtdo per column
+  std::vector<float> col_fluxw;                  // |mu| * wtdo per column (I columns only)
+  // Polarized problems (nst = 3) hold I, Q and U of every ordinate in
+  // separate columns: within each (octant, face class) group the group's
+  // ordinates appear three times, I then Q then U, so a sweep segment's
+  // columns keep one shared trace geometry per ordinate.
+  int nst = 1;
+  std::vector<uint8_t> col_stk;                  // [nang] Stokes component of each column (0 I, 1 Q, 2 U)
   std::vector<float> cmu1, cmu2;                 // [nmu][nlm]
+  std::vector<float> cmu1p, cmu2p;               // nst = 3: [nmu][nlm][6] generalized functions (PLMALL)
   std::vector<float> cphi1, cphi2;               // [nmu][nphi0max][2mm+1]
   std::vector<float> ylmsun;                     // [nlm]
   // ---- medium on the grid
   int npart = 0, numphase = 0;
   std::vector<float> total_ext, dirflux;
   std::vector<float> coef;                       // [npts][ml+1]: albedo * delta-M scaled Legendre term
+  std::vector<float> coefp;                      // nst = 3: [npts][3][ml+1] the same for a2, a3 and b1
   std::vector<int> tms_ptr, tms_iph;             // CSR per point: exact single-scatter mixture
   std::vector<float> tms_w;
   std::vector<float> phasetab;                   // [nscatangle][numphase]
+  std::vector<float> phasetab2;                  // nst = 3: [nscatangle][numphase] the I-Q element
   int nscatangle = 0;
   float albmax = 0.f;
   std::vector<float> rad0;                       // [npts][4] Eddington initial radiance

@@ -49,6 +49,8 @@ struct Epilogue {
   int *err;
   int split;
   const int *rowmap;  // output point of each A row (A holds a compacted subset of the points), or null
+  const uint8_t *stk; // mode 0: Stokes component per output column (only I, 0, is clamped), or null (all I)
+  int ldr;            // mode 1: row stride of R (nlm, or 3 nlm for I, Q, U rows); columns are masked by (col mod nlm) < nr
 };
 
 __device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -370,8 +372,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_gemm(const __grid_constant__
 #pragma unroll
             for (int j = 0; j < HALF; j += 4) {
               const int col = cb + j;
-              const float4 v = make_float4(fmaxf(acc[j], 0.f), fmaxf(acc[j + 1], 0.f), fmaxf(acc[j + 2], 0.f),
-                                           fmaxf(acc[j + 3], 0.f));
+              float4 v = make_float4(fmaxf(acc[j], 0.f), fmaxf(acc[j + 1], 0.f), fmaxf(acc[j + 2], 0.f),
+                                     fmaxf(acc[j + 3], 0.f));
+              if (g.stk) {  // polarized: the Q and U ordinate sources keep their sign
+                if (col < g.N && g.stk[col]) v.x = acc[j];
+                if (col + 1 < g.N && g.stk[col + 1]) v.y = acc[j + 1];
+                if (col + 2 < g.N && g.stk[col + 2]) v.z = acc[j + 2];
+                if (col + 3 < g.N && g.stk[col + 3]) v.w = acc[j + 3];
+              }
               if (col + 3 < g.N) {
                 *reinterpret_cast<float4 *>(out + col) = v;  // col and ldc are multiples of 4
               } else {
@@ -382,11 +390,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_gemm(const __grid_constant__
             }
           } else {
             const int nrp = g.nr[row];
-            float *out = g.R + (size_t)row * g.nlm;
+            float *out = g.R + (size_t)row * (g.ldr ? g.ldr : g.nlm);
 #pragma unroll
             for (int j = 0; j < HALF; ++j) {
               const int col = cb + j;
-              if (col < g.nlm) out[col] = (col < nrp) ? acc[j] : 0.f;
+              const int jt = col < g.nlm ? col : col % g.nlm;
+              if (col < g.N) out[col] = (jt < nrp) ? acc[j] : 0.f;
             }
           }
         }

@@ -13,6 +13,12 @@ distributions of the workload descriptions:
   Gaussian random field thresholded to 30% cloud fraction, in-cloud
   lognormal extinction (mean 30/km, log-sigma 0.5), per-wavelength ssa and
   HG g from the four-wavelength set, 128 Legendre terms.
+* ``polarized_blob``: NSTOKES=3 scene on a 64x64x40 periodic grid with the
+  geometry of ``cloud_blob`` (dx=dy=0.02 km, dz=0.04 km), NMU=8/NPHI=16; the
+  blob extinction field of ``cloud_blob`` (seeded); one phase matrix of six
+  64-term Wigner-function series, the 50/50 mix of a Rayleigh matrix and a
+  Henyey-Greenstein-derived matrix (g=0.8, linear depolarisation 0.03);
+  Lambertian albedo 0.1, sun zenith 45 deg.
 * ``orthographic_views``: parallel rays on a regular pixel grid at the domain
   top for a list of view zenith angles in the azimuth-0 plane; mu and phi
   point towards the sensor (at3d/sensor.py:44-47 convention).
@@ -22,7 +28,7 @@ from __future__ import annotations
 import numpy as np
 
 from ._abi import NumericalParams, Problem, Species
-from .medium import henyey_greenstein_legcoef, rayleigh_legcoef
+from .medium import henyey_greenstein_legcoef, hg_matrix_legcoef6, rayleigh_legcoef, rayleigh_legcoef6
 
 VIEW_ZENITHS = (0.0, 26.1, -26.1, 45.6, -45.6, 60.0, -60.0, 70.5, -70.5)
 FIELD_SSA = (0.99999, 0.9999, 0.999, 0.99)
@@ -51,6 +57,34 @@ def cloud_blob(seed: int = 1, nx: int = 32, ny: int = 32, nz: int = 24, dx: floa
     return Problem(delx=dx, dely=dx, zlevels=z, species=[cloud, rayleigh],
                    solarmu=-float(np.cos(np.deg2rad(30.0))), solaraz=0.0, solarflux=1.0,
                    surface_albedo=0.05, params=params)
+
+
+def polarized_matrix(nterms: int = 64, g: float = 0.8, depol: float = 0.03) -> np.ndarray:
+    """[6, nterms] phase matrix: 0.5 Rayleigh + 0.5 HG-derived (a1 a2 a3 a4 b1 b2)."""
+    ray = np.zeros((6, nterms), np.float32)
+    ray[:, :3] = rayleigh_legcoef6(depol)
+    return (0.5 * ray + 0.5 * hg_matrix_legcoef6(g, depol, nterms)).astype(np.float32)
+
+
+def polarized_blob(seed: int = 1, nx: int = 64, ny: int = 64, nz: int = 40, dx: float = 0.02,
+                   dz: float = 0.04, boundary: str = "periodic", nmu: int = 8, nphi: int = 16,
+                   solacc: float = 1e-5, ssa: float = 0.999999) -> Problem:
+    rng = np.random.default_rng(seed)
+    x = np.arange(nx) * dx
+    y = np.arange(ny) * dx
+    z = (np.arange(nz) * dz).astype(np.float32)
+    cx, cy, cz = nx * dx / 2, ny * dx / 2, z[-1] / 2
+    X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
+    r2 = (X - cx) ** 2 + (Y - cy) ** 2 + (Z - cz) ** 2
+    ln = rng.lognormal(mean=0.0, sigma=0.3, size=(nx, ny, nz))
+    ext = (20.0 * np.exp(-r2 / (2 * 0.15 ** 2)) * ln).astype(np.float32)
+    cloud = Species(extinction=ext, ssalb=np.full_like(ext, ssa), legcoef=polarized_matrix())
+    params = NumericalParams(num_mu_bins=nmu, num_phi_bins=nphi, solution_accuracy=solacc,
+                             split_accuracy=0.0, x_boundary_condition=boundary,
+                             y_boundary_condition=boundary)
+    return Problem(delx=dx, dely=dx, zlevels=z, species=[cloud],
+                   solarmu=-float(np.cos(np.deg2rad(45.0))), solaraz=0.0, solarflux=1.0,
+                   surface_albedo=0.1, params=params, num_stokes=3)
 
 
 def powerlaw_field(rng, shape, fraction: float):

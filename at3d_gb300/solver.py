@@ -88,14 +88,15 @@ class RTE:
 
     def __init__(self, numerical_params: NumericalParams, medium: dict, source, surface, grid,
                  num_stokes: int = 1, name: str | None = None, device: int = 0):
-        if num_stokes != 1:
-            raise ValueError("num_stokes must be 1 (scalar radiance)")
+        if num_stokes not in (1, 3):
+            raise ValueError("num_stokes must be 1 (scalar radiance) or 3 (I, Q, U)")
         species = list(medium.values())
         sa = surface.albedo
         self.problem = Problem(delx=grid.delx, dely=grid.dely, zlevels=np.asarray(grid.z, np.float32),
                                species=species, solarmu=source.solarmu, solaraz=source.solaraz,
                                solarflux=source.solarflux, skyrad=source.skyrad, surface_albedo=sa,
-                               surface_delx=surface.delx, surface_dely=surface.dely, params=numerical_params)
+                               surface_delx=surface.delx, surface_dely=surface.dely, params=numerical_params,
+                               num_stokes=num_stokes)
         self.name = name or f"Radiance {source.wavelength:1.3f} micron"
         self._create(device)
 
@@ -205,19 +206,27 @@ class RTE:
 
     def integrate_to_sensor(self, sensor: dict, single_scatter: bool = False, nosurface: bool = False) -> dict:
         """Radiance along the sensor's rays (at3d/solver.py:633-791); writes
-        sensor['I'] and returns the sensor."""
+        sensor['I'] (and 'Q', 'U' for a polarized solve) and returns the sensor."""
         if single_scatter or nosurface:
             raise NotImplementedError("single_scatter / nosurface rendering is not supported")
         self.check_solved(verbose=False)
         out = self.render(sensor["ray_x"], sensor["ray_y"], sensor["ray_z"], sensor["ray_mu"], sensor["ray_phi"])
-        sensor["I"] = out
+        if out.ndim == 1:
+            sensor["I"] = out
+        else:
+            sensor["I"], sensor["Q"], sensor["U"] = out[:, 0].copy(), out[:, 1].copy(), out[:, 2].copy()
         return sensor
+
+    @property
+    def num_stokes(self) -> int:
+        return int(self.problem.num_stokes)
 
     def render(self, x, y, z, mu, phi) -> np.ndarray:
         x = np.ascontiguousarray(x, np.float32); y = np.ascontiguousarray(y, np.float32)
         z = np.ascontiguousarray(z, np.float32)
         mu = np.ascontiguousarray(mu, np.float64); phi = np.ascontiguousarray(phi, np.float64)
-        out = np.zeros(len(x), np.float32)
+        nst = self.num_stokes
+        out = np.zeros(len(x) if nst == 1 else (len(x), nst), np.float32)  # Stokes fastest, as STOKES(NSTOKES, NPIX)
         dp = C.POINTER(C.c_double)
         _check(self._h, _lib.lib().shdom_render(self._h, len(x), _fp(x), _fp(y), _fp(z), mu.ctypes.data_as(dp),
                                                  phi.ctypes.data_as(dp), _fp(out)))
@@ -233,8 +242,9 @@ class RTE:
 
     def export_state(self) -> dict:
         s = self.sizes
-        n, nlm = s["npts"], s["nlm"]
-        src = np.zeros((n, nlm), np.float32); rad = np.zeros((n, nlm), np.float32)
+        n, nlm, nst = s["npts"], s["nlm"], s["nstokes"]
+        shape = (n, nlm) if nst == 1 else (n, nst, nlm)
+        src = np.zeros(shape, np.float32); rad = np.zeros(shape, np.float32)
         ns = np.zeros(n, np.int32); nr = np.zeros(n, np.int32)
         flx = np.zeros((n, 2), np.float32); dfl = np.zeros(n, np.float32)
         ip = C.POINTER(C.c_int)

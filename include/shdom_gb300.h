@@ -42,6 +42,7 @@ typedef struct shdom_sizes {
     float albmax;
     long long launches; /* kernels launched on this handle since creation */
     long long device_bytes; /* device memory the handle holds (estimate before creation) */
+    int nstokes;   /* Stokes components (1, or 3 for I, Q, U) */
 } shdom_sizes;
 
 /* Builds the grid, the cell structure, the sweep schedule and the medium on
@@ -88,7 +89,8 @@ int shdom_solution_iterations(shdom_handle *h, int maxiter, int *iters, float *s
  * positions are single precision and directions double precision as in the
  * reference's RENDER interface (src/polarized/shdomsub4.f:164-165); mu/phi
  * point towards the sensor.  Replaces core.render (at3d/solver.py:681-759).
- * stokes_out: [nrays] (Stokes I). */
+ * stokes_out: [nrays][nstokes] (Stokes I, or I, Q, U in the meridional
+ * plane of the outgoing direction, the reference's STOKES(NSTOKES,NPIX)). */
 int shdom_render(shdom_handle *h, int nrays, const float *camx, const float *camy, const float *camz,
                  const double *cammu, const double *camphi, float *stokes_out);
 
@@ -109,7 +111,7 @@ int shdom_render_device(shdom_handle *h, int nrays, const float *camx, const flo
  * 'table' derivative method.  gradient: [npx*npy*npz][2] (d/d extinction,
  * d/d albedo) in the property-grid order (z fastest); cost and stokes_out
  * (the rendered radiances, [nrays]) may be NULL.  The solution is frozen:
- * call after shdom_solution_iterations. */
+ * call after shdom_solution_iterations.  Scalar (nstokes = 1) problems. */
 int shdom_levis_gradient(shdom_handle *h, int species, int nrays, const float *camx, const float *camy,
                          const float *camz, const double *cammu, const double *camphi,
                          const float *measurements, double *gradient, double *cost, float *stokes_out);
@@ -124,7 +126,7 @@ int shdom_levis_adjoint(shdom_handle *h, int species, int nrays, const float *ca
                         double *gradient);
 
 /* shdom_render for callers that cannot allocate device memory during the
- * call.  It has no counterpart in the reference.  The rays and radiances of
+ * call (scalar problems).  It has no counterpart in the reference.  The rays and radiances of
  * the call are staged in one fixed device array inside the library (2 MiB)
  * instead of memory allocated per call, so at most 65536 rays per call are
  * accepted; more is refused with an error.  The array is shared by every
@@ -137,7 +139,7 @@ int shdom_render_noalloc(shdom_handle *h, int nrays, const float *camx, const fl
                          const float *camz, const double *cammu, const double *camphi, float *stokes_out);
 
 /* Solution state export (RTE.save_solution fields, at3d/solver.py:1621-1686)
- * in a dense layout: source/radiance [npts][nlm] with the terms beyond each
+ * in a dense layout: source/radiance [npts][nstokes][nlm] with the terms beyond each
  * point's truncation set to zero, ns/nr the truncations (SHPTR/RSHPTR
  * differences), fluxes [npts][2] (down, up) and dirflux [npts].  Any output
  * pointer may be NULL. */

@@ -79,14 +79,31 @@ def test_unsupported_problems_are_refused(kw, msg):
         plan_summary(pb)
 
 
-def test_vector_radiance_is_refused(lib):
+def test_circular_polarization_is_refused(lib):
     from at3d_gb300._lib import ShdomSizes
     from at3d_gb300.scenes import cloud_blob
     st = cloud_blob(nx=8, ny=8, nz=6).to_struct()
-    st.nstokes = 3
+    st.nstokes = 4
     out = ShdomSizes()
     assert lib.shdom_plan_summary(C.byref(st), C.byref(out)) == 1
     assert b"nstokes" in lib.shdom_last_error(None)
+
+
+def test_polarized_plan(lib):
+    """NSTOKES=3 plans: the same grid and schedule as the scalar problem,
+    three Stokes columns per ordinate and Stokes rows of harmonics."""
+    from at3d_gb300.scenes import polarized_blob
+    from at3d_gb300.solver import plan_summary
+    pb = polarized_blob(nx=12, ny=12, nz=10)
+    s3 = plan_summary(pb)
+    pb1 = dataclasses.replace(pb, num_stokes=1, species=[dataclasses.replace(pb.species[0],
+                                                                             legcoef=pb.species[0].legcoef[0])])
+    s1 = plan_summary(pb1)
+    assert s3["nstokes"] == 3 and s1["nstokes"] == 1
+    for k in ("npts", "nlm", "nang", "nlevels_down", "nlevels_up"):
+        assert s3[k] == s1[k]
+    assert s3["nang"] == 90 and s3["nlm"] == 64
+    assert s3["device_bytes"] > s1["device_bytes"]
 
 
 def test_null_arguments(lib):
