@@ -3156,9 +3156,9 @@ int shdom_render(shdom_handle *hh, int nrays, const float *camx, const float *ca
     float *d;
     size_t fb = (size_t)nrays * sizeof(float), db = (size_t)nrays * sizeof(double);
     CK(cudaMalloc(&d, 3 * fb + 2 * db + fb * H.nst));
-    float *dx = d, *dy = d + nrays, *dz = d + 2 * (size_t)nrays;
-    double *dmu = (double *)(d + 3 * (size_t)nrays), *dphi = dmu + nrays;
-    float *dout = (float *)(dphi + nrays);
+    // the double arrays first: every array starts on its own element size for any nrays
+    double *dmu = (double *)d, *dphi = dmu + nrays;
+    float *dx = (float *)(dphi + nrays), *dy = dx + nrays, *dz = dy + nrays, *dout = dz + nrays;
     CK(cudaMemcpyAsync(dx, camx, fb, cudaMemcpyHostToDevice, H.stream));
     CK(cudaMemcpyAsync(dy, camy, fb, cudaMemcpyHostToDevice, H.stream));
     CK(cudaMemcpyAsync(dz, camz, fb, cudaMemcpyHostToDevice, H.stream));

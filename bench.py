@@ -326,6 +326,77 @@ def gradient_block(args, dev):
             "note": "host buffers in and out (rays, measurements, gradient), wall clock"}
 
 
+def polarized_block(args, dev):
+    """The polarized workload (NSTOKES=3): 64x64x40 grid with the cloud-blob
+    geometry, NMU=8/NPHI=16, one six-element phase matrix (Rayleigh +
+    HG-derived mix), Lambertian albedo 0.1, sun zenith 45 deg; Stokes I, Q, U
+    on 64x64 pixels x 9 views.  Periodic boundaries (the stated
+    configuration) and open boundaries.  For each transform arithmetic: a
+    full solve (initialisation to convergence) plus the render, timed with
+    CUDA events after a warm-up solve, inputs resident; the render alone;
+    and the relative RMS of the I, Q, U images against the FP32 mode
+    (normalised by the RMS of I).  With the CPU baseline: the polarized
+    oracle, initialisation plus one iteration scaled to the solve's
+    iterations, single thread."""
+    import torch
+    from at3d_gb300.scenes import orthographic_views, polarized_blob
+    from at3d_gb300.solver import RTE
+    out = {"workload": "NSTOKES=3 64x64x40 blob (dx=dy=0.02 km, dz=0.04 km), NMU=8 NPHI=16, "
+                       "64x64 px x 9 views (I, Q, U)", "boundaries": {}}
+    for bc in ("periodic", "open"):
+        pb = polarized_blob(boundary=bc)
+        rays = orthographic_views(pb, 64, 64)
+        nr = len(rays[0])
+        d = [torch.tensor(np.asarray(r), dtype=torch.float32 if i < 3 else torch.float64, device="cuda")
+             for i, r in enumerate(rays)]
+        img = torch.empty(nr * 3, dtype=torch.float32, device="cuda")
+        res = {}
+        for mode in ("fp32", "tf32x3"):
+            r = RTE.from_problem(pb, device=dev)
+            r.set_transform_mode(mode)
+            ptrs = (d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), d[3].data_ptr(), d[4].data_ptr(), img.data_ptr())
+            r.solve(3, verbose=False)
+            r.render_device(*ptrs, nr, 0)
+            torch.cuda.synchronize()
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            e[0].record()
+            it, sc = r.solve(args.maxiter, verbose=False)
+            e[1].record()
+            r.render_device(*ptrs, nr, 0)
+            e[2].record()
+            torch.cuda.synchronize()
+            t_solve, t_render = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+            res[mode] = {"iterations": it, "solcrit": sc, "ms_solve": t_solve, "ms_render": t_render,
+                         "solves_per_s": 1e3 / (t_solve + t_render), "render_rays_per_s": nr / (t_render / 1e3),
+                         "img": img.view(nr, 3).cpu().numpy().copy()}
+            r.close()
+        ref = res["fp32"]["img"]
+        den = float(np.sqrt(np.mean(ref[:, 0].astype(np.float64) ** 2)))
+        entry = {}
+        for mode, v in res.items():
+            dif = v.pop("img") - ref
+            v["relrms_vs_fp32_iqu"] = [float(np.sqrt(np.mean(dif[:, k].astype(np.float64) ** 2)) / den) for k in range(3)]
+            entry[mode] = v
+        entry["rays"] = nr
+        entry["mean_iqu"] = [float(np.mean(ref[:, k])) for k in range(3)]
+        out["boundaries"][bc] = entry
+    if not args.no_cpu_baseline:
+        from oracle.oracle import Oracle
+        pb = polarized_blob(boundary="periodic")
+        t0 = time.perf_counter()
+        o = Oracle(pb)
+        o.init_solution()
+        t1 = time.perf_counter()
+        o.solve(1)
+        t2 = time.perf_counter()
+        its = out["boundaries"]["periodic"]["fp32"]["iterations"]
+        t = (t1 - t0) + its * (t2 - t1)
+        out["cpu_baseline"] = {"value": 1.0 / t, "unit": "solves/s", "cores": 1, "kind": "port",
+                               "sample": f"polarized oracle on the periodic grid: initialisation ({t1 - t0:.1f} s) "
+                                         f"plus one iteration ({t2 - t1:.1f} s), scaled to {its} iterations"}
+    return out
+
+
 def serving_block(args, dev):
     """A Poisson stream of mixed requests through the continuous-admission
     loop (at3d_gb300.serving): grids 32x32x24 to 128x128x64, NMU/NPHI 8/16
@@ -445,6 +516,7 @@ def main():
         dev = int(os.environ.get("LOCAL_RANK", "0"))
         extras["precision"] = precision_block(args, dev)
         extras["gradient"] = gradient_block(args, dev)
+        extras["polarized"] = polarized_block(args, dev)
         extras["serving"] = serving_block(args, dev)
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:

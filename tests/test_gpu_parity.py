@@ -171,3 +171,15 @@ def test_device_error_is_reported_and_handle_stays_usable(rte_cls):
         r.render(x, y, z, mu, phi)
     again = r.render(*rays)
     assert np.array_equal(again, good)
+
+
+def test_odd_ray_count(rte_cls):
+    """Host-buffer renders of any ray count (the staged double arrays stay
+    8-byte aligned): an odd count equals the leading rays of an even one."""
+    pb = cloud_blob(nx=12, ny=12, nz=10, dz=0.08)
+    r = rte_cls.from_problem(pb)
+    r.solve(20, verbose=False)
+    rays = orthographic_views(pb, 8, 8, (0.0, 26.1))
+    full = r.render(*rays)
+    odd = r.render(*(np.asarray(a)[:127] for a in rays))
+    assert np.array_equal(odd, full[:127])

@@ -15,6 +15,8 @@ import pytest
 from at3d_gb300.medium import hg_matrix_legcoef6
 from at3d_gb300.scenes import VIEW_ZENITHS, cloud_blob, orthographic_views, polarized_blob
 from oracle.oracle import Oracle
+from rico_scene import rico_golden, rico_problem, rico_rays
+from test_oracle_polarized import golden_checks
 
 pytestmark = pytest.mark.gpu
 
@@ -94,3 +96,22 @@ def test_scalar_limit(rte_cls):
     a, b = r3.render(*rays), r1.render(*rays)
     assert np.all(a[:, 1:] == 0.0)
     assert rms(a[:, 0] - b) / rms(b) < 2e-5
+
+
+def test_reference_golden_rico(rte_cls):
+    """The reference's polarized verification scene: the GPU solve against
+    the original SHDOM output (bars of tests/test_oracle_polarized.py, which
+    explains the adaptive-splitting difference) and against the oracle."""
+    pb = rico_problem()
+    r = rte_cls.from_problem(pb)
+    it, sc = r.solve(100, verbose=False)
+    assert sc <= 1e-4
+    rays = rico_rays()
+    img = r.render(*rays)
+    golden_checks(img, rico_golden())
+    o = Oracle(pb)
+    o.solve(100)
+    b = o.render(*rays, nthreads=8)
+    den = rms(b[:, 0])
+    for k in range(3):
+        assert rms(img[:, k] - b[:, k]) / den < 1e-4, k

@@ -1,9 +1,18 @@
 """Pins the polarized (NSTOKES = 3) CPU oracle.
 
-The reference's own polarized golden output (tests/data/rico32x36x26w672ar.out)
-was computed with adaptive cell splitting, which this path leaves out, so the
-restatement is pinned by two properties the reference's equations fix
-exactly:
+Against the reference's own polarized golden output (tests/data/
+rico32x36x26w672ar.out of the reference, Stokes I, Q, U of the Verify_Solver
+scene, tests/test_shdom.py:175-261), stored with its property file as
+tests/golden/rico32x36x26w672_pol.npz by
+tests/golden/make_rico_polarized_fixture.py.  That output was computed with
+adaptive cell splitting (SPLITTING_ACCURACY 0.1 added 1705 points to the
+31104 of the base grid), which this path leaves out, so the comparison is
+not exact: the bar is the reference test's own at3d-vs-SHDOM tolerances
+(atol 3e-3, 2e-4, 7e-5 for I, Q, U) for at least 90% / 95% / 95% of the
+12455 rays, relative RMS within 2.5% (I) and 4% (Q, U), and correlation
+above 0.999 with each golden image, which fixes the sign and rotation
+conventions of Q and U.  Two properties that the reference's equations fix
+exactly pin the restatement further:
 
 * the scalar limit: with b1 = 0 no polarization is created, Q and U stay
   zero, and I equals the scalar solution (CALC_SOURCE_PNT,
@@ -24,6 +33,7 @@ from at3d_gb300 import scenes
 from at3d_gb300._abi import NumericalParams, Problem, Species
 from at3d_gb300.medium import hg_matrix_legcoef6, rayleigh_legcoef6
 from oracle.oracle import Oracle
+from rico_scene import rico_golden, rico_problem, rico_rays
 
 
 def _blob():
@@ -97,3 +107,21 @@ def test_fp32_matches_fp64():
     for k in range(3):
         den = np.sqrt(np.mean(b[:, 0] ** 2))
         assert np.sqrt(np.mean((a[:, k] - b[:, k]) ** 2)) / den < 1e-4
+
+
+def golden_checks(img, gold):
+    atol = (3e-3, 2e-4, 7e-5)
+    within = (0.90, 0.95, 0.95)
+    rel = (0.025, 0.04, 0.04)
+    for k in range(3):
+        d = np.asarray(img[:, k], np.float64) - gold[:, k]
+        assert np.mean(np.abs(d) <= atol[k]) >= within[k], k
+        assert np.sqrt(np.mean(d ** 2)) / np.sqrt(np.mean(gold[:, k].astype(np.float64) ** 2)) < rel[k], k
+        assert np.corrcoef(img[:, k], gold[:, k])[0, 1] > 0.999, k
+
+
+def test_reference_golden_rico():
+    o = Oracle(rico_problem())
+    it, sc = o.solve(100)
+    assert sc <= 1e-4
+    golden_checks(o.render(*rico_rays(), nthreads=8), rico_golden())
