@@ -36,6 +36,7 @@ class ShdomProblem(C.Structure):
         ("tautol", C.c_double), ("transcut", C.c_double),
         ("transmin", C.c_float),
         ("nstokes", C.c_int),
+        ("sfc_brdf", C.c_int), ("nsfcpar", C.c_int), ("sfc_params", _f),
     ]
 
 
@@ -96,6 +97,8 @@ class Problem:
     surface_dely: float = 0.0
     params: NumericalParams = field(default_factory=NumericalParams)
     num_stokes: int = 1               # 1 (scalar) or 3 (I, Q, U)
+    surface_brdf: str = ""            # '' Lambertian (surface_albedo), or 'R' / 'W' with surface_params
+    surface_params: np.ndarray | None = None  # [nxsfc, nysfc, nparams] on (surface_delx, surface_dely)
     _keep: list = field(default_factory=list, repr=False)
 
     @property
@@ -182,6 +185,18 @@ class Problem:
             st.sfc_albedo = _fp(buf)
             st.gndalbedo = float(sa2.mean())
         st.gndtemp = 288.0
+        if self.surface_brdf:
+            par = np.asarray(self.surface_params, np.float32)
+            if par.ndim != 3:
+                raise ValueError("surface_params is [nxsfc, nysfc, nparams]")
+            buf = np.ascontiguousarray(par.transpose(1, 0, 2), np.float32)  # [nysfc][nxsfc][nparams]
+            keep.append(buf)
+            st.sfc_brdf = ord(self.surface_brdf)
+            st.nsfcpar = par.shape[2]
+            st.sfc_params = _fp(buf)
+            st.sfc_variable = 0
+            st.nxsfc, st.nysfc = par.shape[0], par.shape[1]
+            st.delxsfc, st.delysfc = self.surface_delx, self.surface_dely
         st.nmu, st.nphi, st.angle_set = p.num_mu_bins, p.num_phi_bins, p.angle_set
         st.deltam, st.accelflag = int(p.deltam), int(p.acceleration_flag)
         st.highorderrad, st.iterfixsh = int(p.high_order_radiance), p.iterfixsh

@@ -1,4 +1,7 @@
-"""Lambertian surfaces (at3d.surface.lambertian, at3d/surface.py:28-105)."""
+"""Surfaces: Lambertian (at3d.surface.lambertian, at3d/surface.py:28-105)
+and bidirectional ones -- RPV_unpolarized (at3d/surface.py:404-480) and
+wave_fresnel (:106-203) -- with fixed or spatially varying parameters on a
+surface grid of spacing (delx, dely)."""
 from __future__ import annotations
 
 from dataclasses import dataclass
@@ -27,3 +30,40 @@ def lambertian(albedo, ground_temperature=298.15, delx=None, dely=None) -> Lambe
             raise ValueError("dely and delx must be defined for variable surface parameters.")
         return LambertianSurface(np.atleast_2d(a), float(ground_temperature), float(delx), float(dely))
     return LambertianSurface(float(a.reshape(-1)[0]), float(ground_temperature))
+
+
+@dataclass
+class BRDFSurface:
+    """A bidirectional surface: ``kind`` 'R' (RPV: rho0, k, theta) or 'W'
+    (wave-Fresnel: real index, imaginary index, wind speed in m/s), with
+    ``params`` of shape [nxsfc, nysfc, nparams]."""
+    kind: str
+    params: np.ndarray
+    ground_temperature: float = 298.15
+    delx: float = 0.0
+    dely: float = 0.0
+
+
+def _stack(*arrays, delx, dely):
+    arrs = [np.atleast_2d(np.asarray(a, np.float32)) for a in arrays]
+    shape = np.broadcast_shapes(*[a.shape for a in arrs])
+    if any(a.size > 1 and a.shape != shape for a in arrs):
+        raise ValueError("all surface parameters must have the same shape")
+    par = np.stack([np.broadcast_to(a, shape) for a in arrs], axis=-1).astype(np.float32)
+    if par.shape[0] * par.shape[1] > 1 and (delx is None or dely is None):
+        raise ValueError("dely and delx must be defined for variable surface parameters.")
+    return par, float(delx or 1.0), float(dely or 1.0)
+
+
+def RPV_unpolarized(RHO0, K, THETA, ground_temperature=298.15, delx=None, dely=None) -> BRDFSurface:
+    """Rahman-Pinty-Verstraete BRDF (scalar problems only)."""
+    par, dx, dy = _stack(RHO0, K, THETA, delx=delx, dely=dely)
+    return BRDFSurface("R", par, float(ground_temperature), dx, dy)
+
+
+def wave_fresnel(real_refractive_index, imaginary_refractive_index, surface_wind_speed,
+                 ground_temperature=298.15, delx=None, dely=None) -> BRDFSurface:
+    """Polarized Fresnel reflection of a wind-roughened dielectric surface."""
+    par, dx, dy = _stack(real_refractive_index, imaginary_refractive_index, surface_wind_speed,
+                         delx=delx, dely=dely)
+    return BRDFSurface("W", par, float(ground_temperature), dx, dy)

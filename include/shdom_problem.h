@@ -60,7 +60,18 @@ typedef struct shdom_problem {
     float solacc, shacc, splitacc; /* splitacc must be <= 0 (no adaptive splitting) */
     double tautol, transcut;
     float transmin;
-    int nstokes;                   /* 1 (scalar) */
+    int nstokes;                   /* 1 (scalar) or 3 (I, Q, U); with 3, legenp is
+                                      [numphase][nlegp+1][6] (a1 a2 a3 a4 b1 b2 fastest) */
+    /* ---- bidirectional surface reflection (at3d/surface.py RPV_unpolarized,
+     *      wave_fresnel, diner; VARIABLE_BRDF_SURFACE
+     *      src/polarized/shdomsub1.f:2592-2664).  When sfc_brdf != 0 it
+     *      replaces the Lambertian surface; the parameters live on the
+     *      nxsfc x nysfc surface grid (delxsfc, delysfc, periodic) ---- */
+    int sfc_brdf;                  /* 0, 'R' (RPV: rho0, k, theta), 'W' (wave-Fresnel:
+                                      real and imaginary index, wind speed m/s), 'D'
+                                      (Diner: a, k, b, zeta, sigma) */
+    int nsfcpar;                   /* parameters per surface grid point */
+    const float *sfc_params;       /* [nysfc][nxsfc][nsfcpar] */
 } shdom_problem;
 
 #ifdef __cplusplus

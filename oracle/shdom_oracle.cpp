@@ -29,6 +29,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -232,6 +233,12 @@ struct Solver {
   // boundaries
   std::vector<int> topp, botp;
   std::vector<R> sfcgridalb;  // per bottom point
+  // bidirectional surface: type ('R', 'W'; 0 Lambertian), parameters on the
+  // surface grid and at the bottom points, and the downwelling radiances at
+  // the bottom points for every downward ordinate [nbot][nang/2][nst]
+  int brdf = 0, nsfcpar = 0;
+  std::vector<float> sfcpar;
+  std::vector<R> botpar, bcdown;
   std::vector<R> bcrad_top, bcrad_bot;
   bool sweep_ready = false;
 
@@ -249,6 +256,16 @@ struct Solver {
     nstleg = nst == 1 ? 1 : 6;
     legp.assign(p.legenp, p.legenp + (size_t)p.numphase * (p.nlegp + 1) * nstleg);
     if (p.sfc_variable) sfcalb.assign(p.sfc_albedo, p.sfc_albedo + (size_t)p.nxsfc * p.nysfc);
+    brdf = p.sfc_brdf; nsfcpar = p.nsfcpar;
+    if (brdf) {
+      if ((brdf != 'R' && brdf != 'W') || p.nsfcpar < 3 || !p.sfc_params || p.nxsfc < 1 || p.nysfc < 1) {
+        err = "surface BRDF: types 'R' (RPV) and 'W' (wave-Fresnel) with 3 parameters on a surface grid";
+        return false;
+      }
+      if (brdf == 'R' && nst != 1) { err = "RPV BRDF is only for unpolarized case"; return false; }
+      sfcpar.assign(p.sfc_params, p.sfc_params + (size_t)p.nxsfc * p.nysfc * p.nsfcpar);
+    }
+    p.sfc_params = nullptr;
     p.zlevels = nullptr; p.extinctp = p.albedop = p.phasewtp = p.legenp = p.sfc_albedo = nullptr;
     p.iphasep = nullptr;
     if (p.splitacc > 0) { err = "adaptive splitting is not supported"; return false; }
@@ -1160,6 +1177,140 @@ struct Solver {
                             u * (1 - v) * G(ix + 1, iy) + u * v * G(ix + 1, iy + 1));
       }
     }
+    if (brdf) brdf_parameters();
+  }
+
+  // SURFACE_PARM_INTERP (src/polarized/shdomsub1.f:2218-2268) of the BRDF
+  // parameters from the periodic surface grid to the bottom points.
+  void brdf_parameters() {
+    const int nxs = p.nxsfc, nys = p.nysfc, np_ = nsfcpar;
+    botpar.assign(botp.size() * np_, 0);
+    auto G = [&](int x, int y, int j) {
+      return sfcpar[((size_t)((y - 1) % nys) * nxs + ((x - 1) % nxs)) * np_ + j];
+    };
+    for (size_t b = 0; b < botp.size(); ++b) {
+      int i = botp[b];
+      float rx = gridpos[3 * i] / p.delxsfc, ry = gridpos[3 * i + 1] / p.delysfc;
+      int ix = std::max(1, std::min(nxs, (int)rx + 1)), iy = std::max(1, std::min(nys, (int)ry + 1));
+      float u = std::max(0.0f, std::min(1.0f, rx - (ix - 1))), v = std::max(0.0f, std::min(1.0f, ry - (iy - 1)));
+      for (int j = 0; j < np_; ++j)
+        botpar[b * np_ + j] = (R)((1 - u) * (1 - v) * G(ix, iy, j) + (1 - u) * v * G(ix, iy + 1, j) +
+                                  u * (1 - v) * G(ix + 1, iy, j) + u * v * G(ix + 1, iy + 1, j));
+    }
+  }
+
+  // SURFACE_BRDF (src/polarized/shdomsub2.f:1222-1300): the reflection
+  // matrix for incident direction (mu1 < 0, phi1) and outgoing (mu2 > 0,
+  // phi2), normalised so that a Lambertian surface returns its albedo.
+  void surface_brdf(const R *par, float mu2, float phi2, float mu1, float phi1, double refl[3][3]) const {
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) refl[i][j] = 0.0;
+    if (brdf == 'R') {
+      refl[0][0] = rpv_reflection((float)par[0], (float)par[1], (float)par[2], -mu1, mu2,
+                                  phi1 - phi2 - (float)std::acos(-1.0f));
+    } else {
+      wave_fresnel_reflection((float)par[0], (float)par[1], (float)par[2], mu1, mu2, phi1, phi2, refl);
+    }
+  }
+
+  // RPV_REFLECTION (src/polarized/shdomsub2.f:1658-1696): Rahman, Pinty and
+  // Verstraete (1993) with the small-mu floor of 0.03.
+  static float rpv_reflection(float rho0, float k, float theta, float mu1, float mu2, float phi) {
+    const float mu_min = 0.03f;
+    float x1 = std::max(mu1, mu_min), x2 = std::max(mu2, mu_min);
+    float m = std::pow(x1 * x2 * (x1 + x2), k - 1.0f);
+    float cosphi = std::cos(phi);
+    float sin1 = std::sqrt(1.0f - x1 * x1), sin2 = std::sqrt(1.0f - x2 * x2);
+    float cosg = x1 * x2 + sin1 * sin2 * cosphi;
+    float f = (1.0f - theta * theta) / std::pow(1.0f + 2.0f * theta * cosg + theta * theta, 1.5f);
+    float tan1 = sin1 / x1, tan2 = sin2 / x2;
+    float capg = std::sqrt(std::fabs(tan1 * tan1 + tan2 * tan2 - 2.0f * tan1 * tan2 * cosphi));
+    float h = 1.0f + (1.0f - rho0) / (1.0f + capg);
+    return rho0 * m * f * h;
+  }
+
+  // WAVE_FRESNEL_REFLECTION (src/polarized/shdomsub2.f:1358-1525): Fresnel
+  // reflection of a dielectric interface (index mre + i mim) with a Gaussian
+  // distribution of slopes of variance 0.0015 + 0.00256 wind speed (Cox and
+  // Munk) and the shadowing factor; the I, Q, U block of the Mueller matrix.
+  static void wave_fresnel_reflection(float mre, float mim, float wind, float mui, float mur, float phii, float phir,
+                                      double refl[3][3]) {
+    typedef std::complex<double> Cx;
+    const Cx cn1(1.0, 0.0), cn2((double)mre, (double)mim);
+    const double sigma2 = std::max(0.0005, 0.0015 + 0.00256 * (double)wind);
+    double dmui = std::fabs((double)mui), dmur = (double)mur;
+    if (std::fabs(dmui - 1.0) < 1e-10) dmui = 0.999999999999;
+    if (std::fabs(dmur - 1.0) < 1e-10) dmur = 0.999999999999;
+    const double dcosi = std::cos((double)phii), dsini = std::sin((double)phii);
+    const double dcosr = std::cos((double)phir), dsinr = std::sin((double)phir);
+    const double dsi = std::sqrt(1.0 - dmui * dmui), dsr = std::sqrt(1.0 - dmur * dmur);
+    const double vi1 = dsi * dcosi, vi2 = dsi * dsini, vi3 = -dmui;
+    const double vr1 = dsr * dcosr, vr2 = dsr * dsinr, vr3 = dmur;
+    const double u1 = vi1 - vr1, u2 = vi2 - vr2, u3 = vi3 - vr3;
+    const double fact1 = u1 * u1 + u2 * u2 + u3 * u3, factor = std::sqrt(1.0 / fact1);
+    const double xi1 = factor * (u1 * vi1 + u2 * vi2 + u3 * vi3);
+    const Cx cxi2 = std::sqrt(1.0 - (1.0 - xi1 * xi1) * cn1 * cn1 / (cn2 * cn2));
+    Cx c1 = cn1 * xi1, c2 = cn2 * cxi2;
+    const Cx crper = (c1 - c2) / (c1 + c2);
+    c1 = cn2 * xi1; c2 = cn1 * cxi2;
+    const Cx crpar = (c1 - c2) / (c1 + c2);
+    const double ti1 = -dmui * dcosi, ti2 = -dmui * dsini, ti3 = -dsi;
+    const double tr1 = dmur * dcosr, tr2 = dmur * dsinr, tr3 = -dsr;
+    const double pi1 = -dsini, pi2 = dcosi, pr1 = -dsinr, pr2 = dcosr;
+    const double pikr = pi1 * vr1 + pi2 * vr2, prki = pr1 * vi1 + pr2 * vi2;
+    const double tikr = ti1 * vr1 + ti2 * vr2 + ti3 * vr3, trki = tr1 * vi1 + tr2 * vi2 + tr3 * vi3;
+    const double e1 = pikr * prki, e2 = tikr * trki, e3 = tikr * prki, e4 = pikr * trki;
+    const Cx cf11 = e1 * crper + e2 * crpar, cf12 = -e3 * crper + e4 * crpar;
+    const Cx cf21 = -e4 * crper + e3 * crpar, cf22 = e2 * crper + e1 * crpar;
+    const double vp1 = vi2 * vr3 - vi3 * vr2, vp2 = vi3 * vr1 - vi1 * vr3, vp3 = vi1 * vr2 - vi2 * vr1;
+    const double dmod = std::pow(vp1 * vp1 + vp2 * vp2 + vp3 * vp3, 2);
+    const double rdz2 = u3 * u3, rdz4 = rdz2 * rdz2;
+    const double dex = std::exp(-(u1 * u1 + u2 * u2) / (2 * sigma2 * rdz2));
+    const double dcoeff = fact1 * fact1 * dex / (4 * dmui * dmur * dmod * rdz4 * 2 * sigma2);
+    const double af = 0.5 * dcoeff;
+    const double af11 = std::norm(cf11), af12 = std::norm(cf12), af21 = std::norm(cf21), af22 = std::norm(cf22);
+    refl[0][0] = (af11 + af12 + af21 + af22) * af;
+    refl[0][1] = (af11 - af12 + af21 - af22) * af;
+    refl[1][0] = (af11 - af22 + af12 - af21) * af;
+    refl[1][1] = (af11 - af12 - af21 + af22) * af;
+    const Cx c21 = std::conj(cf21), c22 = std::conj(cf22);
+    const Cx ctttp = cf11 * std::conj(cf12), cttpt = cf11 * c21, cttpp = cf11 * c22;
+    const Cx ctppt = cf12 * c21, ctppp = cf12 * c22, cptpp = cf21 * c22;
+    refl[0][2] = ((-ctttp - cptpp) * dcoeff).real();
+    refl[1][2] = ((-ctttp + cptpp) * dcoeff).real();
+    refl[2][0] = ((-cttpt - ctppp) * dcoeff).real();
+    refl[2][1] = ((-cttpt + ctppp) * dcoeff).real();
+    refl[2][2] = ((cttpp + ctppt) * dcoeff).real();
+    const double pp = std::acos(-1.0), s1 = std::sqrt(2 * sigma2 / pp), s3 = 1.0 / std::sqrt(2 * sigma2), s2 = s3 * s3;
+    double dcot = dmui / std::sqrt(1.0 - dmui * dmui);
+    const double shi = 0.5 * (s1 * std::exp(-s2 * dcot * dcot) / dcot - std::erfc(dcot * s3));
+    dcot = dmur / std::sqrt(1.0 - dmur * dmur);
+    const double shr = 0.5 * (s1 * std::exp(-s2 * dcot * dcot) / dcot - std::erfc(dcot * s3));
+    const double shadow = 1.0 / (1.0 + shi + shr);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) refl[i][j] = (double)(float)(refl[i][j] * shadow);
+  }
+
+  // VARIABLE_BRDF_SURFACE (src/polarized/shdomsub1.f:2592-2664) at bottom
+  // point b for the outgoing direction (mu2, phi2): the reflected direct
+  // beam plus the reflection of the stored downwelling radiances (no
+  // surface emission for a solar source).
+  void variable_brdf(size_t b, float mu2, float phi2, R *out) const {
+    const R *par = &botpar[b * nsfcpar];
+    const float opi = 1.0f / (float)std::acos(-1.0f);
+    double refl[3][3];
+    surface_brdf(par, mu2, phi2, p.solarmu, p.solaraz, refl);
+    for (int k = 0; k < nst; ++k) out[k] = (R)(opi * refl[k][0]) * dirflux[botp[b]];
+    const int ndown = nang / 2;
+    int jang = 0;
+    for (int jmu = 0; jmu < nmu / 2; ++jmu)
+      for (int jphi = 0; jphi < nphi0[jmu]; ++jphi, ++jang) {
+        surface_brdf(par, mu2, phi2, mu[jmu], phi[(size_t)jmu * nphi0max + jphi], refl);
+        const R w = (R)(opi * std::fabs(mu[jmu]) * wtdo[(size_t)jmu * nphi0max + jphi]);
+        const R *rin = &bcdown[(b * ndown + jang) * nst];
+        for (int k1 = 0; k1 < nst; ++k1)
+          for (int k = 0; k < nst; ++k) out[k] = out[k] + w * (R)(float)refl[k][k1] * rin[k1];
+      }
   }
 
   // FIXED/VARIABLE_LAMBERTIAN_BOUNDARY (src/polarized/shdomsub1.f:2438-2529).
@@ -1489,8 +1640,12 @@ struct Solver {
     radiance.assign((size_t)npts * nlm * nst, 0);
     std::vector<R> work((size_t)npts * nphi0max * nst, 0);
     auto W = [&](int i, int k, int s) -> R & { return work[((size_t)i * nphi0max + k) * nst + s]; };
+    const int ndown = nang / 2;
+    if (brdf) bcdown.assign(botp.size() * ndown * nst, 0);
+    int jang = 0;
+    std::vector<R> rb(nst);
     for (int imu = 0; imu < nmu; ++imu) {
-      if (imu == nmu / 2) lambertian_boundary();
+      if (imu == nmu / 2 && !brdf) lambertian_boundary();
       if (nst == 3) sh_to_do_pol(imu, work); else sh_to_do(imu, work);
       // the discrete-ordinate I source is made non-negative
       for (int i = 0; i < npts; ++i)
@@ -1504,6 +1659,11 @@ struct Solver {
         } else {
           iupdown = 1;
           for (size_t b = 0; b < botp.size(); ++b) {
+            if (brdf) {  // reflection of the stored downwelling radiances for this ordinate
+              variable_brdf(b, mu[imu], phi[(size_t)imu * nphi0max + iphi], rb.data());
+              for (int s = 0; s < nst; ++s) gridrad[(size_t)botp[b] * nst + s] = rb[s];
+              continue;
+            }
             gridrad[(size_t)botp[b] * nst] = bcrad_bot[b];
             for (int s = 1; s < nst; ++s) gridrad[(size_t)botp[b] * nst + s] = 0;
           }
@@ -1519,6 +1679,11 @@ struct Solver {
         }
         R a = std::fabs((R)mu[imu]) * (R)wtdo[(size_t)imu * nphi0max + iphi];
         for (int i = 0; i < npts; ++i) fluxes[2 * (size_t)i + iupdown] += a * W(i, iphi, 0);
+        if (brdf && mu[imu] < 0) {  // keep the downwelling radiance at the surface
+          for (size_t b = 0; b < botp.size(); ++b)
+            for (int s = 0; s < nst; ++s) bcdown[(b * ndown + jang) * nst + s] = W(botp[b], iphi, s);
+          ++jang;
+        }
       }
       if (nst == 3) do_to_sh_pol(imu, work); else do_to_sh(imu, work);
     }
@@ -1851,8 +2016,8 @@ struct Solver {
       if (transmit < p.transcut || ngrid > maxcellscross) validrad = true;
       else if (inext < 0 && iface >= 4) {
         validrad = true;
-        // FIND_BOUNDARY_RADIANCE, Lambertian, zero surface emission source
-        double xs[4], ys[4], rb[4];
+        // FIND_BOUNDARY_RADIANCE, zero surface emission source
+        double xs[4], ys[4], rb[4], rq[4] = {0, 0, 0, 0}, ru[4] = {0, 0, 0, 0};
         for (int jj = 0; jj < 4; ++jj) {
           int ipb = gridptr[8 * ic + kGridFace[kface][jj]];
           xs[jj] = gridpos[3 * ipb]; ys[jj] = gridpos[3 * ipb + 1];
@@ -1862,13 +2027,25 @@ struct Solver {
           } else {
             auto itb = std::lower_bound(botp.begin(), botp.end(), ipb);
             if (itb == botp.end() || *itb != ipb) { err = "FIND_BOUNDARY_RADIANCE: Not at boundary"; return false; }
-            rb[jj] = bcrad_bot[itb - botp.begin()];
+            if (brdf) {
+              R o[3];
+              variable_brdf(itb - botp.begin(), (float)mu2, (float)phi2, o);
+              rb[jj] = o[0];
+              if (nst == 3) { rq[jj] = o[1]; ru[jj] = o[2]; }
+            } else {
+              rb[jj] = bcrad_bot[itb - botp.begin()];
+            }
           }
         }
         float uu = (xs[1] - xs[0] > 0) ? (float)((xn - xs[0]) / (xs[1] - xs[0])) : 0.f;
         float vv = (ys[2] - ys[0] > 0) ? (float)((yn - ys[0]) / (ys[2] - ys[0])) : 0.f;
         float radbnd = (1 - uu) * (1 - vv) * (float)rb[0] + uu * (1 - vv) * (float)rb[1] + (1 - uu) * vv * (float)rb[2] + uu * vv * (float)rb[3];
-        radiance_acc[0] += transmit * radbnd;  // the boundaries emit unpolarized radiance
+        radiance_acc[0] += transmit * radbnd;
+        if (nst == 3 && brdf && (float)mu2 >= 0.0f) {  // a polarizing surface
+          const double w1 = (1 - uu) * (1 - vv), w2 = uu * (1 - vv), w3 = (1 - uu) * vv, w4 = uu * vv;
+          radiance_acc[1] += transmit * (float)(w1 * rq[0] + w2 * rq[1] + w3 * rq[2] + w4 * rq[3]);
+          radiance_acc[2] += transmit * (float)(w1 * ru[0] + w2 * ru[1] + w3 * ru[2] + w4 * ru[3]);
+        }
       } else {
         icell = inext;
       }
@@ -1930,7 +2107,7 @@ struct Solver {
   bool render(int n, const float *camx, const float *camy, const float *camz, const double *cammu,
               const double *camphi, float *out, int nthreads) {
     if (!precompute_phase()) return false;
-    lambertian_boundary();
+    if (!brdf) lambertian_boundary();
     const double pi = std::acos(-1.0);
     std::vector<int> bad(std::max(1, nthreads), 0);
     std::vector<std::string> errs(std::max(1, nthreads));

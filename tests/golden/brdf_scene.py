@@ -1,11 +1,13 @@
 """The scene of the reference's Verify_Lambertian_Surfaces test
 (tests/test_shdom.py:29-68, :597-632): a 50x1x11 Rayleigh atmosphere at
 0.85 um in independent-pixel mode over a variable Lambertian surface, NMU=16,
-NPHI=32, solar mu0=-0.707, viewed by 19 upward directions at z=30 km."""
+NPHI=32, solar mu0=-0.707, viewed by 19 upward directions at z=30 km; and
+the same atmosphere over the RPV (Verify_RPV_Surfaces, :676-713) and, with
+I, Q, U, the wave-Fresnel (Verify_WaveFresnel_Surfaces, :716-756) surfaces."""
 import numpy as np
 
 from at3d_gb300._abi import NumericalParams, Problem, Species
-from at3d_gb300.medium import rayleigh_extinction_profile, rayleigh_legcoef
+from at3d_gb300.medium import rayleigh_extinction_profile, rayleigh_legcoef, rayleigh_legcoef6
 
 
 def brdf_l1_problem():
@@ -29,3 +31,35 @@ def brdf_l1_rays():
     mu = np.array([0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9] + [1.0] + [0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9][::-1])
     phi = np.array([180.0] * 9 + [0.0] * 10)
     return (np.tile(x, 19), np.zeros(950), np.full(950, 30.0), np.repeat(mu, 50), np.deg2rad(np.repeat(phi, 50)))
+
+
+def _rayleigh6(wavelength=0.85):
+    """The six-element Rayleigh matrix with the King depolarisation factor
+    of RAYLEIGH_PHASE_FUNCTION (src/polarized/shdomsub4.f:2350-2386)."""
+    a_k, b_k, c_k = 1.0469541, 3.2503153e-04, 3.8622851e-05
+    w = np.float32(wavelength)
+    fking = np.float32(a_k + b_k / np.float64(w) ** 2 + c_k / np.float64(w) ** 4)
+    depol = float(np.float32(6.0 * (np.float64(fking) - 1.0) / (3.0 + 7.0 * np.float64(fking))))
+    c = rayleigh_legcoef6(depol)
+    c[0] = rayleigh_legcoef(wavelength)  # the same float32 arithmetic as the scalar row
+    return c
+
+
+def brdf_rpv_problem():
+    pb = brdf_l1_problem()
+    k = np.linspace(0.5, 1.0 - 0.5 / 50, 50)[:, np.newaxis]
+    par = np.stack([np.full((50, 1), 0.1), k, np.full((50, 1), -0.24)], axis=-1).astype(np.float32)
+    pb.surface_brdf, pb.surface_params = "R", par
+    pb.surface_delx = pb.surface_dely = 0.02
+    return pb
+
+
+def brdf_wave_fresnel_problem():
+    pb = brdf_l1_problem()
+    wind = np.linspace(4.0, 12.0 - 8.0 / 50, 50)[:, np.newaxis]
+    par = np.stack([np.full((50, 1), 1.33), np.zeros((50, 1)), wind], axis=-1).astype(np.float32)
+    pb.surface_brdf, pb.surface_params = "W", par
+    pb.surface_delx = pb.surface_dely = 0.02
+    pb.num_stokes = 3
+    pb.species[0].legcoef = _rayleigh6(0.85)
+    return pb

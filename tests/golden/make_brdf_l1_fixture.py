@@ -1,8 +1,10 @@
-"""Generates tests/golden/brdf_L1.npz from the reference's golden files.
+"""Generates tests/golden/brdf_{L,R,W,D}1.npz from the reference's golden files.
 
-Reads the original-SHDOM outputs tests/data/brdf_L1f.out (fluxes) and
-tests/data/brdf_L1r.out (radiances) of the reference repository, parsed the
-way tests/test_shdom.py:17-27 parses them, and stores the numeric columns.
+Reads the original-SHDOM outputs tests/data/brdf_X1f.out (fluxes) and
+tests/data/brdf_X1r.out (radiances) of the reference repository for the
+Lambertian (L), RPV (R), wave-Fresnel (W, polarized) and Diner (D,
+polarized) surfaces, parsed the way tests/test_shdom.py:17-27 parses them,
+and stores the numeric columns.
 Run once in a checkout that has the reference mounted:
 
     python tests/golden/make_brdf_l1_fixture.py /path/to/reference
@@ -24,11 +26,12 @@ def parse(path, comment="!"):
 
 def main(ref):
     d = os.path.join(ref, "tests", "data")
-    fl = parse(os.path.join(d, "brdf_L1f.out"))
-    ra = parse(os.path.join(d, "brdf_L1r.out"))
-    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "brdf_L1.npz")
-    np.savez(out, fluxes=fl, radiances=ra)
-    print(out, fl.shape, ra.shape)
+    for kind in "LRWD":
+        fl = parse(os.path.join(d, f"brdf_{kind}1f.out"))
+        ra = parse(os.path.join(d, f"brdf_{kind}1r.out"))
+        out = os.path.join(os.path.dirname(os.path.abspath(__file__)), f"brdf_{kind}1.npz")
+        np.savez(out, fluxes=fl, radiances=ra)
+        print(out, fl.shape, ra.shape)
 
 
 if __name__ == "__main__":

@@ -1,16 +1,20 @@
 """Pins the CPU oracle against the reference's own golden vectors.
 
-tests/data/brdf_L1{f,r}.out of the reference (original SHDOM output for the
-Verify_Lambertian_Surfaces scene, tests/test_shdom.py:597-632) are stored as
-tests/golden/brdf_L1.npz by tests/golden/make_brdf_l1_fixture.py.  The
-reference test uses atol 4e-6 (fluxes) and 9e-6 (radiance); the golden files
-print five significant digits, so the tolerance here adds half of the last
+tests/data/brdf_{L,R,W}1{f,r}.out of the reference (original SHDOM output
+for the Verify_Lambertian_Surfaces, Verify_RPV_Surfaces and
+Verify_WaveFresnel_Surfaces scenes, tests/test_shdom.py:597-756; the last
+one polarized, Stokes I, Q, U) are stored as tests/golden/brdf_X1.npz by
+tests/golden/make_brdf_l1_fixture.py.  The reference test uses atol 4e-6
+(fluxes) and 9e-6 (radiance and Stokes components); the golden files print
+five significant digits, so the tolerance here adds half of the last
 printed digit of each value.
 """
+import os
+
 import numpy as np
 import pytest
 
-from brdf_scene import brdf_l1_problem, brdf_l1_rays
+from brdf_scene import brdf_l1_problem, brdf_l1_rays, brdf_rpv_problem, brdf_wave_fresnel_problem
 from oracle.oracle import Oracle
 
 GOLD = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "golden", "brdf_L1.npz"))
@@ -52,3 +56,32 @@ def test_radiances(solved):
     got = o.render(*brdf_l1_rays())
     ref = GOLD["radiances"][:, -1]
     assert np.all(np.abs(got - ref) <= 9e-6 + _quantum(ref))
+
+
+SURFACES = {"R1": (brdf_rpv_problem, 3), "W1": (brdf_wave_fresnel_problem, 4)}
+
+
+@pytest.fixture(scope="module", params=sorted(SURFACES))
+def solved_surface(request):
+    mk, iters = SURFACES[request.param]
+    o = Oracle(mk())
+    it, sc = o.solve(100)
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", f"brdf_{request.param}.npz"))
+    return o, it, iters, g
+
+
+def test_brdf_surface_golden(solved_surface):
+    o, it, iters, g = solved_surface
+    assert it == iters
+    st = o.export()
+    bot = np.arange(50) * o.sizes["nz"]
+    fl = g["fluxes"]
+    for got, col in ((st["dirflux"][bot], 4), (st["fluxes"][bot, 0], 3), (st["fluxes"][bot, 1], 2)):
+        assert np.all(np.abs(got - fl[:, col]) <= 4e-6 + _quantum(fl[:, col]))
+    rad = o.render(*brdf_l1_rays())
+    ra = g["radiances"]
+    if rad.ndim == 1:
+        assert np.all(np.abs(rad - ra[:, -1]) <= 9e-6 + _quantum(ra[:, -1]))
+    else:
+        for k in range(3):
+            assert np.all(np.abs(rad[:, k] - ra[:, 2 + k]) <= 9e-6 + _quantum(ra[:, 2 + k])), k
