@@ -951,6 +951,153 @@ __global__ void __launch_bounds__(256) k_do_fluxes(const float *__restrict__ rad
   }
 }
 
+// ------------------------------------------------ bidirectional surfaces
+// SURFACE_BRDF (src/polarized/shdomsub2.f:1222-1300) for the two built
+// types: 'R' RPV_REFLECTION (:1658-1696, single precision) and 'W'
+// WAVE_FRESNEL_REFLECTION (:1358-1525, double precision with complex
+// Fresnel coefficients).  Incident direction (mu1 < 0, phi1), outgoing
+// (mu2 > 0, phi2); R[3][3] is the I, Q, U block of the reflection matrix,
+// normalised so that a Lambertian surface gives its albedo.
+struct BrdfOrd {
+  float mu, phi, w, col, off;  // ordinate, weight |mu| wtdo / pi (downward), I column, Stokes column stride
+};
+
+struct Cd {
+  double r, i;
+};
+__device__ __forceinline__ Cd cadd(Cd a, Cd b) { return {a.r + b.r, a.i + b.i}; }
+__device__ __forceinline__ Cd csub(Cd a, Cd b) { return {a.r - b.r, a.i - b.i}; }
+__device__ __forceinline__ Cd cmul(Cd a, Cd b) { return {a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r}; }
+__device__ __forceinline__ Cd cscale(Cd a, double s) { return {a.r * s, a.i * s}; }
+__device__ __forceinline__ Cd cconj(Cd a) { return {a.r, -a.i}; }
+__device__ __forceinline__ double cnorm(Cd a) { return a.r * a.r + a.i * a.i; }
+__device__ __forceinline__ Cd cdiv(Cd a, Cd b) {
+  const double d = b.r * b.r + b.i * b.i;
+  return {(a.r * b.r + a.i * b.i) / d, (a.i * b.r - a.r * b.i) / d};
+}
+__device__ __forceinline__ Cd csqrt_(Cd a) {  // principal branch
+  const double m = hypot(a.r, a.i);
+  if (m == 0.0) return {0.0, 0.0};
+  const double re = sqrt(0.5 * (m + a.r)), im = sqrt(0.5 * (m - a.r));
+  return {re, signbit(a.i) ? -im : im};
+}
+
+__device__ float rpv_reflection_d(float rho0, float k, float theta, float mu1, float mu2, float phi) {
+  const float mu_min = 0.03f;
+  const float x1 = fmaxf(mu1, mu_min), x2 = fmaxf(mu2, mu_min);
+  const float m = powf(x1 * x2 * (x1 + x2), k - 1.0f);
+  const float cosphi = cosf(phi);
+  const float sin1 = sqrtf(1.0f - x1 * x1), sin2 = sqrtf(1.0f - x2 * x2);
+  const float cosg = x1 * x2 + sin1 * sin2 * cosphi;
+  const float f = (1.0f - theta * theta) / powf(1.0f + 2.0f * theta * cosg + theta * theta, 1.5f);
+  const float tan1 = sin1 / x1, tan2 = sin2 / x2;
+  const float capg = sqrtf(fabsf(tan1 * tan1 + tan2 * tan2 - 2.0f * tan1 * tan2 * cosphi));
+  const float h = 1.0f + (1.0f - rho0) / (1.0f + capg);
+  return rho0 * m * f * h;
+}
+
+__device__ void wave_fresnel_d(float mre, float mim, float wind, float mui, float mur, float phii, float phir,
+                               float R[3][3]) {
+  const Cd cn1 = {1.0, 0.0}, cn2 = {(double)mre, (double)mim};
+  const double sigma2 = fmax(0.0005, 0.0015 + 0.00256 * (double)wind);
+  double dmui = fabs((double)mui), dmur = (double)mur;
+  if (fabs(dmui - 1.0) < 1e-10) dmui = 0.999999999999;
+  if (fabs(dmur - 1.0) < 1e-10) dmur = 0.999999999999;
+  double dsini, dcosi, dsinr, dcosr;
+  sincos((double)phii, &dsini, &dcosi);
+  sincos((double)phir, &dsinr, &dcosr);
+  const double dsi = sqrt(1.0 - dmui * dmui), dsr = sqrt(1.0 - dmur * dmur);
+  const double vi1 = dsi * dcosi, vi2 = dsi * dsini, vi3 = -dmui;
+  const double vr1 = dsr * dcosr, vr2 = dsr * dsinr, vr3 = dmur;
+  const double u1 = vi1 - vr1, u2 = vi2 - vr2, u3 = vi3 - vr3;
+  const double fact1 = u1 * u1 + u2 * u2 + u3 * u3, factor = sqrt(1.0 / fact1);
+  const double xi1 = factor * (u1 * vi1 + u2 * vi2 + u3 * vi3);
+  const Cd cxi2 = csqrt_(csub({1.0, 0.0}, cscale(cdiv(cmul(cn1, cn1), cmul(cn2, cn2)), 1.0 - xi1 * xi1)));
+  Cd c1 = cscale(cn1, xi1), c2 = cmul(cn2, cxi2);
+  const Cd crper = cdiv(csub(c1, c2), cadd(c1, c2));
+  c1 = cscale(cn2, xi1); c2 = cmul(cn1, cxi2);
+  const Cd crpar = cdiv(csub(c1, c2), cadd(c1, c2));
+  const double ti1 = -dmui * dcosi, ti2 = -dmui * dsini, ti3 = -dsi;
+  const double tr1 = dmur * dcosr, tr2 = dmur * dsinr, tr3 = -dsr;
+  const double pikr = -dsini * vr1 + dcosi * vr2, prki = -dsinr * vi1 + dcosr * vi2;
+  const double tikr = ti1 * vr1 + ti2 * vr2 + ti3 * vr3, trki = tr1 * vi1 + tr2 * vi2 + tr3 * vi3;
+  const double e1 = pikr * prki, e2 = tikr * trki, e3 = tikr * prki, e4 = pikr * trki;
+  const Cd cf11 = cadd(cscale(crper, e1), cscale(crpar, e2)), cf12 = cadd(cscale(crper, -e3), cscale(crpar, e4));
+  const Cd cf21 = cadd(cscale(crper, -e4), cscale(crpar, e3)), cf22 = cadd(cscale(crper, e2), cscale(crpar, e1));
+  const double vp1 = vi2 * vr3 - vi3 * vr2, vp2 = vi3 * vr1 - vi1 * vr3, vp3 = vi1 * vr2 - vi2 * vr1;
+  const double vpm = vp1 * vp1 + vp2 * vp2 + vp3 * vp3, dmod = vpm * vpm;
+  const double rdz2 = u3 * u3, rdz4 = rdz2 * rdz2;
+  const double dex = exp(-(u1 * u1 + u2 * u2) / (2 * sigma2 * rdz2));
+  const double dcoeff = fact1 * fact1 * dex / (4 * dmui * dmur * dmod * rdz4 * 2 * sigma2);
+  const double af = 0.5 * dcoeff;
+  const double af11 = cnorm(cf11), af12 = cnorm(cf12), af21 = cnorm(cf21), af22 = cnorm(cf22);
+  double r[3][3];
+  r[0][0] = (af11 + af12 + af21 + af22) * af;
+  r[0][1] = (af11 - af12 + af21 - af22) * af;
+  r[1][0] = (af11 - af22 + af12 - af21) * af;
+  r[1][1] = (af11 - af12 - af21 + af22) * af;
+  const Cd c21 = cconj(cf21), c22 = cconj(cf22);
+  const Cd ctttp = cmul(cf11, cconj(cf12)), cttpt = cmul(cf11, c21), cttpp = cmul(cf11, c22);
+  const Cd ctppt = cmul(cf12, c21), ctppp = cmul(cf12, c22), cptpp = cmul(cf21, c22);
+  r[0][2] = (-ctttp.r - cptpp.r) * dcoeff;
+  r[1][2] = (-ctttp.r + cptpp.r) * dcoeff;
+  r[2][0] = (-cttpt.r - ctppp.r) * dcoeff;
+  r[2][1] = (-cttpt.r + ctppp.r) * dcoeff;
+  r[2][2] = (cttpp.r + ctppt.r) * dcoeff;
+  const double pp = 3.141592653589793, s1 = sqrt(2 * sigma2 / pp), s3 = 1.0 / sqrt(2 * sigma2), s2 = s3 * s3;
+  double dcot = dmui / sqrt(1.0 - dmui * dmui);
+  const double shi = 0.5 * (s1 * exp(-s2 * dcot * dcot) / dcot - erfc(dcot * s3));
+  dcot = dmur / sqrt(1.0 - dmur * dmur);
+  const double shr = 0.5 * (s1 * exp(-s2 * dcot * dcot) / dcot - erfc(dcot * s3));
+  const double shadow = 1.0 / (1.0 + shi + shr);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) R[i][j] = (float)(r[i][j] * shadow);
+}
+
+__device__ __forceinline__ void surface_brdf_d(int type, const float *par, float mu2, float phi2, float mu1, float phi1,
+                                               float R[3][3]) {
+  if (type == 'R') {
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) R[i][j] = 0.f;
+    R[0][0] = rpv_reflection_d(par[0], par[1], par[2], -mu1, mu2, phi1 - phi2 - 3.14159274f);
+  } else {
+    wave_fresnel_d(par[0], par[1], par[2], mu1, mu2, phi1, phi2, R);
+  }
+}
+
+// VARIABLE_BRDF_SURFACE (src/polarized/shdomsub1.f:2592-2664) for every
+// bottom point (block) and upward ordinate (thread): the reflected direct
+// beam plus the reflection of the downwelling radiances that the downward
+// sweep left at the point, written as the upward sweep's boundary values.
+__global__ void __launch_bounds__(128) k_brdf_bottom(const int *__restrict__ botp, int nbot, const float *__restrict__ botpar,
+                                                     int npar, int type, const BrdfOrd *__restrict__ dn, int ndn,
+                                                     const BrdfOrd *__restrict__ up, int nup, const float *__restrict__ dirflux,
+                                                     float solarmu, float solaraz, float *raddo, int ldo, int nst) {
+  const int b = blockIdx.x;
+  if (b >= nbot) return;
+  const int p = botp[b];
+  const float *par = botpar + (size_t)b * npar;
+  const float opi = 0.318309886f;
+  const float *row = raddo + (size_t)p * ldo;
+  for (int u = threadIdx.x; u < nup; u += blockDim.x) {
+    const BrdfOrd o = up[u];
+    float R[3][3], out[3];
+    surface_brdf_d(type, par, o.mu, o.phi, solarmu, solaraz, R);
+    for (int k = 0; k < nst; ++k) out[k] = opi * R[k][0] * dirflux[p];
+    for (int d = 0; d < ndn; ++d) {
+      const BrdfOrd i = dn[d];
+      surface_brdf_d(type, par, o.mu, o.phi, i.mu, i.phi, R);
+      const int ci = (int)i.col, oi = (int)i.off;
+      for (int k1 = 0; k1 < nst; ++k1) {
+        const float rin = row[ci + k1 * oi];
+        for (int k = 0; k < nst; ++k) out[k] += i.w * R[k][k1] * rin;
+      }
+    }
+    const int co = (int)o.col, oo = (int)o.off;
+    for (int k = 0; k < nst; ++k) raddo[(size_t)p * ldo + co + k * oo] = out[k];
+  }
+}
+
 // ---------------------------------------------------------------- source
 struct SourceArgs {
   const float *coef;      // [npts][nl]
@@ -1272,6 +1419,12 @@ struct RenderArgs {
   const float *bcrad_bot;
   const int *bot_index;  // point -> bottom list index or -1
   const float *coefp, *phasetab2;  // polarized: a2/a3/b1 coefficients, I-Q single-scatter table
+  // bidirectional surface (brdf != 0): parameters at the bottom points, the
+  // downward ordinates of the reflection sum and the ordinate radiances of
+  // the last sweep (the downwelling radiances at the surface)
+  int brdf, nsfcpar, nbrdf_dn, ldo;
+  const float *botpar, *raddo;
+  const BrdfOrd *brdf_dn;
   const float *camx, *camy, *camz;
   const double *cammu, *camphi;
   float *out;
@@ -1280,6 +1433,34 @@ struct RenderArgs {
   float solarmu, solaraz, secmu0, skyrad;
   double tautol, transcut;
 };
+
+// Reflected radiance of bottom point bi toward (mu2, phi2) (the BRDF branch
+// of FIND_BOUNDARY_RADIANCE, src/polarized/shdomsub2.f:2748-2863): the
+// warp sums the downward ordinates; every lane gets the Stokes vector.
+__device__ __noinline__ void brdf_radiance_warp(const RenderArgs &a, int bi, float mu2, float phi2, int lane, int nst, float out[3]) {
+  const float *par = a.botpar + (size_t)bi * a.nsfcpar;
+  const int p = a.botp[bi];
+  const float *row = a.raddo + (size_t)p * a.ldo;
+  float acc[3] = {0.f, 0.f, 0.f}, R[3][3];
+  if (lane == 0) {
+    surface_brdf_d(a.brdf, par, mu2, phi2, a.solarmu, a.solaraz, R);
+    for (int k = 0; k < nst; ++k) acc[k] = 0.318309886f * R[k][0] * a.dirflux[p];
+  }
+  for (int d = lane; d < a.nbrdf_dn; d += 32) {
+    const BrdfOrd i = a.brdf_dn[d];
+    surface_brdf_d(a.brdf, par, mu2, phi2, i.mu, i.phi, R);
+    const int ci = (int)i.col, oi = (int)i.off;
+    for (int k1 = 0; k1 < nst; ++k1) {
+      const float rin = row[ci + k1 * oi];
+      for (int k = 0; k < nst; ++k) acc[k] += i.w * R[k][k1] * rin;
+    }
+  }
+  for (int k = 0; k < 3; ++k) {
+    float v = acc[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    out[k] = v;
+  }
+}
 
 __device__ int locate_cell(const RenderArgs &a, double &x0, double &y0, double z0) {
   const int nx = a.nx, ny = a.ny, nz = a.nz;
@@ -1361,6 +1542,7 @@ __device__ __forceinline__ void ylm_dir_warp(float *y, float x, float phf, int m
   }
 }
 
+template <bool BRDF>
 __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
   __shared__ float ydir[RWARPS][RNLM];
   __shared__ float tl[RWARPS][64];
@@ -1542,7 +1724,17 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
         int q = gk[c_face[kface][k]];
         xs[k] = a.gridpos[3 * q]; ys[k] = a.gridpos[3 * q + 1];
         if ((float)mu2 < 0.f) rb[k] = a.skyrad;
-        else { int bi = a.bot_index[q]; rb[k] = bi >= 0 ? a.bcrad_bot[bi] : 0.f; }
+        else {
+          int bi = a.bot_index[q];
+          rb[k] = bi >= 0 ? a.bcrad_bot[bi] : 0.f;
+          if constexpr (BRDF) {
+            if (bi >= 0) {
+              float o[3];
+              brdf_radiance_warp(a, bi, (float)mu2, (float)phi2, lane, 1, o);
+              rb[k] = o[0];
+            }
+          }
+        }
       }
       float uu = (xs[1] - xs[0] > 0) ? (float)((xn - xs[0]) / (xs[1] - xs[0])) : 0.f;
       float vv = (ys[2] - ys[0] > 0) ? (float)((yn - ys[0]) / (ys[2] - ys[0])) : 0.f;
@@ -1625,6 +1817,7 @@ __device__ void ylm6_dir_warp(float *y, int nlm, double x, double phi, int ml, i
 // and ROTATE_POL_PLANE :3277-3316): as k_render, with the I, Q, U sources
 // of each corner and a Stokes vector along the ray.  Dynamic shared memory:
 // the five generalized functions (5 nlm floats) per warp.  out[ray][3].
+template <bool BRDF>
 __global__ void __launch_bounds__(RWARPS * 32) k_render_pol(RenderArgs a) {
   extern __shared__ float rsm[];
   __shared__ float tl[RWARPS][3][64];
@@ -1832,18 +2025,31 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render_pol(RenderArgs a) {
     if (transmit < a.transcut || ngrid > maxcross) {
       validrad = true;
     } else if (nxt < 0 && iface >= 4) {
-      validrad = true;  // unpolarized boundary radiance (I only)
+      validrad = true;  // unpolarized sky and Lambertian surface (I only); a BRDF surface polarizes
       const int *gk = a.gridptr + 8 * (size_t)kc;
-      float xs[4], ys[4], rb[4];
+      float xs[4], ys[4], rb[3][4];
       for (int k = 0; k < 4; ++k) {
         int q = gk[c_face[kface][k]];
         xs[k] = a.gridpos[3 * q]; ys[k] = a.gridpos[3 * q + 1];
-        if ((float)mu2 < 0.f) rb[k] = a.skyrad;
-        else { int bi = a.bot_index[q]; rb[k] = bi >= 0 ? a.bcrad_bot[bi] : 0.f; }
+        rb[1][k] = rb[2][k] = 0.f;
+        if ((float)mu2 < 0.f) rb[0][k] = a.skyrad;
+        else {
+          int bi = a.bot_index[q];
+          rb[0][k] = bi >= 0 ? a.bcrad_bot[bi] : 0.f;
+          if constexpr (BRDF) {
+            if (bi >= 0) {
+              float o[3];
+              brdf_radiance_warp(a, bi, (float)mu2, (float)phi2, lane, 3, o);
+              rb[0][k] = o[0]; rb[1][k] = o[1]; rb[2][k] = o[2];
+            }
+          }
+        }
       }
       float uu = (xs[1] - xs[0] > 0) ? (float)((xn - xs[0]) / (xs[1] - xs[0])) : 0.f;
       float vv = (ys[2] - ys[0] > 0) ? (float)((yn - ys[0]) / (ys[2] - ys[0])) : 0.f;
-      radacc[0] += transmit * ((1 - uu) * (1 - vv) * rb[0] + uu * (1 - vv) * rb[1] + (1 - uu) * vv * rb[2] + uu * vv * rb[3]);
+      for (int c = 0; c < 3; ++c)
+        radacc[c] += transmit * ((1 - uu) * (1 - vv) * rb[c][0] + uu * (1 - vv) * rb[c][1] + (1 - uu) * vv * rb[c][2] +
+                                 uu * vv * rb[c][3]);
     } else {
       cell = nxt;
     }
@@ -1925,6 +2131,9 @@ struct Handle {
   DBuf<uint8_t> col_stk;
   DBuf<float> coefp, phasetab2;
   DBuf<float> pol_t[2];  // FP32 dense transform matrices for the CUDA-core path, [K][N]
+  // bidirectional surface
+  DBuf<float> botpar;
+  DBuf<BrdfOrd> brdf_dn, brdf_up;
   DBuf<int> nphi0, col_of;
   // medium
   DBuf<float> text, dirflux, coef, tms_w, phasetab, botalb, rad0;
@@ -2385,6 +2594,14 @@ static void upload_plan(Handle &H) {
   H.tms_ptr.upload(P.tms_ptr); H.tms_iph.upload(P.tms_iph); H.tms_w.upload(P.tms_w);
   H.phasetab.upload(P.phasetab); H.botalb.upload(P.botalb); H.rad0.upload(P.rad0);
   if (H.nst == 3) { H.col_stk.upload(P.col_stk); H.coefp.upload(P.coefp); H.phasetab2.upload(P.phasetab2); }
+  if (P.brdf) {
+    static_assert(sizeof(BrdfOrd) == sizeof(Plan::BrdfOrd), "BRDF ordinate records");
+    H.botpar.upload(P.botpar);
+    std::vector<BrdfOrd> dn(P.brdf_dn.size()), up(P.brdf_up.size());
+    std::memcpy(dn.data(), P.brdf_dn.data(), dn.size() * sizeof(BrdfOrd));
+    std::memcpy(up.data(), P.brdf_up.data(), up.size() * sizeof(BrdfOrd));
+    H.brdf_dn.upload(dn); H.brdf_up.upload(up);
+  }
   H.ldo = (P.nang + 3) & ~3;
   const size_t nf = (size_t)P.npts * H.nst * P.nlm, nd = (size_t)P.npts * H.ldo;
   H.source.alloc(nf); H.delsource.alloc(nf); H.radiance.alloc(nf);
@@ -2719,7 +2936,7 @@ int shdom_plan_create(const shdom_problem *problem, shdom_plan **out, shdom_size
     // the plan keeps copies of everything it uses; drop the caller's array pointers
     shdom_problem &pr = p->P.prob;
     pr.zlevels = nullptr; pr.extinctp = nullptr; pr.albedop = nullptr; pr.iphasep = nullptr;
-    pr.phasewtp = nullptr; pr.legenp = nullptr; pr.sfc_albedo = nullptr;
+    pr.phasewtp = nullptr; pr.legenp = nullptr; pr.sfc_albedo = nullptr; pr.sfc_params = nullptr;
     if (sizes) {
       shdom::fill_sizes(p->P, sizes);
       sizes->solcrit = 1.f;
@@ -2803,7 +3020,13 @@ int shdom_solution_iterations(shdom_handle *hh, int maxiter, int *iters, float *
         H.launches += 1;
       }
       shdom::sweep_hemisphere(H, 0);
-      if (nbot) {
+      if (nbot && P.brdf) {
+        shdom::k_brdf_bottom<<<nbot, 128, 0, H.stream>>>(H.botp.p, nbot, H.botpar.p, P.nsfcpar, P.brdf, H.brdf_dn.p,
+                                                          (int)P.brdf_dn.size(), H.brdf_up.p, (int)P.brdf_up.size(),
+                                                          H.dirflux.p, P.prob.solarmu, P.prob.solaraz, H.raddo.p, H.ldo,
+                                                          H.nst);
+        H.launches += 1;
+      } else if (nbot) {
         shdom::k_lambertian<<<nbot, 256, 0, H.stream>>>(H.botp.p, nbot, H.botalb.p, H.dirflux.p, H.col_fluxw.p, H.raddo.p,
                                                          nang, H.ldo, P.ncol_down, H.bcrad.p, H.nst == 3 ? H.col_stk.p : nullptr);
         H.launches += 1;
@@ -2898,6 +3121,8 @@ static shdom::RenderArgs render_args(Handle &H, int nrays, const float *camx, co
   a.transcut = P.prob.transcut;
   a.coefp = H.nst == 3 ? H.coefp.p : nullptr;
   a.phasetab2 = H.nst == 3 ? H.phasetab2.p : nullptr;
+  a.brdf = P.brdf; a.nsfcpar = P.nsfcpar; a.nbrdf_dn = (int)P.brdf_dn.size(); a.ldo = H.ldo;
+  a.botpar = H.botpar.p; a.raddo = H.raddo.p; a.brdf_dn = H.brdf_dn.p;
   return a;
 }
 
@@ -2917,10 +3142,17 @@ static int render_impl(shdom_handle *hh, int nrays, const float *camx, const flo
   if (blocks > 0) {
     if (H.nst == 3) {
       const size_t smem = (size_t)shdom::RWARPS * 5 * P.nlm * sizeof(float);
-      CK(cudaFuncSetAttribute(shdom::k_render_pol, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      shdom::k_render_pol<<<blocks, shdom::RWARPS * 32, smem, stream>>>(a);
+      if (P.brdf) {
+        CK(cudaFuncSetAttribute(shdom::k_render_pol<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        shdom::k_render_pol<true><<<blocks, shdom::RWARPS * 32, smem, stream>>>(a);
+      } else {
+        CK(cudaFuncSetAttribute(shdom::k_render_pol<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        shdom::k_render_pol<false><<<blocks, shdom::RWARPS * 32, smem, stream>>>(a);
+      }
+    } else if (P.brdf) {
+      shdom::k_render<true><<<blocks, shdom::RWARPS * 32, 0, stream>>>(a);
     } else {
-      shdom::k_render<<<blocks, shdom::RWARPS * 32, 0, stream>>>(a);
+      shdom::k_render<false><<<blocks, shdom::RWARPS * 32, 0, stream>>>(a);
     }
     H.launches += 1;
   }
@@ -3093,6 +3325,7 @@ static int levis_host(shdom_handle *hh, int species, int nrays, const float *cam
   shdom::Plan &P = H.P;
   if (species < 0 || species >= P.npart) return fail(hh, "levis gradient: species index out of range");
   if (H.nst != 1) return fail(hh, "levis gradient: scalar (nstokes = 1) problems only");
+  if (P.brdf) return fail(hh, "levis gradient: Lambertian surfaces only");
   if (P.ml + 1 > 32 || P.nlm > shdom::RNLM) return fail(hh, "levis gradient: at most 32 Legendre terms are supported");
   if (!H.initialized) return fail(hh, "levis gradient: the solution has not been initialized");
   if (H.grad_ipa != species) prepare_grad(H, species);

@@ -1297,6 +1297,45 @@ bool build_plan(const shdom_problem &p, Plan &P) {
       P.botalb[k] = (1 - u) * (1 - v) * G(ix, iy) + (1 - u) * v * G(ix, iy + 1) + u * (1 - v) * G(ix + 1, iy) + u * v * G(ix + 1, iy + 1);
     }
   }
+  // bidirectional surface: parameters at the bottom points (SURFACE_PARM_INTERP,
+  // src/polarized/shdomsub1.f:2218-2268) and the ordinate tables of the
+  // reflection sums (VARIABLE_BRDF_SURFACE, src/polarized/shdomsub1.f:2592-2664)
+  P.brdf = p.sfc_brdf;
+  P.nsfcpar = 0;
+  P.botpar.clear(); P.brdf_dn.clear(); P.brdf_up.clear();
+  if (p.sfc_brdf) {
+    if ((p.sfc_brdf != 'R' && p.sfc_brdf != 'W') || p.nsfcpar < 3 || !p.sfc_params || p.nxsfc < 1 || p.nysfc < 1) {
+      P.err = "surface BRDF: types 'R' (RPV) and 'W' (wave-Fresnel) with 3 parameters on a surface grid";
+      return false;
+    }
+    if (p.sfc_brdf == 'R' && p.nstokes != 1) { P.err = "RPV BRDF is only for unpolarized case"; return false; }
+    const int nxs = p.nxsfc, nys = p.nysfc, np_ = p.nsfcpar;
+    P.nsfcpar = np_;
+    P.botpar.assign(P.botp.size() * np_, 0.f);
+    auto G = [&](int x, int y, int j) { return p.sfc_params[((size_t)((y - 1) % nys) * nxs + ((x - 1) % nxs)) * np_ + j]; };
+    for (size_t k = 0; k < P.botp.size(); ++k) {
+      int i = P.botp[k];
+      float rx = P.gridpos[3 * i] / p.delxsfc, ry = P.gridpos[3 * i + 1] / p.delysfc;
+      int ix = std::max(1, std::min(nxs, (int)rx + 1)), iy = std::max(1, std::min(nys, (int)ry + 1));
+      float u = std::max(0.f, std::min(1.f, rx - (ix - 1))), v = std::max(0.f, std::min(1.f, ry - (iy - 1)));
+      for (int j = 0; j < np_; ++j)
+        P.botpar[k * np_ + j] = (1 - u) * (1 - v) * G(ix, iy, j) + (1 - u) * v * G(ix, iy + 1, j) +
+                                u * (1 - v) * G(ix + 1, iy, j) + u * v * G(ix + 1, iy + 1, j);
+    }
+    const float opi = 1.0f / (float)std::acos(-1.0f);
+    for (int j = 0; j < P.nmu; ++j)
+      for (int q = 0; q < P.nphi0[j]; ++q) {
+        const int c = P.col_of[(size_t)j * P.nphi0max + q];
+        const int off = P.nst == 3 ? P.cls_ncol[P.col_oct[c] - 1][P.col_cls[c]] / 3 : 0;
+        const float mu = P.mu[j], ph = P.phi[(size_t)j * P.nphi0max + q];
+        if (j < P.nmu / 2) {
+          const float w = opi * std::fabs(mu) * P.wtdo[(size_t)j * P.nphi0max + q];
+          P.brdf_dn.push_back({mu, ph, w, (float)c, (float)off});
+        } else {
+          P.brdf_up.push_back({mu, ph, 0.f, (float)c, (float)off});
+        }
+      }
+  }
   return true;
 }
 

@@ -91,6 +91,14 @@ struct Plan {
   float albmax = 0.f;
   std::vector<float> rad0;                       // [npts][4] Eddington initial radiance
   std::vector<float> botalb;                     // surface albedo at the bottom points
+  // bidirectional surface ('R' RPV, 'W' wave-Fresnel; 0 Lambertian): its
+  // parameters at the bottom points and the downward / upward ordinates of
+  // the reflection sums, in the reference order: mu, phi, weight
+  // (|mu| wtdo / pi, downward only), I column, Stokes column stride
+  int brdf = 0, nsfcpar = 0;
+  std::vector<float> botpar;                     // [nbot][nsfcpar]
+  struct BrdfOrd { float mu, phi, w, col, off; };
+  std::vector<BrdfOrd> brdf_dn, brdf_up;
   // ---- species data kept for the gradient (property grid and grid points)
   int npx = 0, npy = 0, npz = 0, maxnmicro = 0;
   float delx = 0.f, dely = 0.f;

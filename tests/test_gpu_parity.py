@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from at3d_gb300.scenes import cloud_blob, orthographic_views
-from brdf_scene import brdf_l1_problem, brdf_l1_rays
+from brdf_scene import brdf_l1_problem, brdf_l1_rays, brdf_rpv_problem, brdf_wave_fresnel_problem
 from oracle.oracle import Oracle
 
 pytestmark = pytest.mark.gpu
@@ -183,3 +183,30 @@ def test_odd_ray_count(rte_cls):
     full = r.render(*rays)
     odd = r.render(*(np.asarray(a)[:127] for a in rays))
     assert np.array_equal(odd, full[:127])
+
+
+
+@pytest.mark.parametrize("name", ["R1", "W1"])
+def test_golden_brdf_surfaces(rte_cls, name):
+    """The reference's RPV and (polarized, I, Q, U) wave-Fresnel surface
+    scenes against original SHDOM output, with the reference test's
+    tolerances plus half the last printed digit."""
+    import os
+    mk, iters = {"R1": (brdf_rpv_problem, 3), "W1": (brdf_wave_fresnel_problem, 4)}[name]
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", f"brdf_{name}.npz"))
+    r = rte_cls.from_problem(mk())
+    it, _ = r.solve(100, verbose=False)
+    assert it == iters
+    st = r.export_state()
+    bot = np.arange(50) * 11
+    q = lambda v: np.where(np.abs(v) > 0, 0.5 * 10.0 ** (np.floor(np.log10(np.abs(np.where(v != 0, v, 1)))) - 4), 5e-7)
+    fl = g["fluxes"]
+    for got, col in ((st["dirflux"][bot], 4), (st["fluxes"][bot, 0], 3), (st["fluxes"][bot, 1], 2)):
+        assert np.all(np.abs(got - fl[:, col]) <= 4e-6 + q(fl[:, col]))
+    rad = r.render(*brdf_l1_rays())
+    ra = g["radiances"]
+    if rad.ndim == 1:
+        assert np.all(np.abs(rad - ra[:, -1]) <= 9e-6 + q(ra[:, -1]))
+    else:
+        for k in range(3):
+            assert np.all(np.abs(rad[:, k] - ra[:, 2 + k]) <= 9e-6 + q(ra[:, 2 + k])), k
