@@ -952,10 +952,11 @@ __global__ void __launch_bounds__(256) k_do_fluxes(const float *__restrict__ rad
 }
 
 // ------------------------------------------------ bidirectional surfaces
-// SURFACE_BRDF (src/polarized/shdomsub2.f:1222-1300) for the two built
-// types: 'R' RPV_REFLECTION (:1658-1696, single precision) and 'W'
+// SURFACE_BRDF (src/polarized/shdomsub2.f:1222-1300) for the built types:
+// 'R' RPV_REFLECTION (:1658-1696, single precision), 'W'
 // WAVE_FRESNEL_REFLECTION (:1358-1525, double precision with complex
-// Fresnel coefficients).  Incident direction (mu1 < 0, phi1), outgoing
+// Fresnel coefficients) and 'D' DINER_REFLECTION (:1526-1657, single
+// precision; its Fresnel index 1.5 is real, so the coefficients are real).  Incident direction (mu1 < 0, phi1), outgoing
 // (mu2 > 0, phi2); R[3][3] is the I, Q, U block of the reflection matrix,
 // normalised so that a Lambertian surface gives its albedo.
 struct BrdfOrd {
@@ -1054,9 +1055,46 @@ __device__ void wave_fresnel_d(float mre, float mim, float wind, float mui, floa
     for (int j = 0; j < 3; ++j) R[i][j] = (float)(r[i][j] * shadow);
 }
 
+__device__ void diner_d(float a, float k, float b, float zeta, float sigma, float mu1, float mu2, float phi, float R[3][3]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) R[i][j] = 0.f;
+  const float sinth1 = sqrtf(1.0f - mu1 * mu1), sinth2 = sqrtf(1.0f - mu2 * mu2);
+  const float cosphi = cosf(phi);
+  const float cossc = fminf(1.0f, fmaxf(-1.0f, -mu1 * mu2 + sinth1 * sinth2 * cosphi));
+  const float tan1 = sinth1 / mu1, tan2 = sinth2 / mu2;
+  const float capg = sqrtf(fabsf(tan1 * tan1 + tan2 * tan2 + 2 * tan1 * tan2 * cosphi));
+  const float hot = 1 + (1 - a) / (1 + capg);
+  R[0][0] = a * powf((mu1 + mu2) * mu1 * mu2, k - 1) * expf(b * cossc) * hot;
+  if (zeta < 0.0f) return;
+  const float gamma = 0.5f * acosf(-cossc), cosg = cosf(gamma);
+  const float eps = 2.25f;
+  const float d = sqrtf(eps - 1.0f + cosg * cosg);
+  const float rp = (eps * cosg - d) / (eps * cosg + d), rs = (cosg - d) / (cosg + d);
+  const float f11 = 0.5f * (rp * rp + rs * rs), f12 = 0.5f * (rp * rp - rs * rs), f33 = rp * rs;
+  const float cosbeta = 0.5f * (mu1 + mu2) / cosg;
+  const float h = sigma > 0.0f ? zeta * expf(-0.5f * (1 / (cosbeta * cosbeta) - 1) / (sigma * sigma)) /
+                                     (8 * sigma * sigma * mu2 * mu1 * cosbeta * cosbeta * cosbeta * cosbeta)
+                               : zeta / (8 * mu2 * mu1 * cosbeta);
+  R[0][0] += h * f11;
+  const float sinphi = sinf(phi);
+  const float al1 = atanf(sinth2 * sinphi / (mu2 * sinth1 + sinth2 * mu1 * cosphi));
+  const float al2 = atanf(sinth1 * sinphi / (sinth2 * mu1 + mu2 * sinth1 * cosphi));
+  const float c1 = cosf(2 * al1), s1 = sinf(2 * al1), c2 = cosf(2 * al2), s2 = sinf(2 * al2);
+  R[0][1] = h * f12 * c1;
+  R[1][0] = h * f12 * c2;
+  R[1][1] = h * (f11 * c1 * c2 + f33 * s1 * s2);
+  R[0][2] = -h * f12 * s1;
+  R[1][2] = h * (-f11 * s1 * c2 + f33 * c1 * s2);
+  R[2][0] = -h * f12 * s2;
+  R[2][1] = h * (-f11 * c1 * s2 + f33 * s1 * c2);
+  R[2][2] = h * (f11 * s1 * s2 + f33 * c1 * c2);
+}
+
 __device__ __forceinline__ void surface_brdf_d(int type, const float *par, float mu2, float phi2, float mu1, float phi1,
                                                float R[3][3]) {
-  if (type == 'R') {
+  if (type == 'D') {
+    diner_d(par[0], par[1], par[2], par[3], par[4], -mu1, mu2, phi2 - phi1, R);
+  } else if (type == 'R') {
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) R[i][j] = 0.f;
     R[0][0] = rpv_reflection_d(par[0], par[1], par[2], -mu1, mu2, phi1 - phi2 - 3.14159274f);

@@ -1304,8 +1304,9 @@ bool build_plan(const shdom_problem &p, Plan &P) {
   P.nsfcpar = 0;
   P.botpar.clear(); P.brdf_dn.clear(); P.brdf_up.clear();
   if (p.sfc_brdf) {
-    if ((p.sfc_brdf != 'R' && p.sfc_brdf != 'W') || p.nsfcpar < 3 || !p.sfc_params || p.nxsfc < 1 || p.nysfc < 1) {
-      P.err = "surface BRDF: types 'R' (RPV) and 'W' (wave-Fresnel) with 3 parameters on a surface grid";
+    if ((p.sfc_brdf != 'R' && p.sfc_brdf != 'W' && p.sfc_brdf != 'D') || p.nsfcpar < (p.sfc_brdf == 'D' ? 5 : 3) ||
+        !p.sfc_params || p.nxsfc < 1 || p.nysfc < 1) {
+      P.err = "surface BRDF: types 'R' (RPV), 'W' (wave-Fresnel; 3 parameters) and 'D' (Diner; 5) on a surface grid";
       return false;
     }
     if (p.sfc_brdf == 'R' && p.nstokes != 1) { P.err = "RPV BRDF is only for unpolarized case"; return false; }

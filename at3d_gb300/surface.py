@@ -1,6 +1,6 @@
 """Surfaces: Lambertian (at3d.surface.lambertian, at3d/surface.py:28-105)
-and bidirectional ones -- RPV_unpolarized (at3d/surface.py:404-480) and
-wave_fresnel (:106-203) -- with fixed or spatially varying parameters on a
+and bidirectional ones -- RPV_unpolarized (at3d/surface.py:404-480),
+wave_fresnel (:106-203) and diner (:204-307) -- with fixed or spatially varying parameters on a
 surface grid of spacing (delx, dely)."""
 from __future__ import annotations
 
@@ -34,8 +34,9 @@ def lambertian(albedo, ground_temperature=298.15, delx=None, dely=None) -> Lambe
 
 @dataclass
 class BRDFSurface:
-    """A bidirectional surface: ``kind`` 'R' (RPV: rho0, k, theta) or 'W'
-    (wave-Fresnel: real index, imaginary index, wind speed in m/s), with
+    """A bidirectional surface: ``kind`` 'R' (RPV: rho0, k, theta), 'W'
+    (wave-Fresnel: real index, imaginary index, wind speed in m/s) or 'D'
+    (Diner: a, k, b, zeta, sigma), with
     ``params`` of shape [nxsfc, nysfc, nparams]."""
     kind: str
     params: np.ndarray
@@ -67,3 +68,11 @@ def wave_fresnel(real_refractive_index, imaginary_refractive_index, surface_wind
     par, dx, dy = _stack(real_refractive_index, imaginary_refractive_index, surface_wind_speed,
                          delx=delx, dely=dely)
     return BRDFSurface("W", par, float(ground_temperature), dx, dy)
+
+
+def diner(A, K, B, ZETA, SIGMA, ground_temperature=298.15, delx=None, dely=None) -> BRDFSurface:
+    """Diner et al. (2012) polarized BRDF: modified-RPV volume term (a, k, b)
+    plus Fresnel microfacets weighted by zeta, slope spread sigma (uniform
+    orientation when sigma <= 0)."""
+    par, dx, dy = _stack(A, K, B, ZETA, SIGMA, delx=delx, dely=dely)
+    return BRDFSurface("D", par, float(ground_temperature), dx, dy)

@@ -258,8 +258,9 @@ struct Solver {
     if (p.sfc_variable) sfcalb.assign(p.sfc_albedo, p.sfc_albedo + (size_t)p.nxsfc * p.nysfc);
     brdf = p.sfc_brdf; nsfcpar = p.nsfcpar;
     if (brdf) {
-      if ((brdf != 'R' && brdf != 'W') || p.nsfcpar < 3 || !p.sfc_params || p.nxsfc < 1 || p.nysfc < 1) {
-        err = "surface BRDF: types 'R' (RPV) and 'W' (wave-Fresnel) with 3 parameters on a surface grid";
+      if ((brdf != 'R' && brdf != 'W' && brdf != 'D') || p.nsfcpar < (brdf == 'D' ? 5 : 3) || !p.sfc_params ||
+          p.nxsfc < 1 || p.nysfc < 1) {
+        err = "surface BRDF: types 'R' (RPV), 'W' (wave-Fresnel; 3 parameters) and 'D' (Diner; 5) on a surface grid";
         return false;
       }
       if (brdf == 'R' && nst != 1) { err = "RPV BRDF is only for unpolarized case"; return false; }
@@ -1208,9 +1209,60 @@ struct Solver {
     if (brdf == 'R') {
       refl[0][0] = rpv_reflection((float)par[0], (float)par[1], (float)par[2], -mu1, mu2,
                                   phi1 - phi2 - (float)std::acos(-1.0f));
+    } else if (brdf == 'D') {
+      diner_reflection((float)par[0], (float)par[1], (float)par[2], (float)par[3], (float)par[4], -mu1, mu2,
+                       phi2 - phi1, refl);
     } else {
       wave_fresnel_reflection((float)par[0], (float)par[1], (float)par[2], mu1, mu2, phi1, phi2, refl);
     }
+  }
+
+  // DINER_REFLECTION (src/polarized/shdomsub2.f:1526-1657): depolarizing
+  // modified-RPV volume term with the hotspot factor plus Fresnel
+  // reflection (index 1.5) from microfacets with a uniform (sigma <= 0) or
+  // Gaussian slope distribution, rotated into the meridional planes; single
+  // precision (mu1, mu2 > 0, phi = phi2 - phi1).
+  static void diner_reflection(float a, float k, float b, float zeta, float sigma, float mu1, float mu2, float phi,
+                               double refl[3][3]) {
+    float r[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    const float sinth1 = std::sqrt(1.0f - mu1 * mu1), sinth2 = std::sqrt(1.0f - mu2 * mu2);
+    const float cosphi = std::cos(phi);
+    float cossc = -mu1 * mu2 + sinth1 * sinth2 * cosphi;
+    cossc = std::min(1.0f, std::max(-1.0f, cossc));
+    const float tan1 = sinth1 / mu1, tan2 = sinth2 / mu2;
+    const float capg = std::sqrt(std::fabs(tan1 * tan1 + tan2 * tan2 + 2 * tan1 * tan2 * cosphi));
+    const float hot = 1 + (1 - a) / (1 + capg);
+    r[0][0] = a * std::pow((mu1 + mu2) * mu1 * mu2, k - 1) * std::exp(b * cossc);
+    r[0][0] = r[0][0] * hot;
+    if (zeta >= 0.0f) {
+      const float gamma = 0.5f * std::acos(-cossc), cosg = std::cos(gamma);
+      const float eps = 1.5f * 1.5f;
+      const float d = std::sqrt(eps - 1.0f + cosg * cosg);
+      const float rp = (eps * cosg - d) / (eps * cosg + d), rs = (cosg - d) / (cosg + d);
+      const float f11 = 0.5f * (rp * rp + rs * rs), f12 = 0.5f * (rp * rp - rs * rs), f33 = rp * rs;
+      const float cosbeta = 0.5f * (mu1 + mu2) / cosg;
+      float h;
+      if (sigma > 0.0f)
+        h = zeta * std::exp(-0.5f * (1 / (cosbeta * cosbeta) - 1) / (sigma * sigma)) /
+            (8 * sigma * sigma * mu2 * mu1 * cosbeta * cosbeta * cosbeta * cosbeta);
+      else
+        h = zeta / (8 * mu2 * mu1 * cosbeta);
+      r[0][0] = r[0][0] + h * f11;
+      const float sinphi = std::sin(phi);
+      const float al1 = std::atan(sinth2 * sinphi / (mu2 * sinth1 + sinth2 * mu1 * cosphi));
+      const float al2 = std::atan(sinth1 * sinphi / (sinth2 * mu1 + mu2 * sinth1 * cosphi));
+      const float c1 = std::cos(2 * al1), s1 = std::sin(2 * al1), c2 = std::cos(2 * al2), s2 = std::sin(2 * al2);
+      r[0][1] = h * f12 * c1;
+      r[1][0] = h * f12 * c2;
+      r[1][1] = h * (f11 * c1 * c2 + f33 * s1 * s2);
+      r[0][2] = -h * f12 * s1;
+      r[1][2] = h * (-f11 * s1 * c2 + f33 * c1 * s2);
+      r[2][0] = -h * f12 * s2;
+      r[2][1] = h * (-f11 * c1 * s2 + f33 * s1 * c2);
+      r[2][2] = h * (f11 * s1 * s2 + f33 * c1 * c2);
+    }
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) refl[i][j] = r[i][j];
   }
 
   // RPV_REFLECTION (src/polarized/shdomsub2.f:1658-1696): Rahman, Pinty and

@@ -3,7 +3,8 @@
 0.85 um in independent-pixel mode over a variable Lambertian surface, NMU=16,
 NPHI=32, solar mu0=-0.707, viewed by 19 upward directions at z=30 km; and
 the same atmosphere over the RPV (Verify_RPV_Surfaces, :676-713) and, with
-I, Q, U, the wave-Fresnel (Verify_WaveFresnel_Surfaces, :716-756) surfaces."""
+I, Q, U, the wave-Fresnel (Verify_WaveFresnel_Surfaces, :716-756) and Diner
+(Verify_Diner_Surfaces, :759-800) surfaces."""
 import numpy as np
 
 from at3d_gb300._abi import NumericalParams, Problem, Species
@@ -59,6 +60,18 @@ def brdf_wave_fresnel_problem():
     wind = np.linspace(4.0, 12.0 - 8.0 / 50, 50)[:, np.newaxis]
     par = np.stack([np.full((50, 1), 1.33), np.zeros((50, 1)), wind], axis=-1).astype(np.float32)
     pb.surface_brdf, pb.surface_params = "W", par
+    pb.surface_delx = pb.surface_dely = 0.02
+    pb.num_stokes = 3
+    pb.species[0].legcoef = _rayleigh6(0.85)
+    return pb
+
+
+def brdf_diner_problem():
+    pb = brdf_l1_problem()
+    zeta = np.linspace(0.0, 1.0 - 1.0 / 50, 50)[:, np.newaxis]
+    one = np.ones((50, 1))
+    par = np.stack([0.2 * one, 0.8 * one, 0.3 * one, zeta, -1.0 * one], axis=-1).astype(np.float32)
+    pb.surface_brdf, pb.surface_params = "D", par
     pb.surface_delx = pb.surface_dely = 0.02
     pb.num_stokes = 3
     pb.species[0].legcoef = _rayleigh6(0.85)

@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from at3d_gb300.scenes import cloud_blob, orthographic_views
-from brdf_scene import brdf_l1_problem, brdf_l1_rays, brdf_rpv_problem, brdf_wave_fresnel_problem
+from brdf_scene import brdf_diner_problem, brdf_l1_problem, brdf_l1_rays, brdf_rpv_problem, brdf_wave_fresnel_problem
 from oracle.oracle import Oracle
 
 pytestmark = pytest.mark.gpu
@@ -186,13 +186,13 @@ def test_odd_ray_count(rte_cls):
 
 
 
-@pytest.mark.parametrize("name", ["R1", "W1"])
+@pytest.mark.parametrize("name", ["R1", "W1", "D1"])
 def test_golden_brdf_surfaces(rte_cls, name):
-    """The reference's RPV and (polarized, I, Q, U) wave-Fresnel surface
-    scenes against original SHDOM output, with the reference test's
+    """The reference's RPV and (polarized, I, Q, U) wave-Fresnel and Diner
+    surface scenes against original SHDOM output, with the reference test's
     tolerances plus half the last printed digit."""
     import os
-    mk, iters = {"R1": (brdf_rpv_problem, 3), "W1": (brdf_wave_fresnel_problem, 4)}[name]
+    mk, iters = {"R1": (brdf_rpv_problem, 3), "W1": (brdf_wave_fresnel_problem, 4), "D1": (brdf_diner_problem, 4)}[name]
     g = np.load(os.path.join(os.path.dirname(__file__), "golden", f"brdf_{name}.npz"))
     r = rte_cls.from_problem(mk())
     it, _ = r.solve(100, verbose=False)

@@ -1,9 +1,9 @@
 """Pins the CPU oracle against the reference's own golden vectors.
 
-tests/data/brdf_{L,R,W}1{f,r}.out of the reference (original SHDOM output
-for the Verify_Lambertian_Surfaces, Verify_RPV_Surfaces and
-Verify_WaveFresnel_Surfaces scenes, tests/test_shdom.py:597-756; the last
-one polarized, Stokes I, Q, U) are stored as tests/golden/brdf_X1.npz by
+tests/data/brdf_{L,R,W,D}1{f,r}.out of the reference (original SHDOM
+output for the Verify_Lambertian_Surfaces, Verify_RPV_Surfaces,
+Verify_WaveFresnel_Surfaces and Verify_Diner_Surfaces scenes,
+tests/test_shdom.py:597-800; the last two polarized, Stokes I, Q, U) are stored as tests/golden/brdf_X1.npz by
 tests/golden/make_brdf_l1_fixture.py.  The reference test uses atol 4e-6
 (fluxes) and 9e-6 (radiance and Stokes components); the golden files print
 five significant digits, so the tolerance here adds half of the last
@@ -14,7 +14,7 @@ import os
 import numpy as np
 import pytest
 
-from brdf_scene import brdf_l1_problem, brdf_l1_rays, brdf_rpv_problem, brdf_wave_fresnel_problem
+from brdf_scene import brdf_diner_problem, brdf_l1_problem, brdf_l1_rays, brdf_rpv_problem, brdf_wave_fresnel_problem
 from oracle.oracle import Oracle
 
 GOLD = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "golden", "brdf_L1.npz"))
@@ -58,7 +58,7 @@ def test_radiances(solved):
     assert np.all(np.abs(got - ref) <= 9e-6 + _quantum(ref))
 
 
-SURFACES = {"R1": (brdf_rpv_problem, 3), "W1": (brdf_wave_fresnel_problem, 4)}
+SURFACES = {"R1": (brdf_rpv_problem, 3), "W1": (brdf_wave_fresnel_problem, 4), "D1": (brdf_diner_problem, 4)}
 
 
 @pytest.fixture(scope="module", params=sorted(SURFACES))
