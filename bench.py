@@ -343,7 +343,7 @@ def polarized_block(args, dev):
     from at3d_gb300.solver import RTE
     out = {"workload": "NSTOKES=3 64x64x40 blob (dx=dy=0.02 km, dz=0.04 km), NMU=8 NPHI=16, "
                        "64x64 px x 9 views (I, Q, U)", "boundaries": {}}
-    for bc in ("periodic", "open"):
+    for bc in args.pol_boundaries:
         pb = polarized_blob(boundary=bc)
         rays = orthographic_views(pb, 64, 64)
         nr = len(rays[0])
@@ -380,7 +380,7 @@ def polarized_block(args, dev):
         entry["rays"] = nr
         entry["mean_iqu"] = [float(np.mean(ref[:, k])) for k in range(3)]
         out["boundaries"][bc] = entry
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and "periodic" in out["boundaries"]:
         from oracle.oracle import Oracle
         pb = polarized_blob(boundary="periodic")
         t0 = time.perf_counter()
@@ -497,12 +497,22 @@ def main():
     ap.add_argument("--serve-rates", type=str, default="2", help="Poisson arrival rates (requests/s) to run")
     ap.add_argument("--serve-requests", type=int, default=16)
     ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--only", default="", choices=["", "precision", "gradient", "polarized", "serving"],
+                    help="run one extra block alone and print its JSON (for profiling)")
+    ap.add_argument("--pol-boundaries", type=str, default="periodic,open")
     args = ap.parse_args()
     args.serve_rates = [float(x) for x in args.serve_rates.split(",") if x]
+    args.pol_boundaries = [x for x in args.pol_boundaries.split(",") if x]
     args.jobs = args.jobs or args.nwave
     args.ref_iters = [int(x) for x in args.ref_iters.split(",")] if args.ref_iters else \
         SOLVE_ITERS[:args.nwave]
     rank, ws = dist_init()
+    if args.only:
+        dev = int(os.environ.get("LOCAL_RANK", "0"))
+        blk = {"precision": precision_block, "gradient": gradient_block, "polarized": polarized_block,
+               "serving": serving_block}[args.only]
+        print(json.dumps({args.only: blk(args, dev)}))
+        return
     if args.impl == "reference":
         out = reference_arm(args, rank, ws)
         if out:
