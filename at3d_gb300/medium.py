@@ -11,6 +11,8 @@
 * :func:`rayleigh_legcoef6` -- the six Wigner-function expansion elements
   (a1, a2, a3, a4, b1, b2) of the Rayleigh phase matrix with depolarisation
   (RAYLEIGH_PHASE_FUNCTION, src/polarized/shdomsub4.f:2350-2386).
+* :func:`gas_species` -- gaseous absorption as a non-scattering species,
+  the reference's own route for a 3D gas field (at3d/solver.py:1802-1840).
 * :func:`hg_matrix_legcoef6` -- a phase matrix whose I-I element is
   Henyey-Greenstein and whose polarization elements follow the same series
   scaled by a linear depolarisation factor (synthetic polarized medium).
@@ -18,6 +20,8 @@
 from __future__ import annotations
 
 import numpy as np
+
+from ._abi import Species
 
 
 def rayleigh_legcoef(wavelength: float) -> np.ndarray:
@@ -89,3 +93,17 @@ def hg_matrix_legcoef6(g: float, depol: float, nterms: int) -> np.ndarray:
     c[2, 2:] = (1.0 - depol) * a1[2:]
     c[3] = (1.0 - 2.0 * depol) * a1
     return c.astype(np.float32)
+
+
+def gas_species(gas_absorption, num_stokes: int = 1) -> Species:
+    """Gaseous absorption [1/km] on the property grid as a species with
+    single-scattering albedo 0 (its phase function is never used)."""
+    g = np.asarray(gas_absorption, np.float32)
+    if np.any(g < 0):
+        raise ValueError("gas_absorption must be non-negative")
+    leg = np.zeros((6, 2), np.float32) if num_stokes == 3 else np.zeros(2, np.float32)
+    if num_stokes == 3:
+        leg[0, 0] = 1.0
+    else:
+        leg[0] = 1.0
+    return Species(extinction=g, ssalb=np.zeros_like(g), legcoef=leg)

@@ -76,3 +76,27 @@ def brdf_diner_problem():
     pb.num_stokes = 3
     pb.species[0].legcoef = _rayleigh6(0.85)
     return pb
+
+
+def gas_absorption_problem():
+    """Verify_NonuniformGasAbsorption (tests/test_shdom.py:855-908 of the
+    reference): the same grid with the Rayleigh extinction set to zero and a
+    gaseous absorption growing linearly in x from 0 to 1 /km, overhead sun,
+    Lambertian albedo 0.04, TRANSCUT 0; the nadir radiance at 30 km is
+    exp(-tau) 0.04/pi exp(-tau) with tau = 30 km x absorption."""
+    from at3d_gb300.medium import gas_species
+    pb = brdf_l1_problem()
+    ray = pb.species[0]
+    ray.extinction = np.zeros_like(ray.extinction)
+    gas = np.broadcast_to(np.linspace(0.0, 1.0, 50)[:, None, None], ray.extinction.shape).astype(np.float32)
+    pb.species = [ray, gas_species(gas)]
+    pb.solarmu, pb.surface_albedo = -1.0, 0.04
+    pb.params.transcut = 0.0
+    return pb
+
+
+def gas_absorption_rays_and_truth():
+    x = np.linspace(0, 1.0 - 1.0 / 50, 50)
+    rays = (x, np.zeros(50), np.full(50, 30.0), np.ones(50), np.zeros(50))
+    tau = np.linspace(0.0, 1.0, 50) * 30.0
+    return rays, np.exp(-tau) * 0.04 / np.pi * np.exp(-tau)

@@ -210,3 +210,11 @@ def test_golden_brdf_surfaces(rte_cls, name):
     else:
         for k in range(3):
             assert np.all(np.abs(rad[:, k] - ra[:, 2 + k]) <= 9e-6 + q(ra[:, 2 + k])), k
+
+
+def test_gas_absorption_analytic(rte_cls):
+    from brdf_scene import gas_absorption_problem, gas_absorption_rays_and_truth
+    r = rte_cls.from_problem(gas_absorption_problem())
+    r.solve(100, verbose=False)
+    rays, truth = gas_absorption_rays_and_truth()
+    assert np.all(np.abs(r.render(*rays) - truth) <= 2e-7)

@@ -85,3 +85,13 @@ def test_brdf_surface_golden(solved_surface):
     else:
         for k in range(3):
             assert np.all(np.abs(rad[:, k] - ra[:, 2 + k]) <= 9e-6 + _quantum(ra[:, 2 + k])), k
+
+
+def test_gas_absorption_analytic():
+    """Gaseous absorption as a non-scattering species against the reference
+    test's closed form, atol 2e-7 (its own tolerance)."""
+    from brdf_scene import gas_absorption_problem, gas_absorption_rays_and_truth
+    o = Oracle(gas_absorption_problem())
+    o.solve(100)
+    rays, truth = gas_absorption_rays_and_truth()
+    assert np.all(np.abs(o.render(*rays) - truth) <= 2e-7)
