@@ -951,6 +951,92 @@ __global__ void __launch_bounds__(256) k_do_fluxes(const float *__restrict__ rad
   }
 }
 
+// ------------------------------------------------------------ direct beam
+// DIRECT_BEAM_PROP (src/polarized/shdom90.f90:352-867) via MAKE_DIRECT
+// (src/polarized/shdomsub2.f:393-476): per grid point, the delta-M scaled
+// extinction of the property grid integrated exactly (trilinear in each
+// property cell: a + b/2 + c/3 + d/4 of the segment) along the ray to the
+// sun, in double precision; one thread per point.
+struct BeamGeom {
+  const double *edp;      // [npx*npy*npz] delta-M scaled property-grid extinction
+  const float *zlev, *gridpos;
+  float *dirflux;
+  int npts, npx, npy, npz, bcflag, ipflag;
+  float delx, dely, solarmu, solaraz, solarflux;
+};
+
+__global__ void __launch_bounds__(128) k_direct_beam(BeamGeom b) {
+  const int ipt = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ipt >= b.npts) return;
+  const int npx = b.npx, npy = b.npy, npz = b.npz, bc = b.bcflag;
+  const int ipd = (b.ipflag & 4) ? 0 : b.ipflag;
+  const double sunmu = -(double)b.solarmu, sunaz = (double)(float)(b.solaraz + 3.14159274f);
+  double cx = sqrt(1.0 - sunmu * sunmu) * cos(sunaz), cy = sqrt(1.0 - sunmu * sunmu) * sin(sunaz);
+  double cz = fabs(sunmu), cxi, cyi, czi;
+  if (fabs(cx) > 1e-6) cxi = 1.0 / cx; else { cx = 0; cxi = 1e20; }
+  if (fabs(cy) > 1e-6) cyi = 1.0 / cy; else { cy = 0; cyi = 1e20; }
+  if (fabs(cz) > 1e-6) czi = 1.0 / cz; else { cz = 0; czi = 1e20; }
+  const int di = cx >= 0 ? 1 : -1, dj = cy >= 0 ? 1 : -1, dk = cz >= 0 ? 1 : -1;
+  const double epsz = 1.0e-6 * (b.zlev[npz - 1] - b.zlev[0]);
+  const double dxd = b.delx, dyd = b.dely, xdom = dxd * npx, ydom = dyd * npy;
+  const double z = b.gridpos[3 * ipt + 2], x = b.gridpos[3 * ipt], y = b.gridpos[3 * ipt + 1];
+  int il = 0, iu = npz;
+  while (iu - il > 1) { int im = (iu + il) / 2; if (z >= b.zlev[im - 1]) il = im; else iu = im; }
+  int k = max(il, 1), i = (int)(x / dxd) + 1, j = (int)(y / dyd) + 1;
+  if (i > npx && fabs(x - xdom) < 0.001 * dxd) i = npx;
+  if (j > npy && fabs(y - ydom) < 0.001 * dyd) j = npy;
+  double xe = x, ye = y, ze = z, xp = xe, yp = ye, zp = ze;
+  bool cxf = (ipd & 1) || cx == 0.0, cyf = (ipd & 2) || cy == 0.0;
+  if ((bc & 1) && (fabs(x) < 0.01 * dxd || fabs(x - (npx - 1) * dxd) < 0.01 * dxd)) cxf = true;
+  if ((bc & 2) && (fabs(y) < 0.01 * dyd || fabs(y - (npy - 1) * dyd) < 0.01 * dyd)) cyf = true;
+  double path = 0.0;
+  const int guard_max = 4 * (npx + npy + npz) * 64;
+  for (int guard = 0; fabs(ze - b.zlev[npz - 1]) > epsz && guard < guard_max; ++guard) {
+    const int ipn = (i == npx) ? ((bc & 1) ? npx : 1) : i + 1, jpn = (j == npy) ? ((bc & 2) ? npy : 1) : j + 1;
+    const double x0 = dxd * (i - 1), x1 = x0 + dxd, y0 = dyd * (j - 1), y1 = y0 + dyd, z0 = b.zlev[k - 1], z1 = b.zlev[k];
+    const int I1 = (k - 1) + npz * (j - 1) + npz * npy * (i - 1), I2 = (k - 1) + npz * (j - 1) + npz * npy * (ipn - 1);
+    const int I3 = (k - 1) + npz * (jpn - 1) + npz * npy * (i - 1), I4 = (k - 1) + npz * (jpn - 1) + npz * npy * (ipn - 1);
+    const double e1 = b.edp[I1], e2 = b.edp[I2], e3 = b.edp[I3], e4 = b.edp[I4];
+    const double e5 = b.edp[I1 + 1], e6 = b.edp[I2 + 1], e7 = b.edp[I3 + 1], e8 = b.edp[I4 + 1];
+    double sox, soy, soz;
+    if (cxf) sox = 1e30; else if (cx > 0) { sox = (x1 - xe) * cxi; xp = x1; } else { sox = (x0 - xe) * cxi; xp = x0; }
+    if (cyf) soy = 1e30; else if (cy > 0) { soy = (y1 - ye) * cyi; yp = y1; } else { soy = (y0 - ye) * cyi; yp = y0; }
+    if (cz > 0) { soz = (z1 - ze) * czi; zp = z1; } else if (cz < 0) { soz = (z0 - ze) * czi; zp = z0; } else soz = 1e30;
+    double xo = 0, yo = 0, so;
+    if (soz <= sox && soz <= soy) {
+      so = soz; if (!cxf) xp = xe + so * cx; if (!cyf) yp = ye + so * cy; k += dk;
+    } else if (sox <= soy) {
+      so = sox; if (!cyf) yp = ye + so * cy; zp = ze + so * cz; i += di;
+      if (i == 0) { if (bc & 1) { i = 1; cxf = true; } else { i = npx; xo = xdom; } }
+      else if (i == npx + 1) { if (bc & 1) { i = npx; cxf = true; } else { i = 1; xo = -xdom; } }
+    } else {
+      so = soy; if (!cxf) xp = xe + so * cx; zp = ze + so * cz; j += dj;
+      if (j == 0) { if (bc & 2) { j = 1; cyf = true; } else { j = npy; yo = ydom; } }
+      else if (j == npy + 1) { if (bc & 2) { j = npy; cyf = true; } else { j = 1; yo = -ydom; } }
+    }
+    so = fmax(so, 0.0);
+    const double ax = 1.0 / (x1 - x0), ay = 1.0 / (y1 - y0), az = 1.0 / (z1 - z0);
+    const double u0 = (xe - x0) * ax, v0 = (ye - y0) * ay, w0 = (ze - z0) * az;
+    const double du = (xp - x0) * ax - u0, dv = (yp - y0) * ay - v0, dw = (zp - z0) * az - w0;
+    const double u0m = 1 - u0, v0m = 1 - v0, w0m = 1 - w0;
+    const double A = (e1 * u0m + e2 * u0) * v0m * w0m + (e3 * u0m + e4 * u0) * v0 * w0m +
+                     (e5 * u0m + e6 * u0) * v0m * w0 + (e7 * u0m + e8 * u0) * v0 * w0;
+    const double B = (-du * v0m * w0m - dv * u0m * w0m - dw * u0m * v0m) * e1 + (du * v0m * w0m - dv * u0 * w0m - dw * u0 * v0m) * e2 +
+                     (-du * v0 * w0m + dv * u0m * w0m - dw * u0m * v0) * e3 + (du * v0 * w0m + dv * u0 * w0m - dw * u0 * v0) * e4 +
+                     (-du * v0m * w0 - dv * u0m * w0 + dw * u0m * v0m) * e5 + (du * v0m * w0 - dv * u0 * w0 + dw * u0 * v0m) * e6 +
+                     (-du * v0 * w0 + dv * u0m * w0 + dw * u0m * v0) * e7 + (du * v0 * w0 + dv * u0 * w0 + dw * u0 * v0) * e8;
+    const double vw = dv * dw, uw = du * dw, uv = du * dv;
+    const double Cc = (vw * u0m + uw * v0m + uv * w0m) * e1 + (vw * u0 - uw * v0m - uv * w0m) * e2 +
+                      (-vw * u0m + uw * v0 - uv * w0m) * e3 + (-vw * u0 - uw * v0 + uv * w0m) * e4 +
+                      (-vw * u0m - uw * v0m + uv * w0) * e5 + (-vw * u0 + uw * v0m - uv * w0) * e6 +
+                      (vw * u0m - uw * v0 - uv * w0) * e7 + (vw * u0 + uw * v0 + uv * w0) * e8;
+    const double D = du * dv * dw * (e2 + e3 + e5 + e8 - e1 - e4 - e6 - e7);
+    path += so * (A + 0.5 * B + 0.3333333333333333 * Cc + 0.25 * D);
+    xe = xp + xo; ye = yp + yo; ze = zp;
+  }
+  b.dirflux[ipt] = (float)(b.solarflux * exp(-path));
+}
+
 // ------------------------------------------------ bidirectional surfaces
 // SURFACE_BRDF (src/polarized/shdomsub2.f:1222-1300) for the built types:
 // 'R' RPV_REFLECTION (:1658-1696, single precision), 'W'
@@ -1722,6 +1808,9 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
     double taugrid = so * 0.5 * (ext1 + extn);
     int ntau = max(1, 1 + (int)(taugrid * inv_tautol));
     const float delsf = sof / (float)ntau;
+    // the cell's source integral and transmission from its entry, in FP32;
+    // folded into the FP64 ray accumulators once per cell
+    float cacc = 0.f, ctr = 1.f;
     for (int it = 1; it <= ntau; ++it) {
       const float sf_ = it * delsf;
       const float uu_ = fmaf(sf_, du, u0), vv_ = fmaf(sf_, dv, v0), ww_ = fmaf(sf_, dw, w0);
@@ -1736,10 +1825,12 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
         src = (0.5f * (srcext0 + srcext1) + 0.08333333333f * (ext0 * srcext1 - ext1 * srcext0) * delsf *
                                                 (1.f - 0.05f * (ext1 - ext0) * delsf)) / ext;
       } else { absc = 0.f; trc = 1.f; src = 0.f; }
-      radacc += transmit * src * absc;
-      transmit *= trc;
+      cacc = fmaf(ctr * src, absc, cacc);
+      ctr *= trc;
       ext1 = ext0; srcext1 = srcext0;
     }
+    radacc += transmit * (double)cacc;
+    transmit *= (double)ctr;
     int iface, jface;
     bool openbc;
     if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; openbc = (cf & 1) && (a.bcflag & 1); }
@@ -2022,6 +2113,7 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render_pol(RenderArgs a) {
     double taugrid = so * 0.5 * (ext1 + extn);
     int ntau = max(1, 1 + (int)(taugrid * inv_tautol));
     const float delsf = sof / (float)ntau;
+    float cacc[3] = {0.f, 0.f, 0.f}, ctr = 1.f;  // as in k_render: per cell in FP32, folded once per cell
     for (int it = 1; it <= ntau; ++it) {
       const float sf_ = it * delsf;
       const float uu_ = fmaf(sf_, du, u0), vv_ = fmaf(sf_, dv, v0), ww_ = fmaf(sf_, dw, w0);
@@ -2040,14 +2132,17 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render_pol(RenderArgs a) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const float src = (0.5f * (srcext0[c] + srcext1[c]) + 0.08333333333f * (ext0 * srcext1[c] - ext1 * srcext0[c]) * corr) * iext;
-          radacc[c] += transmit * src * absc;
+          cacc[c] = fmaf(ctr * src, absc, cacc[c]);
         }
       } else { trc = 1.f; }
-      transmit *= trc;
+      ctr *= trc;
       ext1 = ext0;
 #pragma unroll
       for (int c = 0; c < 3; ++c) srcext1[c] = srcext0[c];
     }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) radacc[c] += transmit * (double)cacc[c];
+    transmit *= (double)ctr;
     int iface, jface;
     bool openbc;
     if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; openbc = (cf & 1) && (a.bcflag & 1); }
@@ -2513,7 +2608,7 @@ static long long plan_device_bytes(const Plan &P) {
     b += vbytes(P.tasks[h]) + vbytes(P.segs[h]) + vbytes(P.seg_off[h]) + vbytes(P.level_items[h]) + 32LL * P.nirr[h];
   b += 8LL * P.npts * ((P.nang + 3) & ~3) + vbytes(P.kind);  // (radsrc, tr) per point and ordinate
   b += 4LL * 5 * P.nang + vbytes(P.cmu1) + vbytes(P.cmu2) + vbytes(P.cphi1) + vbytes(P.cphi2) + vbytes(P.ylmsun);
-  b += vbytes(P.nphi0) + vbytes(P.col_of) + vbytes(P.total_ext) + vbytes(P.dirflux) + vbytes(P.coef) + vbytes(P.tms_ptr);
+  b += vbytes(P.nphi0) + vbytes(P.col_of) + vbytes(P.total_ext) + 4LL * P.npts + vbytes(P.coef) + vbytes(P.tms_ptr);
   b += vbytes(P.tms_iph) + vbytes(P.tms_w) + vbytes(P.phasetab) + vbytes(P.botalb) + vbytes(P.rad0);
   const long long ldo = (P.nang + 3) & ~3;
   b += 4LL * P.npts * (3LL * P.nst * P.nlm + 2 * ldo + 2 + 3) + 4LL * (long long)P.botp.size() + 64;
@@ -2610,7 +2705,22 @@ static void upload_plan(Handle &H) {
     H.cmu1t.upload(c1t); H.cmu2t.upload(c2t); H.cphi1t.upload(p1t); H.cphi2.upload(P.cphi2);
     H.nphi0.upload(P.nphi0); H.col_of.upload(P.col_of);
   }
-  H.text.upload(P.total_ext); H.dirflux.upload(P.dirflux); H.coef.upload(P.coef);
+  H.text.upload(P.total_ext); H.coef.upload(P.coef);
+  {  // direct beam of every grid point (DIRECT_BEAM_PROP) on the device
+    DBuf<double> edp;
+    edp.upload(P.extdirp);
+    CK(cudaStreamSynchronize(cudaStreamLegacy));
+    H.dirflux.alloc(P.npts);
+    BeamGeom g;
+    g.edp = edp.p; g.zlev = H.zgrid.p; g.gridpos = H.gridpos.p; g.dirflux = H.dirflux.p;
+    g.npts = P.npts; g.npx = P.prob.npx; g.npy = P.prob.npy; g.npz = P.prob.npz; g.bcflag = P.bcflag;
+    g.ipflag = P.ipflag; g.delx = P.prob.delx; g.dely = P.prob.dely; g.solarmu = P.prob.solarmu;
+    g.solaraz = P.prob.solaraz; g.solarflux = P.prob.solarflux;
+    k_direct_beam<<<(P.npts + 127) / 128, 128, 0, H.stream>>>(g);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(H.stream));
+    H.launches += 1;
+  }
   {
     // scattering points (a non-zero coefficient row makes a non-zero source), spread to their cells' corners
     const int nl = P.ml + 1;

@@ -675,79 +675,106 @@ bool build_medium(const shdom_problem &p, Plan &P) {
   P.coef.assign((size_t)npts * nl, 0.f);
   if (nstleg == 6) P.coefp.assign((size_t)npts * 3 * nl, 0.f);
   else P.coefp.clear();
-  std::vector<double> ltp(nstleg == 6 ? 3 * nl : 0);
-  std::vector<float> ltp1(nstleg == 6 ? 3 * nl : 0);
   P.tms_ptr.assign(npts + 1, 0);
   P.tms_iph.clear(); P.tms_w.clear();
-  std::vector<float> lt1(nleg + 1);
-  std::vector<double> lt(nleg + 1);
-  for (int ipt = 0; ipt < npts; ++ipt) {
-    double sumscat = 0.0;
-    std::fill(lt.begin(), lt.end(), 0.0);
-    std::fill(ltp.begin(), ltp.end(), 0.0);
-    float etot = P.total_ext[ipt];
-    for (int ipa = 0; ipa < npart; ++ipa) {
-      size_t o = (size_t)ipa * npts + ipt;
-      const int *IP = &iph[o * nq];
-      const float *PW = &pw[o * nq];
-      std::fill(lt1.begin(), lt1.end(), 0.f);
-      bool single = PW[0] >= phasemax;
-      if (single) for (int l = 0; l <= nleg; ++l) lt1[l] = leg[(size_t)(IP[0] - 1) * (nleg + 1) + l];
-      else
-        for (int q = 0; q < nq; ++q) {
-          if (PW[q] <= 1e-5f) continue;
-          for (int l = 0; l <= nleg; ++l) lt1[l] += leg[(size_t)(IP[q] - 1) * (nleg + 1) + l] * PW[q];
-        }
-      float f = 0.f;
-      if (p.deltam) { f = lt1[ml + 1]; for (int l = 0; l <= ml; ++l) lt1[l] /= (1.f - f); }
-      {  // the species' own series, delta-M scaling undone (COMPUTE_SOURCE_GRAD_1CELL)
-        P.sp_f[o] = f;
-        float *u = &P.sp_legu[o * (ml + 1)];
-        for (int l = 0; l <= ml; ++l) u[l] = p.deltam ? lt1[l] * (1.f - f) + f : lt1[l];
-      }
-      double scat = (double)(ext[o] * alb[o]);
-      sumscat += scat;
-      for (int l = 0; l <= nleg; ++l) lt[l] += scat * lt1[l];
-      if (nstleg == 6) {  // a2, a3, b1 mixed the same way (all six elements are divided by 1 - f)
-        std::fill(ltp1.begin(), ltp1.end(), 0.f);
-        for (int e = 0; e < 3; ++e) {
-          float *L1 = &ltp1[(size_t)e * nl];
-          if (single) for (int l = 0; l < nl; ++l) L1[l] = legp3[((size_t)(IP[0] - 1) * 3 + e) * (nleg + 1) + l];
-          else
-            for (int q = 0; q < nq; ++q) {
-              if (PW[q] <= 1e-5f) continue;
-              for (int l = 0; l < nl; ++l) L1[l] += legp3[((size_t)(IP[q] - 1) * 3 + e) * (nleg + 1) + l] * PW[q];
-            }
-          if (p.deltam) for (int l = 0; l < nl; ++l) L1[l] /= (1.f - f);
-          for (int l = 0; l < nl; ++l) ltp[(size_t)e * nl + l] += scat * L1[l];
-        }
-      }
-      // exact single scatter: weight (albedo * ext_ipa / ext) / (1 - f) per phase function
-      float wgt = (etot == 0.f) ? 1.f : ext[o] / etot;
-      if (wgt != 0.f && p.deltam) {
-        float base = alb[o] * wgt / (1.f - f);
-        if (single) { P.tms_iph.push_back(IP[0] - 1); P.tms_w.push_back(base); }
+  // two passes over the points on host threads: the coefficients and the
+  // number of single-scatter entries of each point, then (after the prefix
+  // sum) the entries themselves
+  std::vector<int> tcnt(npts, 0);
+  parallel_for(npts, [&](int pb, int pe) {
+    std::vector<double> ltp(nstleg == 6 ? 3 * nl : 0);
+    std::vector<float> ltp1(nstleg == 6 ? 3 * nl : 0);
+    std::vector<float> lt1(nleg + 1);
+    std::vector<double> lt(nleg + 1);
+    for (int ipt = pb; ipt < pe; ++ipt) {
+      double sumscat = 0.0;
+      std::fill(lt.begin(), lt.end(), 0.0);
+      std::fill(ltp.begin(), ltp.end(), 0.0);
+      float etot = P.total_ext[ipt];
+      int nt = 0;
+      for (int ipa = 0; ipa < npart; ++ipa) {
+        size_t o = (size_t)ipa * npts + ipt;
+        const int *IP = &iph[o * nq];
+        const float *PW = &pw[o * nq];
+        std::fill(lt1.begin(), lt1.end(), 0.f);
+        bool single = PW[0] >= phasemax;
+        if (single) for (int l = 0; l <= nleg; ++l) lt1[l] = leg[(size_t)(IP[0] - 1) * (nleg + 1) + l];
         else
           for (int q = 0; q < nq; ++q) {
             if (PW[q] <= 1e-5f) continue;
-            P.tms_iph.push_back(IP[q] - 1); P.tms_w.push_back(base * PW[q]);
+            for (int l = 0; l <= nleg; ++l) lt1[l] += leg[(size_t)(IP[q] - 1) * (nleg + 1) + l] * PW[q];
+          }
+        float f = 0.f;
+        if (p.deltam) { f = lt1[ml + 1]; for (int l = 0; l <= ml; ++l) lt1[l] /= (1.f - f); }
+        {  // the species' own series, delta-M scaling undone (COMPUTE_SOURCE_GRAD_1CELL)
+          P.sp_f[o] = f;
+          float *u = &P.sp_legu[o * (ml + 1)];
+          for (int l = 0; l <= ml; ++l) u[l] = p.deltam ? lt1[l] * (1.f - f) + f : lt1[l];
+        }
+        double scat = (double)(ext[o] * alb[o]);
+        sumscat += scat;
+        for (int l = 0; l <= nleg; ++l) lt[l] += scat * lt1[l];
+        if (nstleg == 6) {  // a2, a3, b1 mixed the same way (all six elements are divided by 1 - f)
+          std::fill(ltp1.begin(), ltp1.end(), 0.f);
+          for (int e = 0; e < 3; ++e) {
+            float *L1 = &ltp1[(size_t)e * nl];
+            if (single) for (int l = 0; l < nl; ++l) L1[l] = legp3[((size_t)(IP[0] - 1) * 3 + e) * (nleg + 1) + l];
+            else
+              for (int q = 0; q < nq; ++q) {
+                if (PW[q] <= 1e-5f) continue;
+                for (int l = 0; l < nl; ++l) L1[l] += legp3[((size_t)(IP[q] - 1) * 3 + e) * (nleg + 1) + l] * PW[q];
+              }
+            if (p.deltam) for (int l = 0; l < nl; ++l) L1[l] /= (1.f - f);
+            for (int l = 0; l < nl; ++l) ltp[(size_t)e * nl + l] += scat * L1[l];
+          }
+        }
+        // exact single scatter entries of this species
+        float wgt = (etot == 0.f) ? 1.f : ext[o] / etot;
+        if (wgt != 0.f && p.deltam) {
+          if (single) ++nt;
+          else
+            for (int q = 0; q < nq; ++q) nt += PW[q] > 1e-5f;
+        }
+      }
+      tcnt[ipt] = nt;
+      double albp = (etot > 1e-10f) ? sumscat / etot : 0.0;
+      for (int l = 0; l <= ml; ++l) {
+        double chi = (sumscat > 1e-10) ? lt[l] / sumscat : lt[l] / npart;
+        if (l == 0) chi = 1.0;
+        P.coef[(size_t)ipt * nl + l] = (float)(albp * chi);
+      }
+      if (nstleg == 6)
+        for (int e = 0; e < 3; ++e)
+          for (int l = 0; l < nl; ++l) {
+            const double chi = (sumscat > 1e-10) ? ltp[(size_t)e * nl + l] / sumscat : ltp[(size_t)e * nl + l] / npart;
+            P.coefp[((size_t)ipt * 3 + e) * nl + l] = (float)(albp * chi);
+          }
+    }
+  });
+  for (int ipt = 0; ipt < npts; ++ipt) P.tms_ptr[ipt + 1] = P.tms_ptr[ipt] + tcnt[ipt];
+  P.tms_iph.assign(P.tms_ptr[npts], 0);
+  P.tms_w.assign(P.tms_ptr[npts], 0.f);
+  // exact single scatter: weight (albedo * ext_ipa / ext) / (1 - f) per phase function
+  parallel_for(npts, [&](int pb, int pe) {
+    for (int ipt = pb; ipt < pe; ++ipt) {
+      int w0 = P.tms_ptr[ipt];
+      const float etot = P.total_ext[ipt];
+      for (int ipa = 0; ipa < npart; ++ipa) {
+        const size_t o = (size_t)ipa * npts + ipt;
+        const int *IP = &iph[o * nq];
+        const float *PW = &pw[o * nq];
+        const float wgt = (etot == 0.f) ? 1.f : ext[o] / etot;
+        if (!(wgt != 0.f && p.deltam)) continue;
+        const float base = alb[o] * wgt / (1.f - P.sp_f[o]);
+        if (PW[0] >= phasemax) { P.tms_iph[w0] = IP[0] - 1; P.tms_w[w0] = base; ++w0; }
+        else
+          for (int q = 0; q < nq; ++q) {
+            if (PW[q] <= 1e-5f) continue;
+            P.tms_iph[w0] = IP[q] - 1; P.tms_w[w0] = base * PW[q]; ++w0;
           }
       }
     }
-    double albp = (etot > 1e-10f) ? sumscat / etot : 0.0;
-    for (int l = 0; l <= ml; ++l) {
-      double chi = (sumscat > 1e-10) ? lt[l] / sumscat : lt[l] / npart;
-      if (l == 0) chi = 1.0;
-      P.coef[(size_t)ipt * nl + l] = (float)(albp * chi);
-    }
-    if (nstleg == 6)
-      for (int e = 0; e < 3; ++e)
-        for (int l = 0; l < nl; ++l) {
-          const double chi = (sumscat > 1e-10) ? ltp[(size_t)e * nl + l] / sumscat : ltp[(size_t)e * nl + l] / npart;
-          P.coefp[((size_t)ipt * 3 + e) * nl + l] = (float)(albp * chi);
-        }
-    P.tms_ptr[ipt + 1] = (int)P.tms_iph.size();
-  }
+  });
   // Eddington initial radiance per column (INIT_RADIANCE).
   P.rad0.assign((size_t)npts * 4, 0.f);
   const int nz = P.nz, nlay = nz - 1;
@@ -892,8 +919,11 @@ bool build_medium(const shdom_problem &p, Plan &P) {
 // of the property grid along the ray to the sun (trilinear extinction
 // integrated exactly within each property cell).
 void build_direct(const shdom_problem &p, Plan &P) {
+  // The delta-M scaled extinction of the property grid (the EXTDIRP field of
+  // DIRECT_BEAM_PROP); the per-point path integrals to the sun run on the
+  // device (k_direct_beam) when the plan is put on a GPU.
   const int npx = p.npx, npy = p.npy, npz = p.npz, ng = npx * npy * npz, ml = P.ml, nmic = p.maxnmicro;
-  std::vector<double> edp(ng, 0.0);
+  P.extdirp.assign(ng, 0.0);
   for (int ip = 0; ip < ng; ++ip) {
     float acc = 0.f;
     for (int ipa = 0; ipa < p.npart; ++ipa) {
@@ -910,78 +940,8 @@ void build_direct(const shdom_problem &p, Plan &P) {
       }
       acc = (float)(acc + e);
     }
-    edp[ip] = acc;
+    P.extdirp[ip] = acc;
   }
-  const int ipd = (P.ipflag & 4) ? 0 : P.ipflag, bc = P.bcflag;
-  const double sunmu = -(double)p.solarmu, sunaz = (double)(float)(p.solaraz + (float)std::acos(-1.0f));
-  double cx = std::sqrt(1.0 - sunmu * sunmu) * std::cos(sunaz), cy = std::sqrt(1.0 - sunmu * sunmu) * std::sin(sunaz);
-  double cz = std::fabs(sunmu), cxi, cyi, czi;
-  if (std::fabs(cx) > 1e-6) cxi = 1.0 / cx; else { cx = 0; cxi = 1e20; }
-  if (std::fabs(cy) > 1e-6) cyi = 1.0 / cy; else { cy = 0; cyi = 1e20; }
-  if (std::fabs(cz) > 1e-6) czi = 1.0 / cz; else { cz = 0; czi = 1e20; }
-  const int di = cx >= 0 ? 1 : -1, dj = cy >= 0 ? 1 : -1, dk = cz >= 0 ? 1 : -1;
-  const double epsz = 1.0e-6 * (p.zlevels[npz - 1] - p.zlevels[0]);
-  const double dxd = p.delx, dyd = p.dely, xdom = dxd * npx, ydom = dyd * npy;
-  P.dirflux.assign(P.npts, 0.f);
-  parallel_for(P.npts, [&](int b, int e) {
-    for (int ipt = b; ipt < e; ++ipt) {
-      double z = P.gridpos[3 * ipt + 2], x = P.gridpos[3 * ipt], y = P.gridpos[3 * ipt + 1];
-      int il = 0, iu = npz;
-      while (iu - il > 1) { int im = (iu + il) / 2; if (z >= p.zlevels[im - 1]) il = im; else iu = im; }
-      int k = std::max(il, 1), i = (int)(x / dxd) + 1, j = (int)(y / dyd) + 1;
-      if (i > npx && std::fabs(x - xdom) < 0.001 * dxd) i = npx;
-      if (j > npy && std::fabs(y - ydom) < 0.001 * dyd) j = npy;
-      double xe = x, ye = y, ze = z, xp = xe, yp = ye, zp = ze;
-      bool cxf = (ipd & 1) || cx == 0.0, cyf = (ipd & 2) || cy == 0.0;
-      if ((bc & 1) && (std::fabs(x) < 0.01 * dxd || std::fabs(x - (npx - 1) * dxd) < 0.01 * dxd)) cxf = true;
-      if ((bc & 2) && (std::fabs(y) < 0.01 * dyd || std::fabs(y - (npy - 1) * dyd) < 0.01 * dyd)) cyf = true;
-      double path = 0.0;
-      for (int guard = 0; std::fabs(ze - p.zlevels[npz - 1]) > epsz && guard < 4 * (npx + npy + npz) * 64; ++guard) {
-        int ipn = (i == npx) ? ((bc & 1) ? npx : 1) : i + 1, jpn = (j == npy) ? ((bc & 2) ? npy : 1) : j + 1;
-        double x0 = dxd * (i - 1), x1 = x0 + dxd, y0 = dyd * (j - 1), y1 = y0 + dyd, z0 = p.zlevels[k - 1], z1 = p.zlevels[k];
-        int I1 = (k - 1) + npz * (j - 1) + npz * npy * (i - 1), I2 = (k - 1) + npz * (j - 1) + npz * npy * (ipn - 1);
-        int I3 = (k - 1) + npz * (jpn - 1) + npz * npy * (i - 1), I4 = (k - 1) + npz * (jpn - 1) + npz * npy * (ipn - 1);
-        double e1 = edp[I1], e2 = edp[I2], e3 = edp[I3], e4 = edp[I4], e5 = edp[I1 + 1], e6 = edp[I2 + 1], e7 = edp[I3 + 1], e8 = edp[I4 + 1];
-        double sox, soy, soz;
-        if (cxf) sox = 1e30; else if (cx > 0) { sox = (x1 - xe) * cxi; xp = x1; } else { sox = (x0 - xe) * cxi; xp = x0; }
-        if (cyf) soy = 1e30; else if (cy > 0) { soy = (y1 - ye) * cyi; yp = y1; } else { soy = (y0 - ye) * cyi; yp = y0; }
-        if (cz > 0) { soz = (z1 - ze) * czi; zp = z1; } else if (cz < 0) { soz = (z0 - ze) * czi; zp = z0; } else soz = 1e30;
-        double xo = 0, yo = 0, so;
-        if (soz <= sox && soz <= soy) {
-          so = soz; if (!cxf) xp = xe + so * cx; if (!cyf) yp = ye + so * cy; k += dk;
-        } else if (sox <= soy) {
-          so = sox; if (!cyf) yp = ye + so * cy; zp = ze + so * cz; i += di;
-          if (i == 0) { if (bc & 1) { i = 1; cxf = true; } else { i = npx; xo = xdom; } }
-          else if (i == npx + 1) { if (bc & 1) { i = npx; cxf = true; } else { i = 1; xo = -xdom; } }
-        } else {
-          so = soy; if (!cxf) xp = xe + so * cx; zp = ze + so * cz; j += dj;
-          if (j == 0) { if (bc & 2) { j = 1; cyf = true; } else { j = npy; yo = ydom; } }
-          else if (j == npy + 1) { if (bc & 2) { j = npy; cyf = true; } else { j = 1; yo = -ydom; } }
-        }
-        so = std::max(so, 0.0);
-        double ax = 1.0 / (x1 - x0), ay = 1.0 / (y1 - y0), az = 1.0 / (z1 - z0);
-        double u0 = (xe - x0) * ax, v0 = (ye - y0) * ay, w0 = (ze - z0) * az;
-        double du = (xp - x0) * ax - u0, dv = (yp - y0) * ay - v0, dw = (zp - z0) * az - w0;
-        double u0m = 1 - u0, v0m = 1 - v0, w0m = 1 - w0;
-        // trilinear extinction integrated along the segment: a + b/2 + c/3 + d/4
-        double A = (e1 * u0m + e2 * u0) * v0m * w0m + (e3 * u0m + e4 * u0) * v0 * w0m +
-                   (e5 * u0m + e6 * u0) * v0m * w0 + (e7 * u0m + e8 * u0) * v0 * w0;
-        double B = (-du * v0m * w0m - dv * u0m * w0m - dw * u0m * v0m) * e1 + (du * v0m * w0m - dv * u0 * w0m - dw * u0 * v0m) * e2 +
-                   (-du * v0 * w0m + dv * u0m * w0m - dw * u0m * v0) * e3 + (du * v0 * w0m + dv * u0 * w0m - dw * u0 * v0) * e4 +
-                   (-du * v0m * w0 - dv * u0m * w0 + dw * u0m * v0m) * e5 + (du * v0m * w0 - dv * u0 * w0 + dw * u0 * v0m) * e6 +
-                   (-du * v0 * w0 + dv * u0m * w0 + dw * u0m * v0) * e7 + (du * v0 * w0 + dv * u0 * w0 + dw * u0 * v0) * e8;
-        double vw = dv * dw, uw = du * dw, uv = du * dv;
-        double Cc = (vw * u0m + uw * v0m + uv * w0m) * e1 + (vw * u0 - uw * v0m - uv * w0m) * e2 +
-                    (-vw * u0m + uw * v0 - uv * w0m) * e3 + (-vw * u0 - uw * v0 + uv * w0m) * e4 +
-                    (-vw * u0m - uw * v0m + uv * w0) * e5 + (-vw * u0 + uw * v0m - uv * w0) * e6 +
-                    (vw * u0m - uw * v0 - uv * w0) * e7 + (vw * u0 + uw * v0 + uv * w0) * e8;
-        double D = du * dv * dw * (e2 + e3 + e5 + e8 - e1 - e4 - e6 - e7);
-        path += so * (A + 0.5 * B + 0.3333333333333333 * Cc + 0.25 * D);
-        xe = xp + xo; ye = yp + yo; ze = zp;
-      }
-      P.dirflux[ipt] = (float)(p.solarflux * std::exp(-path));
-    }
-  });
 }
 
 bool build_schedule(const shdom_problem &p, Plan &P) {

@@ -80,7 +80,8 @@ struct Plan {
   std::vector<float> ylmsun;                     // [nlm]
   // ---- medium on the grid
   int npart = 0, numphase = 0;
-  std::vector<float> total_ext, dirflux;
+  std::vector<float> total_ext;
+  std::vector<double> extdirp;                   // [npx*npy*npz] delta-M scaled extinction for the direct beam
   std::vector<float> coef;                       // [npts][ml+1]: albedo * delta-M scaled Legendre term
   std::vector<float> coefp;                      // nst = 3: [npts][3][ml+1] the same for a2, a3 and b1
   std::vector<int> tms_ptr, tms_iph;             // CSR per point: exact single-scatter mixture
