@@ -30,6 +30,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <list>
 #include <mutex>
 #include <stdexcept>
 #include <string>
@@ -2210,10 +2211,16 @@ template <class T>
 struct DBuf {
   T *p = nullptr;
   size_t n = 0;
+  bool own = true;  // false: a view of a buffer that a shared geometry owns
   void alloc(size_t k) {
     free();
     n = k;
+    own = true;
     if (k) CK(cudaMalloc(&p, k * sizeof(T)));
+  }
+  void view(const DBuf &o) {
+    free();
+    p = o.p; n = o.n; own = false;
   }
   void upload(const std::vector<T> &v) {
     alloc(v.size());
@@ -2221,12 +2228,35 @@ struct DBuf {
   }
   // on the handle's (non-blocking) stream, so that later kernels on it are ordered after the fill
   void zero(cudaStream_t st) { if (n) CK(cudaMemsetAsync(p, 0, n * sizeof(T), st)); }
-  void free() { if (p) cudaFree(p); p = nullptr; n = 0; }
+  void free() { if (p && own) cudaFree(p); p = nullptr; n = 0; own = true; }
   ~DBuf() { free(); }
 };
 
+// Device copies of a plan's grid geometry and sweep schedule: shared by all
+// handles whose plans share the host geometry (the wavelengths of one
+// medium, inversion iterates), so a new handle uploads only its medium and
+// allocates only its state.  The last few stay cached after their handles
+// are gone.
+struct DevGeom {
+  int device = -1;
+  std::shared_ptr<const void> key;  // the host geometry (the plan's level table)
+  DBuf<float> gridpos, xgrid, ygrid, zgrid, geo;
+  DBuf<int> gridptr, neighptr, cellflags, rank, start, level, order, topp, botp, bot_index;
+  DBuf<uint8_t> bnd, regular, kind;
+  DBuf<uint32_t> tasks[2];
+  DBuf<Seg> segs[2], p1segs[2], irrsegs[2];
+  DBuf<int> seg_off[2], level_items[2], p1off[2];
+  DBuf<IrrRec> irr[2];
+  bool irr_built = false;
+  std::mutex mu;  // guards the one-time build of irr
+};
+static std::mutex g_devgeom_mu;
+static std::list<std::shared_ptr<DevGeom>> g_devgeom;  // most recent first
+constexpr size_t kDevGeomCache = 2;
+
 struct Handle {
   Plan P;
+  std::shared_ptr<DevGeom> geom;  // device geometry shared with other handles on the same grid
   std::string err;
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -2591,6 +2621,8 @@ static void setup_tc(Handle &H) {
 // solution state and the tensor-core transform matrices.
 template <typename T>
 static long long vbytes(const std::vector<T> &v) { return (long long)v.size() * (long long)sizeof(T); }
+template <typename T>
+static long long vbytes(const SharedVec<T> &v) { return (long long)v.size() * (long long)sizeof(T); }
 
 // A hemisphere is swept in the reference order when its wavefront is too
 // deep for level scheduling.
@@ -2641,17 +2673,56 @@ static void fill_sizes(const Plan &P, shdom_sizes *o) {
 static void upload_plan(Handle &H) {
   Plan &P = H.P;
   H.nst = P.nst;
-  H.gridpos.upload(P.gridpos); H.xgrid.upload(P.xgrid); H.ygrid.upload(P.ygrid); H.zgrid.upload(P.zgrid);
-  H.gridptr.upload(P.gridptr); H.neighptr.upload(P.neighptr); H.cellflags.upload(P.cellflags);
-  H.rank.upload(P.rank); H.start.upload(P.startcell); H.level.upload(P.level);
-  {
-    std::vector<int> ord((size_t)8 * P.npts, 0);
-    for (int b = 0; b < 8; ++b)
-      for (int i = 0; i < P.npts; ++i) {
-        int r = P.rank[(size_t)b * P.npts + i];
-        if (r >= 0) ord[(size_t)b * P.npts + r] = i;
+  {  // the grid geometry and sweep schedule: shared with handles on the same grid and device
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    std::shared_ptr<const void> key = P.level.owner();
+    std::lock_guard<std::mutex> lk(g_devgeom_mu);
+    for (auto it = g_devgeom.begin(); it != g_devgeom.end(); ++it)
+      if ((*it)->device == dev && (*it)->key == key) { H.geom = *it; g_devgeom.splice(g_devgeom.begin(), g_devgeom, it); break; }
+    if (!H.geom) {
+      auto G = std::make_shared<DevGeom>();
+      G->device = dev; G->key = key;
+      G->gridpos.upload(P.gridpos); G->xgrid.upload(P.xgrid); G->ygrid.upload(P.ygrid); G->zgrid.upload(P.zgrid);
+      G->gridptr.upload(P.gridptr); G->neighptr.upload(P.neighptr); G->cellflags.upload(P.cellflags);
+      G->rank.upload(P.rank); G->start.upload(P.startcell); G->level.upload(P.level);
+      std::vector<int> ord((size_t)8 * P.npts, 0);
+      for (int b = 0; b < 8; ++b)
+        for (int i = 0; i < P.npts; ++i) {
+          int r = P.rank[(size_t)b * P.npts + i];
+          if (r >= 0) ord[(size_t)b * P.npts + r] = i;
+        }
+      G->order.upload(ord);
+      G->regular.upload(P.regular); G->geo.upload(P.geo);
+      G->bnd.upload(P.bnd); G->topp.upload(P.topp); G->botp.upload(P.botp);
+      std::vector<int> bi(P.npts, -1);
+      for (size_t k = 0; k < P.botp.size(); ++k) bi[P.botp[k]] = (int)k;
+      G->bot_index.upload(bi);
+      for (int h = 0; h < 2; ++h) {
+        G->tasks[h].upload(P.tasks[h]); G->segs[h].upload(P.segs[h]);
+        G->seg_off[h].upload(P.seg_off[h]); G->level_items[h].upload(P.level_items[h]);
+        G->p1segs[h].upload(P.p1segs[h]); G->p1off[h].upload(P.p1off[h]);
+        // general-trace segments of both phases in irr0 order
+        std::vector<Seg> is(P.p1segs[h]);
+        for (const Seg &g : P.segs[h]) if (!g.regular) is.push_back(g);
+        G->irrsegs[h].upload(is);
       }
-    H.order.upload(ord);
+      G->kind.upload(P.kind);
+      g_devgeom.emplace_front(G);
+      while (g_devgeom.size() > kDevGeomCache) g_devgeom.pop_back();
+      H.geom = G;
+    }
+    DevGeom &G = *H.geom;
+    H.gridpos.view(G.gridpos); H.xgrid.view(G.xgrid); H.ygrid.view(G.ygrid); H.zgrid.view(G.zgrid);
+    H.gridptr.view(G.gridptr); H.neighptr.view(G.neighptr); H.cellflags.view(G.cellflags);
+    H.rank.view(G.rank); H.start.view(G.start); H.level.view(G.level); H.order.view(G.order);
+    H.regular.view(G.regular); H.geo.view(G.geo); H.bnd.view(G.bnd); H.topp.view(G.topp); H.botp.view(G.botp);
+    H.bot_index.view(G.bot_index); H.kind.view(G.kind);
+    for (int h = 0; h < 2; ++h) {
+      H.tasks[h].view(G.tasks[h]); H.segs[h].view(G.segs[h]); H.seg_off[h].view(G.seg_off[h]);
+      H.level_items[h].view(G.level_items[h]); H.p1segs[h].view(G.p1segs[h]); H.p1off[h].view(G.p1off[h]);
+      H.irrsegs[h].view(G.irrsegs[h]);
+    }
   }
   for (int h = 0; h < 2; ++h) {
     int nlev = (int)P.seg_off[h].size() - 1;
@@ -2660,25 +2731,15 @@ static void upload_plan(Handle &H) {
       if (P.seg_off[h][l + 1] - P.seg_off[h][l] > MAXSEG) throw std::runtime_error("sweep schedule: too many segments in a level");
   }
 
-  H.regular.upload(P.regular); H.geo.upload(P.geo);
-  H.bnd.upload(P.bnd); H.topp.upload(P.topp); H.botp.upload(P.botp); H.lofj.upload(P.lofj);
-  std::vector<int> bi(P.npts, -1);
-  for (size_t k = 0; k < P.botp.size(); ++k) bi[P.botp[k]] = (int)k;
-  H.bot_index.upload(bi);
+  H.lofj.upload(P.lofj);
   for (int h = 0; h < 2; ++h) {
-    H.tasks[h].upload(P.tasks[h]); H.segs[h].upload(P.segs[h]);
-    H.seg_off[h].upload(P.seg_off[h]); H.level_items[h].upload(P.level_items[h]);
-    H.p1segs[h].upload(P.p1segs[h]); H.p1off[h].upload(P.p1off[h]);
-    // general-trace segments of both phases in irr0 order
-    std::vector<Seg> is(P.p1segs[h]);
-    H.p2_irrseg0[h] = (int)is.size();
+    H.p2_irrseg0[h] = (int)P.p1segs[h].size();
     H.p2_irr_j0[h] = 0;
     for (const Seg &g : P.p1segs[h]) H.p2_irr_j0[h] = std::max(H.p2_irr_j0[h], g.irr0 + g.ntask * g.ncol);
-    for (const Seg &g : P.segs[h]) if (!g.regular) is.push_back(g);
-    H.n_irrseg[h] = (int)is.size();
-    H.irrsegs[h].upload(is);
+    int nis = (int)P.p1segs[h].size();
+    for (const Seg &g : P.segs[h]) if (!g.regular) ++nis;
+    H.n_irrseg[h] = nis;
   }
-  H.kind.upload(P.kind);
   {
     std::vector<int> cls(P.col_cls.begin(), P.col_cls.end());
     H.col_oct.upload(P.col_oct); H.col_cls.upload(cls);
@@ -2900,17 +2961,26 @@ static SweepArgs sweep_args(Handle &H, int hemi) {
 // they depend on the geometry and the sweep schedule only).
 static void build_irr(Handle &H) {
   Plan &P = H.P;
-  for (int h = 0; h < 2; ++h) {
-    H.irr[h].alloc((size_t)std::max<long long>(P.nirr[h], 1));
-    if (P.nirr[h] == 0 || H.n_irrseg[h] == 0 || H.seq[h]) continue;
-    SweepArgs a = sweep_args(H, h);
-    const int nirr = (int)P.nirr[h];
-    const int blocks = std::min((nirr + 255) / 256, 152 * 16);
-    k_irr_build<<<blocks, 256, 0, H.stream>>>(a, H.irrsegs[h].p, H.n_irrseg[h], nirr, H.irr[h].p);
-    CK(cudaGetLastError());
-    H.launches += 1;
+  {  // once per shared geometry (the records depend on the grid and schedule only)
+    DevGeom &G = *H.geom;
+    std::lock_guard<std::mutex> lk(G.mu);
+    if (!G.irr_built) {
+      for (int h = 0; h < 2; ++h) {
+        G.irr[h].alloc((size_t)std::max<long long>(P.nirr[h], 1));
+        H.irr[h].view(G.irr[h]);
+        if (P.nirr[h] == 0 || H.n_irrseg[h] == 0 || H.seq[h]) continue;
+        SweepArgs a = sweep_args(H, h);
+        const int nirr = (int)P.nirr[h];
+        const int blocks = std::min((nirr + 255) / 256, 152 * 16);
+        k_irr_build<<<blocks, 256, 0, H.stream>>>(a, H.irrsegs[h].p, H.n_irrseg[h], nirr, G.irr[h].p);
+        CK(cudaGetLastError());
+        H.launches += 1;
+      }
+      CK(cudaStreamSynchronize(H.stream));
+      G.irr_built = true;
+    }
+    for (int h = 0; h < 2; ++h) H.irr[h].view(G.irr[h]);
   }
-  CK(cudaStreamSynchronize(H.stream));
   H.sweepw.alloc((size_t)P.npts * H.ldo);
   {  // phase 1 runs on a high-priority stream so its blocks start before the source pass fills the SMs
     int lo = 0, hi = 0;

@@ -191,11 +191,11 @@ bool build_grid(const shdom_problem &p, Plan &P) {
   for (int i = 0; i <= ny; ++i) P.ygrid[i] = ((float)i * (dyp * (float)p.npy)) / (float)ny;
   P.zgrid.assign(p.zlevels, p.zlevels + p.npz);
   P.npts = P.nx1 * P.ny1 * nz;
-  P.gridpos.resize((size_t)P.npts * 3);
+  P.gridpos.mut().resize((size_t)P.npts * 3);
   for (int ix = 0, i = 0; ix < P.nx1; ++ix)
     for (int iy = 0; iy < P.ny1; ++iy)
       for (int iz = 0; iz < nz; ++iz, ++i) {
-        P.gridpos[3 * i] = P.xgrid[ix]; P.gridpos[3 * i + 1] = P.ygrid[iy]; P.gridpos[3 * i + 2] = P.zgrid[iz];
+        P.gridpos.mut()[3 * i] = P.xgrid[ix]; P.gridpos.mut()[3 * i + 1] = P.ygrid[iy]; P.gridpos.mut()[3 * i + 2] = P.zgrid[iz];
       }
   int nxc = (bc & 1) ? nx + 1 : nx, nyc = (bc & 2) ? ny + 1 : ny;
   P.ncells = nxc * nyc * (nz - 1);
@@ -211,25 +211,25 @@ bool build_grid(const shdom_problem &p, Plan &P) {
       if (ip & 2) { y0 = y1 = iy; } else if (bc & 2) { y0 = std::max(1, iy - 1); y1 = std::min(ny, iy); } else { y0 = iy; y1 = iy + 1; }
       for (int iz = 1; iz < nz; ++iz, ++ic) {
         auto pt = [&](int z, int y, int x) { return (z - 1) + nz * (y - 1) + nz * P.ny1 * (x - 1); };
-        int *g = &P.gridptr[8 * (size_t)ic];
+        int *g = &P.gridptr.mut()[8 * (size_t)ic];
         g[0] = pt(iz, y0, x0); g[1] = pt(iz, y0, x1); g[2] = pt(iz, y1, x0); g[3] = pt(iz, y1, x1);
         g[4] = pt(iz + 1, y0, x0); g[5] = pt(iz + 1, y0, x1); g[6] = pt(iz + 1, y1, x0); g[7] = pt(iz + 1, y1, x1);
-        int *nb = &P.neighptr[6 * (size_t)ic];
+        int *nb = &P.neighptr.mut()[6 * (size_t)ic];
         int sx = (nz - 1) * nyc, sy = nz - 1;
-        if (ip & 1) { nb[0] = nb[1] = ic; P.cellflags[ic] |= 1; }
+        if (ip & 1) { nb[0] = nb[1] = ic; P.cellflags.mut()[ic] |= 1; }
         else if (bc & 1) {
           nb[0] = (ix == 1) ? ic : ic - sx;
           nb[1] = (ix == nxc) ? ic : ic + sx;
-          if (ix == 1 || ix == nxc) P.cellflags[ic] |= 1;
+          if (ix == 1 || ix == nxc) P.cellflags.mut()[ic] |= 1;
         } else {
           nb[0] = (ix == 1) ? ic + (nxc - 1) * sx : ic - sx;
           nb[1] = (ix == nx) ? ic - (nxc - 1) * sx : ic + sx;
         }
-        if (ip & 2) { nb[2] = nb[3] = ic; P.cellflags[ic] |= 2; }
+        if (ip & 2) { nb[2] = nb[3] = ic; P.cellflags.mut()[ic] |= 2; }
         else if (bc & 2) {
           nb[2] = (iy == 1) ? ic : ic - sy;
           nb[3] = (iy == nyc) ? ic : ic + sy;
-          if (iy == 1 || iy == nyc) P.cellflags[ic] |= 2;
+          if (iy == 1 || iy == nyc) P.cellflags.mut()[ic] |= 2;
         } else {
           nb[2] = (iy == 1) ? ic + (nyc - 1) * sy : ic - sy;
           nb[3] = (iy == ny) ? ic - (nyc - 1) * sy : ic + sy;
@@ -259,8 +259,8 @@ void sweep_order(Plan &P, int ioct) {
   if (b & 2) { diy = 1; if (bc & 2) { siy = nyc; eiy = std::max(nyc - 1, 1); } else { siy = 1; eiy = nyc; } }
   else { diy = -1; if (bc & 2) { siy = 1; eiy = std::min(2, nyc); } else { siy = nyc; eiy = 1; } }
   if (b & 4) { diz = 1; siz = 1; eiz = nz - 1; } else { diz = -1; siz = nz - 1; eiz = 1; }
-  int *rk = &P.rank[(size_t)b * P.npts];
-  int *sc = &P.startcell[(size_t)b * P.npts];
+  int *rk = &P.rank.mut()[(size_t)b * P.npts];
+  int *sc = &P.startcell.mut()[(size_t)b * P.npts];
   std::fill(rk, rk + P.npts, -1);
   int order = 0, ix = six, iy = siy, iz = siz;
   while (true) {
@@ -977,12 +977,12 @@ bool build_schedule(const shdom_problem &p, Plan &P) {
           int q = g[k];
           if (q == pt || !((P.bnd[q] & hemi_bnd) || rk[q] < r)) fast = false;
         }
-        if (fast) P.regular[(size_t)b * n + pt] = 1;
+        if (fast) P.regular.mut()[(size_t)b * n + pt] = 1;
         for (int cls = 0; cls < 4; ++cls) {
           const int nc = P.cls_ncol[b][cls], c0 = P.cls_col0[b][cls];
           if (nc == 0) continue;
-          int *lv = &P.level[((size_t)b * 4 + cls) * n];
-          uint8_t *kd = &P.kind[((size_t)b * 4 + cls) * n];
+          int *lv = &P.level.mut()[((size_t)b * 4 + cls) * n];
+          uint8_t *kd = &P.kind.mut()[((size_t)b * 4 + cls) * n];
           // the corners the point's traces for this class end on
           corners.clear();
           if (fast) {
@@ -1035,7 +1035,7 @@ bool build_schedule(const shdom_problem &p, Plan &P) {
     for (int ioct : octs)
       if (((((ioct - 1) >> 2) & 1) == hemi) && deep[ioct - 1]) P.deep[hemi] = 1;
     if (P.deep[hemi]) {
-      P.tasks[hemi].clear(); P.p1segs[hemi].clear(); P.p1off[hemi].assign(1, 0); P.p1depth[hemi] = 0;
+      P.tasks[hemi].mut().clear(); P.p1segs[hemi].clear(); P.p1off[hemi].assign(1, 0); P.p1depth[hemi] = 0;
       P.segs[hemi].clear(); P.seg_off[hemi].assign(1, 0); P.level_items[hemi].clear();
       P.nirr[hemi] = 0; P.nitems[hemi] = 0;
       continue;
@@ -1048,7 +1048,7 @@ bool build_schedule(const shdom_problem &p, Plan &P) {
         if (P.cls_ncol[b][cls] > 0) groups.push_back({b, cls});
     }
     const int ng = (int)groups.size();
-    std::vector<uint32_t> &tasks = P.tasks[hemi];
+    std::vector<uint32_t> &tasks = P.tasks[hemi].mut();
     tasks.clear();
     long long irr = 0;
     // Phase 1: per (octant, class) group, one segment per level.

@@ -9,12 +9,43 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
 #include "../../include/shdom_problem.h"
 
 namespace shdom {
+
+// A vector shared between plans of the same grid geometry (the host keeps a
+// cache of geometry plans; a new plan takes references to the large tables
+// instead of copies).  Reads go through the const interface; writes go
+// through mut(), which copies the table first when another plan shares it.
+template <class T>
+class SharedVec {
+ public:
+  SharedVec() : p_(std::make_shared<std::vector<T>>()) {}
+  size_t size() const { return p_->size(); }
+  bool empty() const { return p_->empty(); }
+  const T *data() const { return p_->data(); }
+  const T &operator[](size_t i) const { return (*p_)[i]; }
+  typename std::vector<T>::const_iterator begin() const { return p_->begin(); }
+  typename std::vector<T>::const_iterator end() const { return p_->end(); }
+  operator const std::vector<T> &() const { return *p_; }
+  const std::vector<T> &vec() const { return *p_; }
+  // identity of the shared table (plans that share it share its device copy too)
+  std::shared_ptr<const void> owner() const { return p_; }
+  std::vector<T> &mut() {
+    if (p_.use_count() > 1) p_ = std::make_shared<std::vector<T>>(*p_);
+    return *p_;
+  }
+  void assign(size_t n, const T &v) { mut().assign(n, v); }
+  template <class It>
+  void assign(It a, It b) { mut().assign(a, b); }
+
+ private:
+  std::shared_ptr<std::vector<T>> p_;
+};
 
 // One group of sweep tasks at one wavefront level: the points (tasks[t0,
 // t0+ntask)) of trace octant b whose traces for the ordinates of face class
@@ -33,24 +64,24 @@ struct Plan {
   int nx = 0, ny = 0, nz = 0, nx1 = 0, ny1 = 0, npts = 0, ncells = 0;
   int bcflag = 0, ipflag = 0, is1d = 0, noct = 8;
   std::vector<float> xgrid, ygrid, zgrid;
-  std::vector<float> gridpos;      // [npts][3]
-  std::vector<int> gridptr;        // [ncells][8]
-  std::vector<int> neighptr;       // [ncells][6]
-  std::vector<int> cellflags;      // [ncells]
+  SharedVec<float> gridpos;        // [npts][3]
+  SharedVec<int> gridptr;          // [ncells][8]
+  SharedVec<int> neighptr;         // [ncells][6]
+  SharedVec<int> cellflags;        // [ncells]
   std::vector<uint8_t> bnd;        // [npts] bit0 top boundary point, bit1 bottom
   std::vector<int> topp, botp;     // boundary point lists in point order
   // ---- sweep order per trace octant (index ioct-1): rank and start cell
-  std::vector<int> rank;           // [8][npts], -1 when the octant is unused
-  std::vector<int> startcell;      // [8][npts]
-  std::vector<int> level;          // [8][4][npts] wavefront level per octant and face class (0: preset)
+  SharedVec<int> rank;             // [8][npts], -1 when the octant is unused
+  SharedVec<int> startcell;        // [8][npts]
+  SharedVec<int> level;            // [8][4][npts] wavefront level per octant and face class (0: preset)
   // kind[8][4][npts]: 0 preset or unused, 1 phase-2 regular trace, 2 phase-2
   // general trace, 3 phase 1 (a general-trace point whose dependencies are
   // all preset or phase-1 points: the open-boundary planes' own chains).
-  std::vector<uint8_t> kind;
+  SharedVec<uint8_t> kind;
   // regular[b][p] = 1 when point p's trace for trace octant b crosses one
   // full interior cell whose seven other corners all precede p; such traces
   // depend only on the ordinate and the z layer, tabulated in geo.
-  std::vector<uint8_t> regular;    // [8][npts]
+  SharedVec<uint8_t> regular;      // [8][npts]
   std::vector<float> geo;          // [nz-1][nang][4]: so, u, v, face
   // ---- discrete ordinates
   // nang counts the ordinate columns including the padding ordinates that
@@ -112,7 +143,7 @@ struct Plan {
   // ---- numerical parameters
   shdom_problem prob{};
   // ---- wavefront schedule, per hemisphere (0 down, 1 up)
-  std::vector<uint32_t> tasks[2];                // point indices: phase-1 segments, then phase-2 levels
+  SharedVec<uint32_t> tasks[2];                  // point indices: phase-1 segments, then phase-2 levels
   std::vector<Seg> p1segs[2];                    // phase 1: one segment per level per (octant, class) group
   std::vector<int> p1off[2];                     // group -> first segment (ngroups + 1 entries)
   int p1depth[2] = {0, 0};
