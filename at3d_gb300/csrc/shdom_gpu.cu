@@ -952,6 +952,21 @@ __global__ void __launch_bounds__(256) k_do_fluxes(const float *__restrict__ rad
   }
 }
 
+// Marks every corner of each cell that has a scattering corner (nb zeroed
+// beforehand; concurrent writes all store 1).
+__global__ void k_spread_scat(const int *__restrict__ gridptr, int ncells, const uint8_t *__restrict__ sc,
+                              uint8_t *__restrict__ nb) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  const int *g = gridptr + 8 * (size_t)c;
+  bool any = false;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) any = any || sc[g[k]];
+  if (any)
+#pragma unroll
+    for (int k = 0; k < 8; ++k) nb[g[k]] = 1;
+}
+
 // ------------------------------------------------------------ direct beam
 // DIRECT_BEAM_PROP (src/polarized/shdom90.f90:352-867) via MAKE_DIRECT
 // (src/polarized/shdomsub2.f:393-476): per grid point, the delta-M scaled
@@ -2300,6 +2315,7 @@ struct Handle {
   DBuf<int> nphi0, col_of;
   // medium
   DBuf<float> text, dirflux, coef, tms_w, phasetab, botalb, rad0;
+  DBuf<double> edp;      // delta-M scaled property-grid extinction (input of the direct beam)
   DBuf<uint8_t> nbscat;  // 1 where a cell containing the point has a scattering corner
   DBuf<int> wready;      // per hemisphere: the source pass has filled every item once
   DBuf<int> tms_ptr, tms_iph;
@@ -2596,13 +2612,8 @@ static void setup_tc(Handle &H) {
   // cores; the others get their 4 radiance terms and fluxes on the CUDA
   // cores.  (Not with HIGHORDERRAD, which keeps every radiance term.)
   if (H.tc_ok[0] && H.tc_ok[1] && !P.prob.highorderrad && P.nlm >= 4 && H.nst == 1) {
-    const int nl = P.ml + 1;
     std::vector<int> hv, lt;
-    for (int p = 0; p < P.npts; ++p) {
-      bool sc = false;
-      for (int l = 0; l < nl && !sc; ++l) sc = P.coef[(size_t)p * nl + l] != 0.f;
-      (sc ? hv : lt).push_back(p);
-    }
+    for (int p = 0; p < P.npts; ++p) (P.scat[p] ? hv : lt).push_back(p);
     if (!lt.empty() && (long long)hv.size() * 10 < (long long)P.npts * 9) {
       H.compact = true;
       H.nheavy = (int)hv.size(); H.nlight = (int)lt.size();
@@ -2646,11 +2657,8 @@ static long long plan_device_bytes(const Plan &P) {
   b += 4LL * P.npts * (3LL * P.nst * P.nlm + 2 * ldo + 2 + 3) + 4LL * (long long)P.botp.size() + 64;
   if (P.nst == 3) b += vbytes(P.col_stk) + vbytes(P.coefp) + vbytes(P.phasetab2) + 8LL * P.nlm * 3 * P.nang;
   {  // gathered rows of the scattering points for the compacted transforms
-    const int nl = P.ml + 1;
     long long nh = 0;
-    for (int p = 0; p < P.npts; ++p)
-      for (int l = 0; l < nl; ++l)
-        if (P.coef[(size_t)p * nl + l] != 0.f) { ++nh; break; }
+    for (int p = 0; p < P.npts; ++p) nh += P.scat[p];
     if (nh * 10 < (long long)P.npts * 9) b += 4LL * nh * (P.nlm + ldo) + 4LL * P.npts + 16LL * P.nang;
   }
   const long long nsh = (long long)P.nst * P.nlm;
@@ -2767,36 +2775,30 @@ static void upload_plan(Handle &H) {
     H.nphi0.upload(P.nphi0); H.col_of.upload(P.col_of);
   }
   H.text.upload(P.total_ext); H.coef.upload(P.coef);
-  {  // direct beam of every grid point (DIRECT_BEAM_PROP) on the device
-    DBuf<double> edp;
-    edp.upload(P.extdirp);
+  {  // direct beam of every grid point (DIRECT_BEAM_PROP) on the device, on the handle's stream
+    H.edp.upload(P.extdirp);
     CK(cudaStreamSynchronize(cudaStreamLegacy));
     H.dirflux.alloc(P.npts);
     BeamGeom g;
-    g.edp = edp.p; g.zlev = H.zgrid.p; g.gridpos = H.gridpos.p; g.dirflux = H.dirflux.p;
+    g.edp = H.edp.p; g.zlev = H.zgrid.p; g.gridpos = H.gridpos.p; g.dirflux = H.dirflux.p;
     g.npts = P.npts; g.npx = P.prob.npx; g.npy = P.prob.npy; g.npz = P.prob.npz; g.bcflag = P.bcflag;
     g.ipflag = P.ipflag; g.delx = P.prob.delx; g.dely = P.prob.dely; g.solarmu = P.prob.solarmu;
     g.solaraz = P.prob.solaraz; g.solarflux = P.prob.solarflux;
     k_direct_beam<<<(P.npts + 127) / 128, 128, 0, H.stream>>>(g);
     CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(H.stream));
     H.launches += 1;
   }
   {
     // scattering points (a non-zero coefficient row makes a non-zero source), spread to their cells' corners
-    const int nl = P.ml + 1;
-    std::vector<uint8_t> sc(P.npts, 0), nb(P.npts, 0);
-    for (int p = 0; p < P.npts; ++p)
-      for (int l = 0; l < nl; ++l)
-        if (P.coef[(size_t)p * nl + l] != 0.f) { sc[p] = 1; break; }
-    for (int c = 0; c < P.ncells; ++c) {
-      const int *g = &P.gridptr[8 * (size_t)c];
-      bool any = false;
-      for (int k = 0; k < 8; ++k) any = any || sc[g[k]];
-      if (any)
-        for (int k = 0; k < 8; ++k) nb[g[k]] = 1;
-    }
-    H.nbscat.upload(nb);
+    DBuf<uint8_t> sc;
+    sc.upload(P.scat);
+    CK(cudaStreamSynchronize(cudaStreamLegacy));
+    H.nbscat.alloc(P.npts);
+    H.nbscat.zero(H.stream);
+    if (P.ncells > 0) k_spread_scat<<<(P.ncells + 255) / 256, 256, 0, H.stream>>>(H.gridptr.p, P.ncells, sc.p, H.nbscat.p);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(H.stream));
+    H.launches += 1;
     H.wready.alloc(2);
     H.wready.zero(H.stream);
   }

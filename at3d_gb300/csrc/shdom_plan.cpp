@@ -751,6 +751,9 @@ bool build_medium(const shdom_problem &p, Plan &P) {
           }
     }
   });
+  // scattering points: the coefficient row is non-zero exactly when its l = 0 term (the albedo) is
+  P.scat.assign(npts, 0);
+  for (int ipt = 0; ipt < npts; ++ipt) P.scat[ipt] = P.coef[(size_t)ipt * nl] != 0.f;
   for (int ipt = 0; ipt < npts; ++ipt) P.tms_ptr[ipt + 1] = P.tms_ptr[ipt] + tcnt[ipt];
   P.tms_iph.assign(P.tms_ptr[npts], 0);
   P.tms_w.assign(P.tms_ptr[npts], 0.f);

@@ -115,6 +115,7 @@ struct Plan {
   std::vector<double> extdirp;                   // [npx*npy*npz] delta-M scaled extinction for the direct beam
   std::vector<float> coef;                       // [npts][ml+1]: albedo * delta-M scaled Legendre term
   std::vector<float> coefp;                      // nst = 3: [npts][3][ml+1] the same for a2, a3 and b1
+  std::vector<uint8_t> scat;                     // [npts] 1 where the point scatters (a non-zero coefficient row)
   std::vector<int> tms_ptr, tms_iph;             // CSR per point: exact single-scatter mixture
   std::vector<float> tms_w;
   std::vector<float> phasetab;                   // [nscatangle][numphase]
