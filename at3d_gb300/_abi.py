@@ -37,6 +37,8 @@ class ShdomProblem(C.Structure):
         ("transmin", C.c_float),
         ("nstokes", C.c_int),
         ("sfc_brdf", C.c_int), ("nsfcpar", C.c_int), ("sfc_params", _f),
+        ("srctype", C.c_int), ("units", C.c_int), ("wavelen", C.c_float),
+        ("tempp", _f), ("sfc_temp", _f),
     ]
 
 
@@ -99,6 +101,11 @@ class Problem:
     num_stokes: int = 1               # 1 (scalar) or 3 (I, Q, U)
     surface_brdf: str = ""            # '' Lambertian (surface_albedo), or 'R' / 'W' with surface_params
     surface_params: np.ndarray | None = None  # [nxsfc, nysfc, nparams] on (surface_delx, surface_dely)
+    srctype: str = "S"                # 'S' solar, 'T' thermal, 'B' both (at3d.source solar/thermal/combined)
+    units: str = "R"                  # thermal units: 'R' radiance, 'T' brightness temperature
+    wavelength: float = 0.0           # micron (Planck function)
+    temperature: np.ndarray | None = None       # [npx, npy, npz] K, required for 'T' and 'B'
+    ground_temperature: float | np.ndarray = 288.0  # K; an array lives on the surface grid [nxsfc, nysfc]
     _keep: list = field(default_factory=list, repr=False)
 
     @property
@@ -184,7 +191,8 @@ class Problem:
             st.delxsfc, st.delysfc = self.surface_delx, self.surface_dely
             st.sfc_albedo = _fp(buf)
             st.gndalbedo = float(sa2.mean())
-        st.gndtemp = 288.0
+        gt = np.asarray(self.ground_temperature, np.float32)
+        st.gndtemp = float(gt.reshape(-1)[0]) if gt.size == 1 else float(gt.mean())
         if self.surface_brdf:
             par = np.asarray(self.surface_params, np.float32)
             if par.ndim != 3:
@@ -203,5 +211,22 @@ class Problem:
         st.solacc, st.shacc, st.splitacc = p.solution_accuracy, p.spherical_harmonics_accuracy, p.split_accuracy
         st.tautol, st.transcut, st.transmin = p.tautol, p.transcut, p.transmin
         st.nstokes = self.num_stokes
+        if self.srctype not in ("S", "T", "B"):
+            raise ValueError("srctype must be 'S', 'T' or 'B'")
+        if self.units not in ("R", "T"):
+            raise ValueError("units must be 'R' (radiance) or 'T' (brightness temperature)")
+        st.srctype, st.units, st.wavelen = ord(self.srctype), ord(self.units), float(self.wavelength)
+        if self.srctype != "S":
+            if self.temperature is None:
+                raise KeyError("a thermal source needs the temperature of the medium")
+            tp = np.ascontiguousarray(np.broadcast_to(np.asarray(self.temperature, np.float32), (npx, npy, npz)))
+            keep.append(tp)
+            st.tempp = _fp(tp)
+            if gt.size > 1:
+                if gt.shape != (st.nxsfc, st.nysfc):
+                    raise ValueError("a ground temperature array lives on the surface grid [nxsfc, nysfc]")
+                gbuf = np.ascontiguousarray(gt.T, np.float32)  # [nysfc][nxsfc]
+                keep.append(gbuf)
+                st.sfc_temp = _fp(gbuf)
         self._keep = keep
         return st

@@ -861,8 +861,12 @@ __global__ void k_preset_top(const int *topp, int ntop, float *raddo, int ldo, i
   raddo[(size_t)topp[k] * ldo + c] = (stk && stk[c]) ? 0.f : skyrad;
 }
 
+// FIXED/VARIABLE_LAMBERTIAN_BOUNDARY (src/polarized/shdomsub1.f:2438-2529):
+// the reflected direct beam and downwelling flux plus, with a thermal
+// source, the ground emission (1 - albedo) B (botplanck null otherwise).
 __global__ void k_lambertian(const int *botp, int nbot, const float *botalb, const float *dirflux, const float *fluxw,
-                             float *raddo, int nang, int ldo, int ncol_down, float *bcrad, const uint8_t *stk) {
+                             float *raddo, int nang, int ldo, int ncol_down, float *bcrad, const uint8_t *stk,
+                             const float *botplanck) {
   int k = blockIdx.x;
   if (k >= nbot) return;
   int p = botp[k];
@@ -877,6 +881,7 @@ __global__ void k_lambertian(const int *botp, int nbot, const float *botalb, con
   }
   const float opi = 0.318309886f;
   float b = opi * botalb[k] * (dirflux[p] + red[0]);
+  if (botplanck) b += botplanck[k] * (1.f - botalb[k]);
   if (threadIdx.x == 0) bcrad[k] = b;
   for (int c = ncol_down + threadIdx.x; c < nang; c += blockDim.x) raddo[(size_t)p * ldo + c] = (stk && stk[c]) ? 0.f : b;
 }
@@ -1212,7 +1217,8 @@ __device__ __forceinline__ void surface_brdf_d(int type, const float *par, float
 __global__ void __launch_bounds__(128) k_brdf_bottom(const int *__restrict__ botp, int nbot, const float *__restrict__ botpar,
                                                      int npar, int type, const BrdfOrd *__restrict__ dn, int ndn,
                                                      const BrdfOrd *__restrict__ up, int nup, const float *__restrict__ dirflux,
-                                                     float solarmu, float solaraz, float *raddo, int ldo, int nst) {
+                                                     float solarmu, float solaraz, float *raddo, int ldo, int nst,
+                                                     const float *__restrict__ botplanck) {
   const int b = blockIdx.x;
   if (b >= nbot) return;
   const int p = botp[b];
@@ -1232,6 +1238,11 @@ __global__ void __launch_bounds__(128) k_brdf_bottom(const int *__restrict__ bot
         const float rin = row[ci + k1 * oi];
         for (int k = 0; k < nst; ++k) out[k] += i.w * R[k][k1] * rin;
       }
+      if (botplanck) {  // polarized thermal emission, emissivity 1 - R11
+        const float bp = botplanck[b];
+        out[0] += i.w * (1.f - R[0][0]) * bp;
+        for (int k = 1; k < nst; ++k) out[k] -= i.w * R[k][0] * bp;
+      }
     }
     const int co = (int)o.col, oo = (int)o.off;
     for (int k = 0; k < nst; ++k) raddo[(size_t)p * ldo + co + k * oo] = out[k];
@@ -1243,6 +1254,7 @@ struct SourceArgs {
   const float *coef;      // [npts][nl]
   const float *coefp;     // polarized: [npts][3][nl] a2, a3, b1 times the albedo
   const float *dirflux, *radiance, *ylmsun;
+  const float *thermal;   // thermal source: [npts] extinction-weighted (1 - albedo) B(T), else null
   const int *lofj;
   float *source, *delsource;
   int *ns, *nso, *nr;     // nr is read (current) and rewritten (next)
@@ -1294,6 +1306,7 @@ __global__ void __launch_bounds__(256) k_source(SourceArgs a) {
           for (int q = 0; q < 4; ++q) {
             const float c = cf[a.lofj[j + q]];
             jt[q] = f0 * c * yv[q];
+            if (j + q == 0 && a.thermal) jt[q] += 3.544907703f * a.thermal[p];  // isotropic emission, sqrt(4 pi) B
             if (j + q < nrp) jt[q] += c * rv[q];
             dnew[q] = 0.f;
             if (!a.first) {
@@ -1324,6 +1337,7 @@ __global__ void __launch_bounds__(256) k_source(SourceArgs a) {
       if (j < a.nlm) {
         float c = cf[a.lofj[j]];
         jt = f0 * c * a.ylmsun[j];
+        if (j == 0 && a.thermal) jt += 3.544907703f * a.thermal[p];
         if (j < nrp) jt += c * R[j];
         if (!a.first) {
           float sold = S[j];
@@ -1424,6 +1438,7 @@ __global__ void __launch_bounds__(256) k_source_pol(SourceArgs a) {
         const float ri = j < nrp ? R[j] : 0.f, rq = j < nrp ? R[nlm + j] : 0.f, ru = j < nrp ? R[2 * nlm + j] : 0.f;
         const float ys = f0 * a.ylmsun[j], ca = c1[l], ca2 = cp[l], ca3 = cp[nl + l], cb1 = cp[2 * nl + l];
         jt[0] = ca * ys + ca * ri + cb1 * rq;
+        if (j == 0 && a.thermal) jt[0] += 3.544907703f * a.thermal[p];  // unpolarized emission
         if (j >= 4) { jt[1] = cb1 * ri + ca2 * rq + cb1 * ys; jt[2] = ca3 * ru; }
         if (!a.first) {
 #pragma unroll
@@ -1564,6 +1579,7 @@ struct RenderArgs {
   // the last sweep (the downwelling radiances at the surface)
   int brdf, nsfcpar, nbrdf_dn, ldo;
   const float *botpar, *raddo;
+  const float *botplanck;  // thermal source: B at the bottom points, else null
   const BrdfOrd *brdf_dn;
   const float *camx, *camy, *camz;
   const double *cammu, *camphi;
@@ -1593,6 +1609,11 @@ __device__ __noinline__ void brdf_radiance_warp(const RenderArgs &a, int bi, flo
     for (int k1 = 0; k1 < nst; ++k1) {
       const float rin = row[ci + k1 * oi];
       for (int k = 0; k < nst; ++k) acc[k] += i.w * R[k][k1] * rin;
+    }
+    if (a.botplanck) {
+      const float bp = a.botplanck[bi];
+      acc[0] += i.w * (1.f - R[0][0]) * bp;
+      for (int k = 1; k < nst; ++k) acc[k] -= i.w * R[k][0] * bp;
     }
   }
   for (int k = 0; k < 3; ++k) {
@@ -2208,11 +2229,12 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render_pol(RenderArgs a) {
 }
 
 __global__ void k_bcrad_bottom(const int *botp, int nbot, const float *botalb, const float *dirflux,
-                               const float *fluxes, float *bcrad) {
+                               const float *fluxes, float *bcrad, const float *botplanck) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nbot) return;
   int p = botp[k];
   bcrad[k] = 0.318309886f * botalb[k] * (dirflux[p] + fluxes[2 * (size_t)p]);
+  if (botplanck) bcrad[k] += botplanck[k] * (1.f - botalb[k]);
 }
 
 }  // namespace shdom
@@ -2315,6 +2337,7 @@ struct Handle {
   DBuf<int> nphi0, col_of;
   // medium
   DBuf<float> text, dirflux, coef, tms_w, phasetab, botalb, rad0;
+  DBuf<float> thermal, botplanck;  // thermal source only (empty for a solar source)
   DBuf<double> edp;      // delta-M scaled property-grid extinction (input of the direct beam)
   DBuf<uint8_t> nbscat;  // 1 where a cell containing the point has a scattering corner
   DBuf<int> wready;      // per hemisphere: the source pass has filled every item once
@@ -2653,6 +2676,7 @@ static long long plan_device_bytes(const Plan &P) {
   b += 4LL * 5 * P.nang + vbytes(P.cmu1) + vbytes(P.cmu2) + vbytes(P.cphi1) + vbytes(P.cphi2) + vbytes(P.ylmsun);
   b += vbytes(P.nphi0) + vbytes(P.col_of) + vbytes(P.total_ext) + 4LL * P.npts + vbytes(P.coef) + vbytes(P.tms_ptr);
   b += vbytes(P.tms_iph) + vbytes(P.tms_w) + vbytes(P.phasetab) + vbytes(P.botalb) + vbytes(P.rad0);
+  b += vbytes(P.thermal) + vbytes(P.botplanck);
   const long long ldo = (P.nang + 3) & ~3;
   b += 4LL * P.npts * (3LL * P.nst * P.nlm + 2 * ldo + 2 + 3) + 4LL * (long long)P.botp.size() + 64;
   if (P.nst == 3) b += vbytes(P.col_stk) + vbytes(P.coefp) + vbytes(P.phasetab2) + 8LL * P.nlm * 3 * P.nang;
@@ -2783,7 +2807,7 @@ static void upload_plan(Handle &H) {
     g.edp = H.edp.p; g.zlev = H.zgrid.p; g.gridpos = H.gridpos.p; g.dirflux = H.dirflux.p;
     g.npts = P.npts; g.npx = P.prob.npx; g.npy = P.prob.npy; g.npz = P.prob.npz; g.bcflag = P.bcflag;
     g.ipflag = P.ipflag; g.delx = P.prob.delx; g.dely = P.prob.dely; g.solarmu = P.prob.solarmu;
-    g.solaraz = P.prob.solaraz; g.solarflux = P.prob.solarflux;
+    g.solaraz = P.prob.solaraz; g.solarflux = P.srct == 'T' ? 0.f : P.prob.solarflux;  // no beam for 'T'
     k_direct_beam<<<(P.npts + 127) / 128, 128, 0, H.stream>>>(g);
     CK(cudaGetLastError());
     H.launches += 1;
@@ -2804,6 +2828,7 @@ static void upload_plan(Handle &H) {
   }
   H.tms_ptr.upload(P.tms_ptr); H.tms_iph.upload(P.tms_iph); H.tms_w.upload(P.tms_w);
   H.phasetab.upload(P.phasetab); H.botalb.upload(P.botalb); H.rad0.upload(P.rad0);
+  H.thermal.upload(P.thermal); H.botplanck.upload(P.botplanck);
   if (H.nst == 3) { H.col_stk.upload(P.col_stk); H.coefp.upload(P.coefp); H.phasetab2.upload(P.phasetab2); }
   if (P.brdf) {
     static_assert(sizeof(BrdfOrd) == sizeof(Plan::BrdfOrd), "BRDF ordinate records");
@@ -2832,6 +2857,7 @@ static void launch_source(Handle &H, int first, int fixsh) {
   Plan &P = H.P;
   SourceArgs a;
   a.coef = H.coef.p; a.dirflux = H.dirflux.p; a.radiance = H.radiance.p; a.ylmsun = H.ylmsun.p; a.lofj = H.lofj.p;
+  a.thermal = H.thermal.n ? H.thermal.p : nullptr;
   a.source = H.source.p; a.delsource = H.delsource.p; a.ns = H.ns.p; a.nso = H.nso.p; a.nr = H.nr.p; a.red = H.red.p;
   a.npts = P.npts; a.nlm = P.nlm; a.nl = P.ml + 1; a.ml = P.ml; a.mm = P.mm;
   a.secmu0 = 1.0f / std::fabs(P.prob.solarmu); a.shacc = P.prob.shacc;
@@ -3157,6 +3183,7 @@ int shdom_plan_create(const shdom_problem *problem, shdom_plan **out, shdom_size
     shdom_problem &pr = p->P.prob;
     pr.zlevels = nullptr; pr.extinctp = nullptr; pr.albedop = nullptr; pr.iphasep = nullptr;
     pr.phasewtp = nullptr; pr.legenp = nullptr; pr.sfc_albedo = nullptr; pr.sfc_params = nullptr;
+    pr.tempp = nullptr; pr.sfc_temp = nullptr;
     if (sizes) {
       shdom::fill_sizes(p->P, sizes);
       sizes->solcrit = 1.f;
@@ -3235,7 +3262,7 @@ int shdom_solution_iterations(shdom_handle *hh, int maxiter, int *iters, float *
       int ntop = (int)P.topp.size(), nbot = (int)P.botp.size();
       if (ntop && P.ncol_down) {
         int t = ntop * P.ncol_down;
-        shdom::k_preset_top<<<(t + 255) / 256, 256, 0, H.stream>>>(H.topp.p, ntop, H.raddo.p, H.ldo, P.ncol_down, P.prob.skyrad,
+        shdom::k_preset_top<<<(t + 255) / 256, 256, 0, H.stream>>>(H.topp.p, ntop, H.raddo.p, H.ldo, P.ncol_down, P.skyrad_bc,
                                                                    H.nst == 3 ? H.col_stk.p : nullptr);
         H.launches += 1;
       }
@@ -3244,11 +3271,12 @@ int shdom_solution_iterations(shdom_handle *hh, int maxiter, int *iters, float *
         shdom::k_brdf_bottom<<<nbot, 128, 0, H.stream>>>(H.botp.p, nbot, H.botpar.p, P.nsfcpar, P.brdf, H.brdf_dn.p,
                                                           (int)P.brdf_dn.size(), H.brdf_up.p, (int)P.brdf_up.size(),
                                                           H.dirflux.p, P.prob.solarmu, P.prob.solaraz, H.raddo.p, H.ldo,
-                                                          H.nst);
+                                                          H.nst, H.botplanck.n ? H.botplanck.p : nullptr);
         H.launches += 1;
       } else if (nbot) {
         shdom::k_lambertian<<<nbot, 256, 0, H.stream>>>(H.botp.p, nbot, H.botalb.p, H.dirflux.p, H.col_fluxw.p, H.raddo.p,
-                                                         nang, H.ldo, P.ncol_down, H.bcrad.p, H.nst == 3 ? H.col_stk.p : nullptr);
+                                                         nang, H.ldo, P.ncol_down, H.bcrad.p, H.nst == 3 ? H.col_stk.p : nullptr,
+                                                         H.botplanck.n ? H.botplanck.p : nullptr);
         H.launches += 1;
       }
       shdom::sweep_hemisphere(H, 1);
@@ -3337,7 +3365,8 @@ static shdom::RenderArgs render_args(Handle &H, int nrays, const float *camx, co
   a.out = out; a.err = H.errflag.p; a.nrays = nrays; a.nx = P.nx; a.ny = P.ny; a.nz = P.nz; a.nlm = P.nlm;
   a.nl = P.ml + 1; a.ml = P.ml; a.mm = P.mm; a.bcflag = P.bcflag; a.ipflag = P.ipflag; a.numphase = P.numphase;
   a.nscatangle = P.nscatangle; a.deltam = P.prob.deltam; a.solarmu = P.prob.solarmu; a.solaraz = P.prob.solaraz;
-  a.secmu0 = 1.0f / std::fabs(P.prob.solarmu); a.skyrad = P.prob.skyrad; a.tautol = P.prob.tautol;
+  a.secmu0 = 1.0f / std::fabs(P.prob.solarmu); a.skyrad = P.skyrad_bc; a.tautol = P.prob.tautol;
+  a.botplanck = H.botplanck.n ? H.botplanck.p : nullptr;
   a.transcut = P.prob.transcut;
   a.coefp = H.nst == 3 ? H.coefp.p : nullptr;
   a.phasetab2 = H.nst == 3 ? H.phasetab2.p : nullptr;
@@ -3353,7 +3382,7 @@ static int render_impl(shdom_handle *hh, int nrays, const float *camx, const flo
   int nbot = (int)P.botp.size();
   if (nbot) {
     shdom::k_bcrad_bottom<<<(nbot + 127) / 128, 128, 0, stream>>>(H.botp.p, nbot, H.botalb.p, H.dirflux.p, H.fluxes.p,
-                                                                  H.bcrad.p);
+                                                                  H.bcrad.p, H.botplanck.n ? H.botplanck.p : nullptr);
     H.launches += 1;
   }
   shdom::RenderArgs a = render_args(H, nrays, camx, camy, camz, cammu, camphi, out);
@@ -3546,6 +3575,7 @@ static int levis_host(shdom_handle *hh, int species, int nrays, const float *cam
   if (species < 0 || species >= P.npart) return fail(hh, "levis gradient: species index out of range");
   if (H.nst != 1) return fail(hh, "levis gradient: scalar (nstokes = 1) problems only");
   if (P.brdf) return fail(hh, "levis gradient: Lambertian surfaces only");
+  if (P.srct != 'S') return fail(hh, "levis gradient: solar sources only (as at3d.gradient)");
   if (P.ml + 1 > 32 || P.nlm > shdom::RNLM) return fail(hh, "levis gradient: at most 32 Legendre terms are supported");
   if (!H.initialized) return fail(hh, "levis gradient: the solution has not been initialized");
   if (H.grad_ipa != species) prepare_grad(H, species);

@@ -165,6 +165,16 @@ void ylm_unpol(int ml, int mm, double mu, float phi, float *y) {
   }
 }
 
+// PLANCK_FUNCTION (src/polarized/shdomsub2.f:4756-4791): Planck's law in
+// SHDOM's units and single precision, c1 = 1.1911e8 W um^4/(m^2 sr),
+// c2 = 1.4388e4 um K.
+float planck_fn(float t, char units, float wavelen) {
+  if (units == 'T') return t;
+  if (t <= 0.f) return 0.f;
+  const float w = wavelen;
+  return 1.1911e8f / (w * w * w * w * w) / (std::exp(1.4388e4f / (w * t)) - 1.0f);
+}
+
 namespace {
 
 bool build_grid(const shdom_problem &p, Plan &P) {
@@ -576,6 +586,8 @@ bool build_medium(const shdom_problem &p, Plan &P) {
   std::vector<int> iph((size_t)npart * npts * nq);
   std::vector<float> pw((size_t)npart * npts * nq);
   P.total_ext.assign(npts, 0.f);
+  const bool therm = P.srct != 'S';
+  std::vector<float> temp(therm ? npts : 0);  // TEMP of the grid points (TRILIN_INTERP_PROP)
   bool bad = false;
   for (int ipa = 0; ipa < npart; ++ipa) {
     parallel_for(npts, [&](int b, int e) {
@@ -606,6 +618,11 @@ bool build_medium(const shdom_problem &p, Plan &P) {
         const float *E = p.extinctp + (size_t)ipa * ng, *A = p.albedop + (size_t)ipa * ng;
         double e = 0, sc[8], scat = 0;
         for (int c = 0; c < 8; ++c) { e += f[c] * E[ii[c]]; sc[c] = f[c] * E[ii[c]] * A[ii[c]]; scat += sc[c]; }
+        if (therm && ipa == 0) {
+          double t = 0;
+          for (int c = 0; c < 8; ++c) t += f[c] * p.tempp[ii[c]];
+          temp[ipt] = (float)t;
+        }
         size_t o = (size_t)ipa * npts + ipt;
         ext[o] = (float)e;
         alb[o] = (float)(e > extmin ? scat / e : scat / extmin);
@@ -655,6 +672,24 @@ bool build_medium(const shdom_problem &p, Plan &P) {
   }
   P.albmax = 0.f;
   for (float a : alb) P.albmax = std::max(P.albmax, a);
+  // thermal source: PLANCK = (1 - albedo) B(T) per species after the delta-M
+  // scaling (src/polarized/shdomsub2.f:574-580), mixed with the extinction
+  // weights of COMPUTE_SOURCE (TOTAL_PLANCK, src/polarized/shdomsub1.f:1092-1139)
+  P.thermal.clear();
+  if (therm) {
+    P.thermal.assign(npts, 0.f);
+    parallel_for(npts, [&](int b, int e) {
+      for (int ipt = b; ipt < e; ++ipt) {
+        const float bb = planck_fn(temp[ipt], P.unitc, p.wavelen);
+        float tp = 0.f;
+        for (int ipa = 0; ipa < npart; ++ipa) {
+          const size_t o = (size_t)ipa * npts + ipt;
+          tp += ext[o] * ((1.0f - alb[o]) * bb);
+        }
+        P.thermal[ipt] = P.total_ext[ipt] > 1e-10f ? tp / P.total_ext[ipt] : 0.f;
+      }
+    });
+  }
   // kept for the gradient: the property grid of every species, the stored
   // Legendre table and the scaled species properties on the grid points
   P.npx = npx; P.npy = npy; P.npz = npz; P.maxnmicro = nmic; P.delx = p.delx; P.dely = p.dely;
@@ -753,7 +788,9 @@ bool build_medium(const shdom_problem &p, Plan &P) {
   });
   // scattering points: the coefficient row is non-zero exactly when its l = 0 term (the albedo) is
   P.scat.assign(npts, 0);
-  for (int ipt = 0; ipt < npts; ++ipt) P.scat[ipt] = P.coef[(size_t)ipt * nl] != 0.f;
+  // a point has a source when it scatters or (thermal source) emits
+  for (int ipt = 0; ipt < npts; ++ipt)
+    P.scat[ipt] = P.coef[(size_t)ipt * nl] != 0.f || (!P.thermal.empty() && P.thermal[ipt] != 0.f);
   for (int ipt = 0; ipt < npts; ++ipt) P.tms_ptr[ipt + 1] = P.tms_ptr[ipt] + tcnt[ipt];
   P.tms_iph.assign(P.tms_ptr[npts], 0);
   P.tms_w.assign(P.tms_ptr[npts], 0.f);
@@ -817,7 +854,13 @@ bool build_medium(const shdom_problem &p, Plan &P) {
       // reduced to tridiagonal form; solved with partial pivoting.
       const int n = 2 * nlay + 2;
       const double mu0 = std::fabs((double)p.solarmu), sf = p.solarflux;
+      const double pid = 3.1415926535;
       double tau = 0.0;
+      // thermal layers ('T' only): the Planck function is linear in optical
+      // depth between the column's levels, taken from the top down
+      const bool eth = P.srct == 'T';
+      auto tlev = [&](int k) { return temp[(size_t)(nz - 1 - k) + (size_t)nz * col]; };
+      double planck1 = eth ? pid * (double)planck_fn(tlev(0), P.unitc, p.wavelen) : 0.0;
       for (int l = 0, i = 2; l < nlay; ++l, i += 2) {
         double dt = od[l], tr, rf, sp, sm;
         if (dt == 0.0) { tr = 1; rf = 0; sp = 0; sm = 0; }
@@ -833,12 +876,20 @@ bool build_medium(const shdom_problem &p, Plan &P) {
             rf = x1 * (ep - em) * tr / (2. * lam);
             dd = 1.0 / (x2 * x2 * ep - x1 * x1 * em);
           }
-          double ds = 1.0 / (lam * lam - 1.0 / (mu0 * mu0));
-          double b1 = 0.5 * om * (sf / mu0) * std::exp(-tau / mu0) * ds;
-          double b2 = 0.5 * om * (sf / mu0) * std::exp(-(tau + dt) / mu0) * ds;
-          double spp = 1.0 + 1.5 * g * mu0, spm = -1.0 + 1.5 * g * mu0;
-          double r1p = ((t + 1.0 / mu0) * spp + r * spm) * b1, r2m = ((-t + 1.0 / mu0) * spm - r * spp) * b2;
-          double r2p = ((t + 1.0 / mu0) * spp + r * spm) * b2, r1m = ((-t + 1.0 / mu0) * spm - r * spp) * b1;
+          double r1p, r2m, r2p, r1m;
+          if (eth) {
+            const double planck2 = pid * (double)planck_fn(tlev(l + 1), P.unitc, p.wavelen);
+            const double vv = 2.0 * (planck2 - planck1) / (3.0 * (1. - om * g) * dt);
+            r1p = -vv + planck1; r2m = vv + planck2; r2p = -vv + planck2; r1m = vv + planck1;
+            planck1 = planck2;
+          } else {
+            double ds = 1.0 / (lam * lam - 1.0 / (mu0 * mu0));
+            double b1 = 0.5 * om * (sf / mu0) * std::exp(-tau / mu0) * ds;
+            double b2 = 0.5 * om * (sf / mu0) * std::exp(-(tau + dt) / mu0) * ds;
+            double spp = 1.0 + 1.5 * g * mu0, spm = -1.0 + 1.5 * g * mu0;
+            r1p = ((t + 1.0 / mu0) * spp + r * spm) * b1; r2m = ((-t + 1.0 / mu0) * spm - r * spp) * b2;
+            r2p = ((t + 1.0 / mu0) * spp + r * spm) * b2; r1m = ((-t + 1.0 / mu0) * spm - r * spp) * b1;
+          }
           if (lam == 0.0) {
             double A = (r * dt * r1p - r2m) * dd, B = -(r * r1p + t * r2m) * dd;
             sp = (B - t * (A + B * dt)) / r + r2p; sm = A + r1m;
@@ -846,14 +897,20 @@ bool build_medium(const shdom_problem &p, Plan &P) {
             double cp = (x1 * em * r1p - x2 * r2m) * dd, cm = (-x2 * ep * r1p + x1 * r2m) * dd;
             sp = x1 * cp * ep + x2 * cm * em + r2p; sm = x2 * cp + x1 * cm + r1m;
           }
-          tau += dt;
+          if (!eth) tau += dt;
         }
         dg[i] = -rf; dg[i + 1] = -rf; lo[i] = 1.0; lo[i + 1] = -tr; up[i] = -tr; up[i + 1] = 1.0;
         rhs[i] = sm; rhs[i + 1] = sp;
       }
       double gem = 1.0 - (double)p.gndalbedo;
-      rhs[1] = 3.1415926535 * p.skyrad; dg[1] = 0.0; up[1] = 1.0;
-      dg[n] = -(1.0 - gem); lo[n] = 1.0; rhs[n] = (1.0 - gem) * sf * std::exp(-tau / mu0);
+      if (P.srct == 'S') {
+        rhs[1] = pid * p.skyrad; rhs[n] = (1.0 - gem) * sf * std::exp(-tau / mu0);
+      } else {  // emitting ground and sky ('T' and 'B')
+        rhs[1] = pid * (double)planck_fn(p.skyrad, P.unitc, p.wavelen);
+        rhs[n] = pid * (double)planck_fn(p.gndtemp, P.unitc, p.wavelen) * gem;
+      }
+      dg[1] = 0.0; up[1] = 1.0;
+      dg[n] = -(1.0 - gem); lo[n] = 1.0;
       lo[1] = dg[1]; dg[1] = up[1]; up[1] = 0.0; up[n] = 0.0;
       for (int k = 1; k <= n - 1; ++k) {
         if (std::fabs(lo[k + 1]) >= std::fabs(lo[k])) {
@@ -868,9 +925,10 @@ bool build_medium(const shdom_problem &p, Plan &P) {
       rhs[n] /= lo[n];
       rhs[n - 1] = (rhs[n - 1] - dg[n - 1] * rhs[n]) / lo[n - 1];
       for (int k = n - 2; k >= 1; --k) rhs[k] = (rhs[k] - dg[k] * rhs[k + 1] - up[k] * rhs[k + 2]) / lo[k];
+      const double cfl = P.unitc == 'T' ? 1.0 / pid : 1.0;  // brightness temperature fluxes
       for (int iz = 0; iz < nz; ++iz) {
         int L = nz - 1 - iz;
-        float fu = (float)rhs[2 * L + 1], fd = (float)rhs[2 * L + 2];
+        float fu = (float)(cfl * rhs[2 * L + 1]), fd = (float)(cfl * rhs[2 * L + 2]);
         float *r = &P.rad0[(size_t)(iz + nz * col) * 4];
         r[0] = c0 * (fu + fd); r[1] = 0.f; r[2] = c1 * (fu - fd); r[3] = 0.f;
       }
@@ -1245,6 +1303,16 @@ bool build_plan(const shdom_problem &p, Plan &P) {
   }
   P.prob = p;
   P.err.clear();
+  P.srct = p.srctype ? (char)p.srctype : 'S';
+  P.unitc = p.units ? (char)p.units : 'R';
+  if (P.srct != 'S' && P.srct != 'T' && P.srct != 'B') { P.err = "srctype must be 'S', 'T' or 'B'"; return false; }
+  if (P.unitc != 'R' && P.unitc != 'T') { P.err = "units must be 'R' (radiance) or 'T' (brightness temperature)"; return false; }
+  if (P.srct != 'S') {
+    if (!p.tempp) { P.err = "a thermal source needs the temperature field"; return false; }
+    if (P.unitc == 'R' && !(p.wavelen > 0.f)) { P.err = "a thermal source in radiance units needs the wavelength"; return false; }
+  }
+  // COMPUTE_TOP_RADIANCES: the sky brightness temperature becomes a radiance for 'T'
+  P.skyrad_bc = P.srct == 'T' ? planck_fn(p.skyrad, P.unitc, p.wavelen) : p.skyrad;
   if (!build_medium(p, P)) return false;
   build_direct(p, P);
   // bottom surface albedo (PREP_SURFACE periodic grid + SURFACE_PARM_INTERP)
@@ -1258,6 +1326,24 @@ bool build_plan(const shdom_problem &p, Plan &P) {
       int ix = std::max(1, std::min(nxs, (int)rx + 1)), iy = std::max(1, std::min(nys, (int)ry + 1));
       float u = std::max(0.f, std::min(1.f, rx - (ix - 1))), v = std::max(0.f, std::min(1.f, ry - (iy - 1)));
       P.botalb[k] = (1 - u) * (1 - v) * G(ix, iy) + (1 - u) * v * G(ix, iy + 1) + u * (1 - v) * G(ix + 1, iy) + u * v * G(ix + 1, iy + 1);
+    }
+  }
+  // ground emission: B of the bilinearly interpolated surface temperature
+  // (SURFACE_PARM_INTERP) or of the one ground temperature
+  P.botplanck.clear();
+  if (P.srct != 'S') {
+    P.botplanck.assign(P.botp.size(), planck_fn(p.gndtemp, P.unitc, p.wavelen));
+    if (p.sfc_temp && p.nxsfc > 0 && p.nysfc > 0 && (p.sfc_variable || p.sfc_brdf)) {
+      const int nxs = p.nxsfc, nys = p.nysfc;
+      auto G = [&](int x, int y) { return p.sfc_temp[(size_t)((y - 1) % nys) * nxs + ((x - 1) % nxs)]; };
+      for (size_t k = 0; k < P.botp.size(); ++k) {
+        int i = P.botp[k];
+        float rx = P.gridpos[3 * i] / p.delxsfc, ry = P.gridpos[3 * i + 1] / p.delysfc;
+        int ix = std::max(1, std::min(nxs, (int)rx + 1)), iy = std::max(1, std::min(nys, (int)ry + 1));
+        float u = std::max(0.f, std::min(1.f, rx - (ix - 1))), v = std::max(0.f, std::min(1.f, ry - (iy - 1)));
+        const float t = (1 - u) * (1 - v) * G(ix, iy) + (1 - u) * v * G(ix, iy + 1) + u * (1 - v) * G(ix + 1, iy) + u * v * G(ix + 1, iy + 1);
+        P.botplanck[k] = planck_fn(t, P.unitc, p.wavelen);
+      }
     }
   }
   // bidirectional surface: parameters at the bottom points (SURFACE_PARM_INTERP,

@@ -115,7 +115,8 @@ struct Plan {
   std::vector<double> extdirp;                   // [npx*npy*npz] delta-M scaled extinction for the direct beam
   std::vector<float> coef;                       // [npts][ml+1]: albedo * delta-M scaled Legendre term
   std::vector<float> coefp;                      // nst = 3: [npts][3][ml+1] the same for a2, a3 and b1
-  std::vector<uint8_t> scat;                     // [npts] 1 where the point scatters (a non-zero coefficient row)
+  std::vector<uint8_t> scat;                     // [npts] 1 where the point has a source: it scatters (a non-zero
+                                                 // coefficient row) or emits (a non-zero thermal term)
   std::vector<int> tms_ptr, tms_iph;             // CSR per point: exact single-scatter mixture
   std::vector<float> tms_w;
   std::vector<float> phasetab;                   // [nscatangle][numphase]
@@ -124,6 +125,13 @@ struct Plan {
   float albmax = 0.f;
   std::vector<float> rad0;                       // [npts][4] Eddington initial radiance
   std::vector<float> botalb;                     // surface albedo at the bottom points
+  // thermal emission (srct 'T' thermal, 'B' thermal and solar; empty for
+  // 'S'): thermal[i] the extinction-weighted (1 - albedo) B(T) of point i,
+  // botplanck B at the bottom points, skyrad_bc the top boundary radiance
+  char srct = 'S', unitc = 'R';
+  std::vector<float> thermal;                    // [npts]
+  std::vector<float> botplanck;                  // [nbot]
+  float skyrad_bc = 0.f;
   // bidirectional surface ('R' RPV, 'W' wave-Fresnel; 0 Lambertian): its
   // parameters at the bottom points and the downward / upward ordinates of
   // the reflection sums, in the reference order: mu, phi, weight
@@ -159,6 +167,10 @@ struct Plan {
 
 // Fills every table of the plan; returns false with plan.err set on error.
 bool build_plan(const shdom_problem &p, Plan &plan);
+
+// PLANCK_FUNCTION for units 'R' (W/(m^2 sr micron) at wavelen microns)
+// and 'T' (the temperature itself).
+float planck_fn(float t, char units, float wavelen);
 
 // Real generalized spherical harmonics (unpolarized element) at one
 // direction, NLM values in the SHDOM term order.

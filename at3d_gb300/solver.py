@@ -83,20 +83,37 @@ class RTE:
 
     Parameters follow the reference: ``numerical_params`` (a NumericalParams),
     ``medium`` (dict name -> Species on a common property grid, given by
-    ``grid``), ``source`` (source.solar), ``surface`` (surface.lambertian).
+    ``grid``), ``source`` (source.solar, source.thermal or source.combined),
+    ``surface`` (surface.lambertian or a bidirectional surface.BRDFSurface)
+    and, for a thermal source, ``atmosphere`` with the medium's
+    ``temperature`` [npx, npy, npz] in K (at3d/solver.py:1765-1800).
     """
 
     def __init__(self, numerical_params: NumericalParams, medium: dict, source, surface, grid,
-                 num_stokes: int = 1, name: str | None = None, device: int = 0):
+                 num_stokes: int = 1, name: str | None = None, device: int = 0, atmosphere: dict | None = None):
         if num_stokes not in (1, 3):
             raise ValueError("num_stokes must be 1 (scalar radiance) or 3 (I, Q, U)")
         species = list(medium.values())
-        sa = surface.albedo
+        srctype = getattr(source, "srctype", "S")
+        temperature = None
+        if atmosphere is not None and "temperature" in atmosphere:
+            temperature = np.asarray(atmosphere["temperature"], np.float32)
+            if np.any(temperature <= 0.0):
+                raise ValueError("temperature must be positive")
+        elif srctype in ("T", "B"):
+            raise KeyError("'temperature' variable was not specified in `atmosphere` "
+                           "and is required for a thermal source")
         self.problem = Problem(delx=grid.delx, dely=grid.dely, zlevels=np.asarray(grid.z, np.float32),
                                species=species, solarmu=source.solarmu, solaraz=source.solaraz,
-                               solarflux=source.solarflux, skyrad=source.skyrad, surface_albedo=sa,
+                               solarflux=source.solarflux, skyrad=source.skyrad,
                                surface_delx=surface.delx, surface_dely=surface.dely, params=numerical_params,
-                               num_stokes=num_stokes)
+                               num_stokes=num_stokes, srctype=srctype, units=getattr(source, "units", "R"),
+                               wavelength=source.wavelength, temperature=temperature,
+                               ground_temperature=getattr(surface, "ground_temperature", 288.0))
+        if hasattr(surface, "kind"):      # surface.BRDFSurface
+            self.problem.surface_brdf, self.problem.surface_params = surface.kind, surface.params
+        else:
+            self.problem.surface_albedo = surface.albedo
         self.name = name or f"Radiance {source.wavelength:1.3f} micron"
         self._create(device)
 

@@ -12,7 +12,7 @@ import numpy as np
 @dataclass
 class LambertianSurface:
     albedo: np.ndarray | float
-    ground_temperature: float = 298.15
+    ground_temperature: float | np.ndarray = 298.15
     delx: float = 0.0
     dely: float = 0.0
 
@@ -22,14 +22,23 @@ class LambertianSurface:
 
 
 def lambertian(albedo, ground_temperature=298.15, delx=None, dely=None) -> LambertianSurface:
+    """at3d.surface.lambertian (at3d/surface.py:28-105): a fixed surface, or a
+    variable one when the albedo or the ground temperature is an array on
+    the surface grid [nxsfc, nysfc] of spacing (delx, dely)."""
     a = np.asarray(albedo, np.float32)
+    t = np.asarray(ground_temperature, np.float32)
     if np.any(a > 1.0) or np.any(a < 0.0):
         raise ValueError(f"surface albedo should be in [0, 1] not '{albedo}'")
-    if a.size > 1:
+    if a.size > 1 or t.size > 1:
         if delx is None or dely is None:
             raise ValueError("dely and delx must be defined for variable surface parameters.")
-        return LambertianSurface(np.atleast_2d(a), float(ground_temperature), float(delx), float(dely))
-    return LambertianSurface(float(a.reshape(-1)[0]), float(ground_temperature))
+        if a.size > 1 and t.size > 1 and np.atleast_2d(a).shape != np.atleast_2d(t).shape:
+            raise ValueError("albedo and ground_temperature must have the same shape")
+        shape = np.atleast_2d(a if a.size > 1 else t).shape
+        a2 = np.broadcast_to(np.atleast_2d(a), shape).astype(np.float32)
+        t2 = float(t.reshape(-1)[0]) if t.size == 1 else np.atleast_2d(t).astype(np.float32)
+        return LambertianSurface(a2, t2, float(delx), float(dely))
+    return LambertianSurface(float(a.reshape(-1)[0]), float(t.reshape(-1)[0]))
 
 
 @dataclass

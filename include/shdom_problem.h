@@ -13,6 +13,7 @@
  *   boundary conditions      : at3d/solver.py:2110-2127 (bcflag, ipflag)
  *   source                   : at3d/source.py:14-80 (solar)
  *   surface                  : at3d/surface.py:28-105 (lambertian)
+ *   temperature              : at3d/solver.py:1765-1800 (tempp)
  *   numerical parameters     : at3d/solver.py:1960-2034, default_config.json
  *
  * Array layouts are the Fortran (column-major) layouts of the reference,
@@ -72,6 +73,17 @@ typedef struct shdom_problem {
                                       (Diner: a, k, b, zeta, sigma) */
     int nsfcpar;                   /* parameters per surface grid point */
     const float *sfc_params;       /* [nysfc][nxsfc][nsfcpar] */
+    /* ---- thermal emission (at3d/source.py thermal, combined; PLANCK_FUNCTION
+     *      src/polarized/shdomsub2.f:4756-4791).  srctype 'T' replaces the solar
+     *      beam by emission of (1 - albedo) B(T) from every grid point, the
+     *      ground ((1 - albedo) B(ground temperature), or the BRDF emissivity)
+     *      and the sky (skyrad is then a brightness temperature); 'B' adds
+     *      both sources.  0 means 'S' (solar only) ---- */
+    int srctype;                   /* 0 or 'S', 'T', 'B' */
+    int units;                     /* 'R' radiance W/(m^2 sr um) (0 means 'R'), 'T' brightness temperature */
+    float wavelen;                 /* micron, for the Planck function */
+    const float *tempp;            /* [npx][npy][npz] K on the property grid ('T', 'B') */
+    const float *sfc_temp;         /* [nysfc][nxsfc] K on the surface grid, or NULL: gndtemp everywhere */
 } shdom_problem;
 
 #ifdef __cplusplus

@@ -241,6 +241,23 @@ struct Solver {
   std::vector<R> botpar, bcdown;
   std::vector<R> bcrad_top, bcrad_bot;
   bool sweep_ready = false;
+  // Thermal emission: srct is 'S', 'T' or 'B'; temp the temperature of each
+  // grid point; planck_tot the extinction-weighted (1 - albedo) B(T) of each
+  // point (TOTAL_PLANCK of COMPUTE_SOURCE); botplanck B at the bottom points
+  // (SFCGRIDPARMS(1)); skyrad_bc the radiance of the top boundary.
+  char srct = 'S', unitc = 'R';
+  std::vector<float> tempp_in, sfctemp_in, temp;
+  std::vector<R> planck_tot, botplanck;
+  float skyrad_bc = 0.f;
+
+  // PLANCK_FUNCTION (src/polarized/shdomsub2.f:4756-4791) for units 'R'
+  // (W/(m^2 sr micron) at p.wavelen) and 'T' (brightness temperature).
+  float planck_fn(float t) const {
+    if (unitc == 'T') return t;
+    if (t <= 0.f) return 0.f;
+    const float w = p.wavelen;
+    return 1.1911e8f / (w * w * w * w * w) / (std::exp(1.4388e4f / (w * t)) - 1.0f);
+  }
 
   // ------------------------------------------------------------ setup
   bool init(const shdom_problem *in) {
@@ -266,6 +283,20 @@ struct Solver {
       if (brdf == 'R' && nst != 1) { err = "RPV BRDF is only for unpolarized case"; return false; }
       sfcpar.assign(p.sfc_params, p.sfc_params + (size_t)p.nxsfc * p.nysfc * p.nsfcpar);
     }
+    srct = p.srctype ? (char)p.srctype : 'S';
+    unitc = p.units ? (char)p.units : 'R';
+    if (srct != 'S' && srct != 'T' && srct != 'B') { err = "srctype must be 'S', 'T' or 'B'"; return false; }
+    if (unitc != 'R' && unitc != 'T') { err = "units must be 'R' or 'T'"; return false; }
+    if (srct != 'S') {
+      if (!p.tempp) { err = "a thermal source needs the temperature field"; return false; }
+      if (unitc == 'R' && !(p.wavelen > 0.f)) { err = "a thermal source in radiance units needs the wavelength"; return false; }
+      tempp_in.assign(p.tempp, p.tempp + ng);
+      if (p.sfc_temp && p.nxsfc > 0 && p.nysfc > 0 && (p.sfc_variable || brdf))
+        sfctemp_in.assign(p.sfc_temp, p.sfc_temp + (size_t)p.nxsfc * p.nysfc);
+    }
+    p.tempp = nullptr; p.sfc_temp = nullptr;
+    // COMPUTE_TOP_RADIANCES: the sky temperature becomes a radiance only for 'T'
+    skyrad_bc = (srct == 'T') ? planck_fn(p.skyrad) : p.skyrad;
     p.sfc_params = nullptr;
     p.zlevels = nullptr; p.extinctp = p.albedop = p.phasewtp = p.legenp = p.sfc_albedo = nullptr;
     p.iphasep = nullptr;
@@ -540,6 +571,7 @@ struct Solver {
     extinct.assign((size_t)npart * npts, 0); albedo.assign((size_t)npart * npts, 0);
     total_ext.assign(npts, 0);
     iphase.assign((size_t)npart * npts * nq, 1); phaseinterpwt.assign((size_t)npart * npts * nq, 0);
+    temp.assign(srct != 'S' ? npts : 0, 0.f);
     for (int ipa = 0; ipa < npart; ++ipa) {
       for (int ipt = 0; ipt < npts; ++ipt) {
         float x = gridpos[3 * ipt], y = gridpos[3 * ipt + 1], z = gridpos[3 * ipt + 2];
@@ -574,6 +606,11 @@ struct Solver {
         const float *A = &albp[(size_t)ipa * ng];
         double ext = 0, scat[8], scatter = 0;
         for (int c = 0; c < 8; ++c) { ext += f[c] * E[ii[c]]; scat[c] = f[c] * E[ii[c]] * A[ii[c]]; scatter += scat[c]; }
+        if (ipa == 0 && srct != 'S') {
+          double t = 0;
+          for (int c = 0; c < 8; ++c) t += f[c] * tempp_in[ii[c]];
+          temp[ipt] = (float)t;
+        }
         R extr = (R)ext;
         R alb = (ext > extmin) ? (R)(scatter / ext) : (R)(scatter / extmin);
         extinct[(size_t)ipa * npts + ipt] = extr;
@@ -631,6 +668,18 @@ struct Solver {
           total_ext[ipt] += e;
         }
     }
+    // PLANCK(I,IPA) = (1 - albedo) B(T) after the delta-M scaling
+    // (src/polarized/shdomsub2.f:574-580), summed over the species with the
+    // extinction weights of COMPUTE_SOURCE (src/polarized/shdomsub1.f:1092-1139)
+    planck_tot.assign(npts, 0);
+    if (srct != 'S')
+      for (int ipt = 0; ipt < npts; ++ipt) {
+        const R bb = (R)planck_fn(temp[ipt]);
+        R tp = 0;
+        for (int ipa = 0; ipa < npart; ++ipa)
+          tp = tp + extinct[(size_t)ipa * npts + ipt] * (((R)1 - albedo[(size_t)ipa * npts + ipt]) * bb);
+        planck_tot[ipt] = total_ext[ipt] > (R)1e-10 ? tp / total_ext[ipt] : (R)0;
+      }
     albmax = 0;
     for (auto a : albedo) albmax = std::max(albmax, a);
     return true;
@@ -685,6 +734,7 @@ struct Solver {
   // DIRECT_BEAM_PROP (src/polarized/shdom90.f90:352-867) via MAKE_DIRECT
   // (src/polarized/shdomsub2.f:393-476); regular property grid, no gas.
   void make_direct() {
+    if (srct == 'T') { dirflux.assign(npts, 0); return; }  // no solar beam for a thermal source
     int npx = p.npx, npy = p.npy, npz = p.npz, ng = npx * npy * npz;
     std::vector<double> extdirp(ng, 0.0);
     for (int ip = 0; ip < ng; ++ip) {
@@ -840,7 +890,11 @@ struct Solver {
         }
         as[L] = (scat0 + scat1 > 0) ? (g0 + g1) / (scat0 + scat1) : 0.f;
       }
-      eddrtf(nlayer, od, al, as, fl);
+      // TEMPS from the top: TEMPS(k) = TEMP(NZ+1-k) of this column
+      std::vector<float> temps(nz, 0.f);
+      if (srct != 'S')
+        for (int k = 0; k < nz; ++k) temps[k] = temp[(size_t)(nz - 1 - k) + (size_t)nz * col];
+      eddrtf(nlayer, od, al, as, temps, fl);
       for (int iz = 0; iz < nz; ++iz) {
         int L = nz - 1 - iz;
         // Only the I Stokes parameter is initialised (Q, U stay zero)
@@ -856,11 +910,14 @@ struct Solver {
   }
 
   void eddrtf(int nlayer, const std::vector<float> &od, const std::vector<float> &al,
-              const std::vector<float> &as, std::vector<double> &fluxout) {
+              const std::vector<float> &as, const std::vector<float> &temps, std::vector<double> &fluxout) {
     int n = 2 * nlayer + 2;
     std::vector<double> lower(n + 1), upper(n + 1), diag(n + 1), rhs(n + 1);
     const double pi = 3.1415926535;
     double mu0 = std::fabs((double)p.solarmu), tau = 0.0, sf = p.solarflux;
+    // thermal layers (SRCTYPE 'T' only): Planck function linear in optical depth
+    const bool therm = srct == 'T';
+    double planck1 = therm ? pi * (double)planck_fn(temps[0]) : 0.0;
     int i = 2;
     for (int l = 0; l < nlayer; ++l) {
       double deltau = od[l], trans, reflect, sourcep, sourcem;
@@ -878,14 +935,22 @@ struct Solver {
           reflect = x1 * (exlp - exlm) * trans / (2. * lambda);
           d = 1.0 / (x2 * x2 * exlp - x1 * x1 * exlm);
         }
-        double ds = 1.0 / (lambda * lambda - 1.0 / (mu0 * mu0));
-        double b1 = 0.5 * omega * (sf / mu0) * std::exp(-tau / mu0) * ds;
-        double b2 = 0.5 * omega * (sf / mu0) * std::exp(-(tau + deltau) / mu0) * ds;
-        double solpp = 1.0 + 1.5 * g * mu0, solpm = -1.0 + 1.5 * g * mu0;
-        double radp1p = ((t + 1.0 / mu0) * solpp + r * solpm) * b1;
-        double radp2m = ((-t + 1.0 / mu0) * solpm - r * solpp) * b2;
-        double radp2p = ((t + 1.0 / mu0) * solpp + r * solpm) * b2;
-        double radp1m = ((-t + 1.0 / mu0) * solpm - r * solpp) * b1;
+        double radp1p, radp2m, radp2p, radp1m;
+        if (therm) {
+          const double planck2 = pi * (double)planck_fn(temps[l + 1]);
+          const double v = 2.0 * (planck2 - planck1) / (3.0 * (1. - omega * g) * deltau);
+          radp1p = -v + planck1; radp2m = v + planck2; radp2p = -v + planck2; radp1m = v + planck1;
+          planck1 = planck2;
+        } else {
+          double ds = 1.0 / (lambda * lambda - 1.0 / (mu0 * mu0));
+          double b1 = 0.5 * omega * (sf / mu0) * std::exp(-tau / mu0) * ds;
+          double b2 = 0.5 * omega * (sf / mu0) * std::exp(-(tau + deltau) / mu0) * ds;
+          double solpp = 1.0 + 1.5 * g * mu0, solpm = -1.0 + 1.5 * g * mu0;
+          radp1p = ((t + 1.0 / mu0) * solpp + r * solpm) * b1;
+          radp2m = ((-t + 1.0 / mu0) * solpm - r * solpp) * b2;
+          radp2p = ((t + 1.0 / mu0) * solpp + r * solpm) * b2;
+          radp1m = ((-t + 1.0 / mu0) * solpm - r * solpp) * b1;
+        }
         if (lambda == 0.0) {
           double A = (r * deltau * radp1p - radp2m) * d, B = -(r * radp1p + t * radp2m) * d;
           sourcep = (B - t * (A + B * deltau)) / r + radp2p;
@@ -895,7 +960,7 @@ struct Solver {
           sourcep = x1 * cp * exlp + x2 * cm * exlm + radp2p;
           sourcem = x2 * cp + x1 * cm + radp1m;
         }
-        tau += deltau;
+        if (!therm) tau += deltau;
       }
       diag[i] = -reflect; diag[i + 1] = -reflect;
       lower[i] = 1.0; lower[i + 1] = -trans;
@@ -904,8 +969,14 @@ struct Solver {
       i += 2;
     }
     double gndemis = 1.0 - (double)p.gndalbedo;
-    double gndflux = (1.0 - gndemis) * sf * std::exp(-tau / mu0);
-    double skyflux = pi * p.skyrad;
+    double gndflux, skyflux;
+    if (srct == 'S') {
+      gndflux = (1.0 - gndemis) * sf * std::exp(-tau / mu0);
+      skyflux = pi * p.skyrad;
+    } else {  // 'T' and 'B': emitting ground and sky
+      gndflux = pi * (double)planck_fn(p.gndtemp) * gndemis;
+      skyflux = pi * (double)planck_fn(p.skyrad);
+    }
     rhs[1] = skyflux; diag[1] = 0.0; upper[1] = 1.0;
     diag[n] = -(1.0 - gndemis); lower[n] = 1.0; rhs[n] = gndflux;
     // TRIDIAG (Linpack DGTSL style with pivoting), 1-based arrays
@@ -928,9 +999,10 @@ struct Solver {
       rhs[k] = (rhs[k] - diag[k] * rhs[k + 1] - upper[k] * rhs[k + 2]) / lower[k];
     }
     fluxout.assign(2 * (nlayer + 1), 0.0);
+    const double cfl = unitc == 'T' ? 1.0 / pi : 1.0;
     for (int l = 0, ii = 1; l <= nlayer; ++l, ii += 2) {
-      fluxout[2 * l] = (float)rhs[ii];
-      fluxout[2 * l + 1] = (float)rhs[ii + 1];
+      fluxout[2 * l] = (float)(cfl * rhs[ii]);
+      fluxout[2 * l + 1] = (float)(cfl * rhs[ii + 1]);
     }
   }
 
@@ -957,6 +1029,8 @@ struct Solver {
     R flux0 = dirflux[i] * ((R)1 / std::fabs((R)p.solarmu));
     sourcet.assign(nlm, 0);
     for (int j = 0; j < nlm; ++j) sourcet[j] = flux0 * albr * lt[lofj[j]] * ylmsun[j];
+    // isotropic thermal emission (CALC_SOURCE_PNT_UNPOL, C = sqrt(4 pi))
+    if (srct != 'S') sourcet[0] = sourcet[0] + (R)3.544907703f * planck_tot[i];
     for (int j = 0; j < nr; ++j) sourcet[j] = sourcet[j] + albr * lt[lofj[j]] * rad[(size_t)ir + j];
   }
 
@@ -994,6 +1068,7 @@ struct Solver {
     const R flux0 = dirflux[i] * ((R)1 / std::fabs((R)p.solarmu));
     for (int j = 0; j < nlm; ++j) sourcet[3 * j] += flux0 * albr * a1[lofj[j]] * ylmsun[j];
     for (int j = 4; j < nlm; ++j) sourcet[3 * j + 1] += flux0 * albr * b1[lofj[j]] * ylmsun[j];
+    if (srct != 'S') sourcet[0] += (R)3.544907703f * planck_tot[i];  // unpolarized emission
   }
 
   // COMPUTE_SOURCE (src/polarized/shdomsub1.f:967-1611), NEWMETHOD, 'N'.
@@ -1179,6 +1254,24 @@ struct Solver {
       }
     }
     if (brdf) brdf_parameters();
+    // SURFACE_PARM_INTERP: B of the bilinearly interpolated ground temperature
+    botplanck.assign(botp.size(), 0);
+    if (srct != 'S') {
+      const int nxs = p.nxsfc, nys = p.nysfc;
+      for (size_t b = 0; b < botp.size(); ++b) {
+        float t = p.gndtemp;
+        if (!sfctemp_in.empty()) {
+          const int i = botp[b];
+          float rx = gridpos[3 * i] / p.delxsfc, ry = gridpos[3 * i + 1] / p.delysfc;
+          int ix = std::max(1, std::min(nxs, (int)rx + 1)), iy = std::max(1, std::min(nys, (int)ry + 1));
+          float u = std::max(0.0f, std::min(1.0f, rx - (ix - 1))), v = std::max(0.0f, std::min(1.0f, ry - (iy - 1)));
+          auto G = [&](int x, int y) { return sfctemp_in[(size_t)((y - 1) % nys) * nxs + ((x - 1) % nxs)]; };
+          t = (1 - u) * (1 - v) * G(ix, iy) + (1 - u) * v * G(ix, iy + 1) + u * (1 - v) * G(ix + 1, iy) +
+              u * v * G(ix + 1, iy + 1);
+        }
+        botplanck[b] = (R)planck_fn(t);
+      }
+    }
   }
 
   // SURFACE_PARM_INTERP (src/polarized/shdomsub1.f:2218-2268) of the BRDF
@@ -1362,6 +1455,12 @@ struct Solver {
         const R *rin = &bcdown[(b * ndown + jang) * nst];
         for (int k1 = 0; k1 < nst; ++k1)
           for (int k = 0; k < nst; ++k) out[k] = out[k] + w * (R)(float)refl[k][k1] * rin[k1];
+        // polarized thermal emission, emissivity 1 - R11 (zero for a solar source)
+        if (srct != 'S') {
+          const R bp = botplanck[b];
+          out[0] = out[0] + w * ((R)1 - (R)(float)refl[0][0]) * bp;
+          for (int k = 1; k < nst; ++k) out[k] = out[k] - w * (R)(float)refl[k][0] * bp;
+        }
       }
   }
 
@@ -1372,6 +1471,7 @@ struct Solver {
     for (size_t b = 0; b < botp.size(); ++b) {
       int i = botp[b];
       bcrad_bot[b] = opi * sfcgridalb[b] * (dirflux[i] + fluxes[2 * (size_t)i]);
+      if (srct != 'S') bcrad_bot[b] = bcrad_bot[b] + botplanck[b] * ((R)1 - sfcgridalb[b]);  // ground emission
     }
   }
 
@@ -1707,7 +1807,7 @@ struct Solver {
         // boundary radiances: unpolarized (Q = U = 0) sky and Lambertian surface
         if (mu[imu] < 0) {
           iupdown = 0;
-          for (int t : topp) { gridrad[(size_t)t * nst] = (R)p.skyrad; for (int s = 1; s < nst; ++s) gridrad[(size_t)t * nst + s] = 0; }
+          for (int t : topp) { gridrad[(size_t)t * nst] = (R)skyrad_bc; for (int s = 1; s < nst; ++s) gridrad[(size_t)t * nst + s] = 0; }
         } else {
           iupdown = 1;
           for (size_t b = 0; b < botp.size(); ++b) {
@@ -2074,7 +2174,7 @@ struct Solver {
           int ipb = gridptr[8 * ic + kGridFace[kface][jj]];
           xs[jj] = gridpos[3 * ipb]; ys[jj] = gridpos[3 * ipb + 1];
           if ((float)mu2 < 0.0f) {
-            rb[jj] = p.skyrad;  // isotropic sky radiance at the top boundary
+            rb[jj] = skyrad_bc;  // isotropic sky radiance at the top boundary
             if (std::find(topp.begin(), topp.end(), ipb) == topp.end()) { err = "FIND_BOUNDARY_RADIANCE: Not at boundary"; return false; }
           } else {
             auto itb = std::lower_bound(botp.begin(), botp.end(), ipb);
@@ -2769,6 +2869,7 @@ bool frozen_render(Solver<R> &S, int ipa, int voxel, float dext, float dalb, int
   const int ng = S.p.npx * S.p.npy * S.p.npz;
   if (ipa < 0 || ipa >= S.npart || voxel < 0 || voxel >= ng) { S.err = "frozen_render: bad index"; return false; }
   if (S.nst != 1) { S.err = "frozen_render: scalar problems only"; return false; }
+  if (S.srct != 'S') { S.err = "frozen_render: solar sources only"; return false; }
   auto extp = S.extp, albp = S.albp;
   auto source = S.source;
   auto shptr = S.shptr;
@@ -2797,6 +2898,7 @@ bool levis_gradient(Solver<R> &S, int ipa, int n, const float *camx, const float
                     float *stokesout, int nthreads) {
   if (ipa < 0 || ipa >= S.npart) { S.err = "levis_gradient: bad species index"; return false; }
   if (S.nst != 1) { S.err = "levis_gradient: scalar problems only"; return false; }
+  if (S.srct != 'S') { S.err = "levis_gradient: solar sources only (as at3d.gradient)"; return false; }
   if (!S.render(n, camx, camy, camz, cammu, camphi, stokesout, nthreads)) return false;  // phase 1 (with phasetab, bcrad)
   Levis<R> L(S);
   if (!L.prepare(ipa, S.err)) return false;

@@ -100,3 +100,86 @@ def gas_absorption_rays_and_truth():
     rays = (x, np.zeros(50), np.full(50, 30.0), np.ones(50), np.zeros(50))
     tau = np.linspace(0.0, 1.0, 50) * 30.0
     return rays, np.exp(-tau) * 0.04 / np.pi * np.exp(-tau)
+
+
+def thermal_problem(srctype="T", nmu=32, nphi=64):
+    """Verify_Thermal / VerifyCombined (tests/test_shdom.py:910-1056 of the
+    reference): the same 50x1x11 grid at 11 um with a non-scattering medium
+    whose extinction grows linearly in x from 0.001 to 0.5 /km, isothermal at
+    288 K, over a Lambertian surface of albedo 0.5 at 300 K, independent-pixel
+    mode, no delta-M, a cold (0 K) sky; 'B' adds an overhead sun of flux 1.
+    The reference runs NMU=128, NPHI=256; this scene takes the angular
+    resolution as arguments (its analytic answer does not depend on it)."""
+    pb = brdf_l1_problem()
+    ray = pb.species[0]
+    npx, npy, npz = ray.extinction.shape
+    ray.extinction = np.broadcast_to(np.linspace(0.001, 0.5, npx)[:, None, None], (npx, npy, npz)).astype(np.float32)
+    ray.ssalb = np.zeros((npx, npy, npz), np.float32)
+    pb.surface_albedo = 0.5
+    pb.ground_temperature = 300.0
+    pb.temperature = np.full((npx, npy, npz), 288.0, np.float32)
+    pb.srctype, pb.units, pb.wavelength = srctype, "R", 11.0
+    pb.skyrad = 0.0
+    pb.solarmu, pb.solaraz = -1.0, 0.0
+    pb.solarflux = 1.0 if srctype == "B" else 0.0
+    p = pb.params
+    p.num_mu_bins, p.num_phi_bins = nmu, nphi
+    p.split_accuracy = p.spherical_harmonics_accuracy = 0.0
+    p.solution_accuracy = 1e-5
+    p.x_boundary_condition = p.y_boundary_condition = "periodic"
+    p.ip_flag, p.tautol, p.deltam = 1, 0.1, False
+    return pb
+
+
+def thermal_rays_and_truth(srctype="T"):
+    """Nadir-viewing rays at 30 km and the reference test's closed form: the
+    transmitted ground emission, the emission of the isothermal slab, and the
+    slab's downwelling flux reflected by the surface (2 E3 written with E1);
+    'B' adds the doubly transmitted reflected sun, 0.5 T^2 / pi.  The Planck
+    function with physical constants, as the reference test computes it."""
+    from scipy.special import exp1
+
+    def planck(t, wl, c=2.99792458e8, h=6.62606876e-34, k=1.3806503e-23):
+        wl = wl * 1e-6
+        return 2 * h * c ** 2 / wl ** 5 / (np.exp(h * c / (wl * k * t)) - 1.0) * 1e-6
+
+    x = np.linspace(0, 1.0 - 1.0 / 50, 50)
+    rays = (x, np.zeros(50), np.full(50, 30.0), np.ones(50), np.zeros(50))
+    tau = 30.0 * np.linspace(0.001, 0.5, 50)
+    tr = np.exp(-tau)
+    b288 = planck(288.0, 11.0)
+    rad = 0.5 * planck(300.0, 11.0) * tr + b288 * (1 - tr) + tr * (0.5 * b288 * (-tr * (1 - tau) - tau ** 2 * exp1(tau) + 1))
+    if srctype == "B":
+        rad = rad + 0.5 * tr * tr / np.pi
+    return rays, rad
+
+
+def thermal_cloud_problem(srctype="T", num_stokes=1, boundary="open", isothermal=None, units="R"):
+    """A 16x16x14 absorbing cloud (single-scattering albedo 0.6) in a thin
+    Rayleigh layer at 11 um with a temperature that falls with height and
+    varies across x, over a 295 K Lambertian ground of albedo 0.05 under a
+    200 K sky ('T'; 'B' keeps a zero sky radiance and adds the sun).
+    num_stokes=3 uses the polarized mixture phase matrix.  isothermal=T0
+    puts the medium, the ground and the sky at T0 K."""
+    from at3d_gb300.scenes import cloud_blob, polarized_blob
+    if num_stokes == 3:
+        pb = polarized_blob(seed=5, nx=16, ny=16, nz=14, dx=0.04, dz=0.06, boundary=boundary, ssa=0.6)
+    else:
+        pb = cloud_blob(seed=5, nx=16, ny=16, nz=14, dx=0.04, dz=0.06, boundary=boundary)
+        pb.species[0].ssalb = np.full_like(pb.species[0].extinction, 0.6)
+    npx, npy, npz = pb.shape
+    x = np.arange(npx) * pb.delx
+    X, _, Z = np.meshgrid(x, np.arange(npy) * pb.dely, pb.zlevels, indexing="ij")
+    if isothermal is None:
+        pb.temperature = (285.0 + 5.0 * np.cos(2 * np.pi * X / (npx * pb.delx)) - 6.0 * Z).astype(np.float32)
+        pb.ground_temperature = 295.0
+        pb.skyrad = 200.0 if srctype == "T" else 0.0
+    else:
+        pb.temperature = np.full((npx, npy, npz), isothermal, np.float32)
+        pb.ground_temperature = float(isothermal)
+        pb.skyrad = float(isothermal)
+    pb.srctype, pb.units, pb.wavelength = srctype, units, 11.0
+    if srctype == "T":
+        pb.solarflux = 0.0
+    pb.surface_albedo = 0.05
+    return pb

@@ -1,0 +1,59 @@
+"""Thermal emission in the CPU oracle (srctype 'T' and 'B').
+
+Pinned by the reference's own analytic tests Verify_Thermal and
+VerifyCombined (tests/test_shdom.py:910-1056): a non-scattering isothermal
+slab over an emitting, reflecting Lambertian ground, at the reference's
+resolution NMU=128, NPHI=256 and with its check, np.allclose(atol=3e-4)."""
+import numpy as np
+import pytest
+
+from brdf_scene import thermal_cloud_problem, thermal_problem, thermal_rays_and_truth
+from oracle.oracle import Oracle
+
+
+@pytest.mark.parametrize("srctype", ["T", "B"])
+def test_thermal_slab_closed_form(srctype):
+    o = Oracle(thermal_problem(srctype, nmu=128, nphi=256))
+    o.solve(100)
+    rays, truth = thermal_rays_and_truth(srctype)
+    got = o.render(*rays)
+    assert np.allclose(got, truth, atol=3e-4)
+
+
+def _views(pb, n=64):
+    xs = np.linspace(0.05, 0.55, n)
+    mu = np.where(np.arange(n) % 2 == 0, 1.0, 0.6)
+    return xs, np.full(n, 0.3), np.full(n, float(pb.zlevels[-1])), mu, np.zeros(n)
+
+
+@pytest.mark.parametrize("nst", [1, 3])
+def test_isothermal_enclosure(nst):
+    """Medium, ground and sky at 280 K in brightness-temperature units: the
+    radiance is 280 K in every direction and Q = U = 0.  The reference's
+    discrete ordinates integrate the hemispheric flux to about 1% at NMU=8
+    (the surface reflection term) and its spherical-harmonic source to a
+    few 1e-4, so the check is 1e-3 of 280 K."""
+    pb = thermal_cloud_problem("T", num_stokes=nst, isothermal=280.0, units="T")
+    o = Oracle(pb)
+    o.solve(100)
+    r = o.render(*_views(pb))
+    i = r if nst == 1 else r[:, 0]
+    assert np.abs(i - 280.0).max() < 0.28
+    if nst == 3:
+        assert np.abs(r[:, 1:]).max() < 1e-2
+
+
+def test_thermal_cloud_fp32_matches_fp64():
+    pb = thermal_cloud_problem("T")
+    a, b = Oracle(pb), Oracle(pb, fp64=True)
+    a.solve(100); b.solve(100)
+    ra, rb = a.render(*_views(pb)), b.render(*_views(pb))
+    assert np.sqrt(np.mean((ra - rb) ** 2)) / np.sqrt(np.mean(rb ** 2)) < 1e-5
+
+
+def test_levis_gradient_refuses_thermal():
+    pb = thermal_cloud_problem("T")
+    o = Oracle(pb)
+    o.solve(3)
+    with pytest.raises(RuntimeError, match="solar sources only"):
+        o.levis_gradient(0, _views(pb), np.zeros(64, np.float32))
