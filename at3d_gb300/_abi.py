@@ -38,7 +38,7 @@ class ShdomProblem(C.Structure):
         ("nstokes", C.c_int),
         ("sfc_brdf", C.c_int), ("nsfcpar", C.c_int), ("sfc_params", _f),
         ("srctype", C.c_int), ("units", C.c_int), ("wavelen", C.c_float),
-        ("tempp", _f), ("sfc_temp", _f),
+        ("tempp", _f), ("sfc_temp", _f), ("waveno", C.c_float * 2),
     ]
 
 
@@ -102,7 +102,8 @@ class Problem:
     surface_brdf: str = ""            # '' Lambertian (surface_albedo), or 'R' / 'W' with surface_params
     surface_params: np.ndarray | None = None  # [nxsfc, nysfc, nparams] on (surface_delx, surface_dely)
     srctype: str = "S"                # 'S' solar, 'T' thermal, 'B' both (at3d.source solar/thermal/combined)
-    units: str = "R"                  # thermal units: 'R' radiance, 'T' brightness temperature
+    units: str = "R"                  # thermal units: 'R' radiance, 'T' brightness temperature, 'B' band
+    waveno: tuple = (10000.0, 10001.0)  # cm^-1 band limits for units 'B' (at3d.source's placeholder)
     wavelength: float = 0.0           # micron (Planck function)
     temperature: np.ndarray | None = None       # [npx, npy, npz] K, required for 'T' and 'B'
     ground_temperature: float | np.ndarray = 288.0  # K; an array lives on the surface grid [nxsfc, nysfc]
@@ -213,9 +214,10 @@ class Problem:
         st.nstokes = self.num_stokes
         if self.srctype not in ("S", "T", "B"):
             raise ValueError("srctype must be 'S', 'T' or 'B'")
-        if self.units not in ("R", "T"):
-            raise ValueError("units must be 'R' (radiance) or 'T' (brightness temperature)")
+        if self.units not in ("R", "T", "B"):
+            raise ValueError("units must be 'R' (radiance), 'T' (brightness temperature) or 'B' (band)")
         st.srctype, st.units, st.wavelen = ord(self.srctype), ord(self.units), float(self.wavelength)
+        st.waveno[0], st.waveno[1] = float(self.waveno[0]), float(self.waveno[1])
         if self.srctype != "S":
             if self.temperature is None:
                 raise KeyError("a thermal source needs the temperature of the medium")

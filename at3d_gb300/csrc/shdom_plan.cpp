@@ -25,6 +25,7 @@
 #include "shdom_plan.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <list>
@@ -165,12 +166,51 @@ void ylm_unpol(int ml, int mm, double mu, float phi, float *y) {
   }
 }
 
+
+// Band integral of Planck's law (INTEGRATE_PLANCK, src/polarized/shdomsub2.f:
+// 4795-4873): F = integral of x^3/(e^x - 1) between x1 < x2, from the series
+// x^3/(e^x - 1) = x^2 sum_n B_n x^n / n! below x = 1 (Bernoulli numbers,
+// terms through x^29) and sum_n e^(-n x) (x^3/n + 3x^2/n^2 + 6x/n^3 + 6/n^4)
+// (15 terms) for the tail above it.
+static double planck_int_low(double x) {
+  // coefficient of x^k, built once (thread-safe static initialisation)
+  static const std::array<double, 30> coef = [] {
+    std::array<double, 30> c{};
+    double b[28], bin[30][30];
+    for (int n = 0; n < 30; ++n) { bin[n][0] = bin[n][n] = 1.0; for (int k = 1; k < n; ++k) bin[n][k] = bin[n - 1][k - 1] + bin[n - 1][k]; }
+    b[0] = 1.0;
+    for (int m = 1; m < 27; ++m) { double s = 0; for (int k = 0; k < m; ++k) s += bin[m + 1][k] * b[k]; b[m] = -s / (m + 1); }
+    double fact = 1.0;
+    for (int n = 0; n + 3 < 30; ++n) { if (n > 0) fact *= n; c[n + 3] = b[n] / (fact * (n + 3)); }
+    return c;
+  }();
+  double s = coef[4] * x * x * x * x, f = x;
+  for (int k = 3; k <= 29; k += 2) { f *= x * x; s += coef[k] * f; }
+  return s;
+}
+static double planck_int_high(double x) {
+  double s = 0.0;
+  for (int n = 1; n <= 15; ++n)
+    s += std::exp(-n * x) * (x * x * x / n + 3 * x * x / ((double)n * n) + 6 * x / ((double)n * n * n) + 6.0 / ((double)n * n * n * n));
+  return s;
+}
+static double planck_band(double x1, double x2) {
+  const double c = 1.0;
+  if (x1 < c && x2 < c) return planck_int_low(x2) - planck_int_low(x1);
+  if (x1 < c) return planck_int_low(c) - planck_int_low(x1) + planck_int_high(c) - planck_int_high(x2);
+  return planck_int_high(x1) - planck_int_high(x2);
+}
+
 // PLANCK_FUNCTION (src/polarized/shdomsub2.f:4756-4791): Planck's law in
 // SHDOM's units and single precision, c1 = 1.1911e8 W um^4/(m^2 sr),
-// c2 = 1.4388e4 um K.
-float planck_fn(float t, char units, float wavelen) {
+// c2 = 1.4388e4 um K; units 'B' integrate it over the band waveno (cm^-1).
+float planck_fn(float t, char units, float wavelen, const float *waveno) {
   if (units == 'T') return t;
   if (t <= 0.f) return 0.f;
+  if (units == 'B') {
+    const double x1 = 1.4388 * waveno[0] / t, x2 = 1.4388 * waveno[1] / t;
+    return (float)(1.1911e-8 * std::pow(t / 1.4388, 4) * planck_band(x1, x2));
+  }
   const float w = wavelen;
   return 1.1911e8f / (w * w * w * w * w) / (std::exp(1.4388e4f / (w * t)) - 1.0f);
 }
@@ -680,7 +720,7 @@ bool build_medium(const shdom_problem &p, Plan &P) {
     P.thermal.assign(npts, 0.f);
     parallel_for(npts, [&](int b, int e) {
       for (int ipt = b; ipt < e; ++ipt) {
-        const float bb = planck_fn(temp[ipt], P.unitc, p.wavelen);
+        const float bb = planck_fn(temp[ipt], P.unitc, p.wavelen, p.waveno);
         float tp = 0.f;
         for (int ipa = 0; ipa < npart; ++ipa) {
           const size_t o = (size_t)ipa * npts + ipt;
@@ -860,7 +900,7 @@ bool build_medium(const shdom_problem &p, Plan &P) {
       // depth between the column's levels, taken from the top down
       const bool eth = P.srct == 'T';
       auto tlev = [&](int k) { return temp[(size_t)(nz - 1 - k) + (size_t)nz * col]; };
-      double planck1 = eth ? pid * (double)planck_fn(tlev(0), P.unitc, p.wavelen) : 0.0;
+      double planck1 = eth ? pid * (double)planck_fn(tlev(0), P.unitc, p.wavelen, p.waveno) : 0.0;
       for (int l = 0, i = 2; l < nlay; ++l, i += 2) {
         double dt = od[l], tr, rf, sp, sm;
         if (dt == 0.0) { tr = 1; rf = 0; sp = 0; sm = 0; }
@@ -878,7 +918,7 @@ bool build_medium(const shdom_problem &p, Plan &P) {
           }
           double r1p, r2m, r2p, r1m;
           if (eth) {
-            const double planck2 = pid * (double)planck_fn(tlev(l + 1), P.unitc, p.wavelen);
+            const double planck2 = pid * (double)planck_fn(tlev(l + 1), P.unitc, p.wavelen, p.waveno);
             const double vv = 2.0 * (planck2 - planck1) / (3.0 * (1. - om * g) * dt);
             r1p = -vv + planck1; r2m = vv + planck2; r2p = -vv + planck2; r1m = vv + planck1;
             planck1 = planck2;
@@ -906,8 +946,8 @@ bool build_medium(const shdom_problem &p, Plan &P) {
       if (P.srct == 'S') {
         rhs[1] = pid * p.skyrad; rhs[n] = (1.0 - gem) * sf * std::exp(-tau / mu0);
       } else {  // emitting ground and sky ('T' and 'B')
-        rhs[1] = pid * (double)planck_fn(p.skyrad, P.unitc, p.wavelen);
-        rhs[n] = pid * (double)planck_fn(p.gndtemp, P.unitc, p.wavelen) * gem;
+        rhs[1] = pid * (double)planck_fn(p.skyrad, P.unitc, p.wavelen, p.waveno);
+        rhs[n] = pid * (double)planck_fn(p.gndtemp, P.unitc, p.wavelen, p.waveno) * gem;
       }
       dg[1] = 0.0; up[1] = 1.0;
       dg[n] = -(1.0 - gem); lo[n] = 1.0;
@@ -1306,13 +1346,16 @@ bool build_plan(const shdom_problem &p, Plan &P) {
   P.srct = p.srctype ? (char)p.srctype : 'S';
   P.unitc = p.units ? (char)p.units : 'R';
   if (P.srct != 'S' && P.srct != 'T' && P.srct != 'B') { P.err = "srctype must be 'S', 'T' or 'B'"; return false; }
-  if (P.unitc != 'R' && P.unitc != 'T') { P.err = "units must be 'R' (radiance) or 'T' (brightness temperature)"; return false; }
+  if (P.unitc != 'R' && P.unitc != 'T' && P.unitc != 'B') { P.err = "units must be 'R', 'T' or 'B'"; return false; }
+  if (P.srct != 'S' && P.unitc == 'B' && !(p.waveno[0] > 0.f && p.waveno[1] > p.waveno[0])) {
+    P.err = "band units need 0 < waveno[0] < waveno[1]"; return false;
+  }
   if (P.srct != 'S') {
     if (!p.tempp) { P.err = "a thermal source needs the temperature field"; return false; }
     if (P.unitc == 'R' && !(p.wavelen > 0.f)) { P.err = "a thermal source in radiance units needs the wavelength"; return false; }
   }
   // COMPUTE_TOP_RADIANCES: the sky brightness temperature becomes a radiance for 'T'
-  P.skyrad_bc = P.srct == 'T' ? planck_fn(p.skyrad, P.unitc, p.wavelen) : p.skyrad;
+  P.skyrad_bc = P.srct == 'T' ? planck_fn(p.skyrad, P.unitc, p.wavelen, p.waveno) : p.skyrad;
   if (!build_medium(p, P)) return false;
   build_direct(p, P);
   // bottom surface albedo (PREP_SURFACE periodic grid + SURFACE_PARM_INTERP)
@@ -1332,7 +1375,7 @@ bool build_plan(const shdom_problem &p, Plan &P) {
   // (SURFACE_PARM_INTERP) or of the one ground temperature
   P.botplanck.clear();
   if (P.srct != 'S') {
-    P.botplanck.assign(P.botp.size(), planck_fn(p.gndtemp, P.unitc, p.wavelen));
+    P.botplanck.assign(P.botp.size(), planck_fn(p.gndtemp, P.unitc, p.wavelen, p.waveno));
     if (p.sfc_temp && p.nxsfc > 0 && p.nysfc > 0 && (p.sfc_variable || p.sfc_brdf)) {
       const int nxs = p.nxsfc, nys = p.nysfc;
       auto G = [&](int x, int y) { return p.sfc_temp[(size_t)((y - 1) % nys) * nxs + ((x - 1) % nxs)]; };
@@ -1342,7 +1385,7 @@ bool build_plan(const shdom_problem &p, Plan &P) {
         int ix = std::max(1, std::min(nxs, (int)rx + 1)), iy = std::max(1, std::min(nys, (int)ry + 1));
         float u = std::max(0.f, std::min(1.f, rx - (ix - 1))), v = std::max(0.f, std::min(1.f, ry - (iy - 1)));
         const float t = (1 - u) * (1 - v) * G(ix, iy) + (1 - u) * v * G(ix, iy + 1) + u * (1 - v) * G(ix + 1, iy) + u * v * G(ix + 1, iy + 1);
-        P.botplanck[k] = planck_fn(t, P.unitc, p.wavelen);
+        P.botplanck[k] = planck_fn(t, P.unitc, p.wavelen, p.waveno);
       }
     }
   }

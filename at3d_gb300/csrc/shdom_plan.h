@@ -168,9 +168,9 @@ struct Plan {
 // Fills every table of the plan; returns false with plan.err set on error.
 bool build_plan(const shdom_problem &p, Plan &plan);
 
-// PLANCK_FUNCTION for units 'R' (W/(m^2 sr micron) at wavelen microns)
-// and 'T' (the temperature itself).
-float planck_fn(float t, char units, float wavelen);
+// PLANCK_FUNCTION for units 'R' (W/(m^2 sr micron) at wavelen microns),
+// 'T' (the temperature itself) and 'B' (W/(m^2 sr) over the band waveno[2], cm^-1).
+float planck_fn(float t, char units, float wavelen, const float *waveno);
 
 // Real generalized spherical harmonics (unpolarized element) at one
 // direction, NLM values in the SHDOM term order.

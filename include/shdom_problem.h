@@ -80,10 +80,12 @@ typedef struct shdom_problem {
      *      and the sky (skyrad is then a brightness temperature); 'B' adds
      *      both sources.  0 means 'S' (solar only) ---- */
     int srctype;                   /* 0 or 'S', 'T', 'B' */
-    int units;                     /* 'R' radiance W/(m^2 sr um) (0 means 'R'), 'T' brightness temperature */
+    int units;                     /* 'R' radiance W/(m^2 sr um) (0 means 'R'), 'T' brightness
+                                      temperature, 'B' band-integrated over waveno */
     float wavelen;                 /* micron, for the Planck function */
     const float *tempp;            /* [npx][npy][npz] K on the property grid ('T', 'B') */
     const float *sfc_temp;         /* [nysfc][nxsfc] K on the surface grid, or NULL: gndtemp everywhere */
+    float waveno[2];               /* cm^-1, band limits for units 'B' (band-integrated W/(m^2 sr)) */
 } shdom_problem;
 
 #ifdef __cplusplus

@@ -246,15 +246,50 @@ struct Solver {
   // point (TOTAL_PLANCK of COMPUTE_SOURCE); botplanck B at the bottom points
   // (SFCGRIDPARMS(1)); skyrad_bc the radiance of the top boundary.
   char srct = 'S', unitc = 'R';
+  // INTLOW / INTHIGH: the integral of x^3/(e^x - 1) from 0 to x by its
+  // Taylor series (the Bernoulli-number expansion of x/(e^x - 1), through
+  // x^29) and from x to infinity by the exponential series (15 terms)
+  static double int_low(double x) {
+    double b[28], s = 0, fact = 1, pw;
+    b[0] = 1;
+    for (int m = 1; m < 28; ++m) {
+      double acc = 0, binom = 1;  // C(m+1, k)
+      for (int k = 0; k < m; ++k) { acc += binom * b[k]; binom = binom * (m + 1 - k) / (k + 1); }
+      b[m] = -acc / (m + 1);
+    }
+    for (int n = 0; n + 3 <= 29; ++n) {
+      if (n > 0) fact *= n;
+      if (n != 1 && (n & 1)) continue;
+      pw = std::pow(x, n + 3);
+      s += b[n] / (fact * (n + 3)) * pw;
+    }
+    return s;
+  }
+  static double int_high(double x) {
+    double s = 0;
+    for (int n = 1; n <= 15; ++n)
+      s += std::exp(-n * x) * (std::pow(x, 3) / n + 3 * x * x / std::pow(n, 2) + 6 * x / std::pow(n, 3) + 6.0 / std::pow(n, 4));
+    return s;
+  }
+  static double band_integral(double x1, double x2) {
+    if (x1 < 1.0 && x2 < 1.0) return int_low(x2) - int_low(x1);
+    if (x1 < 1.0) return int_low(1.0) - int_low(x1) + int_high(1.0) - int_high(x2);
+    return int_high(x1) - int_high(x2);
+  }
   std::vector<float> tempp_in, sfctemp_in, temp;
   std::vector<R> planck_tot, botplanck;
   float skyrad_bc = 0.f;
 
   // PLANCK_FUNCTION (src/polarized/shdomsub2.f:4756-4791) for units 'R'
-  // (W/(m^2 sr micron) at p.wavelen) and 'T' (brightness temperature).
+  // (W/(m^2 sr micron) at p.wavelen), 'T' (brightness temperature) and 'B'
+  // (INTEGRATE_PLANCK over the band p.waveno, W/(m^2 sr)).
   float planck_fn(float t) const {
     if (unitc == 'T') return t;
     if (t <= 0.f) return 0.f;
+    if (unitc == 'B') {
+      const double x1 = 1.4388 * p.waveno[0] / t, x2 = 1.4388 * p.waveno[1] / t;
+      return (float)(1.1911e-8 * std::pow(t / 1.4388, 4) * band_integral(x1, x2));
+    }
     const float w = p.wavelen;
     return 1.1911e8f / (w * w * w * w * w) / (std::exp(1.4388e4f / (w * t)) - 1.0f);
   }
@@ -286,7 +321,7 @@ struct Solver {
     srct = p.srctype ? (char)p.srctype : 'S';
     unitc = p.units ? (char)p.units : 'R';
     if (srct != 'S' && srct != 'T' && srct != 'B') { err = "srctype must be 'S', 'T' or 'B'"; return false; }
-    if (unitc != 'R' && unitc != 'T') { err = "units must be 'R' or 'T'"; return false; }
+    if (unitc != 'R' && unitc != 'T' && unitc != 'B') { err = "units must be 'R', 'T' or 'B'"; return false; }
     if (srct != 'S') {
       if (!p.tempp) { err = "a thermal source needs the temperature field"; return false; }
       if (unitc == 'R' && !(p.wavelen > 0.f)) { err = "a thermal source in radiance units needs the wavelength"; return false; }

@@ -120,3 +120,16 @@ def test_levis_gradient_refuses_thermal(rte_cls):
     r.solve(2, verbose=False)
     with pytest.raises(SHDOMError, match="solar sources only"):
         r.levis_gradient(_views(pb), np.zeros(64, np.float32))
+
+
+def test_band_units(rte_cls):
+    """Units 'B' (the band integral of the Planck function over 800-1000
+    cm^-1) on the absorbing cloud, against the oracle."""
+    pb = thermal_cloud_problem("T", units="B")
+    pb.waveno = (800.0, 1000.0)
+    pb.skyrad = 200.0
+    r = rte_cls.from_problem(pb)
+    r.solve(100, verbose=False)
+    o = Oracle(pb)
+    o.solve(100)
+    assert relrms(r.render(*_views(pb)), o.render(*_views(pb))) < 1e-4

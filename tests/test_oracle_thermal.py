@@ -57,3 +57,29 @@ def test_levis_gradient_refuses_thermal():
     o.solve(3)
     with pytest.raises(RuntimeError, match="solar sources only"):
         o.levis_gradient(0, _views(pb), np.zeros(64, np.float32))
+
+
+def planck_band_shdom(t, w1, w2):
+    """Planck's law with SHDOM's constants integrated over [w1, w2] cm^-1
+    by adaptive quadrature, W/(m^2 sr)."""
+    from scipy.integrate import quad
+    c1, c2 = 1.1911e-8, 1.4388  # W/(m^2 sr cm^-4), cm K
+    return quad(lambda nu: c1 * nu ** 3 / np.expm1(c2 * nu / t), w1, w2, epsabs=0, epsrel=1e-12)[0]
+
+
+@pytest.mark.parametrize("band", [(800.0, 1000.0), (20.0, 200.0), (2000.0, 2500.0)])
+def test_band_units_black_enclosure(band):
+    """Units 'B' (INTEGRATE_PLANCK): a black ground, a black sky
+    and the non-scattering slab all at 288 K make every radiance the band
+    integral of the Planck function; the bands cover both series of the
+    integral (x below and above 1)."""
+    pb = thermal_problem("T", nmu=16, nphi=32)
+    pb.units, pb.waveno = "B", band
+    pb.surface_albedo, pb.ground_temperature = 0.0, 288.0
+    pb.skyrad = 288.0
+    o = Oracle(pb)
+    o.solve(100)
+    rays, _ = thermal_rays_and_truth("T")
+    got = o.render(*rays)
+    # float accumulation along the optically thick columns leaves 1e-5
+    assert np.allclose(got, planck_band_shdom(288.0, *band), rtol=2e-5, atol=0)
