@@ -1396,24 +1396,31 @@ bool build_plan(const shdom_problem &p, Plan &P) {
   P.nsfcpar = 0;
   P.botpar.clear(); P.brdf_dn.clear(); P.brdf_up.clear();
   if (p.sfc_brdf) {
-    if ((p.sfc_brdf != 'R' && p.sfc_brdf != 'W' && p.sfc_brdf != 'D') || p.nsfcpar < (p.sfc_brdf == 'D' ? 5 : 3) ||
+    const char bt = (char)p.sfc_brdf;
+    if ((bt != 'R' && bt != 'W' && bt != 'D' && bt != 'O') || p.nsfcpar < (bt == 'D' ? 5 : bt == 'O' ? 2 : 3) ||
         !p.sfc_params || p.nxsfc < 1 || p.nysfc < 1) {
-      P.err = "surface BRDF: types 'R' (RPV), 'W' (wave-Fresnel; 3 parameters) and 'D' (Diner; 5) on a surface grid";
+      P.err = "surface BRDF: types 'R' (RPV), 'W' (wave-Fresnel; 3 parameters), 'D' (Diner; 5) and 'O' (ocean; 2) on a surface grid";
       return false;
     }
-    if (p.sfc_brdf == 'R' && p.nstokes != 1) { P.err = "RPV BRDF is only for unpolarized case"; return false; }
+    if (bt == 'R' && p.nstokes != 1) { P.err = "RPV BRDF is only for unpolarized case"; return false; }
+    if (bt == 'O' && p.nstokes != 1) { P.err = "Ocean BRDF from 6S is only for unpolarized case"; return false; }
+    if (bt == 'O' && !(p.wavelen > 0.f)) { P.err = "the ocean BRDF needs the wavelength"; return false; }
     const int nxs = p.nxsfc, nys = p.nysfc, np_ = p.nsfcpar;
-    P.nsfcpar = np_;
-    P.botpar.assign(P.botp.size() * np_, 0.f);
+    // the ocean model also takes the wavelength: appended to every bottom
+    // point's parameters (wind speed, pigment, wavelength)
+    const int npb = bt == 'O' ? 3 : np_;
+    P.nsfcpar = npb;
+    P.botpar.assign(P.botp.size() * npb, 0.f);
     auto G = [&](int x, int y, int j) { return p.sfc_params[((size_t)((y - 1) % nys) * nxs + ((x - 1) % nxs)) * np_ + j]; };
     for (size_t k = 0; k < P.botp.size(); ++k) {
       int i = P.botp[k];
       float rx = P.gridpos[3 * i] / p.delxsfc, ry = P.gridpos[3 * i + 1] / p.delysfc;
       int ix = std::max(1, std::min(nxs, (int)rx + 1)), iy = std::max(1, std::min(nys, (int)ry + 1));
       float u = std::max(0.f, std::min(1.f, rx - (ix - 1))), v = std::max(0.f, std::min(1.f, ry - (iy - 1)));
-      for (int j = 0; j < np_; ++j)
-        P.botpar[k * np_ + j] = (1 - u) * (1 - v) * G(ix, iy, j) + (1 - u) * v * G(ix, iy + 1, j) +
+      for (int j = 0; j < std::min(np_, npb); ++j)
+        P.botpar[k * npb + j] = (1 - u) * (1 - v) * G(ix, iy, j) + (1 - u) * v * G(ix, iy + 1, j) +
                                 u * (1 - v) * G(ix + 1, iy, j) + u * v * G(ix + 1, iy + 1, j);
+      if (bt == 'O') P.botpar[k * npb + 2] = p.wavelen;
     }
     const float opi = 1.0f / (float)std::acos(-1.0f);
     for (int j = 0; j < P.nmu; ++j)

@@ -85,3 +85,13 @@ def diner(A, K, B, ZETA, SIGMA, ground_temperature=298.15, delx=None, dely=None)
     orientation when sigma <= 0)."""
     par, dx, dy = _stack(A, K, B, ZETA, SIGMA, delx=delx, dely=dely)
     return BRDFSurface("D", par, float(ground_temperature), dx, dy)
+
+
+def ocean_unpolarized(surface_wind_speed, pigmentation, ground_temperature=298.15, delx=None,
+                      dely=None) -> BRDFSurface:
+    """The 6S ocean BRDF (at3d/surface.py ocean_unpolarized; src/ocean_brdf.f):
+    whitecaps, Cox-Munk sun glint and the Case I water body for a wind
+    speed (m/s) and a pigment concentration (mg/m^3); scalar problems only,
+    and the solver needs the wavelength."""
+    par, dx, dy = _stack(surface_wind_speed, pigmentation, delx=delx, dely=dely)
+    return BRDFSurface("O", par, float(ground_temperature), dx, dy)

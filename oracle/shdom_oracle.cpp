@@ -310,12 +310,14 @@ struct Solver {
     if (p.sfc_variable) sfcalb.assign(p.sfc_albedo, p.sfc_albedo + (size_t)p.nxsfc * p.nysfc);
     brdf = p.sfc_brdf; nsfcpar = p.nsfcpar;
     if (brdf) {
-      if ((brdf != 'R' && brdf != 'W' && brdf != 'D') || p.nsfcpar < (brdf == 'D' ? 5 : 3) || !p.sfc_params ||
-          p.nxsfc < 1 || p.nysfc < 1) {
-        err = "surface BRDF: types 'R' (RPV), 'W' (wave-Fresnel; 3 parameters) and 'D' (Diner; 5) on a surface grid";
+      if ((brdf != 'R' && brdf != 'W' && brdf != 'D' && brdf != 'O') ||
+          p.nsfcpar < (brdf == 'D' ? 5 : brdf == 'O' ? 2 : 3) || !p.sfc_params || p.nxsfc < 1 || p.nysfc < 1) {
+        err = "surface BRDF: types 'R' (RPV), 'W' (wave-Fresnel; 3 parameters), 'D' (Diner; 5) and 'O' (ocean; 2) on a surface grid";
         return false;
       }
       if (brdf == 'R' && nst != 1) { err = "RPV BRDF is only for unpolarized case"; return false; }
+      if (brdf == 'O' && nst != 1) { err = "Ocean BRDF from 6S is only for unpolarized case"; return false; }
+      if (brdf == 'O' && !(p.wavelen > 0.f)) { err = "the ocean BRDF needs the wavelength"; return false; }
       sfcpar.assign(p.sfc_params, p.sfc_params + (size_t)p.nxsfc * p.nysfc * p.nsfcpar);
     }
     srct = p.srctype ? (char)p.srctype : 'S';
@@ -1331,10 +1333,185 @@ struct Solver {
   // SURFACE_BRDF (src/polarized/shdomsub2.f:1222-1300): the reflection
   // matrix for incident direction (mu1 < 0, phi1) and outgoing (mu2 > 0,
   // phi2), normalised so that a Lambertian surface returns its albedo.
+
+  // ---- 6S ocean BRDF (src/ocean_brdf.f, the 'O' type of SURFACE_BRDF),
+  // single precision as the reference.  Tables: whitecap reflectance
+  // (Koepke 1984) every 0.1 um, diffuse transmittances of the wavy surface
+  // by zenith angle and wind speed, Morel's (1988) Case I water
+  // coefficients every 5 nm over 400-700 nm, and the Hale & Querry (1973)
+  // refractive index of water.
+  static constexpr float kWhitecap[39] = {
+      0.220f, 0.220f, 0.220f, 0.220f, 0.220f, 0.220f, 0.215f, 0.210f, 0.200f, 0.190f, 0.175f, 0.155f, 0.130f,
+      0.080f, 0.100f, 0.105f, 0.100f, 0.080f, 0.045f, 0.055f, 0.065f, 0.060f, 0.055f, 0.040f, 0.f,    0.f,
+      0.f,    0.f,    0.f,    0.f,    0.f,    0.f,    0.f,    0.f,    0.f,    0.f,    0.f,    0.f,    0.f};
+  static constexpr float kAngBnd[5] = {0.0f, 45.0f, 60.0f, 75.0f, 85.0f};
+  static constexpr float kWsBnd[6] = {1.0f, 3.0f, 5.0f, 7.0f, 9.0f, 20.0f};
+  static constexpr float kTds[5][6] = {{0.9787803f, 0.9787738f, 0.9787626f, 0.9787467f, 0.9787264f, 0.9785573f},
+                                       {0.9706900f, 0.9698871f, 0.9691746f, 0.9685547f, 0.9680276f, 0.9666586f},
+                                       {0.9479931f, 0.9404608f, 0.9385692f, 0.9381815f, 0.9384519f, 0.9430056f},
+                                       {0.9690591f, 0.9275920f, 0.9058769f, 0.8951812f, 0.8899654f, 0.8892645f},
+                                       {0.9980542f, 0.9602273f, 0.9114283f, 0.8713799f, 0.8417820f, 0.7800314f}};
+  static constexpr float kTdv[5][6] = {{0.9787764f, 0.9787535f, 0.9787106f, 0.9786453f, 0.9785548f, 0.9775019f},
+                                       {0.9692680f, 0.9637051f, 0.9564344f, 0.9495727f, 0.9438773f, 0.9288712f},
+                                       {0.9225163f, 0.9069787f, 0.9044844f, 0.9052351f, 0.9068328f, 0.9153687f},
+                                       {0.8048478f, 0.8479503f, 0.8678726f, 0.8797889f, 0.8878716f, 0.9091171f},
+                                       {0.7294627f, 0.8137348f, 0.8453338f, 0.8629867f, 0.8745421f, 0.9036854f}};
+  static constexpr float kKw[61] = {
+      0.0209f, 0.0200f, 0.0196f, 0.0189f, 0.0183f, 0.0182f, 0.0171f, 0.0170f, 0.0168f, 0.0166f, 0.0168f, 0.0170f, 0.0173f,
+      0.0174f, 0.0175f, 0.0184f, 0.0194f, 0.0203f, 0.0217f, 0.0240f, 0.0271f, 0.0320f, 0.0384f, 0.0445f, 0.0490f, 0.0505f,
+      0.0518f, 0.0543f, 0.0568f, 0.0615f, 0.0640f, 0.0640f, 0.0717f, 0.0762f, 0.0807f, 0.0940f, 0.1070f, 0.1280f, 0.1570f,
+      0.2000f, 0.2530f, 0.2790f, 0.2960f, 0.3030f, 0.3100f, 0.3150f, 0.3200f, 0.3250f, 0.3300f, 0.3400f, 0.3500f, 0.3700f,
+      0.4050f, 0.4180f, 0.4300f, 0.4400f, 0.4500f, 0.4700f, 0.5000f, 0.5500f, 0.6500f};
+  static constexpr float kXc[61] = {
+      0.1100f, 0.1110f, 0.1125f, 0.1135f, 0.1126f, 0.1104f, 0.1078f, 0.1065f, 0.1041f, 0.0996f, 0.0971f, 0.0939f, 0.0896f,
+      0.0859f, 0.0823f, 0.0788f, 0.0746f, 0.0726f, 0.0690f, 0.0660f, 0.0636f, 0.0600f, 0.0578f, 0.0540f, 0.0498f, 0.0475f,
+      0.0467f, 0.0450f, 0.0440f, 0.0426f, 0.0410f, 0.0400f, 0.0390f, 0.0375f, 0.0360f, 0.0340f, 0.0330f, 0.0328f, 0.0325f,
+      0.0330f, 0.0340f, 0.0350f, 0.0360f, 0.0375f, 0.0385f, 0.0400f, 0.0420f, 0.0430f, 0.0440f, 0.0445f, 0.0450f, 0.0460f,
+      0.0475f, 0.0490f, 0.0515f, 0.0520f, 0.0505f, 0.0440f, 0.0390f, 0.0340f, 0.0300f};
+  static constexpr float kE[61] = {
+      0.668f, 0.672f, 0.680f, 0.687f, 0.693f, 0.701f, 0.707f, 0.708f, 0.707f, 0.704f, 0.701f, 0.699f, 0.700f, 0.703f, 0.703f,
+      0.703f, 0.703f, 0.704f, 0.702f, 0.700f, 0.700f, 0.695f, 0.690f, 0.685f, 0.680f, 0.675f, 0.670f, 0.665f, 0.660f, 0.655f,
+      0.650f, 0.645f, 0.640f, 0.630f, 0.623f, 0.615f, 0.610f, 0.614f, 0.618f, 0.622f, 0.626f, 0.630f, 0.634f, 0.638f, 0.642f,
+      0.647f, 0.653f, 0.658f, 0.663f, 0.667f, 0.672f, 0.677f, 0.682f, 0.687f, 0.695f, 0.697f, 0.693f, 0.665f, 0.640f, 0.620f,
+      0.600f};
+  static constexpr float kBw[61] = {
+      0.0076f, 0.0072f, 0.0068f, 0.0064f, 0.0061f, 0.0058f, 0.0055f, 0.0052f, 0.0049f, 0.0047f, 0.0045f, 0.0043f, 0.0041f,
+      0.0039f, 0.0037f, 0.0036f, 0.0034f, 0.0033f, 0.0031f, 0.0030f, 0.0029f, 0.0027f, 0.0026f, 0.0025f, 0.0024f, 0.0023f,
+      0.0022f, 0.0022f, 0.0021f, 0.0020f, 0.0019f, 0.0018f, 0.0018f, 0.0017f, 0.0017f, 0.0016f, 0.0016f, 0.0015f, 0.0015f,
+      0.0014f, 0.0014f, 0.0013f, 0.0013f, 0.0012f, 0.0012f, 0.0011f, 0.0011f, 0.0010f, 0.0010f, 0.0010f, 0.0010f, 0.0009f,
+      0.0008f, 0.0008f, 0.0008f, 0.0007f, 0.0007f, 0.0007f, 0.0007f, 0.0007f, 0.0007f};
+  static constexpr float kTwl[62] = {
+      0.250f, 0.275f, 0.300f, 0.325f, 0.345f, 0.375f, 0.400f, 0.425f, 0.445f, 0.475f, 0.500f, 0.525f, 0.550f, 0.575f, 0.600f,
+      0.625f, 0.650f, 0.675f, 0.700f, 0.725f, 0.750f, 0.775f, 0.800f, 0.825f, 0.850f, 0.875f, 0.900f, 0.925f, 0.950f, 0.975f,
+      1.000f, 1.200f, 1.400f, 1.600f, 1.800f, 2.000f, 2.200f, 2.400f, 2.600f, 2.650f, 2.700f, 2.750f, 2.800f, 2.850f, 2.900f,
+      2.950f, 3.000f, 3.050f, 3.100f, 3.150f, 3.200f, 3.250f, 3.300f, 3.350f, 3.400f, 3.450f, 3.500f, 3.600f, 3.700f, 3.800f,
+      3.900f, 4.000f};
+  static constexpr float kTnr[62] = {
+      1.362f, 1.354f, 1.349f, 1.346f, 1.343f, 1.341f, 1.339f, 1.338f, 1.337f, 1.336f, 1.335f, 1.334f, 1.333f, 1.333f, 1.332f,
+      1.332f, 1.331f, 1.331f, 1.331f, 1.330f, 1.330f, 1.330f, 1.329f, 1.329f, 1.329f, 1.328f, 1.328f, 1.328f, 1.327f, 1.327f,
+      1.327f, 1.324f, 1.321f, 1.317f, 1.312f, 1.306f, 1.296f, 1.279f, 1.242f, 1.219f, 1.188f, 1.157f, 1.142f, 1.149f, 1.201f,
+      1.292f, 1.371f, 1.426f, 1.467f, 1.483f, 1.478f, 1.467f, 1.450f, 1.432f, 1.420f, 1.410f, 1.400f, 1.385f, 1.374f, 1.364f,
+      1.357f, 1.351f};
+  static constexpr float kTni[62] = {
+      3.35E-08f, 2.35E-08f, 1.60E-08f, 1.08E-08f, 6.50E-09f, 3.50E-09f, 1.86E-09f, 1.30E-09f, 1.02E-09f, 9.35E-10f, 1.00E-09f,
+      1.32E-09f, 1.96E-09f, 3.60E-09f, 1.09E-08f, 1.39E-08f, 1.64E-08f, 2.23E-08f, 3.35E-08f, 9.15E-08f, 1.56E-07f, 1.48E-07f,
+      1.25E-07f, 1.82E-07f, 2.93E-07f, 3.91E-07f, 4.86E-07f, 1.06E-06f, 2.93E-06f, 3.48E-06f, 2.89E-06f, 9.89E-06f, 1.38E-04f,
+      8.55E-05f, 1.15E-04f, 1.10E-03f, 2.89E-04f, 9.56E-04f, 3.17E-03f, 6.70E-03f, 1.90E-02f, 5.90E-02f, 1.15E-01f, 1.85E-01f,
+      2.68E-01f, 2.98E-01f, 2.72E-01f, 2.40E-01f, 1.92E-01f, 1.35E-01f, 9.24E-02f, 6.10E-02f, 3.68E-02f, 2.61E-02f, 1.95E-02f,
+      1.32E-02f, 9.40E-03f, 5.15E-03f, 3.60E-03f, 3.40E-03f, 3.80E-03f, 4.60E-03f};
+
+  // 1-based bracketing index of x in an increasing table of n entries
+  // (getbound): the searched half depends on the midpoint, and x outside
+  // the table takes the first or the last interval.
+  static int bracket(const float *xv, int n, float x) {
+    const int imid = n / 2 + 1;
+    const int lo = x > xv[imid - 1] ? imid : 1, hi = x > xv[imid - 1] ? n - 1 : imid;
+    for (int i = lo; i <= hi; ++i)
+      if (xv[i - 1] <= x && xv[i] >= x) return i;
+    return x < xv[0] ? 1 : n - 1;
+  }
+
+  // Sea-water reflectance below the surface for Case I waters (morcasiwat):
+  // R = 0.33 bb / (u Kd), iterated on u; zero outside 400-700 nm.
+  static float morel_water(float wl, float c) {
+    if (wl < 0.400f || wl > 0.700f) return 0.f;
+    const int iwl = 1 + (int)std::lround((wl - 0.400f) / 0.005f);  // NINT: half away from zero
+    const float kw = kKw[iwl - 1], xc = kXc[iwl - 1], e = kE[iwl - 1], bw = kBw[iwl - 1];
+    float bb, kd;
+    if (std::fabs(c) < 0.0001f) { bb = 0.5f * bw; kd = kw; }
+    else {
+      const float b = 0.30f * std::pow(c, 0.62f);
+      const float bbt = 0.002f + 0.02f * (0.5f - 0.25f * std::log10(c)) * 0.550f / wl;
+      bb = 0.5f * bw + bbt * b;
+      kd = kw + xc * std::pow(c, e);
+    }
+    float r1 = 0.33f * bb / 0.75f / kd, r2 = r1;
+    for (int it = 0; it < 1000; ++it) {
+      const float u2 = 0.90f * (1.f - r1) / (1.f + 2.25f * r1);
+      r2 = 0.33f * bb / u2 / kd;
+      if (std::fabs((r2 - r1) / r2) < 0.0001f) break;
+      r1 = r2;
+    }
+    return r2;
+  }
+
+  // Unpolarized Fresnel reflectance of a facet (Fresnel), complex index (nr, ni).
+  static float facet_fresnel(float nr, float ni, float coschi, float sinchi) {
+    const float d = nr * nr - ni * ni - sinchi * sinchi;
+    const float a1 = std::fabs(d), a2 = std::sqrt(d * d + 4 * nr * nr * ni * ni);
+    const float u = std::sqrt(0.5f * (a1 + a2)), v = std::sqrt(std::max(0.0f, 0.5f * (-a1 + a2)));
+    const float rr2 = ((coschi - u) * (coschi - u) + v * v) / ((coschi + u) * (coschi + u) + v * v);
+    const float b1 = (nr * nr - ni * ni) * coschi, b2 = 2 * nr * ni * coschi;
+    const float rl2 = ((b1 - u) * (b1 - u) + (b2 - v) * (b2 - v)) / ((b1 + u) * (b1 + u) + (b2 + v) * (b2 + v));
+    return (rr2 + rl2) / 2.f;
+  }
+
+  // Sun glint of the Cox-Munk anisotropic (Gram-Charlier) slope
+  // distribution (sunglint); angles in degrees.
+  static float sun_glint(float wspd, float nr, float ni, float azw, float ts, float tv, float fi) {
+    const float pi = std::atan(1.f) * 4.f, fac = pi / 180.f;
+    const float phw = azw * fac, cs = std::cos(ts * fac), cv = std::cos(tv * fac), ss = std::sin(ts * fac),
+                sv = std::sin(tv * fac), phi = fi * fac;
+    const float zx = -sv * std::sin(phi) / (cs + cv), zy = (ss + sv * std::cos(phi)) / (cs + cv);
+    const float tilt = std::atan(std::sqrt(zx * zx + zy * zy));
+    const float sc = 0.003f + 0.00192f * wspd, su = 0.00316f * wspd;
+    const float c21 = 0.01f - 0.0086f * wspd, c03 = 0.04f - 0.033f * wspd, c40 = 0.40f, c22 = 0.12f, c04 = 0.23f;
+    const float xe = (std::cos(phw) * zx + std::sin(phw) * zy) / std::sqrt(sc);
+    const float xn = (-std::sin(phw) * zx + std::cos(phw) * zy) / std::sqrt(su);
+    const float xe2 = xe * xe, xn2 = xn * xn;
+    float coef = 1 - c21 / 2.f * (xe2 - 1) * xn - c03 / 6.f * (xn2 - 3) * xn;
+    coef = coef + c40 / 24.f * (xe2 * xe2 - 6 * xe2 + 3);
+    coef = coef + c04 / 24.f * (xn2 * xn2 - 6 * xn2 + 3);
+    coef = coef + c22 / 4.f * (xe2 - 1) * (xn2 - 1);
+    const float proba = coef / 2.f / pi / std::sqrt(su) / std::sqrt(sc) * std::exp(-(xe2 + xn2) / 2.f);
+    float cos2chi = cv * cs + sv * ss * std::cos(phi);
+    cos2chi = std::min(1.0f, std::max(-1.0f, cos2chi));
+    const float coschi = std::sqrt(0.5f * (1 + cos2chi)), sinchi = std::sqrt(0.5f * (1 - cos2chi));
+    const float r1 = facet_fresnel(nr, ni, coschi, sinchi);
+    const float ct = std::cos(tilt), ct2 = ct * ct;
+    return pi * r1 * proba / 4.f / cs / cv / (ct2 * ct2);
+  }
+
+  // ocean_brdf_sw with the default salinity: whitecaps + glint + water body.
+  static float ocean_reflection(float pws, float pcl, float pwl, float xmuo, float xmu, float xphi, float xpaw) {
+    const float pi = std::atan(1.f) * 4.f, fac = pi / 180.f;
+    const float paw = xpaw / fac;
+    const float phi = xphi < 0.f ? -xphi : (xphi >= 2.0f * pi ? xphi - 2.0f * pi : xphi);
+    const float tetas = std::acos(xmuo <= 0.028f ? 0.028f : xmuo) / fac;
+    const float tetav = std::acos(xmu <= 0.028f ? 0.028f : xmu) / fac;
+    const float wl = pwl < 0.4f ? 0.4f : (pwl > 4.0f ? 4.0f : pwl);
+    const float fi = 180.0f - phi / fac;
+    const float wspd = std::max(0.25f, pws);
+    // refractive index of sea water (indwat): Hale & Querry pure water,
+    // interpolated, plus 0.006 for the default salinity
+    int i = 2;
+    while (!(wl < kTwl[i - 1]) && i < 62) ++i;
+    const float xwl = kTwl[i - 1] - kTwl[i - 2];
+    float nr = kTnr[i - 2] + (wl - kTwl[i - 2]) * (kTnr[i - 1] - kTnr[i - 2]) / xwl;
+    const float ni = kTni[i - 2] + (wl - kTwl[i - 2]) * (kTni[i - 1] - kTni[i - 2]) / xwl;
+    nr = nr + 0.006f;
+    const float n12 = std::sqrt(nr * nr + ni * ni);
+    // whitecaps (Lambertian)
+    const float w = 2.95E-06f * std::pow(wspd, 3.52f);
+    const int iwl = 1 + (int)((wl - 0.2f) / 0.1f);
+    const float wlp = 0.5f + (iwl - 1) * 0.1f;
+    const float refi = kWhitecap[iwl] + (wl - wlp) / 0.1f * (kWhitecap[iwl - 1] - kWhitecap[iwl]);
+    const float rwc = w * refi;
+    const float rw = morel_water(wl, pcl);
+    const int iws1 = bracket(kWsBnd, 6, wspd), isz1 = bracket(kAngBnd, 5, tetas), ivz1 = bracket(kAngBnd, 5, tetav);
+    const float tds = kTds[isz1 - 1][iws1 - 1], tdv = kTdv[ivz1 - 1][iws1 - 1];
+    const float rog = sun_glint(wspd, nr, ni, paw, tetas, tetav, fi);
+    const float a = 0.485f;
+    const float rwb = (1 / (n12 * n12)) * tds * tdv * rw / (1 - a * rw);
+    return rwc + (1 - w) * rog + (1 - rwc) * rwb;
+  }
+
   void surface_brdf(const R *par, float mu2, float phi2, float mu1, float phi1, double refl[3][3]) const {
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) refl[i][j] = 0.0;
-    if (brdf == 'R') {
+    if (brdf == 'O') {
+      refl[0][0] = ocean_reflection((float)par[0], (float)par[1], p.wavelen, -mu1, mu2, phi1 - phi2, phi1);
+    } else if (brdf == 'R') {
       refl[0][0] = rpv_reflection((float)par[0], (float)par[1], (float)par[2], -mu1, mu2,
                                   phi1 - phi2 - (float)std::acos(-1.0f));
     } else if (brdf == 'D') {

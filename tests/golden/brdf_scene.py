@@ -55,6 +55,19 @@ def brdf_rpv_problem():
     return pb
 
 
+def brdf_ocean_problem():
+    """Verify_Ocean_Unpolarized_Surfaces (tests/test_shdom.py:634-674 of the
+    reference): the 6S ocean BRDF with the wind speed growing in x from 4
+    to 11.84 m/s and no pigment, at 0.85 um."""
+    pb = brdf_l1_problem()
+    wind = np.linspace(4.0, 12.0 - 8.0 / 50, 50)[:, np.newaxis]
+    par = np.stack([wind, np.zeros((50, 1))], axis=-1).astype(np.float32)
+    pb.surface_brdf, pb.surface_params = "O", par
+    pb.surface_delx, pb.surface_dely = 0.02, 0.04
+    pb.wavelength = 0.85
+    return pb
+
+
 def brdf_wave_fresnel_problem():
     pb = brdf_l1_problem()
     wind = np.linspace(4.0, 12.0 - 8.0 / 50, 50)[:, np.newaxis]

@@ -1,9 +1,9 @@
-"""Generates tests/golden/brdf_{L,R,W,D}1.npz from the reference's golden files.
+"""Generates tests/golden/brdf_{L,R,W,D,O}1.npz from the reference's golden files.
 
 Reads the original-SHDOM outputs tests/data/brdf_X1f.out (fluxes) and
 tests/data/brdf_X1r.out (radiances) of the reference repository for the
-Lambertian (L), RPV (R), wave-Fresnel (W, polarized) and Diner (D,
-polarized) surfaces, parsed the way tests/test_shdom.py:17-27 parses them,
+Lambertian (L), RPV (R), wave-Fresnel (W, polarized), Diner (D,
+polarized) and 6S ocean (O) surfaces, parsed the way tests/test_shdom.py:17-27 parses them,
 and stores the numeric columns.
 Run once in a checkout that has the reference mounted:
 
@@ -26,7 +26,7 @@ def parse(path, comment="!"):
 
 def main(ref):
     d = os.path.join(ref, "tests", "data")
-    for kind in "LRWD":
+    for kind in "LRWDO":
         fl = parse(os.path.join(d, f"brdf_{kind}1f.out"))
         ra = parse(os.path.join(d, f"brdf_{kind}1r.out"))
         out = os.path.join(os.path.dirname(os.path.abspath(__file__)), f"brdf_{kind}1.npz")
