@@ -1363,10 +1363,39 @@ __device__ __noinline__ float ocean_reflection_d(float pws, float pcl, float pwl
   return rwc + (1 - w) * rog + (1 - rwc) * rwb;
 }
 
+// ROSS_THICK_LI_SPARSE (src/polarized/shdomsub2.f:1303-1355): the MODIS
+// kernel BRDF fiso + fvol K_vol + fgeo K_geo (RossThick volume kernel,
+// LiSparse geometric kernel with crown shape h/b = 2, b/r = 1), kernels in
+// double precision from single-precision cosines, clipped at zero.
+__device__ __noinline__ float ross_li_reflection_d(float fiso, float fgeo, float fvol, float hb, float br, float mud, float muu,
+                                float relaz) {
+  const double pi = acos(-1.0);
+  double coseta = (double)(mud * muu + sqrtf(1.0f - mud * mud) * sqrtf(1.0f - muu * muu) * cosf(relaz));
+  const float kvol = (float)((((pi / 2.0 - acos(coseta)) * coseta + sqrt(1.0 - coseta * coseta)) /
+                              (double)(mud + muu)) - pi / 4.0);
+  const double thd = fabs(atan(br * sqrt(1.0 - (double)(mud * mud)) / mud));
+  const double thu = fabs(atan(br * sqrt(1.0 - (double)(muu * muu)) / muu));
+  const double md = cos(thd), mu = cos(thu);
+  coseta = md * mu + sqrt(1.0 - md * md) * sqrt(1.0 - mu * mu) * cos((double)relaz);
+  const double secd = 1.0 / md, secu = 1.0 / mu;
+  const double tand = sqrt(1.0 - md * md) / md, tanu = sqrt(1.0 - mu * mu) / mu;
+  const double dsq = tand * tand + tanu * tanu - 2 * tanu * tand * cos((double)relaz);
+  const double tts = tand * tanu * sin((double)relaz);
+  double cost = hb * sqrt(dsq + tts * tts) / (secd + secu);
+  cost = fmin(1.0, fmax(-1.0, cost));
+  const double o = (acos(cost) - cost * sqrt(1.0 - cost * cost)) * (secd + secu) / pi;
+  const float kgeo = (float)(o - secd - secu + 0.5 * (1.0 + coseta) * secu * secd);
+  return fmaxf(fiso + fvol * kvol + fgeo * kgeo, 0.0f);
+}
+
 __device__ __forceinline__ void surface_brdf_d(int type, const float *par, float mu2, float phi2, float mu1, float phi1,
                                                float R[3][3]) {
   if (type == 'D') {
     diner_d(par[0], par[1], par[2], par[3], par[4], -mu1, mu2, phi2 - phi1, R);
+  } else if (type == 'M') {
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) R[i][j] = 0.f;
+    R[0][0] = ross_li_reflection_d(par[0], par[1], par[2], 2.0f, 1.0f, -mu1, mu2, phi1 - phi2);
   } else if (type == 'O') {  // par: wind speed, pigment, wavelength (appended by the plan)
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) R[i][j] = 0.f;

@@ -1397,13 +1397,14 @@ bool build_plan(const shdom_problem &p, Plan &P) {
   P.botpar.clear(); P.brdf_dn.clear(); P.brdf_up.clear();
   if (p.sfc_brdf) {
     const char bt = (char)p.sfc_brdf;
-    if ((bt != 'R' && bt != 'W' && bt != 'D' && bt != 'O') || p.nsfcpar < (bt == 'D' ? 5 : bt == 'O' ? 2 : 3) ||
+    if ((bt != 'R' && bt != 'W' && bt != 'D' && bt != 'O' && bt != 'M') || p.nsfcpar < (bt == 'D' ? 5 : bt == 'O' ? 2 : 3) ||
         !p.sfc_params || p.nxsfc < 1 || p.nysfc < 1) {
-      P.err = "surface BRDF: types 'R' (RPV), 'W' (wave-Fresnel; 3 parameters), 'D' (Diner; 5) and 'O' (ocean; 2) on a surface grid";
+      P.err = "surface BRDF: types 'R' (RPV), 'W' (wave-Fresnel), 'M' (Ross-Li; 3 parameters each), 'D' (Diner; 5) and 'O' (ocean; 2) on a surface grid";
       return false;
     }
     if (bt == 'R' && p.nstokes != 1) { P.err = "RPV BRDF is only for unpolarized case"; return false; }
     if (bt == 'O' && p.nstokes != 1) { P.err = "Ocean BRDF from 6S is only for unpolarized case"; return false; }
+    if (bt == 'M' && p.nstokes != 1) { P.err = "RossLiThick-Sparse is only for unpolarized case"; return false; }
     if (bt == 'O' && !(p.wavelen > 0.f)) { P.err = "the ocean BRDF needs the wavelength"; return false; }
     const int nxs = p.nxsfc, nys = p.nysfc, np_ = p.nsfcpar;
     // the ocean model also takes the wavelength: appended to every bottom

@@ -95,3 +95,17 @@ def ocean_unpolarized(surface_wind_speed, pigmentation, ground_temperature=298.1
     and the solver needs the wavelength."""
     par, dx, dy = _stack(surface_wind_speed, pigmentation, delx=delx, dely=dely)
     return BRDFSurface("O", par, float(ground_temperature), dx, dy)
+
+
+def ross_li_thick_sparse(f_iso, f_geo, f_vol, hb_ratio=2.0, br_ratio=1.0, ground_temperature=298.15, delx=None,
+                         dely=None) -> BRDFSurface:
+    """The MODIS RossThick-LiSparse kernel BRDF (at3d/surface.py
+    ross_li_thick_sparse; ROSS_THICK_LI_SPARSE): f_iso + f_vol K_vol +
+    f_geo K_geo, scalar problems only.  The reference's SURFACE_BRDF calls
+    the kernels with h/b = 2 and b/r = 1 whatever the ratios given, and so
+    does this one."""
+    if hb_ratio != 2.0 or br_ratio != 1.0:
+        import warnings
+        warnings.warn("the Ross-Li surface uses h/b = 2 and b/r = 1 (as the reference's SURFACE_BRDF)")
+    par, dx, dy = _stack(f_iso, f_geo, f_vol, delx=delx, dely=dely)
+    return BRDFSurface("M", par, float(ground_temperature), dx, dy)

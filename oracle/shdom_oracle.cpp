@@ -310,13 +310,14 @@ struct Solver {
     if (p.sfc_variable) sfcalb.assign(p.sfc_albedo, p.sfc_albedo + (size_t)p.nxsfc * p.nysfc);
     brdf = p.sfc_brdf; nsfcpar = p.nsfcpar;
     if (brdf) {
-      if ((brdf != 'R' && brdf != 'W' && brdf != 'D' && brdf != 'O') ||
+      if ((brdf != 'R' && brdf != 'W' && brdf != 'D' && brdf != 'O' && brdf != 'M') ||
           p.nsfcpar < (brdf == 'D' ? 5 : brdf == 'O' ? 2 : 3) || !p.sfc_params || p.nxsfc < 1 || p.nysfc < 1) {
-        err = "surface BRDF: types 'R' (RPV), 'W' (wave-Fresnel; 3 parameters), 'D' (Diner; 5) and 'O' (ocean; 2) on a surface grid";
+        err = "surface BRDF: types 'R' (RPV), 'W' (wave-Fresnel), 'M' (Ross-Li; 3 parameters each), 'D' (Diner; 5) and 'O' (ocean; 2) on a surface grid";
         return false;
       }
       if (brdf == 'R' && nst != 1) { err = "RPV BRDF is only for unpolarized case"; return false; }
       if (brdf == 'O' && nst != 1) { err = "Ocean BRDF from 6S is only for unpolarized case"; return false; }
+      if (brdf == 'M' && nst != 1) { err = "RossLiThick-Sparse is only for unpolarized case"; return false; }
       if (brdf == 'O' && !(p.wavelen > 0.f)) { err = "the ocean BRDF needs the wavelength"; return false; }
       sfcpar.assign(p.sfc_params, p.sfc_params + (size_t)p.nxsfc * p.nysfc * p.nsfcpar);
     }
@@ -1506,10 +1507,38 @@ struct Solver {
     return rwc + (1 - w) * rog + (1 - rwc) * rwb;
   }
 
+
+  // ROSS_THICK_LI_SPARSE (src/polarized/shdomsub2.f:1303-1355): the MODIS
+  // kernel BRDF fiso + fvol K_vol + fgeo K_geo (RossThick volume kernel,
+  // LiSparse geometric kernel with crown shape h/b = 2, b/r = 1), kernels in
+  // double precision from single-precision cosines, clipped at zero.
+  static float ross_li_reflection(float fiso, float fgeo, float fvol, float hb, float br, float mud, float muu,
+                                  float relaz) {
+    const double pi = std::acos(-1.0);
+    double coseta = (double)(mud * muu + std::sqrt(1.0f - mud * mud) * std::sqrt(1.0f - muu * muu) * std::cos(relaz));
+    const float kvol = (float)((((pi / 2.0 - std::acos(coseta)) * coseta + std::sqrt(1.0 - coseta * coseta)) /
+                                (double)(mud + muu)) - pi / 4.0);
+    const double thd = std::fabs(std::atan(br * std::sqrt(1.0 - (double)(mud * mud)) / mud));
+    const double thu = std::fabs(std::atan(br * std::sqrt(1.0 - (double)(muu * muu)) / muu));
+    const double md = std::cos(thd), mu = std::cos(thu);
+    coseta = md * mu + std::sqrt(1.0 - md * md) * std::sqrt(1.0 - mu * mu) * std::cos((double)relaz);
+    const double secd = 1.0 / md, secu = 1.0 / mu;
+    const double tand = std::sqrt(1.0 - md * md) / md, tanu = std::sqrt(1.0 - mu * mu) / mu;
+    const double dsq = tand * tand + tanu * tanu - 2 * tanu * tand * std::cos((double)relaz);
+    const double tts = tand * tanu * std::sin((double)relaz);
+    double cost = hb * std::sqrt(dsq + tts * tts) / (secd + secu);
+    cost = std::min(1.0, std::max(-1.0, cost));
+    const double o = (std::acos(cost) - cost * std::sqrt(1.0 - cost * cost)) * (secd + secu) / pi;
+    const float kgeo = (float)(o - secd - secu + 0.5 * (1.0 + coseta) * secu * secd);
+    return std::max(fiso + fvol * kvol + fgeo * kgeo, 0.0f);
+  }
+
   void surface_brdf(const R *par, float mu2, float phi2, float mu1, float phi1, double refl[3][3]) const {
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) refl[i][j] = 0.0;
-    if (brdf == 'O') {
+    if (brdf == 'M') {
+      refl[0][0] = ross_li_reflection((float)par[0], (float)par[1], (float)par[2], 2.0f, 1.0f, -mu1, mu2, phi1 - phi2);
+    } else if (brdf == 'O') {
       refl[0][0] = ocean_reflection((float)par[0], (float)par[1], p.wavelen, -mu1, mu2, phi1 - phi2, phi1);
     } else if (brdf == 'R') {
       refl[0][0] = rpv_reflection((float)par[0], (float)par[1], (float)par[2], -mu1, mu2,

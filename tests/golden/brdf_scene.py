@@ -196,3 +196,23 @@ def thermal_cloud_problem(srctype="T", num_stokes=1, boundary="open", isothermal
         pb.solarflux = 0.0
     pb.surface_albedo = 0.05
     return pb
+
+
+def brdf_ross_li_problem(lambertian_limit=False):
+    """The 50x1x11 Rayleigh scene over the MODIS Ross-Li kernel surface
+    ('M': fiso, fgeo, fvol).  lambertian_limit=True sets fgeo = fvol = 0
+    and fiso to the albedo ramp of Verify_Lambertian_Surfaces, which makes
+    the reflection the Lambertian one of the brdf_L1 golden scene."""
+    pb = brdf_l1_problem()
+    albedo = np.asarray(pb.surface_albedo, np.float32)
+    if lambertian_limit:
+        fgeo = fvol = np.zeros((50, 1), np.float32)
+        fiso = albedo
+    else:
+        fiso = np.full((50, 1), 0.12, np.float32)
+        fgeo = np.linspace(0.0, 0.04, 50)[:, None].astype(np.float32)
+        fvol = np.linspace(0.08, 0.0, 50)[:, None].astype(np.float32)
+    pb.surface_brdf = "M"
+    pb.surface_params = np.stack([fiso, fgeo, fvol], axis=-1).astype(np.float32)
+    pb.surface_albedo = 0.0
+    return pb

@@ -221,3 +221,25 @@ def test_gas_absorption_analytic(rte_cls):
     r.solve(100, verbose=False)
     rays, truth = gas_absorption_rays_and_truth()
     assert np.all(np.abs(r.render(*rays) - truth) <= 2e-7)
+
+
+@pytest.mark.parametrize("limit", [True, False], ids=["lambertian_limit", "kernels"])
+def test_ross_li_surface(rte_cls, limit):
+    """The MODIS Ross-Li surface: in its isotropic limit against the
+    Lambertian golden scene; with non-zero volume and geometric kernels
+    against the oracle (1e-4 relative RMS)."""
+    import os
+    from brdf_scene import brdf_ross_li_problem
+    pb = brdf_ross_li_problem(lambertian_limit=limit)
+    r = rte_cls.from_problem(pb)
+    r.solve(100, verbose=False)
+    rad = r.render(*brdf_l1_rays())
+    if limit:
+        g = np.load(os.path.join(os.path.dirname(__file__), "golden", "brdf_L1.npz"))
+        ref = g["radiances"][:, -1]
+        q = np.where(np.abs(ref) > 0, 0.5 * 10.0 ** (np.floor(np.log10(np.abs(np.where(ref != 0, ref, 1)))) - 4), 5e-7)
+        assert np.all(np.abs(rad - ref) <= 9e-6 + q)
+    else:
+        o = Oracle(pb)
+        o.solve(100)
+        assert relrms(rad, o.render(*brdf_l1_rays())) < 1e-4

@@ -102,3 +102,20 @@ def test_gas_absorption_analytic():
     o.solve(100)
     rays, truth = gas_absorption_rays_and_truth()
     assert np.all(np.abs(o.render(*rays) - truth) <= 2e-7)
+
+
+def test_ross_li_lambertian_limit():
+    """The Ross-Li surface with only the isotropic kernel (fiso = the albedo
+    ramp) reproduces the Lambertian golden scene: the BRDF reflection sum
+    over the downward ordinates is the Lambertian flux term."""
+    from brdf_scene import brdf_ross_li_problem
+    o = Oracle(brdf_ross_li_problem(lambertian_limit=True))
+    it, _ = o.solve(100)
+    assert it == 3
+    st = o.export()
+    bot = np.arange(50) * o.sizes["nz"]
+    for got, col in ((st["dirflux"][bot], 4), (st["fluxes"][bot, 0], 3), (st["fluxes"][bot, 1], 2)):
+        assert np.all(np.abs(got - GOLD["fluxes"][:, col]) <= 4e-6 + _quantum(GOLD["fluxes"][:, col]))
+    ref = GOLD["radiances"][:, -1]
+    assert np.all(np.abs(o.render(*brdf_l1_rays()) - ref) <= 9e-6 + _quantum(ref))
+
