@@ -397,6 +397,51 @@ def polarized_block(args, dev):
     return out
 
 
+def thermal_block(args, dev):
+    """Thermal emission (srctype 'T') on the headline grid: the 128x128x64
+    cloud field of wavelength 0 made an 11 um scene (cloud single-scattering
+    albedo scaled by 0.55, temperature 290 K at the ground falling 6.5 K/km
+    with a 4 K wave across x, 295 K ground of albedo 0.05, cold sky), one
+    full solve (initialisation to convergence) plus the 64x64x9 render,
+    timed with CUDA events after a warm-up solve, inputs resident."""
+    import torch
+    from at3d_gb300.scenes import cloud_field, orthographic_views
+    from at3d_gb300.solver import RTE
+    pb = cloud_field(seed=2, wavelength_index=0, nx=args.nx, ny=args.nx, nz=args.nz, boundary=args.boundary,
+                     solacc=args.solacc)
+    npx, npy, npz = pb.shape
+    pb.species[0].ssalb = (np.asarray(pb.species[0].ssalb, np.float32) * 0.55).astype(np.float32)
+    X, _, Z = np.meshgrid(np.arange(npx) * pb.delx, np.arange(npy) * pb.dely, pb.zlevels, indexing="ij")
+    pb.temperature = (290.0 - 6.5 * Z + 4.0 * np.sin(2 * np.pi * X / (npx * pb.delx))).astype(np.float32)
+    pb.srctype, pb.wavelength, pb.solarflux, pb.skyrad = "T", 11.0, 0.0, 0.0
+    pb.ground_temperature, pb.surface_albedo = 295.0, 0.05
+    rays = orthographic_views(pb, args.npix, args.npix)
+    nr = len(rays[0])
+    d = [torch.tensor(np.asarray(r), dtype=torch.float32 if i < 3 else torch.float64, device="cuda")
+         for i, r in enumerate(rays)]
+    img = torch.empty(nr, dtype=torch.float32, device="cuda")
+    r = RTE.from_problem(pb, device=dev)
+    ptrs = (d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), d[3].data_ptr(), d[4].data_ptr(), img.data_ptr())
+    r.solve(3, verbose=False)
+    r.render_device(*ptrs, nr, 0)
+    torch.cuda.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    e[0].record()
+    it, sc = r.solve(args.maxiter, verbose=False)
+    e[1].record()
+    r.render_device(*ptrs, nr, 0)
+    e[2].record()
+    torch.cuda.synchronize()
+    t_solve, t_render = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+    im = img.cpu().numpy()
+    r.close()
+    return {"workload": f"thermal 11 um, {npx}x{npy}x{npz} cloud field, NMU=16 NPHI=32, "
+                        f"{args.npix}x{args.npix} px x 9 views", "iterations": it, "solcrit": sc,
+            "ms_solve": t_solve, "ms_render": t_render, "solves_per_s": 1e3 / (t_solve + t_render),
+            "render_rays_per_s": nr / (t_render / 1e3), "mean_radiance": float(im.mean()),
+            "note": "no separate CPU baseline: the oracle's per-iteration cost is the headline cpu_baseline's"}
+
+
 def serving_block(args, dev):
     """A Poisson stream of mixed requests through the continuous-admission
     loop (at3d_gb300.serving): grids 32x32x24 to 128x128x64, NMU/NPHI 8/16
@@ -497,7 +542,7 @@ def main():
     ap.add_argument("--serve-rates", type=str, default="2", help="Poisson arrival rates (requests/s) to run")
     ap.add_argument("--serve-requests", type=int, default=16)
     ap.add_argument("--serve-slots", type=int, default=4)
-    ap.add_argument("--only", default="", choices=["", "precision", "gradient", "polarized", "serving"],
+    ap.add_argument("--only", default="", choices=["", "precision", "gradient", "polarized", "serving", "thermal"],
                     help="run one extra block alone and print its JSON (for profiling)")
     ap.add_argument("--pol-boundaries", type=str, default="periodic,open")
     args = ap.parse_args()
@@ -510,7 +555,7 @@ def main():
     if args.only:
         dev = int(os.environ.get("LOCAL_RANK", "0"))
         blk = {"precision": precision_block, "gradient": gradient_block, "polarized": polarized_block,
-               "serving": serving_block}[args.only]
+               "serving": serving_block, "thermal": thermal_block}[args.only]
         print(json.dumps({args.only: blk(args, dev)}))
         return
     if args.impl == "reference":
@@ -527,6 +572,7 @@ def main():
         extras["precision"] = precision_block(args, dev)
         extras["gradient"] = gradient_block(args, dev)
         extras["polarized"] = polarized_block(args, dev)
+        extras["thermal"] = thermal_block(args, dev)
         extras["serving"] = serving_block(args, dev)
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
