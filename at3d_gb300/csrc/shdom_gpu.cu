@@ -2536,7 +2536,7 @@ struct Handle {
   DBuf<int> nphi0, col_of;
   // medium
   DBuf<float> text, dirflux, coef, tms_w, phasetab, botalb, rad0;
-  DBuf<float> thermal, botplanck;  // thermal source only (empty for a solar source)
+  DBuf<float> thermal, botplanck, planckpt;  // thermal source only (empty for a solar source)
   DBuf<double> edp;      // delta-M scaled property-grid extinction (input of the direct beam)
   DBuf<uint8_t> nbscat;  // 1 where a cell containing the point has a scattering corner
   DBuf<int> wready;      // per hemisphere: the source pass has filled every item once
@@ -2875,7 +2875,7 @@ static long long plan_device_bytes(const Plan &P) {
   b += 4LL * 5 * P.nang + vbytes(P.cmu1) + vbytes(P.cmu2) + vbytes(P.cphi1) + vbytes(P.cphi2) + vbytes(P.ylmsun);
   b += vbytes(P.nphi0) + vbytes(P.col_of) + vbytes(P.total_ext) + 4LL * P.npts + vbytes(P.coef) + vbytes(P.tms_ptr);
   b += vbytes(P.tms_iph) + vbytes(P.tms_w) + vbytes(P.phasetab) + vbytes(P.botalb) + vbytes(P.rad0);
-  b += vbytes(P.thermal) + vbytes(P.botplanck);
+  b += vbytes(P.thermal) + vbytes(P.botplanck) + vbytes(P.planckpt);
   const long long ldo = (P.nang + 3) & ~3;
   b += 4LL * P.npts * (3LL * P.nst * P.nlm + 2 * ldo + 2 + 3) + 4LL * (long long)P.botp.size() + 64;
   if (P.nst == 3) b += vbytes(P.col_stk) + vbytes(P.coefp) + vbytes(P.phasetab2) + 8LL * P.nlm * 3 * P.nang;
@@ -3027,7 +3027,7 @@ static void upload_plan(Handle &H) {
   }
   H.tms_ptr.upload(P.tms_ptr); H.tms_iph.upload(P.tms_iph); H.tms_w.upload(P.tms_w);
   H.phasetab.upload(P.phasetab); H.botalb.upload(P.botalb); H.rad0.upload(P.rad0);
-  H.thermal.upload(P.thermal); H.botplanck.upload(P.botplanck);
+  H.thermal.upload(P.thermal); H.botplanck.upload(P.botplanck); H.planckpt.upload(P.planckpt);
   if (H.nst == 3) { H.col_stk.upload(P.col_stk); H.coefp.upload(P.coefp); H.phasetab2.upload(P.phasetab2); }
   if (P.brdf) {
     static_assert(sizeof(BrdfOrd) == sizeof(Plan::BrdfOrd), "BRDF ordinate records");
@@ -3744,6 +3744,7 @@ static void levis_adjoint_device(Handle &H, int nrays, const float *dx, const fl
   G.r = render_args(H, nrays, dx, dy, dz, dmu, dphi, nullptr);
   G.radiance = H.radiance.p; G.nr = H.nr.p; G.interpptr = H.g_interpptr.p; G.optinterpwt = H.g_optwt.p;
   G.dextm = H.g_dextm.p; G.dalbm = H.g_dalbm.p; G.dfj = H.g_dfj.p; G.alb_sp = H.g_albsp.p;
+  G.planck = H.planckpt.n ? H.planckpt.p : nullptr;
   G.sj_ptr = H.g_sjptr.p; G.sj_iph = H.g_sjiph.p; G.sj_w = H.g_sjw.p; G.legent_u = H.g_legu.p; G.legent_s = H.g_legs.p;
   G.fmix = H.g_fmix.p; G.scatterj = H.g_scatj.p; G.legenp_u = H.g_legp.p; G.extp = H.g_extp.p; G.albp = H.g_albp.p;
   G.piph = H.g_piph.p; G.pphw = H.g_pphw.p; G.adj = dadj; G.gradout = H.g_grad.p; G.beam = H.g_beam.p;
@@ -3774,7 +3775,6 @@ static int levis_host(shdom_handle *hh, int species, int nrays, const float *cam
   if (species < 0 || species >= P.npart) return fail(hh, "levis gradient: species index out of range");
   if (H.nst != 1) return fail(hh, "levis gradient: scalar (nstokes = 1) problems only");
   if (P.brdf) return fail(hh, "levis gradient: Lambertian surfaces only");
-  if (P.srct != 'S') return fail(hh, "levis gradient: solar sources only (as at3d.gradient)");
   if (P.ml + 1 > 32 || P.nlm > shdom::RNLM) return fail(hh, "levis gradient: at most 32 Legendre terms are supported");
   if (!H.initialized) return fail(hh, "levis gradient: the solution has not been initialized");
   if (H.grad_ipa != species) prepare_grad(H, species);

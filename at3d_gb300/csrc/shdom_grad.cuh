@@ -34,6 +34,7 @@ struct GradArgs {
   const int *nr;                           // radiance truncation per point
   const int *interpptr;                    // [npts][8] property point of each trilinear corner
   const float *optinterpwt;                // [npts][8]
+  const float *planck;                     // thermal source: [npts] B(T) of each point, else null
   const float *dextm;                      // [ng][2] delta-M scaled d(extinction)/d(unknown)
   const float *dalbm, *dfj;                // [npts][8][2]
   const float *alb_sp;                     // [npts] scaled albedo of the species
@@ -240,6 +241,10 @@ __device__ void levis_traverse(const GradArgs &G, int ray, const float *ydir, co
             const float DFJ = G.dfj[((size_t)ip * 8 + nb) * 2 + d];
             const float dsource = (DE * ap + DA * ep) * d1 + DFJ * d2;
             float v = xi * (sourcet * (albip * G.dextm[(size_t)ib * 2 + d] + G.dalbm[((size_t)ip * 8 + nb) * 2 + d]) + dsource);
+            // emission e (1 - albedo) B (src/polarized/shdomsub4.f:2009-2016), no temperature unknowns
+            if (G.planck)
+              v += xi * (G.planck[ip] * (1.f - albip) * G.dextm[(size_t)ib * 2 + d] -
+                         G.planck[ip] * G.dalbm[((size_t)ip * 8 + nb) * 2 + d]);
             if (a.deltam) v += dirf * secmu0 * xi * (singscatj * DFJ + DA * (ssp - singscatj) * ep + DE * (ssp - singscatj) * ap);
             if ((nb >> 1) == gl) g4[(nb & 1) * 2 + d] = v;
           }

@@ -715,12 +715,14 @@ bool build_medium(const shdom_problem &p, Plan &P) {
   // thermal source: PLANCK = (1 - albedo) B(T) per species after the delta-M
   // scaling (src/polarized/shdomsub2.f:574-580), mixed with the extinction
   // weights of COMPUTE_SOURCE (TOTAL_PLANCK, src/polarized/shdomsub1.f:1092-1139)
-  P.thermal.clear();
+  P.thermal.clear(); P.planckpt.clear();
   if (therm) {
     P.thermal.assign(npts, 0.f);
+    P.planckpt.assign(npts, 0.f);
     parallel_for(npts, [&](int b, int e) {
       for (int ipt = b; ipt < e; ++ipt) {
         const float bb = planck_fn(temp[ipt], P.unitc, p.wavelen, p.waveno);
+        P.planckpt[ipt] = bb;
         float tp = 0.f;
         for (int ipa = 0; ipa < npart; ++ipa) {
           const size_t o = (size_t)ipa * npts + ipt;

@@ -130,6 +130,7 @@ struct Plan {
   // botplanck B at the bottom points, skyrad_bc the top boundary radiance
   char srct = 'S', unitc = 'R';
   std::vector<float> thermal;                    // [npts]
+  std::vector<float> planckpt;                   // [npts] B(T) of each point (the gradient's emission term)
   std::vector<float> botplanck;                  // [nbot]
   float skyrad_bc = 0.f;
   // bidirectional surface ('R' RPV, 'W' wave-Fresnel; 0 Lambertian): its

@@ -2738,6 +2738,9 @@ struct Levis {
       for (int l = 0; l <= ml; ++l) legent[l] = legent[l] * ((R)1 - F) + F;
     std::vector<R> legenp(nl1), dlegt(nl1);
     const R albip = S.albedo[(size_t)ipa * npts + ip];
+    // thermal source: B(T) of the point for the emission term of the source
+    // derivative (src/polarized/shdomsub4.f:1792-1799, :2009-2016)
+    const R bpl = S.srct != 'S' ? (R)S.planck_fn(S.temp[ip]) : (R)0;
     for (int nb = 0; nb < 8; ++nb) {
       const int ib = interpptr[(size_t)ip * 8 + nb];
       const R xi = optinterpwt[(size_t)ip * 8 + nb];
@@ -2760,6 +2763,10 @@ struct Levis {
         }
         const R dsource = source_direction(dlegt.data(), ip, ylmdir, secmu0);
         R g = xi * (sourcet * (albip * dextm[(size_t)ib * NUMDER + idr] + dalbm[((size_t)ip * 8 + nb) * NUMDER + idr]) + dsource);
+        // emission e (1 - albedo) B: no temperature unknowns, so only the
+        // extinction and albedo derivatives enter
+        if (S.srct != 'S')
+          g += xi * (bpl * ((R)1 - albip) * dextm[(size_t)ib * NUMDER + idr] - bpl * dalbm[((size_t)ip * 8 + nb) * NUMDER + idr]);
         if (p.deltam)
           g += S.dirflux[ip] * secmu0 * xi *
                (singscatj * DFJ + DA * (singscatp - singscatj) * extp(ib) + DE * (singscatp - singscatj) * albp(ib));
@@ -3110,8 +3117,9 @@ bool frozen_render(Solver<R> &S, int ipa, int voxel, float dext, float dalb, int
   const int ng = S.p.npx * S.p.npy * S.p.npz;
   if (ipa < 0 || ipa >= S.npart || voxel < 0 || voxel >= ng) { S.err = "frozen_render: bad index"; return false; }
   if (S.nst != 1) { S.err = "frozen_render: scalar problems only"; return false; }
-  if (S.srct != 'S') { S.err = "frozen_render: solar sources only"; return false; }
   auto extp = S.extp, albp = S.albp;
+  auto planck_tot = S.planck_tot;
+  auto temp = S.temp;
   auto source = S.source;
   auto shptr = S.shptr;
   auto extinct = S.extinct, albedo = S.albedo, total_ext = S.total_ext, phaseinterpwt = S.phaseinterpwt;
@@ -3129,7 +3137,7 @@ bool frozen_render(Solver<R> &S, int ipa, int voxel, float dext, float dalb, int
   }
   S.extp = extp; S.albp = albp; S.source = source; S.shptr = shptr; S.extinct = extinct; S.albedo = albedo;
   S.total_ext = total_ext; S.phaseinterpwt = phaseinterpwt; S.iphase = iphase; S.dirflux = dirflux; S.legen = legen;
-  S.albmax = albmax;
+  S.albmax = albmax; S.planck_tot = planck_tot; S.temp = temp;
   return ok;
 }
 
@@ -3139,7 +3147,6 @@ bool levis_gradient(Solver<R> &S, int ipa, int n, const float *camx, const float
                     float *stokesout, int nthreads) {
   if (ipa < 0 || ipa >= S.npart) { S.err = "levis_gradient: bad species index"; return false; }
   if (S.nst != 1) { S.err = "levis_gradient: scalar problems only"; return false; }
-  if (S.srct != 'S') { S.err = "levis_gradient: solar sources only (as at3d.gradient)"; return false; }
   if (!S.render(n, camx, camy, camz, cammu, camphi, stokesout, nthreads)) return false;  // phase 1 (with phasetab, bcrad)
   Levis<R> L(S);
   if (!L.prepare(ipa, S.err)) return false;

@@ -216,3 +216,18 @@ def brdf_ross_li_problem(lambertian_limit=False):
     pb.surface_params = np.stack([fiso, fgeo, fvol], axis=-1).astype(np.float32)
     pb.surface_albedo = 0.0
     return pb
+
+
+def thermal_absorbing_blob():
+    """A 10x10x8 open-boundary cloud that only absorbs and emits (single-
+    scattering albedo 0) in a thin Rayleigh layer, 11 um, temperature
+    falling with height and varying across x, 295 K ground, cold sky: the
+    gradient case of a thermal source."""
+    from at3d_gb300.scenes import cloud_blob
+    pb = cloud_blob(seed=4, nx=10, ny=10, nz=8, dx=0.05, dz=0.1, boundary="open")
+    pb.species[0].ssalb = np.zeros_like(pb.species[0].extinction)
+    npx, npy, _ = pb.shape
+    X, _, Z = np.meshgrid(np.arange(npx) * pb.delx, np.arange(npy) * pb.dely, pb.zlevels, indexing="ij")
+    pb.temperature = (285.0 + 5 * np.cos(2 * np.pi * X / (npx * pb.delx)) - 6.0 * Z).astype(np.float32)
+    pb.srctype, pb.wavelength, pb.solarflux, pb.skyrad, pb.ground_temperature = "T", 11.0, 0.0, 0.0, 295.0
+    return pb

@@ -51,13 +51,33 @@ def test_thermal_cloud_fp32_matches_fp64():
     assert np.sqrt(np.mean((ra - rb) ** 2)) / np.sqrt(np.mean(rb ** 2)) < 1e-5
 
 
-def test_levis_gradient_refuses_thermal():
-    pb = thermal_cloud_problem("T")
-    o = Oracle(pb)
-    o.solve(3)
-    with pytest.raises(RuntimeError, match="solar sources only"):
-        o.levis_gradient(0, _views(pb), np.zeros(64, np.float32))
-
+def test_thermal_gradient_matches_frozen_field_differences():
+    """The emission term of the Levis source derivative
+    (src/polarized/shdomsub4.f:2009-2016): on a cloud that only absorbs and
+    emits, the gradient of the L2 cost with respect to the cloud's
+    extinction matches central differences of the frozen-field forward
+    model within 2% on the interior voxels that carry the most gradient
+    (measured: 0.05% to 0.7%)."""
+    from at3d_gb300.scenes import orthographic_views
+    from brdf_scene import thermal_absorbing_blob
+    pb = thermal_absorbing_blob()
+    o = Oracle(pb, fp64=True)
+    o.solve(100)
+    rays = orthographic_views(pb, 8, 8, zeniths=[0.0, 45.6, -60.0])
+    base = o.frozen_render(0, 0, 0.0, 0.0, rays)
+    meas = (base * (1 + 0.1 * np.random.default_rng(0).standard_normal(base.shape))).astype(np.float32)
+    grad, cost, stokes = o.levis_gradient(0, rays, meas, nthreads=4)
+    npx, npy, npz = pb.shape
+    ext = pb.species[0].extinction.ravel()
+    ix, iy = np.unravel_index(np.arange(npx * npy * npz), (npx, npy, npz))[:2]
+    interior = (ix > 0) & (ix < npx - 1) & (iy > 0) & (iy < npy - 1)
+    order = np.argsort(-np.abs(grad[:, 0]))
+    for v in [v for v in order if interior[v]][:4]:
+        h = 1e-3 * ext[v]
+        pp = o.frozen_render(0, int(v), h, 0.0, rays).astype(np.float64)
+        pm = o.frozen_render(0, int(v), -h, 0.0, rays).astype(np.float64)
+        fd = (0.5 * np.sum((pp - meas) ** 2) - 0.5 * np.sum((pm - meas) ** 2)) / (2 * h)
+        assert abs(grad[v, 0] / fd - 1) < 0.02, (v, grad[v, 0], fd)
 
 def planck_band_shdom(t, w1, w2):
     """Planck's law with SHDOM's constants integrated over [w1, w2] cm^-1
