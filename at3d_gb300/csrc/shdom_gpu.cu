@@ -3007,9 +3007,13 @@ static void upload_plan(Handle &H) {
     g.npts = P.npts; g.npx = P.prob.npx; g.npy = P.prob.npy; g.npz = P.prob.npz; g.bcflag = P.bcflag;
     g.ipflag = P.ipflag; g.delx = P.prob.delx; g.dely = P.prob.dely; g.solarmu = P.prob.solarmu;
     g.solaraz = P.prob.solaraz; g.solarflux = P.srct == 'T' ? 0.f : P.prob.solarflux;  // no beam for 'T'
-    k_direct_beam<<<(P.npts + 127) / 128, 128, 0, H.stream>>>(g);
-    CK(cudaGetLastError());
-    H.launches += 1;
+    if (P.srct == 'T') {
+      H.dirflux.zero(H.stream);  // a thermal source has no solar beam: skip the path integrals
+    } else {
+      k_direct_beam<<<(P.npts + 127) / 128, 128, 0, H.stream>>>(g);
+      CK(cudaGetLastError());
+      H.launches += 1;
+    }
   }
   {
     // scattering points (a non-zero coefficient row makes a non-zero source), spread to their cells' corners
