@@ -19,7 +19,8 @@ class ShdomSizes(C.Structure):
                 ("nlm", C.c_int), ("nmu", C.c_int), ("nang", C.c_int), ("ml", C.c_int), ("mm", C.c_int),
                 ("bcflag", C.c_int), ("ipflag", C.c_int), ("iters", C.c_int), ("nlevels_down", C.c_int),
                 ("nlevels_up", C.c_int), ("solcrit", C.c_float), ("albmax", C.c_float),
-                ("launches", C.c_longlong), ("device_bytes", C.c_longlong), ("nstokes", C.c_int)]
+                ("launches", C.c_longlong), ("device_bytes", C.c_longlong), ("nstokes", C.c_int),
+                ("march", C.c_int)]
 
 
 # name -> (restype, argtypes): the exported surface of include/shdom_gb300.h
@@ -37,10 +38,12 @@ SIGNATURES = {
     "shdom_sweep_timings": (C.c_int, [C.c_void_p, _f, _i]),
     "shdom_set_transform_mode": (C.c_int, [C.c_void_p, C.c_int]),
     "shdom_set_sweep_mode": (C.c_int, [C.c_void_p, C.c_int]),
+    "shdom_set_render_options": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "shdom_plan_summary": (C.c_int, [C.c_void_p, C.POINTER(ShdomSizes)]),
     "shdom_levis_gradient": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _f, _f, _f, _d, _d, _f, _d,
                                        C.POINTER(C.c_double), _f]),
     "shdom_levis_adjoint": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _f, _f, _f, _d, _d, _d, _d]),
+    "shdom_levis_adjoint_device": (C.c_int, [C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 8),
     "shdom_last_error": (C.c_char_p, [C.c_void_p]),
     "shdom_destroy": (None, [C.c_void_p]),
     "shdom_plan_create": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(ShdomSizes)]),

@@ -4,6 +4,7 @@ Single translation unit pair, one -gencode for sm_103a, no CMake.
 """
 from __future__ import annotations
 
+import glob
 import os
 import subprocess
 import sys
@@ -13,8 +14,8 @@ ROOT = os.path.dirname(HERE)
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libshdom_gb300.so")
 SOURCES = [os.path.join(HERE, "csrc", "shdom_gpu.cu"), os.path.join(HERE, "csrc", "shdom_plan.cpp")]
-HEADERS = [os.path.join(HERE, "csrc", "shdom_plan.h"), os.path.join(ROOT, "include", "shdom_gb300.h"),
-           os.path.join(ROOT, "include", "shdom_problem.h")]
+HEADERS = (sorted(glob.glob(os.path.join(HERE, "csrc", "*.h"))) + sorted(glob.glob(os.path.join(HERE, "csrc", "*.cuh")))
+           + sorted(glob.glob(os.path.join(ROOT, "include", "*.h"))))
 
 
 def nvcc():

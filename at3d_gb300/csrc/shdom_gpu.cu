@@ -226,7 +226,7 @@ struct SweepArgs {
   const IrrRec *irr;               // stored single-cell general traces of this hemisphere
   const uint8_t *stk;              // polarized: Stokes component per column (null: all I)
   int *err;
-  int npts, nang, ldo, is1d, nz, ny1;
+  int npts, nang, ldo, is1d, nz, ny1, nx1;
   float transmin;
   int oct_col0[8], oct_ncol[8];
 };
@@ -718,6 +718,168 @@ __global__ void __launch_bounds__(256) k_sweep_levels(SweepArgs a, const Seg *__
     __syncthreads();
     sweep_level(a, sg, ns, level_items[l], w, gtid, gstride);
     grid.sync();
+  }
+}
+
+// ------------------------------------------------------------ plane march
+// Phase 2 of a hemisphere whose (octant, face class) groups all march
+// (MarchGrp, planned on the host): each phase-2 point's regular trace stops
+// on a face in the previous plane along the group's class axis, so the
+// group's columns are swept plane by plane, every point of a plane
+// independent of the others.  One thread-block cluster per (group, column
+// slice): the cluster's CTAs split each plane into strips of rows along U.
+// A CTA keeps its strip's radiances of the previous and the current plane
+// in shared memory (two buffers, swapped every plane), reads the bordering
+// row of the upwind strip from that CTA's shared memory (distributed
+// shared memory), and the cluster meets at one cluster barrier per plane.
+// The source pass is fused: (radsrc, tr) of BACK_INT_GRID3D's cell
+// integral come from the ordinate source and extinction of the point and
+// of the face corners (the arithmetic of reg_trace).  DRAM sees one read of
+// the point's ordinate source (loaded one plane ahead) and one write of its
+// radiance per item; the corners' ordinate sources and extinctions were
+// read one plane earlier by the same SM and come from L1.
+struct MarchUnit {
+  int grp, c0, nc, tw;  // group, absolute columns [c0, c0+nc), rows per CTA
+};
+constexpr int MT = 256;  // threads per CTA
+constexpr int MK = 16;   // (row, v) pairs per thread at most
+
+__host__ __device__ inline size_t march_smem_bytes(int tw, int nv, int nc) {
+  return 2 * (size_t)tw * nv * nc * sizeof(float);
+}
+
+__global__ void __launch_bounds__(MT, 3) k_sweep_march(SweepArgs a, const MarchGrp *__restrict__ grps,
+                                                       const MarchUnit *__restrict__ units) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  const int cs = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+  const MarchUnit U = units[blockIdx.x / cs];
+  const MarchGrp G = grps[U.grp];
+  const int nc = U.nc, nV = G.nV, tw = U.tw, ldo = a.ldo;
+  const int u0 = rank * tw, nrow = max(0, min(tw, G.nU - u0));
+  extern __shared__ float mrad[];  // [2][tw][nV][nc]
+  const int plane_sz = tw * nV * nc;
+  // the strip on the upwind side along U and its row that borders this strip
+  const int nbr = rank + G.upu;
+  const bool has_nb = nbr >= 0 && nbr < cs && nbr * tw < G.nU;
+  const int nb_row = G.upu > 0 ? 0 : tw - 1;
+  const float *nb_rad = has_nb ? cl.map_shared_rank(mrad, nbr) : nullptr;
+  // thread -> column c and the strip's (row, v) pairs k0, k0 + tpc, ... (at most MK)
+  const int tpc = MT / nc, c = threadIdx.x % nc, k0 = threadIdx.x / nc;
+  const int col = U.c0 + c;
+  const bool clamp = !a.stk || !a.stk[col];
+  const bool pad = __ldg(a.col_cz + col) == 0.f;
+  const int kn = k0 < tpc ? max(0, (nrow * nV - k0 + tpc - 1) / tpc) : 0;
+  auto fixed_at = [&](int A, int u, int v) {
+    const int ix = G.cls == 0 ? A : u, iy = G.cls == 1 ? A : (G.cls == 0 ? u : v), iz = G.cls == 2 ? A : v;
+    return pad || iz == G.zfix || (G.xedge && (ix == 0 || ix == a.nx1 - 1)) ||
+           (G.yedge && (iy == 0 || iy == a.ny1 - 1));
+  };
+  auto rv_of = [&](int j, int &r, int &v) {
+    const int k = k0 + j * tpc;
+    r = k / nV; v = k - r * nV;
+  };
+  // plane 0 (the upwind boundary plane) is fixed: its radiances into buffer 0
+#pragma unroll 1
+  for (int j = 0; j < kn; ++j) {
+    int r, v;
+    rv_of(j, r, v);
+    const int p = G.a0 * G.sa + (u0 + r) * G.su + v * G.sv;
+    mrad[(r * nV + v) * nc + c] = __ldg(a.raddo + (size_t)p * ldo + col);
+  }
+  // the point's own ordinate source and extinction (or, at fixed points, its
+  // final radiance), loaded one plane ahead
+  float ps[MK], pe[MK];
+#pragma unroll
+  for (int j = 0; j < MK; ++j) {
+    ps[j] = 0.f; pe[j] = 0.f;
+    if (j < kn && G.nA > 1) {
+      int r, v;
+      rv_of(j, r, v);
+      const int A = G.a0 + G.da, u = u0 + r;
+      const int p = A * G.sa + u * G.su + v * G.sv;
+      if (fixed_at(A, u, v)) {
+        ps[j] = __ldg(a.raddo + (size_t)p * ldo + col);
+      } else {
+        ps[j] = __ldg(a.srcdo + (size_t)p * ldo + col);
+        pe[j] = __ldg(a.text + p);
+      }
+    }
+  }
+  cl.sync();
+  // corner offsets in the point index relative to the point itself in the previous plane
+  int qoff[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) qoff[k] = G.du[k] * G.su + G.dv[k] * G.sv;
+  for (int t = 1; t < G.nA; ++t) {
+    const int A = G.a0 + t * G.da, An = A + G.da;
+    const bool more = t + 1 < G.nA;
+    const float *prev = mrad + ((t - 1) & 1) * plane_sz;
+    float *cur = mrad + (t & 1) * plane_sz;
+    const float *nprev = has_nb ? nb_rad + ((t - 1) & 1) * plane_sz + nb_row * nV * nc : nullptr;
+    float4 gz = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (G.cls == 2 && kn > 0) {
+      const int layer = (G.b & 4) ? A - 1 : A;
+      gz = __ldg(reinterpret_cast<const float4 *>(a.geo) + (size_t)layer * a.nang + col);
+    }
+#pragma unroll
+    for (int j = 0; j < MK; ++j) {
+      if (j < kn) {
+        int r, v;
+        rv_of(j, r, v);
+        const int u = u0 + r;
+        const int p = A * G.sa + u * G.su + v * G.sv;
+        float rad;
+        if (fixed_at(A, u, v)) {
+          rad = ps[j];
+        } else {
+          const int pp = p - G.da * G.sa;  // same (u, v), previous plane
+          const float s1 = ps[j], e1 = pe[j];
+          float4 g = gz;
+          if (G.cls != 2) {
+            const int layer = (G.b & 4) ? v - 1 : v;
+            g = __ldg(reinterpret_cast<const float4 *>(a.geo) + (size_t)layer * a.nang + col);
+          }
+          const float fu = g.y, fv = g.z;
+          const float f[4] = {(1.f - fu) * (1.f - fv), (1.f - fu) * fv, fu * (1.f - fv), fu * fv};
+          float ext0 = 0.f, srcext0 = 0.f, rk[4];
+          bool ok = true;
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk) {
+            const int q = pp + qoff[kk];
+            const float e = __ldg(a.text + q), sk = __ldg(a.srcdo + (size_t)q * ldo + col);
+            const int lr = r + G.du[kk], lv = v + G.dv[kk];
+            const int lvc = min(max(lv, 0), nV - 1);
+            if (lr >= 0 && lr < nrow) {
+              rk[kk] = prev[(lr * nV + lvc) * nc + c];
+            } else {
+              ok = ok && has_nb;
+              rk[kk] = has_nb ? nprev[lvc * nc + c] : 0.f;
+            }
+            ok = ok && lv == lvc;
+            ext0 += f[kk] * e;
+            srcext0 += f[kk] * sk * e;
+          }
+          float radsrc, tr;
+          cell_source(ext0, srcext0, e1, e1 * s1, g.x, radsrc, tr, clamp);
+          rad = radsrc;
+          if (tr != 0.f) rad += tr * (f[0] * rk[0] + f[1] * rk[1] + f[2] * rk[2] + f[3] * rk[3]);
+          if (!ok) { atomicCAS(a.err, ERR_NONE, ERR_SWEEP_NOFACE); rad = 0.f; }
+          a.raddo[(size_t)p * ldo + col] = rad;
+        }
+        cur[(r * nV + v) * nc + c] = rad;
+        if (more) {  // this pair's values in the next plane
+          const int pn = An * G.sa + u * G.su + v * G.sv;
+          if (fixed_at(An, u, v)) {
+            ps[j] = __ldg(a.raddo + (size_t)pn * ldo + col);
+          } else {
+            ps[j] = __ldg(a.srcdo + (size_t)pn * ldo + col);
+            pe[j] = __ldg(a.text + pn);
+          }
+        }
+      }
+    }
+    cl.sync();  // plane t is in every strip's current buffer; the previous buffers are free
   }
 }
 
@@ -1785,6 +1947,9 @@ struct RenderArgs {
   float *out;
   int *err;
   int nrays, nx, ny, nz, nlm, nl, ml, mm, bcflag, ipflag, numphase, nscatangle, deltam;
+  // RENDER's SINGLESCATTER (the source is the exact single scatter of the
+  // direct beam only) and NOSURFACE (no boundary radiance is added)
+  int single_scatter = 0, nosurface = 0;
   float solarmu, solaraz, secmu0, skyrad;
   double tautol, transcut;
 };
@@ -1973,7 +2138,7 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
     for (int k = 0; k < 8; ++k) if (oldp[k] == mypt) reuse = k;
     float cval = 0.f, cext = a.text[mypt];
     const bool need = reuse < 0;
-    const int ns = need ? a.ns[mypt] : 0;
+    const int ns = (need && !a.single_scatter) ? a.ns[mypt] : 0;
     float s = 0.f;
     {
       const float *S = a.source + (size_t)mypt * a.nlm;
@@ -2103,7 +2268,8 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
       }
       float uu = (xs[1] - xs[0] > 0) ? (float)((xn - xs[0]) / (xs[1] - xs[0])) : 0.f;
       float vv = (ys[2] - ys[0] > 0) ? (float)((yn - ys[0]) / (ys[2] - ys[0])) : 0.f;
-      radacc += transmit * ((1 - uu) * (1 - vv) * rb[0] + uu * (1 - vv) * rb[1] + (1 - uu) * vv * rb[2] + uu * vv * rb[3]);
+      if (!a.nosurface)
+        radacc += transmit * ((1 - uu) * (1 - vv) * rb[0] + uu * (1 - vv) * rb[1] + (1 - uu) * vv * rb[2] + uu * vv * rb[3]);
     } else {
       cell = nxt;
     }
@@ -2268,7 +2434,7 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render_pol(RenderArgs a) {
     for (int k = 0; k < 8; ++k) if (oldp[k] == mypt) reuse = k;
     const float cext = a.text[mypt];
     const bool need = reuse < 0;
-    const int ns = need ? a.ns[mypt] : 0;
+    const int ns = (need && !a.single_scatter) ? a.ns[mypt] : 0;
     float sI = 0.f, sQ = 0.f, sU = 0.f;
     {
       const float *S = a.source + (size_t)mypt * 3 * nlm;
@@ -2416,9 +2582,10 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render_pol(RenderArgs a) {
       }
       float uu = (xs[1] - xs[0] > 0) ? (float)((xn - xs[0]) / (xs[1] - xs[0])) : 0.f;
       float vv = (ys[2] - ys[0] > 0) ? (float)((yn - ys[0]) / (ys[2] - ys[0])) : 0.f;
-      for (int c = 0; c < 3; ++c)
-        radacc[c] += transmit * ((1 - uu) * (1 - vv) * rb[c][0] + uu * (1 - vv) * rb[c][1] + (1 - uu) * vv * rb[c][2] +
-                                 uu * vv * rb[c][3]);
+      if (!a.nosurface)
+        for (int c = 0; c < 3; ++c)
+          radacc[c] += transmit * ((1 - uu) * (1 - vv) * rb[c][0] + uu * (1 - vv) * rb[c][1] + (1 - uu) * vv * rb[c][2] +
+                                   uu * vv * rb[c][3]);
     } else {
       cell = nxt;
     }
@@ -2516,6 +2683,7 @@ struct Handle {
       g_albp, g_pphw;
   DBuf<double> g_grad, g_beam, g_adj;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_caller[2] = {nullptr, nullptr};  // ordering against a caller's stream (device-buffer calls)
   int coop_blocks = 0;
   int nsm = 152;  // streaming multiprocessors of the handle's device
   // 0: cooperative persistent kernel when available; 1: one launch per level;
@@ -2561,6 +2729,15 @@ struct Handle {
   DBuf<float> tc_bh[2], tc_bl[2];
   CUtensorMap tm_a[2], tm_bh[2], tm_bl[2];
   bool seq[2] = {false, false};  // reference-order sweep engine per hemisphere
+  // plane-march phase 2 per hemisphere (k_sweep_march): units of (group,
+  // column slice), one cluster of mcs[h] CTAs each
+  bool march[2] = {false, false};
+  bool march_off = false;  // sweep mode 3: the level schedule even where the march applies
+  int render_single_scatter = 0, render_nosurface = 0;  // RENDER options of the following renders
+  DBuf<MarchGrp> mgrp[2];
+  DBuf<MarchUnit> munit[2];
+  int mnunits[2] = {0, 0}, mcs[2] = {0, 0};
+  size_t msmem[2] = {0, 0};
 
   bool initialized = false;
   int iters = 0;
@@ -2899,6 +3076,79 @@ static void fill_sizes(const Plan &P, shdom_sizes *o) {
   o->nlevels_up = (int)P.seg_off[1].size() - 1;
   o->device_bytes = plan_device_bytes(P);
   o->nstokes = P.nst;
+  o->march = (P.march[0].empty() ? 0 : 1) | (P.march[1].empty() ? 0 : 2);
+}
+
+// Units and cluster shape of the plane march of each hemisphere that has
+// one: 16-CTA clusters (8 where the device allows no larger), each group
+// split into column slices of roughly equal work so that there are about
+// two CTAs per SM.  A hemisphere whose units cannot be launched on this
+// device keeps the level schedule.
+static void setup_march(Handle &H) {
+  Plan &P = H.P;
+  int dev = 0, clus = 0, nsm = 0, maxsm = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&clus, cudaDevAttrClusterLaunch, dev));
+  CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  for (int h = 0; h < 2; ++h) {
+    H.march[h] = false;
+    if (P.march[h].empty() || H.seq[h] || !clus) continue;
+    for (int cs : {16, 8}) {
+      if (cs > 8 && cudaFuncSetAttribute(k_sweep_march, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+        cudaGetLastError();
+        continue;
+      }
+      // work of each group: planes x plane points x columns
+      double tot = 0;
+      for (const MarchGrp &g : P.march[h]) tot += (double)g.nA * g.nU * g.nV * g.ncol;
+      const int target_units = std::max(1, 2 * nsm / cs);
+      std::vector<MarchUnit> units;
+      size_t smem = 0;
+      for (size_t gi = 0; gi < P.march[h].size(); ++gi) {
+        const MarchGrp &g = P.march[h][gi];
+        const double w = (double)g.nA * g.nU * g.nV * g.ncol;
+        int nsl = std::max(1, (int)std::lround(target_units * w / tot));
+        nsl = std::min(nsl, g.ncol);
+        const int tw = (g.nU + cs - 1) / cs;
+        // every thread of a CTA takes one column and at most MK (row, v) pairs of
+        // its strip; a CTA's two radiance planes fit a third of an SM's shared memory
+        auto fits = [&](int nc) {
+          const int tpc = MT / nc;
+          return (tw * g.nV + tpc - 1) / tpc <= MK && march_smem_bytes(tw, g.nV, nc) <= 72 * 1024;
+        };
+        while (nsl < g.ncol && !fits((g.ncol + nsl - 1) / nsl)) ++nsl;
+        if (!fits((g.ncol + nsl - 1) / nsl)) { units.clear(); break; }
+        const int base = g.ncol / nsl, extra = g.ncol % nsl;
+        int c0 = g.col0;
+        for (int k = 0; k < nsl; ++k) {
+          const int nc = base + (k < extra ? 1 : 0);
+          units.push_back(MarchUnit{(int)gi, c0, nc, tw});
+          smem = std::max(smem, march_smem_bytes(tw, g.nV, nc));
+          c0 += nc;
+        }
+      }
+      if (units.empty()) continue;
+      CK(cudaFuncSetAttribute(k_sweep_march, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm));
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = cs; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3((unsigned)(units.size() * cs)); cfg.blockDim = dim3(MT); cfg.dynamicSmemBytes = smem;
+      cfg.attrs = at; cfg.numAttrs = 1;
+      int nclusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&nclusters, k_sweep_march, &cfg) != cudaSuccess || nclusters < 1) {
+        cudaGetLastError();
+        continue;
+      }
+      std::vector<MarchGrp> grps(P.march[h].begin(), P.march[h].end());
+      H.mgrp[h].upload(grps);
+      H.munit[h].upload(units);
+      H.mnunits[h] = (int)units.size(); H.mcs[h] = cs; H.msmem[h] = smem;
+      H.march[h] = true;
+      break;
+    }
+  }
 }
 
 static void upload_plan(Handle &H) {
@@ -3180,7 +3430,7 @@ static SweepArgs sweep_args(Handle &H, int hemi) {
   a.bnd = H.bnd.p; a.rank = H.rank.p; a.start = H.start.p; a.level = H.level.p; a.text = H.text.p;
   a.srcdo = H.srcdo.p; a.raddo = H.raddo.p; a.col_cx = H.col_cx.p; a.col_cy = H.col_cy.p; a.col_cz = H.col_cz.p;
   a.tasks = H.tasks[hemi].p; a.err = H.errflag.p; a.npts = P.npts; a.nang = P.nang; a.ldo = H.ldo; a.is1d = P.is1d;
-  a.regular = H.regular.p; a.geo = H.geo.p; a.nz = P.nz; a.ny1 = P.ny1;
+  a.regular = H.regular.p; a.geo = H.geo.p; a.nz = P.nz; a.ny1 = P.ny1; a.nx1 = P.nx1;
   a.transmin = P.prob.transmin;
   a.irr = H.irr[hemi].p;
   a.stk = H.nst == 3 ? H.col_stk.p : nullptr;
@@ -3212,7 +3462,9 @@ static void build_irr(Handle &H) {
     }
     for (int h = 0; h < 2; ++h) H.irr[h].view(G.irr[h]);
   }
-  H.sweepw.alloc((size_t)P.npts * H.ldo);
+  setup_march(H);
+  if ((!H.march[0] && !H.seq[0] && P.seg_off[0].size() > 1) || (!H.march[1] && !H.seq[1] && P.seg_off[1].size() > 1))
+    H.sweepw.alloc((size_t)P.npts * H.ldo);
   {  // phase 1 runs on a high-priority stream so its blocks start before the source pass fills the SMs
     int lo = 0, hi = 0;
     CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
@@ -3242,8 +3494,29 @@ static void sweep_hemisphere(Handle &H, int hemi) {
   }
   const std::vector<int> &off = P.seg_off[hemi];
   const int nlev = (int)off.size() - 1;
-  // phase 1 on the second stream, after everything queued so far
   const int ng1 = (int)P.p1off[hemi].size() - 1;
+  if (H.march[hemi] && !H.march_off) {
+    // phase 1 (the boundary-plane chains), then the plane march of phase 2
+    if (ng1 > 0) {
+      k_sweep_p1<<<ng1 * P1_SPLIT, P1_THREADS, 0, H.stream>>>(a, H.p1segs[hemi].p, H.p1off[hemi].p);
+      CK(cudaGetLastError());
+      H.launches += 1;
+    }
+    if (H.ktime_on) CK(cudaEventRecord(H.ev_k[hemi][1], H.stream));
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = H.mcs[hemi]; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)(H.mnunits[hemi] * H.mcs[hemi])); cfg.blockDim = dim3(MT);
+    cfg.dynamicSmemBytes = H.msmem[hemi]; cfg.stream = H.stream; cfg.attrs = at; cfg.numAttrs = 1;
+    const MarchGrp *gp = H.mgrp[hemi].p;
+    const MarchUnit *up = H.munit[hemi].p;
+    CK(cudaLaunchKernelEx(&cfg, k_sweep_march, a, gp, up));
+    H.launches += 1;
+    if (H.ktime_on) CK(cudaEventRecord(H.ev_k[hemi][2], H.stream));
+    return;
+  }
+  // phase 1 on the second stream, after everything queued so far
   if (ng1 > 0) {
     CK(cudaEventRecord(H.ev_fork, H.stream));
     CK(cudaStreamWaitEvent(H.stream2, H.ev_fork, 0));
@@ -3328,6 +3601,8 @@ struct shdom_handle {
     if (h.stream2) cudaStreamDestroy(h.stream2);
     if (h.ev_fork) cudaEventDestroy(h.ev_fork);
     if (h.ev_join) cudaEventDestroy(h.ev_join);
+    for (auto &e : h.ev_caller)
+      if (e) cudaEventDestroy(e);
     for (auto &hs : h.ev_k)
       for (auto &e : hs)
         if (e) cudaEventDestroy(e);
@@ -3344,6 +3619,29 @@ static int fail(shdom_handle *h, const std::string &m) {
   if (h) h->h.err = m; else g_static_err = m;
   return 1;
 }
+
+// Makes a handle's device current for the length of an entry point and puts
+// the caller's current device back afterwards, so that a handle created on
+// one device can be used from a thread whose current device is another.
+struct DevGuard {
+  int prev = -1;
+  explicit DevGuard(int dev) {
+    int cur = -1;
+    if (cudaGetDevice(&cur) == cudaSuccess && cur != dev && cudaSetDevice(dev) == cudaSuccess) prev = cur;
+  }
+  ~DevGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+// Device staging memory of one host-buffer call, freed on every return path.
+struct CallMem {
+  void *p = nullptr;
+  void alloc(size_t bytes) { CK(cudaMalloc(&p, bytes)); }
+  ~CallMem() {
+    if (p) cudaFree(p);
+  }
+};
 
 extern "C" {
 
@@ -3413,6 +3711,7 @@ void shdom_plan_destroy(shdom_plan *plan) { delete plan; }
 int shdom_init_solution(shdom_handle *hh) {
   if (!hh) return fail(nullptr, "null handle");
   Handle &H = hh->h;
+  DevGuard dg(H.device);
   try {
     shdom::Plan &P = H.P;
     size_t tot = (size_t)P.npts * H.nst * P.nlm;
@@ -3440,6 +3739,7 @@ int shdom_init_solution(shdom_handle *hh) {
 int shdom_solution_iterations(shdom_handle *hh, int maxiter, int *iters, float *solcrit) {
   if (!hh) return fail(nullptr, "null handle");
   Handle &H = hh->h;
+  DevGuard dg(H.device);
   if (!H.initialized) {
     int rc = shdom_init_solution(hh);
     if (rc) return rc;
@@ -3578,17 +3878,23 @@ static shdom::RenderArgs render_args(Handle &H, int nrays, const float *camx, co
   return a;
 }
 
+// Bottom-boundary radiance of the Lambertian surface from the solved fluxes
+// (what the render and the adjoint read at the ground).
+static void bcrad_update(Handle &H, cudaStream_t stream) {
+  const int nbot = (int)H.P.botp.size();
+  if (!nbot) return;
+  shdom::k_bcrad_bottom<<<(nbot + 127) / 128, 128, 0, stream>>>(H.botp.p, nbot, H.botalb.p, H.dirflux.p, H.fluxes.p,
+                                                                H.bcrad.p, H.botplanck.n ? H.botplanck.p : nullptr);
+  H.launches += 1;
+}
+
 static int render_impl(shdom_handle *hh, int nrays, const float *camx, const float *camy, const float *camz,
                        const double *cammu, const double *camphi, float *out, cudaStream_t stream) {
   Handle &H = hh->h;
   shdom::Plan &P = H.P;
-  int nbot = (int)P.botp.size();
-  if (nbot) {
-    shdom::k_bcrad_bottom<<<(nbot + 127) / 128, 128, 0, stream>>>(H.botp.p, nbot, H.botalb.p, H.dirflux.p, H.fluxes.p,
-                                                                  H.bcrad.p, H.botplanck.n ? H.botplanck.p : nullptr);
-    H.launches += 1;
-  }
+  bcrad_update(H, stream);
   shdom::RenderArgs a = render_args(H, nrays, camx, camy, camz, cammu, camphi, out);
+  a.single_scatter = H.render_single_scatter; a.nosurface = H.render_nosurface;
   if (P.nlm > shdom::RNLM || P.ml + 1 > 64) return fail(hh, "render: too many spherical-harmonic terms");
   int blocks = (nrays + shdom::RWARPS - 1) / shdom::RWARPS;
   if (blocks > 0) {
@@ -3768,12 +4074,9 @@ static void levis_adjoint_device(Handle &H, int nrays, const float *dx, const fl
   H.launches += 2;
 }
 
-// Host-buffer form of the gradient: measurements given -> L2 cost and its
-// adjoint weights (COMPUTE_ADJOINT_WEIGHTS, unit uncertainty); otherwise
-// the caller's weights.
-static int levis_host(shdom_handle *hh, int species, int nrays, const float *camx, const float *camy,
-                      const float *camz, const double *cammu, const double *camphi, const float *meas,
-                      const double *weights, double *gradient, double *cost, float *stokes_out) {
+// Checks shared by the gradient entry points; builds the derivative tables
+// of the species on its first use.
+static int levis_ready(shdom_handle *hh, int species) {
   Handle &H = hh->h;
   shdom::Plan &P = H.P;
   if (species < 0 || species >= P.npart) return fail(hh, "levis gradient: species index out of range");
@@ -3782,10 +4085,23 @@ static int levis_host(shdom_handle *hh, int species, int nrays, const float *cam
   if (P.ml + 1 > 32 || P.nlm > shdom::RNLM) return fail(hh, "levis gradient: at most 32 Legendre terms are supported");
   if (!H.initialized) return fail(hh, "levis gradient: the solution has not been initialized");
   if (H.grad_ipa != species) prepare_grad(H, species);
+  return 0;
+}
+
+// Host-buffer form of the gradient: measurements given -> L2 cost and its
+// adjoint weights (COMPUTE_ADJOINT_WEIGHTS, unit uncertainty); otherwise
+// the caller's weights.
+static int levis_host(shdom_handle *hh, int species, int nrays, const float *camx, const float *camy,
+                      const float *camz, const double *cammu, const double *camphi, const float *meas,
+                      const double *weights, double *gradient, double *cost, float *stokes_out) {
+  Handle &H = hh->h;
+  shdom::Plan &P = H.P;
+  if (int rc = levis_ready(hh, species)) return rc;
   const int ng = P.npx * P.npy * P.npz;
-  float *d;
+  CallMem mem;
   const size_t fb = (size_t)nrays * sizeof(float), db = (size_t)nrays * sizeof(double);
-  CK(cudaMalloc(&d, 4 * fb + 3 * db));
+  mem.alloc(4 * fb + 3 * db);
+  float *d = (float *)mem.p;
   float *dx = d, *dy = d + nrays, *dz = d + 2 * (size_t)nrays, *dout = d + 3 * (size_t)nrays;
   double *dmu = (double *)(d + 4 * (size_t)nrays), *dphi = dmu + nrays, *dadj = dphi + nrays;
   int rc = 0;
@@ -3817,7 +4133,6 @@ static int levis_host(shdom_handle *hh, int species, int nrays, const float *cam
     CK(cudaMemcpyAsync(gradient, H.g_grad.p, (size_t)ng * 2 * sizeof(double), cudaMemcpyDeviceToHost, H.stream));
   }
   CK(cudaStreamSynchronize(H.stream));
-  cudaFree(d);
   if (rc) return rc;
   if (shdom::check_device_error(H)) return 1;
   return 0;
@@ -3826,6 +4141,7 @@ static int levis_host(shdom_handle *hh, int species, int nrays, const float *cam
 int shdom_render_device(shdom_handle *hh, int nrays, const float *camx, const float *camy, const float *camz,
                         const double *cammu, const double *camphi, float *stokes_out, void *stream) {
   if (!hh) return fail(nullptr, "null handle");
+  DevGuard dg(hh->h.device);
   try {
     return render_impl(hh, nrays, camx, camy, camz, cammu, camphi, stokes_out, (cudaStream_t)stream);
   } catch (const std::exception &e) {
@@ -3838,10 +4154,12 @@ int shdom_render(shdom_handle *hh, int nrays, const float *camx, const float *ca
   if (!hh) return fail(nullptr, "null handle");
   Handle &H = hh->h;
   if (nrays <= 0) return 0;
+  DevGuard dg(H.device);
   try {
-    float *d;
+    CallMem mem;
     size_t fb = (size_t)nrays * sizeof(float), db = (size_t)nrays * sizeof(double);
-    CK(cudaMalloc(&d, 3 * fb + 2 * db + fb * H.nst));
+    mem.alloc(3 * fb + 2 * db + fb * H.nst);
+    float *d = (float *)mem.p;
     // the double arrays first: every array starts on its own element size for any nrays
     double *dmu = (double *)d, *dphi = dmu + nrays;
     float *dx = (float *)(dphi + nrays), *dy = dx + nrays, *dz = dy + nrays, *dout = dz + nrays;
@@ -3853,7 +4171,6 @@ int shdom_render(shdom_handle *hh, int nrays, const float *camx, const float *ca
     int rc = render_impl(hh, nrays, dx, dy, dz, dmu, dphi, dout, H.stream);
     if (!rc) CK(cudaMemcpyAsync(stokes_out, dout, fb * H.nst, cudaMemcpyDeviceToHost, H.stream));
     CK(cudaStreamSynchronize(H.stream));
-    cudaFree(d);
     if (rc) return rc;
     if (shdom::check_device_error(H)) return 1;
   } catch (const std::exception &e) {
@@ -3867,6 +4184,7 @@ int shdom_levis_gradient(shdom_handle *hh, int species, int nrays, const float *
                          double *gradient, double *cost, float *stokes_out) {
   if (!hh) return fail(nullptr, "null handle");
   if (nrays <= 0 || !measurements || !gradient) return fail(hh, "shdom_levis_gradient: bad arguments");
+  DevGuard dg(hh->h.device);
   try {
     return levis_host(hh, species, nrays, camx, camy, camz, cammu, camphi, measurements, nullptr, gradient, cost,
                       stokes_out);
@@ -3880,12 +4198,43 @@ int shdom_levis_adjoint(shdom_handle *hh, int species, int nrays, const float *c
                         double *gradient) {
   if (!hh) return fail(nullptr, "null handle");
   if (nrays <= 0 || !weights || !gradient) return fail(hh, "shdom_levis_adjoint: bad arguments");
+  DevGuard dg(hh->h.device);
   try {
     return levis_host(hh, species, nrays, camx, camy, camz, cammu, camphi, nullptr, weights, gradient, nullptr,
                       nullptr);
   } catch (const std::exception &e) {
     return fail(hh, e.what());
   }
+}
+
+int shdom_levis_adjoint_device(shdom_handle *hh, int species, int nrays, const float *camx, const float *camy,
+                               const float *camz, const double *cammu, const double *camphi, const double *weights,
+                               double *gradient, void *stream) {
+  if (!hh) return fail(nullptr, "null handle");
+  if (nrays <= 0 || !camx || !camy || !camz || !cammu || !camphi || !weights || !gradient)
+    return fail(hh, "shdom_levis_adjoint_device: bad arguments");
+  Handle &H = hh->h;
+  DevGuard dg(H.device);
+  try {
+    if (int rc = levis_ready(hh, species)) return rc;
+    const cudaStream_t cs = (cudaStream_t)stream;
+    for (auto &e : H.ev_caller)
+      if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    // the caller's stream has produced the rays and weights: the handle's stream waits for it
+    CK(cudaEventRecord(H.ev_caller[0], cs));
+    CK(cudaStreamWaitEvent(H.stream, H.ev_caller[0], 0));
+    bcrad_update(H, H.stream);
+    levis_adjoint_device(H, nrays, camx, camy, camz, cammu, camphi, weights);
+    const shdom::Plan &P = H.P;
+    CK(cudaMemcpyAsync(gradient, H.g_grad.p, (size_t)P.npx * P.npy * P.npz * 2 * sizeof(double),
+                       cudaMemcpyDeviceToDevice, H.stream));
+    // and the caller's stream waits for the gradient
+    CK(cudaEventRecord(H.ev_caller[1], H.stream));
+    CK(cudaStreamWaitEvent(cs, H.ev_caller[1], 0));
+  } catch (const std::exception &e) {
+    return fail(hh, e.what());
+  }
+  return 0;
 }
 
 }  // extern "C"
@@ -3904,12 +4253,14 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 static std::mutex g_noalloc_mu;
 static void *g_noalloc_ptr[64] = {nullptr};
 
-// Address of the scratch array on the current device (set up on first use).
-static void *noalloc_scratch(std::string &err) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) { err = std::string("cudaGetDevice: ") + cudaGetErrorString(e); return nullptr; }
+// Address of the scratch array on device `dev`, which must be the current
+// device (set up on first use on that device).
+static void *noalloc_scratch(int dev, std::string &err) {
   if (dev < 0 || dev >= 64) { err = "shdom_render_noalloc: device index out of range"; return nullptr; }
+  int cur = -1;
+  cudaError_t e = cudaGetDevice(&cur);
+  if (e != cudaSuccess) { err = std::string("cudaGetDevice: ") + cudaGetErrorString(e); return nullptr; }
+  if (cur != dev) { err = "shdom_render_noalloc: the handle's device is not the current device"; return nullptr; }
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
   if (!g_noalloc_ptr[dev]) {
     void *p = nullptr;
@@ -3935,9 +4286,11 @@ int shdom_render_noalloc(shdom_handle *hh, int nrays, const float *camx, const f
                         " rays per call (got " + std::to_string(nrays) + ")");
   if (!camx || !camy || !camz || !cammu || !camphi || !stokes_out) return fail(hh, "shdom_render_noalloc: null argument");
   if (H.nst != 1) return fail(hh, "shdom_render_noalloc: scalar (nstokes = 1) problems only");
+  // the handle's device is made current, so the staging array is the one on that device
+  DevGuard dg(H.device);
   try {
     std::string err;
-    void *base = noalloc_scratch(err);
+    void *base = noalloc_scratch(H.device, err);
     if (!base) return fail(hh, err);
     const size_t n = (size_t)nrays, cap = (size_t)shdom::kNoAllocMaxRays;
     double *dmu = (double *)base, *dphi = dmu + cap;
@@ -3964,6 +4317,7 @@ int shdom_export_state(shdom_handle *hh, float *source, int *ns, float *radiance
                        float *dirflux) {
   if (!hh) return fail(nullptr, "null handle");
   Handle &H = hh->h;
+  DevGuard dg(H.device);
   shdom::Plan &P = H.P;
   try {
     CK(cudaStreamSynchronize(H.stream));
@@ -3982,8 +4336,32 @@ int shdom_export_state(shdom_handle *hh, float *source, int *ns, float *radiance
 
 int shdom_set_sweep_mode(shdom_handle *hh, int mode) {
   if (!hh) return fail(nullptr, "null handle");
-  if (mode < 0 || mode > 2) return fail(hh, "shdom_set_sweep_mode: mode must be 0, 1 or 2");
-  hh->h.sweep_mode = mode;
+  if (mode < 0 || mode > 3) return fail(hh, "shdom_set_sweep_mode: mode must be 0, 1, 2 or 3");
+  Handle &H = hh->h;
+  DevGuard dg(H.device);
+  try {
+    const bool levels_only = mode == 3;
+    if (levels_only != H.march_off) {
+      H.march_off = levels_only;
+      // the level schedule's source pass needs its (radsrc, tr) table
+      if (levels_only && !H.sweepw.p && (H.march[0] || H.march[1])) {
+        CK(cudaStreamSynchronize(H.stream));
+        H.sweepw.alloc((size_t)H.P.npts * H.ldo);
+      }
+      for (auto &g : H.iter_graph)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    }
+    H.sweep_mode = levels_only ? 0 : mode;
+  } catch (const std::exception &e) {
+    return fail(hh, e.what());
+  }
+  return 0;
+}
+
+int shdom_set_render_options(shdom_handle *hh, int single_scatter, int nosurface) {
+  if (!hh) return fail(nullptr, "null handle");
+  hh->h.render_single_scatter = single_scatter ? 1 : 0;
+  hh->h.render_nosurface = nosurface ? 1 : 0;
   return 0;
 }
 
@@ -3999,6 +4377,7 @@ int shdom_get_sizes(shdom_handle *hh, shdom_sizes *o) {
   shdom::fill_sizes(hh->h.P, o);
   o->iters = hh->h.iters; o->solcrit = hh->h.solcrit;
   o->launches = hh->h.launches;
+  o->march = hh->h.march_off ? 0 : ((hh->h.march[0] ? 1 : 0) | (hh->h.march[1] ? 2 : 0));
   return 0;
 }
 
@@ -4033,6 +4412,10 @@ int shdom_sweep_timings(shdom_handle *hh, float *ms2, int *launches2) {
 
 const char *shdom_last_error(shdom_handle *hh) { return hh ? hh->h.err.c_str() : g_static_err.c_str(); }
 
-void shdom_destroy(shdom_handle *hh) { delete hh; }
+void shdom_destroy(shdom_handle *hh) {
+  if (!hh) return;
+  DevGuard dg(hh->h.device);
+  delete hh;
+}
 
 }  // extern "C"

@@ -267,27 +267,30 @@ __device__ void levis_traverse(const GradArgs &G, int ray, const float *ydir, co
     const int ip1 = g[0], ip2 = g[7];
     const float *P1 = a.gridpos + 3 * ip1, *P2 = a.gridpos + 3 * ip2;
     const float delx = P2[0] - P1[0], dely = P2[1] - P1[1], delz = P2[2] - P1[2];
-    const float idx = delx <= 0.f ? 1.f : 1.f / delx, idy = dely <= 0.f ? 1.f : 1.f / dely, idz = 1.f / delz;
-    // Positions and path lengths stay in FP64 (as the reference's); the
-    // trilinear weights come from cell-relative coordinates in [0, 1] in
-    // FP32, and so do the interpolated extinction and source (GB300's FP64
-    // rate is a small fraction of FP32's).  The integrals, the future
-    // radiance and the gradient accumulations stay in FP64.
-    const float u0 = (float)(xe - P1[0]) * idx, v0 = (float)(ye - P1[1]) * idy, w0c = (float)(ze - P1[2]) * idz;
-    const float du = (float)cx * idx, dv = (float)cy * idy, dw = (float)cz * idz;
-    auto kernel8 = [&](float s, float fc[8]) {
-      const float u = fmaf(s, du, u0), v = fmaf(s, dv, v0), w = fmaf(s, dw, w0c);
+    const double idx = delx <= 0.f ? 1.0 : 1.0 / delx, idy = dely <= 0.f ? 1.0 : 1.0 / dely, idz = 1.0 / delz;
+    // Positions, path lengths and the trilinear weights are FP64, as in
+    // ADJOINT_INTEGRATE_1RAY; the interpolated extinction and source are
+    // single precision sums of FP64 products.  The weight terms of the
+    // gradient divide by the interpolated extinction, which cancels to
+    // nearly zero beside clouds and in the extrapolating open-boundary edge
+    // cells, so FP32 weights (relative error 1e-7 of terms of size 50/km)
+    // would not do there.
+    auto kernel8 = [&](double s, double fc[8]) {
+      const double u = (xe + s * cx - P1[0]) * idx, v = (ye + s * cy - P1[1]) * idy, w = (ze + s * cz - P1[2]) * idz;
       fc[0] = (1 - w) * (1 - v) * (1 - u); fc[1] = (1 - w) * (1 - v) * u; fc[2] = (1 - w) * v * (1 - u); fc[3] = (1 - w) * v * u;
       fc[4] = w * (1 - v) * (1 - u); fc[5] = w * (1 - v) * u; fc[6] = w * v * (1 - u); fc[7] = w * v * u;
     };
-    float fc1[8], fc0[8];
-    kernel8(0.f, fc1);
-    float srcext1 = 0.f, ext1 = 0.f;
+    // sum_k fc[k] val[k], each step rounded to single precision
+    auto interp = [](const double fc[8], const float val[8]) {
+      float acc = 0.f;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) srcext1 = fmaf(fc1[k], src8[k], srcext1);
-    srcext1 = fmaxf(0.f, srcext1);
-#pragma unroll
-    for (int k = 0; k < 8; ++k) ext1 = fmaf(fc1[k], ext8[k], ext1);
+      for (int k = 0; k < 8; ++k) acc = (float)((double)acc + fc[k] * (double)val[k]);
+      return acc;
+    };
+    double fc1[8], fc0[8];
+    kernel8(0.0, fc1);
+    float srcext1 = fmaxf(0.f, interp(fc1, src8));
+    float ext1 = interp(fc1, ext8);
     const int cf = a.cellflags[cell];
     const bool ipinx = (cf & 1) && !((a.bcflag & 1) && ((cx > 0 && xe < xm) || (cx < 0 && xe > xm)));
     const bool ipiny = (cf & 2) && !((a.bcflag & 2) && ((cy > 0 && ye < ym) || (cy < 0 && ye > ym)));
@@ -298,27 +301,18 @@ __device__ void levis_traverse(const GradArgs &G, int ray, const float *ydir, co
     const double so = fmin(sox, fmin(soy, soz));
     if (so < -eps) { if (lane == 0) atomicCAS(a.err, ERR_NONE, ERR_RAY_SO); break; }
     double xn = xe + so * cx, yn = ye + so * cy, zn = ze + so * cz;
-    float fcn[8];
-    kernel8((float)so, fcn);
-    float extn = 0.f;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) extn = fmaf(fcn[k], ext8[k], extn);
+    double fcn[8];
+    kernel8(so, fcn);
+    const float extn = interp(fcn, ext8);
     const double taugrid = so * 0.5 * (ext1 + extn);
     const int ntau = max(1, 1 + (int)(taugrid / a.tautol));
     const double dels = so / ntau;
     double accG = 0.0, accS = 0.0, accR = 0.0;  // per-cell weights of this lane's corner
     const float ss8 = myss * myext;                // this corner's single scatter x extinction
     for (int it = 1; it <= ntau; ++it) {
-      kernel8((float)(it * dels), fc0);
-      float srcext0 = 0.f, ext0 = 0.f;
-#pragma unroll
-      for (int k = 0; k < 8; ++k) srcext0 = fmaf(fc0[k], src8[k], srcext0);
-      if (it != ntau) {
-#pragma unroll
-        for (int k = 0; k < 8; ++k) ext0 = fmaf(fc0[k], ext8[k], ext0);
-      } else {
-        ext0 = extn;
-      }
+      kernel8(it * dels, fc0);
+      float srcext0 = interp(fc0, src8);
+      const float ext0 = it != ntau ? interp(fc0, ext8) : extn;
       srcext0 = fmaxf(0.f, srcext0);
       const double ext = 0.5 * ((double)ext0 + (double)ext1);
       double transcell;
@@ -343,10 +337,9 @@ __device__ void levis_traverse(const GradArgs &G, int ray, const float *ydir, co
           const double pr1 = (rtot - cumf) / transmit;
           const double tnext = transmit * transcell;
           const double pr0 = (rtot - cumf - fn) / tnext;
-          float e0f = 0.f, e1f = 0.f;
+          double e0 = 0.0, e1 = 0.0;  // (COMPUTE_RADIANCE_DERIVATIVE_ADJOINT sums these in double)
 #pragma unroll
-          for (int k = 0; k < 8; ++k) { e0f = fmaf(ext8[k], fc0[k], e0f); e1f = fmaf(ext8[k], fc1[k], e1f); }
-          const double e0 = e0f, e1 = e1f;
+          for (int k = 0; k < 8; ++k) { e0 += (double)ext8[k] * fc0[k]; e1 += (double)ext8[k] * fc1[k]; }
           const double eavg = 0.5 * (e0 + e1);
           if (eavg != 0.0) {
             const double gb0 = -adj * pr0 * w0, gb1 = -adj * pr1 * w1;

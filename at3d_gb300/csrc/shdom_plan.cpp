@@ -1277,6 +1277,62 @@ void expand_stokes(Plan &P) {
   }
 }
 
+// Plane-march groups of each hemisphere (see MarchGrp).  A hemisphere
+// marches when every one of its (octant, class) groups has a face class
+// x, y or z, no general-trace phase-2 point, and exactly the points the
+// kernel treats as fixed (the hemisphere's preset boundary layer and, on
+// open boundaries, the edge planes) are not phase-2 points.  Runs on the
+// scalar column layout's kind table, so it does not depend on the Stokes
+// expansion; the groups' columns are set after it.
+void build_march(Plan &P) {
+  const int n = P.npts;
+  const int stride[3] = {P.ny1 * P.nz, P.nz, 1}, cnt[3] = {P.nx1, P.ny1, P.nz};
+  const bool xopen = (P.bcflag & 1) != 0, yopen = (P.bcflag & 2) != 0;
+  for (int h = 0; h < 2; ++h) {
+    P.march[h].clear();
+    if (P.is1d || P.deep[h] || P.segs[h].empty()) continue;
+    std::vector<MarchGrp> out;
+    bool ok = true;
+    for (int b = 0; b < 8 && ok; ++b) {
+      if (((b >> 2) & 1) != h) continue;
+      for (int cls = 0; cls < 4 && ok; ++cls) {
+        if (P.cls_ncol[b][cls] == 0) continue;
+        if (cls == 3) { ok = false; break; }
+        MarchGrp g{};
+        g.b = b; g.cls = cls; g.col0 = P.cls_col0[b][cls]; g.ncol = P.cls_ncol[b][cls];
+        const int ia = cls, iu = cls == 0 ? 1 : 0, iv = cls == 2 ? 1 : 2;
+        g.nA = cnt[ia]; g.nU = cnt[iu]; g.nV = cnt[iv];
+        g.sa = stride[ia]; g.su = stride[iu]; g.sv = stride[iv];
+        const int sA = ((b >> ia) & 1) ? -1 : 1;  // the stopping face lies at a + sA
+        g.da = -sA;
+        g.a0 = sA > 0 ? g.nA - 1 : 0;
+        const int iface = 2 * cls + 1 - ((b >> cls) & 1);
+        for (int k = 0; k < 4; ++k) {
+          const int d = kFace[iface][k] ^ b;
+          g.du[k] = ((d >> iu) & 1) ? ((((b >> iu) & 1) ? -1 : 1)) : 0;
+          g.dv[k] = ((d >> iv) & 1) ? ((((b >> iv) & 1) ? -1 : 1)) : 0;
+        }
+        g.upu = ((b >> iu) & 1) ? -1 : 1;
+        g.zfix = h == 0 ? P.nz - 1 : 0;
+        g.xedge = xopen ? 1 : 0; g.yedge = yopen ? 1 : 0;
+        const uint8_t *kd = &P.kind[((size_t)b * 4 + cls) * n];
+        for (int p = 0; p < n && ok; ++p) {
+          const int ix = p / (P.ny1 * P.nz), iy = (p / P.nz) % P.ny1, iz = p % P.nz;
+          const bool fixed = iz == g.zfix || (xopen && (ix == 0 || ix == P.nx1 - 1)) ||
+                             (yopen && (iy == 0 || iy == P.ny1 - 1));
+          const int ic[3] = {ix, iy, iz};
+          // fixed points are exactly the non-phase-2 ones; phase-2 points are
+          // regular and never lie in the first plane of the march
+          if (fixed ? (kd[p] == 1 || kd[p] == 2) : (kd[p] != 1)) ok = false;
+          if (!fixed && ic[ia] == g.a0) ok = false;
+        }
+        out.push_back(g);
+      }
+    }
+    if (ok) P.march[h] = out;
+  }
+}
+
 // Exit geometry of regular-point traces per (layer, ordinate): so, u, v, face.
 void build_geo(Plan &P) {
   const int nl = P.nz - 1, nang = P.nang;
@@ -1336,7 +1392,10 @@ bool build_plan(const shdom_problem &p, Plan &P) {
     if (!build_schedule(p, P)) return false;
     P.nst = p.nstokes;
     P.col_stk.assign(P.nang, 0);
+    build_march(P);
     if (P.nst == 3) expand_stokes(P);
+    for (int h = 0; h < 2; ++h)  // the groups' columns in the final (Stokes-expanded) layout
+      for (MarchGrp &g : P.march[h]) { g.col0 = P.cls_col0[g.b][g.cls]; g.ncol = P.cls_ncol[g.b][g.cls]; }
     build_geo(P);
     auto keep = std::make_shared<const Plan>(P);
     std::lock_guard<std::mutex> lk(g_geom_mu);

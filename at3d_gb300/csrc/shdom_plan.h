@@ -57,6 +57,23 @@ struct Seg {
   int t0, ntask, start, b, cls, col0, ncol, regular, irr0;
 };
 
+// Plane march of one (octant, face class) group of columns: every phase-2
+// point of the group has a regular trace whose stopping face lies in the
+// neighbouring plane along the class axis (x, y or z), so the group's
+// phase-2 points can be swept plane by plane, each plane depending only on
+// the one before.  Axes: A the march (class) axis, U and V the two others
+// (U the strip axis, V the row axis); points are p = a*sa + u*su + v*sv.
+struct MarchGrp {
+  int b, cls, col0, ncol;
+  int nA, nU, nV, sa, su, sv;
+  int a0, da;          // first plane in march order (the upwind boundary plane) and the step
+  int du[4], dv[4];    // transverse offsets (0 or +-1) of the stopping face's corners, face-weight order
+  int upu;             // the sign of the U offsets: +1 when the upwind rows are at higher U
+  // fixed points (preset boundary or phase 1): the layer iz == zfix, and
+  // with open x (y) boundaries the planes ix == 0 or nx1 - 1 (iy == 0 or ny1 - 1)
+  int zfix, xedge, yedge;
+};
+
 struct Plan {
   // Level numbers of phase-2 points start at kPhase2 (phase 1 < kPhase2).
   static constexpr int kPhase2 = 1 << 16;
@@ -163,6 +180,10 @@ struct Plan {
   std::vector<int> level_items[2];               // level -> task x column items
   long long nirr[2] = {0, 0};                    // general-trace items per hemisphere
   long long nitems[2] = {0, 0};                  // phase-2 task x column items per hemisphere
+  // plane-march groups per hemisphere; empty when some group of the
+  // hemisphere does not march (general phase-2 traces, the mixed face
+  // class, points other than the boundary and edge planes that are fixed)
+  std::vector<MarchGrp> march[2];
   std::string err;
 };
 

@@ -146,11 +146,13 @@ class RTE:
         if rc:
             raise SHDOMError(L.shdom_last_error(None).decode())
         self._h = h
+        self._device = int(device)
         self._initialized = False
         return self
 
     def _create(self, device, defer: bool = False):
         L = _lib.lib()
+        self._device = int(device)
         self._struct = self.problem.to_struct()
         self._initialized = False
 
@@ -223,11 +225,17 @@ class RTE:
 
     def integrate_to_sensor(self, sensor: dict, single_scatter: bool = False, nosurface: bool = False) -> dict:
         """Radiance along the sensor's rays (at3d/solver.py:633-791); writes
-        sensor['I'] (and 'Q', 'U' for a polarized solve) and returns the sensor."""
-        if single_scatter or nosurface:
-            raise NotImplementedError("single_scatter / nosurface rendering is not supported")
+        sensor['I'] (and 'Q', 'U' for a polarized solve) and returns the sensor.
+        single_scatter: only the exact single scattering of the direct beam
+        is integrated; nosurface: no boundary radiance is added where a ray
+        leaves the domain (RENDER's SINGLESCATTER / NOSURFACE)."""
         self.check_solved(verbose=False)
-        out = self.render(sensor["ray_x"], sensor["ray_y"], sensor["ray_z"], sensor["ray_mu"], sensor["ray_phi"])
+        L = _lib.lib()
+        _check(self._h, L.shdom_set_render_options(self._h, int(bool(single_scatter)), int(bool(nosurface))))
+        try:
+            out = self.render(sensor["ray_x"], sensor["ray_y"], sensor["ray_z"], sensor["ray_mu"], sensor["ray_phi"])
+        finally:
+            _check(self._h, L.shdom_set_render_options(self._h, 0, 0))
         if out.ndim == 1:
             sensor["I"] = out
         else:
@@ -319,12 +327,53 @@ class RTE:
             w.ctypes.data_as(dp), grad.ctypes.data_as(dp)))
         return grad.reshape(shp + (2,))
 
+    def levis_adjoint_device(self, rays_dev, weights_ptr: int, grad_ptr: int, species: int = 0, stream: int = 0):
+        """Device-resident form of ``levis_adjoint``: ``rays_dev`` holds the
+        device pointers (x, y, z float32; mu, phi float64) and the number of
+        rays, ``weights_ptr`` a float64 device array of ray weights and
+        ``grad_ptr`` a float64 device array [npx*npy*npz*2] for the result;
+        ordered on ``stream`` (a CUDA stream handle, 0 = legacy default)."""
+        (x, y, z, mu, phi), nrays = rays_dev
+        args = [C.c_void_p(v) for v in (x, y, z, mu, phi, weights_ptr, grad_ptr, stream)]
+        _check(self._h, _lib.lib().shdom_levis_adjoint_device(self._h, int(species), int(nrays), *args))
+
+    def species_properties(self, species: int = 0):
+        """(extinction, ssalb) of one species on the property grid, as solved."""
+        sp = self.problem.species[species]
+        return np.asarray(sp.extinction, np.float32), np.asarray(sp.ssalb, np.float32)
+
+    def update_species(self, species: int, extinction=None, ssalb=None):
+        """Replace the extinction and/or single-scattering albedo of one
+        species (property grid) and rebuild the device state for the new
+        medium (the grid geometry is reused); the solution is reset and must
+        be solved again.  This is the step an inversion makes between
+        iterates (the reference builds a new medium and re-solves)."""
+        import dataclasses
+        sp = self.problem.species[species]
+        shp = np.asarray(sp.extinction).shape
+        ext = sp.extinction if extinction is None else np.ascontiguousarray(extinction, np.float32).reshape(shp)
+        alb = sp.ssalb if ssalb is None else np.ascontiguousarray(ssalb, np.float32).reshape(shp)
+        if np.any(ext < 0) or np.any(alb < 0) or np.any(alb > 1):
+            raise ValueError("extinction must be >= 0 and ssalb within [0, 1]")
+        species_list = list(self.problem.species)
+        species_list[species] = dataclasses.replace(sp, extinction=ext, ssalb=alb)
+        self.problem = dataclasses.replace(self.problem, species=species_list, _keep=[])
+        modes = (getattr(self, "_sweep_mode", None), getattr(self, "_transform_mode", None))
+        self.close()
+        self._create(getattr(self, "_device", 0))
+        if modes[0]:
+            self.set_sweep_mode(modes[0])
+        if modes[1]:
+            self.set_transform_mode(modes[1])
+
     def set_sweep_mode(self, mode: str):
         """'persistent' (one cooperative kernel per hemisphere; default),
         'per_level' (one launch per wavefront level; for solves that run
-        concurrently on one device) or 'graph' (per-level launches, each
-        iteration replayed from a captured CUDA graph)."""
-        modes = {"persistent": 0, "per_level": 1, "graph": 2}
+        concurrently on one device), 'graph' (per-level launches, each
+        iteration replayed from a captured CUDA graph) or 'levels_only'
+        ('persistent' with the plane march turned off).  Hemispheres that
+        the plane march can sweep use it in the first three modes."""
+        modes = {"persistent": 0, "per_level": 1, "graph": 2, "levels_only": 3}
         if mode not in modes:
             raise ValueError(f"sweep mode must be one of {sorted(modes)}")
         _check(self._h, _lib.lib().shdom_set_sweep_mode(self._h, modes[mode]))
@@ -343,6 +392,7 @@ class RTE:
         if mode not in self.TRANSFORM_MODES:
             raise ValueError(f"transform mode must be one of {sorted(self.TRANSFORM_MODES)}")
         _check(self._h, _lib.lib().shdom_set_transform_mode(self._h, self.TRANSFORM_MODES[mode]))
+        self._transform_mode = mode
 
     def timings(self) -> np.ndarray:
         t = np.zeros(5, np.float32)

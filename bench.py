@@ -35,11 +35,6 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 NWAVE = 4
-# Iterations per solve of the four benchmark scenes at 128x128x64 (measured
-# on the GPU path; the oracle converges in the same count to +-1, see
-# tests/test_gpu_parity.py).  Used by the CPU arms to scale a one-iteration
-# sample to a full solve.
-SOLVE_ITERS = [30, 30, 30, 23]
 # DRAM bytes (read + write) per point-ordinate of one k_sweep_levels launch,
 # from ncu on the 96x96x48 field (2.195 GB for 73.5M point-ordinates);
 # profiles/k_sweep_levels_cloud_field_96x96x48.md.
@@ -442,6 +437,58 @@ def thermal_block(args, dev):
             "note": "no separate CPU baseline: the oracle's per-iteration cost is the headline cpu_baseline's"}
 
 
+def config1_block(args, dev):
+    """The plain scalar workload as stated: the 32x32x24 periodic cloud blob
+    (two species: cloud with HG g 0.85 as 64 Legendre terms and a Rayleigh
+    layer), NMU 8 / NPHI 16, solution accuracy 1e-5, 32x32 pixels x 9 view
+    zeniths.  A full solve from initialisation plus the render, timed with
+    CUDA events after a warm-up solve, inputs resident; beside it the oracle
+    solving the same problem on one host thread (a full solve, measured)."""
+    import torch
+    from at3d_gb300.scenes import cloud_blob, orthographic_views
+    from at3d_gb300.solver import RTE
+    pb = cloud_blob()
+    rays = orthographic_views(pb, 32, 32)
+    nr = len(rays[0])
+    d = [torch.tensor(np.asarray(r), dtype=torch.float32 if i < 3 else torch.float64, device="cuda")
+         for i, r in enumerate(rays)]
+    img = torch.empty(nr, dtype=torch.float32, device="cuda")
+    r = RTE.from_problem(pb, device=dev)
+    ptrs = (d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), d[3].data_ptr(), d[4].data_ptr(), img.data_ptr())
+    r.solve(args.maxiter, verbose=False)
+    r.render_device(*ptrs, nr, 0)
+    torch.cuda.synchronize()
+    reps, ms = 3, []
+    for _ in range(reps):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record()
+        it, sc = r.solve(args.maxiter, verbose=False)
+        e[1].record()
+        r.render_device(*ptrs, nr, 0)
+        e[2].record()
+        torch.cuda.synchronize()
+        ms.append((e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])))
+    t_solve, t_render = (float(np.median([m[0] for m in ms])), float(np.median([m[1] for m in ms])))
+    s = r.sizes
+    out = {"workload": "32x32x24 periodic cloud blob + Rayleigh, NMU=8 NPHI=16, solacc 1e-5, 32x32 px x 9 views",
+           "iterations": it, "solcrit": sc, "ms_solve": t_solve, "ms_render": t_render,
+           "solves_per_s": 1e3 / (t_solve + t_render), "render_rays_per_s": nr / (t_render / 1e3),
+           "sweep": "reference-order walk" if s["nlevels_down"] == 0 else f"{s['nlevels_down']} wavefront levels"}
+    r.close()
+    if not args.no_cpu_baseline:
+        from oracle.oracle import Oracle
+        t0 = time.perf_counter()
+        o = Oracle(pb, fp64=False)
+        ito, _ = o.solve(args.maxiter)
+        t1 = time.perf_counter()
+        o.render(*rays, nthreads=1)
+        t2 = time.perf_counter()
+        out["cpu_baseline"] = {"value": 1.0 / (t2 - t0), "unit": "solves/s", "cores": 1, "kind": "port",
+                               "sample": f"the full solve ({ito} iterations, {t1 - t0:.2f} s) and render "
+                                         f"({t2 - t1:.2f} s) of the same problem, measured, one host thread"}
+    return out
+
+
 def serving_block(args, dev):
     """A Poisson stream of mixed requests through the continuous-admission
     loop (at3d_gb300.serving): grids 32x32x24 to 128x128x64, NMU/NPHI 8/16
@@ -461,55 +508,174 @@ def serving_block(args, dev):
     return out
 
 
-def cpu_sample(args, wavelength: int, iters: int):
-    """One oracle iteration of one wavelength, scaled to a full solve."""
-    from oracle.oracle import Oracle
-    pbs, _ = scenes(args)
-    o = Oracle(pbs[wavelength], fp64=False)
-    t0 = time.perf_counter()
-    o.init_solution()
-    t_init = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    o.solve(1)
-    t_it = time.perf_counter() - t0
-    cpu_sample.oracle = o
-    return t_init + iters * t_it, t_init, t_it
+class CpuSolves:
+    """The oracle (the C++ restatement of the reference Fortran) solving the
+    benchmark wavelengths concurrently, one host thread per wavelength, as
+    the reference's SolversDict.solve(n_jobs) does (at3d/containers.py:
+    699-744; each solve is single-threaded Fortran).  The solves advance in
+    slices: init() creates the solvers and runs INIT_SOLUTION; step(k)
+    runs the next k iterations of every unconverged wavelength (each slice
+    is one call of the solver's iteration loop, which restarts its
+    acceleration state as SOLUTION_ITERATIONS does per call).  Every slice
+    is timed with the wall clock; the iteration counts and the solution
+    criteria come from the CPU solves themselves."""
+
+    def __init__(self, pbs):
+        from oracle.oracle import Oracle
+        self.pbs = pbs
+        self.Oracle = Oracle
+        self.solacc = [pb.params.solution_accuracy for pb in pbs]
+
+    def _parallel(self, fn):
+        res = [None] * len(self.pbs)
+
+        def run(w):
+            res[w] = fn(w)
+
+        th = [threading.Thread(target=run, args=(w,)) for w in range(len(self.pbs))]
+        t0 = time.perf_counter()
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        return time.perf_counter() - t0, res
+
+    def init(self):
+        self.orc = [None] * len(self.pbs)
+        self.iters = [0] * len(self.pbs)
+        self.crit = [[] for _ in self.pbs]  # solution criterion after each iteration
+
+        def mk(w):
+            self.orc[w] = self.Oracle(self.pbs[w], fp64=False)
+            self.orc[w].init_solution()
+
+        self.t_init, _ = self._parallel(mk)
+        return self.t_init
+
+    def converged(self, w):
+        return bool(self.crit[w]) and self.crit[w][-1] <= self.solacc[w]
+
+    def step(self, k: int = 1):
+        def adv(w):
+            for _ in range(k):
+                if self.converged(w) or self.iters[w] >= 100:
+                    break
+                it, sc = self.orc[w].solve(self.iters[w] + 1)
+                self.iters[w] = it
+                self.crit[w].append(sc)
+
+        wall, _ = self._parallel(adv)
+        return wall
+
+    def remaining_iterations(self, w):
+        """Iterations still needed by wavelength w: 0 when converged, else
+        the solution criterion's geometric trend over the last iterations
+        extrapolated to the solution accuracy."""
+        c = self.crit[w]
+        if self.converged(w):
+            return 0
+        if len(c) < 3:
+            return None
+        y = np.log(np.asarray(c[-4:], np.float64))
+        slope = np.polyfit(np.arange(len(y)), y, 1)[0]
+        if slope >= 0:
+            return None
+        return int(np.ceil((np.log(self.solacc[w]) - y[-1]) / slope))
+
+
+def cpu_solve_rate(pbs, iters_hint, slices: int = 1):
+    """A bounded sample of the CPU solves (initialisation plus `slices`
+    iterations of every wavelength at once), projected to a full solve with
+    the measured mean iteration wall time: (solves/s, description)."""
+    cs = CpuSolves(pbs)
+    t_init = cs.init()
+    walls = [cs.step(1) for _ in range(slices)]
+    rem = [cs.remaining_iterations(w) for w in range(len(pbs))]
+    need = max(cs.iters[w] + (rem[w] if rem[w] is not None else iters_hint[w] - cs.iters[w])
+               for w in range(len(pbs)))
+    t_it = float(np.mean(walls))
+    t_solve = t_init + need * t_it
+    cpu_solve_rate.last = cs
+    return len(pbs) / t_solve, (f"{len(pbs)} wavelengths solved at once on {len(pbs)} host threads (oracle, the "
+                                f"C++ restatement of the reference Fortran): initialisation {t_init:.1f} s plus "
+                                f"{slices} iterations measured ({t_it:.1f} s each, wall), projected to {need} "
+                                f"iterations per solve")
 
 
 def cpu_render_sample(args, nrays: int = 4096):
     """The oracle's render of the first nrays rays of the benchmark views on
     every host core (one ray slice per thread, as the reference's joblib
-    ray slicing), from the state of the last cpu_sample: rays/s and cores."""
+    ray slicing), from the state of the last CPU sample: rays/s and cores."""
     _, rays = scenes(args)
     sub = tuple(np.ascontiguousarray(np.asarray(a)[:nrays]) for a in rays)
     cores = os.cpu_count() or 1
-    o = cpu_sample.oracle
+    o = cpu_solve_rate.last.orc[0]
     t0 = time.perf_counter()
     o.render(*sub, nthreads=cores)
     dt = time.perf_counter() - t0
     return nrays / dt, cores
 
 
+def host_cpu():
+    """Model name and logical core count of the host."""
+    model = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"model": model or "unknown", "logical_cores": os.cpu_count()}
+
+
 def reference_arm(args, rank, ws):
+    """The reference's CPU path timed on the host: the oracle solving the
+    benchmark wavelengths concurrently, one thread per wavelength.  Each
+    step is a measured slice of those solves (args.ref_slice iterations of
+    every wavelength; the first step also holds the initialisation), and
+    ms_per_step is the measured wall time of a timed step.  When the solves
+    converge within the steps, the time per solve is measured in full;
+    otherwise the remaining iterations come from the CPU solves' own
+    convergence trend and the rate is marked projected."""
     if rank != 0:
         return None
-    iters = args.ref_iters
-    per_step = []
-    for s in range(args.warmup + args.steps):
-        w = s % args.nwave
-        t_solve, t_init, t_it = cpu_sample(args, w, iters[w])
-        if s >= args.warmup:
-            per_step.append(t_solve)
-    sec_per_solve = float(np.mean(per_step))
-    v = 1.0 / sec_per_solve
+    pbs, _ = scenes(args)
+    cs = CpuSolves(pbs)
+    t_init = cs.init()
+    slices = [cs.step(args.ref_slice) for _ in range(args.warmup + args.steps)]
+    walls = [w + (t_init if i == 0 else 0.0) for i, w in enumerate(slices)]  # per step, as run
+    timed = walls[args.warmup:] if args.steps > 0 else walls
+    ms_step = float(np.mean(timed)) * 1e3
+    # wall time of the concurrent solves: the initialisation and every measured slice, plus,
+    # when they have not converged yet, the remaining slices at the mean wall of the last three
+    rem = [cs.remaining_iterations(w) for w in range(len(pbs))]
+    done = all(r == 0 for r in rem)
+    extra, known = 0, True
+    if not done:
+        est = [r for r in rem if r is not None]
+        known = len(est) == len(rem)
+        extra = int(np.ceil(max(est, default=0) / max(1, args.ref_slice)))
+    t_solves = t_init + float(np.sum(slices)) + extra * float(np.mean(slices[-3:]))
+    v = len(pbs) / t_solves
+    iters = [cs.iters[w] + (rem[w] or 0) for w in range(len(pbs))]
+    sample = (f"one step = {args.ref_slice} iteration(s) of each of the {len(pbs)} wavelength solves at once "
+              f"({len(pbs)} host threads, one per solve as SolversDict.solve(n_jobs)); initialisation "
+              f"{t_init:.1f} s in the first step; {sum(cs.iters)} iterations measured in total")
+    cpu = host_cpu()
     return {"metric": "SHDOM solves/s", "value": v, "unit": "solves/s", "impl": "reference", "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec_per_solve * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic",
             "config": config_dict(args),
-            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": 1, "kind": "port",
-                             "sample": f"one SHDOM iteration of one wavelength per step on the full grid, "
-                                       f"scaled by the iterations per solve {iters} plus the measured "
-                                       f"initialisation; single thread (one solve per thread, as the reference)"},
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": len(pbs), "kind": "port", "sample": sample,
+                             "host": cpu},
+            "projection": {"projected": not done, "measured_iterations": list(cs.iters),
+                           "iterations_per_solve": iters, "solution_criteria": [c[-1] if c else None
+                                                                                for c in cs.crit],
+                           "init_s": t_init, "step_walls_s": walls,
+                           "remaining_slices_estimated": extra,
+                           "estimate_complete": known},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -535,27 +701,26 @@ def main():
     ap.add_argument("--solacc", type=float, default=1e-4)
     ap.add_argument("--maxiter", type=int, default=100)
     ap.add_argument("--nwave", type=int, default=NWAVE, help="wavelengths per step (profiling runs use 1)")
-    ap.add_argument("--ref-iters", type=str, default="")
+    ap.add_argument("--ref-slice", type=int, default=1, help="CPU solve iterations per reference-arm step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--jobs", type=int, default=0, help="wavelengths solved at once (default: all)")
     ap.add_argument("--no-extras", action="store_true", help="skip the precision, gradient and serving blocks")
     ap.add_argument("--serve-rates", type=str, default="2", help="Poisson arrival rates (requests/s) to run")
     ap.add_argument("--serve-requests", type=int, default=16)
     ap.add_argument("--serve-slots", type=int, default=4)
-    ap.add_argument("--only", default="", choices=["", "precision", "gradient", "polarized", "serving", "thermal"],
+    ap.add_argument("--only", default="", choices=["", "precision", "gradient", "polarized", "serving", "thermal",
+                                                    "config1"],
                     help="run one extra block alone and print its JSON (for profiling)")
     ap.add_argument("--pol-boundaries", type=str, default="periodic,open")
     args = ap.parse_args()
     args.serve_rates = [float(x) for x in args.serve_rates.split(",") if x]
     args.pol_boundaries = [x for x in args.pol_boundaries.split(",") if x]
     args.jobs = args.jobs or args.nwave
-    args.ref_iters = [int(x) for x in args.ref_iters.split(",")] if args.ref_iters else \
-        SOLVE_ITERS[:args.nwave]
     rank, ws = dist_init()
     if args.only:
         dev = int(os.environ.get("LOCAL_RANK", "0"))
         blk = {"precision": precision_block, "gradient": gradient_block, "polarized": polarized_block,
-               "serving": serving_block, "thermal": thermal_block}[args.only]
+               "serving": serving_block, "thermal": thermal_block, "config1": config1_block}[args.only]
         print(json.dumps({args.only: blk(args, dev)}))
         return
     if args.impl == "reference":
@@ -573,15 +738,15 @@ def main():
         extras["gradient"] = gradient_block(args, dev)
         extras["polarized"] = polarized_block(args, dev)
         extras["thermal"] = thermal_block(args, dev)
+        extras["config1"] = config1_block(args, dev)
         extras["serving"] = serving_block(args, dev)
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
-        t_solve, t_init, t_it = cpu_sample(args, 0, r["iters"][0])
+        pbs, _ = scenes(args)
+        v, desc = cpu_solve_rate(pbs, r["iters"])
         rr, cores = cpu_render_sample(args)
-        cpu = {"value": 1.0 / t_solve, "unit": "solves/s", "cores": 1, "kind": "port",
-               "sample": f"oracle (CPU restatement of the reference Fortran): initialisation ({t_init:.1f} s) "
-                         f"plus one iteration ({t_it:.1f} s) of wavelength 0 on the full grid, scaled to the "
-                         f"{r['iters'][0]} iterations of its solve; single thread",
+        cpu = {"value": v, "unit": "solves/s", "cores": len(pbs), "kind": "port", "sample": desc,
+               "projected": True, "host": host_cpu(),
                "render_rays_per_s": rr, "render_cores": cores,
                "render_sample": "4096 rays of the benchmark views, one ray slice per host core"}
     out = {"metric": "SHDOM solves/s", "value": r["solves_per_s"], "unit": "solves/s", "n_gpus": ws,

@@ -43,6 +43,7 @@ typedef struct shdom_sizes {
     long long launches; /* kernels launched on this handle since creation */
     long long device_bytes; /* device memory the handle holds (estimate before creation) */
     int nstokes;   /* Stokes components (1, or 3 for I, Q, U) */
+    int march;     /* hemispheres swept by the plane march (bit 0 down, bit 1 up; plan: eligible, handle: in use) */
 } shdom_sizes;
 
 /* Builds the grid, the cell structure, the sweep schedule and the medium on
@@ -125,6 +126,20 @@ int shdom_levis_adjoint(shdom_handle *h, int species, int nrays, const float *ca
                         const float *camz, const double *cammu, const double *camphi, const double *weights,
                         double *gradient);
 
+/* Device-resident form of shdom_levis_adjoint, for automatic
+ * differentiation with the data on the GPU: rays (float x/y/z, double
+ * mu/phi), the ray weights w_r (double) and the output gradient
+ * ([npx*npy*npz][2] double, d/d extinction and d/d albedo of `species`) are
+ * device buffers.  The work is ordered after what the caller queued on
+ * `stream` (cudaStream_t as void*, NULL = legacy default stream), and work
+ * queued on `stream` after the call sees the gradient; the call returns after
+ * the launch.  Same reference routine as shdom_levis_adjoint (the adjoint
+ * pass of LEVISAPPROX_GRADIENT, src/polarized/shdomsub4.f:288-809, with
+ * ADJ_WEIGHTS given). */
+int shdom_levis_adjoint_device(shdom_handle *h, int species, int nrays, const float *camx, const float *camy,
+                               const float *camz, const double *cammu, const double *camphi,
+                               const double *weights, double *gradient, void *stream);
+
 /* shdom_render for callers that cannot allocate device memory during the
  * call (scalar problems).  It has no counterpart in the reference.  The rays and radiances of
  * the call are staged in one fixed device array inside the library (2 MiB)
@@ -162,6 +177,18 @@ int shdom_last_timings(shdom_handle *h, float *ms5);
  * none.  No reference counterpart (diagnostics). */
 int shdom_sweep_timings(shdom_handle *h, float *ms2, int *launches2);
 
+/* RENDER's SINGLESCATTER and NOSURFACE switches for the renders that follow
+ * on this handle (shdom_render, shdom_render_device, shdom_render_noalloc;
+ * the Levis gradient always renders the full radiance):
+ *   single_scatter != 0: the source along the ray is only the exact single
+ *     scattering of the direct solar beam (with delta-M; zero without), not
+ *     the spherical-harmonic source (src/polarized/shdomsub2.f:3107-3142);
+ *   nosurface != 0: the radiance leaving the domain boundary (surface or
+ *     sky) is not added where the ray ends (:2721-2723).
+ * Replaces the single_scatter / nosurface arguments of
+ * RTE.integrate_to_sensor (at3d/solver.py:633, :684-686).  Both 0 by default. */
+int shdom_set_render_options(shdom_handle *h, int single_scatter, int nosurface);
+
 /* Arithmetic of the two spherical-harmonic <-> discrete-ordinate transforms
  * of each iteration (SH_TO_DO / DO_TO_SH, src/polarized/shdomsub1.f:2928-3254,
  * which the reference runs in FP32 on the CPU):
@@ -173,12 +200,19 @@ int shdom_sweep_timings(shdom_handle *h, float *ms2, int *launches2);
  * mode.  No reference counterpart: the reference has a single FP32 path. */
 int shdom_set_transform_mode(shdom_handle *h, int mode);
 
-/* How the interior sweep levels are launched: 0 (default) one persistent
+/* How the sweep's interior points are scheduled.  A hemisphere whose
+ * interior points all trace through one full cell to the previous plane
+ * along their ordinate group's face axis (open boundaries) is swept by the
+ * plane march: one kernel per hemisphere, thread-block clusters that keep
+ * the previous plane in shared memory, no waits between clusters.  Other
+ * hemispheres use the wavefront level schedule: 0 (default) one persistent
  * cooperative kernel per hemisphere with a grid barrier between levels
  * (when the device supports cooperative launch), 1 one kernel launch per
  * level, 2 as 1 with each solution iteration's launches captured once in
- * a CUDA graph (one per source-truncation state) and replayed.  Use 1 or 2
- * when several handles solve concurrently on one device: they have no
+ * a CUDA graph (one per source-truncation state) and replayed; mode 2
+ * replays the plane march from the graph as well.  3 is 0 with the plane
+ * march turned off (the level schedule everywhere; for comparisons).  Use 1
+ * or 2 when several handles solve concurrently on one device: they have no
  * waits between thread blocks.  In mode 2 shdom_last_timings reports the
  * whole iteration in its first entry.  No reference counterpart. */
 int shdom_set_sweep_mode(shdom_handle *h, int mode);

@@ -34,7 +34,7 @@ def lib():
         L.oracle_error.argtypes = [C.c_void_p]
         for n in ("oracle_sizes", "oracle_solve", "oracle_init_solution", "oracle_export",
                   "oracle_render", "oracle_grid", "oracle_angles", "oracle_levis_gradient",
-                  "oracle_frozen_render"):
+                  "oracle_frozen_render", "oracle_set_render_options", "oracle_levis_adjoint"):
             getattr(L, n).restype = C.c_int
         L.oracle_destroy.argtypes = [C.c_void_p]
         _LIB = L
@@ -88,7 +88,8 @@ class Oracle:
                                 _p(flx), _p(dfl))
         return dict(source=src, ns=ns, radiance=rad, nr=nr, fluxes=flx, dirflux=dfl)
 
-    def render(self, x, y, z, mu, phi, nthreads: int = 1):
+    def render(self, x, y, z, mu, phi, nthreads: int = 1, single_scatter: bool = False, nosurface: bool = False):
+        self._lib.oracle_set_render_options(C.c_void_p(self._h), int(single_scatter), int(nosurface))
         x = np.ascontiguousarray(x, np.float32); y = np.ascontiguousarray(y, np.float32)
         z = np.ascontiguousarray(z, np.float32)
         mu = np.ascontiguousarray(mu, np.float64); phi = np.ascontiguousarray(phi, np.float64)
@@ -96,6 +97,7 @@ class Oracle:
         out = np.zeros(len(x) if nst == 1 else (len(x), nst), np.float32)
         rc = self._lib.oracle_render(C.c_void_p(self._h), len(x), _p(x), _p(y), _p(z), _p(mu, C.c_double),
                                      _p(phi, C.c_double), _p(out), int(nthreads))
+        self._lib.oracle_set_render_options(C.c_void_p(self._h), 0, 0)
         if rc:
             raise RuntimeError(self._lib.oracle_error(C.c_void_p(self._h)).decode())
         return out
@@ -123,6 +125,20 @@ class Oracle:
         if rc:
             raise RuntimeError(self._lib.oracle_error(C.c_void_p(self._h)).decode())
         return grad, float(cost.value), out
+
+    def levis_adjoint(self, species: int, rays, weights, nthreads: int = 1):
+        """The adjoint pass with given ray weights w_r: the Levis gradient
+        of sum_r w_r I_r, [npx*npy*npz, 2]."""
+        x, y, z, mu, phi = self._rays(*rays)
+        w = np.ascontiguousarray(weights, np.float64)
+        ng = self._problem.species[0].extinction.size
+        grad = np.zeros((ng, 2), np.float64)
+        rc = self._lib.oracle_levis_adjoint(C.c_void_p(self._h), int(species), len(x), _p(x), _p(y), _p(z),
+                                            _p(mu, C.c_double), _p(phi, C.c_double), _p(w, C.c_double),
+                                            _p(grad, C.c_double), int(nthreads))
+        if rc:
+            raise RuntimeError(self._lib.oracle_error(C.c_void_p(self._h)).decode())
+        return grad
 
     def frozen_render(self, species: int, voxel: int, dext: float, dalb: float, rays, nthreads: int = 1):
         """Render with one voxel's extinction / albedo perturbed and the source

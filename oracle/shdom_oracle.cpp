@@ -220,6 +220,8 @@ struct Solver {
   std::vector<R> legen6;  // [numphase][6][nleg+1] all six elements when nst = 3
   double extmin = 0, scatmin = 0;
   R albmax = 0;
+  // RENDER's SINGLESCATTER / NOSURFACE switches (src/polarized/shdomsub2.f:3107-3142, :2721-2723)
+  int rsingle = 0, rnosfc = 0;
   const float phasemax = 0.999f;
 
   // direct beam
@@ -2304,7 +2306,8 @@ struct Solver {
         }
         R ext = total_ext[ip];
         oldipts[n] = ip;
-        int is = shptr[ip], ns = shptr[ip + 1] - is;
+        // with SINGLESCATTER neither the harmonic source nor its truncated single scatter enters
+        int is = shptr[ip], ns = rsingle ? 0 : shptr[ip + 1] - is;
         if (nst == 3) {
           R sv[3];
           source_1cell_pol(ip, ns, is, ext, y6, singscat, secmu0, sv);
@@ -2433,8 +2436,8 @@ struct Solver {
         float uu = (xs[1] - xs[0] > 0) ? (float)((xn - xs[0]) / (xs[1] - xs[0])) : 0.f;
         float vv = (ys[2] - ys[0] > 0) ? (float)((yn - ys[0]) / (ys[2] - ys[0])) : 0.f;
         float radbnd = (1 - uu) * (1 - vv) * (float)rb[0] + uu * (1 - vv) * (float)rb[1] + (1 - uu) * vv * (float)rb[2] + uu * vv * (float)rb[3];
-        radiance_acc[0] += transmit * radbnd;
-        if (nst == 3 && brdf && (float)mu2 >= 0.0f) {  // a polarizing surface
+        if (!rnosfc) radiance_acc[0] += transmit * radbnd;
+        if (!rnosfc && nst == 3 && brdf && (float)mu2 >= 0.0f) {  // a polarizing surface
           const double w1 = (1 - uu) * (1 - vv), w2 = uu * (1 - vv), w3 = (1 - uu) * vv, w4 = uu * vv;
           radiance_acc[1] += transmit * (float)(w1 * rq[0] + w2 * rq[1] + w3 * rq[2] + w4 * rq[3]);
           radiance_acc[2] += transmit * (float)(w1 * ru[0] + w2 * ru[1] + w3 * ru[2] + w4 * ru[3]);
@@ -3142,11 +3145,15 @@ bool frozen_render(Solver<R> &S, int ipa, int voxel, float dext, float dalb, int
 }
 
 template <typename R>
+// With meas: the L2 cost of one-ray pixels and its adjoint weights; with
+// weights (meas null): those ray weights (the gradient of sum_r w_r I_r).
 bool levis_gradient(Solver<R> &S, int ipa, int n, const float *camx, const float *camy, const float *camz,
-                    const double *cammu, const double *camphi, const float *meas, double *gradout, double *cost,
-                    float *stokesout, int nthreads) {
+                    const double *cammu, const double *camphi, const float *meas, const double *weights,
+                    double *gradout, double *cost, float *stokesout, int nthreads) {
   if (ipa < 0 || ipa >= S.npart) { S.err = "levis_gradient: bad species index"; return false; }
   if (S.nst != 1) { S.err = "levis_gradient: scalar problems only"; return false; }
+  std::vector<float> own;
+  if (!stokesout) { own.resize(n); stokesout = own.data(); }
   if (!S.render(n, camx, camy, camz, cammu, camphi, stokesout, nthreads)) return false;  // phase 1 (with phasetab, bcrad)
   Levis<R> L(S);
   if (!L.prepare(ipa, S.err)) return false;
@@ -3154,11 +3161,15 @@ bool levis_gradient(Solver<R> &S, int ipa, int n, const float *camx, const float
   std::vector<double> adj(n);
   double c = 0.0;
   for (int i = 0; i < n; ++i) {
-    const double e = (double)stokesout[i] - (double)meas[i];
-    c += 0.5 * e * e;
-    adj[i] = e;
+    if (meas) {
+      const double e = (double)stokesout[i] - (double)meas[i];
+      c += 0.5 * e * e;
+      adj[i] = e;
+    } else {
+      adj[i] = weights[i];
+    }
   }
-  *cost = c;
+  if (cost) *cost = c;
   // phase 3: adjoint rays (per-thread accumulators)
   const int nt = std::max(1, nthreads);
   std::vector<std::vector<double>> g(nt, std::vector<double>((size_t)L.ng * 2, 0.0)), bw(nt, std::vector<double>(S.npts, 0.0));
@@ -3283,6 +3294,13 @@ int oracle_export(void *hv, float *source, int *ns, float *radiance, int *nr, fl
   return 0;
 }
 
+int oracle_set_render_options(void *hv, int single_scatter, int nosurface) {
+  Handle *h = (Handle *)hv;
+  if (h->fp64) { h->s64->rsingle = single_scatter != 0; h->s64->rnosfc = nosurface != 0; }
+  else { h->s32->rsingle = single_scatter != 0; h->s32->rnosfc = nosurface != 0; }
+  return 0;
+}
+
 int oracle_render(void *hv, int n, const float *camx, const float *camy, const float *camz, const double *cammu,
                   const double *camphi, float *out, int nthreads) {
   Handle *h = (Handle *)hv;
@@ -3299,10 +3317,23 @@ int oracle_levis_gradient(void *hv, int ipa, int n, const float *camx, const flo
                           const double *cammu, const double *camphi, const float *meas, double *gradout,
                           double *cost, float *stokesout, int nthreads) {
   Handle *h = (Handle *)hv;
-  bool ok = h->fp64 ? orc::levis_gradient(*h->s64, ipa, n, camx, camy, camz, cammu, camphi, meas, gradout, cost,
+  bool ok = h->fp64 ? orc::levis_gradient(*h->s64, ipa, n, camx, camy, camz, cammu, camphi, meas, nullptr, gradout, cost,
                                           stokesout, nthreads)
-                    : orc::levis_gradient(*h->s32, ipa, n, camx, camy, camz, cammu, camphi, meas, gradout, cost,
+                    : orc::levis_gradient(*h->s32, ipa, n, camx, camy, camz, cammu, camphi, meas, nullptr, gradout, cost,
                                           stokesout, nthreads);
+  return ok ? 0 : 1;
+}
+
+// The same adjoint pass with caller-supplied ray weights: the Levis
+// gradient of sum_r w_r I_r, gradout [npx*npy*npz][2].
+int oracle_levis_adjoint(void *hv, int ipa, int n, const float *camx, const float *camy, const float *camz,
+                         const double *cammu, const double *camphi, const double *weights, double *gradout,
+                         int nthreads) {
+  Handle *h = (Handle *)hv;
+  bool ok = h->fp64 ? orc::levis_gradient(*h->s64, ipa, n, camx, camy, camz, cammu, camphi, nullptr, weights, gradout,
+                                          nullptr, nullptr, nthreads)
+                    : orc::levis_gradient(*h->s32, ipa, n, camx, camy, camz, cammu, camphi, nullptr, weights, gradout,
+                                          nullptr, nullptr, nthreads);
   return ok ? 0 : 1;
 }
 

@@ -1,6 +1,6 @@
 """Builds tests/golden/rico32x36x26w672_pol.npz from the reference's own
-polarized verification files (read as text; run once in a checkout that has
-the reference next to it):
+polarized verification files (read as text; run once with the path of a reference checkout
+as its argument):
 
 * tests/data/rico32x36x26w672.prp -- SHDOM polarized tabulated-phase-function
   property file: NX NY NZ, DELX DELY and the z levels, NUMPHASE, then for
@@ -18,7 +18,9 @@ import sys
 
 import numpy as np
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if __name__ == "__main__" and len(sys.argv) != 2:
+    sys.exit("usage: make_rico_polarized_fixture.py REFERENCE_CHECKOUT")
+REF = sys.argv[1] if len(sys.argv) > 1 else None
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "rico32x36x26w672_pol.npz")
 
 

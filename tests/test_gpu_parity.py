@@ -141,19 +141,21 @@ def test_transform_modes(rte_cls, mode, tol):
 
 @pytest.mark.parametrize("mode", ["tf32x3", "fp32"])
 def test_precision_vs_fp64_fixture(rte_cls, mode):
-    """The 128x128x64 benchmark field (wavelength 3, ssa 0.99) after 30
-    iterations against the oracle run in FP64 (committed fixture): the
-    tensor-core 3xTF32 and the CUDA-core FP32 transforms both within 1e-4
-    relative RMS of the FP64 radiances."""
+    """The 128x128x64 benchmark field, all four wavelengths (ssa 0.99999 to
+    0.99, HG g 0.85 to 0.80), after 30 iterations against the oracle run in
+    FP64 (committed fixture): the tensor-core 3xTF32 and the CUDA-core FP32
+    transforms both within 1e-4 relative RMS of the FP64 radiances."""
     import os
     from at3d_gb300.scenes import cloud_field
     fx = np.load(os.path.join(os.path.dirname(__file__), "golden", "fp64_cloud_field_128x128x64.npz"))
-    pb = cloud_field(seed=2, wavelength_index=3, solacc=0.0)
-    r = rte_cls.from_problem(pb)
-    r.set_transform_mode(mode)
-    r.solve(int(fx["iterations"]), verbose=False)
-    rad = r.render(*orthographic_views(pb, 64, 64))
-    assert relrms(rad, fx["radiance_3"]) < 1e-4
+    for w in range(4):
+        pb = cloud_field(seed=2, wavelength_index=w, solacc=0.0)
+        r = rte_cls.from_problem(pb)
+        r.set_transform_mode(mode)
+        r.solve(int(fx["iterations"]), verbose=False)
+        rad = r.render(*orthographic_views(pb, 64, 64))
+        r.close()
+        assert relrms(rad, fx[f"radiance_{w}"]) < 1e-4, w
 
 
 def test_device_error_is_reported_and_handle_stays_usable(rte_cls):
@@ -243,3 +245,57 @@ def test_ross_li_surface(rte_cls, limit):
         o = Oracle(pb)
         o.solve(100)
         assert relrms(rad, o.render(*brdf_l1_rays())) < 1e-4
+
+
+@pytest.mark.parametrize("scene", ["scalar_nmu16", "scalar_8_16", "polarized"])
+def test_plane_march_matches_level_schedule(rte_cls, scene):
+    """On open boundaries every hemisphere's interior is swept by the plane
+    march (thread-block clusters, previous plane in shared memory); it runs
+    the same traces, faces and cell integrals as the wavefront level
+    schedule in another order, so the state after 3 iterations is the level
+    schedule's to FP32 rounding.  Grids with nx != ny and strips that do not
+    divide the grid evenly (partial and empty cluster ranks)."""
+    from at3d_gb300.scenes import cloud_field, polarized_blob
+    if scene == "scalar_nmu16":
+        pb = cloud_field(seed=7, wavelength_index=3, nx=26, ny=20, nz=12, nleg=128)
+    elif scene == "scalar_8_16":
+        pb = cloud_field(seed=9, nx=21, ny=34, nz=15, nmu=8, nphi=16, nleg=64)
+    else:
+        pb = polarized_blob(nx=20, ny=18, nz=14, boundary="open")
+    a = rte_cls.from_problem(pb)
+    assert a.sizes["march"] == 3
+    a.solve(3, verbose=False)
+    b = rte_cls.from_problem(pb)
+    b.set_sweep_mode("levels_only")
+    assert b.sizes["march"] == 0
+    b.solve(3, verbose=False)
+    sa, sb = a.export_state(), b.export_state()
+    assert np.array_equal(sa["nr"], sb["nr"])
+    for k in ("source", "radiance", "fluxes"):
+        assert relrms(sa[k], sb[k]) < 2e-6, k
+    o = Oracle(pb, fp64=False)
+    o.solve(3)
+    so = o.export()
+    assert relrms(sa["radiance"], so["radiance"]) < 1e-4
+
+
+@pytest.mark.parametrize("single_scatter,nosurface", [(True, False), (False, True), (True, True)])
+def test_render_options_single_scatter_nosurface(rte_cls, single_scatter, nosurface):
+    """integrate_to_sensor(single_scatter, nosurface): only the exact single
+    scattering of the direct beam along the ray, and no boundary radiance
+    at the ray's end (RENDER's SINGLESCATTER / NOSURFACE), against the
+    oracle; the next plain render is the full radiance again."""
+    from at3d_gb300.sensor import make_sensor_dataset
+    pb = cloud_blob(seed=5, nx=16, ny=16, nz=14, dx=0.04, dz=0.06, boundary="open")
+    r = rte_cls.from_problem(pb)
+    r.solve(3, verbose=False)
+    o = Oracle(pb, fp64=False)
+    o.solve(3)
+    rays = orthographic_views(pb, 12, 12, zeniths=[0.0, -45.6, 60.0])
+    sensor = make_sensor_dataset(*rays)
+    r.integrate_to_sensor(sensor, single_scatter=single_scatter, nosurface=nosurface)
+    ref = o.render(*rays, nthreads=8, single_scatter=single_scatter, nosurface=nosurface)
+    full = o.render(*rays, nthreads=8)
+    assert relrms(sensor["I"], ref) < 1e-4
+    assert relrms(ref, full) > 1e-2  # the options change the radiances
+    assert relrms(r.render(*rays), full) < 1e-4

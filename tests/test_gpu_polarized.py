@@ -56,6 +56,25 @@ def test_state_fixed_iterations(rte_cls, mode):
     assert rms(a["fluxes"] - b["fluxes"]) / rms(b["fluxes"]) < 1e-4
 
 
+@pytest.mark.parametrize("boundary", ["periodic", "open"])
+def test_state_fixed_iterations_stated_size(rte_cls, boundary):
+    """The polarized workload at its stated size (64x64x40, NMU 8 / NPHI 16,
+    169,000 points on the periodic grid): the Stokes state after 3
+    iterations against the oracle, 1e-4 of the RMS of I."""
+    pb = polarized_blob(boundary=boundary)
+    r = rte_cls.from_problem(pb)
+    r.solve(3, verbose=False)
+    o = Oracle(pb)
+    o.solve(3)
+    a, b = r.export_state(), o.export()
+    assert np.array_equal(a["ns"], b["ns"]) and np.array_equal(a["nr"], b["nr"])
+    for key in ("source", "radiance"):
+        den = rms(b[key][:, 0])
+        for k in range(3):
+            assert rms(a[key][:, k] - b[key][:, k]) / den < 1e-4, (key, k)
+    assert rms(a["fluxes"] - b["fluxes"]) / rms(b["fluxes"]) < 1e-4
+
+
 @pytest.mark.parametrize("mode", ["tf32x3", "fp32"])
 def test_converged_render(rte_cls, mode):
     pb = _scene()

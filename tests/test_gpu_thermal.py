@@ -115,23 +115,24 @@ def test_thermal_brdf_emission(rte_cls, make):
 
 def test_thermal_levis_gradient(rte_cls):
     """The Levis gradient with a thermal source (its emission term) on the
-    absorbing cloud: GPU against the oracle, relative RMS 2e-3 as in
-    test_gpu_gradient.py (the residual is the two converged states)."""
+    absorbing cloud: GPU against the oracle after the same 3 iterations
+    (the same frozen field up to FP32 rounding), relative RMS 1e-4."""
     from at3d_gb300.scenes import orthographic_views
     from brdf_scene import thermal_absorbing_blob
     pb = thermal_absorbing_blob()
     rays = orthographic_views(pb, 8, 8, zeniths=[0.0, 45.6, -60.0])
     r = rte_cls.from_problem(pb)
-    r.solve(100, verbose=False)
+    r.solve(3, verbose=False)
     o = Oracle(pb)
-    o.solve(100)
+    o.solve(3)
     base = o.render(*rays)
     meas = (base * (1 + 0.1 * np.random.default_rng(0).standard_normal(base.shape))).astype(np.float32)
     g_gpu, cost_gpu, _ = r.levis_gradient(rays, meas, 0)
     g_orc, cost_orc, _ = o.levis_gradient(0, rays, meas, nthreads=4)
     g_gpu = np.asarray(g_gpu).reshape(-1, 2)
-    assert relrms(g_gpu[:, 0], g_orc[:, 0]) < 2e-3
-    assert np.isclose(cost_gpu, cost_orc, rtol=1e-3)
+    for d in range(2):
+        assert relrms(g_gpu[:, d], g_orc[:, d]) < 1e-4, d
+    assert np.isclose(cost_gpu, cost_orc, rtol=1e-4)
 
 def test_band_units(rte_cls):
     """Units 'B' (the band integral of the Planck function over 800-1000

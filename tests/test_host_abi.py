@@ -144,3 +144,13 @@ def test_deep_periodic_plans():
     from at3d_gb300.solver import plan_summary
     s = plan_summary(cloud_field(seed=4, nx=64, ny=64, nz=32, nmu=8, nphi=16, nleg=64, boundary="periodic"))
     assert s["npts"] == 65 * 65 * 32 and s["nlevels_down"] == 0 and s["nlevels_up"] == 0
+
+
+def test_plane_march_eligibility():
+    """Open boundaries: both hemispheres' interiors are swept by the plane
+    march; periodic boundaries (wrap-around traces chain the planes) keep the
+    level schedule or the reference-order sweep."""
+    from at3d_gb300.scenes import cloud_blob, cloud_field
+    from at3d_gb300.solver import plan_summary
+    assert plan_summary(cloud_field(seed=2, nx=24, ny=20, nz=16))["march"] == 3
+    assert plan_summary(cloud_blob(nx=16, ny=16, nz=10))["march"] == 0
