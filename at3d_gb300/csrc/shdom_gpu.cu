@@ -592,40 +592,102 @@ __global__ void __launch_bounds__(256) k_irr_build(SweepArgs a, const Seg *__res
 // of a group are independent of one another, so a group's columns are
 // split into P1_SPLIT contiguous ranges, one block each (block b: group
 // b / P1_SPLIT, range b % P1_SPLIT): shorter levels per block, more SMs.
+// The levels are software-pipelined: a thread's first P1_STAGE items of the
+// next level that have a stored face record get their record, point and
+// the face corners' extinctions and ordinate sources loaded before the
+// barrier; after it only the corners' radiances, which the level just
+// finished may have written, are read.  Further items and traces that
+// walk several cells are done in place.
 constexpr int P1_THREADS = 512;
 constexpr int P1_SPLIT = 4;
+constexpr int P1_STAGE = 2;
 
 __global__ void __launch_bounds__(P1_THREADS) k_sweep_p1(SweepArgs a, const Seg *__restrict__ p1segs,
                                                          const int *__restrict__ p1off) {
   const int grp = blockIdx.x / P1_SPLIT, sid = blockIdx.x % P1_SPLIT;
   const int s0 = p1off[grp], s1 = p1off[grp + 1];
+  const int ldo = a.ldo;
+  // staged items: the inputs of a single-face trace but the corner radiances
+  RegLoad st[P1_STAGE];
+  int sq[P1_STAGE][4];
+  bool staged[P1_STAGE];
+  auto items_of = [&](const Seg &g, int &cbeg, int &ncs) {
+    const int cw = (g.ncol + P1_SPLIT - 1) / P1_SPLIT;
+    cbeg = sid * cw; ncs = max(0, min(g.ncol, cbeg + cw) - cbeg);
+    return g.ntask * ncs;
+  };
+  auto stage = [&](int si) {
+#pragma unroll
+    for (int k = 0; k < P1_STAGE; ++k) staged[k] = false;
+    if (si >= s1) return;
+    const Seg g = p1segs[si];
+    int cbeg, ncs;
+    const int items = items_of(g, cbeg, ncs);
+#pragma unroll
+    for (int k = 0; k < P1_STAGE; ++k) {
+      const int ii = threadIdx.x + k * blockDim.x;
+      if (ii >= items) break;
+      const int task = ii / ncs, slot = cbeg + (ii - task * ncs);
+      const IrrRec rec = a.irr[g.irr0 + task * g.ncol + slot];
+      if (rec.g.w <= 0.5f) continue;  // a cell walk: done in place
+      const int pt = (int)__ldg(a.tasks + g.t0 + task), col = g.col0 + slot;
+      rec_load(a, rec, pt, col, st[k], false);
+      sq[k][0] = rec.q.x; sq[k][1] = rec.q.y; sq[k][2] = rec.q.z; sq[k][3] = rec.q.w;
+      staged[k] = true;
+    }
+  };
+  stage(s0);
   for (int si = s0; si < s1; ++si) {
     const Seg g = p1segs[si];
-    const int cw = (g.ncol + P1_SPLIT - 1) / P1_SPLIT, cbeg = sid * cw, ncs = max(0, min(g.ncol, cbeg + cw) - cbeg);
-    const int items = g.ntask * ncs;
-    for (int ii = threadIdx.x; ii < items; ii += blockDim.x) {
-      const int task = ii / ncs, slot = cbeg + (ii - task * ncs);
-      const int i = task * g.ncol + slot;  // item of the segment
-      const int pt = (int)__ldg(a.tasks + g.t0 + task), col = g.col0 + slot;
+    int cbeg, ncs;
+    const int items = items_of(g, cbeg, ncs);
+    auto coords = [&](int ii, int &task, int &i, int &col) {
+      task = ii / ncs;
+      const int slot = cbeg + (ii - task * ncs);
+      i = task * g.ncol + slot;  // item of the segment
+      col = g.col0 + slot;
+    };
+    auto item_staged = [&](int ii, RegLoad &x, const int (&q)[4]) {
+      int task, i, col;
+      coords(ii, task, i, col);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) x.r[c] = a.raddo[(size_t)q[c] * ldo + col];
+      const Trace t = reg_trace(x, g.b, x.pt);
+      float rad = t.radsrc;
+      if (t.tr != 0.f) rad += t.tr * (t.f[0] * x.r[0] + t.f[1] * x.r[1] + t.f[2] * x.r[2] + t.f[3] * x.r[3]);
+      a.raddo[(size_t)x.pt * ldo + col] = rad;
+    };
+    auto item_plain = [&](int ii) {
+      int task, i, col;
+      coords(ii, task, i, col);
+      const int pt = (int)__ldg(a.tasks + g.t0 + task);
       const IrrRec rec = a.irr[g.irr0 + i];
       float rad;
       if (rec.g.w > 0.5f) {
-        RegLoad x;
-        rec_load(a, rec, pt, col, x, true);
-        const Trace t = reg_trace(x, g.b, pt);
+        RegLoad y;
+        rec_load(a, rec, pt, col, y, true);
+        const Trace t = reg_trace(y, g.b, pt);
         rad = t.radsrc;
-        if (t.tr != 0.f) rad += t.tr * (t.f[0] * x.r[0] + t.f[1] * x.r[1] + t.f[2] * x.r[2] + t.f[3] * x.r[3]);
+        if (t.tr != 0.f) rad += t.tr * (t.f[0] * y.r[0] + t.f[1] * y.r[1] + t.f[2] * y.r[2] + t.f[3] * y.r[3]);
       } else {
         const Trace t = trace_general(a, g.b, g.cls, pt, col, true);
         if (t.status != ERR_NONE) atomicCAS(a.err, ERR_NONE, t.status);
-        const int ldo = a.ldo;
         rad = t.radsrc;
         if (t.tr != 0.f)
           rad += t.tr * (t.f[0] * a.raddo[(size_t)t.q[0] * ldo + col] + t.f[1] * a.raddo[(size_t)t.q[1] * ldo + col] +
                          t.f[2] * a.raddo[(size_t)t.q[2] * ldo + col] + t.f[3] * a.raddo[(size_t)t.q[3] * ldo + col]);
       }
-      a.raddo[(size_t)pt * a.ldo + col] = rad;
+      a.raddo[(size_t)pt * ldo + col] = rad;
+    };
+    static_assert(P1_STAGE == 2, "the staged items are handled one by one below");
+    if (threadIdx.x < items) {
+      if (staged[0]) item_staged(threadIdx.x, st[0], sq[0]); else item_plain(threadIdx.x);
     }
+    if (threadIdx.x + blockDim.x < items) {
+      if (staged[1]) item_staged(threadIdx.x + blockDim.x, st[1], sq[1]); else item_plain(threadIdx.x + blockDim.x);
+    }
+    for (int ii = threadIdx.x + P1_STAGE * blockDim.x; ii < items; ii += blockDim.x) item_plain(ii);
+    stage(si + 1);  // the next level's inputs that do not depend on this level
     __syncthreads();
   }
 }
