@@ -790,27 +790,34 @@ __global__ void __launch_bounds__(256) k_sweep_levels(SweepArgs a, const Seg *__
 // group's columns are swept plane by plane, every point of a plane
 // independent of the others.  One thread-block cluster per (group, column
 // slice): the cluster's CTAs split each plane into strips of rows along U.
-// A CTA keeps its strip's radiances of the previous and the current plane
-// in shared memory (two buffers, swapped every plane), reads the bordering
-// row of the upwind strip from that CTA's shared memory (distributed
-// shared memory), and the cluster meets at one cluster barrier per plane.
+// A CTA keeps, for the previous and the current plane (two buffers swapped
+// every plane), its strip's radiances, ordinate sources times extinction
+// and extinctions in shared memory, plus one halo row on the upwind side
+// that the upwind CTA stores into it (distributed shared memory) when it
+// computes that row; the cluster meets at one cluster barrier per plane.
 // The source pass is fused: (radsrc, tr) of BACK_INT_GRID3D's cell
-// integral come from the ordinate source and extinction of the point and
-// of the face corners (the arithmetic of reg_trace).  DRAM sees one read of
-// the point's ordinate source (loaded one plane ahead) and one write of its
-// radiance per item; the corners' ordinate sources and extinctions were
-// read one plane earlier by the same SM and come from L1.
+// integral come from the ordinate source and extinction of the point
+// (loaded from global memory one plane ahead) and of the face corners (the
+// previous plane, in shared memory), with the arithmetic of reg_trace.
+// DRAM sees one read of the point's ordinate source and one write of its
+// radiance per item.
 struct MarchUnit {
   int grp, c0, nc, tw;  // group, absolute columns [c0, c0+nc), rows per CTA
 };
 constexpr int MT = 256;  // threads per CTA
 constexpr int MK = 16;   // (row, v) pairs per thread at most
 
+// Shared memory of one CTA: the face geometry of the strip's columns
+// [nv][nc] (float4), then two plane buffers, each rad[tw+2][nv][nc],
+// se[tw+2][nv][nc] and ext[tw+2][nv] (rows -1 and tw are halo rows).
+__host__ __device__ inline size_t march_buf_floats(int tw, int nv, int nc) {
+  return (size_t)(tw + 2) * nv * (2 * nc + 1);
+}
 __host__ __device__ inline size_t march_smem_bytes(int tw, int nv, int nc) {
-  return 2 * (size_t)tw * nv * nc * sizeof(float);
+  return sizeof(float) * (4 * (size_t)nv * nc + 2 * march_buf_floats(tw, nv, nc));
 }
 
-__global__ void __launch_bounds__(MT, 3) k_sweep_march(SweepArgs a, const MarchGrp *__restrict__ grps,
+__global__ void __launch_bounds__(MT, 2) k_sweep_march(SweepArgs a, const MarchGrp *__restrict__ grps,
                                                        const MarchUnit *__restrict__ units) {
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
@@ -819,129 +826,169 @@ __global__ void __launch_bounds__(MT, 3) k_sweep_march(SweepArgs a, const MarchG
   const MarchGrp G = grps[U.grp];
   const int nc = U.nc, nV = G.nV, tw = U.tw, ldo = a.ldo;
   const int u0 = rank * tw, nrow = max(0, min(tw, G.nU - u0));
-  extern __shared__ float mrad[];  // [2][tw][nV][nc]
-  const int plane_sz = tw * nV * nc;
-  // the strip on the upwind side along U and its row that borders this strip
-  const int nbr = rank + G.upu;
-  const bool has_nb = nbr >= 0 && nbr < cs && nbr * tw < G.nU;
-  const int nb_row = G.upu > 0 ? 0 : tw - 1;
-  const float *nb_rad = has_nb ? cl.map_shared_rank(mrad, nbr) : nullptr;
+  extern __shared__ float4 msm4[];
+  float4 *sgeo = msm4;                                   // [nV][nc]
+  float *buf0 = reinterpret_cast<float *>(msm4 + (size_t)nV * nc);
+  const int bsz = (int)march_buf_floats(tw, nV, nc);
+  const int rsz = (tw + 2) * nV * nc;                    // one rad (or se) array
+  // this CTA's row that the downwind CTA (rank - upu) reads as its halo row,
+  // and the halo row's index in that CTA's buffers
+  const int cons = rank - G.upu;
+  const bool push = nrow > 0 && cons >= 0 && cons < cs && cons * tw < G.nU;
+  const int push_row = G.upu > 0 ? 0 : tw - 1;
+  const int halo_lr = G.upu > 0 ? tw : -1;
+  float *cons_buf0 = push ? cl.map_shared_rank(buf0, cons) : nullptr;
   // thread -> column c and the strip's (row, v) pairs k0, k0 + tpc, ... (at most MK)
   const int tpc = MT / nc, c = threadIdx.x % nc, k0 = threadIdx.x / nc;
   const int col = U.c0 + c;
   const bool clamp = !a.stk || !a.stk[col];
   const bool pad = __ldg(a.col_cz + col) == 0.f;
   const int kn = k0 < tpc ? max(0, (nrow * nV - k0 + tpc - 1) / tpc) : 0;
-  auto fixed_at = [&](int A, int u, int v) {
-    const int ix = G.cls == 0 ? A : u, iy = G.cls == 1 ? A : (G.cls == 0 ? u : v), iz = G.cls == 2 ? A : v;
-    return pad || iz == G.zfix || (G.xedge && (ix == 0 || ix == a.nx1 - 1)) ||
-           (G.yedge && (iy == 0 || iy == a.ny1 - 1));
+  const int r0 = k0 / nV, v0 = k0 - r0 * nV;
+  const int ndn = G.cls == 0 ? a.nx1 : (G.cls == 1 ? a.ny1 : a.nz);  // extent of the class axis
+  auto plane_fixed = [&](int A) {
+    return pad || (G.cls == 2 && A == G.zfix) || (G.cls == 0 && G.xedge && (A == 0 || A == ndn - 1)) ||
+           (G.cls == 1 && G.yedge && (A == 0 || A == ndn - 1));
   };
-  auto rv_of = [&](int j, int &r, int &v) {
-    const int k = k0 + j * tpc;
-    r = k / nV; v = k - r * nV;
-  };
-  // plane 0 (the upwind boundary plane) is fixed: its radiances into buffer 0
+  // per pair: fixed in every plane (from u, v alone), and whether the face
+  // corners lie inside the grid
+  unsigned uvfix = 0, valid = 0;
+  {
+    int r = r0, v = v0;
 #pragma unroll 1
-  for (int j = 0; j < kn; ++j) {
-    int r, v;
-    rv_of(j, r, v);
-    const int p = G.a0 * G.sa + (u0 + r) * G.su + v * G.sv;
-    mrad[(r * nV + v) * nc + c] = __ldg(a.raddo + (size_t)p * ldo + col);
-  }
-  // the point's own ordinate source and extinction (or, at fixed points, its
-  // final radiance), loaded one plane ahead
-  float ps[MK], pe[MK];
+    for (int j = 0; j < kn; ++j) {
+      const int u = u0 + r;
+      const bool f = (G.cls != 2 && v == G.zfix) || (G.xedge && G.cls != 0 && (u == 0 || u == a.nx1 - 1)) ||
+                     (G.yedge && ((G.cls == 0 && (u == 0 || u == a.ny1 - 1)) ||
+                                  (G.cls == 2 && (v == 0 || v == a.ny1 - 1))));
+      bool ok = true;
 #pragma unroll
-  for (int j = 0; j < MK; ++j) {
-    ps[j] = 0.f; pe[j] = 0.f;
-    if (j < kn && G.nA > 1) {
-      int r, v;
-      rv_of(j, r, v);
-      const int A = G.a0 + G.da, u = u0 + r;
-      const int p = A * G.sa + u * G.su + v * G.sv;
-      if (fixed_at(A, u, v)) {
-        ps[j] = __ldg(a.raddo + (size_t)p * ldo + col);
-      } else {
-        ps[j] = __ldg(a.srcdo + (size_t)p * ldo + col);
-        pe[j] = __ldg(a.text + p);
+      for (int k = 0; k < 4; ++k) {
+        const int uu = u + G.du[k], vv = v + G.dv[k];
+        ok = ok && uu >= 0 && uu < G.nU && vv >= 0 && vv < nV;
       }
+      uvfix |= (unsigned)f << j;
+      valid |= (unsigned)ok << j;
+      v += tpc;
+      while (v >= nV) { v -= nV; ++r; }
     }
   }
-  cl.sync();
-  // corner offsets in the point index relative to the point itself in the previous plane
-  int qoff[4];
+  // face geometry of the x and y classes: one entry per (v, column)
+  if (G.cls != 2) {
+    for (int i = threadIdx.x; i < nV * nc; i += MT) {
+      const int v = i / nc, cc = i - v * nc;
+      const int layer = (G.b & 4) ? v - 1 : v;
+      sgeo[i] = (layer >= 0 && layer < a.nz - 1)
+                    ? __ldg(reinterpret_cast<const float4 *>(a.geo) + (size_t)layer * a.nang + U.c0 + cc)
+                    : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+  // plane 0 (the upwind boundary plane) is fixed: radiance, source x extinction
+  // and extinction into buffer 0 (and its halo row into the downwind CTA's)
+  {
+    int r = r0, v = v0;
+#pragma unroll 1
+    for (int j = 0; j < kn; ++j) {
+      const int p = G.a0 * G.sa + (u0 + r) * G.su + v * G.sv;
+      const float rad = __ldg(a.raddo + (size_t)p * ldo + col), s = __ldg(a.srcdo + (size_t)p * ldo + col),
+                  e = __ldg(a.text + p);
+      const int sp = (r + 1) * nV + v, si = sp * nc + c;
+      buf0[si] = rad; buf0[rsz + si] = s * e; buf0[2 * rsz + sp] = e;
+      if (push && r == push_row) {
+        const int hp = (halo_lr + 1) * nV + v, hi = hp * nc + c;
+        cons_buf0[hi] = rad; cons_buf0[rsz + hi] = s * e; cons_buf0[2 * rsz + hp] = e;
+      }
+      v += tpc;
+      while (v >= nV) { v -= nV; ++r; }
+    }
+  }
+  // the point's own ordinate source and extinction (and, at fixed points,
+  // its final radiance), loaded one plane ahead
+  float ps[MK], pe[MK], pr[MK];
+  {
+    const int A = G.a0 + G.da;
+    const bool pf = G.nA > 1 && plane_fixed(A);
+    int r = r0, v = v0;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) qoff[k] = G.du[k] * G.su + G.dv[k] * G.sv;
+    for (int j = 0; j < MK; ++j) {
+      ps[j] = 0.f; pe[j] = 0.f; pr[j] = 0.f;
+      if (j < kn && G.nA > 1) {
+        const int p = A * G.sa + (u0 + r) * G.su + v * G.sv;
+        ps[j] = __ldg(a.srcdo + (size_t)p * ldo + col);
+        pe[j] = __ldg(a.text + p);
+        if (pf || ((uvfix >> j) & 1)) pr[j] = __ldg(a.raddo + (size_t)p * ldo + col);
+      }
+      v += tpc;
+      while (v >= nV) { v -= nV; ++r; }
+    }
+  }
+  float4 gz = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto load_gz = [&](int A) {
+    const int layer = (G.b & 4) ? A - 1 : A;
+    return (G.cls == 2 && kn > 0 && layer >= 0 && layer < a.nz - 1)
+               ? __ldg(reinterpret_cast<const float4 *>(a.geo) + (size_t)layer * a.nang + col)
+               : make_float4(0.f, 0.f, 0.f, 0.f);
+  };
+  if (G.nA > 1) gz = load_gz(G.a0 + G.da);
+  // corner offsets relative to the point itself, in the previous plane's buffers
+  int qs[4], qe[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) { qe[k] = G.du[k] * nV + G.dv[k]; qs[k] = qe[k] * nc; }
+  cl.sync();
   for (int t = 1; t < G.nA; ++t) {
     const int A = G.a0 + t * G.da, An = A + G.da;
     const bool more = t + 1 < G.nA;
-    const float *prev = mrad + ((t - 1) & 1) * plane_sz;
-    float *cur = mrad + (t & 1) * plane_sz;
-    const float *nprev = has_nb ? nb_rad + ((t - 1) & 1) * plane_sz + nb_row * nV * nc : nullptr;
-    float4 gz = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (G.cls == 2 && kn > 0) {
-      const int layer = (G.b & 4) ? A - 1 : A;
-      gz = __ldg(reinterpret_cast<const float4 *>(a.geo) + (size_t)layer * a.nang + col);
-    }
+    const bool pf = plane_fixed(A), pfn = more && plane_fixed(An);
+    const float *prev = buf0 + ((t - 1) & 1) * bsz;
+    float *cur = buf0 + (t & 1) * bsz;
+    float *ccur = push ? cons_buf0 + (t & 1) * bsz : nullptr;
+    const float4 g2 = gz;
+    if (more) gz = load_gz(An);
+    int r = r0, v = v0;
 #pragma unroll
     for (int j = 0; j < MK; ++j) {
       if (j < kn) {
-        int r, v;
-        rv_of(j, r, v);
-        const int u = u0 + r;
-        const int p = A * G.sa + u * G.su + v * G.sv;
+        const int sp = (r + 1) * nV + v, si = sp * nc + c;
+        const int p = A * G.sa + (u0 + r) * G.su + v * G.sv;
+        const float s1 = ps[j], e1 = pe[j];
         float rad;
-        if (fixed_at(A, u, v)) {
-          rad = ps[j];
+        if (pf || ((uvfix >> j) & 1)) {
+          rad = pr[j];
+        } else if (!((valid >> j) & 1)) {
+          atomicCAS(a.err, ERR_NONE, ERR_SWEEP_NOFACE);
+          rad = 0.f;
+          a.raddo[(size_t)p * ldo + col] = rad;
         } else {
-          const int pp = p - G.da * G.sa;  // same (u, v), previous plane
-          const float s1 = ps[j], e1 = pe[j];
-          float4 g = gz;
-          if (G.cls != 2) {
-            const int layer = (G.b & 4) ? v - 1 : v;
-            g = __ldg(reinterpret_cast<const float4 *>(a.geo) + (size_t)layer * a.nang + col);
-          }
+          const float4 g = G.cls == 2 ? g2 : sgeo[v * nc + c];
           const float fu = g.y, fv = g.z;
-          const float f[4] = {(1.f - fu) * (1.f - fv), (1.f - fu) * fv, fu * (1.f - fv), fu * fv};
-          float ext0 = 0.f, srcext0 = 0.f, rk[4];
-          bool ok = true;
-#pragma unroll
-          for (int kk = 0; kk < 4; ++kk) {
-            const int q = pp + qoff[kk];
-            const float e = __ldg(a.text + q), sk = __ldg(a.srcdo + (size_t)q * ldo + col);
-            const int lr = r + G.du[kk], lv = v + G.dv[kk];
-            const int lvc = min(max(lv, 0), nV - 1);
-            if (lr >= 0 && lr < nrow) {
-              rk[kk] = prev[(lr * nV + lvc) * nc + c];
-            } else {
-              ok = ok && has_nb;
-              rk[kk] = has_nb ? nprev[lvc * nc + c] : 0.f;
-            }
-            ok = ok && lv == lvc;
-            ext0 += f[kk] * e;
-            srcext0 += f[kk] * sk * e;
-          }
+          const float f0 = (1.f - fu) * (1.f - fv), f1 = (1.f - fu) * fv, f2 = fu * (1.f - fv), f3 = fu * fv;
+          const float ext0 = f0 * prev[2 * rsz + sp + qe[0]] + f1 * prev[2 * rsz + sp + qe[1]] +
+                             f2 * prev[2 * rsz + sp + qe[2]] + f3 * prev[2 * rsz + sp + qe[3]];
+          const float srcext0 = f0 * prev[rsz + si + qs[0]] + f1 * prev[rsz + si + qs[1]] +
+                                f2 * prev[rsz + si + qs[2]] + f3 * prev[rsz + si + qs[3]];
           float radsrc, tr;
           cell_source(ext0, srcext0, e1, e1 * s1, g.x, radsrc, tr, clamp);
           rad = radsrc;
-          if (tr != 0.f) rad += tr * (f[0] * rk[0] + f[1] * rk[1] + f[2] * rk[2] + f[3] * rk[3]);
-          if (!ok) { atomicCAS(a.err, ERR_NONE, ERR_SWEEP_NOFACE); rad = 0.f; }
+          if (tr != 0.f)
+            rad += tr * (f0 * prev[si + qs[0]] + f1 * prev[si + qs[1]] + f2 * prev[si + qs[2]] + f3 * prev[si + qs[3]]);
           a.raddo[(size_t)p * ldo + col] = rad;
         }
-        cur[(r * nV + v) * nc + c] = rad;
+        cur[si] = rad; cur[rsz + si] = s1 * e1; cur[2 * rsz + sp] = e1;
+        if (push && r == push_row) {
+          const int hp = (halo_lr + 1) * nV + v, hi = hp * nc + c;
+          ccur[hi] = rad; ccur[rsz + hi] = s1 * e1; ccur[2 * rsz + hp] = e1;
+        }
         if (more) {  // this pair's values in the next plane
-          const int pn = An * G.sa + u * G.su + v * G.sv;
-          if (fixed_at(An, u, v)) {
-            ps[j] = __ldg(a.raddo + (size_t)pn * ldo + col);
-          } else {
-            ps[j] = __ldg(a.srcdo + (size_t)pn * ldo + col);
-            pe[j] = __ldg(a.text + pn);
-          }
+          const int pn = p + G.da * G.sa;
+          ps[j] = __ldg(a.srcdo + (size_t)pn * ldo + col);
+          pe[j] = __ldg(a.text + pn);
+          if (pfn || ((uvfix >> j) & 1)) pr[j] = __ldg(a.raddo + (size_t)pn * ldo + col);
         }
       }
+      v += tpc;
+      while (v >= nV) { v -= nV; ++r; }
     }
-    cl.sync();  // plane t is in every strip's current buffer; the previous buffers are free
+    cl.sync();  // plane t is in every strip's current buffer and halo row; the previous buffers are free
   }
 }
 
@@ -3142,42 +3189,68 @@ static void fill_sizes(const Plan &P, shdom_sizes *o) {
 }
 
 // Units and cluster shape of the plane march of each hemisphere that has
-// one: 16-CTA clusters (8 where the device allows no larger), each group
-// split into column slices of roughly equal work so that there are about
-// two CTAs per SM.  A hemisphere whose units cannot be launched on this
-// device keeps the level schedule.
+// one.  Of 16-CTA and 8-CTA clusters the shape with more CTAs resident at
+// once is taken; the groups are split into column slices of roughly equal
+// work, as many units as clusters fit on the device at once, so that the
+// march runs as one wave.  A hemisphere whose units cannot be launched on
+// this device keeps the level schedule.
+constexpr size_t kMarchSmemCap = 110 * 1024;  // two CTAs per SM
+
+static int march_max_clusters(int cs, size_t smem) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = cs; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3((unsigned)cs); cfg.blockDim = dim3(MT); cfg.dynamicSmemBytes = smem;
+  cfg.attrs = at; cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, k_sweep_march, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
 static void setup_march(Handle &H) {
   Plan &P = H.P;
-  int dev = 0, clus = 0, nsm = 0, maxsm = 0;
+  int dev = 0, clus = 0, maxsm = 0;
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&clus, cudaDevAttrClusterLaunch, dev));
   CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  H.march[0] = H.march[1] = false;
+  if (!clus || (size_t)maxsm < kMarchSmemCap) return;
+  CK(cudaFuncSetAttribute(k_sweep_march, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm));
+  const bool big = cudaFuncSetAttribute(k_sweep_march, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+  if (!big) cudaGetLastError();
+  // resident clusters of each shape at the shared-memory cap
+  int best_cs = 0, best_n = 0;
+  for (int cs : {16, 8}) {
+    if (cs > 8 && !big) continue;
+    const int n = march_max_clusters(cs, kMarchSmemCap);
+    if (n * cs > best_n * best_cs) { best_cs = cs; best_n = n; }
+  }
+  if (best_n < 1) return;
   for (int h = 0; h < 2; ++h) {
-    H.march[h] = false;
-    if (P.march[h].empty() || H.seq[h] || !clus) continue;
-    for (int cs : {16, 8}) {
-      if (cs > 8 && cudaFuncSetAttribute(k_sweep_march, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
-        cudaGetLastError();
-        continue;
-      }
+    if (P.march[h].empty() || H.seq[h]) continue;
+    for (int cs : {best_cs, best_cs == 16 ? 8 : 0}) {
+      if (cs == 0) break;
+      const int nclusters = march_max_clusters(cs, kMarchSmemCap);
+      if (nclusters < 1) continue;
       // work of each group: planes x plane points x columns
       double tot = 0;
       for (const MarchGrp &g : P.march[h]) tot += (double)g.nA * g.nU * g.nV * g.ncol;
-      const int target_units = std::max(1, 2 * nsm / cs);
       std::vector<MarchUnit> units;
       size_t smem = 0;
       for (size_t gi = 0; gi < P.march[h].size(); ++gi) {
         const MarchGrp &g = P.march[h][gi];
         const double w = (double)g.nA * g.nU * g.nV * g.ncol;
-        int nsl = std::max(1, (int)std::lround(target_units * w / tot));
+        int nsl = std::max(1, (int)std::floor(nclusters * w / tot));
         nsl = std::min(nsl, g.ncol);
         const int tw = (g.nU + cs - 1) / cs;
-        // every thread of a CTA takes one column and at most MK (row, v) pairs of
-        // its strip; a CTA's two radiance planes fit a third of an SM's shared memory
+        // every thread of a CTA takes one column and at most MK (row, v) pairs of its strip
         auto fits = [&](int nc) {
           const int tpc = MT / nc;
-          return (tw * g.nV + tpc - 1) / tpc <= MK && march_smem_bytes(tw, g.nV, nc) <= 72 * 1024;
+          return tpc >= 1 && (tw * g.nV + tpc - 1) / tpc <= MK && march_smem_bytes(tw, g.nV, nc) <= kMarchSmemCap;
         };
         while (nsl < g.ncol && !fits((g.ncol + nsl - 1) / nsl)) ++nsl;
         if (!fits((g.ncol + nsl - 1) / nsl)) { units.clear(); break; }
@@ -3191,18 +3264,6 @@ static void setup_march(Handle &H) {
         }
       }
       if (units.empty()) continue;
-      CK(cudaFuncSetAttribute(k_sweep_march, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm));
-      cudaLaunchConfig_t cfg = {};
-      cudaLaunchAttribute at[1];
-      at[0].id = cudaLaunchAttributeClusterDimension;
-      at[0].val.clusterDim.x = cs; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
-      cfg.gridDim = dim3((unsigned)(units.size() * cs)); cfg.blockDim = dim3(MT); cfg.dynamicSmemBytes = smem;
-      cfg.attrs = at; cfg.numAttrs = 1;
-      int nclusters = 0;
-      if (cudaOccupancyMaxActiveClusters(&nclusters, k_sweep_march, &cfg) != cudaSuccess || nclusters < 1) {
-        cudaGetLastError();
-        continue;
-      }
       std::vector<MarchGrp> grps(P.march[h].begin(), P.march[h].end());
       H.mgrp[h].upload(grps);
       H.munit[h].upload(units);
