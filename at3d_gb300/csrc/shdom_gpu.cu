@@ -297,7 +297,9 @@ __device__ __forceinline__ void rec_load(const SweepArgs &a, const IrrRec &rec, 
 }
 
 // Source integral over one cell (the reference's linear-in-tau source
-// approximation, with the large-tau limiting form).
+// approximation, with the large-tau limiting form).  Quotients use the
+// fast reciprocal-based division (2 ulp), which keeps the integral free of
+// the IEEE division's slow-path branches.
 __device__ __forceinline__ void cell_source(float ext0, float srcext0, float ext1, float srcext1, float so,
                                             float &radsrc, float &transcell, bool clamp = true) {
   const float ext = 0.5f * (ext0 + ext1), tau = ext * so;
@@ -308,12 +310,17 @@ __device__ __forceinline__ void cell_source(float ext0, float srcext0, float ext
     transcell = 1.f - abscell;
   }
   if (tau <= 2.f) {
-    src = (ext == 0.f) ? 0.f : (0.5f * (srcext0 + srcext1) + 0.08333333333f * (ext0 * srcext1 - ext1 * srcext0) * so) / ext;
+    src = (ext == 0.f) ? 0.f
+                       : __fdividef(0.5f * (srcext0 + srcext1) + 0.08333333333f * (ext0 * srcext1 - ext1 * srcext0) * so, ext);
   } else {
     float ext0p = ext0, srcext0p = srcext0;
-    if (tau > 4.f) { ext0p = ext1 + (ext0 - ext1) * 4.f / tau; if (ext0 > 0.f) srcext0p = srcext0 * ext0p / ext0; }
-    src = 1.f / (ext0p + ext1) *
-          (srcext0p + srcext1 + (ext0p * srcext1 - ext1 * srcext0p) * 2.f / (ext0p + ext1) * (1.f - 2.f / tau + 2.f * transcell / abscell));
+    if (tau > 4.f) {
+      ext0p = ext1 + __fdividef((ext0 - ext1) * 4.f, tau);
+      if (ext0 > 0.f) srcext0p = __fdividef(srcext0 * ext0p, ext0);
+    }
+    const float rs = __fdividef(1.f, ext0p + ext1);
+    src = rs * (srcext0p + srcext1 + (ext0p * srcext1 - ext1 * srcext0p) * 2.f * rs *
+                                         (1.f - __fdividef(2.f, tau) + __fdividef(2.f * transcell, abscell)));
   }
   if (clamp) src = fmaxf(src, 0.f);  // the I source only; Q and U keep their sign
   radsrc = src * abscell;
@@ -934,6 +941,9 @@ __global__ void __launch_bounds__(MT, 2) k_sweep_march(SweepArgs a, const MarchG
   int qs[4], qe[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) { qe[k] = G.du[k] * nV + G.dv[k]; qs[k] = qe[k] * nc; }
+  // pair j sits at strip point k0 + j tpc: buffer point sp0 + j tpc, item si0 + j tpc nc
+  const int sp0 = k0 + nV, si0 = sp0 * nc + c, sstep = tpc * nc;
+  const int pb0 = (u0 + r0) * G.su + v0 * G.sv;  // pair 0's point index less the plane's
   cl.sync();
   for (int t = 1; t < G.nA; ++t) {
     const int A = G.a0 + t * G.da, An = A + G.da;
@@ -944,49 +954,50 @@ __global__ void __launch_bounds__(MT, 2) k_sweep_march(SweepArgs a, const MarchG
     float *ccur = push ? cons_buf0 + (t & 1) * bsz : nullptr;
     const float4 g2 = gz;
     if (more) gz = load_gz(An);
-    int r = r0, v = v0;
+    // the plane's radiances from the previous plane, into shared memory,
+    // and each pair's inputs in the next plane into registers
+    const int Aoff = A * G.sa, step_n = G.da * G.sa;
+    {
+      int r = r0, v = v0, pb = pb0;
 #pragma unroll
-    for (int j = 0; j < MK; ++j) {
-      if (j < kn) {
-        const int sp = (r + 1) * nV + v, si = sp * nc + c;
-        const int p = A * G.sa + (u0 + r) * G.su + v * G.sv;
-        const float s1 = ps[j], e1 = pe[j];
-        float rad;
-        if (pf || ((uvfix >> j) & 1)) {
-          rad = pr[j];
-        } else if (!((valid >> j) & 1)) {
-          atomicCAS(a.err, ERR_NONE, ERR_SWEEP_NOFACE);
-          rad = 0.f;
-          a.raddo[(size_t)p * ldo + col] = rad;
-        } else {
-          const float4 g = G.cls == 2 ? g2 : sgeo[v * nc + c];
-          const float fu = g.y, fv = g.z;
-          const float f0 = (1.f - fu) * (1.f - fv), f1 = (1.f - fu) * fv, f2 = fu * (1.f - fv), f3 = fu * fv;
-          const float ext0 = f0 * prev[2 * rsz + sp + qe[0]] + f1 * prev[2 * rsz + sp + qe[1]] +
-                             f2 * prev[2 * rsz + sp + qe[2]] + f3 * prev[2 * rsz + sp + qe[3]];
-          const float srcext0 = f0 * prev[rsz + si + qs[0]] + f1 * prev[rsz + si + qs[1]] +
-                                f2 * prev[rsz + si + qs[2]] + f3 * prev[rsz + si + qs[3]];
-          float radsrc, tr;
-          cell_source(ext0, srcext0, e1, e1 * s1, g.x, radsrc, tr, clamp);
-          rad = radsrc;
-          if (tr != 0.f)
-            rad += tr * (f0 * prev[si + qs[0]] + f1 * prev[si + qs[1]] + f2 * prev[si + qs[2]] + f3 * prev[si + qs[3]]);
-          a.raddo[(size_t)p * ldo + col] = rad;
+      for (int j = 0; j < MK; ++j) {
+        if (j < kn) {
+          const int sp = sp0 + j * tpc, si = si0 + j * sstep;
+          const float s1 = ps[j], e1 = pe[j];
+          float rad;
+          if (pf || ((uvfix >> j) & 1)) {
+            rad = pr[j];
+          } else if (!((valid >> j) & 1)) {
+            atomicCAS(a.err, ERR_NONE, ERR_SWEEP_NOFACE);
+            rad = 0.f;
+          } else {
+            const float4 g = G.cls == 2 ? g2 : sgeo[v * nc + c];
+            const float fu = g.y, fv = g.z;
+            const float f0 = (1.f - fu) * (1.f - fv), f1 = (1.f - fu) * fv, f2 = fu * (1.f - fv), f3 = fu * fv;
+            const float *pe_ = prev + 2 * rsz + sp, *ps_ = prev + rsz + si, *pr_ = prev + si;
+            const float ext0 = f0 * pe_[qe[0]] + f1 * pe_[qe[1]] + f2 * pe_[qe[2]] + f3 * pe_[qe[3]];
+            const float srcext0 = f0 * ps_[qs[0]] + f1 * ps_[qs[1]] + f2 * ps_[qs[2]] + f3 * ps_[qs[3]];
+            float radsrc, tr;
+            cell_source(ext0, srcext0, e1, e1 * s1, g.x, radsrc, tr, clamp);
+            rad = radsrc;
+            if (tr != 0.f) rad += tr * (f0 * pr_[qs[0]] + f1 * pr_[qs[1]] + f2 * pr_[qs[2]] + f3 * pr_[qs[3]]);
+          }
+          if (!(pf || ((uvfix >> j) & 1))) a.raddo[(size_t)(Aoff + pb) * ldo + col] = rad;
+          cur[si] = rad; cur[rsz + si] = s1 * e1; cur[2 * rsz + sp] = e1;
+          if (push && r == push_row) {
+            const int hp = (halo_lr + 1) * nV + v, hi = hp * nc + c;
+            ccur[hi] = rad; ccur[rsz + hi] = s1 * e1; ccur[2 * rsz + hp] = e1;
+          }
+          if (more) {
+            const int pn = Aoff + pb + step_n;
+            ps[j] = __ldg(a.srcdo + (size_t)pn * ldo + col);
+            pe[j] = __ldg(a.text + pn);
+            if (pfn || ((uvfix >> j) & 1)) pr[j] = __ldg(a.raddo + (size_t)pn * ldo + col);
+          }
         }
-        cur[si] = rad; cur[rsz + si] = s1 * e1; cur[2 * rsz + sp] = e1;
-        if (push && r == push_row) {
-          const int hp = (halo_lr + 1) * nV + v, hi = hp * nc + c;
-          ccur[hi] = rad; ccur[rsz + hi] = s1 * e1; ccur[2 * rsz + hp] = e1;
-        }
-        if (more) {  // this pair's values in the next plane
-          const int pn = p + G.da * G.sa;
-          ps[j] = __ldg(a.srcdo + (size_t)pn * ldo + col);
-          pe[j] = __ldg(a.text + pn);
-          if (pfn || ((uvfix >> j) & 1)) pr[j] = __ldg(a.raddo + (size_t)pn * ldo + col);
-        }
+        v += tpc; pb += tpc * G.sv;
+        while (v >= nV) { v -= nV; ++r; pb += G.su - nV * G.sv; }
       }
-      v += tpc;
-      while (v >= nV) { v -= nV; ++r; }
     }
     cl.sync();  // plane t is in every strip's current buffer and halo row; the previous buffers are free
   }

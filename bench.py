@@ -39,6 +39,9 @@ NWAVE = 4
 # from ncu on the 96x96x48 field (2.195 GB for 73.5M point-ordinates);
 # profiles/k_sweep_levels_cloud_field_96x96x48.md.
 LEVELS_DRAM_BYTES_PER_ITEM = 29.9
+# The same for one k_sweep_march launch (ncu on the 96x96x48 field);
+# profiles/k_sweep_march_cloud_field_96x96x48.md.
+MARCH_DRAM_BYTES_PER_ITEM = None
 
 
 def scenes(args):
@@ -188,7 +191,9 @@ def gb300_arm(args, rank, ws):
     e2e = {"value": ws * args.nwave / (e2e_ms / 1e3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms}
 
-    # ---- roofline of the dominant kernel: the sweep's level pass (k_sweep_levels)
+    # ---- roofline of the dominant kernel: the sweep's phase-2 pass, the plane
+    # march (k_sweep_march) where both hemispheres march, else the level pass
+    # (k_sweep_levels)
     s0 = rtes[0].sizes
     npts, nlm, nang = s0["npts"], s0["nlm"], s0["nang"]
     total_iters = sum(iters)
@@ -198,17 +203,26 @@ def gb300_arm(args, rank, ws):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     nsweeps = max(1.0, sweep_parts[2])
     items = npts * (nang / 2.0)                # point-ordinates of one hemisphere
-    alg = 12.0 * items                         # (radsrc, tr) read + radiance write per point-ordinate
-    levels_ms = sweep_parts[1] / nsweeps       # mean CUDA-event time of one level-pass launch
-    achieved = alg / (levels_ms / 1e3) / 1e9
-    # DRAM bytes per launch from ncu (96x96x48 capture, 29.9 bytes per point-ordinate), scaled
-    traffic = LEVELS_DRAM_BYTES_PER_ITEM * items
-    roofline = {"kernel": "k_sweep_levels", "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+    march = s0.get("march", 0) == 3 and rtes[0].sweep_mode != "levels_only"
+    if march:
+        # ordinate source read + radiance write per point-ordinate (the
+        # source pass is fused; extinction and face geometry are per point)
+        alg = 8.0 * items
+        per_item = MARCH_DRAM_BYTES_PER_ITEM
+        kernel, p1_name, p2_name = "k_sweep_march", "phase1", "plane_march"
+    else:
+        alg = 12.0 * items                     # (radsrc, tr) read + radiance write per point-ordinate
+        per_item = LEVELS_DRAM_BYTES_PER_ITEM
+        kernel, p1_name, p2_name = "k_sweep_levels", "phase1_and_source_pass", "level_pass"
+    p2_ms = sweep_parts[1] / nsweeps           # mean CUDA-event time of one phase-2 launch
+    achieved = alg / (p2_ms / 1e3) / 1e9
+    # DRAM bytes per launch from ncu (96x96x48 capture, bytes per point-ordinate), scaled
+    traffic = per_item * items if per_item else None
+    roofline = {"kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "traffic": traffic, "alg_bytes_per_launch": alg,
-                "ms_per_launch": levels_ms, "peak_source": "measured" if peaks else "fallback",
+                "ms_per_launch": p2_ms, "peak_source": "measured" if peaks else "fallback",
                 "phase_ms_per_iter": {n: float(phase[i] / max(1, total_iters)) for i, n in enumerate(names)},
-                "sweep_ms_per_hemisphere": {"phase1_and_source_pass": float(sweep_parts[0] / nsweeps),
-                                            "level_pass": float(levels_ms)}}
+                "sweep_ms_per_hemisphere": {p1_name: float(sweep_parts[0] / nsweeps), p2_name: float(p2_ms)}}
     # the whole iteration against the per-iteration algorithmic bytes of the scope table:
     # 4 NPTS (NLM (4 + 2 accel) + 8)
     it_ms = phase[4] / max(1, total_iters)
@@ -680,11 +694,14 @@ def reference_arm(args, rank, ws):
 
 
 def config_dict(args):
-    return {"workload": f"4-wavelength scalar SHDOM {args.nx}x{args.nx}x{args.nz}, NMU=16 NPHI=32, "
+    return {"workload": f"{args.nwave}-wavelength scalar SHDOM {args.nx}x{args.nx}x{args.nz}, NMU=16 NPHI=32, "
                         f"{args.npix}x{args.npix}x9 renders per wavelength",
-            "grid": [args.nx, args.nx, args.nz], "wavelengths": NWAVE, "nmu": 16, "nphi": 32,
+            "grid": [args.nx, args.nx, args.nz], "wavelengths": args.nwave, "nmu": 16, "nphi": 32,
             "boundary": args.boundary, "solution_accuracy": args.solacc,
             "rays_per_wavelength": args.npix * args.npix * 9,
+            "transform_mode": "tf32x3 (SH<->DO transforms on tcgen05 tensor cores, 3-product TF32 split, "
+                              "FP32-level accuracy)",
+            "sweep": "plane march (open boundaries) / level schedule / reference order (periodic), per hemisphere",
             "l2": "inputs larger than L2 (about 6 GB of state per wavelength)"}
 
 
