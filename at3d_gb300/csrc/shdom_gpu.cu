@@ -2187,6 +2187,27 @@ __device__ __forceinline__ void ylm_dir_warp(float *y, float x, float phf, int m
   }
 }
 
+// The ray's direction for the cell walk, in FP32: direction cosines,
+// their inverses (1e6 where a cosine is below 1e-6 and set to zero, as the
+// reference's INTEGRATE_1RAY) and the octant bits.
+struct RayDir {
+  float c[3], ci[3];
+  int bit[3], ioct;
+};
+__device__ __forceinline__ RayDir ray_dir(double mu2, double phi2) {
+  const double pi = 3.141592653589793;
+  const double st = sqrt(1.0 - mu2 * mu2);
+  double c[3] = {st * cos(phi2 - pi), st * sin(phi2 - pi), -mu2};
+  RayDir r;
+  for (int k = 0; k < 3; ++k) {
+    double ci;
+    if (fabs(c[k]) > 1e-6) ci = 1.0 / c[k]; else { c[k] = 0.0; ci = 1e6; }
+    r.c[k] = (float)c[k]; r.ci[k] = (float)ci; r.bit[k] = c[k] < 0;
+  }
+  r.ioct = r.bit[0] + 2 * r.bit[1] + 4 * r.bit[2];
+  return r;
+}
+
 template <bool BRDF>
 __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
   __shared__ float ydir[RWARPS][RNLM];
@@ -2229,22 +2250,24 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
     int J = min(a.nscatangle - 1, (int)F);
     sf = F - J; sj = J - 1;
   }
-  double cx = sqrt(1.0 - mu2 * mu2) * cos(phi2 - pi), cy = sqrt(1.0 - mu2 * mu2) * sin(phi2 - pi), cz = -mu2;
-  double cxinv, cyinv, czinv;
-  if (fabs(cx) > 1e-6) cxinv = 1.0 / cx; else { cx = 0; cxinv = 1e6; }
-  if (fabs(cy) > 1e-6) cyinv = 1.0 / cy; else { cy = 0; cyinv = 1e6; }
-  if (fabs(cz) > 1e-6) czinv = 1.0 / cz; else { cz = 0; czinv = 1e6; }
-  const int bitx = cx < 0, bity = cy < 0, bitz = cz < 0, ioct0 = bitx + 2 * bity + 4 * bitz;
+  RayDir rd = ray_dir(mu2, phi2);
+  const int ioct0 = rd.ioct;
   const float xm = 0.5f * (a.xgrid[0] + a.xgrid[a.nx - 1]), ym = 0.5f * (a.ygrid[0] + a.ygrid[a.ny - 1]);
   double xe = x0, ye = y0, ze = z0;
   int cell = locate_cell(a, xe, ye, ze);
-  const double eps = 1.0e-5 * (a.gridpos[3 * a.gridptr[7] + 2] - a.gridpos[3 * a.gridptr[0] + 2]);
+  // the position as the cell's low corner (grid coordinates) plus an FP32 offset
+  float lx, ly, lz;
+  if (cell >= 0) {
+    const float *P = a.gridpos + 3 * a.gridptr[8 * (size_t)cell];
+    lx = (float)(xe - P[0]); ly = (float)(ye - P[1]); lz = (float)(ze - P[2]);
+  }
+  const float eps = 1.0e-5f * (a.gridpos[3 * a.gridptr[7] + 2] - a.gridpos[3 * a.gridptr[0] + 2]);
   const int maxcross = 500 * max(a.nx, max(a.ny, a.nz));
   int oldp[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
   float osrc[8] = {0};
   float ext8[8], src8[8];
   double radacc = 0.0, transmit = 1.0;
-  const double inv_tautol = 1.0 / (double)a.tautol;
+  const float inv_tautol = 1.0f / a.tautol;
   int ngrid = 0;
   bool validrad = false;
   const int grp = lane >> 2, gl = lane & 3;  // 8 groups of 4 lanes, one corner per group
@@ -2300,33 +2323,35 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
     const float *P1 = a.gridpos + 3 * ip1, *P2 = a.gridpos + 3 * ip2;
     const float delx = P2[0] - P1[0], dely = P2[1] - P1[1], delz = P2[2] - P1[2];
     const float idx = delx <= 0.f ? 1.f : 1.f / delx, idy = dely <= 0.f ? 1.f : 1.f / dely, idz = 1.f / delz;
-    // Positions and path lengths stay in FP64 (as the reference's); the
-    // trilinear weights are cell-relative coordinates in [0, 1] and the
-    // blend runs in FP32 (GB300's FP64 rate is a small fraction of FP32's).
+    // The geometry of the step runs in FP32 on cell-relative offsets (an
+    // offset from the cell's own corner keeps FP32's relative precision on
+    // the cell size); only the two ray accumulators stay FP64.  The
+    // trilinear weights are cell-relative coordinates in [0, 1].
     auto tri = [&](const float *v, float u, float vv, float ww) {
       const float a0 = fmaf(u, v[1] - v[0], v[0]), a1 = fmaf(u, v[3] - v[2], v[2]);
       const float a2 = fmaf(u, v[5] - v[4], v[4]), a3 = fmaf(u, v[7] - v[6], v[6]);
       const float b0 = fmaf(vv, a1 - a0, a0), b1 = fmaf(vv, a3 - a2, a2);
       return fmaf(ww, b1 - b0, b0);
     };
-    const float u0 = (float)(xe - P1[0]) * idx, v0 = (float)(ye - P1[1]) * idy, w0 = (float)(ze - P1[2]) * idz;
+    const float u0 = lx * idx, v0 = ly * idy, w0 = lz * idz;
     float srcext1 = fmaxf(0.f, tri(src8, u0, v0, w0));
     float ext1 = tri(ext8, u0, v0, w0);
     const int cf = a.cellflags[cell];
-    bool ipinx = (cf & 1) && !((a.bcflag & 1) && ((cx > 0 && xe < xm) || (cx < 0 && xe > xm)));
-    bool ipiny = (cf & 2) && !((a.bcflag & 2) && ((cy > 0 && ye < ym) || (cy < 0 && ye > ym)));
-    const int iopp = g[7 - ioct0];
-    double sox = ipinx ? 1e20 : (a.gridpos[3 * iopp] - xe) * cxinv;
-    double soy = ipiny ? 1e20 : (a.gridpos[3 * iopp + 1] - ye) * cyinv;
-    double soz = (a.gridpos[3 * iopp + 2] - ze) * czinv;
-    double so = fmin(sox, fmin(soy, soz));
+    const float cx = rd.c[0], cy = rd.c[1], cz = rd.c[2];
+    bool ipinx = (cf & 1) && !((a.bcflag & 1) && ((cx > 0 && P1[0] + lx < xm) || (cx < 0 && P1[0] + lx > xm)));
+    bool ipiny = (cf & 2) && !((a.bcflag & 2) && ((cy > 0 && P1[1] + ly < ym) || (cy < 0 && P1[1] + ly > ym)));
+    const float *Po = a.gridpos + 3 * g[7 - ioct0];
+    const float sox = ipinx ? 1e20f : ((Po[0] - P1[0]) - lx) * rd.ci[0];
+    const float soy = ipiny ? 1e20f : ((Po[1] - P1[1]) - ly) * rd.ci[1];
+    const float soz = ((Po[2] - P1[2]) - lz) * rd.ci[2];
+    const float so = fminf(sox, fminf(soy, soz));
     if (so < -eps) { if (lane == 0) atomicCAS(a.err, ERR_NONE, ERR_RAY_SO); break; }
-    double xn = xe + so * cx, yn = ye + so * cy, zn = ze + so * cz;
+    const float lxn = fmaf(so, cx, lx), lyn = fmaf(so, cy, ly), lzn = fmaf(so, cz, lz);
     // per unit path length, the cell-relative coordinates move by (du, dv, dw)
-    const float du = (float)cx * idx, dv = (float)cy * idy, dw = (float)cz * idz;
-    const float sof = (float)so;
+    const float du = cx * idx, dv = cy * idy, dw = cz * idz;
+    const float sof = so;
     float extn = tri(ext8, fmaf(sof, du, u0), fmaf(sof, dv, v0), fmaf(sof, dw, w0));
-    double taugrid = so * 0.5 * (ext1 + extn);
+    const float taugrid = so * 0.5f * (ext1 + extn);
     int ntau = max(1, 1 + (int)(taugrid * inv_tautol));
     const float delsf = sof / (float)ntau;
     // the cell's source integral and transmission from its entry, in FP32;
@@ -2354,16 +2379,12 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
     transmit *= (double)ctr;
     int iface, jface;
     bool openbc;
-    if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; openbc = (cf & 1) && (a.bcflag & 1); }
-    else if (soy <= soz) { iface = 3 - bity; jface = 1; openbc = (cf & 2) && (a.bcflag & 2); }
-    else { iface = 5 - bitz; jface = 2; openbc = false; }
+    if (sox <= soz && sox <= soy) { iface = 1 - rd.bit[0]; jface = 0; openbc = (cf & 1) && (a.bcflag & 1); }
+    else if (soy <= soz) { iface = 3 - rd.bit[1]; jface = 1; openbc = (cf & 2) && (a.bcflag & 2); }
+    else { iface = 5 - rd.bit[2]; jface = 2; openbc = false; }
     int nxt = a.neighptr[6 * (size_t)cell + iface];
     int kface = iface, kc = cell;
     if (openbc) { kface = iface ^ 1; kc = nxt; iface = -1; }
-    if (nxt >= 0) {
-      const float *q = a.gridpos + 3 * a.gridptr[8 * (size_t)nxt + ioct0];
-      if (jface == 0) xn = q[0]; else if (jface == 1) yn = q[1]; else zn = q[2];
-    }
     if (transmit < a.transcut || ngrid > maxcross) {
       validrad = true;
     } else if (nxt < 0 && iface >= 4) {
@@ -2386,14 +2407,20 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render(RenderArgs a) {
           }
         }
       }
-      float uu = (xs[1] - xs[0] > 0) ? (float)((xn - xs[0]) / (xs[1] - xs[0])) : 0.f;
-      float vv = (ys[2] - ys[0] > 0) ? (float)((yn - ys[0]) / (ys[2] - ys[0])) : 0.f;
+      float uu = (xs[1] - xs[0] > 0) ? ((P1[0] - xs[0]) + lxn) / (xs[1] - xs[0]) : 0.f;
+      float vv = (ys[2] - ys[0] > 0) ? ((P1[1] - ys[0]) + lyn) / (ys[2] - ys[0]) : 0.f;
       if (!a.nosurface)
         radacc += transmit * ((1 - uu) * (1 - vv) * rb[0] + uu * (1 - vv) * rb[1] + (1 - uu) * vv * rb[2] + uu * vv * rb[3]);
     } else {
+      // into the next cell: offsets from its corner, the crossed face's
+      // coordinate taken from the grid
+      const float *Pn = a.gridpos + 3 * a.gridptr[8 * (size_t)nxt];
+      const float *q = a.gridpos + 3 * a.gridptr[8 * (size_t)nxt + ioct0];
+      lx = jface == 0 ? q[0] - Pn[0] : (P1[0] - Pn[0]) + lxn;
+      ly = jface == 1 ? q[1] - Pn[1] : (P1[1] - Pn[1]) + lyn;
+      lz = jface == 2 ? q[2] - Pn[2] : (P1[2] - Pn[2]) + lzn;
       cell = nxt;
     }
-    xe = xn; ye = yn; ze = zn;
   }
   if (lane == 0) a.out[ray] = (float)radacc;
 }
@@ -2525,22 +2552,24 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render_pol(RenderArgs a) {
     cos22 = (float)(1.0 - 2.0 * sin2 * sin2);
     sin22 = (float)(2.0 * sin2 * cos2);
   }
-  double cx = sqrt(1.0 - mu2 * mu2) * cos(phi2 - pi), cy = sqrt(1.0 - mu2 * mu2) * sin(phi2 - pi), cz = -mu2;
-  double cxinv, cyinv, czinv;
-  if (fabs(cx) > 1e-6) cxinv = 1.0 / cx; else { cx = 0; cxinv = 1e6; }
-  if (fabs(cy) > 1e-6) cyinv = 1.0 / cy; else { cy = 0; cyinv = 1e6; }
-  if (fabs(cz) > 1e-6) czinv = 1.0 / cz; else { cz = 0; czinv = 1e6; }
-  const int bitx = cx < 0, bity = cy < 0, bitz = cz < 0, ioct0 = bitx + 2 * bity + 4 * bitz;
+  RayDir rd = ray_dir(mu2, phi2);
+  const int ioct0 = rd.ioct;
   const float xm = 0.5f * (a.xgrid[0] + a.xgrid[a.nx - 1]), ym = 0.5f * (a.ygrid[0] + a.ygrid[a.ny - 1]);
   double xe = x0, ye = y0, ze = z0;
   int cell = locate_cell(a, xe, ye, ze);
-  const double eps = 1.0e-5 * (a.gridpos[3 * a.gridptr[7] + 2] - a.gridpos[3 * a.gridptr[0] + 2]);
+  // the position as the cell's low corner (grid coordinates) plus an FP32 offset (as k_render)
+  float lx, ly, lz;
+  if (cell >= 0) {
+    const float *P = a.gridpos + 3 * a.gridptr[8 * (size_t)cell];
+    lx = (float)(xe - P[0]); ly = (float)(ye - P[1]); lz = (float)(ze - P[2]);
+  }
+  const float eps = 1.0e-5f * (a.gridpos[3 * a.gridptr[7] + 2] - a.gridpos[3 * a.gridptr[0] + 2]);
   const int maxcross = 500 * max(a.nx, max(a.ny, a.nz));
   int oldp[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
   float osrc[3][8] = {{0}};
   float ext8[8], src8[3][8];
   double radacc[3] = {0.0, 0.0, 0.0}, transmit = 1.0;
-  const double inv_tautol = 1.0 / (double)a.tautol;
+  const float inv_tautol = 1.0f / a.tautol;
   const int nl = a.nl;
   int ngrid = 0;
   bool validrad = false;
@@ -2613,26 +2642,27 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render_pol(RenderArgs a) {
       const float b0 = fmaf(vv, a1 - a0, a0), b1 = fmaf(vv, a3 - a2, a2);
       return fmaf(ww, b1 - b0, b0);
     };
-    const float u0 = (float)(xe - P1[0]) * idx, v0 = (float)(ye - P1[1]) * idy, w0 = (float)(ze - P1[2]) * idz;
+    const float u0 = lx * idx, v0 = ly * idy, w0 = lz * idz;
     float srcext1[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) srcext1[c] = tri(src8[c], u0, v0, w0);
     srcext1[0] = fmaxf(0.f, srcext1[0]);
     float ext1 = tri(ext8, u0, v0, w0);
     const int cf = a.cellflags[cell];
-    bool ipinx = (cf & 1) && !((a.bcflag & 1) && ((cx > 0 && xe < xm) || (cx < 0 && xe > xm)));
-    bool ipiny = (cf & 2) && !((a.bcflag & 2) && ((cy > 0 && ye < ym) || (cy < 0 && ye > ym)));
-    const int iopp = g[7 - ioct0];
-    double sox = ipinx ? 1e20 : (a.gridpos[3 * iopp] - xe) * cxinv;
-    double soy = ipiny ? 1e20 : (a.gridpos[3 * iopp + 1] - ye) * cyinv;
-    double soz = (a.gridpos[3 * iopp + 2] - ze) * czinv;
-    double so = fmin(sox, fmin(soy, soz));
+    const float cx = rd.c[0], cy = rd.c[1], cz = rd.c[2];
+    bool ipinx = (cf & 1) && !((a.bcflag & 1) && ((cx > 0 && P1[0] + lx < xm) || (cx < 0 && P1[0] + lx > xm)));
+    bool ipiny = (cf & 2) && !((a.bcflag & 2) && ((cy > 0 && P1[1] + ly < ym) || (cy < 0 && P1[1] + ly > ym)));
+    const float *Po = a.gridpos + 3 * g[7 - ioct0];
+    const float sox = ipinx ? 1e20f : ((Po[0] - P1[0]) - lx) * rd.ci[0];
+    const float soy = ipiny ? 1e20f : ((Po[1] - P1[1]) - ly) * rd.ci[1];
+    const float soz = ((Po[2] - P1[2]) - lz) * rd.ci[2];
+    const float so = fminf(sox, fminf(soy, soz));
     if (so < -eps) { if (lane == 0) atomicCAS(a.err, ERR_NONE, ERR_RAY_SO); break; }
-    double xn = xe + so * cx, yn = ye + so * cy, zn = ze + so * cz;
-    const float du = (float)cx * idx, dv = (float)cy * idy, dw = (float)cz * idz;
-    const float sof = (float)so;
+    const float lxn = fmaf(so, cx, lx), lyn = fmaf(so, cy, ly), lzn = fmaf(so, cz, lz);
+    const float du = cx * idx, dv = cy * idy, dw = cz * idz;
+    const float sof = so;
     float extn = tri(ext8, fmaf(sof, du, u0), fmaf(sof, dv, v0), fmaf(sof, dw, w0));
-    double taugrid = so * 0.5 * (ext1 + extn);
+    const float taugrid = so * 0.5f * (ext1 + extn);
     int ntau = max(1, 1 + (int)(taugrid * inv_tautol));
     const float delsf = sof / (float)ntau;
     float cacc[3] = {0.f, 0.f, 0.f}, ctr = 1.f;  // as in k_render: per cell in FP32, folded once per cell
@@ -2667,16 +2697,12 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render_pol(RenderArgs a) {
     transmit *= (double)ctr;
     int iface, jface;
     bool openbc;
-    if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; openbc = (cf & 1) && (a.bcflag & 1); }
-    else if (soy <= soz) { iface = 3 - bity; jface = 1; openbc = (cf & 2) && (a.bcflag & 2); }
-    else { iface = 5 - bitz; jface = 2; openbc = false; }
+    if (sox <= soz && sox <= soy) { iface = 1 - rd.bit[0]; jface = 0; openbc = (cf & 1) && (a.bcflag & 1); }
+    else if (soy <= soz) { iface = 3 - rd.bit[1]; jface = 1; openbc = (cf & 2) && (a.bcflag & 2); }
+    else { iface = 5 - rd.bit[2]; jface = 2; openbc = false; }
     int nxt = a.neighptr[6 * (size_t)cell + iface];
     int kface = iface, kc = cell;
     if (openbc) { kface = iface ^ 1; kc = nxt; iface = -1; }
-    if (nxt >= 0) {
-      const float *q = a.gridpos + 3 * a.gridptr[8 * (size_t)nxt + ioct0];
-      if (jface == 0) xn = q[0]; else if (jface == 1) yn = q[1]; else zn = q[2];
-    }
     if (transmit < a.transcut || ngrid > maxcross) {
       validrad = true;
     } else if (nxt < 0 && iface >= 4) {
@@ -2700,16 +2726,20 @@ __global__ void __launch_bounds__(RWARPS * 32) k_render_pol(RenderArgs a) {
           }
         }
       }
-      float uu = (xs[1] - xs[0] > 0) ? (float)((xn - xs[0]) / (xs[1] - xs[0])) : 0.f;
-      float vv = (ys[2] - ys[0] > 0) ? (float)((yn - ys[0]) / (ys[2] - ys[0])) : 0.f;
+      float uu = (xs[1] - xs[0] > 0) ? ((P1[0] - xs[0]) + lxn) / (xs[1] - xs[0]) : 0.f;
+      float vv = (ys[2] - ys[0] > 0) ? ((P1[1] - ys[0]) + lyn) / (ys[2] - ys[0]) : 0.f;
       if (!a.nosurface)
         for (int c = 0; c < 3; ++c)
           radacc[c] += transmit * ((1 - uu) * (1 - vv) * rb[c][0] + uu * (1 - vv) * rb[c][1] + (1 - uu) * vv * rb[c][2] +
                                    uu * vv * rb[c][3]);
     } else {
+      const float *Pn = a.gridpos + 3 * a.gridptr[8 * (size_t)nxt];
+      const float *q = a.gridpos + 3 * a.gridptr[8 * (size_t)nxt + ioct0];
+      lx = jface == 0 ? q[0] - Pn[0] : (P1[0] - Pn[0]) + lxn;
+      ly = jface == 1 ? q[1] - Pn[1] : (P1[1] - Pn[1]) + lyn;
+      lz = jface == 2 ? q[2] - Pn[2] : (P1[2] - Pn[2]) + lzn;
       cell = nxt;
     }
-    xe = xn; ye = yn; ze = zn;
   }
   if (lane < 3) a.out[(size_t)ray * 3 + lane] = (float)radacc[lane];
 }
