@@ -20,7 +20,8 @@ class ShdomSizes(C.Structure):
                 ("bcflag", C.c_int), ("ipflag", C.c_int), ("iters", C.c_int), ("nlevels_down", C.c_int),
                 ("nlevels_up", C.c_int), ("solcrit", C.c_float), ("albmax", C.c_float),
                 ("launches", C.c_longlong), ("device_bytes", C.c_longlong), ("nstokes", C.c_int),
-                ("march", C.c_int)]
+                ("march", C.c_int), ("march_units_down", C.c_int), ("march_units_up", C.c_int),
+                ("march_cluster_down", C.c_int), ("march_cluster_up", C.c_int)]
 
 
 # name -> (restype, argtypes): the exported surface of include/shdom_gb300.h

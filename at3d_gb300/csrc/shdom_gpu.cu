@@ -3227,14 +3227,18 @@ static void fill_sizes(const Plan &P, shdom_sizes *o) {
   o->device_bytes = plan_device_bytes(P);
   o->nstokes = P.nst;
   o->march = (P.march[0].empty() ? 0 : 1) | (P.march[1].empty() ? 0 : 2);
+  o->march_units_down = o->march_units_up = o->march_cluster_down = o->march_cluster_up = 0;
 }
 
 // Units and cluster shape of the plane march of each hemisphere that has
 // one.  Of 16-CTA and 8-CTA clusters the shape with more CTAs resident at
-// once is taken; the groups are split into column slices of roughly equal
-// work, as many units as clusters fit on the device at once, so that the
-// march runs as one wave.  A hemisphere whose units cannot be launched on
-// this device keeps the level schedule.
+// once is taken; the groups are split into column slices in proportion to
+// their work, about as many units as clusters fit on the device at once.
+// (Measured against two other plans: filling whole waves with twice as many
+// narrower units, and the fewest, widest units that fit; both were slower,
+// since a plane's time is mostly the latency of its dependent chain.)  A
+// hemisphere whose units cannot be launched on this device keeps the level
+// schedule.
 constexpr size_t kMarchSmemCap = 110 * 1024;  // two CTAs per SM
 
 static int march_max_clusters(int cs, size_t smem) {
@@ -3263,7 +3267,8 @@ static void setup_march(Handle &H) {
   CK(cudaFuncSetAttribute(k_sweep_march, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm));
   const bool big = cudaFuncSetAttribute(k_sweep_march, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
   if (!big) cudaGetLastError();
-  // resident clusters of each shape at the shared-memory cap
+  // resident clusters of each shape at the shared-memory cap; the shape with
+  // more CTAs resident at once is taken
   int best_cs = 0, best_n = 0;
   for (int cs : {16, 8}) {
     if (cs > 8 && !big) continue;
@@ -3277,7 +3282,10 @@ static void setup_march(Handle &H) {
       if (cs == 0) break;
       const int nclusters = march_max_clusters(cs, kMarchSmemCap);
       if (nclusters < 1) continue;
-      // work of each group: planes x plane points x columns
+      // Column slices per group in proportion to its work (planes x plane
+      // points x columns), about one unit per resident cluster, and at
+      // least as many as fit: every thread of a CTA takes one column and at
+      // most MK (row, v) pairs of its strip.
       double tot = 0;
       for (const MarchGrp &g : P.march[h]) tot += (double)g.nA * g.nU * g.nV * g.ncol;
       std::vector<MarchUnit> units;
@@ -3288,7 +3296,6 @@ static void setup_march(Handle &H) {
         int nsl = std::max(1, (int)std::floor(nclusters * w / tot));
         nsl = std::min(nsl, g.ncol);
         const int tw = (g.nU + cs - 1) / cs;
-        // every thread of a CTA takes one column and at most MK (row, v) pairs of its strip
         auto fits = [&](int nc) {
           const int tpc = MT / nc;
           return tpc >= 1 && (tw * g.nV + tpc - 1) / tpc <= MK && march_smem_bytes(tw, g.nV, nc) <= kMarchSmemCap;
@@ -4541,7 +4548,10 @@ int shdom_get_sizes(shdom_handle *hh, shdom_sizes *o) {
   shdom::fill_sizes(hh->h.P, o);
   o->iters = hh->h.iters; o->solcrit = hh->h.solcrit;
   o->launches = hh->h.launches;
-  o->march = hh->h.march_off ? 0 : ((hh->h.march[0] ? 1 : 0) | (hh->h.march[1] ? 2 : 0));
+  const shdom::Handle &H = hh->h;
+  o->march = H.march_off ? 0 : ((H.march[0] ? 1 : 0) | (H.march[1] ? 2 : 0));
+  o->march_units_down = H.march[0] ? H.mnunits[0] : 0; o->march_units_up = H.march[1] ? H.mnunits[1] : 0;
+  o->march_cluster_down = H.march[0] ? H.mcs[0] : 0; o->march_cluster_up = H.march[1] ? H.mcs[1] : 0;
   return 0;
 }
 

@@ -223,6 +223,10 @@ def gb300_arm(args, rank, ws):
                 "ms_per_launch": p2_ms, "peak_source": "measured" if peaks else "fallback",
                 "phase_ms_per_iter": {n: float(phase[i] / max(1, total_iters)) for i, n in enumerate(names)},
                 "sweep_ms_per_hemisphere": {p1_name: float(sweep_parts[0] / nsweeps), p2_name: float(p2_ms)}}
+    if march:
+        sz = rtes[0].sizes
+        roofline["march_launch"] = {"clusters": [sz["march_units_down"], sz["march_units_up"]],
+                                    "ctas_per_cluster": [sz["march_cluster_down"], sz["march_cluster_up"]]}
     # the whole iteration against the per-iteration algorithmic bytes of the scope table:
     # 4 NPTS (NLM (4 + 2 accel) + 8)
     it_ms = phase[4] / max(1, total_iters)

@@ -44,6 +44,8 @@ typedef struct shdom_sizes {
     long long device_bytes; /* device memory the handle holds (estimate before creation) */
     int nstokes;   /* Stokes components (1, or 3 for I, Q, U) */
     int march;     /* hemispheres swept by the plane march (bit 0 down, bit 1 up; plan: eligible, handle: in use) */
+    int march_units_down, march_units_up;     /* handle: thread-block clusters of each hemisphere's march launch */
+    int march_cluster_down, march_cluster_up; /* handle: CTAs per cluster (16 or 8) */
 } shdom_sizes;
 
 /* Builds the grid, the cell structure, the sweep schedule and the medium on
