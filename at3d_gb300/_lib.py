@@ -40,6 +40,7 @@ SIGNATURES = {
     "shdom_set_transform_mode": (C.c_int, [C.c_void_p, C.c_int]),
     "shdom_set_sweep_mode": (C.c_int, [C.c_void_p, C.c_int]),
     "shdom_set_render_options": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "shdom_set_transform_wait_limit": (C.c_int, [C.c_void_p, C.c_int]),
     "shdom_plan_summary": (C.c_int, [C.c_void_p, C.POINTER(ShdomSizes)]),
     "shdom_levis_gradient": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _f, _f, _f, _d, _d, _f, _d,
                                        C.POINTER(C.c_double), _f]),

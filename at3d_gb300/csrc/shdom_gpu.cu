@@ -2884,6 +2884,7 @@ struct Handle {
   bool march[2] = {false, false};
   bool march_off = false;  // sweep mode 3: the level schedule even where the march applies
   int render_single_scatter = 0, render_nosurface = 0;  // RENDER options of the following renders
+  int tc_wait_limit = tc::kWaitLimit;  // polls of a tensor-core pipeline wait (0 only to test the abort path)
   DBuf<MarchGrp> mgrp[2];
   DBuf<MarchUnit> munit[2];
   int mnunits[2] = {0, 0}, mcs[2] = {0, 0};
@@ -3526,6 +3527,7 @@ static void transform(Handle &H, int dir) {
     Plan &P = H.P;
     tc::Epilogue g{};
     g.M = P.npts; g.err = H.errflag.p; g.split = H.xf_mode == 0 ? 1 : 0;
+    g.wait_limit = H.tc_wait_limit;
     if (dir == 0) {
       g.N = P.nang; g.mode = 0; g.C = H.srcdo.p; g.ldc = H.ldo;
       g.stk = H.nst == 3 ? H.col_stk.p : nullptr;
@@ -4523,6 +4525,21 @@ int shdom_set_sweep_mode(shdom_handle *hh, int mode) {
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
     }
     H.sweep_mode = levels_only ? 0 : mode;
+  } catch (const std::exception &e) {
+    return fail(hh, e.what());
+  }
+  return 0;
+}
+
+int shdom_set_transform_wait_limit(shdom_handle *hh, int limit) {
+  if (!hh) return fail(nullptr, "null handle");
+  if (limit > shdom::tc::kWaitLimit) return fail(hh, "shdom_set_transform_wait_limit: limit above the default");
+  Handle &H = hh->h;
+  DevGuard dg(H.device);
+  try {
+    H.tc_wait_limit = limit < 0 ? shdom::tc::kWaitLimit : limit;
+    for (auto &g : H.iter_graph)  // captured launches hold the old limit
+      if (g) { cudaGraphExecDestroy(g); g = nullptr; }
   } catch (const std::exception &e) {
     return fail(hh, e.what());
   }

@@ -51,6 +51,7 @@ struct Epilogue {
   const int *rowmap;  // output point of each A row (A holds a compacted subset of the points), or null
   const uint8_t *stk; // mode 0: Stokes component per output column (only I, 0, is clamped), or null (all I)
   int ldr;            // mode 1: row stride of R (nlm, or 3 nlm for I, Q, U rows); columns are masked by (col mod nlm) < nr
+  int wait_limit;     // polls of a pipeline wait before the kernel gives up (kWaitLimit; 0 in the abort-path test)
 };
 
 __device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -61,8 +62,8 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (int i = 0; i < kWaitLimit; ++i) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int limit = kWaitLimit) {
+  for (int i = 0; i < limit; ++i) {
     uint32_t ok;
     asm volatile(
         "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
@@ -221,7 +222,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_gemm(const __grid_constant__
       int issued = 0;
       for (int gc = 0; gc < G && !*abort_flag; ++gc) {
         const int s = gc % S;
-        if (gc >= S && !mbar_wait(empty0 + 8 * s, ((gc / S) - 1) & 1)) { *abort_flag = 1; break; }
+        if (gc >= S && !mbar_wait(empty0 + 8 * s, ((gc / S) - 1) & 1, g.wait_limit)) { *abort_flag = 1; break; }
         int m0, n0;
         tile_origin(gc, m0, n0);
         const int kx = (gc % KB) * BK;
@@ -232,10 +233,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_gemm(const __grid_constant__
         tma_load(st + 2 * A_BYTES + B_BYTES, &tmBl, full0 + 8 * s, kx, n0);
         issued = gc + 1;
       }
-      if (*abort_flag) {
-        // let the loads still in flight land before the shared memory is released
-        for (int gc = issued > S ? issued - S : 0; gc < issued; ++gc) mbar_wait(full0 + 8 * (gc % S), (gc / S) & 1);
-      }
+      // Every load issued has landed before the shared memory is released:
+      // the last S issued stages' phases (already complete unless the
+      // consumers gave up before waiting on them).  Unconditional, since
+      // a consumer may give up after this thread left its loop; the full
+      // limit here, whatever the pipeline's.
+      for (int gc = issued > S ? issued - S : 0; gc < issued; ++gc)
+        mbar_wait(full0 + 8 * (gc % S), (gc / S) & 1, kWaitLimit);
     }
   } else if (warp == 1) {
     // ---------------------------------------------------------- MMA issuer
@@ -245,8 +249,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_gemm(const __grid_constant__
       for (int gc = 0; gc < G; ++gc) {
         const int s = gc % S, b = gc & 1;
         if (*abort_flag) break;
-        if (!mbar_wait(split0 + 8 * s, (gc / S) & 1)) { *abort_flag = 1; break; }
-        if (gc >= 2 && !mbar_wait(acce0 + 8 * b, ((gc >> 1) - 1) & 1)) { *abort_flag = 1; break; }
+        if (!mbar_wait(split0 + 8 * s, (gc / S) & 1, g.wait_limit)) { *abort_flag = 1; break; }
+        if (gc >= 2 && !mbar_wait(acce0 + 8 * b, ((gc >> 1) - 1) & 1, g.wait_limit)) { *abort_flag = 1; break; }
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t st = sbase + s * STAGE, dt = tmem + (uint32_t)(b * BN);
 #pragma unroll
@@ -266,9 +270,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_gemm(const __grid_constant__
         mma_commit(empty0 + 8 * s);
         mma_commit(accf0 + 8 * b);
       }
-      // every MMA issued has finished before tensor memory is released
+      // every MMA issued has finished before tensor memory is released (the
+      // full limit here, whatever the pipeline's)
       mma_commit(fin);
-      mbar_wait(fin, 0);
+      mbar_wait(fin, 0, kWaitLimit);
     }
   } else if (warp < 6) {
     // ---------------------------------------------------------- split
@@ -283,7 +288,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_gemm(const __grid_constant__
     }
     for (int gc = 0; gc < G; ++gc) {
       const int s = gc % S, c = gc % KB;
-      const bool go = !*abort_flag && mbar_wait(full0 + 8 * s, (gc / S) & 1);
+      const bool go = !*abort_flag && mbar_wait(full0 + 8 * s, (gc / S) & 1, g.wait_limit);
       if (!__all_sync(0xffffffffu, go)) { *abort_flag = 1; break; }
       uint8_t *arow = smem + s * STAGE + (srow >> 3) * 1024 + swz * 128;
       float4 v[8];
@@ -340,7 +345,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_gemm(const __grid_constant__
     for (int j = 0; j < HALF; ++j) acc[j] = 0.f;
     for (int gc = 0; gc < G; ++gc) {
       const int b = gc & 1;
-      const bool go = !*abort_flag && mbar_wait(accf0 + 8 * b, (gc >> 1) & 1);
+      const bool go = !*abort_flag && mbar_wait(accf0 + 8 * b, (gc >> 1) & 1, g.wait_limit);
       if (!__all_sync(0xffffffffu, go)) { *abort_flag = 1; break; }
       asm volatile("tcgen05.fence::after_thread_sync;");
       const uint32_t ta = tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)(b * BN + half * HALF);

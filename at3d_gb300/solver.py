@@ -394,6 +394,13 @@ class RTE:
         _check(self._h, _lib.lib().shdom_set_transform_mode(self._h, self.TRANSFORM_MODES[mode]))
         self._transform_mode = mode
 
+    def set_transform_wait_limit(self, limit: int):
+        """Polls of each tensor-core pipeline wait before a transform gives
+        up and reports "pipeline wait expired" (the solve raises SHDOMError;
+        the handle stays usable).  A negative limit restores the default; 0
+        makes every transform give up at its first wait, to test that path."""
+        _check(self._h, _lib.lib().shdom_set_transform_wait_limit(self._h, int(limit)))
+
     def timings(self) -> np.ndarray:
         t = np.zeros(5, np.float32)
         _check(self._h, _lib.lib().shdom_last_timings(self._h, _fp(t)))

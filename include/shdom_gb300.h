@@ -191,6 +191,14 @@ int shdom_sweep_timings(shdom_handle *h, float *ms2, int *launches2);
  * RTE.integrate_to_sensor (at3d/solver.py:633, :684-686).  Both 0 by default. */
 int shdom_set_render_options(shdom_handle *h, int single_scatter, int nosurface);
 
+/* Polls of each pipeline wait in the tensor-core transforms before the
+ * kernel gives up, drains the loads and products it has issued, releases
+ * its tensor memory and reports "pipeline wait expired" (the next
+ * shdom_solution_iterations returns 1 with that message; the handle stays
+ * usable).  limit < 0 restores the default; 0 makes every transform give up
+ * at its first wait (for testing that path).  No reference counterpart. */
+int shdom_set_transform_wait_limit(shdom_handle *h, int limit);
+
 /* Arithmetic of the two spherical-harmonic <-> discrete-ordinate transforms
  * of each iteration (SH_TO_DO / DO_TO_SH, src/polarized/shdomsub1.f:2928-3254,
  * which the reference runs in FP32 on the CPU):

@@ -176,6 +176,29 @@ def test_device_error_is_reported_and_handle_stays_usable(rte_cls):
     assert np.array_equal(again, good)
 
 
+def test_transform_wait_limit_abort_path(rte_cls):
+    """The tensor-core transforms' bounded pipeline waits: with a limit of 0
+    polls every transform gives up at its first wait, drains the loads and
+    products it issued, releases its tensor memory and reports error 6; the
+    solve raises SHDOMError with that message.  With the default limit
+    restored, the same handle solves again and its state equals that of a
+    fresh handle."""
+    from at3d_gb300.solver import SHDOMError
+    pb = cloud_blob(seed=3, nx=16, ny=16, nz=12)
+    rays = orthographic_views(pb, 8, 8)
+    ref = rte_cls.from_problem(pb)
+    ref.solve(3, verbose=False)
+    want = ref.render(*rays)
+    r = rte_cls.from_problem(pb)
+    r.set_transform_mode("tf32x3")
+    r.set_transform_wait_limit(0)
+    with pytest.raises(SHDOMError, match="pipeline wait expired"):
+        r.solve(3, verbose=False)
+    r.set_transform_wait_limit(-1)
+    r.solve(3, verbose=False)
+    assert np.array_equal(r.render(*rays), want)
+
+
 def test_odd_ray_count(rte_cls):
     """Host-buffer renders of any ray count (the staged double arrays stay
     8-byte aligned): an odd count equals the leading rays of an even one."""
