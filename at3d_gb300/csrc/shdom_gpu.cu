@@ -1005,72 +1005,136 @@ __global__ void __launch_bounds__(MT, 2) k_sweep_march(SweepArgs a, const MarchG
 
 // Sequential-order sweep for grids whose wavefront is too deep (periodic
 // wrap-around long characteristics chain points of one ordinate through the
-// whole grid): one block per ordinate walks the reference sweep order in
-// windows of SEQW points.  The traces of a window run in parallel; the
-// final combination is resolved warp by warp in rank order, in-window
-// dependencies through shared memory.
-constexpr int SEQW = 256;
+// whole grid), in two kernels.
+//  * k_seq_prep: every (ordinate, point) trace of the hemisphere at once,
+//    since a trace depends on the source function only: its (radsrc, tr),
+//    the four corners of the face it stops on and the face coordinates, as
+//    a 32-byte record in [ordinate][rank] order.  The long characteristics
+//    (a row's first point crossing the wrap-around to the previous row, a
+//    chain of cells) run here in parallel instead of inside the walk.
+//  * k_sweep_seq: one block per ordinate walks the reference sweep order in
+//    windows of SEQN ranks.  The block's threads read a window's records
+//    (coalesced), add the dependencies on earlier windows (final, read from
+//    the radiance field) and list each item's in-window dependencies with
+//    their weights; then one thread runs the window's chain in rank order,
+//    the item just before in a register (the usual dependency: the
+//    neighbour along the row) and the others in shared memory, and the
+//    block writes the window's radiances back.  A chain step is a few
+//    dependent instructions instead of a round of warp votes.
+constexpr int SEQW = 256;   // threads of a walking block
+constexpr int SEQN = 1024;  // ranks of a window
 
-__global__ void __launch_bounds__(SEQW) k_sweep_seq(SweepArgs a, const int *order, int col_begin) {
-  __shared__ float sval[SEQW];
-  __shared__ int sdone[SEQW];
-  const int col = col_begin + blockIdx.x, ldo = a.ldo, n = a.npts;
-  if (a.col_cz[col] == 0.f) return;  // padding ordinate
+struct SeqRec {
+  float radsrc, tr, u, v;  // rad = radsrc + tr * sum_k f_k(u, v) rad(q_k)
+  int4 q;
+};
+
+__device__ __forceinline__ int col_octant(const SweepArgs &a, int col) {
   int b = 0;
   for (int k = 0; k < 8; ++k)
     if (a.oct_ncol[k] > 0 && col >= a.oct_col0[k] && col < a.oct_col0[k] + a.oct_ncol[k]) b = k;
+  return b;
+}
+
+__global__ void __launch_bounds__(256) k_seq_prep(SweepArgs a, const int *__restrict__ order, int col_begin, int nc,
+                                                   SeqRec *__restrict__ rec) {
+  const int n = a.npts;
+  const long long total = (long long)nc * n;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int cl = (int)(i / n), r = (int)(i - (long long)cl * n);
+    const int col = col_begin + cl;
+    if (a.col_cz[col] == 0.f) continue;  // padding ordinate
+    const int b = col_octant(a, col);
+    const int hb = (b & 4) ? 2 : 1;
+    const int pt = order[(size_t)b * n + r];
+    if (a.bnd[pt] & hb) continue;  // preset boundary point
+    const Trace t = trace_point(a, b, pt, col);
+    if (t.status != ERR_NONE) atomicCAS(a.err, ERR_NONE, t.status);
+    SeqRec x;
+    x.radsrc = t.radsrc; x.tr = t.tr; x.u = t.u; x.v = t.v;
+    x.q = make_int4(t.q[0], t.q[1], t.q[2], t.q[3]);
+    rec[i] = x;
+  }
+}
+
+__global__ void __launch_bounds__(SEQW) k_sweep_seq(SweepArgs a, const int *order, int col_begin,
+                                                    const SeqRec *__restrict__ rec) {
+  // per window item: the value, the part from final dependencies, the weight
+  // of the item just before it, and up to four other in-window dependencies
+  __shared__ float sval[SEQN], swv[SEQN], scp[SEQN];
+  __shared__ float4 sc[SEQN];
+  __shared__ short4 sd[SEQN];
+  const int col = col_begin + blockIdx.x, ldo = a.ldo, n = a.npts;
+  if (a.col_cz[col] == 0.f) return;  // padding ordinate
+  const int b = col_octant(a, col);
   const int hb = (b & 4) ? 2 : 1;
   const int *ord = order + (size_t)b * n, *rk = a.rank + (size_t)b * n;
-  const int tid = threadIdx.x, warp = tid >> 5;
-  for (int r0 = 0; r0 < n; r0 += SEQW) {
-    const int r = r0 + tid;
-    const int pt = r < n ? ord[r] : 0;
-    bool pending = r < n && !(a.bnd[pt] & hb);
-    Trace t;
-    if (pending) {
-      t = trace_point(a, b, pt, col);
-      if (t.status != ERR_NONE) atomicCAS(a.err, ERR_NONE, t.status);
-    }
-    int wl[4];
-    float wv = 0.f;  // contribution of the dependencies already final
-    if (pending) {
-      wv = t.radsrc;
+  const SeqRec *crec = rec + (size_t)blockIdx.x * n;
+  const int tid = threadIdx.x;
+  for (int j = tid; j < SEQN; j += SEQW) sval[j] = 0.f;
+  for (int r0 = 0; r0 < n; r0 += SEQN) {
+    const int m = min(SEQN, n - r0);
+    // (1) all threads: each item's final part and in-window dependencies
+    int pts[SEQN / SEQW];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        int q = t.q[k];
-        if (t.f[k] == 0.f || t.tr == 0.f) { wl[k] = -1; continue; }
-        int rq = (a.bnd[q] & hb) ? -1 : rk[q];
-        if (rq >= r0 && t.f[k] != 0.f) wl[k] = rq - r0;
-        else { wl[k] = -1; wv += t.tr * t.f[k] * a.raddo[(size_t)q * ldo + col]; }
-      }
-    }
-    sdone[tid] = pending ? 0 : 1;
-    __syncthreads();
-    for (int w = 0; w < SEQW / 32; ++w) {
-      if (warp == w) {
-        bool todo = pending;
-        for (int round = 0; round < 33 && __any_sync(0xffffffffu, todo); ++round) {
-          if (todo) {
-            bool ready = true;
+    for (int u = 0; u < SEQN / SEQW; ++u) {
+      const int j = tid + u * SEQW, r = r0 + j;
+      float wv = 0.f, cp = 0.f;
+      float c[4] = {0.f, 0.f, 0.f, 0.f};
+      short d[4] = {0, 0, 0, 0};
+      int pt = -1;
+      if (j < m) {
+        const int p = ord[r];
+        if (!(a.bnd[p] & hb)) {
+          pt = p;
+          const SeqRec R = crec[r];
+          const int q[4] = {R.q.x, R.q.y, R.q.z, R.q.w};
+          const float f[4] = {(1.f - R.u) * (1.f - R.v), (1.f - R.u) * R.v, R.u * (1.f - R.v), R.u * R.v};
+          wv = R.radsrc;
 #pragma unroll
-            for (int k = 0; k < 4; ++k) if (wl[k] >= 0 && !sdone[wl[k]]) ready = false;
-            if (ready) {
-              float v = wv;
-#pragma unroll
-              for (int k = 0; k < 4; ++k) if (wl[k] >= 0) v += t.tr * t.f[k] * sval[wl[k]];
-              sval[tid] = v;
-              a.raddo[(size_t)pt * ldo + col] = v;
-              todo = false;
+          for (int k = 0; k < 4; ++k) {
+            const float w = R.tr * f[k];
+            if (w == 0.f) continue;
+            const int rq = (a.bnd[q[k]] & hb) ? -1 : rk[q[k]];
+            if (rq >= r0) {
+              const int off = rq - r0;
+              if (off >= j) { atomicCAS(a.err, ERR_NONE, ERR_SWEEP_NOFACE); continue; }  // not rank-earlier
+              if (off == j - 1) cp += w;
+              else { d[k] = (short)off; c[k] = w; }
+            } else {
+              wv += w * a.raddo[(size_t)q[k] * ldo + col];
             }
           }
-          __syncwarp();
-          if (!todo && pending) sdone[tid] = 1;
-          __syncwarp();
         }
-        if (todo) atomicCAS(a.err, ERR_NONE, ERR_SWEEP_STEPS);
       }
-      __syncthreads();
+      pts[u] = pt;
+      swv[j] = wv; scp[j] = cp;
+      sc[j] = make_float4(c[0], c[1], c[2], c[3]);
+      sd[j] = make_short4(d[0], d[1], d[2], d[3]);
     }
+    __syncthreads();
+    // (2) one thread: the chain in rank order; the item just before is in a
+    // register, the others (written at least two steps earlier, or weight 0)
+    // in shared memory
+    if (tid == 0) {
+      float prev = 0.f;
+#pragma unroll 4
+      for (int i = 0; i < m; ++i) {
+        const float4 cc = sc[i];
+        const short4 dd = sd[i];
+        float v = swv[i] + cc.x * sval[dd.x] + cc.y * sval[dd.y] + cc.z * sval[dd.z] + cc.w * sval[dd.w];
+        v = fmaf(scp[i], prev, v);
+        sval[i] = v;
+        prev = v;
+      }
+    }
+    __syncthreads();
+    // (3) all threads: the window's radiances to the field
+#pragma unroll
+    for (int u = 0; u < SEQN / SEQW; ++u)
+      if (pts[u] >= 0) a.raddo[(size_t)pts[u] * ldo + col] = sval[tid + u * SEQW];
+    __syncthreads();
   }
 }
 
@@ -2879,6 +2943,7 @@ struct Handle {
   DBuf<float> tc_bh[2], tc_bl[2];
   CUtensorMap tm_a[2], tm_bh[2], tm_bl[2];
   bool seq[2] = {false, false};  // reference-order sweep engine per hemisphere
+  DBuf<SeqRec> seqrec;            // its trace records, [ordinate][rank] of one hemisphere
   // plane-march phase 2 per hemisphere (k_sweep_march): units of (group,
   // column slice), one cluster of mcs[h] CTAs each
   bool march[2] = {false, false};
@@ -3211,6 +3276,12 @@ static long long plan_device_bytes(const Plan &P) {
     long long nh = 0;
     for (int p = 0; p < P.npts; ++p) nh += P.scat[p];
     if (nh * 10 < (long long)P.npts * 9) b += 4LL * nh * (P.nlm + ldo) + 4LL * P.npts + 16LL * P.nang;
+  }
+  {  // trace records of a reference-order sweep (32 bytes per point and ordinate of a hemisphere)
+    long long nrec = 0;
+    for (int h = 0; h < 2; ++h)
+      if (reference_order(P, h)) nrec = std::max<long long>(nrec, (long long)P.npts * (h ? P.nang - P.ncol_down : P.ncol_down));
+    b += 32LL * nrec;
   }
   const long long nsh = (long long)P.nst * P.nlm;
   const long long kp0 = (nsh + 31) / 32 * 32, kp1 = (P.nang + 31) / 32 * 32;
@@ -3638,6 +3709,12 @@ static void build_irr(Handle &H) {
   setup_march(H);
   if ((!H.march[0] && !H.seq[0] && P.seg_off[0].size() > 1) || (!H.march[1] && !H.seq[1] && P.seg_off[1].size() > 1))
     H.sweepw.alloc((size_t)P.npts * H.ldo);
+  {  // trace records of the reference-order sweep, sized for its larger hemisphere
+    size_t nrec = 0;
+    for (int h = 0; h < 2; ++h)
+      if (H.seq[h]) nrec = std::max(nrec, (size_t)P.npts * (h ? P.nang - P.ncol_down : P.ncol_down));
+    if (nrec) H.seqrec.alloc(nrec);
+  }
   {  // phase 1 runs on a high-priority stream so its blocks start before the source pass fills the SMs
     int lo = 0, hi = 0;
     CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
@@ -3656,9 +3733,15 @@ static void sweep_hemisphere(Handle &H, int hemi) {
   if (H.ktime_on) CK(cudaEventRecord(H.ev_k[hemi][0], H.stream));
   if (H.seq[hemi]) {
     const int c0 = hemi ? P.ncol_down : 0, nc = hemi ? P.nang - P.ncol_down : P.ncol_down;
-    if (nc > 0) k_sweep_seq<<<nc, SEQW, 0, H.stream>>>(a, H.order.p, c0);
-    CK(cudaGetLastError());
-    H.launches += 1;
+    if (nc > 0) {
+      const long long total = (long long)nc * P.npts;
+      const int blocks = (int)std::min<long long>((total + 255) / 256, (long long)H.nsm * 8);
+      k_seq_prep<<<blocks, 256, 0, H.stream>>>(a, H.order.p, c0, nc, H.seqrec.p);
+      CK(cudaGetLastError());
+      k_sweep_seq<<<nc, SEQW, 0, H.stream>>>(a, H.order.p, c0, H.seqrec.p);
+      CK(cudaGetLastError());
+      H.launches += 2;
+    }
     if (H.ktime_on) {
       CK(cudaEventRecord(H.ev_k[hemi][1], H.stream));
       CK(cudaEventRecord(H.ev_k[hemi][2], H.stream));
