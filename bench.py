@@ -514,13 +514,14 @@ def serving_block(args, dev):
     from at3d_gb300.scenes import request_mix
     from at3d_gb300.serving import SolveServer, poisson_arrivals, run_stream
     out = []
-    reqs = request_mix(100, args.serve_requests)  # the same requests at every rate
-    for k, rate in enumerate(args.serve_rates):
-        arr = poisson_arrivals(rate, len(reqs), seed=7 + k)
-        with SolveServer(device=dev, slots=args.serve_slots) as srv:
+    reqs = request_mix(100, args.serve_requests)  # the same requests at every rate and slot count
+    runs = [(rate, slots) for rate in args.serve_rates for slots in args.serve_slots]
+    for k, (rate, slots) in enumerate(runs):
+        arr = poisson_arrivals(rate, len(reqs), seed=7 + args.serve_rates.index(rate))
+        with SolveServer(device=dev, slots=slots) as srv:
             run_stream(srv, reqs, arr, maxiter=args.maxiter)
             st = srv.stats()
-        st.update({"rate_per_s": rate, "requests": len(reqs), "slots": args.serve_slots,
+        st.update({"rate_per_s": rate, "requests": len(reqs), "slots": slots,
                    "wavelength_solves": int(sum(len(p) for p, _ in reqs))})
         out.append(st)
     return out
@@ -726,15 +727,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--jobs", type=int, default=0, help="wavelengths solved at once (default: all)")
     ap.add_argument("--no-extras", action="store_true", help="skip the precision, gradient and serving blocks")
-    ap.add_argument("--serve-rates", type=str, default="2", help="Poisson arrival rates (requests/s) to run")
+    ap.add_argument("--serve-rates", type=str, default="1,4,16", help="Poisson arrival rates (requests/s) to run")
     ap.add_argument("--serve-requests", type=int, default=16)
-    ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--serve-slots", type=str, default="4,8,16", help="slot counts to run at each rate")
     ap.add_argument("--only", default="", choices=["", "precision", "gradient", "polarized", "serving", "thermal",
                                                     "config1"],
                     help="run one extra block alone and print its JSON (for profiling)")
     ap.add_argument("--pol-boundaries", type=str, default="periodic,open")
     args = ap.parse_args()
     args.serve_rates = [float(x) for x in args.serve_rates.split(",") if x]
+    args.serve_slots = [int(x) for x in args.serve_slots.split(",") if x]
     args.pol_boundaries = [x for x in args.pol_boundaries.split(",") if x]
     args.jobs = args.jobs or args.nwave
     rank, ws = dist_init()
