@@ -1013,16 +1013,15 @@ __global__ void __launch_bounds__(MT, 2) k_sweep_march(SweepArgs a, const MarchG
 //    (a row's first point crossing the wrap-around to the previous row, a
 //    chain of cells) run here in parallel instead of inside the walk.
 //  * k_sweep_seq: one block per ordinate walks the reference sweep order in
-//    windows of SEQN ranks.  The block's threads read a window's records
-//    (coalesced), add the dependencies on earlier windows (final, read from
-//    the radiance field) and list each item's in-window dependencies with
-//    their weights; then one thread runs the window's chain in rank order,
-//    the item just before in a register (the usual dependency: the
-//    neighbour along the row) and the others in shared memory, and the
-//    block writes the window's radiances back.  A chain step is a few
-//    dependent instructions instead of a round of warp votes.
-constexpr int SEQW = 256;   // threads of a walking block
-constexpr int SEQN = 1024;  // ranks of a window
+//    windows of SEQN ranks.  One thread runs a window's chain in rank
+//    order, the item just before in a register (the usual dependency: the
+//    neighbour along the row) and the others in shared memory; a chain
+//    step is a few dependent instructions instead of a round of warp
+//    votes.  Meanwhile the other seven warps prepare the next window (read
+//    its records, coalesced; add its final dependencies; list the others
+//    with their weights) and write the window before back to the field.
+constexpr int SEQW = 256;  // threads of a walking block
+constexpr int SEQN = 512;  // ranks of a window
 
 struct SeqRec {
   float radsrc, tr, u, v;  // rad = radsrc + tr * sum_k f_k(u, v) rad(q_k)
@@ -1060,26 +1059,34 @@ __global__ void __launch_bounds__(256) k_seq_prep(SweepArgs a, const int *__rest
 
 __global__ void __launch_bounds__(SEQW) k_sweep_seq(SweepArgs a, const int *order, int col_begin,
                                                     const SeqRec *__restrict__ rec) {
-  // per window item: the value, the part from final dependencies, the weight
-  // of the item just before it, and up to four other in-window dependencies
-  __shared__ float sval[SEQN], swv[SEQN], scp[SEQN];
-  __shared__ float4 sc[SEQN];
-  __shared__ short4 sd[SEQN];
+  // sval: the values of the last two windows walked, by window parity (a
+  // ring of 2 SEQN).  Per item of a window being walked or prepared (by
+  // parity): the part from final dependencies, the weight of the item just
+  // before it, and up to four other dependencies (ring indices, weight 0 for
+  // none).  spt: the items' points, kept three windows for the write-back.
+  __shared__ float sval[2 * SEQN];
+  __shared__ float swv[2][SEQN], scp[2][SEQN];
+  __shared__ float4 sc[2][SEQN];
+  __shared__ short4 sd[2][SEQN];
+  __shared__ int spt[3][SEQN];
   const int col = col_begin + blockIdx.x, ldo = a.ldo, n = a.npts;
   if (a.col_cz[col] == 0.f) return;  // padding ordinate
   const int b = col_octant(a, col);
   const int hb = (b & 4) ? 2 : 1;
   const int *ord = order + (size_t)b * n, *rk = a.rank + (size_t)b * n;
   const SeqRec *crec = rec + (size_t)blockIdx.x * n;
-  const int tid = threadIdx.x;
-  for (int j = tid; j < SEQN; j += SEQW) sval[j] = 0.f;
-  for (int r0 = 0; r0 < n; r0 += SEQN) {
-    const int m = min(SEQN, n - r0);
-    // (1) all threads: each item's final part and in-window dependencies
-    int pts[SEQN / SEQW];
-#pragma unroll
-    for (int u = 0; u < SEQN / SEQW; ++u) {
-      const int j = tid + u * SEQW, r = r0 + j;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int nwin = (n + SEQN - 1) / SEQN;
+  for (int j = tid; j < 2 * SEQN; j += SEQW) sval[j] = 0.f;
+
+  // window w's item list, by threads [t0, t0 + nt).  Dependencies: on a
+  // preset point or a window before w - 2, final in the field; on window
+  // w - 2, final in the ring; on window w - 1 or w, ring indices for the
+  // walk (window w - 1 may still be walking while w is prepared).
+  auto prep = [&](int w, int t0, int nt) {
+    const int r0 = w * SEQN, m = min(SEQN, n - r0), pw = w & 1;
+    for (int j = tid - t0; j < SEQN; j += nt) {
+      const int r = r0 + j;
       float wv = 0.f, cp = 0.f;
       float c[4] = {0.f, 0.f, 0.f, 0.f};
       short d[4] = {0, 0, 0, 0};
@@ -1094,48 +1101,67 @@ __global__ void __launch_bounds__(SEQW) k_sweep_seq(SweepArgs a, const int *orde
           wv = R.radsrc;
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
-            const float w = R.tr * f[k];
-            if (w == 0.f) continue;
-            const int rq = (a.bnd[q[k]] & hb) ? -1 : rk[q[k]];
-            if (rq >= r0) {
+            const float wt = R.tr * f[k];
+            if (wt == 0.f) continue;
+            if (a.bnd[q[k]] & hb) {  // a preset boundary point: final
+              wv += wt * a.raddo[(size_t)q[k] * ldo + col];
+              continue;
+            }
+            const int rq = rk[q[k]];
+            if (rq >= r0) {  // this window
               const int off = rq - r0;
               if (off >= j) { atomicCAS(a.err, ERR_NONE, ERR_SWEEP_NOFACE); continue; }  // not rank-earlier
-              if (off == j - 1) cp += w;
-              else { d[k] = (short)off; c[k] = w; }
+              if (off == j - 1) cp += wt;
+              else { d[k] = (short)(pw * SEQN + off); c[k] = wt; }
+            } else if (rq >= r0 - SEQN) {  // window w - 1: walked just before this one
+              d[k] = (short)((pw ^ 1) * SEQN + (rq - (r0 - SEQN))); c[k] = wt;
+            } else if (rq >= r0 - 2 * SEQN) {  // window w - 2: final, in the ring
+              wv += wt * sval[pw * SEQN + (rq - (r0 - 2 * SEQN))];
             } else {
-              wv += w * a.raddo[(size_t)q[k] * ldo + col];
+              wv += wt * a.raddo[(size_t)q[k] * ldo + col];
             }
           }
         }
       }
-      pts[u] = pt;
-      swv[j] = wv; scp[j] = cp;
-      sc[j] = make_float4(c[0], c[1], c[2], c[3]);
-      sd[j] = make_short4(d[0], d[1], d[2], d[3]);
+      spt[w % 3][j] = pt;
+      swv[pw][j] = wv; scp[pw][j] = cp;
+      sc[pw][j] = make_float4(c[0], c[1], c[2], c[3]);
+      sd[pw][j] = make_short4(d[0], d[1], d[2], d[3]);
     }
-    __syncthreads();
-    // (2) one thread: the chain in rank order; the item just before is in a
-    // register, the others (written at least two steps earlier, or weight 0)
-    // in shared memory
-    if (tid == 0) {
-      float prev = 0.f;
+  };
+  // window w's radiances to the field, by threads [t0, t0 + nt)
+  auto writeback = [&](int w, int t0, int nt) {
+    const int pw = w & 1;
+    for (int j = tid - t0; j < SEQN; j += nt) {
+      const int pt = spt[w % 3][j];
+      if (pt >= 0) a.raddo[(size_t)pt * ldo + col] = sval[pw * SEQN + j];
+    }
+  };
+  if (nwin > 0) prep(0, 0, SEQW);
+  __syncthreads();
+  for (int w = 0; w < nwin; ++w) {
+    if (warp == 0) {
+      if (tid == 0) {  // the chain of window w in rank order, the item just before in a register
+        const int pw = w & 1, m = min(SEQN, n - w * SEQN);
+        float *out = sval + pw * SEQN;
+        float prev = 0.f;
 #pragma unroll 4
-      for (int i = 0; i < m; ++i) {
-        const float4 cc = sc[i];
-        const short4 dd = sd[i];
-        float v = swv[i] + cc.x * sval[dd.x] + cc.y * sval[dd.y] + cc.z * sval[dd.z] + cc.w * sval[dd.w];
-        v = fmaf(scp[i], prev, v);
-        sval[i] = v;
-        prev = v;
+        for (int i = 0; i < m; ++i) {
+          const float4 cc = sc[pw][i];
+          const short4 dd = sd[pw][i];
+          float v = swv[pw][i] + cc.x * sval[dd.x] + cc.y * sval[dd.y] + cc.z * sval[dd.z] + cc.w * sval[dd.w];
+          v = fmaf(scp[pw][i], prev, v);
+          out[i] = v;
+          prev = v;
+        }
       }
+    } else {  // meanwhile: prepare window w + 1, write back window w - 1
+      if (w + 1 < nwin) prep(w + 1, 32, SEQW - 32);
+      if (w >= 1) writeback(w - 1, 32, SEQW - 32);
     }
-    __syncthreads();
-    // (3) all threads: the window's radiances to the field
-#pragma unroll
-    for (int u = 0; u < SEQN / SEQW; ++u)
-      if (pts[u] >= 0) a.raddo[(size_t)pts[u] * ldo + col] = sval[tid + u * SEQW];
     __syncthreads();
   }
+  if (nwin > 0) writeback(nwin - 1, 0, SEQW);
 }
 
 // Preset boundary radiances for one hemisphere: top points get the sky
