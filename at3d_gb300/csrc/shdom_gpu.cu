@@ -212,6 +212,13 @@ struct IrrRec {
   float4 g;
 };
 
+// A trace reduced to what the radiance combination needs: rad = radsrc +
+// tr * sum_k f_k(u, v) rad(q_k), f the bilinear weights of the stopping face.
+struct TraceRec {
+  float radsrc, tr, u, v;
+  int4 q;
+};
+
 struct SweepArgs {
   const float *gridpos;
   const int *gridptr, *neighptr, *cellflags;
@@ -608,6 +615,7 @@ __global__ void __launch_bounds__(256) k_irr_build(SweepArgs a, const Seg *__res
 constexpr int P1_THREADS = 512;
 constexpr int P1_SPLIT = 4;
 constexpr int P1_STAGE = 2;
+constexpr int P1_SEGCAP = 512;  // level segments of a phase-1 group kept in shared memory
 
 __global__ void __launch_bounds__(P1_THREADS) k_sweep_p1(SweepArgs a, const Seg *__restrict__ p1segs,
                                                          const int *__restrict__ p1off) {
@@ -701,6 +709,233 @@ __global__ void __launch_bounds__(P1_THREADS) k_sweep_p1(SweepArgs a, const Seg 
 
 // Phase 2, one item: point, (radsrc, tr), face corners and weights, then the
 // four upstream radiances.
+// Phase 1 ahead of the plane march: every phase-1 item's trace (its
+// stored first face, or the cell walk) in one parallel pass, as records
+// indexed like the general-trace table (irr entries [0, n)); traces depend
+// on the source function only.
+__global__ void __launch_bounds__(256) k_p1_prep(SweepArgs a, const Seg *__restrict__ segs, int nseg, int n,
+                                                 TraceRec *__restrict__ out) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const Seg g = segs[irr_seg_find(segs, nseg, j)];
+    const int li = j - g.irr0, task = li / g.ncol, slot = li - task * g.ncol;
+    const int pt = (int)__ldg(a.tasks + g.t0 + task), col = g.col0 + slot;
+    const IrrRec rec = a.irr[j];
+    Trace t;
+    if (rec.g.w > 0.5f) {
+      RegLoad x;
+      rec_load(a, rec, pt, col, x, false);
+      t = reg_trace(x, g.b, pt);
+      t.q[0] = rec.q.x; t.q[1] = rec.q.y; t.q[2] = rec.q.z; t.q[3] = rec.q.w;
+    } else {
+      t = trace_general(a, g.b, g.cls, pt, col, true);
+      if (t.status != ERR_NONE) atomicCAS(a.err, ERR_NONE, t.status);
+    }
+    TraceRec r;
+    r.radsrc = t.radsrc; r.tr = t.tr; r.u = t.u; r.v = t.v;
+    r.q = make_int4(t.q[0], t.q[1], t.q[2], t.q[3]);
+    out[j] = r;
+  }
+}
+
+// Phase 1 from the records of k_p1_prep: per level and item, the four
+// corner radiances (written by earlier levels) and the combination.  Block
+// layout as k_sweep_p1; a thread's first P1_STAGE items of the next level
+// have their record and point loaded before the barrier.
+__global__ void __launch_bounds__(P1_THREADS) k_sweep_p1r(SweepArgs a, const Seg *__restrict__ p1segs,
+                                                          const int *__restrict__ p1off,
+                                                          const TraceRec *__restrict__ recs) {
+  const int grp = blockIdx.x / P1_SPLIT, sid = blockIdx.x % P1_SPLIT;
+  const int s0 = p1off[grp], s1 = p1off[grp + 1];
+  const int ldo = a.ldo;
+  // the group's level segments, in shared memory when they fit
+  __shared__ Seg ssg[P1_SEGCAP];
+  const bool local = s1 - s0 <= P1_SEGCAP;
+  if (local)
+    for (int t = threadIdx.x; t < s1 - s0; t += blockDim.x) ssg[t] = p1segs[s0 + t];
+  __syncthreads();
+  auto seg = [&](int si) { return local ? ssg[si - s0] : p1segs[si]; };
+  TraceRec sr[P1_STAGE];
+  int spt[P1_STAGE], scol[P1_STAGE];
+  auto items_of = [&](const Seg &g, int &cbeg, int &ncs) {
+    const int cw = (g.ncol + P1_SPLIT - 1) / P1_SPLIT;
+    cbeg = sid * cw; ncs = max(0, min(g.ncol, cbeg + cw) - cbeg);
+    return g.ntask * ncs;
+  };
+  auto locate = [&](const Seg &g, int cbeg, int ncs, int ii, int &pt, int &col, int &j) {
+    const int task = ii / ncs, slot = cbeg + (ii - task * ncs);
+    pt = (int)__ldg(a.tasks + g.t0 + task);
+    col = g.col0 + slot;
+    j = g.irr0 + task * g.ncol + slot;
+  };
+  auto combine = [&](const TraceRec &R, int pt, int col) {
+    float rad = R.radsrc;
+    if (R.tr != 0.f) {
+      const float r0 = a.raddo[(size_t)R.q.x * ldo + col], r1 = a.raddo[(size_t)R.q.y * ldo + col];
+      const float r2 = a.raddo[(size_t)R.q.z * ldo + col], r3 = a.raddo[(size_t)R.q.w * ldo + col];
+      const float u = R.u, v = R.v;
+      rad += R.tr * ((1.f - u) * (1.f - v) * r0 + (1.f - u) * v * r1 + u * (1.f - v) * r2 + u * v * r3);
+    }
+    a.raddo[(size_t)pt * ldo + col] = rad;
+  };
+  auto stage = [&](int si) {
+    if (si >= s1) return;
+    const Seg g = seg(si);
+    int cbeg, ncs;
+    const int items = items_of(g, cbeg, ncs);
+#pragma unroll
+    for (int k = 0; k < P1_STAGE; ++k) {
+      const int ii = threadIdx.x + k * blockDim.x;
+      if (ii < items) {
+        int j;
+        locate(g, cbeg, ncs, ii, spt[k], scol[k], j);
+        sr[k] = recs[j];
+      }
+    }
+  };
+  stage(s0);
+  for (int si = s0; si < s1; ++si) {
+    const Seg g = seg(si);
+    int cbeg, ncs;
+    const int items = items_of(g, cbeg, ncs);
+#pragma unroll
+    for (int k = 0; k < P1_STAGE; ++k)
+      if (threadIdx.x + k * blockDim.x < items) combine(sr[k], spt[k], scol[k]);
+    for (int ii = threadIdx.x + P1_STAGE * blockDim.x; ii < items; ii += blockDim.x) {
+      int pt, col, j;
+      locate(g, cbeg, ncs, ii, pt, col, j);
+      combine(recs[j], pt, col);
+    }
+    stage(si + 1);  // the next level's records, which do not depend on this level
+    __syncthreads();
+  }
+}
+
+// Phase 1 with block-local radiances.  A phase-1 point's corners are
+// preset boundary points (final before phase 1) or phase-1 points of the
+// same ordinates, i.e. of the same (octant, class) group.  Each group's
+// phase-1 points are numbered in level order (slots); a block owns a slice
+// of the group's columns and keeps the slice's radiances of all the
+// group's phase-1 points in shared memory, so a level reads its corners
+// from there.  k_p1_prep_s folds the boundary corners into radsrc and
+// turns the other corners into slots (q[k] = slot, or -1).
+struct P1Blk {
+  int grp, cbeg, ncs, nslots;  // group, its column slice [cbeg, cbeg + ncs), the group's phase-1 points
+};
+
+__global__ void __launch_bounds__(256) k_p1_prep_s(SweepArgs a, const Seg *__restrict__ segs, int nseg, int n,
+                                                   const int *__restrict__ seggrp, const int *__restrict__ p1slot,
+                                                   TraceRec *__restrict__ out) {
+  const int ldo = a.ldo;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const int si = irr_seg_find(segs, nseg, j);
+    const Seg g = segs[si];
+    const int li = j - g.irr0, task = li / g.ncol, slot = li - task * g.ncol;
+    const int pt = (int)__ldg(a.tasks + g.t0 + task), col = g.col0 + slot;
+    const IrrRec rec = a.irr[j];
+    Trace t;
+    if (rec.g.w > 0.5f) {
+      RegLoad x;
+      rec_load(a, rec, pt, col, x, false);
+      t = reg_trace(x, g.b, pt);
+      t.q[0] = rec.q.x; t.q[1] = rec.q.y; t.q[2] = rec.q.z; t.q[3] = rec.q.w;
+    } else {
+      t = trace_general(a, g.b, g.cls, pt, col, true);
+      if (t.status != ERR_NONE) atomicCAS(a.err, ERR_NONE, t.status);
+    }
+    const int hb = (g.b & 4) ? 2 : 1;
+    const int *slots = p1slot + (size_t)seggrp[si] * a.npts;
+    const float f[4] = {(1.f - t.u) * (1.f - t.v), (1.f - t.u) * t.v, t.u * (1.f - t.v), t.u * t.v};
+    TraceRec r;
+    r.radsrc = t.radsrc; r.tr = t.tr; r.u = t.u; r.v = t.v;
+    int sl[4] = {-1, -1, -1, -1};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float w = t.tr * f[k];
+      if (w == 0.f) continue;
+      if (a.bnd[t.q[k]] & hb) {
+        r.radsrc += w * a.raddo[(size_t)t.q[k] * ldo + col];  // preset: final
+      } else {
+        sl[k] = slots[t.q[k]];
+        if (sl[k] < 0) atomicCAS(a.err, ERR_NONE, ERR_SWEEP_NOFACE);  // not a phase-1 point of the group
+      }
+    }
+    r.q = make_int4(sl[0], sl[1], sl[2], sl[3]);
+    out[j] = r;
+  }
+}
+
+__global__ void __launch_bounds__(P1_THREADS) k_sweep_p1s(SweepArgs a, const Seg *__restrict__ p1segs,
+                                                          const int *__restrict__ p1off, const P1Blk *__restrict__ blks,
+                                                          const int *__restrict__ segbase,
+                                                          const TraceRec *__restrict__ recs) {
+  extern __shared__ float sv[];  // [slot][column of the slice]
+  __shared__ Seg ssg[P1_SEGCAP];
+  __shared__ int sbase[P1_SEGCAP];
+  const P1Blk B = blks[blockIdx.x];
+  const int s0 = p1off[B.grp], s1 = p1off[B.grp + 1], ncs = B.ncs;
+  const int ldo = a.ldo;
+  for (int t = threadIdx.x; t < s1 - s0; t += blockDim.x) { ssg[t] = p1segs[s0 + t]; sbase[t] = segbase[s0 + t]; }
+  __syncthreads();
+  TraceRec sr[P1_STAGE];
+  int spt[P1_STAGE];
+  auto rec_of = [&](const Seg &g, int ii, int &pt, int &col, int &slot, int &c) {
+    const int task = ii / ncs;
+    c = ii - task * ncs;
+    pt = (int)__ldg(a.tasks + g.t0 + task);
+    col = g.col0 + B.cbeg + c;
+    slot = task;
+    return g.irr0 + task * g.ncol + B.cbeg + c;
+  };
+  auto combine = [&](const TraceRec &R, int pt, int col, int slot, int c) {
+    float rad = R.radsrc;
+    if (R.tr != 0.f) {
+      const float u = R.u, v = R.v;
+      const float f0 = (1.f - u) * (1.f - v), f1 = (1.f - u) * v, f2 = u * (1.f - v), f3 = u * v;
+      float acc = 0.f;
+      if (R.q.x >= 0) acc += f0 * sv[R.q.x * ncs + c];
+      if (R.q.y >= 0) acc += f1 * sv[R.q.y * ncs + c];
+      if (R.q.z >= 0) acc += f2 * sv[R.q.z * ncs + c];
+      if (R.q.w >= 0) acc += f3 * sv[R.q.w * ncs + c];
+      rad += R.tr * acc;
+    }
+    sv[slot * ncs + c] = rad;
+    a.raddo[(size_t)pt * ldo + col] = rad;
+  };
+  auto stage = [&](int si) {
+    if (si >= s1) return;
+    const Seg &g = ssg[si - s0];
+    const int items = g.ntask * ncs;
+#pragma unroll
+    for (int k = 0; k < P1_STAGE; ++k) {
+      const int ii = threadIdx.x + k * blockDim.x;
+      if (ii < items) {
+        int col, slot, c;
+        sr[k] = recs[rec_of(g, ii, spt[k], col, slot, c)];
+      }
+    }
+  };
+  stage(s0);
+  for (int si = s0; si < s1; ++si) {
+    const Seg &g = ssg[si - s0];
+    const int items = g.ntask * ncs, base = sbase[si - s0];
+#pragma unroll
+    for (int k = 0; k < P1_STAGE; ++k) {
+      const int ii = threadIdx.x + k * blockDim.x;
+      if (ii < items) {
+        const int task = ii / ncs, c = ii - task * ncs;
+        combine(sr[k], spt[k], g.col0 + B.cbeg + c, base + task, c);
+      }
+    }
+    for (int ii = threadIdx.x + P1_STAGE * blockDim.x; ii < items; ii += blockDim.x) {
+      int pt, col, slot, c;
+      const int j = rec_of(g, ii, pt, col, slot, c);
+      combine(recs[j], pt, col, base + slot, c);
+    }
+    stage(si + 1);  // the next level's records, which do not depend on this level
+    __syncthreads();
+  }
+}
+
 struct LevelItem {
   float2 w;
   float u, v;
@@ -1023,11 +1258,6 @@ __global__ void __launch_bounds__(MT, 2) k_sweep_march(SweepArgs a, const MarchG
 constexpr int SEQW = 256;  // threads of a walking block
 constexpr int SEQN = 512;  // ranks of a window
 
-struct SeqRec {
-  float radsrc, tr, u, v;  // rad = radsrc + tr * sum_k f_k(u, v) rad(q_k)
-  int4 q;
-};
-
 __device__ __forceinline__ int col_octant(const SweepArgs &a, int col) {
   int b = 0;
   for (int k = 0; k < 8; ++k)
@@ -1036,7 +1266,7 @@ __device__ __forceinline__ int col_octant(const SweepArgs &a, int col) {
 }
 
 __global__ void __launch_bounds__(256) k_seq_prep(SweepArgs a, const int *__restrict__ order, int col_begin, int nc,
-                                                   SeqRec *__restrict__ rec) {
+                                                   TraceRec *__restrict__ rec) {
   const int n = a.npts;
   const long long total = (long long)nc * n;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
@@ -1050,7 +1280,7 @@ __global__ void __launch_bounds__(256) k_seq_prep(SweepArgs a, const int *__rest
     if (a.bnd[pt] & hb) continue;  // preset boundary point
     const Trace t = trace_point(a, b, pt, col);
     if (t.status != ERR_NONE) atomicCAS(a.err, ERR_NONE, t.status);
-    SeqRec x;
+    TraceRec x;
     x.radsrc = t.radsrc; x.tr = t.tr; x.u = t.u; x.v = t.v;
     x.q = make_int4(t.q[0], t.q[1], t.q[2], t.q[3]);
     rec[i] = x;
@@ -1058,7 +1288,7 @@ __global__ void __launch_bounds__(256) k_seq_prep(SweepArgs a, const int *__rest
 }
 
 __global__ void __launch_bounds__(SEQW) k_sweep_seq(SweepArgs a, const int *order, int col_begin,
-                                                    const SeqRec *__restrict__ rec) {
+                                                    const TraceRec *__restrict__ rec) {
   // sval: the values of the last two windows walked, by window parity (a
   // ring of 2 SEQN).  Per item of a window being walked or prepared (by
   // parity): the part from final dependencies, the weight of the item just
@@ -1074,7 +1304,7 @@ __global__ void __launch_bounds__(SEQW) k_sweep_seq(SweepArgs a, const int *orde
   const int b = col_octant(a, col);
   const int hb = (b & 4) ? 2 : 1;
   const int *ord = order + (size_t)b * n, *rk = a.rank + (size_t)b * n;
-  const SeqRec *crec = rec + (size_t)blockIdx.x * n;
+  const TraceRec *crec = rec + (size_t)blockIdx.x * n;
   const int tid = threadIdx.x, warp = tid >> 5;
   const int nwin = (n + SEQN - 1) / SEQN;
   for (int j = tid; j < 2 * SEQN; j += SEQW) sval[j] = 0.f;
@@ -1095,7 +1325,7 @@ __global__ void __launch_bounds__(SEQW) k_sweep_seq(SweepArgs a, const int *orde
         const int p = ord[r];
         if (!(a.bnd[p] & hb)) {
           pt = p;
-          const SeqRec R = crec[r];
+          const TraceRec R = crec[r];
           const int q[4] = {R.q.x, R.q.y, R.q.z, R.q.w};
           const float f[4] = {(1.f - R.u) * (1.f - R.v), (1.f - R.u) * R.v, R.u * (1.f - R.v), R.u * R.v};
           wv = R.radsrc;
@@ -2969,7 +3199,13 @@ struct Handle {
   DBuf<float> tc_bh[2], tc_bl[2];
   CUtensorMap tm_a[2], tm_bh[2], tm_bl[2];
   bool seq[2] = {false, false};  // reference-order sweep engine per hemisphere
-  DBuf<SeqRec> seqrec;            // its trace records, [ordinate][rank] of one hemisphere
+  DBuf<TraceRec> seqrec;            // its trace records, [ordinate][rank] of one hemisphere
+  DBuf<TraceRec> p1rec;             // phase-1 trace records ahead of the plane march, [irr entry]
+  bool p1s[2] = {false, false};     // phase 1 with block-local radiances (k_sweep_p1s)
+  DBuf<P1Blk> p1blk[2];
+  int np1blk[2] = {0, 0};
+  size_t p1smem[2] = {0, 0};
+  DBuf<int> p1base[2], p1grp[2], p1slot[2];  // per segment: first slot, group; [group][point]: slot or -1
   // plane-march phase 2 per hemisphere (k_sweep_march): units of (group,
   // column slice), one cluster of mcs[h] CTAs each
   bool march[2] = {false, false};
@@ -3303,6 +3539,16 @@ static long long plan_device_bytes(const Plan &P) {
     for (int p = 0; p < P.npts; ++p) nh += P.scat[p];
     if (nh * 10 < (long long)P.npts * 9) b += 4LL * nh * (P.nlm + ldo) + 4LL * P.npts + 16LL * P.nang;
   }
+  {  // phase-1 trace records ahead of a plane march (at most one per general-trace item), and the
+     // block-local phase 1's slot tables ([group][point])
+    long long n1 = 0;
+    for (int h = 0; h < 2; ++h)
+      if (!P.march[h].empty()) {
+        n1 = std::max<long long>(n1, (long long)P.nirr[h]);
+        b += 4LL * P.npts * std::max(0, (int)P.p1off[h].size() - 1) + 8LL * (long long)P.p1segs[h].size();
+      }
+    b += 32LL * n1;
+  }
   {  // trace records of a reference-order sweep (32 bytes per point and ordinate of a hemisphere)
     long long nrec = 0;
     for (int h = 0; h < 2; ++h)
@@ -3417,6 +3663,71 @@ static void setup_march(Handle &H) {
       H.march[h] = true;
       break;
     }
+  }
+}
+
+// Block-local phase 1 (k_sweep_p1s) for each marching hemisphere whose
+// phase-1 groups fit: a group's phase-1 points are numbered in level order,
+// and a block takes as many of its columns as keep the slice's radiances
+// of all those points in kP1SmemCap bytes (and a level's items within four
+// per thread).  Otherwise the hemisphere keeps k_sweep_p1r.
+constexpr size_t kP1SmemCap = 192 * 1024;
+
+static void setup_p1s(Handle &H) {
+  Plan &P = H.P;
+  int dev = 0, maxsm = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const size_t static_smem = sizeof(Seg) * P1_SEGCAP + sizeof(int) * P1_SEGCAP;
+  for (int h = 0; h < 2; ++h) {
+    H.p1s[h] = false;
+    const std::vector<int> &off = P.p1off[h];
+    const int ng1 = (int)off.size() - 1;
+    if (!H.march[h] || ng1 <= 0 || (size_t)maxsm < kP1SmemCap + static_smem) continue;
+    const std::vector<Seg> &sg = P.p1segs[h];
+    std::vector<int> base(sg.size(), 0), grp(sg.size(), 0), nslots(ng1, 0);
+    bool ok = true;
+    for (int g = 0; g < ng1 && ok; ++g) {
+      if (off[g + 1] - off[g] > P1_SEGCAP) ok = false;
+      int maxtask = 0;
+      for (int si = off[g]; si < off[g + 1]; ++si) {
+        base[si] = nslots[g];
+        grp[si] = g;
+        nslots[g] += sg[si].ntask;
+        maxtask = std::max(maxtask, sg[si].ntask);
+        if (sg[si].col0 != sg[off[g]].col0 || sg[si].ncol != sg[off[g]].ncol) ok = false;
+      }
+      if ((size_t)nslots[g] * sizeof(float) > kP1SmemCap) ok = false;
+      (void)maxtask;
+    }
+    if (!ok) continue;
+    std::vector<P1Blk> blks;
+    size_t smem = 0;
+    for (int g = 0; g < ng1; ++g) {
+      if (off[g + 1] == off[g]) continue;
+      const Seg &s0 = sg[off[g]];
+      int maxtask = 0;
+      for (int si = off[g]; si < off[g + 1]; ++si) maxtask = std::max(maxtask, sg[si].ntask);
+      int ncs = (int)std::min<size_t>(kP1SmemCap / ((size_t)nslots[g] * sizeof(float)), (size_t)s0.ncol);
+      ncs = std::max(1, std::min(ncs, 4 * P1_THREADS / std::max(1, maxtask)));
+      for (int c0 = 0; c0 < s0.ncol; c0 += ncs) {
+        const int nc = std::min(ncs, s0.ncol - c0);
+        blks.push_back(P1Blk{g, c0, nc, nslots[g]});
+        smem = std::max(smem, (size_t)nslots[g] * nc * sizeof(float));
+      }
+    }
+    std::vector<int> slot((size_t)ng1 * P.npts, -1);
+    for (int g = 0; g < ng1; ++g)
+      for (int si = off[g]; si < off[g + 1]; ++si)
+        for (int t = 0; t < sg[si].ntask; ++t) slot[(size_t)g * P.npts + P.tasks[h][sg[si].t0 + t]] = base[si] + t;
+    CK(cudaFuncSetAttribute(k_sweep_p1s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(maxsm - static_smem)));
+    H.p1blk[h].upload(blks);
+    H.p1base[h].upload(base);
+    H.p1grp[h].upload(grp);
+    H.p1slot[h].upload(slot);
+    H.np1blk[h] = (int)blks.size();
+    H.p1smem[h] = smem;
+    H.p1s[h] = true;
   }
 }
 
@@ -3733,8 +4044,15 @@ static void build_irr(Handle &H) {
     for (int h = 0; h < 2; ++h) H.irr[h].view(G.irr[h]);
   }
   setup_march(H);
+  setup_p1s(H);
   if ((!H.march[0] && !H.seq[0] && P.seg_off[0].size() > 1) || (!H.march[1] && !H.seq[1] && P.seg_off[1].size() > 1))
     H.sweepw.alloc((size_t)P.npts * H.ldo);
+  {  // phase-1 trace records ahead of the plane march
+    int n1 = 0;
+    for (int h = 0; h < 2; ++h)
+      if (H.march[h]) n1 = std::max(n1, H.p2_irr_j0[h]);
+    if (n1) H.p1rec.alloc((size_t)n1);
+  }
   {  // trace records of the reference-order sweep, sized for its larger hemisphere
     size_t nrec = 0;
     for (int h = 0; h < 2; ++h)
@@ -3778,9 +4096,28 @@ static void sweep_hemisphere(Handle &H, int hemi) {
   const int nlev = (int)off.size() - 1;
   const int ng1 = (int)P.p1off[hemi].size() - 1;
   if (H.march[hemi] && !H.march_off) {
-    // phase 1 (the boundary-plane chains), then the plane march of phase 2
+    // phase 1 (the boundary-plane chains: their traces in one parallel pass,
+    // then the levels), then the plane march of phase 2
     if (ng1 > 0) {
-      k_sweep_p1<<<ng1 * P1_SPLIT, P1_THREADS, 0, H.stream>>>(a, H.p1segs[hemi].p, H.p1off[hemi].p);
+      const int n1 = H.p2_irr_j0[hemi];
+      const int blocks = std::min((n1 + 255) / 256, H.nsm * 8);
+      if (H.p1s[hemi]) {
+        if (n1 > 0) {
+          k_p1_prep_s<<<blocks, 256, 0, H.stream>>>(a, H.irrsegs[hemi].p, H.p2_irrseg0[hemi], n1, H.p1grp[hemi].p,
+                                                    H.p1slot[hemi].p, H.p1rec.p);
+          CK(cudaGetLastError());
+          H.launches += 1;
+        }
+        k_sweep_p1s<<<H.np1blk[hemi], P1_THREADS, H.p1smem[hemi], H.stream>>>(
+            a, H.p1segs[hemi].p, H.p1off[hemi].p, H.p1blk[hemi].p, H.p1base[hemi].p, H.p1rec.p);
+      } else {
+        if (n1 > 0) {
+          k_p1_prep<<<blocks, 256, 0, H.stream>>>(a, H.irrsegs[hemi].p, H.p2_irrseg0[hemi], n1, H.p1rec.p);
+          CK(cudaGetLastError());
+          H.launches += 1;
+        }
+        k_sweep_p1r<<<ng1 * P1_SPLIT, P1_THREADS, 0, H.stream>>>(a, H.p1segs[hemi].p, H.p1off[hemi].p, H.p1rec.p);
+      }
       CK(cudaGetLastError());
       H.launches += 1;
     }
