@@ -667,6 +667,14 @@ def reference_arm(args, rank, ws):
     walls = [w + (t_init if i == 0 else 0.0) for i, w in enumerate(slices)]  # per step, as run
     timed = walls[args.warmup:] if args.steps > 0 else walls
     ms_step = float(np.mean(timed)) * 1e3
+    # the remaining iterations come from each CPU solve's own convergence trend, which
+    # needs three solution criteria: a run shorter than that measures up to three more
+    # slices (counted in the solves' time, not in the steps)
+    extra_measured = 0
+    while extra_measured < 3 and any(cs.remaining_iterations(w) is None and not cs.converged(w)
+                                     for w in range(len(pbs))):
+        slices.append(cs.step(args.ref_slice))
+        extra_measured += 1
     # wall time of the concurrent solves: the initialisation and every measured slice, plus,
     # when they have not converged yet, the remaining slices at the mean wall of the last three
     rem = [cs.remaining_iterations(w) for w in range(len(pbs))]
@@ -694,6 +702,7 @@ def reference_arm(args, rank, ws):
                                                                                 for c in cs.crit],
                            "init_s": t_init, "step_walls_s": walls,
                            "remaining_slices_estimated": extra,
+                           "slices_measured_beyond_the_steps": extra_measured,
                            "estimate_complete": known},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
