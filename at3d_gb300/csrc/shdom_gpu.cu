@@ -3121,7 +3121,13 @@ struct DevGeom {
   DBuf<int> seg_off[2], level_items[2], p1off[2];
   DBuf<IrrRec> irr[2];
   bool irr_built = false;
-  std::mutex mu;  // guards the one-time build of irr
+  // block-local phase 1 (setup_p1s): per hemisphere, built once per grid and device
+  bool p1s_built = false, p1s_ok[2] = {false, false};
+  DBuf<P1Blk> p1blk[2];
+  DBuf<int> p1base[2], p1grp[2], p1slot[2];
+  int np1blk[2] = {0, 0};
+  size_t p1smem[2] = {0, 0};
+  std::mutex mu;  // guards the one-time builds of irr and of the phase-1 tables
 };
 static std::mutex g_devgeom_mu;
 static std::list<std::shared_ptr<DevGeom>> g_devgeom;  // most recent first
@@ -3679,55 +3685,65 @@ static void setup_p1s(Handle &H) {
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   const size_t static_smem = sizeof(Seg) * P1_SEGCAP + sizeof(int) * P1_SEGCAP;
-  for (int h = 0; h < 2; ++h) {
-    H.p1s[h] = false;
-    const std::vector<int> &off = P.p1off[h];
-    const int ng1 = (int)off.size() - 1;
-    if (!H.march[h] || ng1 <= 0 || (size_t)maxsm < kP1SmemCap + static_smem) continue;
-    const std::vector<Seg> &sg = P.p1segs[h];
-    std::vector<int> base(sg.size(), 0), grp(sg.size(), 0), nslots(ng1, 0);
-    bool ok = true;
-    for (int g = 0; g < ng1 && ok; ++g) {
-      if (off[g + 1] - off[g] > P1_SEGCAP) ok = false;
-      int maxtask = 0;
-      for (int si = off[g]; si < off[g + 1]; ++si) {
-        base[si] = nslots[g];
-        grp[si] = g;
-        nslots[g] += sg[si].ntask;
-        maxtask = std::max(maxtask, sg[si].ntask);
-        if (sg[si].col0 != sg[off[g]].col0 || sg[si].ncol != sg[off[g]].ncol) ok = false;
-      }
-      if ((size_t)nslots[g] * sizeof(float) > kP1SmemCap) ok = false;
-      (void)maxtask;
-    }
-    if (!ok) continue;
-    std::vector<P1Blk> blks;
-    size_t smem = 0;
-    for (int g = 0; g < ng1; ++g) {
-      if (off[g + 1] == off[g]) continue;
-      const Seg &s0 = sg[off[g]];
-      int maxtask = 0;
-      for (int si = off[g]; si < off[g + 1]; ++si) maxtask = std::max(maxtask, sg[si].ntask);
-      int ncs = (int)std::min<size_t>(kP1SmemCap / ((size_t)nslots[g] * sizeof(float)), (size_t)s0.ncol);
-      ncs = std::max(1, std::min(ncs, 4 * P1_THREADS / std::max(1, maxtask)));
-      for (int c0 = 0; c0 < s0.ncol; c0 += ncs) {
-        const int nc = std::min(ncs, s0.ncol - c0);
-        blks.push_back(P1Blk{g, c0, nc, nslots[g]});
-        smem = std::max(smem, (size_t)nslots[g] * nc * sizeof(float));
-      }
-    }
-    std::vector<int> slot((size_t)ng1 * P.npts, -1);
-    for (int g = 0; g < ng1; ++g)
-      for (int si = off[g]; si < off[g + 1]; ++si)
-        for (int t = 0; t < sg[si].ntask; ++t) slot[(size_t)g * P.npts + P.tasks[h][sg[si].t0 + t]] = base[si] + t;
+  if ((size_t)maxsm >= kP1SmemCap + static_smem)
     CK(cudaFuncSetAttribute(k_sweep_p1s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(maxsm - static_smem)));
-    H.p1blk[h].upload(blks);
-    H.p1base[h].upload(base);
-    H.p1grp[h].upload(grp);
-    H.p1slot[h].upload(slot);
-    H.np1blk[h] = (int)blks.size();
-    H.p1smem[h] = smem;
-    H.p1s[h] = true;
+  DevGeom &G = *H.geom;
+  std::lock_guard<std::mutex> lk(G.mu);
+  if (!G.p1s_built) {
+    for (int h = 0; h < 2; ++h) {
+      G.p1s_ok[h] = false;
+      const std::vector<int> &off = P.p1off[h];
+      const int ng1 = (int)off.size() - 1;
+      if (!H.march[h] || ng1 <= 0 || (size_t)maxsm < kP1SmemCap + static_smem) continue;
+      const std::vector<Seg> &sg = P.p1segs[h];
+      std::vector<int> base(sg.size(), 0), grp(sg.size(), 0), nslots(ng1, 0);
+      bool ok = true;
+      for (int g = 0; g < ng1 && ok; ++g) {
+        if (off[g + 1] - off[g] > P1_SEGCAP) ok = false;
+        for (int si = off[g]; si < off[g + 1]; ++si) {
+          base[si] = nslots[g];
+          grp[si] = g;
+          nslots[g] += sg[si].ntask;
+          if (sg[si].col0 != sg[off[g]].col0 || sg[si].ncol != sg[off[g]].ncol) ok = false;
+        }
+        if ((size_t)nslots[g] * sizeof(float) > kP1SmemCap) ok = false;
+      }
+      if (!ok) continue;
+      std::vector<P1Blk> blks;
+      size_t smem = 0;
+      for (int g = 0; g < ng1; ++g) {
+        if (off[g + 1] == off[g]) continue;
+        const Seg &s0 = sg[off[g]];
+        int maxtask = 0;
+        for (int si = off[g]; si < off[g + 1]; ++si) maxtask = std::max(maxtask, sg[si].ntask);
+        int ncs = (int)std::min<size_t>(kP1SmemCap / ((size_t)nslots[g] * sizeof(float)), (size_t)s0.ncol);
+        ncs = std::max(1, std::min(ncs, 4 * P1_THREADS / std::max(1, maxtask)));
+        for (int c0 = 0; c0 < s0.ncol; c0 += ncs) {
+          const int nc = std::min(ncs, s0.ncol - c0);
+          blks.push_back(P1Blk{g, c0, nc, nslots[g]});
+          smem = std::max(smem, (size_t)nslots[g] * nc * sizeof(float));
+        }
+      }
+      std::vector<int> slot((size_t)ng1 * P.npts, -1);
+      for (int g = 0; g < ng1; ++g)
+        for (int si = off[g]; si < off[g + 1]; ++si)
+          for (int t = 0; t < sg[si].ntask; ++t) slot[(size_t)g * P.npts + P.tasks[h][sg[si].t0 + t]] = base[si] + t;
+      G.p1blk[h].upload(blks);
+      G.p1base[h].upload(base);
+      G.p1grp[h].upload(grp);
+      G.p1slot[h].upload(slot);
+      G.np1blk[h] = (int)blks.size();
+      G.p1smem[h] = smem;
+      G.p1s_ok[h] = true;
+    }
+    G.p1s_built = true;
+  }
+  for (int h = 0; h < 2; ++h) {
+    H.p1s[h] = G.p1s_ok[h] && H.march[h];
+    if (!H.p1s[h]) continue;
+    H.p1blk[h].view(G.p1blk[h]); H.p1base[h].view(G.p1base[h]);
+    H.p1grp[h].view(G.p1grp[h]); H.p1slot[h].view(G.p1slot[h]);
+    H.np1blk[h] = G.np1blk[h]; H.p1smem[h] = G.p1smem[h];
   }
 }
 
