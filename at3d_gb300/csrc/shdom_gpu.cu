@@ -4644,7 +4644,7 @@ static void prepare_grad(Handle &H, int ipa) {
     }
     sjptr[ip + 1] = (int)sjiph.size();
     if (P.npart == 1) {
-      for (int l = 0; l < nl; ++l) legu[(size_t)ip * nl + l] = P.sp_legu[o * nl + l];
+      shdom::species_series(P, ipa, ip, &legu[(size_t)ip * nl]);
     } else {
       std::fill(lt.begin(), lt.end(), 0.f);
       for (int nb = 0; nb < 8; ++nb) {

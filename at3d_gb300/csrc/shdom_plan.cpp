@@ -685,7 +685,7 @@ bool build_medium(const shdom_problem &p, Plan &P) {
     for (int ipt = 0; ipt < npts; ++ipt) P.total_ext[ipt] += ext[(size_t)ipa * npts + ipt];
   }
   if (bad) { P.err = "TRILIN: grid point beyond the property grid"; return false; }
-  const float phasemax = 0.999f;
+  const float phasemax = kPhaseMax;
   auto fterm = [&](size_t o) {  // f = mixed Legendre term ML+1 of one species at one point
     const int *IP = &iph[o * nq];
     const float *PW = &pw[o * nq];
@@ -743,7 +743,6 @@ bool build_medium(const shdom_problem &p, Plan &P) {
   P.leg = leg;
   P.sp_ext = ext; P.sp_alb = alb;
   P.sp_f.assign((size_t)npart * npts, 0.f);
-  P.sp_legu.assign((size_t)npart * npts * (ml + 1), 0.f);
   // Per-point source coefficients c_l = albedo_mix * chi_mix(l) (the
   // NEWMETHOD mixing of COMPUTE_SOURCE, src/polarized/shdomsub1.f:1413-1485)
   // and the exact single-scatter mixture of COMPUTE_SOURCE_1CELL_UNPOL
@@ -783,11 +782,7 @@ bool build_medium(const shdom_problem &p, Plan &P) {
           }
         float f = 0.f;
         if (p.deltam) { f = lt1[ml + 1]; for (int l = 0; l <= ml; ++l) lt1[l] /= (1.f - f); }
-        {  // the species' own series, delta-M scaling undone (COMPUTE_SOURCE_GRAD_1CELL)
-          P.sp_f[o] = f;
-          float *u = &P.sp_legu[o * (ml + 1)];
-          for (int l = 0; l <= ml; ++l) u[l] = p.deltam ? lt1[l] * (1.f - f) + f : lt1[l];
-        }
+        P.sp_f[o] = f;
         double scat = (double)(ext[o] * alb[o]);
         sumscat += scat;
         for (int l = 0; l <= nleg; ++l) lt[l] += scat * lt1[l];
@@ -1015,6 +1010,10 @@ bool build_medium(const shdom_problem &p, Plan &P) {
       }
     }
   }
+  // the per-point phase indices and weights, kept for species_series
+  P.sp_iph = std::move(iph);
+  P.sp_pw = std::move(pw);
+  P.sp_nq = nq;
   return true;
 }
 
@@ -1499,6 +1498,29 @@ bool build_plan(const shdom_problem &p, Plan &P) {
       }
   }
   return true;
+}
+
+// The species' own series at a grid point, delta-M scaling undone (the
+// series COMPUTE_SOURCE_GRAD_1CELL uses): the same mixture and scaling as
+// the coefficient loop of build_medium.
+void species_series(const Plan &P, int ipa, int ipt, float *u) {
+  const int nq = P.sp_nq, nl1 = P.nleg + 1, ml = P.ml;
+  const size_t o = (size_t)ipa * P.npts + ipt;
+  const int *IP = &P.sp_iph[o * nq];
+  const float *PW = &P.sp_pw[o * nq];
+  std::vector<float> lt1(nl1, 0.f);
+  if (PW[0] >= kPhaseMax) {
+    for (int l = 0; l < nl1; ++l) lt1[l] = P.leg[(size_t)(IP[0] - 1) * nl1 + l];
+  } else {
+    for (int q = 0; q < nq; ++q) {
+      if (PW[q] <= 1e-5f) continue;
+      for (int l = 0; l < nl1; ++l) lt1[l] += P.leg[(size_t)(IP[q] - 1) * nl1 + l] * PW[q];
+    }
+  }
+  const bool deltam = P.prob.deltam != 0;
+  float f = 0.f;
+  if (deltam) { f = lt1[ml + 1]; for (int l = 0; l <= ml; ++l) lt1[l] /= (1.f - f); }
+  for (int l = 0; l <= ml; ++l) u[l] = deltam ? lt1[l] * (1.f - f) + f : lt1[l];
 }
 
 }  // namespace shdom

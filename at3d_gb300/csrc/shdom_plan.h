@@ -166,7 +166,12 @@ struct Plan {
   std::vector<int> prop_iph;                        // [npart][ng][maxnmicro], 1-based table rows
   std::vector<float> leg;                           // [numphase][nleg+1] l/(2l+1) scaled, minus f for l <= ML with delta-M
   std::vector<float> sp_ext, sp_alb, sp_f;          // [npart][npts] delta-M scaled extinction, albedo, f
-  std::vector<float> sp_legu;                       // [npart][npts][ml+1] species phase series, unscaled
+  // [npart][npts][sp_nq] the phase-table indices (1-based) and weights each
+  // grid point interpolates from the property grid (for the gradient's
+  // species phase series, formed on demand by species_series)
+  std::vector<int> sp_iph;
+  std::vector<float> sp_pw;
+  int sp_nq = 0;
   // ---- numerical parameters
   shdom_problem prob{};
   // ---- wavefront schedule, per hemisphere (0 down, 1 up)
@@ -189,6 +194,13 @@ struct Plan {
 
 // Fills every table of the plan; returns false with plan.err set on error.
 bool build_plan(const shdom_problem &p, Plan &plan);
+
+// A phase-table weight at or above this makes a point use that one entry.
+constexpr float kPhaseMax = 0.999f;
+
+// The Legendre series of species ipa at grid point ipt with the delta-M
+// scaling undone (u[0..ml]), formed with the medium build's arithmetic.
+void species_series(const Plan &P, int ipa, int ipt, float *u);
 
 // PLANCK_FUNCTION for units 'R' (W/(m^2 sr micron) at wavelen microns),
 // 'T' (the temperature itself) and 'B' (W/(m^2 sr) over the band waveno[2], cm^-1).

@@ -19,6 +19,7 @@ from . import _lib
 from ._abi import NumericalParams, Problem, Species
 
 
+
 class SHDOMError(RuntimeError):
     """Raised for a non-zero SHDOM error code (at3d/checks.py:300-311)."""
 
