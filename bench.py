@@ -410,6 +410,45 @@ def polarized_block(args, dev):
     return out
 
 
+def render_block(args, dev):
+    """The render alone on the differentiation field (64x64x32 at 20% cloud,
+    NMU 8 / NPHI 16, 64x64 px x 9 views = 36,864 rays), solved first: mean
+    CUDA-event time of a device-resident render (rays and radiances in HBM)
+    and of the host-buffer call."""
+    import torch
+    from at3d_gb300.scenes import cloud_field, orthographic_views
+    from at3d_gb300.solver import RTE
+    pb = cloud_field(seed=4, nx=64, ny=64, nz=32, fraction=0.2, nmu=8, nphi=16, nleg=64)
+    rays = orthographic_views(pb, 64, 64)
+    n = len(rays[0])
+    r = RTE.from_problem(pb, device=dev)
+    it, _ = r.solve(args.maxiter, verbose=False)
+    d = [torch.tensor(np.asarray(x), dtype=torch.float32 if i < 3 else torch.float64, device=f"cuda:{dev}")
+         for i, x in enumerate(rays)]
+    out = torch.zeros(n, dtype=torch.float32, device=f"cuda:{dev}")
+    st = torch.cuda.current_stream()
+    args_dev = [t.data_ptr() for t in d] + [out.data_ptr(), n, st.cuda_stream]
+    for _ in range(3):
+        r.render_device(*args_dev)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 10
+    e0.record()
+    for _ in range(reps):
+        r.render_device(*args_dev)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_dev = e0.elapsed_time(e1) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        host = r.render(*rays)
+    ms_host = (time.perf_counter() - t0) * 1e3 / reps
+    r.close()
+    return {"workload": "64x64x32 cloud field, 20% cloud fraction, NMU=8 NPHI=16, 64x64 px x 9 views",
+            "rays": n, "iterations": it, "ms_device": ms_dev, "ms_host_buffers": ms_host,
+            "rays_per_s": n / (ms_dev / 1e3), "mean_radiance": float(np.mean(host))}
+
+
 def thermal_block(args, dev):
     """Thermal emission (srctype 'T') on the headline grid: the 128x128x64
     cloud field of wavelength 0 made an 11 um scene (cloud single-scattering
@@ -740,7 +779,7 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=16)
     ap.add_argument("--serve-slots", type=str, default="4,8,16", help="slot counts to run at each rate")
     ap.add_argument("--only", default="", choices=["", "precision", "gradient", "polarized", "serving", "thermal",
-                                                    "config1"],
+                                                    "config1", "render"],
                     help="run one extra block alone and print its JSON (for profiling)")
     ap.add_argument("--pol-boundaries", type=str, default="periodic,open")
     args = ap.parse_args()
@@ -752,7 +791,8 @@ def main():
     if args.only:
         dev = int(os.environ.get("LOCAL_RANK", "0"))
         blk = {"precision": precision_block, "gradient": gradient_block, "polarized": polarized_block,
-               "serving": serving_block, "thermal": thermal_block, "config1": config1_block}[args.only]
+               "serving": serving_block, "thermal": thermal_block, "config1": config1_block,
+               "render": render_block}[args.only]
         print(json.dumps({args.only: blk(args, dev)}))
         return
     if args.impl == "reference":
@@ -771,6 +811,7 @@ def main():
         extras["polarized"] = polarized_block(args, dev)
         extras["thermal"] = thermal_block(args, dev)
         extras["config1"] = config1_block(args, dev)
+        extras["render"] = render_block(args, dev)
         extras["serving"] = serving_block(args, dev)
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
