@@ -3079,17 +3079,76 @@ __global__ void k_bcrad_bottom(const int *botp, int nbot, const float *botalb, c
 
 namespace shdom {
 
+// ----------------------------------------------------------------- memory
+// Device memory comes from the device's stream-ordered pool, which keeps
+// freed memory for reuse (release threshold: never): a handle's state is
+// put back without cudaFree, whose device-wide synchronization would stall
+// every other handle's work (the serving loop frees units while others
+// solve), and a new handle of the same sizes takes it again in
+// microseconds.  Allocations and frees go through one non-blocking stream
+// per device and are synchronized there, so a buffer is ready for any
+// stream when alloc returns; a buffer is freed only after every stream that
+// used it has been synchronized (the handle's destructor).
+constexpr int kMaxDevices = 64;
+static std::mutex g_alloc_mu;
+static cudaStream_t g_alloc_stream[kMaxDevices] = {};
+
+static cudaStream_t alloc_stream(int dev) {
+  if (dev < 0 || dev >= kMaxDevices) throw std::runtime_error("device index out of range");
+  std::lock_guard<std::mutex> lk(g_alloc_mu);
+  if (!g_alloc_stream[dev]) {
+    cudaMemPool_t pool;
+    CK(cudaDeviceGetDefaultMemPool(&pool, dev));
+    uint64_t keep = UINT64_MAX;
+    CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    CK(cudaStreamCreateWithFlags(&g_alloc_stream[dev], cudaStreamNonBlocking));
+  }
+  return g_alloc_stream[dev];
+}
+
+// bytes on the current device; dev receives that device
+static void *dev_alloc(size_t bytes, int &dev) {
+  CK(cudaGetDevice(&dev));
+  cudaStream_t s = alloc_stream(dev);
+  void *p = nullptr;
+  cudaError_t e = cudaMallocAsync(&p, bytes, s);
+  if (e == cudaErrorMemoryAllocation) {  // give the pool's unused memory back and try once more
+    cudaGetLastError();
+    CK(cudaStreamSynchronize(s));
+    cudaMemPool_t pool;
+    CK(cudaDeviceGetDefaultMemPool(&pool, dev));
+    CK(cudaMemPoolTrimTo(pool, 0));
+    e = cudaMallocAsync(&p, bytes, s);
+  }
+  CK(e);
+  CK(cudaStreamSynchronize(s));
+  return p;
+}
+
+static void dev_free(void *p, int dev) {
+  if (!p || dev < 0 || dev >= kMaxDevices) return;
+  int cur = -1;
+  cudaGetDevice(&cur);
+  if (cur != dev) cudaSetDevice(dev);
+  try {
+    cudaFreeAsync(p, alloc_stream(dev));
+  } catch (const std::exception &) {
+  }
+  if (cur != dev && cur >= 0) cudaSetDevice(cur);
+}
+
 // ----------------------------------------------------------------- handle
 template <class T>
 struct DBuf {
   T *p = nullptr;
   size_t n = 0;
   bool own = true;  // false: a view of a buffer that a shared geometry owns
+  int dev = -1;
   void alloc(size_t k) {
     free();
     n = k;
     own = true;
-    if (k) CK(cudaMalloc(&p, k * sizeof(T)));
+    if (k) p = static_cast<T *>(dev_alloc(k * sizeof(T), dev));
   }
   void view(const DBuf &o) {
     free();
@@ -3101,7 +3160,10 @@ struct DBuf {
   }
   // on the handle's (non-blocking) stream, so that later kernels on it are ordered after the fill
   void zero(cudaStream_t st) { if (n) CK(cudaMemsetAsync(p, 0, n * sizeof(T), st)); }
-  void free() { if (p && own) cudaFree(p); p = nullptr; n = 0; own = true; }
+  void free() {
+    if (p && own) dev_free(p, dev);
+    p = nullptr; n = 0; own = true;
+  }
   ~DBuf() { free(); }
 };
 
@@ -3160,6 +3222,7 @@ struct Handle {
   DBuf<double> g_grad, g_beam, g_adj;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaEvent_t ev_caller[2] = {nullptr, nullptr};  // ordering against a caller's stream (device-buffer calls)
+  cudaEvent_t ev_ext = nullptr;  // after the last render launched on a caller's stream
   int coop_blocks = 0;
   int nsm = 152;  // streaming multiprocessors of the handle's device
   // 0: cooperative persistent kernel when available; 1: one launch per level;
@@ -4230,8 +4293,15 @@ using shdom::Handle;
 struct shdom_handle {
   Handle h;
   ~shdom_handle() {
+    // the state's buffers go back to the pool after this body: first let every
+    // stream that used them finish (the handle's two, and a caller's stream
+    // that a device-buffer render ran on)
+    if (h.stream) cudaStreamSynchronize(h.stream);
+    if (h.stream2) cudaStreamSynchronize(h.stream2);
+    if (h.ev_ext) cudaEventSynchronize(h.ev_ext);
     for (auto &g : h.iter_graph)
       if (g) cudaGraphExecDestroy(g);
+    if (h.ev_ext) cudaEventDestroy(h.ev_ext);
     if (h.stream) cudaStreamDestroy(h.stream);
     if (h.stream2) cudaStreamDestroy(h.stream2);
     if (h.ev_fork) cudaEventDestroy(h.ev_fork);
@@ -4270,12 +4340,13 @@ struct DevGuard {
 };
 
 // Device staging memory of one host-buffer call, freed on every return path.
+// A call's temporary device buffer; the call synchronizes the streams that
+// used it before returning.
 struct CallMem {
   void *p = nullptr;
-  void alloc(size_t bytes) { CK(cudaMalloc(&p, bytes)); }
-  ~CallMem() {
-    if (p) cudaFree(p);
-  }
+  int dev = -1;
+  void alloc(size_t bytes) { p = shdom::dev_alloc(bytes, dev); }
+  ~CallMem() { shdom::dev_free(p, dev); }
 };
 
 extern "C" {
@@ -4550,6 +4621,10 @@ static int render_impl(shdom_handle *hh, int nrays, const float *camx, const flo
     H.launches += 1;
   }
   CK(cudaGetLastError());
+  if (stream != H.stream) {  // the handle's buffers are in use on the caller's stream until this event
+    if (!H.ev_ext) CK(cudaEventCreateWithFlags(&H.ev_ext, cudaEventDisableTiming));
+    CK(cudaEventRecord(H.ev_ext, stream));
+  }
   return 0;
 }
 
