@@ -677,9 +677,13 @@ bool build_medium(const shdom_problem &p, Plan &P) {
         for (int q = 0; q < nq; ++q)
           for (int q2 = q + 1; q2 < nq; ++q2)
             if (IP[q] == IP[q2]) { PW[q] += PW[q2]; PW[q2] = 0.f; }
-        for (int q = 0; q < nq; ++q) srt[q] = {PW[q], IP[q]};
-        std::stable_sort(srt.begin(), srt.end(), [](const std::pair<float, int> &a, const std::pair<float, int> &b2) { return a.first > b2.first; });
-        for (int q = 0; q < nq; ++q) { PW[q] = srt[q].first; IP[q] = srt[q].second; }
+        bool sorted = true;  // weights already non-increasing: the stable sort would keep them as they are
+        for (int q = 1; q < nq && sorted; ++q) sorted = !(PW[q] > PW[q - 1]);
+        if (!sorted) {
+          for (int q = 0; q < nq; ++q) srt[q] = {PW[q], IP[q]};
+          std::stable_sort(srt.begin(), srt.end(), [](const std::pair<float, int> &a, const std::pair<float, int> &b2) { return a.first > b2.first; });
+          for (int q = 0; q < nq; ++q) { PW[q] = srt[q].first; IP[q] = srt[q].second; }
+        }
       }
     });
     for (int ipt = 0; ipt < npts; ++ipt) P.total_ext[ipt] += ext[(size_t)ipa * npts + ipt];
@@ -694,21 +698,22 @@ bool build_medium(const shdom_problem &p, Plan &P) {
     for (int q = 0; q < nq; ++q) f += leg[(size_t)(IP[q] - 1) * (nleg + 1) + ml + 1] * PW[q];
     return f;
   };
-  if (p.deltam) {
-    for (int ipt = 0; ipt < npts; ++ipt) {
-      float s = 0.f;
-      for (int ipa = 0; ipa < npart; ++ipa) s += ext[(size_t)ipa * npts + ipt];
-      P.total_ext[ipt] = std::max(0.f, P.total_ext[ipt] - s);
-    }
-    for (int ipa = 0; ipa < npart; ++ipa)
-      for (int ipt = 0; ipt < npts; ++ipt) {
-        size_t o = (size_t)ipa * npts + ipt;
-        float f = fterm(o);
-        float a = alb[o];
-        alb[o] = (1.f - f) * a / (1.f - a * f);
-        ext[o] = (1.f - a * f) * ext[o];
-        P.total_ext[ipt] += ext[o];
+  if (p.deltam) {  // per point, the species in order (the additions of the serial loops)
+    parallel_for(npts, [&](int b, int e) {
+      for (int ipt = b; ipt < e; ++ipt) {
+        float s = 0.f;
+        for (int ipa = 0; ipa < npart; ++ipa) s += ext[(size_t)ipa * npts + ipt];
+        P.total_ext[ipt] = std::max(0.f, P.total_ext[ipt] - s);
+        for (int ipa = 0; ipa < npart; ++ipa) {
+          size_t o = (size_t)ipa * npts + ipt;
+          float f = fterm(o);
+          float a = alb[o];
+          alb[o] = (1.f - f) * a / (1.f - a * f);
+          ext[o] = (1.f - a * f) * ext[o];
+          P.total_ext[ipt] += ext[o];
+        }
       }
+    });
   }
   P.albmax = 0.f;
   for (float a : alb) P.albmax = std::max(P.albmax, a);
@@ -810,24 +815,24 @@ bool build_medium(const shdom_problem &p, Plan &P) {
       }
       tcnt[ipt] = nt;
       double albp = (etot > 1e-10f) ? sumscat / etot : 0.0;
+      // chi = lt / sumscat (lt / npart without scattering), by one reciprocal per point
+      const double inv = (sumscat > 1e-10) ? 1.0 / sumscat : 1.0 / npart;
       for (int l = 0; l <= ml; ++l) {
-        double chi = (sumscat > 1e-10) ? lt[l] / sumscat : lt[l] / npart;
-        if (l == 0) chi = 1.0;
+        const double chi = (l == 0) ? 1.0 : lt[l] * inv;
         P.coef[(size_t)ipt * nl + l] = (float)(albp * chi);
       }
       if (nstleg == 6)
         for (int e = 0; e < 3; ++e)
-          for (int l = 0; l < nl; ++l) {
-            const double chi = (sumscat > 1e-10) ? ltp[(size_t)e * nl + l] / sumscat : ltp[(size_t)e * nl + l] / npart;
-            P.coefp[((size_t)ipt * 3 + e) * nl + l] = (float)(albp * chi);
-          }
+          for (int l = 0; l < nl; ++l) P.coefp[((size_t)ipt * 3 + e) * nl + l] = (float)(albp * (ltp[(size_t)e * nl + l] * inv));
     }
   });
   // scattering points: the coefficient row is non-zero exactly when its l = 0 term (the albedo) is
   P.scat.assign(npts, 0);
   // a point has a source when it scatters or (thermal source) emits
-  for (int ipt = 0; ipt < npts; ++ipt)
-    P.scat[ipt] = P.coef[(size_t)ipt * nl] != 0.f || (!P.thermal.empty() && P.thermal[ipt] != 0.f);
+  parallel_for(npts, [&](int b, int e) {
+    for (int ipt = b; ipt < e; ++ipt)
+      P.scat[ipt] = P.coef[(size_t)ipt * nl] != 0.f || (!P.thermal.empty() && P.thermal[ipt] != 0.f);
+  });
   for (int ipt = 0; ipt < npts; ++ipt) P.tms_ptr[ipt + 1] = P.tms_ptr[ipt] + tcnt[ipt];
   P.tms_iph.assign(P.tms_ptr[npts], 0);
   P.tms_w.assign(P.tms_ptr[npts], 0.f);
