@@ -1588,74 +1588,100 @@ struct BeamGeom {
   float delx, dely, solarmu, solaraz, solarflux;
 };
 
+// DIRECT_BEAM_PROP per grid point: the ray toward the sun through the
+// property grid, the exact integral of the trilinear extinction over each
+// cell it crosses.  The reference runs the walk in double precision; here
+// the per-cell geometry and the cell integral are FP32 on offsets from the
+// cell's own corner (cell-relative coordinates in [0, 1], as the render
+// does), and the path sum and the set-up stay FP64.
 __global__ void __launch_bounds__(128) k_direct_beam(BeamGeom b) {
   const int ipt = blockIdx.x * blockDim.x + threadIdx.x;
   if (ipt >= b.npts) return;
   const int npx = b.npx, npy = b.npy, npz = b.npz, bc = b.bcflag;
   const int ipd = (b.ipflag & 4) ? 0 : b.ipflag;
   const double sunmu = -(double)b.solarmu, sunaz = (double)(float)(b.solaraz + 3.14159274f);
-  double cx = sqrt(1.0 - sunmu * sunmu) * cos(sunaz), cy = sqrt(1.0 - sunmu * sunmu) * sin(sunaz);
-  double cz = fabs(sunmu), cxi, cyi, czi;
-  if (fabs(cx) > 1e-6) cxi = 1.0 / cx; else { cx = 0; cxi = 1e20; }
-  if (fabs(cy) > 1e-6) cyi = 1.0 / cy; else { cy = 0; cyi = 1e20; }
-  if (fabs(cz) > 1e-6) czi = 1.0 / cz; else { cz = 0; czi = 1e20; }
-  const int di = cx >= 0 ? 1 : -1, dj = cy >= 0 ? 1 : -1, dk = cz >= 0 ? 1 : -1;
-  const double epsz = 1.0e-6 * (b.zlev[npz - 1] - b.zlev[0]);
+  double cxd = sqrt(1.0 - sunmu * sunmu) * cos(sunaz), cyd = sqrt(1.0 - sunmu * sunmu) * sin(sunaz);
+  double czd = fabs(sunmu), cxid, cyid, czid;
+  if (fabs(cxd) > 1e-6) cxid = 1.0 / cxd; else { cxd = 0; cxid = 1e20; }
+  if (fabs(cyd) > 1e-6) cyid = 1.0 / cyd; else { cyd = 0; cyid = 1e20; }
+  if (fabs(czd) > 1e-6) czid = 1.0 / czd; else { czd = 0; czid = 1e20; }
+  const float cx = (float)cxd, cy = (float)cyd, cz = (float)czd;
+  const float cxi = (float)cxid, cyi = (float)cyid, czi = (float)czid;
+  const int di = cxd >= 0 ? 1 : -1, dj = cyd >= 0 ? 1 : -1, dk = czd >= 0 ? 1 : -1;
   const double dxd = b.delx, dyd = b.dely, xdom = dxd * npx, ydom = dyd * npy;
+  const float dx = b.delx, dy = b.dely;
   const double z = b.gridpos[3 * ipt + 2], x = b.gridpos[3 * ipt], y = b.gridpos[3 * ipt + 1];
   int il = 0, iu = npz;
   while (iu - il > 1) { int im = (iu + il) / 2; if (z >= b.zlev[im - 1]) il = im; else iu = im; }
   int k = max(il, 1), i = (int)(x / dxd) + 1, j = (int)(y / dyd) + 1;
   if (i > npx && fabs(x - xdom) < 0.001 * dxd) i = npx;
   if (j > npy && fabs(y - ydom) < 0.001 * dyd) j = npy;
-  double xe = x, ye = y, ze = z, xp = xe, yp = ye, zp = ze;
-  bool cxf = (ipd & 1) || cx == 0.0, cyf = (ipd & 2) || cy == 0.0;
+  bool cxf = (ipd & 1) || cxd == 0.0, cyf = (ipd & 2) || cyd == 0.0;
   if ((bc & 1) && (fabs(x) < 0.01 * dxd || fabs(x - (npx - 1) * dxd) < 0.01 * dxd)) cxf = true;
   if ((bc & 2) && (fabs(y) < 0.01 * dyd || fabs(y - (npy - 1) * dyd) < 0.01 * dyd)) cyf = true;
+  // the position as offsets from the current cell's low corner
+  float lx = (float)(x - dxd * (i - 1)), ly = (float)(y - dyd * (j - 1)), lz = (float)(z - (double)b.zlev[k - 1]);
+  const float epsz = 1.0e-6f * (b.zlev[npz - 1] - b.zlev[0]);
   double path = 0.0;
   const int guard_max = 4 * (npx + npy + npz) * 64;
-  for (int guard = 0; fabs(ze - b.zlev[npz - 1]) > epsz && guard < guard_max; ++guard) {
+  for (int guard = 0; guard < guard_max; ++guard) {
+    if (k >= npz || fabsf((b.zlev[k - 1] + lz) - b.zlev[npz - 1]) <= epsz) break;  // at the top level
     const int ipn = (i == npx) ? ((bc & 1) ? npx : 1) : i + 1, jpn = (j == npy) ? ((bc & 2) ? npy : 1) : j + 1;
-    const double x0 = dxd * (i - 1), x1 = x0 + dxd, y0 = dyd * (j - 1), y1 = y0 + dyd, z0 = b.zlev[k - 1], z1 = b.zlev[k];
+    const float dz = b.zlev[k] - b.zlev[k - 1];
     const int I1 = (k - 1) + npz * (j - 1) + npz * npy * (i - 1), I2 = (k - 1) + npz * (j - 1) + npz * npy * (ipn - 1);
     const int I3 = (k - 1) + npz * (jpn - 1) + npz * npy * (i - 1), I4 = (k - 1) + npz * (jpn - 1) + npz * npy * (ipn - 1);
-    const double e1 = b.edp[I1], e2 = b.edp[I2], e3 = b.edp[I3], e4 = b.edp[I4];
-    const double e5 = b.edp[I1 + 1], e6 = b.edp[I2 + 1], e7 = b.edp[I3 + 1], e8 = b.edp[I4 + 1];
-    double sox, soy, soz;
-    if (cxf) sox = 1e30; else if (cx > 0) { sox = (x1 - xe) * cxi; xp = x1; } else { sox = (x0 - xe) * cxi; xp = x0; }
-    if (cyf) soy = 1e30; else if (cy > 0) { soy = (y1 - ye) * cyi; yp = y1; } else { soy = (y0 - ye) * cyi; yp = y0; }
-    if (cz > 0) { soz = (z1 - ze) * czi; zp = z1; } else if (cz < 0) { soz = (z0 - ze) * czi; zp = z0; } else soz = 1e30;
-    double xo = 0, yo = 0, so;
+    const float e1 = (float)b.edp[I1], e2 = (float)b.edp[I2], e3 = (float)b.edp[I3], e4 = (float)b.edp[I4];
+    const float e5 = (float)b.edp[I1 + 1], e6 = (float)b.edp[I2 + 1], e7 = (float)b.edp[I3 + 1], e8 = (float)b.edp[I4 + 1];
+    float sox, soy, soz, lxp = lx, lyp = ly, lzp = lz;
+    if (cxf) sox = 1e30f; else if (cx > 0) { sox = (dx - lx) * cxi; lxp = dx; } else { sox = (0.f - lx) * cxi; lxp = 0.f; }
+    if (cyf) soy = 1e30f; else if (cy > 0) { soy = (dy - ly) * cyi; lyp = dy; } else { soy = (0.f - ly) * cyi; lyp = 0.f; }
+    if (cz > 0) { soz = (dz - lz) * czi; lzp = dz; } else if (cz < 0) { soz = (0.f - lz) * czi; lzp = 0.f; } else soz = 1e30f;
+    float so;
+    int face;  // 0 x, 1 y, 2 z
     if (soz <= sox && soz <= soy) {
-      so = soz; if (!cxf) xp = xe + so * cx; if (!cyf) yp = ye + so * cy; k += dk;
+      so = soz; if (!cxf) lxp = lx + so * cx; if (!cyf) lyp = ly + so * cy; face = 2;
     } else if (sox <= soy) {
-      so = sox; if (!cyf) yp = ye + so * cy; zp = ze + so * cz; i += di;
-      if (i == 0) { if (bc & 1) { i = 1; cxf = true; } else { i = npx; xo = xdom; } }
-      else if (i == npx + 1) { if (bc & 1) { i = npx; cxf = true; } else { i = 1; xo = -xdom; } }
+      so = sox; if (!cyf) lyp = ly + so * cy; lzp = lz + so * cz; face = 0;
     } else {
-      so = soy; if (!cxf) xp = xe + so * cx; zp = ze + so * cz; j += dj;
-      if (j == 0) { if (bc & 2) { j = 1; cyf = true; } else { j = npy; yo = ydom; } }
-      else if (j == npy + 1) { if (bc & 2) { j = npy; cyf = true; } else { j = 1; yo = -ydom; } }
+      so = soy; if (!cxf) lxp = lx + so * cx; lzp = lz + so * cz; face = 1;
     }
-    so = fmax(so, 0.0);
-    const double ax = 1.0 / (x1 - x0), ay = 1.0 / (y1 - y0), az = 1.0 / (z1 - z0);
-    const double u0 = (xe - x0) * ax, v0 = (ye - y0) * ay, w0 = (ze - z0) * az;
-    const double du = (xp - x0) * ax - u0, dv = (yp - y0) * ay - v0, dw = (zp - z0) * az - w0;
-    const double u0m = 1 - u0, v0m = 1 - v0, w0m = 1 - w0;
-    const double A = (e1 * u0m + e2 * u0) * v0m * w0m + (e3 * u0m + e4 * u0) * v0 * w0m +
-                     (e5 * u0m + e6 * u0) * v0m * w0 + (e7 * u0m + e8 * u0) * v0 * w0;
-    const double B = (-du * v0m * w0m - dv * u0m * w0m - dw * u0m * v0m) * e1 + (du * v0m * w0m - dv * u0 * w0m - dw * u0 * v0m) * e2 +
-                     (-du * v0 * w0m + dv * u0m * w0m - dw * u0m * v0) * e3 + (du * v0 * w0m + dv * u0 * w0m - dw * u0 * v0) * e4 +
-                     (-du * v0m * w0 - dv * u0m * w0 + dw * u0m * v0m) * e5 + (du * v0m * w0 - dv * u0 * w0 + dw * u0 * v0m) * e6 +
-                     (-du * v0 * w0 + dv * u0m * w0 + dw * u0m * v0) * e7 + (du * v0 * w0 + dv * u0 * w0 + dw * u0 * v0) * e8;
-    const double vw = dv * dw, uw = du * dw, uv = du * dv;
-    const double Cc = (vw * u0m + uw * v0m + uv * w0m) * e1 + (vw * u0 - uw * v0m - uv * w0m) * e2 +
-                      (-vw * u0m + uw * v0 - uv * w0m) * e3 + (-vw * u0 - uw * v0 + uv * w0m) * e4 +
-                      (-vw * u0m - uw * v0m + uv * w0) * e5 + (-vw * u0 + uw * v0m - uv * w0) * e6 +
-                      (vw * u0m - uw * v0 - uv * w0) * e7 + (vw * u0 + uw * v0 + uv * w0) * e8;
-    const double D = du * dv * dw * (e2 + e3 + e5 + e8 - e1 - e4 - e6 - e7);
-    path += so * (A + 0.5 * B + 0.3333333333333333 * Cc + 0.25 * D);
-    xe = xp + xo; ye = yp + yo; ze = zp;
+    so = fmaxf(so, 0.f);
+    const float ax = 1.f / dx, ay = 1.f / dy, az = 1.f / dz;
+    const float u0 = lx * ax, v0 = ly * ay, w0 = lz * az;
+    const float du = lxp * ax - u0, dv = lyp * ay - v0, dw = lzp * az - w0;
+    const float u0m = 1 - u0, v0m = 1 - v0, w0m = 1 - w0;
+    const float A = (e1 * u0m + e2 * u0) * v0m * w0m + (e3 * u0m + e4 * u0) * v0 * w0m +
+                    (e5 * u0m + e6 * u0) * v0m * w0 + (e7 * u0m + e8 * u0) * v0 * w0;
+    const float B = (-du * v0m * w0m - dv * u0m * w0m - dw * u0m * v0m) * e1 + (du * v0m * w0m - dv * u0 * w0m - dw * u0 * v0m) * e2 +
+                    (-du * v0 * w0m + dv * u0m * w0m - dw * u0m * v0) * e3 + (du * v0 * w0m + dv * u0 * w0m - dw * u0 * v0) * e4 +
+                    (-du * v0m * w0 - dv * u0m * w0 + dw * u0m * v0m) * e5 + (du * v0m * w0 - dv * u0 * w0 + dw * u0 * v0m) * e6 +
+                    (-du * v0 * w0 + dv * u0m * w0 + dw * u0m * v0) * e7 + (du * v0 * w0 + dv * u0 * w0 + dw * u0 * v0) * e8;
+    const float vw = dv * dw, uw = du * dw, uv = du * dv;
+    const float Cc = (vw * u0m + uw * v0m + uv * w0m) * e1 + (vw * u0 - uw * v0m - uv * w0m) * e2 +
+                     (-vw * u0m + uw * v0 - uv * w0m) * e3 + (-vw * u0 - uw * v0 + uv * w0m) * e4 +
+                     (-vw * u0m - uw * v0m + uv * w0) * e5 + (-vw * u0 + uw * v0m - uv * w0) * e6 +
+                     (vw * u0m - uw * v0 - uv * w0) * e7 + (vw * u0 + uw * v0 + uv * w0) * e8;
+    const float D = du * dv * dw * (e2 + e3 + e5 + e8 - e1 - e4 - e6 - e7);
+    path += (double)(so * (A + 0.5f * B + 0.3333333333f * Cc + 0.25f * D));
+    // into the next cell: the crossed face's offset is 0 or the new cell's extent
+    if (face == 2) {
+      k += dk;
+      lx = lxp; ly = lyp;
+      lz = (dk > 0) ? 0.f : ((k >= 1 && k < npz) ? b.zlev[k] - b.zlev[k - 1] : 0.f);
+      if (k < 1) break;
+    } else if (face == 0) {
+      i += di;
+      if (i == 0) { if (bc & 1) { i = 1; cxf = true; } else { i = npx; } }
+      else if (i == npx + 1) { if (bc & 1) { i = npx; cxf = true; } else { i = 1; } }
+      lx = cxf ? lxp : ((di > 0) ? 0.f : dx);
+      ly = lyp; lz = lzp;
+    } else {
+      j += dj;
+      if (j == 0) { if (bc & 2) { j = 1; cyf = true; } else { j = npy; } }
+      else if (j == npy + 1) { if (bc & 2) { j = npy; cyf = true; } else { j = 1; } }
+      ly = cyf ? lyp : ((dj > 0) ? 0.f : dy);
+      lx = lxp; lz = lzp;
+    }
   }
   b.dirflux[ipt] = (float)(b.solarflux * exp(-path));
 }
