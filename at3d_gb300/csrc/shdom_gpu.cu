@@ -1420,35 +1420,45 @@ __global__ void __launch_bounds__(256) k_do_to_sh_light(const float *__restrict_
                                                          const int *__restrict__ pts, int npts_light,
                                                          const float *__restrict__ t4, const float *__restrict__ fluxw,
                                                          float *__restrict__ radiance, int nlm, float *__restrict__ fluxes) {
-  const int lane = threadIdx.x & 31;
+  // weights per column, padded with zeros to ldo: the four l <= 1 terms,
+  // then the downward and the upward flux weights
+  extern __shared__ float4 wsm4[];
+  float *wsm = reinterpret_cast<float *>(wsm4);
+  for (int i = threadIdx.x; i < 6 * ldo; i += blockDim.x) {
+    const int r = i / ldo, c = i - r * ldo;
+    float v = 0.f;
+    if (c < nang) {
+      if (r < 4) v = __ldg(t4 + r * nang + c);
+      else if (r == 4) v = c < ncol_down ? __ldg(fluxw + c) : 0.f;
+      else v = c >= ncol_down ? __ldg(fluxw + c) : 0.f;
+    }
+    wsm[i] = v;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, n4 = ldo >> 2;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < npts_light; w += nw) {
     const int p = __ldg(pts + w);
-    const float *row = raddo + (size_t)p * ldo;
-    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f, fd = 0.f, fu = 0.f;
-    for (int c = lane; c < nang; c += 32) {
-      const float v = row[c];
-      a0 = fmaf(__ldg(t4 + c), v, a0);
-      a1 = fmaf(__ldg(t4 + nang + c), v, a1);
-      a2 = fmaf(__ldg(t4 + 2 * nang + c), v, a2);
-      a3 = fmaf(__ldg(t4 + 3 * nang + c), v, a3);
-      const float fv = __ldg(fluxw + c) * v;
-      if (c < ncol_down) fd += fv; else fu += fv;
+    const float4 *row = reinterpret_cast<const float4 *>(raddo + (size_t)p * ldo);
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
+    for (int q = lane; q < n4; q += 32) {
+      const float4 v = __ldcs(row + q);  // read once: streamed past L1
+#pragma unroll
+      for (int r = 0; r < 6; ++r) {
+        const float4 wr = wsm4[r * n4 + q];
+        acc[r] = fmaf(wr.x, v.x, fmaf(wr.y, v.y, fmaf(wr.z, v.z, fmaf(wr.w, v.w, acc[r]))));
+      }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
-      a3 += __shfl_xor_sync(0xffffffffu, a3, o);
-      fd += __shfl_xor_sync(0xffffffffu, fd, o);
-      fu += __shfl_xor_sync(0xffffffffu, fu, o);
-    }
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int r = 0; r < 6; ++r) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
     if (lane == 0) {
-      float *r = radiance + (size_t)p * nlm;
-      r[0] = a0; r[1] = a1; r[2] = a2; r[3] = a3;
-      fluxes[2 * (size_t)p] = fd;
-      fluxes[2 * (size_t)p + 1] = fu;
+      float *rr = radiance + (size_t)p * nlm;
+      rr[0] = acc[0]; rr[1] = acc[1]; rr[2] = acc[2]; rr[3] = acc[3];
+      fluxes[2 * (size_t)p] = acc[4];
+      fluxes[2 * (size_t)p + 1] = acc[5];
     }
   }
 }
@@ -4068,7 +4078,7 @@ static void transform(Handle &H, int dir) {
       }
       if (dir == 1 && H.nlight > 0) {
         const int lb = std::min((H.nlight + 7) / 8, 152 * 16);
-        k_do_to_sh_light<<<lb, 256, 0, H.stream>>>(H.raddo.p, H.ldo, P.nang, P.ncol_down, H.light.p, H.nlight, H.t4.p,
+        k_do_to_sh_light<<<lb, 256, 6 * H.ldo * sizeof(float), H.stream>>>(H.raddo.p, H.ldo, P.nang, P.ncol_down, H.light.p, H.nlight, H.t4.p,
                                                     H.col_fluxw.p, H.radiance.p, P.nlm, H.fluxes.p);
         CK(cudaGetLastError());
         H.launches += 1;
