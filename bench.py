@@ -36,11 +36,11 @@ sys.path.insert(0, ROOT)
 
 NWAVE = 4
 # DRAM bytes (read + write) per point-ordinate of one k_sweep_levels launch,
-# from ncu on the 96x96x48 field (2.195 GB for 73.5M point-ordinates);
-# profiles/k_sweep_levels_cloud_field_96x96x48.md.
+# from an ncu capture of that kernel on the 96x96x48 field (2.195 GB for
+# 73.5M point-ordinates).
 LEVELS_DRAM_BYTES_PER_ITEM = 29.9
-# The same for one k_sweep_march launch, from ncu on the 96x96x48 field
-# (1.846 GB for 78.3M point-ordinates); profiles/k_sweep_march_cloud_field_96x96x48.md.
+# The same for one k_sweep_march launch, from an ncu capture of that kernel
+# on the 96x96x48 field (1.846 GB for 78.3M point-ordinates).
 MARCH_DRAM_BYTES_PER_ITEM = 23.6
 
 
