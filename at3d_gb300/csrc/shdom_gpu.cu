@@ -3762,6 +3762,15 @@ static void setup_march(Handle &H) {
         }
       }
       if (units.empty()) continue;
+      // longest units first (planes x pairs per thread), so that the units
+      // left for the second wave of clusters are the short ones
+      auto unit_time = [&](const MarchUnit &u) {
+        const MarchGrp &g = P.march[h][u.grp];
+        const int tpc = MT / u.nc;
+        return (long long)g.nA * ((u.tw * g.nV + tpc - 1) / tpc);
+      };
+      std::stable_sort(units.begin(), units.end(),
+                       [&](const MarchUnit &x, const MarchUnit &y) { return unit_time(x) > unit_time(y); });
       std::vector<MarchGrp> grps(P.march[h].begin(), P.march[h].end());
       H.mgrp[h].upload(grps);
       H.munit[h].upload(units);
