@@ -37,7 +37,11 @@ class SolversDict(OrderedDict):
     def solve(self, n_jobs: int = 1, mpi_comm=None, overwrite_solver: bool = False, maxiter: int = 100,
               verbose: bool = True, init_solution: bool = True, setup_grid: bool = True):
         """Solve every solver not yet converged (all with overwrite_solver);
-        n_jobs > 1 solves up to n_jobs of them at once on the device."""
+        n_jobs > 1 solves up to n_jobs of them at once on the device.  On one
+        GB300, n_jobs = 1 is the fastest for grids whose sweep runs as a plane
+        march (each solve already fills the GPU; four 128x128x64 wavelengths:
+        3.9 solves/s one at a time, 3.55 four at once); solvers created with
+        defer=True still plan on host threads while earlier ones solve."""
         if mpi_comm is not None:
             raise NotImplementedError("MPI distribution is not supported: one process drives one GPU")
         _, to_solve = self.to_solve(overwrite_solver)

@@ -773,7 +773,9 @@ def main():
     ap.add_argument("--nwave", type=int, default=NWAVE, help="wavelengths per step (profiling runs use 1)")
     ap.add_argument("--ref-slice", type=int, default=1, help="CPU solve iterations per reference-arm step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--jobs", type=int, default=0, help="wavelengths solved at once (default: all)")
+    ap.add_argument("--jobs", type=int, default=1,
+                    help="wavelengths solved at once (0: all; default 1, the fastest on one GPU: each solve's "
+                         "plane march already fills it)")
     ap.add_argument("--no-extras", action="store_true", help="skip the precision, gradient and serving blocks")
     ap.add_argument("--serve-rates", type=str, default="1,4,16", help="Poisson arrival rates (requests/s) to run")
     ap.add_argument("--serve-requests", type=int, default=16)
