@@ -109,6 +109,8 @@ def gb300_arm(args, rank, ws):
     pbs, rays = scenes(args)
     nr = len(rays[0])
     rtes = [RTE.from_problem(pb, device=dev, name=f"wavelength {w}") for w, pb in enumerate(pbs)]
+    for r in rtes:
+        r.set_sweep_mode(args.sweep_mode)
     solvers = SolversDict()
     for w, r in enumerate(rtes):
         solvers.add_solver(w, r)
@@ -118,7 +120,7 @@ def gb300_arm(args, rank, ws):
     iters = [0] * args.nwave
 
     def step():
-        # the wavelengths solve at once on the device (SolversDict.solve with n_jobs threads)
+        # the wavelengths' solves (SolversDict.solve; n_jobs of them at once), then their renders
         solvers.solve(n_jobs=args.jobs, overwrite_solver=True, maxiter=args.maxiter, verbose=False)
         for w, r in enumerate(rtes):
             iters[w] = r.sizes["iters"]
@@ -150,6 +152,7 @@ def gb300_arm(args, rank, ws):
     # per-kernel times (CUDA events on each handle's stream) from one more
     # step solved one wavelength at a time with the persistent sweep, for the roofline
     for w, r in enumerate(rtes):
+        r.set_sweep_mode("persistent")  # per-phase event times need the launches one by one
         r.solve(args.maxiter, verbose=False)
         phase += np.asarray(r.timings(), np.float64)
         st = r.sweep_timings()
@@ -167,6 +170,9 @@ def gb300_arm(args, rank, ws):
         for w, pb in enumerate(pbs):
             # host planning on background threads, overlapping the solves already running
             sd.add_solver(w, RTE.from_problem(pb, device=dev, defer=True))
+        if args.sweep_mode != "persistent":
+            for r in sd.values():
+                r.set_sweep_mode(args.sweep_mode)
         sd.solve(n_jobs=args.jobs, maxiter=args.maxiter, verbose=False)
         res = [r.render(*rays) for r in sd.values()]
         for r in sd.values():
@@ -773,6 +779,8 @@ def main():
     ap.add_argument("--nwave", type=int, default=NWAVE, help="wavelengths per step (profiling runs use 1)")
     ap.add_argument("--ref-slice", type=int, default=1, help="CPU solve iterations per reference-arm step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sweep-mode", default="persistent", choices=["persistent", "per_level", "graph", "levels_only"],
+                    help="RTE.set_sweep_mode of the headline solves")
     ap.add_argument("--jobs", type=int, default=1,
                     help="wavelengths solved at once (0: all; default 1, the fastest on one GPU: each solve's "
                          "plane march already fills it)")
