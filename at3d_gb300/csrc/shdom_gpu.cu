@@ -4371,6 +4371,12 @@ static int fail(shdom_handle *h, const std::string &m) {
   return 1;
 }
 
+namespace shdom {
+// Error return of the host-only entry points (no handle): the message is read
+// back with shdom_last_error(NULL) on the same thread.
+int host_fail(const std::string &m) { return fail(nullptr, m); }
+}  // namespace shdom
+
 // Makes a handle's device current for the length of an entry point and puts
 // the caller's current device back afterwards, so that a handle created on
 // one device can be used from a thread whose current device is another.

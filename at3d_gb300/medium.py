@@ -16,6 +16,8 @@
 * :func:`hg_matrix_legcoef6` -- a phase matrix whose I-I element is
   Henyey-Greenstein and whose polarization elements follow the same series
   scaled by a linear depolarisation factor (synthetic polarized medium).
+* :func:`table_to_grid` -- optical properties on the grid from microphysics
+  through a poly table (at3d.medium.table_to_grid, at3d/medium.py:1927).
 """
 from __future__ import annotations
 
@@ -107,3 +109,83 @@ def gas_species(gas_absorption, num_stokes: int = 1) -> Species:
     else:
         leg[0] = 1.0
     return Species(extinction=g, ssalb=np.zeros_like(g), legcoef=leg)
+
+
+def table_to_grid(microphysics, poly_table, inverse_mode: bool = False, num_stokes: int = 1) -> Species:
+    """Optical properties on the property grid from microphysics and a poly
+    table (table_to_grid, at3d/medium.py:1927-2080).
+
+    ``microphysics``: a mapping with 'density' [npx, npy, npz] (g/m^3, or the
+    unit the table's extinction is per) and, for each coordinate of the
+    table (e.g. 'reff', 'veff'), an array of the same shape.  Every
+    coordinate value must lie strictly inside the table's range.
+
+    * extinction = density x the table's extinction interpolated linearly in
+      all coordinates (only the interpolated extinction per unit density
+      with ``inverse_mode``);
+    * ssalb: linear interpolation;
+    * phase functions: the table entry nearest in every coordinate; the
+      entries used are gathered into the species' Legendre table and the
+      grid holds their 1-based index (``table_index`` [1, npx, npy, npz],
+      ``phase_weights`` ones);
+    * a table without coordinates gives every point its single entry.
+
+    The Legendre rows are a1 ([ntable, nleg+1]) for a scalar problem, all six
+    elements ([ntable, 6, nleg+1]) for ``num_stokes`` = 3."""
+    from scipy.interpolate import RegularGridInterpolator
+
+    density = np.asarray(microphysics["density"], np.float64)
+    if np.any(density < 0) or np.any(~np.isfinite(density)):
+        raise ValueError("'density' must be finite and non-negative")
+    leg = np.asarray(poly_table.legcoef, np.float64)
+    if leg.shape[0] != 6:
+        raise ValueError("'stokes_index' dimension of 'legcoef' must have 6 components.")
+    if not inverse_mode:
+        a0 = leg[0, 0]
+        if not np.allclose(a0, 1.0, atol=1e-7):
+            raise ValueError("0th Legendre/Wigner Coefficients must be normalized to 1.0")
+        if np.any(np.abs(leg[0, 1] / 3.0) > 1.0):
+            raise ValueError("Asymmetry Parameter (1st Legendre coefficient divided by 3)is not in the range "
+                             "[-1.0, 1.0]")
+    names = list(poly_table.coords)
+    missing = [n for n in names if n not in microphysics]
+    if missing:
+        raise KeyError("microphysics dataset is missing variables for interpolation of table onto grid.",
+                       *missing)
+    if not names:
+        ext_eff = np.full(density.shape, float(np.asarray(poly_table.extinction).reshape(-1)[0]))
+        ssalb = np.full(density.shape, float(np.asarray(poly_table.ssalb).reshape(-1)[0]))
+        rows = leg.reshape(6, leg.shape[1], -1)[..., :1]
+        index = np.ones(density.shape, np.int32)
+    else:
+        axes = [np.asarray(poly_table.coords[n], np.float64) for n in names]
+        pts = []
+        for n, ax in zip(names, axes):
+            v = np.asarray(microphysics[n], np.float64)
+            if v.shape != density.shape:
+                raise ValueError(f"microphysical variable '{n}' has shape {v.shape}, density {density.shape}")
+            if np.any(v <= ax.min()) or np.any(v >= ax.max()):
+                raise ValueError(f"Microphysical coordinate '{n}' is not within the range of the mie table.")
+            pts.append(v.reshape(-1))
+        pts = np.stack(pts, axis=1)
+        lin = lambda table: RegularGridInterpolator(axes, np.asarray(table, np.float64), method="linear")(pts)
+        ext_eff = lin(poly_table.extinction).reshape(density.shape)
+        ssalb = lin(poly_table.ssalb).reshape(density.shape)
+        nearest = np.stack([np.abs(ax[None, :] - p[:, None]).argmin(axis=1) for ax, p in zip(axes, pts.T)],
+                           axis=1)
+        flat = np.ravel_multi_index(tuple(nearest.T), tuple(ax.size for ax in axes))
+        used, inverse = np.unique(flat, return_inverse=True)
+        rows = leg.reshape(6, leg.shape[1], -1)[..., used]
+        index = (inverse.reshape(density.shape) + 1).astype(np.int32)
+    extinction = ext_eff if inverse_mode else ext_eff * density
+    if np.any(np.isnan(extinction)) or np.any(np.isnan(ssalb)):
+        raise ValueError("Unexpected NaN in interpolated optical properties")
+    if num_stokes == 3:
+        legcoef = np.ascontiguousarray(rows.transpose(2, 0, 1), np.float32)       # [ntable, 6, L+1]
+    elif num_stokes == 1:
+        legcoef = np.ascontiguousarray(rows[0].T, np.float32)                     # [ntable, L+1]
+    else:
+        raise ValueError("num_stokes must be 1 or 3")
+    return Species(extinction=extinction.astype(np.float32), ssalb=ssalb.astype(np.float32), legcoef=legcoef,
+                   table_index=index[None].astype(np.int32),
+                   phase_weights=np.ones((1,) + density.shape, np.float32))

@@ -1,0 +1,236 @@
+"""The retrieval loop: a cost and its Levis-approximate gradient as a
+function of a state vector, minimised with scipy.
+
+Mirrors at3d.optimize (at3d/optimize.py): ``ObjectiveFunction`` (:20-152)
+with its ``LevisApproxUncorrelatedL2`` constructor (:67-145), and
+``Optimizer`` (:154-248), a wrapper of ``scipy.optimize.minimize`` that
+adds prior terms to the cost and gradient, counts iterations and calls the
+user's callbacks with the optimizer.
+
+The state vector maps onto the solvers' media through a state generator:
+
+* :class:`ExtinctionState` -- the state is the extinction of one species at
+  the masked points of the property grid (one vector shared by every
+  solver, as for a gray medium);
+* :class:`DensityState` -- the state is the condensate density at the masked
+  points; each solver's extinction is density x the extinction per unit
+  density that its poly table gives for the fixed microphysics (reff,
+  veff...), through :func:`at3d_gb300.medium.table_to_grid`.  The gradient
+  is sum over solvers of dCost/dExtinction x extinction-per-density.
+
+Only extinction (or density) is retrieved: the Levis adjoint on the device
+gives dCost/dExtinction and dCost/dAlbedo, not the derivative through the
+phase functions that a retrieval of effective radius needs.
+"""
+from __future__ import annotations
+
+import time
+
+import numpy as np
+
+from .gradient import levis_approximation_grad
+
+
+class ObjectiveFunction:
+    """The data-misfit term: ``loss_fn(state, measurements) -> (loss,
+    gradient)``, with optional per-element bounds for the minimiser."""
+
+    def __init__(self, measurements, loss_fn, min_bounds=None, max_bounds=None):
+        self.measurements = measurements
+        self.loss_fn = loss_fn
+        self._bounds = list(zip(np.atleast_1d(min_bounds), np.atleast_1d(max_bounds)))
+        self._loss = None
+        self._total_obj_fn_time = 0.0
+        self._ncalls = 0
+
+    def __call__(self, state):
+        t0 = time.perf_counter()
+        loss, gradient = self.loss_fn(state, self.measurements)
+        self._total_obj_fn_time += time.perf_counter() - t0
+        self._loss = loss
+        self._ncalls += 1
+        return loss, gradient
+
+    @classmethod
+    def LevisApproxUncorrelatedL2(cls, measurements, solvers, unknown_species, set_state_fn,
+                                  project_gradient_to_state, solve_kwargs=None, gradient_kwargs=None,
+                                  min_bounds=None, max_bounds=None):
+        """The weighted least-squares misfit of every sensor in
+        ``measurements`` (a list of sensor dicts, each with its 'wavelength'
+        -- the key of its solver in ``solvers`` -- and measured 'I'), and its
+        Levis-approximate gradient (at3d/optimize.py:67-145).  Each call sets
+        the state (``set_state_fn(state)``), solves every solver
+        (``solvers.solve(**solve_kwargs)``), sums the cost and the gridded
+        gradients of the sensors of each solver, and maps the gradients onto
+        the state with ``project_gradient_to_state(state, {key: gradient
+        [npx, npy, npz, 2]})``.  ``unknown_species``: the species whose
+        extinction and albedo are differentiated.  ``gradient_kwargs`` are
+        passed to ``levis_approximation_grad`` (cost_function,
+        uncertainties...)."""
+        solve_kwargs = dict({"maxiter": 100, "verbose": False, "init_solution": True}, **(solve_kwargs or {}))
+        gradient_kwargs = dict(gradient_kwargs or {})
+
+        def loss_function(state, measurements):
+            set_state_fn(state)
+            solvers.solve(overwrite_solver=True, **solve_kwargs)
+            loss = 0.0
+            grads = {}
+            for sensor in measurements:
+                key = sensor["wavelength"]
+                if key not in solvers:
+                    raise KeyError(f"no solver for the sensor's wavelength {key}")
+                g, l, _, _ = levis_approximation_grad(solvers[key], sensor, species=unknown_species,
+                                                      **gradient_kwargs)
+                loss += l
+                grads[key] = grads[key] + g if key in grads else g
+            return loss, project_gradient_to_state(state, grads)
+
+        return cls(measurements, loss_function, min_bounds=min_bounds, max_bounds=max_bounds)
+
+    @property
+    def loss(self):
+        return self._loss
+
+    @property
+    def bounds(self):
+        return self._bounds
+
+    @property
+    def ncalls(self):
+        return self._ncalls
+
+
+class Optimizer:
+    """scipy.optimize.minimize over an :class:`ObjectiveFunction`, with prior
+    terms ``prior(state, iteration) -> (loss, gradient)`` added to the cost
+    and callbacks ``callback(optimizer=self)`` after every iteration."""
+
+    def __init__(self, objective_fn, prior_fn=None, callback_fn=None, method="L-BFGS-B",
+                 options=None):
+        self._method = method
+        self._options = dict(options) if options is not None else \
+            {"maxiter": 100, "maxls": 10, "disp": False, "gtol": 1e-16, "ftol": 1e-8}
+        self._objective_fn = objective_fn
+        self._prior_fn = list(np.atleast_1d(prior_fn)) if prior_fn is not None else None
+        self._callback_fn = list(np.atleast_1d(callback_fn)) if callback_fn is not None else []
+        self._iteration = None
+        self._state = None
+
+    def callback(self, state):
+        self._iteration += 1
+        for fn in self._callback_fn:
+            fn(optimizer=self)
+
+    def objective(self, state):
+        self._state = state
+        loss, gradient = self._objective_fn(state)
+        gradient = np.array(gradient, np.float64, copy=True)
+        if self._prior_fn is not None:
+            for prior in self._prior_fn:
+                ploss, pgrad = prior(state, self._iteration)
+                loss += ploss
+                gradient += pgrad
+        return loss, gradient
+
+    def minimize(self, initial_state, iteration_step=0, **kwargs):
+        """Local minimisation from ``initial_state``; returns scipy's result."""
+        import scipy.optimize
+
+        self._iteration = iteration_step
+        args = {"fun": self.objective, "x0": np.asarray(initial_state, np.float64), "method": self._method,
+                "jac": True, "options": self._options, "callback": self.callback}
+        args.update(kwargs)
+        if self._method not in ("CG", "Newton-CG") and "bounds" not in kwargs:
+            bounds = self._objective_fn.bounds
+            n = len(args["x0"])
+            if len(bounds) == 1:
+                args["bounds"] = [bounds[0]] * n
+            elif len(bounds) == n:
+                args["bounds"] = bounds
+        return scipy.optimize.minimize(**args)
+
+    @property
+    def objective_fn(self):
+        return self._objective_fn
+
+    @property
+    def iteration(self):
+        return self._iteration
+
+    @property
+    def method(self):
+        return self._method
+
+    @property
+    def options(self):
+        return self._options
+
+    @property
+    def state(self):
+        return self._state
+
+
+class ExtinctionState:
+    """State = extinction of ``species`` at the points where ``mask`` is
+    true; the other points keep the solvers' current extinction."""
+
+    def __init__(self, solvers, species: int, mask):
+        self.solvers = solvers
+        self.species = species
+        self.mask = np.asarray(mask, bool)
+
+    def initial_state(self, key=None):
+        s = self.solvers[key if key is not None else next(iter(self.solvers))]
+        ext, _ = s.species_properties(self.species)
+        return np.asarray(ext, np.float64)[self.mask]
+
+    def set_state(self, state):
+        for solver in self.solvers.values():
+            ext, _ = solver.species_properties(self.species)
+            ext = np.array(ext, np.float32, copy=True)
+            ext[self.mask] = np.asarray(state, np.float32)
+            solver.update_species(self.species, extinction=ext)
+
+    def project_gradient_to_state(self, state, gradients):
+        g = np.zeros(int(self.mask.sum()))
+        for grad in gradients.values():
+            g += grad[..., 0][self.mask]
+        return g
+
+
+class DensityState:
+    """State = condensate density at the masked points.  ``microphysics``:
+    the fixed parameters of the table (e.g. {'reff': [...], 'veff': [...]},
+    arrays on the property grid); ``poly_tables``: {solver key: PolyTable}.
+    The phase functions stay as the solvers hold them (density does not
+    change them); the albedo is set from the table."""
+
+    def __init__(self, solvers, species: int, mask, microphysics: dict, poly_tables: dict, density=None):
+        from .medium import table_to_grid
+
+        self.solvers = solvers
+        self.species = species
+        self.mask = np.asarray(mask, bool)
+        shape = self.mask.shape
+        self.density = np.zeros(shape) if density is None else np.array(density, np.float64, copy=True)
+        self.per_density = {}
+        self.ssalb = {}
+        for key in solvers:
+            sp = table_to_grid(dict(microphysics, density=np.ones(shape)), poly_tables[key], inverse_mode=True)
+            self.per_density[key] = np.asarray(sp.extinction, np.float64)
+            self.ssalb[key] = np.asarray(sp.ssalb, np.float32)
+
+    def initial_state(self):
+        return self.density[self.mask].copy()
+
+    def set_state(self, state):
+        self.density[self.mask] = np.asarray(state, np.float64)
+        for key, solver in self.solvers.items():
+            ext = (self.density * self.per_density[key]).astype(np.float32)
+            solver.update_species(self.species, extinction=ext, ssalb=self.ssalb[key])
+
+    def project_gradient_to_state(self, state, gradients):
+        g = np.zeros(int(self.mask.sum()))
+        for key, grad in gradients.items():
+            g += (grad[..., 0] * self.per_density[key])[self.mask]
+        return g

@@ -19,6 +19,14 @@ distributions of the workload descriptions:
   64-term Wigner-function series, the 50/50 mix of a Rayleigh matrix and a
   Henyey-Greenstein-derived matrix (g=0.8, linear depolarisation 0.03);
   Lambertian albedo 0.1, sun zenith 45 deg.
+* ``mie_cloud``: a water cloud from microphysics through Mie tables
+  (gamma size distributions, veff 0.1, water index 1.331 - 1.6e-8 i at
+  0.672 um): condensate density a Gaussian blob (sigma a quarter of the
+  domain width, peak 0.1 g/m^3) times lognormal noise (sigma 0.3),
+  effective radius rising linearly from 6 um at the base to 14 um at the
+  top, on a 24x24x16 open grid
+  (dx = dz = 0.04 km), plus a Rayleigh layer; NMU=8/NPHI=16, Lambertian
+  albedo 0.05, sun zenith 30 deg; scalar (a1 rows) or NSTOKES=3 (all six).
 * ``orthographic_views``: parallel rays on a regular pixel grid at the domain
   top for a list of view zenith angles in the azimuth-0 plane; mu and phi
   point towards the sensor (at3d/sensor.py:44-47 convention).
@@ -119,6 +127,53 @@ def cloud_field(seed: int = 2, wavelength_index: int = 0, nx: int = 128, ny: int
     return Problem(delx=dx, dely=dx, zlevels=z, species=[cloud],
                    solarmu=-float(np.cos(np.deg2rad(30.0))), solaraz=0.0, solarflux=1.0,
                    surface_albedo=0.05, params=params)
+
+
+def mie_poly_table(wavelength: float = 0.672, reff=(4.0, 20.0, 17), veff=(0.09, 0.11),
+                   max_radius: float = 30.0, refractive_index: complex = 1.331 - 1.6e-8j):
+    """Poly table of water spheres, gamma distributions on a logarithmic
+    effective-radius grid (min, max, points) and the given veff points."""
+    from .mie import get_mono_table, get_poly_table
+    from .size_distribution import gamma, get_size_distribution_grid
+    mono = get_mono_table("Water", (wavelength, wavelength), minimum_effective_radius=reff[0],
+                          max_integration_radius=max_radius, refractive_index=refractive_index, verbose=False)
+    grid = get_size_distribution_grid(
+        mono.radius, size_distribution_function=gamma, particle_density=1.0,
+        reff={"coord_min": reff[0], "coord_max": reff[1], "npoints": reff[2], "spacing": "logarithmic"},
+        veff=np.asarray(veff, np.float64))
+    return get_poly_table(grid, mono)
+
+
+def mie_microphysics(seed: int = 1, nx: int = 24, ny: int = 24, nz: int = 16, dx: float = 0.04,
+                     dz: float = 0.04, peak: float = 0.1, reff=(6.0, 14.0), veff: float = 0.1) -> dict:
+    """Density [g/m^3], reff and veff on the property grid."""
+    rng = np.random.default_rng(seed)
+    x, y, z = np.arange(nx) * dx, np.arange(ny) * dx, np.arange(nz) * dz
+    X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
+    r2 = (X - nx * dx / 2) ** 2 + (Y - ny * dx / 2) ** 2 + (Z - z[-1] / 2) ** 2
+    density = peak * np.exp(-r2 / (2 * (0.25 * nx * dx) ** 2)) * rng.lognormal(0.0, 0.3, (nx, ny, nz))
+    re = reff[0] + (reff[1] - reff[0]) * Z / max(z[-1], 1e-6)
+    return {"density": density, "reff": re, "veff": np.full_like(density, veff)}
+
+
+def mie_cloud(seed: int = 1, nx: int = 24, ny: int = 24, nz: int = 16, dx: float = 0.04, dz: float = 0.04,
+              boundary: str = "open", nmu: int = 8, nphi: int = 16, solacc: float = 1e-5,
+              num_stokes: int = 1, poly_table=None, microphysics=None) -> Problem:
+    """Water cloud whose optical properties come from Mie tables through
+    ``table_to_grid``, plus a Rayleigh layer."""
+    from .medium import table_to_grid
+    poly = mie_poly_table() if poly_table is None else poly_table
+    micro = mie_microphysics(seed, nx, ny, nz, dx, dz) if microphysics is None else microphysics
+    cloud = table_to_grid(micro, poly, num_stokes=num_stokes)
+    ray_ext = np.full((nx, ny, nz), 0.01, np.float32)
+    ray_leg = rayleigh_legcoef6(0.03) if num_stokes == 3 else rayleigh_legcoef(0.672)
+    rayleigh = Species(extinction=ray_ext, ssalb=np.ones_like(ray_ext), legcoef=ray_leg)
+    params = NumericalParams(num_mu_bins=nmu, num_phi_bins=nphi, solution_accuracy=solacc,
+                             split_accuracy=0.0, x_boundary_condition=boundary,
+                             y_boundary_condition=boundary)
+    return Problem(delx=dx, dely=dx, zlevels=(np.arange(nz) * dz).astype(np.float32), species=[cloud, rayleigh],
+                   solarmu=-float(np.cos(np.deg2rad(30.0))), solaraz=0.0, solarflux=1.0,
+                   surface_albedo=0.05, params=params, num_stokes=num_stokes)
 
 
 def orthographic_views(problem: Problem, npix_x: int, npix_y: int, zeniths=VIEW_ZENITHS):

@@ -227,6 +227,21 @@ int shdom_set_transform_mode(shdom_handle *h, int mode);
  * whole iteration in its first entry.  No reference counterpart. */
 int shdom_set_sweep_mode(shdom_handle *h, int mode);
 
+/* Lorenz-Mie single scattering of homogeneous spheres at one wavelength, a
+ * table over radii (host computation in FP64, threaded over radii; no device
+ * work and no handle).  Replaces core.compute_mie_all_sizes with avgflag 'C'
+ * (at3d/mie.py:223-236; MIE_ONE, src/polarized/miewig.f:5-108, from
+ * COMPUTE_MIE_ALL_SIZES, src/polarized/make_mie_table.f90:381-482).
+ * wavelength and radii in microns; the refractive index is m_re + i m_im
+ * with m_im <= 0 for absorbing particles (n - ik, the reference's sign).  nthreads
+ * <= 0 uses every core.  Outputs: extinct, scatter [nsize] cross sections in
+ * um^2; nleg [nsize] = min(maxleg, 2 x series length); legcoef
+ * [nsize][maxleg+1][6] the Wigner expansion coefficients a1, a2, a3, a4, b1,
+ * b2 of the phase matrix times the scattering cross section (zero beyond
+ * nleg).  Errors: 1, message from shdom_last_error(NULL). */
+int shdom_mie_mono(double wavelength, double m_re, double m_im, int nsize, const float *radii, int maxleg,
+                   int nthreads, float *extinct, float *scatter, int *nleg, float *legcoef);
+
 /* Message of the last non-zero return on this handle (CHARACTER*600 errmsg
  * of the reference); a static message when h is NULL. */
 const char *shdom_last_error(shdom_handle *h);
