@@ -53,6 +53,9 @@ SIGNATURES = {
     "shdom_plan_destroy": (None, [C.c_void_p]),
     "shdom_mie_mono": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_int, _f, C.c_int, C.c_int, _f, _f, _i,
                                  _f]),
+    "shdom_phase_function_mixing": (C.c_int, [C.c_int, C.c_int, C.c_int, _f, _i, _f, C.c_int, C.c_int, C.c_int, _f,
+                                              C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, _f, _i, _i,
+                                              _i]),
 }
 
 _LIB = None

@@ -18,6 +18,8 @@
   scaled by a linear depolarisation factor (synthetic polarized medium).
 * :func:`table_to_grid` -- optical properties on the grid from microphysics
   through a poly table (at3d.medium.table_to_grid, at3d/medium.py:1927).
+* :func:`mix_optical_properties` -- several species as one, with a reduced
+  table of mixed phase functions (at3d/medium.py:900).
 """
 from __future__ import annotations
 
@@ -189,3 +191,104 @@ def table_to_grid(microphysics, poly_table, inverse_mode: bool = False, num_stok
     return Species(extinction=extinction.astype(np.float32), ssalb=ssalb.astype(np.float32), legcoef=legcoef,
                    table_index=index[None].astype(np.int32),
                    phase_weights=np.ones((1,) + density.shape, np.float32))
+
+
+def _species_table(sp: Species, num_stokes: int):
+    """A species' Legendre rows as [ntable, nleg+1, 6] (scalar rows fill a1),
+    its 1-based indices and weights as [nmicro, npts] in x-fastest order."""
+    lc = np.asarray(sp.legcoef, np.float32)
+    if num_stokes == 3:
+        lc = lc.reshape(-1, 6, lc.shape[-1])
+        rows = np.ascontiguousarray(lc.transpose(0, 2, 1))
+    else:
+        lc = np.atleast_2d(lc)
+        rows = np.zeros(lc.shape + (6,), np.float32)
+        rows[..., 0] = lc
+    shape = np.asarray(sp.extinction).shape
+    if sp.table_index is None:
+        idx = np.ones((1, int(np.prod(shape))), np.int32)
+        wt = np.ones((1, idx.shape[1]), np.float32)
+    else:
+        ti = np.asarray(sp.table_index)
+        nm = ti.shape[0]
+        idx = ti.reshape((nm,) + shape).transpose(0, 3, 2, 1).reshape(nm, -1).astype(np.int32)
+        wt = np.asarray(sp.phase_weights, np.float32).reshape((nm,) + shape).transpose(0, 3, 2, 1).reshape(nm, -1)
+    return rows, idx, wt
+
+
+def mix_optical_properties(*species, asymmetry_tol: float = 0.002, phase_tol: float = 0.01,
+                           linear_polarization_tol: float = 0.01, nangles: int = 180, maxnphase=None,
+                           maxiter: int = 1, num_stokes: int = 1) -> Species:
+    """One species equivalent to the given species on the same grid
+    (mix_optical_properties, at3d/medium.py:900-1068): extinctions add,
+    the albedo is the scattering-weighted mean, and the phase functions are
+    the greedy subset of the library's ``shdom_phase_function_mixing``: each
+    point's scattering-weighted mixture is represented by a kept entry whose
+    asymmetry, P11 at ``nangles`` angles and P12/P11 are within
+    ``asymmetry_tol``, ``phase_tol`` and ``linear_polarization_tol`` of it.
+    Points are visited x fastest, as the reference does.  ``maxnphase``
+    (default: all input phase functions) bounds the table; with ``maxiter``
+    > 1 an overflow retries with the table size extrapolated from the points
+    mixed so far.  Where nothing scatters the point takes entry 1 (its
+    phase function is never used there).  ``num_stokes``: the row layout of
+    the inputs and the result (1: a1 rows, 3: all six elements)."""
+    import ctypes as C
+
+    from . import _lib
+
+    if not species:
+        raise ValueError("no species to mix")
+    shape = np.asarray(species[0].extinction).shape
+    for sp in species:
+        if np.asarray(sp.extinction).shape != shape or np.asarray(sp.ssalb).shape != shape:
+            raise ValueError("species must be on the same grid")
+    parts = [_species_table(sp, num_stokes) for sp in species]
+    nleg = max(p[0].shape[1] for p in parts) - 1
+    nmicro = max(p[1].shape[0] for p in parts)
+    npts = int(np.prod(shape))
+    tables, offsets = [], []
+    for rows, _, _ in parts:
+        offsets.append(sum(t.shape[0] for t in tables))
+        pad = np.zeros((rows.shape[0], nleg + 1, 6), np.float32)
+        pad[:, :rows.shape[1]] = rows
+        tables.append(pad)
+    table = np.ascontiguousarray(np.concatenate(tables))
+    idx = np.ones((len(species), npts, nmicro), np.int32)
+    wt = np.zeros((len(species), npts, nmicro), np.float32)
+    scat = np.zeros((npts, len(species)), np.float32)
+    for k, ((rows, ix, w), sp) in enumerate(zip(parts, species)):
+        idx[k, :, :ix.shape[0]] = ix.T + offsets[k]
+        wt[k, :, :w.shape[0]] = w.T
+        e = np.asarray(sp.extinction, np.float32).transpose(2, 1, 0).reshape(-1)
+        a = np.asarray(sp.ssalb, np.float32).transpose(2, 1, 0).reshape(-1)
+        scat[:, k] = e * a
+    maxn = int(table.shape[0] if maxnphase is None else maxnphase)
+    lib = _lib.lib()
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))
+    for attempt in range(max(1, int(maxiter))):
+        mixed = np.zeros((maxn, nleg + 1, 6), np.float32)
+        index = np.zeros(npts, np.int32)
+        nphase = np.zeros(1, np.int32)
+        fail = np.zeros(1, np.int32)
+        rc = lib.shdom_phase_function_mixing(npts, len(species), nmicro, fp(scat), ip(idx), fp(wt), table.shape[0],
+                                             nleg, 6, fp(table), float(asymmetry_tol), float(phase_tol),
+                                             float(linear_polarization_tol), int(nangles), maxn, fp(mixed),
+                                             ip(index), ip(nphase), ip(fail))
+        if rc == 0:
+            break
+        msg = lib.shdom_last_error(None).decode()
+        if attempt == max(1, int(maxiter)) - 1 or fail[0] <= 0:
+            raise ValueError(msg)
+        maxn = int(nphase[0] / fail[0] * npts) + 10
+    n = int(nphase[0])
+    mixed = mixed[:max(n, 1)]
+    mixed[:, 0, 0] = 1.0
+    ext = np.sum([np.asarray(sp.extinction, np.float64) for sp in species], axis=0)
+    sca = scat.sum(axis=1).reshape(shape[::-1]).transpose(2, 1, 0).astype(np.float64)
+    alb = np.where(ext > 0, sca / np.where(ext > 0, ext, 1.0), 0.0)
+    index = np.where(index > 0, index, 1).reshape(shape[::-1]).transpose(2, 1, 0)
+    legcoef = mixed.transpose(0, 2, 1) if num_stokes == 3 else mixed[:, :, 0]
+    return Species(extinction=ext.astype(np.float32), ssalb=alb.astype(np.float32),
+                   legcoef=np.ascontiguousarray(legcoef, np.float32),
+                   table_index=index[None].astype(np.int32), phase_weights=np.ones((1,) + shape, np.float32))

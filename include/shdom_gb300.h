@@ -242,6 +242,25 @@ int shdom_set_sweep_mode(shdom_handle *h, int mode);
 int shdom_mie_mono(double wavelength, double m_re, double m_im, int nsize, const float *radii, int maxleg,
                    int nthreads, float *extinct, float *scatter, int *nleg, float *legcoef);
 
+/* Phase-function mixing of several species into one table (host only, no
+ * handle).  Replaces core.phase_function_mixing (at3d/medium.py:1007-1017;
+ * phase_function_mixing, src/util.f90:240-348).  For each of npts grid
+ * points in the given order, the scattering-weighted mean of the species'
+ * series (scatter [npts][npart]; 1-based phase_index and phase_weight
+ * [npart][npts][nmicro] into phase_tables [numphase][nleg+1][nstleg],
+ * nstleg 1 or 6) is matched against the entries kept so far by asymmetry,
+ * P11 and P12/P11 at nangles angles within asym_tol, phase_tol, dolp_tol,
+ * or kept as a new entry.  Outputs: mixed_table [maxnphase][nleg+1][nstleg],
+ * mixed_index [npts] (1-based; 0 where nothing scatters), *nphase.  When
+ * more than maxnphase entries are needed: 1, with *nphase the count reached
+ * and *fail_point the 1-based point (may be NULL).  A non-positive P11 is
+ * an error.  Errors: message from shdom_last_error(NULL). */
+int shdom_phase_function_mixing(int npts, int npart, int nmicro, const float *scatter, const int *phase_index,
+                                const float *phase_weight, int numphase, int nleg, int nstleg,
+                                const float *phase_tables, double asym_tol, double phase_tol, double dolp_tol,
+                                int nangles, int maxnphase, float *mixed_table, int *mixed_index, int *nphase,
+                                int *fail_point);
+
 /* Message of the last non-zero return on this handle (CHARACTER*600 errmsg
  * of the reference); a static message when h is NULL. */
 const char *shdom_last_error(shdom_handle *h);
