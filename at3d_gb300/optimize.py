@@ -31,6 +31,14 @@ import numpy as np
 from .gradient import levis_approximation_grad
 
 
+def _sensor_list(measurements):
+    """(sensor, uncertainty model) pairs of a SensorsDict or a list of sensors."""
+    from .containers import SensorsDict
+    if isinstance(measurements, SensorsDict):
+        return [(s, inst.get("uncertainty_model")) for inst in measurements.values() for s in inst["sensor_list"]]
+    return [(s, None) for s in measurements]
+
+
 class ObjectiveFunction:
     """The data-misfit term: ``loss_fn(state, measurements) -> (loss,
     gradient)``, with optional per-element bounds for the minimiser."""
@@ -56,8 +64,10 @@ class ObjectiveFunction:
                                   project_gradient_to_state, solve_kwargs=None, gradient_kwargs=None,
                                   min_bounds=None, max_bounds=None):
         """The weighted least-squares misfit of every sensor in
-        ``measurements`` (a list of sensor dicts, each with its 'wavelength'
-        -- the key of its solver in ``solvers`` -- and measured 'I'), and its
+        ``measurements`` (a SensorsDict, or a list of sensor dicts, each with
+        its 'wavelength' -- the key of its solver in ``solvers`` -- and
+        measured 'I'; a sensor's 'uncertainties' and its instrument's
+        uncertainty model set the weights and the cost function), and its
         Levis-approximate gradient (at3d/optimize.py:67-145).  Each call sets
         the state (``set_state_fn(state)``), solves every solver
         (``solvers.solve(**solve_kwargs)``), sums the cost and the gridded
@@ -75,12 +85,16 @@ class ObjectiveFunction:
             solvers.solve(overwrite_solver=True, **solve_kwargs)
             loss = 0.0
             grads = {}
-            for sensor in measurements:
+            for sensor, model in _sensor_list(measurements):
                 key = sensor["wavelength"]
                 if key not in solvers:
                     raise KeyError(f"no solver for the sensor's wavelength {key}")
-                g, l, _, _ = levis_approximation_grad(solvers[key], sensor, species=unknown_species,
-                                                      **gradient_kwargs)
+                kw = dict(gradient_kwargs)
+                if "uncertainties" in sensor and "uncertainties" not in kw:
+                    kw["uncertainties"] = np.asarray(sensor["uncertainties"]).transpose(2, 0, 1)
+                if model is not None and "cost_function" not in kw:
+                    kw["cost_function"] = model.cost_function
+                g, l, _, _ = levis_approximation_grad(solvers[key], sensor, species=unknown_species, **kw)
                 loss += l
                 grads[key] = grads[key] + g if key in grads else g
             return loss, project_gradient_to_state(state, grads)

@@ -89,29 +89,33 @@ def test_mie_cloud_levis_gradient(rte_cls, poly):
 
 
 def test_density_retrieval(rte_cls, poly):
-    """Nine views of a cloud rendered from the true density; the retrieval
+    """Nine views of a cloud rendered from the true density (through
+    SensorsDict.get_measurements, unit uncertainties); the retrieval
     starts from 0.6 x the truth inside the cloud and must bring the cost
     down by 100x and the density error down by 2.5x within 20 iterations
     (on the oracle the same loop reaches 1/465 of the cost and 0.13 from
     0.40 relative error)."""
-    from at3d_gb300.containers import SolversDict
+    from at3d_gb300.containers import SensorsDict, SolversDict
     from at3d_gb300.optimize import DensityState, ObjectiveFunction, Optimizer
     from at3d_gb300.sensor import orthographic_projection
+    from at3d_gb300.uncertainties import NullUncertainty
 
     shape = (16, 16, 12)
     micro = scenes.mie_microphysics(nx=16, ny=16, nz=12)
     truth = micro["density"]
     pb = scenes.mie_cloud(nx=16, ny=16, nz=12, poly_table=poly, microphysics=micro, solacc=1e-5)
-    true_rte = rte_cls.from_problem(pb)
-    true_rte.solve(100, verbose=False)
+    truth_solvers = SolversDict()
+    truth_solvers.add_solver(0.672, rte_cls.from_problem(pb))
     lx = shape[0] * pb.delx
     box = SimpleNamespace(x=np.array([0.0, lx]), y=np.array([0.0, lx]), z=np.array([0.0, float(pb.zlevels[-1])]))
-    sensors = []
+    sensors = SensorsDict()
     for zen, az in ((0.0, 0.0), (30.0, 0.0), (30.0, 90.0), (30.0, 180.0), (30.0, 270.0),
                     (50.0, 45.0), (50.0, 135.0), (50.0, 225.0), (50.0, 315.0)):
-        s = orthographic_projection(0.672, box, 0.04, 0.04, az, zen)
-        s["I"] = true_rte.integrate_to_sensor(dict(s))["I"].copy()
-        sensors.append(s)
+        sensors.add_sensor("camera", orthographic_projection(0.672, box, 0.04, 0.04, az, zen))
+    sensors.get_measurements(truth_solvers, maxiter=100, verbose=False)
+    sensors.add_uncertainty_model("camera", NullUncertainty("L2"))
+    sensors.calculate_uncertainties("camera")
+    assert sensors.npixels > 9 * 16 * 16
     start = scenes.mie_cloud(nx=16, ny=16, nz=12, poly_table=poly, microphysics=dict(micro, density=0.6 * truth),
                              solacc=1e-5)
     solvers = SolversDict()
