@@ -3191,9 +3191,11 @@ struct DBuf {
     free();
     p = o.p; n = o.n; own = false;
   }
-  void upload(const std::vector<T> &v) {
-    alloc(v.size());
-    if (n) CK(cudaMemcpy(p, v.data(), n * sizeof(T), cudaMemcpyHostToDevice));
+  void upload(const std::vector<T> &v) { upload(v.data(), v.size()); }
+  void upload(const HostVec<T> &v) { upload(v.data(), v.size()); }
+  void upload(const T *src, size_t count) {
+    alloc(count);
+    if (n) CK(cudaMemcpy(p, src, n * sizeof(T), cudaMemcpyHostToDevice));
   }
   // on the handle's (non-blocking) stream, so that later kernels on it are ordered after the fill
   void zero(cudaStream_t st) { if (n) CK(cudaMemsetAsync(p, 0, n * sizeof(T), st)); }
@@ -3613,8 +3615,8 @@ static void setup_tc(Handle &H) {
 
 // Device memory a handle for this plan holds: the uploaded tables, the
 // solution state and the tensor-core transform matrices.
-template <typename T>
-static long long vbytes(const std::vector<T> &v) { return (long long)v.size() * (long long)sizeof(T); }
+template <typename T, typename A>
+static long long vbytes(const std::vector<T, A> &v) { return (long long)v.size() * (long long)sizeof(T); }
 template <typename T>
 static long long vbytes(const SharedVec<T> &v) { return (long long)v.size() * (long long)sizeof(T); }
 

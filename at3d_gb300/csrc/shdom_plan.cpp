@@ -28,12 +28,56 @@
 #include <array>
 #include <cmath>
 #include <cstring>
+#include <cstdlib>
 #include <list>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <thread>
 
 namespace shdom {
+
+namespace {
+std::mutex g_pool_mu;
+std::multimap<size_t, void *> g_pool;          // free blocks by size
+size_t g_pool_bytes = 0;
+constexpr size_t kPoolMin = size_t(1) << 20;   // smaller blocks use the ordinary heap
+constexpr size_t kPoolKeep = size_t(4) << 30;  // bytes of free blocks kept at most
+size_t pool_size(size_t bytes) { return (bytes + 65535) & ~size_t(65535); }
+}  // namespace
+
+void *host_block_alloc(size_t bytes) {
+  if (bytes < kPoolMin) return ::operator new(bytes);
+  const size_t sz = pool_size(bytes);
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    auto it = g_pool.find(sz);
+    if (it != g_pool.end()) {
+      void *p = it->second;
+      g_pool.erase(it);
+      g_pool_bytes -= sz;
+      return p;
+    }
+  }
+  void *p = std::aligned_alloc(4096, sz);
+  if (!p) throw std::bad_alloc();
+  return p;
+}
+
+void host_block_free(void *p, size_t bytes) noexcept {
+  if (!p) return;
+  if (bytes < kPoolMin) { ::operator delete(p); return; }
+  const size_t sz = pool_size(bytes);
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  g_pool.emplace(sz, p);
+  g_pool_bytes += sz;
+  while (g_pool_bytes > kPoolKeep) {  // drop the largest free blocks first
+    auto it = std::prev(g_pool.end());
+    g_pool_bytes -= it->first;
+    std::free(it->second);
+    g_pool.erase(it);
+  }
+}
 
 namespace {
 
@@ -622,12 +666,15 @@ bool build_medium(const shdom_problem &p, Plan &P) {
     if (p.iphasep[k] < 1 || p.iphasep[k] > p.numphase) { P.err = "Phase function indices are out of bounds."; return false; }
   const float zspan = p.zlevels[npz - 1] - p.zlevels[0];
   const double extmin = (double)(1.0e-5f / (zspan / (float)npz)), scatmin = 0.1 * extmin;
-  std::vector<float> ext((size_t)npart * npts), alb((size_t)npart * npts);
-  std::vector<int> iph((size_t)npart * npts * nq);
-  std::vector<float> pw((size_t)npart * npts * nq);
+  // every element of these is written by the interpolation pass
+  HostVec<float> &ext = P.sp_ext, &alb = P.sp_alb;  // the delta-M scaled species properties, kept for the gradient
+  ext.clear(); ext.resize((size_t)npart * npts);
+  alb.clear(); alb.resize((size_t)npart * npts);
+  HostVec<int> iph((size_t)npart * npts * nq);
+  HostVec<float> pw((size_t)npart * npts * nq);
   P.total_ext.assign(npts, 0.f);
   const bool therm = P.srct != 'S';
-  std::vector<float> temp(therm ? npts : 0);  // TEMP of the grid points (TRILIN_INTERP_PROP)
+  HostVec<float> temp(therm ? npts : 0);  // TEMP of the grid points (TRILIN_INTERP_PROP)
   bool bad = false;
   for (int ipa = 0; ipa < npart; ++ipa) {
     parallel_for(npts, [&](int b, int e) {
@@ -722,8 +769,8 @@ bool build_medium(const shdom_problem &p, Plan &P) {
   // weights of COMPUTE_SOURCE (TOTAL_PLANCK, src/polarized/shdomsub1.f:1092-1139)
   P.thermal.clear(); P.planckpt.clear();
   if (therm) {
-    P.thermal.assign(npts, 0.f);
-    P.planckpt.assign(npts, 0.f);
+    P.thermal.clear(); P.thermal.resize(npts);      // written for every point below
+    P.planckpt.clear(); P.planckpt.resize(npts);
     parallel_for(npts, [&](int b, int e) {
       for (int ipt = b; ipt < e; ++ipt) {
         const float bb = planck_fn(temp[ipt], P.unitc, p.wavelen, p.waveno);
@@ -746,22 +793,23 @@ bool build_medium(const shdom_problem &p, Plan &P) {
   P.prop_iph.assign(p.iphasep, p.iphasep + (size_t)npart * ng * nmic);
   P.prop_phw.assign(p.phasewtp, p.phasewtp + (size_t)npart * ng * nmic);
   P.leg = leg;
-  P.sp_ext = ext; P.sp_alb = alb;
-  P.sp_f.assign((size_t)npart * npts, 0.f);
+  P.sp_f.clear(); P.sp_f.resize((size_t)npart * npts);  // written for every (species, point) below
   // Per-point source coefficients c_l = albedo_mix * chi_mix(l) (the
   // NEWMETHOD mixing of COMPUTE_SOURCE, src/polarized/shdomsub1.f:1413-1485)
   // and the exact single-scatter mixture of COMPUTE_SOURCE_1CELL_UNPOL
   // (src/polarized/shdomsub2.f:3113-3170).
   const int nl = ml + 1;
-  P.coef.assign((size_t)npts * nl, 0.f);
-  if (nstleg == 6) P.coefp.assign((size_t)npts * 3 * nl, 0.f);
-  else P.coefp.clear();
-  P.tms_ptr.assign(npts + 1, 0);
+  // coefficient rows: every entry is written by the pass below
+  P.coef.clear(); P.coef.resize((size_t)npts * nl);
+  P.coefp.clear();
+  if (nstleg == 6) P.coefp.resize((size_t)npts * 3 * nl);
+  P.tms_ptr.clear(); P.tms_ptr.resize(npts + 1);
+  P.tms_ptr[0] = 0;
   P.tms_iph.clear(); P.tms_w.clear();
   // two passes over the points on host threads: the coefficients and the
   // number of single-scatter entries of each point, then (after the prefix
   // sum) the entries themselves
-  std::vector<int> tcnt(npts, 0);
+  HostVec<int> tcnt(npts);  // written for every point
   parallel_for(npts, [&](int pb, int pe) {
     std::vector<double> ltp(nstleg == 6 ? 3 * nl : 0);
     std::vector<float> ltp1(nstleg == 6 ? 3 * nl : 0);
@@ -834,8 +882,8 @@ bool build_medium(const shdom_problem &p, Plan &P) {
       P.scat[ipt] = P.coef[(size_t)ipt * nl] != 0.f || (!P.thermal.empty() && P.thermal[ipt] != 0.f);
   });
   for (int ipt = 0; ipt < npts; ++ipt) P.tms_ptr[ipt + 1] = P.tms_ptr[ipt] + tcnt[ipt];
-  P.tms_iph.assign(P.tms_ptr[npts], 0);
-  P.tms_w.assign(P.tms_ptr[npts], 0.f);
+  P.tms_iph.clear(); P.tms_iph.resize(P.tms_ptr[npts]);  // every entry is written below
+  P.tms_w.clear(); P.tms_w.resize(P.tms_ptr[npts]);
   // exact single scatter: weight (albedo * ext_ipa / ext) / (1 - f) per phase function
   parallel_for(npts, [&](int pb, int pe) {
     for (int ipt = pb; ipt < pe; ++ipt) {
@@ -858,7 +906,7 @@ bool build_medium(const shdom_problem &p, Plan &P) {
     }
   });
   // Eddington initial radiance per column (INIT_RADIANCE).
-  P.rad0.assign((size_t)npts * 4, 0.f);
+  P.rad0.clear(); P.rad0.resize((size_t)npts * 4);  // all four terms of every point are written below
   const int nz = P.nz, nlay = nz - 1;
   const float pif = (float)std::acos(-1.0f);
   const float c0 = std::sqrt(1.0f / pif), c1 = std::sqrt(3.0f / (4 * pif));
@@ -1030,7 +1078,7 @@ void build_direct(const shdom_problem &p, Plan &P) {
   // DIRECT_BEAM_PROP); the per-point path integrals to the sun run on the
   // device (k_direct_beam) when the plan is put on a GPU.
   const int npx = p.npx, npy = p.npy, npz = p.npz, ng = npx * npy * npz, ml = P.ml, nmic = p.maxnmicro;
-  P.extdirp.assign(ng, 0.0);
+  P.extdirp.clear(); P.extdirp.resize(ng);  // written for every property point
   for (int ip = 0; ip < ng; ++ip) {
     float acc = 0.f;
     for (int ipa = 0; ipa < p.npart; ++ipa) {

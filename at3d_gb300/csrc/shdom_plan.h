@@ -8,9 +8,11 @@
 // medium, direct beam and Eddington initial radiance.
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 #include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/shdom_problem.h"
@@ -46,6 +48,36 @@ class SharedVec {
  private:
   std::shared_ptr<std::vector<T>> p_;
 };
+
+// The large per-medium host tables (a few bytes per grid point each) live
+// in blocks taken from a process-wide pool of warm blocks and are not
+// zero-filled when allocated: re-planning a medium of the same size (the
+// next wavelength, the next iterate of a retrieval) reuses memory that is
+// already mapped instead of faulting in and clearing fresh pages.  Blocks
+// under 1 MiB use the ordinary heap; at most 4 GiB of free blocks are kept.
+// Every element must be written before it is read (resize() and the size
+// constructor leave the elements uninitialised; assign(n, v) sets them).
+void *host_block_alloc(size_t bytes);
+void host_block_free(void *p, size_t bytes) noexcept;
+template <class T>
+struct HostAlloc {
+  using value_type = T;
+  HostAlloc() = default;
+  template <class U>
+  HostAlloc(const HostAlloc<U> &) {}
+  T *allocate(size_t n) { return static_cast<T *>(host_block_alloc(n * sizeof(T))); }
+  void deallocate(T *p, size_t n) noexcept { host_block_free(p, n * sizeof(T)); }
+  template <class U, class... A>
+  void construct(U *p, A &&...a) { ::new ((void *)p) U(std::forward<A>(a)...); }
+  template <class U>
+  void construct(U *p) { ::new ((void *)p) U; }
+  template <class U>
+  bool operator==(const HostAlloc<U> &) const { return true; }
+  template <class U>
+  bool operator!=(const HostAlloc<U> &) const { return false; }
+};
+template <class T>
+using HostVec = std::vector<T, HostAlloc<T>>;
 
 // One group of sweep tasks at one wavefront level: the points (tasks[t0,
 // t0+ntask)) of trace octant b whose traces for the ordinates of face class
@@ -128,26 +160,26 @@ struct Plan {
   std::vector<float> ylmsun;                     // [nlm]
   // ---- medium on the grid
   int npart = 0, numphase = 0;
-  std::vector<float> total_ext;
-  std::vector<double> extdirp;                   // [npx*npy*npz] delta-M scaled extinction for the direct beam
-  std::vector<float> coef;                       // [npts][ml+1]: albedo * delta-M scaled Legendre term
-  std::vector<float> coefp;                      // nst = 3: [npts][3][ml+1] the same for a2, a3 and b1
+  HostVec<float> total_ext;
+  HostVec<double> extdirp;                   // [npx*npy*npz] delta-M scaled extinction for the direct beam
+  HostVec<float> coef;                       // [npts][ml+1]: albedo * delta-M scaled Legendre term
+  HostVec<float> coefp;                      // nst = 3: [npts][3][ml+1] the same for a2, a3 and b1
   std::vector<uint8_t> scat;                     // [npts] 1 where the point has a source: it scatters (a non-zero
                                                  // coefficient row) or emits (a non-zero thermal term)
-  std::vector<int> tms_ptr, tms_iph;             // CSR per point: exact single-scatter mixture
-  std::vector<float> tms_w;
+  HostVec<int> tms_ptr, tms_iph;             // CSR per point: exact single-scatter mixture
+  HostVec<float> tms_w;
   std::vector<float> phasetab;                   // [nscatangle][numphase]
   std::vector<float> phasetab2;                  // nst = 3: [nscatangle][numphase] the I-Q element
   int nscatangle = 0;
   float albmax = 0.f;
-  std::vector<float> rad0;                       // [npts][4] Eddington initial radiance
+  HostVec<float> rad0;                       // [npts][4] Eddington initial radiance
   std::vector<float> botalb;                     // surface albedo at the bottom points
   // thermal emission (srct 'T' thermal, 'B' thermal and solar; empty for
   // 'S'): thermal[i] the extinction-weighted (1 - albedo) B(T) of point i,
   // botplanck B at the bottom points, skyrad_bc the top boundary radiance
   char srct = 'S', unitc = 'R';
-  std::vector<float> thermal;                    // [npts]
-  std::vector<float> planckpt;                   // [npts] B(T) of each point (the gradient's emission term)
+  HostVec<float> thermal;                    // [npts]
+  HostVec<float> planckpt;                   // [npts] B(T) of each point (the gradient's emission term)
   std::vector<float> botplanck;                  // [nbot]
   float skyrad_bc = 0.f;
   // bidirectional surface ('R' RPV, 'W' wave-Fresnel; 0 Lambertian): its
@@ -162,15 +194,15 @@ struct Plan {
   int npx = 0, npy = 0, npz = 0, maxnmicro = 0;
   float delx = 0.f, dely = 0.f;
   double scatmin = 0.0;
-  std::vector<float> prop_ext, prop_alb, prop_phw;  // [npart][ng], [npart][ng][maxnmicro]
-  std::vector<int> prop_iph;                        // [npart][ng][maxnmicro], 1-based table rows
+  HostVec<float> prop_ext, prop_alb, prop_phw;  // [npart][ng], [npart][ng][maxnmicro]
+  HostVec<int> prop_iph;                        // [npart][ng][maxnmicro], 1-based table rows
   std::vector<float> leg;                           // [numphase][nleg+1] l/(2l+1) scaled, minus f for l <= ML with delta-M
-  std::vector<float> sp_ext, sp_alb, sp_f;          // [npart][npts] delta-M scaled extinction, albedo, f
+  HostVec<float> sp_ext, sp_alb, sp_f;          // [npart][npts] delta-M scaled extinction, albedo, f
   // [npart][npts][sp_nq] the phase-table indices (1-based) and weights each
   // grid point interpolates from the property grid (for the gradient's
   // species phase series, formed on demand by species_series)
-  std::vector<int> sp_iph;
-  std::vector<float> sp_pw;
+  HostVec<int> sp_iph;
+  HostVec<float> sp_pw;
   int sp_nq = 0;
   // ---- numerical parameters
   shdom_problem prob{};
