@@ -20,6 +20,23 @@ from ._abi import NumericalParams, Problem, Species
 
 
 
+_CREATOR = None
+_CREATOR_LOCK = threading.Lock()
+
+
+def _deferred_creator():
+    """The one background thread that builds deferred handles, in the order
+    they were requested: the first solver's planning has every host core to
+    itself, and the later ones plan (and upload) while the earlier ones
+    solve, instead of all competing for the cores before the first solve."""
+    global _CREATOR
+    with _CREATOR_LOCK:
+        if _CREATOR is None:
+            from concurrent.futures import ThreadPoolExecutor
+            _CREATOR = ThreadPoolExecutor(max_workers=1, thread_name_prefix="shdom-create")
+        return _CREATOR
+
+
 class SHDOMError(RuntimeError):
     """Raised for a non-zero SHDOM error code (at3d/checks.py:300-311)."""
 
@@ -124,7 +141,8 @@ class RTE:
         the upload run on a background thread: the call returns at once, the
         first method that needs the device state waits for them, and a
         planning error is raised there (so several solvers can be planned
-        while others already solve)."""
+        while others already solve).  Deferred creations run one at a time
+        in the order they were requested."""
         self = cls.__new__(cls)
         self.problem = problem
         self.name = name or "RTE"
@@ -154,10 +172,10 @@ class RTE:
     def _create(self, device, defer: bool = False):
         L = _lib.lib()
         self._device = int(device)
-        self._struct = self.problem.to_struct()
         self._initialized = False
 
         def make():
+            self._struct = self.problem.to_struct()
             h = C.c_void_p()
             rc = L.shdom_create(C.byref(self._struct), int(device), C.byref(h))
             if rc:
@@ -167,26 +185,17 @@ class RTE:
         if not defer:
             self._h = make()
             return
-        box = {}
-
-        def job():
-            try:
-                box["h"] = make()
-            except BaseException as e:  # raised at the first use of the handle
-                box["err"] = e
-
-        self.__dict__["_pending"] = (threading.Thread(target=job, daemon=True), box)
-        self.__dict__["_pending"][0].start()
+        self.__dict__["_pending"] = _deferred_creator().submit(make)
 
     @property
     def _h(self):
         pend = self.__dict__.pop("_pending", None)
         if pend is not None:
-            pend[0].join()
-            if "err" in pend[1]:
+            try:
+                self.__dict__["_hv"] = pend.result()
+            except BaseException:  # a planning error is raised at the first use of the handle
                 self.__dict__["_hv"] = None
-                raise pend[1]["err"]
-            self.__dict__["_hv"] = pend[1]["h"]
+                raise
         return self.__dict__.get("_hv")
 
     @_h.setter
