@@ -4,15 +4,19 @@ The numerical work runs in the CUDA library built from at3d_gb300/csrc
 (include/shdom_gb300.h is its C-ABI); this package holds the host-side
 mirror of the reference's Python interface.
 """
-from . import configuration, grid, medium, scenes, sensor, source, surface  # noqa: F401
+from . import (configuration, grid, medium, mie, scenes, sensor, size_distribution, source,  # noqa: F401
+               surface, uncertainties)
 from ._abi import NumericalParams, Problem, Species  # noqa: F401
 
-__all__ = ["RTE", "NumericalParams", "Problem", "Species", "configuration", "grid", "medium", "scenes",
-           "sensor", "source", "surface"]
+__all__ = ["RTE", "NumericalParams", "Problem", "Species", "configuration", "grid", "medium", "mie", "scenes",
+           "sensor", "size_distribution", "source", "surface", "uncertainties", "optimize", "containers"]
 
 
 def __getattr__(name):
     if name == "RTE":
         from .solver import RTE
         return RTE
+    if name in ("optimize", "containers"):   # import the solver (and its library binding) on first use
+        import importlib
+        return importlib.import_module(f".{name}", __name__)
     raise AttributeError(name)
