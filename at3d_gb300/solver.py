@@ -24,6 +24,18 @@ _CREATOR = None
 _CREATOR_LOCK = threading.Lock()
 
 
+def _lower_priority():
+    """Nice +10 for the calling thread (and the planning threads it starts,
+    which inherit it): planning then yields the cores to the thread that
+    launches a running solve's kernels, and still has them all when nothing
+    else runs."""
+    import os
+    try:
+        os.setpriority(os.PRIO_PROCESS, threading.get_native_id(), 10)
+    except (AttributeError, OSError):
+        pass
+
+
 def _deferred_creator():
     """The one background thread that builds deferred handles, in the order
     they were requested: the first solver's planning has every host core to
@@ -33,7 +45,8 @@ def _deferred_creator():
     with _CREATOR_LOCK:
         if _CREATOR is None:
             from concurrent.futures import ThreadPoolExecutor
-            _CREATOR = ThreadPoolExecutor(max_workers=1, thread_name_prefix="shdom-create")
+            _CREATOR = ThreadPoolExecutor(max_workers=1, thread_name_prefix="shdom-create",
+                                          initializer=_lower_priority)
         return _CREATOR
 
 

@@ -154,3 +154,20 @@ def test_plane_march_eligibility():
     from at3d_gb300.solver import plan_summary
     assert plan_summary(cloud_field(seed=2, nx=24, ny=20, nz=16))["march"] == 3
     assert plan_summary(cloud_blob(nx=16, ny=16, nz=10))["march"] == 0
+
+
+def test_deferred_creation_is_ordered_and_low_priority():
+    """Deferred handle creations run one at a time in request order on one
+    worker thread at nice +10 (the solver's host thread keeps its core)."""
+    import threading
+    from at3d_gb300 import solver
+    order = []
+
+    def job(i):
+        order.append(i)
+        return os.getpriority(os.PRIO_PROCESS, threading.get_native_id())
+
+    ex = solver._deferred_creator()
+    futs = [ex.submit(job, i) for i in range(6)]
+    assert [f.result() for f in futs] == [10] * 6
+    assert order == list(range(6))
