@@ -240,8 +240,11 @@ class RTE:
         return it.value, sc.value
 
     def check_solved(self, verbose: bool = True) -> bool:
-        s = self.sizes
-        ok = self._initialized and s["solcrit"] <= self.problem.params.solution_accuracy
+        # a solver whose deferred creation has not been collected has never
+        # solved: answer without waiting for it (SolversDict.to_solve asks
+        # every solver before the first one solves)
+        ok = "_pending" not in self.__dict__ and self._initialized
+        ok = ok and self.sizes["solcrit"] <= self.problem.params.solution_accuracy
         if not ok and verbose:
             warnings.warn("RTE is not converged to the specified solution_accuracy")
         return ok

@@ -171,3 +171,24 @@ def test_deferred_creation_is_ordered_and_low_priority():
     futs = [ex.submit(job, i) for i in range(6)]
     assert [f.result() for f in futs] == [10] * 6
     assert order == list(range(6))
+
+
+def test_check_solved_does_not_wait_for_a_pending_creation():
+    """SolversDict.to_solve asks every solver before the first solves: a
+    solver whose deferred creation is still queued answers 'not solved'
+    at once instead of waiting for its plan."""
+    import threading
+    import time
+    from at3d_gb300 import solver
+    from at3d_gb300.scenes import cloud_blob
+    gate = threading.Event()
+    blocker = solver._deferred_creator().submit(gate.wait, 30)
+    try:
+        r = solver.RTE.from_problem(cloud_blob(nx=8, ny=8, nz=6), defer=True)
+        t0 = time.perf_counter()
+        assert r.check_solved(verbose=False) is False
+        assert time.perf_counter() - t0 < 1.0 and "_pending" in r.__dict__
+    finally:
+        gate.set()
+    blocker.result()
+    r.__dict__["_pending"].exception(timeout=120)   # let the queued creation finish (it fails without a GPU)
