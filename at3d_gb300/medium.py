@@ -20,6 +20,9 @@
   through a poly table (at3d.medium.table_to_grid, at3d/medium.py:1927).
 * :func:`mix_optical_properties` -- several species as one, with a reduced
   table of mixed phase functions (at3d/medium.py:900).
+* :class:`OpticalPropertyGenerator` -- a scatterer's optical properties at
+  several wavelengths from its microphysics, by poly-table interpolation or
+  exact size distributions (at3d/medium.py:152).
 """
 from __future__ import annotations
 
@@ -134,6 +137,13 @@ def table_to_grid(microphysics, poly_table, inverse_mode: bool = False, num_stok
 
     The Legendre rows are a1 ([ntable, nleg+1]) for a scalar problem, all six
     elements ([ntable, 6, nleg+1]) for ``num_stokes`` = 3."""
+    return _poly_to_species(microphysics, poly_table, inverse_mode, num_stokes, strict=True)
+
+
+def _poly_to_species(microphysics, poly_table, inverse_mode: bool, num_stokes: int, strict: bool) -> Species:
+    """table_to_grid's interpolation; ``strict``: coordinates must lie strictly
+    inside the table (table_to_grid), else on or inside its bounds (the
+    nearest mode of OpticalPropertyGenerator)."""
     from scipy.interpolate import RegularGridInterpolator
 
     density = np.asarray(microphysics["density"], np.float64)
@@ -166,7 +176,9 @@ def table_to_grid(microphysics, poly_table, inverse_mode: bool = False, num_stok
             v = np.asarray(microphysics[n], np.float64)
             if v.shape != density.shape:
                 raise ValueError(f"microphysical variable '{n}' has shape {v.shape}, density {density.shape}")
-            if np.any(v <= ax.min()) or np.any(v >= ax.max()):
+            outside = (np.any(v <= ax.min()) or np.any(v >= ax.max())) if strict else \
+                (np.any(v < ax.min()) or np.any(v > ax.max()))
+            if outside:
                 raise ValueError(f"Microphysical coordinate '{n}' is not within the range of the mie table.")
             pts.append(v.reshape(-1))
         pts = np.stack(pts, axis=1)
@@ -292,3 +304,189 @@ def mix_optical_properties(*species, asymmetry_tol: float = 0.002, phase_tol: fl
     return Species(extinction=ext.astype(np.float32), ssalb=alb.astype(np.float32),
                    legcoef=np.ascontiguousarray(legcoef, np.float32),
                    table_index=index[None].astype(np.int32), phase_weights=np.ones((1,) + shape, np.float32))
+
+
+class OpticalPropertyGenerator:
+    """Optical properties of one scatterer at several wavelengths from its
+    microphysics (at3d.medium.OpticalPropertyGenerator,
+    at3d/medium.py:152-900).
+
+    ``monodisperse_tables``: {key (wavelength): MonoTable};
+    ``size_distribution_function``: ``size_distribution.gamma`` or
+    ``lognormal`` (called with ``normalization=density_normalization``);
+    ``size_distribution_parameters``: the grid of distribution parameters
+    (e.g. ``reff={'coord_min': 4, 'coord_max': 25, 'npoints': 30,
+    'spacing': 'logarithmic'}``, ``veff=np.array([...])``).
+
+    Calling it with microphysics (a mapping with 'density' and each
+    parameter on the property grid) returns {key: Species}:
+
+    * ``interpolation_mode='nearest'``: the poly table of the parameter grid
+      (made once per key), extinction and albedo interpolated linearly,
+      phase functions from the nearest table entry (the poly table route of
+      :func:`table_to_grid`, with the parameter range inclusive);
+    * ``'exact'``: a size distribution for each distinct parameter tuple of
+      the grid, integrated over the Mie table; when there are more than
+      ``maxnphase`` distinct tuples (default: the number of distributions of
+      the parameter grid), parameters are turned into tables one at a time
+      (those whose bracketing grid points repeat most, first) until the
+      bracketing tuples are few enough, and each point mixes the
+      distributions at the corners of its bracket with multilinear phase
+      weights (``table_index`` and ``phase_weights`` of num_micro = 2^k
+      entries).  Parameters left exact must then be uniform over the grid.
+
+    The last call's result is kept and returned again for the same
+    microphysics."""
+
+    VALID_INTERPOLATION_MODES = ("exact", "nearest")
+
+    def __init__(self, scatterer_name, monodisperse_tables, size_distribution_function, particle_density=1.0,
+                 maxnphase=None, interpolation_mode="exact", density_normalization="density",
+                 num_stokes: int = 1, **size_distribution_parameters):
+        import functools
+
+        from . import size_distribution as sdmod
+        if not isinstance(monodisperse_tables, dict):
+            raise TypeError("`monodisperse_tables` should be a dictionary of mie monodisperse tables.")
+        if interpolation_mode not in self.VALID_INTERPOLATION_MODES:
+            raise ValueError(f"`interpolation_mode` must be in '{self.VALID_INTERPOLATION_MODES}' not "
+                             f"'{interpolation_mode}'")
+        self.scatterer_name = scatterer_name
+        self.interpolation_mode = interpolation_mode
+        self.num_stokes = num_stokes
+        self._particle_density = particle_density
+        self._size_distribution_function = functools.update_wrapper(
+            functools.partial(size_distribution_function, normalization=density_normalization),
+            size_distribution_function)
+        self._monodisperse_tables = monodisperse_tables
+        self.size_distribution_parameters = dict(size_distribution_parameters)
+        self.size_distribution_grids = {
+            key: sdmod.get_size_distribution_grid(table.radius, size_distribution_function=self._size_distribution_function,
+                                                  particle_density=particle_density, radius_units="micron",
+                                                  **size_distribution_parameters)
+            for key, table in monodisperse_tables.items()}
+        first = next(iter(self.size_distribution_grids.values()))
+        self._names = list(first.coords)
+        self._grid_coords = [np.asarray(first.coords[n], np.float64) for n in self._names]
+        self._maxnphase = int(np.prod([c.size for c in self._grid_coords])) if maxnphase is None else int(maxnphase)
+        self._poly_tables = {}
+        self._cache = None
+
+    @property
+    def size_distribution_function(self):
+        return self._size_distribution_function
+
+    def _check_input(self, microphysics):
+        density = np.asarray(microphysics["density"], np.float64)
+        if np.any(density < 0) or np.any(~np.isfinite(density)):
+            raise ValueError("'density' must be finite and non-negative")
+        missing = [n for n in self._names if n not in microphysics]
+        if missing:
+            raise KeyError("microphysics dataset is missing variables for interpolation of table onto grid.",
+                           *missing)
+        data = []
+        for n, c in zip(self._names, self._grid_coords):
+            v = np.asarray(microphysics[n], np.float64)
+            if v.shape != density.shape:
+                raise ValueError(f"microphysical variable '{n}' has shape {v.shape}, density {density.shape}")
+            if np.any(v < c.min()) or np.any(v > c.max()):
+                raise ValueError(f"Microphysical coordinate '{n}' is not within the range of the size "
+                                 "distribution parameters.")
+            data.append(v.reshape(-1))
+        return density, np.stack(data) if data else np.zeros((0, density.size))
+
+    def __call__(self, microphysics) -> dict:
+        key = {k: np.asarray(v) for k, v in microphysics.items() if k == "density" or k in self._names}
+        if self._cache is not None and key.keys() == self._cache[0].keys() and \
+                all(np.array_equal(key[k], self._cache[0][k]) for k in key):
+            return dict(self._cache[1])
+        density, data = self._check_input(microphysics)
+        out = {}
+        if self.interpolation_mode == "nearest":
+            from .mie import get_poly_table
+            for k, table in self._monodisperse_tables.items():
+                if k not in self._poly_tables:
+                    self._poly_tables[k] = get_poly_table(self.size_distribution_grids[k], table)
+                out[k] = _poly_to_species(dict(microphysics), self._poly_tables[k], False, self.num_stokes,
+                                          strict=False)
+        else:
+            params, weights, phase_index = self._exact_size_distributions(data)
+            for k, table in self._monodisperse_tables.items():
+                out[k] = self._exact_species(density, table, params, weights, phase_index)
+        self._cache = ({k: v.copy() for k, v in key.items()}, dict(out))
+        return out
+
+    def _exact_size_distributions(self, data):
+        """Distinct parameter tuples (or the bracketing table tuples), the
+        per-point weights [ncorner, npts] and indices into the tuples."""
+        import itertools
+        nvar, npts = data.shape
+        uniq, inv = np.unique(data, axis=1, return_inverse=True)
+        inv = np.asarray(inv).reshape(-1)
+        if uniq.shape[1] <= self._maxnphase or nvar == 0:
+            return ({n: uniq[i] for i, n in enumerate(self._names)}, np.ones((1, npts)), inv[None, :])
+        # bracketing grid indices of every point in every parameter, clipped so
+        # that a value on the top grid point is bracketed by the last interval
+        dig = np.stack([np.clip(np.digitize(data[i], self._grid_coords[i]), 1, self._grid_coords[i].size - 1)
+                        for i in range(nvar)])
+        flags = np.array(list(itertools.product([-1, 0], repeat=nvar)))          # [ncorner, nvar]
+        corners = dig[None] + flags[..., None]                                   # [ncorner, nvar, npts]
+        exact_vals, combos = [], []
+        for i in range(nvar):
+            u, iv = np.unique(data[i], return_inverse=True)
+            exact_vals.append(u)
+            combos.append(np.asarray(iv).reshape(-1))
+        combos = np.repeat(np.stack(combos)[None], flags.shape[0], axis=0)
+        ucorn = np.unique(corners, axis=2)
+        ratio = np.array([np.unique(ucorn[:, i, :]).size / exact_vals[i].size for i in range(nvar)])
+        order = np.argsort(ratio, kind="stable")
+        ntab, nuniq = 0, uniq.shape[1]
+        if self._maxnphase <= 0:
+            ntab = nvar
+        while nuniq > self._maxnphase and ntab < nvar:
+            idx = order[ntab]
+            combos[:, idx, :] = corners[:, idx, :]
+            nuniq = np.unique(combos.transpose(0, 2, 1).reshape(-1, nvar), axis=0).shape[0]
+            ntab += 1
+        if nuniq > self._maxnphase:
+            raise ValueError(f"All variables are represented using tables but `maxnphase`='{self._maxnphase}' is "
+                             f"still exceeded num_unique='{nuniq}'. Please increase `maxnphase` or set to `None` "
+                             "so that all of the table may be used.")
+        tab = order[:ntab]
+        tflags = np.array(list(itertools.product([-1, 0], repeat=ntab)))       # [nct, ntab]
+        tcorn = dig[tab][None] + tflags[..., None]                              # [nct, ntab, npts]
+        tuniq, tinv = np.unique(tcorn.transpose(0, 2, 1).reshape(-1, ntab), axis=0, return_inverse=True)
+        phase_index = np.asarray(tinv).reshape(tflags.shape[0], npts)
+        weights = np.ones((tflags.shape[0], ntab, npts))
+        params = {}
+        for i, idx in enumerate(tab):
+            g = self._grid_coords[idx]
+            params[self._names[idx]] = g[tuniq[:, i]]
+            lower, upper = g[tuniq[phase_index[0], i]], g[tuniq[phase_index[-1], i]]
+            w = (data[idx] - lower) / (upper - lower)
+            weights[tflags[:, i] == -1, i] = 1.0 - w
+            weights[tflags[:, i] == 0, i] = w
+        for idx in order[ntab:]:
+            if exact_vals[idx].size != 1:
+                raise ValueError(f"parameter '{self._names[idx]}' varies over the grid but is not tabulated: "
+                                 "increase `maxnphase` or use interpolation_mode='nearest'")
+            params[self._names[idx]] = np.full(tuniq.shape[0], exact_vals[idx][0])
+        params = {n: params[n] for n in self._names}
+        return params, np.prod(weights, axis=1), phase_index
+
+    def _exact_species(self, density, table, params, weights, phase_index):
+        from .mie import get_poly_table
+        from .size_distribution import SizeDistributionGrid
+        nd = self._size_distribution_function(table.radius, **params, particle_density=self._particle_density)
+        poly = get_poly_table(SizeDistributionGrid(radius=np.asarray(table.radius), number_density=nd,
+                                                   coords={}, attrs={}), table)
+        ext = np.sum(weights * np.asarray(poly.extinction, np.float64)[phase_index], axis=0)
+        alb = np.sum(weights * np.asarray(poly.ssalb, np.float64)[phase_index], axis=0)
+        shape = density.shape
+        leg = np.asarray(poly.legcoef, np.float32)                               # [6, L+1, n]
+        legcoef = leg.transpose(2, 0, 1) if self.num_stokes == 3 else leg[0].T
+        return Species(extinction=(density * ext.reshape(shape)).astype(np.float32),
+                       ssalb=alb.reshape(shape).astype(np.float32),
+                       legcoef=np.ascontiguousarray(legcoef, np.float32),
+                       table_index=(1 + phase_index).reshape((-1,) + shape).astype(np.int32),
+                       phase_weights=weights.reshape((-1,) + shape).astype(np.float32))

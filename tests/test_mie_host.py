@@ -285,3 +285,92 @@ def test_band_average(built):
     ext = sum(wt * p[0].astype(np.float64) for wt, p in zip(weights, parts)) / sum(weights)
     assert np.allclose(t.extinction, ext, rtol=1e-5)
     assert np.allclose(t.legendre[0, 0], t.scatter, rtol=1e-5)
+
+
+@pytest.fixture(scope="module")
+def generator_tables(built):
+    kw = dict(minimum_effective_radius=4.0, max_integration_radius=30.0, verbose=False)
+    return {0.672: mie.get_mono_table("Water", (0.672, 0.672), refractive_index=1.331 - 1.6e-8j, **kw),
+            0.86: mie.get_mono_table("Water", (0.86, 0.86), refractive_index=1.329 - 3e-7j, **kw)}
+
+
+def _generator(tables, mode, **kw):
+    from at3d_gb300.medium import OpticalPropertyGenerator
+    return OpticalPropertyGenerator("cloud", tables, sd.gamma, interpolation_mode=mode,
+                                    reff={"coord_min": 4.0, "coord_max": 20.0, "npoints": 17,
+                                          "spacing": "logarithmic"},
+                                    veff=np.array([0.09, 0.1, 0.11]), **kw)
+
+
+def _micro(seed=0, shape=(5, 4, 3)):
+    rng = np.random.default_rng(seed)
+    return {"density": rng.uniform(0.0, 0.4, shape), "reff": rng.uniform(5.0, 18.0, shape),
+            "veff": np.full(shape, 0.1)}
+
+
+def test_generator_nearest_is_table_to_grid(generator_tables):
+    g = _generator(generator_tables, "nearest")
+    micro = _micro()
+    out = g(micro)
+    assert list(out) == [0.672, 0.86]
+    for key in out:
+        poly = mie.get_poly_table(g.size_distribution_grids[key], generator_tables[key])
+        ref = table_to_grid(micro, poly)
+        for f in ("extinction", "ssalb", "legcoef", "table_index", "phase_weights"):
+            assert np.array_equal(getattr(out[key], f), getattr(ref, f)), f
+    assert g(micro)[0.672] is out[0.672]        # the same microphysics returns the kept result
+
+
+def test_generator_exact_few_tuples(generator_tables):
+    """Fewer distinct (reff, veff) tuples than maxnphase: each point gets the
+    poly properties of its own exact distribution."""
+    g = _generator(generator_tables, "exact")
+    micro = _micro()
+    micro["reff"] = np.round(micro["reff"])           # a handful of distinct radii
+    sp = g(micro)[0.672]
+    r = np.unique(micro["reff"])
+    assert sp.legcoef.shape[0] == r.size and sp.table_index.shape[0] == 1
+    table = generator_tables[0.672]
+    for k, re in enumerate(r):
+        nd = sd.gamma(table.radius, [re], veff=[0.1])
+        one = mie.get_poly_table(sd.SizeDistributionGrid(radius=table.radius, number_density=nd, coords={}), table)
+        at = micro["reff"] == re
+        assert np.all(sp.table_index[0][at] == k + 1)
+        assert np.allclose(sp.extinction[at], micro["density"][at] * one.extinction[0], rtol=1e-6)
+        assert np.allclose(sp.legcoef[k], one.legcoef[0, :, 0], rtol=1e-6, atol=1e-9)
+
+
+def test_generator_exact_table_fallback(generator_tables):
+    """More distinct radii than maxnphase: reff becomes a table, every point
+    mixes the distributions at its bracketing grid radii with linear weights,
+    so the extinction equals the linear interpolation of the poly table."""
+    g = _generator(generator_tables, "exact", maxnphase=20)
+    micro = _micro(1)
+    sp = g(micro)[0.86]
+    assert sp.table_index.shape[0] == 2 and sp.phase_weights.shape[0] == 2
+    assert np.allclose(sp.phase_weights.sum(axis=0), 1.0)
+    assert sp.legcoef.shape[0] <= 17
+    near = _generator(generator_tables, "nearest")(micro)[0.86]
+    assert np.allclose(sp.extinction, near.extinction, rtol=2e-5)
+    assert np.allclose(sp.ssalb, near.ssalb, rtol=1e-6)
+    reff_grid = g.size_distribution_grids[0.86].coords["reff"]
+    lo = reff_grid[np.clip(np.digitize(micro["reff"], reff_grid), 1, reff_grid.size - 1) - 1]
+    assert np.allclose(sp.phase_weights[0], (reff_grid[np.searchsorted(reff_grid, lo) + 1] - micro["reff"]) /
+                       (reff_grid[np.searchsorted(reff_grid, lo) + 1] - lo), rtol=1e-5)
+
+
+def test_generator_errors(generator_tables):
+    from at3d_gb300.medium import OpticalPropertyGenerator
+    with pytest.raises(ValueError, match="interpolation_mode"):
+        _generator(generator_tables, "linear")
+    with pytest.raises(TypeError):
+        OpticalPropertyGenerator("c", [1], sd.gamma, reff=np.array([5.0, 6.0]))
+    g = _generator(generator_tables, "exact", maxnphase=20)
+    micro = _micro(2)
+    with pytest.raises(KeyError):
+        g({"density": micro["density"], "reff": micro["reff"]})
+    with pytest.raises(ValueError, match="within the range"):
+        g(dict(micro, reff=np.full(micro["reff"].shape, 25.0)))
+    micro["veff"] = np.where(micro["reff"] > 10, 0.095, 0.105)   # two veff values, reff tabulated
+    with pytest.raises(ValueError, match="not tabulated|maxnphase"):
+        _generator(generator_tables, "exact", maxnphase=1)(micro)
