@@ -4,12 +4,13 @@ The numerical work runs in the CUDA library built from at3d_gb300/csrc
 (include/shdom_gb300.h is its C-ABI); this package holds the host-side
 mirror of the reference's Python interface.
 """
-from . import (configuration, grid, medium, mie, scenes, sensor, size_distribution, source,  # noqa: F401
-               surface, uncertainties)
+from . import (configuration, grid, medium, mie, regularization, scenes, sensor,  # noqa: F401
+               size_distribution, source, surface, transforms, uncertainties)
 from ._abi import NumericalParams, Problem, Species  # noqa: F401
 
 __all__ = ["RTE", "NumericalParams", "Problem", "Species", "configuration", "grid", "medium", "mie", "scenes",
-           "sensor", "size_distribution", "source", "surface", "uncertainties", "optimize", "containers"]
+           "regularization", "sensor", "size_distribution", "source", "surface", "transforms", "uncertainties",
+           "optimize", "containers"]
 
 
 def __getattr__(name):

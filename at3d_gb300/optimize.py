@@ -7,16 +7,21 @@ with its ``LevisApproxUncorrelatedL2`` constructor (:67-145), and
 adds prior terms to the cost and gradient, counts iterations and calls the
 user's callbacks with the optimizer.
 
-The state vector maps onto the solvers' media through a state generator:
+The state vector maps onto the solvers' media through a state generator,
+which takes a coordinate transform and a state-to-grid map
+(:mod:`at3d_gb300.transforms`; by default the identity and one element per
+masked point) and carries the chain rule through both:
 
-* :class:`ExtinctionState` -- the state is the extinction of one species at
-  the masked points of the property grid (one vector shared by every
-  solver, as for a gray medium);
-* :class:`DensityState` -- the state is the condensate density at the masked
-  points; each solver's extinction is density x the extinction per unit
-  density that its poly table gives for the fixed microphysics (reff,
-  veff...), through :func:`at3d_gb300.medium.table_to_grid`.  The gradient
-  is sum over solvers of dCost/dExtinction x extinction-per-density.
+* :class:`ExtinctionState` -- the state sets the extinction of one species
+  (the same field in every solver, as for a gray medium);
+* :class:`DensityState` -- the state sets the condensate density; each
+  solver's extinction is density x the extinction per unit density that its
+  poly table gives for the fixed microphysics (reff, veff...), through
+  :func:`at3d_gb300.medium.table_to_grid`.  The gradient is the sum over
+  solvers of dCost/dExtinction x extinction-per-density.
+
+Prior terms (:mod:`at3d_gb300.regularization`) act on a generator's gridded
+field and are passed to :class:`Optimizer` as ``prior_fn``.
 
 Only extinction (or density) is retrieved: the Levis adjoint on the device
 gives dCost/dExtinction and dCost/dAlbedo, not the derivative through the
@@ -184,47 +189,88 @@ class Optimizer:
         return self._state
 
 
-class ExtinctionState:
-    """State = extinction of ``species`` at the points where ``mask`` is
-    true; the other points keep the solvers' current extinction."""
+class _GridState:
+    """A state vector mapped onto one field of the property grid: physical =
+    transform(state) placed on the grid by ``state_to_grid`` (default: one
+    element per point of ``mask``); the points the map does not set keep
+    their current values."""
 
-    def __init__(self, solvers, species: int, mask):
+    def __init__(self, solvers, species: int, mask=None, transform=None, state_to_grid=None, grid=None,
+                 grid_shape=None):
+        from .transforms import CoordinateTransform, StateToGridMask
         self.solvers = solvers
         self.species = species
-        self.mask = np.asarray(mask, bool)
+        if state_to_grid is None:
+            if mask is None and grid_shape is None:
+                raise ValueError("give a mask, a grid shape or a state_to_grid map")
+            state_to_grid = StateToGridMask(grid_shape=grid_shape, mask=mask)
+        self.state_to_grid = state_to_grid
+        self.transform = transform if transform is not None else CoordinateTransform()
+        self.mask = np.asarray(state_to_grid.mask, bool)
+        self._grid = grid
+
+    @property
+    def grid_shape(self):
+        return self.mask.shape
+
+    @property
+    def grid(self):
+        """The property grid (x, y, z) of the first solver, for smoothing priors."""
+        if self._grid is None:
+            from .grid import make_grid
+            pb = next(iter(self.solvers.values())).problem
+            npx, npy, _ = self.grid_shape
+            self._grid = make_grid(pb.delx, npx, pb.dely, npy, pb.zlevels)
+        return self._grid
+
+    def gridded(self, state):
+        """The physical field the state sets (NaN or 0 where it sets nothing)."""
+        return self.state_to_grid(self.transform(np.asarray(state, np.float64)))
+
+    def project_gridded_gradient(self, state, gridded_gradient):
+        """d/d(state) from d/d(gridded field), through the map and the transform."""
+        return self.transform.gradient_transform(np.asarray(state, np.float64),
+                                                 self.state_to_grid.gradient_transform(gridded_gradient))
+
+    def _state_of(self, field):
+        return self.transform.inverse_transform(self.state_to_grid.inverse_transform(field))
+
+    def _place(self, current, state):
+        out = np.array(current, np.float64, copy=True)
+        out[self.mask] = self.gridded(state)[self.mask]
+        return out
+
+
+class ExtinctionState(_GridState):
+    """State = the extinction of ``species`` where the map sets it (by default
+    one element per point of ``mask``), the same in every solver."""
 
     def initial_state(self, key=None):
         s = self.solvers[key if key is not None else next(iter(self.solvers))]
         ext, _ = s.species_properties(self.species)
-        return np.asarray(ext, np.float64)[self.mask]
+        return self._state_of(np.asarray(ext, np.float64))
 
     def set_state(self, state):
         for solver in self.solvers.values():
             ext, _ = solver.species_properties(self.species)
-            ext = np.array(ext, np.float32, copy=True)
-            ext[self.mask] = np.asarray(state, np.float32)
-            solver.update_species(self.species, extinction=ext)
+            solver.update_species(self.species, extinction=self._place(ext, state).astype(np.float32))
 
     def project_gradient_to_state(self, state, gradients):
-        g = np.zeros(int(self.mask.sum()))
-        for grad in gradients.values():
-            g += grad[..., 0][self.mask]
-        return g
+        total = sum(np.asarray(g[..., 0], np.float64) for g in gradients.values())
+        return self.project_gridded_gradient(state, total)
 
 
-class DensityState:
-    """State = condensate density at the masked points.  ``microphysics``:
+class DensityState(_GridState):
+    """State = the condensate density where the map sets it.  ``microphysics``:
     the fixed parameters of the table (e.g. {'reff': [...], 'veff': [...]},
     arrays on the property grid); ``poly_tables``: {solver key: PolyTable}.
     The phase functions stay as the solvers hold them (density does not
     change them); the albedo is set from the table."""
 
-    def __init__(self, solvers, species: int, mask, microphysics: dict, poly_tables: dict, density=None):
+    def __init__(self, solvers, species: int, mask, microphysics: dict, poly_tables: dict, density=None,
+                 transform=None, state_to_grid=None, grid=None):
         from .medium import table_to_grid
-
-        self.solvers = solvers
-        self.species = species
-        self.mask = np.asarray(mask, bool)
+        super().__init__(solvers, species, mask, transform, state_to_grid, grid)
         shape = self.mask.shape
         self.density = np.zeros(shape) if density is None else np.array(density, np.float64, copy=True)
         self.per_density = {}
@@ -235,16 +281,14 @@ class DensityState:
             self.ssalb[key] = np.asarray(sp.ssalb, np.float32)
 
     def initial_state(self):
-        return self.density[self.mask].copy()
+        return self._state_of(self.density)
 
     def set_state(self, state):
-        self.density[self.mask] = np.asarray(state, np.float64)
+        self.density = self._place(self.density, state)
         for key, solver in self.solvers.items():
             ext = (self.density * self.per_density[key]).astype(np.float32)
             solver.update_species(self.species, extinction=ext, ssalb=self.ssalb[key])
 
     def project_gradient_to_state(self, state, gradients):
-        g = np.zeros(int(self.mask.sum()))
-        for key, grad in gradients.items():
-            g += (grad[..., 0] * self.per_density[key])[self.mask]
-        return g
+        total = sum(np.asarray(g[..., 0], np.float64) * self.per_density[k] for k, g in gradients.items())
+        return self.project_gridded_gradient(state, total)
