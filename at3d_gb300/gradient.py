@@ -218,3 +218,93 @@ def render_differentiable(rte: RTE, extinction, ssalb, rays, species: int = 0, m
     When the tensors differ from the medium `rte` holds, `rte` is updated to
     them and re-solved (up to `maxiter` iterations) first."""
     return _LevisRenderFn.get().apply(extinction, ssalb, rte, tuple(rays), species, maxiter)
+
+
+class LevisApproxGradientUncorrelated:
+    """Cost and Levis gradient of every sensor of a SensorsDict, wavelengths
+    uncorrelated (LevisApproxGradient / LevisApproxGradientUncorrelated,
+    at3d/gradient.py:21-449).
+
+    On construction every instrument gets its uncertainty model (the
+    ``NullUncertainty`` of ``gradient_kwargs['cost_function']`` when it has
+    none, with a warning; a model assuming another cost function is an
+    error), its uncertainties are evaluated, and with
+    ``uncertainty_kwargs['add_noise']`` its measurements are perturbed by the
+    model.  A call solves the solvers (``parallel_solve_kwargs``), runs
+    ``levis_approximation_grad`` for every sensor with its solver (the key
+    is the sensor's 'wavelength'), stores the forward pixel values in the
+    matching sensor of ``forward_sensors`` (when given) and returns (loss,
+    {solver key: gradient [npx, npy, npz, 2]}, Jacobian rows or None), the
+    loss and gradients divided by the number of measurements.
+    ``unknown_scatterers``: the species index whose extinction and albedo
+    are differentiated."""
+
+    def __init__(self, measurements, solvers, forward_sensors, unknown_scatterers, parallel_solve_kwargs=None,
+                 gradient_kwargs=None, uncertainty_kwargs=None):
+        import warnings
+
+        from .containers import SensorsDict, SolversDict
+        from .uncertainties import NullUncertainty
+        if not isinstance(measurements, SensorsDict):
+            raise TypeError(f"`measurements` should be of type '{SensorsDict}' not '{type(measurements)}'")
+        if not isinstance(solvers, SolversDict):
+            raise TypeError(f"`solvers` should be of type '{SolversDict}' not '{type(solvers)}'")
+        if forward_sensors is not None and not isinstance(forward_sensors, SensorsDict):
+            raise TypeError(f"`forward_sensors` should be of type '{SensorsDict}' not '{type(forward_sensors)}'")
+        uncertainty_kwargs = dict(uncertainty_kwargs or {})
+        if "add_noise" not in uncertainty_kwargs:
+            uncertainty_kwargs["add_noise"] = False
+        elif not isinstance(uncertainty_kwargs["add_noise"], bool):
+            raise TypeError("uncertainty_kwargs['add_noise'] should be of boolean type.")
+        gradient_kwargs = dict(gradient_kwargs if gradient_kwargs is not None else {"cost_function": "L2"})
+        if "cost_function" not in gradient_kwargs:
+            raise ValueError("'cost_function' must be specified in `gradient_kwargs`. Supported values are 'L2' "
+                             "or 'LL'.")
+        if not isinstance(gradient_kwargs["cost_function"], str):
+            raise TypeError("gradient_kwargs['cost_function'] should be of string type.")
+        self.measurements = measurements
+        self.solvers = solvers
+        self.forward_sensors = forward_sensors
+        self.unknown_scatterers = unknown_scatterers
+        self.parallel_solve_kwargs = dict({"maxiter": 100, "verbose": False, "init_solution": True},
+                                          **(parallel_solve_kwargs or {}))
+        self.gradient_kwargs = gradient_kwargs
+        self.uncertainty_kwargs = uncertainty_kwargs
+        cost = gradient_kwargs["cost_function"]
+        for name, instrument in measurements.items():
+            if instrument.get("uncertainty_model") is None:
+                warnings.warn(f"No uncertainty model supplied for instrument '{name}'. Using "
+                              "at3d_gb300.uncertainties.NullUncertainty, which is unweighted least squares.")
+                measurements.add_uncertainty_model(name, NullUncertainty(cost))
+            if measurements[name]["uncertainty_model"].cost_function != cost:
+                raise ValueError(f"Uncertainty model's assumed cost_function "
+                                 f"'{measurements[name]['uncertainty_model'].cost_function}' is inconsistent with "
+                                 f"the one being used '{cost}'")
+            measurements.calculate_uncertainties(name)
+            if uncertainty_kwargs["add_noise"]:
+                measurements.add_noise(name)
+
+    def __call__(self):
+        kw = dict(self.parallel_solve_kwargs)
+        kw.setdefault("overwrite_solver", True)
+        self.solvers.solve(**kw)
+        idx = self.gradient_kwargs.get("indices_for_jacobian")
+        loss, grads, jac = 0.0, {}, []
+        for name, instrument in self.measurements.items():
+            for i, sensor in enumerate(instrument["sensor_list"]):
+                key = sensor["wavelength"]
+                if key not in self.solvers:
+                    raise KeyError(f"no solver for the sensor's wavelength {key}")
+                g, l, pixels, j = levis_approximation_grad(
+                    self.solvers[key], sensor, species=self.unknown_scatterers,
+                    cost_function=self.gradient_kwargs["cost_function"],
+                    uncertainties=np.asarray(sensor["uncertainties"]).transpose(2, 0, 1),
+                    indices_for_jacobian=idx)
+                loss += l
+                grads[key] = grads[key] + g if key in grads else g
+                if j is not None:
+                    jac.append(j)
+                if self.forward_sensors is not None:
+                    self.forward_sensors[name]["sensor_list"][i]["I"] = pixels
+        n = max(1, self.measurements.nmeasurements)
+        return loss / n, {k: v / n for k, v in grads.items()}, (jac if jac else None)

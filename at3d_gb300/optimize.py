@@ -33,15 +33,6 @@ import time
 
 import numpy as np
 
-from .gradient import levis_approximation_grad
-
-
-def _sensor_list(measurements):
-    """(sensor, uncertainty model) pairs of a SensorsDict or a list of sensors."""
-    from .containers import SensorsDict
-    if isinstance(measurements, SensorsDict):
-        return [(s, inst.get("uncertainty_model")) for inst in measurements.values() for s in inst["sensor_list"]]
-    return [(s, None) for s in measurements]
 
 
 class ObjectiveFunction:
@@ -65,44 +56,39 @@ class ObjectiveFunction:
         return loss, gradient
 
     @classmethod
-    def LevisApproxUncorrelatedL2(cls, measurements, solvers, unknown_species, set_state_fn,
-                                  project_gradient_to_state, solve_kwargs=None, gradient_kwargs=None,
-                                  min_bounds=None, max_bounds=None):
-        """The weighted least-squares misfit of every sensor in
-        ``measurements`` (a SensorsDict, or a list of sensor dicts, each with
-        its 'wavelength' -- the key of its solver in ``solvers`` -- and
-        measured 'I'; a sensor's 'uncertainties' and its instrument's
-        uncertainty model set the weights and the cost function), and its
-        Levis-approximate gradient (at3d/optimize.py:67-145).  Each call sets
-        the state (``set_state_fn(state)``), solves every solver
-        (``solvers.solve(**solve_kwargs)``), sums the cost and the gridded
-        gradients of the sensors of each solver, and maps the gradients onto
-        the state with ``project_gradient_to_state(state, {key: gradient
-        [npx, npy, npz, 2]})``.  ``unknown_species``: the species whose
-        extinction and albedo are differentiated.  ``gradient_kwargs`` are
-        passed to ``levis_approximation_grad`` (cost_function,
-        uncertainties...)."""
-        solve_kwargs = dict({"maxiter": 100, "verbose": False, "init_solution": True}, **(solve_kwargs or {}))
-        gradient_kwargs = dict(gradient_kwargs or {})
+    def LevisApproxUncorrelatedL2(cls, measurements, solvers, forward_sensors, unknown_scatterers, set_state_fn,
+                                  project_gradient_to_state, parallel_solve_kwargs=None, gradient_kwargs=None,
+                                  uncertainty_kwargs=None, min_bounds=None, max_bounds=None):
+        """The uncertainty-weighted misfit of the measurements and its
+        Levis-approximate gradient (at3d/optimize.py:67-145), through
+        :class:`at3d_gb300.gradient.LevisApproxGradientUncorrelated`: each
+        call sets the state (``set_state_fn(state)``), solves, and maps the
+        gridded gradients onto the state with
+        ``project_gradient_to_state(state, {solver key: gradient [npx, npy,
+        npz, 2]})``; cost and gradient are divided by the number of
+        measurements.  ``measurements``: a SensorsDict (or a list of sensor
+        dicts, taken as one instrument with unit uncertainties), each sensor
+        with its 'wavelength' (the key of its solver) and measured 'I';
+        ``forward_sensors`` (or None) receives the forward model's pixel
+        values; ``unknown_scatterers``: the species index whose extinction
+        and albedo are differentiated."""
+        from .containers import SensorsDict
+        from .gradient import LevisApproxGradientUncorrelated
+        if not isinstance(measurements, SensorsDict):
+            from .uncertainties import NullUncertainty
+            sd = SensorsDict()
+            cost = (gradient_kwargs or {}).get("cost_function", "L2")
+            sd.add_uncertainty_model("sensors", NullUncertainty(cost))
+            for sensor in measurements:
+                sd.add_sensor("sensors", sensor)
+            measurements = sd
+        gradient_fn = LevisApproxGradientUncorrelated(measurements, solvers, forward_sensors, unknown_scatterers,
+                                                      parallel_solve_kwargs, gradient_kwargs, uncertainty_kwargs)
 
         def loss_function(state, measurements):
             set_state_fn(state)
-            solvers.solve(overwrite_solver=True, **solve_kwargs)
-            loss = 0.0
-            grads = {}
-            for sensor, model in _sensor_list(measurements):
-                key = sensor["wavelength"]
-                if key not in solvers:
-                    raise KeyError(f"no solver for the sensor's wavelength {key}")
-                kw = dict(gradient_kwargs)
-                if "uncertainties" in sensor and "uncertainties" not in kw:
-                    kw["uncertainties"] = np.asarray(sensor["uncertainties"]).transpose(2, 0, 1)
-                if model is not None and "cost_function" not in kw:
-                    kw["cost_function"] = model.cost_function
-                g, l, _, _ = levis_approximation_grad(solvers[key], sensor, species=unknown_species, **kw)
-                loss += l
-                grads[key] = grads[key] + g if key in grads else g
-            return loss, project_gradient_to_state(state, grads)
+            loss, gradient, _ = gradient_fn()
+            return loss, project_gradient_to_state(state, gradient)
 
         return cls(measurements, loss_function, min_bounds=min_bounds, max_bounds=max_bounds)
 

@@ -123,9 +123,10 @@ def test_density_retrieval(rte_cls, poly):
     mask = truth > 0.005
     state = DensityState(solvers, 0, mask, {"reff": micro["reff"], "veff": micro["veff"]}, {0.672: poly},
                          density=np.where(mask, 0.6 * truth, truth))
-    obj = ObjectiveFunction.LevisApproxUncorrelatedL2(sensors, solvers, 0, state.set_state,
+    forward = sensors.make_forward_sensors()
+    obj = ObjectiveFunction.LevisApproxUncorrelatedL2(sensors, solvers, forward, 0, state.set_state,
                                                       state.project_gradient_to_state,
-                                                      solve_kwargs={"maxiter": 100}, min_bounds=0.0,
+                                                      parallel_solve_kwargs={"maxiter": 100}, min_bounds=0.0,
                                                       max_bounds=2.0)
     x0 = state.initial_state()
     loss0, _ = obj(x0)
@@ -134,3 +135,6 @@ def test_density_retrieval(rte_cls, poly):
     err = np.linalg.norm(res.x - truth[mask]) / np.linalg.norm(truth[mask])
     assert res.fun < 1e-2 * loss0, (res.fun, loss0)
     assert err < 0.4 * err0, (err, err0)
+    # the forward model's last pixel values are close to the measurements
+    f, m = forward["camera"]["sensor_list"][0]["I"], sensors["camera"]["sensor_list"][0]["I"]
+    assert np.sqrt(np.mean((f - m) ** 2)) < 0.2 * np.sqrt(np.mean(m ** 2))

@@ -43,16 +43,13 @@ class LinearSolver:
         return g
 
 
-class Solvers(dict):
-    def solve(self, overwrite_solver=True, **kw):
-        for s in self.values():
-            s.solve(**kw)
+from at3d_gb300.containers import SolversDict as Solvers   # filled by item assignment (no RTE type check)
 
 
 def sensor(nrays, wavelength, meas):
     z = np.zeros(nrays)
     return {"wavelength": wavelength, "ray_x": z, "ray_y": z, "ray_z": z, "ray_mu": np.ones(nrays),
-            "ray_phi": z, "I": meas}
+            "ray_phi": z, "cam_mu": np.ones(nrays), "stokes": [True, False, False, False], "I": meas}
 
 
 def setup(seed=0, shape=(3, 3, 2), nrays=40):
@@ -72,7 +69,7 @@ def test_extinction_retrieval_recovers_truth():
     truth, solvers, sensors = setup()
     mask = np.ones(truth.shape, bool)
     state = ExtinctionState(solvers, 0, mask)
-    obj = ObjectiveFunction.LevisApproxUncorrelatedL2(sensors, solvers, 0, state.set_state,
+    obj = ObjectiveFunction.LevisApproxUncorrelatedL2(sensors, solvers, None, 0, state.set_state,
                                                       state.project_gradient_to_state, min_bounds=0.0,
                                                       max_bounds=10.0)
     seen = []
@@ -148,7 +145,7 @@ def test_density_retrieval_recovers_truth():
         sensors.append(sensor(s.A.shape[0], wl, (s.A @ ext.reshape(-1)).astype(np.float32)))
     mask = np.ones(shape, bool)
     st = DensityState(solvers, 0, mask, {"reff": reff}, polys, density=np.full(shape, 0.5))
-    obj = ObjectiveFunction.LevisApproxUncorrelatedL2(sensors, solvers, 0, st.set_state,
+    obj = ObjectiveFunction.LevisApproxUncorrelatedL2(sensors, solvers, None, 0, st.set_state,
                                                       st.project_gradient_to_state, min_bounds=0.0,
                                                       max_bounds=5.0)
     res = Optimizer(obj, options={"maxiter": 300, "ftol": 1e-15, "gtol": 1e-12}).minimize(st.initial_state())
@@ -170,7 +167,7 @@ def test_unknown_wavelength_is_an_error():
     truth, solvers, sensors = setup(5)
     state = ExtinctionState(solvers, 0, np.ones(truth.shape, bool))
     bad = dict(sensors[0], wavelength=1.6)
-    obj = ObjectiveFunction.LevisApproxUncorrelatedL2([bad], solvers, 0, state.set_state,
+    obj = ObjectiveFunction.LevisApproxUncorrelatedL2([bad], solvers, None, 0, state.set_state,
                                                       state.project_gradient_to_state)
     with pytest.raises(KeyError, match="1.6"):
         obj(state.initial_state())

@@ -143,26 +143,35 @@ def test_radiometric_uncertainty():
 
 def test_objective_reads_sensors_dict():
     """The retrieval objective takes a SensorsDict: uncertainties per pixel
-    and the instrument's cost function reach the gradient call."""
-    from at3d_gb300 import optimize
+    and the cost function reach the gradient call, instruments without a
+    model get the null model of that cost function, the forward pixel values
+    land in forward_sensors, and cost and gradient are per measurement."""
+    from at3d_gb300 import gradient, optimize
     seen = []
 
     def fake_grad(solver, sensor, species=0, **kw):
         seen.append(kw)
-        return np.zeros((2, 2, 2, 2)), 1.0, None, None
+        return np.ones((2, 2, 2, 2)), 1.0, np.full(len(sensor["cam_mu"]), 7.0), None
 
     solvers, sd = make()
     sd.get_measurements(solvers)
     sd.add_uncertainty_model("cam", NullUncertainty("LL", 3.0))
-    sd.calculate_uncertainties("cam")
-    orig = optimize.levis_approximation_grad
-    optimize.levis_approximation_grad = fake_grad
+    fwd = sd.make_forward_sensors()
+    orig = gradient.levis_approximation_grad
+    gradient.levis_approximation_grad = fake_grad
     try:
-        obj = optimize.ObjectiveFunction.LevisApproxUncorrelatedL2(sd, solvers, 0, lambda s: None,
-                                                                   lambda s, g: np.zeros(1))
-        loss, _ = obj(np.zeros(1))
+        with pytest.warns(UserWarning, match="No uncertainty model"):
+            obj = optimize.ObjectiveFunction.LevisApproxUncorrelatedL2(
+                sd, solvers, fwd, 0, lambda s: None, lambda s, g: sum(v.sum() for v in g.values()) * np.ones(1),
+                gradient_kwargs={"cost_function": "LL"})
+        loss, grad = obj(np.zeros(1))
     finally:
-        optimize.levis_approximation_grad = orig
-    assert loss == 3.0 and len(seen) == 3
-    assert seen[0]["cost_function"] == "LL" and seen[0]["uncertainties"].shape[1:] == (2, 2)
-    assert "uncertainties" not in seen[2] and "cost_function" not in seen[2]
+        gradient.levis_approximation_grad = orig
+    n = sd.nmeasurements
+    assert loss == pytest.approx(3.0 / n) and grad[0] == pytest.approx(3 * 16.0 / n)
+    assert len(seen) == 3 and all(k["cost_function"] == "LL" for k in seen)
+    assert seen[0]["uncertainties"].shape[1:] == (2, 2) and np.all(seen[0]["uncertainties"] == 3.0)
+    assert np.all(fwd["cam"]["sensor_list"][1]["I"] == 7.0)
+    with pytest.raises(ValueError, match="inconsistent"):
+        optimize.ObjectiveFunction.LevisApproxUncorrelatedL2(sd, solvers, None, 0, lambda s: None, lambda s, g: 0,
+                                                             gradient_kwargs={"cost_function": "L2"})

@@ -82,7 +82,7 @@ def test_log_state_retrieval_with_priors():
     truth, solvers, sensors = setup(7)
     state = ExtinctionState(solvers, 0, np.ones(truth.shape, bool), transform=T.CoordinateTransformLog(),
                             grid=make_grid(0.1, 3, 0.1, 3, [0.0, 0.1]))
-    obj = ObjectiveFunction.LevisApproxUncorrelatedL2(sensors, solvers, 0, state.set_state,
+    obj = ObjectiveFunction.LevisApproxUncorrelatedL2(sensors, solvers, None, 0, state.set_state,
                                                       state.project_gradient_to_state)
     smooth = R.SpatialSmoothing(state, 1e-6, mode="l2")
     tik = R.Tikhonov(state, 1e-7)
