@@ -278,3 +278,24 @@ class DensityState(_GridState):
     def project_gradient_to_state(self, state, gradients):
         total = sum(np.asarray(g[..., 0], np.float64) * self.per_density[k] for k, g in gradients.items())
         return self.project_gridded_gradient(state, total)
+
+
+class CallbackFn:
+    """An Optimizer callback that records what ``callback_fn(optimizer=...)``
+    returns (a dict of values) at most once every ``ckpt_period`` seconds
+    (every iteration with the default of -1) into ``self.output`` {name:
+    [value per recorded iteration]} (at3d/callback.py:32-49).  The
+    reference's tensorboard writer is not included."""
+
+    def __init__(self, callback_fn, ckpt_period=-1):
+        self._ckpt_period = ckpt_period
+        self._ckpt_time = time.time()
+        self._callback_fn = callback_fn
+        self.output = {}
+
+    def __call__(self, optimizer=None):
+        if time.time() - self._ckpt_time > self._ckpt_period:
+            self._ckpt_time = time.time()
+            out = self._callback_fn(optimizer=optimizer)
+            for name, value in out.items():
+                self.output.setdefault(name, []).append(value)

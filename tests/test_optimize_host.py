@@ -171,3 +171,15 @@ def test_unknown_wavelength_is_an_error():
                                                       state.project_gradient_to_state)
     with pytest.raises(KeyError, match="1.6"):
         obj(state.initial_state())
+
+
+def test_callback_records_iterations():
+    from at3d_gb300.optimize import CallbackFn
+    obj = ObjectiveFunction(None, lambda s, m: (float(np.sum((s - 1.0) ** 2)), 2 * (s - 1.0)))
+    cb = CallbackFn(lambda optimizer: {"iteration": optimizer.iteration, "loss": obj.loss})
+    slow = CallbackFn(lambda optimizer: {"iteration": optimizer.iteration}, ckpt_period=3600.0)
+    res = Optimizer(obj, callback_fn=[cb, slow], options={"maxiter": 50}).minimize(np.zeros(3))
+    assert np.allclose(res.x, 1.0, atol=1e-6)
+    assert cb.output["iteration"] == list(range(1, len(cb.output["iteration"]) + 1))
+    assert cb.output["loss"][-1] <= cb.output["loss"][0]
+    assert slow.output == {}
