@@ -50,6 +50,37 @@ def _deferred_creator():
         return _CREATOR
 
 
+def compute_sh(radiance, dirflux, solarmu: float, solaraz: float, srctype: str = "S", mm: int = 1) -> np.ndarray:
+    """COMPUTE_SH (src/polarized/shdomsub2.f:1770-1836) for its four outputs:
+    per grid point the mean intensity C0 R_00, the net flux vector
+    Fx = -A (R_11 + R_1-1), Fy = -A (R_1-1 - R_11), Fz = C R_10 (A = sqrt(2 pi/3),
+    C = sqrt(4 pi/3), C0 = 1/sqrt(4 pi), terms j = 0..3 of the radiance
+    series; Fx = Fy = 0 when MM = 0), plus the direct beam for solar sources
+    (mean intensity + F sec(mu0)/4pi, horizontal flux + F tan(theta0) (cos,
+    sin of the solar azimuth), Fz - F).  ``radiance``: [npts, nlm] or
+    [npts, nstokes, nlm] (the I row is used).  Returns [4, npts]."""
+    r = np.asarray(radiance, np.float64)
+    if r.ndim == 3:
+        r = r[:, 0, :]
+    f = np.asarray(dirflux, np.float64)
+    pi = np.pi
+    a, c, c0 = np.sqrt(2 * pi / 3), np.sqrt(4 * pi / 3), 1 / np.sqrt(4 * pi)
+    out = np.zeros((4, r.shape[0]))
+    out[0] = c0 * r[:, 0]
+    out[3] = c * r[:, 2]
+    if mm > 0:
+        out[1] = -a * (r[:, 3] + r[:, 1])
+        out[2] = -a * (r[:, 1] - r[:, 3])
+    if srctype in ("S", "B"):
+        sec = 1.0 / abs(solarmu)
+        sin0 = np.sqrt(1.0 - solarmu ** 2)
+        out[0] += f * sec / (4 * pi)
+        out[1] += f * sin0 * np.cos(solaraz) * sec
+        out[2] += f * sin0 * np.sin(solaraz) * sec
+        out[3] -= f
+    return out.astype(np.float32)
+
+
 class SHDOMError(RuntimeError):
     """Raised for a non-zero SHDOM error code (at3d/checks.py:300-311)."""
 
@@ -312,6 +343,29 @@ class RTE:
         shp = (s["nx1"], s["ny1"], s["nz"])
         return {"flux_down": st["fluxes"][:, 0].reshape(shp), "flux_up": st["fluxes"][:, 1].reshape(shp),
                 "flux_direct": st["dirflux"].reshape(shp)}
+
+    @property
+    def spherical_harmonics(self) -> dict:
+        """Mean intensity and net flux vector (Fx, Fy, Fz) on the base grid,
+        [nx1, ny1, nz] each (RTE.spherical_harmonics, at3d/solver.py:1039-1129,
+        through COMPUTE_SH; the extra root-mean-square term of HIGHORDERRAD
+        solves is not included)."""
+        s = self.sizes
+        st = self.export_state()
+        p = self.problem
+        sh = compute_sh(st["radiance"], st["dirflux"], p.solarmu, p.solaraz, p.srctype, s["mm"])
+        shp = (s["nx1"], s["ny1"], s["nz"])
+        return {"mean_intensity": sh[0].reshape(shp), "Fx": sh[1].reshape(shp), "Fy": sh[2].reshape(shp),
+                "Fz": sh[3].reshape(shp)}
+
+    @property
+    def solution_accuracy(self) -> float:
+        return float(self.problem.params.solution_accuracy)
+
+    @property
+    def num_iterations(self) -> int:
+        """Iterations of the current solution (RTE.num_iterations)."""
+        return int(self.sizes["iters"])
 
     def _property_shape(self):
         sp = self.problem.species[0]
