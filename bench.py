@@ -552,6 +552,39 @@ def config1_block(args, dev):
     return out
 
 
+def producers_block(args):
+    """Host cost of the optical-property producers that feed a solve: a full
+    water Mie table at 0.672 um (radii 0.08-65 um), the poly table of 25 x 2
+    gamma distributions over it, and table_to_grid of a microphysics field
+    on the benchmark grid (density from the benchmark cloud field, effective
+    radius rising with height).  Wall clock, host threads."""
+    from at3d_gb300 import medium, mie
+    from at3d_gb300 import size_distribution as sd
+    from at3d_gb300.scenes import cloud_field
+    out = {"workload": "water Mie table 0.672 um (4-65 um), 25x2 gamma poly table, table_to_grid on "
+                       f"{args.nx}x{args.nx}x{args.nz}", "host_threads": os.cpu_count()}
+    t0 = time.perf_counter()
+    mono = mie.get_mono_table("Water", (0.672, 0.672), refractive_index=1.331 - 1.6e-8j, verbose=False)
+    out["mono_s"] = time.perf_counter() - t0
+    out["mono_radii"], out["mono_legendre"] = int(mono.radius.size), int(mono.legendre.shape[1] - 1)
+    t0 = time.perf_counter()
+    grid = sd.get_size_distribution_grid(mono.radius, sd.gamma, reff={"coord_min": 4.0, "coord_max": 25.0,
+                                                                       "npoints": 25, "spacing": "logarithmic"},
+                                         veff=np.array([0.09, 0.11]))
+    poly = mie.get_poly_table(grid, mono)
+    out["poly_s"] = time.perf_counter() - t0
+    pb = cloud_field(seed=2, wavelength_index=0, nx=args.nx, ny=args.nx, nz=args.nz)
+    ext = np.asarray(pb.species[0].extinction, np.float64)
+    z = np.linspace(0.0, 1.0, args.nz)[None, None, :]
+    micro = {"density": ext / 150.0, "reff": np.broadcast_to(6.0 + 10.0 * z, ext.shape),
+             "veff": np.full(ext.shape, 0.1)}
+    t0 = time.perf_counter()
+    sp = medium.table_to_grid(micro, poly)
+    out["table_to_grid_s"] = time.perf_counter() - t0
+    out["phase_functions"] = int(sp.legcoef.shape[0])
+    return out
+
+
 def serving_block(args, dev):
     """A Poisson stream of mixed requests through the continuous-admission
     loop (at3d_gb300.serving): grids 32x32x24 to 128x128x64, NMU/NPHI 8/16
@@ -823,6 +856,7 @@ def main():
         extras["config1"] = config1_block(args, dev)
         extras["render"] = render_block(args, dev)
         extras["serving"] = serving_block(args, dev)
+        extras["producers"] = producers_block(args)
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
         pbs, _ = scenes(args)
