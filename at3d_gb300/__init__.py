@@ -5,11 +5,11 @@ The numerical work runs in the CUDA library built from at3d_gb300/csrc
 mirror of the reference's Python interface.
 """
 from . import (configuration, grid, medium, mie, regularization, scenes, sensor,  # noqa: F401
-               size_distribution, source, surface, transforms, uncertainties)
+               size_distribution, source, surface, transforms, uncertainties, util)
 from ._abi import NumericalParams, Problem, Species  # noqa: F401
 
 __all__ = ["RTE", "NumericalParams", "Problem", "Species", "configuration", "grid", "medium", "mie", "scenes",
-           "regularization", "sensor", "size_distribution", "source", "surface", "transforms", "uncertainties",
+           "regularization", "sensor", "size_distribution", "source", "surface", "transforms", "uncertainties", "util",
            "optimize", "containers"]
 
 
