@@ -164,6 +164,8 @@ def mie_cloud(seed: int = 1, nx: int = 24, ny: int = 24, nz: int = 16, dx: float
     from .medium import table_to_grid
     poly = mie_poly_table() if poly_table is None else poly_table
     micro = mie_microphysics(seed, nx, ny, nz, dx, dz) if microphysics is None else microphysics
+    if np.shape(micro["density"]) != (nx, ny, nz):
+        raise ValueError(f"microphysics of shape {np.shape(micro['density'])} for a {nx}x{ny}x{nz} grid")
     cloud = table_to_grid(micro, poly, num_stokes=num_stokes)
     ray_ext = np.full((nx, ny, nz), 0.01, np.float32)
     ray_leg = rayleigh_legcoef6(0.03) if num_stokes == 3 else rayleigh_legcoef(0.672)
