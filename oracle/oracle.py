@@ -34,7 +34,8 @@ def lib():
         L.oracle_error.argtypes = [C.c_void_p]
         for n in ("oracle_sizes", "oracle_solve", "oracle_init_solution", "oracle_export",
                   "oracle_render", "oracle_grid", "oracle_angles", "oracle_levis_gradient",
-                  "oracle_frozen_render", "oracle_set_render_options", "oracle_levis_adjoint"):
+                  "oracle_frozen_render", "oracle_set_render_options", "oracle_levis_adjoint",
+                  "oracle_levis_adjoint_phase", "oracle_frozen_render_phase"):
             getattr(L, n).restype = C.c_int
         L.oracle_destroy.argtypes = [C.c_void_p]
         _LIB = L
@@ -149,6 +150,40 @@ class Oracle:
         rc = self._lib.oracle_frozen_render(C.c_void_p(self._h), int(species), int(voxel), C.c_float(dext),
                                             C.c_float(dalb), len(x), _p(x), _p(y), _p(z), _p(mu, C.c_double),
                                             _p(phi, C.c_double), _p(out), int(nthreads))
+        if rc:
+            raise RuntimeError(self._lib.oracle_error(C.c_void_p(self._h)).decode())
+        return out
+
+    def levis_adjoint_phase(self, species: int, rays, weights, dleg, diph, nthreads: int = 1):
+        """The adjoint pass with a third unknown: the phase function moved
+        along derivative series ``dleg`` [ndphase, nleg+1] (with the 2l+1
+        factor), row ``diph`` [npx*npy*npz, maxnmicro] (1-based) at each
+        property point (DLEG and DIPHASEP of LEVISAPPROX_GRADIENT).  Returns
+        the gradient of sum_r w_r I_r, [npx*npy*npz, 3] (extinction,
+        albedo, phase)."""
+        x, y, z, mu, phi = self._rays(*rays)
+        w = np.ascontiguousarray(weights, np.float64)
+        dl = np.ascontiguousarray(np.atleast_2d(dleg), np.float32)
+        di = np.ascontiguousarray(diph, np.int32)
+        ng = self._problem.species[0].extinction.size
+        grad = np.zeros((ng, 3), np.float64)
+        rc = self._lib.oracle_levis_adjoint_phase(C.c_void_p(self._h), int(species), len(x), _p(x), _p(y), _p(z),
+                                                  _p(mu, C.c_double), _p(phi, C.c_double), _p(w, C.c_double),
+                                                  dl.shape[0], dl.shape[1] - 1, _p(dl), _p(di, C.c_int),
+                                                  _p(grad, C.c_double), int(nthreads))
+        if rc:
+            raise RuntimeError(self._lib.oracle_error(C.c_void_p(self._h)).decode())
+        return grad
+
+    def frozen_render_phase(self, species: int, voxel: int, eps: float, dleg_row, rays, nthreads: int = 1):
+        """frozen_render with one voxel's phase function (its current mixture)
+        plus eps x ``dleg_row`` (Legendre series with the 2l+1 factor)."""
+        x, y, z, mu, phi = self._rays(*rays)
+        row = np.ascontiguousarray(dleg_row, np.float32)
+        out = np.zeros(len(x), np.float32)
+        rc = self._lib.oracle_frozen_render_phase(C.c_void_p(self._h), int(species), int(voxel), C.c_float(eps),
+                                                  row.size - 1, _p(row), len(x), _p(x), _p(y), _p(z),
+                                                  _p(mu, C.c_double), _p(phi, C.c_double), _p(out), int(nthreads))
         if rc:
             raise RuntimeError(self._lib.oracle_error(C.c_void_p(self._h)).decode())
         return out

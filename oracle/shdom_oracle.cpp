@@ -2551,12 +2551,57 @@ struct Levis {
   std::vector<int> interpptr;     // [npts][8] property point per trilinear corner (0-based)
   std::vector<R> optinterpwt;     // [npts][8]
   std::vector<R> fp, dextm;       // [ng], [ng][2]
-  std::vector<R> dalbm, dfj;      // [npts][8][2]
-  static constexpr int NUMDER = 2;
+  std::vector<R> dalbm, dfj;      // [npts][8][3]
+  // Unknowns: 0 extinction, 1 albedo, 2 the phase function along a given
+  // derivative series (DLEG with DIPHASEP of the reference; zero when none
+  // is given): dleg [ndphase][nleg+1] in the LEGEN representation (divided
+  // by 2l+1), diph [ng][maxnmicro] its 1-based rows at each property point
+  // (weighted by the species' phase weights), dphasetab [nscatangle][ndphase]
+  // its phase function for the exact single scatter, dfp [ng] the
+  // derivative of the delta-M fraction f at each property point.
+  static constexpr int NUMDER = 3;
+  bool has_phase = false;
+  int ndphase = 0;
+  std::vector<R> dleg, dphasetab, dfp;
+  std::vector<int> diph;
   explicit Levis(const Solver<R> &s) : S(s) {}
 
   R dext(int, int idr) const { return idr == 0 ? (R)1 : (R)0; }
   R dalb(int, int idr) const { return idr == 1 ? (R)1 : (R)0; }
+  int diphp(int q, int ib) const { return diph[(size_t)ib * S.maxnmicro + q]; }
+
+  // The phase-derivative table (given with the 2l+1 factor, like the
+  // phase functions) and its phase function at the scattering angles of
+  // PRECOMPUTE_PHASE_CHECK, without the positivity check.
+  bool set_phase(int nd, int nlegd, const float *dleg_in, const int *diph_in, std::string &err) {
+    const int ngp = S.p.npx * S.p.npy * S.p.npz, nl1 = S.nleg + 1;
+    if (nd < 1 || nlegd < 0 || !dleg_in || !diph_in) { err = "phase derivative: bad table"; return false; }
+    for (size_t k = 0; k < (size_t)ngp * S.maxnmicro; ++k)
+      if (diph_in[k] < 1 || diph_in[k] > nd) { err = "phase derivative: index out of range"; return false; }
+    has_phase = true;
+    ndphase = nd;
+    diph.assign(diph_in, diph_in + (size_t)ngp * S.maxnmicro);
+    dleg.assign((size_t)nd * nl1, 0);
+    for (int k = 0; k < nd; ++k)
+      for (int l = 0; l <= std::min(nlegd, S.nleg); ++l)
+        dleg[(size_t)k * nl1 + l] = (R)(dleg_in[(size_t)k * (nlegd + 1) + l] / (float)(2 * l + 1));
+    const double pi = std::acos(-1.0), ofourpi = 1.0 / (4.0 * pi);
+    dphasetab.assign((size_t)S.nscatangle * nd, 0);
+    std::vector<double> d(nlegd + 1);
+    for (int j = 0; j < S.nscatangle; ++j) {
+      const double x = std::cos(pi * (double)j / (S.nscatangle - 1));
+      d[0] = 1.0;
+      if (nlegd >= 1) d[1] = x;
+      for (int n = 1; n < nlegd; ++n) d[n + 1] = ((2 * n + 1) * x * d[n] - n * d[n - 1]) / (n + 1);
+      for (int k = 0; k < nd; ++k) {
+        double a1 = 0.0;
+        for (int l = 0; l <= nlegd; ++l)
+          a1 += (2.0 * l + 1.0) * (double)(float)(dleg_in[(size_t)k * (nlegd + 1) + l] / (float)(2 * l + 1)) * d[l];
+        dphasetab[(size_t)j * nd + k] = (R)(a1 * ofourpi);
+      }
+    }
+    return true;
+  }
   R extp(int ib) const { return (R)S.extp[(size_t)ipa * ng + ib]; }
   R albp(int ib) const { return (R)S.albp[(size_t)ipa * ng + ib]; }
   int iphp(int q, int ib) const { return S.iphp[((size_t)ipa * ng + ib) * S.maxnmicro + q]; }
@@ -2598,14 +2643,19 @@ struct Levis {
       const int ii[8] = {i1, i2, i3, i4, i1 + 1, i2 + 1, i3 + 1, i4 + 1};
       for (int k = 0; k < 8; ++k) { interpptr[(size_t)ip * 8 + k] = ii[k]; optinterpwt[(size_t)ip * 8 + k] = (R)f[k]; }
     }
-    fp.assign(ng, 0); dextm.assign((size_t)ng * NUMDER, 0);
+    fp.assign(ng, 0); dfp.assign(ng, 0); dextm.assign((size_t)ng * NUMDER, 0);
     for (int ib = 0; ib < ng; ++ib) {
-      R fv = 0;
+      R fv = 0, dfv = 0;
       if (p.deltam)
-        for (int q = 0; q < S.maxnmicro; ++q) fv += phwtp(q, ib) * S.legen[(size_t)(iphp(q, ib) - 1) * nl1 + ml + 1];
+        for (int q = 0; q < S.maxnmicro; ++q) {
+          fv += phwtp(q, ib) * S.legen[(size_t)(iphp(q, ib) - 1) * nl1 + ml + 1];
+          if (has_phase) dfv += phwtp(q, ib) * dleg[(size_t)(diphp(q, ib) - 1) * nl1 + ml + 1];
+        }
       fp[ib] = fv;
+      dfp[ib] = dfv;
       for (int idr = 0; idr < NUMDER; ++idr)
-        dextm[(size_t)ib * NUMDER + idr] = dext(ib, idr) * ((R)1 - fv * albp(ib)) - dalb(ib, idr) * fv * extp(ib);
+        dextm[(size_t)ib * NUMDER + idr] = dext(ib, idr) * ((R)1 - fv * albp(ib)) - dalb(ib, idr) * fv * extp(ib) -
+                                           (idr == 2 ? extp(ib) * albp(ib) * dfv : (R)0);
     }
     dalbm.assign((size_t)npts * 8 * NUMDER, 0); dfj.assign((size_t)npts * 8 * NUMDER, 0);
     for (int ip = 0; ip < npts; ++ip) {
@@ -2628,11 +2678,13 @@ struct Levis {
       for (int nb = 0; nb < 8; ++nb) {
         const int ib = interpptr[(size_t)ip * 8 + nb];
         for (int idr = 0; idr < NUMDER; ++idr) {
-          const R DE = dext(ib, idr), DA = dalb(ib, idr), FP = fp[ib];
+          const R DE = dext(ib, idr), DA = dalb(ib, idr), FP = fp[ib], DFP = idr == 2 ? dfp[ib] : (R)0;
           dalbm[((size_t)ip * 8 + nb) * NUMDER + idr] =
               divide * (DE * (((R)1 - F) * (albp(ib) - albj) + (albj - 1) * albp(ib) * (FP - F)) +
-                        DA * (((R)1 - F) * extp(ib) + (albj - 1) * extp(ib) * (FP - F)));
-          dfj[((size_t)ip * 8 + nb) * NUMDER + idr] = (DE * (FP - F) * albp(ib) + DA * (FP - F) * extp(ib)) / ((R)1 - F);
+                        DA * (((R)1 - F) * extp(ib) + (albj - 1) * extp(ib) * (FP - F)) +
+                        DFP * (albj - 1) * extp(ib) * albp(ib));
+          dfj[((size_t)ip * 8 + nb) * NUMDER + idr] =
+              (DE * (FP - F) * albp(ib) + DA * (FP - F) * extp(ib) + DFP * extp(ib) * albp(ib)) / ((R)1 - F);
         }
       }
     }
@@ -2652,8 +2704,8 @@ struct Levis {
   // COMPUTE_SOURCE_GRAD_1CELL (src/polarized/shdomsub4.f:1546-2042) for one
   // new grid point: extinction, source x extinction, single scatter x
   // extinction and GRAD8(NB, IDR).
-  void point_grad(int ip, const std::vector<R> &ylmdir, const std::vector<R> &singscat, R &ext8, R &srcext8,
-                  R &singscat8, R grad8[8][NUMDER]) const {
+  void point_grad(int ip, const std::vector<R> &ylmdir, const std::vector<R> &singscat,
+                  const std::vector<R> &dsingscat, R &ext8, R &srcext8, R &singscat8, R grad8[8][NUMDER]) const {
     const auto &p = S.p;
     const int npts = S.npts, ml = S.ml, mm = S.mm, nl1 = S.nleg + 1;
     const R secmu0 = (R)1 / std::fabs((R)p.solarmu);
@@ -2758,11 +2810,21 @@ struct Levis {
       if (p.deltam)
         for (int q = 0; q < S.maxnmicro; ++q) singscatp += phwtp(q, ib) * singscat[iphp(q, ib) - 1];
       for (int idr = 0; idr < NUMDER; ++idr) {
+        if (idr == 2 && !has_phase) continue;
         const R DE = dext(ib, idr), DA = dalb(ib, idr);
         const R DFJ = dfj[((size_t)ip * 8 + nb) * NUMDER + idr];
         for (int l = 0; l < nl1; ++l) {
           const R diff = legenp[l] - legent[l];
           dlegt[l] = DE * diff * albp(ib) + DA * diff * extp(ib) + (legent[l] - 1) * DFJ;
+        }
+        R dsingscatp = 0;
+        if (idr == 2) {  // DLEGP (and DSINGSCATP): the derivative series at the property point
+          for (int q = 0; q < S.maxnmicro; ++q) {
+            const R w = phwtp(q, ib);
+            const R *D = &dleg[(size_t)(diphp(q, ib) - 1) * nl1];
+            for (int l = 0; l < nl1; ++l) dlegt[l] += w * D[l] * extp(ib) * albp(ib);
+            if (p.deltam) dsingscatp += w * dsingscat[diphp(q, ib) - 1];
+          }
         }
         const R dsource = source_direction(dlegt.data(), ip, ylmdir, secmu0);
         R g = xi * (sourcet * (albip * dextm[(size_t)ib * NUMDER + idr] + dalbm[((size_t)ip * 8 + nb) * NUMDER + idr]) + dsource);
@@ -2772,7 +2834,8 @@ struct Levis {
           g += xi * (bpl * ((R)1 - albip) * dextm[(size_t)ib * NUMDER + idr] - bpl * dalbm[((size_t)ip * 8 + nb) * NUMDER + idr]);
         if (p.deltam)
           g += S.dirflux[ip] * secmu0 * xi *
-               (singscatj * DFJ + DA * (singscatp - singscatj) * extp(ib) + DE * (singscatp - singscatj) * albp(ib));
+               (singscatj * DFJ + DA * (singscatp - singscatj) * extp(ib) + DE * (singscatp - singscatj) * albp(ib) +
+                dsingscatp * extp(ib) * albp(ib));
         grad8[nb][idr] += g;
       }
     }
@@ -2791,7 +2854,7 @@ struct Levis {
     const int nx = S.nx, ny = S.ny;
     const double eps = 1.0e-5 * (S.gridpos[3 * S.gridptr[7] + 2] - S.gridpos[3 * S.gridptr[0] + 2]);
     std::vector<R> ylmdir = S.ylmall((double)(float)mu2, (float)phi2);
-    std::vector<R> singscat(S.numphase, 0);
+    std::vector<R> singscat(S.numphase, 0), dsingscat(std::max(1, ndphase), 0);
     if (p.deltam) {
       double cosscat = (double)p.solarmu * mu2 +
                        std::sqrt((1.0 - (double)p.solarmu * p.solarmu) * (1.0 - mu2 * mu2)) * std::cos((double)p.solaraz - phi2);
@@ -2801,6 +2864,8 @@ struct Levis {
       F = F - J;
       for (int i = 0; i < S.numphase; ++i)
         singscat[i] = (R)((1 - F) * S.phasetab[(size_t)(J - 1) * S.numphase + i] + F * S.phasetab[(size_t)J * S.numphase + i]);
+      for (int i = 0; i < ndphase; ++i)
+        dsingscat[i] = (R)((1 - F) * dphasetab[(size_t)(J - 1) * ndphase + i] + F * dphasetab[(size_t)J * ndphase + i]);
     }
     double cx = std::sqrt(1.0 - mu2 * mu2) * std::cos(phi2 - pi), cy = std::sqrt(1.0 - mu2 * mu2) * std::sin(phi2 - pi);
     double cz = -mu2, cxinv, cyinv, czinv;
@@ -2845,7 +2910,7 @@ struct Levis {
           continue;
         }
         oldipts[n] = ip;
-        point_grad(ip, ylmdir, singscat, extinct8[n], srcext8[n], singscat8[n], grad8[n]);
+        point_grad(ip, ylmdir, singscat, dsingscat, extinct8[n], srcext8[n], singscat8[n], grad8[n]);
       }
       const int ipt1 = S.gridptr[8 * icell], ipt2 = S.gridptr[8 * icell + 7];
       const double delx = S.gridpos[3 * ipt2] - S.gridpos[3 * ipt1], dely = S.gridpos[3 * ipt2 + 1] - S.gridpos[3 * ipt1 + 1];
@@ -3144,18 +3209,58 @@ bool frozen_render(Solver<R> &S, int ipa, int voxel, float dext, float dalb, int
   return ok;
 }
 
+// A phase-derivative direction for the third unknown: a table of
+// derivative series and its rows at each property point.
+struct PhaseDeriv {
+  int ndphase = 0, nlegd = 0;
+  const float *dleg = nullptr;  // [ndphase][nlegd+1], with the 2l+1 factor
+  const int *diph = nullptr;    // [npx*npy*npz][maxnmicro], 1-based
+};
+
+// frozen_render with the phase function of one voxel of species ipa moved
+// along a derivative series: the voxel gets a phase-table row of its own,
+// its current mixture plus eps x dleg_row (nlegd+1 terms with the 2l+1
+// factor), with weight 1.
+template <typename R>
+bool frozen_render_phase(Solver<R> &S, int ipa, int voxel, float eps, int nlegd, const float *dleg_row, int n,
+                         const float *camx, const float *camy, const float *camz, const double *cammu,
+                         const double *camphi, float *out, int nthreads) {
+  const int ng = S.p.npx * S.p.npy * S.p.npz, nm = S.p.maxnmicro, nlp = S.p.nlegp;
+  if (ipa < 0 || ipa >= S.npart || voxel < 0 || voxel >= ng) { S.err = "frozen_render_phase: bad index"; return false; }
+  if (S.nst != 1) { S.err = "frozen_render_phase: scalar problems only"; return false; }
+  const auto legp = S.legp;
+  const auto iphp = S.iphp;
+  const auto phwtp = S.phwtp;
+  const shdom_problem p0 = S.p;
+  std::vector<float> row(nlp + 1, 0.f);
+  const size_t o = ((size_t)ipa * ng + voxel) * nm;
+  for (int q = 0; q < nm; ++q)
+    for (int l = 0; l <= nlp; ++l) row[l] += phwtp[o + q] * legp[(size_t)(iphp[o + q] - 1) * (nlp + 1) + l];
+  for (int l = 0; l <= std::min(nlp, nlegd); ++l) row[l] += eps * dleg_row[l];
+  S.legp.insert(S.legp.end(), row.begin(), row.end());
+  S.p.numphase += 1;
+  for (int q = 0; q < nm; ++q) { S.iphp[o + q] = S.p.numphase; S.phwtp[o + q] = q == 0 ? 1.f : 0.f; }
+  bool ok = frozen_render(S, ipa, voxel, 0.f, 0.f, n, camx, camy, camz, cammu, camphi, out, nthreads);
+  S.legp = legp; S.iphp = iphp; S.phwtp = phwtp; S.p = p0;
+  if (ok) ok = S.transfer_properties();   // back to the solver's own tables
+  return ok;
+}
+
 template <typename R>
 // With meas: the L2 cost of one-ray pixels and its adjoint weights; with
 // weights (meas null): those ray weights (the gradient of sum_r w_r I_r).
+// gradout [ng][nout]: extinction, albedo and (nout = 3, with pd) the phase.
 bool levis_gradient(Solver<R> &S, int ipa, int n, const float *camx, const float *camy, const float *camz,
                     const double *cammu, const double *camphi, const float *meas, const double *weights,
-                    double *gradout, double *cost, float *stokesout, int nthreads) {
+                    double *gradout, double *cost, float *stokesout, int nthreads, const PhaseDeriv *pd = nullptr,
+                    int nout = 2) {
   if (ipa < 0 || ipa >= S.npart) { S.err = "levis_gradient: bad species index"; return false; }
   if (S.nst != 1) { S.err = "levis_gradient: scalar problems only"; return false; }
   std::vector<float> own;
   if (!stokesout) { own.resize(n); stokesout = own.data(); }
   if (!S.render(n, camx, camy, camz, cammu, camphi, stokesout, nthreads)) return false;  // phase 1 (with phasetab, bcrad)
   Levis<R> L(S);
+  if (pd && !L.set_phase(pd->ndphase, pd->nlegd, pd->dleg, pd->diph, S.err)) return false;
   if (!L.prepare(ipa, S.err)) return false;
   // phase 2: L2 adjoint weights and cost
   std::vector<double> adj(n);
@@ -3172,7 +3277,8 @@ bool levis_gradient(Solver<R> &S, int ipa, int n, const float *camx, const float
   if (cost) *cost = c;
   // phase 3: adjoint rays (per-thread accumulators)
   const int nt = std::max(1, nthreads);
-  std::vector<std::vector<double>> g(nt, std::vector<double>((size_t)L.ng * 2, 0.0)), bw(nt, std::vector<double>(S.npts, 0.0));
+  const int ND = Levis<R>::NUMDER;
+  std::vector<std::vector<double>> g(nt, std::vector<double>((size_t)L.ng * ND, 0.0)), bw(nt, std::vector<double>(S.npts, 0.0));
   std::vector<std::string> errs(nt);
   std::vector<int> bad(nt, 0);
   const double pi = std::acos(-1.0);
@@ -3198,7 +3304,7 @@ bool levis_gradient(Solver<R> &S, int ipa, int n, const float *camx, const float
     for (auto &x : th) x.join();
   }
   for (int t = 0; t < nt; ++t) if (bad[t]) { S.err = errs[t]; return false; }
-  std::vector<double> G((size_t)L.ng * 2, 0.0), beam(S.npts, 0.0);
+  std::vector<double> G((size_t)L.ng * ND, 0.0), beam(S.npts, 0.0);
   for (int t = 0; t < nt; ++t) {
     for (size_t k = 0; k < G.size(); ++k) G[k] += g[t][k];
     for (int k = 0; k < S.npts; ++k) beam[k] += bw[t][k];
@@ -3206,7 +3312,8 @@ bool levis_gradient(Solver<R> &S, int ipa, int n, const float *camx, const float
   // phase 4: direct-beam derivative per grid point
   for (int ip = 0; ip < S.npts; ++ip)
     if (beam[ip] != 0.0) L.direct_beam_deriv(ip, beam[ip], G);
-  for (size_t k = 0; k < G.size(); ++k) gradout[k] = G[k];
+  for (int ib = 0; ib < L.ng; ++ib)
+    for (int d = 0; d < nout; ++d) gradout[(size_t)ib * nout + d] = G[(size_t)ib * ND + d];
   return true;
 }
 
@@ -3334,6 +3441,32 @@ int oracle_levis_adjoint(void *hv, int ipa, int n, const float *camx, const floa
                                           nullptr, nullptr, nthreads)
                     : orc::levis_gradient(*h->s32, ipa, n, camx, camy, camz, cammu, camphi, nullptr, weights, gradout,
                                           nullptr, nullptr, nthreads);
+  return ok ? 0 : 1;
+}
+
+// The adjoint pass with the phase-derivative direction as a third unknown:
+// gradout [npx*npy*npz][3] (extinction, albedo, phase).
+int oracle_levis_adjoint_phase(void *hv, int ipa, int n, const float *camx, const float *camy, const float *camz,
+                               const double *cammu, const double *camphi, const double *weights, int ndphase,
+                               int nlegd, const float *dleg, const int *diph, double *gradout, int nthreads) {
+  Handle *h = (Handle *)hv;
+  orc::PhaseDeriv pd;
+  pd.ndphase = ndphase; pd.nlegd = nlegd; pd.dleg = dleg; pd.diph = diph;
+  bool ok = h->fp64 ? orc::levis_gradient(*h->s64, ipa, n, camx, camy, camz, cammu, camphi, nullptr, weights, gradout,
+                                          nullptr, nullptr, nthreads, &pd, 3)
+                    : orc::levis_gradient(*h->s32, ipa, n, camx, camy, camz, cammu, camphi, nullptr, weights, gradout,
+                                          nullptr, nullptr, nthreads, &pd, 3);
+  return ok ? 0 : 1;
+}
+
+int oracle_frozen_render_phase(void *hv, int ipa, int voxel, float eps, int nlegd, const float *dleg_row, int n,
+                               const float *camx, const float *camy, const float *camz, const double *cammu,
+                               const double *camphi, float *out, int nthreads) {
+  Handle *h = (Handle *)hv;
+  bool ok = h->fp64 ? orc::frozen_render_phase(*h->s64, ipa, voxel, eps, nlegd, dleg_row, n, camx, camy, camz, cammu,
+                                               camphi, out, nthreads)
+                    : orc::frozen_render_phase(*h->s32, ipa, voxel, eps, nlegd, dleg_row, n, camx, camy, camz, cammu,
+                                               camphi, out, nthreads);
   return ok ? 0 : 1;
 }
 

@@ -62,3 +62,29 @@ def test_matches_frozen_field_differences(solved, idr, tol):
     for v in [v for v in order if not interior[v]][:3]:
         fd = _fd(o, pb, rays, meas, v, idr)
         assert abs(grad[v, idr] - fd) <= 0.15 * abs(fd), (v, grad[v, idr], fd)
+
+
+def test_phase_derivative_matches_frozen_field_differences(solved):
+    """The third unknown of LEVISAPPROX_GRADIENT: the phase function moved
+    along a derivative series (DLEG / DIPHASEP; here d/dg of the cloud's
+    Henyey-Greenstein series, with delta-M, so the DFP terms of
+    PREPARE_DERIV_INTERPS and the DSINGSCAT term enter).  Against central
+    differences of the frozen-field forward model with that voxel's phase
+    function moved, 1% on the five voxels that carry most of the gradient;
+    the extinction and albedo columns are those of the two-unknown pass."""
+    pb, o, rays, meas, grad, cost, stokes, base = solved
+    nleg = pb.species[0].legcoef.shape[-1]
+    l = np.arange(nleg)
+    dleg = ((2 * l + 1) * l * 0.85 ** np.maximum(l - 1, 0)).astype(np.float32)
+    ng = pb.species[0].extinction.size
+    w = np.random.default_rng(1).standard_normal(len(rays[0]))
+    before = o.render(*rays)
+    G = o.levis_adjoint_phase(0, rays, w, dleg[None], np.ones((ng, 1), np.int32), nthreads=4)
+    assert np.array_equal(G[:, :2], o.levis_adjoint(0, rays, w, nthreads=4).reshape(-1, 2))
+    for v in np.argsort(-np.abs(G[:, 2]))[:5]:
+        h = 1e-3
+        pp = o.frozen_render_phase(0, int(v), h, dleg, rays).astype(np.float64)
+        pm = o.frozen_render_phase(0, int(v), -h, dleg, rays).astype(np.float64)
+        fd = np.dot(w, pp - pm) / (2 * h)
+        assert abs(G[v, 2] - fd) <= 0.01 * abs(fd), (v, G[v, 2], fd)
+    assert np.array_equal(o.render(*rays), before)      # the perturbed renders leave the solver as it was
