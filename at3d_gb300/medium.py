@@ -490,3 +490,51 @@ class OpticalPropertyGenerator:
                        legcoef=np.ascontiguousarray(legcoef, np.float32),
                        table_index=(1 + phase_index).reshape((-1,) + shape).astype(np.int32),
                        phase_weights=weights.reshape((-1,) + shape).astype(np.float32))
+
+
+def _point_mixtures(sp: Species, num_stokes: int) -> np.ndarray:
+    """Per grid point the phase mixture sum_q w_q legcoef[table_index_q - 1]:
+    [npts, nleg+1] (scalar) or [npts, 6, nleg+1]."""
+    leg = np.asarray(sp.legcoef, np.float64)
+    ti = np.asarray(sp.table_index).reshape(np.asarray(sp.table_index).shape[0], -1)
+    pw = np.asarray(sp.phase_weights, np.float64).reshape(ti.shape)
+    out = np.zeros((ti.shape[1],) + leg.shape[1:])
+    for q in range(ti.shape[0]):
+        out += pw[q].reshape((-1,) + (1,) * (leg.ndim - 1)) * leg[ti[q] - 1]
+    return out
+
+
+def _generator_derivatives(self, variable_names, microphysics, rel_step: float = 0.01) -> dict:
+    """Derivatives of the optical properties with respect to microphysical
+    variables (OpticalPropertyGenerator.calculate_derivatives,
+    at3d/medium.py:322-510), by central differences of this generator's own
+    output: each named variable ('density' or a distribution parameter) is
+    moved by +-rel_step x its value (+-rel_step where it is 0) at every
+    point at once (the properties are pointwise).  Returns {key: {name:
+    {'extinction', 'ssalb': [npx, npy, npz], 'legcoef': the derivative of
+    each point's phase mixture, [npts, nleg+1] or [npts, 6, nleg+1]}}}.
+    Inside a bracket of a tabulated parameter the mixing is multilinear, so
+    the differences are the exact derivative there.  The phase derivatives
+    hold one series per point: for large grids ask for few variables."""
+    out = {k: {} for k in self._monodisperse_tables}
+    for name in np.atleast_1d(variable_names):
+        name = str(name)
+        if name != "density" and name not in self._names:
+            raise ValueError(f"Invalid variable name to differentiate '{name}'")
+        v = np.asarray(microphysics[name], np.float64)
+        step = np.where(v != 0, rel_step * np.abs(v), rel_step)
+        plus = self(dict(microphysics, **{name: v + step}))
+        minus = self(dict(microphysics, **{name: v - step}))
+        for k in out:
+            d = 2.0 * step
+            dleg = (_point_mixtures(plus[k], self.num_stokes) - _point_mixtures(minus[k], self.num_stokes))
+            out[k][name] = {
+                "extinction": (np.asarray(plus[k].extinction, np.float64) - minus[k].extinction) / d,
+                "ssalb": (np.asarray(plus[k].ssalb, np.float64) - minus[k].ssalb) / d,
+                "legcoef": dleg / d.reshape((-1,) + (1,) * (dleg.ndim - 1)),
+            }
+    self(microphysics)   # keep the result of the unperturbed microphysics
+    return out
+
+
+OpticalPropertyGenerator.calculate_derivatives = _generator_derivatives

@@ -175,14 +175,17 @@ class Oracle:
             raise RuntimeError(self._lib.oracle_error(C.c_void_p(self._h)).decode())
         return grad
 
-    def frozen_render_phase(self, species: int, voxel: int, eps: float, dleg_row, rays, nthreads: int = 1):
+    def frozen_render_phase(self, species: int, voxel: int, eps: float, dleg_row, rays, nthreads: int = 1,
+                            dext: float = 0.0, dalb: float = 0.0):
         """frozen_render with one voxel's phase function (its current mixture)
-        plus eps x ``dleg_row`` (Legendre series with the 2l+1 factor)."""
+        plus eps x ``dleg_row`` (Legendre series with the 2l+1 factor), and
+        its extinction and albedo moved by dext, dalb."""
         x, y, z, mu, phi = self._rays(*rays)
         row = np.ascontiguousarray(dleg_row, np.float32)
         out = np.zeros(len(x), np.float32)
         rc = self._lib.oracle_frozen_render_phase(C.c_void_p(self._h), int(species), int(voxel), C.c_float(eps),
-                                                  row.size - 1, _p(row), len(x), _p(x), _p(y), _p(z),
+                                                  row.size - 1, _p(row), C.c_float(dext), C.c_float(dalb),
+                                                  len(x), _p(x), _p(y), _p(z),
                                                   _p(mu, C.c_double), _p(phi, C.c_double), _p(out), int(nthreads))
         if rc:
             raise RuntimeError(self._lib.oracle_error(C.c_void_p(self._h)).decode())

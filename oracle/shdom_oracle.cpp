@@ -3218,13 +3218,13 @@ struct PhaseDeriv {
 };
 
 // frozen_render with the phase function of one voxel of species ipa moved
-// along a derivative series: the voxel gets a phase-table row of its own,
-// its current mixture plus eps x dleg_row (nlegd+1 terms with the 2l+1
-// factor), with weight 1.
+// along a derivative series (and its extinction and albedo by dext, dalb):
+// the voxel gets a phase-table row of its own, its current mixture plus
+// eps x dleg_row (nlegd+1 terms with the 2l+1 factor), with weight 1.
 template <typename R>
-bool frozen_render_phase(Solver<R> &S, int ipa, int voxel, float eps, int nlegd, const float *dleg_row, int n,
-                         const float *camx, const float *camy, const float *camz, const double *cammu,
-                         const double *camphi, float *out, int nthreads) {
+bool frozen_render_phase(Solver<R> &S, int ipa, int voxel, float eps, int nlegd, const float *dleg_row, float dext,
+                         float dalb, int n, const float *camx, const float *camy, const float *camz,
+                         const double *cammu, const double *camphi, float *out, int nthreads) {
   const int ng = S.p.npx * S.p.npy * S.p.npz, nm = S.p.maxnmicro, nlp = S.p.nlegp;
   if (ipa < 0 || ipa >= S.npart || voxel < 0 || voxel >= ng) { S.err = "frozen_render_phase: bad index"; return false; }
   if (S.nst != 1) { S.err = "frozen_render_phase: scalar problems only"; return false; }
@@ -3240,7 +3240,7 @@ bool frozen_render_phase(Solver<R> &S, int ipa, int voxel, float eps, int nlegd,
   S.legp.insert(S.legp.end(), row.begin(), row.end());
   S.p.numphase += 1;
   for (int q = 0; q < nm; ++q) { S.iphp[o + q] = S.p.numphase; S.phwtp[o + q] = q == 0 ? 1.f : 0.f; }
-  bool ok = frozen_render(S, ipa, voxel, 0.f, 0.f, n, camx, camy, camz, cammu, camphi, out, nthreads);
+  bool ok = frozen_render(S, ipa, voxel, dext, dalb, n, camx, camy, camz, cammu, camphi, out, nthreads);
   S.legp = legp; S.iphp = iphp; S.phwtp = phwtp; S.p = p0;
   if (ok) ok = S.transfer_properties();   // back to the solver's own tables
   return ok;
@@ -3459,14 +3459,14 @@ int oracle_levis_adjoint_phase(void *hv, int ipa, int n, const float *camx, cons
   return ok ? 0 : 1;
 }
 
-int oracle_frozen_render_phase(void *hv, int ipa, int voxel, float eps, int nlegd, const float *dleg_row, int n,
-                               const float *camx, const float *camy, const float *camz, const double *cammu,
-                               const double *camphi, float *out, int nthreads) {
+int oracle_frozen_render_phase(void *hv, int ipa, int voxel, float eps, int nlegd, const float *dleg_row, float dext,
+                               float dalb, int n, const float *camx, const float *camy, const float *camz,
+                               const double *cammu, const double *camphi, float *out, int nthreads) {
   Handle *h = (Handle *)hv;
-  bool ok = h->fp64 ? orc::frozen_render_phase(*h->s64, ipa, voxel, eps, nlegd, dleg_row, n, camx, camy, camz, cammu,
-                                               camphi, out, nthreads)
-                    : orc::frozen_render_phase(*h->s32, ipa, voxel, eps, nlegd, dleg_row, n, camx, camy, camz, cammu,
-                                               camphi, out, nthreads);
+  bool ok = h->fp64 ? orc::frozen_render_phase(*h->s64, ipa, voxel, eps, nlegd, dleg_row, dext, dalb, n, camx, camy,
+                                               camz, cammu, camphi, out, nthreads)
+                    : orc::frozen_render_phase(*h->s32, ipa, voxel, eps, nlegd, dleg_row, dext, dalb, n, camx, camy,
+                                               camz, cammu, camphi, out, nthreads);
   return ok ? 0 : 1;
 }
 
