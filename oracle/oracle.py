@@ -35,7 +35,7 @@ def lib():
         for n in ("oracle_sizes", "oracle_solve", "oracle_init_solution", "oracle_export",
                   "oracle_render", "oracle_grid", "oracle_angles", "oracle_levis_gradient",
                   "oracle_frozen_render", "oracle_set_render_options", "oracle_levis_adjoint",
-                  "oracle_levis_adjoint_phase", "oracle_frozen_render_phase"):
+                  "oracle_levis_adjoint_phase", "oracle_frozen_render_phase", "oracle_tree"):
             getattr(L, n).restype = C.c_int
         L.oracle_destroy.argtypes = [C.c_void_p]
         _LIB = L
@@ -197,6 +197,14 @@ class Oracle:
         nb = np.zeros((nc, 6), np.int32); cf = np.zeros(nc, np.int16)
         self._lib.oracle_grid(C.c_void_p(self._h), _p(gp), _p(gptr, C.c_int), _p(nb, C.c_int), _p(cf, C.c_short))
         return gp, gptr, nb, cf
+
+    def tree(self):
+        """The cell tree of an adaptive grid, [ncells, 2]: parent (-1 for a
+        base cell) and first child (0 for an end cell); a neighbour pointer
+        v <= -2 in grid() names cell -v - 2, which has children."""
+        t = np.zeros((self.sizes["ncells"], 2), np.int32)
+        self._lib.oracle_tree(C.c_void_p(self._h), _p(t, C.c_int))
+        return t
 
     def __del__(self):
         try:

@@ -197,6 +197,19 @@ struct Solver {
   std::vector<float> xgrid, ygrid, zgrid, gridpos;  // gridpos[npts][3]
   std::vector<int> gridptr, neighptr;              // [ncells][8], [ncells][6]
   std::vector<short> cellflags;
+  // Adaptive grid (SPLIT_GRID and its helpers, src/polarized/shdomsub1.f:
+  // 4703-5902): treeptr [ncells][2] holds the parent (-1 for a base cell)
+  // and the first of the two children (0 for an end cell); bits 2-3 of
+  // cellflags hold the direction a parent was split in (1 X, 2 Y, 3 Z).  A
+  // neighbour that has children is stored as -(cell + 2); -1 is no
+  // neighbour.  nbpts / nbcells: the base grid.
+  std::vector<int> treeptr;
+  int nbpts = 0, nbcells = 0;
+  float adapt_grid_factor = 5.f, cell_to_point_ratio = 1.5f, num_sh_term_factor = 1.f;
+  static int nb_cell(int v) { return v >= -1 ? v : -v - 2; }
+  static int nb_parent(int c) { return -c - 2; }
+  int split_dir(int c) const { return (cellflags[c] >> 2) & 3; }
+  bool outofmem = false;
   int noct = 8;
   std::vector<int> sweep_cell, sweep_corner;  // [noct][npts]
 
@@ -340,8 +353,8 @@ struct Solver {
     p.sfc_params = nullptr;
     p.zlevels = nullptr; p.extinctp = p.albedop = p.phasewtp = p.legenp = p.sfc_albedo = nullptr;
     p.iphasep = nullptr;
-    if (p.splitacc > 0) { err = "adaptive splitting is not supported"; return false; }
     if (!setup_grid()) return false;
+    if (p.splitacc > 0 && ipflag != 0) { err = "adaptive splitting is restated for 3D grids only"; return false; }
     setup_angles();
     if (!transfer_properties()) return false;
     return true;
@@ -424,7 +437,26 @@ struct Solver {
         }
       }
     }
+    treeptr.assign((size_t)2 * ncells, 0);
+    for (int c = 0; c < ncells; ++c) treeptr[2 * c] = -1;
+    nbpts = npts; nbcells = ncells;
     return true;
+  }
+
+  // NEXT_CELL (src/polarized/shdomsub1.f:4470-4527): the end cell across face
+  // iface (0-5: -X,+X,-Y,+Y,-Z,+Z; jface its axis) of icell that contains
+  // (xe, ye, ze).
+  int next_cell(double xe, double ye, double ze, int iface, int jface, int icell) const {
+    int v = neighptr[6 * icell + iface];
+    if (v >= -1) return v;
+    int ic = nb_cell(v);
+    const double pos[3] = {xe, ye, ze};
+    while (treeptr[2 * ic + 1] > 0) {
+      int dir = split_dir(ic), c1 = treeptr[2 * ic + 1];
+      if (dir == jface + 1) ic = c1 + 1 - (iface % 2);
+      else ic = (pos[dir - 1] > gridpos[3 * gridptr[8 * c1 + 7] + dir - 1]) ? c1 + 1 : c1;
+    }
+    return ic;
   }
 
   // SWEEPING_ORDER / SWEEP_BASE_CELL (src/polarized/shdomsub1.f:3261-3351,
@@ -451,16 +483,30 @@ struct Solver {
       std::fill(done.begin(), done.end(), 0);
       int iorder = 0;
       int ix = six, iy = siy, iz = siz;
+      std::vector<int> stack;
       while (true) {
-        int icell = (iz - 1) + (nz - 1) * (iy - 1) + (nz - 1) * nyc * (ix - 1);
-        for (int k = 0; k < 8; ++k) {
-          int corner = (k ^ b) ^ 7;
-          int ipt = gridptr[8 * icell + corner];
-          if (done[ipt]) continue;
-          done[ipt] = 1;
-          sweep_cell[(size_t)joct * npts + iorder] = icell;
-          sweep_corner[(size_t)joct * npts + iorder] = corner;
-          ++iorder;
+        // SWEEP_NEXT_CELL: the end cells of this base cell's tree, the child
+        // on the upwind side of each split first
+        stack.assign(1, (iz - 1) + (nz - 1) * (iy - 1) + (nz - 1) * nyc * (ix - 1));
+        while (!stack.empty()) {
+          int icell = stack.back();
+          stack.pop_back();
+          if (treeptr[2 * icell + 1] > 0) {
+            int c1 = treeptr[2 * icell + 1];
+            bool first_neg = (b >> (split_dir(icell) - 1)) & 1;
+            stack.push_back(first_neg ? c1 + 1 : c1);
+            stack.push_back(first_neg ? c1 : c1 + 1);
+            continue;
+          }
+          for (int k = 0; k < 8; ++k) {
+            int corner = (k ^ b) ^ 7;
+            int ipt = gridptr[8 * icell + corner];
+            if (done[ipt]) continue;
+            done[ipt] = 1;
+            sweep_cell[(size_t)joct * npts + iorder] = icell;
+            sweep_corner[(size_t)joct * npts + iorder] = corner;
+            ++iorder;
+          }
         }
         if (ix == eix) {
           if (iy == eiy) {
@@ -590,10 +636,98 @@ struct Solver {
   // TRANSFER_PA_TO_GRID -> INTERP_GRID -> TRILIN_INTERP_PROP -> PREPARE_PROP
   // (src/polarized/shdomsub1.f:19-110, src/polarized/shdomsub2.f:313-390,
   // src/polarized/shdom90.f90:17-350, src/polarized/shdomsub2.f:479-611).
+  // TRILIN_INTERP_PROP (src/polarized/shdomsub2.f), 'N' method: species ipa
+  // at grid point ipt from the property grid, before the delta-M scaling
+  // (extinction, albedo, the phase indices and weights of the 8 corners
+  // merged and sorted, and the temperature).
+  bool trilin_point(int ipa, int ipt, R &extr) {
+    const int npx = p.npx, npy = p.npy, npz = p.npz, ng = npx * npy * npz;
+    float x = gridpos[3 * ipt], y = gridpos[3 * ipt + 1], z = gridpos[3 * ipt + 2];
+    int il = 0, iu = npz;
+    while (iu - il > 1) { int im = (iu + il) / 2; if (z >= zlev[im - 1]) il = im; else iu = im; }
+    int iz = std::max(il, 1);
+    double w = (double)(z - zlev[iz - 1]) / (zlev[iz] - zlev[iz - 1]);
+    w = std::max(std::min(w, 1.0), 0.0);
+    int ix = (int)(x / p.delx) + 1;
+    if (std::fabs(x - npx * p.delx) < 0.01f * p.delx) ix = npx;
+    if (ix < 1 || ix > npx) { err = "TRILIN: Beyond X domain"; return false; }
+    int ixp = ix % npx + 1;
+    double u = (double)(x - p.delx * (ix - 1)) / p.delx;
+    u = std::max(std::min(u, 1.0), 0.0);
+    if (u < 1e-5) u = 0; if (u > 1 - 1e-5) u = 1;
+    int iy = (int)(y / p.dely) + 1;
+    if (std::fabs(y - npy * p.dely) < 0.01f * p.dely) iy = npy;
+    if (iy < 1 || iy > npy) { err = "TRILIN: Beyond Y domain"; return false; }
+    int iyp = iy % npy + 1;
+    double v = (double)(y - p.dely * (iy - 1)) / p.dely;
+    v = std::max(std::min(v, 1.0), 0.0);
+    if (v < 1e-5) v = 0; if (v > 1 - 1e-5) v = 1;
+    double f[8] = {(1 - u) * (1 - v) * (1 - w), u * (1 - v) * (1 - w), (1 - u) * v * (1 - w),
+                   u * v * (1 - w),             (1 - u) * (1 - v) * w, u * (1 - v) * w,
+                   (1 - u) * v * w,             u * v * w};
+    int i1 = (iz - 1) + npz * (iy - 1) + npz * npy * (ix - 1);
+    int i2 = (iz - 1) + npz * (iy - 1) + npz * npy * (ixp - 1);
+    int i3 = (iz - 1) + npz * (iyp - 1) + npz * npy * (ix - 1);
+    int i4 = (iz - 1) + npz * (iyp - 1) + npz * npy * (ixp - 1);
+    int ii[8] = {i1, i2, i3, i4, i1 + 1, i2 + 1, i3 + 1, i4 + 1};
+    const float *E = &extp[(size_t)ipa * ng];
+    const float *A = &albp[(size_t)ipa * ng];
+    double ext = 0, scat[8], scatter = 0;
+    for (int c = 0; c < 8; ++c) { ext += f[c] * E[ii[c]]; scat[c] = f[c] * E[ii[c]] * A[ii[c]]; scatter += scat[c]; }
+    if (ipa == 0 && srct != 'S') {
+      double t = 0;
+      for (int c = 0; c < 8; ++c) t += f[c] * tempp_in[ii[c]];
+      temp[ipt] = (float)t;
+    }
+    extr = (R)ext;
+    R alb = (ext > extmin) ? (R)(scatter / ext) : (R)(scatter / extmin);
+    extinct[(size_t)ipa * npts + ipt] = extr;
+    albedo[(size_t)ipa * npts + ipt] = alb;
+    int *IPH = &iphase[((size_t)ipa * npts + ipt) * nq];
+    R *PW = &phaseinterpwt[((size_t)ipa * npts + ipt) * nq];
+    for (int c = 0; c < 8; ++c)
+      for (int q = 0; q < maxnmicro; ++q) {
+        IPH[c * maxnmicro + q] = iphp[((size_t)ipa * ng + ii[c]) * maxnmicro + q];
+        double pw = phwtp[((size_t)ipa * ng + ii[c]) * maxnmicro + q];
+        PW[c * maxnmicro + q] = (R)(scatter >= scatmin ? pw * scat[c] / scatter : pw * scat[c] / scatmin);
+      }
+    for (int q = 0; q < nq; ++q)
+      for (int q2 = q + 1; q2 < nq; ++q2)
+        if (IPH[q] == IPH[q2]) { PW[q] += PW[q2]; PW[q2] = 0; }
+    std::vector<std::pair<R, int>> srt(nq);
+    for (int q = 0; q < nq; ++q) srt[q] = {PW[q], IPH[q]};
+    std::stable_sort(srt.begin(), srt.end(), [](const std::pair<R, int> &a, const std::pair<R, int> &b) { return a.first > b.first; });
+    for (int q = 0; q < nq; ++q) { PW[q] = srt[q].first; IPH[q] = srt[q].second; }
+    return true;
+  }
+
+  // The delta-M scaling of one species' extinction and albedo at a grid point
+  // (PREPARE_PROP / INTERPOLATE_POINT, 'N' method).
+  void deltam_point(int ipa, int ipt) {
+    const int *IPH = &iphase[((size_t)ipa * npts + ipt) * nq];
+    const R *PW = &phaseinterpwt[((size_t)ipa * npts + ipt) * nq];
+    R f;
+    if (PW[0] >= phasemax) f = legen[(size_t)(IPH[0] - 1) * (nleg + 1) + ml + 1];
+    else { f = 0; for (int q = 0; q < nq; ++q) f += legen[(size_t)(IPH[q] - 1) * (nleg + 1) + ml + 1] * PW[q]; }
+    R &e = extinct[(size_t)ipa * npts + ipt];
+    R &a = albedo[(size_t)ipa * npts + ipt];
+    R anew = ((R)1 - f) * a / ((R)1 - a * f);
+    e = ((R)1 - a * f) * e;
+    a = anew;
+  }
+
+  void planck_point(int ipt) {
+    const R bb = (R)planck_fn(temp[ipt]);
+    R tp = 0;
+    for (int ipa = 0; ipa < npart; ++ipa)
+      tp = tp + extinct[(size_t)ipa * npts + ipt] * (((R)1 - albedo[(size_t)ipa * npts + ipt]) * bb);
+    planck_tot[ipt] = total_ext[ipt] > (R)1e-10 ? tp / total_ext[ipt] : (R)0;
+  }
+
   bool transfer_properties() {
     npart = p.npart; maxnmicro = p.maxnmicro; numphase = p.numphase;
     nq = 8 * maxnmicro;
-    int npx = p.npx, npy = p.npy, npz = p.npz, ng = npx * npy * npz;
+    const int npz = p.npz;
     legen.assign((size_t)numphase * (nleg + 1), 0);
     for (int i = 0; i < numphase; ++i)
       for (int l = 0; l <= nleg; ++l)
@@ -612,67 +746,12 @@ struct Solver {
     total_ext.assign(npts, 0);
     iphase.assign((size_t)npart * npts * nq, 1); phaseinterpwt.assign((size_t)npart * npts * nq, 0);
     temp.assign(srct != 'S' ? npts : 0, 0.f);
-    for (int ipa = 0; ipa < npart; ++ipa) {
+    for (int ipa = 0; ipa < npart; ++ipa)
       for (int ipt = 0; ipt < npts; ++ipt) {
-        float x = gridpos[3 * ipt], y = gridpos[3 * ipt + 1], z = gridpos[3 * ipt + 2];
-        int il = 0, iu = npz;
-        while (iu - il > 1) { int im = (iu + il) / 2; if (z >= zlev[im - 1]) il = im; else iu = im; }
-        int iz = std::max(il, 1);
-        double w = (double)(z - zlev[iz - 1]) / (zlev[iz] - zlev[iz - 1]);
-        w = std::max(std::min(w, 1.0), 0.0);
-        int ix = (int)(x / p.delx) + 1;
-        if (std::fabs(x - npx * p.delx) < 0.01f * p.delx) ix = npx;
-        if (ix < 1 || ix > npx) { err = "TRILIN: Beyond X domain"; return false; }
-        int ixp = ix % npx + 1;
-        double u = (double)(x - p.delx * (ix - 1)) / p.delx;
-        u = std::max(std::min(u, 1.0), 0.0);
-        if (u < 1e-5) u = 0; if (u > 1 - 1e-5) u = 1;
-        int iy = (int)(y / p.dely) + 1;
-        if (std::fabs(y - npy * p.dely) < 0.01f * p.dely) iy = npy;
-        if (iy < 1 || iy > npy) { err = "TRILIN: Beyond Y domain"; return false; }
-        int iyp = iy % npy + 1;
-        double v = (double)(y - p.dely * (iy - 1)) / p.dely;
-        v = std::max(std::min(v, 1.0), 0.0);
-        if (v < 1e-5) v = 0; if (v > 1 - 1e-5) v = 1;
-        double f[8] = {(1 - u) * (1 - v) * (1 - w), u * (1 - v) * (1 - w), (1 - u) * v * (1 - w),
-                       u * v * (1 - w),             (1 - u) * (1 - v) * w, u * (1 - v) * w,
-                       (1 - u) * v * w,             u * v * w};
-        int i1 = (iz - 1) + npz * (iy - 1) + npz * npy * (ix - 1);
-        int i2 = (iz - 1) + npz * (iy - 1) + npz * npy * (ixp - 1);
-        int i3 = (iz - 1) + npz * (iyp - 1) + npz * npy * (ix - 1);
-        int i4 = (iz - 1) + npz * (iyp - 1) + npz * npy * (ixp - 1);
-        int ii[8] = {i1, i2, i3, i4, i1 + 1, i2 + 1, i3 + 1, i4 + 1};
-        const float *E = &extp[(size_t)ipa * ng];
-        const float *A = &albp[(size_t)ipa * ng];
-        double ext = 0, scat[8], scatter = 0;
-        for (int c = 0; c < 8; ++c) { ext += f[c] * E[ii[c]]; scat[c] = f[c] * E[ii[c]] * A[ii[c]]; scatter += scat[c]; }
-        if (ipa == 0 && srct != 'S') {
-          double t = 0;
-          for (int c = 0; c < 8; ++c) t += f[c] * tempp_in[ii[c]];
-          temp[ipt] = (float)t;
-        }
-        R extr = (R)ext;
-        R alb = (ext > extmin) ? (R)(scatter / ext) : (R)(scatter / extmin);
-        extinct[(size_t)ipa * npts + ipt] = extr;
-        albedo[(size_t)ipa * npts + ipt] = alb;
-        int *IPH = &iphase[((size_t)ipa * npts + ipt) * nq];
-        R *PW = &phaseinterpwt[((size_t)ipa * npts + ipt) * nq];
-        for (int c = 0; c < 8; ++c)
-          for (int q = 0; q < maxnmicro; ++q) {
-            IPH[c * maxnmicro + q] = iphp[((size_t)ipa * ng + ii[c]) * maxnmicro + q];
-            double pw = phwtp[((size_t)ipa * ng + ii[c]) * maxnmicro + q];
-            PW[c * maxnmicro + q] = (R)(scatter >= scatmin ? pw * scat[c] / scatter : pw * scat[c] / scatmin);
-          }
-        for (int q = 0; q < nq; ++q)
-          for (int q2 = q + 1; q2 < nq; ++q2)
-            if (IPH[q] == IPH[q2]) { PW[q] += PW[q2]; PW[q2] = 0; }
-        std::vector<std::pair<R, int>> srt(nq);
-        for (int q = 0; q < nq; ++q) srt[q] = {PW[q], IPH[q]};
-        std::stable_sort(srt.begin(), srt.end(), [](const std::pair<R, int> &a, const std::pair<R, int> &b) { return a.first > b.first; });
-        for (int q = 0; q < nq; ++q) { PW[q] = srt[q].first; IPH[q] = srt[q].second; }
+        R extr;
+        if (!trilin_point(ipa, ipt, extr)) return false;
         total_ext[ipt] += extr;
       }
-    }
     // PREPARE_PROP, 'N' interpolation method
     if (p.deltam) {
       for (int i = 0; i < numphase; ++i) {
@@ -695,17 +774,8 @@ struct Solver {
       }
       for (int ipa = 0; ipa < npart; ++ipa)
         for (int ipt = 0; ipt < npts; ++ipt) {
-          const int *IPH = &iphase[((size_t)ipa * npts + ipt) * nq];
-          const R *PW = &phaseinterpwt[((size_t)ipa * npts + ipt) * nq];
-          R f;
-          if (PW[0] >= phasemax) f = legen[(size_t)(IPH[0] - 1) * (nleg + 1) + ml + 1];
-          else { f = 0; for (int q = 0; q < nq; ++q) f += legen[(size_t)(IPH[q] - 1) * (nleg + 1) + ml + 1] * PW[q]; }
-          R &e = extinct[(size_t)ipa * npts + ipt];
-          R &a = albedo[(size_t)ipa * npts + ipt];
-          R anew = ((R)1 - f) * a / ((R)1 - a * f);
-          e = ((R)1 - a * f) * e;
-          a = anew;
-          total_ext[ipt] += e;
+          deltam_point(ipa, ipt);
+          total_ext[ipt] += extinct[(size_t)ipa * npts + ipt];
         }
     }
     // PLANCK(I,IPA) = (1 - albedo) B(T) after the delta-M scaling
@@ -713,13 +783,7 @@ struct Solver {
     // extinction weights of COMPUTE_SOURCE (src/polarized/shdomsub1.f:1092-1139)
     planck_tot.assign(npts, 0);
     if (srct != 'S')
-      for (int ipt = 0; ipt < npts; ++ipt) {
-        const R bb = (R)planck_fn(temp[ipt]);
-        R tp = 0;
-        for (int ipa = 0; ipa < npart; ++ipa)
-          tp = tp + extinct[(size_t)ipa * npts + ipt] * (((R)1 - albedo[(size_t)ipa * npts + ipt]) * bb);
-        planck_tot[ipt] = total_ext[ipt] > (R)1e-10 ? tp / total_ext[ipt] : (R)0;
-      }
+      for (int ipt = 0; ipt < npts; ++ipt) planck_point(ipt);
     albmax = 0;
     for (auto a : albedo) albmax = std::max(albmax, a);
     return true;
@@ -773,8 +837,10 @@ struct Solver {
 
   // DIRECT_BEAM_PROP (src/polarized/shdom90.f90:352-867) via MAKE_DIRECT
   // (src/polarized/shdomsub2.f:393-476); regular property grid, no gas.
-  void make_direct() {
-    if (srct == 'T') { dirflux.assign(npts, 0); return; }  // no solar beam for a thermal source
+  // Points from `from` to `to` (new points of a split get theirs one at a time).
+  void make_direct(int from = 0, int to = -1) {
+    if (from == 0) dirflux.assign(npts, 0); else dirflux.resize(npts, 0);
+    if (srct == 'T') return;  // no solar beam for a thermal source
     int npx = p.npx, npy = p.npy, npz = p.npz, ng = npx * npy * npz;
     std::vector<double> extdirp(ng, 0.0);
     for (int ip = 0; ip < ng; ++ip) {
@@ -813,8 +879,7 @@ struct Solver {
     double delxd = p.delx, delyd = p.dely;
     epss = std::max(std::max(0.001 * delxd, 0.001 * delyd), epss);
     double xdomain = delxd * npx, ydomain = delyd * npy;
-    dirflux.assign(npts, 0);
-    for (int ipt = 0; ipt < npts; ++ipt) {
+    for (int ipt = from; ipt < (to < 0 ? npts : to); ++ipt) {
       double z = gridpos[3 * ipt + 2], x = gridpos[3 * ipt], y = gridpos[3 * ipt + 1];
       int il = 0, iu = npz;
       while (iu - il > 1) { int im = (iu + il) / 2; if (z >= zlev[im - 1]) il = im; else iu = im; }
@@ -1910,10 +1975,14 @@ struct Solver {
         if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; }
         else if (soy <= soz) { iface = 3 - bity; jface = 1; }
         else { iface = 5 - bitz; jface = 2; }
-        int inext = neighptr[6 * icell + iface];
-        const int *g = &gridptr[8 * icell];
-        int i1 = g[kGridFace[iface][0]], i2 = g[kGridFace[iface][1]], i3 = g[kGridFace[iface][2]],
-            i4 = g[kGridFace[iface][3]];
+        // across a face into smaller cells, the next cell's (smaller) face is
+        // interpolated, otherwise this cell's
+        const int nbv = neighptr[6 * icell + iface];
+        const int inext = nbv >= -1 ? nbv : next_cell(xe, ye, ze, iface, jface, icell);
+        const int kface = nbv >= -1 ? iface : kOppFace[iface];
+        const int *g = &gridptr[8 * (nbv >= -1 ? icell : inext)];
+        int i1 = g[kGridFace[kface][0]], i2 = g[kGridFace[kface][1]], i3 = g[kGridFace[kface][2]],
+            i4 = g[kGridFace[kface][3]];
         double u, v;
         if (jface == 0) {
           u = (ze - gridpos[3 * i1 + 2]) / (gridpos[3 * i3 + 2] - gridpos[3 * i1 + 2]);
@@ -2110,12 +2179,406 @@ struct Solver {
     }
   }
 
-  // SOLUTION_ITERATIONS (src/polarized/shdomsub1.f:445-818), no splitting.
+  // ------------------------------------------------------ adaptive grid
+  // Every per-point array grown to n points (gridpos may already be); the
+  // species-major arrays ([npart][npts]) are laid out again with the new
+  // stride.  The SH pointers of the new points are set by interpolate_point.
+  void grow_points(int n) {
+    const int old = npts;
+    auto relayout = [&](auto &v, size_t per) {
+      typename std::decay<decltype(v)>::type nv((size_t)npart * n * per);
+      for (int ipa = 0; ipa < npart; ++ipa)
+        std::copy(v.begin() + (size_t)ipa * old * per, v.begin() + ((size_t)ipa * old + old) * per,
+                  nv.begin() + (size_t)ipa * n * per);
+      v.swap(nv);
+    };
+    relayout(extinct, 1); relayout(albedo, 1); relayout(iphase, nq); relayout(phaseinterpwt, nq);
+    total_ext.resize(n, 0); dirflux.resize(n, 0); planck_tot.resize(n, 0);
+    if (!temp.empty()) temp.resize(n, 0.f);
+    gridpos.resize((size_t)3 * n);
+    fluxes.resize((size_t)2 * n, 0);
+    shptr.resize(n + 1, shptr[old]);
+    oshptr.resize(n + 1, oshptr[old]);
+    rshptr.resize(n + 2, rshptr[old]);
+    // room for every point's full SH series (COMPUTE_SOURCE truncates in place)
+    const size_t full = (size_t)n * nlm * nst;
+    if (source.size() < full) source.resize(full, 0);
+    if (p.accelflag && delsource.size() < full) delsource.resize(full, 0);
+    npts = n;
+  }
+
+  // CELL_SPLIT_TEST (src/polarized/shdomsub1.f:5702-5791): for each axis the
+  // mean over the four edges across it of |delta(ext J)| rms over angles
+  // (from the SH terms of the I source) / ext x (1 - exp(-tau)); the largest
+  // and its axis (1 X, 2 Y, 3 Z).
+  void cell_split_test(int icell, float &maxadapt, int &idir) const {
+    static const int gc[3][4][2] = {{{0, 1}, {2, 3}, {4, 5}, {6, 7}}, {{0, 2}, {1, 3}, {4, 6}, {5, 7}},
+                                    {{0, 4}, {1, 5}, {2, 6}, {3, 7}}};
+    const float c0 = 0.282095f;
+    maxadapt = -1.0f; idir = 0;
+    for (int id = 0; id < 3; ++id) {
+      float sum1 = 0.0f;
+      int num = 0;
+      for (int ie = 0; ie < 4; ++ie) {
+        const int ip1 = gridptr[8 * icell + gc[id][ie][0]], ip2 = gridptr[8 * icell + gc[id][ie][1]];
+        if (ip1 == ip2) continue;
+        ++num;
+        const int is1 = shptr[ip1], is2 = shptr[ip2], ns1 = shptr[ip1 + 1] - is1, ns2 = shptr[ip2 + 1] - is2;
+        const int ns = std::min(ns1, ns2);
+        const float e1 = (float)total_ext[ip1], e2 = (float)total_ext[ip2];
+        auto S = [&](int is, int j) { return (float)source[(size_t)(is + j) * nst]; };
+        float jay = 0.0f;
+        for (int j = 0; j < ns; ++j) { float d = e2 * S(is2, j) - e1 * S(is1, j); jay += d * d; }
+        for (int j = ns; j < ns1; ++j) { float d = e1 * S(is1, j); jay += d * d; }
+        for (int j = ns; j < ns2; ++j) { float d = e2 * S(is2, j); jay += d * d; }
+        const float ext = 0.5f * (e1 + e2);
+        jay = ext > 0.0f ? c0 * std::sqrt(jay) / ext : 0.0f;
+        const float tau = std::fabs(ext * (gridpos[3 * ip2 + id] - gridpos[3 * ip1 + id]));
+        sum1 += std::fabs(jay) * (1.0f - std::exp(-tau));
+      }
+      const float crit = num > 0 ? sum1 / (float)num : 0.0f;
+      if (crit > maxadapt) { maxadapt = crit; idir = id + 1; }
+    }
+  }
+
+  // MATCH_GRID_POINT (src/polarized/shdomsub1.f:5599-5700): an existing grid
+  // point at (xp, yp, zp) on the cells across face iface of icell, or -1.
+  int match_grid_point(float xp, float yp, float zp, int icell, int iface) const {
+    const int idir = iface / 2 + 1, kface = kOppFace[iface];
+    int ic = nb_cell(neighptr[6 * icell + iface]);
+    if (ic < 0) return -1;
+    const float pos[3] = {xp, yp, zp};
+    std::vector<int> stack;
+    while (true) {
+      while (treeptr[2 * ic + 1] == 0) {
+        for (int i = 0; i < 4; ++i) {
+          const int ipt = gridptr[8 * ic + kGridFace[kface][i]];
+          if (xp == gridpos[3 * ipt] && yp == gridpos[3 * ipt + 1] && zp == gridpos[3 * ipt + 2]) return ipt;
+        }
+        if (stack.empty()) return -1;
+        ic = stack.back();
+        stack.pop_back();
+      }
+      const int dir = split_dir(ic), ic1 = treeptr[2 * ic + 1];
+      if (dir == idir) { ic = ic1 + 1 - (iface % 2); continue; }
+      // a split across the face: follow the child holding the point, both when
+      // the point is on the split line
+      const float c = gridpos[3 * gridptr[8 * ic1 + 7] + dir - 1];
+      ic = ic1;
+      if (pos[dir - 1] == c) stack.push_back(ic1 + 1);
+      else if (pos[dir - 1] > c) ic = ic1 + 1;
+    }
+  }
+
+  // INHERIT_NEIGHBOR (src/polarized/shdomsub1.f:5454-5507): icell and every
+  // descendant bordering face iface get neighbour `in`.
+  void inherit_neighbor(int icell, int iface, int in) {
+    const int jface = iface / 2 + 1;
+    std::vector<int> stack;
+    int ic = icell;
+    while (true) {
+      neighptr[6 * ic + iface] = in;
+      if (treeptr[2 * ic + 1] == 0) {
+        if (stack.empty()) return;
+        ic = stack.back();
+        stack.pop_back();
+      } else if (split_dir(ic) == jface) {
+        ic = treeptr[2 * ic + 1] + (iface % 2);
+      } else {
+        stack.push_back(treeptr[2 * ic + 1] + 1);
+        ic = treeptr[2 * ic + 1];
+      }
+    }
+  }
+
+  // MATCH_NEIGHBOR_FACE (src/polarized/shdomsub1.f:5371-5451): the neighbour
+  // pointer of new cell ic across face iface, and those of the cells on the
+  // other side, from the sizes of the faces down the neighbour's tree.
+  void match_neighbor_face(int iface, int ic) {
+    int in = nb_cell(neighptr[6 * ic + iface]);
+    if (in < 0) return;
+    const int jface = iface / 2 + 1, dir1 = jface % 3 + 1, dir2 = (jface + 1) % 3 + 1;
+    const int ic1 = gridptr[8 * ic], ic8 = gridptr[8 * ic + 7];
+    auto G = [&](int ip, int d) { return gridpos[3 * ip + d - 1]; };
+    float pos[3] = {0, 0, 0};
+    pos[dir1 - 1] = (G(ic1, dir1) + G(ic8, dir1)) / 2;
+    pos[dir2 - 1] = (G(ic1, dir2) + G(ic8, dir2)) / 2;
+    bool done = false;
+    while (!done && ic != in) {
+      const int in1 = gridptr[8 * in], in8 = gridptr[8 * in + 7];
+      if (G(ic1, dir1) >= G(in1, dir1) && G(ic8, dir1) <= G(in8, dir1) && G(ic1, dir2) >= G(in1, dir2) &&
+          G(ic8, dir2) <= G(in8, dir2))
+        neighptr[6 * ic + iface] = treeptr[2 * in + 1] == 0 ? in : nb_parent(in);
+      if (G(in1, dir1) >= G(ic1, dir1) && G(in8, dir1) <= G(ic8, dir1) && G(in1, dir2) >= G(ic1, dir2) &&
+          G(in8, dir2) <= G(ic8, dir2)) {
+        inherit_neighbor(in, kOppFace[iface], ic);
+      } else {
+        int &w = neighptr[6 * in + kOppFace[iface]];
+        if (w != -1) w = nb_parent(nb_cell(w));
+      }
+      if (treeptr[2 * in + 1] == 0) done = true;
+      else {
+        const int dir = split_dir(in), inn = treeptr[2 * in + 1];
+        if (dir == jface) in = inn + 1 - (iface % 2);
+        else in = pos[dir - 1] > G(gridptr[8 * inn + 7], dir) ? inn + 1 : inn;
+      }
+    }
+  }
+
+  // NEW_GRID_POINTS (src/polarized/shdomsub1.f:5509-5597): the corner
+  // pointers of the two children, with a point at the middle of each of the
+  // four edges along the split unless a neighbour already has one there.
+  // newp[i] = {parent point 1, parent point 2, new point or -1}.
+  void new_grid_points(int idir, int icell, int nc, int newp[4][3], int &nnew) {
+    static const int gc[3][4][2] = {{{0, 1}, {2, 3}, {4, 5}, {6, 7}}, {{0, 2}, {1, 3}, {4, 6}, {5, 7}},
+                                    {{0, 4}, {1, 5}, {2, 6}, {3, 7}}};
+    static const int fg[3][4][2] = {{{2, 4}, {3, 4}, {2, 5}, {3, 5}}, {{0, 4}, {1, 4}, {0, 5}, {1, 5}},
+                                    {{0, 2}, {1, 2}, {0, 3}, {1, 3}}};
+    for (int k = 0; k < 8; ++k) gridptr[8 * nc + k] = gridptr[8 * (nc + 1) + k] = gridptr[8 * icell + k];
+    for (int i = 0; i < 4; ++i) {
+      const int i1 = gc[idir - 1][i][0], i2 = gc[idir - 1][i][1];
+      const int ip1 = gridptr[8 * icell + i1], ip2 = gridptr[8 * icell + i2];
+      const float xp = (gridpos[3 * ip1] + gridpos[3 * ip2]) / 2, yp = (gridpos[3 * ip1 + 1] + gridpos[3 * ip2 + 1]) / 2,
+                  zp = (gridpos[3 * ip1 + 2] + gridpos[3 * ip2 + 2]) / 2;
+      const int f1 = fg[idir - 1][i][0], f2 = fg[idir - 1][i][1];
+      int ipm = match_grid_point(xp, yp, zp, icell, f1);
+      if (ipm < 0) ipm = match_grid_point(xp, yp, zp, icell, f2);
+      if (ipm < 0) {
+        const int icell2 = nb_cell(neighptr[6 * icell + f1]);
+        if (icell2 >= 0) ipm = match_grid_point(xp, yp, zp, icell2, f2);
+      }
+      if (ipm < 0) {
+        const int ip = (int)(gridpos.size() / 3);
+        gridpos.push_back(xp); gridpos.push_back(yp); gridpos.push_back(zp);
+        gridptr[8 * nc + i2] = ip; gridptr[8 * (nc + 1) + i1] = ip;
+        newp[i][0] = ip1; newp[i][1] = ip2; newp[i][2] = ip;
+        ++nnew;
+      } else {
+        gridptr[8 * nc + i2] = ipm; gridptr[8 * (nc + 1) + i1] = ipm;
+        newp[i][2] = -1;
+      }
+    }
+  }
+
+  // DIVIDE_CELL (src/polarized/shdomsub1.f:5286-5368): end cell icell split
+  // in two along idir; the children are cells ncells and ncells + 1.
+  void divide_cell(int icell, int idir, int newp[4][3], int &nnew) {
+    const int nc = ncells;
+    ncells += 2;
+    treeptr.resize((size_t)2 * ncells, 0);
+    gridptr.resize((size_t)8 * ncells, 0);
+    neighptr.resize((size_t)6 * ncells, -1);
+    cellflags.resize(ncells, 0);
+    treeptr[2 * icell + 1] = nc;
+    treeptr[2 * nc] = icell; treeptr[2 * nc + 1] = 0;
+    treeptr[2 * (nc + 1)] = icell; treeptr[2 * (nc + 1) + 1] = 0;
+    cellflags[icell] = (short)(cellflags[icell] | (idir << 2));
+    cellflags[nc] = cellflags[nc + 1] = (short)(cellflags[icell] & 3);
+    nnew = 0;
+    new_grid_points(idir, icell, nc, newp, nnew);
+    for (int iface = 0; iface < 6; ++iface) {
+      const int v = neighptr[6 * icell + iface];
+      if (v == icell) {
+        neighptr[6 * nc + iface] = nc;
+        neighptr[6 * (nc + 1) + iface] = nc + 1;
+      } else if (iface == 2 * idir - 1) {
+        neighptr[6 * nc + iface] = nc + 1;
+        neighptr[6 * (nc + 1) + iface] = v;
+      } else if (iface == 2 * idir - 2) {
+        neighptr[6 * (nc + 1) + iface] = nc;
+        neighptr[6 * nc + iface] = v;
+      } else {
+        neighptr[6 * nc + iface] = v;
+        neighptr[6 * (nc + 1) + iface] = v;
+      }
+      match_neighbor_face(iface, nc);
+      match_neighbor_face(iface, nc + 1);
+    }
+  }
+
+  // GRID_SMOOTH_TEST (src/polarized/shdomsub1.f:5794-5902): the axis to split
+  // icell along so that the grid stays smooth (finer cells on both sides, the
+  // two opposite neighbours split alike, or a neighbour more than 2.5 times
+  // finer where there is a source), 0 for none.
+  int grid_smooth_test(int icell) const {
+    static const int ec[3][2] = {{0, 1}, {0, 2}, {0, 4}};
+    int idir = 0;
+    float sizeratio = 1.0f;
+    for (int id = 1; id <= 3; ++id) {
+      const int ip1 = gridptr[8 * icell + ec[id - 1][0]], ip2 = gridptr[8 * icell + ec[id - 1][1]];
+      if (ip1 == ip2) continue;
+      const float cur = std::fabs(gridpos[3 * ip1 + id - 1] - gridpos[3 * ip2 + id - 1]);
+      const float inv = 1.0f / cur;
+      float gsize[2];
+      int dirsplit[2];
+      for (int j = 0; j < 2; ++j) {
+        dirsplit[j] = 0;
+        const int iface = 2 * (id - 1) + j;
+        double xe = 0, ye = 0, ze = 0;
+        for (int i = 0; i < 4; ++i) {
+          const int ip = gridptr[8 * icell + kGridFace[iface][i]];
+          xe += gridpos[3 * ip] * 0.25f; ye += gridpos[3 * ip + 1] * 0.25f; ze += gridpos[3 * ip + 2] * 0.25f;
+        }
+        const int inc = next_cell(xe, ye, ze, iface, id - 1, icell);
+        if (inc < 0) gsize[j] = cur;
+        else {
+          gsize[j] = std::fabs(gridpos[3 * gridptr[8 * inc] + id - 1] - gridpos[3 * gridptr[8 * inc + 7] + id - 1]);
+          if (treeptr[2 * inc] < 0) gsize[j] = cur;
+          if (id <= 2 && ((cellflags[inc] >> (id - 1)) & 1)) gsize[j] = cur;
+        }
+        const int in = neighptr[6 * icell + iface];
+        if (in <= -2) dirsplit[j] = split_dir(nb_cell(in));
+      }
+      if (gsize[0] * inv < 0.75f && gsize[1] * inv < 0.75f) idir = id;
+      if (dirsplit[0] > 0 && dirsplit[0] != id && dirsplit[0] == dirsplit[1]) idir = dirsplit[0];
+      const float ratio = std::min(gsize[0] * inv, gsize[1] * inv);
+      if (ratio < 0.4f && ratio < sizeratio) {
+        int isum = 0;
+        for (int i = 0; i < 8; ++i) { const int ip = gridptr[8 * icell + i]; isum += shptr[ip + 1] - shptr[ip]; }
+        if (isum > 0) { idir = id; sizeratio = ratio; }
+      }
+    }
+    return idir;
+  }
+
+  // INTERPOLATE_POINT (src/polarized/shdomsub1.f:4934-5283): the medium of a
+  // new point from the property grid, its direct beam, its radiance the mean
+  // of its two parent points', and its source from that radiance.
+  bool interpolate_point(int ip1, int ip2, int ip) {
+    total_ext[ip] = 0;
+    for (int ipa = 0; ipa < npart; ++ipa) {
+      R e;
+      if (!trilin_point(ipa, ip, e)) return false;
+      if (p.deltam) deltam_point(ipa, ip);
+      total_ext[ip] += extinct[(size_t)ipa * npts + ip];
+    }
+    if (srct != 'S') planck_point(ip);
+    make_direct(ip, ip + 1);
+    const int ir1 = rshptr[ip1], ir2 = rshptr[ip2], nr1 = rshptr[ip1 + 1] - ir1, nr2 = rshptr[ip2 + 1] - ir2;
+    const int nr = std::max(nr1, nr2), ir = rshptr[ip];
+    rshptr[ip + 1] = ir + nr;
+    if (radiance.size() < (size_t)(ir + nr) * nst) radiance.resize((size_t)(ir + nr) * nst, 0);
+    for (int j = 0; j < nr; ++j)
+      for (int k = 0; k < nst; ++k) {
+        const R r1 = j < nr1 ? radiance[(size_t)(ir1 + j) * nst + k] : (R)0;
+        const R r2 = j < nr2 ? radiance[(size_t)(ir2 + j) * nst + k] : (R)0;
+        radiance[(size_t)(ir + j) * nst + k] = (R)0.5 * (r1 + r2);
+      }
+    const int ns = std::max(shptr[ip1 + 1] - shptr[ip1], shptr[ip2 + 1] - shptr[ip2]), is = shptr[ip];
+    shptr[ip + 1] = is + ns;
+    if (p.accelflag) oshptr[ip + 1] = oshptr[ip];
+    std::vector<R> sourcet, lt, lt1;
+    point_source(ip, sourcet, radiance, ir, nr, lt, lt1);
+    if (source.size() < (size_t)(is + ns) * nst) source.resize((size_t)(is + ns) * nst, 0);
+    for (int t = 0; t < ns * nst; ++t) source[(size_t)is * nst + t] = sourcet[t];
+    return true;
+  }
+
+  bool divide_and_interpolate(int icell, int idir) {
+    int newp[4][3], nnew = 0;
+    divide_cell(icell, idir, newp, nnew);
+    if (nnew == 0) return true;
+    grow_points(npts + nnew);
+    for (int i = 0; i < 4; ++i)
+      if (newp[i][2] >= 0 && !interpolate_point(newp[i][0], newp[i][1], newp[i][2])) return false;
+    rshptr[npts + 1] = rshptr[npts];
+    return true;
+  }
+
+  // SPLIT_GRID (src/polarized/shdomsub1.f:4703-4931): when dosplit, the end
+  // cells are tested in batches (the cells split in one batch are tested in
+  // the next), those above cursplitacc split in decreasing order of the
+  // criterion while the memory limits allow, and the rest tested for grid
+  // smoothness.  splitcrit: the largest criterion left after the divisions.
+  bool split_grid(bool dosplit, float cursplit, float &splitcrit_out) {
+    if (dosplit) {
+      const long maxig = (long)(adapt_grid_factor * (float)nbpts);
+      const long maxic = std::max((long)(cell_to_point_ratio * (float)maxig), (long)nbcells);
+      const long maxiv = std::max((long)(num_sh_term_factor * (float)nlm * (float)maxig), (long)nbpts * 4);
+      const long maxido = maxig * nphi0max;
+      int icell1 = 0;
+      bool outofmem0 = outofmem;
+      while (icell1 < ncells) {
+        std::vector<std::pair<float, int>> crit;
+        for (int ic = icell1; ic < ncells; ++ic)
+          if (treeptr[2 * ic + 1] == 0) {
+            float c; int d;
+            cell_split_test(ic, c, d);
+            crit.push_back({c, 4 * ic + d});
+          }
+        icell1 = ncells;
+        std::stable_sort(crit.begin(), crit.end(),
+                         [](const std::pair<float, int> &a, const std::pair<float, int> &b) { return a.first > b.first; });
+        const float frac = 0.03f;
+        long maxcells = (long)(maxic - frac * (maxic - ncells) - 2);
+        long maxpts = (long)(maxig - frac * (maxig - npts) - 4);
+        long maxwork = (long)(maxido - frac * (maxido - (long)nphi0max * npts) - 4 * nphi0max);
+        long maxsh = (long)(maxiv - frac * (maxiv - shptr[npts]) - 4 * nlm);
+        long maxrad = (long)(maxiv + maxig - frac * (maxiv + maxig - rshptr[npts]) - 4 * nlm);
+        auto full = [&]() {
+          return ncells > maxcells || npts > maxpts || (long)npts * nphi0max > maxwork || shptr[npts] > maxsh ||
+                 rshptr[npts] > maxrad;
+        };
+        outofmem0 = outofmem;
+        size_t i = 0;
+        while (i < crit.size() && crit[i].first > cursplit && !outofmem0) {
+          if (full()) outofmem0 = true;
+          else if (!divide_and_interpolate(crit[i].second / 4, crit[i].second & 3)) return false;
+          ++i;
+        }
+        maxcells = maxic - 2; maxpts = maxig - 4; maxwork = maxido - 4 * nphi0max;
+        maxsh = maxiv - 4 * nlm; maxrad = maxiv + maxig - 4 * nlm;
+        while (!outofmem && i < crit.size()) {
+          if (full()) outofmem = true;
+          else {
+            const int d = grid_smooth_test(crit[i].second / 4);
+            if (d > 0 && !divide_and_interpolate(crit[i].second / 4, d)) return false;
+          }
+          ++i;
+        }
+      }
+      if (outofmem0) outofmem = true;
+      boundary_points();
+      sweep_ready = false;
+    }
+    splitcrit_out = 0;
+    for (int ic = 0; ic < ncells; ++ic)
+      if (treeptr[2 * ic + 1] == 0) {
+        float c; int d;
+        cell_split_test(ic, c, d);
+        splitcrit_out = std::max(splitcrit_out, c);
+      }
+    return true;
+  }
+
+  // SOLUTION_ITERATIONS (src/polarized/shdomsub1.f:445-818), with the
+  // adaptive splitting schedule: splitting starts when the solution
+  // criterion falls below 0.1, and the current splitting accuracy is lowered
+  // from splitacc x 33.3 to splitacc as a geometric mean of the criterion
+  // goes from 0.1 to 0.003 (all splitting stops below 0.001).
   bool solution_iterations(int maxiter, int verbose) {
     bool fixsh = false;
     const R endadaptsol = (R)0.001;
-    while (iter < maxiter && solcrit > (R)p.solacc) {
+    const float splitacc = p.splitacc, startadapt = 0.1f, endadapt = 0.001f;
+    const float adaptrange = startadapt / (3.0f * endadapt);
+    float cursplit = splitacc * adaptrange, startsplit = cursplit, avgsolcrit = (float)solcrit, splitcrit = 0.0f;
+    bool splittesting = true;
+    while (iter < maxiter &&
+           (solcrit > (R)p.solacc || (splitcrit > splitacc && cursplit > splitacc && !outofmem))) {
       ++iter;
+      if (splitacc > 0.0f) {
+        const float sc = (float)solcrit;
+        avgsolcrit = std::sqrt(avgsolcrit * sc);
+        const bool dosplit = sc <= startadapt && (sc > endadapt || cursplit > splitacc) && !outofmem;
+        const float beta = std::log(startsplit / splitacc) / std::log(adaptrange);
+        cursplit = std::min(cursplit, std::max(splitacc, splitacc * std::pow(avgsolcrit / (3.0f * endadapt), beta)));
+        if (sc <= endadapt) cursplit = splitacc;
+        if (splittesting) {
+          if (!split_grid(dosplit, cursplit, splitcrit)) return false;
+          if (sc > startadapt) startsplit = splitcrit;
+        }
+        if (sc <= endadapt) splittesting = false;
+      }
       radiance_truncation(fixsh);
       if (!path_integration()) return false;
       if (solcrit < endadaptsol || iter > p.iterfixsh) fixsh = true;
@@ -2123,7 +2586,7 @@ struct Solver {
       accel_solcrit();
       if (albmax < (R)p.solacc) solcrit = (R)p.solacc;
       if (verbose)
-        std::printf("  %4d %8.3f %10.3e %8d %8.2f\n", iter, std::log10(std::max((double)solcrit, 1e-20)), 0.0,
+        std::printf("  %4d %8.3f %10.3e %8d %8.2f\n", iter, std::log10(std::max((double)solcrit, 1e-20)), (double)splitcrit,
                     npts, (double)shptr[npts] / npts);
     }
     return true;
@@ -2219,7 +2682,15 @@ struct Solver {
       nyc = ny + 1;
       if (y0 < ygrid[0]) iy = 1; else if (y0 > ygrid[ny - 1]) iy = ny + 1; else iy = iy + 1;
     }
-    return (iz - 1) + (nz - 1) * (iy - 1) + (nz - 1) * nyc * (ix - 1);
+    int icell = (iz - 1) + (nz - 1) * (iy - 1) + (nz - 1) * nyc * (ix - 1);
+    // down the tree to the end cell that holds the point
+    const double pos[3] = {x0, y0, z0};
+    while (treeptr[2 * icell + 1] > 0) {
+      int dir = split_dir(icell), c = treeptr[2 * icell + 1] + 1;
+      if (pos[dir - 1] < gridpos[3 * gridptr[8 * c] + dir - 1]) c -= 1;
+      icell = c;
+    }
+    return icell;
   }
 
   // INTEGRATE_1RAY + COMPUTE_SOURCE_1CELL_UNPOL + FIND_BOUNDARY_RADIANCE
@@ -2400,9 +2871,10 @@ struct Solver {
       if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; openbcface = (cellflags[icell] & 1) && (bcflag & 1); }
       else if (soy <= soz) { iface = 3 - bity; jface = 1; openbcface = (cellflags[icell] & 2) && (bcflag & 2); }
       else { iface = 5 - bitz; jface = 2; openbcface = false; }
-      int inext = neighptr[6 * icell + iface];
+      const int nbv = neighptr[6 * icell + iface];
+      int inext = nbv >= -1 ? nbv : next_cell(xn, yn, zn, iface, jface, icell);
       int kface, ic;
-      if (!openbcface) { kface = iface; ic = icell; }
+      if (nbv >= -1 && !openbcface) { kface = iface; ic = icell; }
       else { kface = kOppFace[iface]; ic = inext; iface = -1; }
       if (inext >= 0) {
         if (jface == 0) xn = gridpos[3 * gridptr[8 * inext + ioct - 1]];
@@ -2611,6 +3083,7 @@ struct Levis {
   // PREPARE_DERIV_INTERPS (src/polarized/shdomsub4.f:2917-3080).
   bool prepare(int ipa_der, std::string &err) {
     ipa = ipa_der;
+    if (S.npts != S.nbpts) { err = "the Levis gradient is restated for the base grid (no split cells)"; return false; }
     const auto &p = S.p;
     const int npx = p.npx, npy = p.npy, npz = p.npz, npts = S.npts, ml = S.ml, nl1 = S.nleg + 1;
     ng = npx * npy * npz;
@@ -3185,6 +3658,7 @@ bool frozen_render(Solver<R> &S, int ipa, int voxel, float dext, float dalb, int
   const int ng = S.p.npx * S.p.npy * S.p.npz;
   if (ipa < 0 || ipa >= S.npart || voxel < 0 || voxel >= ng) { S.err = "frozen_render: bad index"; return false; }
   if (S.nst != 1) { S.err = "frozen_render: scalar problems only"; return false; }
+  if (S.npts != S.nbpts) { S.err = "frozen_render: base grid only (no split cells)"; return false; }
   auto extp = S.extp, albp = S.albp;
   auto planck_tot = S.planck_tot;
   auto temp = S.temp;
@@ -3487,6 +3961,15 @@ int oracle_grid(void *hv, float *gridpos, int *gridptr, int *neighptr, short *ce
     if (neighptr) std::memcpy(neighptr, s->neighptr.data(), s->neighptr.size() * sizeof(int));
     if (cellflags) std::memcpy(cellflags, s->cellflags.data(), s->cellflags.size() * sizeof(short));
   };
+  if (h->fp64) g(h->s64); else g(h->s32);
+  return 0;
+}
+
+// The cell tree of an adaptive grid: treeptr [ncells][2] (parent or -1,
+// first child or 0).
+int oracle_tree(void *hv, int *treeptr) {
+  Handle *h = (Handle *)hv;
+  auto g = [&](auto *s) { std::memcpy(treeptr, s->treeptr.data(), s->treeptr.size() * sizeof(int)); };
   if (h->fp64) g(h->s64); else g(h->s32);
   return 0;
 }

@@ -2,7 +2,8 @@
 tests/test_shdom.py:175-261 of the reference) rebuilt from the committed
 fixture tests/golden/rico32x36x26w672_pol.npz: the property grid, the
 six-element phase-matrix table and the scene parameters of the original
-SHDOM output, with adaptive splitting off (the one difference)."""
+SHDOM output.  ``rico_problem(split_accuracy=...)``: the original run split
+cells adaptively at 0.1 (the fixture's 'splitacc'); 0 keeps the base grid."""
 import os
 
 import numpy as np
@@ -12,14 +13,14 @@ from at3d_gb300._abi import NumericalParams, Problem, Species
 FIXTURE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "rico32x36x26w672_pol.npz")
 
 
-def rico_problem():
+def rico_problem(split_accuracy: float = 0.0):
     g = np.load(FIXTURE)
     sp = Species(extinction=g["extinction"], ssalb=g["ssalb"], legcoef=g["legcoef"],
                  table_index=g["table_index"][None].astype(np.int32),
                  phase_weights=np.ones((1,) + g["extinction"].shape, np.float32))
     prm = NumericalParams(num_mu_bins=int(g["nmu"]), num_phi_bins=int(g["nphi"]),
                           solution_accuracy=float(g["solacc"]), spherical_harmonics_accuracy=float(g["shacc"]),
-                          split_accuracy=0.0, tautol=0.1, x_boundary_condition="open",
+                          split_accuracy=float(split_accuracy), tautol=0.1, x_boundary_condition="open",
                           y_boundary_condition="open")
     return Problem(delx=float(g["delx"]), dely=float(g["dely"]), zlevels=g["zlevels"], species=[sp],
                    solarmu=float(g["solarmu"]), solaraz=float(g["solaraz"]), solarflux=1.0,
