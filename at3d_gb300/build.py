@@ -14,6 +14,7 @@ ROOT = os.path.dirname(HERE)
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libshdom_gb300.so")
 SOURCES = [os.path.join(HERE, "csrc", "shdom_gpu.cu"), os.path.join(HERE, "csrc", "shdom_plan.cpp"),
+           os.path.join(HERE, "csrc", "shdom_paths.cpp"),
            os.path.join(HERE, "csrc", "shdom_mie.cpp"), os.path.join(HERE, "csrc", "shdom_mix.cpp")]
 HEADERS = (sorted(glob.glob(os.path.join(HERE, "csrc", "*.h"))) + sorted(glob.glob(os.path.join(HERE, "csrc", "*.cuh")))
            + sorted(glob.glob(os.path.join(ROOT, "include", "*.h"))))

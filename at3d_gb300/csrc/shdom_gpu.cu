@@ -4468,6 +4468,25 @@ int shdom_create_planned(shdom_plan *plan, int device, shdom_handle **out) {
 
 void shdom_plan_destroy(shdom_plan *plan) { delete plan; }
 
+int shdom_plan_optical_path(const shdom_plan *plan, int nrays, const float *camx, const float *camy,
+                            const float *camz, const double *cammu, const double *camphi, int deltam_path,
+                            float *path_out) {
+  if (!plan) return fail(nullptr, "shdom_plan_optical_path: null plan");
+  std::string err;
+  if (!shdom::optical_path(plan->P, nrays, camx, camy, camz, cammu, camphi, deltam_path, path_out, err))
+    return fail(nullptr, err);
+  return 0;
+}
+
+int shdom_optical_path(shdom_handle *h, int nrays, const float *camx, const float *camy, const float *camz,
+                       const double *cammu, const double *camphi, int deltam_path, float *path_out) {
+  if (!h) return fail(nullptr, "shdom_optical_path: null handle");
+  std::string err;
+  if (!shdom::optical_path(h->h.P, nrays, camx, camy, camz, cammu, camphi, deltam_path, path_out, err))
+    return fail(h, err);
+  return 0;
+}
+
 int shdom_init_solution(shdom_handle *hh) {
   if (!hh) return fail(nullptr, "null handle");
   Handle &H = hh->h;

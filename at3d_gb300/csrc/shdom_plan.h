@@ -238,6 +238,13 @@ void species_series(const Plan &P, int ipa, int ipt, float *u);
 // 'T' (the temperature itself) and 'B' (W/(m^2 sr) over the band waveno[2], cm^-1).
 float planck_fn(float t, char units, float wavelen, const float *waveno);
 
+// OPTICAL_DEPTH (src/shdomsub5.f:387-739 of the reference): the extinction
+// integrated along each ray (x, y, z, mu, phi as for the render) through
+// the base grid, trapezoid per cell crossing, with the delta-M scaling
+// undone unless deltam_path.  Host code on the plan's medium; out [n].
+bool optical_path(const Plan &P, int n, const float *camx, const float *camy, const float *camz,
+                  const double *cammu, const double *camphi, int deltam_path, float *out, std::string &err);
+
 // Real generalized spherical harmonics (unpolarized element) at one
 // direction, NLM values in the SHDOM term order.
 void ylm_unpol(int ml, int mm, double mu, float phi, float *y);

@@ -111,6 +111,21 @@ def plan_summary(problem: Problem) -> dict:
     return _sizes_dict(out)
 
 
+def _optical_path(call, handle, sensor: dict, deltam_scaled_path: bool) -> dict:
+    for k in ("ray_x", "ray_y", "ray_z", "ray_mu", "ray_phi"):
+        if k not in sensor:
+            raise KeyError(f"sensor needs '{k}'")
+    x, y, z, mu, phi = RTE._ray_arrays(sensor["ray_x"], sensor["ray_y"], sensor["ray_z"], sensor["ray_mu"],
+                                       sensor["ray_phi"])
+    out = np.zeros(len(x), np.float32)
+    dp = C.POINTER(C.c_double)
+    rc = call(len(x), _fp(x), _fp(y), _fp(z), mu.ctypes.data_as(dp), phi.ctypes.data_as(dp),
+              int(bool(deltam_scaled_path)), _fp(out))
+    _check(handle, rc)
+    sensor["optical_path_deltam" if deltam_scaled_path else "optical_path"] = out
+    return sensor
+
+
 class HostPlan:
     """A problem planned on the host (grid, sweep schedule, ordinates,
     medium, direct beam), not yet on a GPU; ``sizes["device_bytes"]`` is the
@@ -127,6 +142,13 @@ class HostPlan:
         self.problem = problem
         self.sizes = _sizes_dict(out)
         self._p = p
+
+    def optical_path(self, sensor: dict, deltam_scaled_path: bool = False) -> dict:
+        """RTE.optical_path on the host plan (no GPU needed)."""
+        if not self._p:
+            raise ValueError("plan already used or released")
+        return _optical_path(lambda *a: _lib.lib().shdom_plan_optical_path(self._p, *a), None, sensor,
+                             deltam_scaled_path)
 
     def release(self):
         if self._p:
@@ -370,6 +392,16 @@ class RTE:
     def _property_shape(self):
         sp = self.problem.species[0]
         return tuple(np.asarray(sp.extinction).shape)
+
+    def optical_path(self, sensor: dict, deltam_scaled_path: bool = False) -> dict:
+        """The extinction integrated along each ray of ``sensor`` ('ray_x',
+        'ray_y', 'ray_z', 'ray_mu', 'ray_phi'), stored in it as
+        'optical_path' (or 'optical_path_deltam' with the delta-M scaled
+        extinction) (RTE.optical_path, at3d/solver.py:793-867; OPTICAL_DEPTH).
+        Computed on the host from the solver's medium, before or after a
+        solve."""
+        return _optical_path(lambda *a: _lib.lib().shdom_optical_path(self._h, *a), self._h, sensor,
+                             deltam_scaled_path)
 
     @staticmethod
     def _ray_arrays(x, y, z, mu, phi):

@@ -76,6 +76,20 @@ int shdom_plan_create(const shdom_problem *problem, shdom_plan **out, shdom_size
 int shdom_create_planned(shdom_plan *plan, int device, shdom_handle **out);
 void shdom_plan_destroy(shdom_plan *plan);
 
+/* The extinction integrated along each ray (RTE.optical_path,
+ * at3d/solver.py:793-867; OPTICAL_DEPTH, src/shdomsub5.f:387-739): rays as
+ * for shdom_render (position, mu and phi toward the sensor), traced back
+ * through the base grid with the trapezoid rule per cell crossing; the
+ * delta-M scaled extinction when deltam_path, else the unscaled one.  Host
+ * computation on the plan's medium (no GPU work); a ray starting above the
+ * domain is extended to its top, one leaving upward gets 0.  3D grids. */
+int shdom_plan_optical_path(const shdom_plan *plan, int nrays, const float *camx, const float *camy,
+                            const float *camz, const double *cammu, const double *camphi, int deltam_path,
+                            float *path_out);
+/* The same on a handle's medium. */
+int shdom_optical_path(shdom_handle *h, int nrays, const float *camx, const float *camy, const float *camz,
+                       const double *cammu, const double *camphi, int deltam_path, float *path_out);
+
 /* Direct beam, Eddington initial radiance and the first source function.
  * Replaces core.make_angle_set, core.make_sh_do_coef and core.init_solution
  * (at3d/solver.py:2539-2798). */
