@@ -4478,6 +4478,20 @@ int shdom_plan_optical_path(const shdom_plan *plan, int nrays, const float *camx
   return 0;
 }
 
+int shdom_plan_point_absorption(const shdom_plan *plan, float *absorb, float *emit) {
+  if (!plan) return fail(nullptr, "shdom_plan_point_absorption: null plan");
+  std::string err;
+  if (!shdom::point_absorption(plan->P, absorb, emit, err)) return fail(nullptr, err);
+  return 0;
+}
+
+int shdom_point_absorption(shdom_handle *h, float *absorb, float *emit) {
+  if (!h) return fail(nullptr, "shdom_point_absorption: null handle");
+  std::string err;
+  if (!shdom::point_absorption(h->h.P, absorb, emit, err)) return fail(h, err);
+  return 0;
+}
+
 int shdom_optical_path(shdom_handle *h, int nrays, const float *camx, const float *camy, const float *camz,
                        const double *cammu, const double *camphi, int deltam_path, float *path_out) {
   if (!h) return fail(nullptr, "shdom_optical_path: null handle");

@@ -178,4 +178,24 @@ bool optical_path(const Plan &P, int n, const float *camx, const float *camy, co
   return true;
 }
 
+bool point_absorption(const Plan &P, float *absorb, float *emit, std::string &err) {
+  const int npts = P.npts, npart = P.prob.npart;
+  if (!absorb || !emit) { err = "point_absorption: null output"; return false; }
+  if (P.sp_ext.size() < (size_t)npart * npts) { err = "point_absorption: the plan holds no species properties"; return false; }
+  const bool thermal = P.prob.srctype == 'T' || P.prob.srctype == 'B';
+  if (thermal && P.planckpt.size() < (size_t)npts) { err = "point_absorption: no Planck values"; return false; }
+  for (int i = 0; i < npts; ++i) {
+    float a = 0.f, e = 0.f;
+    for (int ipa = 0; ipa < npart; ++ipa) {
+      const size_t o = (size_t)ipa * npts + i;
+      const float k = P.sp_ext[o], w = P.sp_alb[o];
+      a += k * (1.0f - w);
+      if (thermal) e += k * ((1.0f - w) * P.planckpt[i]);
+    }
+    absorb[i] = a;
+    emit[i] = e;
+  }
+  return true;
+}
+
 }  // namespace shdom

@@ -245,6 +245,11 @@ float planck_fn(float t, char units, float wavelen, const float *waveno);
 bool optical_path(const Plan &P, int n, const float *camx, const float *camy, const float *camz,
                   const double *cammu, const double *camphi, int deltam_path, float *out, std::string &err);
 
+// Per grid point the absorption sum_species ext (1 - albedo) and the
+// emission sum_species ext (1 - albedo) B(T) of the delta-M scaled medium
+// (ABSORB and EMIT of COMPUTE_NETFLUXDIV, src/polarized/shdomsub2.f:1725-1764).
+bool point_absorption(const Plan &P, float *absorb, float *emit, std::string &err);
+
 // Real generalized spherical harmonics (unpolarized element) at one
 // direction, NLM values in the SHDOM term order.
 void ylm_unpol(int ml, int mm, double mu, float phi, float *y);

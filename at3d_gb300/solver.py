@@ -111,6 +111,26 @@ def plan_summary(problem: Problem) -> dict:
     return _sizes_dict(out)
 
 
+def compute_netfluxdiv(radiance, dirflux, absorb, emit, solarmu: float, srctype: str = "S") -> np.ndarray:
+    """COMPUTE_NETFLUXDIV (src/polarized/shdomsub2.f:1725-1764): per grid
+    point -(sqrt(4 pi) absorb R_00 + absorb F sec(mu0) - 4 pi emit), the
+    solar term for 'S' and 'B' sources, the emission for 'T' and 'B'.
+    ``radiance`` [npts, nlm] or [npts, nstokes, nlm] (the I row is used);
+    ``absorb`` / ``emit`` as ``shdom_point_absorption`` gives them."""
+    r = np.asarray(radiance, np.float32)
+    if r.ndim == 3:
+        r = r[:, 0, :]
+    pi = np.float32(np.arccos(np.float32(-1.0)))
+    c = np.sqrt(np.float32(4.0) * pi)
+    a = np.asarray(absorb, np.float32)
+    hr = c * a * r[:, 0]
+    if srctype in ("S", "B"):
+        hr = hr + a * np.asarray(dirflux, np.float32) * (np.float32(1.0) / np.float32(abs(solarmu)))
+    if srctype in ("T", "B"):
+        hr = hr - np.float32(4.0) * pi * np.asarray(emit, np.float32)
+    return -hr
+
+
 def _optical_path(call, handle, sensor: dict, deltam_scaled_path: bool) -> dict:
     for k in ("ray_x", "ray_y", "ray_z", "ray_mu", "ray_phi"):
         if k not in sensor:
@@ -142,6 +162,15 @@ class HostPlan:
         self.problem = problem
         self.sizes = _sizes_dict(out)
         self._p = p
+
+    def point_absorption(self):
+        """(absorb, emit) per grid point of the plan's medium."""
+        if not self._p:
+            raise ValueError("plan already used or released")
+        n = self.sizes["npts"]
+        absorb = np.zeros(n, np.float32); emit = np.zeros(n, np.float32)
+        _check(None, _lib.lib().shdom_plan_point_absorption(self._p, _fp(absorb), _fp(emit)))
+        return absorb, emit
 
     def optical_path(self, sensor: dict, deltam_scaled_path: bool = False) -> dict:
         """RTE.optical_path on the host plan (no GPU needed)."""
@@ -379,6 +408,21 @@ class RTE:
         shp = (s["nx1"], s["ny1"], s["nz"])
         return {"mean_intensity": sh[0].reshape(shp), "Fx": sh[1].reshape(shp), "Fy": sh[2].reshape(shp),
                 "Fz": sh[3].reshape(shp)}
+
+    @property
+    def net_flux_divergence(self) -> dict:
+        """The net flux divergence on the base grid, [nx1, ny1, nz]
+        (RTE.net_flux_divergence, at3d/solver.py:1207-1260): the solved
+        radiance's mean term and direct beam from the device, the absorption
+        and emission of the medium from the host plan."""
+        s = self.sizes
+        st = self.export_state()
+        n = s["npts"]
+        absorb = np.zeros(n, np.float32); emit = np.zeros(n, np.float32)
+        _check(self._h, _lib.lib().shdom_point_absorption(self._h, _fp(absorb), _fp(emit)))
+        p = self.problem
+        nfd = compute_netfluxdiv(st["radiance"], st["dirflux"], absorb, emit, p.solarmu, p.srctype)
+        return {"net_flux_div": nfd.reshape(s["nx1"], s["ny1"], s["nz"])}
 
     @property
     def solution_accuracy(self) -> float:

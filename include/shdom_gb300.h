@@ -86,6 +86,13 @@ void shdom_plan_destroy(shdom_plan *plan);
 int shdom_plan_optical_path(const shdom_plan *plan, int nrays, const float *camx, const float *camy,
                             const float *camz, const double *cammu, const double *camphi, int deltam_path,
                             float *path_out);
+/* Per grid point [npts] the absorption sum_species ext (1 - albedo) and the
+ * emission sum_species ext (1 - albedo) B(T) of the delta-M scaled medium
+ * (ABSORB and EMIT of COMPUTE_NETFLUXDIV, src/polarized/shdomsub2.f:
+ * 1725-1764, for RTE.net_flux_divergence, at3d/solver.py:1207-1260); emit
+ * is 0 for a solar source.  Host computation. */
+int shdom_plan_point_absorption(const shdom_plan *plan, float *absorb, float *emit);
+int shdom_point_absorption(shdom_handle *h, float *absorb, float *emit);
 /* The same on a handle's medium. */
 int shdom_optical_path(shdom_handle *h, int nrays, const float *camx, const float *camy, const float *camz,
                        const double *cammu, const double *camphi, int deltam_path, float *path_out);

@@ -61,3 +61,29 @@ def test_deltam_path_and_errors():
     assert hp.optical_path(up)["optical_path"][0] == 0.0
     with pytest.raises(SHDOMError, match="below the domain"):
         hp.optical_path(_sensor([0.1], [0.1], [-1.0], [1.0], [0.0]))
+
+
+def test_net_flux_divergence_conserves_energy():
+    """COMPUTE_NETFLUXDIV on a solved state (the oracle's radiance and direct
+    beam, the plan's absorption): over a periodic domain the volume integral
+    of the net flux divergence equals the net vertical flux (diffuse and
+    direct, COMPUTE_SH) through the top less that through the bottom, 2%."""
+    from at3d_gb300.solver import compute_netfluxdiv, compute_sh
+    from oracle.oracle import Oracle
+    pb = scenes.cloud_field(seed=3, nx=16, ny=16, nz=12, dx=0.05, dz=0.05, mean_ext=10.0, boundary="periodic",
+                            nmu=8, nphi=16, nleg=128, ssa=0.9, g=0.85)
+    hp = HostPlan(pb)
+    absorb, emit = hp.point_absorption()
+    o = Oracle(pb, fp64=True)
+    o.solve(100)
+    st = o.export()
+    nfd = compute_netfluxdiv(st["radiance"], st["dirflux"], absorb, emit, pb.solarmu, "S")
+    nx1, ny1, nz = hp.sizes["nx1"], hp.sizes["ny1"], hp.sizes["nz"]
+    nfd = nfd.reshape(nx1, ny1, nz)[:-1, :-1]           # periodic: drop the wrap-around planes
+    fz = compute_sh(st["radiance"], st["dirflux"], pb.solarmu, pb.solaraz, "S")[3].reshape(nx1, ny1, nz)[:-1, :-1]
+    z = np.asarray(pb.zlevels, np.float64)
+    lhs = np.trapezoid(nfd.mean(axis=(0, 1)).astype(np.float64), z)
+    rhs = fz[..., -1].mean() - fz[..., 0].mean()
+    assert lhs < 0 and rhs < 0
+    assert abs(lhs - rhs) <= 0.02 * abs(rhs), (lhs, rhs)
+    assert np.all(absorb >= 0) and np.all(emit == 0)
