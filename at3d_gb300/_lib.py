@@ -54,6 +54,7 @@ SIGNATURES = {
     "shdom_plan_optical_path": (C.c_int, [C.c_void_p, C.c_int, _f, _f, _f, _d, _d, C.c_int, _f]),
     "shdom_optical_path": (C.c_int, [C.c_void_p, C.c_int, _f, _f, _f, _d, _d, C.c_int, _f]),
     "shdom_plan_point_absorption": (C.c_int, [C.c_void_p, _f, _f]),
+    "shdom_plan_min_optical_path": (C.c_int, [C.c_void_p, C.c_int, _f, _f, _f, _d, _d, C.c_int, C.c_int, _f]),
     "shdom_point_absorption": (C.c_int, [C.c_void_p, _f, _f]),
     "shdom_mie_mono": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_int, _f, C.c_int, C.c_int, _f, _f, _i,
                                  _f]),

@@ -4478,6 +4478,16 @@ int shdom_plan_optical_path(const shdom_plan *plan, int nrays, const float *camx
   return 0;
 }
 
+int shdom_plan_min_optical_path(const shdom_plan *plan, int nrays, const float *camx, const float *camy,
+                                const float *camz, const double *cammu, const double *camphi, int deltam_path,
+                                int do_all, float *minpath_out) {
+  if (!plan) return fail(nullptr, "shdom_plan_min_optical_path: null plan");
+  std::string err;
+  if (!shdom::min_optical_path(plan->P, nrays, camx, camy, camz, cammu, camphi, deltam_path, do_all, minpath_out, err))
+    return fail(nullptr, err);
+  return 0;
+}
+
 int shdom_plan_point_absorption(const shdom_plan *plan, float *absorb, float *emit) {
   if (!plan) return fail(nullptr, "shdom_plan_point_absorption: null plan");
   std::string err;

@@ -51,8 +51,30 @@ int locate_cell(const Plan &P, double &x0, double &y0, double z0) {
 
 }  // namespace
 
+bool ray_paths(const Plan &P, int n, const float *camx, const float *camy, const float *camz,
+               const double *cammu, const double *camphi, int deltam_path, float *out, float *minpath, int do_all,
+               std::string &err);
+
 bool optical_path(const Plan &P, int n, const float *camx, const float *camy, const float *camz,
                   const double *cammu, const double *camphi, int deltam_path, float *out, std::string &err) {
+  return ray_paths(P, n, camx, camy, camz, cammu, camphi, deltam_path, out, nullptr, 0, err);
+}
+
+bool min_optical_path(const Plan &P, int n, const float *camx, const float *camy, const float *camz,
+                      const double *cammu, const double *camphi, int deltam_path, int do_all, float *minpath,
+                      std::string &err) {
+  if (!minpath) { err = "min_optical_path: null output"; return false; }
+  std::vector<float> tau(std::max(n, 0));
+  return ray_paths(P, n, camx, camy, camz, cammu, camphi, deltam_path, tau.data(), minpath, do_all, err);
+}
+
+// The ray walk shared by OPTICAL_DEPTH and MIN_OPTICAL_DEPTH
+// (src/shdomsub5.f:17-385): out[r] the path of ray r; with minpath, after
+// each cell crossing every corner of the cell keeps the smallest path so far
+// ([npts], or [n][npts] per ray with do_all; 999 where no ray passed).
+bool ray_paths(const Plan &P, int n, const float *camx, const float *camy, const float *camz,
+               const double *cammu, const double *camphi, int deltam_path, float *out, float *minpath, int do_all,
+               std::string &err) {
   if (n < 0 || (n > 0 && (!camx || !camy || !camz || !cammu || !camphi || !out))) {
     err = "optical_path: bad arguments";
     return false;
@@ -97,7 +119,7 @@ bool optical_path(const Plan &P, int n, const float *camx, const float *camy, co
   const float xm = 0.5f * (P.xgrid[0] + P.xgrid[nx - 1]), ym = 0.5f * (P.ygrid[0] + P.ygrid[ny - 1]);
   std::vector<std::string> errs;
 
-  auto one_ray = [&](int r, std::string &rerr) -> bool {
+  auto one_ray = [&](int r, float *mp, std::string &rerr) -> bool {
     double x0 = camx[r], y0 = camy[r], z0 = camz[r];
     const double mu2 = cammu[r], phi2 = camphi[r];
     const double muray = -mu2, phiray = phi2 - std::acos(-1.0);
@@ -147,6 +169,10 @@ bool optical_path(const Plan &P, int n, const float *camx, const float *camy, co
       double xn = xe + so * cx, yn = ye + so * cy, zn = ze + so * cz;
       const float extn = ext_at(icell, xn, yn, zn);
       tau = (float)(tau + so * 0.5 * (ext1 + extn));
+      if (mp) {
+        float *col = do_all ? mp + (size_t)r * npts : mp;
+        for (int k = 0; k < 8; ++k) { float &m = col[gptr[8 * icell + k]]; m = std::min(m, tau); }
+      }
       int iface, jface;
       if (sox <= soz && sox <= soy) { iface = 1 - bitx; jface = 0; }
       else if (soy <= soz) { iface = 3 - bity; jface = 1; }
@@ -166,13 +192,20 @@ bool optical_path(const Plan &P, int n, const float *camx, const float *camy, co
 
   const int nt = std::max(1, std::min<int>(16, std::min<int>((int)std::thread::hardware_concurrency(), n / 64 + 1)));
   errs.assign(nt, std::string());
+  // one minimum buffer per thread when the rays share it, folded afterwards
+  std::vector<std::vector<float>> part(minpath && !do_all ? nt : 0);
+  if (minpath) std::fill(minpath, minpath + (size_t)npts * (do_all ? n : 1), 999.0f);
+  for (auto &v : part) v.assign(npts, 999.0f);
   std::vector<std::thread> pool;
   for (int t = 0; t < nt; ++t)
     pool.emplace_back([&, t]() {
+      float *mp = !minpath ? nullptr : do_all ? minpath : part[t].data();
       for (int r = t; r < n; r += nt)
-        if (!one_ray(r, errs[t])) return;
+        if (!one_ray(r, mp, errs[t])) return;
     });
   for (auto &th : pool) th.join();
+  for (auto &v : part)
+    for (int i = 0; i < npts; ++i) minpath[i] = std::min(minpath[i], v[i]);
   for (auto &m : errs)
     if (!m.empty()) { err = m; return false; }
   return true;

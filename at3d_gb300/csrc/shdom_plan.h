@@ -245,6 +245,14 @@ float planck_fn(float t, char units, float wavelen, const float *waveno);
 bool optical_path(const Plan &P, int n, const float *camx, const float *camy, const float *camz,
                   const double *cammu, const double *camphi, int deltam_path, float *out, std::string &err);
 
+// MIN_OPTICAL_DEPTH (src/shdomsub5.f:17-385): per grid point the smallest
+// optical path, over the rays, at which a ray leaves a cell the point is a
+// corner of; minpath [npts] (or [n][npts] per ray with do_all), 999 where no
+// ray passes.
+bool min_optical_path(const Plan &P, int n, const float *camx, const float *camy, const float *camz,
+                      const double *cammu, const double *camphi, int deltam_path, int do_all, float *minpath,
+                      std::string &err);
+
 // Per grid point the absorption sum_species ext (1 - albedo) and the
 // emission sum_species ext (1 - albedo) B(T) of the delta-M scaled medium
 // (ABSORB and EMIT of COMPUTE_NETFLUXDIV, src/polarized/shdomsub2.f:1725-1764).

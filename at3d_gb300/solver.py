@@ -163,6 +163,25 @@ class HostPlan:
         self.sizes = _sizes_dict(out)
         self._p = p
 
+    def min_optical_path(self, sensor: dict, deltam_scaled_path: bool = False, do_all: bool = False) -> np.ndarray:
+        """RTE.min_optical_path (at3d/solver.py:921-990; MIN_OPTICAL_DEPTH):
+        per grid point the smallest optical path, over the rays of ``sensor``,
+        at which a ray leaves a cell the point is a corner of; [nx1, ny1, nz],
+        or [nrays, nx1, ny1, nz] with ``do_all``; 999 where no ray passes."""
+        if not self._p:
+            raise ValueError("plan already used or released")
+        x, y, z, mu, phi = RTE._ray_arrays(sensor["ray_x"], sensor["ray_y"], sensor["ray_z"], sensor["ray_mu"],
+                                           sensor["ray_phi"])
+        s = self.sizes
+        shp = (s["nx1"], s["ny1"], s["nz"])
+        out = np.zeros(((len(x) if do_all else 1) * s["npts"]), np.float32)
+        dp = C.POINTER(C.c_double)
+        _check(None, _lib.lib().shdom_plan_min_optical_path(self._p, len(x), _fp(x), _fp(y), _fp(z),
+                                                            mu.ctypes.data_as(dp), phi.ctypes.data_as(dp),
+                                                            int(bool(deltam_scaled_path)), int(bool(do_all)),
+                                                            _fp(out)))
+        return out.reshape((len(x),) + shp) if do_all else out.reshape(shp)
+
     def point_absorption(self):
         """(absorb, emit) per grid point of the plan's medium."""
         if not self._p:
@@ -436,6 +455,11 @@ class RTE:
     def _property_shape(self):
         sp = self.problem.species[0]
         return tuple(np.asarray(sp.extinction).shape)
+
+    def min_optical_path(self, sensor: dict, deltam_scaled_path: bool = False, do_all: bool = False):
+        """HostPlan.min_optical_path of this solver's problem (planned on the
+        host again; no GPU work)."""
+        return HostPlan(self.problem).min_optical_path(sensor, deltam_scaled_path, do_all)
 
     def optical_path(self, sensor: dict, deltam_scaled_path: bool = False) -> dict:
         """The extinction integrated along each ray of ``sensor`` ('ray_x',

@@ -86,6 +86,14 @@ void shdom_plan_destroy(shdom_plan *plan);
 int shdom_plan_optical_path(const shdom_plan *plan, int nrays, const float *camx, const float *camy,
                             const float *camz, const double *cammu, const double *camphi, int deltam_path,
                             float *path_out);
+/* RTE.min_optical_path (at3d/solver.py:921-990; MIN_OPTICAL_DEPTH,
+ * src/shdomsub5.f:17-385): per grid point the smallest optical path, over
+ * the rays, at which a ray leaves a cell the point is a corner of;
+ * minpath_out [npts], or [nrays][npts] per ray with do_all; 999 where no
+ * ray passes.  Host computation on the plan's medium. */
+int shdom_plan_min_optical_path(const shdom_plan *plan, int nrays, const float *camx, const float *camy,
+                                const float *camz, const double *cammu, const double *camphi, int deltam_path,
+                                int do_all, float *minpath_out);
 /* Per grid point [npts] the absorption sum_species ext (1 - albedo) and the
  * emission sum_species ext (1 - albedo) B(T) of the delta-M scaled medium
  * (ABSORB and EMIT of COMPUTE_NETFLUXDIV, src/polarized/shdomsub2.f:

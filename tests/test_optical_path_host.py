@@ -87,3 +87,31 @@ def test_net_flux_divergence_conserves_energy():
     assert lhs < 0 and rhs < 0
     assert abs(lhs - rhs) <= 0.02 * abs(rhs), (lhs, rhs)
     assert np.all(absorb >= 0) and np.all(emit == 0)
+
+
+def test_min_optical_path_one_nadir_ray():
+    """MIN_OPTICAL_DEPTH: one nadir ray down the middle of a cell column of a
+    horizontally uniform medium marks the four corner columns of the cells
+    it crosses with the path from the top to each level (the top level with
+    the path through the first cell); every other point keeps 999."""
+    pb = scenes.cloud_blob(seed=1, nx=6, ny=6, nz=7, dx=0.05, dz=0.1, boundary="periodic")
+    pb = copy.deepcopy(pb)
+    prof = np.linspace(1.0, 4.0, 7).astype(np.float32)
+    pb.species[0].extinction = np.broadcast_to(prof, np.shape(pb.species[0].extinction)).copy()
+    pb.species[1].extinction = np.zeros_like(pb.species[1].extinction)
+    hp = HostPlan(pb)
+    i, j = 2, 3
+    s = _sensor([(i + 0.5) * pb.delx], [(j + 0.5) * pb.dely], [5.0], [1.0], [0.0])
+    m = hp.min_optical_path(s)
+    z = np.asarray(pb.zlevels, np.float64)
+    want = np.array([np.trapezoid(prof[k:], z[k:]) for k in range(len(z))])
+    want[-1] = want[-2]
+    for a in (i, i + 1):
+        for b in (j, j + 1):
+            np.testing.assert_allclose(m[a, b], want, rtol=2e-5)
+    others = np.ones(m.shape[:2], bool)
+    others[i:i + 2, j:j + 2] = False
+    assert np.all(m[others] == 999.0)
+    both = hp.min_optical_path(_sensor([(i + 0.5) * pb.delx] * 2, [(j + 0.5) * pb.dely] * 2, [5.0, 5.0],
+                                       [1.0, 1.0], [0.0, 0.0]), do_all=True)
+    assert both.shape == (2,) + m.shape and np.array_equal(both[0], m) and np.array_equal(both[1], m)
